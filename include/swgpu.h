@@ -1,0 +1,293 @@
+/*
+ * swgpu.h — C ABI of the GB300 world-rendering path of Square-Wheel.
+ *
+ * The Rust host (or any other host) keeps BSP/portal visibility, leaf ordering, per-polygon surface
+ * preparation and per-polygon draw setup.  It hands the results to this library in two arrays:
+ *   - SwSurfaceDesc: one per visible polygon surface, the arguments the reference passes to
+ *     build_surface_{simple,directional}_lightmap and mix_surface_with_texture
+ *     (src/square_wheel/partial_renderer.rs:1682-1819);
+ *   - SwDrawCmd + SwVertex16: one per rasterised polygon in exact submission order, the arguments the
+ *     reference passes to Rasterizer::fill_polygon (src/square_wheel/partial_renderer.rs:4084-4140).
+ * The library builds the surfaces, rasterises them into a colour32/colour64 frame, and runs the HDR
+ * postprocessor (bloom + tonemap + auto exposure) and the frame upscaler.
+ *
+ * Conventions
+ *   - Every function returns SW_OK (0) or a negative SwStatus and never aborts; sw_last_error() gives text.
+ *   - The context owns every device buffer; the caller owns host buffers.
+ *   - One SwCtx is used by one caller thread; work is ordered on the context's CUDA stream and is
+ *     asynchronous until sw_sync() unless a call reads results back into host memory.
+ *   - Colour layouts are the reference's: Color32 = A<<24|R<<16|G<<8|B (src/common/color.rs:21-24),
+ *     Color64 = A<<48|R<<32|G<<16|B (src/common/color.rs:144-147).
+ *   - Arithmetic follows the reference's generic (non-SSE) fast_math semantics bit-exactly:
+ *     exact 1/x and 1/sqrt(x), truncating float->int, unfused multiply-add
+ *     (src/square_wheel/fast_math.rs:370-740).
+ */
+#ifndef SWGPU_H
+#define SWGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWGPU_ABI_VERSION 1
+
+typedef enum SwStatus {
+	SW_OK = 0,
+	SW_ERR_INVALID_ARGUMENT = -1,
+	SW_ERR_OUT_OF_MEMORY = -2,
+	SW_ERR_CUDA = -3,
+	SW_ERR_LIMIT = -4,
+	SW_ERR_NO_DEVICE = -5,
+	SW_ERR_STATE = -6,
+	SW_ERR_KERNEL = -7,
+} SwStatus;
+
+typedef enum SwPixelFormat {
+	SW_PIXEL_C32 = 0, /* Color32, 4 bytes per pixel */
+	SW_PIXEL_C64 = 1, /* Color64, 8 bytes per pixel (HDR) */
+} SwPixelFormat;
+
+/* BlendingMode, src/common/material.rs (None, Average, Additive, AlphaTest, AlphaBlend). */
+typedef enum SwBlend {
+	SW_BLEND_NONE = 0,
+	SW_BLEND_AVERAGE = 1,
+	SW_BLEND_ADDITIVE = 2,
+	SW_BLEND_ALPHA_TEST = 3,
+	SW_BLEND_ALPHA_BLEND = 4,
+} SwBlend;
+
+/* TetureCoordinatesInterpolationMode, src/square_wheel/rasterizer.rs:4-10. */
+typedef enum SwRasterMode {
+	SW_RASTER_FULL_PERSPECTIVE = 0,
+	SW_RASTER_LINE_Z_CORRECTED = 1,
+	SW_RASTER_AFFINE = 2,
+} SwRasterMode;
+
+/* ---- static data, uploaded once (Renderer::new, src/square_wheel/renderer.rs:24-59) ---- */
+
+/* Texture flags, src/square_wheel/textures.rs:11-18. */
+#define SW_TEX_HAS_NORMAL_MAP 1u
+#define SW_TEX_HAS_NON_ONE_ROUGHNESS 2u
+#define SW_TEX_IS_METAL 4u
+
+/* One mip level of a material texture. Texels are TextureElement (8 bytes: Color32 diffuse +
+ * packed i8x4 normal/roughness, src/square_wheel/textures.rs:20-62), stored row-major. */
+typedef struct SwTextureMip {
+	uint64_t offset; /* in texels, into SwCreateInfo.texels */
+	uint32_t width;
+	uint32_t height;
+	uint32_t flags; /* SW_TEX_* of the material */
+	uint32_t reserved;
+} SwTextureMip;
+
+/* One mip level of an emissive texture (TextureLite = Color32 image, src/square_wheel/textures.rs:89-91). */
+typedef struct SwEmissiveMip {
+	uint64_t offset; /* in pixels, into SwCreateInfo.emissive_pixels */
+	uint32_t width;
+	uint32_t height;
+} SwEmissiveMip;
+
+/* DirectionalLightmapElement, src/common/bsp_map_compact.rs:144-156 (40 bytes). */
+typedef struct SwDirectionalLightmapElement {
+	float ambient_light[3];
+	float light_direction_vector_scaled[3];
+	float directional_light_deviation;
+	float directional_light_color[3];
+} SwDirectionalLightmapElement;
+
+typedef struct SwCreateInfo {
+	uint32_t abi_version; /* SWGPU_ABI_VERSION */
+	uint32_t device;      /* CUDA device ordinal */
+	const uint64_t* texels; /* TextureElement raw 8-byte values */
+	uint64_t num_texels;
+	const SwTextureMip* texture_mips;
+	uint32_t num_texture_mips;
+	uint32_t num_emissive_mips;
+	const uint32_t* emissive_pixels; /* Color32 raw values */
+	uint64_t num_emissive_pixels;
+	const SwEmissiveMip* emissive_mips;
+	/* LightmapElement = [f32;3] (src/common/bsp_map_compact.rs:142); element 0 is never used (offset 0 = no lightmap). */
+	const float* lightmaps;
+	uint64_t num_lightmap_elements;
+	const SwDirectionalLightmapElement* directional_lightmaps;
+	uint64_t num_directional_lightmap_elements;
+	/* Capacity hints (0 = defaults). Exceeding them later grows the buffers. */
+	uint64_t max_surface_texels;
+	uint32_t max_surfaces;
+	uint32_t max_draws;
+} SwCreateInfo;
+
+/* ---- per-frame data ---- */
+
+/* DynamicLightWithShadow without a shadow map (shadow factor 1), src/square_wheel/light.rs:4-11,
+ * created as in src/square_wheel/renderer_structs.rs:228-238. */
+typedef struct SwLight {
+	float position[3];
+	float radius;
+	float inv_square_radius; /* 1/(radius*radius), computed by the host */
+	float color[3];
+} SwLight;
+
+#define SW_MAX_POLYGON_LIGHTS 6 /* MAX_POLYGON_LIGHTS, src/square_wheel/partial_renderer.rs:1666 */
+#define SW_NO_LIGHTMAP 0u
+#define SW_NO_EMISSIVE 0xFFFFFFFFu
+
+/* Surface flags */
+#define SW_SURF_DIFFUSE_LAYER 1u /* material.light && material.diffuse (partial_renderer.rs:1701) */
+
+/* One visible polygon surface: the arguments of build_surface_impl_6_static_params
+ * (src/square_wheel/surfaces.rs:433-451) plus the emissive layer of mix_surface_with_texture
+ * (src/square_wheel/surfaces.rs:854-901), as computed in src/square_wheel/partial_renderer.rs:1682-1819. */
+typedef struct SwSurfaceDesc {
+	float basis_u[3];      /* PolygonBasisVecs scaled for the mip and shifted (partial_renderer.rs:1736-1740) */
+	float basis_v[3];
+	float basis_start[3];
+	float basis_normal[3];
+	uint32_t size[2];      /* surface_size */
+	int32_t tc_start[2];   /* surface_tc_min + texture shift >> mip */
+	uint32_t texture_mip;  /* index into SwCreateInfo.texture_mips */
+	uint32_t emissive_mip; /* index into SwCreateInfo.emissive_mips, or SW_NO_EMISSIVE */
+	uint32_t lightmap_offset; /* element offset, SW_NO_LIGHTMAP (0) if none */
+	uint32_t lightmap_size[2];
+	uint32_t lightmap_scale_log2; /* LIGHTMAP_SCALE_LOG2 - mip, 0..4 */
+	uint32_t lightmap_tc_shift[2];
+	uint32_t flags;        /* SW_SURF_* */
+	uint32_t num_lights;   /* <= SW_MAX_POLYGON_LIGHTS */
+	uint16_t lights[SW_MAX_POLYGON_LIGHTS]; /* indices into the frame's SwLight array */
+	float emissive_light[3];
+	uint64_t out_offset;   /* first texel of this surface in the frame's surface arena */
+} SwSurfaceDesc;
+
+/* A projected polygon vertex in 16.16 fixed point (PolygonPointProjected, rasterizer.rs:1484-1489). */
+typedef struct SwVertex16 {
+	int32_t x;
+	int32_t y;
+} SwVertex16;
+
+#define SW_MAX_POLYGON_VERTICES 24 /* MAX_VERTICES, src/square_wheel/renderer_utils.rs:4 */
+
+/* One Rasterizer::fill_polygon call (src/square_wheel/rasterizer.rs:35-80) as emitted by
+ * draw_polygon (src/square_wheel/partial_renderer.rs:4011-4142). Equations are the ones passed to
+ * fill_polygon (already scaled by z_scale for the non-affine modes). */
+typedef struct SwDrawCmd {
+	uint32_t first_vertex; /* into the SwVertex16 array */
+	uint32_t vertex_count; /* 3..SW_MAX_POLYGON_VERTICES, clockwise */
+	uint32_t mode;         /* SwRasterMode */
+	uint32_t blend;        /* SwBlend */
+	float depth_eq[3];     /* d_inv_z_dx, d_inv_z_dy, k */
+	float tc_eq[6];        /* d_tc_dx[2], d_tc_dy[2], k[2] */
+	uint32_t tex_size[2];  /* surface size */
+	uint32_t reserved;
+	uint64_t tex_offset;   /* surface's first texel in the surface arena */
+} SwDrawCmd;
+
+typedef struct SwFrameParams {
+	uint32_t pixel_format; /* SwPixelFormat of surfaces and framebuffer */
+	uint32_t width;
+	uint32_t height;
+	uint32_t use_directional_lightmaps; /* RendererConfig::use_directional_lightmaps && data present */
+	float cam_pos[3];
+	uint32_t clear_background; /* draw_background before rasterisation (partial_renderer.rs:249-257) */
+	uint32_t reserved;
+} SwFrameParams;
+
+/* PostprocessorConfig after synchronize_config clamping (src/square_wheel/postprocessor_config.rs,
+ * src/square_wheel/postprocessor.rs:958-977). */
+typedef struct SwPostConfig {
+	float exposure_update_speed;
+	float base_brightness;
+	float zero_level_brightness;
+	float brightness_scale_power;
+	float min_exposure;
+	float max_exposure;
+	float bloom_sigma;
+	uint32_t bloom_buffer_scale_log2;
+	float bloom_scale;
+	uint32_t linear_bloom_filter;
+} SwPostConfig;
+
+typedef enum SwUpscaleMode {
+	SW_UPSCALE_NEAREST = 0, /* FrameUpscaler::perform_upscale_impl::<SCALE> */
+	SW_UPSCALE_AVG2X = 1,   /* FrameUpscaler::perform_upscale_2x_linear */
+} SwUpscaleMode;
+
+typedef struct SwCtx SwCtx;
+
+/* Renderer::new (src/square_wheel/renderer.rs:24-59): upload static map data. */
+int sw_create(const SwCreateInfo* info, SwCtx** out_ctx);
+int sw_destroy(SwCtx* ctx);
+const char* sw_last_error(const SwCtx* ctx);
+int sw_sync(SwCtx* ctx);
+
+/* Start a frame: camera, lights, pixel format and frame size (Renderer::prepare_frame, renderer.rs:61-104). */
+int sw_frame_begin(SwCtx* ctx, const SwFrameParams* params, const SwLight* lights, uint32_t num_lights);
+
+/* Surfaces of the frame's visible polygons, in any order; out_offset values must not overlap.
+ * Builds them on the GPU (build_polygons_surfaces, partial_renderer.rs:1640-1832).
+ * total_texels = size of the surface arena for this frame. */
+int sw_submit_surfaces(SwCtx* ctx, const SwSurfaceDesc* surfaces, uint32_t num_surfaces, uint64_t total_texels);
+
+/* Build the surfaces of the last sw_submit_surfaces again without re-uploading descriptors (after a
+ * sw_frame_begin that changed only the camera position or the lights' parameters). */
+int sw_rebuild_surfaces(SwCtx* ctx);
+
+/* Use a surface arena built elsewhere (host memory, pixel_format of sw_frame_begin) instead of
+ * sw_submit_surfaces, e.g. textures the caller prepared itself. */
+int sw_set_surfaces(SwCtx* ctx, const void* texels, uint64_t total_texels);
+
+/* Draw commands in exact submission order (draw_tree/draw_leaf/draw_polygon,
+ * partial_renderer.rs:2450-2559, 4011-4142). */
+int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices,
+	uint32_t num_vertices);
+
+/* Rasterise the submitted draws (Renderer::draw_frame, renderer.rs:106-124) into the context's
+ * framebuffer. If dst != NULL the frame (pixel_format of sw_frame_begin) is also copied there:
+ * dst_is_device != 0 means a device pointer, otherwise host memory; pitch is in pixels. */
+int sw_render(SwCtx* ctx, void* dst, uint32_t pitch, int dst_is_device);
+
+/* Postprocessor::perform_postprocessing (src/square_wheel/postprocessor.rs:68-204) on the context's
+ * colour64 framebuffer, writing Color32 to dst (pitch in pixels). Exposure state lives in the context,
+ * starting at 1.0; the frame's average colour updates it for the next frame. */
+int sw_postprocess(SwCtx* ctx, const SwPostConfig* config, float frame_duration_s, const float color_modulate[3],
+	void* dst, uint32_t pitch, int dst_is_device);
+
+/* FrameUpscaler::perform_upscale (src/square_wheel/frame_upscaler.rs:42-70): src is a Color32 frame of
+ * (dst_width/scale) x (dst_height/scale) pixels with pitch = its width; dst has dst_pitch pixels per row. */
+int sw_upscale(SwCtx* ctx, uint32_t mode, uint32_t scale, const void* src, int src_is_device, void* dst,
+	uint32_t dst_width, uint32_t dst_height, uint32_t dst_pitch, int dst_is_device);
+
+/* Load a frame into the context's frame buffer (e.g. an HDR frame to postprocess that was rendered
+ * elsewhere, Postprocessor::get_hdr_buffer, postprocessor.rs:56-66). Pixels are tightly packed. */
+int sw_set_framebuffer(SwCtx* ctx, const void* src, uint32_t width, uint32_t height, uint32_t pixel_format,
+	int src_is_device);
+
+typedef struct SwStats {
+	uint64_t surfaces;          /* surfaces built since sw_create */
+	uint64_t surface_texels;    /* texels built since sw_create */
+	uint64_t draws;             /* draw commands submitted since sw_create */
+	uint64_t bad_texel_fetches; /* rasteriser fetches outside a surface (always 0 for well-formed draws) */
+} SwStats;
+int sw_get_stats(SwCtx* ctx, SwStats* out_stats);
+
+/* The context's CUDA stream (cudaStream_t) for callers that order their own work after the frame. */
+int sw_get_stream(SwCtx* ctx, void** out_stream);
+
+/* sizeof() of the ABI structs in this order: SwCreateInfo, SwTextureMip, SwEmissiveMip,
+ * SwDirectionalLightmapElement, SwLight, SwSurfaceDesc, SwVertex16, SwDrawCmd, SwFrameParams,
+ * SwPostConfig, SwStats. Writes min(count, 11) values; returns the number of structs (11).
+ * Needs no GPU: bindings use it to check their mirrored layouts. */
+int sw_abi_layout(uint32_t* sizes, uint32_t count);
+
+/* Diagnostics: copy the frame's surface arena (total_texels of sw_submit_surfaces) to host memory. */
+int sw_read_surfaces(SwCtx* ctx, void* dst_host, uint64_t max_bytes);
+/* Current exposure (Postprocessor::current_exposure). */
+int sw_get_exposure(SwCtx* ctx, float* out_exposure);
+int sw_set_exposure(SwCtx* ctx, float exposure);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SWGPU_H */

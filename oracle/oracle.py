@@ -1,0 +1,108 @@
+"""Test infrastructure: ctypes binding of the CPU oracle (oracle/build/liboracle.so).
+
+The oracle restates the reference's CPU renderer for the GPU path; only tests, the smoke check and
+bench.py's CPU-baseline leg use it, as the checker. It takes the same descriptors as the GPU library.
+"""
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "build", "liboracle.so")
+sys.path.insert(0, os.path.join(HERE, "..", "square-wheel_gb300"))
+from sqwheel import abi  # noqa: E402
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "-j4"], check=True)
+    return LIB_PATH
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        build()
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, u32, u64, i32, f32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_float
+    lib.orc_build_surfaces.argtypes = [vp, vp, u32, vp, u32, vp, vp, u64, u32]
+    lib.orc_rasterize.argtypes = [vp, u32, vp, u32, vp, u64, vp, vp, u32, u32, ctypes.POINTER(u64)]
+    lib.orc_clear_background.argtypes = [vp, vp, u32]
+    lib.orc_postprocess.argtypes = [vp, vp, u32, u32, f32, vp, ctypes.POINTER(f32), vp, u32, vp]
+    lib.orc_upscale.argtypes = [u32, u32, vp, vp, u32, u32, u32]
+    lib.orc_gaussian_kernel.argtypes = [f32, u32, vp]
+    for fn in (lib.orc_build_surfaces, lib.orc_rasterize, lib.orc_clear_background, lib.orc_postprocess,
+               lib.orc_upscale, lib.orc_gaussian_kernel):
+        fn.restype = i32
+    _lib = lib
+    return lib
+
+
+def _check(r, what):
+    if r != 0:
+        raise RuntimeError(f"{what} failed with status {r}")
+
+
+def build_surfaces(static, surfaces, lights, frame_params, total_texels, num_threads=1):
+    lib = load()
+    ci = static.create_info()
+    surfaces = np.ascontiguousarray(surfaces, dtype=abi.SURFACE_DESC)
+    lights = np.ascontiguousarray(lights if lights is not None else np.zeros(0, abi.LIGHT), dtype=abi.LIGHT)
+    dt = np.uint64 if frame_params.pixel_format == abi.SW_PIXEL_C64 else np.uint32
+    arena = np.zeros(int(total_texels), dt)
+    _check(lib.orc_build_surfaces(ctypes.byref(ci), abi.ptr(surfaces), surfaces.size, abi.ptr(lights), lights.size,
+                                  ctypes.byref(frame_params), abi.ptr(arena), arena.size, num_threads),
+           "orc_build_surfaces")
+    return arena
+
+
+def rasterize(draws, vertices, arena, frame_params, framebuffer, num_threads=1):
+    """Rasterise into `framebuffer` (height, pitch) in place; returns the count of bad texel fetches."""
+    lib = load()
+    draws = np.ascontiguousarray(draws, dtype=abi.DRAW_CMD)
+    vertices = np.ascontiguousarray(vertices, dtype=abi.VERTEX16)
+    bad = ctypes.c_uint64(0)
+    _check(lib.orc_rasterize(abi.ptr(draws), draws.size, abi.ptr(vertices), vertices.size, abi.ptr(arena), arena.size,
+                             ctypes.byref(frame_params), abi.ptr(framebuffer), framebuffer.shape[1], num_threads,
+                             ctypes.byref(bad)), "orc_rasterize")
+    return bad.value
+
+
+def clear_background(frame_params, framebuffer):
+    _check(load().orc_clear_background(ctypes.byref(frame_params), abi.ptr(framebuffer), framebuffer.shape[1]),
+           "orc_clear_background")
+
+
+def postprocess(config, hdr, frame_duration_s, color_modulate, exposure, pitch=None):
+    """Returns (ldr frame (h, pitch) uint32, new exposure, average colour lanes)."""
+    lib = load()
+    hdr = np.ascontiguousarray(hdr, dtype=np.uint64)
+    h, w = hdr.shape
+    pitch = pitch or w
+    out = np.zeros((h, pitch), np.uint32)
+    e = ctypes.c_float(exposure)
+    avg = np.zeros(4, np.float32)
+    mod = (ctypes.c_float * 3)(*[float(c) for c in color_modulate])
+    _check(lib.orc_postprocess(ctypes.byref(config), abi.ptr(hdr), w, h, float(frame_duration_s), mod, ctypes.byref(e),
+                               abi.ptr(out), pitch, abi.ptr(avg)), "orc_postprocess")
+    return out, e.value, avg
+
+
+def upscale(mode, scale, src, dst_width, dst_height):
+    lib = load()
+    src = np.ascontiguousarray(src, dtype=np.uint32)
+    out = np.zeros((dst_height, dst_width), np.uint32)
+    _check(lib.orc_upscale(mode, scale, abi.ptr(src), abi.ptr(out), dst_width, dst_height, dst_width), "orc_upscale")
+    return out
+
+
+def gaussian_kernel(sigma, radius):
+    out = np.zeros(33, np.float32)
+    _check(load().orc_gaussian_kernel(float(sigma), radius, abi.ptr(out)), "orc_gaussian_kernel")
+    return out

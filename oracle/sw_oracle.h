@@ -1,0 +1,51 @@
+// Test infrastructure: C ABI of the CPU oracle for the GB300 rendering path.
+//
+// The oracle restates the reference's CPU renderer for the hot path (surface building, polygon
+// rasterisation, HDR postprocessing, frame upscaling) in plain C++. Only the tests, the smoke check
+// and the CPU-baseline leg of bench.py load it; the product never does. It consumes the same
+// descriptors as the GPU library (include/swgpu.h), so both sides see identical inputs.
+#pragma once
+
+#include "../include/swgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* build_polygons_surfaces' per-polygon work (partial_renderer.rs:1682-1831): builds every surface of
+ * `surfaces` into `arena` (pixel_format texels). num_threads 0/1 = sequential, N = N worker threads
+ * with one task per surface (the reference's rayon par_iter). Returns 0 or a negative SwStatus. */
+int orc_build_surfaces(const SwCreateInfo* data, const SwSurfaceDesc* surfaces, uint32_t num_surfaces,
+	const SwLight* lights, uint32_t num_lights, const SwFrameParams* frame, void* arena, uint64_t arena_texels,
+	uint32_t num_threads);
+
+/* Rasterizer::fill_polygon for every draw in order (perform_rasterization, partial_renderer.rs:1192-1283)
+ * into `framebuffer` (pixel_format of frame, pitch in pixels). num_threads 0/1 = the reference's
+ * single-thread path (one full-screen ClipRect); N > 1 = split_rect into N regions with one ClipRect each.
+ * Out-of-range texel fetches (impossible for well-formed draws) read texel 0 and are counted in
+ * *bad_fetches when the pointer is non-null. */
+int orc_rasterize(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices,
+	const void* arena, uint64_t arena_texels, const SwFrameParams* frame, void* framebuffer, uint32_t pitch,
+	uint32_t num_threads, uint64_t* bad_fetches);
+
+/* draw_background, partial_renderer.rs:3987-4009, colour (32,16,8) via ColorVec. */
+int orc_clear_background(const SwFrameParams* frame, void* framebuffer, uint32_t pitch);
+
+/* Postprocessor::perform_postprocessing (postprocessor.rs:68-204) single-threaded: reads the HDR
+ * Color64 frame (width*height, tightly packed), writes Color32 to dst (pitch in pixels) and updates
+ * *exposure in place. If average_color is non-null it receives the frame's average colour (4 lanes). */
+int orc_postprocess(const SwPostConfig* config, const uint64_t* hdr, uint32_t width, uint32_t height,
+	float frame_duration_s, const float color_modulate[3], float* exposure, uint32_t* dst, uint32_t pitch,
+	float* average_color);
+
+/* FrameUpscaler::perform_upscale (frame_upscaler.rs:42-239). */
+int orc_upscale(uint32_t mode, uint32_t scale, const uint32_t* src, uint32_t* dst, uint32_t dst_width,
+	uint32_t dst_height, uint32_t dst_pitch);
+
+/* compute_gaussian_kernel (postprocessor.rs:1026-1045) and the integer blur weights of
+ * perform_blur_impl (postprocessor.rs:848-907); exported for known-answer tests. */
+int orc_gaussian_kernel(float sigma, uint32_t radius, float* out33);
+
+#ifdef __cplusplus
+}
+#endif

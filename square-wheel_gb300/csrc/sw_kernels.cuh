@@ -1,0 +1,119 @@
+// Kernel argument blocks and launch entry points of the GB300 rendering path.
+#pragma once
+
+#include "sw_device.cuh"
+
+namespace swgpu
+{
+
+struct SurfaceKernelArgs
+{
+	const SwSurfaceDesc* surfaces;
+	const uint64_t* work_prefix; // num_surfaces + 1 entries, texel prefix sums in descriptor order
+	uint32_t num_surfaces;
+	uint32_t directional;
+	uint64_t total_work;
+	const uint64_t* texels;
+	const SwTextureMip* texture_mips;
+	const uint32_t* emissive_pixels;
+	const SwEmissiveMip* emissive_mips;
+	const float* lightmaps;
+	const SwDirectionalLightmapElement* directional_lightmaps;
+	const SwLight* lights;
+	float cam_pos[3];
+	void* arena;
+};
+
+int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream);
+
+// ---- rasteriser ----
+
+// One polygon part of the edge walk (a draw_func call of fill_polygon_impl_2_static_params,
+// src/square_wheel/rasterizer.rs:198-254), reduced to what a pixel needs to find its span.
+struct RasterPart
+{
+	int32_t y_start_int; // first row, clipped to the frame
+	int32_t y_end_int;   // one past the last row, clipped
+	int32_t x_left0;     // x_left at row y_start_int (includes the +0.5 bias), 16.16
+	int32_t x_right0;
+	int32_t dx_dy_left;
+	int32_t dx_dy_right;
+	// Affine mode only (rasterizer.rs:616-682): per-edge texture coordinates at row y_start_int and
+	// their per-row steps, 16.16.
+	int32_t tc_left0[2];
+	int32_t tc_right0[2];
+	int32_t d_tc_left[2];
+	int32_t d_tc_right[2];
+};
+
+#define SW_RASTER_MAX_PARTS SW_MAX_POLYGON_VERTICES
+
+// Per-draw setup shared by all of its parts (integer plane equations of fill_polygon_part*,
+// rasterizer.rs:287-310), plus the pixel bounding box used for tile binning.
+struct RasterDraw
+{
+	int64_t d_inv_z_dx, d_inv_z_dy, inv_z_k;
+	int64_t d_tc_dx[2], d_tc_dy[2], tc_k[2];
+	uint64_t tex_offset;
+	uint32_t tex_w, tex_h;
+	uint32_t mode, blend;
+	uint32_t num_parts;
+	uint32_t reserved;
+};
+
+// Conservative pixel bounds of a draw: [x0, x1) x [y0, y1); empty when x0 >= x1 or y0 >= y1.
+struct RasterBox
+{
+	int16_t x0, y0, x1, y1;
+};
+
+struct RasterArgs
+{
+	const SwDrawCmd* draws;
+	const SwVertex16* vertices;
+	uint32_t num_draws;
+	int32_t width, height;
+	uint32_t clear_background;
+	RasterDraw* rdraws;
+	RasterPart* parts; // num_draws * SW_RASTER_MAX_PARTS
+	RasterBox* boxes;
+	const void* arena;
+	uint64_t arena_texels;
+	void* framebuffer; // width * height pixels, tightly packed
+	unsigned int* error_counter;
+};
+
+int launch_raster(const RasterArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream);
+
+// ---- postprocessor / upscaler ----
+
+struct PostArgs
+{
+	const uint64_t* hdr;
+	uint32_t width, height;
+	uint32_t scale; // bloom buffer scale S (2, 4 or 8)
+	uint32_t bw, bh;
+	uint64_t* bloom0;
+	uint64_t* bloom1;
+	int32_t* line_sums; // bh * 4 lanes (bloom) or unused
+	float* line_sums_f; // height * 4 lanes (no bloom)
+	float* average;     // 4 lanes
+	uint32_t radius;
+	int32_t kernel_h[33];
+	int32_t kernel_v[33];
+	float inv_scale[4]; // TonemappingFunction::inv_scale_vec lanes
+	float inv_255[4];
+	uint32_t linear_filter;
+	uint32_t use_bloom;
+	uint32_t* dst;
+	uint32_t dst_pitch;
+};
+
+int launch_postprocess(const PostArgs& args, int num_sms, cudaStream_t stream);
+
+int launch_upscale(uint32_t mode, uint32_t scale, const uint32_t* src, uint32_t* dst, uint32_t dst_width,
+	uint32_t dst_height, uint32_t dst_pitch, cudaStream_t stream);
+
+int launch_fill(void* dst, uint64_t count, uint64_t value, uint32_t bytes_per_pixel, cudaStream_t stream);
+
+} // namespace swgpu

@@ -1,0 +1,763 @@
+// C ABI of the GB300 rendering path (include/swgpu.h): context, device memory, uploads, launches.
+//
+// Device memory layout (HBM):
+//   static, uploaded once by sw_create: all material texture mips as one TextureElement array, their
+//   SwTextureMip table, emissive Color32 mips + table, simple (12 B) and directional (40 B) lightmap
+//   element arrays;
+//   per frame, grown on demand and reused: lights, surface descriptors + texel prefix sums, the surface
+//   arena (one Color32/Color64 texel per surface texel, surfaces contiguous and row-major), draw
+//   commands + vertices, raster setup output (per-draw equations, parts, boxes), the frame buffer
+//   (width*height pixels), bloom buffers and the exposure-average scratch.
+// Host->device uploads go through pinned staging buffers on the context's stream. Every descriptor is
+// validated on the host before launch so that no kernel can read outside its buffers.
+#include "sw_kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace swgpu;
+
+namespace
+{
+
+struct DevBuf
+{
+	void* ptr = nullptr;
+	size_t bytes = 0;
+};
+
+struct Staging
+{
+	void* host = nullptr;
+	size_t bytes = 0;
+	cudaEvent_t done = nullptr;
+	bool pending = false;
+};
+
+} // namespace
+
+struct SwCtx
+{
+	int device = 0;
+	int num_sms = 0;
+	cudaStream_t stream = nullptr;
+	std::string last_error;
+
+	// static
+	DevBuf texels, texture_mips, emissive, emissive_mips, lightmaps, dir_lightmaps;
+	std::vector<SwTextureMip> h_texture_mips;
+	std::vector<SwEmissiveMip> h_emissive_mips;
+	uint64_t num_lightmap_elements = 0, num_dir_lightmap_elements = 0;
+	uint64_t num_texels = 0, num_emissive_pixels = 0;
+
+	// frame
+	bool frame_open = false;
+	SwFrameParams frame{};
+	uint32_t num_lights = 0;
+	DevBuf lights, surfaces, work_prefix, arena;
+	uint64_t arena_texels = 0;
+	uint32_t arena_format = SW_PIXEL_C32;
+	bool arena_valid = false;
+	uint32_t last_num_surfaces = 0, last_surface_format = SW_PIXEL_C32, last_max_light = 0;
+	uint64_t last_surface_work = 0;
+	bool last_surface_directional = false;
+	DevBuf draws, vertices, rdraws, parts, boxes;
+	uint32_t num_draws = 0;
+	bool draws_valid = false;
+	DevBuf framebuffer;
+	uint32_t fb_width = 0, fb_height = 0, fb_format = SW_PIXEL_C32;
+	bool fb_valid = false;
+
+	// postprocessor
+	DevBuf bloom0, bloom1, line_sums, line_sums_f, average, error_counter;
+	float exposure = 1.0f;
+	bool exposure_pending = false;
+	SwPostConfig pending_config{};
+	float pending_dt = 0.0f;
+	float* h_average = nullptr; // pinned, 4 floats
+	cudaEvent_t average_ready = nullptr;
+
+	Staging stage_lights, stage_surfaces, stage_prefix, stage_draws, stage_vertices, stage_io;
+
+	// upscale scratch (src/dst copies for host buffers)
+	DevBuf up_src, up_dst;
+
+	SwStats stats{};
+};
+
+namespace
+{
+
+int fail(SwCtx* ctx, int code, const char* fmt, ...)
+{
+	char buf[512];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof(buf), fmt, ap);
+	va_end(ap);
+	if (ctx) ctx->last_error = buf;
+	return code;
+}
+
+int cuda_fail(SwCtx* ctx, cudaError_t e, const char* what)
+{
+	return fail(ctx, SW_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define SW_CUDA(ctx, call)                                  \
+	do                                                      \
+	{                                                       \
+		cudaError_t e_ = (call);                            \
+		if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+	} while (0)
+
+int ensure(SwCtx* ctx, DevBuf& b, size_t bytes)
+{
+	if (bytes <= b.bytes && b.ptr) return SW_OK;
+	size_t want = std::max(bytes, b.bytes + b.bytes / 2);
+	if (want == 0) want = 256;
+	if (b.ptr)
+	{
+		cudaError_t e = cudaStreamSynchronize(ctx->stream);
+		if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamSynchronize");
+		cudaFree(b.ptr);
+		b.ptr = nullptr;
+		b.bytes = 0;
+	}
+	cudaError_t e = cudaMalloc(&b.ptr, want);
+	if (e != cudaSuccess)
+	{
+		cudaGetLastError();
+		return fail(ctx, SW_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu bytes) failed: %s", want, cudaGetErrorString(e));
+	}
+	b.bytes = want;
+	return SW_OK;
+}
+
+void release(DevBuf& b)
+{
+	if (b.ptr) cudaFree(b.ptr);
+	b.ptr = nullptr;
+	b.bytes = 0;
+}
+
+// Copy `bytes` from host memory `src` into device buffer `dst` through a pinned staging buffer.
+int upload(SwCtx* ctx, Staging& st, void* dst, const void* src, size_t bytes)
+{
+	if (bytes == 0) return SW_OK;
+	if (st.pending)
+	{
+		SW_CUDA(ctx, cudaEventSynchronize(st.done));
+		st.pending = false;
+	}
+	if (st.bytes < bytes)
+	{
+		if (st.host) cudaFreeHost(st.host);
+		st.host = nullptr;
+		size_t want = std::max(bytes, st.bytes * 2);
+		SW_CUDA(ctx, cudaMallocHost(&st.host, want));
+		st.bytes = want;
+	}
+	if (!st.done) SW_CUDA(ctx, cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming));
+	std::memcpy(st.host, src, bytes);
+	SW_CUDA(ctx, cudaMemcpyAsync(dst, st.host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+	SW_CUDA(ctx, cudaEventRecord(st.done, ctx->stream));
+	st.pending = true;
+	return SW_OK;
+}
+
+int upload_static(SwCtx* ctx, DevBuf& b, const void* src, size_t bytes)
+{
+	int r = ensure(ctx, b, bytes ? bytes : 16);
+	if (r) return r;
+	if (bytes) SW_CUDA(ctx, cudaMemcpy(b.ptr, src, bytes, cudaMemcpyHostToDevice));
+	return SW_OK;
+}
+
+// Device -> user buffer copy of a width x height image with row pitches in pixels.
+int copy_out(SwCtx* ctx, void* dst, uint32_t dst_pitch, int dst_is_device, const void* src, uint32_t src_pitch,
+	uint32_t width, uint32_t height, uint32_t bpp)
+{
+	const size_t row = size_t(width) * bpp;
+	if (dst_is_device)
+	{
+		SW_CUDA(ctx, cudaMemcpy2DAsync(dst, size_t(dst_pitch) * bpp, src, size_t(src_pitch) * bpp, row, height,
+						 cudaMemcpyDeviceToDevice, ctx->stream));
+		return SW_OK;
+	}
+	Staging& st = ctx->stage_io;
+	const size_t bytes = row * height;
+	if (st.pending)
+	{
+		SW_CUDA(ctx, cudaEventSynchronize(st.done));
+		st.pending = false;
+	}
+	if (st.bytes < bytes)
+	{
+		if (st.host) cudaFreeHost(st.host);
+		st.host = nullptr;
+		SW_CUDA(ctx, cudaMallocHost(&st.host, bytes));
+		st.bytes = bytes;
+	}
+	SW_CUDA(ctx, cudaMemcpy2DAsync(st.host, row, src, size_t(src_pitch) * bpp, row, height, cudaMemcpyDeviceToHost, ctx->stream));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	for (uint32_t y = 0; y < height; ++y)
+		std::memcpy(static_cast<char*>(dst) + size_t(y) * dst_pitch * bpp, static_cast<const char*>(st.host) + y * row, row);
+	return SW_OK;
+}
+
+int check_kernel(SwCtx* ctx, int launch_result, const char* what)
+{
+	if (launch_result != 0)
+		return fail(ctx, SW_ERR_CUDA, "%s launch failed: %s", what, cudaGetErrorString(cudaError_t(launch_result)));
+	return SW_OK;
+}
+
+uint32_t bpp_of(uint32_t format) { return format == SW_PIXEL_C64 ? 8u : 4u; }
+
+// f32 -> i32 `as` conversion: truncating, saturating, NaN -> 0.
+int32_t f2i32_sat(float x)
+{
+	if (x != x) return 0;
+	if (x >= 2147483648.0f) return INT32_MAX;
+	if (x <= -2147483648.0f) return INT32_MIN;
+	return int32_t(x);
+}
+
+// Apply the exposure update of the previous postprocessed frame (update_exposure,
+// src/square_wheel/postprocessor.rs:206-223, with get_color_brightness :1047-1051), on the host in f32
+// with the C library's expf/logf/powf exactly as the reference does.
+int finalize_exposure(SwCtx* ctx)
+{
+	if (!ctx->exposure_pending) return SW_OK;
+	SW_CUDA(ctx, cudaEventSynchronize(ctx->average_ready));
+	ctx->exposure_pending = false;
+	const SwPostConfig& c = ctx->pending_config;
+	const float* avg = ctx->h_average;
+	const float brightness_raw = (avg[0] + avg[1] + avg[2]) * 0.33f;
+	const float brightness = std::fmin(std::fmax(brightness_raw, 1.0f / 1024.0f), 65536.0f) / 255.0f;
+	const float target =
+		std::pow(brightness / c.zero_level_brightness, c.brightness_scale_power) * 0.5f * c.base_brightness / brightness;
+	const float clamped = std::fmin(std::fmax(target, c.min_exposure), c.max_exposure);
+	const float mix = std::exp(-c.exposure_update_speed * ctx->pending_dt);
+	ctx->exposure = std::exp(std::log(ctx->exposure) * mix + std::log(clamped) * (1.0f - mix));
+	return SW_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int sw_create(const SwCreateInfo* info, SwCtx** out_ctx)
+{
+	if (!info || !out_ctx) return SW_ERR_INVALID_ARGUMENT;
+	*out_ctx = nullptr;
+	if (info->abi_version != SWGPU_ABI_VERSION) return SW_ERR_INVALID_ARGUMENT;
+	int count = 0;
+	if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+	{
+		cudaGetLastError();
+		return SW_ERR_NO_DEVICE;
+	}
+	if (int(info->device) >= count) return SW_ERR_INVALID_ARGUMENT;
+	// Validate static tables.
+	for (uint32_t i = 0; i < info->num_texture_mips; ++i)
+	{
+		const SwTextureMip& m = info->texture_mips[i];
+		if (m.width == 0 || m.height == 0 || m.offset + uint64_t(m.width) * m.height > info->num_texels)
+			return SW_ERR_INVALID_ARGUMENT;
+	}
+	for (uint32_t i = 0; i < info->num_emissive_mips; ++i)
+	{
+		const SwEmissiveMip& m = info->emissive_mips[i];
+		if (m.width == 0 || m.height == 0 || m.offset + uint64_t(m.width) * m.height > info->num_emissive_pixels)
+			return SW_ERR_INVALID_ARGUMENT;
+	}
+
+	SwCtx* ctx = new (std::nothrow) SwCtx();
+	if (!ctx) return SW_ERR_OUT_OF_MEMORY;
+	auto bail = [&](int r) {
+		sw_destroy(ctx);
+		return r;
+	};
+	ctx->device = int(info->device);
+	if (cudaSetDevice(ctx->device) != cudaSuccess) return bail(SW_ERR_CUDA);
+	if (cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess)
+		return bail(SW_ERR_CUDA);
+	if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(SW_ERR_CUDA);
+	if (cudaEventCreateWithFlags(&ctx->average_ready, cudaEventDisableTiming) != cudaSuccess) return bail(SW_ERR_CUDA);
+	if (cudaMallocHost(reinterpret_cast<void**>(&ctx->h_average), 4 * sizeof(float)) != cudaSuccess)
+		return bail(SW_ERR_CUDA);
+
+	int r;
+	if ((r = upload_static(ctx, ctx->texels, info->texels, info->num_texels * 8))) return bail(r);
+	if ((r = upload_static(ctx, ctx->texture_mips, info->texture_mips, info->num_texture_mips * sizeof(SwTextureMip))))
+		return bail(r);
+	if ((r = upload_static(ctx, ctx->emissive, info->emissive_pixels, info->num_emissive_pixels * 4))) return bail(r);
+	if ((r = upload_static(ctx, ctx->emissive_mips, info->emissive_mips, info->num_emissive_mips * sizeof(SwEmissiveMip))))
+		return bail(r);
+	if ((r = upload_static(ctx, ctx->lightmaps, info->lightmaps, info->num_lightmap_elements * 12))) return bail(r);
+	if ((r = upload_static(ctx, ctx->dir_lightmaps, info->directional_lightmaps,
+			 info->num_directional_lightmap_elements * sizeof(SwDirectionalLightmapElement))))
+		return bail(r);
+	ctx->h_texture_mips.assign(info->texture_mips, info->texture_mips + info->num_texture_mips);
+	ctx->h_emissive_mips.assign(info->emissive_mips, info->emissive_mips + info->num_emissive_mips);
+	ctx->num_texels = info->num_texels;
+	ctx->num_emissive_pixels = info->num_emissive_pixels;
+	ctx->num_lightmap_elements = info->num_lightmap_elements;
+	ctx->num_dir_lightmap_elements = info->num_directional_lightmap_elements;
+	if ((r = ensure(ctx, ctx->error_counter, 16))) return bail(r);
+	if (cudaMemset(ctx->error_counter.ptr, 0, 16) != cudaSuccess) return bail(SW_ERR_CUDA);
+	if ((r = ensure(ctx, ctx->average, 16))) return bail(r);
+	if (info->max_surface_texels && (r = ensure(ctx, ctx->arena, info->max_surface_texels * 8))) return bail(r);
+	*out_ctx = ctx;
+	return SW_OK;
+}
+
+int sw_destroy(SwCtx* ctx)
+{
+	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
+	cudaSetDevice(ctx->device);
+	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+	DevBuf* bufs[] = {&ctx->texels, &ctx->texture_mips, &ctx->emissive, &ctx->emissive_mips, &ctx->lightmaps,
+		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
+		&ctx->rdraws, &ctx->parts, &ctx->boxes, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
+		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst};
+	for (DevBuf* b : bufs) release(*b);
+	Staging* st[] = {&ctx->stage_lights, &ctx->stage_surfaces, &ctx->stage_prefix, &ctx->stage_draws,
+		&ctx->stage_vertices, &ctx->stage_io};
+	for (Staging* s : st)
+	{
+		if (s->host) cudaFreeHost(s->host);
+		if (s->done) cudaEventDestroy(s->done);
+	}
+	if (ctx->h_average) cudaFreeHost(ctx->h_average);
+	if (ctx->average_ready) cudaEventDestroy(ctx->average_ready);
+	if (ctx->stream) cudaStreamDestroy(ctx->stream);
+	delete ctx;
+	return SW_OK;
+}
+
+const char* sw_last_error(const SwCtx* ctx)
+{
+	if (!ctx) return "null context";
+	return ctx->last_error.c_str();
+}
+
+int sw_sync(SwCtx* ctx)
+{
+	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	return SW_OK;
+}
+
+int sw_get_stream(SwCtx* ctx, void** out_stream)
+{
+	if (!ctx || !out_stream) return SW_ERR_INVALID_ARGUMENT;
+	*out_stream = ctx->stream;
+	return SW_OK;
+}
+
+int sw_frame_begin(SwCtx* ctx, const SwFrameParams* params, const SwLight* lights, uint32_t num_lights)
+{
+	if (!ctx || !params || (num_lights && !lights)) return SW_ERR_INVALID_ARGUMENT;
+	if (params->pixel_format > SW_PIXEL_C64) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "bad pixel format");
+	if (params->width == 0 || params->height == 0 || params->width > 16384 || params->height > 16384)
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "bad frame size %ux%u", params->width, params->height);
+	if (params->use_directional_lightmaps && ctx->num_dir_lightmap_elements == 0)
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "directional lightmaps requested but none uploaded");
+	if (num_lights > 65535) return fail(ctx, SW_ERR_LIMIT, "too many lights");
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	ctx->frame = *params;
+	ctx->num_lights = num_lights;
+	int r = ensure(ctx, ctx->lights, std::max<size_t>(num_lights, 1) * sizeof(SwLight));
+	if (r) return r;
+	if ((r = upload(ctx, ctx->stage_lights, ctx->lights.ptr, lights, num_lights * sizeof(SwLight)))) return r;
+	ctx->frame_open = true;
+	ctx->arena_valid = false;
+	ctx->draws_valid = false;
+	return SW_OK;
+}
+
+static int launch_surfaces(SwCtx* ctx)
+{
+	SurfaceKernelArgs a;
+	a.surfaces = static_cast<const SwSurfaceDesc*>(ctx->surfaces.ptr);
+	a.work_prefix = static_cast<const uint64_t*>(ctx->work_prefix.ptr);
+	a.num_surfaces = ctx->last_num_surfaces;
+	a.directional = ctx->last_surface_directional ? 1u : 0u;
+	a.total_work = ctx->last_surface_work;
+	a.texels = static_cast<const uint64_t*>(ctx->texels.ptr);
+	a.texture_mips = static_cast<const SwTextureMip*>(ctx->texture_mips.ptr);
+	a.emissive_pixels = static_cast<const uint32_t*>(ctx->emissive.ptr);
+	a.emissive_mips = static_cast<const SwEmissiveMip*>(ctx->emissive_mips.ptr);
+	a.lightmaps = static_cast<const float*>(ctx->lightmaps.ptr);
+	a.directional_lightmaps = static_cast<const SwDirectionalLightmapElement*>(ctx->dir_lightmaps.ptr);
+	a.lights = static_cast<const SwLight*>(ctx->lights.ptr);
+	for (int i = 0; i < 3; ++i) a.cam_pos[i] = ctx->frame.cam_pos[i];
+	a.arena = ctx->arena.ptr;
+	int r = check_kernel(ctx, launch_surface_build(a, ctx->frame.pixel_format, ctx->num_sms, ctx->stream), "surface build");
+	if (r) return r;
+	ctx->arena_valid = true;
+	ctx->stats.surfaces += ctx->last_num_surfaces;
+	ctx->stats.surface_texels += ctx->last_surface_work;
+	return SW_OK;
+}
+
+int sw_submit_surfaces(SwCtx* ctx, const SwSurfaceDesc* surfaces, uint32_t num_surfaces, uint64_t total_texels)
+{
+	if (!ctx || (num_surfaces && !surfaces)) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_submit_surfaces");
+	const bool directional = ctx->frame.use_directional_lightmaps != 0;
+	const uint64_t lm_elems = directional ? ctx->num_dir_lightmap_elements : ctx->num_lightmap_elements;
+	std::vector<uint64_t> prefix(size_t(num_surfaces) + 1);
+	uint64_t acc = 0;
+	for (uint32_t i = 0; i < num_surfaces; ++i)
+	{
+		const SwSurfaceDesc& s = surfaces[i];
+		prefix[i] = acc;
+		const uint64_t area = uint64_t(s.size[0]) * s.size[1];
+		if (s.size[0] == 0 || s.size[1] == 0 || s.size[0] > 65536 || s.size[1] > 65536)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: bad size", i);
+		if (s.out_offset + area > total_texels) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: outside arena", i);
+		if ((s.flags & SW_SURF_DIFFUSE_LAYER) && s.texture_mip >= ctx->h_texture_mips.size())
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: bad texture mip", i);
+		if (s.emissive_mip != SW_NO_EMISSIVE && s.emissive_mip >= ctx->h_emissive_mips.size())
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: bad emissive mip", i);
+		if (s.num_lights > SW_MAX_POLYGON_LIGHTS) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: too many lights", i);
+		for (uint32_t l = 0; l < s.num_lights; ++l)
+			if (s.lights[l] >= ctx->num_lights) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: bad light index", i);
+		if ((s.flags & SW_SURF_DIFFUSE_LAYER) && s.lightmap_offset != SW_NO_LIGHTMAP)
+		{
+			// Every texel reads lightmap rows lv, lv+1 and columns lu, lu+1 (surfaces.rs:479-543).
+			if (s.lightmap_scale_log2 > 4) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: bad lightmap scale", i);
+			const uint64_t lu_max = (uint64_t(s.size[0]) - 1 + s.lightmap_tc_shift[0]) >> s.lightmap_scale_log2;
+			const uint64_t lv_max = (uint64_t(s.size[1]) - 1 + s.lightmap_tc_shift[1]) >> s.lightmap_scale_log2;
+			if (lu_max + 1 >= s.lightmap_size[0] || lv_max + 1 >= s.lightmap_size[1] ||
+				uint64_t(s.lightmap_offset) + uint64_t(s.lightmap_size[0]) * s.lightmap_size[1] > lm_elems)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: lightmap reads out of range", i);
+		}
+		acc += area;
+	}
+	prefix[num_surfaces] = acc;
+	const uint32_t bpp = bpp_of(ctx->frame.pixel_format);
+	int r;
+	if ((r = ensure(ctx, ctx->arena, std::max<uint64_t>(total_texels, 1) * bpp))) return r;
+	if ((r = ensure(ctx, ctx->surfaces, std::max<size_t>(num_surfaces, 1) * sizeof(SwSurfaceDesc)))) return r;
+	if ((r = ensure(ctx, ctx->work_prefix, prefix.size() * 8))) return r;
+	if ((r = upload(ctx, ctx->stage_surfaces, ctx->surfaces.ptr, surfaces, num_surfaces * sizeof(SwSurfaceDesc)))) return r;
+	if ((r = upload(ctx, ctx->stage_prefix, ctx->work_prefix.ptr, prefix.data(), prefix.size() * 8))) return r;
+	ctx->arena_texels = total_texels;
+	ctx->arena_format = ctx->frame.pixel_format;
+
+	ctx->last_num_surfaces = num_surfaces;
+	ctx->last_surface_work = acc;
+	ctx->last_surface_directional = directional;
+	ctx->last_surface_format = ctx->frame.pixel_format;
+	ctx->last_max_light = 0;
+	for (uint32_t i = 0; i < num_surfaces; ++i)
+		for (uint32_t l = 0; l < surfaces[i].num_lights; ++l)
+			ctx->last_max_light = std::max<uint32_t>(ctx->last_max_light, surfaces[i].lights[l] + 1u);
+	return launch_surfaces(ctx);
+}
+
+int sw_rebuild_surfaces(SwCtx* ctx)
+{
+	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_rebuild_surfaces");
+	if (ctx->last_surface_work == 0 && ctx->last_num_surfaces == 0) return fail(ctx, SW_ERR_STATE, "no surfaces submitted");
+	if (ctx->frame.pixel_format != ctx->last_surface_format ||
+		(ctx->frame.use_directional_lightmaps != 0) != ctx->last_surface_directional)
+		return fail(ctx, SW_ERR_STATE, "frame format or lightmap kind changed since sw_submit_surfaces");
+	if (ctx->last_max_light > ctx->num_lights) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "fewer lights than the surfaces use");
+	return launch_surfaces(ctx);
+}
+
+int sw_set_surfaces(SwCtx* ctx, const void* texels, uint64_t total_texels)
+{
+	if (!ctx || (total_texels && !texels)) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_set_surfaces");
+	const uint32_t bpp = bpp_of(ctx->frame.pixel_format);
+	int r;
+	if ((r = ensure(ctx, ctx->arena, std::max<uint64_t>(total_texels, 1) * bpp))) return r;
+	if ((r = upload(ctx, ctx->stage_io, ctx->arena.ptr, texels, total_texels * bpp))) return r;
+	ctx->arena_texels = total_texels;
+	ctx->arena_format = ctx->frame.pixel_format;
+	ctx->arena_valid = true;
+	return SW_OK;
+}
+
+int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices)
+{
+	if (!ctx || (num_draws && (!draws || !vertices))) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_submit_draws");
+	if (!ctx->arena_valid && num_draws) return fail(ctx, SW_ERR_STATE, "sw_submit_surfaces must precede sw_submit_draws");
+	for (uint32_t i = 0; i < num_draws; ++i)
+	{
+		const SwDrawCmd& d = draws[i];
+		if (d.vertex_count < 3 || d.vertex_count > SW_MAX_POLYGON_VERTICES)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: bad vertex count", i);
+		if (uint64_t(d.first_vertex) + d.vertex_count > num_vertices)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: vertices out of range", i);
+		if (d.mode > SW_RASTER_AFFINE || d.blend > SW_BLEND_ALPHA_BLEND)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: bad mode/blend", i);
+		if (d.tex_size[0] == 0 || d.tex_size[1] == 0 || d.tex_offset + uint64_t(d.tex_size[0]) * d.tex_size[1] > ctx->arena_texels)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: texture outside the surface arena", i);
+	}
+	int r;
+	if ((r = ensure(ctx, ctx->draws, std::max<size_t>(num_draws, 1) * sizeof(SwDrawCmd)))) return r;
+	if ((r = ensure(ctx, ctx->vertices, std::max<size_t>(num_vertices, 1) * sizeof(SwVertex16)))) return r;
+	if ((r = ensure(ctx, ctx->rdraws, std::max<size_t>(num_draws, 1) * sizeof(RasterDraw)))) return r;
+	if ((r = ensure(ctx, ctx->parts, std::max<size_t>(num_draws, 1) * SW_RASTER_MAX_PARTS * sizeof(RasterPart)))) return r;
+	if ((r = ensure(ctx, ctx->boxes, std::max<size_t>(num_draws, 1) * sizeof(RasterBox)))) return r;
+	if ((r = upload(ctx, ctx->stage_draws, ctx->draws.ptr, draws, num_draws * sizeof(SwDrawCmd)))) return r;
+	if ((r = upload(ctx, ctx->stage_vertices, ctx->vertices.ptr, vertices, num_vertices * sizeof(SwVertex16)))) return r;
+	ctx->num_draws = num_draws;
+	ctx->draws_valid = true;
+	ctx->stats.draws += num_draws;
+	return SW_OK;
+}
+
+int sw_render(SwCtx* ctx, void* dst, uint32_t pitch, int dst_is_device)
+{
+	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->frame_open || !ctx->draws_valid) return fail(ctx, SW_ERR_STATE, "nothing submitted for this frame");
+	if (ctx->num_draws && ctx->arena_format != ctx->frame.pixel_format)
+		return fail(ctx, SW_ERR_STATE, "surface arena format differs from frame format");
+	const uint32_t w = ctx->frame.width, h = ctx->frame.height, fmt = ctx->frame.pixel_format, bpp = bpp_of(fmt);
+	if (dst && pitch < w) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");
+	int r;
+	if ((r = ensure(ctx, ctx->framebuffer, size_t(w) * h * bpp))) return r;
+	if (!ctx->fb_valid || ctx->fb_width != w || ctx->fb_height != h || ctx->fb_format != fmt)
+	{
+		// A new frame buffer starts black, like a freshly allocated HDR buffer (postprocessor.rs:56-66).
+		SW_CUDA(ctx, cudaMemsetAsync(ctx->framebuffer.ptr, 0, size_t(w) * h * bpp, ctx->stream));
+		ctx->fb_width = w;
+		ctx->fb_height = h;
+		ctx->fb_format = fmt;
+		ctx->fb_valid = true;
+	}
+	RasterArgs a;
+	a.draws = static_cast<const SwDrawCmd*>(ctx->draws.ptr);
+	a.vertices = static_cast<const SwVertex16*>(ctx->vertices.ptr);
+	a.num_draws = ctx->num_draws;
+	a.width = int32_t(w);
+	a.height = int32_t(h);
+	a.clear_background = ctx->frame.clear_background;
+	a.rdraws = static_cast<RasterDraw*>(ctx->rdraws.ptr);
+	a.parts = static_cast<RasterPart*>(ctx->parts.ptr);
+	a.boxes = static_cast<RasterBox*>(ctx->boxes.ptr);
+	a.arena = ctx->arena.ptr;
+	a.arena_texels = ctx->arena_texels;
+	a.framebuffer = ctx->framebuffer.ptr;
+	a.error_counter = static_cast<unsigned int*>(ctx->error_counter.ptr);
+	if ((r = check_kernel(ctx, launch_raster(a, fmt, ctx->num_sms, ctx->stream), "raster"))) return r;
+	ctx->frame_open = false;
+	if (dst) return copy_out(ctx, dst, pitch, dst_is_device, ctx->framebuffer.ptr, w, w, h, bpp);
+	return SW_OK;
+}
+
+int sw_set_framebuffer(SwCtx* ctx, const void* src, uint32_t width, uint32_t height, uint32_t pixel_format, int src_is_device)
+{
+	if (!ctx || !src || width == 0 || height == 0 || pixel_format > SW_PIXEL_C64) return SW_ERR_INVALID_ARGUMENT;
+	const uint32_t bpp = bpp_of(pixel_format);
+	const size_t bytes = size_t(width) * height * bpp;
+	int r;
+	if ((r = ensure(ctx, ctx->framebuffer, bytes))) return r;
+	if (src_is_device)
+		SW_CUDA(ctx, cudaMemcpyAsync(ctx->framebuffer.ptr, src, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+	else if ((r = upload(ctx, ctx->stage_io, ctx->framebuffer.ptr, src, bytes)))
+		return r;
+	ctx->fb_width = width;
+	ctx->fb_height = height;
+	ctx->fb_format = pixel_format;
+	ctx->fb_valid = true;
+	return SW_OK;
+}
+
+int sw_postprocess(SwCtx* ctx, const SwPostConfig* config, float frame_duration_s, const float color_modulate[3], void* dst,
+	uint32_t pitch, int dst_is_device)
+{
+	if (!ctx || !config || !color_modulate || !dst) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->fb_valid || ctx->fb_format != SW_PIXEL_C64)
+		return fail(ctx, SW_ERR_STATE, "postprocessing needs a colour64 frame");
+	const uint32_t w = ctx->fb_width, h = ctx->fb_height;
+	if (pitch < w) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");
+	int r;
+	if ((r = finalize_exposure(ctx))) return r;
+
+	PostArgs a;
+	std::memset(&a, 0, sizeof(a));
+	a.hdr = static_cast<const uint64_t*>(ctx->framebuffer.ptr);
+	a.width = w;
+	a.height = h;
+	a.use_bloom = config->bloom_sigma > 0.0f ? 1u : 0u;
+	a.linear_filter = config->linear_bloom_filter ? 1u : 0u;
+	// TonemappingFunction::new (postprocessor.rs:1005-1017), lanes [b, g, r, a].
+	const float inv_255 = 1.0f / 255.0f;
+	a.inv_scale[0] = 1.0f / (ctx->exposure * color_modulate[2]);
+	a.inv_scale[1] = 1.0f / (ctx->exposure * color_modulate[1]);
+	a.inv_scale[2] = 1.0f / (ctx->exposure * color_modulate[0]);
+	a.inv_scale[3] = 0.0f;
+	a.inv_255[0] = a.inv_255[1] = a.inv_255[2] = inv_255;
+	a.inv_255[3] = 0.0f;
+	a.average = static_cast<float*>(ctx->average.ptr);
+	if (a.use_bloom)
+	{
+		// perform_bloom, postprocessor.rs:729-789 (kernel weights computed here, on the host).
+		const int log2 = std::min(std::max(int(config->bloom_buffer_scale_log2), 1), 3);
+		const uint32_t S = 1u << log2;
+		a.scale = S;
+		a.bw = w / S;
+		a.bh = h / S;
+		if (a.bw < 2 || a.bh < 2) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "frame too small for bloom");
+		if ((r = ensure(ctx, ctx->bloom0, size_t(a.bw) * a.bh * 8))) return r;
+		if ((r = ensure(ctx, ctx->bloom1, size_t(a.bw) * a.bh * 8))) return r;
+		if ((r = ensure(ctx, ctx->line_sums, size_t(a.bh) * 16))) return r;
+		a.bloom0 = static_cast<uint64_t*>(ctx->bloom0.ptr);
+		a.bloom1 = static_cast<uint64_t*>(ctx->bloom1.ptr);
+		a.line_sums = static_cast<int32_t*>(ctx->line_sums.ptr);
+		const float sigma = config->bloom_sigma / float(S);
+		const float rf = std::ceil(3.0f * sigma - 0.5f);
+		uint32_t radius = rf > 0.0f ? uint32_t(rf) : 0u;
+		if (radius > 16) radius = 16;
+		a.radius = radius;
+		float kernel[33] = {0};
+		const float samples[4] = {-0.375f, -0.125f, 0.125f, 0.375f};
+		const float tau = 6.28318530717958647692f;
+		for (int32_t x = -int32_t(radius); x <= int32_t(radius); ++x)
+		{
+			float val = 0.0f;
+			for (float smp : samples)
+			{
+				float coord = float(x) + smp;
+				val += std::exp(-0.5f * (coord / sigma) * (coord / sigma)) / (sigma * std::sqrt(tau));
+			}
+			kernel[x + int32_t(radius)] = val / 4.0f;
+		}
+		for (int i = 0; i < 33; ++i)
+		{
+			const float kh = kernel[i] * float(1 << 14);
+			const float kv = kernel[i] * config->bloom_scale * float(1 << 14);
+			a.kernel_h[i] = f2i32_sat(kh);
+			a.kernel_v[i] = f2i32_sat(kv);
+		}
+	}
+	else
+	{
+		if ((r = ensure(ctx, ctx->line_sums_f, size_t(h) * 16))) return r;
+		a.line_sums_f = static_cast<float*>(ctx->line_sums_f.ptr);
+	}
+	void* out = dst;
+	uint32_t out_pitch = pitch;
+	if (!dst_is_device)
+	{
+		if ((r = ensure(ctx, ctx->up_dst, size_t(w) * h * 4))) return r;
+		out = ctx->up_dst.ptr;
+		out_pitch = w;
+	}
+	a.dst = static_cast<uint32_t*>(out);
+	a.dst_pitch = out_pitch;
+	if ((r = check_kernel(ctx, launch_postprocess(a, ctx->num_sms, ctx->stream), "postprocess"))) return r;
+	SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_average, ctx->average.ptr, 16, cudaMemcpyDeviceToHost, ctx->stream));
+	SW_CUDA(ctx, cudaEventRecord(ctx->average_ready, ctx->stream));
+	ctx->exposure_pending = true;
+	ctx->pending_config = *config;
+	ctx->pending_dt = frame_duration_s;
+	if (!dst_is_device) return copy_out(ctx, dst, pitch, 0, out, w, w, h, 4);
+	return SW_OK;
+}
+
+int sw_upscale(SwCtx* ctx, uint32_t mode, uint32_t scale, const void* src, int src_is_device, void* dst, uint32_t dst_width,
+	uint32_t dst_height, uint32_t dst_pitch, int dst_is_device)
+{
+	if (!ctx || !src || !dst || dst_pitch < dst_width) return SW_ERR_INVALID_ARGUMENT;
+	if (mode == SW_UPSCALE_AVG2X)
+		scale = 2;
+	else if (mode != SW_UPSCALE_NEAREST || scale < 1 || scale > 6)
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "bad upscale mode/scale");
+	const uint32_t sw = dst_width / scale, sh = dst_height / scale;
+	if (sw < 1 || sh < 1 || (mode == SW_UPSCALE_AVG2X && (sw < 2 || sh < 2)))
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "frame too small");
+	int r;
+	const void* s = src;
+	if (!src_is_device)
+	{
+		if ((r = ensure(ctx, ctx->up_src, size_t(sw) * sh * 4))) return r;
+		if ((r = upload(ctx, ctx->stage_io, ctx->up_src.ptr, src, size_t(sw) * sh * 4))) return r;
+		s = ctx->up_src.ptr;
+	}
+	void* d = dst;
+	uint32_t dp = dst_pitch;
+	if (!dst_is_device)
+	{
+		if ((r = ensure(ctx, ctx->up_dst, size_t(dst_width) * dst_height * 4))) return r;
+		d = ctx->up_dst.ptr;
+		dp = dst_width;
+	}
+	if ((r = check_kernel(ctx,
+			 launch_upscale(mode, scale, static_cast<const uint32_t*>(s), static_cast<uint32_t*>(d), dst_width, dst_height, dp,
+				 ctx->stream),
+			 "upscale")))
+		return r;
+	if (!dst_is_device) return copy_out(ctx, dst, dst_pitch, 0, d, dp, dst_width, dst_height, 4);
+	return SW_OK;
+}
+
+int sw_read_surfaces(SwCtx* ctx, void* dst_host, uint64_t max_bytes)
+{
+	if (!ctx || !dst_host) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->arena_valid && ctx->arena_texels == 0) return fail(ctx, SW_ERR_STATE, "no surfaces built");
+	const uint64_t bytes = ctx->arena_texels * bpp_of(ctx->arena_format);
+	if (bytes > max_bytes) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "destination too small (%llu bytes needed)", (unsigned long long)bytes);
+	SW_CUDA(ctx, cudaMemcpyAsync(dst_host, ctx->arena.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	return SW_OK;
+}
+
+int sw_get_exposure(SwCtx* ctx, float* out_exposure)
+{
+	if (!ctx || !out_exposure) return SW_ERR_INVALID_ARGUMENT;
+	int r = finalize_exposure(ctx);
+	if (r) return r;
+	*out_exposure = ctx->exposure;
+	return SW_OK;
+}
+
+int sw_set_exposure(SwCtx* ctx, float exposure)
+{
+	if (!ctx || !(exposure > 0.0f)) return SW_ERR_INVALID_ARGUMENT;
+	int r = finalize_exposure(ctx);
+	if (r) return r;
+	ctx->exposure = exposure;
+	return SW_OK;
+}
+
+int sw_abi_layout(uint32_t* sizes, uint32_t count)
+{
+	const uint32_t s[11] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
+		uint32_t(sizeof(SwDirectionalLightmapElement)), uint32_t(sizeof(SwLight)), uint32_t(sizeof(SwSurfaceDesc)),
+		uint32_t(sizeof(SwVertex16)), uint32_t(sizeof(SwDrawCmd)), uint32_t(sizeof(SwFrameParams)),
+		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats))};
+	for (uint32_t i = 0; sizes && i < count && i < 11; ++i) sizes[i] = s[i];
+	return 11;
+}
+
+int sw_get_stats(SwCtx* ctx, SwStats* out)
+{
+	if (!ctx || !out) return SW_ERR_INVALID_ARGUMENT;
+	unsigned int errs[4] = {0, 0, 0, 0};
+	SW_CUDA(ctx, cudaMemcpyAsync(errs, ctx->error_counter.ptr, 16, cudaMemcpyDeviceToHost, ctx->stream));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	*out = ctx->stats;
+	out->bad_texel_fetches = errs[0];
+	return SW_OK;
+}
+
+} // extern "C"

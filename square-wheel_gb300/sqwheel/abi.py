@@ -1,0 +1,111 @@
+"""numpy / ctypes mirrors of the structs in include/swgpu.h.
+
+Arrays of descriptors are numpy structured arrays (aligned like the C structs) so that they can be
+handed to the C ABI by pointer; single parameter blocks are ctypes Structures.
+"""
+import ctypes
+
+import numpy as np
+
+SWGPU_ABI_VERSION = 1
+
+SW_OK = 0
+SW_ERR_INVALID_ARGUMENT = -1
+SW_ERR_OUT_OF_MEMORY = -2
+SW_ERR_CUDA = -3
+SW_ERR_LIMIT = -4
+SW_ERR_NO_DEVICE = -5
+SW_ERR_STATE = -6
+
+SW_PIXEL_C32 = 0
+SW_PIXEL_C64 = 1
+
+SW_BLEND_NONE, SW_BLEND_AVERAGE, SW_BLEND_ADDITIVE, SW_BLEND_ALPHA_TEST, SW_BLEND_ALPHA_BLEND = range(5)
+SW_RASTER_FULL_PERSPECTIVE, SW_RASTER_LINE_Z_CORRECTED, SW_RASTER_AFFINE = range(3)
+SW_UPSCALE_NEAREST, SW_UPSCALE_AVG2X = range(2)
+
+SW_TEX_HAS_NORMAL_MAP = 1
+SW_TEX_HAS_NON_ONE_ROUGHNESS = 2
+SW_TEX_IS_METAL = 4
+
+SW_MAX_POLYGON_LIGHTS = 6
+SW_MAX_POLYGON_VERTICES = 24
+SW_NO_LIGHTMAP = 0
+SW_NO_EMISSIVE = 0xFFFFFFFF
+SW_SURF_DIFFUSE_LAYER = 1
+
+TEXTURE_MIP = np.dtype([("offset", "<u8"), ("width", "<u4"), ("height", "<u4"), ("flags", "<u4"), ("reserved", "<u4")], align=True)
+EMISSIVE_MIP = np.dtype([("offset", "<u8"), ("width", "<u4"), ("height", "<u4")], align=True)
+DIR_LIGHTMAP_ELEMENT = np.dtype(
+    [("ambient_light", "<f4", 3), ("light_direction_vector_scaled", "<f4", 3), ("directional_light_deviation", "<f4"),
+     ("directional_light_color", "<f4", 3)], align=True)
+LIGHT = np.dtype([("position", "<f4", 3), ("radius", "<f4"), ("inv_square_radius", "<f4"), ("color", "<f4", 3)], align=True)
+SURFACE_DESC = np.dtype([
+    ("basis_u", "<f4", 3), ("basis_v", "<f4", 3), ("basis_start", "<f4", 3), ("basis_normal", "<f4", 3),
+    ("size", "<u4", 2), ("tc_start", "<i4", 2), ("texture_mip", "<u4"), ("emissive_mip", "<u4"),
+    ("lightmap_offset", "<u4"), ("lightmap_size", "<u4", 2), ("lightmap_scale_log2", "<u4"),
+    ("lightmap_tc_shift", "<u4", 2), ("flags", "<u4"), ("num_lights", "<u4"), ("lights", "<u2", 6),
+    ("emissive_light", "<f4", 3), ("out_offset", "<u8")], align=True)
+VERTEX16 = np.dtype([("x", "<i4"), ("y", "<i4")], align=True)
+DRAW_CMD = np.dtype([
+    ("first_vertex", "<u4"), ("vertex_count", "<u4"), ("mode", "<u4"), ("blend", "<u4"), ("depth_eq", "<f4", 3),
+    ("tc_eq", "<f4", 6), ("tex_size", "<u4", 2), ("reserved", "<u4"), ("tex_offset", "<u8")], align=True)
+
+
+class CreateInfo(ctypes.Structure):
+    _fields_ = [
+        ("abi_version", ctypes.c_uint32), ("device", ctypes.c_uint32),
+        ("texels", ctypes.c_void_p), ("num_texels", ctypes.c_uint64),
+        ("texture_mips", ctypes.c_void_p), ("num_texture_mips", ctypes.c_uint32), ("num_emissive_mips", ctypes.c_uint32),
+        ("emissive_pixels", ctypes.c_void_p), ("num_emissive_pixels", ctypes.c_uint64), ("emissive_mips", ctypes.c_void_p),
+        ("lightmaps", ctypes.c_void_p), ("num_lightmap_elements", ctypes.c_uint64),
+        ("directional_lightmaps", ctypes.c_void_p), ("num_directional_lightmap_elements", ctypes.c_uint64),
+        ("max_surface_texels", ctypes.c_uint64), ("max_surfaces", ctypes.c_uint32), ("max_draws", ctypes.c_uint32),
+    ]
+
+
+class FrameParams(ctypes.Structure):
+    _fields_ = [
+        ("pixel_format", ctypes.c_uint32), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+        ("use_directional_lightmaps", ctypes.c_uint32), ("cam_pos", ctypes.c_float * 3),
+        ("clear_background", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+    ]
+
+
+class PostConfig(ctypes.Structure):
+    """PostprocessorConfig after synchronize_config clamping (postprocessor.rs:958-977)."""
+    _fields_ = [
+        ("exposure_update_speed", ctypes.c_float), ("base_brightness", ctypes.c_float),
+        ("zero_level_brightness", ctypes.c_float), ("brightness_scale_power", ctypes.c_float),
+        ("min_exposure", ctypes.c_float), ("max_exposure", ctypes.c_float), ("bloom_sigma", ctypes.c_float),
+        ("bloom_buffer_scale_log2", ctypes.c_uint32), ("bloom_scale", ctypes.c_float),
+        ("linear_bloom_filter", ctypes.c_uint32),
+    ]
+
+    @classmethod
+    def default(cls):
+        """Defaults of postprocessor_config.rs:13-41 (bloom on, sigma 1, scale log2 1)."""
+        return cls(1.0, 1.0, 1.0, 0.25, 1.0 / 65536.0, 128.0, 1.0, 1, 0.25, 0)
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("surfaces", ctypes.c_uint64), ("surface_texels", ctypes.c_uint64), ("draws", ctypes.c_uint64),
+                ("bad_texel_fetches", ctypes.c_uint64)]
+
+
+# Order reported by sw_abi_layout.
+LAYOUT_ORDER = [
+    ("SwCreateInfo", ctypes.sizeof(CreateInfo)), ("SwTextureMip", TEXTURE_MIP.itemsize),
+    ("SwEmissiveMip", EMISSIVE_MIP.itemsize), ("SwDirectionalLightmapElement", DIR_LIGHTMAP_ELEMENT.itemsize),
+    ("SwLight", LIGHT.itemsize), ("SwSurfaceDesc", SURFACE_DESC.itemsize), ("SwVertex16", VERTEX16.itemsize),
+    ("SwDrawCmd", DRAW_CMD.itemsize), ("SwFrameParams", ctypes.sizeof(FrameParams)),
+    ("SwPostConfig", ctypes.sizeof(PostConfig)), ("SwStats", ctypes.sizeof(Stats)),
+]
+
+
+def ptr(a):
+    """Raw pointer of a contiguous numpy array (or None for an empty/None array)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
+    return ctypes.c_void_p(a.ctypes.data) if a.size else None

@@ -1,0 +1,238 @@
+"""Python binding of the GB300 rendering library (libswgpu.so, C ABI in include/swgpu.h).
+
+`GpuRenderer` mirrors the reference's per-frame API for the GPU path:
+  Renderer::new            -> GpuRenderer(scene)                  (src/square_wheel/renderer.rs:24-59)
+  Renderer::prepare_frame  -> frame_begin + submit_surfaces        (renderer.rs:61-104)
+  Renderer::draw_frame     -> submit_draws + render               (renderer.rs:106-124)
+  Postprocessor::perform_postprocessing -> postprocess            (postprocessor.rs:68-204)
+  FrameUpscaler::perform_upscale        -> upscale                (frame_upscaler.rs:42-70)
+There is no CPU fallback: constructing a renderer without the built library or without a GPU raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import abi
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libswgpu.so")
+
+EXPORTED = [
+    "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_set_surfaces",
+    "sw_submit_draws",
+    "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_get_exposure", "sw_set_exposure",
+    "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout",
+]
+
+_lib = None
+
+
+class SwError(RuntimeError):
+    pass
+
+
+def load_library(path=LIB_PATH):
+    """Load libswgpu.so (built by square-wheel_gb300/build.py). Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise SwError(f"{path} is missing: build it with `python square-wheel_gb300/build.py`")
+    lib = ctypes.CDLL(path)
+    vp, u32, u64, i32, f32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_float
+    sig = {
+        "sw_create": ([vp, ctypes.POINTER(vp)], i32),
+        "sw_destroy": ([vp], i32),
+        "sw_last_error": ([vp], ctypes.c_char_p),
+        "sw_sync": ([vp], i32),
+        "sw_frame_begin": ([vp, vp, vp, u32], i32),
+        "sw_submit_surfaces": ([vp, vp, u32, u64], i32),
+        "sw_rebuild_surfaces": ([vp], i32),
+        "sw_set_surfaces": ([vp, vp, u64], i32),
+        "sw_submit_draws": ([vp, vp, u32, vp, u32], i32),
+        "sw_render": ([vp, vp, u32, i32], i32),
+        "sw_postprocess": ([vp, vp, f32, vp, vp, u32, i32], i32),
+        "sw_upscale": ([vp, u32, u32, vp, i32, vp, u32, u32, u32, i32], i32),
+        "sw_read_surfaces": ([vp, vp, u64], i32),
+        "sw_get_exposure": ([vp, ctypes.POINTER(f32)], i32),
+        "sw_set_exposure": ([vp, f32], i32),
+        "sw_set_framebuffer": ([vp, vp, u32, u32, u32, i32], i32),
+        "sw_get_stats": ([vp, vp], i32),
+        "sw_get_stream": ([vp, ctypes.POINTER(vp)], i32),
+        "sw_abi_layout": ([ctypes.POINTER(u32), u32], i32),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def abi_layout():
+    lib = load_library()
+    sizes = (ctypes.c_uint32 * 16)()
+    n = lib.sw_abi_layout(sizes, 16)
+    return [int(sizes[i]) for i in range(n)]
+
+
+class StaticData:
+    """Static map data uploaded once: textures with mips, emissive textures, lightmaps."""
+
+    def __init__(self, texels, texture_mips, emissive_pixels=None, emissive_mips=None, lightmaps=None,
+                 directional_lightmaps=None):
+        self.texels = np.ascontiguousarray(texels, dtype=np.uint64)
+        self.texture_mips = np.ascontiguousarray(texture_mips, dtype=abi.TEXTURE_MIP)
+        self.emissive_pixels = np.ascontiguousarray(
+            emissive_pixels if emissive_pixels is not None else np.zeros(0, np.uint32), dtype=np.uint32)
+        self.emissive_mips = np.ascontiguousarray(
+            emissive_mips if emissive_mips is not None else np.zeros(0, abi.EMISSIVE_MIP), dtype=abi.EMISSIVE_MIP)
+        self.lightmaps = np.ascontiguousarray(
+            lightmaps if lightmaps is not None else np.zeros((1, 3), np.float32), dtype=np.float32).reshape(-1, 3)
+        self.directional_lightmaps = np.ascontiguousarray(
+            directional_lightmaps if directional_lightmaps is not None else np.zeros(0, abi.DIR_LIGHTMAP_ELEMENT),
+            dtype=abi.DIR_LIGHTMAP_ELEMENT)
+
+    def create_info(self, device=0):
+        ci = abi.CreateInfo()
+        ci.abi_version = abi.SWGPU_ABI_VERSION
+        ci.device = device
+        ci.texels = abi.ptr(self.texels)
+        ci.num_texels = self.texels.size
+        ci.texture_mips = abi.ptr(self.texture_mips)
+        ci.num_texture_mips = self.texture_mips.size
+        ci.emissive_pixels = abi.ptr(self.emissive_pixels)
+        ci.num_emissive_pixels = self.emissive_pixels.size
+        ci.emissive_mips = abi.ptr(self.emissive_mips)
+        ci.num_emissive_mips = self.emissive_mips.size
+        ci.lightmaps = abi.ptr(self.lightmaps)
+        ci.num_lightmap_elements = self.lightmaps.shape[0]
+        ci.directional_lightmaps = abi.ptr(self.directional_lightmaps)
+        ci.num_directional_lightmap_elements = self.directional_lightmaps.size
+        return ci
+
+
+def frame_params(width, height, pixel_format, cam_pos, directional=True, clear_background=False):
+    fp = abi.FrameParams()
+    fp.pixel_format = pixel_format
+    fp.width = width
+    fp.height = height
+    fp.use_directional_lightmaps = 1 if directional else 0
+    for i in range(3):
+        fp.cam_pos[i] = float(cam_pos[i])
+    fp.clear_background = 1 if clear_background else 0
+    return fp
+
+
+class GpuRenderer:
+    """One rendering context on one GPU (SwCtx)."""
+
+    def __init__(self, static: StaticData, device=0):
+        self.lib = load_library()
+        self.static = static  # keep host arrays alive for the duration of sw_create
+        self.ctx = ctypes.c_void_p()
+        ci = static.create_info(device)
+        r = self.lib.sw_create(ctypes.byref(ci), ctypes.byref(self.ctx))
+        if r != abi.SW_OK:
+            raise SwError(f"sw_create failed with status {r}")
+
+    def _check(self, r, what):
+        if r != abi.SW_OK:
+            msg = self.lib.sw_last_error(self.ctx)
+            raise SwError(f"{what} failed ({r}): {msg.decode() if msg else ''}")
+
+    def close(self):
+        if self.ctx:
+            self.lib.sw_destroy(self.ctx)
+            self.ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stream_handle(self):
+        s = ctypes.c_void_p()
+        self._check(self.lib.sw_get_stream(self.ctx, ctypes.byref(s)), "sw_get_stream")
+        return s.value or 0
+
+    def frame_begin(self, params, lights=None):
+        lights = np.ascontiguousarray(lights if lights is not None else np.zeros(0, abi.LIGHT), dtype=abi.LIGHT)
+        self._lights = lights
+        self._check(self.lib.sw_frame_begin(self.ctx, ctypes.byref(params), abi.ptr(lights), lights.size), "sw_frame_begin")
+
+    def submit_surfaces(self, surfaces, total_texels):
+        surfaces = np.ascontiguousarray(surfaces, dtype=abi.SURFACE_DESC)
+        self._check(self.lib.sw_submit_surfaces(self.ctx, abi.ptr(surfaces), surfaces.size, int(total_texels)),
+                    "sw_submit_surfaces")
+
+    def rebuild_surfaces(self):
+        self._check(self.lib.sw_rebuild_surfaces(self.ctx), "sw_rebuild_surfaces")
+
+    def set_surfaces(self, arena):
+        arena = np.ascontiguousarray(arena)
+        self._check(self.lib.sw_set_surfaces(self.ctx, abi.ptr(arena), arena.size), "sw_set_surfaces")
+
+    def submit_draws(self, draws, vertices):
+        draws = np.ascontiguousarray(draws, dtype=abi.DRAW_CMD)
+        vertices = np.ascontiguousarray(vertices, dtype=abi.VERTEX16)
+        self._check(self.lib.sw_submit_draws(self.ctx, abi.ptr(draws), draws.size, abi.ptr(vertices), vertices.size),
+                    "sw_submit_draws")
+
+    def render(self, out=None, device_ptr=None, pitch=None):
+        """Rasterise. `out` = host numpy array (height, pitch) to receive the frame, or device_ptr."""
+        if out is not None:
+            p = pitch or out.shape[1]
+            self._check(self.lib.sw_render(self.ctx, abi.ptr(out), p, 0), "sw_render")
+        elif device_ptr is not None:
+            self._check(self.lib.sw_render(self.ctx, ctypes.c_void_p(device_ptr), pitch, 1), "sw_render")
+        else:
+            self._check(self.lib.sw_render(self.ctx, None, 0, 0), "sw_render")
+
+    def set_framebuffer(self, frame, pixel_format):
+        frame = np.ascontiguousarray(frame)
+        h, w = frame.shape
+        self._check(self.lib.sw_set_framebuffer(self.ctx, abi.ptr(frame), w, h, pixel_format, 0), "sw_set_framebuffer")
+
+    def postprocess(self, config, frame_duration_s, color_modulate, out=None, device_ptr=None, pitch=None):
+        mod = (ctypes.c_float * 3)(*[float(c) for c in color_modulate])
+        if out is not None:
+            r = self.lib.sw_postprocess(self.ctx, ctypes.byref(config), float(frame_duration_s), mod, abi.ptr(out),
+                                        pitch or out.shape[1], 0)
+        else:
+            r = self.lib.sw_postprocess(self.ctx, ctypes.byref(config), float(frame_duration_s), mod,
+                                        ctypes.c_void_p(device_ptr), pitch, 1)
+        self._check(r, "sw_postprocess")
+
+    def upscale(self, mode, scale, src, out):
+        src = np.ascontiguousarray(src, dtype=np.uint32)
+        h, w = out.shape
+        self._check(self.lib.sw_upscale(self.ctx, mode, scale, abi.ptr(src), 0, abi.ptr(out), w, h, w, 0), "sw_upscale")
+
+    def upscale_device(self, mode, scale, src_ptr, dst_ptr, width, height, pitch):
+        self._check(self.lib.sw_upscale(self.ctx, mode, scale, ctypes.c_void_p(src_ptr), 1, ctypes.c_void_p(dst_ptr),
+                                        width, height, pitch, 1), "sw_upscale")
+
+    def read_surfaces(self, total_texels, pixel_format):
+        dt = np.uint64 if pixel_format == abi.SW_PIXEL_C64 else np.uint32
+        out = np.empty(int(total_texels), dt)
+        self._check(self.lib.sw_read_surfaces(self.ctx, abi.ptr(out), out.nbytes), "sw_read_surfaces")
+        return out
+
+    def exposure(self):
+        e = ctypes.c_float()
+        self._check(self.lib.sw_get_exposure(self.ctx, ctypes.byref(e)), "sw_get_exposure")
+        return e.value
+
+    def set_exposure(self, e):
+        self._check(self.lib.sw_set_exposure(self.ctx, float(e)), "sw_set_exposure")
+
+    def stats(self):
+        s = abi.Stats()
+        self._check(self.lib.sw_get_stats(self.ctx, ctypes.byref(s)), "sw_get_stats")
+        return s
+
+    def sync(self):
+        self._check(self.lib.sw_sync(self.ctx), "sw_sync")

@@ -1,0 +1,135 @@
+"""Random, well-formed raster workloads for parity tests.
+
+Builds planar quads in view space, projects them with a pinhole camera, derives the screen-space depth
+and texture-coordinate equations the way prepare_polygon_surface does (src/square_wheel/
+partial_renderer.rs:1531-1635: inverse-depth plane, tc/z planes, surface rect from the projected
+vertices, equations shifted by tc_min), clips them to the frame, converts vertices to 16.16 fixed point
+(draw_polygon, partial_renderer.rs:4065-4077) and applies the power-of-two z_scale of the
+non-affine modes (partial_renderer.rs:4103-4109).
+"""
+import numpy as np
+
+from sqwheel import abi
+
+
+def clip_to_rect(pts, w, h):
+    """Sutherland-Hodgman clip of a convex polygon against [0,w]x[0,h]."""
+    def clip(poly, f):
+        out = []
+        n = len(poly)
+        for i in range(n):
+            a, b = poly[i - 1], poly[i]
+            fa, fb = f(a), f(b)
+            if fb >= 0:
+                if fa < 0:
+                    t = fa / (fa - fb)
+                    out.append(a + (b - a) * t)
+                out.append(b)
+            elif fa >= 0:
+                t = fa / (fa - fb)
+                out.append(a + (b - a) * t)
+        return out
+    poly = [np.asarray(p, np.float64) for p in pts]
+    for f in (lambda p: p[0], lambda p: w - p[0], lambda p: p[1], lambda p: h - p[1]):
+        poly = clip(poly, f)
+        if len(poly) < 3:
+            return []
+    return poly
+
+
+def make_raster_scene(seed, width, height, num_quads, modes=(0, 1, 2), blends=(0,), pixel_format=abi.SW_PIXEL_C32,
+                      texel_density=1.0, max_texture_side=256):
+    """Returns (arena, draws, vertices): a random surface arena with one surface per quad, and draws."""
+    rng = np.random.default_rng(seed)
+    f = 0.5 * width / np.tan(np.pi * 0.375 * 0.5)
+    cx, cy = width * 0.5, height * 0.5
+    draws = []
+    verts = []
+    surfaces = []
+    offset = 0
+    tries = 0
+    while len(draws) < num_quads and tries < num_quads * 20:
+        tries += 1
+        z0 = rng.uniform(40, 1500)
+        center = np.array([rng.uniform(-1, 1) * z0 * cx / f, rng.uniform(-1, 1) * z0 * cy / f, z0])
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        n = q[2]
+        if n @ center > 0:
+            n = -n  # face the camera
+        u_axis, v_axis = q[0], q[1]
+        half = rng.uniform(5, 400, 2)
+        corners = [center + u_axis * su * half[0] + v_axis * sv * half[1] for su, sv in ((-1, -1), (1, -1), (1, 1), (-1, 1))]
+        if min(c[2] for c in corners) < 1.0:
+            continue
+        proj = [np.array([f * c[0] / c[2] + cx, f * c[1] / c[2] + cy]) for c in corners]
+        poly = clip_to_rect(proj, width, height)
+        if len(poly) < 3:
+            continue
+        # Clockwise on screen (y down): positive signed area with this formula.
+        area = sum(poly[i - 1][0] * poly[i][1] - poly[i][0] * poly[i - 1][1] for i in range(len(poly)))
+        if area < 0:
+            poly = poly[::-1]
+        if abs(area) < 1.0:
+            continue
+        d = float(n @ center)
+        # 1/z = (n . q)/d with q = ((x-cx)/f, (y-cy)/f, 1)
+        dz = np.array([n[0] / (f * d), n[1] / (f * d), (n[2] - n[0] * cx / f - n[1] * cy / f) / d])
+        # tc = a . p + b per axis, density texels per unit, random shift
+        tcs = []
+        for axis in (u_axis, v_axis):
+            a = axis * texel_density
+            b = rng.uniform(-300, 300)
+            tcs.append((a, b))
+        # tc/z = a.q + b*(1/z)
+        te = np.zeros(6)
+        for i, (a, b) in enumerate(tcs):
+            te[i] = a[0] / f + b * dz[0]
+            te[2 + i] = a[1] / f + b * dz[1]
+            te[4 + i] = (a[2] - a[0] * cx / f - a[1] * cy / f) + b * dz[2]
+        # surface rect from the clipped vertices
+        tcv = []
+        for p in poly:
+            inv_z = dz[0] * p[0] + dz[1] * p[1] + dz[2]
+            tcv.append([(te[i] * p[0] + te[2 + i] * p[1] + te[4 + i]) / inv_z for i in range(2)])
+        tcv = np.array(tcv)
+        tmin = np.floor(tcv.min(axis=0) + 1.0 / 32)
+        tmax = np.ceil(tcv.max(axis=0) - 1.0 / 32)
+        size = np.maximum(tmax - tmin, 1).astype(np.int64)
+        if size.max() > max_texture_side:
+            continue
+        for i in range(2):
+            te[i] -= tmin[i] * dz[0]
+            te[2 + i] -= tmin[i] * dz[1]
+            te[4 + i] -= tmin[i] * dz[2]
+        dz32 = dz.astype(np.float32)
+        te32 = te.astype(np.float32)
+        mode = int(rng.choice(modes))
+        if mode != abi.SW_RASTER_AFFINE:
+            max_inv_z = max(float(dz32[0] * p[0] + dz32[1] * p[1] + dz32[2]) for p in poly)
+            z_scale = np.float32(2.0) ** np.float32(-5.0 - np.ceil(np.log2(max(max_inv_z, 2.0 ** -20))))
+            dz32 = (dz32 * z_scale).astype(np.float32)
+            te32 = (te32 * z_scale).astype(np.float32)
+        first = len(verts)
+        for p in poly:
+            verts.append((int(np.trunc(np.float32(p[0]) * np.float32(65536.0))),
+                          int(np.trunc(np.float32(p[1]) * np.float32(65536.0)))))
+        dc = np.zeros((), abi.DRAW_CMD)
+        dc["first_vertex"] = first
+        dc["vertex_count"] = len(poly)
+        dc["mode"] = mode
+        dc["blend"] = int(rng.choice(blends))
+        dc["depth_eq"] = dz32
+        dc["tc_eq"] = te32
+        dc["tex_size"] = size.astype(np.uint32)
+        dc["tex_offset"] = offset
+        draws.append(dc)
+        surfaces.append((offset, size))
+        offset += int(size[0] * size[1])
+    dt = np.uint64 if pixel_format == abi.SW_PIXEL_C64 else np.uint32
+    if pixel_format == abi.SW_PIXEL_C64:
+        arena = rng.integers(0, 1 << 62, offset, dtype=np.uint64)
+    else:
+        arena = rng.integers(0, 1 << 32, offset, dtype=np.uint64).astype(np.uint32)
+    draws = np.array(draws, dtype=abi.DRAW_CMD) if draws else np.zeros(0, abi.DRAW_CMD)
+    vertices = np.array(verts, dtype=abi.VERTEX16) if verts else np.zeros(0, abi.VERTEX16)
+    return arena.astype(dt), draws, vertices
