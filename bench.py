@@ -1,14 +1,22 @@
-"""Benchmark of the GB300 Square-Wheel rendering path.
+"""Benchmark of the GB300 Square-Wheel world-rendering path.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--workload frame|surfaces] [--impl gpu|reference]
 
-Prints one JSON line (rank 0). A step is one pass of the hot path over one batch of synthetic input:
-  surfaces: the batched-surface workload (4,096 surfaces, sides log-uniform 4..512 texels, mips 0..3,
-            directional lightmaps, normal-mapped dielectric/metal materials) built in one launch.
-Timing: W untimed warm-up steps, then K steps, each preceded by an L2 flush (a 512 MiB write) outside
-the timed span; device time from CUDA events on the library's stream, summed over the K steps.
-Multi-GPU: the workload is replicated (independent surface batches per rank, no collective); value is
-the sum over ranks of units / max-over-ranks time.
+Prints one JSON line (rank 0). A step is one pass of the hot path over one batch of synthetic input.
+
+Workloads
+  frame (default, the headline): one 1920x1080 HDR frame of the 64-room map (~32k polygons,
+      directional lightmaps, 256x256 textures with mips and normal maps, 25% metal / 25% dielectric
+      specular, 8 moving point lights): surface build -> tile raster -> bloom + tonemap + exposure.
+      Frames walk the seeded 256-frame camera path. The host's per-frame work (visibility, surface
+      preparation, draw setup) is done before the timed region; `value` is frames/s of device time
+      (sum of the three stages' CUDA-event times on the library's stream, inputs resident in HBM);
+      `e2e` is frames/s through the C ABI from host memory (host work + uploads + GPU + 8.3 MB readback).
+  surfaces: 4,096 surfaces, sides log-uniform 4..512 texels, mips 0..3, directional lightmaps,
+      built in one launch; value in Mtexels/s.
+Timing: W >= 3 untimed warm-up steps, K timed steps, each preceded by an L2 flush (a 512 MiB write)
+outside the timed span. Multi-GPU: independent replicas (different camera-path offsets), no collective;
+value = sum over ranks of frames / max-over-ranks time.
 """
 import argparse
 import json
@@ -25,6 +33,7 @@ sys.path.insert(0, os.path.join(ROOT, "square-wheel_gb300"))
 import numpy as np  # noqa: E402
 
 METRIC = "1080p frames/s: learned 2x upscale vs plain GPU (PSNR>=38 dB); Mtexels/s"
+W, H = 1920, 1080
 
 
 def peaks():
@@ -72,8 +81,8 @@ class ClockSampler:
 
     def summary(self):
         sm, mx, reasons = [], [], set()
-        for l in self.lines:
-            f = [x.strip() for x in l.split(",")]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
             try:
@@ -90,21 +99,279 @@ class ClockSampler:
 
 
 def dist_env():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
-def cpu_surfaces_baseline(work, max_seconds=20.0):
-    """Oracle (C++ restatement of the reference CPU surface builder, one task per surface on all host
-    threads) on a bounded sample of the same surface batch."""
+def frame_indices(n, offset=0):
+    """Frames spread over the 256-frame camera path."""
+    return [(offset + i * 37) % 256 for i in range(n)]
+
+
+# ---------------------------------------------------------------------------------------------------------
+# frame workload
+
+def post_bytes(w, h, scale=2):
+    """Algorithmic bytes of bloom + tonemap: downscale read, blur read+write twice, tonemap read of HDR
+    and bloom + write of Color32."""
+    bw, bh = w // scale, h // scale
+    return w * h * 8 + 2 * bw * bh * 8 * 2 + w * h * (8 + 4) + bw * bh * 8
+
+
+class FrameWorkload:
+    name = ("frame: 1920x1080 colour64 + bloom + tonemap, 64-room map (~32k polygons), directional lightmaps, "
+            "256^2 textures + normal maps, 25% metal / 25% dielectric, 8 moving point lights")
+    unit = "frames/s"
+
+    def __init__(self, frames, offset=0):
+        from sqwheel import abi, host
+        self.abi = abi
+        self.host = host
+        self.scene = host.Scene(**host.FULL_MAP)
+        self.static = self.scene.static_data()
+        self.opts = host.frame_options(W, H, abi.SW_PIXEL_C64, directional=True)
+        fr = host.Frame(self.scene)
+        self.frames = []
+        self.prep_ms = []
+        for fi in frame_indices(frames, offset):
+            t0 = time.perf_counter()
+            fr.prepare(fi, self.opts)
+            self.prep_ms.append((time.perf_counter() - t0) * 1e3)
+            self.frames.append(dict(index=fi, surfaces=fr.surfaces, draws=fr.draws, vertices=fr.vertices,
+                                    lights=fr.lights, params=fr.params, total_texels=fr.total_texels))
+        self.config = abi.PostConfig.default()
+
+    def lm_elements(self, f):
+        s = f["surfaces"]
+        sh = s["lightmap_tc_shift"].astype(np.int64)
+        lg = s["lightmap_scale_log2"].astype(np.int64)
+        lu = ((s["size"][:, 0] - 1 + sh[:, 0]) >> lg) + 2
+        lv = ((s["size"][:, 1] - 1 + sh[:, 1]) >> lg) + 2
+        return int((lu * lv).sum())
+
+    def surface_bytes(self, f):
+        return f["total_texels"] * (8 + 8) + self.lm_elements(f) * 40
+
+
+def run_frame_gpu(args, world, rank, local):
+    import torch
+    from sqwheel import abi, gpu
+    torch.cuda.set_device(local)
+    nsteps = args.warmup + args.steps
+    work = FrameWorkload(nsteps, offset=rank * 11)
+    r = gpu.GpuRenderer(work.static, device=local)
+    r.enable_timing(True)
+    stream = torch.cuda.ExternalStream(r.stream_handle())
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    ldr = torch.empty((H, W), dtype=torch.int32, device=f"cuda:{local}")
+    totals = {"surf": 0.0, "raster": 0.0, "post": 0.0}
+    texels = 0
+    surf_bytes = 0
+    pix_before = r.stats().pixel_writes
+    pix_writes = 0
+    launches = 0
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for step, f in enumerate(work.frames):
+            timed = step >= args.warmup
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            r.frame_begin(f["params"], f["lights"])
+            r.submit_surfaces(f["surfaces"], f["total_texels"])
+            r.submit_draws(f["draws"], f["vertices"])
+            r.render()
+            r.postprocess(work.config, 1.0 / 60.0, (1.0, 1.0, 1.0), device_ptr=ldr.data_ptr(), pitch=W)
+            t = r.timings()
+            if timed:
+                totals["surf"] += t[0]
+                totals["raster"] += t[1]
+                totals["post"] += t[2]
+                texels += f["total_texels"]
+                surf_bytes += work.surface_bytes(f)
+                launches += 1 + 2 + 5
+            if step == args.warmup - 1:
+                pix_before = r.stats().pixel_writes
+        pix_writes = r.stats().pixel_writes - pix_before
+        torch.cuda.synchronize()
+    frame_ms = (totals["surf"] + totals["raster"] + totals["post"]) / args.steps
+    if world > 1:
+        tt = torch.tensor([frame_ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        frame_ms = float(tt.item())
+    value = world * 1e3 / frame_ms
+
+    # e2e: the C++ renderer drives the C ABI from host memory; postprocess reads the LDR frame back.
+    from sqwheel import host
+    e2e_ms = []
+    h2d = d2h = 0
+    hr = host.HostRenderer(work.scene, device=local)
+    glib = gpu.load_library()
+    out = np.zeros((H, W), np.uint32)
+    import ctypes
+    mod = (ctypes.c_float * 3)(1.0, 1.0, 1.0)
+    for i, f in enumerate(work.frames[: max(3, min(args.steps, 12))]):
+        t0 = time.perf_counter()
+        hr.prepare_frame(f["index"], work.opts)
+        hr.draw_frame()
+        rc = glib.sw_postprocess(hr.context(), ctypes.byref(work.config), 1.0 / 60.0, mod, abi.ptr(out), W, 0)
+        if rc != 0:
+            raise RuntimeError(f"sw_postprocess failed: {rc}")
+        if i > 0:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        h2d = (f["surfaces"].nbytes + f["draws"].nbytes + f["vertices"].nbytes + f["lights"].nbytes
+               + (f["surfaces"].size + 1) * 8)
+        d2h = out.nbytes
+    hr.close()
+    e2e_val = 1e3 / statistics.median(e2e_ms)
+
+    peak, peak_kind = peaks()
+    s = args.steps
+    stage_bytes = {
+        "surf": surf_bytes / s,
+        "raster": (pix_writes / s) * 8 + W * H * 8 * 2,
+        "post": post_bytes(W, H),
+    }
+    stages = {}
+    for k, ms in totals.items():
+        ms_per = ms / s
+        gbs = stage_bytes[k] / (ms_per / 1e3) / 1e9 if ms_per > 0 else 0.0
+        stages[k] = {"ms": round(ms_per, 4), "algorithmic_bytes": int(stage_bytes[k]), "GB/s": round(gbs, 1),
+                     "frac_of_measured_hbm": round(gbs / peak, 4)}
+    dom = max(totals, key=totals.get)
+    kernel_names = {"surf": "surf_build_kernel", "raster": "raster_setup_kernel + raster_tiles_kernel",
+                    "post": "pp_downscale/pp_blur_h/pp_blur_v/pp_tonemap_bloom"}
+    out_line = None
+    if rank == 0:
+        cpu = cpu_frame_baseline(work)
+        out_line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world, "steps": s,
+            "warmup": args.warmup, "ms_per_step": round(frame_ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (lighting) / int (raster)", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": work.name, "width": W, "height": H, "pixel_format": "C64",
+                       "frames": [f["index"] for f in work.frames[args.warmup:]],
+                       "mean_surface_texels": int(texels / s), "mtexels_per_s": round(texels / totals["surf"] / 1e3, 1),
+                       "mean_pixel_writes": int(pix_writes / s),
+                       "mean_host_prep_ms": round(statistics.mean(work.prep_ms), 3),
+                       "l2": "flushed (512 MiB write) before every timed step",
+                       "timing": "sum of per-stage CUDA-event device times (surfaces, raster, postprocess)",
+                       "learned_upscale": "not in this measurement", "parallelism": f"replicas x{world}"},
+            "stages": stages,
+            "roofline": {"bound": "hbm", "kernel": kernel_names[dom], "achieved": stages[dom]["GB/s"], "peak": peak,
+                         "unit": "GB/s", "frac": stages[dom]["frac_of_measured_hbm"],
+                         "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": stages[dom]["algorithmic_bytes"],
+                         "traffic": None},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_val, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "clocks": clocks.summary(),
+            "gpu_launches": launches,
+        }
+        print(json.dumps(out_line), flush=True)
+    r.close()
+    return out_line
+
+
+def cpu_frame_baseline(work, max_frames=4):
+    """The oracle (C++ restatement of the reference CPU renderer) on the machine's host cores: the same host
+    work, surfaces with one task per surface, split_rect rasterisation with one region per thread, and
+    the postprocessor single-threaded (the reference's default, use_multithreading = false)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    from sqwheel import abi, gpu
+    threads = os.cpu_count() or 1
+    host = work.host
+    fr = host.Frame(work.scene)
+    ts = []
+    frames = [f["index"] for f in work.frames[:max_frames]]
+    exposure = 1.0
+    for fi in frames:
+        t0 = time.perf_counter()
+        fr.prepare(fi, work.opts)
+        arena = oracle.build_surfaces(work.static, fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=threads)
+        fb = np.zeros((H, W), np.uint64)
+        oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, fb, num_threads=threads)
+        _, exposure, _ = oracle.postprocess(work.config, fb, 1.0 / 60.0, (1.0, 1.0, 1.0), exposure)
+        ts.append(time.perf_counter() - t0)
+    v = len(ts) / sum(ts)
+    return {"value": round(v, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"{len(frames)} frames {frames} of the same workload; host work + oracle surfaces ({threads} threads) + "
+                      f"split_rect raster ({threads} regions) + single-thread postprocess"}
+
+
+# ---------------------------------------------------------------------------------------------------------
+# surfaces workload
+
+class SurfaceWorkload:
+    name = "batched surfaces: 4096 surfaces, sides log-uniform 4-512, mips 0-3, directional lightmaps, C64"
+
+    def __init__(self, seed=3):
+        from sqwheel import abi, synth
+        self.batch = synth.BatchedSurfaces(seed=seed, count=4096, num_lights=0, pixel_format=abi.SW_PIXEL_C64)
+
+
+def run_surfaces_gpu(args, world, rank, local):
+    import torch
+    from sqwheel import gpu
+    torch.cuda.set_device(local)
+    work = SurfaceWorkload(seed=3 + rank)
+    b = work.batch
+    r = gpu.GpuRenderer(b.static_data(), device=local)
+    fp = gpu.frame_params(W, H, b.pixel_format, b.cam_pos, directional=True)
+    r.frame_begin(fp, b.lights)
+    r.submit_surfaces(b.surfaces, b.total_texels)
+    r.enable_timing(True)
+    stream = torch.cuda.ExternalStream(r.stream_handle())
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    for _ in range(args.warmup):
+        r.rebuild_surfaces()
+    total = 0.0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            r.rebuild_surfaces()
+            total += r.timings()[0]
+    ms = total / args.steps
+    if world > 1:
+        tt = torch.tensor([ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = world * b.total_texels / 1e6 / (ms / 1e3)
+    e2e = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        r.frame_begin(fp, b.lights)
+        r.submit_surfaces(b.surfaces, b.total_texels)
+        outa = r.read_surfaces(b.total_texels, b.pixel_format)
+        e2e.append(time.perf_counter() - t0)
+    peak, peak_kind = peaks()
+    alg = b.algorithmic_bytes()
+    gbs = alg / (ms / 1e3) / 1e9
+    if rank == 0:
+        cpu = cpu_surfaces_baseline(work)
+        print(json.dumps({
+            "metric": METRIC, "value": round(value, 2), "unit": "Mtexels/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": work.name, "texels_per_step": int(b.total_texels),
+                       "l2": "flushed (512 MiB write) before every timed step", "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "kernel": "surf_build_kernel", "achieved": round(gbs, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(gbs / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+                         "algorithmic_bytes_per_launch": int(alg), "traffic": None},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(b.total_texels / 1e6 / statistics.median(e2e), 2), "unit": "Mtexels/s",
+                    "h2d_bytes_per_step": int(b.surfaces.nbytes + (b.surfaces.size + 1) * 8),
+                    "d2h_bytes_per_step": int(outa.nbytes)},
+            "clocks": clocks.summary(), "gpu_launches": args.steps}), flush=True)
+    r.close()
+
+
+def cpu_surfaces_baseline(work):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from sqwheel import gpu
     threads = os.cpu_count() or 1
     b = work.batch
-    # Sample: the first surfaces of the batch up to ~1/8 of its texels.
     area = b.surfaces["size"][:, 0].astype(np.int64) * b.surfaces["size"][:, 1]
     cum = np.cumsum(area)
     n = int(np.searchsorted(cum, max(cum[-1] // 8, 1)) + 1)
@@ -114,163 +381,46 @@ def cpu_surfaces_baseline(work, max_seconds=20.0):
     fp = gpu.frame_params(64, 64, b.pixel_format, b.cam_pos, directional=b.directional)
     static = b.static_data()
     t0 = time.perf_counter()
-    reps = 0
-    while True:
-        oracle.build_surfaces(static, sub, b.lights, fp, texels, num_threads=threads)
-        reps += 1
-        if time.perf_counter() - t0 > min(max_seconds, 3.0) or reps >= 3:
-            break
-    dt = (time.perf_counter() - t0) / reps
-    return {"value": texels / dt / 1e6, "unit": "Mtexels/s", "cores": threads, "kind": "port",
-            "sample": f"{n} of {b.surfaces.size} surfaces ({texels} texels), {reps} reps, oracle with {threads} threads"}
+    oracle.build_surfaces(static, sub, b.lights, fp, texels, num_threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": round(texels / dt / 1e6, 2), "unit": "Mtexels/s", "cores": threads, "kind": "port",
+            "sample": f"{n} of {b.surfaces.size} surfaces ({texels} texels), oracle with {threads} threads"}
 
 
-class SurfaceWorkload:
-    name = "batched surfaces: 4096 surfaces, sides log-uniform 4-512, mips 0-3, directional lightmaps, C64"
+# ---------------------------------------------------------------------------------------------------------
 
-    def __init__(self, seed=3):
-        from sqwheel import abi, synth
-        self.batch = synth.BatchedSurfaces(seed=seed, count=4096, num_lights=0, pixel_format=abi.SW_PIXEL_C64)
-
-    def setup(self, renderer):
-        from sqwheel import gpu
-        b = self.batch
-        self.fp = gpu.frame_params(1920, 1080, b.pixel_format, b.cam_pos, directional=True)
-        renderer.frame_begin(self.fp, b.lights)
-        renderer.submit_surfaces(b.surfaces, b.total_texels)
-        renderer.sync()
-
-    def device_step(self, renderer):
-        renderer.rebuild_surfaces()
-        return 1  # kernel launches
-
-    def e2e_step(self, renderer):
-        """Through the C ABI with host buffers: upload descriptors, build, read the arena back."""
-        b = self.batch
-        renderer.frame_begin(self.fp, b.lights)
-        renderer.submit_surfaces(b.surfaces, b.total_texels)
-        out = renderer.read_surfaces(b.total_texels, b.pixel_format)
-        h2d = b.surfaces.nbytes + (b.surfaces.size + 1) * 8
-        return h2d, out.nbytes
-
-    def units(self):
-        return self.batch.total_texels / 1e6  # Mtexels per step
-
-    unit = "Mtexels/s"
-
-    def algorithmic_bytes(self):
-        return self.batch.algorithmic_bytes()
-
-
-def run_gpu(args):
-    import torch
-    from sqwheel import gpu
-    world, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    work = SurfaceWorkload(seed=3 + rank)
-    r = gpu.GpuRenderer(work.batch.static_data(), device=local)
-    work.setup(r)
-    stream = torch.cuda.ExternalStream(r.stream_handle())
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
-
-    for _ in range(args.warmup):
-        work.device_step(r)
-    r.sync()
-
-    def barrier():
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-
-    total_ms = 0.0
-    launches = 0
-    barrier()
-    with ClockSampler(local) as clocks:
-        for _ in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(1.0)
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                launches += work.device_step(r)
-                e1.record(stream)
-            e1.synchronize()
-            total_ms += e0.elapsed_time(e1)
-        barrier()
-    ms_per_step = total_ms / args.steps
-    if world > 1:
-        t = torch.tensor([ms_per_step], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_per_step = float(t.item())
-    value = work.units() * world / (ms_per_step / 1e3)
-
-    # End to end through the C ABI with host buffers.
-    e2e_ms = []
-    h2d = d2h = 0
-    for _ in range(max(1, min(args.steps, 5))):
-        barrier()
-        t0 = time.perf_counter()
-        h2d, d2h = work.e2e_step(r)
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_val = work.units() / (statistics.median(e2e_ms) / 1e3)
-
-    peak, peak_kind = peaks()
-    alg = work.algorithmic_bytes()
-    achieved = alg / (ms_per_step / 1e3) / 1e9
-    out = None
-    if rank == 0:
-        cpu = cpu_surfaces_baseline(work)
-        out = {
-            "metric": METRIC, "value": round(value, 2), "unit": work.unit, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": work.name, "surfaces": int(work.batch.surfaces.size),
-                       "texels_per_step": int(work.batch.total_texels), "pixel_format": "C64",
-                       "l2": "flushed (512 MiB write) before every timed step", "parallelism": f"replicas x{world}"},
-            "roofline": {"bound": "hbm", "kernel": "surf_build_kernel", "achieved": round(achieved, 1),
-                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": int(alg),
-                         "traffic": None},
-            "cpu_baseline": cpu,
-            "e2e": {"value": round(e2e_val, 2), "unit": work.unit, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h)},
-            "clocks": clocks.summary(),
-            "gpu_launches": launches,
-        }
-        print(json.dumps(out), flush=True)
-    r.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
-    return out
-
-
-def run_reference(args):
-    """The reference's CPU path, restated in C++ (the Rust reference cannot be built here), on all host
-    threads, on bounded samples of the same workload."""
-    world, rank, _ = dist_env()
+def run_reference(args, world, rank):
+    """The reference's CPU path restated in C++ (the Rust reference cannot be built here), all host
+    threads, one frame per step (host work + surfaces + split_rect raster + postprocess)."""
     if rank != 0:
         return
-    work = SurfaceWorkload(seed=3)
-    vals = []
-    for _ in range(args.warmup):
-        cpu_surfaces_baseline(work, max_seconds=5.0)
-    t_steps = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        c = cpu_surfaces_baseline(work, max_seconds=5.0)
-        t_steps.append(time.perf_counter() - t0)
-        vals.append(c["value"])
-    v = statistics.median(vals)
-    out = {"metric": METRIC, "impl": "reference", "value": round(v, 3), "unit": "Mtexels/s", "n_gpus": world,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * statistics.median(t_steps), 3),
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+    if args.workload == "surfaces":
+        work = SurfaceWorkload(seed=3)
+        vals = [cpu_surfaces_baseline(work) for _ in range(args.warmup + args.steps)][args.warmup:]
+        c = vals[-1]
+        v = statistics.median(x["value"] for x in vals)
+        unit = "Mtexels/s"
+        ms = None
+    else:
+        work = FrameWorkload(args.warmup + args.steps)
+        # Each step: one frame of the same workload (bounded: the whole run stays within minutes).
+        work_frames = work.frames
+        ts = []
+        for i in range(len(work_frames)):
+            work.frames = work_frames[i:i + 1]
+            c = cpu_frame_baseline(work, max_frames=1)
+            if i >= args.warmup:
+                ts.append(1.0 / c["value"])
+        v = len(ts) / sum(ts)
+        unit = "frames/s"
+        ms = 1e3 * statistics.median(ts)
+        c["sample"] = f"{len(ts)} frames, one per step; " + c["sample"].split("; ", 1)[1]
+    out = {"metric": METRIC, "impl": "reference", "value": round(v, 3), "unit": unit, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3) if ms else None,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (lighting) / int (raster)",
            "data": "synthetic (seeded)", "config": {"workload": work.name},
-           "cpu_baseline": {"value": round(v, 3), "unit": "Mtexels/s", "cores": c["cores"], "kind": "port",
-                            "sample": c["sample"]},
-           "e2e": {"value": round(v, 3), "unit": "Mtexels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "cpu_baseline": {"value": round(v, 3), "unit": unit, "cores": c["cores"], "kind": "port", "sample": c["sample"]},
+           "e2e": {"value": round(v, 3), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
@@ -279,14 +429,28 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", default="frame", choices=["frame", "surfaces"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_env()
     if args.impl == "reference":
-        run_reference(args)
-    else:
-        run_gpu(args)
+        run_reference(args, world, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    try:
+        if args.workload == "surfaces":
+            run_surfaces_gpu(args, world, rank, local)
+        else:
+            run_frame_gpu(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
 
 
 if __name__ == "__main__":

@@ -268,8 +268,15 @@ typedef struct SwStats {
 	uint64_t surface_texels;    /* texels built since sw_create */
 	uint64_t draws;             /* draw commands submitted since sw_create */
 	uint64_t bad_texel_fetches; /* rasteriser fetches outside a surface (always 0 for well-formed draws) */
+	uint64_t pixel_writes;      /* span pixels the rasteriser wrote (texel fetch + blend) since sw_create */
 } SwStats;
 int sw_get_stats(SwCtx* ctx, SwStats* out_stats);
+
+/* Device-time measurement of the last call of each stage (CUDA events on the context's stream around
+ * the stage's kernels only): [0] surface build, [1] rasterisation, [2] postprocess, [3] upscale, in ms.
+ * Timing is off by default; sw_enable_timing(ctx, 1) turns it on. sw_get_timings synchronises. */
+int sw_enable_timing(SwCtx* ctx, int enable);
+int sw_get_timings(SwCtx* ctx, float out_ms[4]);
 
 /* The context's CUDA stream (cudaStream_t) for callers that order their own work after the frame. */
 int sw_get_stream(SwCtx* ctx, void** out_stream);

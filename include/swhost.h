@@ -1,0 +1,101 @@
+/*
+ * swhost.h — C ABI of the host side of the GB300 renderer (libswhost.so).
+ *
+ * The reference keeps visibility, leaf ordering and per-polygon setup on the host in Rust; this library
+ * is their C++ restatement (the Rust toolchain is not available to build the reference host), plus a
+ * seeded synthetic scene generator that stands in for the map compiler and lightmapper. It produces the
+ * SwSurfaceDesc / SwDrawCmd arrays of include/swgpu.h and can drive libswgpu.so itself:
+ *   swh_renderer_prepare_frame  ~ Renderer::prepare_frame  (src/square_wheel/renderer.rs:61-104)
+ *   swh_renderer_draw_frame     ~ Renderer::draw_frame     (src/square_wheel/renderer.rs:106-124)
+ * Every function returns 0 or a negative SwStatus and never aborts.
+ */
+#ifndef SWHOST_H
+#define SWHOST_H
+
+#include "swgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct SwhSceneConfig {
+	uint64_t seed;
+	uint32_t grid_x, grid_y;      /* rooms in a grid_x x grid_y layout */
+	float room_min, room_max;     /* room edge range, within [256, 1024] */
+	float tile_size;              /* faces are cut into tiles of this size (16..256 units) */
+	uint32_t texture_size;        /* material texture side (power of two) */
+	uint32_t num_materials;
+	float metal_frac, dielectric_frac; /* fractions of specular materials */
+	uint32_t normal_maps;
+	uint32_t directional_lightmaps;
+	uint32_t lights_per_room;     /* static lights baked into the lightmaps */
+	uint32_t num_dynamic_lights;  /* moving point lights */
+	uint32_t num_frames;          /* camera path length */
+	float emissive_frac;          /* fraction of materials with an emissive layer */
+} SwhSceneConfig;
+
+typedef struct SwhSceneInfo {
+	uint32_t nodes, leafs, polygons, portals, materials, frames, dynamic_lights, reserved;
+	uint64_t lightmap_elements, texels;
+} SwhSceneInfo;
+
+typedef struct SwhScene SwhScene;
+
+int swh_scene_create(const SwhSceneConfig* config, SwhScene** out_scene);
+int swh_scene_destroy(SwhScene* scene);
+int swh_scene_info(const SwhScene* scene, SwhSceneInfo* out_info);
+/* Static data for sw_create; pointers stay valid while the scene lives. */
+int swh_scene_create_info(const SwhScene* scene, uint32_t device, SwCreateInfo* out_info);
+const char* swh_last_error(void);
+
+typedef struct SwhFrameOptions {
+	uint32_t width, height, pixel_format;
+	uint32_t use_directional_lightmaps;
+	uint32_t clear_background;
+	float fov;      /* radians; 0 = 0.375*pi */
+	float mip_bias;
+} SwhFrameOptions;
+
+typedef struct SwhFrameOutputs {
+	const SwSurfaceDesc* surfaces;
+	uint32_t num_surfaces;
+	uint32_t num_draws;
+	uint64_t total_texels;
+	const SwDrawCmd* draws;
+	const SwVertex16* vertices;
+	uint32_t num_vertices;
+	uint32_t num_lights;
+	const SwLight* lights;
+	SwFrameParams params;
+	uint32_t visible_leafs, camera_leaf;
+} SwhFrameOutputs;
+
+typedef struct SwhFrame SwhFrame;
+
+/* Per-frame host state (visibility marks, per-polygon frame data, output arrays). */
+int swh_frame_create(const SwhScene* scene, SwhFrame** out_frame);
+int swh_frame_destroy(SwhFrame* frame);
+/* Host work of one frame of the scene's camera path: visibility, surface preparation, light
+ * selection, back-to-front traversal and draw setup. */
+int swh_frame_prepare(SwhFrame* frame, uint32_t frame_index, const SwhFrameOptions* options);
+/* Pointers into the frame's arrays, valid until the next swh_frame_prepare. */
+int swh_frame_outputs(const SwhFrame* frame, SwhFrameOutputs* out);
+
+typedef struct SwhRenderer SwhRenderer;
+
+/* Renderer::new: upload the scene's static data to `device` (sw_create). */
+int swh_renderer_create(const SwhScene* scene, uint32_t device, SwhRenderer** out_renderer);
+int swh_renderer_destroy(SwhRenderer* renderer);
+/* Renderer::prepare_frame: host work + sw_frame_begin + sw_submit_surfaces. */
+int swh_renderer_prepare_frame(SwhRenderer* renderer, uint32_t frame_index, const SwhFrameOptions* options);
+/* Renderer::draw_frame: sw_submit_draws + sw_render into dst (optional). */
+int swh_renderer_draw_frame(SwhRenderer* renderer, void* dst, uint32_t pitch, int dst_is_device);
+/* The GPU context and the frame used by the renderer. */
+SwCtx* swh_renderer_context(SwhRenderer* renderer);
+SwhFrame* swh_renderer_frame(SwhRenderer* renderer);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SWHOST_H */

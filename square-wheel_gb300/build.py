@@ -71,7 +71,45 @@ def build(force=False, verbose=False):
                 print(err)
     if jobs or not os.path.exists(LIB):
         run([cc] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs)
+    build_host(force, verbose)
     return LIB
+
+
+HOST_SOURCES = ["scene.cpp", "frame.cpp", "swhost.cpp"]
+HOST_LIB = os.path.join(LIB_DIR, "libswhost.so")
+
+
+def build_host(force=False, verbose=False):
+    """Host side (visibility, per-polygon setup, scene generator) as libswhost.so, linked to libswgpu.so."""
+    host_dir = os.path.join(PKG, "host")
+    inc = os.path.join(PKG, "..", "include")
+    deps = [os.path.join(host_dir, f) for f in os.listdir(host_dir) if f.endswith((".h", ".cpp"))]
+    deps += [os.path.join(inc, "swgpu.h"), os.path.join(inc, "swhost.h"), LIB]
+    if not force and _newer(HOST_LIB, deps):
+        return HOST_LIB
+    cxx = shutil.which("g++") or "g++"
+    objs = []
+    cmds = []
+    for src in HOST_SOURCES:
+        o = os.path.join(BUILD_DIR, "host_" + src.replace(".cpp", ".o"))
+        objs.append(o)
+        cmds.append([cxx, "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wextra",
+                     "-Wno-unused-parameter", "-I", inc, "-c", os.path.join(host_dir, src), "-o", o])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("host build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+        return r.stderr
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(cmds)) as ex:
+        for err in ex.map(run, cmds):
+            if verbose and err:
+                print(err)
+    run([cxx, "-shared", "-o", HOST_LIB] + objs + ["-L", LIB_DIR, "-lswgpu", "-Wl,-rpath,$ORIGIN", "-lpthread"])
+    return HOST_LIB
 
 
 if __name__ == "__main__":

@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 		else
 			pix = fb[uint64_t(y) * a.width + x];
 	}
-	unsigned int local_errors = 0;
+	unsigned int local_errors = 0, local_writes = 0;
 
 	const int lane = tid & 31, warp = tid >> 5;
 	for (uint32_t chunk = 0; chunk < a.num_draws; chunk += 256)
@@ -401,6 +401,7 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 						}
 						const T texel = arena[rd.tex_offset + ua];
 						blend_into<P>(pix, texel, rd.blend);
+						++local_writes;
 					}
 					break;
 				}
@@ -409,6 +410,10 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 	}
 	if (valid) fb[uint64_t(y) * a.width + x] = pix;
 	if (local_errors) atomicAdd(a.error_counter, local_errors);
+	// Pixel writes (span pixels processed) for the traffic accounting, one atomic per warp.
+	for (int o = 16; o > 0; o >>= 1) local_writes += __shfl_xor_sync(0xFFFFFFFFu, local_writes, o);
+	if ((tid & 31) == 0 && local_writes)
+		atomicAdd(reinterpret_cast<unsigned long long*>(a.error_counter + 2), (unsigned long long)local_writes);
 }
 
 } // namespace

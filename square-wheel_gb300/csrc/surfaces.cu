@@ -7,13 +7,16 @@
 //
 // Work decomposition: the frame's surfaces form one flat texel index space (prefix sums of surface
 // areas, in descriptor order). A grid of (#SMs x resident blocks) threads strides over it, so surfaces
-// from 4x4 to 512x512 texels share one launch without tail effects. Each thread owns one output texel:
-// it finds its surface by binary search over the prefix array (held in L1), rebuilds the reference's
-// row-interpolated lightmap line entries it needs (the two vertical mixes of the line buffer and the
-// horizontal mix, in the reference's operation order), evaluates lighting and stores the texel.
-// Neighbouring threads read neighbouring TextureElements and share lightmap elements, so texture reads
-// and surface writes are coalesced and lightmap reads are L1 broadcasts.
+// from 4x4 to 512x512 texels share one launch without tail effects. Each warp owns 32 consecutive
+// texels: lane 0 finds the first texel's surface by binary search over the prefix array, every lane
+// then steps forward to its own surface (at most a few steps, only across tiny surfaces). Each thread
+// rebuilds the reference's row-interpolated lightmap line entries it needs (the two vertical mixes of
+// the line buffer and the horizontal mix, in the reference's operation order), evaluates lighting and
+// stores its texel. Neighbouring threads read neighbouring TextureElements and share lightmap elements,
+// so texture reads and surface writes are coalesced and lightmap reads are L1 broadcasts.
 #include "sw_kernels.cuh"
+
+#include <cmath>
 
 namespace swgpu
 {
@@ -65,15 +68,17 @@ __device__ __forceinline__ Lm lm_load(const SurfaceKernelArgs& a, uint64_t index
 	Lm e;
 	if (DIRECTIONAL)
 	{
-		const float* p = reinterpret_cast<const float*>(a.directional_lightmaps + index);
-		e.amb[0] = __ldg(p + 0);
-		e.amb[1] = __ldg(p + 1);
-		e.amb[2] = __ldg(p + 2);
-		e.dir = mkv3(__ldg(p + 3), __ldg(p + 4), __ldg(p + 5));
-		e.dev = __ldg(p + 6);
-		e.col[0] = __ldg(p + 7);
-		e.col[1] = __ldg(p + 8);
-		e.col[2] = __ldg(p + 9);
+		// 40-byte element, 8-byte aligned: five 64-bit read-only loads.
+		const float2* p = reinterpret_cast<const float2*>(a.directional_lightmaps + index);
+		const float2 q0 = __ldg(p + 0), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3), q4 = __ldg(p + 4);
+		e.amb[0] = q0.x;
+		e.amb[1] = q0.y;
+		e.amb[2] = q1.x;
+		e.dir = mkv3(q1.y, q2.x, q2.y);
+		e.dev = q3.x;
+		e.col[0] = q3.y;
+		e.col[1] = q4.x;
+		e.col[2] = q4.y;
 	}
 	else
 	{
@@ -104,28 +109,25 @@ __device__ __forceinline__ Lm lm_mix(const Lm& a, const Lm& b, float ratio)
 	return r;
 }
 
-__device__ __forceinline__ int32_t rem_euclid(int32_t a, int32_t b)
+__device__ __forceinline__ uint32_t wrap(int32_t a, uint32_t b)
 {
-	int32_t r = a % b;
-	return r < 0 ? r + b : r;
+	int32_t r = a % int32_t(b);
+	return uint32_t(r < 0 ? r + int32_t(b) : r);
 }
 
-// Lighting of one texel for one lightmap kind; returns the ColorVec before conversion.
+// Lighting of one texel (surfaces.rs:515-842); returns the ColorVec before conversion.
 template <bool DIRECTIONAL>
-__device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const SwSurfaceDesc& s, uint32_t tex_flags,
-	uint64_t texel, uint32_t u, uint32_t v)
+__device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const SurfaceGpu& s, uint64_t texel, uint32_t u,
+	uint32_t v)
 {
+	const uint32_t tex_flags = s.flags & 7u;
 	const bool use_normal_map = (tex_flags & SW_TEX_HAS_NORMAL_MAP) != 0;
 	const int spec = (tex_flags & SW_TEX_HAS_NON_ONE_ROUGHNESS) ? ((tex_flags & SW_TEX_IS_METAL) ? 2 : 1) : 0;
 
-	const V3 u_vec = mkv3(s.basis_u[0], s.basis_u[1], s.basis_u[2]);
-	const V3 v_vec = mkv3(s.basis_v[0], s.basis_v[1], s.basis_v[2]);
-	const V3 bnormal = mkv3(s.basis_normal[0], s.basis_normal[1], s.basis_normal[2]);
-	// start_pos = start + u*(tc0+0.5) + v*(tc1+0.5), surfaces.rs:456-457
-	const V3 start_pos = v3add(v3add(mkv3(s.basis_start[0], s.basis_start[1], s.basis_start[2]),
-								   v3scale(u_vec, fadd(float(s.tc_start[0]), 0.5f))),
-		v3scale(v_vec, fadd(float(s.tc_start[1]), 0.5f)));
-	const V3 pos = v3sma(u_vec, float(u), v3sma(v_vec, float(v), start_pos));
+	const V3 u_vec = mkv3(s.u[0], s.u[1], s.u[2]);
+	const V3 v_vec = mkv3(s.v[0], s.v[1], s.v[2]);
+	const V3 bnormal = mkv3(s.normal[0], s.normal[1], s.normal[2]);
+	const V3 pos = v3sma(u_vec, float(u), v3sma(v_vec, float(v), mkv3(s.start_pos[0], s.start_pos[1], s.start_pos[2])));
 
 	V3 tn = mkv3(0.0f, 0.0f, 1.0f);
 	float rough = 0.0f;
@@ -140,30 +142,22 @@ __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const SwSu
 	else if (spec != 0)
 		rough = fmul(float(packed >> 24), NORMAL_UNPACK_SCALE);
 
-	V3 u_norm = mkv3(0, 0, 0), v_norm = mkv3(0, 0, 0);
-	if (spec != 0 || (use_normal_map && s.num_lights > 0))
-	{
-		u_norm = v3scale(u_vec, inv_sqrt_fast(fmaxf(v3dot(u_vec, u_vec), MIN_POSITIVE_VALUE)));
-		v_norm = v3scale(v_vec, inv_sqrt_fast(fmaxf(v3dot(v_vec, v_vec), MIN_POSITIVE_VALUE)));
-	}
 	const V3 cam = mkv3(a.cam_pos[0], a.cam_pos[1], a.cam_pos[2]);
 
 	CV albedo = cv_zero(); // total_light_albedo_modulated
 	CV direct = cv_zero(); // total_light_direct
-	if (s.lightmap_offset != SW_NO_LIGHTMAP)
+	if (s.flags & SW_SG_LIGHTMAP)
 	{
-		const uint32_t log2 = s.lightmap_scale_log2;
-		const float inv_scale = __fdiv_rn(1.0f, float(1u << log2));
-		const float k_shift = fmul(0.5f, inv_scale);
+		const uint32_t log2 = s.lm_log2;
 		const uint32_t mask = (1u << log2) - 1u;
-		const uint32_t base_v = v + s.lightmap_tc_shift[1];
+		const uint32_t base_v = v + s.lm_shift1;
 		const uint32_t lv = base_v >> log2;
-		const float kv = mad2(float(base_v & mask), inv_scale, k_shift);
-		const uint32_t base_u = u + s.lightmap_tc_shift[0];
+		const float kv = mad2(float(base_v & mask), s.inv_scale, s.k_shift);
+		const uint32_t base_u = u + s.lm_shift0;
 		const uint32_t lu = base_u >> log2;
-		const float ku = mad2(float(base_u & mask), inv_scale, k_shift);
-		const uint64_t row0 = uint64_t(s.lightmap_offset) + uint64_t(lv) * s.lightmap_size[0];
-		const uint64_t row1 = row0 + s.lightmap_size[0];
+		const float ku = mad2(float(base_u & mask), s.inv_scale, s.k_shift);
+		const uint64_t row0 = uint64_t(s.lm_offset) + uint64_t(lv) * s.lm_width;
+		const uint64_t row1 = row0 + s.lm_width;
 		// line_lightmap[lu] and [lu + 1] of the reference's row buffer, then the horizontal mix.
 		const Lm line0 = lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1 + lu), lm_load<DIRECTIONAL>(a, row0 + lu), kv);
 		const Lm line1 =
@@ -181,6 +175,8 @@ __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const SwSu
 		}
 		else
 		{
+			const V3 u_norm = mkv3(s.u_norm[0], s.u_norm[1], s.u_norm[2]);
+			const V3 v_norm = mkv3(s.v_norm[0], s.v_norm[1], s.v_norm[2]);
 			const V3 normal = use_normal_map ? tn : mkv3(0.0f, 0.0f, 1.0f);
 			const V3 to_cam = v3sub(cam, pos);
 			const V3 to_cam_ts = mkv3(v3dot(to_cam, u_norm), v3dot(to_cam, v_norm), v3dot(to_cam, bnormal));
@@ -222,9 +218,13 @@ __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const SwSu
 	{
 		V3 normal = bnormal;
 		if (use_normal_map)
+		{
+			const V3 u_norm = mkv3(s.u_norm[0], s.u_norm[1], s.u_norm[2]);
+			const V3 v_norm = mkv3(s.v_norm[0], s.v_norm[1], s.v_norm[2]);
 			normal = mkv3(mad2(tn.x, u_norm.x, mad2(tn.y, v_norm.x, fmul(tn.z, bnormal.x))),
 				mad2(tn.x, u_norm.y, mad2(tn.y, v_norm.y, fmul(tn.z, bnormal.y))),
 				mad2(tn.x, u_norm.z, mad2(tn.y, v_norm.z, fmul(tn.z, bnormal.z))));
+		}
 		V3 refl = mkv3(0.0f, 0.0f, 0.0f);
 		float refl_len2 = MIN_POSITIVE_VALUE;
 		float sk = 0.0f, inv_rough = 0.0f;
@@ -272,20 +272,14 @@ __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const SwSu
 }
 
 template <class P>
-__device__ __forceinline__ typename P::T emissive_mix(const SurfaceKernelArgs& a, const SwSurfaceDesc& s, uint32_t u,
+__device__ __forceinline__ typename P::T emissive_mix(const SurfaceKernelArgs& a, const SurfaceGpu& s, uint32_t u,
 	uint32_t v, typename P::T dst, bool additive)
 {
-	const SwEmissiveMip em = a.emissive_mips[s.emissive_mip];
-	const int32_t w = int32_t(em.width), h = int32_t(em.height);
-	const int32_t sv = rem_euclid(s.tc_start[1] + int32_t(v), h);
-	const int32_t su = rem_euclid(s.tc_start[0] + int32_t(u), w);
-	const uint32_t texel = __ldg(a.emissive_pixels + em.offset + uint64_t(sv) * em.width + uint32_t(su));
-	// ColorVecI::from_color_f32x3([l0*256, l1*256, l2*256]) -> [b, g, r, 0], truncating conversion.
-	const int32_t lb = __float2int_rz(fmul(s.emissive_light[2], 256.0f));
-	const int32_t lg = __float2int_rz(fmul(s.emissive_light[1], 256.0f));
-	const int32_t lr = __float2int_rz(fmul(s.emissive_light[0], 256.0f));
+	const uint32_t sv = wrap(s.tc1 + int32_t(v), s.em_h);
+	const uint32_t su = wrap(s.tc0 + int32_t(u), s.em_w);
+	const uint32_t texel = __ldg(a.emissive_pixels + s.em_offset + uint64_t(sv) * s.em_w + su);
 	const CI t = ci_from_c32(texel);
-	CI m{{wmul(t.v[0], lb) >> 8, wmul(t.v[1], lg) >> 8, wmul(t.v[2], lr) >> 8, 0}};
+	CI m{{wmul(t.v[0], s.em_light[0]) >> 8, wmul(t.v[1], s.em_light[1]) >> 8, wmul(t.v[2], s.em_light[2]) >> 8, 0}};
 	if (!additive) return P::from_ci(m);
 	const CI d = P::to_ci(dst);
 #pragma unroll
@@ -294,54 +288,145 @@ __device__ __forceinline__ typename P::T emissive_mix(const SurfaceKernelArgs& a
 }
 
 template <class P, bool DIRECTIONAL>
-__global__ void __launch_bounds__(256) surf_build_kernel(SurfaceKernelArgs a)
+__global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
 {
 	typedef typename P::T T;
 	T* arena = static_cast<T*>(a.arena);
 	const uint64_t total = a.total_work;
 	const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-	for (uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride)
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint64_t warp_first = uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u);
+	for (uint64_t wbase = warp_first; wbase < total; wbase += stride)
 	{
-		// Surface owning work item t: last s with prefix[s] <= t.
-		uint32_t lo = 0, hi = a.num_surfaces; // invariant: prefix[lo] <= t < prefix[hi]
-		while (hi - lo > 1)
+		const uint64_t t = wbase + lane;
+		// Surface of the warp's first texel (binary search by lane 0), then forward steps per lane.
+		uint32_t s0 = 0;
+		if (lane == 0)
 		{
-			uint32_t mid = (lo + hi) >> 1;
-			if (__ldg(a.work_prefix + mid) <= t)
-				lo = mid;
-			else
-				hi = mid;
+			uint32_t lo = 0, hi = a.num_surfaces; // prefix[lo] <= wbase < prefix[hi]
+			while (hi - lo > 1)
+			{
+				const uint32_t mid = (lo + hi) >> 1;
+				if (__ldg(a.work_prefix + mid) <= wbase)
+					lo = mid;
+				else
+					hi = mid;
+			}
+			s0 = lo;
 		}
-		const SwSurfaceDesc& s = a.surfaces[lo];
-		const uint64_t local = t - __ldg(a.work_prefix + lo);
-		const uint32_t w = s.size[0];
-		const uint32_t v = uint32_t(local / w);
-		const uint32_t u = uint32_t(local - uint64_t(v) * w);
+		uint32_t si = __shfl_sync(0xFFFFFFFFu, s0, 0);
+		if (t >= total) continue;
+		uint64_t next = __ldg(a.work_prefix + si + 1);
+		while (next <= t)
+		{
+			++si;
+			next = __ldg(a.work_prefix + si + 1);
+		}
+		const SurfaceGpu& s = a.surfaces[si];
+		const uint32_t local = uint32_t(t - __ldg(a.work_prefix + si));
+		const uint32_t v = local / s.width;
+		const uint32_t u = local - v * s.width;
 
 		T out = T(0);
-		const bool diffuse_layer = (s.flags & SW_SURF_DIFFUSE_LAYER) != 0;
+		const bool diffuse_layer = (s.flags & SW_SG_DIFFUSE) != 0;
 		if (diffuse_layer)
 		{
-			const SwTextureMip tm = a.texture_mips[s.texture_mip];
-			const int32_t sv = rem_euclid(s.tc_start[1] + int32_t(v), int32_t(tm.height));
-			const int32_t su = rem_euclid(s.tc_start[0] + int32_t(u), int32_t(tm.width));
-			const uint64_t texel = __ldg(reinterpret_cast<const unsigned long long*>(a.texels) + tm.offset +
-				uint64_t(sv) * tm.width + uint32_t(su));
-			out = P::from_cv(shade_texel<DIRECTIONAL>(a, s, tm.flags, texel, u, v));
+			const uint32_t sv = wrap(s.tc1 + int32_t(v), s.tex_h);
+			const uint32_t su = wrap(s.tc0 + int32_t(u), s.tex_w);
+			const uint64_t texel =
+				__ldg(reinterpret_cast<const unsigned long long*>(a.texels) + s.tex_offset + uint64_t(sv) * s.tex_w + su);
+			out = P::from_cv(shade_texel<DIRECTIONAL>(a, s, texel, u, v));
 		}
-		if (s.emissive_mip != SW_NO_EMISSIVE) out = emissive_mix<P>(a, s, u, v, out, diffuse_layer);
+		if (s.flags & SW_SG_EMISSIVE) out = emissive_mix<P>(a, s, u, v, out, diffuse_layer);
 		arena[s.out_offset + local] = out;
 	}
 }
 
+// f32 -> i32 `as` conversion: truncating, saturating, NaN -> 0.
+int32_t host_f2i32(float x)
+{
+	if (x != x) return 0;
+	if (x >= 2147483648.0f) return INT32_MAX;
+	if (x <= -2147483648.0f) return INT32_MIN;
+	return int32_t(x);
+}
+
+float host_dot(const float* a, const float* b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
+
 } // namespace
+
+void make_surface_gpu(const SwSurfaceDesc& d, const SwTextureMip* tex, const SwEmissiveMip* em, SurfaceGpu& o)
+{
+	// surfaces.rs:456-462: start + u*(tc0+0.5) + v*(tc1+0.5); normalised basis vectors.
+	const float a0 = float(d.tc_start[0]) + 0.5f, a1 = float(d.tc_start[1]) + 0.5f;
+	for (int i = 0; i < 3; ++i)
+	{
+		o.start_pos[i] = (d.basis_start[i] + d.basis_u[i] * a0) + d.basis_v[i] * a1;
+		o.u[i] = d.basis_u[i];
+		o.v[i] = d.basis_v[i];
+		o.normal[i] = d.basis_normal[i];
+	}
+	const float iu = 1.0f / std::sqrt(std::fmax(host_dot(d.basis_u, d.basis_u), MIN_POSITIVE_VALUE));
+	const float iv = 1.0f / std::sqrt(std::fmax(host_dot(d.basis_v, d.basis_v), MIN_POSITIVE_VALUE));
+	for (int i = 0; i < 3; ++i)
+	{
+		o.u_norm[i] = d.basis_u[i] * iu;
+		o.v_norm[i] = d.basis_v[i] * iv;
+	}
+	const bool has_lm = d.lightmap_offset != SW_NO_LIGHTMAP;
+	const uint32_t log2 = has_lm ? d.lightmap_scale_log2 : 0u;
+	o.inv_scale = 1.0f / float(1u << log2);
+	o.k_shift = 0.5f * o.inv_scale;
+	o.width = d.size[0];
+	o.flags = 0;
+	if (d.flags & SW_SURF_DIFFUSE_LAYER)
+	{
+		o.tex_offset = tex->offset;
+		o.tex_w = tex->width;
+		o.tex_h = tex->height;
+		o.flags |= (tex->flags & 7u) | SW_SG_DIFFUSE;
+	}
+	else
+	{
+		o.tex_offset = 0;
+		o.tex_w = o.tex_h = 1;
+	}
+	if (has_lm) o.flags |= SW_SG_LIGHTMAP;
+	o.tc0 = d.tc_start[0];
+	o.tc1 = d.tc_start[1];
+	o.lm_offset = d.lightmap_offset;
+	o.lm_width = d.lightmap_size[0];
+	o.lm_log2 = log2;
+	o.lm_shift0 = d.lightmap_tc_shift[0];
+	o.lm_shift1 = d.lightmap_tc_shift[1];
+	o.num_lights = d.num_lights;
+	for (int i = 0; i < SW_MAX_POLYGON_LIGHTS; ++i) o.lights[i] = d.lights[i];
+	if (em)
+	{
+		o.flags |= SW_SG_EMISSIVE;
+		o.em_offset = em->offset;
+		o.em_w = em->width;
+		o.em_h = em->height;
+		// ColorVecI::from_color_f32x3([l0*256, l1*256, l2*256]) -> lanes [b, g, r] (surfaces.rs:911-914)
+		o.em_light[0] = host_f2i32(d.emissive_light[2] * 256.0f);
+		o.em_light[1] = host_f2i32(d.emissive_light[1] * 256.0f);
+		o.em_light[2] = host_f2i32(d.emissive_light[0] * 256.0f);
+	}
+	else
+	{
+		o.em_offset = 0;
+		o.em_w = o.em_h = 1;
+		o.em_light[0] = o.em_light[1] = o.em_light[2] = 0;
+	}
+	o.out_offset = d.out_offset;
+}
 
 int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream)
 {
 	if (args.total_work == 0) return 0;
 	const int threads = 256;
 	uint64_t blocks_needed = (args.total_work + threads - 1) / threads;
-	uint64_t blocks_max = uint64_t(num_sms) * 8;
+	uint64_t blocks_max = uint64_t(num_sms) * 3;
 	unsigned blocks = unsigned(blocks_needed < blocks_max ? blocks_needed : blocks_max);
 	if (pixel_format == SW_PIXEL_C64)
 	{

@@ -6,23 +6,57 @@
 namespace swgpu
 {
 
+// Per-surface record the surface kernel reads (built on the host from SwSurfaceDesc and the texture
+// tables). Everything that is constant over a surface is evaluated once here, with the same IEEE f32
+// operations and order as the reference's per-surface prologue (surfaces.rs:453-471), so the per-texel
+// work in the kernel is only the reference's inner loop.
+struct __align__(16) SurfaceGpu
+{
+	float start_pos[3]; // basis.start + u*(tc0 + 0.5) + v*(tc1 + 0.5)
+	float u[3];
+	float v[3];
+	float normal[3];
+	float u_norm[3];    // u * inv_sqrt_fast(max(|u|^2, MIN_POSITIVE_VALUE))
+	float v_norm[3];
+	float inv_scale;    // 1 / (1 << lightmap_scale_log2)
+	float k_shift;      // 0.5 * inv_scale
+	uint64_t tex_offset;
+	uint32_t width;     // surface width in texels
+	uint32_t tex_w, tex_h;
+	uint32_t flags;     // SW_TEX_* in bits 0..2, SW_SURF_DIFFUSE_LAYER << 8, has lightmap << 9, emissive << 10
+	int32_t tc0, tc1;
+	uint32_t lm_offset, lm_width, lm_log2, lm_shift0, lm_shift1;
+	uint32_t num_lights;
+	uint16_t lights[SW_MAX_POLYGON_LIGHTS];
+	uint64_t em_offset;
+	uint32_t em_w, em_h;
+	int32_t em_light[3]; // ColorVecI lanes [b, g, r] of the emissive light * 256 (truncated)
+	uint64_t out_offset;
+};
+
+#define SW_SG_DIFFUSE (1u << 8)
+#define SW_SG_LIGHTMAP (1u << 9)
+#define SW_SG_EMISSIVE (1u << 10)
+
 struct SurfaceKernelArgs
 {
-	const SwSurfaceDesc* surfaces;
+	const SurfaceGpu* surfaces;
 	const uint64_t* work_prefix; // num_surfaces + 1 entries, texel prefix sums in descriptor order
 	uint32_t num_surfaces;
 	uint32_t directional;
 	uint64_t total_work;
 	const uint64_t* texels;
-	const SwTextureMip* texture_mips;
 	const uint32_t* emissive_pixels;
-	const SwEmissiveMip* emissive_mips;
 	const float* lightmaps;
 	const SwDirectionalLightmapElement* directional_lightmaps;
 	const SwLight* lights;
 	float cam_pos[3];
 	void* arena;
 };
+
+// Host-side construction of one SurfaceGpu (exact f32 arithmetic; the file is compiled without FMA
+// contraction).
+void make_surface_gpu(const SwSurfaceDesc& d, const SwTextureMip* tex, const SwEmissiveMip* em, SurfaceGpu& out);
 
 int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream);
 

@@ -89,7 +89,37 @@ struct SwCtx
 	DevBuf up_src, up_dst;
 
 	SwStats stats{};
+
+	// Optional per-stage device timing (sw_enable_timing).
+	bool timing = false;
+	cudaEvent_t t_begin[4] = {nullptr, nullptr, nullptr, nullptr};
+	cudaEvent_t t_end[4] = {nullptr, nullptr, nullptr, nullptr};
+	bool t_valid[4] = {false, false, false, false};
 };
+
+namespace
+{
+enum Stage
+{
+	STAGE_SURFACES = 0,
+	STAGE_RASTER = 1,
+	STAGE_POST = 2,
+	STAGE_UPSCALE = 3
+};
+
+void stage_begin(SwCtx* ctx, int s)
+{
+	if (ctx->timing) cudaEventRecord(ctx->t_begin[s], ctx->stream);
+}
+void stage_end(SwCtx* ctx, int s)
+{
+	if (ctx->timing)
+	{
+		cudaEventRecord(ctx->t_end[s], ctx->stream);
+		ctx->t_valid[s] = true;
+	}
+}
+} // namespace
 
 namespace
 {
@@ -147,10 +177,10 @@ void release(DevBuf& b)
 	b.bytes = 0;
 }
 
-// Copy `bytes` from host memory `src` into device buffer `dst` through a pinned staging buffer.
-int upload(SwCtx* ctx, Staging& st, void* dst, const void* src, size_t bytes)
+// Pinned staging: acquire() waits until the previous copy out of the buffer finished and grows it;
+// the caller fills it; commit() enqueues the host-to-device copy on the context's stream.
+int staging_acquire(SwCtx* ctx, Staging& st, size_t bytes, void** host)
 {
-	if (bytes == 0) return SW_OK;
 	if (st.pending)
 	{
 		SW_CUDA(ctx, cudaEventSynchronize(st.done));
@@ -158,18 +188,36 @@ int upload(SwCtx* ctx, Staging& st, void* dst, const void* src, size_t bytes)
 	}
 	if (st.bytes < bytes)
 	{
+		const size_t want = std::max(bytes, st.bytes * 2);
 		if (st.host) cudaFreeHost(st.host);
 		st.host = nullptr;
-		size_t want = std::max(bytes, st.bytes * 2);
+		st.bytes = 0;
 		SW_CUDA(ctx, cudaMallocHost(&st.host, want));
 		st.bytes = want;
 	}
 	if (!st.done) SW_CUDA(ctx, cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming));
-	std::memcpy(st.host, src, bytes);
+	*host = st.host;
+	return SW_OK;
+}
+
+int staging_commit(SwCtx* ctx, Staging& st, void* dst, size_t bytes)
+{
+	if (bytes == 0) return SW_OK;
 	SW_CUDA(ctx, cudaMemcpyAsync(dst, st.host, bytes, cudaMemcpyHostToDevice, ctx->stream));
 	SW_CUDA(ctx, cudaEventRecord(st.done, ctx->stream));
 	st.pending = true;
 	return SW_OK;
+}
+
+// Copy `bytes` from host memory `src` into device buffer `dst` through a pinned staging buffer.
+int upload(SwCtx* ctx, Staging& st, void* dst, const void* src, size_t bytes)
+{
+	if (bytes == 0) return SW_OK;
+	void* h = nullptr;
+	int r = staging_acquire(ctx, st, bytes, &h);
+	if (r) return r;
+	std::memcpy(h, src, bytes);
+	return staging_commit(ctx, st, dst, bytes);
 }
 
 int upload_static(SwCtx* ctx, DevBuf& b, const void* src, size_t bytes)
@@ -339,6 +387,11 @@ int sw_destroy(SwCtx* ctx)
 	}
 	if (ctx->h_average) cudaFreeHost(ctx->h_average);
 	if (ctx->average_ready) cudaEventDestroy(ctx->average_ready);
+	for (int i = 0; i < 4; ++i)
+	{
+		if (ctx->t_begin[i]) cudaEventDestroy(ctx->t_begin[i]);
+		if (ctx->t_end[i]) cudaEventDestroy(ctx->t_end[i]);
+	}
 	if (ctx->stream) cudaStreamDestroy(ctx->stream);
 	delete ctx;
 	return SW_OK;
@@ -354,6 +407,32 @@ int sw_sync(SwCtx* ctx)
 {
 	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
 	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	return SW_OK;
+}
+
+int sw_enable_timing(SwCtx* ctx, int enable)
+{
+	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
+	if (enable && !ctx->t_begin[0])
+		for (int i = 0; i < 4; ++i)
+		{
+			SW_CUDA(ctx, cudaEventCreate(&ctx->t_begin[i]));
+			SW_CUDA(ctx, cudaEventCreate(&ctx->t_end[i]));
+		}
+	ctx->timing = enable != 0;
+	for (int i = 0; i < 4; ++i) ctx->t_valid[i] = false;
+	return SW_OK;
+}
+
+int sw_get_timings(SwCtx* ctx, float out_ms[4])
+{
+	if (!ctx || !out_ms) return SW_ERR_INVALID_ARGUMENT;
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	for (int i = 0; i < 4; ++i)
+	{
+		out_ms[i] = 0.0f;
+		if (ctx->t_valid[i]) SW_CUDA(ctx, cudaEventElapsedTime(&out_ms[i], ctx->t_begin[i], ctx->t_end[i]));
+	}
 	return SW_OK;
 }
 
@@ -388,21 +467,21 @@ int sw_frame_begin(SwCtx* ctx, const SwFrameParams* params, const SwLight* light
 static int launch_surfaces(SwCtx* ctx)
 {
 	SurfaceKernelArgs a;
-	a.surfaces = static_cast<const SwSurfaceDesc*>(ctx->surfaces.ptr);
+	a.surfaces = static_cast<const SurfaceGpu*>(ctx->surfaces.ptr);
 	a.work_prefix = static_cast<const uint64_t*>(ctx->work_prefix.ptr);
 	a.num_surfaces = ctx->last_num_surfaces;
 	a.directional = ctx->last_surface_directional ? 1u : 0u;
 	a.total_work = ctx->last_surface_work;
 	a.texels = static_cast<const uint64_t*>(ctx->texels.ptr);
-	a.texture_mips = static_cast<const SwTextureMip*>(ctx->texture_mips.ptr);
 	a.emissive_pixels = static_cast<const uint32_t*>(ctx->emissive.ptr);
-	a.emissive_mips = static_cast<const SwEmissiveMip*>(ctx->emissive_mips.ptr);
 	a.lightmaps = static_cast<const float*>(ctx->lightmaps.ptr);
 	a.directional_lightmaps = static_cast<const SwDirectionalLightmapElement*>(ctx->dir_lightmaps.ptr);
 	a.lights = static_cast<const SwLight*>(ctx->lights.ptr);
 	for (int i = 0; i < 3; ++i) a.cam_pos[i] = ctx->frame.cam_pos[i];
 	a.arena = ctx->arena.ptr;
+	stage_begin(ctx, STAGE_SURFACES);
 	int r = check_kernel(ctx, launch_surface_build(a, ctx->frame.pixel_format, ctx->num_sms, ctx->stream), "surface build");
+	stage_end(ctx, STAGE_SURFACES);
 	if (r) return r;
 	ctx->arena_valid = true;
 	ctx->stats.surfaces += ctx->last_num_surfaces;
@@ -416,7 +495,14 @@ int sw_submit_surfaces(SwCtx* ctx, const SwSurfaceDesc* surfaces, uint32_t num_s
 	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_submit_surfaces");
 	const bool directional = ctx->frame.use_directional_lightmaps != 0;
 	const uint64_t lm_elems = directional ? ctx->num_dir_lightmap_elements : ctx->num_lightmap_elements;
-	std::vector<uint64_t> prefix(size_t(num_surfaces) + 1);
+	int r;
+	SurfaceGpu* gs = nullptr;
+	uint64_t* prefix = nullptr;
+	if ((r = staging_acquire(ctx, ctx->stage_surfaces, std::max<size_t>(num_surfaces, 1) * sizeof(SurfaceGpu),
+			 reinterpret_cast<void**>(&gs))))
+		return r;
+	if ((r = staging_acquire(ctx, ctx->stage_prefix, (size_t(num_surfaces) + 1) * 8, reinterpret_cast<void**>(&prefix))))
+		return r;
 	uint64_t acc = 0;
 	for (uint32_t i = 0; i < num_surfaces; ++i)
 	{
@@ -443,16 +529,17 @@ int sw_submit_surfaces(SwCtx* ctx, const SwSurfaceDesc* surfaces, uint32_t num_s
 				uint64_t(s.lightmap_offset) + uint64_t(s.lightmap_size[0]) * s.lightmap_size[1] > lm_elems)
 				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: lightmap reads out of range", i);
 		}
+		make_surface_gpu(s, (s.flags & SW_SURF_DIFFUSE_LAYER) ? &ctx->h_texture_mips[s.texture_mip] : nullptr,
+			s.emissive_mip != SW_NO_EMISSIVE ? &ctx->h_emissive_mips[s.emissive_mip] : nullptr, gs[i]);
 		acc += area;
 	}
 	prefix[num_surfaces] = acc;
 	const uint32_t bpp = bpp_of(ctx->frame.pixel_format);
-	int r;
 	if ((r = ensure(ctx, ctx->arena, std::max<uint64_t>(total_texels, 1) * bpp))) return r;
-	if ((r = ensure(ctx, ctx->surfaces, std::max<size_t>(num_surfaces, 1) * sizeof(SwSurfaceDesc)))) return r;
-	if ((r = ensure(ctx, ctx->work_prefix, prefix.size() * 8))) return r;
-	if ((r = upload(ctx, ctx->stage_surfaces, ctx->surfaces.ptr, surfaces, num_surfaces * sizeof(SwSurfaceDesc)))) return r;
-	if ((r = upload(ctx, ctx->stage_prefix, ctx->work_prefix.ptr, prefix.data(), prefix.size() * 8))) return r;
+	if ((r = ensure(ctx, ctx->surfaces, std::max<size_t>(num_surfaces, 1) * sizeof(SurfaceGpu)))) return r;
+	if ((r = ensure(ctx, ctx->work_prefix, (size_t(num_surfaces) + 1) * 8))) return r;
+	if ((r = staging_commit(ctx, ctx->stage_surfaces, ctx->surfaces.ptr, num_surfaces * sizeof(SurfaceGpu)))) return r;
+	if ((r = staging_commit(ctx, ctx->stage_prefix, ctx->work_prefix.ptr, (size_t(num_surfaces) + 1) * 8))) return r;
 	ctx->arena_texels = total_texels;
 	ctx->arena_format = ctx->frame.pixel_format;
 
@@ -557,7 +644,10 @@ int sw_render(SwCtx* ctx, void* dst, uint32_t pitch, int dst_is_device)
 	a.arena_texels = ctx->arena_texels;
 	a.framebuffer = ctx->framebuffer.ptr;
 	a.error_counter = static_cast<unsigned int*>(ctx->error_counter.ptr);
-	if ((r = check_kernel(ctx, launch_raster(a, fmt, ctx->num_sms, ctx->stream), "raster"))) return r;
+	stage_begin(ctx, STAGE_RASTER);
+	r = check_kernel(ctx, launch_raster(a, fmt, ctx->num_sms, ctx->stream), "raster");
+	stage_end(ctx, STAGE_RASTER);
+	if (r) return r;
 	ctx->frame_open = false;
 	if (dst) return copy_out(ctx, dst, pitch, dst_is_device, ctx->framebuffer.ptr, w, w, h, bpp);
 	return SW_OK;
@@ -664,7 +754,10 @@ int sw_postprocess(SwCtx* ctx, const SwPostConfig* config, float frame_duration_
 	}
 	a.dst = static_cast<uint32_t*>(out);
 	a.dst_pitch = out_pitch;
-	if ((r = check_kernel(ctx, launch_postprocess(a, ctx->num_sms, ctx->stream), "postprocess"))) return r;
+	stage_begin(ctx, STAGE_POST);
+	r = check_kernel(ctx, launch_postprocess(a, ctx->num_sms, ctx->stream), "postprocess");
+	stage_end(ctx, STAGE_POST);
+	if (r) return r;
 	SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_average, ctx->average.ptr, 16, cudaMemcpyDeviceToHost, ctx->stream));
 	SW_CUDA(ctx, cudaEventRecord(ctx->average_ready, ctx->stream));
 	ctx->exposure_pending = true;
@@ -701,11 +794,12 @@ int sw_upscale(SwCtx* ctx, uint32_t mode, uint32_t scale, const void* src, int s
 		d = ctx->up_dst.ptr;
 		dp = dst_width;
 	}
-	if ((r = check_kernel(ctx,
-			 launch_upscale(mode, scale, static_cast<const uint32_t*>(s), static_cast<uint32_t*>(d), dst_width, dst_height, dp,
-				 ctx->stream),
-			 "upscale")))
-		return r;
+	stage_begin(ctx, STAGE_UPSCALE);
+	r = check_kernel(ctx,
+		launch_upscale(mode, scale, static_cast<const uint32_t*>(s), static_cast<uint32_t*>(d), dst_width, dst_height, dp, ctx->stream),
+		"upscale");
+	stage_end(ctx, STAGE_UPSCALE);
+	if (r) return r;
 	if (!dst_is_device) return copy_out(ctx, dst, dst_pitch, 0, d, dp, dst_width, dst_height, 4);
 	return SW_OK;
 }
@@ -757,6 +851,7 @@ int sw_get_stats(SwCtx* ctx, SwStats* out)
 	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 	*out = ctx->stats;
 	out->bad_texel_fetches = errs[0];
+	out->pixel_writes = uint64_t(errs[2]) | (uint64_t(errs[3]) << 32);
 	return SW_OK;
 }
 

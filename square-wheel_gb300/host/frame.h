@@ -1,0 +1,132 @@
+// Per-frame host work of the renderer: everything above the C ABI of the GPU path.
+//
+// Restates, for world polygons, the reference's host-side per-frame steps:
+//   MapVisibilityCalculator::update_visibility (src/square_wheel/map_visibility_calculator.rs:52-326),
+//   DynamicObjectsIndex::position_dynamic_lights (src/square_wheel/dynamic_objects_index.rs:108-241),
+//   prepare_polygons_surfaces / prepare_polygon_surface (src/square_wheel/partial_renderer.rs:1327-1638),
+//   the descriptor half of build_polygons_surfaces (partial_renderer.rs:1640-1819) with
+//   polygon_is_affected_by_light (:3877-3985),
+//   draw_tree / draw_leaf / draw_polygon (:2450-2559, :4011-4142) with project_and_clip_polygon,
+//   calculate_mip and the interpolation-mode tests (src/square_wheel/renderer_utils.rs), the clipping
+//   helpers (src/common/clipping.rs:4-185) and ClippingPolygon (src/common/clipping_polygon.rs).
+// Output: the SwSurfaceDesc list (in the reference's surface allocation order) and the SwDrawCmd list
+// (in exact submission order) that the GPU path consumes.
+#pragma once
+
+#include <vector>
+
+#include "scene.h"
+
+namespace swhost
+{
+
+struct ClipAxis
+{
+	float min, max;
+};
+struct ClippingPolygon
+{
+	ClipAxis x, y, x_plus_y, x_minus_y;
+	static ClippingPolygon from_box(float min_x, float min_y, float max_x, float max_y);
+	static ClippingPolygon from_point(Vec2 p);
+	bool is_valid_and_non_empty() const;
+	bool contains(const ClippingPolygon& o) const;
+	void extend(const ClippingPolygon& o);
+	void extend_with_point(Vec2 p);
+	void intersect(const ClippingPolygon& o);
+	void get_clip_planes(Vec3 out[8]) const;
+};
+
+struct DepthEquation
+{
+	float d_inv_z_dx, d_inv_z_dy, k;
+	float sample(Vec2 p) const { return d_inv_z_dx * p.x + d_inv_z_dy * p.y + k; }
+};
+struct TexCoordEquation
+{
+	float d_tc_dx[2], d_tc_dy[2], k[2];
+};
+
+struct FrameOptions
+{
+	uint32_t width = 640, height = 480;
+	uint32_t pixel_format = SW_PIXEL_C32;
+	bool use_directional_lightmaps = true;
+	bool clear_background = false;
+	float fov = 3.14159265358979323846f * 0.375f; // test game FOV, src/test_game/game_map.rs:865
+	float mip_bias = 0.0f;                        // textures_mip_bias default, dynamic_mip_bias off
+};
+
+struct FrameStats
+{
+	uint32_t visible_leafs = 0, visible_polygons = 0, draws = 0, camera_leaf = 0;
+	uint64_t surface_texels = 0;
+};
+
+class FramePrep
+{
+public:
+	explicit FramePrep(const Scene& scene);
+	// Camera and lights of scene frame `frame_index` (camera path key, moving lights).
+	void prepare(uint32_t frame_index, const FrameOptions& opt);
+	// Same with an explicit camera and light list.
+	void prepare_with_camera(const CameraMatrices& cam, const std::vector<SwLight>& lights, const FrameOptions& opt);
+
+	std::vector<SwSurfaceDesc> surfaces;
+	uint64_t total_texels = 0;
+	std::vector<SwDrawCmd> draws;
+	std::vector<SwVertex16> vertices;
+	std::vector<SwLight> lights;
+	SwFrameParams params{};
+	FrameStats stats;
+
+private:
+	struct LeafData
+	{
+		uint32_t visible_frame = 0;
+		ClippingPolygon bounds{};
+	};
+	struct PortalData
+	{
+		uint32_t visible_frame = 0;
+		bool has_projection = false;
+		ClippingPolygon projection{};
+	};
+	struct PolyData
+	{
+		uint32_t visible_frame = 0;
+		DepthEquation depth;
+		TexCoordEquation tc;
+		uint64_t offset = 0;
+		uint32_t size[2] = {0, 0};
+		uint32_t mip = 0;
+		int32_t tc_min[2] = {0, 0};
+	};
+
+	const Scene& sc;
+	uint32_t current_frame = 0;
+	std::vector<LeafData> leaf_data;
+	std::vector<PortalData> portal_data;
+	std::vector<uint32_t> wave0, wave1;
+	std::vector<PolyData> poly;
+	std::vector<Vec3> vertices_transformed;
+	std::vector<uint32_t> visible_polygons;
+	std::vector<std::vector<uint32_t>> leaf_lights;
+	CameraMatrices cam{};
+	FrameOptions opt;
+
+	uint32_t find_current_leaf() const;
+	void update_visibility(const ClippingPolygon& frame_bounds);
+	void mark_reachable_leafs(const uint32_t* start, uint32_t n, const ClippingPolygon& bounds);
+	bool project_portal(const MapPortal& p, ClippingPolygon& out) const;
+	void position_lights();
+	void position_sphere(uint32_t id, Vec3 center, float radius, uint32_t node);
+	void prepare_polygons_surfaces();
+	void prepare_polygon_surface(const Vec3 clip_planes[8], uint64_t& offset, uint32_t polygon_index);
+	void build_surface_descs();
+	void draw_tree();
+	void draw_leaf(const ClippingPolygon& bounds, uint32_t leaf_index);
+	void draw_polygon(const Vec3 clip_planes[8], uint32_t polygon_index);
+};
+
+} // namespace swhost

@@ -1,0 +1,905 @@
+// Seeded synthetic scene generator (see scene.h). Load-time work, not on the timed path.
+#include "scene.h"
+
+#include <algorithm>
+#include <cstring>
+#include <functional>
+
+namespace swhost
+{
+
+namespace
+{
+
+// Deterministic RNG (splitmix64): identical sequences on every platform.
+struct Rng
+{
+	uint64_t s;
+	explicit Rng(uint64_t seed) : s(seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull) {}
+	uint64_t next()
+	{
+		uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+		z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+		z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+		return z ^ (z >> 31);
+	}
+	float uniform() { return float(next() >> 40) * (1.0f / 16777216.0f); } // [0, 1)
+	float uniform(float a, float b) { return a + (b - a) * uniform(); }
+	uint32_t below(uint32_t n) { return n ? uint32_t(next() % n) : 0u; }
+};
+
+constexpr float CELL_PITCH = 1280.0f;   // cell slot 1024 + 256 gap
+constexpr float CELL_SLOT = 1024.0f;
+constexpr float CORRIDOR_HALF = 64.0f;  // corridors are 128 wide and 128 high
+constexpr float CORRIDOR_HEIGHT = 128.0f;
+
+struct Room
+{
+	float x0, x1, y0, y1, h;
+	float cx, cy; // corridor centre lines (cell centre lines)
+	uint32_t mat_wall, mat_floor, mat_ceiling;
+	int32_t tc_shift[2];
+	std::vector<Vec3> lights;
+	std::vector<Vec3> light_colors;
+};
+
+float snap16(float v) { return std::floor(v / 16.0f) * 16.0f; }
+
+// ---- textures -------------------------------------------------------------------------------
+
+uint32_t pack_normal_roughness(Vec3 n, float roughness)
+{
+	// PackedNormalRoughness::pack with the generic pack_f32x4_into_bytes (truncating), textures.rs:33-39
+	const float v[4] = {n.x, n.y, n.z, roughness};
+	uint32_t r = 0;
+	for (int i = 0; i < 4; ++i)
+	{
+		float s = std::fmin(std::fmax(v[i] * 127.0f, -127.0f), 127.0f);
+		r |= (uint32_t(int32_t(s)) & 0xFFu) << (i * 8);
+	}
+	return r;
+}
+
+void unpack_normal_roughness(uint32_t p, Vec3& n, float& r)
+{
+	float o[4];
+	for (int i = 0; i < 4; ++i) o[i] = float(int32_t(p << (24 - i * 8)) >> 24) * (1.0f / 127.0f);
+	n = v3(o[0], o[1], o[2]);
+	r = o[3];
+}
+
+uint32_t average4(uint32_t a, uint32_t b, uint32_t c, uint32_t d)
+{
+	// Color32::get_average_4, src/common/color.rs:51-71
+	uint32_t s[4] = {0, 0, 0, 0};
+	for (uint32_t x : {a, b, c, d})
+	{
+		s[0] += x & 0xFFu;
+		s[1] += x & 0xFF00u;
+		s[2] += x & 0xFF0000u;
+		s[3] += (x & 0xFF000000u) >> 2;
+	}
+	return (s[0] >> 2) | ((s[1] >> 2) & 0xFF00u) | ((s[2] >> 2) & 0xFF0000u) | (s[3] & 0xFF000000u);
+}
+
+// build_texture_mip, src/square_wheel/textures.rs:309-362
+void build_mip(const std::vector<uint64_t>& src, uint32_t sw, uint32_t sh, std::vector<uint64_t>& dst)
+{
+	const uint32_t w = sw >> 1, h = sh >> 1;
+	dst.assign(size_t(w) * h, 0);
+	for (uint32_t y = 0; y < h; ++y)
+		for (uint32_t x = 0; x < w; ++x)
+		{
+			const uint64_t p00 = src[(2 * y) * sw + 2 * x], p01 = src[(2 * y + 1) * sw + 2 * x];
+			const uint64_t p10 = src[(2 * y) * sw + 2 * x + 1], p11 = src[(2 * y + 1) * sw + 2 * x + 1];
+			const uint32_t diffuse = average4(uint32_t(p00), uint32_t(p01), uint32_t(p10), uint32_t(p11));
+			Vec3 n[4];
+			float r[4];
+			const uint64_t ps[4] = {p00, p01, p10, p11};
+			for (int i = 0; i < 4; ++i) unpack_normal_roughness(uint32_t(ps[i] >> 32), n[i], r[i]);
+			const Vec3 sum = n[0] + n[1] + n[2] + n[3];
+			const float len = std::fmax(magnitude(sum), 0.000001f);
+			const Vec3 nn = sum / len;
+			const float deviation = (1.0f - len * 0.25f) / (1.0f - 0.5f);
+			const float rs = r[0] + r[1] + r[2] + r[3];
+			const float rough = std::fmin(std::fmax(rs * 0.25f + deviation, 1.0f / 126.0f), 1.0f);
+			dst[size_t(y) * w + x] = uint64_t(diffuse) | (uint64_t(pack_normal_roughness(nn, rough)) << 32);
+		}
+}
+
+std::vector<float> value_noise(Rng& rng, uint32_t size, uint32_t cells)
+{
+	std::vector<float> g((cells + 1) * (cells + 1));
+	for (float& v : g) v = rng.uniform();
+	for (uint32_t i = 0; i <= cells; ++i) g[cells * (cells + 1) + i] = g[i]; // tileable
+	for (uint32_t j = 0; j <= cells; ++j) g[j * (cells + 1) + cells] = g[j * (cells + 1)];
+	std::vector<float> out(size_t(size) * size);
+	for (uint32_t y = 0; y < size; ++y)
+		for (uint32_t x = 0; x < size; ++x)
+		{
+			float fx = float(x) * cells / size, fy = float(y) * cells / size;
+			uint32_t ix = uint32_t(fx), iy = uint32_t(fy);
+			float tx = fx - ix, ty = fy - iy;
+			tx = tx * tx * (3 - 2 * tx);
+			ty = ty * ty * (3 - 2 * ty);
+			const float a = g[iy * (cells + 1) + ix], b = g[iy * (cells + 1) + ix + 1];
+			const float c = g[(iy + 1) * (cells + 1) + ix], d = g[(iy + 1) * (cells + 1) + ix + 1];
+			out[size_t(y) * size + x] = (a * (1 - tx) + b * tx) * (1 - ty) + (c * (1 - tx) + d * tx) * ty;
+		}
+	return out;
+}
+
+void make_material_texture(Rng& rng, uint32_t size, bool normal_map, float roughness, bool metal, Scene& sc)
+{
+	const std::vector<float> n1 = value_noise(rng, size, 8), n2 = value_noise(rng, size, 32);
+	const float base[3] = {rng.uniform(0.3f, 0.9f), rng.uniform(0.3f, 0.9f), rng.uniform(0.3f, 0.9f)};
+	const uint32_t check = std::max(size / 8, 1u);
+	std::vector<float> height(size_t(size) * size);
+	std::vector<uint64_t> level(size_t(size) * size);
+	for (uint32_t y = 0; y < size; ++y)
+		for (uint32_t x = 0; x < size; ++x)
+		{
+			const size_t i = size_t(y) * size + x;
+			const float checker = float(((x / check) + (y / check)) & 1u);
+			const float lum = 0.55f + 0.3f * n1[i] + 0.15f * n2[i] - 0.12f * checker;
+			uint32_t c[3];
+			for (int k = 0; k < 3; ++k) c[k] = uint32_t(std::fmin(std::fmax(lum * base[k] * 255.0f, 0.0f), 255.0f));
+			level[i] = uint64_t((255u << 24) | (c[0] << 16) | (c[1] << 8) | c[2]);
+			height[i] = n1[i] * 2.0f + n2[i] * 0.5f + checker * 0.5f;
+		}
+	for (uint32_t y = 0; y < size; ++y)
+		for (uint32_t x = 0; x < size; ++x)
+		{
+			const size_t i = size_t(y) * size + x;
+			Vec3 n = v3(0, 0, 1);
+			if (normal_map)
+			{
+				const float gx = (height[y * size + (x + 1) % size] - height[y * size + (x + size - 1) % size]) * (size / 64.0f);
+				const float gy = (height[((y + 1) % size) * size + x] - height[((y + size - 1) % size) * size + x]) * (size / 64.0f);
+				n = v3(-gx, -gy, 1.0f);
+				n = n / magnitude(n);
+			}
+			float r = 1.0f;
+			if (roughness < 1.0f) r = std::fmin(std::fmax(roughness * (0.8f + 0.2f * n2[i]), 1.0f / 126.0f), 1.0f);
+			level[i] |= uint64_t(pack_normal_roughness(n, r)) << 32;
+		}
+	uint32_t flags = 0;
+	if (normal_map) flags |= SW_TEX_HAS_NORMAL_MAP;
+	if (roughness < 1.0f) flags |= SW_TEX_HAS_NON_ONE_ROUGHNESS;
+	if (metal) flags |= SW_TEX_IS_METAL;
+	uint32_t w = size, h = size;
+	for (uint32_t m = 0; m < NUM_MIPS; ++m)
+	{
+		SwTextureMip tm;
+		tm.offset = sc.texels.size();
+		tm.width = w;
+		tm.height = h;
+		tm.flags = flags;
+		tm.reserved = 0;
+		sc.texture_mips.push_back(tm);
+		sc.texels.insert(sc.texels.end(), level.begin(), level.end());
+		if (m + 1 < NUM_MIPS)
+		{
+			std::vector<uint64_t> next;
+			build_mip(level, w, h, next);
+			level.swap(next);
+			w >>= 1;
+			h >>= 1;
+		}
+	}
+}
+
+void make_emissive_texture(Rng& rng, uint32_t size, Scene& sc)
+{
+	std::vector<uint32_t> level(size_t(size) * size);
+	const std::vector<float> n = value_noise(rng, size, 16);
+	for (size_t i = 0; i < level.size(); ++i)
+	{
+		const uint32_t v = uint32_t(std::fmin(n[i] * n[i] * 400.0f, 255.0f));
+		level[i] = (255u << 24) | (v << 16) | ((v * 3 / 4) << 8) | (v / 3);
+	}
+	uint32_t w = size, h = size;
+	for (uint32_t m = 0; m < NUM_MIPS; ++m)
+	{
+		sc.emissive_mips.push_back(SwEmissiveMip{sc.emissive_pixels.size(), w, h});
+		sc.emissive_pixels.insert(sc.emissive_pixels.end(), level.begin(), level.end());
+		if (m + 1 < NUM_MIPS)
+		{
+			std::vector<uint32_t> next(size_t(w / 2) * (h / 2));
+			for (uint32_t y = 0; y < h / 2; ++y)
+				for (uint32_t x = 0; x < w / 2; ++x)
+					next[y * (w / 2) + x] = average4(level[(2 * y) * w + 2 * x], level[(2 * y + 1) * w + 2 * x],
+						level[(2 * y) * w + 2 * x + 1], level[(2 * y + 1) * w + 2 * x + 1]);
+			level.swap(next);
+			w >>= 1;
+			h >>= 1;
+		}
+	}
+}
+
+// ---- geometry -------------------------------------------------------------------------------
+
+struct Builder
+{
+	const SceneConfig& cfg;
+	Scene& sc;
+	Rng& rng;
+	std::vector<Room> rooms;
+	std::vector<uint8_t> edge_x, edge_y; // edge_x[i + j*gx]: (i,j)-(i+1,j); edge_y: (i,j)-(i,j+1)
+	std::vector<int32_t> leaf_room;      // owner room of each leaf
+	struct PendingPortal
+	{
+		uint32_t leafs[2];
+		Plane plane;
+		Vec3 v[4];
+	};
+	std::vector<PendingPortal> portals;
+
+	Builder(const SceneConfig& c, Scene& s, Rng& r) : cfg(c), sc(s), rng(r) {}
+
+	uint32_t gx() const { return cfg.grid_x; }
+	uint32_t gy() const { return cfg.grid_y; }
+	Room& room(uint32_t i, uint32_t j) { return rooms[j * gx() + i]; }
+	bool has_x(uint32_t i, uint32_t j) const { return i + 1 < cfg.grid_x && edge_x[j * cfg.grid_x + i]; }
+	bool has_y(uint32_t i, uint32_t j) const { return j + 1 < cfg.grid_y && edge_y[j * cfg.grid_x + i]; }
+
+	void make_rooms()
+	{
+		rooms.resize(size_t(gx()) * gy());
+		for (uint32_t j = 0; j < gy(); ++j)
+			for (uint32_t i = 0; i < gx(); ++i)
+			{
+				Room& r = room(i, j);
+				const float ox = i * CELL_PITCH, oy = j * CELL_PITCH;
+				const float sx = snap16(rng.uniform(cfg.room_min, cfg.room_max + 1.0f));
+				const float sy = snap16(rng.uniform(cfg.room_min, cfg.room_max + 1.0f));
+				r.h = snap16(rng.uniform(std::max(cfg.room_min, 256.0f), cfg.room_max + 1.0f));
+				// Each room covers the cell's centre band so corridors at the centre lines always fit.
+				const float cx = ox + CELL_SLOT * 0.5f, cy = oy + CELL_SLOT * 0.5f;
+				const float lo_x = std::max(ox, cx + CORRIDOR_HALF + 16.0f - sx), hi_x = std::min(cx - CORRIDOR_HALF - 16.0f, ox + CELL_SLOT - sx);
+				const float lo_y = std::max(oy, cy + CORRIDOR_HALF + 16.0f - sy), hi_y = std::min(cy - CORRIDOR_HALF - 16.0f, oy + CELL_SLOT - sy);
+				r.x0 = snap16(rng.uniform(lo_x, std::max(lo_x, hi_x)));
+				r.y0 = snap16(rng.uniform(lo_y, std::max(lo_y, hi_y)));
+				r.x1 = r.x0 + sx;
+				r.y1 = r.y0 + sy;
+				r.cx = cx;
+				r.cy = cy;
+				r.mat_wall = rng.below(cfg.num_materials);
+				r.mat_floor = rng.below(cfg.num_materials);
+				r.mat_ceiling = rng.below(cfg.num_materials);
+				r.tc_shift[0] = int32_t(rng.below(256));
+				r.tc_shift[1] = int32_t(rng.below(256));
+				for (uint32_t l = 0; l < std::max(cfg.lights_per_room, 1u); ++l)
+				{
+					r.lights.push_back(v3(rng.uniform(r.x0 + 32, r.x1 - 32), rng.uniform(r.y0 + 32, r.y1 - 32), rng.uniform(96.0f, r.h - 32.0f)));
+					const float intensity = rng.uniform(0.6e5f, 1.6e5f);
+					r.light_colors.push_back(v3(intensity * rng.uniform(0.8f, 1.0f), intensity * rng.uniform(0.7f, 1.0f), intensity * rng.uniform(0.6f, 1.0f)));
+				}
+			}
+		// Connectivity: random spanning tree over the grid plus extra edges.
+		edge_x.assign(size_t(gx()) * gy(), 0);
+		edge_y.assign(size_t(gx()) * gy(), 0);
+		std::vector<uint8_t> seen(size_t(gx()) * gy(), 0);
+		std::vector<uint32_t> stack{0};
+		seen[0] = 1;
+		while (!stack.empty())
+		{
+			const uint32_t c = stack.back();
+			const uint32_t i = c % gx(), j = c / gx();
+			uint32_t cand[4];
+			int n = 0;
+			if (i + 1 < gx() && !seen[c + 1]) cand[n++] = c + 1;
+			if (i > 0 && !seen[c - 1]) cand[n++] = c - 1;
+			if (j + 1 < gy() && !seen[c + gx()]) cand[n++] = c + gx();
+			if (j > 0 && !seen[c - gx()]) cand[n++] = c - gx();
+			if (n == 0)
+			{
+				stack.pop_back();
+				continue;
+			}
+			const uint32_t d = cand[rng.below(uint32_t(n))];
+			if (d == c + 1) edge_x[c] = 1;
+			else if (d == c - 1) edge_x[c - 1] = 1;
+			else if (d == c + gx()) edge_y[c] = 1;
+			else edge_y[c - gx()] = 1;
+			seen[d] = 1;
+			stack.push_back(d);
+		}
+		for (uint32_t j = 0; j < gy(); ++j)
+			for (uint32_t i = 0; i < gx(); ++i)
+			{
+				if (i + 1 < gx() && rng.uniform() < 0.35f) edge_x[j * gx() + i] = 1;
+				if (j + 1 < gy() && rng.uniform() < 0.35f) edge_y[j * gx() + i] = 1;
+			}
+	}
+
+	// Append one convex quad (clockwise seen from the front) with its tc equations.
+	void add_quad(Vec3 p00, Vec3 p10, Vec3 p11, Vec3 p01, Vec3 normal, uint32_t material, const int32_t tc_shift[2])
+	{
+		// Clockwise on screen when seen from the front <=> cross(v1-v0, v2-v0) . normal < 0.
+		Vec3 q[4] = {p00, p10, p11, p01};
+		if (dot(cross(q[1] - q[0], q[2] - q[0]), normal) > 0.0f) std::swap(q[1], q[3]);
+		MapPolygon p;
+		p.first_vertex = uint32_t(sc.vertices.size());
+		p.num_vertices = 4;
+		for (const Vec3& v : q) sc.vertices.push_back(v);
+		p.plane = Plane{normal, dot(normal, p00)};
+		// Quake-style axis projection, one texel per unit.
+		Vec3 ta, tb;
+		if (std::fabs(normal.z) > 0.5f)
+		{
+			ta = v3(1, 0, 0);
+			tb = v3(0, -1, 0);
+		}
+		else if (std::fabs(normal.x) > 0.5f)
+		{
+			ta = v3(0, 1, 0);
+			tb = v3(0, 0, -1);
+		}
+		else
+		{
+			ta = v3(1, 0, 0);
+			tb = v3(0, 0, -1);
+		}
+		p.tex_coord_equation[0] = Plane{ta, float(tc_shift[0])};
+		p.tex_coord_equation[1] = Plane{tb, float(tc_shift[1])};
+		// Integer tc bounds as the map compiler computes them (bsp_map_compact_conversion.rs:204-238).
+		const float inf = float(1 << 29);
+		float tmin[2] = {inf, inf}, tmax[2] = {-inf, -inf};
+		for (const Vec3& v : q)
+			for (int i = 0; i < 2; ++i)
+			{
+				const float tc = dot(p.tex_coord_equation[i].vec, v) + p.tex_coord_equation[i].dist;
+				tmin[i] = std::fmin(tmin[i], tc);
+				tmax[i] = std::fmax(tmax[i], tc);
+			}
+		for (int i = 0; i < 2; ++i)
+		{
+			p.tex_coord_min[i] = int32_t(std::floor(tmin[i] + 1.0f / 32.0f));
+			p.tex_coord_max[i] = std::max(int32_t(std::ceil(tmax[i] - 1.0f / 32.0f)), p.tex_coord_min[i] + 1);
+		}
+		p.lightmap_data_offset = 0;
+		p.texture = material;
+		sc.polygons.push_back(p);
+	}
+
+	// Tile an axis-aligned rectangle of a face. axis = normal axis (0,1,2), w = coordinate on it,
+	// (a0..a1) x (b0..b1) along the other two axes in increasing order.
+	void add_face_rect(int axis, float w, float sign, float a0, float a1, float b0, float b1, uint32_t material,
+		const int32_t tc_shift[2])
+	{
+		if (a1 - a0 < 0.5f || b1 - b0 < 0.5f) return;
+		const float T = cfg.tile_size;
+		auto cuts = [&](float lo, float hi) {
+			std::vector<float> c{lo};
+			for (float x = std::floor(lo / T) * T + T; x < hi - 0.5f; x += T)
+				if (x > lo + 0.5f) c.push_back(x);
+			c.push_back(hi);
+			return c;
+		};
+		const std::vector<float> ca = cuts(a0, a1), cb = cuts(b0, b1);
+		const Vec3 normal = axis == 0 ? v3(sign, 0, 0) : axis == 1 ? v3(0, sign, 0) : v3(0, 0, sign);
+		auto P = [&](float a, float b) {
+			return axis == 0 ? v3(w, a, b) : axis == 1 ? v3(a, w, b) : v3(a, b, w);
+		};
+		for (size_t ib = 0; ib + 1 < cb.size(); ++ib)
+			for (size_t ia = 0; ia + 1 < ca.size(); ++ia)
+				add_quad(P(ca[ia], cb[ib]), P(ca[ia + 1], cb[ib]), P(ca[ia + 1], cb[ib + 1]), P(ca[ia], cb[ib + 1]), normal, material,
+					tc_shift);
+	}
+
+	// Wall with an optional opening at [o0, o1] x [0, CORRIDOR_HEIGHT] (the opening touches the floor).
+	void add_wall(int axis, float w, float sign, float a0, float a1, float h, bool opening, float o0, float o1,
+		uint32_t material, const int32_t tc_shift[2])
+	{
+		if (!opening)
+		{
+			add_face_rect(axis, w, sign, a0, a1, 0.0f, h, material, tc_shift);
+			return;
+		}
+		add_face_rect(axis, w, sign, a0, o0, 0.0f, h, material, tc_shift);
+		add_face_rect(axis, w, sign, o1, a1, 0.0f, h, material, tc_shift);
+		add_face_rect(axis, w, sign, o0, o1, CORRIDOR_HEIGHT, h, material, tc_shift);
+	}
+
+	uint32_t begin_leaf(int32_t owner_room)
+	{
+		BspLeaf l;
+		l.first_polygon = uint32_t(sc.polygons.size());
+		l.num_polygons = 0;
+		l.first_leaf_portal = 0;
+		l.num_leaf_portals = 0;
+		sc.leafs.push_back(l);
+		leaf_room.push_back(owner_room);
+		return uint32_t(sc.leafs.size() - 1);
+	}
+	void end_leaf(uint32_t leaf) { sc.leafs[leaf].num_polygons = uint32_t(sc.polygons.size()) - sc.leafs[leaf].first_polygon; }
+
+	uint32_t add_node(Plane plane, uint32_t front, uint32_t back)
+	{
+		sc.nodes.push_back(BspNode{{front, back}, plane});
+		return uint32_t(sc.nodes.size() - 1);
+	}
+
+	// Corridor-half leaf: axis 0 = corridor along x spanning [l0, l1], centre line y = c.
+	uint32_t corridor_leaf(int axis, float l0, float l1, float c, uint32_t owner)
+	{
+		const Room& r = rooms[owner];
+		const uint32_t leaf = begin_leaf(int32_t(owner));
+		add_face_rect(2, 0.0f, 1.0f, axis == 0 ? l0 : c - CORRIDOR_HALF, axis == 0 ? l1 : c + CORRIDOR_HALF,
+			axis == 0 ? c - CORRIDOR_HALF : l0, axis == 0 ? c + CORRIDOR_HALF : l1, r.mat_floor, r.tc_shift);
+		add_face_rect(2, CORRIDOR_HEIGHT, -1.0f, axis == 0 ? l0 : c - CORRIDOR_HALF, axis == 0 ? l1 : c + CORRIDOR_HALF,
+			axis == 0 ? c - CORRIDOR_HALF : l0, axis == 0 ? c + CORRIDOR_HALF : l1, r.mat_ceiling, r.tc_shift);
+		const int side_axis = axis == 0 ? 1 : 0;
+		add_face_rect(side_axis, c - CORRIDOR_HALF, 1.0f, l0, l1, 0.0f, CORRIDOR_HEIGHT, r.mat_wall, r.tc_shift);
+		add_face_rect(side_axis, c + CORRIDOR_HALF, -1.0f, l0, l1, 0.0f, CORRIDOR_HEIGHT, r.mat_wall, r.tc_shift);
+		end_leaf(leaf);
+		return leaf;
+	}
+
+	void add_portal(uint32_t front_leaf, uint32_t back_leaf, int axis, float w, float sign, float a0, float a1, float b0, float b1)
+	{
+		PendingPortal p;
+		p.leafs[0] = front_leaf;
+		p.leafs[1] = back_leaf;
+		const Vec3 n = axis == 0 ? v3(sign, 0, 0) : axis == 1 ? v3(0, sign, 0) : v3(0, 0, sign);
+		p.plane = Plane{n, sign * w};
+		auto P = [&](float a, float b) { return axis == 0 ? v3(w, a, b) : axis == 1 ? v3(a, w, b) : v3(a, b, w); };
+		p.v[0] = P(a0, b0);
+		p.v[1] = P(a1, b0);
+		p.v[2] = P(a1, b1);
+		p.v[3] = P(a0, b1);
+		portals.push_back(p);
+	}
+
+	// Corridor halves of cell (i, j) towards its neighbours, created while building the cell subtree.
+	struct CellLeafs
+	{
+		int32_t east = -1, west = -1, north = -1, south = -1;
+	};
+	std::vector<CellLeafs> cell_leafs;
+
+	uint32_t build_cell(uint32_t i, uint32_t j)
+	{
+		const uint32_t ri = j * gx() + i;
+		const Room& r = rooms[ri];
+		const bool E = has_x(i, j), W = i > 0 && has_x(i - 1, j), N = has_y(i, j), S = j > 0 && has_y(i, j - 1);
+		const float gap_e = (i + 1) * CELL_PITCH - 128.0f, gap_w = i * CELL_PITCH - 128.0f;
+		const float gap_n = (j + 1) * CELL_PITCH - 128.0f, gap_s = j * CELL_PITCH - 128.0f;
+		CellLeafs& cl = cell_leafs[ri];
+
+		// Room leaf.
+		const uint32_t room_leaf = begin_leaf(int32_t(ri));
+		add_face_rect(2, 0.0f, 1.0f, r.x0, r.x1, r.y0, r.y1, r.mat_floor, r.tc_shift);
+		add_face_rect(2, r.h, -1.0f, r.x0, r.x1, r.y0, r.y1, r.mat_ceiling, r.tc_shift);
+		add_wall(0, r.x1, -1.0f, r.y0, r.y1, r.h, E, r.cy - CORRIDOR_HALF, r.cy + CORRIDOR_HALF, r.mat_wall, r.tc_shift);
+		add_wall(0, r.x0, 1.0f, r.y0, r.y1, r.h, W, r.cy - CORRIDOR_HALF, r.cy + CORRIDOR_HALF, r.mat_wall, r.tc_shift);
+		add_wall(1, r.y1, -1.0f, r.x0, r.x1, r.h, N, r.cx - CORRIDOR_HALF, r.cx + CORRIDOR_HALF, r.mat_wall, r.tc_shift);
+		add_wall(1, r.y0, 1.0f, r.x0, r.x1, r.h, S, r.cx - CORRIDOR_HALF, r.cx + CORRIDOR_HALF, r.mat_wall, r.tc_shift);
+		end_leaf(room_leaf);
+
+		uint32_t child = room_leaf + FIRST_LEAF_INDEX;
+		if (S)
+		{
+			const uint32_t l = corridor_leaf(1, gap_s, r.y0, r.cx, ri);
+			cl.south = int32_t(l);
+			add_portal(l, room_leaf, 1, r.y0, -1.0f, r.cx - CORRIDOR_HALF, r.cx + CORRIDOR_HALF, 0.0f, CORRIDOR_HEIGHT);
+			child = add_node(Plane{v3(0, -1, 0), -r.y0}, l + FIRST_LEAF_INDEX, child);
+		}
+		if (N)
+		{
+			const uint32_t l = corridor_leaf(1, r.y1, gap_n, r.cx, ri);
+			cl.north = int32_t(l);
+			add_portal(l, room_leaf, 1, r.y1, 1.0f, r.cx - CORRIDOR_HALF, r.cx + CORRIDOR_HALF, 0.0f, CORRIDOR_HEIGHT);
+			child = add_node(Plane{v3(0, 1, 0), r.y1}, l + FIRST_LEAF_INDEX, child);
+		}
+		if (W)
+		{
+			const uint32_t l = corridor_leaf(0, gap_w, r.x0, r.cy, ri);
+			cl.west = int32_t(l);
+			add_portal(l, room_leaf, 0, r.x0, -1.0f, r.cy - CORRIDOR_HALF, r.cy + CORRIDOR_HALF, 0.0f, CORRIDOR_HEIGHT);
+			child = add_node(Plane{v3(-1, 0, 0), -r.x0}, l + FIRST_LEAF_INDEX, child);
+		}
+		if (E)
+		{
+			const uint32_t l = corridor_leaf(0, r.x1, gap_e, r.cy, ri);
+			cl.east = int32_t(l);
+			add_portal(l, room_leaf, 0, r.x1, 1.0f, r.cy - CORRIDOR_HALF, r.cy + CORRIDOR_HALF, 0.0f, CORRIDOR_HEIGHT);
+			child = add_node(Plane{v3(1, 0, 0), r.x1}, l + FIRST_LEAF_INDEX, child);
+		}
+		return child;
+	}
+
+	uint32_t build(uint32_t ix0, uint32_t ix1, uint32_t iy0, uint32_t iy1)
+	{
+		const uint32_t nx = ix1 - ix0, ny = iy1 - iy0;
+		if (nx == 1 && ny == 1) return build_cell(ix0, iy0);
+		if (nx >= ny)
+		{
+			const uint32_t mid = ix0 + nx / 2;
+			const uint32_t back = build(ix0, mid, iy0, iy1);
+			const uint32_t front = build(mid, ix1, iy0, iy1);
+			return add_node(Plane{v3(1, 0, 0), mid * CELL_PITCH - 128.0f}, front, back);
+		}
+		const uint32_t mid = iy0 + ny / 2;
+		const uint32_t back = build(ix0, ix1, iy0, mid);
+		const uint32_t front = build(ix0, ix1, mid, iy1);
+		return add_node(Plane{v3(0, 1, 0), mid * CELL_PITCH - 128.0f}, front, back);
+	}
+
+	void link_corridor_halves()
+	{
+		for (uint32_t j = 0; j < gy(); ++j)
+			for (uint32_t i = 0; i < gx(); ++i)
+			{
+				const Room& r = room(i, j);
+				if (has_x(i, j))
+				{
+					const uint32_t back = uint32_t(cell_leafs[j * gx() + i].east), front = uint32_t(cell_leafs[j * gx() + i + 1].west);
+					add_portal(front, back, 0, (i + 1) * CELL_PITCH - 128.0f, 1.0f, r.cy - CORRIDOR_HALF, r.cy + CORRIDOR_HALF, 0.0f,
+						CORRIDOR_HEIGHT);
+				}
+				if (has_y(i, j))
+				{
+					const uint32_t back = uint32_t(cell_leafs[j * gx() + i].north), front = uint32_t(cell_leafs[(j + 1) * gx() + i].south);
+					add_portal(front, back, 1, (j + 1) * CELL_PITCH - 128.0f, 1.0f, r.cx - CORRIDOR_HALF, r.cx + CORRIDOR_HALF, 0.0f,
+						CORRIDOR_HEIGHT);
+				}
+			}
+		// Store portals and per-leaf portal lists.
+		std::vector<std::vector<uint32_t>> per_leaf(sc.leafs.size());
+		for (size_t k = 0; k < portals.size(); ++k)
+		{
+			const PendingPortal& p = portals[k];
+			MapPortal mp;
+			mp.leafs[0] = p.leafs[0];
+			mp.leafs[1] = p.leafs[1];
+			mp.plane = p.plane;
+			mp.first_vertex = uint32_t(sc.vertices.size());
+			mp.num_vertices = 4;
+			for (const Vec3& v : p.v) sc.vertices.push_back(v);
+			sc.portals.push_back(mp);
+			per_leaf[p.leafs[0]].push_back(uint32_t(k));
+			per_leaf[p.leafs[1]].push_back(uint32_t(k));
+		}
+		for (size_t l = 0; l < sc.leafs.size(); ++l)
+		{
+			sc.leafs[l].first_leaf_portal = uint32_t(sc.leafs_portals.size());
+			sc.leafs[l].num_leaf_portals = uint32_t(per_leaf[l].size());
+			sc.leafs_portals.insert(sc.leafs_portals.end(), per_leaf[l].begin(), per_leaf[l].end());
+		}
+	}
+
+	// Lightmaps: direct light of the owner room's lights, simple (RGB) and directional (ambient +
+	// dominant tangent-space direction, lightmaps_builder.rs:1076-1083 convention).
+	void build_lightmaps()
+	{
+		sc.lightmaps.assign(3, 0.0f);
+		sc.directional_lightmaps.assign(1, SwDirectionalLightmapElement{});
+		uint64_t offset = 1;
+		for (size_t pi = 0; pi < sc.polygons.size(); ++pi)
+		{
+			MapPolygon& p = sc.polygons[pi];
+			const uint32_t lw = uint32_t(((p.tex_coord_max[0] + 15) >> 4) - (p.tex_coord_min[0] >> 4) + 1);
+			const uint32_t lh = uint32_t(((p.tex_coord_max[1] + 15) >> 4) - (p.tex_coord_min[1] >> 4) + 1);
+			p.lightmap_data_offset = uint32_t(offset);
+			offset += uint64_t(lw) * lh;
+			// calculate_lightmap_basis, src/common/lightmap.rs:36-62
+			const float s = 1.0f / float(LIGHTMAP_SCALE);
+			Mat4 m;
+			m.c[0] = extend(p.tex_coord_equation[0].vec, p.tex_coord_equation[0].dist) * s;
+			m.c[1] = extend(p.tex_coord_equation[1].vec, p.tex_coord_equation[1].dist) * s;
+			m.c[2] = extend(p.plane.vec, -p.plane.dist);
+			m.c[3] = v4(0, 0, 0, 1);
+			Mat4 inv;
+			invert(transpose(m), inv);
+			const Vec3 u_vec = truncate(inv.c[0]), v_vec = truncate(inv.c[1]);
+			const Vec3 pos0 = truncate(inv.c[3]) + u_vec * float(p.tex_coord_min[0] >> 4) + v_vec * float(p.tex_coord_min[1] >> 4);
+			const Vec3 n = p.plane.vec / magnitude(p.plane.vec);
+			const Vec3 un = u_vec / magnitude(u_vec), vn = v_vec / magnitude(v_vec);
+			const Room& room_ = rooms[leaf_room[sc.polygon_leaf[pi]]];
+			for (uint32_t y = 0; y < lh; ++y)
+				for (uint32_t x = 0; x < lw; ++x)
+				{
+					const Vec3 tp = pos0 + u_vec * float(x) + v_vec * float(y) + n;
+					float irr[3] = {0, 0, 0}, total[3] = {0, 0, 0};
+					Vec3 dsum = v3(0, 0, 0);
+					float lsum = 0.0f;
+					for (size_t li = 0; li < room_.lights.size(); ++li)
+					{
+						const Vec3 d = room_.lights[li] - tp;
+						const float nd = dot(n, d);
+						if (nd <= 0.0f) continue;
+						const float d2 = std::fmax(magnitude2(d), 1.0f);
+						const float len = std::sqrt(d2);
+						const float cosv = nd / len;
+						const Vec3 c = room_.light_colors[li] / d2;
+						irr[0] += c.x * cosv;
+						irr[1] += c.y * cosv;
+						irr[2] += c.z * cosv;
+						total[0] += c.x;
+						total[1] += c.y;
+						total[2] += c.z;
+						const float lum = (c.x + c.y + c.z) * (1.0f / 3.0f);
+						dsum = dsum + v3(dot(d, un), dot(d, vn), nd) * (lum / len);
+						lsum += lum;
+					}
+					const float ambient = 0.06f;
+					sc.lightmaps.push_back(irr[0] + ambient);
+					sc.lightmaps.push_back(irr[1] + ambient);
+					sc.lightmaps.push_back(irr[2] + ambient);
+					SwDirectionalLightmapElement de;
+					const float dl = magnitude(dsum);
+					const float deviation = lsum > 0.0f ? std::fmin(std::fmax(1.0f - dl / lsum, 0.0f), 1.0f) : 1.0f;
+					for (int k = 0; k < 3; ++k) de.ambient_light[k] = ambient + total[k] * (0.25f + 0.5f * deviation);
+					const Vec3 dir = dl > 0.0f ? dsum * ((1.0f - 0.5f * deviation)) : v3(0, 0, 0.001f);
+					de.light_direction_vector_scaled[0] = dir.x;
+					de.light_direction_vector_scaled[1] = dir.y;
+					de.light_direction_vector_scaled[2] = std::fmax(dir.z, 0.001f);
+					de.directional_light_deviation = deviation;
+					const float mx = std::fmax(std::fmax(total[0], total[1]), std::fmax(total[2], 1e-6f));
+					for (int k = 0; k < 3; ++k) de.directional_light_color[k] = lsum > 0.0f ? total[k] / mx : 1.0f;
+					sc.directional_lightmaps.push_back(de);
+				}
+		}
+		sc.lightmap_elements = offset;
+	}
+
+	// Camera path: a walk through connected rooms, Catmull-Rom through waypoints, resampled by arc length.
+	void build_camera_path()
+	{
+		const float eye = 64.0f;
+		std::vector<Vec3> way;
+		uint32_t cur = rng.below(uint32_t(rooms.size()));
+		uint32_t prev = ~0u;
+		way.push_back(v3(rooms[cur].cx, rooms[cur].cy, eye));
+		for (int step = 0; step < 64; ++step)
+		{
+			const uint32_t i = cur % gx(), j = cur / gx();
+			uint32_t nb[4];
+			int n = 0;
+			if (has_x(i, j)) nb[n++] = cur + 1;
+			if (i > 0 && has_x(i - 1, j)) nb[n++] = cur - 1;
+			if (has_y(i, j)) nb[n++] = cur + gx();
+			if (j > 0 && has_y(i, j - 1)) nb[n++] = cur - gx();
+			if (n == 0) break;
+			// Prefer not to turn straight back.
+			uint32_t cand[4];
+			int m = 0;
+			for (int k = 0; k < n; ++k)
+				if (nb[k] != prev) cand[m++] = nb[k];
+			const uint32_t next = m > 0 ? cand[rng.below(uint32_t(m))] : nb[0];
+			const Room& a = rooms[cur];
+			const Room& b = rooms[next];
+			if (next == cur + 1)
+			{
+				way.push_back(v3(a.x1 - 96, a.cy, eye));
+				way.push_back(v3(a.x1, a.cy, eye));
+				way.push_back(v3(b.x0, a.cy, eye));
+				way.push_back(v3(b.x0 + 96, a.cy, eye));
+			}
+			else if (next + 1 == cur)
+			{
+				way.push_back(v3(a.x0 + 96, a.cy, eye));
+				way.push_back(v3(a.x0, a.cy, eye));
+				way.push_back(v3(b.x1, a.cy, eye));
+				way.push_back(v3(b.x1 - 96, a.cy, eye));
+			}
+			else if (next == cur + gx())
+			{
+				way.push_back(v3(a.cx, a.y1 - 96, eye));
+				way.push_back(v3(a.cx, a.y1, eye));
+				way.push_back(v3(a.cx, b.y0, eye));
+				way.push_back(v3(a.cx, b.y0 + 96, eye));
+			}
+			else
+			{
+				way.push_back(v3(a.cx, a.y0 + 96, eye));
+				way.push_back(v3(a.cx, a.y0, eye));
+				way.push_back(v3(a.cx, b.y1, eye));
+				way.push_back(v3(a.cx, b.y1 - 96, eye));
+			}
+			way.push_back(v3(b.cx + rng.uniform(-64, 64), b.cy + rng.uniform(-64, 64), eye));
+			prev = cur;
+			cur = next;
+		}
+		// Dense Catmull-Rom polyline.
+		std::vector<Vec3> dense;
+		for (size_t k = 0; k + 1 < way.size(); ++k)
+		{
+			const Vec3 p0 = way[k == 0 ? 0 : k - 1], p1 = way[k], p2 = way[k + 1], p3 = way[std::min(k + 2, way.size() - 1)];
+			for (int s = 0; s < 32; ++s)
+			{
+				const float t = s / 32.0f, t2 = t * t, t3 = t2 * t;
+				dense.push_back((p1 * 2.0f + (p2 - p0) * t + (p0 * 2.0f - p1 * 5.0f + p2 * 4.0f - p3) * t2 +
+					(p1 * 3.0f - p0 - p2 * 3.0f + p3) * t3) * 0.5f);
+			}
+		}
+		dense.push_back(way.back());
+		const float speed = 6.0f; // units per frame
+		sc.camera_path.clear();
+		size_t seg = 0;
+		float along = 0.0f;
+		Vec3 pos = dense[0];
+		for (uint32_t f = 0; f < cfg.num_frames; ++f)
+		{
+			// Advance `speed` units along the polyline.
+			float left = f == 0 ? 0.0f : speed;
+			while (left > 0.0f && seg + 1 < dense.size())
+			{
+				const float seg_len = magnitude(dense[seg + 1] - dense[seg]);
+				if (along + left < seg_len)
+				{
+					along += left;
+					left = 0.0f;
+				}
+				else
+				{
+					left -= seg_len - along;
+					along = 0.0f;
+					++seg;
+				}
+			}
+			const size_t s2 = std::min(seg + 1, dense.size() - 1);
+			const float seg_len = std::fmax(magnitude(dense[s2] - dense[seg]), 1e-6f);
+			pos = dense[seg] + (dense[s2] - dense[seg]) * (along / seg_len);
+			const size_t ahead = std::min(seg + 6, dense.size() - 1);
+			Vec3 dir = dense[ahead] - pos;
+			if (magnitude2(dir) < 1e-6f) dir = v3(1, 0, 0);
+			CameraKey k;
+			k.position = pos;
+			k.azimuth = std::atan2(dir.y, dir.x);
+			k.elevation = 0.08f * std::sin(float(f) * 0.07f);
+			sc.camera_path.push_back(k);
+		}
+	}
+};
+
+} // namespace
+
+PolygonBasisVecs form_plane_and_tex_coord_equation(const Plane& plane, const Plane tc[2])
+{
+	// src/square_wheel/surfaces.rs:18-47
+	Mat4 m;
+	m.c[0] = extend(tc[0].vec, tc[0].dist);
+	m.c[1] = extend(tc[1].vec, tc[1].dist);
+	m.c[2] = extend(plane.vec, -plane.dist);
+	m.c[3] = v4(0, 0, 0, 1);
+	Mat4 inv;
+	PolygonBasisVecs b;
+	if (!invert(transpose(m), inv))
+	{
+		b.u = v3(1, 0, 0);
+		b.v = v3(0, 1, 0);
+		b.start = v3(0, 0, 0);
+		b.normal = v3(0, 0, 1);
+		return b;
+	}
+	b.u = truncate(inv.c[0]);
+	b.v = truncate(inv.c[1]);
+	b.start = truncate(inv.c[3]);
+	b.normal = plane.vec / std::fmax(magnitude(plane.vec), 1.0f / float(1 << 30));
+	return b;
+}
+
+void Scene::frame_lights(uint32_t frame, std::vector<SwLight>& out) const
+{
+	out.clear();
+	if (camera_path.empty()) return;
+	for (size_t k = 0; k < dynamic_lights.size(); ++k)
+	{
+		const DynamicLightSpec& d = dynamic_lights[k];
+		const CameraKey& key = camera_path[std::min<size_t>(frame + d.path_offset, camera_path.size() - 1)];
+		const float a = float(frame) * 0.05f + float(k);
+		SwLight l;
+		const Vec3 p = key.position + d.offset + v3(std::cos(a), std::sin(a), 0.0f) * d.orbit_radius;
+		l.position[0] = p.x;
+		l.position[1] = p.y;
+		l.position[2] = p.z;
+		l.radius = d.radius;
+		l.inv_square_radius = 1.0f / (d.radius * d.radius); // renderer_structs.rs:237
+		for (int i = 0; i < 3; ++i) l.color[i] = d.color[i];
+		out.push_back(l);
+	}
+}
+
+SwCreateInfo Scene::create_info(uint32_t device) const
+{
+	SwCreateInfo ci;
+	std::memset(&ci, 0, sizeof(ci));
+	ci.abi_version = SWGPU_ABI_VERSION;
+	ci.device = device;
+	ci.texels = texels.data();
+	ci.num_texels = texels.size();
+	ci.texture_mips = texture_mips.data();
+	ci.num_texture_mips = uint32_t(texture_mips.size());
+	ci.emissive_pixels = emissive_pixels.data();
+	ci.num_emissive_pixels = emissive_pixels.size();
+	ci.emissive_mips = emissive_mips.data();
+	ci.num_emissive_mips = uint32_t(emissive_mips.size());
+	ci.lightmaps = lightmaps.data();
+	ci.num_lightmap_elements = lightmaps.size() / 3;
+	ci.directional_lightmaps = directional_lightmaps.data();
+	ci.num_directional_lightmap_elements = directional_lightmaps.size();
+	return ci;
+}
+
+bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
+{
+	if (cfg.grid_x == 0 || cfg.grid_y == 0 || cfg.grid_x * cfg.grid_y > 4096)
+	{
+		error = "bad grid size";
+		return false;
+	}
+	if (cfg.room_min < 256.0f || cfg.room_max > 1024.0f || cfg.room_min > cfg.room_max)
+	{
+		error = "room edges must lie in [256, 1024]";
+		return false;
+	}
+	if (cfg.tile_size < 16.0f || cfg.tile_size > 256.0f)
+	{
+		error = "tile_size must lie in [16, 256] (lightmaps stay within 17 texels)";
+		return false;
+	}
+	if (cfg.texture_size < 16 || (cfg.texture_size & (cfg.texture_size - 1)) || cfg.num_materials == 0)
+	{
+		error = "texture_size must be a power of two >= 16";
+		return false;
+	}
+	sc = Scene();
+	sc.config = cfg;
+	Rng rng(cfg.seed);
+	Builder b(cfg, sc, rng);
+	b.make_rooms();
+	b.cell_leafs.assign(b.rooms.size(), Builder::CellLeafs());
+	b.build(0, cfg.grid_x, 0, cfg.grid_y);
+	b.link_corridor_halves();
+	sc.polygon_leaf.assign(sc.polygons.size(), 0);
+	for (size_t l = 0; l < sc.leafs.size(); ++l)
+		for (uint32_t p = 0; p < sc.leafs[l].num_polygons; ++p) sc.polygon_leaf[sc.leafs[l].first_polygon + p] = uint32_t(l);
+	b.build_lightmaps();
+
+	// Materials and textures.
+	Rng trng(cfg.seed ^ 0x5EEDu);
+	const uint32_t n_metal = uint32_t(cfg.metal_frac * cfg.num_materials + 0.5f);
+	const uint32_t n_diel = uint32_t(cfg.dielectric_frac * cfg.num_materials + 0.5f);
+	uint32_t n_emissive_tex = 0;
+	for (uint32_t m = 0; m < cfg.num_materials; ++m)
+	{
+		const bool metal = m < n_metal;
+		const bool diel = !metal && m < n_metal + n_diel;
+		make_material_texture(trng, cfg.texture_size, cfg.normal_maps, metal ? 0.35f : diel ? 0.5f : 1.0f, metal, sc);
+		Material mat;
+		if (trng.uniform() < cfg.emissive_frac)
+		{
+			mat.emissive = int32_t(n_emissive_tex++);
+			make_emissive_texture(trng, cfg.texture_size, sc);
+			mat.emissive_light[0] = trng.uniform(0.5f, 2.0f);
+			mat.emissive_light[1] = trng.uniform(0.5f, 2.0f);
+			mat.emissive_light[2] = trng.uniform(0.5f, 2.0f);
+		}
+		sc.materials.push_back(mat);
+	}
+
+	sc.basis.resize(sc.polygons.size());
+	for (size_t p = 0; p < sc.polygons.size(); ++p)
+		sc.basis[p] = form_plane_and_tex_coord_equation(sc.polygons[p].plane, sc.polygons[p].tex_coord_equation);
+
+	b.build_camera_path();
+	for (uint32_t k = 0; k < cfg.num_dynamic_lights; ++k)
+	{
+		DynamicLightSpec d;
+		d.path_offset = 8 + rng.below(48);
+		d.offset = v3(rng.uniform(-24, 24), rng.uniform(-24, 24), rng.uniform(-16, 40));
+		d.orbit_radius = rng.uniform(8, 40);
+		d.radius = rng.uniform(192, 448);
+		const float intensity = rng.uniform(4e4f, 1.2e5f);
+		d.color[0] = intensity * rng.uniform(0.5f, 1.0f);
+		d.color[1] = intensity * rng.uniform(0.5f, 1.0f);
+		d.color[2] = intensity * rng.uniform(0.5f, 1.0f);
+		sc.dynamic_lights.push_back(d);
+	}
+	return true;
+}
+
+} // namespace swhost

@@ -1,0 +1,138 @@
+// Host-side map model and seeded synthetic scene generator.
+//
+// The map model is the subset of BSPMap (src/common/bsp_map_compact.rs:6-75) that world rendering
+// reads: BSP nodes (last node is the root, children >= FIRST_LEAF_INDEX are leafs), leafs with their
+// polygons and portals, polygons with plane, texture-coordinate equations, integer tc bounds and
+// lightmap offset, portals, vertices, simple and directional lightmaps.
+//
+// The reference's map compiler and lightmapper (Rust executables) cannot run here and no compiled maps
+// ship with it, so scenes are generated: a grid of axis-aligned box rooms (edges uniform in
+// [room_min, room_max]) joined by 128x128 corridors, one convex BSP leaf per room and per corridor half,
+// portals at the room walls and at the cell boundaries, faces cut around the corridor openings and
+// tiled (tile_size) so every lightmap stays within the reference's size limit; lightmaps are lit by
+// seeded point lights per room with a direct-light model; textures are procedural (value noise +
+// checker, height-field normal maps) with full mip chains built as build_texture_mip does.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/swgpu.h"
+#include "hmath.h"
+
+namespace swhost
+{
+
+constexpr uint32_t FIRST_LEAF_INDEX = 1u << 31;
+constexpr uint32_t LIGHTMAP_SCALE_LOG2 = 4;
+constexpr uint32_t LIGHTMAP_SCALE = 1u << LIGHTMAP_SCALE_LOG2;
+constexpr uint32_t NUM_MIPS = 5;
+
+struct BspNode
+{
+	uint32_t children[2];
+	Plane plane;
+};
+struct BspLeaf
+{
+	uint32_t first_polygon, num_polygons, first_leaf_portal, num_leaf_portals;
+};
+struct MapPolygon
+{
+	uint32_t first_vertex, num_vertices;
+	Plane plane;
+	Plane tex_coord_equation[2];
+	int32_t tex_coord_min[2], tex_coord_max[2];
+	uint32_t lightmap_data_offset;
+	uint32_t texture; // material index
+};
+struct MapPortal
+{
+	uint32_t leafs[2];
+	Plane plane;
+	uint32_t first_vertex, num_vertices;
+};
+
+// Material flags the renderer reads (src/common/material.rs): draw, light, diffuse layer, blending,
+// optional emissive layer.
+struct Material
+{
+	bool draw = true;
+	bool light = true;
+	bool has_diffuse = true;
+	uint32_t blending_mode = SW_BLEND_NONE;
+	int32_t emissive = -1; // emissive texture index or -1
+	float emissive_light[3] = {1.0f, 1.0f, 1.0f};
+};
+
+// PolygonBasisVecs, src/square_wheel/surfaces.rs:6-64
+struct PolygonBasisVecs
+{
+	Vec3 u, v, start, normal;
+};
+
+struct DynamicLightSpec
+{
+	uint32_t path_offset; // frames ahead of the camera on its path
+	Vec3 offset;          // displacement from the path point
+	float orbit_radius;
+	float radius;
+	float color[3];
+};
+
+struct CameraKey
+{
+	Vec3 position;
+	float azimuth, elevation;
+};
+
+struct SceneConfig
+{
+	uint64_t seed = 1;
+	uint32_t grid_x = 4, grid_y = 2;
+	float room_min = 256.0f, room_max = 1024.0f;
+	float tile_size = 128.0f;
+	uint32_t texture_size = 128;
+	uint32_t num_materials = 16;
+	float metal_frac = 0.0f, dielectric_frac = 0.0f;
+	bool normal_maps = false;
+	bool directional_lightmaps = false;
+	uint32_t lights_per_room = 1;
+	uint32_t num_dynamic_lights = 0;
+	uint32_t num_frames = 64;
+	float emissive_frac = 0.0f;
+};
+
+struct Scene
+{
+	SceneConfig config;
+	std::vector<BspNode> nodes;
+	std::vector<BspLeaf> leafs;
+	std::vector<MapPolygon> polygons;
+	std::vector<MapPortal> portals;
+	std::vector<uint32_t> leafs_portals;
+	std::vector<Vec3> vertices;
+	std::vector<float> lightmaps; // [f32; 3] elements, element 0 unused
+	std::vector<SwDirectionalLightmapElement> directional_lightmaps;
+	std::vector<Material> materials;
+	std::vector<uint64_t> texels; // TextureElement raw values of all materials' mips
+	std::vector<SwTextureMip> texture_mips; // material * NUM_MIPS + mip
+	std::vector<uint32_t> emissive_pixels;
+	std::vector<SwEmissiveMip> emissive_mips; // emissive * NUM_MIPS + mip
+	std::vector<PolygonBasisVecs> basis;      // per polygon, precomputed at load (partial_renderer.rs:63-78)
+	std::vector<uint32_t> polygon_leaf;       // leaf of each polygon
+	std::vector<CameraKey> camera_path;       // one key per frame
+	std::vector<DynamicLightSpec> dynamic_lights;
+	uint64_t lightmap_elements = 0;
+
+	uint32_t root_node() const { return nodes.empty() ? FIRST_LEAF_INDEX : uint32_t(nodes.size() - 1); }
+	void frame_lights(uint32_t frame, std::vector<SwLight>& out) const;
+	SwCreateInfo create_info(uint32_t device) const;
+};
+
+bool generate_scene(const SceneConfig& cfg, Scene& out, std::string& error);
+
+PolygonBasisVecs form_plane_and_tex_coord_equation(const Plane& plane, const Plane tc[2]);
+
+} // namespace swhost

@@ -1,0 +1,233 @@
+// C ABI of the host library (include/swhost.h).
+#include "../../include/swhost.h"
+
+#include <new>
+#include <string>
+
+#include "frame.h"
+#include "scene.h"
+
+using namespace swhost;
+
+struct SwhScene
+{
+	Scene scene;
+};
+struct SwhFrame
+{
+	explicit SwhFrame(const Scene& s) : prep(s) {}
+	FramePrep prep;
+};
+struct SwhRenderer
+{
+	const SwhScene* scene = nullptr;
+	SwCtx* ctx = nullptr;
+	SwhFrame* frame = nullptr;
+};
+
+namespace
+{
+thread_local std::string g_error;
+
+FrameOptions to_options(const SwhFrameOptions* o)
+{
+	FrameOptions f;
+	f.width = o->width;
+	f.height = o->height;
+	f.pixel_format = o->pixel_format;
+	f.use_directional_lightmaps = o->use_directional_lightmaps != 0;
+	f.clear_background = o->clear_background != 0;
+	if (o->fov > 0.0f) f.fov = o->fov;
+	f.mip_bias = o->mip_bias;
+	return f;
+}
+
+bool valid_options(const SwhFrameOptions* o)
+{
+	return o && o->width > 0 && o->height > 0 && o->width <= 16384 && o->height <= 16384 && o->pixel_format <= SW_PIXEL_C64;
+}
+} // namespace
+
+extern "C" {
+
+const char* swh_last_error(void) { return g_error.c_str(); }
+
+int swh_scene_create(const SwhSceneConfig* c, SwhScene** out)
+{
+	if (!c || !out) return SW_ERR_INVALID_ARGUMENT;
+	*out = nullptr;
+	SceneConfig cfg;
+	cfg.seed = c->seed;
+	cfg.grid_x = c->grid_x;
+	cfg.grid_y = c->grid_y;
+	cfg.room_min = c->room_min;
+	cfg.room_max = c->room_max;
+	cfg.tile_size = c->tile_size;
+	cfg.texture_size = c->texture_size;
+	cfg.num_materials = c->num_materials;
+	cfg.metal_frac = c->metal_frac;
+	cfg.dielectric_frac = c->dielectric_frac;
+	cfg.normal_maps = c->normal_maps != 0;
+	cfg.directional_lightmaps = c->directional_lightmaps != 0;
+	cfg.lights_per_room = c->lights_per_room;
+	cfg.num_dynamic_lights = c->num_dynamic_lights;
+	cfg.num_frames = c->num_frames ? c->num_frames : 1;
+	cfg.emissive_frac = c->emissive_frac;
+	SwhScene* s = new (std::nothrow) SwhScene();
+	if (!s) return SW_ERR_OUT_OF_MEMORY;
+	try
+	{
+		if (!generate_scene(cfg, s->scene, g_error))
+		{
+			delete s;
+			return SW_ERR_INVALID_ARGUMENT;
+		}
+	}
+	catch (const std::bad_alloc&)
+	{
+		delete s;
+		g_error = "out of host memory";
+		return SW_ERR_OUT_OF_MEMORY;
+	}
+	*out = s;
+	return SW_OK;
+}
+
+int swh_scene_destroy(SwhScene* s)
+{
+	if (!s) return SW_ERR_INVALID_ARGUMENT;
+	delete s;
+	return SW_OK;
+}
+
+int swh_scene_info(const SwhScene* s, SwhSceneInfo* out)
+{
+	if (!s || !out) return SW_ERR_INVALID_ARGUMENT;
+	const Scene& sc = s->scene;
+	out->nodes = uint32_t(sc.nodes.size());
+	out->leafs = uint32_t(sc.leafs.size());
+	out->polygons = uint32_t(sc.polygons.size());
+	out->portals = uint32_t(sc.portals.size());
+	out->materials = uint32_t(sc.materials.size());
+	out->frames = uint32_t(sc.camera_path.size());
+	out->dynamic_lights = uint32_t(sc.dynamic_lights.size());
+	out->reserved = 0;
+	out->lightmap_elements = sc.lightmap_elements;
+	out->texels = sc.texels.size();
+	return SW_OK;
+}
+
+int swh_scene_create_info(const SwhScene* s, uint32_t device, SwCreateInfo* out)
+{
+	if (!s || !out) return SW_ERR_INVALID_ARGUMENT;
+	*out = s->scene.create_info(device);
+	return SW_OK;
+}
+
+int swh_frame_create(const SwhScene* s, SwhFrame** out)
+{
+	if (!s || !out) return SW_ERR_INVALID_ARGUMENT;
+	*out = new (std::nothrow) SwhFrame(s->scene);
+	return *out ? SW_OK : SW_ERR_OUT_OF_MEMORY;
+}
+
+int swh_frame_destroy(SwhFrame* f)
+{
+	if (!f) return SW_ERR_INVALID_ARGUMENT;
+	delete f;
+	return SW_OK;
+}
+
+int swh_frame_prepare(SwhFrame* f, uint32_t frame_index, const SwhFrameOptions* o)
+{
+	if (!f || !valid_options(o)) return SW_ERR_INVALID_ARGUMENT;
+	try
+	{
+		f->prep.prepare(frame_index, to_options(o));
+	}
+	catch (const std::bad_alloc&)
+	{
+		g_error = "out of host memory";
+		return SW_ERR_OUT_OF_MEMORY;
+	}
+	return SW_OK;
+}
+
+int swh_frame_outputs(const SwhFrame* f, SwhFrameOutputs* out)
+{
+	if (!f || !out) return SW_ERR_INVALID_ARGUMENT;
+	const FramePrep& p = f->prep;
+	out->surfaces = p.surfaces.data();
+	out->num_surfaces = uint32_t(p.surfaces.size());
+	out->total_texels = p.total_texels;
+	out->draws = p.draws.data();
+	out->num_draws = uint32_t(p.draws.size());
+	out->vertices = p.vertices.data();
+	out->num_vertices = uint32_t(p.vertices.size());
+	out->lights = p.lights.data();
+	out->num_lights = uint32_t(p.lights.size());
+	out->params = p.params;
+	out->visible_leafs = p.stats.visible_leafs;
+	out->camera_leaf = p.stats.camera_leaf;
+	return SW_OK;
+}
+
+int swh_renderer_create(const SwhScene* s, uint32_t device, SwhRenderer** out)
+{
+	if (!s || !out) return SW_ERR_INVALID_ARGUMENT;
+	*out = nullptr;
+	SwhRenderer* r = new (std::nothrow) SwhRenderer();
+	if (!r) return SW_ERR_OUT_OF_MEMORY;
+	r->scene = s;
+	SwCreateInfo ci = s->scene.create_info(device);
+	int st = sw_create(&ci, &r->ctx);
+	if (st != SW_OK)
+	{
+		g_error = "sw_create failed";
+		delete r;
+		return st;
+	}
+	r->frame = new (std::nothrow) SwhFrame(s->scene);
+	if (!r->frame)
+	{
+		sw_destroy(r->ctx);
+		delete r;
+		return SW_ERR_OUT_OF_MEMORY;
+	}
+	*out = r;
+	return SW_OK;
+}
+
+int swh_renderer_destroy(SwhRenderer* r)
+{
+	if (!r) return SW_ERR_INVALID_ARGUMENT;
+	if (r->ctx) sw_destroy(r->ctx);
+	delete r->frame;
+	delete r;
+	return SW_OK;
+}
+
+int swh_renderer_prepare_frame(SwhRenderer* r, uint32_t frame_index, const SwhFrameOptions* o)
+{
+	if (!r) return SW_ERR_INVALID_ARGUMENT;
+	int st = swh_frame_prepare(r->frame, frame_index, o);
+	if (st) return st;
+	const FramePrep& p = r->frame->prep;
+	st = sw_frame_begin(r->ctx, &p.params, p.lights.data(), uint32_t(p.lights.size()));
+	if (st) return st;
+	return sw_submit_surfaces(r->ctx, p.surfaces.data(), uint32_t(p.surfaces.size()), p.total_texels);
+}
+
+int swh_renderer_draw_frame(SwhRenderer* r, void* dst, uint32_t pitch, int dst_is_device)
+{
+	if (!r) return SW_ERR_INVALID_ARGUMENT;
+	const FramePrep& p = r->frame->prep;
+	int st = sw_submit_draws(r->ctx, p.draws.data(), uint32_t(p.draws.size()), p.vertices.data(), uint32_t(p.vertices.size()));
+	if (st) return st;
+	return sw_render(r->ctx, dst, pitch, dst_is_device);
+}
+
+SwCtx* swh_renderer_context(SwhRenderer* r) { return r ? r->ctx : nullptr; }
+SwhFrame* swh_renderer_frame(SwhRenderer* r) { return r ? r->frame : nullptr; }
+
+} // extern "C"

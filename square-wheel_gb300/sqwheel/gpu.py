@@ -22,7 +22,7 @@ EXPORTED = [
     "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_set_surfaces",
     "sw_submit_draws",
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_get_exposure", "sw_set_exposure",
-    "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout",
+    "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
 ]
 
 _lib = None
@@ -61,6 +61,8 @@ def load_library(path=LIB_PATH):
         "sw_get_stats": ([vp, vp], i32),
         "sw_get_stream": ([vp, ctypes.POINTER(vp)], i32),
         "sw_abi_layout": ([ctypes.POINTER(u32), u32], i32),
+        "sw_enable_timing": ([vp, i32], i32),
+        "sw_get_timings": ([vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -233,6 +235,15 @@ class GpuRenderer:
         s = abi.Stats()
         self._check(self.lib.sw_get_stats(self.ctx, ctypes.byref(s)), "sw_get_stats")
         return s
+
+    def enable_timing(self, on=True):
+        self._check(self.lib.sw_enable_timing(self.ctx, 1 if on else 0), "sw_enable_timing")
+
+    def timings(self):
+        """Device ms of the last surface build, raster, postprocess, upscale."""
+        t = (ctypes.c_float * 4)()
+        self._check(self.lib.sw_get_timings(self.ctx, t), "sw_get_timings")
+        return list(t)
 
     def sync(self):
         self._check(self.lib.sw_sync(self.ctx), "sw_sync")

@@ -1,0 +1,229 @@
+"""Python binding of the host library (libswhost.so, C ABI in include/swhost.h): synthetic scenes and the
+per-frame host work (visibility, surface preparation, draw setup) that produces the GPU path's inputs."""
+import ctypes
+import os
+
+import numpy as np
+
+from . import abi
+from .gpu import PKG_DIR, SwError, load_library
+
+HOST_LIB_PATH = os.path.join(PKG_DIR, "lib", "libswhost.so")
+_lib = None
+
+
+class SceneConfig(ctypes.Structure):
+    _fields_ = [
+        ("seed", ctypes.c_uint64), ("grid_x", ctypes.c_uint32), ("grid_y", ctypes.c_uint32),
+        ("room_min", ctypes.c_float), ("room_max", ctypes.c_float), ("tile_size", ctypes.c_float),
+        ("texture_size", ctypes.c_uint32), ("num_materials", ctypes.c_uint32),
+        ("metal_frac", ctypes.c_float), ("dielectric_frac", ctypes.c_float),
+        ("normal_maps", ctypes.c_uint32), ("directional_lightmaps", ctypes.c_uint32),
+        ("lights_per_room", ctypes.c_uint32), ("num_dynamic_lights", ctypes.c_uint32),
+        ("num_frames", ctypes.c_uint32), ("emissive_frac", ctypes.c_float),
+    ]
+
+
+class SceneInfo(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_uint32), ("leafs", ctypes.c_uint32), ("polygons", ctypes.c_uint32),
+                ("portals", ctypes.c_uint32), ("materials", ctypes.c_uint32), ("frames", ctypes.c_uint32),
+                ("dynamic_lights", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("lightmap_elements", ctypes.c_uint64), ("texels", ctypes.c_uint64)]
+
+
+class FrameOptions(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("pixel_format", ctypes.c_uint32),
+                ("use_directional_lightmaps", ctypes.c_uint32), ("clear_background", ctypes.c_uint32),
+                ("fov", ctypes.c_float), ("mip_bias", ctypes.c_float)]
+
+
+class FrameOutputs(ctypes.Structure):
+    _fields_ = [("surfaces", ctypes.c_void_p), ("num_surfaces", ctypes.c_uint32), ("num_draws", ctypes.c_uint32),
+                ("total_texels", ctypes.c_uint64), ("draws", ctypes.c_void_p), ("vertices", ctypes.c_void_p),
+                ("num_vertices", ctypes.c_uint32), ("num_lights", ctypes.c_uint32), ("lights", ctypes.c_void_p),
+                ("params", abi.FrameParams), ("visible_leafs", ctypes.c_uint32), ("camera_leaf", ctypes.c_uint32)]
+
+
+def load_host_library():
+    global _lib
+    if _lib is not None:
+        return _lib
+    load_library()  # libswgpu.so first (dependency)
+    if not os.path.exists(HOST_LIB_PATH):
+        raise SwError(f"{HOST_LIB_PATH} is missing: build it with `python square-wheel_gb300/build.py`")
+    lib = ctypes.CDLL(HOST_LIB_PATH)
+    vp, u32, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
+    sig = {
+        "swh_scene_create": ([vp, ctypes.POINTER(vp)], i32), "swh_scene_destroy": ([vp], i32),
+        "swh_scene_info": ([vp, vp], i32), "swh_scene_create_info": ([vp, u32, vp], i32),
+        "swh_last_error": ([], ctypes.c_char_p), "swh_frame_create": ([vp, ctypes.POINTER(vp)], i32),
+        "swh_frame_destroy": ([vp], i32), "swh_frame_prepare": ([vp, u32, vp], i32),
+        "swh_frame_outputs": ([vp, vp], i32), "swh_renderer_create": ([vp, u32, ctypes.POINTER(vp)], i32),
+        "swh_renderer_destroy": ([vp], i32), "swh_renderer_prepare_frame": ([vp, u32, vp], i32),
+        "swh_renderer_draw_frame": ([vp, vp, u32, i32], i32), "swh_renderer_context": ([vp], vp),
+        "swh_renderer_frame": ([vp], vp),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+HOST_EXPORTED = ["swh_scene_create", "swh_scene_destroy", "swh_scene_info", "swh_scene_create_info", "swh_last_error",
+                 "swh_frame_create", "swh_frame_destroy", "swh_frame_prepare", "swh_frame_outputs",
+                 "swh_renderer_create", "swh_renderer_destroy", "swh_renderer_prepare_frame",
+                 "swh_renderer_draw_frame", "swh_renderer_context", "swh_renderer_frame"]
+
+# The two map configurations of the benchmark plan.
+SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, num_materials=16, metal_frac=0.0,
+                 dielectric_frac=0.0, normal_maps=0, directional_lightmaps=0, lights_per_room=1,
+                 num_dynamic_lights=0, num_frames=64)
+FULL_MAP = dict(seed=2, grid_x=8, grid_y=8, tile_size=80.0, texture_size=256, num_materials=32, metal_frac=0.25,
+                dielectric_frac=0.25, normal_maps=1, directional_lightmaps=1, lights_per_room=2,
+                num_dynamic_lights=8, num_frames=256)
+
+
+def _check(lib, r, what):
+    if r != 0:
+        msg = lib.swh_last_error()
+        raise SwError(f"{what} failed ({r}): {msg.decode() if msg else ''}")
+
+
+class Scene:
+    def __init__(self, **kw):
+        self.lib = load_host_library()
+        c = SceneConfig(seed=1, grid_x=4, grid_y=2, room_min=256.0, room_max=1024.0, tile_size=128.0, texture_size=128,
+                        num_materials=16, metal_frac=0.0, dielectric_frac=0.0, normal_maps=0, directional_lightmaps=0,
+                        lights_per_room=1, num_dynamic_lights=0, num_frames=64, emissive_frac=0.0)
+        for k, v in kw.items():
+            setattr(c, k, v)
+        self.config = c
+        self.handle = ctypes.c_void_p()
+        _check(self.lib, self.lib.swh_scene_create(ctypes.byref(c), ctypes.byref(self.handle)), "swh_scene_create")
+
+    def info(self):
+        i = SceneInfo()
+        _check(self.lib, self.lib.swh_scene_info(self.handle, ctypes.byref(i)), "swh_scene_info")
+        return i
+
+    def create_info(self, device=0):
+        ci = abi.CreateInfo()
+        _check(self.lib, self.lib.swh_scene_create_info(self.handle, device, ctypes.byref(ci)), "swh_scene_create_info")
+        return ci
+
+    def static_data(self):
+        """numpy copies of the static data (for the oracle and GpuRenderer)."""
+        from .gpu import StaticData
+        ci = self.create_info()
+
+        def arr(p, n, dt):
+            if not p or n == 0:
+                return np.zeros(0, dt)
+            return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)),
+                                         shape=(int(n) * np.dtype(dt).itemsize,)).view(dt).copy()
+        return StaticData(arr(ci.texels, ci.num_texels, np.uint64), arr(ci.texture_mips, ci.num_texture_mips, abi.TEXTURE_MIP),
+                          arr(ci.emissive_pixels, ci.num_emissive_pixels, np.uint32),
+                          arr(ci.emissive_mips, ci.num_emissive_mips, abi.EMISSIVE_MIP),
+                          arr(ci.lightmaps, ci.num_lightmap_elements * 3, np.float32),
+                          arr(ci.directional_lightmaps, ci.num_directional_lightmap_elements, abi.DIR_LIGHTMAP_ELEMENT))
+
+    def close(self):
+        if self.handle:
+            self.lib.swh_scene_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def frame_options(width, height, pixel_format, directional=True, clear_background=False, fov=0.0, mip_bias=0.0):
+    return FrameOptions(width, height, pixel_format, 1 if directional else 0, 1 if clear_background else 0, fov, mip_bias)
+
+
+class Frame:
+    """Per-frame host work; outputs are copied into numpy arrays."""
+
+    def __init__(self, scene):
+        self.scene = scene
+        self.lib = scene.lib
+        self.handle = ctypes.c_void_p()
+        _check(self.lib, self.lib.swh_frame_create(scene.handle, ctypes.byref(self.handle)), "swh_frame_create")
+
+    def prepare(self, frame_index, options):
+        _check(self.lib, self.lib.swh_frame_prepare(self.handle, frame_index, ctypes.byref(options)), "swh_frame_prepare")
+        o = FrameOutputs()
+        _check(self.lib, self.lib.swh_frame_outputs(self.handle, ctypes.byref(o)), "swh_frame_outputs")
+
+        def arr(p, n, dt):
+            if not p or n == 0:
+                return np.zeros(0, dt)
+            return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)),
+                                         shape=(int(n) * np.dtype(dt).itemsize,)).view(dt).copy()
+        self.surfaces = arr(o.surfaces, o.num_surfaces, abi.SURFACE_DESC)
+        self.draws = arr(o.draws, o.num_draws, abi.DRAW_CMD)
+        self.vertices = arr(o.vertices, o.num_vertices, abi.VERTEX16)
+        self.lights = arr(o.lights, o.num_lights, abi.LIGHT)
+        self.total_texels = int(o.total_texels)
+        self.params = abi.FrameParams()
+        ctypes.pointer(self.params)[0] = o.params
+        self.visible_leafs = int(o.visible_leafs)
+        self.camera_leaf = int(o.camera_leaf)
+        return self
+
+    def close(self):
+        if self.handle:
+            self.lib.swh_frame_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class HostRenderer:
+    """Renderer API mirror driving the GPU library from C++ (swh_renderer_*)."""
+
+    def __init__(self, scene, device=0):
+        self.scene = scene
+        self.lib = scene.lib
+        self.handle = ctypes.c_void_p()
+        _check(self.lib, self.lib.swh_renderer_create(scene.handle, device, ctypes.byref(self.handle)), "swh_renderer_create")
+
+    def _err(self, r, what):
+        if r != 0:
+            glib = load_library()
+            ctx = self.lib.swh_renderer_context(self.handle)
+            msg = glib.sw_last_error(ctx) if ctx else b""
+            raise SwError(f"{what} failed ({r}): {msg.decode() if msg else ''}")
+
+    def prepare_frame(self, frame_index, options):
+        self._err(self.lib.swh_renderer_prepare_frame(self.handle, frame_index, ctypes.byref(options)), "prepare_frame")
+
+    def draw_frame(self, out=None, device_ptr=None, pitch=None):
+        if out is not None:
+            self._err(self.lib.swh_renderer_draw_frame(self.handle, abi.ptr(out), pitch or out.shape[1], 0), "draw_frame")
+        elif device_ptr is not None:
+            self._err(self.lib.swh_renderer_draw_frame(self.handle, ctypes.c_void_p(device_ptr), pitch, 1), "draw_frame")
+        else:
+            self._err(self.lib.swh_renderer_draw_frame(self.handle, None, 0, 0), "draw_frame")
+
+    def context(self):
+        return self.lib.swh_renderer_context(self.handle)
+
+    def close(self):
+        if self.handle:
+            self.lib.swh_renderer_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -15,6 +15,8 @@ def render_both(arena, draws, verts, w, h, fmt, clear=False, init=None):
     fp = gpu.frame_params(w, h, fmt, (0, 0, 0), clear_background=clear)
     dt = np.uint64 if fmt == abi.SW_PIXEL_C64 else np.uint32
     want = np.zeros((h, w), dt) if init is None else init.copy()
+    if clear:
+        oracle.clear_background(fp, want)
     bad = oracle.rasterize(draws, verts, arena, fp, want)
     st = synth.BatchedSurfaces(seed=1, count=1, max_side=8)
     r = gpu.GpuRenderer(st.static_data())
