@@ -253,6 +253,23 @@ int sw_render(SwCtx* ctx, void* dst, uint32_t pitch, int dst_is_device);
 int sw_postprocess(SwCtx* ctx, const SwPostConfig* config, float frame_duration_s, const float color_modulate[3],
 	void* dst, uint32_t pitch, int dst_is_device);
 
+/* No counterpart in the reference. The postprocessor for callers that cannot allocate device memory
+ * (engines that hand out all device memory from their own fixed pools, frame loops that cannot afford
+ * cudaMalloc's implicit device synchronisation): no context, no allocation. hdr (width x height
+ * Color64, tightly packed), dst (Color32, pitch in pixels) and average (4 floats, lanes b, g, r, a; may
+ * be NULL) are device pointers; config and color_modulate are host memory; stream is a cudaStream_t
+ * (NULL = default stream). The bloom buffers and per-line sums live in one static device array of
+ * SW_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit, so frames are limited
+ * to SW_NOALLOC_MAX_WIDTH x SW_NOALLOC_MAX_HEIGHT (SW_ERR_LIMIT beyond). The first call on a device
+ * (with that device current) looks the array's address up once; make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race. The exposure is an input; the frame's
+ * average colour (postprocessor.rs:206-223 feeds it to update_exposure) is written to `average`. */
+#define SW_NOALLOC_MAX_WIDTH 1920u
+#define SW_NOALLOC_MAX_HEIGHT 1080u
+#define SW_NOALLOC_SCRATCH_BYTES 8320512u
+int sw_postprocess_noalloc(const uint64_t* hdr, uint32_t width, uint32_t height, const SwPostConfig* config,
+	float exposure, const float color_modulate[3], uint32_t* dst, uint32_t pitch, float* average, void* stream);
+
 /* FrameUpscaler::perform_upscale (src/square_wheel/frame_upscaler.rs:42-70): src is a Color32 frame of
  * (dst_width/scale) x (dst_height/scale) pixels with pitch = its width; dst has dst_pitch pixels per row. */
 int sw_upscale(SwCtx* ctx, uint32_t mode, uint32_t scale, const void* src, int src_is_device, void* dst,

@@ -23,6 +23,7 @@ EXPORTED = [
     "sw_submit_draws",
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
+    "sw_postprocess_noalloc",
 ]
 
 _lib = None
@@ -61,6 +62,7 @@ def load_library(path=LIB_PATH):
         "sw_get_stats": ([vp, vp], i32),
         "sw_get_stream": ([vp, ctypes.POINTER(vp)], i32),
         "sw_abi_layout": ([ctypes.POINTER(u32), u32], i32),
+        "sw_postprocess_noalloc": ([vp, u32, u32, vp, f32, vp, vp, u32, vp, vp], i32),
         "sw_enable_timing": ([vp, i32], i32),
         "sw_get_timings": ([vp, vp], i32),
     }
