@@ -164,6 +164,7 @@ def run_frame_gpu(args, world, rank, local):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     ldr = torch.empty((H, W), dtype=torch.int32, device=f"cuda:{local}")
     totals = {"surf": 0.0, "raster": 0.0, "post": 0.0}
+    frame_span = 0.0
     texels = 0
     surf_bytes = 0
     pix_before = r.stats().pixel_writes
@@ -187,6 +188,7 @@ def run_frame_gpu(args, world, rank, local):
                 totals["surf"] += t[0]
                 totals["raster"] += t[1]
                 totals["post"] += t[2]
+                frame_span += t[4]
                 texels += f["total_texels"]
                 surf_bytes += work.surface_bytes(f)
                 launches += 1 + 2 + 5
@@ -255,6 +257,7 @@ def run_frame_gpu(args, world, rank, local):
                        "mean_host_prep_ms": round(statistics.mean(work.prep_ms), 3),
                        "l2": "flushed (512 MiB write) before every timed step",
                        "timing": "sum of per-stage CUDA-event device times (surfaces, raster, postprocess)",
+                       "frame_span_ms": round(frame_span / s, 4),
                        "learned_upscale": "not in this measurement", "parallelism": f"replicas x{world}"},
             "stages": stages,
             "roofline": {"bound": "hbm", "kernel": kernel_names[dom], "achieved": stages[dom]["GB/s"], "peak": peak,

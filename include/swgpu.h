@@ -290,10 +290,13 @@ typedef struct SwStats {
 int sw_get_stats(SwCtx* ctx, SwStats* out_stats);
 
 /* Device-time measurement of the last call of each stage (CUDA events on the context's stream around
- * the stage's kernels only): [0] surface build, [1] rasterisation, [2] postprocess, [3] upscale, in ms.
- * Timing is off by default; sw_enable_timing(ctx, 1) turns it on. sw_get_timings synchronises. */
+ * the stage's kernels only): [0] surface build, [1] rasterisation, [2] postprocess, [3] upscale, and
+ * [4] the whole frame from sw_frame_begin to the end of sw_postprocess (both internal streams joined,
+ * uploads and any idle time waiting for the host included), in ms. A stage not run since timing was
+ * enabled reads 0. Timing is off by default; sw_enable_timing(ctx, 1) turns it on. sw_get_timings
+ * synchronises. */
 int sw_enable_timing(SwCtx* ctx, int enable);
-int sw_get_timings(SwCtx* ctx, float out_ms[4]);
+int sw_get_timings(SwCtx* ctx, float out_ms[5]);
 
 /* The context's CUDA stream (cudaStream_t) for callers that order their own work after the frame. */
 int sw_get_stream(SwCtx* ctx, void** out_stream);

@@ -18,9 +18,14 @@ namespace
 
 __device__ __forceinline__ CV tonemap(CV c, const PostArgs& a)
 {
-	// TonemappingFunction::do_it: c / (c * inv_255 + inv_scale), unfused (postprocessor.rs:1019-1023)
+	// TonemappingFunction::do_it: c / (c * inv_255 + inv_scale), unfused (postprocessor.rs:1019-1023).
+	// The alpha lane of both vectors is 0 (from_color_f32x3), so for the non-negative alpha sums here it
+	// divides by +0: +inf or NaN, which the Color32 conversion's min(255) turns into 255 either way.
+	const float alpha = (a.inv_255[3] == 0.0f && a.inv_scale[3] == 0.0f)
+		? 255.0f
+		: __fdiv_rn(c.a, mad2(c.a, a.inv_255[3], a.inv_scale[3]));
 	return CV{__fdiv_rn(c.b, mad2(c.b, a.inv_255[0], a.inv_scale[0])), __fdiv_rn(c.g, mad2(c.g, a.inv_255[1], a.inv_scale[1])),
-		__fdiv_rn(c.r, mad2(c.r, a.inv_255[2], a.inv_scale[2])), __fdiv_rn(c.a, mad2(c.a, a.inv_255[3], a.inv_scale[3]))};
+		__fdiv_rn(c.r, mad2(c.r, a.inv_255[2], a.inv_scale[2])), alpha};
 }
 
 // downscale_hdr_buffer::<S>, postprocessor.rs:792-844: one thread per bloom pixel.
@@ -37,11 +42,24 @@ __global__ void __launch_bounds__(256) pp_downscale_kernel(PostArgs a)
 		for (uint32_t dy = 0; dy < S; ++dy)
 		{
 			const uint64_t* row = a.hdr + uint64_t(by * S + dy) * a.width + bx * S;
-			for (uint32_t dx = 0; dx < S; ++dx)
+			for (uint32_t dx = 0; dx < S; dx += 2)
 			{
-				const CI c = ci_from_c64(__ldg(reinterpret_cast<const unsigned long long*>(row) + dx));
+				// Pairs of pixels; one 16-byte load when the pair is aligned (even row start).
+				unsigned long long q0, q1;
+				if ((reinterpret_cast<uintptr_t>(row + dx) & 15) == 0)
+				{
+					const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(row + dx));
+					q0 = v.x;
+					q1 = v.y;
+				}
+				else
+				{
+					q0 = __ldg(reinterpret_cast<const unsigned long long*>(row) + dx);
+					q1 = __ldg(reinterpret_cast<const unsigned long long*>(row) + dx + 1);
+				}
+				const CI c0 = ci_from_c64(q0), c1 = ci_from_c64(q1);
 #pragma unroll
-				for (int i = 0; i < 4; ++i) sum[i] = wadd(sum[i], c.v[i]);
+				for (int i = 0; i < 4; ++i) sum[i] = wadd(wadd(sum[i], c0.v[i]), c1.v[i]);
 			}
 		}
 		const int32_t scaler = 256 / int32_t(S * S);
@@ -59,17 +77,32 @@ __global__ void __launch_bounds__(256) pp_downscale_kernel(PostArgs a)
 	}
 }
 
-// Average colour: f32 sum of the line sums in line order, then scale (postprocessor.rs:835-843).
-__global__ void pp_average_bloom_kernel(PostArgs a)
+// Sequential f32 sum over `n` lines of 4-lane values, in line order, as the reference's loop does; the
+// block stages chunks of lines in shared memory with coalesced loads and threads 0..3 (one per lane)
+// run the ordered additions from shared memory.
+template <class LoadT>
+__device__ __forceinline__ void ordered_line_sum(uint32_t n, LoadT load, float inv, float* out)
 {
-	if (threadIdx.x != 0 || blockIdx.x != 0) return;
-	float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-	for (uint32_t y = 0; y < a.bh; ++y)
-#pragma unroll
-		for (int i = 0; i < 4; ++i) s[i] = fadd(s[i], float(a.line_sums[y * 4 + i]));
-	const float inv = __fdiv_rn(1.0f, float(a.bw * a.bh));
-#pragma unroll
-	for (int i = 0; i < 4; ++i) a.average[i] = fmul(s[i], inv);
+	constexpr uint32_t CHUNK = 2048;
+	__shared__ float s_lines[CHUNK * 4];
+	float acc = 0.0f;
+	for (uint32_t base = 0; base < n; base += CHUNK)
+	{
+		const uint32_t m = min(CHUNK, n - base);
+		for (uint32_t i = threadIdx.x; i < m * 4; i += blockDim.x) s_lines[i] = load(base * 4 + i);
+		__syncthreads();
+		if (threadIdx.x < 4)
+			for (uint32_t y = 0; y < m; ++y) acc = fadd(acc, s_lines[y * 4 + threadIdx.x]);
+		__syncthreads();
+	}
+	if (threadIdx.x < 4) out[threadIdx.x] = fmul(acc, inv);
+}
+
+// Average colour: f32 sum of the line sums in line order, then scale (postprocessor.rs:835-843).
+__global__ void __launch_bounds__(256) pp_average_bloom_kernel(PostArgs a)
+{
+	const int32_t* sums = a.line_sums;
+	ordered_line_sum(a.bh, [&](uint32_t i) { return float(sums[i]); }, __fdiv_rn(1.0f, float(a.bw * a.bh)), a.average);
 }
 
 // perform_blur_impl, horizontal pass buf0 -> buf1 (postprocessor.rs:862-900)
@@ -120,13 +153,9 @@ __device__ __forceinline__ CV bloom_at(const PostArgs& a, uint32_t x, uint32_t y
 	return cv_from_c64(a.bloom0[uint64_t(y) * a.bw + x]);
 }
 
-// Tonemapping with bloom, nearest (postprocessor.rs:346-462) or linear (:464-726) bloom filter.
-__global__ void __launch_bounds__(256) pp_tonemap_bloom_kernel(PostArgs a)
+// HDR pixel (x, y) plus its bloom sample, nearest (postprocessor.rs:346-462) or linear (:464-726).
+__device__ __forceinline__ CV bloom_sum(const PostArgs& a, uint32_t x, uint32_t y, CV c)
 {
-	const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-	const uint32_t y = blockIdx.y;
-	if (x >= a.width) return;
-	const CV c = cv_from_c64(__ldg(reinterpret_cast<const unsigned long long*>(a.hdr) + uint64_t(y) * a.width + x));
 	const uint32_t S = a.scale;
 	CV sum;
 	if (!a.linear_filter)
@@ -165,7 +194,45 @@ __global__ void __launch_bounds__(256) pp_tonemap_bloom_kernel(PostArgs a)
 		else // corners
 			sum = cv_add(bloom_at(a, sx, sy), c);
 	}
-	a.dst[uint64_t(y) * a.dst_pitch + x] = cv_to_c32(tonemap(sum, a));
+	return sum;
+}
+
+// Tonemapping with bloom: two horizontally adjacent pixels per thread (16-byte HDR loads and 8-byte
+// stores where aligned).
+__global__ void __launch_bounds__(256) pp_tonemap_bloom_kernel(PostArgs a)
+{
+	const uint32_t x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+	const uint32_t y = blockIdx.y;
+	if (x >= a.width) return;
+	const uint64_t src = uint64_t(y) * a.width + x;
+	const uint64_t dst = uint64_t(y) * a.dst_pitch + x;
+	const bool pair = x + 1 < a.width;
+	unsigned long long p0, p1 = 0;
+	if (pair && (src & 1) == 0)
+	{
+		const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(a.hdr + src));
+		p0 = v.x;
+		p1 = v.y;
+	}
+	else
+	{
+		p0 = __ldg(reinterpret_cast<const unsigned long long*>(a.hdr) + src);
+		if (pair) p1 = __ldg(reinterpret_cast<const unsigned long long*>(a.hdr) + src + 1);
+	}
+	const uint32_t o0 = cv_to_c32(tonemap(bloom_sum(a, x, y, cv_from_c64(p0)), a));
+	if (!pair)
+	{
+		a.dst[dst] = o0;
+		return;
+	}
+	const uint32_t o1 = cv_to_c32(tonemap(bloom_sum(a, x + 1, y, cv_from_c64(p1)), a));
+	if ((dst & 1) == 0)
+		*reinterpret_cast<uint2*>(a.dst + dst) = make_uint2(o0, o1);
+	else
+	{
+		a.dst[dst] = o0;
+		a.dst[dst + 1] = o1;
+	}
 }
 
 // Without bloom: sequential per-line f32 colour sums (postprocessor.rs:237-253), one thread per line.
@@ -182,16 +249,11 @@ __global__ void pp_line_sums_kernel(PostArgs a)
 	a.line_sums_f[y * 4 + 3] = s.a;
 }
 
-__global__ void pp_average_plain_kernel(PostArgs a)
+__global__ void __launch_bounds__(256) pp_average_plain_kernel(PostArgs a)
 {
-	if (threadIdx.x != 0 || blockIdx.x != 0) return;
-	float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-	for (uint32_t y = 0; y < a.height; ++y)
-#pragma unroll
-		for (int i = 0; i < 4; ++i) s[i] = fadd(s[i], a.line_sums_f[y * 4 + i]);
-	const float inv = __fdiv_rn(1.0f, float(uint64_t(a.width) * a.height));
-#pragma unroll
-	for (int i = 0; i < 4; ++i) a.average[i] = fmul(s[i], inv);
+	const float* sums = a.line_sums_f;
+	ordered_line_sum(a.height, [&](uint32_t i) { return sums[i]; }, __fdiv_rn(1.0f, float(uint64_t(a.width) * a.height)),
+		a.average);
 }
 
 __global__ void __launch_bounds__(256) pp_tonemap_plain_kernel(PostArgs a)
@@ -275,7 +337,8 @@ __global__ void fill_kernel(void* dst, uint64_t count, uint64_t value, uint32_t 
 
 } // namespace
 
-int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream)
+int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream, cudaStream_t aux, cudaEvent_t fork,
+	cudaEvent_t join)
 {
 	(void)num_sms;
 	const dim3 block(256);
@@ -283,18 +346,28 @@ int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream)
 	{
 		cudaMemsetAsync(a.line_sums, 0, sizeof(int32_t) * 4 * a.bh, stream);
 		pp_downscale_kernel<<<dim3((a.bw + 255) / 256, a.bh), block, 0, stream>>>(a);
-		pp_average_bloom_kernel<<<1, 32, 0, stream>>>(a);
+		// The exposure average is consumed only after the frame: with an auxiliary stream it runs
+		// beside the blur and tonemap passes.
+		const bool overlap = aux && fork && join;
+		if (overlap)
+		{
+			cudaEventRecord(fork, stream);
+			cudaStreamWaitEvent(aux, fork, 0);
+		}
+		pp_average_bloom_kernel<<<1, 256, 0, overlap ? aux : stream>>>(a);
+		if (overlap) cudaEventRecord(join, aux);
 		if (a.radius > 0)
 		{
 			pp_blur_h_kernel<<<dim3((a.bw + 255) / 256, a.bh), block, 0, stream>>>(a);
 			pp_blur_v_kernel<<<dim3((a.bw + 255) / 256, a.bh), block, 0, stream>>>(a);
 		}
-		pp_tonemap_bloom_kernel<<<dim3((a.width + 255) / 256, a.height), block, 0, stream>>>(a);
+		pp_tonemap_bloom_kernel<<<dim3((a.width / 2 + 256) / 256, a.height), block, 0, stream>>>(a);
+		if (overlap) cudaStreamWaitEvent(stream, join, 0);
 	}
 	else
 	{
 		pp_line_sums_kernel<<<(a.height + 127) / 128, 128, 0, stream>>>(a);
-		pp_average_plain_kernel<<<1, 32, 0, stream>>>(a);
+		pp_average_plain_kernel<<<1, 256, 0, stream>>>(a);
 		pp_tonemap_plain_kernel<<<dim3((a.width + 255) / 256, a.height), block, 0, stream>>>(a);
 	}
 	return int(cudaGetLastError());

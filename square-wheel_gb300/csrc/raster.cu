@@ -4,19 +4,25 @@
 // running Rasterizer::fill_polygon for each draw in submission order (src/square_wheel/rasterizer.rs:
 // 137-729, write_into_framebuffer :1511-1536).
 //
-// Two launches:
-//   raster_setup: one thread per draw runs the reference's edge walk (rasterizer.rs:160-270) and stores
-//     each polygon part's first-row edge positions, the draw's integer plane equations
-//     (rasterizer.rs:287-310) and a conservative pixel box.
-//   raster_tiles: one 256-thread CTA per 16x16 tile, one thread per pixel. The CTA streams over the
-//     draws in submission order, 256 at a time; each thread tests one draw's box against the tile and
-//     a ballot + prefix sum compacts the hits into shared memory in order. Every thread then walks the
-//     hits in order for its own pixel and keeps the pixel in a register, so blending order is the
-//     reference's and the framebuffer is read and written once per frame.
-// Span setup is evaluated over the whole span with the frame as clip rectangle (the reference's
-// num_threads == 1 ClipRect); a pixel at span index i takes start + i*step, which is the reference's
-// repeated wrapping addition. Coverage and texel addresses are therefore bit-exact.
+// Three launches:
+//   raster_walk: one thread per draw runs the reference's edge walk (rasterizer.rs:160-270) into the
+//     draw's parts and derives its tile-binning box.
+//   raster_rows: one thread per (draw, row) record (row ranges and record offsets come from the host):
+//     the span [xs, xe) and the start and step of the mode's interpolants (the span setup of
+//     rasterizer.rs:329-422 / 513-556 / 686-703), evaluated once per (draw, row) over the whole span
+//     with the frame as clip rectangle (the reference's num_threads == 1 ClipRect).
+//   raster_tiles: one 256-thread CTA per 64x16 tile, each thread a 1x4 pixel strip of one row (about
+//     one wave of CTAs at 1080p). The CTA streams over the draws in submission order, 256 at a time;
+//     each thread tests one draw's box against the tile and a ballot + prefix sum compacts the hits
+//     (with their draw records) into shared memory in order. For batches of 32 hits the CTA stages
+//     their 16 rows of this tile in shared memory with parallel loads; every thread then walks the
+//     hits in order for its strip: for span pixel i it takes start + i*step (the reference's repeated
+//     wrapping addition), the per-pixel z division and the texel address, issues its four texel loads
+//     at once and blends them in submission order into registers. Blending order is the reference's,
+//     the frame buffer is read and written once, and coverage and texel addresses are bit-exact.
 #include "sw_kernels.cuh"
+
+#include <algorithm>
 
 namespace swgpu
 {
@@ -33,7 +39,7 @@ constexpr int Z_CALC_SHIFT = 31;
 constexpr int TC_FINAL_SHIFT = TC_SHIFT + Z_CALC_SHIFT - INV_Z_SHIFT + INV_Z_PRE_SHIFT; // 34
 constexpr float TC_SCALE = float(1 << TC_SHIFT);
 constexpr float INV_Z_SCALE = float(1 << INV_Z_SHIFT);
-constexpr int TILE = 16;
+
 
 __device__ __forceinline__ Fixed16 int_to_fixed16(int32_t x) { return int32_t(uint32_t(x) << 16); }
 __device__ __forceinline__ int32_t round_to_int(Fixed16 x) { return wadd(x, FIXED16_HALF) >> 16; }
@@ -52,10 +58,9 @@ __device__ __forceinline__ int64_t w64mul(int64_t a, int64_t b) { return int64_t
 struct SetupState
 {
 	const SwDrawCmd* d;
-	int32_t width, height;
+	int32_t height;
 	RasterPart* parts;
 	uint32_t num_parts;
-	int32_t bx0, by0, bx1, by1;
 };
 
 // The draw_func body up to the row loop: first-row edge positions (rasterizer.rs:316-320) and, for
@@ -112,35 +117,17 @@ __device__ void emit_part(SetupState& st, Fixed16 y_start, Fixed16 y_end, Fixed1
 		}
 	}
 	st.parts[st.num_parts++] = p;
-	// Box: x is linear in the row, so the extremes over the part are at its first and last rows.
-	const int32_t last = y_end_int - 1 - y_start_int;
-	const int32_t xl0 = p.x_left0 >> 16, xl1 = wadd(p.x_left0, wmul(last, dxl)) >> 16;
-	const int32_t xr0 = p.x_right0 >> 16, xr1 = wadd(p.x_right0, wmul(last, dxr)) >> 16;
-	st.bx0 = min(st.bx0, min(xl0, xl1));
-	st.bx1 = max(st.bx1, max(xr0, xr1));
-	st.by0 = min(st.by0, y_start_int);
-	st.by1 = max(st.by1, y_end_int);
 }
 
-__global__ void __launch_bounds__(128) raster_setup_kernel(RasterArgs a)
+// Edge walk of fill_polygon_impl_2_static_params (rasterizer.rs:160-270) for one draw.
+__device__ uint32_t edge_walk(const SwDrawCmd& d, const SwVertex16* vtx, int32_t height, RasterPart* parts)
 {
-	const uint32_t di = blockIdx.x * blockDim.x + threadIdx.x;
-	if (di >= a.num_draws) return;
-	const SwDrawCmd& d = a.draws[di];
 	SetupState st;
 	st.d = &d;
-	st.width = a.width;
-	st.height = a.height;
-	st.parts = a.parts + uint64_t(di) * SW_RASTER_MAX_PARTS;
+	st.height = height;
+	st.parts = parts;
 	st.num_parts = 0;
-	st.bx0 = INT32_MAX;
-	st.by0 = INT32_MAX;
-	st.bx1 = INT32_MIN;
-	st.by1 = INT32_MIN;
-
-	const SwVertex16* vtx = a.vertices + d.first_vertex;
 	const uint32_t n = d.vertex_count;
-	// Edge walk, rasterizer.rs:160-270.
 	uint32_t lower = 0;
 	Fixed16 min_y = vtx[0].y;
 	for (uint32_t i = 0; i < n; ++i)
@@ -187,35 +174,199 @@ __global__ void __launch_bounds__(128) raster_setup_kernel(RasterArgs a)
 			li = nli;
 		cur_y = next_y;
 	}
+	return st.num_parts;
+}
 
-	RasterDraw rd;
+// Integer plane equations of fill_polygon_part* (rasterizer.rs:287-310).
+struct DrawEq
+{
+	int64_t d_inv_z_dx, d_inv_z_dy, inv_z_k;
+	int64_t d_tc_dx[2], d_tc_dy[2], tc_k[2];
+};
+
+__device__ __forceinline__ DrawEq draw_equations(const SwDrawCmd& d)
+{
+	DrawEq e;
 	const float* de = d.depth_eq;
 	const float* te = d.tc_eq;
-	rd.d_inv_z_dx = f2i64(fmul(INV_Z_SCALE, de[0]));
-	rd.d_inv_z_dy = f2i64(fmul(INV_Z_SCALE, de[1]));
-	rd.inv_z_k = f2i64(fmul(INV_Z_SCALE, fadd(de[2], fmul(fadd(de[0], de[1]), 0.5f))));
+	e.d_inv_z_dx = f2i64(fmul(INV_Z_SCALE, de[0]));
+	e.d_inv_z_dy = f2i64(fmul(INV_Z_SCALE, de[1]));
+	e.inv_z_k = f2i64(fmul(INV_Z_SCALE, fadd(de[2], fmul(fadd(de[0], de[1]), 0.5f))));
 #pragma unroll
 	for (int i = 0; i < 2; ++i)
 	{
-		rd.d_tc_dx[i] = f2i64(fmul(TC_SCALE, te[i]));
-		rd.d_tc_dy[i] = f2i64(fmul(TC_SCALE, te[2 + i]));
-		rd.tc_k[i] = f2i64(fmul(TC_SCALE, fadd(te[4 + i], fmul(fadd(te[i], te[2 + i]), 0.5f))));
+		e.d_tc_dx[i] = f2i64(fmul(TC_SCALE, te[i]));
+		e.d_tc_dy[i] = f2i64(fmul(TC_SCALE, te[2 + i]));
+		e.tc_k[i] = f2i64(fmul(TC_SCALE, fadd(te[4 + i], fmul(fadd(te[i], te[2 + i]), 0.5f))));
 	}
+	return e;
+}
+
+// Span setup of one row (rasterizer.rs:329-422 full perspective, :513-556 line-z, :686-703 affine),
+// evaluated over the whole span with the frame as clip rectangle.
+__device__ RasterRow row_setup(const SwDrawCmd& d, const DrawEq& e, const RasterPart& p, int32_t y, int32_t width)
+{
+	RasterRow r;
+	r.a0 = r.b0 = r.a1 = r.b1 = r.a2 = r.b2 = 0;
+	const int32_t k = y - p.y_start_int;
+	const Fixed16 x_left = wadd(p.x_left0, wmul(k, p.dx_dy_left));
+	const Fixed16 x_right = wadd(p.x_right0, wmul(k, p.dx_dy_right));
+	const int32_t xs = max(x_left >> 16, 0);
+	const int32_t xe = min(x_right >> 16, width);
+	r.xs = xs;
+	r.xe = xe;
+	if (xs >= xe) return r;
+	const int32_t len1 = (xe - 1) - xs;
+	const int64_t span_start_x = xs, span_end_x = xe - 1;
+	if (d.mode == SW_RASTER_AFFINE)
+	{
+		const Fixed16 x_delta = max(wsub(x_right, x_left), FIXED16_ONE);
+		const int32_t tcl0 = wadd(p.tc_left0[0], wmul(k, p.d_tc_left[0]));
+		const int32_t tcl1 = wadd(p.tc_left0[1], wmul(k, p.d_tc_left[1]));
+		const int32_t tcr0 = wadd(p.tc_right0[0], wmul(k, p.d_tc_right[0]));
+		const int32_t tcr1 = wadd(p.tc_right0[1], wmul(k, p.d_tc_right[1]));
+		r.a1 = tcl0;
+		r.b1 = fx_div(wsub(tcr0, tcl0), x_delta);
+		r.a2 = tcl1;
+		r.b2 = fx_div(wsub(tcr1, tcl1), x_delta);
+		return r;
+	}
+	const int64_t line_inv_z = w64add(w64mul(int64_t(y), e.d_inv_z_dy), e.inv_z_k);
+	const int64_t inv_z_min = 1 << INV_Z_PRE_SHIFT, inv_z_max = 1 << 29;
+	if (d.mode == SW_RASTER_LINE_Z_CORRECTED)
+	{
+		const uint32_t izs = uint32_t(min(max(w64add(w64mul(span_start_x, e.d_inv_z_dx), line_inv_z), inv_z_min), inv_z_max));
+		const uint32_t ize = uint32_t(min(max(w64add(w64mul(span_end_x, e.d_inv_z_dx), line_inv_z), inv_z_min), inv_z_max));
+		const uint64_t zs = (1u << Z_CALC_SHIFT) / (izs >> INV_Z_PRE_SHIFT);
+		const uint64_t ze = (1u << Z_CALC_SHIFT) / (ize >> INV_Z_PRE_SHIFT);
+		int32_t start[2], step[2];
+#pragma unroll
+		for (int c = 0; c < 2; ++c)
+		{
+			const int64_t line_tc = w64add(w64mul(int64_t(y), e.d_tc_dy[c]), e.tc_k[c]);
+			const uint64_t ts = uint64_t(max(w64add(line_tc, w64mul(span_start_x, e.d_tc_dx[c])), int64_t(0)));
+			const uint64_t te = uint64_t(max(w64add(line_tc, w64mul(span_end_x, e.d_tc_dx[c])), int64_t(0)));
+			const uint64_t max_tc = (uint64_t(d.tex_size[c]) << 16) - 1;
+			const int32_t s0 = int32_t(min((zs * ts) >> (TC_FINAL_SHIFT - 16), max_tc));
+			const int32_t s1 = int32_t(min((ze * te) >> (TC_FINAL_SHIFT - 16), max_tc));
+			start[c] = s0;
+			step[c] = len1 > 0 ? (s1 - s0) / len1 : 0;
+		}
+		r.a1 = start[0];
+		r.b1 = step[0];
+		r.a2 = start[1];
+		r.b2 = step[1];
+		return r;
+	}
+	// Full perspective.
+	const int32_t izs = int32_t(max(inv_z_min, min(w64add(w64mul(span_start_x, e.d_inv_z_dx), line_inv_z), inv_z_max)));
+	const int32_t ize = int32_t(max(inv_z_min, min(w64add(w64mul(span_end_x, e.d_inv_z_dx), line_inv_z), inv_z_max)));
+	const int32_t d_inv_z = len1 > 0 ? (ize - izs) / len1 : 0;
+	const int64_t izc = int64_t(izs - (1 << INV_Z_PRE_SHIFT));
+	const int tc_max_shift = INV_Z_SHIFT - TC_SHIFT;
+	const int64_t tc_max_max = 1 << 29;
+	int32_t start[2], step[2];
+#pragma unroll
+	for (int c = 0; c < 2; ++c)
+	{
+		const int64_t size = int64_t(d.tex_size[c]);
+		const int64_t line_tc = w64add(w64mul(int64_t(y), e.d_tc_dy[c]), e.tc_k[c]);
+		const int64_t tc_max_start = max(int64_t(0), min((w64mul(izc, size) >> tc_max_shift) - 1, tc_max_max));
+		const int32_t tcs = int32_t(max(int64_t(0), min(w64add(w64mul(span_start_x, e.d_tc_dx[c]), line_tc), tc_max_start)));
+		int32_t s = tcs, st = 0;
+		if (len1 > 0)
+		{
+			const int64_t tc_max_end =
+				max(int64_t(0), min((w64mul(izc + int64_t(wmul(d_inv_z, len1)), size) >> tc_max_shift) - 1, tc_max_max));
+			const int32_t tce = int32_t(max(int64_t(0), min(w64add(w64mul(span_end_x, e.d_tc_dx[c]), line_tc), tc_max_end)));
+			st = (tce - tcs) / len1;
+			s = tce > tcs ? tcs : wsub(tce, wmul(st, len1));
+		}
+		start[c] = s;
+		step[c] = st;
+	}
+	r.a0 = izs;
+	r.b0 = d_inv_z;
+	r.a1 = start[0];
+	r.b1 = step[0];
+	r.a2 = start[1];
+	r.b2 = step[1];
+	return r;
+}
+
+// Edge walk per draw (one thread per draw): the draw's parts, its tile-binning box (conservative: x
+// is linear in the row, so its extremes over a part are at the part's first and last rows) and the
+// per-draw record of the tile kernel.
+__global__ void __launch_bounds__(128) raster_walk_kernel(RasterArgs a)
+{
+	const uint32_t di = blockIdx.x * blockDim.x + threadIdx.x;
+	if (di >= a.num_draws) return;
+	const SwDrawCmd d = a.draws[di];
+	RasterPart* parts = a.parts + uint64_t(di) * SW_RASTER_MAX_PARTS;
+	const uint32_t np = edge_walk(d, a.vertices + d.first_vertex, a.height, parts);
+	a.part_counts[di] = np;
+	int32_t bx0 = INT32_MAX, bx1 = INT32_MIN, by0 = INT32_MAX, by1 = INT32_MIN;
+	for (uint32_t pi = 0; pi < np; ++pi)
+	{
+		const RasterPart& p = parts[pi];
+		const int32_t last = p.y_end_int - 1 - p.y_start_int;
+		bx0 = min(bx0, min(p.x_left0 >> 16, wadd(p.x_left0, wmul(last, p.dx_dy_left)) >> 16));
+		bx1 = max(bx1, max(p.x_right0 >> 16, wadd(p.x_right0, wmul(last, p.dx_dy_right)) >> 16));
+		by0 = min(by0, p.y_start_int);
+		by1 = max(by1, p.y_end_int);
+	}
+	bx0 = max(bx0, 0);
+	bx1 = min(bx1, a.width);
+	const DrawRows dr = a.draw_rows[di];
+	// Rows outside the host's row range have no record; clamp the box to it.
+	by0 = max(by0, dr.y0);
+	by1 = min(by1, dr.y0 + int32_t(dr.nrows));
+	a.boxes[di] = (np > 0 && bx0 < bx1 && by0 < by1) ? RasterBox{int16_t(bx0), int16_t(by0), int16_t(bx1), int16_t(by1)}
+														: RasterBox{0, 0, 0, 0};
+	RasterDraw rd;
 	rd.tex_offset = d.tex_offset;
 	rd.tex_w = d.tex_size[0];
 	rd.tex_h = d.tex_size[1];
+	rd.row_base = dr.row_base;
+	rd.y0 = dr.y0;
 	rd.mode = d.mode;
 	rd.blend = d.blend;
-	rd.num_parts = st.num_parts;
-	rd.reserved = 0;
 	a.rdraws[di] = rd;
+}
 
-	RasterBox box;
-	if (st.num_parts == 0 || st.bx0 >= a.width || st.bx1 <= 0)
-		box = RasterBox{0, 0, 0, 0};
-	else
-		box = RasterBox{int16_t(max(st.bx0, 0)), int16_t(st.by0), int16_t(min(st.bx1, a.width)), int16_t(st.by1)};
-	a.boxes[di] = box;
+// Span setup of every covered row of every draw (one thread per row record).
+__global__ void __launch_bounds__(128) raster_rows_kernel(RasterArgs a)
+{
+	const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= a.total_rows) return;
+	// Draw owning row record t: the last draw whose row_base <= t.
+	uint32_t lo = 0, hi = a.num_draws;
+	while (hi - lo > 1)
+	{
+		const uint32_t mid = (lo + hi) >> 1;
+		if (a.draw_rows[mid].row_base <= t)
+			lo = mid;
+		else
+			hi = mid;
+	}
+	const DrawRows dr = a.draw_rows[lo];
+	const int32_t y = dr.y0 + int32_t(t - dr.row_base);
+	const SwDrawCmd d = a.draws[lo];
+	const RasterPart* parts = a.parts + uint64_t(lo) * SW_RASTER_MAX_PARTS;
+	const uint32_t np = a.part_counts[lo];
+	RasterRow row;
+	row.xs = row.xe = 0;
+	row.a0 = row.b0 = row.a1 = row.b1 = row.a2 = row.b2 = 0;
+	for (uint32_t pi = 0; pi < np; ++pi)
+	{
+		const RasterPart p = parts[pi];
+		if (y >= p.y_start_int && y < p.y_end_int)
+		{
+			row = row_setup(d, draw_equations(d), p, y, a.width);
+			break;
+		}
+	}
+	a.rows[t] = row;
 }
 
 template <class P>
@@ -233,196 +384,183 @@ __device__ __forceinline__ void blend_into(typename P::T& dst, typename P::T tex
 	}
 }
 
-// Texel address of pixel (x, y) for one draw; returns false if the pixel is not covered. Addresses
-// are the reference's (u32 arithmetic for the perspective modes, i32 for affine, then as usize).
-__device__ __forceinline__ bool texel_address(const RasterDraw& rd, const RasterPart& p, int32_t x, int32_t y,
-	int32_t width, uint64_t& address)
+// Texel address of span pixel i (rasterizer.rs:424-445, 558-572, 705-719): u32 arithmetic for the
+// perspective modes, i32 for affine, then as usize.
+__device__ __forceinline__ uint64_t pixel_address(const RasterRow& r, uint32_t mode, int32_t i, uint32_t tex_w)
 {
-	const int32_t k = y - p.y_start_int;
-	const Fixed16 x_left = wadd(p.x_left0, wmul(k, p.dx_dy_left));
-	const Fixed16 x_right = wadd(p.x_right0, wmul(k, p.dx_dy_right));
-	const int32_t xs = max(x_left >> 16, 0);
-	const int32_t xe = min(x_right >> 16, width);
-	if (x < xs || x >= xe) return false;
-	const int32_t i = x - xs;
-	const int32_t len1 = (xe - 1) - xs;
-	const int64_t span_start_x = xs, span_end_x = xe - 1;
-
-	if (rd.mode == SW_RASTER_AFFINE) // rasterizer.rs:684-719
+	const int32_t t0 = wadd(r.a1, wmul(i, r.b1));
+	const int32_t t1 = wadd(r.a2, wmul(i, r.b2));
+	if (mode == SW_RASTER_FULL_PERSPECTIVE)
 	{
-		int32_t tcl[2], tcr[2];
-#pragma unroll
-		for (int c = 0; c < 2; ++c)
-		{
-			tcl[c] = wadd(p.tc_left0[c], wmul(k, p.d_tc_left[c]));
-			tcr[c] = wadd(p.tc_right0[c], wmul(k, p.d_tc_right[c]));
-		}
-		const Fixed16 x_delta = max(wsub(x_right, x_left), FIXED16_ONE);
-		const int32_t tc0 = wadd(tcl[0], wmul(i, fx_div(wsub(tcr[0], tcl[0]), x_delta)));
-		const int32_t tc1 = wadd(tcl[1], wmul(i, fx_div(wsub(tcr[1], tcl[1]), x_delta)));
-		address = uint64_t(int64_t(wadd(tc0 >> 16, wmul(tc1 >> 16, int32_t(rd.tex_w)))));
-		return true;
+		const int32_t inv_z = wadd(r.a0, wmul(i, r.b0));
+		const uint32_t zdiv = uint32_t(inv_z) >> INV_Z_PRE_SHIFT;
+		const uint32_t z = (1u << Z_CALC_SHIFT) / (zdiv ? zdiv : 1u);
+		const uint32_t pu = uint32_t((uint64_t(z) * uint64_t(int64_t(t0))) >> TC_FINAL_SHIFT);
+		const uint32_t pv = uint32_t((uint64_t(z) * uint64_t(int64_t(t1))) >> TC_FINAL_SHIFT);
+		return uint32_t(pu + pv * tex_w);
 	}
-
-	const int64_t line_inv_z = w64add(w64mul(int64_t(y), rd.d_inv_z_dy), rd.inv_z_k);
-	const int64_t inv_z_min = 1 << INV_Z_PRE_SHIFT, inv_z_max = 1 << 29;
-	if (rd.mode == SW_RASTER_LINE_Z_CORRECTED) // rasterizer.rs:528-572
-	{
-		const uint32_t izs = uint32_t(min(max(w64add(w64mul(span_start_x, rd.d_inv_z_dx), line_inv_z), inv_z_min), inv_z_max));
-		const uint32_t ize = uint32_t(min(max(w64add(w64mul(span_end_x, rd.d_inv_z_dx), line_inv_z), inv_z_min), inv_z_max));
-		const uint64_t zs = (1u << Z_CALC_SHIFT) / (izs >> INV_Z_PRE_SHIFT);
-		const uint64_t ze = (1u << Z_CALC_SHIFT) / (ize >> INV_Z_PRE_SHIFT);
-		int32_t tc[2];
-#pragma unroll
-		for (int c = 0; c < 2; ++c)
-		{
-			const int64_t line_tc = w64add(w64mul(int64_t(y), rd.d_tc_dy[c]), rd.tc_k[c]);
-			const uint64_t ts = uint64_t(max(w64add(line_tc, w64mul(span_start_x, rd.d_tc_dx[c])), int64_t(0)));
-			const uint64_t te = uint64_t(max(w64add(line_tc, w64mul(span_end_x, rd.d_tc_dx[c])), int64_t(0)));
-			const uint64_t max_tc = (uint64_t(c == 0 ? rd.tex_w : rd.tex_h) << 16) - 1;
-			const int32_t s0 = int32_t(min((zs * ts) >> (TC_FINAL_SHIFT - 16), max_tc));
-			const int32_t s1 = int32_t(min((ze * te) >> (TC_FINAL_SHIFT - 16), max_tc));
-			const int32_t step = len1 > 0 ? (s1 - s0) / len1 : 0;
-			tc[c] = wadd(s0, wmul(i, step));
-		}
-		address = uint32_t(tc[0] >> 16) + uint32_t(tc[1] >> 16) * rd.tex_w;
-		return true;
-	}
-
-	// Full perspective, rasterizer.rs:340-445.
-	const int32_t izs = int32_t(max(inv_z_min, min(w64add(w64mul(span_start_x, rd.d_inv_z_dx), line_inv_z), inv_z_max)));
-	const int32_t ize = int32_t(max(inv_z_min, min(w64add(w64mul(span_end_x, rd.d_inv_z_dx), line_inv_z), inv_z_max)));
-	const int32_t d_inv_z = len1 > 0 ? (ize - izs) / len1 : 0;
-	const int32_t inv_z = wadd(izs, wmul(i, d_inv_z));
-	const int64_t izc = int64_t(izs - (1 << INV_Z_PRE_SHIFT));
-	const int tc_max_shift = INV_Z_SHIFT - TC_SHIFT;
-	const int64_t tc_max_max = 1 << 29;
-	int32_t tc[2];
-#pragma unroll
-	for (int c = 0; c < 2; ++c)
-	{
-		const int64_t size = int64_t(c == 0 ? rd.tex_w : rd.tex_h);
-		const int64_t line_tc = w64add(w64mul(int64_t(y), rd.d_tc_dy[c]), rd.tc_k[c]);
-		const int64_t tc_max_start = max(int64_t(0), min((w64mul(izc, size) >> tc_max_shift) - 1, tc_max_max));
-		const int32_t tcs = int32_t(max(int64_t(0), min(w64add(w64mul(span_start_x, rd.d_tc_dx[c]), line_tc), tc_max_start)));
-		int32_t start = tcs, step = 0;
-		if (len1 > 0)
-		{
-			const int64_t tc_max_end =
-				max(int64_t(0), min((w64mul(izc + int64_t(wmul(d_inv_z, len1)), size) >> tc_max_shift) - 1, tc_max_max));
-			const int32_t tce = int32_t(max(int64_t(0), min(w64add(w64mul(span_end_x, rd.d_tc_dx[c]), line_tc), tc_max_end)));
-			step = (tce - tcs) / len1;
-			start = tce > tcs ? tcs : wsub(tce, wmul(step, len1));
-		}
-		tc[c] = wadd(start, wmul(i, step));
-	}
-	const uint32_t zdiv = uint32_t(inv_z) >> INV_Z_PRE_SHIFT;
-	const uint32_t z = (1u << Z_CALC_SHIFT) / (zdiv ? zdiv : 1u);
-	const uint32_t pu = uint32_t((uint64_t(z) * uint64_t(int64_t(tc[0]))) >> TC_FINAL_SHIFT);
-	const uint32_t pv = uint32_t((uint64_t(z) * uint64_t(int64_t(tc[1]))) >> TC_FINAL_SHIFT);
-	address = uint32_t(pu + pv * rd.tex_w);
-	return true;
+	if (mode == SW_RASTER_LINE_Z_CORRECTED) return uint32_t(t0 >> 16) + uint32_t(t1 >> 16) * tex_w;
+	return uint64_t(int64_t(wadd(t0 >> 16, wmul(t1 >> 16, int32_t(tex_w)))));
 }
+
+constexpr int TILE_W = 64;  // tile: 64 x 16 pixels, 256 threads, each thread a 1 x 4 strip of a row
+constexpr int TILE_H = 16;
+constexpr int STRIP = 4;
+constexpr int BATCH = 32;   // draws whose tile rows are staged in shared memory at a time
 
 template <class P>
 __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 {
 	typedef typename P::T T;
-	__shared__ uint32_t hits[256];
-	__shared__ uint32_t warp_counts[8];
+	__shared__ uint32_t s_warp_counts[8];
+	__shared__ RasterDraw s_rd[256];
+	__shared__ RasterBox s_box[256];
+	__shared__ RasterRow s_row[BATCH][TILE_H];
 
-	const int tiles_x = (a.width + TILE - 1) / TILE;
-	const int tx0 = int(blockIdx.x % tiles_x) * TILE;
-	const int ty0 = int(blockIdx.x / tiles_x) * TILE;
+	const int tiles_x = (a.width + TILE_W - 1) / TILE_W;
+	const int tx0 = int(blockIdx.x % tiles_x) * TILE_W;
+	const int ty0 = int(blockIdx.x / tiles_x) * TILE_H;
 	const int tid = threadIdx.x;
-	const int x = tx0 + (tid & (TILE - 1));
-	const int y = ty0 + (tid >> 4);
-	const bool valid = x < a.width && y < a.height;
-	const int tx1 = min(tx0 + TILE, a.width), ty1 = min(ty0 + TILE, a.height);
+	const int ly = tid >> 4;
+	const int xb = tx0 + (tid & 15) * STRIP; // first pixel of this thread's strip
+	const int y = ty0 + ly;
+	const bool row_valid = y < a.height;
+	const int tx1 = min(tx0 + TILE_W, a.width), ty1 = min(ty0 + TILE_H, a.height);
 
 	T* fb = static_cast<T*>(a.framebuffer);
 	const T* arena = static_cast<const T*>(a.arena);
-	T pix = T(0);
-	if (valid)
+	T pix[STRIP];
+#pragma unroll
+	for (int k = 0; k < STRIP; ++k)
 	{
-		if (a.clear_background)
+		pix[k] = T(0);
+		const int x = xb + k;
+		if (row_valid && x < a.width)
 		{
-			// ColorVec::from_color_f32x3(&[32.0, 16.0, 8.0]).into(), partial_renderer.rs:255
-			pix = P::FORMAT == SW_PIXEL_C64 ? T(8ull | (16ull << 16) | (32ull << 32)) : T(0x00201008u);
+			if (a.clear_background) // ColorVec::from_color_f32x3(&[32.0, 16.0, 8.0]).into(), partial_renderer.rs:255
+				pix[k] = P::FORMAT == SW_PIXEL_C64 ? T(8ull | (16ull << 16) | (32ull << 32)) : T(0x00201008u);
+			else
+				pix[k] = fb[uint64_t(y) * a.width + x];
 		}
-		else
-			pix = fb[uint64_t(y) * a.width + x];
 	}
 	unsigned int local_errors = 0, local_writes = 0;
 
 	const int lane = tid & 31, warp = tid >> 5;
 	for (uint32_t chunk = 0; chunk < a.num_draws; chunk += 256)
 	{
+		// Ordered compaction of the chunk's draws whose box meets the tile; the hitting thread stages
+		// the draw's record and box.
 		const uint32_t di = chunk + tid;
 		bool hit = false;
+		RasterBox b{0, 0, 0, 0};
+		RasterDraw rd{};
 		if (di < a.num_draws)
 		{
-			const RasterBox b = a.boxes[di];
+			b = a.boxes[di];
 			hit = b.x0 < tx1 && b.x1 > tx0 && b.y0 < ty1 && b.y1 > ty0 && b.x0 < b.x1 && b.y0 < b.y1;
+			if (hit) rd = a.rdraws[di];
 		}
 		const unsigned mask = __ballot_sync(0xFFFFFFFFu, hit);
-		if (lane == 0) warp_counts[warp] = __popc(mask);
+		if (lane == 0) s_warp_counts[warp] = __popc(mask);
 		__syncthreads();
 		uint32_t base = 0, total = 0;
 #pragma unroll
 		for (int w = 0; w < 8; ++w)
 		{
-			const uint32_t c = warp_counts[w];
+			const uint32_t c = s_warp_counts[w];
 			if (w < warp) base += c;
 			total += c;
 		}
-		if (hit) hits[base + __popc(mask & ((1u << lane) - 1u))] = di;
+		if (hit)
+		{
+			const uint32_t pos = base + __popc(mask & ((1u << lane) - 1u));
+			s_rd[pos] = rd;
+			s_box[pos] = b;
+		}
 		__syncthreads();
 
-		if (valid)
-			for (uint32_t h = 0; h < total; ++h)
+		for (uint32_t b0 = 0; b0 < total; b0 += BATCH)
+		{
+			const uint32_t n = min(uint32_t(BATCH), total - b0);
+			// Stage the batch's rows of this tile (independent loads, one per thread).
+			for (uint32_t k = tid; k < n * TILE_H; k += 256)
 			{
-				const uint32_t d = hits[h];
-				const RasterBox b = a.boxes[d];
-				if (x < b.x0 || x >= b.x1 || y < b.y0 || y >= b.y1) continue;
-				const RasterDraw rd = a.rdraws[d];
-				const RasterPart* parts = a.parts + uint64_t(d) * SW_RASTER_MAX_PARTS;
-				for (uint32_t pi = 0; pi < rd.num_parts; ++pi)
+				const uint32_t h = k / TILE_H, r = k % TILE_H;
+				const RasterBox bx = s_box[b0 + h];
+				const int32_t ry = ty0 + int32_t(r);
+				RasterRow row;
+				if (ry >= bx.y0 && ry < bx.y1)
 				{
-					const RasterPart p = parts[pi];
-					if (y < p.y_start_int || y >= p.y_end_int) continue;
-					uint64_t ua;
-					if (texel_address(rd, p, x, y, a.width, ua))
-					{
-						if (ua >= uint64_t(rd.tex_w) * rd.tex_h)
-						{
-							++local_errors;
-							ua = 0;
-						}
-						const T texel = arena[rd.tex_offset + ua];
-						blend_into<P>(pix, texel, rd.blend);
-						++local_writes;
-					}
-					break;
+					const RasterDraw& d = s_rd[b0 + h];
+					row = a.rows[d.row_base + uint32_t(ry - d.y0)];
 				}
+				else
+					row.xs = row.xe = 0;
+				s_row[h][r] = row;
 			}
-		__syncthreads();
+			__syncthreads();
+			if (row_valid)
+				for (uint32_t h = 0; h < n; ++h)
+				{
+					const RasterRow row = s_row[h][ly];
+					if (xb + STRIP <= row.xs || xb >= row.xe) continue;
+					const RasterDraw& d = s_rd[b0 + h];
+					// Up to four independent texel loads, then the blends in pixel order.
+					T tex[STRIP];
+					bool ok[STRIP];
+#pragma unroll
+					for (int k = 0; k < STRIP; ++k)
+					{
+						const int x = xb + k;
+						ok[k] = x >= row.xs && x < row.xe;
+						tex[k] = T(0);
+						if (ok[k])
+						{
+							uint64_t ua = pixel_address(row, d.mode, x - row.xs, d.tex_w);
+							if (ua >= uint64_t(d.tex_w) * d.tex_h)
+							{
+								++local_errors;
+								ua = 0;
+							}
+							tex[k] = arena[d.tex_offset + ua];
+						}
+					}
+#pragma unroll
+					for (int k = 0; k < STRIP; ++k)
+						if (ok[k])
+						{
+							blend_into<P>(pix[k], tex[k], d.blend);
+							++local_writes;
+						}
+				}
+			__syncthreads();
+		}
 	}
-	if (valid) fb[uint64_t(y) * a.width + x] = pix;
+	if (row_valid)
+	{
+#pragma unroll
+		for (int k = 0; k < STRIP; ++k)
+			if (xb + k < a.width) fb[uint64_t(y) * a.width + xb + k] = pix[k];
+	}
 	if (local_errors) atomicAdd(a.error_counter, local_errors);
 	// Pixel writes (span pixels processed) for the traffic accounting, one atomic per warp.
 	for (int o = 16; o > 0; o >>= 1) local_writes += __shfl_xor_sync(0xFFFFFFFFu, local_writes, o);
-	if ((tid & 31) == 0 && local_writes)
+	if (lane == 0 && local_writes)
 		atomicAdd(reinterpret_cast<unsigned long long*>(a.error_counter + 2), (unsigned long long)local_writes);
 }
 
 } // namespace
 
-int launch_raster(const RasterArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream)
+int launch_raster_setup(const RasterArgs& args, cudaStream_t stream)
 {
-	if (args.num_draws > 0)
-		raster_setup_kernel<<<(args.num_draws + 127) / 128, 128, 0, stream>>>(args);
-	const unsigned tiles = unsigned(((args.width + TILE - 1) / TILE) * ((args.height + TILE - 1) / TILE));
+	if (args.num_draws > 0) raster_walk_kernel<<<(args.num_draws + 127) / 128, 128, 0, stream>>>(args);
+	if (args.total_rows > 0) raster_rows_kernel<<<(args.total_rows + 127) / 128, 128, 0, stream>>>(args);
+	return int(cudaGetLastError());
+}
+
+int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream)
+{
+	const unsigned tiles = unsigned(((args.width + TILE_W - 1) / TILE_W) * ((args.height + TILE_H - 1) / TILE_H));
 	if (tiles == 0) return 0;
 	if (pixel_format == SW_PIXEL_C64)
 		raster_tiles_kernel<PixC64><<<tiles, 256, 0, stream>>>(args);
@@ -430,6 +568,23 @@ int launch_raster(const RasterArgs& args, uint32_t pixel_format, int num_sms, cu
 		raster_tiles_kernel<PixC32><<<tiles, 256, 0, stream>>>(args);
 	(void)num_sms;
 	return int(cudaGetLastError());
+}
+
+// Rows a draw can cover: [round(min_y), round(max_y)) clipped to the frame (the edge walk's parts lie
+// inside, rasterizer.rs:160-271 with fixed16_round_to_int).
+void draw_row_range(const SwDrawCmd& d, const SwVertex16* v, int32_t height, int32_t& y0, uint32_t& nrows)
+{
+	int32_t mn = v[d.first_vertex].y, mx = mn;
+	for (uint32_t i = 1; i < d.vertex_count; ++i)
+	{
+		mn = std::min(mn, v[d.first_vertex + i].y);
+		mx = std::max(mx, v[d.first_vertex + i].y);
+	}
+	auto round_i = [](int32_t f) { return int32_t(uint32_t(f) + uint32_t(FIXED16_HALF)) >> 16; };
+	const int32_t a = std::max(round_i(mn), 0);
+	const int32_t b = std::min(round_i(mx), height);
+	y0 = a;
+	nrows = b > a ? uint32_t(b - a) : 0u;
 }
 
 } // namespace swgpu

@@ -426,7 +426,9 @@ int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, i
 	if (args.total_work == 0) return 0;
 	const int threads = 256;
 	uint64_t blocks_needed = (args.total_work + threads - 1) / threads;
-	uint64_t blocks_max = uint64_t(num_sms) * 3;
+	// Up to 8 waves of resident blocks: small frames get one texel per thread (latency hidden by
+	// parallelism), large batches stride.
+	uint64_t blocks_max = uint64_t(num_sms) * 3 * 8;
 	unsigned blocks = unsigned(blocks_needed < blocks_max ? blocks_needed : blocks_max);
 	if (pixel_format == SW_PIXEL_C64)
 	{

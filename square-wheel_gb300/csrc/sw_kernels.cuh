@@ -63,7 +63,7 @@ int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, i
 // ---- rasteriser ----
 
 // One polygon part of the edge walk (a draw_func call of fill_polygon_impl_2_static_params,
-// src/square_wheel/rasterizer.rs:198-254), reduced to what a pixel needs to find its span.
+// src/square_wheel/rasterizer.rs:198-254), reduced to what a row needs to find its span.
 struct RasterPart
 {
 	int32_t y_start_int; // first row, clipped to the frame
@@ -82,20 +82,38 @@ struct RasterPart
 
 #define SW_RASTER_MAX_PARTS SW_MAX_POLYGON_VERTICES
 
-// Per-draw setup shared by all of its parts (integer plane equations of fill_polygon_part*,
-// rasterizer.rs:287-310), plus the pixel bounding box used for tile binning.
-struct RasterDraw
+// Rows a draw can cover, computed on the host from its vertices: [y0, y0 + nrows) contains every
+// part's rows; row records of the draw start at row_base.
+struct DrawRows
 {
-	int64_t d_inv_z_dx, d_inv_z_dy, inv_z_k;
-	int64_t d_tc_dx[2], d_tc_dy[2], tc_k[2];
-	uint64_t tex_offset;
-	uint32_t tex_w, tex_h;
-	uint32_t mode, blend;
-	uint32_t num_parts;
+	uint32_t row_base;
+	int32_t y0;
+	uint32_t nrows;
 	uint32_t reserved;
 };
 
-// Conservative pixel bounds of a draw: [x0, x1) x [y0, y1); empty when x0 >= x1 or y0 >= y1.
+// One row of one draw after span setup (rasterizer.rs:329-422 / 513-556 / 686-703): the span
+// [xs, xe) and, for pixel i = x - xs, the interpolants start + i * step of the draw's mode:
+//   full perspective: (a0, b0) span inv_z, (a1, b1) and (a2, b2) span tc (i32, wrapping)
+//   line-z corrected / affine: (a1, b1) and (a2, b2) the 16.16 texture coordinates.
+// xs >= xe: the row holds no pixel.
+struct RasterRow
+{
+	int32_t xs, xe;
+	int32_t a0, b0, a1, b1, a2, b2;
+};
+
+// Per-draw record of the tile kernel.
+struct RasterDraw
+{
+	uint64_t tex_offset;
+	uint32_t tex_w, tex_h;
+	uint32_t row_base;
+	int32_t y0;
+	uint32_t mode, blend;
+};
+
+// Pixel bounds of a draw: [x0, x1) x [y0, y1); empty when x0 >= x1 or y0 >= y1.
 struct RasterBox
 {
 	int16_t x0, y0, x1, y1;
@@ -105,11 +123,15 @@ struct RasterArgs
 {
 	const SwDrawCmd* draws;
 	const SwVertex16* vertices;
+	const DrawRows* draw_rows;
 	uint32_t num_draws;
+	uint32_t total_rows; // row records of all draws
 	int32_t width, height;
 	uint32_t clear_background;
+	RasterPart* parts;     // num_draws * SW_RASTER_MAX_PARTS
+	uint32_t* part_counts; // num_draws
 	RasterDraw* rdraws;
-	RasterPart* parts; // num_draws * SW_RASTER_MAX_PARTS
+	RasterRow* rows;
 	RasterBox* boxes;
 	const void* arena;
 	uint64_t arena_texels;
@@ -117,7 +139,12 @@ struct RasterArgs
 	unsigned int* error_counter;
 };
 
-int launch_raster(const RasterArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream);
+// Edge walk + row setup (raster_walk, raster_rows), then the tile pass (raster_tiles).
+int launch_raster_setup(const RasterArgs& args, cudaStream_t stream);
+int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream);
+
+// Host side: rows [y0, y0 + nrows) a draw can cover (from its vertices).
+void draw_row_range(const SwDrawCmd& d, const SwVertex16* vertices, int32_t height, int32_t& y0, uint32_t& nrows);
 
 // ---- postprocessor / upscaler ----
 
@@ -143,7 +170,9 @@ struct PostArgs
 	uint32_t dst_pitch;
 };
 
-int launch_postprocess(const PostArgs& args, int num_sms, cudaStream_t stream);
+// aux/fork/join (optional): run the exposure-average reduction on `aux`, joined back before returning.
+int launch_postprocess(const PostArgs& args, int num_sms, cudaStream_t stream, cudaStream_t aux = nullptr,
+	cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 
 int launch_upscale(uint32_t mode, uint32_t scale, const uint32_t* src, uint32_t* dst, uint32_t dst_width,
 	uint32_t dst_height, uint32_t dst_pitch, cudaStream_t stream);

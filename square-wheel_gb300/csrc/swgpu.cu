@@ -6,7 +6,8 @@
 //   element arrays;
 //   per frame, grown on demand and reused: lights, surface descriptors + texel prefix sums, the surface
 //   arena (one Color32/Color64 texel per surface texel, surfaces contiguous and row-major), draw
-//   commands + vertices, raster setup output (per-draw equations, parts, boxes), the frame buffer
+//   commands + vertices + per-draw row ranges, raster setup output (per-draw records, per-row span
+//   records, pixel boxes), the frame buffer
 //   (width*height pixels), bloom buffers and the exposure-average scratch.
 // Host->device uploads go through pinned staging buffers on the context's stream. Every descriptor is
 // validated on the host before launch so that no kernel can read outside its buffers.
@@ -47,6 +48,11 @@ struct SwCtx
 	int device = 0;
 	int num_sms = 0;
 	cudaStream_t stream = nullptr;
+	// Second stream: draw uploads + raster setup run beside the surface build; the exposure average
+	// runs beside blur/tonemap. ev_setup / ev_tiles / ev_fork / ev_join order the two streams.
+	cudaStream_t aux = nullptr;
+	cudaEvent_t ev_setup = nullptr, ev_tiles = nullptr, ev_fork = nullptr, ev_join = nullptr;
+	bool tiles_recorded = false;
 	std::string last_error;
 
 	// static
@@ -67,7 +73,8 @@ struct SwCtx
 	uint32_t last_num_surfaces = 0, last_surface_format = SW_PIXEL_C32, last_max_light = 0;
 	uint64_t last_surface_work = 0;
 	bool last_surface_directional = false;
-	DevBuf draws, vertices, rdraws, parts, boxes;
+	DevBuf draws, vertices, draw_rows, rdraws, rows, boxes, parts, part_counts;
+	uint64_t num_rows = 0;
 	uint32_t num_draws = 0;
 	bool draws_valid = false;
 	DevBuf framebuffer;
@@ -83,7 +90,7 @@ struct SwCtx
 	float* h_average = nullptr; // pinned, 4 floats
 	cudaEvent_t average_ready = nullptr;
 
-	Staging stage_lights, stage_surfaces, stage_prefix, stage_draws, stage_vertices, stage_io;
+	Staging stage_lights, stage_surfaces, stage_prefix, stage_draws, stage_vertices, stage_draw_rows, stage_io;
 
 	// upscale scratch (src/dst copies for host buffers)
 	DevBuf up_src, up_dst;
@@ -92,9 +99,9 @@ struct SwCtx
 
 	// Optional per-stage device timing (sw_enable_timing).
 	bool timing = false;
-	cudaEvent_t t_begin[4] = {nullptr, nullptr, nullptr, nullptr};
-	cudaEvent_t t_end[4] = {nullptr, nullptr, nullptr, nullptr};
-	bool t_valid[4] = {false, false, false, false};
+	cudaEvent_t t_begin[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+	cudaEvent_t t_end[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+	bool t_valid[5] = {false, false, false, false, false};
 };
 
 namespace
@@ -104,8 +111,33 @@ enum Stage
 	STAGE_SURFACES = 0,
 	STAGE_RASTER = 1,
 	STAGE_POST = 2,
-	STAGE_UPSCALE = 3
+	STAGE_UPSCALE = 3,
+	STAGE_FRAME = 4, // sw_frame_begin .. end of sw_postprocess, both streams joined
+	NUM_STAGES = 5
 };
+
+RasterArgs raster_args(SwCtx* ctx)
+{
+	RasterArgs a;
+	a.draws = static_cast<const SwDrawCmd*>(ctx->draws.ptr);
+	a.vertices = static_cast<const SwVertex16*>(ctx->vertices.ptr);
+	a.num_draws = ctx->num_draws;
+	a.width = int32_t(ctx->frame.width);
+	a.height = int32_t(ctx->frame.height);
+	a.clear_background = ctx->frame.clear_background;
+	a.draw_rows = static_cast<const DrawRows*>(ctx->draw_rows.ptr);
+	a.total_rows = uint32_t(ctx->num_rows);
+	a.parts = static_cast<RasterPart*>(ctx->parts.ptr);
+	a.part_counts = static_cast<uint32_t*>(ctx->part_counts.ptr);
+	a.rdraws = static_cast<RasterDraw*>(ctx->rdraws.ptr);
+	a.rows = static_cast<RasterRow*>(ctx->rows.ptr);
+	a.boxes = static_cast<RasterBox*>(ctx->boxes.ptr);
+	a.arena = ctx->arena.ptr;
+	a.arena_texels = ctx->arena_texels;
+	a.framebuffer = ctx->framebuffer.ptr;
+	a.error_counter = static_cast<unsigned int*>(ctx->error_counter.ptr);
+	return a;
+}
 
 void stage_begin(SwCtx* ctx, int s)
 {
@@ -155,6 +187,7 @@ int ensure(SwCtx* ctx, DevBuf& b, size_t bytes)
 	if (b.ptr)
 	{
 		cudaError_t e = cudaStreamSynchronize(ctx->stream);
+		if (e == cudaSuccess && ctx->aux) e = cudaStreamSynchronize(ctx->aux);
 		if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamSynchronize");
 		cudaFree(b.ptr);
 		b.ptr = nullptr;
@@ -200,24 +233,25 @@ int staging_acquire(SwCtx* ctx, Staging& st, size_t bytes, void** host)
 	return SW_OK;
 }
 
-int staging_commit(SwCtx* ctx, Staging& st, void* dst, size_t bytes)
+int staging_commit(SwCtx* ctx, Staging& st, void* dst, size_t bytes, cudaStream_t stream = nullptr)
 {
 	if (bytes == 0) return SW_OK;
-	SW_CUDA(ctx, cudaMemcpyAsync(dst, st.host, bytes, cudaMemcpyHostToDevice, ctx->stream));
-	SW_CUDA(ctx, cudaEventRecord(st.done, ctx->stream));
+	if (!stream) stream = ctx->stream;
+	SW_CUDA(ctx, cudaMemcpyAsync(dst, st.host, bytes, cudaMemcpyHostToDevice, stream));
+	SW_CUDA(ctx, cudaEventRecord(st.done, stream));
 	st.pending = true;
 	return SW_OK;
 }
 
 // Copy `bytes` from host memory `src` into device buffer `dst` through a pinned staging buffer.
-int upload(SwCtx* ctx, Staging& st, void* dst, const void* src, size_t bytes)
+int upload(SwCtx* ctx, Staging& st, void* dst, const void* src, size_t bytes, cudaStream_t stream = nullptr)
 {
 	if (bytes == 0) return SW_OK;
 	void* h = nullptr;
 	int r = staging_acquire(ctx, st, bytes, &h);
 	if (r) return r;
 	std::memcpy(h, src, bytes);
-	return staging_commit(ctx, st, dst, bytes);
+	return staging_commit(ctx, st, dst, bytes, stream);
 }
 
 int upload_static(SwCtx* ctx, DevBuf& b, const void* src, size_t bytes)
@@ -339,6 +373,9 @@ int sw_create(const SwCreateInfo* info, SwCtx** out_ctx)
 	if (cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess)
 		return bail(SW_ERR_CUDA);
 	if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(SW_ERR_CUDA);
+	if (cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) != cudaSuccess) return bail(SW_ERR_CUDA);
+	for (cudaEvent_t* e : {&ctx->ev_setup, &ctx->ev_tiles, &ctx->ev_fork, &ctx->ev_join})
+		if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return bail(SW_ERR_CUDA);
 	if (cudaEventCreateWithFlags(&ctx->average_ready, cudaEventDisableTiming) != cudaSuccess) return bail(SW_ERR_CUDA);
 	if (cudaMallocHost(reinterpret_cast<void**>(&ctx->h_average), 4 * sizeof(float)) != cudaSuccess)
 		return bail(SW_ERR_CUDA);
@@ -373,13 +410,14 @@ int sw_destroy(SwCtx* ctx)
 	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
 	cudaSetDevice(ctx->device);
 	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+	if (ctx->aux) cudaStreamSynchronize(ctx->aux);
 	DevBuf* bufs[] = {&ctx->texels, &ctx->texture_mips, &ctx->emissive, &ctx->emissive_mips, &ctx->lightmaps,
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
-		&ctx->rdraws, &ctx->parts, &ctx->boxes, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
+		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->parts, &ctx->part_counts, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst};
 	for (DevBuf* b : bufs) release(*b);
 	Staging* st[] = {&ctx->stage_lights, &ctx->stage_surfaces, &ctx->stage_prefix, &ctx->stage_draws,
-		&ctx->stage_vertices, &ctx->stage_io};
+		&ctx->stage_vertices, &ctx->stage_draw_rows, &ctx->stage_io};
 	for (Staging* s : st)
 	{
 		if (s->host) cudaFreeHost(s->host);
@@ -387,12 +425,15 @@ int sw_destroy(SwCtx* ctx)
 	}
 	if (ctx->h_average) cudaFreeHost(ctx->h_average);
 	if (ctx->average_ready) cudaEventDestroy(ctx->average_ready);
-	for (int i = 0; i < 4; ++i)
+	for (int i = 0; i < 5; ++i)
 	{
 		if (ctx->t_begin[i]) cudaEventDestroy(ctx->t_begin[i]);
 		if (ctx->t_end[i]) cudaEventDestroy(ctx->t_end[i]);
 	}
 	if (ctx->stream) cudaStreamDestroy(ctx->stream);
+	if (ctx->aux) cudaStreamDestroy(ctx->aux);
+	for (cudaEvent_t e : {ctx->ev_setup, ctx->ev_tiles, ctx->ev_fork, ctx->ev_join})
+		if (e) cudaEventDestroy(e);
 	delete ctx;
 	return SW_OK;
 }
@@ -414,21 +455,21 @@ int sw_enable_timing(SwCtx* ctx, int enable)
 {
 	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
 	if (enable && !ctx->t_begin[0])
-		for (int i = 0; i < 4; ++i)
+		for (int i = 0; i < 5; ++i)
 		{
 			SW_CUDA(ctx, cudaEventCreate(&ctx->t_begin[i]));
 			SW_CUDA(ctx, cudaEventCreate(&ctx->t_end[i]));
 		}
 	ctx->timing = enable != 0;
-	for (int i = 0; i < 4; ++i) ctx->t_valid[i] = false;
+	for (int i = 0; i < 5; ++i) ctx->t_valid[i] = false;
 	return SW_OK;
 }
 
-int sw_get_timings(SwCtx* ctx, float out_ms[4])
+int sw_get_timings(SwCtx* ctx, float out_ms[5])
 {
 	if (!ctx || !out_ms) return SW_ERR_INVALID_ARGUMENT;
 	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-	for (int i = 0; i < 4; ++i)
+	for (int i = 0; i < 5; ++i)
 	{
 		out_ms[i] = 0.0f;
 		if (ctx->t_valid[i]) SW_CUDA(ctx, cudaEventElapsedTime(&out_ms[i], ctx->t_begin[i], ctx->t_end[i]));
@@ -455,6 +496,7 @@ int sw_frame_begin(SwCtx* ctx, const SwFrameParams* params, const SwLight* light
 	SW_CUDA(ctx, cudaSetDevice(ctx->device));
 	ctx->frame = *params;
 	ctx->num_lights = num_lights;
+	stage_begin(ctx, STAGE_FRAME);
 	int r = ensure(ctx, ctx->lights, std::max<size_t>(num_lights, 1) * sizeof(SwLight));
 	if (r) return r;
 	if ((r = upload(ctx, ctx->stage_lights, ctx->lights.ptr, lights, num_lights * sizeof(SwLight)))) return r;
@@ -585,6 +627,12 @@ int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, cons
 	if (!ctx || (num_draws && (!draws || !vertices))) return SW_ERR_INVALID_ARGUMENT;
 	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_submit_draws");
 	if (!ctx->arena_valid && num_draws) return fail(ctx, SW_ERR_STATE, "sw_submit_surfaces must precede sw_submit_draws");
+	int r;
+	DrawRows* rows = nullptr;
+	if ((r = staging_acquire(ctx, ctx->stage_draw_rows, std::max<size_t>(num_draws, 1) * sizeof(DrawRows),
+			 reinterpret_cast<void**>(&rows))))
+		return r;
+	uint64_t row_acc = 0;
 	for (uint32_t i = 0; i < num_draws; ++i)
 	{
 		const SwDrawCmd& d = draws[i];
@@ -596,16 +644,33 @@ int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, cons
 			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: bad mode/blend", i);
 		if (d.tex_size[0] == 0 || d.tex_size[1] == 0 || d.tex_offset + uint64_t(d.tex_size[0]) * d.tex_size[1] > ctx->arena_texels)
 			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: texture outside the surface arena", i);
+		int32_t y0;
+		uint32_t nrows;
+		draw_row_range(d, vertices, int32_t(ctx->frame.height), y0, nrows);
+		rows[i] = DrawRows{uint32_t(row_acc), y0, nrows, 0u};
+		row_acc += nrows;
+		if (row_acc > 0xFFFFFFFFull) return fail(ctx, SW_ERR_LIMIT, "too many draw rows in one frame");
 	}
-	int r;
 	if ((r = ensure(ctx, ctx->draws, std::max<size_t>(num_draws, 1) * sizeof(SwDrawCmd)))) return r;
 	if ((r = ensure(ctx, ctx->vertices, std::max<size_t>(num_vertices, 1) * sizeof(SwVertex16)))) return r;
+	if ((r = ensure(ctx, ctx->draw_rows, std::max<size_t>(num_draws, 1) * sizeof(DrawRows)))) return r;
 	if ((r = ensure(ctx, ctx->rdraws, std::max<size_t>(num_draws, 1) * sizeof(RasterDraw)))) return r;
-	if ((r = ensure(ctx, ctx->parts, std::max<size_t>(num_draws, 1) * SW_RASTER_MAX_PARTS * sizeof(RasterPart)))) return r;
+	if ((r = ensure(ctx, ctx->rows, std::max<size_t>(row_acc, 1) * sizeof(RasterRow)))) return r;
 	if ((r = ensure(ctx, ctx->boxes, std::max<size_t>(num_draws, 1) * sizeof(RasterBox)))) return r;
-	if ((r = upload(ctx, ctx->stage_draws, ctx->draws.ptr, draws, num_draws * sizeof(SwDrawCmd)))) return r;
-	if ((r = upload(ctx, ctx->stage_vertices, ctx->vertices.ptr, vertices, num_vertices * sizeof(SwVertex16)))) return r;
+	if ((r = ensure(ctx, ctx->parts, std::max<size_t>(num_draws, 1) * SW_RASTER_MAX_PARTS * sizeof(RasterPart)))) return r;
+	if ((r = ensure(ctx, ctx->part_counts, std::max<size_t>(num_draws, 1) * sizeof(uint32_t)))) return r;
+	// The draw uploads and the raster setup run on the auxiliary stream, beside the surface build; they
+	// first wait until the previous frame's tile pass has finished reading these buffers.
+	if (ctx->tiles_recorded) SW_CUDA(ctx, cudaStreamWaitEvent(ctx->aux, ctx->ev_tiles, 0));
+	if ((r = upload(ctx, ctx->stage_draws, ctx->draws.ptr, draws, num_draws * sizeof(SwDrawCmd), ctx->aux))) return r;
+	if ((r = upload(ctx, ctx->stage_vertices, ctx->vertices.ptr, vertices, num_vertices * sizeof(SwVertex16), ctx->aux)))
+		return r;
+	if ((r = staging_commit(ctx, ctx->stage_draw_rows, ctx->draw_rows.ptr, num_draws * sizeof(DrawRows), ctx->aux))) return r;
+	ctx->num_rows = row_acc;
 	ctx->num_draws = num_draws;
+	const RasterArgs a = raster_args(ctx);
+	if ((r = check_kernel(ctx, launch_raster_setup(a, ctx->aux), "raster setup"))) return r;
+	SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, ctx->aux));
 	ctx->draws_valid = true;
 	ctx->stats.draws += num_draws;
 	return SW_OK;
@@ -630,24 +695,14 @@ int sw_render(SwCtx* ctx, void* dst, uint32_t pitch, int dst_is_device)
 		ctx->fb_format = fmt;
 		ctx->fb_valid = true;
 	}
-	RasterArgs a;
-	a.draws = static_cast<const SwDrawCmd*>(ctx->draws.ptr);
-	a.vertices = static_cast<const SwVertex16*>(ctx->vertices.ptr);
-	a.num_draws = ctx->num_draws;
-	a.width = int32_t(w);
-	a.height = int32_t(h);
-	a.clear_background = ctx->frame.clear_background;
-	a.rdraws = static_cast<RasterDraw*>(ctx->rdraws.ptr);
-	a.parts = static_cast<RasterPart*>(ctx->parts.ptr);
-	a.boxes = static_cast<RasterBox*>(ctx->boxes.ptr);
-	a.arena = ctx->arena.ptr;
-	a.arena_texels = ctx->arena_texels;
-	a.framebuffer = ctx->framebuffer.ptr;
-	a.error_counter = static_cast<unsigned int*>(ctx->error_counter.ptr);
+	const RasterArgs a = raster_args(ctx);
+	SW_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_setup, 0));
 	stage_begin(ctx, STAGE_RASTER);
-	r = check_kernel(ctx, launch_raster(a, fmt, ctx->num_sms, ctx->stream), "raster");
+	r = check_kernel(ctx, launch_raster_tiles(a, fmt, ctx->num_sms, ctx->stream), "raster");
 	stage_end(ctx, STAGE_RASTER);
 	if (r) return r;
+	SW_CUDA(ctx, cudaEventRecord(ctx->ev_tiles, ctx->stream));
+	ctx->tiles_recorded = true;
 	ctx->frame_open = false;
 	if (dst) return copy_out(ctx, dst, pitch, dst_is_device, ctx->framebuffer.ptr, w, w, h, bpp);
 	return SW_OK;
@@ -755,11 +810,13 @@ int sw_postprocess(SwCtx* ctx, const SwPostConfig* config, float frame_duration_
 	a.dst = static_cast<uint32_t*>(out);
 	a.dst_pitch = out_pitch;
 	stage_begin(ctx, STAGE_POST);
-	r = check_kernel(ctx, launch_postprocess(a, ctx->num_sms, ctx->stream), "postprocess");
+	r = check_kernel(ctx, launch_postprocess(a, ctx->num_sms, ctx->stream, ctx->aux, ctx->ev_fork, ctx->ev_join),
+		"postprocess");
 	stage_end(ctx, STAGE_POST);
 	if (r) return r;
 	SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_average, ctx->average.ptr, 16, cudaMemcpyDeviceToHost, ctx->stream));
 	SW_CUDA(ctx, cudaEventRecord(ctx->average_ready, ctx->stream));
+	stage_end(ctx, STAGE_FRAME);
 	ctx->exposure_pending = true;
 	ctx->pending_config = *config;
 	ctx->pending_dt = frame_duration_s;

@@ -242,8 +242,8 @@ class GpuRenderer:
         self._check(self.lib.sw_enable_timing(self.ctx, 1 if on else 0), "sw_enable_timing")
 
     def timings(self):
-        """Device ms of the last surface build, raster, postprocess, upscale."""
-        t = (ctypes.c_float * 4)()
+        """Device ms of the last surface build, raster, postprocess, upscale and whole frame."""
+        t = (ctypes.c_float * 5)()
         self._check(self.lib.sw_get_timings(self.ctx, t), "sw_get_timings")
         return list(t)
 
