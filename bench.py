@@ -1,6 +1,7 @@
 """Benchmark of the GB300 Square-Wheel world-rendering path.
 
-python bench.py [--gpus N] [--steps K] [--warmup W] [--workload frame|surfaces] [--impl gpu|reference]
+python bench.py [--gpus N] [--steps K] [--warmup W] [--workload frame|surfaces|upscale] [--impl gpu|reference]
+                [--learn-steps S]
 
 Prints one JSON line (rank 0). A step is one pass of the hot path over one batch of synthetic input.
 
@@ -12,8 +13,12 @@ Workloads
       preparation, draw setup) is done before the timed region; `value` is frames/s of device time
       (sum of the three stages' CUDA-event times on the library's stream, inputs resident in HBM);
       `e2e` is frames/s through the C ABI from host memory (host work + uploads + GPU + 8.3 MB readback).
+      The same frames are then rendered the learned way (960x540 + learned 2x upscale, network trained
+      first for --learn-steps steps on two other maps) and reported under "learned" with their PSNR
+      against the plain frames.
   surfaces: 4,096 surfaces, sides log-uniform 4..512 texels, mips 0..3, directional lightmaps,
       built in one launch; value in Mtexels/s.
+  upscale: the learned 2x upscale alone (960x540 -> 1920x1080); value in frames/s, tensor roofline.
 Timing: W >= 3 untimed warm-up steps, K timed steps, each preceded by an L2 flush (a 512 MiB write)
 outside the timed span. Multi-GPU: independent replicas (different camera-path offsets), no collective;
 value = sum over ranks of frames / max-over-ranks time.
@@ -151,6 +156,79 @@ class FrameWorkload:
     def surface_bytes(self, f):
         return f["total_texels"] * (8 + 8) + self.lm_elements(f) * 40
 
+    def half_resolution_frames(self):
+        """Host work of the same camera poses at 960x540 (the learned path's render size)."""
+        opts = self.host.frame_options(W // 2, H // 2, self.abi.SW_PIXEL_C64, directional=True)
+        fr = self.host.Frame(self.scene)
+        out = []
+        for f in self.frames:
+            fr.prepare(f["index"], opts)
+            out.append(dict(index=f["index"], surfaces=fr.surfaces, draws=fr.draws, vertices=fr.vertices,
+                            lights=fr.lights, params=fr.params, total_texels=fr.total_texels))
+        return out
+
+
+UPSCALER_FLOPS = 2 * (W // 2) * (H // 2) * 9 * (3 * 32 + 32 * 32 + 32 * 32 + 32 * 12)  # algorithmic, per frame
+LEARN_MAPS = (21, 22)  # training maps: the full-size configuration with other seeds than the bench map
+
+
+def run_learned(args, work, r, plain_ldr, local):
+    """The learned form of the same frames: 960x540 render + bloom + tonemap, then the learned 2x
+    upscale (tcgen05 kernels) to 1920x1080, PSNR against the plain full-resolution frames of the same
+    steps. The network is trained first, on frame pairs the plain renderer draws from random poses of
+    two other maps of the same configuration (the bench map is not among them)."""
+    import torch
+    from sqwheel import abi, host, learned
+    t0 = time.perf_counter()
+    ups = learned.Upscaler(local, seed=1)
+    srcs = [learned.PairRenderer(host.Scene(**dict(host.FULL_MAP, seed=s, num_frames=1024)), (W // 2, H // 2),
+                                 device=local, hdr=True) for s in LEARN_MAPS]
+    learned.train(ups, srcs, args.learn_steps, crops_per_step=16, lr=1e-3, pool=24, seed=5)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    for src in srcs:
+        src.close()
+    lo_frames = work.half_resolution_frames()
+    r.attach_upscaler(ups)
+    r.set_exposure(1.0)
+    stream = torch.cuda.ExternalStream(r.stream_handle())
+    dev = f"cuda:{local}"
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    lo = torch.empty((H // 2, W // 2), dtype=torch.int32, device=dev)
+    out = torch.empty((H, W), dtype=torch.int32, device=dev)
+    tmp = torch.empty((H, W), dtype=torch.int32, device=dev)
+    totals = {"surf": 0.0, "raster": 0.0, "post": 0.0, "upscale": 0.0}
+    psnr = {"learned": [], "avg2x": [], "nearest": []}
+    for step, f in enumerate(lo_frames):
+        timed = step >= args.warmup
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        r.frame_begin(f["params"], f["lights"])
+        r.submit_surfaces(f["surfaces"], f["total_texels"])
+        r.submit_draws(f["draws"], f["vertices"])
+        r.render()
+        r.postprocess(work.config, 1.0 / 60.0, (1.0, 1.0, 1.0), device_ptr=lo.data_ptr(), pitch=W // 2)
+        r.upscale_device(abi.SW_UPSCALE_LEARNED, 2, lo.data_ptr(), out.data_ptr(), W, H, W)
+        t = r.timings()
+        if not timed:
+            continue
+        for k, i in (("surf", 0), ("raster", 1), ("post", 2), ("upscale", 3)):
+            totals[k] += t[i]
+        psnr["learned"].append(ups.psnr(out, plain_ldr[step], stream=r.stream_handle()))
+        for name, mode in (("avg2x", abi.SW_UPSCALE_AVG2X), ("nearest", abi.SW_UPSCALE_NEAREST)):
+            r.upscale_device(mode, 2, lo.data_ptr(), tmp.data_ptr(), W, H, W)
+            psnr[name].append(ups.psnr(tmp, plain_ldr[step], stream=r.stream_handle()))
+    r.attach_upscaler(None)
+    ups.close()
+    s = args.steps
+    ms = sum(totals.values()) / s
+    up_ms = totals["upscale"] / s
+    return {
+        "ms": ms, "upscale_ms": up_ms, "train_s": train_s,
+        "stages_ms": {k: round(v / s, 4) for k, v in totals.items()},
+        "psnr": psnr,
+    }
+
 
 def run_frame_gpu(args, world, rank, local):
     import torch
@@ -162,7 +240,7 @@ def run_frame_gpu(args, world, rank, local):
     r.enable_timing(True)
     stream = torch.cuda.ExternalStream(r.stream_handle())
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
-    ldr = torch.empty((H, W), dtype=torch.int32, device=f"cuda:{local}")
+    ldr_frames = torch.empty((len(work.frames), H, W), dtype=torch.int32, device=f"cuda:{local}")
     totals = {"surf": 0.0, "raster": 0.0, "post": 0.0}
     frame_span = 0.0
     texels = 0
@@ -182,7 +260,7 @@ def run_frame_gpu(args, world, rank, local):
             r.submit_surfaces(f["surfaces"], f["total_texels"])
             r.submit_draws(f["draws"], f["vertices"])
             r.render()
-            r.postprocess(work.config, 1.0 / 60.0, (1.0, 1.0, 1.0), device_ptr=ldr.data_ptr(), pitch=W)
+            r.postprocess(work.config, 1.0 / 60.0, (1.0, 1.0, 1.0), device_ptr=ldr_frames[step].data_ptr(), pitch=W)
             t = r.timings()
             if timed:
                 totals["surf"] += t[0]
@@ -191,7 +269,7 @@ def run_frame_gpu(args, world, rank, local):
                 frame_span += t[4]
                 texels += f["total_texels"]
                 surf_bytes += work.surface_bytes(f)
-                launches += 1 + 2 + 5
+                launches += 1 + 3 + 5  # surfaces; raster walk, rows, tiles; postprocess (5 kernels)
             if step == args.warmup - 1:
                 pix_before = r.stats().pixel_writes
         pix_writes = r.stats().pixel_writes - pix_before
@@ -227,6 +305,10 @@ def run_frame_gpu(args, world, rank, local):
     hr.close()
     e2e_val = 1e3 / statistics.median(e2e_ms)
 
+    lr = run_learned(args, work, r, ldr_frames, local) if args.learn_steps > 0 else None
+    if lr is not None:
+        launches += args.steps * (1 + 3 + 5 + 5)  # half-resolution frame + convert and four convolutions
+
     peak, peak_kind = peaks()
     s = args.steps
     stage_bytes = {
@@ -258,7 +340,7 @@ def run_frame_gpu(args, world, rank, local):
                        "l2": "flushed (512 MiB write) before every timed step",
                        "timing": "sum of per-stage CUDA-event device times (surfaces, raster, postprocess)",
                        "frame_span_ms": round(frame_span / s, 4),
-                       "learned_upscale": "not in this measurement", "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}"},
             "stages": stages,
             "roofline": {"bound": "hbm", "kernel": kernel_names[dom], "achieved": stages[dom]["GB/s"], "peak": peak,
                          "unit": "GB/s", "frac": stages[dom]["frac_of_measured_hbm"],
@@ -270,9 +352,46 @@ def run_frame_gpu(args, world, rank, local):
             "clocks": clocks.summary(),
             "gpu_launches": launches,
         }
+        if lr is not None:
+            out_line["learned"] = learned_summary(lr, frame_ms, args)
         print(json.dumps(out_line), flush=True)
     r.close()
     return out_line
+
+
+def learned_summary(lr, plain_ms, args):
+    p = lr["psnr"]
+    tf = UPSCALER_FLOPS / (lr["upscale_ms"] / 1e3) / 1e12
+    peak = None
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        peak = float(json.load(open(pp)).get("bf16_tflops", 0)) or None
+    kind = "measured bf16_tflops (burst)"
+    if peak is None:
+        peak, kind = 1900.0, "fallback"
+    n = len(p["learned"])
+    # with the quality monitor: every 16th frame also renders the plain frame for the PSNR check
+    check_ms = lr["ms"] + plain_ms / 16.0
+    return {
+        "what": "960x540 render + bloom + tonemap, learned 2x upscale to 1920x1080 (BF16 tcgen05, FP32 accumulate), "
+                "same frames as the plain measurement",
+        "frames_per_s": round(1e3 / lr["ms"], 2), "ms_per_frame": round(lr["ms"], 4),
+        "speedup_vs_plain": round(plain_ms / lr["ms"], 3),
+        "with_psnr_check_every_16th_frame": {"frames_per_s": round(1e3 / check_ms, 2),
+                                             "speedup_vs_plain": round(plain_ms / check_ms, 3)},
+        "stages_ms": lr["stages_ms"],
+        "psnr_db": {"learned_mean": round(float(np.mean(p["learned"])), 3),
+                    "learned_min": round(float(np.min(p["learned"])), 3),
+                    "avg2x_mean": round(float(np.mean(p["avg2x"])), 3),
+                    "nearest_mean": round(float(np.mean(p["nearest"])), 3),
+                    "frames_at_or_above_38db": f"{sum(x >= 38.0 for x in p['learned'])}/{n}"},
+        "upscaler_roofline": {"bound": "tensor", "kernel": "conv_kernel (4 launches) + convert_input_kernel",
+                              "achieved": round(tf, 1), "peak": peak, "unit": "TFLOP/s", "frac": round(tf / peak, 4),
+                              "peak_source": kind, "algorithmic_flops_per_launch": UPSCALER_FLOPS},
+        "train": {"steps": args.learn_steps, "crops_per_step": 16, "crop": "128x64 half-resolution pixels",
+                  "maps": f"full-size configuration, seeds {list(LEARN_MAPS)} (bench map: seed 2)",
+                  "seconds": round(lr["train_s"], 2)},
+    }
 
 
 def cpu_frame_baseline(work, max_frames=4):
@@ -391,6 +510,99 @@ def cpu_surfaces_baseline(work):
 
 
 # ---------------------------------------------------------------------------------------------------------
+# upscale workload (the learned upscaler alone)
+
+def bf16_peak():
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        v = float(json.load(open(pp)).get("bf16_tflops", 0))
+        if v > 0:
+            return v, "measured bf16_tflops (burst)"
+    return 1900.0, "fallback"
+
+
+def run_upscale_gpu(args, world, rank, local):
+    """Learned 2x upscale of a 960x540 Color32 frame to 1920x1080: convert + four tcgen05 convolution
+    launches per step, inputs resident in HBM, L2 flushed between steps."""
+    import ctypes
+
+    import torch
+    from sqwheel import abi, gpu, host, learned
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+    # a tonemapped half-resolution frame of the full-size map as input
+    src = learned.PairRenderer(host.Scene(**host.FULL_MAP), (W // 2, H // 2), device=local, hdr=True)
+    lo = torch.empty((H // 2, W // 2), dtype=torch.int32, device=dev)
+    src.render_lo(37 + rank, lo)
+    src.sync()
+    src.close()
+    ups = learned.Upscaler(local, seed=1)
+    hi = torch.empty((H, W), dtype=torch.int32, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    # a stream of our own: its handle is non-zero, so the upscaler runs on it (NULL selects the
+    # upscaler's internal stream) and the events bracket exactly its kernels
+    st = torch.cuda.Stream(device=dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(st):
+        for _ in range(args.warmup):
+            flush.fill_(1.0)
+            ups.infer(lo, hi, stream=st.cuda_stream)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks, torch.cuda.stream(st):
+        for i in range(args.steps):
+            flush.fill_(1.0)
+            ev[i][0].record(st)
+            ups.infer(lo, hi, stream=st.cuda_stream)
+            ev[i][1].record(st)
+        torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    if world > 1:
+        tt = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    # e2e: through the C ABI (sw_upscale, learned mode) from and to host memory
+    r = gpu.GpuRenderer(host.Scene(**host.SMALL_MAP).static_data(), device=local)
+    r.attach_upscaler(ups)
+    lo_h = lo.cpu().numpy().view(np.uint32).copy()
+    out_h = np.zeros((H, W), np.uint32)
+    e2e = []
+    for i in range(max(4, min(args.steps, 16))):
+        t0 = time.perf_counter()
+        r.upscale(abi.SW_UPSCALE_LEARNED, 2, lo_h, out_h)
+        if i:
+            e2e.append(time.perf_counter() - t0)
+    r.attach_upscaler(None)
+    r.close()
+    peak, kind = bf16_peak()
+    tf = UPSCALER_FLOPS / (ms / 1e3) / 1e12
+    if rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import upscaler_oracle
+        p = ups.params()
+        t0 = time.perf_counter()
+        upscaler_oracle.infer(p, lo_h[:135])
+        cpu_s = (time.perf_counter() - t0) * 4
+        print(json.dumps({
+            "metric": METRIC, "value": round(world * 1e3 / ms, 2), "unit": "frames/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic (seeded)",
+            "config": {"workload": "learned 2x upscale 960x540 -> 1920x1080 (4-layer 3x3 CNN, 32 channels, pixel shuffle)",
+                       "input": "tonemapped 960x540 frame of the 64-room map", "weights": "seeded initialisation",
+                       "l2": "flushed (512 MiB write) before every timed step", "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "tensor", "kernel": "conv_kernel (4 launches) + convert_input_kernel", "achieved": round(tf, 1),
+                         "peak": peak, "unit": "TFLOP/s", "frac": round(tf / peak, 4), "peak_source": kind,
+                         "algorithmic_flops_per_launch": UPSCALER_FLOPS, "traffic": None},
+            "cpu_baseline": {"value": round(1.0 / cpu_s, 4), "unit": "frames/s", "cores": 1, "kind": "port",
+                             "sample": "a quarter frame (135 of 540 rows) through the numpy FP32 oracle, scaled x4"},
+            "e2e": {"value": round(1.0 / statistics.median(e2e), 2), "unit": "frames/s",
+                    "h2d_bytes_per_step": int(lo_h.nbytes), "d2h_bytes_per_step": int(out_h.nbytes)},
+            "clocks": clocks.summary(), "gpu_launches": 5 * args.steps}), flush=True)
+    ups.close()
+
+
+# ---------------------------------------------------------------------------------------------------------
 
 def run_reference(args, world, rank):
     """The reference's CPU path restated in C++ (the Rust reference cannot be built here), all host
@@ -432,8 +644,10 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="frame", choices=["frame", "surfaces"])
+    ap.add_argument("--workload", default="frame", choices=["frame", "surfaces", "upscale"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--learn-steps", type=int, default=2000,
+                    help="training steps of the learned upscaler before its measurement (0: skip it)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()
@@ -448,6 +662,8 @@ def main():
     try:
         if args.workload == "surfaces":
             run_surfaces_gpu(args, world, rank, local)
+        elif args.workload == "upscale":
+            run_upscale_gpu(args, world, rank, local)
         else:
             run_frame_gpu(args, world, rank, local)
     finally:

@@ -211,6 +211,7 @@ typedef struct SwPostConfig {
 typedef enum SwUpscaleMode {
 	SW_UPSCALE_NEAREST = 0, /* FrameUpscaler::perform_upscale_impl::<SCALE> */
 	SW_UPSCALE_AVG2X = 1,   /* FrameUpscaler::perform_upscale_2x_linear */
+	SW_UPSCALE_LEARNED = 2, /* no reference counterpart: learned 2x upscaler (swlearn.h), scale must be 2 */
 } SwUpscaleMode;
 
 typedef struct SwCtx SwCtx;

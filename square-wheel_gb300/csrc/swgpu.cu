@@ -13,6 +13,8 @@
 // validated on the host before launch so that no kernel can read outside its buffers.
 #include "sw_kernels.cuh"
 
+#include "../../include/swlearn.h"
+
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -94,6 +96,7 @@ struct SwCtx
 
 	// upscale scratch (src/dst copies for host buffers)
 	DevBuf up_src, up_dst;
+	SwUpscaler* learned = nullptr; // sw_set_learned_upscaler
 
 	SwStats stats{};
 
@@ -828,7 +831,13 @@ int sw_upscale(SwCtx* ctx, uint32_t mode, uint32_t scale, const void* src, int s
 	uint32_t dst_height, uint32_t dst_pitch, int dst_is_device)
 {
 	if (!ctx || !src || !dst || dst_pitch < dst_width) return SW_ERR_INVALID_ARGUMENT;
-	if (mode == SW_UPSCALE_AVG2X)
+	if (mode == SW_UPSCALE_LEARNED)
+	{
+		if (!ctx->learned) return fail(ctx, SW_ERR_STATE, "no learned upscaler attached (sw_set_learned_upscaler)");
+		if (scale != 2 || (dst_width & 1) || (dst_height & 1))
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "the learned upscaler doubles both sides (scale 2, even size)");
+	}
+	if (mode == SW_UPSCALE_AVG2X || mode == SW_UPSCALE_LEARNED)
 		scale = 2;
 	else if (mode != SW_UPSCALE_NEAREST || scale < 1 || scale > 6)
 		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "bad upscale mode/scale");
@@ -845,19 +854,35 @@ int sw_upscale(SwCtx* ctx, uint32_t mode, uint32_t scale, const void* src, int s
 	}
 	void* d = dst;
 	uint32_t dp = dst_pitch;
-	if (!dst_is_device)
+	if (!dst_is_device || (mode == SW_UPSCALE_LEARNED && ((dst_pitch & 1) || (reinterpret_cast<uintptr_t>(dst) & 7))))
 	{
 		if ((r = ensure(ctx, ctx->up_dst, size_t(dst_width) * dst_height * 4))) return r;
 		d = ctx->up_dst.ptr;
 		dp = dst_width;
 	}
 	stage_begin(ctx, STAGE_UPSCALE);
-	r = check_kernel(ctx,
-		launch_upscale(mode, scale, static_cast<const uint32_t*>(s), static_cast<uint32_t*>(d), dst_width, dst_height, dp, ctx->stream),
-		"upscale");
+	if (mode == SW_UPSCALE_LEARNED)
+	{
+		r = sw_upscaler_infer(ctx->learned, static_cast<const uint32_t*>(s), sw, sh, sw, static_cast<uint32_t*>(d), dp, ctx->stream);
+		if (r) r = fail(ctx, r, "learned upscale: %s", sw_upscaler_last_error(ctx->learned));
+	}
+	else
+		r = check_kernel(ctx,
+			launch_upscale(mode, scale, static_cast<const uint32_t*>(s), static_cast<uint32_t*>(d), dst_width, dst_height, dp,
+				ctx->stream),
+			"upscale");
 	stage_end(ctx, STAGE_UPSCALE);
+	if (!r && dst_is_device && d != dst)
+		r = copy_out(ctx, dst, dst_pitch, 1, d, dp, dst_width, dst_height, 4);
 	if (r) return r;
 	if (!dst_is_device) return copy_out(ctx, dst, dst_pitch, 0, d, dp, dst_width, dst_height, 4);
+	return SW_OK;
+}
+
+int sw_set_learned_upscaler(SwCtx* ctx, SwUpscaler* ups)
+{
+	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
+	ctx->learned = ups;
 	return SW_OK;
 }
 

@@ -22,7 +22,7 @@ SW_PIXEL_C64 = 1
 
 SW_BLEND_NONE, SW_BLEND_AVERAGE, SW_BLEND_ADDITIVE, SW_BLEND_ALPHA_TEST, SW_BLEND_ALPHA_BLEND = range(5)
 SW_RASTER_FULL_PERSPECTIVE, SW_RASTER_LINE_Z_CORRECTED, SW_RASTER_AFFINE = range(3)
-SW_UPSCALE_NEAREST, SW_UPSCALE_AVG2X = range(2)
+SW_UPSCALE_NEAREST, SW_UPSCALE_AVG2X, SW_UPSCALE_LEARNED = range(3)
 
 SW_TEX_HAS_NORMAL_MAP = 1
 SW_TEX_HAS_NON_ONE_ROUGHNESS = 2

@@ -23,7 +23,12 @@ EXPORTED = [
     "sw_submit_draws",
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
-    "sw_postprocess_noalloc",
+    "sw_postprocess_noalloc", "sw_set_learned_upscaler",
+    # learned upscaler (include/swlearn.h)
+    "sw_upscaler_create", "sw_upscaler_destroy", "sw_upscaler_last_error", "sw_upscaler_get_params",
+    "sw_upscaler_set_params", "sw_upscaler_gradients", "sw_upscaler_train_step", "sw_upscaler_steps",
+    "sw_upscaler_infer", "sw_upscaler_psnr", "sw_upscaler_save", "sw_upscaler_load",
+    "sw_monitor_init", "sw_monitor_plan", "sw_monitor_report",
 ]
 
 _lib = None
@@ -65,6 +70,22 @@ def load_library(path=LIB_PATH):
         "sw_postprocess_noalloc": ([vp, u32, u32, vp, f32, vp, vp, u32, vp, vp], i32),
         "sw_enable_timing": ([vp, i32], i32),
         "sw_get_timings": ([vp, vp], i32),
+        "sw_set_learned_upscaler": ([vp, vp], i32),
+        "sw_upscaler_create": ([i32, u64, ctypes.POINTER(vp)], i32),
+        "sw_upscaler_destroy": ([vp], i32),
+        "sw_upscaler_last_error": ([vp], ctypes.c_char_p),
+        "sw_upscaler_get_params": ([vp, vp, u32], i32),
+        "sw_upscaler_set_params": ([vp, vp, u32], i32),
+        "sw_upscaler_gradients": ([vp, vp, u32, vp, ctypes.POINTER(f32)], i32),
+        "sw_upscaler_train_step": ([vp, vp, u32, f32, ctypes.POINTER(f32)], i32),
+        "sw_upscaler_steps": ([vp, ctypes.POINTER(u64)], i32),
+        "sw_upscaler_infer": ([vp, vp, u32, u32, u32, vp, u32, vp], i32),
+        "sw_upscaler_psnr": ([vp, vp, u32, vp, u32, u32, u32, vp, ctypes.POINTER(ctypes.c_double)], i32),
+        "sw_upscaler_save": ([vp, ctypes.c_char_p], i32),
+        "sw_upscaler_load": ([vp, ctypes.c_char_p], i32),
+        "sw_monitor_init": ([vp, u32, f32, u32], i32),
+        "sw_monitor_plan": ([vp, ctypes.POINTER(u32)], i32),
+        "sw_monitor_report": ([vp, ctypes.c_double], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -218,6 +239,11 @@ class GpuRenderer:
     def upscale_device(self, mode, scale, src_ptr, dst_ptr, width, height, pitch):
         self._check(self.lib.sw_upscale(self.ctx, mode, scale, ctypes.c_void_p(src_ptr), 1, ctypes.c_void_p(dst_ptr),
                                         width, height, pitch, 1), "sw_upscale")
+
+    def attach_upscaler(self, ups):
+        """Use a learned upscaler (sqwheel.learned.Upscaler, or None) for SW_UPSCALE_LEARNED."""
+        self._check(self.lib.sw_set_learned_upscaler(self.ctx, ups.h if ups is not None else None),
+                    "sw_set_learned_upscaler")
 
     def read_surfaces(self, total_texels, pixel_format):
         dt = np.uint64 if pixel_format == abi.SW_PIXEL_C64 else np.uint32

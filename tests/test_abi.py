@@ -15,8 +15,8 @@ def declared_functions(header):
 
 
 def test_header_symbols_exported(built_libs):
-    names = declared_functions("swgpu.h")
-    assert len(names) >= 15
+    names = sorted(declared_functions("swgpu.h") + declared_functions("swlearn.h"))
+    assert len(names) >= 30
     lib = ctypes.CDLL(gpu.LIB_PATH)
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, f"not exported: {missing}"
