@@ -302,10 +302,57 @@ int sw_get_timings(SwCtx* ctx, float out_ms[5]);
 /* The context's CUDA stream (cudaStream_t) for callers that order their own work after the frame. */
 int sw_get_stream(SwCtx* ctx, void** out_stream);
 
+/* ---- whole frame in one call, as one CUDA graph (no reference counterpart) ----
+ * Everything one frame of Renderer::prepare_frame + draw_frame + Postprocessor::perform_postprocessing
+ * (renderer.rs:61-124, postprocessor.rs:68-204) hands to the GPU: sw_draw_frame is the same as
+ * sw_frame_begin + sw_submit_surfaces + sw_submit_draws + sw_render (+ sw_postprocess), with the same
+ * validation, results and exposure state, but the host prepares all of the frame's arrays first and the
+ * device work (uploads, surface build, raster setup and tiles, postprocess, exposure readback) is
+ * captured into one CUDA graph: the first frame instantiates it, later frames update it in place and
+ * replay it, so the kernels run back to back without host submission gaps. */
+typedef struct SwFrameInput {
+	SwFrameParams params;
+	uint32_t num_lights;
+	const SwLight* lights;
+	const SwSurfaceDesc* surfaces;
+	uint64_t total_texels;
+	uint32_t num_surfaces;
+	uint32_t num_draws;
+	const SwDrawCmd* draws;
+	const SwVertex16* vertices;
+	uint32_t num_vertices;
+	uint32_t postprocess;      /* 1: postprocess the colour64 frame to Color32 into dst; 0: stop after rasterisation */
+	SwPostConfig post;
+	float frame_duration_s;
+	float color_modulate[3];
+	void* dst;                 /* postprocess: Color32 output; otherwise the frame (pixel_format); may be NULL */
+	uint32_t dst_pitch;        /* pixels */
+	int32_t dst_is_device;
+} SwFrameInput;
+int sw_draw_frame(SwCtx* ctx, const SwFrameInput* frame);
+/* Graph capture of sw_draw_frame: on (default) or off (the same work launched directly). */
+int sw_set_frame_graph(SwCtx* ctx, int enable);
+
+/* ---- launch configuration (no reference counterpart) ---- */
+#define SW_RASTER_TILE_VARIANTS 5
+typedef struct SwTuning {
+	/* tile shape of the tile pass, 256 threads each: 0 = 64x16 pixels (4-pixel strips), 1 = 32x32 (4),
+	 * 2 = 128x8 (4), 3 = 64x32 (8-pixel strips), 4 = 32x16 (2-pixel strips); all give the same frame */
+	uint32_t raster_tile;
+	/* persistent grid of the surface build: blocks per SM, 1..64 */
+	uint32_t surface_blocks_per_sm;
+} SwTuning;
+int sw_set_tuning(SwCtx* ctx, const SwTuning* tuning);
+int sw_get_tuning(SwCtx* ctx, SwTuning* out_tuning);
+/* Autotuner: times `reps` replays of the sample frame (sw_draw_frame) for every raster tile shape and a
+ * set of surface grid sizes, keeps the fastest configuration in the context and returns it with its
+ * median device time per frame in ms. The exposure state is restored afterwards. */
+int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning* out_best, float* out_best_ms);
+
 /* sizeof() of the ABI structs in this order: SwCreateInfo, SwTextureMip, SwEmissiveMip,
  * SwDirectionalLightmapElement, SwLight, SwSurfaceDesc, SwVertex16, SwDrawCmd, SwFrameParams,
- * SwPostConfig, SwStats. Writes min(count, 11) values; returns the number of structs (11).
- * Needs no GPU: bindings use it to check their mirrored layouts. */
+ * SwPostConfig, SwStats, SwFrameInput, SwTuning. Writes min(count, 13) values; returns the number of
+ * structs (13). Needs no GPU: bindings use it to check their mirrored layouts. */
 int sw_abi_layout(uint32_t* sizes, uint32_t count);
 
 /* Diagnostics: copy the frame's surface arena (total_texels of sw_submit_surfaces) to host memory. */

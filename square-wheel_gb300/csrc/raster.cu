@@ -403,14 +403,21 @@ __device__ __forceinline__ uint64_t pixel_address(const RasterRow& r, uint32_t m
 	return uint64_t(int64_t(wadd(t0 >> 16, wmul(t1 >> 16, int32_t(tex_w)))));
 }
 
-constexpr int TILE_W = 64;  // tile: 64 x 16 pixels, 256 threads, each thread a 1 x 4 strip of a row
-constexpr int TILE_H = 16;
-constexpr int STRIP = 4;
-constexpr int BATCH = 32;   // draws whose tile rows are staged in shared memory at a time
+constexpr int BATCH = 32; // draws whose tile rows are staged in shared memory at a time
 
-template <class P>
+// Tile shapes of the tile pass (the autotuner's choice, SwTuning.raster_tile): TILE_W x TILE_H pixels,
+// 256 threads, each thread a 1 x STRIP strip of one row. Every shape gives the same frame.
+struct TileShape
+{
+	int w, h, strip;
+};
+constexpr TileShape TILE_SHAPES[SW_RASTER_TILE_VARIANTS] = {{64, 16, 4}, {32, 32, 4}, {128, 8, 4}, {64, 32, 8}, {32, 16, 2}};
+
+template <class P, int TILE_W, int TILE_H, int STRIP>
 __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 {
+	static_assert((TILE_W / STRIP) * TILE_H == 256, "256 threads per tile");
+	constexpr int TPR = TILE_W / STRIP; // threads per tile row
 	typedef typename P::T T;
 	__shared__ uint32_t s_warp_counts[8];
 	__shared__ RasterDraw s_rd[256];
@@ -421,8 +428,8 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 	const int tx0 = int(blockIdx.x % tiles_x) * TILE_W;
 	const int ty0 = int(blockIdx.x / tiles_x) * TILE_H;
 	const int tid = threadIdx.x;
-	const int ly = tid >> 4;
-	const int xb = tx0 + (tid & 15) * STRIP; // first pixel of this thread's strip
+	const int ly = tid / TPR;
+	const int xb = tx0 + (tid % TPR) * STRIP; // first pixel of this thread's strip
 	const int y = ty0 + ly;
 	const bool row_valid = y < a.height;
 	const int tx1 = min(tx0 + TILE_W, a.width), ty1 = min(ty0 + TILE_H, a.height);
@@ -558,15 +565,32 @@ int launch_raster_setup(const RasterArgs& args, cudaStream_t stream)
 	return int(cudaGetLastError());
 }
 
-int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream)
+namespace
 {
-	const unsigned tiles = unsigned(((args.width + TILE_W - 1) / TILE_W) * ((args.height + TILE_H - 1) / TILE_H));
-	if (tiles == 0) return 0;
+template <int V>
+void launch_tiles_variant(const RasterArgs& args, uint32_t pixel_format, cudaStream_t stream)
+{
+	constexpr TileShape t = TILE_SHAPES[V];
+	const unsigned tiles = unsigned(((args.width + t.w - 1) / t.w) * ((args.height + t.h - 1) / t.h));
+	if (tiles == 0) return;
 	if (pixel_format == SW_PIXEL_C64)
-		raster_tiles_kernel<PixC64><<<tiles, 256, 0, stream>>>(args);
+		raster_tiles_kernel<PixC64, t.w, t.h, t.strip><<<tiles, 256, 0, stream>>>(args);
 	else
-		raster_tiles_kernel<PixC32><<<tiles, 256, 0, stream>>>(args);
-	(void)num_sms;
+		raster_tiles_kernel<PixC32, t.w, t.h, t.strip><<<tiles, 256, 0, stream>>>(args);
+}
+} // namespace
+
+int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, uint32_t variant, cudaStream_t stream)
+{
+	switch (variant)
+	{
+	case 0: launch_tiles_variant<0>(args, pixel_format, stream); break;
+	case 1: launch_tiles_variant<1>(args, pixel_format, stream); break;
+	case 2: launch_tiles_variant<2>(args, pixel_format, stream); break;
+	case 3: launch_tiles_variant<3>(args, pixel_format, stream); break;
+	case 4: launch_tiles_variant<4>(args, pixel_format, stream); break;
+	default: return int(cudaErrorInvalidValue);
+	}
 	return int(cudaGetLastError());
 }
 

@@ -421,14 +421,14 @@ void make_surface_gpu(const SwSurfaceDesc& d, const SwTextureMip* tex, const SwE
 	o.out_offset = d.out_offset;
 }
 
-int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream)
+int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, int blocks_per_sm, cudaStream_t stream)
 {
 	if (args.total_work == 0) return 0;
 	const int threads = 256;
 	uint64_t blocks_needed = (args.total_work + threads - 1) / threads;
-	// Up to 8 waves of resident blocks: small frames get one texel per thread (latency hidden by
-	// parallelism), large batches stride.
-	uint64_t blocks_max = uint64_t(num_sms) * 3 * 8;
+	// At most blocks_per_sm blocks per SM (several waves of resident blocks): small frames get one
+	// texel per thread (latency hidden by parallelism), large batches stride.
+	uint64_t blocks_max = uint64_t(num_sms) * uint64_t(blocks_per_sm);
 	unsigned blocks = unsigned(blocks_needed < blocks_max ? blocks_needed : blocks_max);
 	if (pixel_format == SW_PIXEL_C64)
 	{

@@ -58,7 +58,8 @@ struct SurfaceKernelArgs
 // contraction).
 void make_surface_gpu(const SwSurfaceDesc& d, const SwTextureMip* tex, const SwEmissiveMip* em, SurfaceGpu& out);
 
-int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream);
+// Persistent grid of at most num_sms * blocks_per_sm blocks of 256 threads.
+int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, int blocks_per_sm, cudaStream_t stream);
 
 // ---- rasteriser ----
 
@@ -141,7 +142,8 @@ struct RasterArgs
 
 // Edge walk + row setup (raster_walk, raster_rows), then the tile pass (raster_tiles).
 int launch_raster_setup(const RasterArgs& args, cudaStream_t stream);
-int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, int num_sms, cudaStream_t stream);
+// variant: tile shape index (< SW_RASTER_TILE_VARIANTS, see SwTuning); every variant gives the same frame.
+int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, uint32_t variant, cudaStream_t stream);
 
 // Host side: rows [y0, y0 + nrows) a draw can cover (from its vertices).
 void draw_row_range(const SwDrawCmd& d, const SwVertex16* vertices, int32_t height, int32_t& y0, uint32_t& nrows);

@@ -100,6 +100,17 @@ struct SwCtx
 
 	SwStats stats{};
 
+	// Launch configuration (sw_set_tuning / sw_autotune).
+	SwTuning tuning{0u, 24u};
+
+	// Whole-frame CUDA graph (sw_draw_frame): double-buffered pinned staging of all per-frame arrays,
+	// the instantiated graph, updated in place from each frame's capture.
+	bool graph_enabled = true;
+	bool capturing = false; // stage timing events are not recorded inside a capture
+	cudaGraphExec_t gexec = nullptr;
+	Staging gstage[2];
+	uint32_t gset = 0;
+
 	// Optional per-stage device timing (sw_enable_timing).
 	bool timing = false;
 	cudaEvent_t t_begin[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -144,11 +155,11 @@ RasterArgs raster_args(SwCtx* ctx)
 
 void stage_begin(SwCtx* ctx, int s)
 {
-	if (ctx->timing) cudaEventRecord(ctx->t_begin[s], ctx->stream);
+	if (ctx->timing && !ctx->capturing) cudaEventRecord(ctx->t_begin[s], ctx->stream);
 }
 void stage_end(SwCtx* ctx, int s)
 {
-	if (ctx->timing)
+	if (ctx->timing && !ctx->capturing)
 	{
 		cudaEventRecord(ctx->t_end[s], ctx->stream);
 		ctx->t_valid[s] = true;
@@ -419,8 +430,9 @@ int sw_destroy(SwCtx* ctx)
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->parts, &ctx->part_counts, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst};
 	for (DevBuf* b : bufs) release(*b);
+	if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
 	Staging* st[] = {&ctx->stage_lights, &ctx->stage_surfaces, &ctx->stage_prefix, &ctx->stage_draws,
-		&ctx->stage_vertices, &ctx->stage_draw_rows, &ctx->stage_io};
+		&ctx->stage_vertices, &ctx->stage_draw_rows, &ctx->stage_io, &ctx->gstage[0], &ctx->gstage[1]};
 	for (Staging* s : st)
 	{
 		if (s->host) cudaFreeHost(s->host);
@@ -525,7 +537,9 @@ static int launch_surfaces(SwCtx* ctx)
 	for (int i = 0; i < 3; ++i) a.cam_pos[i] = ctx->frame.cam_pos[i];
 	a.arena = ctx->arena.ptr;
 	stage_begin(ctx, STAGE_SURFACES);
-	int r = check_kernel(ctx, launch_surface_build(a, ctx->frame.pixel_format, ctx->num_sms, ctx->stream), "surface build");
+	int r = check_kernel(ctx,
+		launch_surface_build(a, ctx->frame.pixel_format, ctx->num_sms, int(ctx->tuning.surface_blocks_per_sm), ctx->stream),
+		"surface build");
 	stage_end(ctx, STAGE_SURFACES);
 	if (r) return r;
 	ctx->arena_valid = true;
@@ -534,21 +548,17 @@ static int launch_surfaces(SwCtx* ctx)
 	return SW_OK;
 }
 
-int sw_submit_surfaces(SwCtx* ctx, const SwSurfaceDesc* surfaces, uint32_t num_surfaces, uint64_t total_texels)
+namespace
 {
-	if (!ctx || (num_surfaces && !surfaces)) return SW_ERR_INVALID_ARGUMENT;
-	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_submit_surfaces");
+// Host side of sw_submit_surfaces: validate every descriptor against the static data and the frame's
+// lights, and write the SurfaceGpu records and texel prefix sums (num_surfaces + 1 entries).
+int prepare_surfaces(SwCtx* ctx, const SwSurfaceDesc* surfaces, uint32_t num_surfaces, uint64_t total_texels, SurfaceGpu* gs,
+	uint64_t* prefix, uint64_t* out_work, uint32_t* out_max_light)
+{
 	const bool directional = ctx->frame.use_directional_lightmaps != 0;
 	const uint64_t lm_elems = directional ? ctx->num_dir_lightmap_elements : ctx->num_lightmap_elements;
-	int r;
-	SurfaceGpu* gs = nullptr;
-	uint64_t* prefix = nullptr;
-	if ((r = staging_acquire(ctx, ctx->stage_surfaces, std::max<size_t>(num_surfaces, 1) * sizeof(SurfaceGpu),
-			 reinterpret_cast<void**>(&gs))))
-		return r;
-	if ((r = staging_acquire(ctx, ctx->stage_prefix, (size_t(num_surfaces) + 1) * 8, reinterpret_cast<void**>(&prefix))))
-		return r;
 	uint64_t acc = 0;
+	uint32_t max_light = 0;
 	for (uint32_t i = 0; i < num_surfaces; ++i)
 	{
 		const SwSurfaceDesc& s = surfaces[i];
@@ -563,7 +573,10 @@ int sw_submit_surfaces(SwCtx* ctx, const SwSurfaceDesc* surfaces, uint32_t num_s
 			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: bad emissive mip", i);
 		if (s.num_lights > SW_MAX_POLYGON_LIGHTS) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: too many lights", i);
 		for (uint32_t l = 0; l < s.num_lights; ++l)
+		{
 			if (s.lights[l] >= ctx->num_lights) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "surface %u: bad light index", i);
+			max_light = std::max<uint32_t>(max_light, s.lights[l] + 1u);
+		}
 		if ((s.flags & SW_SURF_DIFFUSE_LAYER) && s.lightmap_offset != SW_NO_LIGHTMAP)
 		{
 			// Every texel reads lightmap rows lv, lv+1 and columns lu, lu+1 (surfaces.rs:479-543).
@@ -579,23 +592,46 @@ int sw_submit_surfaces(SwCtx* ctx, const SwSurfaceDesc* surfaces, uint32_t num_s
 		acc += area;
 	}
 	prefix[num_surfaces] = acc;
+	*out_work = acc;
+	*out_max_light = max_light;
+	return SW_OK;
+}
+
+// Records what the surface launch needs after the descriptors of this frame were prepared.
+void note_surfaces(SwCtx* ctx, uint32_t num_surfaces, uint64_t total_texels, uint64_t work, uint32_t max_light)
+{
+	ctx->arena_texels = total_texels;
+	ctx->arena_format = ctx->frame.pixel_format;
+	ctx->last_num_surfaces = num_surfaces;
+	ctx->last_surface_work = work;
+	ctx->last_surface_directional = ctx->frame.use_directional_lightmaps != 0;
+	ctx->last_surface_format = ctx->frame.pixel_format;
+	ctx->last_max_light = max_light;
+}
+} // namespace
+
+int sw_submit_surfaces(SwCtx* ctx, const SwSurfaceDesc* surfaces, uint32_t num_surfaces, uint64_t total_texels)
+{
+	if (!ctx || (num_surfaces && !surfaces)) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_submit_surfaces");
+	int r;
+	SurfaceGpu* gs = nullptr;
+	uint64_t* prefix = nullptr;
+	if ((r = staging_acquire(ctx, ctx->stage_surfaces, std::max<size_t>(num_surfaces, 1) * sizeof(SurfaceGpu),
+			 reinterpret_cast<void**>(&gs))))
+		return r;
+	if ((r = staging_acquire(ctx, ctx->stage_prefix, (size_t(num_surfaces) + 1) * 8, reinterpret_cast<void**>(&prefix))))
+		return r;
+	uint64_t work = 0;
+	uint32_t max_light = 0;
+	if ((r = prepare_surfaces(ctx, surfaces, num_surfaces, total_texels, gs, prefix, &work, &max_light))) return r;
 	const uint32_t bpp = bpp_of(ctx->frame.pixel_format);
 	if ((r = ensure(ctx, ctx->arena, std::max<uint64_t>(total_texels, 1) * bpp))) return r;
 	if ((r = ensure(ctx, ctx->surfaces, std::max<size_t>(num_surfaces, 1) * sizeof(SurfaceGpu)))) return r;
 	if ((r = ensure(ctx, ctx->work_prefix, (size_t(num_surfaces) + 1) * 8))) return r;
 	if ((r = staging_commit(ctx, ctx->stage_surfaces, ctx->surfaces.ptr, num_surfaces * sizeof(SurfaceGpu)))) return r;
 	if ((r = staging_commit(ctx, ctx->stage_prefix, ctx->work_prefix.ptr, (size_t(num_surfaces) + 1) * 8))) return r;
-	ctx->arena_texels = total_texels;
-	ctx->arena_format = ctx->frame.pixel_format;
-
-	ctx->last_num_surfaces = num_surfaces;
-	ctx->last_surface_work = acc;
-	ctx->last_surface_directional = directional;
-	ctx->last_surface_format = ctx->frame.pixel_format;
-	ctx->last_max_light = 0;
-	for (uint32_t i = 0; i < num_surfaces; ++i)
-		for (uint32_t l = 0; l < surfaces[i].num_lights; ++l)
-			ctx->last_max_light = std::max<uint32_t>(ctx->last_max_light, surfaces[i].lights[l] + 1u);
+	note_surfaces(ctx, num_surfaces, total_texels, work, max_light);
 	return launch_surfaces(ctx);
 }
 
@@ -625,16 +661,13 @@ int sw_set_surfaces(SwCtx* ctx, const void* texels, uint64_t total_texels)
 	return SW_OK;
 }
 
-int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices)
+namespace
 {
-	if (!ctx || (num_draws && (!draws || !vertices))) return SW_ERR_INVALID_ARGUMENT;
-	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_submit_draws");
-	if (!ctx->arena_valid && num_draws) return fail(ctx, SW_ERR_STATE, "sw_submit_surfaces must precede sw_submit_draws");
-	int r;
-	DrawRows* rows = nullptr;
-	if ((r = staging_acquire(ctx, ctx->stage_draw_rows, std::max<size_t>(num_draws, 1) * sizeof(DrawRows),
-			 reinterpret_cast<void**>(&rows))))
-		return r;
+// Host side of sw_submit_draws: validate every draw against its vertices and the surface arena, and
+// compute the rows each draw can cover (row records are numbered in draw order).
+int prepare_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices,
+	DrawRows* rows, uint64_t* out_rows)
+{
 	uint64_t row_acc = 0;
 	for (uint32_t i = 0; i < num_draws; ++i)
 	{
@@ -654,14 +687,39 @@ int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, cons
 		row_acc += nrows;
 		if (row_acc > 0xFFFFFFFFull) return fail(ctx, SW_ERR_LIMIT, "too many draw rows in one frame");
 	}
+	*out_rows = row_acc;
+	return SW_OK;
+}
+
+// Device buffers of the raster pass for num_draws draws, num_vertices vertices and `rows` row records.
+int ensure_raster_buffers(SwCtx* ctx, uint32_t num_draws, uint32_t num_vertices, uint64_t rows)
+{
+	int r;
 	if ((r = ensure(ctx, ctx->draws, std::max<size_t>(num_draws, 1) * sizeof(SwDrawCmd)))) return r;
 	if ((r = ensure(ctx, ctx->vertices, std::max<size_t>(num_vertices, 1) * sizeof(SwVertex16)))) return r;
 	if ((r = ensure(ctx, ctx->draw_rows, std::max<size_t>(num_draws, 1) * sizeof(DrawRows)))) return r;
 	if ((r = ensure(ctx, ctx->rdraws, std::max<size_t>(num_draws, 1) * sizeof(RasterDraw)))) return r;
-	if ((r = ensure(ctx, ctx->rows, std::max<size_t>(row_acc, 1) * sizeof(RasterRow)))) return r;
+	if ((r = ensure(ctx, ctx->rows, std::max<size_t>(rows, 1) * sizeof(RasterRow)))) return r;
 	if ((r = ensure(ctx, ctx->boxes, std::max<size_t>(num_draws, 1) * sizeof(RasterBox)))) return r;
 	if ((r = ensure(ctx, ctx->parts, std::max<size_t>(num_draws, 1) * SW_RASTER_MAX_PARTS * sizeof(RasterPart)))) return r;
 	if ((r = ensure(ctx, ctx->part_counts, std::max<size_t>(num_draws, 1) * sizeof(uint32_t)))) return r;
+	return SW_OK;
+}
+} // namespace
+
+int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices)
+{
+	if (!ctx || (num_draws && (!draws || !vertices))) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_submit_draws");
+	if (!ctx->arena_valid && num_draws) return fail(ctx, SW_ERR_STATE, "sw_submit_surfaces must precede sw_submit_draws");
+	int r;
+	DrawRows* rows = nullptr;
+	if ((r = staging_acquire(ctx, ctx->stage_draw_rows, std::max<size_t>(num_draws, 1) * sizeof(DrawRows),
+			 reinterpret_cast<void**>(&rows))))
+		return r;
+	uint64_t row_acc = 0;
+	if ((r = prepare_draws(ctx, draws, num_draws, vertices, num_vertices, rows, &row_acc))) return r;
+	if ((r = ensure_raster_buffers(ctx, num_draws, num_vertices, row_acc))) return r;
 	// The draw uploads and the raster setup run on the auxiliary stream, beside the surface build; they
 	// first wait until the previous frame's tile pass has finished reading these buffers.
 	if (ctx->tiles_recorded) SW_CUDA(ctx, cudaStreamWaitEvent(ctx->aux, ctx->ev_tiles, 0));
@@ -701,7 +759,7 @@ int sw_render(SwCtx* ctx, void* dst, uint32_t pitch, int dst_is_device)
 	const RasterArgs a = raster_args(ctx);
 	SW_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_setup, 0));
 	stage_begin(ctx, STAGE_RASTER);
-	r = check_kernel(ctx, launch_raster_tiles(a, fmt, ctx->num_sms, ctx->stream), "raster");
+	r = check_kernel(ctx, launch_raster_tiles(a, fmt, ctx->tuning.raster_tile, ctx->stream), "raster");
 	stage_end(ctx, STAGE_RASTER);
 	if (r) return r;
 	SW_CUDA(ctx, cudaEventRecord(ctx->ev_tiles, ctx->stream));
@@ -729,18 +787,17 @@ int sw_set_framebuffer(SwCtx* ctx, const void* src, uint32_t width, uint32_t hei
 	return SW_OK;
 }
 
-int sw_postprocess(SwCtx* ctx, const SwPostConfig* config, float frame_duration_s, const float color_modulate[3], void* dst,
-	uint32_t pitch, int dst_is_device)
+namespace
 {
-	if (!ctx || !config || !color_modulate || !dst) return SW_ERR_INVALID_ARGUMENT;
-	if (!ctx->fb_valid || ctx->fb_format != SW_PIXEL_C64)
-		return fail(ctx, SW_ERR_STATE, "postprocessing needs a colour64 frame");
+// Postprocessor arguments for the context's colour64 frame buffer (everything but the destination):
+// tonemapping factors from the current exposure and colour modulation, bloom kernel weights, scratch
+// buffers. Runs finalize_exposure first (the previous frame's average updates the exposure).
+int prepare_post(SwCtx* ctx, const SwPostConfig* config, const float color_modulate[3], PostArgs& a)
+{
 	const uint32_t w = ctx->fb_width, h = ctx->fb_height;
-	if (pitch < w) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");
 	int r;
 	if ((r = finalize_exposure(ctx))) return r;
 
-	PostArgs a;
 	std::memset(&a, 0, sizeof(a));
 	a.hdr = static_cast<const uint64_t*>(ctx->framebuffer.ptr);
 	a.width = w;
@@ -802,6 +859,21 @@ int sw_postprocess(SwCtx* ctx, const SwPostConfig* config, float frame_duration_
 		if ((r = ensure(ctx, ctx->line_sums_f, size_t(h) * 16))) return r;
 		a.line_sums_f = static_cast<float*>(ctx->line_sums_f.ptr);
 	}
+	return SW_OK;
+}
+} // namespace
+
+int sw_postprocess(SwCtx* ctx, const SwPostConfig* config, float frame_duration_s, const float color_modulate[3], void* dst,
+	uint32_t pitch, int dst_is_device)
+{
+	if (!ctx || !config || !color_modulate || !dst) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->fb_valid || ctx->fb_format != SW_PIXEL_C64)
+		return fail(ctx, SW_ERR_STATE, "postprocessing needs a colour64 frame");
+	const uint32_t w = ctx->fb_width, h = ctx->fb_height;
+	if (pitch < w) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");
+	int r;
+	PostArgs a;
+	if ((r = prepare_post(ctx, config, color_modulate, a))) return r;
 	void* out = dst;
 	uint32_t out_pitch = pitch;
 	if (!dst_is_device)
@@ -915,14 +987,290 @@ int sw_set_exposure(SwCtx* ctx, float exposure)
 	return SW_OK;
 }
 
+namespace
+{
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// sw_draw_frame without a graph: the per-call API in order.
+int draw_frame_direct(SwCtx* ctx, const SwFrameInput& f)
+{
+	int r;
+	if ((r = sw_frame_begin(ctx, &f.params, f.lights, f.num_lights))) return r;
+	if ((r = sw_submit_surfaces(ctx, f.surfaces, f.num_surfaces, f.total_texels))) return r;
+	if ((r = sw_submit_draws(ctx, f.draws, f.num_draws, f.vertices, f.num_vertices))) return r;
+	if (!f.postprocess) return sw_render(ctx, f.dst, f.dst_pitch, f.dst_is_device);
+	if ((r = sw_render(ctx, nullptr, 0, 0))) return r;
+	if (!f.dst) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocess needs a destination");
+	return sw_postprocess(ctx, &f.post, f.frame_duration_s, f.color_modulate, f.dst, f.dst_pitch, f.dst_is_device);
+}
+
+// Device work of one graph frame, issued on the context's streams while they are being captured.
+int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, const size_t* off, uint64_t rows,
+	const PostArgs* post)
+{
+	cudaStream_t s = ctx->stream, aux = ctx->aux;
+	SW_CUDA(ctx, cudaMemcpyAsync(ctx->lights.ptr, h + off[0], f.num_lights * sizeof(SwLight), cudaMemcpyHostToDevice, s));
+	SW_CUDA(ctx, cudaMemcpyAsync(ctx->surfaces.ptr, h + off[1], f.num_surfaces * sizeof(SurfaceGpu), cudaMemcpyHostToDevice, s));
+	SW_CUDA(ctx, cudaMemcpyAsync(ctx->work_prefix.ptr, h + off[2], (size_t(f.num_surfaces) + 1) * 8, cudaMemcpyHostToDevice, s));
+	// draw uploads and raster setup on the auxiliary stream, beside the surface build
+	SW_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
+	SW_CUDA(ctx, cudaStreamWaitEvent(aux, ctx->ev_fork, 0));
+	SW_CUDA(ctx, cudaMemcpyAsync(ctx->draws.ptr, h + off[3], f.num_draws * sizeof(SwDrawCmd), cudaMemcpyHostToDevice, aux));
+	SW_CUDA(ctx, cudaMemcpyAsync(ctx->vertices.ptr, h + off[4], f.num_vertices * sizeof(SwVertex16), cudaMemcpyHostToDevice, aux));
+	SW_CUDA(ctx, cudaMemcpyAsync(ctx->draw_rows.ptr, h + off[5], f.num_draws * sizeof(DrawRows), cudaMemcpyHostToDevice, aux));
+	int r;
+	const RasterArgs ra = raster_args(ctx);
+	if ((r = check_kernel(ctx, launch_raster_setup(ra, aux), "raster setup"))) return r;
+	SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, aux));
+	if ((r = launch_surfaces(ctx))) return r;
+	SW_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_setup, 0));
+	if ((r = check_kernel(ctx, launch_raster_tiles(ra, f.params.pixel_format, ctx->tuning.raster_tile, s), "raster"))) return r;
+	(void)rows;
+	if (post)
+	{
+		if ((r = check_kernel(ctx, launch_postprocess(*post, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join), "postprocess")))
+			return r;
+		SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_average, ctx->average.ptr, 16, cudaMemcpyDeviceToHost, s));
+	}
+	else if (f.dst && f.dst_is_device)
+	{
+		const uint32_t bpp = bpp_of(f.params.pixel_format);
+		SW_CUDA(ctx, cudaMemcpy2DAsync(f.dst, size_t(f.dst_pitch) * bpp, ctx->framebuffer.ptr, size_t(f.params.width) * bpp,
+						 size_t(f.params.width) * bpp, f.params.height, cudaMemcpyDeviceToDevice, s));
+	}
+	return SW_OK;
+}
+} // namespace
+
+int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
+{
+	if (!ctx || !in) return SW_ERR_INVALID_ARGUMENT;
+	const SwFrameInput& f = *in;
+	if ((f.num_lights && !f.lights) || (f.num_surfaces && !f.surfaces) || (f.num_draws && (!f.draws || !f.vertices)))
+		return SW_ERR_INVALID_ARGUMENT;
+	if (f.postprocess && f.params.pixel_format != SW_PIXEL_C64)
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocessing needs a colour64 frame");
+	if (f.dst && f.dst_pitch < f.params.width) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");
+	if (!ctx->graph_enabled) return draw_frame_direct(ctx, f);
+	int r;
+	// frame parameters (the checks of sw_frame_begin)
+	const SwFrameParams& p = f.params;
+	if (p.pixel_format > SW_PIXEL_C64) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "bad pixel format");
+	if (p.width == 0 || p.height == 0 || p.width > 16384 || p.height > 16384)
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "bad frame size %ux%u", p.width, p.height);
+	if (p.use_directional_lightmaps && ctx->num_dir_lightmap_elements == 0)
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "directional lightmaps requested but none uploaded");
+	if (f.num_lights > 65535) return fail(ctx, SW_ERR_LIMIT, "too many lights");
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	ctx->frame = p;
+	ctx->num_lights = f.num_lights;
+
+	// 1. every per-frame array into one pinned staging block (two blocks alternate between frames)
+	Staging& st = ctx->gstage[ctx->gset];
+	ctx->gset ^= 1u;
+	size_t off[7];
+	off[0] = 0;
+	off[1] = align_up(off[0] + std::max<size_t>(f.num_lights, 1) * sizeof(SwLight), 256);
+	off[2] = align_up(off[1] + std::max<size_t>(f.num_surfaces, 1) * sizeof(SurfaceGpu), 256);
+	off[3] = align_up(off[2] + (size_t(f.num_surfaces) + 1) * 8, 256);
+	off[4] = align_up(off[3] + std::max<size_t>(f.num_draws, 1) * sizeof(SwDrawCmd), 256);
+	off[5] = align_up(off[4] + std::max<size_t>(f.num_vertices, 1) * sizeof(SwVertex16), 256);
+	off[6] = align_up(off[5] + std::max<size_t>(f.num_draws, 1) * sizeof(DrawRows), 256);
+	void* hv = nullptr;
+	if ((r = staging_acquire(ctx, st, off[6], &hv))) return r;
+	unsigned char* h = static_cast<unsigned char*>(hv);
+	if (f.num_lights) std::memcpy(h + off[0], f.lights, f.num_lights * sizeof(SwLight));
+	uint64_t work = 0;
+	uint32_t max_light = 0;
+	if ((r = prepare_surfaces(ctx, f.surfaces, f.num_surfaces, f.total_texels, reinterpret_cast<SurfaceGpu*>(h + off[1]),
+			 reinterpret_cast<uint64_t*>(h + off[2]), &work, &max_light)))
+		return r;
+	note_surfaces(ctx, f.num_surfaces, f.total_texels, work, max_light);
+	if (f.num_draws) std::memcpy(h + off[3], f.draws, f.num_draws * sizeof(SwDrawCmd));
+	if (f.num_vertices) std::memcpy(h + off[4], f.vertices, f.num_vertices * sizeof(SwVertex16));
+	uint64_t rows = 0;
+	if ((r = prepare_draws(ctx, f.draws, f.num_draws, f.vertices, f.num_vertices, reinterpret_cast<DrawRows*>(h + off[5]), &rows)))
+		return r;
+
+	// 2. device buffers (growing them synchronises; the next capture picks up the new addresses)
+	const uint32_t bpp = bpp_of(p.pixel_format);
+	if ((r = ensure(ctx, ctx->lights, std::max<size_t>(f.num_lights, 1) * sizeof(SwLight)))) return r;
+	if ((r = ensure(ctx, ctx->arena, std::max<uint64_t>(f.total_texels, 1) * bpp))) return r;
+	if ((r = ensure(ctx, ctx->surfaces, std::max<size_t>(f.num_surfaces, 1) * sizeof(SurfaceGpu)))) return r;
+	if ((r = ensure(ctx, ctx->work_prefix, (size_t(f.num_surfaces) + 1) * 8))) return r;
+	if ((r = ensure_raster_buffers(ctx, f.num_draws, f.num_vertices, rows))) return r;
+	if ((r = ensure(ctx, ctx->framebuffer, size_t(p.width) * p.height * bpp))) return r;
+	if (!ctx->fb_valid || ctx->fb_width != p.width || ctx->fb_height != p.height || ctx->fb_format != p.pixel_format)
+	{
+		// a new frame buffer starts black (postprocessor.rs:56-66), before the graph
+		SW_CUDA(ctx, cudaMemsetAsync(ctx->framebuffer.ptr, 0, size_t(p.width) * p.height * bpp, ctx->stream));
+		ctx->fb_width = p.width;
+		ctx->fb_height = p.height;
+		ctx->fb_format = p.pixel_format;
+		ctx->fb_valid = true;
+	}
+	ctx->num_rows = rows;
+	ctx->num_draws = f.num_draws;
+	PostArgs pa;
+	void* post_out = nullptr;
+	if (f.postprocess)
+	{
+		if (!f.dst) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocess needs a destination");
+		if ((r = prepare_post(ctx, &f.post, f.color_modulate, pa))) return r;
+		post_out = f.dst;
+		pa.dst_pitch = f.dst_pitch;
+		if (!f.dst_is_device)
+		{
+			if ((r = ensure(ctx, ctx->up_dst, size_t(p.width) * p.height * 4))) return r;
+			post_out = ctx->up_dst.ptr;
+			pa.dst_pitch = p.width;
+		}
+		pa.dst = static_cast<uint32_t*>(post_out);
+	}
+
+	// 3. capture the device work and update (or instantiate) the frame graph
+	SW_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+	ctx->capturing = true;
+	const int er = enqueue_frame(ctx, f, h, off, rows, f.postprocess ? &pa : nullptr);
+	ctx->capturing = false;
+	cudaGraph_t g = nullptr;
+	const cudaError_t ee = cudaStreamEndCapture(ctx->stream, &g);
+	if (er || ee != cudaSuccess)
+	{
+		if (g) cudaGraphDestroy(g);
+		cudaGetLastError();
+		return er ? er : cuda_fail(ctx, ee, "cudaStreamEndCapture");
+	}
+	if (ctx->gexec)
+	{
+		cudaGraphExecUpdateResultInfo info;
+		if (cudaGraphExecUpdate(ctx->gexec, g, &info) != cudaSuccess)
+		{
+			cudaGetLastError(); // the topology changed: instantiate anew
+			cudaGraphExecDestroy(ctx->gexec);
+			ctx->gexec = nullptr;
+		}
+	}
+	if (!ctx->gexec)
+	{
+		const cudaError_t ie = cudaGraphInstantiate(&ctx->gexec, g, 0);
+		if (ie != cudaSuccess)
+		{
+			cudaGraphDestroy(g);
+			ctx->gexec = nullptr;
+			return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+		}
+	}
+	cudaGraphDestroy(g);
+	stage_begin(ctx, STAGE_FRAME);
+	SW_CUDA(ctx, cudaGraphLaunch(ctx->gexec, ctx->stream));
+	stage_end(ctx, STAGE_FRAME);
+	SW_CUDA(ctx, cudaEventRecord(st.done, ctx->stream));
+	st.pending = true;
+	SW_CUDA(ctx, cudaEventRecord(ctx->ev_tiles, ctx->stream));
+	ctx->tiles_recorded = true;
+	ctx->arena_valid = true;
+	ctx->draws_valid = false;
+	ctx->frame_open = false;
+	ctx->stats.draws += f.num_draws; // (surfaces are counted by launch_surfaces)
+	if (f.postprocess)
+	{
+		SW_CUDA(ctx, cudaEventRecord(ctx->average_ready, ctx->stream));
+		ctx->exposure_pending = true;
+		ctx->pending_config = f.post;
+		ctx->pending_dt = f.frame_duration_s;
+		if (!f.dst_is_device) return copy_out(ctx, f.dst, f.dst_pitch, 0, post_out, p.width, p.width, p.height, 4);
+	}
+	else if (f.dst && !f.dst_is_device)
+		return copy_out(ctx, f.dst, f.dst_pitch, 0, ctx->framebuffer.ptr, p.width, p.width, p.height, bpp);
+	return SW_OK;
+}
+
+int sw_set_frame_graph(SwCtx* ctx, int enable)
+{
+	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
+	ctx->graph_enabled = enable != 0;
+	return SW_OK;
+}
+
+int sw_set_tuning(SwCtx* ctx, const SwTuning* t)
+{
+	if (!ctx || !t) return SW_ERR_INVALID_ARGUMENT;
+	if (t->raster_tile >= SW_RASTER_TILE_VARIANTS || t->surface_blocks_per_sm < 1 || t->surface_blocks_per_sm > 64)
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "tuning out of range");
+	if (t->raster_tile != ctx->tuning.raster_tile || t->surface_blocks_per_sm != ctx->tuning.surface_blocks_per_sm)
+	{
+		// other kernels: the frame graph is instantiated anew
+		SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+		if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+		ctx->gexec = nullptr;
+	}
+	ctx->tuning = *t;
+	return SW_OK;
+}
+
+int sw_get_tuning(SwCtx* ctx, SwTuning* out)
+{
+	if (!ctx || !out) return SW_ERR_INVALID_ARGUMENT;
+	*out = ctx->tuning;
+	return SW_OK;
+}
+
+int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning* out_best, float* out_best_ms)
+{
+	if (!ctx || !sample || reps == 0 || reps > 1000) return SW_ERR_INVALID_ARGUMENT;
+	int r;
+	if ((r = finalize_exposure(ctx))) return r;
+	const float exposure = ctx->exposure;
+	const bool timing = ctx->timing;
+	const SwTuning start = ctx->tuning;
+	if (!ctx->timing && (r = sw_enable_timing(ctx, 1))) return r;
+	const uint32_t blocks[] = {8u, 16u, 24u, 32u, 48u};
+	SwTuning best = start;
+	float best_ms = 1e30f;
+	std::vector<float> ms(reps);
+	for (uint32_t tile = 0; tile < SW_RASTER_TILE_VARIANTS && r == SW_OK; ++tile)
+		for (uint32_t b : blocks)
+		{
+			const SwTuning t{tile, b};
+			if ((r = sw_set_tuning(ctx, &t))) break;
+			for (uint32_t i = 0; i < 2 + reps && r == SW_OK; ++i)
+			{
+				if ((r = sw_draw_frame(ctx, sample))) break;
+				float t5[5];
+				if ((r = sw_get_timings(ctx, t5))) break;
+				if (i >= 2) ms[i - 2] = t5[STAGE_FRAME];
+			}
+			if (r) break;
+			std::vector<float> sorted = ms;
+			std::sort(sorted.begin(), sorted.end());
+			const float med = sorted[sorted.size() / 2];
+			if (med < best_ms)
+			{
+				best_ms = med;
+				best = t;
+			}
+		}
+	// restore the exposure state and the timing switch; keep the best configuration
+	const int r2 = finalize_exposure(ctx);
+	ctx->exposure = exposure;
+	ctx->exposure_pending = false;
+	if (!timing) sw_enable_timing(ctx, 0);
+	if (r || r2) return r ? r : r2;
+	if ((r = sw_set_tuning(ctx, &best))) return r;
+	if (out_best) *out_best = best;
+	if (out_best_ms) *out_best_ms = best_ms;
+	return SW_OK;
+}
+
 int sw_abi_layout(uint32_t* sizes, uint32_t count)
 {
-	const uint32_t s[11] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
+	const uint32_t s[13] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
 		uint32_t(sizeof(SwDirectionalLightmapElement)), uint32_t(sizeof(SwLight)), uint32_t(sizeof(SwSurfaceDesc)),
 		uint32_t(sizeof(SwVertex16)), uint32_t(sizeof(SwDrawCmd)), uint32_t(sizeof(SwFrameParams)),
-		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats))};
-	for (uint32_t i = 0; sizes && i < count && i < 11; ++i) sizes[i] = s[i];
-	return 11;
+		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats)), uint32_t(sizeof(SwFrameInput)), uint32_t(sizeof(SwTuning))};
+	for (uint32_t i = 0; sizes && i < count && i < 13; ++i) sizes[i] = s[i];
+	return 13;
 }
 
 int sw_get_stats(SwCtx* ctx, SwStats* out)

@@ -94,12 +94,30 @@ class Stats(ctypes.Structure):
 
 
 # Order reported by sw_abi_layout.
+class FrameInput(ctypes.Structure):
+    """SwFrameInput: one whole frame for sw_draw_frame."""
+    _fields_ = [("params", FrameParams), ("num_lights", ctypes.c_uint32), ("lights", ctypes.c_void_p),
+                ("surfaces", ctypes.c_void_p), ("total_texels", ctypes.c_uint64), ("num_surfaces", ctypes.c_uint32),
+                ("num_draws", ctypes.c_uint32), ("draws", ctypes.c_void_p), ("vertices", ctypes.c_void_p),
+                ("num_vertices", ctypes.c_uint32), ("postprocess", ctypes.c_uint32), ("post", PostConfig),
+                ("frame_duration_s", ctypes.c_float), ("color_modulate", ctypes.c_float * 3), ("dst", ctypes.c_void_p),
+                ("dst_pitch", ctypes.c_uint32), ("dst_is_device", ctypes.c_int32)]
+
+
+class Tuning(ctypes.Structure):
+    """SwTuning: launch configuration (raster tile shape, surface-build blocks per SM)."""
+    _fields_ = [("raster_tile", ctypes.c_uint32), ("surface_blocks_per_sm", ctypes.c_uint32)]
+
+
+SW_RASTER_TILE_VARIANTS = 5
+
 LAYOUT_ORDER = [
     ("SwCreateInfo", ctypes.sizeof(CreateInfo)), ("SwTextureMip", TEXTURE_MIP.itemsize),
     ("SwEmissiveMip", EMISSIVE_MIP.itemsize), ("SwDirectionalLightmapElement", DIR_LIGHTMAP_ELEMENT.itemsize),
     ("SwLight", LIGHT.itemsize), ("SwSurfaceDesc", SURFACE_DESC.itemsize), ("SwVertex16", VERTEX16.itemsize),
     ("SwDrawCmd", DRAW_CMD.itemsize), ("SwFrameParams", ctypes.sizeof(FrameParams)),
     ("SwPostConfig", ctypes.sizeof(PostConfig)), ("SwStats", ctypes.sizeof(Stats)),
+    ("SwFrameInput", ctypes.sizeof(FrameInput)), ("SwTuning", ctypes.sizeof(Tuning)),
 ]
 
 

@@ -23,7 +23,8 @@ EXPORTED = [
     "sw_submit_draws",
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
-    "sw_postprocess_noalloc", "sw_set_learned_upscaler",
+    "sw_postprocess_noalloc", "sw_set_learned_upscaler", "sw_draw_frame", "sw_set_frame_graph", "sw_set_tuning",
+    "sw_get_tuning", "sw_autotune",
     # learned upscaler (include/swlearn.h)
     "sw_upscaler_create", "sw_upscaler_destroy", "sw_upscaler_last_error", "sw_upscaler_get_params",
     "sw_upscaler_set_params", "sw_upscaler_gradients", "sw_upscaler_train_step", "sw_upscaler_steps",
@@ -71,6 +72,11 @@ def load_library(path=LIB_PATH):
         "sw_enable_timing": ([vp, i32], i32),
         "sw_get_timings": ([vp, vp], i32),
         "sw_set_learned_upscaler": ([vp, vp], i32),
+        "sw_draw_frame": ([vp, vp], i32),
+        "sw_set_frame_graph": ([vp, i32], i32),
+        "sw_set_tuning": ([vp, vp], i32),
+        "sw_get_tuning": ([vp, vp], i32),
+        "sw_autotune": ([vp, vp, u32, vp, ctypes.POINTER(f32)], i32),
         "sw_upscaler_create": ([i32, u64, ctypes.POINTER(vp)], i32),
         "sw_upscaler_destroy": ([vp], i32),
         "sw_upscaler_last_error": ([vp], ctypes.c_char_p),
@@ -239,6 +245,61 @@ class GpuRenderer:
     def upscale_device(self, mode, scale, src_ptr, dst_ptr, width, height, pitch):
         self._check(self.lib.sw_upscale(self.ctx, mode, scale, ctypes.c_void_p(src_ptr), 1, ctypes.c_void_p(dst_ptr),
                                         width, height, pitch, 1), "sw_upscale")
+
+    def frame_input(self, params, lights, surfaces, total_texels, draws, vertices, post_config=None,
+                    frame_duration_s=1.0 / 60.0, color_modulate=(1.0, 1.0, 1.0), dst=None, dst_device_ptr=None, pitch=None):
+        """SwFrameInput for draw_frame / autotune (keeps the arrays it points to alive on the object)."""
+        fi = abi.FrameInput()
+        fi.params = params
+        keep = []
+        def arr(a, dt):
+            a = np.ascontiguousarray(a if a is not None else np.zeros(0, dt), dtype=dt)
+            keep.append(a)
+            return a
+        lights = arr(lights, abi.LIGHT)
+        surfaces = arr(surfaces, abi.SURFACE_DESC)
+        draws = arr(draws, abi.DRAW_CMD)
+        vertices = arr(vertices, abi.VERTEX16)
+        fi.num_lights, fi.lights = lights.size, abi.ptr(lights)
+        fi.num_surfaces, fi.surfaces, fi.total_texels = surfaces.size, abi.ptr(surfaces), int(total_texels)
+        fi.num_draws, fi.draws = draws.size, abi.ptr(draws)
+        fi.num_vertices, fi.vertices = vertices.size, abi.ptr(vertices)
+        if post_config is not None:
+            fi.postprocess = 1
+            fi.post = post_config
+        fi.frame_duration_s = frame_duration_s
+        fi.color_modulate = (ctypes.c_float * 3)(*color_modulate)
+        if dst is not None:
+            keep.append(dst)
+            fi.dst, fi.dst_pitch, fi.dst_is_device = abi.ptr(dst), pitch or dst.shape[1], 0
+        elif dst_device_ptr is not None:
+            fi.dst, fi.dst_pitch, fi.dst_is_device = ctypes.c_void_p(dst_device_ptr), pitch, 1
+        fi._keep = keep
+        return fi
+
+    def draw_frame(self, frame_input):
+        """One whole frame through sw_draw_frame (one CUDA graph unless disabled)."""
+        self._check(self.lib.sw_draw_frame(self.ctx, ctypes.byref(frame_input)), "sw_draw_frame")
+
+    def set_frame_graph(self, enable):
+        self._check(self.lib.sw_set_frame_graph(self.ctx, 1 if enable else 0), "sw_set_frame_graph")
+
+    def tuning(self):
+        t = abi.Tuning()
+        self._check(self.lib.sw_get_tuning(self.ctx, ctypes.byref(t)), "sw_get_tuning")
+        return t
+
+    def set_tuning(self, raster_tile, surface_blocks_per_sm):
+        t = abi.Tuning(raster_tile, surface_blocks_per_sm)
+        self._check(self.lib.sw_set_tuning(self.ctx, ctypes.byref(t)), "sw_set_tuning")
+
+    def autotune(self, frame_input, reps=5):
+        """Returns (Tuning, median ms per frame) of the fastest configuration, which stays selected."""
+        t = abi.Tuning()
+        ms = ctypes.c_float()
+        self._check(self.lib.sw_autotune(self.ctx, ctypes.byref(frame_input), reps, ctypes.byref(t), ctypes.byref(ms)),
+                    "sw_autotune")
+        return t, ms.value
 
     def attach_upscaler(self, ups):
         """Use a learned upscaler (sqwheel.learned.Upscaler, or None) for SW_UPSCALE_LEARNED."""
