@@ -252,7 +252,10 @@ def run_frame_gpu(args, world, rank, local):
                              post_config=work.config, dst_device_ptr=ldr_frames[step].data_ptr(), pitch=W)
 
     # autotuner: tile shape of the tile pass and surface-build grid, on the first frame
-    tune, tune_ms = r.autotune(frame_input(0, work.frames[0]), reps=5)
+    if args.autotune_reps > 0:
+        tune, tune_ms = r.autotune(frame_input(0, work.frames[0]), reps=args.autotune_reps)
+    else:
+        tune, tune_ms = r.tuning(), 0.0
     r.set_exposure(1.0)
     if world > 1:
         torch.distributed.barrier()
@@ -671,6 +674,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", default="frame", choices=["frame", "surfaces", "upscale"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--autotune-reps", type=int, default=5,
+                    help="frames per configuration of the autotuner before the frame measurement (0: keep the default)")
     ap.add_argument("--learn-steps", type=int, default=2000,
                     help="training steps of the learned upscaler before its measurement (0: skip it)")
     args = ap.parse_args()

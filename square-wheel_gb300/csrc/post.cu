@@ -28,52 +28,90 @@ __device__ __forceinline__ CV tonemap(CV c, const PostArgs& a)
 		__fdiv_rn(c.r, mad2(c.r, a.inv_255[2], a.inv_scale[2])), alpha};
 }
 
-// downscale_hdr_buffer::<S>, postprocessor.rs:792-844: one thread per bloom pixel.
+// downscale_hdr_buffer::<S>, postprocessor.rs:792-844. Each thread computes two horizontally adjacent
+// bloom pixels (all 2*S*S HDR pixels are loaded before any is used: S is a template parameter, so the
+// loops unroll); a block covers 512 bloom pixels of one line and adds its lanes' exact integer line
+// sums with one atomic per lane.
+template <int S>
 __global__ void __launch_bounds__(256) pp_downscale_kernel(PostArgs a)
 {
-	const uint32_t bx = blockIdx.x * blockDim.x + threadIdx.x;
+	__shared__ int32_t s_sum[8][4];
+	const uint32_t bx = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
 	const uint32_t by = blockIdx.y;
-	const bool active = bx < a.bw;
-	int32_t avg[4] = {0, 0, 0, 0};
-	if (active)
+	int32_t avg[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+	constexpr int32_t scaler = 256 / (S * S);
+#pragma unroll
+	for (int k = 0; k < 2; ++k)
 	{
-		const uint32_t S = a.scale;
+		if (bx + k >= a.bw) break;
 		int32_t sum[4] = {0, 0, 0, 0};
-		for (uint32_t dy = 0; dy < S; ++dy)
+		unsigned long long q[S][S];
+#pragma unroll
+		for (int dy = 0; dy < S; ++dy)
 		{
-			const uint64_t* row = a.hdr + uint64_t(by * S + dy) * a.width + bx * S;
-			for (uint32_t dx = 0; dx < S; dx += 2)
+			const uint64_t* row = a.hdr + uint64_t(by * S + dy) * a.width + (bx + k) * S;
+			const bool aligned = (reinterpret_cast<uintptr_t>(row) & 15) == 0;
+#pragma unroll
+			for (int dx = 0; dx < S; dx += 2)
 			{
-				// Pairs of pixels; one 16-byte load when the pair is aligned (even row start).
-				unsigned long long q0, q1;
-				if ((reinterpret_cast<uintptr_t>(row + dx) & 15) == 0)
+				if (aligned)
 				{
 					const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(row + dx));
-					q0 = v.x;
-					q1 = v.y;
+					q[dy][dx] = v.x;
+					q[dy][dx + 1] = v.y;
 				}
 				else
 				{
-					q0 = __ldg(reinterpret_cast<const unsigned long long*>(row) + dx);
-					q1 = __ldg(reinterpret_cast<const unsigned long long*>(row) + dx + 1);
+					q[dy][dx] = __ldg(reinterpret_cast<const unsigned long long*>(row) + dx);
+					q[dy][dx + 1] = __ldg(reinterpret_cast<const unsigned long long*>(row) + dx + 1);
 				}
-				const CI c0 = ci_from_c64(q0), c1 = ci_from_c64(q1);
-#pragma unroll
-				for (int i = 0; i < 4; ++i) sum[i] = wadd(wadd(sum[i], c0.v[i]), c1.v[i]);
 			}
 		}
-		const int32_t scaler = 256 / int32_t(S * S);
 #pragma unroll
-		for (int i = 0; i < 4; ++i) avg[i] = wmul(sum[i], scaler) >> 8;
-		a.bloom0[uint64_t(by) * a.bw + bx] = ci_to_c64(CI{{avg[0], avg[1], avg[2], avg[3]}});
+		for (int dy = 0; dy < S; ++dy)
+#pragma unroll
+			for (int dx = 0; dx < S; ++dx)
+			{
+				const CI c = ci_from_c64(q[dy][dx]);
+#pragma unroll
+				for (int i = 0; i < 4; ++i) sum[i] = wadd(sum[i], c.v[i]);
+			}
+#pragma unroll
+		for (int i = 0; i < 4; ++i) avg[k][i] = wmul(sum[i], scaler) >> 8;
 	}
-	// Exact per-line sums of the averages (wrapping i32, order-independent).
+	if (bx < a.bw)
+	{
+		const uint64_t o = uint64_t(by) * a.bw + bx;
+		const uint64_t v0 = ci_to_c64(CI{{avg[0][0], avg[0][1], avg[0][2], avg[0][3]}});
+		if (bx + 1 < a.bw)
+		{
+			const uint64_t v1 = ci_to_c64(CI{{avg[1][0], avg[1][1], avg[1][2], avg[1][3]}});
+			if ((o & 1) == 0)
+				*reinterpret_cast<ulonglong2*>(a.bloom0 + o) = make_ulonglong2(v0, v1);
+			else
+			{
+				a.bloom0[o] = v0;
+				a.bloom0[o + 1] = v1;
+			}
+		}
+		else
+			a.bloom0[o] = v0;
+	}
+	// Exact per-line sums of the averages (wrapping i32: order-independent): warp, then block.
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
 	for (int i = 0; i < 4; ++i)
 	{
-		int32_t v = avg[i];
+		int32_t v = wadd(avg[0][i], avg[1][i]);
 		for (int o = 16; o > 0; o >>= 1) v = wadd(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
-		if ((threadIdx.x & 31) == 0) atomicAdd(a.line_sums + by * 4 + i, v);
+		if (lane == 0) s_sum[warp][i] = v;
+	}
+	__syncthreads();
+	if (threadIdx.x < 4)
+	{
+		int32_t t = 0;
+		for (int w = 0; w < 8; ++w) t = wadd(t, s_sum[w][threadIdx.x]);
+		atomicAdd(a.line_sums + by * 4 + threadIdx.x, t);
 	}
 }
 
@@ -150,22 +188,22 @@ __global__ void __launch_bounds__(256) pp_blur_v_kernel(PostArgs a)
 
 __device__ __forceinline__ CV bloom_at(const PostArgs& a, uint32_t x, uint32_t y)
 {
-	return cv_from_c64(a.bloom0[uint64_t(y) * a.bw + x]);
+	return cv_from_c64(__ldg(reinterpret_cast<const unsigned long long*>(a.bloom0) + uint64_t(y) * a.bw + x));
 }
 
 // HDR pixel (x, y) plus its bloom sample, nearest (postprocessor.rs:346-462) or linear (:464-726).
+template <int S, bool LINEAR>
 __device__ __forceinline__ CV bloom_sum(const PostArgs& a, uint32_t x, uint32_t y, CV c)
 {
-	const uint32_t S = a.scale;
 	CV sum;
-	if (!a.linear_filter)
+	if (!LINEAR)
 	{
 		sum = cv_add(bloom_at(a, min(x / S, a.bw - 1), min(y / S, a.bh - 1)), c);
 	}
 	else
 	{
-		const uint32_t half = S / 2;
-		const float sf = float(S);
+		constexpr uint32_t half = S / 2;
+		constexpr float sf = float(S);
 		const uint32_t rbx = (a.bw - 1) * S + half; // right_border_begin_x
 		const uint32_t uby = (a.bh - 1) * S + half; // upper_border_begin_y
 		const bool x_inner = x >= half && x < rbx;
@@ -197,41 +235,45 @@ __device__ __forceinline__ CV bloom_sum(const PostArgs& a, uint32_t x, uint32_t 
 	return sum;
 }
 
-// Tonemapping with bloom: two horizontally adjacent pixels per thread (16-byte HDR loads and 8-byte
-// stores where aligned).
+// Tonemapping with bloom: four horizontally adjacent pixels per thread (two 16-byte HDR loads issued
+// together, one 16-byte store where aligned).
+template <int S, bool LINEAR>
 __global__ void __launch_bounds__(256) pp_tonemap_bloom_kernel(PostArgs a)
 {
-	const uint32_t x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+	const uint32_t x = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
 	const uint32_t y = blockIdx.y;
 	if (x >= a.width) return;
 	const uint64_t src = uint64_t(y) * a.width + x;
 	const uint64_t dst = uint64_t(y) * a.dst_pitch + x;
-	const bool pair = x + 1 < a.width;
-	unsigned long long p0, p1 = 0;
-	if (pair && (src & 1) == 0)
+	const uint32_t n = min(4u, a.width - x);
+	unsigned long long p[4] = {0, 0, 0, 0};
+	const unsigned long long* h = reinterpret_cast<const unsigned long long*>(a.hdr) + src;
+	if (n == 4 && (src & 1) == 0)
 	{
-		const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(a.hdr + src));
-		p0 = v.x;
-		p1 = v.y;
+		const ulonglong2 v0 = __ldg(reinterpret_cast<const ulonglong2*>(h));
+		const ulonglong2 v1 = __ldg(reinterpret_cast<const ulonglong2*>(h + 2));
+		p[0] = v0.x;
+		p[1] = v0.y;
+		p[2] = v1.x;
+		p[3] = v1.y;
 	}
 	else
 	{
-		p0 = __ldg(reinterpret_cast<const unsigned long long*>(a.hdr) + src);
-		if (pair) p1 = __ldg(reinterpret_cast<const unsigned long long*>(a.hdr) + src + 1);
+#pragma unroll
+		for (int k = 0; k < 4; ++k)
+			if (k < int(n)) p[k] = __ldg(h + k);
 	}
-	const uint32_t o0 = cv_to_c32(tonemap(bloom_sum(a, x, y, cv_from_c64(p0)), a));
-	if (!pair)
-	{
-		a.dst[dst] = o0;
-		return;
-	}
-	const uint32_t o1 = cv_to_c32(tonemap(bloom_sum(a, x + 1, y, cv_from_c64(p1)), a));
-	if ((dst & 1) == 0)
-		*reinterpret_cast<uint2*>(a.dst + dst) = make_uint2(o0, o1);
+	uint32_t o[4];
+#pragma unroll
+	for (int k = 0; k < 4; ++k)
+		o[k] = k < int(n) ? cv_to_c32(tonemap(bloom_sum<S, LINEAR>(a, x + k, y, cv_from_c64(p[k])), a)) : 0u;
+	if (n == 4 && (dst & 3) == 0)
+		*reinterpret_cast<uint4*>(a.dst + dst) = make_uint4(o[0], o[1], o[2], o[3]);
 	else
 	{
-		a.dst[dst] = o0;
-		a.dst[dst + 1] = o1;
+#pragma unroll
+		for (int k = 0; k < 4; ++k)
+			if (k < int(n)) a.dst[dst + k] = o[k];
 	}
 }
 
@@ -335,6 +377,32 @@ __global__ void fill_kernel(void* dst, uint64_t count, uint64_t value, uint32_t 
 	}
 }
 
+template <int S>
+void launch_bloom_passes(const PostArgs& a, cudaStream_t stream, bool downscale)
+{
+	const dim3 block(256);
+	if (downscale)
+	{
+		pp_downscale_kernel<S><<<dim3((a.bw + 511) / 512, a.bh), block, 0, stream>>>(a);
+		return;
+	}
+	const dim3 grid((a.width + 1023) / 1024, a.height);
+	if (a.linear_filter)
+		pp_tonemap_bloom_kernel<S, true><<<grid, block, 0, stream>>>(a);
+	else
+		pp_tonemap_bloom_kernel<S, false><<<grid, block, 0, stream>>>(a);
+}
+
+void launch_bloom(const PostArgs& a, cudaStream_t stream, bool downscale)
+{
+	if (a.scale == 2)
+		launch_bloom_passes<2>(a, stream, downscale);
+	else if (a.scale == 4)
+		launch_bloom_passes<4>(a, stream, downscale);
+	else
+		launch_bloom_passes<8>(a, stream, downscale);
+}
+
 } // namespace
 
 int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream, cudaStream_t aux, cudaEvent_t fork,
@@ -345,7 +413,8 @@ int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream, cuda
 	if (a.use_bloom)
 	{
 		cudaMemsetAsync(a.line_sums, 0, sizeof(int32_t) * 4 * a.bh, stream);
-		pp_downscale_kernel<<<dim3((a.bw + 255) / 256, a.bh), block, 0, stream>>>(a);
+		if (a.scale != 2 && a.scale != 4 && a.scale != 8) return int(cudaErrorInvalidValue);
+		launch_bloom(a, stream, true);
 		// The exposure average is consumed only after the frame: with an auxiliary stream it runs
 		// beside the blur and tonemap passes.
 		const bool overlap = aux && fork && join;
@@ -361,7 +430,7 @@ int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream, cuda
 			pp_blur_h_kernel<<<dim3((a.bw + 255) / 256, a.bh), block, 0, stream>>>(a);
 			pp_blur_v_kernel<<<dim3((a.bw + 255) / 256, a.bh), block, 0, stream>>>(a);
 		}
-		pp_tonemap_bloom_kernel<<<dim3((a.width / 2 + 256) / 256, a.height), block, 0, stream>>>(a);
+		launch_bloom(a, stream, false);
 		if (overlap) cudaStreamWaitEvent(stream, join, 0);
 	}
 	else
