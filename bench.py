@@ -331,7 +331,7 @@ def run_frame_gpu(args, world, rank, local):
 
     lr = run_learned(args, work, r, ldr_frames, local) if args.learn_steps > 0 else None
     if lr is not None:
-        launches += args.steps * (1 + 3 + 5 + 5)  # half-resolution frame + convert and four convolutions
+        launches += args.steps * (1 + 3 + 5 + 1)  # half-resolution frame + the fused upscale kernel
 
     peak, peak_kind = peaks()
     s = args.steps
@@ -413,7 +413,7 @@ def learned_summary(lr, plain_ms, args):
                     "avg2x_mean": round(float(np.mean(p["avg2x"])), 3),
                     "nearest_mean": round(float(np.mean(p["nearest"])), 3),
                     "frames_at_or_above_38db": f"{sum(x >= 38.0 for x in p['learned'])}/{n}"},
-        "upscaler_roofline": {"bound": "tensor", "kernel": "conv_kernel (4 launches) + convert_input_kernel",
+        "upscaler_roofline": {"bound": "tensor", "kernel": "fused_upscale_kernel (one launch, four layers)",
                               "achieved": round(tf, 1), "peak": peak, "unit": "TFLOP/s", "frac": round(tf / peak, 4),
                               "peak_source": kind, "algorithmic_flops_per_launch": UPSCALER_FLOPS},
         "train": {"steps": args.learn_steps, "crops_per_step": 16, "crop": "128x64 half-resolution pixels",
@@ -550,8 +550,9 @@ def bf16_peak():
 
 
 def run_upscale_gpu(args, world, rank, local):
-    """Learned 2x upscale of a 960x540 Color32 frame to 1920x1080: convert + four tcgen05 convolution
-    launches per step, inputs resident in HBM, L2 flushed between steps."""
+    """Learned 2x upscale of a 960x540 Color32 frame to 1920x1080 by the fused four-layer tcgen05 kernel
+    (one launch per step; the layer-by-layer form, five launches, is timed beside it), inputs resident
+    in HBM, L2 flushed between steps."""
     import ctypes
 
     import torch
@@ -570,22 +571,30 @@ def run_upscale_gpu(args, world, rank, local):
     # a stream of our own: its handle is non-zero, so the upscaler runs on it (NULL selects the
     # upscaler's internal stream) and the events bracket exactly its kernels
     st = torch.cuda.Stream(device=dev)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    with torch.cuda.stream(st):
-        for _ in range(args.warmup):
-            flush.fill_(1.0)
-            ups.infer(lo, hi, stream=st.cuda_stream)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clocks, torch.cuda.stream(st):
-        for i in range(args.steps):
-            flush.fill_(1.0)
-            ev[i][0].record(st)
-            ups.infer(lo, hi, stream=st.cuda_stream)
-            ev[i][1].record(st)
+
+    def timed(steps):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(st):
+            for _ in range(args.warmup):
+                flush.fill_(1.0)
+                ups.infer(lo, hi, stream=st.cuda_stream)
+        if world > 1:
+            torch.distributed.barrier()
         torch.cuda.synchronize()
-    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+        with ClockSampler(local) as clocks, torch.cuda.stream(st):
+            for i in range(steps):
+                flush.fill_(1.0)
+                ev[i][0].record(st)
+                ups.infer(lo, hi, stream=st.cuda_stream)
+                ev[i][1].record(st)
+            torch.cuda.synchronize()
+        ups.check()
+        return sum(a.elapsed_time(b) for a, b in ev) / steps, clocks
+
+    ups.set_fused(False)
+    layered_ms, _ = timed(min(args.steps, 20))
+    ups.set_fused(True)
+    ms, clocks = timed(args.steps)
     if world > 1:
         tt = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
@@ -619,14 +628,15 @@ def run_upscale_gpu(args, world, rank, local):
             "config": {"workload": "learned 2x upscale 960x540 -> 1920x1080 (4-layer 3x3 CNN, 32 channels, pixel shuffle)",
                        "input": "tonemapped 960x540 frame of the 64-room map", "weights": "seeded initialisation",
                        "l2": "flushed (512 MiB write) before every timed step", "parallelism": f"replicas x{world}"},
-            "roofline": {"bound": "tensor", "kernel": "conv_kernel (4 launches) + convert_input_kernel", "achieved": round(tf, 1),
+            "layer_by_layer_ms": round(layered_ms, 5),
+            "roofline": {"bound": "tensor", "kernel": "fused_upscale_kernel (one launch, four layers)", "achieved": round(tf, 1),
                          "peak": peak, "unit": "TFLOP/s", "frac": round(tf / peak, 4), "peak_source": kind,
                          "algorithmic_flops_per_launch": UPSCALER_FLOPS, "traffic": None},
             "cpu_baseline": {"value": round(1.0 / cpu_s, 4), "unit": "frames/s", "cores": 1, "kind": "port",
                              "sample": "a quarter frame (135 of 540 rows) through the numpy FP32 oracle, scaled x4"},
             "e2e": {"value": round(1.0 / statistics.median(e2e), 2), "unit": "frames/s",
                     "h2d_bytes_per_step": int(lo_h.nbytes), "d2h_bytes_per_step": int(out_h.nbytes)},
-            "clocks": clocks.summary(), "gpu_launches": 5 * args.steps}), flush=True)
+            "clocks": clocks.summary(), "gpu_launches": args.steps}), flush=True)
     ups.close()
 
 

@@ -74,6 +74,12 @@ int sw_upscaler_steps(SwUpscaler* ups, uint64_t* out_steps);
 int sw_upscaler_infer(SwUpscaler* ups, const uint32_t* lo, uint32_t lo_width, uint32_t lo_height, uint32_t lo_pitch,
 	uint32_t* hi, uint32_t hi_pitch, void* stream);
 
+/* Inference by one fused kernel for all four layers (1, default; activations stay in shared memory) or
+ * by one launch per layer (0; activations through HBM). Both give the same bytes. */
+int sw_upscaler_set_fused(SwUpscaler* ups, int enable);
+/* Wait for the device and report whether any upscaler kernel gave up on a bounded wait. */
+int sw_upscaler_check(SwUpscaler* ups);
+
 /* PSNR (dB, colour channels b, g, r) between two device Color32 frames; 99 when identical. Waits. */
 int sw_upscaler_psnr(SwUpscaler* ups, const uint32_t* a, uint32_t a_pitch, const uint32_t* b, uint32_t b_pitch,
 	uint32_t width, uint32_t height, void* stream, double* out_psnr);

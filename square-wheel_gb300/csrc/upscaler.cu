@@ -544,6 +544,466 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_kernel(const __grid_cons
 	}
 }
 
+// ---- fused inference: all four layers in one kernel ----
+//
+// One CTA owns a strip of 128 computed columns [c0, c0 + 128), c0 = 120 t - 4, and a segment of output
+// rows [y_lo, y_hi). Every layer computes the strip's 128 columns; a column's value is exact while its
+// receptive field lies inside the strip, so after four 3x3 layers the middle 120 columns are exact and
+// are the strip's output (8 strips tile 960 columns). Layer l computes rows [y_lo - 3 + l, y_hi + 3 - l),
+// reading rows one further up and down; rows or columns outside the frame are zero, exactly as the zero
+// padding of the layer-by-layer convolution.
+//
+// Activations never leave the SM: layer l's input rows live in a shared-memory ring of FNS rows of
+// C8_l chunks x 136 pixels (the layout conv_kernel stages from HBM), written by
+//   warp 0 (all lanes) for layer 0: Color32 source -> (b, g, r) / 255 in bf16 (the input conversion),
+//   the epilogue warps of layer l - 1 for layers 1..3: TMEM -> bias + ReLU -> bf16.
+// MMAs are the dy-folded implicit GEMM of conv_kernel (128 pixels x 3 C_out x 16 per MMA, accumulated
+// in place in a TMEM ring of 4 output rows per layer), issued by two threads: warp 1 for layers 0 and
+// 2, warp 10 for layers 1 and 3 (in step s, layer l's input row s - FLAG l). Epilogue warps 2..5 drain
+// layers 0 and 2, warps 6..9 layers 1 and 3 (the last one writes the Color32 output: pixel shuffle +
+// bilinear residual); in step s they handle layer l's output row s - 2 - FLAG l. A layer's output row is
+// complete two rows after its first input row, so FLAG - 2 steps of slack separate the epilogue that
+// writes a row from the MMAs that read it: enough to cover the tensor pipe's queue and the epilogue
+// itself, so that the roles run as a pipeline rather than a chain. The slot an epilogue writes was read
+// about FNS + 2 - FLAG steps earlier.
+constexpr int FNS = 5;          // input-row slots per layer
+constexpr int FR = 4;           // TMEM output-row accumulators per layer
+constexpr int FLAG = 5;         // rows of lag between layers
+constexpr int F_THREADS = 352;  // 11 warps
+constexpr int F_VALID = 120;    // output columns per strip
+constexpr uint32_t F_TMEM_COLS = 512;
+
+struct FusedArgs
+{
+	const uint32_t* lo;
+	uint32_t lo_w, lo_h, lo_pitch;
+	uint32_t* hi;
+	uint32_t hi_pitch;
+	const uint16_t* w[NUM_LAYERS]; // packed B operands (conv_kernel's forward layout)
+	const float* bias[NUM_LAYERS];
+	uint32_t strips, segments;     // grid = strips x segments
+	int* error;
+};
+
+// Per-layer constants.
+template <int L>
+struct FL
+{
+	static constexpr int C8 = L == 0 ? 2 : 4;
+	static constexpr int N = L == 3 ? 16 : 32;
+	static constexpr int KSTEPS = C8 / 2;
+	static constexpr int NB = 3 * N;
+	static constexpr uint32_t SLOT = (C8 * CXS_BYTES + 127) / 128 * 128;
+	static constexpr uint32_t WBYTES = 3 * KSTEPS * 2 * NB * 16;
+	static constexpr uint32_t TCOL = L * 4 * 32; // TMEM column base (layers 0..2: 128 columns, 3: 64)
+};
+
+struct FusedSmem
+{
+	static constexpr uint32_t RING0 = 0;
+	static constexpr uint32_t RING1 = RING0 + FNS * FL<0>::SLOT;
+	static constexpr uint32_t RING2 = RING1 + FNS * FL<1>::SLOT;
+	static constexpr uint32_t RING3 = RING2 + FNS * FL<2>::SLOT;
+	static constexpr uint32_t W0 = RING3 + FNS * FL<3>::SLOT;
+	static constexpr uint32_t W1 = W0 + FL<0>::WBYTES;
+	static constexpr uint32_t W2 = W1 + FL<1>::WBYTES;
+	static constexpr uint32_t W3 = W2 + FL<2>::WBYTES;
+	static constexpr uint32_t BARS = W3 + FL<3>::WBYTES;
+	// barriers: full[4][FNS], rowbar[4][NBAR], accfree[4][FR], wbar, done[2]
+	static constexpr uint32_t NUM_BARS = 4 * FNS + 4 * NBAR + 4 * FR + 3;
+	static constexpr uint32_t MISC = BARS + NUM_BARS * 8;
+	static constexpr uint32_t TOTAL = MISC + 64;
+};
+static_assert(FusedSmem::TOTAL <= 227 * 1024, "fused kernel shared memory");
+
+__device__ __forceinline__ uint32_t ring_base(int l)
+{
+	return l == 0 ? FusedSmem::RING0 : l == 1 ? FusedSmem::RING1 : l == 2 ? FusedSmem::RING2 : FusedSmem::RING3;
+}
+
+// Barriers of layer l: full[FNS] (input row written), rowbar[NBAR] (input row's MMAs done), accfree[FR]
+// (output-row accumulator drained).
+__device__ __forceinline__ uint64_t* f_full(unsigned char* smem, int l)
+{
+	return reinterpret_cast<uint64_t*>(smem + FusedSmem::BARS) + l * FNS;
+}
+__device__ __forceinline__ uint64_t* f_rowbar(unsigned char* smem, int l)
+{
+	return reinterpret_cast<uint64_t*>(smem + FusedSmem::BARS) + 4 * FNS + l * NBAR;
+}
+// Each MMA issuer commits once per step (issuer l & 1 serves layers l and l + 2; layer l's input row i
+// is issued in step i + FLAG l), so "input row i of layer l consumed" is the completion of that step.
+__device__ __forceinline__ bool f_wait_input_done(unsigned char* smem, int l, int i)
+{
+	const int s = i + FLAG * l;
+	const bool ok = mbar_wait_bounded(&f_rowbar(smem, l & 1)[s % NBAR], (s / NBAR) & 1, POLL_LIMIT);
+	return __all_sync(0xFFFFFFFFu, ok);
+}
+__device__ __forceinline__ uint64_t* f_accfree(unsigned char* smem, int l)
+{
+	return reinterpret_cast<uint64_t*>(smem + FusedSmem::BARS) + 4 * FNS + 4 * NBAR + l * FR;
+}
+
+// Rows of layer l of a segment: outputs [A, B), inputs [A - 1, B] (input index i <-> row A - 1 + i).
+// Layer l + 1's input index i is layer l's output index i.
+struct LayerRows
+{
+	int A, B;
+	__device__ int inputs() const { return B - A + 2; }
+	__device__ int outputs() const { return B - A; }
+};
+__device__ __forceinline__ LayerRows layer_rows(int l, int y_lo, int y_hi) { return LayerRows{y_lo - 3 + l, y_hi + 3 - l}; }
+
+// Layer 0's source pixels of row y, columns c0 - 1 + j for j = lane + 32 k (the 136 staged pixels); 0
+// outside the frame (converts to the zero padding) or when `valid` is false.
+constexpr int F0_PX = (CXS + 31) / 32;
+constexpr int F0_AHEAD = 3;
+__device__ __forceinline__ void f0_load_row(const FusedArgs& a, int y, bool valid, int c0, int lane, uint32_t (&px)[F0_PX])
+{
+	const bool row_in = valid && y >= 0 && y < int(a.lo_h);
+	const uint32_t* row = a.lo + size_t(row_in ? y : 0) * a.lo_pitch;
+#pragma unroll
+	for (int k = 0; k < F0_PX; ++k)
+	{
+		const int j = lane + 32 * k, x = c0 - 1 + j;
+		px[k] = row_in && j < CXS && x >= 0 && x < int(a.lo_w) ? __ldg(row + x) : 0u;
+	}
+}
+
+// MMA group of layer L for its input index i (row A - 1 + i): the dy-folded K steps into the TMEM ring.
+// Returns false if a bounded wait expired.
+template <int L>
+__device__ __forceinline__ bool fused_mma(unsigned char* smem, uint32_t tmem, int y_lo, int y_hi, int i)
+{
+	using F = FL<L>;
+	constexpr int N = F::N;
+	const LayerRows lr = layer_rows(L, y_lo, y_hi);
+	uint64_t* full = f_full(smem, L);
+	uint64_t* accfree = f_accfree(smem, L);
+	if (!mbar_wait_bounded(&full[i % FNS], (i / FNS) & 1, POLL_LIMIT)) return false;
+	const int yi = lr.A - 1 + i;
+	const int j_lo = max(0, yi + 2 - lr.B), j_hi = min(2, yi + 1 - lr.A);
+	const uint32_t o_first = uint32_t(yi + 1 - j_lo - lr.A);
+	const uint32_t b0 = (FR - o_first % FR) % FR;
+	if (j_lo == 0 && o_first >= FR && !mbar_wait_bounded(&accfree[b0], ((o_first / FR) - 1) & 1, POLL_LIMIT)) return false;
+	fence_after_sync();
+	const uint64_t a_row = make_sdesc(smem_addr(smem + ring_base(L) + (i % FNS) * F::SLOT), CXS_BYTES, 128);
+	const uint32_t wofs = L == 0 ? FusedSmem::W0 : L == 1 ? FusedSmem::W1 : L == 2 ? FusedSmem::W2 : FusedSmem::W3;
+	const uint64_t b_base = make_sdesc(smem_addr(smem + wofs), F::NB * 16, 128);
+	constexpr uint32_t ID1 = make_idesc_bf16(128, N, 0, 0), ID2 = make_idesc_bf16(128, 2 * N, 0, 0),
+					   ID3 = make_idesc_bf16(128, 3 * N, 0, 0);
+	const uint32_t tcol = tmem + F::TCOL;
+	if (j_lo == 0 && j_hi == 2 && b0 + 3 <= uint32_t(FR))
+	{
+		const uint32_t d = tcol + b0 * N;
+#pragma unroll
+		for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+			for (int ks = 0; ks < F::KSTEPS; ++ks)
+				mma_bf16(d, a_row + ((2 * ks * CXS_BYTES + dx * 16) >> 4), b_base + (((dx * F::KSTEPS + ks) * (2 * F::NB * 16)) >> 4),
+					ID3, 1u);
+	}
+	else
+	{
+		const int nj = j_hi - j_lo + 1;
+		const int len0 = min(nj, int(FR - b0));
+		const uint32_t bo0 = uint32_t(j_lo * N * 16) >> 4, bo1 = uint32_t((j_lo + len0) * N * 16) >> 4;
+		const uint32_t id0 = len0 == 1 ? ID1 : len0 == 2 ? ID2 : ID3;
+		const uint32_t id1 = nj - len0 == 1 ? ID1 : ID2;
+		const bool two = len0 < nj;
+#pragma unroll
+		for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+			for (int ks = 0; ks < F::KSTEPS; ++ks)
+			{
+				const uint64_t ad = a_row + ((2 * ks * CXS_BYTES + dx * 16) >> 4);
+				const uint64_t bk = b_base + (((dx * F::KSTEPS + ks) * (2 * F::NB * 16)) >> 4);
+				mma_bf16(tcol + b0 * N, ad, bk + bo0, id0, 1u);
+				if (two) mma_bf16(tcol, ad, bk + bo1, id1, 1u);
+			}
+	}
+	return true;
+}
+
+// Epilogue of layer L for its output index o (row A + o): accumulators -> registers, zero and release the
+// accumulator, then the next layer's input row (layers 0..2) or the Color32 output (layer 3). The four
+// warps of one group call this together (warp quad = lane quadrant = pixels quad*32..).
+template <int L>
+__device__ __forceinline__ bool fused_epilogue(const FusedArgs& a, unsigned char* smem, uint32_t tmem, int y_lo, int y_hi, int o, int c0,
+	int quad, int lane, const float (&bias)[FL<L>::N])
+{
+	using F = FL<L>;
+	constexpr int N = F::N;
+	const LayerRows lr = layer_rows(L, y_lo, y_hi);
+	uint64_t* accfree = f_accfree(smem, L);
+	const int i = quad * 32 + lane; // pixel of the strip
+	const int x = c0 + i;
+	const int y = lr.A + o;
+	// layer 3: the source pixels of the bilinear residual, loaded before the wait (rows y - 1, y, y + 1
+	// and columns x - 1, x, x + 1, clamped to the frame)
+	const bool out_px = L == 3 && i >= 4 && i < 4 + F_VALID && x < int(a.lo_w) && y < int(a.lo_h);
+	uint32_t p[3][3];
+	if constexpr (L == 3)
+	{
+		if (out_px)
+		{
+#pragma unroll
+			for (int r = 0; r < 3; ++r)
+			{
+				const uint32_t* row = a.lo + size_t(min(max(y - 1 + r, 0), int(a.lo_h) - 1)) * a.lo_pitch;
+				p[r][0] = __ldg(row + max(x - 1, 0));
+				p[r][1] = __ldg(row + x);
+				p[r][2] = __ldg(row + min(x + 1, int(a.lo_w) - 1));
+			}
+		}
+	}
+	const int kc = o + 2; // the layer's input index that completes output o
+	if (!f_wait_input_done(smem, L, kc)) return false;
+	fence_after_sync();
+	const uint32_t b = (FR - uint32_t(o) % FR) % FR;
+	const uint32_t taddr = tmem + (uint32_t(quad * 32) << 16) + F::TCOL + b * N;
+	float v[N];
+#pragma unroll
+	for (int c8 = 0; c8 < N / 8; ++c8)
+	{
+		float t8[8];
+		tmem_ld8(taddr + c8 * 8, t8);
+#pragma unroll
+		for (int e = 0; e < 8; ++e) v[c8 * 8 + e] = t8[e];
+	}
+	tmem_ld_wait();
+#pragma unroll
+	for (int c8 = 0; c8 < N / 8; ++c8) tmem_zero8(taddr + c8 * 8);
+	tmem_st_wait();
+	fence_before_sync();
+	__syncwarp();
+	if (lane == 0) mbar_arrive(&accfree[b]);
+	if constexpr (L < 3)
+	{
+		uint64_t* next_full = f_full(smem, L + 1);
+		// next layer's input index o: wait until its slot's previous row was consumed
+		if (o >= FNS && !f_wait_input_done(smem, L + 1, o - FNS)) return false;
+		const bool inside = x >= 0 && x < int(a.lo_w) && y >= 0 && y < int(a.lo_h);
+		unsigned char* dst = smem + ring_base(L + 1) + (o % FNS) * FL<L + 1>::SLOT + (1 + i) * 16;
+#pragma unroll
+		for (int c8 = 0; c8 < N / 8; ++c8)
+		{
+			uint32_t w4[4];
+#pragma unroll
+			for (int q = 0; q < 4; ++q)
+				w4[q] = inside ? pack2(fmaxf(v[c8 * 8 + 2 * q] + bias[c8 * 8 + 2 * q], 0.0f),
+									 fmaxf(v[c8 * 8 + 2 * q + 1] + bias[c8 * 8 + 2 * q + 1], 0.0f))
+							   : 0u;
+			*reinterpret_cast<uint4*>(dst + c8 * CXS_BYTES) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+		}
+		fence_proxy_async();
+		__syncwarp();
+		if (lane == 0) mbar_arrive(&next_full[o % FNS]);
+	}
+	else
+	{
+		// output stage: columns c0 + 4 .. c0 + 123 of the strip, inside the frame
+		if (out_px)
+		{
+#pragma unroll
+			for (int sy = 0; sy < 2; ++sy)
+			{
+				const uint32_t p11 = p[1][1], p10 = p[1][0], p12 = p[1][2];
+				const uint32_t p21 = p[sy ? 2 : 0][1], p20 = p[sy ? 2 : 0][0], p22 = p[sy ? 2 : 0][2];
+				uint32_t px[2];
+#pragma unroll
+				for (int sx = 0; sx < 2; ++sx)
+				{
+					const int s = sy * 2 + sx;
+					const uint32_t a01 = sx ? p12 : p10, a11 = sx ? p22 : p20;
+					uint32_t bytes = p11 & 0xFF000000u;
+#pragma unroll
+					for (int ch = 0; ch < 3; ++ch)
+					{
+						const float top = 0.75f * float((p11 >> (8 * ch)) & 255u) + 0.25f * float((a01 >> (8 * ch)) & 255u);
+						const float bot = 0.75f * float((p21 >> (8 * ch)) & 255u) + 0.25f * float((a11 >> (8 * ch)) & 255u);
+						const float pred = (0.75f * top + 0.25f * bot) * (1.0f / 255.0f) + (v[ch * 4 + s] + bias[ch * 4 + s]);
+						bytes |= to_byte(pred) << (8 * ch);
+					}
+					px[sx] = bytes;
+				}
+				*reinterpret_cast<uint2*>(a.hi + size_t(2 * y + sy) * a.hi_pitch + 2 * x) = make_uint2(px[0], px[1]);
+			}
+		}
+	}
+	return true;
+}
+
+__global__ void __launch_bounds__(F_THREADS, 1) fused_upscale_kernel(const __grid_constant__ FusedArgs a)
+{
+	extern __shared__ __align__(1024) unsigned char smem[];
+	uint64_t* wbar = reinterpret_cast<uint64_t*>(smem + FusedSmem::BARS) + 4 * FNS + 4 * NBAR + 4 * FR;
+	uint64_t* done = wbar + 1; // [2]: one per MMA issuer
+	uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + FusedSmem::MISC);
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int strip = int(blockIdx.x % a.strips), seg = int(blockIdx.x / a.strips);
+	const int H = int(a.lo_h);
+	const int y_lo = int((int64_t(seg) * H) / int(a.segments)), y_hi = int((int64_t(seg + 1) * H) / int(a.segments));
+	const int c0 = strip * F_VALID - 4;
+
+	// zero every ring slot (halo pixels are never written; layer 0's second chunk stays zero)
+	for (uint32_t off = tid * 16; off < FusedSmem::W0; off += F_THREADS * 16)
+		*reinterpret_cast<uint4*>(smem + off) = make_uint4(0u, 0u, 0u, 0u);
+	if (tid == 0)
+	{
+		for (int l = 0; l < 4; ++l)
+		{
+			for (int k = 0; k < FNS; ++k) mbar_init(&f_full(smem, l)[k], l == 0 ? 32 : 4);
+			for (int k = 0; k < NBAR; ++k) mbar_init(&f_rowbar(smem, l)[k], 1);
+			for (int k = 0; k < FR; ++k) mbar_init(&f_accfree(smem, l)[k], 4);
+		}
+		mbar_init(wbar, 1);
+		mbar_init(&done[0], 1);
+		mbar_init(&done[1], 1);
+		fence_mbar_init();
+	}
+	if (warp == 1)
+	{
+		tmem_alloc(s_tmem, F_TMEM_COLS);
+		tmem_relinquish();
+	}
+	fence_proxy_async();
+	fence_before_sync();
+	__syncthreads();
+	fence_after_sync();
+	const uint32_t tmem = *s_tmem;
+	if (warp >= 2 && warp <= 9)
+	{
+		// every accumulator starts at zero (the MMAs always accumulate)
+		const uint32_t lb = uint32_t((warp & 3) * 32) << 16;
+		const uint32_t c_lo = warp <= 5 ? 0u : 256u, c_hi = warp <= 5 ? 256u : 448u; // halves of the 448 used columns
+		for (uint32_t c = c_lo; c < c_hi; c += 8) tmem_zero8(tmem + lb + c);
+		tmem_st_wait();
+	}
+	fence_before_sync();
+	__syncthreads();
+	fence_after_sync();
+
+	const LayerRows lr0 = layer_rows(0, y_lo, y_hi);
+	const int steps = lr0.inputs() + 3 * FLAG;
+	bool failed = false;
+
+	if (warp == 0)
+	{
+		// layer 0 input rows from the Color32 source. Lane t holds pixels t + 32 k (k < F0_PX) of a row;
+		// the loads of a row are issued F0_AHEAD rows before it is stored, so their latency overlaps the
+		// waits for ring slots instead of adding to every row.
+		uint64_t* full0 = f_full(smem, 0);
+
+		const int n0 = lr0.inputs();
+		uint32_t pre[F0_AHEAD + 1][F0_PX];
+#pragma unroll
+		for (int r = 0; r < F0_AHEAD; ++r) f0_load_row(a, lr0.A - 1 + r, r < n0, c0, lane, pre[r]);
+		for (int q = 0; q < n0 && !failed; ++q)
+		{
+			f0_load_row(a, lr0.A - 1 + q + F0_AHEAD, q + F0_AHEAD < n0, c0, lane, pre[F0_AHEAD]);
+			if (q >= FNS && !f_wait_input_done(smem, 0, q - FNS))
+			{
+				failed = true;
+				break;
+			}
+			unsigned char* dst = smem + FusedSmem::RING0 + (q % FNS) * FL<0>::SLOT;
+#pragma unroll
+			for (int k = 0; k < F0_PX; ++k)
+			{
+				const int j = lane + 32 * k;
+				if (j < CXS)
+				{
+					const uint32_t px = pre[0][k];
+					uint4 w4;
+					w4.x = pack2(float(px & 255u) * (1.0f / 255.0f), float((px >> 8) & 255u) * (1.0f / 255.0f));
+					w4.y = pack2(float((px >> 16) & 255u) * (1.0f / 255.0f), 0.0f);
+					w4.z = 0u;
+					w4.w = 0u;
+					*reinterpret_cast<uint4*>(dst + j * 16) = w4;
+				}
+			}
+			fence_proxy_async();
+			mbar_arrive(&full0[q % FNS]);
+#pragma unroll
+			for (int r = 0; r < F0_AHEAD; ++r)
+#pragma unroll
+				for (int k = 0; k < F0_PX; ++k) pre[r][k] = pre[r + 1][k];
+		}
+	}
+	else if (warp == 1 || warp == 10)
+	{
+		if (lane == 0)
+		{
+			if (warp == 1)
+			{
+				mbar_expect_tx(wbar, FL<0>::WBYTES + FL<1>::WBYTES + FL<2>::WBYTES + FL<3>::WBYTES);
+				bulk_g2s(smem + FusedSmem::W0, a.w[0], FL<0>::WBYTES, wbar);
+				bulk_g2s(smem + FusedSmem::W1, a.w[1], FL<1>::WBYTES, wbar);
+				bulk_g2s(smem + FusedSmem::W2, a.w[2], FL<2>::WBYTES, wbar);
+				bulk_g2s(smem + FusedSmem::W3, a.w[3], FL<3>::WBYTES, wbar);
+			}
+			failed = !mbar_wait_bounded(wbar, 0, POLL_LIMIT);
+			const int la = warp == 1 ? 0 : 1; // this issuer's layers: la and la + 2
+			const int n_a = layer_rows(la, y_lo, y_hi).inputs(), n_b = layer_rows(la + 2, y_lo, y_hi).inputs();
+			for (int s = 0; s < steps && !failed; ++s)
+			{
+				const int i0 = s - FLAG * la, i1 = s - FLAG * (la + 2);
+				if (i0 >= 0 && i0 < n_a)
+					failed = !(la == 0 ? fused_mma<0>(smem, tmem, y_lo, y_hi, i0) : fused_mma<1>(smem, tmem, y_lo, y_hi, i0));
+				if (!failed && i1 >= 0 && i1 < n_b)
+					failed = !(la == 0 ? fused_mma<2>(smem, tmem, y_lo, y_hi, i1) : fused_mma<3>(smem, tmem, y_lo, y_hi, i1));
+				if (!failed) mma_commit(&f_rowbar(smem, la)[s % NBAR]); // the step's rows are consumed
+			}
+			uint64_t* d = &done[warp == 1 ? 0 : 1];
+			mma_commit(d);
+			if (!mbar_wait_bounded(d, 0, POLL_LIMIT)) failed = true;
+		}
+	}
+	else
+	{
+		const int quad = warp & 3;
+		const bool group_a = warp <= 5; // layers 0 and 2; otherwise 1 and 3
+		const int la = group_a ? 0 : 1, lb = la + 2;
+		float bias_a[32], bias_b2[32], bias_b3[16];
+#pragma unroll
+		for (int c = 0; c < 32; ++c)
+		{
+			bias_a[c] = a.bias[la][c];
+			bias_b2[c] = a.bias[2][c];
+		}
+#pragma unroll
+		for (int c = 0; c < 16; ++c) bias_b3[c] = a.bias[3][c];
+		const int n_a = layer_rows(la, y_lo, y_hi).outputs(), n_b = layer_rows(lb, y_lo, y_hi).outputs();
+		for (int s = 0; s < steps && !failed; ++s)
+		{
+			// layer l's output o completes at its input o + 2, i.e. in step o + 2 + FLAG * l
+			const int oa = s - 2 - FLAG * la, ob = s - 2 - FLAG * lb;
+			if (oa >= 0 && oa < n_a)
+			{
+				const bool ok = group_a ? fused_epilogue<0>(a, smem, tmem, y_lo, y_hi, oa, c0, quad, lane, bias_a)
+										: fused_epilogue<1>(a, smem, tmem, y_lo, y_hi, oa, c0, quad, lane, bias_a);
+				if (!ok) failed = true;
+			}
+			if (!failed && ob >= 0 && ob < n_b)
+			{
+				const bool ok = group_a ? fused_epilogue<2>(a, smem, tmem, y_lo, y_hi, ob, c0, quad, lane, bias_b2)
+										: fused_epilogue<3>(a, smem, tmem, y_lo, y_hi, ob, c0, quad, lane, bias_b3);
+				if (!ok) failed = true;
+			}
+		}
+	}
+	if (failed) atomicExch(a.error, 1);
+	fence_before_sync();
+	__syncthreads();
+	if (warp == 1)
+	{
+		fence_after_sync();
+		tmem_dealloc(tmem, F_TMEM_COLS);
+	}
+}
+
 // ---- weight gradient ----
 
 struct WgradArgs
@@ -877,6 +1337,7 @@ struct SwUpscaler
 	uint32_t i_w = 0, i_h = 0;
 	CropGpu i_crop_host{};
 	bool i_crop_valid = false;
+	bool fused = true; // inference by fused_upscale_kernel (else the four layer launches)
 	DevMem psnr_sum;
 	unsigned long long* h_psnr = nullptr;
 	cudaEvent_t ev = nullptr;
@@ -1353,6 +1814,33 @@ int sw_upscaler_infer(SwUpscaler* u, const uint32_t* lo, uint32_t lo_width, uint
 	UP_CUDA(u, cudaSetDevice(u->device));
 	cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : u->stream;
 	int r;
+	if (u->fused)
+	{
+		static bool configured = false;
+		if (!configured)
+		{
+			UP_CUDA(u, cudaFuncSetAttribute(fused_upscale_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, FusedSmem::TOTAL));
+			configured = true;
+		}
+		FusedArgs f;
+		f.lo = lo;
+		f.lo_w = lo_width;
+		f.lo_h = lo_height;
+		f.lo_pitch = lo_pitch;
+		f.hi = hi;
+		f.hi_pitch = hi_pitch;
+		for (int l = 0; l < NUM_LAYERS; ++l)
+		{
+			f.w[l] = static_cast<const uint16_t*>(u->wfwd[l].ptr);
+			f.bias[l] = static_cast<const float*>(u->bias[l].ptr);
+		}
+		f.strips = (lo_width + F_VALID - 1) / F_VALID;
+		f.segments = std::max(1u, std::min(lo_height, uint32_t(u->num_sms) / f.strips));
+		f.error = static_cast<int*>(u->error.ptr);
+		fused_upscale_kernel<<<f.strips * f.segments, F_THREADS, FusedSmem::TOTAL, s>>>(f);
+		UP_CUDA(u, cudaGetLastError());
+		return SW_OK;
+	}
 	if (lo_width != u->i_w || lo_height != u->i_h)
 	{
 		UP_CUDA(u, cudaStreamSynchronize(s));
@@ -1396,6 +1884,21 @@ int sw_upscaler_infer(SwUpscaler* u, const uint32_t* lo, uint32_t lo_width, uint
 	a.in = P, a.wpack = static_cast<uint16_t*>(u->wfwd[3].ptr), a.bias = static_cast<float*>(u->bias[3].ptr);
 	if ((r = launch_conv<4, 16, EPI_INFER>(u, a, s))) return r;
 	return SW_OK;
+}
+
+int sw_upscaler_set_fused(SwUpscaler* u, int enable)
+{
+	if (!u) return SW_ERR_INVALID_ARGUMENT;
+	u->fused = enable != 0;
+	return SW_OK;
+}
+
+int sw_upscaler_check(SwUpscaler* u)
+{
+	if (!u) return SW_ERR_INVALID_ARGUMENT;
+	UP_CUDA(u, cudaSetDevice(u->device));
+	UP_CUDA(u, cudaDeviceSynchronize());
+	return check_error_flag(u, u->stream);
 }
 
 int sw_upscaler_psnr(SwUpscaler* u, const uint32_t* a, uint32_t a_pitch, const uint32_t* b, uint32_t b_pitch, uint32_t width,

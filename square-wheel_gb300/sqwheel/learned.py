@@ -125,6 +125,13 @@ class Upscaler:
         self._check(self.lib.sw_upscaler_infer(self.h, _ptr(lo), lo.shape[1], lo.shape[0], lo.stride(0), _ptr(hi),
                                                hi.stride(0), ctypes.c_void_p(stream or None)), "infer")
 
+    def set_fused(self, enable):
+        self._check(self.lib.sw_upscaler_set_fused(self.h, 1 if enable else 0), "set_fused")
+
+    def check(self):
+        """Wait for the device; raises if a kernel gave up on a bounded wait."""
+        self._check(self.lib.sw_upscaler_check(self.h), "check")
+
     def psnr(self, a, b, stream=0):
         out = ctypes.c_double()
         self._check(self.lib.sw_upscaler_psnr(self.h, _ptr(a), a.stride(0), _ptr(b), b.stride(0), a.shape[1], a.shape[0],

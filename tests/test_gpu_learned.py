@@ -80,6 +80,28 @@ def test_inference_matches_oracle(ups, w, h):
     assert np.all(got[:, 2 * w:] == 0)  # nothing written past the row
 
 
+@pytest.mark.parametrize("w,h", [(960, 540), (250, 37), (121, 240), (120, 3)])
+def test_fused_inference_equals_layered(ups, w, h):
+    """The fused four-layer kernel gives the same bytes as one launch per layer (strip edges, segment
+    edges, frame borders, widths that are not multiples of the 120-column strips)."""
+    import torch
+    rng = np.random.default_rng(w + 7 * h)
+    lo = _dev(_frame(rng, h, w))
+    a = torch.zeros((2 * h, 2 * w), dtype=torch.int32, device="cuda:0")
+    b = torch.zeros_like(a)
+    try:
+        ups.set_fused(True)
+        ups.infer(lo, a)
+        ups.check()
+        ups.set_fused(False)
+        ups.infer(lo, b)
+        ups.check()
+    finally:
+        ups.set_fused(True)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b), int((a != b).sum())
+
+
 def test_learned_mode_through_context(ups, gpu_ok):
     import torch
     scene = host.Scene(**host.SMALL_MAP)
