@@ -168,6 +168,13 @@ typedef struct SwVertex16 {
 
 #define SW_MAX_POLYGON_VERTICES 24 /* MAX_VERTICES, src/square_wheel/renderer_utils.rs:4 */
 
+/* Where a draw's texture lives. */
+typedef enum SwTexSource {
+	SW_TEXSRC_SURFACE = 0, /* a surface of the frame's surface arena (world polygons) */
+	SW_TEXSRC_SKYBOX = 1,  /* a skybox side texture at one mip (draw_skybox, partial_renderer.rs:2311-2448),
+	                       in the texels uploaded by sw_set_skybox */
+} SwTexSource;
+
 /* One Rasterizer::fill_polygon call (src/square_wheel/rasterizer.rs:35-80) as emitted by
  * draw_polygon (src/square_wheel/partial_renderer.rs:4011-4142). Equations are the ones passed to
  * fill_polygon (already scaled by z_scale for the non-affine modes). */
@@ -178,9 +185,9 @@ typedef struct SwDrawCmd {
 	uint32_t blend;        /* SwBlend */
 	float depth_eq[3];     /* d_inv_z_dx, d_inv_z_dy, k */
 	float tc_eq[6];        /* d_tc_dx[2], d_tc_dy[2], k[2] */
-	uint32_t tex_size[2];  /* surface size */
-	uint32_t reserved;
-	uint64_t tex_offset;   /* surface's first texel in the surface arena */
+	uint32_t tex_size[2];  /* texture size (surface, or skybox side mip: size x size) */
+	uint32_t tex_source;   /* SwTexSource */
+	uint64_t tex_offset;   /* texture's first texel in the surface arena or the skybox texels */
 } SwDrawCmd;
 
 typedef struct SwFrameParams {
@@ -238,8 +245,16 @@ int sw_rebuild_surfaces(SwCtx* ctx);
  * sw_submit_surfaces, e.g. textures the caller prepared itself. */
 int sw_set_surfaces(SwCtx* ctx, const void* texels, uint64_t total_texels);
 
-/* Draw commands in exact submission order (draw_tree/draw_leaf/draw_polygon,
- * partial_renderer.rs:2450-2559, 4011-4142). */
+/* Skybox side textures of the map's sky material (SkyboxTextures<Color32> and <Color64>,
+ * src/square_wheel/textures.rs:79-87, as MapMaterialsProcessor::get_skybox_textures returns them:
+ * make_skybox_side_texture{,64} + make_skybox_side_texture_mips, textures.rs:183-290). Every side's mips
+ * concatenated in the same order in both formats, so one texel offset (SwDrawCmd::tex_offset with
+ * tex_source SW_TEXSRC_SKYBOX) addresses both; draws read the array of the frame's pixel format.
+ * Synchronous upload; NULL / 0 texels removes the skybox. Load-time data like sw_create's. */
+int sw_set_skybox(SwCtx* ctx, const uint32_t* texels32, const uint64_t* texels64, uint64_t num_texels);
+
+/* Draw commands in exact submission order (draw_skybox, then draw_tree/draw_leaf/draw_polygon,
+ * partial_renderer.rs:1285-1325, 2311-2559, 4011-4142). */
 int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices,
 	uint32_t num_vertices);
 

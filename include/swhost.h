@@ -32,11 +32,18 @@ typedef struct SwhSceneConfig {
 	uint32_t num_dynamic_lights;  /* moving point lights */
 	uint32_t num_frames;          /* camera path length */
 	float emissive_frac;          /* fraction of materials with an emissive layer */
+	uint32_t sky_rooms;           /* rooms whose ceiling is sky (0 = no sky material) */
+	uint32_t skybox_size;         /* skybox side texture size (power of two, 16..2048) */
+	float skybox_brightness;      /* skybox material brightness (SkyboxParams) */
+	int32_t skybox_missing_side;  /* a side without texture (0..5: -X, +X, -Y, +Y, -Z, +Z), -1 = none */
+	float sky_rotation_speed;     /* skybox rotation about the vertical axis, radians per frame */
+	float camera_pitch;           /* added to the camera path's elevation (radians, up > 0) */
 } SwhSceneConfig;
 
 typedef struct SwhSceneInfo {
 	uint32_t nodes, leafs, polygons, portals, materials, frames, dynamic_lights, reserved;
 	uint64_t lightmap_elements, texels;
+	uint64_t skybox_texels; /* texels of all skybox sides and mips (per format) */
 } SwhSceneInfo;
 
 typedef struct SwhScene SwhScene;
@@ -46,6 +53,11 @@ int swh_scene_destroy(SwhScene* scene);
 int swh_scene_info(const SwhScene* scene, SwhSceneInfo* out_info);
 /* Static data for sw_create; pointers stay valid while the scene lives. */
 int swh_scene_create_info(const SwhScene* scene, uint32_t device, SwCreateInfo* out_info);
+/* Skybox texels for sw_set_skybox (Color32 and Color64 copies, the same layout) and, per side
+ * (-X, +X, -Y, +Y, -Z, +Z) and mip, the first texel and size (0 = none): mip_offsets[side * 5 + mip].
+ * Pointers stay valid while the scene lives; *out_count is 0 without a sky material. */
+int swh_scene_skybox(const SwhScene* scene, const uint32_t** out_texels32, const uint64_t** out_texels64,
+	uint64_t* out_count, uint64_t mip_offsets[30], uint32_t mip_sizes[30]);
 const char* swh_last_error(void);
 
 typedef struct SwhFrameOptions {
@@ -68,6 +80,7 @@ typedef struct SwhFrameOutputs {
 	const SwLight* lights;
 	SwFrameParams params;
 	uint32_t visible_leafs, camera_leaf;
+	uint32_t skybox_draws; /* draws of the skybox (the first ones) */
 } SwhFrameOutputs;
 
 typedef struct SwhFrame SwhFrame;

@@ -32,7 +32,7 @@ def load():
     lib = ctypes.CDLL(LIB_PATH)
     vp, u32, u64, i32, f32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_float
     lib.orc_build_surfaces.argtypes = [vp, vp, u32, vp, u32, vp, vp, u64, u32]
-    lib.orc_rasterize.argtypes = [vp, u32, vp, u32, vp, u64, vp, vp, u32, u32, ctypes.POINTER(u64)]
+    lib.orc_rasterize.argtypes = [vp, u32, vp, u32, vp, u64, vp, u64, vp, vp, u32, u32, ctypes.POINTER(u64)]
     lib.orc_clear_background.argtypes = [vp, vp, u32]
     lib.orc_postprocess.argtypes = [vp, vp, u32, u32, f32, vp, ctypes.POINTER(f32), vp, u32, vp]
     lib.orc_upscale.argtypes = [u32, u32, vp, vp, u32, u32, u32]
@@ -62,15 +62,17 @@ def build_surfaces(static, surfaces, lights, frame_params, total_texels, num_thr
     return arena
 
 
-def rasterize(draws, vertices, arena, frame_params, framebuffer, num_threads=1):
-    """Rasterise into `framebuffer` (height, pitch) in place; returns the count of bad texel fetches."""
+def rasterize(draws, vertices, arena, frame_params, framebuffer, num_threads=1, skybox=None):
+    """Rasterise into `framebuffer` (height, pitch) in place; returns the count of bad texel fetches.
+    skybox: the skybox texels (frame's pixel format) that SW_TEXSRC_SKYBOX draws read."""
     lib = load()
     draws = np.ascontiguousarray(draws, dtype=abi.DRAW_CMD)
     vertices = np.ascontiguousarray(vertices, dtype=abi.VERTEX16)
     bad = ctypes.c_uint64(0)
+    sky_ptr, sky_n = (None, 0) if skybox is None or len(skybox) == 0 else (abi.ptr(skybox), len(skybox))
     _check(lib.orc_rasterize(abi.ptr(draws), draws.size, abi.ptr(vertices), vertices.size, abi.ptr(arena), arena.size,
-                             ctypes.byref(frame_params), abi.ptr(framebuffer), framebuffer.shape[1], num_threads,
-                             ctypes.byref(bad)), "orc_rasterize")
+                             sky_ptr, sky_n, ctypes.byref(frame_params), abi.ptr(framebuffer), framebuffer.shape[1],
+                             num_threads, ctypes.byref(bad)), "orc_rasterize")
     return bad.value
 
 

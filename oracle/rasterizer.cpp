@@ -435,8 +435,8 @@ void split_rect_r(const RectF& r, uint32_t num_parts, std::vector<RectF>& out, s
 
 template <class P>
 void rasterize_all(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, const void* arena,
-	uint64_t arena_texels, const SwFrameParams* frame, void* framebuffer, uint32_t pitch, uint32_t num_threads,
-	uint64_t* bad_fetches)
+	uint64_t arena_texels, const void* skybox, uint64_t skybox_texels, const SwFrameParams* frame, void* framebuffer,
+	uint32_t pitch, uint32_t num_threads, uint64_t* bad_fetches)
 {
 	typedef typename P::T T;
 	auto run = [&](ClipRect clip, uint64_t* bad) {
@@ -448,8 +448,11 @@ void rasterize_all(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16*
 		for (uint32_t i = 0; i < num_draws; ++i)
 		{
 			const SwDrawCmd& d = draws[i];
-			r.texture_data = static_cast<const T*>(arena) + d.tex_offset;
-			uint64_t avail = arena_texels > d.tex_offset ? arena_texels - d.tex_offset : 0;
+			// draw_polygon's texture: a surface, or a skybox side mip (draw_skybox, partial_renderer.rs:2434-2444)
+			const bool sky = d.tex_source == SW_TEXSRC_SKYBOX;
+			const uint64_t texels = sky ? skybox_texels : arena_texels;
+			r.texture_data = static_cast<const T*>(sky ? skybox : arena) + d.tex_offset;
+			uint64_t avail = texels > d.tex_offset ? texels - d.tex_offset : 0;
 			uint64_t want = uint64_t(d.tex_size[0]) * d.tex_size[1];
 			r.texture_len = want < avail ? want : avail;
 			if (r.texture_len == 0) continue;
@@ -481,8 +484,8 @@ void rasterize_all(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16*
 using namespace sworacle;
 
 extern "C" int orc_rasterize(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices,
-	uint32_t num_vertices, const void* arena, uint64_t arena_texels, const SwFrameParams* frame, void* framebuffer,
-	uint32_t pitch, uint32_t num_threads, uint64_t* bad_fetches)
+	uint32_t num_vertices, const void* arena, uint64_t arena_texels, const void* skybox, uint64_t skybox_texels,
+	const SwFrameParams* frame, void* framebuffer, uint32_t pitch, uint32_t num_threads, uint64_t* bad_fetches)
 {
 	if (!frame || !framebuffer || (num_draws && (!draws || !vertices || !arena))) return SW_ERR_INVALID_ARGUMENT;
 	if (pitch < frame->width) return SW_ERR_INVALID_ARGUMENT;
@@ -493,11 +496,14 @@ extern "C" int orc_rasterize(const SwDrawCmd* draws, uint32_t num_draws, const S
 		if (uint64_t(d.first_vertex) + d.vertex_count > num_vertices) return SW_ERR_INVALID_ARGUMENT;
 		if (d.mode > SW_RASTER_AFFINE || d.blend > SW_BLEND_ALPHA_BLEND) return SW_ERR_INVALID_ARGUMENT;
 		if (d.tex_size[0] == 0 || d.tex_size[1] == 0) return SW_ERR_INVALID_ARGUMENT;
+		if (d.tex_source > SW_TEXSRC_SKYBOX || (d.tex_source == SW_TEXSRC_SKYBOX && !skybox)) return SW_ERR_INVALID_ARGUMENT;
 	}
 	if (frame->pixel_format == SW_PIXEL_C64)
-		rasterize_all<C64>(draws, num_draws, vertices, arena, arena_texels, frame, framebuffer, pitch, num_threads, bad_fetches);
+		rasterize_all<C64>(draws, num_draws, vertices, arena, arena_texels, skybox, skybox_texels, frame, framebuffer, pitch,
+			num_threads, bad_fetches);
 	else
-		rasterize_all<C32>(draws, num_draws, vertices, arena, arena_texels, frame, framebuffer, pitch, num_threads, bad_fetches);
+		rasterize_all<C32>(draws, num_draws, vertices, arena, arena_texels, skybox, skybox_texels, frame, framebuffer, pitch,
+			num_threads, bad_fetches);
 	return SW_OK;
 }
 

@@ -22,11 +22,12 @@ int orc_build_surfaces(const SwCreateInfo* data, const SwSurfaceDesc* surfaces, 
 /* Rasterizer::fill_polygon for every draw in order (perform_rasterization, partial_renderer.rs:1192-1283)
  * into `framebuffer` (pixel_format of frame, pitch in pixels). num_threads 0/1 = the reference's
  * single-thread path (one full-screen ClipRect); N > 1 = split_rect into N regions with one ClipRect each.
+ * Draws with tex_source SW_TEXSRC_SKYBOX read `skybox` (the frame's pixel format) instead of `arena`.
  * Out-of-range texel fetches (impossible for well-formed draws) read texel 0 and are counted in
  * *bad_fetches when the pointer is non-null. */
 int orc_rasterize(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices,
-	const void* arena, uint64_t arena_texels, const SwFrameParams* frame, void* framebuffer, uint32_t pitch,
-	uint32_t num_threads, uint64_t* bad_fetches);
+	const void* arena, uint64_t arena_texels, const void* skybox, uint64_t skybox_texels, const SwFrameParams* frame,
+	void* framebuffer, uint32_t pitch, uint32_t num_threads, uint64_t* bad_fetches);
 
 /* draw_background, partial_renderer.rs:3987-4009, colour (32,16,8) via ColorVec. */
 int orc_clear_background(const SwFrameParams* frame, void* framebuffer, uint32_t pitch);

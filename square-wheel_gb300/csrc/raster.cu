@@ -330,7 +330,8 @@ __global__ void __launch_bounds__(128) raster_walk_kernel(RasterArgs a)
 	rd.row_base = dr.row_base;
 	rd.y0 = dr.y0;
 	rd.mode = d.mode;
-	rd.blend = d.blend;
+	rd.blend = uint16_t(d.blend);
+	rd.tex_source = uint16_t(d.tex_source);
 	a.rdraws[di] = rd;
 }
 
@@ -436,6 +437,7 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 
 	T* fb = static_cast<T*>(a.framebuffer);
 	const T* arena = static_cast<const T*>(a.arena);
+	const T* skybox = static_cast<const T*>(a.skybox);
 	T pix[STRIP];
 #pragma unroll
 	for (int k = 0; k < STRIP; ++k)
@@ -529,7 +531,7 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 								++local_errors;
 								ua = 0;
 							}
-							tex[k] = arena[d.tex_offset + ua];
+							tex[k] = (d.tex_source == SW_TEXSRC_SKYBOX ? skybox : arena)[d.tex_offset + ua];
 						}
 					}
 #pragma unroll

@@ -111,7 +111,8 @@ struct RasterDraw
 	uint32_t tex_w, tex_h;
 	uint32_t row_base;
 	int32_t y0;
-	uint32_t mode, blend;
+	uint32_t mode;
+	uint16_t blend, tex_source; // SwBlend, SwTexSource
 };
 
 // Pixel bounds of a draw: [x0, x1) x [y0, y1); empty when x0 >= x1 or y0 >= y1.
@@ -136,7 +137,8 @@ struct RasterArgs
 	RasterBox* boxes;
 	const void* arena;
 	uint64_t arena_texels;
-	void* framebuffer; // width * height pixels, tightly packed
+	const void* skybox; // skybox texels of the frame's pixel format (SW_TEXSRC_SKYBOX draws)
+	void* framebuffer;  // width * height pixels, tightly packed
 	unsigned int* error_counter;
 };
 

@@ -59,6 +59,8 @@ struct SwCtx
 
 	// static
 	DevBuf texels, texture_mips, emissive, emissive_mips, lightmaps, dir_lightmaps;
+	DevBuf skybox32, skybox64; // sw_set_skybox: the same texels in Color32 and Color64
+	uint64_t skybox_texels = 0;
 	std::vector<SwTextureMip> h_texture_mips;
 	std::vector<SwEmissiveMip> h_emissive_mips;
 	uint64_t num_lightmap_elements = 0, num_dir_lightmap_elements = 0;
@@ -148,6 +150,7 @@ RasterArgs raster_args(SwCtx* ctx)
 	a.boxes = static_cast<RasterBox*>(ctx->boxes.ptr);
 	a.arena = ctx->arena.ptr;
 	a.arena_texels = ctx->arena_texels;
+	a.skybox = ctx->frame.pixel_format == SW_PIXEL_C64 ? ctx->skybox64.ptr : ctx->skybox32.ptr;
 	a.framebuffer = ctx->framebuffer.ptr;
 	a.error_counter = static_cast<unsigned int*>(ctx->error_counter.ptr);
 	return a;
@@ -425,7 +428,8 @@ int sw_destroy(SwCtx* ctx)
 	cudaSetDevice(ctx->device);
 	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
 	if (ctx->aux) cudaStreamSynchronize(ctx->aux);
-	DevBuf* bufs[] = {&ctx->texels, &ctx->texture_mips, &ctx->emissive, &ctx->emissive_mips, &ctx->lightmaps,
+	DevBuf* bufs[] = {&ctx->texels, &ctx->texture_mips, &ctx->emissive, &ctx->emissive_mips, &ctx->lightmaps, &ctx->skybox32,
+		&ctx->skybox64,
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->parts, &ctx->part_counts, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst};
@@ -647,6 +651,21 @@ int sw_rebuild_surfaces(SwCtx* ctx)
 	return launch_surfaces(ctx);
 }
 
+int sw_set_skybox(SwCtx* ctx, const uint32_t* texels32, const uint64_t* texels64, uint64_t num_texels)
+{
+	if (!ctx || (num_texels && (!texels32 || !texels64))) return SW_ERR_INVALID_ARGUMENT;
+	if (num_texels > (uint64_t(1) << 32)) return fail(ctx, SW_ERR_LIMIT, "skybox too large");
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	// frames in flight may read the old texels
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	if (ctx->aux) SW_CUDA(ctx, cudaStreamSynchronize(ctx->aux));
+	int r;
+	if ((r = upload_static(ctx, ctx->skybox32, texels32, size_t(num_texels) * 4))) return r;
+	if ((r = upload_static(ctx, ctx->skybox64, texels64, size_t(num_texels) * 8))) return r;
+	ctx->skybox_texels = num_texels;
+	return SW_OK;
+}
+
 int sw_set_surfaces(SwCtx* ctx, const void* texels, uint64_t total_texels)
 {
 	if (!ctx || (total_texels && !texels)) return SW_ERR_INVALID_ARGUMENT;
@@ -678,8 +697,12 @@ int prepare_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const 
 			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: vertices out of range", i);
 		if (d.mode > SW_RASTER_AFFINE || d.blend > SW_BLEND_ALPHA_BLEND)
 			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: bad mode/blend", i);
-		if (d.tex_size[0] == 0 || d.tex_size[1] == 0 || d.tex_offset + uint64_t(d.tex_size[0]) * d.tex_size[1] > ctx->arena_texels)
-			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: texture outside the surface arena", i);
+		if (d.tex_source > SW_TEXSRC_SKYBOX) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: bad texture source", i);
+		const uint64_t limit = d.tex_source == SW_TEXSRC_SKYBOX ? ctx->skybox_texels : ctx->arena_texels;
+		const uint64_t area = uint64_t(d.tex_size[0]) * d.tex_size[1];
+		if (d.tex_size[0] == 0 || d.tex_size[1] == 0 || d.tex_offset > limit || area > limit - d.tex_offset)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: texture outside the %s", i,
+				d.tex_source == SW_TEXSRC_SKYBOX ? "skybox texels" : "surface arena");
 		int32_t y0;
 		uint32_t nrows;
 		draw_row_range(d, vertices, int32_t(ctx->frame.height), y0, nrows);

@@ -466,6 +466,20 @@ void FramePrep::prepare_polygon_surface(const Vec3 clip_planes[8], uint64_t& off
 	Vec2 v2d[MAX_VERTICES];
 	const uint32_t count = project_and_clip_polygon(clip_planes, &vertices_transformed[p.first_vertex], p.num_vertices, v2d);
 	if (count < 3) return;
+	if (material.skybox)
+	{
+		// Sky polygons are not drawn; their screen bounds say where draw_skybox must draw (:1510-1528).
+		ClippingPolygon b = ClippingPolygon::from_point(v2d[0]);
+		for (uint32_t k = 1; k < count; ++k) b.extend_with_point(v2d[k]);
+		if (has_sky)
+			sky_bounds.extend(b);
+		else
+		{
+			sky_bounds = b;
+			has_sky = true;
+		}
+		return;
+	}
 
 	// DepthEquation::from_transformed_plane_equation, equations.rs:23-31
 	const float pw = -plane_transformed.w;
@@ -547,6 +561,7 @@ void FramePrep::prepare_polygons_surfaces()
 {
 	// partial_renderer.rs:1327-1359 (world leafs; no submodels in these maps)
 	visible_polygons.clear();
+	has_sky = false; // current_sky = None (:1336)
 	uint64_t offset = 0;
 	for (uint32_t i = 0; i < sc.leafs.size(); ++i)
 	{
@@ -655,18 +670,26 @@ void FramePrep::build_surface_descs()
 
 void FramePrep::draw_polygon(const Vec3 clip_planes[8], uint32_t polygon_index)
 {
-	// partial_renderer.rs:4011-4142
+	// draw_leaf's call of draw_polygon for a world polygon: its surface is the texture
 	const MapPolygon& p = sc.polygons[polygon_index];
 	const PolyData& pd = poly[polygon_index];
 	if (p.num_vertices < 3) return;
+	emit_draw(clip_planes, &vertices_transformed[p.first_vertex], p.num_vertices, pd.depth, pd.tc, pd.size[0], pd.size[1],
+		pd.offset, SW_TEXSRC_SURFACE, sc.materials[p.texture].blending_mode);
+}
+
+void FramePrep::emit_draw(const Vec3 clip_planes[8], const Vec3* vt, uint32_t num_vertices, const DepthEquation& depth,
+	const TexCoordEquation& tc, uint32_t tex_w, uint32_t tex_h, uint64_t tex_offset, uint32_t tex_source, uint32_t blend)
+{
+	// partial_renderer.rs:4011-4142
 	Vec2 v2d[MAX_VERTICES];
-	const uint32_t count = project_and_clip_polygon(clip_planes, &vertices_transformed[p.first_vertex], p.num_vertices, v2d);
+	const uint32_t count = project_and_clip_polygon(clip_planes, vt, num_vertices, v2d);
 	if (count < 3) return;
 	float min_inv_z = 1e24f, max_inv_z = -1e24f, min_x = 1e24f, max_x = -1e24f;
 	uint32_t min_i = 0, max_i = 0;
 	for (uint32_t k = 0; k < count; ++k)
 	{
-		const float inv_z = pd.depth.sample(v2d[k]);
+		const float inv_z = depth.sample(v2d[k]);
 		if (inv_z < min_inv_z)
 		{
 			min_inv_z = inv_z;
@@ -686,13 +709,14 @@ void FramePrep::draw_polygon(const Vec3 clip_planes[8], uint32_t polygon_index)
 	d.vertex_count = count;
 	for (uint32_t k = 0; k < count; ++k) // f32_to_fixed16_unchecked, fixed_math.rs:335-338
 		vertices.push_back(SwVertex16{as_i32(v2d[k].x * 65536.0f), as_i32(v2d[k].y * 65536.0f)});
-	d.blend = sc.materials[p.texture].blending_mode;
-	d.tex_size[0] = pd.size[0];
-	d.tex_size[1] = pd.size[1];
-	d.tex_offset = pd.offset;
-	DepthEquation de = pd.depth;
-	TexCoordEquation te = pd.tc;
-	if (affine_may_be_used(pd.depth, pd.tc, v2d[min_i], v2d[max_i]))
+	d.blend = blend;
+	d.tex_size[0] = tex_w;
+	d.tex_size[1] = tex_h;
+	d.tex_source = tex_source;
+	d.tex_offset = tex_offset;
+	DepthEquation de = depth;
+	TexCoordEquation te = tc;
+	if (affine_may_be_used(depth, tc, v2d[min_i], v2d[max_i]))
 		d.mode = SW_RASTER_AFFINE;
 	else
 	{
@@ -704,8 +728,8 @@ void FramePrep::draw_polygon(const Vec3 clip_planes[8], uint32_t polygon_index)
 			te.d_tc_dy[i] *= z_scale;
 			te.k[i] *= z_scale;
 		}
-		d.mode = line_z_may_be_used(pd.depth, pd.tc, v2d[max_i], min_x, max_x) ? SW_RASTER_LINE_Z_CORRECTED
-																			   : SW_RASTER_FULL_PERSPECTIVE;
+		d.mode = line_z_may_be_used(depth, tc, v2d[max_i], min_x, max_x) ? SW_RASTER_LINE_Z_CORRECTED
+																		 : SW_RASTER_FULL_PERSPECTIVE;
 	}
 	d.depth_eq[0] = de.d_inv_z_dx;
 	d.depth_eq[1] = de.d_inv_z_dy;
@@ -730,6 +754,87 @@ void FramePrep::draw_leaf(const ClippingPolygon& bounds, uint32_t leaf_index)
 		const uint32_t pi = leaf.first_polygon + k;
 		if (poly[pi].visible_frame != current_frame) continue;
 		draw_polygon(planes, pi);
+	}
+}
+
+void FramePrep::draw_skybox(const ClippingPolygon& viewport)
+{
+	// partial_renderer.rs:2311-2448
+	if (!has_sky || sc.sky_material < 0) return;
+	ClippingPolygon bounds = sky_bounds;
+	bounds.intersect(viewport);
+	if (!bounds.is_valid_and_non_empty()) return;
+
+	static const float BOX_VERTICES[8][3] = {{-1, -1, -1}, {-1, -1, 1}, {-1, 1, -1}, {-1, 1, 1}, {1, -1, -1}, {1, -1, 1},
+		{1, 1, -1}, {1, 1, 1}};
+	struct Side
+	{
+		uint32_t v[4];
+		Vec3 normal, u, v_dir;
+	};
+	const Vec3 X = v3(1, 0, 0), Y = v3(0, 1, 0), Z = v3(0, 0, 1);
+	const Side sides[6] = {
+		{{0, 1, 3, 2}, X, Y, -Z},  // -X
+		{{4, 6, 7, 5}, -X, -Y, -Z}, // +X
+		{{0, 4, 5, 1}, Y, -X, -Z},  // -Y
+		{{2, 3, 7, 6}, -Y, X, -Z},  // +Y
+		{{0, 2, 6, 4}, Z, X, -Y},   // -Z
+		{{1, 5, 7, 3}, -Z, X, Y},   // +Z
+	};
+	const float side_plane_dist = -1.0f, side_tc_shift = 1.0f;
+
+	// get_object_matrix(position, rotation) = translate * rotate (src/common/matrix.rs:111-117)
+	Mat4 translate = Mat4::identity();
+	translate.c[3] = v4(cam.position.x, cam.position.y, cam.position.z, 1.0f);
+	const Mat4 skybox_matrix = translate * mat4_from_quat(sky_rotation);
+	Mat4 skybox_matrix_inverse;
+	if (!invert(transpose(skybox_matrix), skybox_matrix_inverse)) return;
+	const Mat4 skybox_view_matrix = cam.view_matrix * skybox_matrix;
+	const Mat4 skybox_planes_matrix = cam.planes_matrix * skybox_matrix_inverse;
+
+	const float SKY_SCALE = 16384.0f;
+	Vec3 box[8];
+	for (int i = 0; i < 8; ++i)
+		box[i] = view_transform(skybox_view_matrix, v3(BOX_VERTICES[i][0], BOX_VERTICES[i][1], BOX_VERTICES[i][2]) * SKY_SCALE);
+	Vec3 clip_planes[8];
+	bounds.get_clip_planes(clip_planes);
+
+	for (uint32_t side = 0; side < 6; ++side)
+	{
+		const SkyboxMip* mips = sc.skybox_mips[side];
+		if (mips[0].size == 0) continue; // no texture for this side
+		const Side& sd = sides[side];
+		const Vec3 vt[4] = {box[sd.v[0]], box[sd.v[1]], box[sd.v[2]], box[sd.v[3]]};
+		const Vec4 pt = skybox_planes_matrix * extend(sd.normal, -side_plane_dist);
+		const float pw = -pt.w;
+		const DepthEquation de{pt.x / pw, pt.y / pw, pt.z / pw};
+		const float tc_equation_scale = float(mips[0].size) * 0.5f;
+		const Vec4 tb[2] = {skybox_planes_matrix * (extend(sd.u, side_tc_shift) * tc_equation_scale),
+			skybox_planes_matrix * (extend(sd.v_dir, side_tc_shift) * tc_equation_scale)};
+		TexCoordEquation te;
+		for (int i = 0; i < 2; ++i)
+		{
+			te.d_tc_dx[i] = tb[i].x + tb[i].w * de.d_inv_z_dx;
+			te.d_tc_dy[i] = tb[i].y + tb[i].w * de.d_inv_z_dy;
+			te.k[i] = tb[i].z + tb[i].w * de.k;
+		}
+		Vec2 v2d[MAX_VERTICES];
+		const uint32_t count = project_and_clip_polygon(clip_planes, vt, 4, v2d);
+		if (count < 3) continue;
+		const uint32_t mip = calculate_mip(v2d, count, de, te, opt.mip_bias);
+		const float mip_scale = 1.0f / float(1u << mip);
+		TexCoordEquation ts;
+		for (int i = 0; i < 2; ++i)
+		{
+			ts.d_tc_dx[i] = te.d_tc_dx[i] * mip_scale;
+			ts.d_tc_dy[i] = te.d_tc_dy[i] * mip_scale;
+			ts.k[i] = te.k[i] * mip_scale;
+		}
+		const SkyboxMip& t = mips[mip];
+		if (t.size == 0) continue;
+		const size_t before = draws.size();
+		emit_draw(clip_planes, vt, 4, de, ts, t.size, t.size, t.offset, SW_TEXSRC_SKYBOX, SW_BLEND_NONE);
+		stats.skybox_draws += uint32_t(draws.size() - before);
 	}
 }
 
@@ -772,10 +877,11 @@ void FramePrep::draw_tree()
 }
 
 void FramePrep::prepare_with_camera(const CameraMatrices& camera, const std::vector<SwLight>& frame_lights,
-	const FrameOptions& options)
+	const FrameOptions& options, Quat skybox_rotation)
 {
 	cam = camera;
 	opt = options;
+	sky_rotation = skybox_rotation;
 	lights = frame_lights;
 	stats = FrameStats();
 	++current_frame;
@@ -785,6 +891,8 @@ void FramePrep::prepare_with_camera(const CameraMatrices& camera, const std::vec
 	build_surface_descs();
 	draws.clear();
 	vertices.clear();
+	// perform_rasterization_for_viewport_part (:1285-1325): skybox first, then the tree
+	draw_skybox(ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height)));
 	draw_tree();
 	std::memset(&params, 0, sizeof(params));
 	params.pixel_format = opt.pixel_format;
@@ -807,7 +915,7 @@ void FramePrep::prepare(uint32_t frame_index, const FrameOptions& options)
 		build_view_matrix(k.position, k.azimuth, k.elevation, options.fov, float(options.width), float(options.height));
 	std::vector<SwLight> l;
 	sc.frame_lights(frame_index % uint32_t(sc.camera_path.size()), l);
-	prepare_with_camera(camera, l, options);
+	prepare_with_camera(camera, l, options, quat_from_angle_z(float(frame_index) * sc.config.sky_rotation_speed));
 }
 
 } // namespace swhost

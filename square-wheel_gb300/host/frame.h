@@ -6,6 +6,7 @@
 //   prepare_polygons_surfaces / prepare_polygon_surface (src/square_wheel/partial_renderer.rs:1327-1638),
 //   the descriptor half of build_polygons_surfaces (partial_renderer.rs:1640-1819) with
 //   polygon_is_affected_by_light (:3877-3985),
+//   draw_skybox (:2311-2448) with the sky bounds collected in prepare_polygon_surface (:1510-1528),
 //   draw_tree / draw_leaf / draw_polygon (:2450-2559, :4011-4142) with project_and_clip_polygon,
 //   calculate_mip and the interpolation-mode tests (src/square_wheel/renderer_utils.rs), the clipping
 //   helpers (src/common/clipping.rs:4-185) and ClippingPolygon (src/common/clipping_polygon.rs).
@@ -59,7 +60,7 @@ struct FrameOptions
 
 struct FrameStats
 {
-	uint32_t visible_leafs = 0, visible_polygons = 0, draws = 0, camera_leaf = 0;
+	uint32_t visible_leafs = 0, visible_polygons = 0, draws = 0, camera_leaf = 0, skybox_draws = 0;
 	uint64_t surface_texels = 0;
 };
 
@@ -67,10 +68,11 @@ class FramePrep
 {
 public:
 	explicit FramePrep(const Scene& scene);
-	// Camera and lights of scene frame `frame_index` (camera path key, moving lights).
+	// Camera, lights and skybox rotation of scene frame `frame_index` (camera path key, moving lights).
 	void prepare(uint32_t frame_index, const FrameOptions& opt);
-	// Same with an explicit camera and light list.
-	void prepare_with_camera(const CameraMatrices& cam, const std::vector<SwLight>& lights, const FrameOptions& opt);
+	// Same with an explicit camera, light list and skybox rotation (FrameWorldInfo::skybox_rotation).
+	void prepare_with_camera(const CameraMatrices& cam, const std::vector<SwLight>& lights, const FrameOptions& opt,
+		Quat skybox_rotation = Quat{1.0f, Vec3{0.0f, 0.0f, 0.0f}});
 
 	std::vector<SwSurfaceDesc> surfaces;
 	uint64_t total_texels = 0;
@@ -114,6 +116,9 @@ private:
 	std::vector<std::vector<uint32_t>> leaf_lights;
 	CameraMatrices cam{};
 	FrameOptions opt;
+	Quat sky_rotation{1.0f, Vec3{0.0f, 0.0f, 0.0f}};
+	bool has_sky = false;        // current_sky (partial_renderer.rs:35): a sky polygon is visible
+	ClippingPolygon sky_bounds{}; // union of the visible sky polygons' screen bounds
 
 	uint32_t find_current_leaf() const;
 	void update_visibility(const ClippingPolygon& frame_bounds);
@@ -124,9 +129,14 @@ private:
 	void prepare_polygons_surfaces();
 	void prepare_polygon_surface(const Vec3 clip_planes[8], uint64_t& offset, uint32_t polygon_index);
 	void build_surface_descs();
+	void draw_skybox(const ClippingPolygon& viewport);
 	void draw_tree();
 	void draw_leaf(const ClippingPolygon& bounds, uint32_t leaf_index);
 	void draw_polygon(const Vec3 clip_planes[8], uint32_t polygon_index);
+	// draw_polygon (partial_renderer.rs:4011-4142) of transformed vertices with their equations and texture.
+	void emit_draw(const Vec3 clip_planes[8], const Vec3* vertices_transformed, uint32_t num_vertices,
+		const DepthEquation& depth, const TexCoordEquation& tc, uint32_t tex_w, uint32_t tex_h, uint64_t tex_offset,
+		uint32_t tex_source, uint32_t blend);
 };
 
 } // namespace swhost

@@ -38,6 +38,7 @@ struct Room
 	float x0, x1, y0, y1, h;
 	float cx, cy; // corridor centre lines (cell centre lines)
 	uint32_t mat_wall, mat_floor, mat_ceiling;
+	uint32_t ceiling_first = 0, ceiling_end = 0; // the ceiling's polygons
 	int32_t tc_shift[2];
 	std::vector<Vec3> lights;
 	std::vector<Vec3> light_colors;
@@ -186,6 +187,113 @@ void make_material_texture(Rng& rng, uint32_t size, bool normal_map, float rough
 			w >>= 1;
 			h >>= 1;
 		}
+	}
+}
+
+// ---- skybox ----------------------------------------------------------------------------------
+
+// One procedural RGBA8 side image (the stand-in for the skybox image files): a vertical gradient from
+// horizon haze to zenith blue on the four walls, the zenith colour on top, dark ground at the bottom,
+// with value-noise clouds. Raw Color32 values (A << 24 | R << 16 | G << 8 | B).
+std::vector<uint32_t> make_sky_image(Rng& rng, uint32_t size, uint32_t side)
+{
+	const std::vector<float> clouds = value_noise(rng, size, 8), detail = value_noise(rng, size, 32);
+	std::vector<uint32_t> img(size_t(size) * size);
+	for (uint32_t y = 0; y < size; ++y)
+		for (uint32_t x = 0; x < size; ++x)
+		{
+			const size_t i = size_t(y) * size + x;
+			// walls (sides 0..3): v runs from the zenith (y = 0) to the horizon; top (5) and bottom (4) flat
+			const float t = side < 4 ? float(y) / float(size) : side == 5 ? 0.0f : 1.2f;
+			float rgb[3] = {40.0f + 150.0f * t, 90.0f + 120.0f * t, 200.0f + 40.0f * std::fmin(t, 1.0f)};
+			if (side == 4)
+				for (float& c : rgb) c *= 0.3f;
+			const float cloud = std::fmax(clouds[i] * 1.6f - 0.7f + 0.2f * detail[i], 0.0f);
+			for (float& c : rgb) c = c + (250.0f - c) * std::fmin(cloud, 1.0f);
+			uint32_t c8[3];
+			for (int k = 0; k < 3; ++k) c8[k] = uint32_t(std::fmin(std::fmax(rgb[k], 0.0f), 255.0f));
+			img[i] = (255u << 24) | (c8[0] << 16) | (c8[1] << 8) | c8[2];
+		}
+	return img;
+}
+
+// Lane helpers of the generic ColorVecI (src/square_wheel/fast_math.rs:600-720): lanes b, g, r, a.
+struct Lanes
+{
+	int32_t v[4];
+};
+Lanes lanes32(uint32_t c)
+{
+	Lanes l;
+	for (int i = 0; i < 4; ++i) l.v[i] = int32_t((c >> (i * 8)) & 0xFFu);
+	return l;
+}
+Lanes lanes64(uint64_t c)
+{
+	Lanes l;
+	for (int i = 0; i < 4; ++i) l.v[i] = int32_t((c >> (i * 16)) & 0xFFFFu);
+	return l;
+}
+// into_color32 / into_color64: lane as unsigned, min(255) / min(65535)
+uint32_t from_lanes32(const Lanes& l)
+{
+	uint32_t r = 0;
+	for (int i = 0; i < 4; ++i) r |= std::min(uint32_t(l.v[i]), 255u) << (i * 8);
+	return r;
+}
+uint64_t from_lanes64(const Lanes& l)
+{
+	uint64_t r = 0;
+	for (int i = 0; i < 4; ++i) r |= uint64_t(std::min(uint32_t(l.v[i]), 65535u)) << (i * 16);
+	return r;
+}
+
+// make_skybox_side_texture{,64} (textures.rs:183-229) + make_skybox_side_texture_mips (:231-290) of one
+// side image, appended to the scene's skybox arrays. The 64-bit image of an 8-bit file holds the 8-bit
+// values as 16-bit lanes (image::load64, src/common/image.rs:50-58).
+void add_skybox_side(const std::vector<uint32_t>& img, uint32_t size, float brightness, uint32_t side, Scene& sc)
+{
+	const int32_t bi = int32_t(brightness * 256.0f); // (brightness * SCALE) as i32
+	std::vector<uint32_t> l32(img.size());
+	std::vector<uint64_t> l64(img.size());
+	for (size_t i = 0; i < img.size(); ++i)
+	{
+		Lanes c = lanes32(img[i]);
+		for (int k = 0; k < 3; ++k) c.v[k] = (c.v[k] * bi) >> 8;
+		c.v[3] = 0; // brightness vector (b, b, b, 0)
+		l32[i] = from_lanes32(c);
+		l64[i] = from_lanes64(c); // the same lanes: 8-bit values * brightness, 16-bit range
+	}
+	uint32_t s = size;
+	for (uint32_t m = 0; m < NUM_MIPS; ++m)
+	{
+		if (s == 0) break;
+		sc.skybox_mips[side][m] = SkyboxMip{sc.skybox32.size(), s};
+		sc.skybox32.insert(sc.skybox32.end(), l32.begin(), l32.end());
+		sc.skybox64.insert(sc.skybox64.end(), l64.begin(), l64.end());
+		const uint32_t n = s >> 1;
+		if (m + 1 == NUM_MIPS || n == 0) break;
+		std::vector<uint32_t> n32(size_t(n) * n);
+		std::vector<uint64_t> n64(size_t(n) * n);
+		for (uint32_t y = 0; y < n; ++y)
+			for (uint32_t x = 0; x < n; ++x)
+			{
+				const size_t o0 = size_t(2 * y) * s + 2 * x, o1 = size_t(2 * y + 1) * s + 2 * x;
+				Lanes a32 = lanes32(l32[o0]), b32 = lanes32(l32[o1]), c32 = lanes32(l32[o0 + 1]), d32 = lanes32(l32[o1 + 1]);
+				Lanes a64 = lanes64(l64[o0]), b64 = lanes64(l64[o1]), c64 = lanes64(l64[o0 + 1]), d64 = lanes64(l64[o1 + 1]);
+				Lanes r32, r64;
+				for (int k = 0; k < 4; ++k)
+				{
+					// shift_right::<2>(add(add(p00, p01), add(p10, p11)))
+					r32.v[k] = ((a32.v[k] + b32.v[k]) + (c32.v[k] + d32.v[k])) >> 2;
+					r64.v[k] = ((a64.v[k] + b64.v[k]) + (c64.v[k] + d64.v[k])) >> 2;
+				}
+				n32[size_t(y) * n + x] = from_lanes32(r32);
+				n64[size_t(y) * n + x] = from_lanes64(r64);
+			}
+		l32.swap(n32);
+		l64.swap(n64);
+		s = n;
 	}
 }
 
@@ -458,6 +566,7 @@ struct Builder
 		int32_t east = -1, west = -1, north = -1, south = -1;
 	};
 	std::vector<CellLeafs> cell_leafs;
+	uint32_t path_start_room = 0; // room of the camera path's first key
 
 	uint32_t build_cell(uint32_t i, uint32_t j)
 	{
@@ -471,7 +580,9 @@ struct Builder
 		// Room leaf.
 		const uint32_t room_leaf = begin_leaf(int32_t(ri));
 		add_face_rect(2, 0.0f, 1.0f, r.x0, r.x1, r.y0, r.y1, r.mat_floor, r.tc_shift);
+		rooms[ri].ceiling_first = uint32_t(sc.polygons.size());
 		add_face_rect(2, r.h, -1.0f, r.x0, r.x1, r.y0, r.y1, r.mat_ceiling, r.tc_shift);
+		rooms[ri].ceiling_end = uint32_t(sc.polygons.size());
 		add_wall(0, r.x1, -1.0f, r.y0, r.y1, r.h, E, r.cy - CORRIDOR_HALF, r.cy + CORRIDOR_HALF, r.mat_wall, r.tc_shift);
 		add_wall(0, r.x0, 1.0f, r.y0, r.y1, r.h, W, r.cy - CORRIDOR_HALF, r.cy + CORRIDOR_HALF, r.mat_wall, r.tc_shift);
 		add_wall(1, r.y1, -1.0f, r.x0, r.x1, r.h, N, r.cx - CORRIDOR_HALF, r.cx + CORRIDOR_HALF, r.mat_wall, r.tc_shift);
@@ -651,6 +762,7 @@ struct Builder
 		const float eye = 64.0f;
 		std::vector<Vec3> way;
 		uint32_t cur = rng.below(uint32_t(rooms.size()));
+		path_start_room = cur;
 		uint32_t prev = ~0u;
 		way.push_back(v3(rooms[cur].cx, rooms[cur].cy, eye));
 		for (int step = 0; step < 64; ++step)
@@ -749,7 +861,7 @@ struct Builder
 			CameraKey k;
 			k.position = pos;
 			k.azimuth = std::atan2(dir.y, dir.x);
-			k.elevation = 0.08f * std::sin(float(f) * 0.07f);
+			k.elevation = 0.08f * std::sin(float(f) * 0.07f) + cfg.camera_pitch;
 			sc.camera_path.push_back(k);
 		}
 	}
@@ -846,6 +958,12 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 		error = "texture_size must be a power of two >= 16";
 		return false;
 	}
+	if (cfg.sky_rooms && (cfg.skybox_size < 16 || cfg.skybox_size > 2048 || (cfg.skybox_size & (cfg.skybox_size - 1)) ||
+							 !(cfg.skybox_brightness > 0.0f && cfg.skybox_brightness <= 64.0f) || cfg.skybox_missing_side > 5))
+	{
+		error = "skybox_size must be a power of two in [16, 2048], skybox_brightness in (0, 64]";
+		return false;
+	}
 	sc = Scene();
 	sc.config = cfg;
 	Rng rng(cfg.seed);
@@ -880,12 +998,51 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 		}
 		sc.materials.push_back(mat);
 	}
+	if (cfg.sky_rooms)
+	{
+		// The sky material (material index num_materials) with a stub regular texture, and its six side
+		// textures (SpecialMaterialEffect::Skybox, src/common/material.rs; textures loaded as
+		// resources_manager.rs:321-392 does).
+		Rng krng(cfg.seed ^ 0x5CB0Bu);
+		make_material_texture(krng, cfg.texture_size, false, 1.0f, false, sc);
+		Material sky;
+		sky.skybox = true;
+		sky.light = false;
+		sc.sky_material = int32_t(sc.materials.size());
+		sc.materials.push_back(sky);
+		for (uint32_t side = 0; side < 6; ++side)
+		{
+			const std::vector<uint32_t> img = make_sky_image(krng, cfg.skybox_size, side);
+			if (int32_t(side) == cfg.skybox_missing_side) continue; // SkyboxSideTextureWithMips::default()
+			add_skybox_side(img, cfg.skybox_size, cfg.skybox_brightness, side, sc);
+		}
+	}
 
 	sc.basis.resize(sc.polygons.size());
 	for (size_t p = 0; p < sc.polygons.size(); ++p)
 		sc.basis[p] = form_plane_and_tex_coord_equation(sc.polygons[p].plane, sc.polygons[p].tex_coord_equation);
 
 	b.build_camera_path();
+	if (cfg.sky_rooms)
+	{
+		// Ceilings open to the sky: the room the camera path starts in and others drawn by their own
+		// generator (the rest of the scene is the one without sky).
+		Rng srng(cfg.seed ^ 0x5C1B0Bu);
+		std::vector<uint8_t> sky(b.rooms.size(), 0);
+		const uint32_t n = std::min<uint32_t>(cfg.sky_rooms, uint32_t(b.rooms.size()));
+		sky[b.path_start_room] = 1;
+		for (uint32_t k = 1; k < n;)
+		{
+			const uint32_t ri = srng.below(uint32_t(b.rooms.size()));
+			if (sky[ri]) continue;
+			sky[ri] = 1;
+			++k;
+		}
+		for (size_t ri = 0; ri < b.rooms.size(); ++ri)
+			if (sky[ri])
+				for (uint32_t p = b.rooms[ri].ceiling_first; p < b.rooms[ri].ceiling_end; ++p)
+					sc.polygons[p].texture = uint32_t(sc.sky_material);
+	}
 	for (uint32_t k = 0; k < cfg.num_dynamic_lights; ++k)
 	{
 		DynamicLightSpec d;

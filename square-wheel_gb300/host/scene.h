@@ -64,6 +64,15 @@ struct Material
 	uint32_t blending_mode = SW_BLEND_NONE;
 	int32_t emissive = -1; // emissive texture index or -1
 	float emissive_light[3] = {1.0f, 1.0f, 1.0f};
+	bool skybox = false; // SpecialMaterialEffect::Skybox: polygons only mark where the sky shows
+};
+
+// One mip of a skybox side (SkyboxSideTexture, src/square_wheel/textures.rs:83-87): size x size texels
+// at `offset` in Scene::skybox32 / skybox64; size 0 = no texture.
+struct SkyboxMip
+{
+	uint64_t offset = 0;
+	uint32_t size = 0;
 };
 
 // PolygonBasisVecs, src/square_wheel/surfaces.rs:6-64
@@ -102,6 +111,12 @@ struct SceneConfig
 	uint32_t num_dynamic_lights = 0;
 	uint32_t num_frames = 64;
 	float emissive_frac = 0.0f;
+	uint32_t sky_rooms = 0;           // rooms whose ceiling is sky (a skybox material)
+	uint32_t skybox_size = 128;       // skybox side texture size (power of two)
+	float skybox_brightness = 1.0f;   // SkyboxParams::brightness
+	int32_t skybox_missing_side = -1; // a side without texture (0..5), -1 = none
+	float sky_rotation_speed = 0.01f; // skybox rotation about the vertical axis, radians per frame
+	float camera_pitch = 0.0f;        // added to the camera path's elevation (radians, up > 0)
 };
 
 struct Scene
@@ -125,6 +140,12 @@ struct Scene
 	std::vector<CameraKey> camera_path;       // one key per frame
 	std::vector<DynamicLightSpec> dynamic_lights;
 	uint64_t lightmap_elements = 0;
+	// Skybox of the sky material (SkyboxTextures<Color32> / <Color64>): sides in the reference's order
+	// (-X, +X, -Y, +Y, -Z, +Z), NUM_MIPS mips each, the same layout in both formats.
+	int32_t sky_material = -1;
+	std::vector<uint32_t> skybox32;
+	std::vector<uint64_t> skybox64;
+	SkyboxMip skybox_mips[6][NUM_MIPS];
 
 	uint32_t root_node() const { return nodes.empty() ? FIRST_LEAF_INDEX : uint32_t(nodes.size() - 1); }
 	void frame_lights(uint32_t frame, std::vector<SwLight>& out) const;

@@ -73,6 +73,12 @@ int swh_scene_create(const SwhSceneConfig* c, SwhScene** out)
 	cfg.num_dynamic_lights = c->num_dynamic_lights;
 	cfg.num_frames = c->num_frames ? c->num_frames : 1;
 	cfg.emissive_frac = c->emissive_frac;
+	cfg.sky_rooms = c->sky_rooms;
+	cfg.skybox_size = c->skybox_size ? c->skybox_size : 128;
+	cfg.skybox_brightness = c->skybox_brightness > 0.0f ? c->skybox_brightness : 1.0f;
+	cfg.skybox_missing_side = c->skybox_missing_side;
+	cfg.sky_rotation_speed = c->sky_rotation_speed;
+	cfg.camera_pitch = c->camera_pitch;
 	SwhScene* s = new (std::nothrow) SwhScene();
 	if (!s) return SW_ERR_OUT_OF_MEMORY;
 	try
@@ -114,6 +120,24 @@ int swh_scene_info(const SwhScene* s, SwhSceneInfo* out)
 	out->reserved = 0;
 	out->lightmap_elements = sc.lightmap_elements;
 	out->texels = sc.texels.size();
+	out->skybox_texels = sc.skybox32.size();
+	return SW_OK;
+}
+
+int swh_scene_skybox(const SwhScene* s, const uint32_t** t32, const uint64_t** t64, uint64_t* count,
+	uint64_t mip_offsets[30], uint32_t mip_sizes[30])
+{
+	if (!s || !t32 || !t64 || !count) return SW_ERR_INVALID_ARGUMENT;
+	const Scene& sc = s->scene;
+	*t32 = sc.skybox32.data();
+	*t64 = sc.skybox64.data();
+	*count = sc.skybox32.size();
+	for (uint32_t side = 0; side < 6; ++side)
+		for (uint32_t m = 0; m < NUM_MIPS; ++m)
+		{
+			if (mip_offsets) mip_offsets[side * NUM_MIPS + m] = sc.skybox_mips[side][m].offset;
+			if (mip_sizes) mip_sizes[side * NUM_MIPS + m] = sc.skybox_mips[side][m].size;
+		}
 	return SW_OK;
 }
 
@@ -169,6 +193,7 @@ int swh_frame_outputs(const SwhFrame* f, SwhFrameOutputs* out)
 	out->params = p.params;
 	out->visible_leafs = p.stats.visible_leafs;
 	out->camera_leaf = p.stats.camera_leaf;
+	out->skybox_draws = p.stats.skybox_draws;
 	return SW_OK;
 }
 
@@ -184,6 +209,14 @@ int swh_renderer_create(const SwhScene* s, uint32_t device, SwhRenderer** out)
 	if (st != SW_OK)
 	{
 		g_error = "sw_create failed";
+		delete r;
+		return st;
+	}
+	if (!s->scene.skybox32.empty() &&
+		(st = sw_set_skybox(r->ctx, s->scene.skybox32.data(), s->scene.skybox64.data(), s->scene.skybox32.size())) != SW_OK)
+	{
+		g_error = "sw_set_skybox failed";
+		sw_destroy(r->ctx);
 		delete r;
 		return st;
 	}

@@ -22,6 +22,7 @@ SW_PIXEL_C64 = 1
 
 SW_BLEND_NONE, SW_BLEND_AVERAGE, SW_BLEND_ADDITIVE, SW_BLEND_ALPHA_TEST, SW_BLEND_ALPHA_BLEND = range(5)
 SW_RASTER_FULL_PERSPECTIVE, SW_RASTER_LINE_Z_CORRECTED, SW_RASTER_AFFINE = range(3)
+SW_TEXSRC_SURFACE, SW_TEXSRC_SKYBOX = range(2)
 SW_UPSCALE_NEAREST, SW_UPSCALE_AVG2X, SW_UPSCALE_LEARNED = range(3)
 
 SW_TEX_HAS_NORMAL_MAP = 1
@@ -49,7 +50,7 @@ SURFACE_DESC = np.dtype([
 VERTEX16 = np.dtype([("x", "<i4"), ("y", "<i4")], align=True)
 DRAW_CMD = np.dtype([
     ("first_vertex", "<u4"), ("vertex_count", "<u4"), ("mode", "<u4"), ("blend", "<u4"), ("depth_eq", "<f4", 3),
-    ("tc_eq", "<f4", 6), ("tex_size", "<u4", 2), ("reserved", "<u4"), ("tex_offset", "<u8")], align=True)
+    ("tc_eq", "<f4", 6), ("tex_size", "<u4", 2), ("tex_source", "<u4"), ("tex_offset", "<u8")], align=True)
 
 
 class CreateInfo(ctypes.Structure):

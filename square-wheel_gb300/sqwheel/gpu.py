@@ -19,7 +19,7 @@ PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_DIR, "lib", "libswgpu.so")
 
 EXPORTED = [
-    "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_set_surfaces",
+    "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_set_surfaces", "sw_set_skybox",
     "sw_submit_draws",
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
@@ -57,6 +57,7 @@ def load_library(path=LIB_PATH):
         "sw_submit_surfaces": ([vp, vp, u32, u64], i32),
         "sw_rebuild_surfaces": ([vp], i32),
         "sw_set_surfaces": ([vp, vp, u64], i32),
+        "sw_set_skybox": ([vp, vp, vp, u64], i32),
         "sw_submit_draws": ([vp, vp, u32, vp, u32], i32),
         "sw_render": ([vp, vp, u32, i32], i32),
         "sw_postprocess": ([vp, vp, f32, vp, vp, u32, i32], i32),
@@ -207,6 +208,15 @@ class GpuRenderer:
     def set_surfaces(self, arena):
         arena = np.ascontiguousarray(arena)
         self._check(self.lib.sw_set_surfaces(self.ctx, abi.ptr(arena), arena.size), "sw_set_surfaces")
+
+    def set_skybox(self, texels32, texels64):
+        """Skybox side textures (all sides and mips, Color32 and Color64 copies of the same layout)."""
+        t32 = np.ascontiguousarray(texels32, dtype=np.uint32)
+        t64 = np.ascontiguousarray(texels64, dtype=np.uint64)
+        if t32.size != t64.size:
+            raise SwError("skybox texel arrays differ in size")
+        self._check(self.lib.sw_set_skybox(self.ctx, abi.ptr(t32) if t32.size else None,
+                                           abi.ptr(t64) if t64.size else None, t32.size), "sw_set_skybox")
 
     def submit_draws(self, draws, vertices):
         draws = np.ascontiguousarray(draws, dtype=abi.DRAW_CMD)

@@ -21,6 +21,9 @@ class SceneConfig(ctypes.Structure):
         ("normal_maps", ctypes.c_uint32), ("directional_lightmaps", ctypes.c_uint32),
         ("lights_per_room", ctypes.c_uint32), ("num_dynamic_lights", ctypes.c_uint32),
         ("num_frames", ctypes.c_uint32), ("emissive_frac", ctypes.c_float),
+        ("sky_rooms", ctypes.c_uint32), ("skybox_size", ctypes.c_uint32), ("skybox_brightness", ctypes.c_float),
+        ("skybox_missing_side", ctypes.c_int32), ("sky_rotation_speed", ctypes.c_float),
+        ("camera_pitch", ctypes.c_float),
     ]
 
 
@@ -28,7 +31,8 @@ class SceneInfo(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_uint32), ("leafs", ctypes.c_uint32), ("polygons", ctypes.c_uint32),
                 ("portals", ctypes.c_uint32), ("materials", ctypes.c_uint32), ("frames", ctypes.c_uint32),
                 ("dynamic_lights", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
-                ("lightmap_elements", ctypes.c_uint64), ("texels", ctypes.c_uint64)]
+                ("lightmap_elements", ctypes.c_uint64), ("texels", ctypes.c_uint64),
+                ("skybox_texels", ctypes.c_uint64)]
 
 
 class FrameOptions(ctypes.Structure):
@@ -41,7 +45,8 @@ class FrameOutputs(ctypes.Structure):
     _fields_ = [("surfaces", ctypes.c_void_p), ("num_surfaces", ctypes.c_uint32), ("num_draws", ctypes.c_uint32),
                 ("total_texels", ctypes.c_uint64), ("draws", ctypes.c_void_p), ("vertices", ctypes.c_void_p),
                 ("num_vertices", ctypes.c_uint32), ("num_lights", ctypes.c_uint32), ("lights", ctypes.c_void_p),
-                ("params", abi.FrameParams), ("visible_leafs", ctypes.c_uint32), ("camera_leaf", ctypes.c_uint32)]
+                ("params", abi.FrameParams), ("visible_leafs", ctypes.c_uint32), ("camera_leaf", ctypes.c_uint32),
+                ("skybox_draws", ctypes.c_uint32)]
 
 
 def load_host_library():
@@ -62,6 +67,7 @@ def load_host_library():
         "swh_renderer_destroy": ([vp], i32), "swh_renderer_prepare_frame": ([vp, u32, vp], i32),
         "swh_renderer_draw_frame": ([vp, vp, u32, i32], i32), "swh_renderer_context": ([vp], vp),
         "swh_renderer_frame": ([vp], vp),
+        "swh_scene_skybox": ([vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_uint64), vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -74,7 +80,7 @@ def load_host_library():
 HOST_EXPORTED = ["swh_scene_create", "swh_scene_destroy", "swh_scene_info", "swh_scene_create_info", "swh_last_error",
                  "swh_frame_create", "swh_frame_destroy", "swh_frame_prepare", "swh_frame_outputs",
                  "swh_renderer_create", "swh_renderer_destroy", "swh_renderer_prepare_frame",
-                 "swh_renderer_draw_frame", "swh_renderer_context", "swh_renderer_frame"]
+                 "swh_renderer_draw_frame", "swh_renderer_context", "swh_renderer_frame", "swh_scene_skybox"]
 
 # The two map configurations of the benchmark plan.
 SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, num_materials=16, metal_frac=0.0,
@@ -83,6 +89,10 @@ SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, 
 FULL_MAP = dict(seed=2, grid_x=8, grid_y=8, tile_size=80.0, texture_size=256, num_materials=32, metal_frac=0.25,
                 dielectric_frac=0.25, normal_maps=1, directional_lightmaps=1, lights_per_room=2,
                 num_dynamic_lights=8, num_frames=256)
+# The small map with a sky: three rooms open to a skybox (the sky material's six 128x128 sides, HDR
+# brightness 2, rotating slowly), the camera looking 0.45 rad up so ceilings are in view.
+SKY_MAP = dict(SMALL_MAP, sky_rooms=3, skybox_size=128, skybox_brightness=2.0, sky_rotation_speed=0.01,
+               camera_pitch=0.45)
 
 
 def _check(lib, r, what):
@@ -96,7 +106,9 @@ class Scene:
         self.lib = load_host_library()
         c = SceneConfig(seed=1, grid_x=4, grid_y=2, room_min=256.0, room_max=1024.0, tile_size=128.0, texture_size=128,
                         num_materials=16, metal_frac=0.0, dielectric_frac=0.0, normal_maps=0, directional_lightmaps=0,
-                        lights_per_room=1, num_dynamic_lights=0, num_frames=64, emissive_frac=0.0)
+                        lights_per_room=1, num_dynamic_lights=0, num_frames=64, emissive_frac=0.0, sky_rooms=0,
+                        skybox_size=128, skybox_brightness=1.0, skybox_missing_side=-1, sky_rotation_speed=0.01,
+                        camera_pitch=0.0)
         for k, v in kw.items():
             setattr(c, k, v)
         self.config = c
@@ -112,6 +124,22 @@ class Scene:
         ci = abi.CreateInfo()
         _check(self.lib, self.lib.swh_scene_create_info(self.handle, device, ctypes.byref(ci)), "swh_scene_create_info")
         return ci
+
+    def skybox(self):
+        """(texels32, texels64, mip_offsets[6, 5], mip_sizes[6, 5]) numpy copies; empty arrays without sky."""
+        t32, t64, n = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_uint64()
+        offs = np.zeros(30, np.uint64)
+        sizes = np.zeros(30, np.uint32)
+        _check(self.lib, self.lib.swh_scene_skybox(self.handle, ctypes.byref(t32), ctypes.byref(t64), ctypes.byref(n),
+                                                   abi.ptr(offs), abi.ptr(sizes)), "swh_scene_skybox")
+        count = int(n.value)
+
+        def arr(p, dt):
+            if not p.value or count == 0:
+                return np.zeros(0, dt)
+            return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)),
+                                         shape=(count * np.dtype(dt).itemsize,)).view(dt).copy()
+        return arr(t32, np.uint32), arr(t64, np.uint64), offs.reshape(6, 5), sizes.reshape(6, 5)
 
     def static_data(self):
         """numpy copies of the static data (for the oracle and GpuRenderer)."""
@@ -173,6 +201,7 @@ class Frame:
         ctypes.pointer(self.params)[0] = o.params
         self.visible_leafs = int(o.visible_leafs)
         self.camera_leaf = int(o.camera_leaf)
+        self.skybox_draws = int(o.skybox_draws)
         return self
 
     def close(self):

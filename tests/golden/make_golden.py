@@ -20,7 +20,7 @@ for p in (os.path.join(ROOT, "square-wheel_gb300"), os.path.join(ROOT, "oracle")
 
 import oracle  # noqa: E402
 import scenes  # noqa: E402
-from sqwheel import abi, gpu, synth  # noqa: E402
+from sqwheel import abi, gpu, host, synth  # noqa: E402
 
 SURFACE_CASES = {
     # name: BatchedSurfaces arguments
@@ -34,6 +34,12 @@ RASTER_CASES = {
                        pixel_format=abi.SW_PIXEL_C32, texel_density=0.2, max_texture_side=48),
     "raster_c64": dict(seed=202, width=160, height=120, num_quads=30, modes=(0, 1, 2), blends=(0, 1, 2, 3, 4),
                        pixel_format=abi.SW_PIXEL_C64, texel_density=0.2, max_texture_side=48),
+}
+# A frame of the sky map (draw_skybox first, then the world) at 160x120 Color64: skybox sides of 32 texels
+# at HDR brightness 2, rotated by the frame's sky angle.
+SKY_RASTER_CASES = {
+    "raster_sky_c64": dict(scene=dict(host.SKY_MAP, skybox_size=32), frame=5, width=160, height=120,
+                           pixel_format=abi.SW_PIXEL_C64),
 }
 POST_CASES = {
     # name: (PostConfig overrides, frames)
@@ -77,6 +83,24 @@ def make_raster(name, kw):
                         frame_params=frame_params_array(fp), framebuffer_in=fb0, want=want)
 
 
+def make_sky_raster(name, kw):
+    sc = host.Scene(**kw["scene"])
+    w, h, fmt = kw["width"], kw["height"], kw["pixel_format"]
+    fr = host.Frame(sc).prepare(kw["frame"], host.frame_options(w, h, fmt, directional=False))
+    assert fr.skybox_draws > 0
+    t32, t64, _, _ = sc.skybox()
+    arena = oracle.build_surfaces(sc.static_data(), fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=1)
+    rng = np.random.default_rng(9)
+    dt = np.uint64 if fmt == abi.SW_PIXEL_C64 else np.uint32
+    fb0 = rng.integers(0, 1 << 16, (h, w), dtype=np.uint64).astype(dt)
+    want = fb0.copy()
+    bad = oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, want, skybox=t64 if fmt == abi.SW_PIXEL_C64 else t32)
+    assert bad == 0
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), arena=arena, draws=fr.draws, vertices=fr.vertices,
+                        frame_params=frame_params_array(fr.params), framebuffer_in=fb0, want=want, skybox32=t32,
+                        skybox64=t64)
+
+
 def make_post(name, overrides, frames):
     cfg = abi.PostConfig.default()
     for k, v in overrides.items():
@@ -110,6 +134,8 @@ def main():
         make_surfaces(name, kw)
     for name, kw in RASTER_CASES.items():
         make_raster(name, kw)
+    for name, kw in SKY_RASTER_CASES.items():
+        make_sky_raster(name, kw)
     for name, (ov, n) in POST_CASES.items():
         make_post(name, ov, n)
     for f in sorted(os.listdir(HERE)):

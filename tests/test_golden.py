@@ -56,7 +56,9 @@ def test_oracle_reproduces_fixture(built_libs, path):
         assert np.array_equal(got, d["want"])
     elif kind == "raster":
         fb = d["framebuffer_in"].copy()
-        bad = oracle.rasterize(d["draws"], d["vertices"], d["arena"], _frame_params(d["frame_params"]), fb)
+        fp = _frame_params(d["frame_params"])
+        sky = d.get("skybox64" if fp.pixel_format == abi.SW_PIXEL_C64 else "skybox32")
+        bad = oracle.rasterize(d["draws"], d["vertices"], d["arena"], fp, fb, skybox=sky)
         assert bad == 0 and np.array_equal(fb, d["want"])
     else:
         cfg = _post_config(d["config"])
@@ -218,6 +220,8 @@ def test_gpu_reproduces_fixture(gpu_ok, path):
             r.frame_begin(fp, None)
             r.set_framebuffer(fb_in, fp.pixel_format)
             r.set_surfaces(d["arena"])
+            if "skybox32" in d:
+                r.set_skybox(d["skybox32"], d["skybox64"])
             r.submit_draws(d["draws"], d["vertices"])
             got = np.zeros_like(fb_in)
             r.render(got)

@@ -9,15 +9,20 @@ from sqwheel import abi, gpu, host
 pytestmark = pytest.mark.gpu
 
 
-def run_frames(scene, frames, w, h, fmt, directional, post=False):
+def run_frames(scene, frames, w, h, fmt, directional, post=False, clear=False):
     st = scene.static_data()
     fr = host.Frame(scene)
     r = gpu.GpuRenderer(st)
+    t32, t64, _, _ = scene.skybox()
+    sky = None
+    if t32.size:
+        r.set_skybox(t32, t64)
+        sky = t64 if fmt == abi.SW_PIXEL_C64 else t32
     exposure = 1.0
     cfg = abi.PostConfig.default()
     try:
         for fi in frames:
-            fr.prepare(fi, host.frame_options(w, h, fmt, directional=directional))
+            fr.prepare(fi, host.frame_options(w, h, fmt, directional=directional, clear_background=clear))
             want_arena = oracle.build_surfaces(st, fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=8)
             r.frame_begin(fr.params, fr.lights)
             r.submit_surfaces(fr.surfaces, fr.total_texels)
@@ -25,8 +30,11 @@ def run_frames(scene, frames, w, h, fmt, directional, post=False):
             assert np.array_equal(want_arena, got_arena), f"frame {fi}: surfaces differ"
             dt = np.uint64 if fmt == abi.SW_PIXEL_C64 else np.uint32
             want = np.zeros((h, w), dt)
-            bad = oracle.rasterize(fr.draws, fr.vertices, want_arena, fr.params, want)
+            if clear:
+                oracle.clear_background(fr.params, want)
+            bad = oracle.rasterize(fr.draws, fr.vertices, want_arena, fr.params, want, skybox=sky)
             assert bad == 0
+            assert sky is None or fr.skybox_draws > 0
             r.submit_draws(fr.draws, fr.vertices)
             got = np.zeros((h, w), dt)
             r.render(got)
@@ -53,6 +61,57 @@ def test_full_map_frames_hdr_with_postprocess(gpu_ok):
     bloom + tonemap + exposure, at a reduced resolution so the single-thread oracle stays fast."""
     scene = host.Scene(**dict(host.FULL_MAP, grid_x=4, grid_y=4))
     run_frames(scene, [0, 30, 31, 32, 90], 480, 270, abi.SW_PIXEL_C64, directional=True, post=True)
+
+
+@pytest.mark.parametrize("fmt", [abi.SW_PIXEL_C32, abi.SW_PIXEL_C64])
+def test_sky_map_frames(gpu_ok, fmt):
+    """draw_skybox: the skybox sides (HDR brightness 2) behind open ceilings, rotating, drawn first."""
+    scene = host.Scene(**host.SKY_MAP)
+    run_frames(scene, [0, 5, 23, 47, 63], 400, 300, fmt, directional=False, post=fmt == abi.SW_PIXEL_C64)
+
+
+def test_sky_map_missing_side_and_validation(gpu_ok):
+    scene = host.Scene(**dict(host.SKY_MAP, skybox_missing_side=5, skybox_size=64))
+    # the sky's top is missing: those pixels keep the background (cleared here, draw_background)
+    run_frames(scene, [3, 31], 320, 240, abi.SW_PIXEL_C32, directional=False, clear=True)
+    # a skybox draw needs sw_set_skybox; an unknown texture source is rejected
+    st = scene.static_data()
+    fr = host.Frame(scene).prepare(3, host.frame_options(320, 240, abi.SW_PIXEL_C32, directional=False))
+    r = gpu.GpuRenderer(st)
+    try:
+        r.frame_begin(fr.params, fr.lights)
+        r.submit_surfaces(fr.surfaces, fr.total_texels)
+        with pytest.raises(gpu.SwError, match="skybox"):
+            r.submit_draws(fr.draws, fr.vertices)
+        t32, t64, _, _ = scene.skybox()
+        r.set_skybox(t32, t64)
+        bad = fr.draws.copy()
+        bad["tex_source"][0] = 2
+        with pytest.raises(gpu.SwError, match="texture source"):
+            r.submit_draws(bad, fr.vertices)
+        r.submit_draws(fr.draws, fr.vertices)
+    finally:
+        r.close()
+
+
+def test_host_renderer_sky_map(gpu_ok):
+    """The C++ host renderer uploads the scene's skybox itself (swh_renderer_create)."""
+    scene = host.Scene(**host.SKY_MAP)
+    hr = host.HostRenderer(scene)
+    try:
+        opts = host.frame_options(320, 240, abi.SW_PIXEL_C64, directional=False)
+        hr.prepare_frame(17, opts)
+        got = np.zeros((240, 320), np.uint64)
+        hr.draw_frame(got)
+    finally:
+        hr.close()
+    st = scene.static_data()
+    fr = host.Frame(scene).prepare(17, opts)
+    assert fr.skybox_draws > 0
+    arena = oracle.build_surfaces(st, fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=4)
+    want = np.zeros((240, 320), np.uint64)
+    oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, want, skybox=scene.skybox()[1])
+    assert np.array_equal(want, got)
 
 
 def test_host_renderer_matches_python_driven_path(gpu_ok):
