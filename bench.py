@@ -116,10 +116,11 @@ def frame_indices(n, offset=0):
 # frame workload
 
 def post_bytes(w, h, scale=2):
-    """Algorithmic bytes of bloom + tonemap: downscale read, blur read+write twice, tonemap read of HDR
-    and bloom + write of Color32."""
+    """Algorithmic bytes of bloom + tonemap as two passes over the frame: HDR read by the downscale and
+    again by the tonemap, the blurred bloom buffer written once and read once, the Color32 frame written
+    (the separate downscale / blur / blur passes would add 12 MB of bloom traffic at 1080p)."""
     bw, bh = w // scale, h // scale
-    return w * h * 8 + 2 * bw * bh * 8 * 2 + w * h * (8 + 4) + bw * bh * 8
+    return w * h * 8 * 2 + bw * bh * 8 * 2 + w * h * 4
 
 
 class FrameWorkload:
@@ -279,7 +280,7 @@ def run_frame_gpu(args, world, rank, local):
                 frame_span += t[4]
                 texels += f["total_texels"]
                 surf_bytes += work.surface_bytes(f)
-                launches += 1 + 3 + 5  # surfaces; raster walk, rows, tiles; postprocess (5 kernels)
+                launches += 1 + 3 + 3  # surfaces; raster walk, rows, tiles; postprocess (3 kernels)
             if step == args.warmup - 1:
                 pix_before = r.stats().pixel_writes
         pix_writes = r.stats().pixel_writes - pix_before
@@ -294,7 +295,7 @@ def run_frame_gpu(args, world, rank, local):
             t = r.timings()
             if step >= args.warmup:
                 graph_ms.append(t[4])
-                launches += 1 + 3 + 5
+                launches += 1 + 3 + 3
         torch.cuda.synchronize()
     stage_sum_ms = (totals["surf"] + totals["raster"] + totals["post"]) / args.steps
     frame_ms = statistics.mean(graph_ms)
@@ -331,7 +332,7 @@ def run_frame_gpu(args, world, rank, local):
 
     lr = run_learned(args, work, r, ldr_frames, local) if args.learn_steps > 0 else None
     if lr is not None:
-        launches += args.steps * (1 + 3 + 5 + 1)  # half-resolution frame + the fused upscale kernel
+        launches += args.steps * (1 + 3 + 3 + 1)  # half-resolution frame + the fused upscale kernel
 
     peak, peak_kind = peaks()
     s = args.steps
@@ -348,7 +349,7 @@ def run_frame_gpu(args, world, rank, local):
                      "frac_of_measured_hbm": round(gbs / peak, 4)}
     dom = max(totals, key=totals.get)
     kernel_names = {"surf": "surf_build_kernel", "raster": "raster_setup_kernel + raster_tiles_kernel",
-                    "post": "pp_downscale/pp_blur_h/pp_blur_v/pp_tonemap_bloom"}
+                    "post": "pp_downscale_blur_h + pp_blur_v_tonemap"}
     out_line = None
     if rank == 0:
         cpu = cpu_frame_baseline(work)

@@ -5,10 +5,12 @@
 // Gaussian blur (:846-956), Reinhard tonemapping with nearest or linear bloom (:226-726, :997-1024);
 // and FrameUpscaler::perform_upscale (src/square_wheel/frame_upscaler.rs:42-239).
 //
-// All passes are HBM-bound streaming kernels with one thread per output pixel. Integer sums use
-// wrapping 32-bit adds, which are associative, so the per-line sums can be reduced in any order and
-// remain bit-exact; the single float reduction over lines (sum of line sums, in line order) runs in one
-// thread exactly as the reference's sequential loop does.
+// With bloom the frame takes two streaming launches: downscale + horizontal blur (one block per bloom
+// line, the downscaled line kept in shared memory) and vertical blur + tonemap (one block per output
+// tile, the bloom cells it samples blurred in shared memory), plus the exposure average on the side.
+// Integer sums use wrapping 32-bit adds, which are associative, so the per-line sums can be reduced in
+// any order and remain bit-exact; the single float reduction over lines (sum of line sums, in line
+// order) runs in one thread exactly as the reference's sequential loop does.
 #include "sw_kernels.cuh"
 
 namespace swgpu
@@ -28,93 +30,6 @@ __device__ __forceinline__ CV tonemap(CV c, const PostArgs& a)
 		__fdiv_rn(c.r, mad2(c.r, a.inv_255[2], a.inv_scale[2])), alpha};
 }
 
-// downscale_hdr_buffer::<S>, postprocessor.rs:792-844. Each thread computes two horizontally adjacent
-// bloom pixels (all 2*S*S HDR pixels are loaded before any is used: S is a template parameter, so the
-// loops unroll); a block covers 512 bloom pixels of one line and adds its lanes' exact integer line
-// sums with one atomic per lane.
-template <int S>
-__global__ void __launch_bounds__(256) pp_downscale_kernel(PostArgs a)
-{
-	__shared__ int32_t s_sum[8][4];
-	const uint32_t bx = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-	const uint32_t by = blockIdx.y;
-	int32_t avg[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
-	constexpr int32_t scaler = 256 / (S * S);
-#pragma unroll
-	for (int k = 0; k < 2; ++k)
-	{
-		if (bx + k >= a.bw) break;
-		int32_t sum[4] = {0, 0, 0, 0};
-		unsigned long long q[S][S];
-#pragma unroll
-		for (int dy = 0; dy < S; ++dy)
-		{
-			const uint64_t* row = a.hdr + uint64_t(by * S + dy) * a.width + (bx + k) * S;
-			const bool aligned = (reinterpret_cast<uintptr_t>(row) & 15) == 0;
-#pragma unroll
-			for (int dx = 0; dx < S; dx += 2)
-			{
-				if (aligned)
-				{
-					const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(row + dx));
-					q[dy][dx] = v.x;
-					q[dy][dx + 1] = v.y;
-				}
-				else
-				{
-					q[dy][dx] = __ldg(reinterpret_cast<const unsigned long long*>(row) + dx);
-					q[dy][dx + 1] = __ldg(reinterpret_cast<const unsigned long long*>(row) + dx + 1);
-				}
-			}
-		}
-#pragma unroll
-		for (int dy = 0; dy < S; ++dy)
-#pragma unroll
-			for (int dx = 0; dx < S; ++dx)
-			{
-				const CI c = ci_from_c64(q[dy][dx]);
-#pragma unroll
-				for (int i = 0; i < 4; ++i) sum[i] = wadd(sum[i], c.v[i]);
-			}
-#pragma unroll
-		for (int i = 0; i < 4; ++i) avg[k][i] = wmul(sum[i], scaler) >> 8;
-	}
-	if (bx < a.bw)
-	{
-		const uint64_t o = uint64_t(by) * a.bw + bx;
-		const uint64_t v0 = ci_to_c64(CI{{avg[0][0], avg[0][1], avg[0][2], avg[0][3]}});
-		if (bx + 1 < a.bw)
-		{
-			const uint64_t v1 = ci_to_c64(CI{{avg[1][0], avg[1][1], avg[1][2], avg[1][3]}});
-			if ((o & 1) == 0)
-				*reinterpret_cast<ulonglong2*>(a.bloom0 + o) = make_ulonglong2(v0, v1);
-			else
-			{
-				a.bloom0[o] = v0;
-				a.bloom0[o + 1] = v1;
-			}
-		}
-		else
-			a.bloom0[o] = v0;
-	}
-	// Exact per-line sums of the averages (wrapping i32: order-independent): warp, then block.
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-	for (int i = 0; i < 4; ++i)
-	{
-		int32_t v = wadd(avg[0][i], avg[1][i]);
-		for (int o = 16; o > 0; o >>= 1) v = wadd(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
-		if (lane == 0) s_sum[warp][i] = v;
-	}
-	__syncthreads();
-	if (threadIdx.x < 4)
-	{
-		int32_t t = 0;
-		for (int w = 0; w < 8; ++w) t = wadd(t, s_sum[w][threadIdx.x]);
-		atomicAdd(a.line_sums + by * 4 + threadIdx.x, t);
-	}
-}
-
 // Sequential f32 sum over `n` lines of 4-lane values, in line order, as the reference's loop does; the
 // block stages chunks of lines in shared memory with coalesced loads and threads 0..3 (one per lane)
 // run the ordered additions from shared memory.
@@ -122,15 +37,41 @@ template <class LoadT>
 __device__ __forceinline__ void ordered_line_sum(uint32_t n, LoadT load, float inv, float* out)
 {
 	constexpr uint32_t CHUNK = 2048;
+	constexpr int LOADS = 8; // global loads in flight per thread while staging
 	__shared__ float s_lines[CHUNK * 4];
 	float acc = 0.0f;
 	for (uint32_t base = 0; base < n; base += CHUNK)
 	{
 		const uint32_t m = min(CHUNK, n - base);
-		for (uint32_t i = threadIdx.x; i < m * 4; i += blockDim.x) s_lines[i] = load(base * 4 + i);
+		const uint32_t total = m * 4;
+		for (uint32_t i0 = threadIdx.x; i0 < total; i0 += LOADS * blockDim.x)
+		{
+			float v[LOADS];
+#pragma unroll
+			for (int k = 0; k < LOADS; ++k)
+			{
+				const uint32_t i = i0 + k * blockDim.x;
+				v[k] = i < total ? load(base * 4 + i) : 0.0f;
+			}
+#pragma unroll
+			for (int k = 0; k < LOADS; ++k)
+				if (i0 + k * blockDim.x < total) s_lines[i0 + k * blockDim.x] = v[k];
+		}
 		__syncthreads();
 		if (threadIdx.x < 4)
-			for (uint32_t y = 0; y < m; ++y) acc = fadd(acc, s_lines[y * 4 + threadIdx.x]);
+		{
+			// the additions stay in line order; only the shared-memory reads are batched ahead of them
+			uint32_t y = 0;
+			for (; y + 8 <= m; y += 8)
+			{
+				float t[8];
+#pragma unroll
+				for (int k = 0; k < 8; ++k) t[k] = s_lines[(y + k) * 4 + threadIdx.x];
+#pragma unroll
+				for (int k = 0; k < 8; ++k) acc = fadd(acc, t[k]);
+			}
+			for (; y < m; ++y) acc = fadd(acc, s_lines[y * 4 + threadIdx.x]);
+		}
 		__syncthreads();
 	}
 	if (threadIdx.x < 4) out[threadIdx.x] = fmul(acc, inv);
@@ -143,58 +84,19 @@ __global__ void __launch_bounds__(256) pp_average_bloom_kernel(PostArgs a)
 	ordered_line_sum(a.bh, [&](uint32_t i) { return float(sums[i]); }, __fdiv_rn(1.0f, float(a.bw * a.bh)), a.average);
 }
 
-// perform_blur_impl, horizontal pass buf0 -> buf1 (postprocessor.rs:862-900)
-__global__ void __launch_bounds__(256) pp_blur_h_kernel(PostArgs a)
+// Bloom cells of a tile held in shared memory: cell (x, y) of the bloom buffer at [y - y0][x - x0].
+struct BloomTile
 {
-	const int32_t x = int32_t(blockIdx.x * blockDim.x + threadIdx.x);
-	const int32_t y = int32_t(blockIdx.y);
-	if (x >= int32_t(a.bw)) return;
-	const uint64_t* line = a.bloom0 + uint64_t(y) * a.bw;
-	const int32_t r = int32_t(a.radius);
-	const CI c = ci_from_c64(line[x]);
-	int32_t sum[4];
-#pragma unroll
-	for (int i = 0; i < 4; ++i) sum[i] = wmul(c.v[i], a.kernel_h[r]);
-	for (int32_t dx = 1; dx <= r; ++dx)
-	{
-		const CI c0 = ci_from_c64(line[max(x - dx, 0)]);
-		const CI c1 = ci_from_c64(line[min(x + dx, int32_t(a.bw) - 1)]);
-#pragma unroll
-		for (int i = 0; i < 4; ++i) sum[i] = wadd(sum[i], wmul(wadd(c0.v[i], c1.v[i]), a.kernel_h[dx + r]));
-	}
-	a.bloom1[uint64_t(y) * a.bw + x] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
-}
-
-// perform_blur_impl, vertical pass buf1 -> buf0 with bloom_scale folded into the weights (:902-955)
-__global__ void __launch_bounds__(256) pp_blur_v_kernel(PostArgs a)
-{
-	const int32_t x = int32_t(blockIdx.x * blockDim.x + threadIdx.x);
-	const int32_t y = int32_t(blockIdx.y);
-	if (x >= int32_t(a.bw)) return;
-	const int32_t r = int32_t(a.radius);
-	const CI c = ci_from_c64(a.bloom1[uint64_t(y) * a.bw + x]);
-	int32_t sum[4];
-#pragma unroll
-	for (int i = 0; i < 4; ++i) sum[i] = wmul(c.v[i], a.kernel_v[r]);
-	for (int32_t dy = 1; dy <= r; ++dy)
-	{
-		const CI c0 = ci_from_c64(a.bloom1[uint64_t(max(y - dy, 0)) * a.bw + x]);
-		const CI c1 = ci_from_c64(a.bloom1[uint64_t(min(y + dy, int32_t(a.bh) - 1)) * a.bw + x]);
-#pragma unroll
-		for (int i = 0; i < 4; ++i) sum[i] = wadd(sum[i], wmul(wadd(c0.v[i], c1.v[i]), a.kernel_v[dy + r]));
-	}
-	a.bloom0[uint64_t(y) * a.bw + x] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
-}
-
-__device__ __forceinline__ CV bloom_at(const PostArgs& a, uint32_t x, uint32_t y)
-{
-	return cv_from_c64(__ldg(reinterpret_cast<const unsigned long long*>(a.bloom0) + uint64_t(y) * a.bw + x));
-}
+	const uint64_t* cells;
+	uint32_t x0, y0, pitch;
+	__device__ CV at(uint32_t x, uint32_t y) const { return cv_from_c64(cells[(y - y0) * pitch + (x - x0)]); }
+};
 
 // HDR pixel (x, y) plus its bloom sample, nearest (postprocessor.rs:346-462) or linear (:464-726).
-template <int S, bool LINEAR>
-__device__ __forceinline__ CV bloom_sum(const PostArgs& a, uint32_t x, uint32_t y, CV c)
+template <int S, bool LINEAR, class Bloom>
+__device__ __forceinline__ CV bloom_sum(const PostArgs& a, const Bloom& bl, uint32_t x, uint32_t y, CV c)
 {
+	auto bloom_at = [&](const PostArgs&, uint32_t bx, uint32_t by) { return bl.at(bx, by); };
 	CV sum;
 	if (!LINEAR)
 	{
@@ -235,45 +137,254 @@ __device__ __forceinline__ CV bloom_sum(const PostArgs& a, uint32_t x, uint32_t 
 	return sum;
 }
 
-// Tonemapping with bloom: four horizontally adjacent pixels per thread (two 16-byte HDR loads issued
-// together, one 16-byte store where aligned).
-template <int S, bool LINEAR>
-__global__ void __launch_bounds__(256) pp_tonemap_bloom_kernel(PostArgs a)
+// ---- fused bloom passes: two launches instead of downscale, blur h, blur v, tonemap ----
+//
+// pp_downscale_blur_h_kernel: one block per bloom line. The S lines of HDR pixels are box-averaged into
+// the line (downscale_hdr_buffer, postprocessor.rs:792-844) in shared memory, the line's exact integer
+// lane sums are written for the exposure average (no atomics: the block owns the line), and the
+// horizontal blur pass (:862-900) runs from shared memory into bloom1. The downscaled line never goes
+// to HBM. With radius 0 (no blur) the downscaled line itself is written.
+template <int S>
+__global__ void __launch_bounds__(256) pp_downscale_blur_h_kernel(PostArgs a)
 {
-	const uint32_t x = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
-	const uint32_t y = blockIdx.y;
-	if (x >= a.width) return;
-	const uint64_t src = uint64_t(y) * a.width + x;
-	const uint64_t dst = uint64_t(y) * a.dst_pitch + x;
-	const uint32_t n = min(4u, a.width - x);
-	unsigned long long p[4] = {0, 0, 0, 0};
-	const unsigned long long* h = reinterpret_cast<const unsigned long long*>(a.hdr) + src;
-	if (n == 4 && (src & 1) == 0)
+	extern __shared__ __align__(16) uint64_t s_line[]; // bw packed Color64 bloom pixels
+	__shared__ int32_t s_sum[8][4];
+	const uint32_t by = blockIdx.x;
+	constexpr int32_t scaler = 256 / (S * S);
+	// U bloom pixels per thread per pass, all their HDR loads issued before any is used
+	constexpr int U = S == 2 ? 4 : S == 4 ? 2 : 1;
+	const unsigned long long* hdr = reinterpret_cast<const unsigned long long*>(a.hdr);
+	const bool vec = ((a.width & 1) == 0) && ((reinterpret_cast<uintptr_t>(a.hdr) & 15) == 0); // 16-byte pairs
+	int32_t lsum[4] = {0, 0, 0, 0};
+	for (uint32_t base = threadIdx.x; base < a.bw; base += blockDim.x * U)
 	{
-		const ulonglong2 v0 = __ldg(reinterpret_cast<const ulonglong2*>(h));
-		const ulonglong2 v1 = __ldg(reinterpret_cast<const ulonglong2*>(h + 2));
-		p[0] = v0.x;
-		p[1] = v0.y;
-		p[2] = v1.x;
-		p[3] = v1.y;
+		unsigned long long q[U][S][S];
+#pragma unroll
+		for (int u = 0; u < U; ++u)
+		{
+			const uint32_t bx = base + u * blockDim.x;
+			if (bx >= a.bw) break;
+#pragma unroll
+			for (int dy = 0; dy < S; ++dy)
+			{
+				const unsigned long long* row = hdr + uint64_t(by * S + dy) * a.width + uint64_t(bx) * S;
+#pragma unroll
+				for (int dx = 0; dx < S; dx += 2)
+				{
+					if (vec)
+					{
+						const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(row + dx));
+						q[u][dy][dx] = v.x;
+						q[u][dy][dx + 1] = v.y;
+					}
+					else
+					{
+						q[u][dy][dx] = __ldg(row + dx);
+						q[u][dy][dx + 1] = __ldg(row + dx + 1);
+					}
+				}
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < U; ++u)
+		{
+			const uint32_t bx = base + u * blockDim.x;
+			if (bx >= a.bw) break;
+			int32_t sum[4] = {0, 0, 0, 0};
+#pragma unroll
+			for (int dy = 0; dy < S; ++dy)
+#pragma unroll
+				for (int dx = 0; dx < S; ++dx)
+				{
+					const CI c = ci_from_c64(q[u][dy][dx]);
+#pragma unroll
+					for (int i = 0; i < 4; ++i) sum[i] = wadd(sum[i], c.v[i]);
+				}
+			CI avg;
+#pragma unroll
+			for (int i = 0; i < 4; ++i)
+			{
+				avg.v[i] = wmul(sum[i], scaler) >> 8;
+				lsum[i] = wadd(lsum[i], avg.v[i]);
+			}
+			s_line[bx] = ci_to_c64(avg);
+		}
 	}
-	else
+	// exact per-line sums of the averages (wrapping i32: order-independent)
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+	for (int i = 0; i < 4; ++i)
 	{
+		int32_t v = lsum[i];
+		for (int o = 16; o > 0; o >>= 1) v = wadd(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+		if (lane == 0) s_sum[warp][i] = v;
+	}
+	__syncthreads();
+	if (threadIdx.x < 4)
+	{
+		int32_t t = 0;
+		for (int w = 0; w < int(blockDim.x >> 5); ++w) t = wadd(t, s_sum[w][threadIdx.x]);
+		a.line_sums[by * 4 + threadIdx.x] = t;
+	}
+	const int32_t r = int32_t(a.radius);
+	uint64_t* out = a.bloom1 + uint64_t(by) * a.bw;
+	for (int32_t x = int32_t(threadIdx.x); x < int32_t(a.bw); x += int32_t(blockDim.x))
+	{
+		if (r == 0)
+		{
+			out[x] = s_line[x];
+			continue;
+		}
+		const CI c = ci_from_c64(s_line[x]);
+		int32_t sum[4];
+#pragma unroll
+		for (int i = 0; i < 4; ++i) sum[i] = wmul(c.v[i], a.kernel_h[r]);
+		for (int32_t dx = 1; dx <= r; ++dx)
+		{
+			const CI c0 = ci_from_c64(s_line[max(x - dx, 0)]);
+			const CI c1 = ci_from_c64(s_line[min(x + dx, int32_t(a.bw) - 1)]);
+#pragma unroll
+			for (int i = 0; i < 4; ++i) sum[i] = wadd(sum[i], wmul(wadd(c0.v[i], c1.v[i]), a.kernel_h[dx + r]));
+		}
+		out[x] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
+	}
+}
+
+// pp_blur_v_tonemap_kernel: one block per TM_W x TM_H tile of the output. It stages the h-blurred bloom
+// lines its tile needs (the bloom cells its pixels sample, +-radius lines) in shared memory, runs the
+// vertical blur pass (:902-955, bloom_scale folded into the weights) for those cells, then tonemaps its
+// pixels with the nearest or linear bloom sample (:346-726) read from shared memory.
+constexpr uint32_t TM_W = 256, TM_H = 16;
+
+template <int S>
+__host__ __device__ __forceinline__ void bloom_tile_range(uint32_t p0, uint32_t n, uint32_t cells, uint32_t& lo, uint32_t& hi)
+{
+	constexpr uint32_t half = S / 2;
+	lo = min(p0 >= half ? (p0 - half) / S : 0u, cells - 1);
+	hi = min((p0 + n - 1) / S + 1, cells - 1);
+}
+
+template <int S>
+__host__ __device__ __forceinline__ uint32_t tonemap_tile_smem(uint32_t radius)
+{
+	// cells: (TM_W / S + 3) columns x (TM_H / S + 3) lines, staged lines + 2 radius more
+	const uint32_t cols = TM_W / S + 3, lines = TM_H / S + 3;
+	return (cols * (lines + 2 * radius) + cols * lines) * 8u;
+}
+
+template <int S, bool LINEAR>
+__global__ void __launch_bounds__(256) pp_blur_v_tonemap_kernel(PostArgs a)
+{
+	extern __shared__ __align__(16) uint64_t s_tile[];
+	const uint32_t x0 = blockIdx.x * TM_W, y0 = blockIdx.y * TM_H;
+	const uint32_t tw = min(TM_W, a.width - x0), th = min(TM_H, a.height - y0);
+	uint32_t cx0, cx1, cy0, cy1;
+	bloom_tile_range<S>(x0, tw, a.bw, cx0, cx1);
+	bloom_tile_range<S>(y0, th, a.bh, cy0, cy1);
+	const uint32_t cols = cx1 - cx0 + 1, lines = cy1 - cy0 + 1;
+	const int32_t r = int32_t(a.radius);
+	// staged h-blurred lines cy0 - r .. cy1 + r (clamped to the buffer when read)
+	const uint32_t staged = lines + 2 * uint32_t(r);
+	uint64_t* s_h = s_tile;
+	uint64_t* s_v = s_tile + staged * cols;
+	{
+		// four loads in flight per thread
+		const uint32_t total = staged * cols;
+		for (uint32_t i0 = threadIdx.x; i0 < total; i0 += 4 * blockDim.x)
+		{
+			unsigned long long v[4];
+#pragma unroll
+			for (int k = 0; k < 4; ++k)
+			{
+				const uint32_t i = i0 + k * blockDim.x;
+				if (i < total)
+				{
+					const uint32_t l = i / cols, c = i % cols;
+					const int32_t by = min(max(int32_t(cy0) - r + int32_t(l), 0), int32_t(a.bh) - 1);
+					v[k] = __ldg(reinterpret_cast<const unsigned long long*>(a.bloom1) + uint64_t(by) * a.bw + cx0 + c);
+				}
+			}
+#pragma unroll
+			for (int k = 0; k < 4; ++k)
+				if (i0 + k * blockDim.x < total) s_h[i0 + k * blockDim.x] = v[k];
+		}
+	}
+	__syncthreads();
+	for (uint32_t i = threadIdx.x; i < lines * cols; i += blockDim.x)
+	{
+		const uint32_t l = i / cols, c = i % cols;
+		if (r == 0)
+		{
+			s_v[i] = s_h[l * cols + c];
+			continue;
+		}
+		// line cy0 + l is staged at l + r; its neighbours at l + r -+ dy (clamping already applied)
+		const CI cc = ci_from_c64(s_h[(l + r) * cols + c]);
+		int32_t sum[4];
+#pragma unroll
+		for (int k = 0; k < 4; ++k) sum[k] = wmul(cc.v[k], a.kernel_v[r]);
+		for (int32_t dy = 1; dy <= r; ++dy)
+		{
+			const CI c0 = ci_from_c64(s_h[(l + r - dy) * cols + c]);
+			const CI c1 = ci_from_c64(s_h[(l + r + dy) * cols + c]);
+#pragma unroll
+			for (int k = 0; k < 4; ++k) sum[k] = wadd(sum[k], wmul(wadd(c0.v[k], c1.v[k]), a.kernel_v[dy + r]));
+		}
+		s_v[i] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
+	}
+	__syncthreads();
+	const BloomTile tile{s_v, cx0, cy0, cols};
+	// 4 horizontally adjacent pixels per thread: 64 threads per 256-pixel line, lines ly, ly + 4, ly + 8,
+	// ly + 12 of the tile (TM_H = 16), their HDR loads all issued first
+	const uint32_t lx = 4 * (threadIdx.x & 63), ly0 = threadIdx.x >> 6;
+	if (lx >= tw) return;
+	const uint32_t n = min(4u, tw - lx);
+	const unsigned long long* hdr = reinterpret_cast<const unsigned long long*>(a.hdr);
+	unsigned long long p[TM_H / 4][4];
+#pragma unroll
+	for (int j = 0; j < int(TM_H / 4); ++j)
+	{
+		const uint32_t ly = ly0 + 4 * j;
+#pragma unroll
+		for (int k = 0; k < 4; ++k) p[j][k] = 0;
+		if (ly >= th) continue;
+		const uint64_t src = uint64_t(y0 + ly) * a.width + x0 + lx;
+		const unsigned long long* h = hdr + src;
+		if (n == 4 && (src & 1) == 0 && (reinterpret_cast<uintptr_t>(a.hdr) & 15) == 0)
+		{
+			const ulonglong2 v0 = __ldg(reinterpret_cast<const ulonglong2*>(h));
+			const ulonglong2 v1 = __ldg(reinterpret_cast<const ulonglong2*>(h + 2));
+			p[j][0] = v0.x;
+			p[j][1] = v0.y;
+			p[j][2] = v1.x;
+			p[j][3] = v1.y;
+		}
+		else
+		{
+#pragma unroll
+			for (int k = 0; k < 4; ++k)
+				if (k < int(n)) p[j][k] = __ldg(h + k);
+		}
+	}
+#pragma unroll
+	for (int j = 0; j < int(TM_H / 4); ++j)
+	{
+		const uint32_t ly = ly0 + 4 * j;
+		if (ly >= th) break;
+		const uint32_t x = x0 + lx, y = y0 + ly;
+		const uint64_t dst = uint64_t(y) * a.dst_pitch + x;
+		uint32_t o[4];
 #pragma unroll
 		for (int k = 0; k < 4; ++k)
-			if (k < int(n)) p[k] = __ldg(h + k);
-	}
-	uint32_t o[4];
+			o[k] = k < int(n) ? cv_to_c32(tonemap(bloom_sum<S, LINEAR>(a, tile, x + k, y, cv_from_c64(p[j][k])), a)) : 0u;
+		if (n == 4 && (dst & 3) == 0 && (reinterpret_cast<uintptr_t>(a.dst) & 15) == 0)
+			*reinterpret_cast<uint4*>(a.dst + dst) = make_uint4(o[0], o[1], o[2], o[3]);
+		else
+		{
 #pragma unroll
-	for (int k = 0; k < 4; ++k)
-		o[k] = k < int(n) ? cv_to_c32(tonemap(bloom_sum<S, LINEAR>(a, x + k, y, cv_from_c64(p[k])), a)) : 0u;
-	if (n == 4 && (dst & 3) == 0)
-		*reinterpret_cast<uint4*>(a.dst + dst) = make_uint4(o[0], o[1], o[2], o[3]);
-	else
-	{
-#pragma unroll
-		for (int k = 0; k < 4; ++k)
-			if (k < int(n)) a.dst[dst + k] = o[k];
+			for (int k = 0; k < 4; ++k)
+				if (k < int(n)) a.dst[dst + k] = o[k];
+		}
 	}
 }
 
@@ -377,30 +488,45 @@ __global__ void fill_kernel(void* dst, uint64_t count, uint64_t value, uint32_t 
 	}
 }
 
-template <int S>
-void launch_bloom_passes(const PostArgs& a, cudaStream_t stream, bool downscale)
+// Dynamic shared memory above the default 48 KB needs the kernel's opt-in (set once, before use).
+template <class K>
+int allow_smem(K kernel, uint32_t bytes)
 {
-	const dim3 block(256);
-	if (downscale)
-	{
-		pp_downscale_kernel<S><<<dim3((a.bw + 511) / 512, a.bh), block, 0, stream>>>(a);
-		return;
-	}
-	const dim3 grid((a.width + 1023) / 1024, a.height);
-	if (a.linear_filter)
-		pp_tonemap_bloom_kernel<S, true><<<grid, block, 0, stream>>>(a);
-	else
-		pp_tonemap_bloom_kernel<S, false><<<grid, block, 0, stream>>>(a);
+	if (bytes <= 48 * 1024) return 0;
+	if (bytes > 200 * 1024) return int(cudaErrorInvalidValue);
+	return int(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
 }
 
-void launch_bloom(const PostArgs& a, cudaStream_t stream, bool downscale)
+template <int S>
+int launch_fused_bloom(const PostArgs& a, cudaStream_t stream, bool first)
 {
-	if (a.scale == 2)
-		launch_bloom_passes<2>(a, stream, downscale);
-	else if (a.scale == 4)
-		launch_bloom_passes<4>(a, stream, downscale);
+	if (first)
+	{
+		const uint32_t smem = a.bw * 8;
+		if (int e = allow_smem(pp_downscale_blur_h_kernel<S>, smem)) return e;
+		pp_downscale_blur_h_kernel<S><<<a.bh, 256, smem, stream>>>(a);
+		return 0;
+	}
+	const uint32_t smem = tonemap_tile_smem<S>(a.radius);
+	const dim3 grid((a.width + TM_W - 1) / TM_W, (a.height + TM_H - 1) / TM_H);
+	if (a.linear_filter)
+	{
+		if (int e = allow_smem(pp_blur_v_tonemap_kernel<S, true>, smem)) return e;
+		pp_blur_v_tonemap_kernel<S, true><<<grid, 256, smem, stream>>>(a);
+	}
 	else
-		launch_bloom_passes<8>(a, stream, downscale);
+	{
+		if (int e = allow_smem(pp_blur_v_tonemap_kernel<S, false>, smem)) return e;
+		pp_blur_v_tonemap_kernel<S, false><<<grid, 256, smem, stream>>>(a);
+	}
+	return 0;
+}
+
+int launch_fused(const PostArgs& a, cudaStream_t stream, bool first)
+{
+	return a.scale == 2 ? launch_fused_bloom<2>(a, stream, first)
+		: a.scale == 4  ? launch_fused_bloom<4>(a, stream, first)
+						: launch_fused_bloom<8>(a, stream, first);
 }
 
 } // namespace
@@ -412,11 +538,12 @@ int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream, cuda
 	const dim3 block(256);
 	if (a.use_bloom)
 	{
-		cudaMemsetAsync(a.line_sums, 0, sizeof(int32_t) * 4 * a.bh, stream);
 		if (a.scale != 2 && a.scale != 4 && a.scale != 8) return int(cudaErrorInvalidValue);
-		launch_bloom(a, stream, true);
+		if (a.radius > 16 || a.bw == 0 || a.bh == 0) return int(cudaErrorInvalidValue);
+		// downscale + horizontal blur (writes every line's exact lane sums)
+		if (int e = launch_fused(a, stream, true)) return e;
 		// The exposure average is consumed only after the frame: with an auxiliary stream it runs
-		// beside the blur and tonemap passes.
+		// beside the vertical blur and tonemap pass.
 		const bool overlap = aux && fork && join;
 		if (overlap)
 		{
@@ -425,12 +552,8 @@ int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream, cuda
 		}
 		pp_average_bloom_kernel<<<1, 256, 0, overlap ? aux : stream>>>(a);
 		if (overlap) cudaEventRecord(join, aux);
-		if (a.radius > 0)
-		{
-			pp_blur_h_kernel<<<dim3((a.bw + 255) / 256, a.bh), block, 0, stream>>>(a);
-			pp_blur_v_kernel<<<dim3((a.bw + 255) / 256, a.bh), block, 0, stream>>>(a);
-		}
-		launch_bloom(a, stream, false);
+		// vertical blur + tonemap with the bloom sample
+		if (int e = launch_fused(a, stream, false)) return e;
 		if (overlap) cudaStreamWaitEvent(stream, join, 0);
 	}
 	else
