@@ -4,13 +4,13 @@
 // running Rasterizer::fill_polygon for each draw in submission order (src/square_wheel/rasterizer.rs:
 // 137-729, write_into_framebuffer :1511-1536).
 //
-// Three launches:
-//   raster_walk: one thread per draw runs the reference's edge walk (rasterizer.rs:160-270) into the
-//     draw's parts and derives its tile-binning box.
-//   raster_rows: one thread per (draw, row) record (row ranges and record offsets come from the host):
-//     the span [xs, xe) and the start and step of the mode's interpolants (the span setup of
-//     rasterizer.rs:329-422 / 513-556 / 686-703), evaluated once per (draw, row) over the whole span
-//     with the frame as clip rectangle (the reference's num_threads == 1 ClipRect).
+// Two launches:
+//   raster_setup: one CTA per draw. Thread 0 runs the reference's edge walk (rasterizer.rs:160-270)
+//     into the draw's parts and derives its tile-binning box; then the CTA's threads take the draw's
+//     (row) records (row ranges and record offsets come from the host): the span [xs, xe) and the
+//     start and step of the mode's interpolants (the span setup of rasterizer.rs:329-422 / 513-556 /
+//     686-703), evaluated once per (draw, row) over the whole span with the frame as clip rectangle
+//     (the reference's num_threads == 1 ClipRect).
 //   raster_tiles: one 256-thread CTA per 64x16 tile, each thread a 1x4 pixel strip of one row (about
 //     one wave of CTAs at 1080p). The CTA streams over the draws in submission order, 256 at a time;
 //     each thread tests one draw's box against the tile and a ballot + prefix sum compacts the hits
@@ -294,80 +294,83 @@ __device__ RasterRow row_setup(const SwDrawCmd& d, const DrawEq& e, const Raster
 	return r;
 }
 
-// Edge walk per draw (one thread per draw): the draw's parts, its tile-binning box (conservative: x
-// is linear in the row, so its extremes over a part are at the part's first and last rows) and the
-// per-draw record of the tile kernel.
-__global__ void __launch_bounds__(128) raster_walk_kernel(RasterArgs a)
+// Raster setup of one draw per CTA. The draw and its vertices are staged in shared memory; thread 0
+// runs the edge walk into shared memory (its loop reads vertices on the walk's dependency chain, which
+// from shared memory costs a few cycles per step) and writes the draw's tile-binning box (conservative:
+// x is linear in the row, so its extremes over a part are at the part's first and last rows) and the
+// per-draw record of the tile kernel; then every thread sets up rows of the draw (its row records,
+// numbered by the host in draw order) from those parts.
+__global__ void __launch_bounds__(256) raster_setup_kernel(RasterArgs a)
 {
-	const uint32_t di = blockIdx.x * blockDim.x + threadIdx.x;
-	if (di >= a.num_draws) return;
-	const SwDrawCmd d = a.draws[di];
-	RasterPart* parts = a.parts + uint64_t(di) * SW_RASTER_MAX_PARTS;
-	const uint32_t np = edge_walk(d, a.vertices + d.first_vertex, a.height, parts);
-	a.part_counts[di] = np;
-	int32_t bx0 = INT32_MAX, bx1 = INT32_MIN, by0 = INT32_MAX, by1 = INT32_MIN;
-	for (uint32_t pi = 0; pi < np; ++pi)
+	__shared__ __align__(8) SwDrawCmd s_d;
+	__shared__ SwVertex16 s_v[SW_MAX_POLYGON_VERTICES];
+	__shared__ RasterPart s_parts[SW_RASTER_MAX_PARTS];
+	__shared__ DrawRows s_dr;
+	__shared__ uint32_t s_np;
+	const uint32_t di = blockIdx.x;
+	static_assert(sizeof(SwDrawCmd) % 4 == 0 && sizeof(SwDrawCmd) / 4 <= 256, "draw record");
+	if (threadIdx.x < sizeof(SwDrawCmd) / 4)
+		reinterpret_cast<uint32_t*>(&s_d)[threadIdx.x] = reinterpret_cast<const uint32_t*>(a.draws + di)[threadIdx.x];
+	if (threadIdx.x == 0) s_dr = a.draw_rows[di];
+	__syncthreads();
+	if (threadIdx.x < s_d.vertex_count && threadIdx.x < SW_MAX_POLYGON_VERTICES)
+		s_v[threadIdx.x] = a.vertices[s_d.first_vertex + threadIdx.x];
+	__syncthreads();
+	if (threadIdx.x == 0)
 	{
-		const RasterPart& p = parts[pi];
-		const int32_t last = p.y_end_int - 1 - p.y_start_int;
-		bx0 = min(bx0, min(p.x_left0 >> 16, wadd(p.x_left0, wmul(last, p.dx_dy_left)) >> 16));
-		bx1 = max(bx1, max(p.x_right0 >> 16, wadd(p.x_right0, wmul(last, p.dx_dy_right)) >> 16));
-		by0 = min(by0, p.y_start_int);
-		by1 = max(by1, p.y_end_int);
-	}
-	bx0 = max(bx0, 0);
-	bx1 = min(bx1, a.width);
-	const DrawRows dr = a.draw_rows[di];
-	// Rows outside the host's row range have no record; clamp the box to it.
-	by0 = max(by0, dr.y0);
-	by1 = min(by1, dr.y0 + int32_t(dr.nrows));
-	a.boxes[di] = (np > 0 && bx0 < bx1 && by0 < by1) ? RasterBox{int16_t(bx0), int16_t(by0), int16_t(bx1), int16_t(by1)}
-														: RasterBox{0, 0, 0, 0};
-	RasterDraw rd;
-	rd.tex_offset = d.tex_offset;
-	rd.tex_w = d.tex_size[0];
-	rd.tex_h = d.tex_size[1];
-	rd.row_base = dr.row_base;
-	rd.y0 = dr.y0;
-	rd.mode = d.mode;
-	rd.blend = uint16_t(d.blend);
-	rd.tex_source = uint16_t(d.tex_source);
-	a.rdraws[di] = rd;
-}
-
-// Span setup of every covered row of every draw (one thread per row record).
-__global__ void __launch_bounds__(128) raster_rows_kernel(RasterArgs a)
-{
-	const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= a.total_rows) return;
-	// Draw owning row record t: the last draw whose row_base <= t.
-	uint32_t lo = 0, hi = a.num_draws;
-	while (hi - lo > 1)
-	{
-		const uint32_t mid = (lo + hi) >> 1;
-		if (a.draw_rows[mid].row_base <= t)
-			lo = mid;
-		else
-			hi = mid;
-	}
-	const DrawRows dr = a.draw_rows[lo];
-	const int32_t y = dr.y0 + int32_t(t - dr.row_base);
-	const SwDrawCmd d = a.draws[lo];
-	const RasterPart* parts = a.parts + uint64_t(lo) * SW_RASTER_MAX_PARTS;
-	const uint32_t np = a.part_counts[lo];
-	RasterRow row;
-	row.xs = row.xe = 0;
-	row.a0 = row.b0 = row.a1 = row.b1 = row.a2 = row.b2 = 0;
-	for (uint32_t pi = 0; pi < np; ++pi)
-	{
-		const RasterPart p = parts[pi];
-		if (y >= p.y_start_int && y < p.y_end_int)
+		const SwDrawCmd& d = s_d;
+		const uint32_t np = edge_walk(d, s_v, a.height, s_parts);
+		s_np = np;
+		int32_t bx0 = INT32_MAX, bx1 = INT32_MIN, by0 = INT32_MAX, by1 = INT32_MIN;
+		for (uint32_t pi = 0; pi < np; ++pi)
 		{
-			row = row_setup(d, draw_equations(d), p, y, a.width);
-			break;
+			const RasterPart& p = s_parts[pi];
+			const int32_t last = p.y_end_int - 1 - p.y_start_int;
+			bx0 = min(bx0, min(p.x_left0 >> 16, wadd(p.x_left0, wmul(last, p.dx_dy_left)) >> 16));
+			bx1 = max(bx1, max(p.x_right0 >> 16, wadd(p.x_right0, wmul(last, p.dx_dy_right)) >> 16));
+			by0 = min(by0, p.y_start_int);
+			by1 = max(by1, p.y_end_int);
 		}
+		bx0 = max(bx0, 0);
+		bx1 = min(bx1, a.width);
+		const DrawRows dr = s_dr;
+		// Rows outside the host's row range have no record; clamp the box to it.
+		by0 = max(by0, dr.y0);
+		by1 = min(by1, dr.y0 + int32_t(dr.nrows));
+		a.boxes[di] = (np > 0 && bx0 < bx1 && by0 < by1) ? RasterBox{int16_t(bx0), int16_t(by0), int16_t(bx1), int16_t(by1)}
+															: RasterBox{0, 0, 0, 0};
+		RasterDraw rd;
+		rd.tex_offset = d.tex_offset;
+		rd.tex_w = d.tex_size[0];
+		rd.tex_h = d.tex_size[1];
+		rd.row_base = dr.row_base;
+		rd.y0 = dr.y0;
+		rd.mode = d.mode;
+		rd.blend = uint16_t(d.blend);
+		rd.tex_source = uint16_t(d.tex_source);
+		a.rdraws[di] = rd;
 	}
-	a.rows[t] = row;
+	__syncthreads();
+	const uint32_t np = s_np;
+	const DrawEq e = draw_equations(s_d);
+	const DrawRows dr = s_dr;
+	for (uint32_t k = threadIdx.x; k < dr.nrows; k += blockDim.x)
+	{
+		const int32_t y = dr.y0 + int32_t(k);
+		RasterRow row;
+		row.xs = row.xe = 0;
+		row.a0 = row.b0 = row.a1 = row.b1 = row.a2 = row.b2 = 0;
+		for (uint32_t pi = 0; pi < np; ++pi)
+		{
+			const RasterPart& p = s_parts[pi];
+			if (y >= p.y_start_int && y < p.y_end_int)
+			{
+				row = row_setup(s_d, e, p, y, a.width);
+				break;
+			}
+		}
+		a.rows[dr.row_base + k] = row;
+	}
 }
 
 template <class P>
@@ -562,8 +565,7 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 
 int launch_raster_setup(const RasterArgs& args, cudaStream_t stream)
 {
-	if (args.num_draws > 0) raster_walk_kernel<<<(args.num_draws + 127) / 128, 128, 0, stream>>>(args);
-	if (args.total_rows > 0) raster_rows_kernel<<<(args.total_rows + 127) / 128, 128, 0, stream>>>(args);
+	if (args.num_draws > 0) raster_setup_kernel<<<args.num_draws, 256, 0, stream>>>(args);
 	return int(cudaGetLastError());
 }
 

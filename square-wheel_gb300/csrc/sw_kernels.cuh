@@ -142,7 +142,7 @@ struct RasterArgs
 	unsigned int* error_counter;
 };
 
-// Edge walk + row setup (raster_walk, raster_rows), then the tile pass (raster_tiles).
+// Edge walk + row setup (raster_setup, one CTA per draw), then the tile pass (raster_tiles).
 int launch_raster_setup(const RasterArgs& args, cudaStream_t stream);
 // variant: tile shape index (< SW_RASTER_TILE_VARIANTS, see SwTuning); every variant gives the same frame.
 int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, uint32_t variant, cudaStream_t stream);
