@@ -60,6 +60,7 @@ struct SwCtx
 	// static
 	DevBuf texels, texture_mips, emissive, emissive_mips, lightmaps, dir_lightmaps;
 	DevBuf skybox32, skybox64; // sw_set_skybox: the same texels in Color32 and Color64
+	DevBuf frame_in;           // sw_draw_frame: all per-frame arrays of one frame, uploaded by one copy
 	uint64_t skybox_texels = 0;
 	std::vector<SwTextureMip> h_texture_mips;
 	std::vector<SwEmissiveMip> h_emissive_mips;
@@ -429,7 +430,7 @@ int sw_destroy(SwCtx* ctx)
 	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
 	if (ctx->aux) cudaStreamSynchronize(ctx->aux);
 	DevBuf* bufs[] = {&ctx->texels, &ctx->texture_mips, &ctx->emissive, &ctx->emissive_mips, &ctx->lightmaps, &ctx->skybox32,
-		&ctx->skybox64,
+		&ctx->skybox64, &ctx->frame_in,
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->parts, &ctx->part_counts, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst};
@@ -525,11 +526,19 @@ int sw_frame_begin(SwCtx* ctx, const SwFrameParams* params, const SwLight* light
 	return SW_OK;
 }
 
-static int launch_surfaces(SwCtx* ctx)
+// Surface build of the last submitted surfaces; `in` (optional) holds the lights, surface records and
+// prefix sums instead of the context's own buffers.
+struct SurfaceInputs
+{
+	const SwLight* lights;
+	const SurfaceGpu* surfaces;
+	const uint64_t* work_prefix;
+};
+static int launch_surfaces(SwCtx* ctx, const SurfaceInputs* in = nullptr)
 {
 	SurfaceKernelArgs a;
-	a.surfaces = static_cast<const SurfaceGpu*>(ctx->surfaces.ptr);
-	a.work_prefix = static_cast<const uint64_t*>(ctx->work_prefix.ptr);
+	a.surfaces = in ? in->surfaces : static_cast<const SurfaceGpu*>(ctx->surfaces.ptr);
+	a.work_prefix = in ? in->work_prefix : static_cast<const uint64_t*>(ctx->work_prefix.ptr);
 	a.num_surfaces = ctx->last_num_surfaces;
 	a.directional = ctx->last_surface_directional ? 1u : 0u;
 	a.total_work = ctx->last_surface_work;
@@ -537,7 +546,7 @@ static int launch_surfaces(SwCtx* ctx)
 	a.emissive_pixels = static_cast<const uint32_t*>(ctx->emissive.ptr);
 	a.lightmaps = static_cast<const float*>(ctx->lightmaps.ptr);
 	a.directional_lightmaps = static_cast<const SwDirectionalLightmapElement*>(ctx->dir_lightmaps.ptr);
-	a.lights = static_cast<const SwLight*>(ctx->lights.ptr);
+	a.lights = in ? in->lights : static_cast<const SwLight*>(ctx->lights.ptr);
 	for (int i = 0; i < 3; ++i) a.cam_pos[i] = ctx->frame.cam_pos[i];
 	a.arena = ctx->arena.ptr;
 	stage_begin(ctx, STAGE_SURFACES);
@@ -1032,20 +1041,22 @@ int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, con
 	const PostArgs* post)
 {
 	cudaStream_t s = ctx->stream, aux = ctx->aux;
-	SW_CUDA(ctx, cudaMemcpyAsync(ctx->lights.ptr, h + off[0], f.num_lights * sizeof(SwLight), cudaMemcpyHostToDevice, s));
-	SW_CUDA(ctx, cudaMemcpyAsync(ctx->surfaces.ptr, h + off[1], f.num_surfaces * sizeof(SurfaceGpu), cudaMemcpyHostToDevice, s));
-	SW_CUDA(ctx, cudaMemcpyAsync(ctx->work_prefix.ptr, h + off[2], (size_t(f.num_surfaces) + 1) * 8, cudaMemcpyHostToDevice, s));
-	// draw uploads and raster setup on the auxiliary stream, beside the surface build
+	// every per-frame array in one copy: the device buffer has the staging block's layout
+	unsigned char* d = static_cast<unsigned char*>(ctx->frame_in.ptr);
+	SW_CUDA(ctx, cudaMemcpyAsync(d, h, off[6], cudaMemcpyHostToDevice, s));
+	// raster setup on the auxiliary stream, beside the surface build
 	SW_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
 	SW_CUDA(ctx, cudaStreamWaitEvent(aux, ctx->ev_fork, 0));
-	SW_CUDA(ctx, cudaMemcpyAsync(ctx->draws.ptr, h + off[3], f.num_draws * sizeof(SwDrawCmd), cudaMemcpyHostToDevice, aux));
-	SW_CUDA(ctx, cudaMemcpyAsync(ctx->vertices.ptr, h + off[4], f.num_vertices * sizeof(SwVertex16), cudaMemcpyHostToDevice, aux));
-	SW_CUDA(ctx, cudaMemcpyAsync(ctx->draw_rows.ptr, h + off[5], f.num_draws * sizeof(DrawRows), cudaMemcpyHostToDevice, aux));
 	int r;
-	const RasterArgs ra = raster_args(ctx);
+	RasterArgs ra = raster_args(ctx);
+	ra.draws = reinterpret_cast<const SwDrawCmd*>(d + off[3]);
+	ra.vertices = reinterpret_cast<const SwVertex16*>(d + off[4]);
+	ra.draw_rows = reinterpret_cast<const DrawRows*>(d + off[5]);
 	if ((r = check_kernel(ctx, launch_raster_setup(ra, aux), "raster setup"))) return r;
 	SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, aux));
-	if ((r = launch_surfaces(ctx))) return r;
+	const SurfaceInputs si{reinterpret_cast<const SwLight*>(d + off[0]), reinterpret_cast<const SurfaceGpu*>(d + off[1]),
+		reinterpret_cast<const uint64_t*>(d + off[2])};
+	if ((r = launch_surfaces(ctx, &si))) return r;
 	SW_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_setup, 0));
 	if ((r = check_kernel(ctx, launch_raster_tiles(ra, f.params.pixel_format, ctx->tuning.raster_tile, s), "raster"))) return r;
 	(void)rows;
@@ -1117,6 +1128,7 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 
 	// 2. device buffers (growing them synchronises; the next capture picks up the new addresses)
 	const uint32_t bpp = bpp_of(p.pixel_format);
+	if ((r = ensure(ctx, ctx->frame_in, off[6]))) return r;
 	if ((r = ensure(ctx, ctx->lights, std::max<size_t>(f.num_lights, 1) * sizeof(SwLight)))) return r;
 	if ((r = ensure(ctx, ctx->arena, std::max<uint64_t>(f.total_texels, 1) * bpp))) return r;
 	if ((r = ensure(ctx, ctx->surfaces, std::max<size_t>(f.num_surfaces, 1) * sizeof(SurfaceGpu)))) return r;
