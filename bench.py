@@ -305,28 +305,27 @@ def run_frame_gpu(args, world, rank, local):
         frame_ms = float(tt.item())
     value = world * 1e3 / frame_ms
 
-    # e2e: the C++ renderer drives the C ABI from host memory; postprocess reads the LDR frame back.
+    # e2e: the C++ host renderer (host work: visibility, surface and draw setup) drives the C ABI per
+    # frame (swh_renderer_render_frame: one graph with uploads from host memory, surfaces, raster and
+    # postprocess) and the Color32 frame is copied back into a host buffer the caller registered once.
     from sqwheel import host
     e2e_ms = []
     h2d = d2h = 0
     hr = host.HostRenderer(work.scene, device=local)
-    glib = gpu.load_library()
-    out = np.zeros((H, W), np.uint32)
     import ctypes
-    mod = (ctypes.c_float * 3)(1.0, 1.0, 1.0)
+    gpu.load_library().sw_set_tuning(hr.context(), ctypes.byref(tune))
+    out = np.zeros((H, W), np.uint32)
+    hr.register_host_buffer(out)
     for i, f in enumerate(work.frames[: max(3, min(args.steps, 12))]):
         t0 = time.perf_counter()
-        hr.prepare_frame(f["index"], work.opts)
-        hr.draw_frame()
-        rc = glib.sw_postprocess(hr.context(), ctypes.byref(work.config), 1.0 / 60.0, mod, abi.ptr(out), W, 0)
-        if rc != 0:
-            raise RuntimeError(f"sw_postprocess failed: {rc}")
+        hr.render_frame(f["index"], work.opts, out=out, post=work.config)
         if i > 0:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
         h2d += (f["surfaces"].nbytes + f["draws"].nbytes + f["vertices"].nbytes + f["lights"].nbytes
                 + (f["surfaces"].size + 1) * 8)
         d2h += out.nbytes
         n_e2e = i + 1
+    hr.unregister_host_buffer(out)
     hr.close()
     e2e_val = 1e3 / statistics.median(e2e_ms)
 

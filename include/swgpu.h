@@ -253,6 +253,13 @@ int sw_set_surfaces(SwCtx* ctx, const void* texels, uint64_t total_texels);
  * Synchronous upload; NULL / 0 texels removes the skybox. Load-time data like sw_create's. */
 int sw_set_skybox(SwCtx* ctx, const uint32_t* texels32, const uint64_t* texels64, uint64_t num_texels);
 
+/* Page-lock a host buffer the caller reuses for its frames (the window surface's pixels, say) with
+ * cudaHostRegister, so that frames written to host memory inside it go straight from the device into
+ * it instead of through the library's pinned staging buffer and a host copy. Unregister it (or
+ * destroy the context) before freeing the memory; registered buffers must not overlap. */
+int sw_register_host_buffer(SwCtx* ctx, void* ptr, uint64_t bytes);
+int sw_unregister_host_buffer(SwCtx* ctx, void* ptr);
+
 /* Draw commands in exact submission order (draw_skybox, then draw_tree/draw_leaf/draw_polygon,
  * partial_renderer.rs:1285-1325, 2311-2559, 4011-4142). */
 int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices,

@@ -103,6 +103,12 @@ int swh_renderer_destroy(SwhRenderer* renderer);
 int swh_renderer_prepare_frame(SwhRenderer* renderer, uint32_t frame_index, const SwhFrameOptions* options);
 /* Renderer::draw_frame: sw_submit_draws + sw_render into dst (optional). */
 int swh_renderer_draw_frame(SwhRenderer* renderer, void* dst, uint32_t pitch, int dst_is_device);
+/* One whole frame as the host's frame loop runs it (host.rs:400-416: prepare_frame, draw_frame and,
+ * when `post` is not NULL, perform_postprocessing): host work, then sw_draw_frame (one CUDA graph:
+ * uploads, surfaces, raster, postprocess) with the Color32 result (post) or the frame (no post) in dst. */
+int swh_renderer_render_frame(SwhRenderer* renderer, uint32_t frame_index, const SwhFrameOptions* options,
+	const SwPostConfig* post, float frame_duration_s, const float color_modulate[3], void* dst, uint32_t pitch,
+	int dst_is_device);
 /* The GPU context and the frame used by the renderer. */
 SwCtx* swh_renderer_context(SwhRenderer* renderer);
 SwhFrame* swh_renderer_frame(SwhRenderer* renderer);

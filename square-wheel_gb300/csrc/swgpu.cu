@@ -61,6 +61,12 @@ struct SwCtx
 	DevBuf texels, texture_mips, emissive, emissive_mips, lightmaps, dir_lightmaps;
 	DevBuf skybox32, skybox64; // sw_set_skybox: the same texels in Color32 and Color64
 	DevBuf frame_in;           // sw_draw_frame: all per-frame arrays of one frame, uploaded by one copy
+	struct HostRange
+	{
+		char* ptr;
+		size_t bytes;
+	};
+	std::vector<HostRange> registered; // sw_register_host_buffer
 	uint64_t skybox_texels = 0;
 	std::vector<SwTextureMip> h_texture_mips;
 	std::vector<SwEmissiveMip> h_emissive_mips;
@@ -291,8 +297,18 @@ int copy_out(SwCtx* ctx, void* dst, uint32_t dst_pitch, int dst_is_device, const
 						 cudaMemcpyDeviceToDevice, ctx->stream));
 		return SW_OK;
 	}
-	Staging& st = ctx->stage_io;
 	const size_t bytes = row * height;
+	const size_t span = size_t(height - 1) * dst_pitch * bpp + row;
+	for (const SwCtx::HostRange& hr : ctx->registered)
+		if (static_cast<char*>(dst) >= hr.ptr && static_cast<char*>(dst) + span <= hr.ptr + hr.bytes)
+		{
+			// page-locked by sw_register_host_buffer: straight from the device into the caller's rows
+			SW_CUDA(ctx, cudaMemcpy2DAsync(dst, size_t(dst_pitch) * bpp, src, size_t(src_pitch) * bpp, row, height,
+							 cudaMemcpyDeviceToHost, ctx->stream));
+			SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+			return SW_OK;
+		}
+	Staging& st = ctx->stage_io;
 	if (st.pending)
 	{
 		SW_CUDA(ctx, cudaEventSynchronize(st.done));
@@ -435,6 +451,7 @@ int sw_destroy(SwCtx* ctx)
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->parts, &ctx->part_counts, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst};
 	for (DevBuf* b : bufs) release(*b);
+	for (const SwCtx::HostRange& h : ctx->registered) cudaHostUnregister(h.ptr);
 	if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
 	Staging* st[] = {&ctx->stage_lights, &ctx->stage_surfaces, &ctx->stage_prefix, &ctx->stage_draws,
 		&ctx->stage_vertices, &ctx->stage_draw_rows, &ctx->stage_io, &ctx->gstage[0], &ctx->gstage[1]};
@@ -673,6 +690,34 @@ int sw_set_skybox(SwCtx* ctx, const uint32_t* texels32, const uint64_t* texels64
 	if ((r = upload_static(ctx, ctx->skybox64, texels64, size_t(num_texels) * 8))) return r;
 	ctx->skybox_texels = num_texels;
 	return SW_OK;
+}
+
+int sw_register_host_buffer(SwCtx* ctx, void* ptr, uint64_t bytes)
+{
+	if (!ctx || !ptr || bytes == 0) return SW_ERR_INVALID_ARGUMENT;
+	char* p = static_cast<char*>(ptr);
+	for (const SwCtx::HostRange& h : ctx->registered)
+		if (p < h.ptr + h.bytes && h.ptr < p + bytes) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "buffer overlaps a registered one");
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	SW_CUDA(ctx, cudaHostRegister(ptr, size_t(bytes), cudaHostRegisterDefault));
+	ctx->registered.push_back(SwCtx::HostRange{p, size_t(bytes)});
+	return SW_OK;
+}
+
+int sw_unregister_host_buffer(SwCtx* ctx, void* ptr)
+{
+	if (!ctx || !ptr) return SW_ERR_INVALID_ARGUMENT;
+	for (size_t i = 0; i < ctx->registered.size(); ++i)
+		if (ctx->registered[i].ptr == ptr)
+		{
+			SW_CUDA(ctx, cudaSetDevice(ctx->device));
+			// copies into it may still be in flight
+			SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+			SW_CUDA(ctx, cudaHostUnregister(ptr));
+			ctx->registered.erase(ctx->registered.begin() + long(i));
+			return SW_OK;
+		}
+	return fail(ctx, SW_ERR_INVALID_ARGUMENT, "buffer not registered");
 }
 
 int sw_set_surfaces(SwCtx* ctx, const void* texels, uint64_t total_texels)

@@ -1,6 +1,7 @@
 // C ABI of the host library (include/swhost.h).
 #include "../../include/swhost.h"
 
+#include <cstring>
 #include <new>
 #include <string>
 
@@ -258,6 +259,38 @@ int swh_renderer_draw_frame(SwhRenderer* r, void* dst, uint32_t pitch, int dst_i
 	int st = sw_submit_draws(r->ctx, p.draws.data(), uint32_t(p.draws.size()), p.vertices.data(), uint32_t(p.vertices.size()));
 	if (st) return st;
 	return sw_render(r->ctx, dst, pitch, dst_is_device);
+}
+
+int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFrameOptions* o, const SwPostConfig* post,
+	float frame_duration_s, const float color_modulate[3], void* dst, uint32_t pitch, int dst_is_device)
+{
+	if (!r || (post && (!dst || !color_modulate))) return SW_ERR_INVALID_ARGUMENT;
+	int st = swh_frame_prepare(r->frame, frame_index, o);
+	if (st) return st;
+	const FramePrep& p = r->frame->prep;
+	SwFrameInput in;
+	std::memset(&in, 0, sizeof(in));
+	in.params = p.params;
+	in.num_lights = uint32_t(p.lights.size());
+	in.lights = p.lights.data();
+	in.surfaces = p.surfaces.data();
+	in.total_texels = p.total_texels;
+	in.num_surfaces = uint32_t(p.surfaces.size());
+	in.num_draws = uint32_t(p.draws.size());
+	in.draws = p.draws.data();
+	in.vertices = p.vertices.data();
+	in.num_vertices = uint32_t(p.vertices.size());
+	if (post)
+	{
+		in.postprocess = 1;
+		in.post = *post;
+		in.frame_duration_s = frame_duration_s;
+		for (int i = 0; i < 3; ++i) in.color_modulate[i] = color_modulate[i];
+	}
+	in.dst = dst;
+	in.dst_pitch = pitch;
+	in.dst_is_device = dst_is_device;
+	return sw_draw_frame(r->ctx, &in);
 }
 
 SwCtx* swh_renderer_context(SwhRenderer* r) { return r ? r->ctx : nullptr; }

@@ -19,7 +19,7 @@ PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_DIR, "lib", "libswgpu.so")
 
 EXPORTED = [
-    "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_set_surfaces", "sw_set_skybox",
+    "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_set_surfaces", "sw_set_skybox", "sw_register_host_buffer", "sw_unregister_host_buffer",
     "sw_submit_draws",
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
@@ -58,6 +58,8 @@ def load_library(path=LIB_PATH):
         "sw_rebuild_surfaces": ([vp], i32),
         "sw_set_surfaces": ([vp, vp, u64], i32),
         "sw_set_skybox": ([vp, vp, vp, u64], i32),
+        "sw_register_host_buffer": ([vp, vp, u64], i32),
+        "sw_unregister_host_buffer": ([vp, vp], i32),
         "sw_submit_draws": ([vp, vp, u32, vp, u32], i32),
         "sw_render": ([vp, vp, u32, i32], i32),
         "sw_postprocess": ([vp, vp, f32, vp, vp, u32, i32], i32),

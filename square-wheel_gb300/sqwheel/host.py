@@ -68,6 +68,7 @@ def load_host_library():
         "swh_renderer_draw_frame": ([vp, vp, u32, i32], i32), "swh_renderer_context": ([vp], vp),
         "swh_renderer_frame": ([vp], vp),
         "swh_scene_skybox": ([vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_uint64), vp, vp], i32),
+        "swh_renderer_render_frame": ([vp, u32, vp, vp, ctypes.c_float, vp, vp, u32, i32], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -80,7 +81,8 @@ def load_host_library():
 HOST_EXPORTED = ["swh_scene_create", "swh_scene_destroy", "swh_scene_info", "swh_scene_create_info", "swh_last_error",
                  "swh_frame_create", "swh_frame_destroy", "swh_frame_prepare", "swh_frame_outputs",
                  "swh_renderer_create", "swh_renderer_destroy", "swh_renderer_prepare_frame",
-                 "swh_renderer_draw_frame", "swh_renderer_context", "swh_renderer_frame", "swh_scene_skybox"]
+                 "swh_renderer_draw_frame", "swh_renderer_context", "swh_renderer_frame", "swh_scene_skybox",
+                 "swh_renderer_render_frame"]
 
 # The two map configurations of the benchmark plan.
 SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, num_materials=16, metal_frac=0.0,
@@ -242,6 +244,28 @@ class HostRenderer:
             self._err(self.lib.swh_renderer_draw_frame(self.handle, ctypes.c_void_p(device_ptr), pitch, 1), "draw_frame")
         else:
             self._err(self.lib.swh_renderer_draw_frame(self.handle, None, 0, 0), "draw_frame")
+
+    def render_frame(self, frame_index, options, out=None, device_ptr=None, pitch=None, post=None,
+                     frame_duration_s=1.0 / 60.0, color_modulate=(1.0, 1.0, 1.0)):
+        """Host work + the whole frame as one graph (sw_draw_frame); with `post` (an abi.PostConfig) the
+        Color32 result, else the frame, lands in `out` (host) or at device_ptr."""
+        mod = (ctypes.c_float * 3)(*[float(c) for c in color_modulate])
+        post_p = ctypes.byref(post) if post is not None else None
+        if out is not None:
+            dst, pitch, dev = abi.ptr(out), pitch or out.shape[1], 0
+        elif device_ptr is not None:
+            dst, dev = ctypes.c_void_p(device_ptr), 1
+        else:
+            dst, pitch, dev = None, 0, 0
+        self._err(self.lib.swh_renderer_render_frame(self.handle, frame_index, ctypes.byref(options), post_p,
+                                                     frame_duration_s, mod, dst, pitch or 0, dev), "render_frame")
+
+    def register_host_buffer(self, arr):
+        """Page-lock `arr` (reused for frames) so frames are copied straight into it."""
+        self._err(load_library().sw_register_host_buffer(self.context(), abi.ptr(arr), arr.nbytes), "register")
+
+    def unregister_host_buffer(self, arr):
+        self._err(load_library().sw_unregister_host_buffer(self.context(), abi.ptr(arr)), "unregister")
 
     def context(self):
         return self.lib.swh_renderer_context(self.handle)

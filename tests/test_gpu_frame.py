@@ -114,6 +114,34 @@ def test_host_renderer_sky_map(gpu_ok):
     assert np.array_equal(want, got)
 
 
+def test_host_renderer_render_frame_graph(gpu_ok):
+    """swh_renderer_render_frame: host work + the whole frame as one graph with postprocess, the result
+    copied straight into a registered host buffer; equal to the oracle's frame and tonemap."""
+    scene = host.Scene(**host.SMALL_MAP)
+    hr = host.HostRenderer(scene)
+    cfg = abi.PostConfig.default()
+    opts = host.frame_options(320, 240, abi.SW_PIXEL_C64, directional=False)
+    out = np.zeros((240, 320), np.uint32)
+    try:
+        hr.register_host_buffer(out)
+        with pytest.raises(gpu.SwError):
+            hr.register_host_buffer(out[10:20])  # overlaps a registered buffer
+        hr.render_frame(12, opts, out=out, post=cfg)
+        got_registered = out.copy()
+        hr.unregister_host_buffer(out)
+        with pytest.raises(gpu.SwError):
+            hr.unregister_host_buffer(out)
+    finally:
+        hr.close()
+    st = scene.static_data()
+    fr = host.Frame(scene).prepare(12, opts)
+    arena = oracle.build_surfaces(st, fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=4)
+    hdr = np.zeros((240, 320), np.uint64)
+    oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, hdr)
+    want, _, _ = oracle.postprocess(cfg, hdr, 1.0 / 60.0, (1.0, 1.0, 1.0), 1.0)
+    assert np.array_equal(want, got_registered)
+
+
 def test_host_renderer_matches_python_driven_path(gpu_ok):
     """swh_renderer_* (C++ host driving the C ABI) renders the same frame as the step-by-step path."""
     scene = host.Scene(**host.SMALL_MAP)
