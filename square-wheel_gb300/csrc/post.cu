@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256) pp_downscale_blur_h_kernel(PostArgs a)
 // lines its tile needs (the bloom cells its pixels sample, +-radius lines) in shared memory, runs the
 // vertical blur pass (:902-955, bloom_scale folded into the weights) for those cells, then tonemaps its
 // pixels with the nearest or linear bloom sample (:346-726) read from shared memory.
-constexpr uint32_t TM_W = 256, TM_H = 8;
+constexpr uint32_t TM_W = 256, TM_H = 16;
 
 template <int S>
 __host__ __device__ __forceinline__ void bloom_tile_range(uint32_t p0, uint32_t n, uint32_t cells, uint32_t& lo, uint32_t& hi)
@@ -273,7 +273,7 @@ __host__ __device__ __forceinline__ uint32_t tonemap_tile_smem(uint32_t radius)
 }
 
 template <int S, bool LINEAR>
-__global__ void __launch_bounds__(256, 5) pp_blur_v_tonemap_kernel(PostArgs a)
+__global__ void __launch_bounds__(256) pp_blur_v_tonemap_kernel(PostArgs a)
 {
 	extern __shared__ __align__(16) uint64_t s_tile[];
 	const uint32_t x0 = blockIdx.x * TM_W, y0 = blockIdx.y * TM_H;
