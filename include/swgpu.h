@@ -254,9 +254,10 @@ int sw_set_surfaces(SwCtx* ctx, const void* texels, uint64_t total_texels);
 int sw_set_skybox(SwCtx* ctx, const uint32_t* texels32, const uint64_t* texels64, uint64_t num_texels);
 
 /* Page-lock a host buffer the caller reuses for its frames (the window surface's pixels, say) with
- * cudaHostRegister, so that frames written to host memory inside it go straight from the device into
- * it instead of through the library's pinned staging buffer and a host copy. Unregister it (or
- * destroy the context) before freeing the memory; registered buffers must not overlap. */
+ * cudaHostRegister (mapped), so that frames written to host memory inside it go straight from the
+ * device into it instead of through the library's pinned staging buffer and a host copy (sw_draw_frame's
+ * tonemap writes its rows there directly). Unregister it (or destroy the context) before freeing the
+ * memory; registered buffers must not overlap. */
 int sw_register_host_buffer(SwCtx* ctx, void* ptr, uint64_t bytes);
 int sw_unregister_host_buffer(SwCtx* ctx, void* ptr);
 

@@ -328,6 +328,24 @@ int copy_out(SwCtx* ctx, void* dst, uint32_t dst_pitch, int dst_is_device, const
 	return SW_OK;
 }
 
+// Device address of host memory [ptr, ptr + bytes) inside a buffer registered with
+// sw_register_host_buffer (registered memory is mapped), or nullptr.
+void* registered_device_pointer(SwCtx* ctx, void* ptr, size_t bytes)
+{
+	for (const SwCtx::HostRange& hr : ctx->registered)
+		if (static_cast<char*>(ptr) >= hr.ptr && static_cast<char*>(ptr) + bytes <= hr.ptr + hr.bytes)
+		{
+			void* d = nullptr;
+			if (cudaHostGetDevicePointer(&d, ptr, 0) != cudaSuccess)
+			{
+				cudaGetLastError();
+				return nullptr;
+			}
+			return d;
+		}
+	return nullptr;
+}
+
 int check_kernel(SwCtx* ctx, int launch_result, const char* what)
 {
 	if (launch_result != 0)
@@ -699,7 +717,7 @@ int sw_register_host_buffer(SwCtx* ctx, void* ptr, uint64_t bytes)
 	for (const SwCtx::HostRange& h : ctx->registered)
 		if (p < h.ptr + h.bytes && h.ptr < p + bytes) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "buffer overlaps a registered one");
 	SW_CUDA(ctx, cudaSetDevice(ctx->device));
-	SW_CUDA(ctx, cudaHostRegister(ptr, size_t(bytes), cudaHostRegisterDefault));
+	SW_CUDA(ctx, cudaHostRegister(ptr, size_t(bytes), cudaHostRegisterMapped | cudaHostRegisterPortable));
 	ctx->registered.push_back(SwCtx::HostRange{p, size_t(bytes)});
 	return SW_OK;
 }
@@ -1193,6 +1211,7 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	ctx->num_draws = f.num_draws;
 	PostArgs pa;
 	void* post_out = nullptr;
+	bool direct_host = false;
 	if (f.postprocess)
 	{
 		if (!f.dst) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocess needs a destination");
@@ -1201,9 +1220,20 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 		pa.dst_pitch = f.dst_pitch;
 		if (!f.dst_is_device)
 		{
-			if ((r = ensure(ctx, ctx->up_dst, size_t(p.width) * p.height * 4))) return r;
-			post_out = ctx->up_dst.ptr;
-			pa.dst_pitch = p.width;
+			// A registered host buffer is mapped into the device's address space: the tonemap writes the
+			// Color32 rows straight into it. Otherwise it writes to a device buffer copied out after.
+			void* mapped = registered_device_pointer(ctx, f.dst, (size_t(p.height) - 1) * f.dst_pitch * 4 + size_t(p.width) * 4);
+			if (mapped)
+			{
+				post_out = mapped;
+				direct_host = true;
+			}
+			else
+			{
+				if ((r = ensure(ctx, ctx->up_dst, size_t(p.width) * p.height * 4))) return r;
+				post_out = ctx->up_dst.ptr;
+				pa.dst_pitch = p.width;
+			}
 		}
 		pa.dst = static_cast<uint32_t*>(post_out);
 	}
@@ -1259,6 +1289,11 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 		ctx->exposure_pending = true;
 		ctx->pending_config = f.post;
 		ctx->pending_dt = f.frame_duration_s;
+		if (direct_host)
+		{
+			SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // the frame is in the caller's buffer on return
+			return SW_OK;
+		}
 		if (!f.dst_is_device) return copy_out(ctx, f.dst, f.dst_pitch, 0, post_out, p.width, p.width, p.height, 4);
 	}
 	else if (f.dst && !f.dst_is_device)
