@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(256) pp_downscale_blur_h_kernel(PostArgs a)
 	extern __shared__ __align__(16) uint64_t s_line[]; // bw packed Color64 bloom pixels
 	__shared__ int32_t s_sum[8][4];
 	const uint32_t by = blockIdx.x;
+	pdl_wait(); // the frame's rasterisation has completed
 	constexpr int32_t scaler = 256 / (S * S);
 	// U bloom pixels per thread per pass, all their HDR loads issued before any is used
 	constexpr int U = S == 2 ? 4 : S == 4 ? 2 : 1;
@@ -248,6 +249,7 @@ __global__ void __launch_bounds__(256) pp_downscale_blur_h_kernel(PostArgs a)
 		}
 		out[x] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
 	}
+	pdl_trigger();
 }
 
 // pp_blur_v_tonemap_kernel: one block per TM_W x TM_H tile of the output. It stages the h-blurred bloom
@@ -277,6 +279,7 @@ __global__ void __launch_bounds__(256) pp_blur_v_tonemap_kernel(PostArgs a)
 {
 	extern __shared__ __align__(16) uint64_t s_tile[];
 	const uint32_t x0 = blockIdx.x * TM_W, y0 = blockIdx.y * TM_H;
+	pdl_wait(); // the downscale + horizontal blur pass has completed
 	const uint32_t tw = min(TM_W, a.width - x0), th = min(TM_H, a.height - y0);
 	uint32_t cx0, cx1, cy0, cy1;
 	bloom_tile_range<S>(x0, tw, a.bw, cx0, cx1);
@@ -504,22 +507,17 @@ int launch_fused_bloom(const PostArgs& a, cudaStream_t stream, bool first)
 	{
 		const uint32_t smem = a.bw * 8;
 		if (int e = allow_smem(pp_downscale_blur_h_kernel<S>, smem)) return e;
-		pp_downscale_blur_h_kernel<S><<<a.bh, 256, smem, stream>>>(a);
-		return 0;
+		return int(launch_dependent(pp_downscale_blur_h_kernel<S>, dim3(a.bh), dim3(256), smem, stream, a));
 	}
 	const uint32_t smem = tonemap_tile_smem<S>(a.radius);
 	const dim3 grid((a.width + TM_W - 1) / TM_W, (a.height + TM_H - 1) / TM_H);
 	if (a.linear_filter)
 	{
 		if (int e = allow_smem(pp_blur_v_tonemap_kernel<S, true>, smem)) return e;
-		pp_blur_v_tonemap_kernel<S, true><<<grid, 256, smem, stream>>>(a);
+		return int(launch_dependent(pp_blur_v_tonemap_kernel<S, true>, grid, dim3(256), smem, stream, a));
 	}
-	else
-	{
-		if (int e = allow_smem(pp_blur_v_tonemap_kernel<S, false>, smem)) return e;
-		pp_blur_v_tonemap_kernel<S, false><<<grid, 256, smem, stream>>>(a);
-	}
-	return 0;
+	if (int e = allow_smem(pp_blur_v_tonemap_kernel<S, false>, smem)) return e;
+	return int(launch_dependent(pp_blur_v_tonemap_kernel<S, false>, grid, dim3(256), smem, stream, a));
 }
 
 int launch_fused(const PostArgs& a, cudaStream_t stream, bool first)

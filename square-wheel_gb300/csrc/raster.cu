@@ -433,6 +433,7 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 	const int ty0 = int(blockIdx.x / tiles_x) * TILE_H;
 	const int tid = threadIdx.x;
 	const int ly = tid / TPR;
+	pdl_wait(); // the surface build (launched before this kernel) has completed
 	const int xb = tx0 + (tid % TPR) * STRIP; // first pixel of this thread's strip
 	const int y = ty0 + ly;
 	const bool row_valid = y < a.height;
@@ -559,6 +560,7 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 	for (int o = 16; o > 0; o >>= 1) local_writes += __shfl_xor_sync(0xFFFFFFFFu, local_writes, o);
 	if (lane == 0 && local_writes)
 		atomicAdd(reinterpret_cast<unsigned long long*>(a.error_counter + 2), (unsigned long long)local_writes);
+	pdl_trigger();
 }
 
 } // namespace
@@ -578,9 +580,9 @@ void launch_tiles_variant(const RasterArgs& args, uint32_t pixel_format, cudaStr
 	const unsigned tiles = unsigned(((args.width + t.w - 1) / t.w) * ((args.height + t.h - 1) / t.h));
 	if (tiles == 0) return;
 	if (pixel_format == SW_PIXEL_C64)
-		raster_tiles_kernel<PixC64, t.w, t.h, t.strip><<<tiles, 256, 0, stream>>>(args);
+		launch_dependent(raster_tiles_kernel<PixC64, t.w, t.h, t.strip>, dim3(tiles), dim3(256), 0, stream, args);
 	else
-		raster_tiles_kernel<PixC32, t.w, t.h, t.strip><<<tiles, 256, 0, stream>>>(args);
+		launch_dependent(raster_tiles_kernel<PixC32, t.w, t.h, t.strip>, dim3(tiles), dim3(256), 0, stream, args);
 }
 } // namespace
 

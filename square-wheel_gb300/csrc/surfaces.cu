@@ -340,6 +340,7 @@ __global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
 		if (s.flags & SW_SG_EMISSIVE) out = emissive_mix<P>(a, s, u, v, out, diffuse_layer);
 		arena[s.out_offset + local] = out;
 	}
+	pdl_trigger(); // the tile pass may be scheduled (it waits for this grid before reading the arena)
 }
 
 // f32 -> i32 `as` conversion: truncating, saturating, NaN -> 0.

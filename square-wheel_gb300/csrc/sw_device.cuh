@@ -16,6 +16,31 @@ namespace swgpu
 
 constexpr float MIN_POSITIVE_VALUE = 1.0f / float(1 << 30);
 
+// Programmatic dependent launch between the frame's kernels: a kernel launched with
+// launch_dependent() may start while its predecessor in the stream is still running and must call
+// pdl_wait() before it reads anything the predecessor writes (it waits for the predecessor grid to
+// complete and its memory to be visible; a no-op without such a predecessor). pdl_trigger() tells the
+// runtime that the successor may be scheduled (each CTA calls it once its work is done).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <class... KArgs, class... Args>
+cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+	Args&&... args)
+{
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = grid;
+	cfg.blockDim = block;
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = stream;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 __device__ __forceinline__ float inv_fast(float x) { return __fdiv_rn(1.0f, x); }
 __device__ __forceinline__ float inv_sqrt_fast(float x) { return __fdiv_rn(1.0f, __fsqrt_rn(x)); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
