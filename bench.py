@@ -229,6 +229,93 @@ def run_learned(args, work, r, plain_ldr, local):
     }
 
 
+LEARN_SMALL_MAPS = (11, 12, 13)  # training maps for the 8-room evaluation: other seeds of that configuration
+
+
+def run_learned_small_map(args, local):
+    """The learned path on the map configuration the learned-upscaler benchmark names (the 8-room map of
+    the CPU-runnable configuration, its own camera path), at 1920x1080: plain frames (colour64 + bloom +
+    tonemap as one CUDA graph) against half-resolution frames (the same graph at 960x540) + the learned
+    upscale, each path in its own context (its own exposure sequence), L2 flushed before every frame.
+    The network is trained first on frame pairs of three other 8-room maps."""
+    import torch
+    from sqwheel import abi, gpu, host, learned
+    dev = f"cuda:{local}"
+    t0 = time.perf_counter()
+    ups = learned.Upscaler(local, seed=1)
+    srcs = [learned.PairRenderer(host.Scene(**dict(host.SMALL_MAP, seed=s, num_frames=1024)), (W // 2, H // 2),
+                                 device=local, hdr=True) for s in LEARN_SMALL_MAPS]
+    learned.train(ups, srcs, args.learn_steps, crops_per_step=16, lr=1e-3, pool=24, seed=5)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    for src in srcs:
+        src.close()
+    scene = host.Scene(**host.SMALL_MAP)
+    static = scene.static_data()
+    cfg = abi.PostConfig.default()
+    plain_r, learned_r = gpu.GpuRenderer(static, device=local), gpu.GpuRenderer(static, device=local)
+    for x in (plain_r, learned_r):
+        x.enable_timing(True)
+    learned_r.attach_upscaler(ups)
+    fr = host.Frame(scene)
+    hi_opts = host.frame_options(W, H, abi.SW_PIXEL_C64, directional=False)
+    lo_opts = host.frame_options(W // 2, H // 2, abi.SW_PIXEL_C64, directional=False)
+    plain = torch.empty((H, W), dtype=torch.int32, device=dev)
+    lo = torch.empty((H // 2, W // 2), dtype=torch.int32, device=dev)
+    out = torch.empty((H, W), dtype=torch.int32, device=dev)
+    tmp = torch.empty((H, W), dtype=torch.int32, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    frames = list(range(0, 64, 3))
+    warm = 3
+    plain_ms, learned_ms = [], []
+    psnr = {"learned": [], "avg2x": [], "nearest": []}
+
+    def frame_in(x, opts, fi, dst, pitch):
+        fr.prepare(fi, opts)
+        return x.frame_input(fr.params, fr.lights, fr.surfaces, fr.total_texels, fr.draws, fr.vertices, post_config=cfg,
+                             dst_device_ptr=dst, pitch=pitch)
+
+    for step, fi in enumerate(frames):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        plain_r.draw_frame(frame_in(plain_r, hi_opts, fi, plain.data_ptr(), W))
+        tp = plain_r.timings()[4]
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        learned_r.draw_frame(frame_in(learned_r, lo_opts, fi, lo.data_ptr(), W // 2))
+        learned_r.upscale_device(abi.SW_UPSCALE_LEARNED, 2, lo.data_ptr(), out.data_ptr(), W, H, W)
+        t = learned_r.timings()
+        torch.cuda.synchronize()
+        if step < warm:
+            continue
+        plain_ms.append(tp)
+        learned_ms.append(t[4] + t[3])
+        psnr["learned"].append(ups.psnr(out, plain))
+        for name, mode in (("avg2x", abi.SW_UPSCALE_AVG2X), ("nearest", abi.SW_UPSCALE_NEAREST)):
+            learned_r.upscale_device(mode, 2, lo.data_ptr(), tmp.data_ptr(), W, H, W)
+            torch.cuda.synchronize()
+            psnr[name].append(ups.psnr(tmp, plain))
+    learned_r.attach_upscaler(None)
+    plain_r.close()
+    learned_r.close()
+    ups.close()
+    pm, lm = statistics.mean(plain_ms), statistics.mean(learned_ms)
+    n = len(psnr["learned"])
+    return {
+        "map": "8-room map of the CPU-runnable configuration (its own 64-frame camera path, every 3rd frame), "
+               "1920x1080, colour64 + bloom + tonemap",
+        "plain_frames_per_s": round(1e3 / pm, 2), "learned_frames_per_s": round(1e3 / lm, 2),
+        "speedup_vs_plain": round(pm / lm, 3),
+        "psnr_db": {"learned_mean": round(float(np.mean(psnr["learned"])), 3),
+                    "learned_min": round(float(np.min(psnr["learned"])), 3),
+                    "avg2x_mean": round(float(np.mean(psnr["avg2x"])), 3),
+                    "nearest_mean": round(float(np.mean(psnr["nearest"])), 3),
+                    "frames_at_or_above_38db": f"{sum(x >= 38.0 for x in psnr['learned'])}/{n}"},
+        "train": {"steps": args.learn_steps, "crops_per_step": 16, "maps": f"8-room configuration, seeds {list(LEARN_SMALL_MAPS)}",
+                  "seconds": round(train_s, 2)},
+    }
+
+
 def run_frame_gpu(args, world, rank, local):
     import torch
     from sqwheel import abi, gpu
@@ -332,6 +419,7 @@ def run_frame_gpu(args, world, rank, local):
     lr = run_learned(args, work, r, ldr_frames, local) if args.learn_steps > 0 else None
     if lr is not None:
         launches += args.steps * (1 + 3 + 3 + 1)  # half-resolution frame + the fused upscale kernel
+    lr_small = run_learned_small_map(args, local) if args.learn_steps > 0 else None
 
     peak, peak_kind = peaks()
     s = args.steps
@@ -382,6 +470,8 @@ def run_frame_gpu(args, world, rank, local):
         }
         if lr is not None:
             out_line["learned"] = learned_summary(lr, frame_ms, args)
+        if lr_small is not None:
+            out_line["learned_8_room_map"] = lr_small
         print(json.dumps(out_line), flush=True)
     r.close()
     return out_line
