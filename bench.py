@@ -107,6 +107,21 @@ def dist_env():
     return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(ms, world, device="cpu"):
+    """The job's time over `world` replicas: the slowest rank's (every rank gets it)."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_offset(rank):
+    """Camera-path offset of a replica: every rank draws different frames of the same workload."""
+    return rank * 11
+
+
 def frame_indices(n, offset=0):
     """Frames spread over the 256-frame camera path."""
     return [(offset + i * 37) % 256 for i in range(n)]
@@ -321,7 +336,7 @@ def run_frame_gpu(args, world, rank, local):
     from sqwheel import abi, gpu
     torch.cuda.set_device(local)
     nsteps = args.warmup + args.steps
-    work = FrameWorkload(nsteps, offset=rank * 11)
+    work = FrameWorkload(nsteps, offset=replica_offset(rank))
     r = gpu.GpuRenderer(work.static, device=local)
     r.enable_timing(True)
     stream = torch.cuda.ExternalStream(r.stream_handle())
@@ -385,11 +400,7 @@ def run_frame_gpu(args, world, rank, local):
                 launches += 1 + 3 + 3
         torch.cuda.synchronize()
     stage_sum_ms = (totals["surf"] + totals["raster"] + totals["post"]) / args.steps
-    frame_ms = statistics.mean(graph_ms)
-    if world > 1:
-        tt = torch.tensor([frame_ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        frame_ms = float(tt.item())
+    frame_ms = max_over_ranks(statistics.mean(graph_ms), world, f"cuda:{local}")
     value = world * 1e3 / frame_ms
 
     # e2e: the C++ host renderer (host work: visibility, surface and draw setup) drives the C ABI per
@@ -571,11 +582,7 @@ def run_surfaces_gpu(args, world, rank, local):
                 flush.fill_(1.0)
             r.rebuild_surfaces()
             total += r.timings()[0]
-    ms = total / args.steps
-    if world > 1:
-        tt = torch.tensor([ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(total / args.steps, world, f"cuda:{local}")
     value = world * b.total_texels / 1e6 / (ms / 1e3)
     e2e = []
     for _ in range(3):
@@ -685,10 +692,7 @@ def run_upscale_gpu(args, world, rank, local):
     layered_ms, _ = timed(min(args.steps, 20))
     ups.set_fused(True)
     ms, clocks = timed(args.steps)
-    if world > 1:
-        tt = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(ms, world, dev)
     # e2e: through the C ABI (sw_upscale, learned mode) from and to host memory
     r = gpu.GpuRenderer(host.Scene(**host.SMALL_MAP).static_data(), device=local)
     r.attach_upscaler(ups)
