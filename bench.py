@@ -130,6 +130,17 @@ def frame_indices(n, offset=0):
 # ---------------------------------------------------------------------------------------------------------
 # frame workload
 
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each stage's kernels at the
+# frame workload, from one ncu capture each (cold cache: ncu replays every kernel alone); the captures are
+# summarised in profiles/postprocess_1080p_c64.md, profiles/raster_tiles_1080p_c64.md and
+# profiles/surf_build_4096_surfaces_c64.md.
+STAGE_TRAFFIC = {
+    "post": 16.604928e6 + 20.803840e6,   # pp_downscale_blur_h_kernel + pp_blur_v_tonemap_kernel
+    "raster": 19.322368e6 + 0.054272e6,  # raster_tiles_kernel + raster_setup_kernel
+    "surf": None,                        # captured only at the 4,096-surface workload
+}
+
+
 def post_bytes(w, h, scale=2):
     """Algorithmic bytes of bloom + tonemap as two passes over the frame: HDR read by the downscale and
     again by the tonemap, the blurred bloom buffer written once and read once, the Color32 frame written
@@ -472,7 +483,7 @@ def run_frame_gpu(args, world, rank, local):
             "roofline": {"bound": "hbm", "kernel": kernel_names[dom], "achieved": stages[dom]["GB/s"], "peak": peak,
                          "unit": "GB/s", "frac": stages[dom]["frac_of_measured_hbm"],
                          "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": stages[dom]["algorithmic_bytes"],
-                         "traffic": None},
+                         "traffic": STAGE_TRAFFIC.get(dom)},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_val, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d / n_e2e),
                     "d2h_bytes_per_step": int(d2h / n_e2e)},
