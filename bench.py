@@ -131,9 +131,8 @@ def frame_indices(n, offset=0):
 # frame workload
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each stage's kernels at the
-# frame workload, from one ncu capture each (cold cache: ncu replays every kernel alone); the captures are
-# summarised in profiles/postprocess_1080p_c64.md, profiles/raster_tiles_1080p_c64.md and
-# profiles/surf_build_4096_surfaces_c64.md.
+# frame workload, from one `ncu --set full` capture of this command (cold cache: ncu replays every kernel
+# alone; the frame's writes are still in L2 when a kernel ends).
 STAGE_TRAFFIC = {
     "post": 16.604928e6 + 20.803840e6,   # pp_downscale_blur_h_kernel + pp_blur_v_tonemap_kernel
     "raster": 19.322368e6 + 0.054272e6,  # raster_tiles_kernel + raster_setup_kernel
