@@ -356,6 +356,92 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* frame);
 /* Graph capture of sw_draw_frame: on (default) or off (the same work launched directly). */
 int sw_set_frame_graph(SwCtx* ctx, int enable);
 
+/* ---- GPU-side surface and draw preparation (no reference counterpart; the reference runs these steps
+ * on the host in prepare_polygons_surfaces / build_polygons_surfaces / draw_tree, see below) ----
+ *
+ * The host keeps what is serial and tiny (visibility, light positioning, the BSP's back-to-front leaf
+ * order, the skybox) and hands the GPU the visible leafs; the GPU runs, for every polygon of those
+ * leafs, prepare_polygon_surface (partial_renderer.rs:1464-1638), the surface descriptor of
+ * build_polygons_surfaces with polygon_is_affected_by_light (:1640-1819, :3877-3985) and draw_polygon
+ * (:4011-4142), compacts surfaces in the reference's allocation order and draws in exact submission
+ * order, and feeds the surface build and the rasteriser without a host round trip. Results equal the
+ * host path's (sw_draw_frame with the host's SwSurfaceDesc / SwDrawCmd arrays) bit for bit. */
+
+/* SwMapPolygon.flags */
+#define SW_POLY_DRAW 1u          /* material.draw */
+#define SW_POLY_SKY 2u           /* sky material: marks where the skybox shows, never a surface */
+#define SW_POLY_DIFFUSE_LAYER 4u /* material.light && material has a diffuse layer */
+
+/* One world polygon of the map with the material fields its surface needs (bsp_map_compact::Polygon,
+ * src/common/bsp_map_compact.rs:60-74, PolygonBasisVecs, src/square_wheel/surfaces.rs:7-47). */
+typedef struct SwMapPolygon {
+	float plane[4];                 /* vec.xyz, dist: points p of the plane have dot(vec, p) = dist */
+	float tex_coord_equation[2][4]; /* tc_i(p) = dot(vec_i, p) + dist_i */
+	float basis_u[3], basis_v[3], basis_start[3], basis_normal[3];
+	int32_t tex_coord_min[2], tex_coord_max[2];
+	uint32_t first_vertex, num_vertices; /* into sw_set_map's vertices */
+	uint32_t texture;                    /* material texture: texture_mip = texture * 5 + mip */
+	uint32_t lightmap_data_offset;
+	uint32_t flags;                      /* SW_POLY_* */
+	uint32_t blending_mode;              /* SwBlend of the material */
+	uint32_t emissive_texture;           /* emissive_mip = emissive_texture * 5 + mip, or SW_NO_EMISSIVE */
+	float emissive_light[3];
+} SwMapPolygon;
+
+/* Upload the world polygons and their vertices (xyz floats) for sw_draw_frame_view. Load-time data
+ * like sw_create's; synchronous. */
+int sw_set_map(SwCtx* ctx, const SwMapPolygon* polygons, uint32_t num_polygons, const float* vertices,
+	uint32_t num_vertices);
+
+/* One visible BSP leaf (MapVisibilityCalculator's leaf bounds, map_visibility_calculator.rs:157-267).
+ * Clip planes are ClippingPolygon::get_clip_planes of the bounds (clipping_polygon.rs:140-152): 8 x
+ * (a, b, c) with a*x + b*y >= c inside. */
+typedef struct SwViewLeaf {
+	uint32_t first_polygon, num_polygons; /* the leaf's polygons in SwMapPolygon order */
+	uint32_t first_light, num_lights;     /* the leaf's lights (DynamicObjectsIndex order) in leaf_lights */
+	uint32_t draw_order;                  /* position in draw_tree's back-to-front order, or SW_LEAF_NOT_DRAWN */
+	uint32_t reserved;
+	float clip_planes[8][3];              /* leaf bounds: surface preparation */
+	float draw_clip_planes[8][3];         /* leaf bounds intersected with the viewport: draw_leaf */
+} SwViewLeaf;
+#define SW_LEAF_NOT_DRAWN 0xFFFFFFFFu
+
+typedef struct SwViewFrameInput {
+	SwFrameParams params;
+	uint32_t num_lights;
+	const SwLight* lights;
+	float view_matrix[16];   /* CameraMatrices::view_matrix, column-major */
+	float planes_matrix[16]; /* CameraMatrices::planes_matrix, column-major */
+	float mip_bias;
+	uint32_t num_leafs;       /* visible leafs in leaf index order */
+	const SwViewLeaf* leafs;
+	uint32_t num_leaf_lights;
+	const uint16_t* leaf_lights;
+	uint32_t num_draws;       /* draws before the leafs' (draw_skybox), in submission order */
+	const SwDrawCmd* draws;
+	const SwVertex16* vertices;
+	uint32_t num_vertices;
+	uint32_t postprocess;     /* as SwFrameInput */
+	SwPostConfig post;
+	float frame_duration_s;
+	float color_modulate[3];
+	void* dst;
+	uint32_t dst_pitch;
+	int32_t dst_is_device;
+} SwViewFrameInput;
+
+/* One whole frame like sw_draw_frame, with the surfaces and the leafs' draws prepared on the GPU. */
+int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* frame);
+
+/* What the last sw_draw_frame_view prepared (diagnostics and tests; synchronises): the counts, and up
+ * to the given capacities the surface descriptors, draw commands (the host's draws first) and vertices. */
+typedef struct SwViewCounts {
+	uint32_t num_surfaces, num_draws, num_vertices, error; /* error != 0: a capacity was exceeded */
+	uint64_t total_texels, num_rows;
+} SwViewCounts;
+int sw_read_view_prep(SwCtx* ctx, SwViewCounts* out_counts, SwSurfaceDesc* surfaces, uint32_t max_surfaces,
+	SwDrawCmd* draws, uint32_t max_draws, SwVertex16* vertices, uint32_t max_vertices);
+
 /* ---- launch configuration (no reference counterpart) ---- */
 #define SW_RASTER_TILE_VARIANTS 5
 typedef struct SwTuning {
@@ -374,8 +460,9 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 
 /* sizeof() of the ABI structs in this order: SwCreateInfo, SwTextureMip, SwEmissiveMip,
  * SwDirectionalLightmapElement, SwLight, SwSurfaceDesc, SwVertex16, SwDrawCmd, SwFrameParams,
- * SwPostConfig, SwStats, SwFrameInput, SwTuning. Writes min(count, 13) values; returns the number of
- * structs (13). Needs no GPU: bindings use it to check their mirrored layouts. */
+ * SwPostConfig, SwStats, SwFrameInput, SwTuning, SwMapPolygon, SwViewLeaf, SwViewFrameInput,
+ * SwViewCounts. Writes min(count, 17) values; returns the number of structs (17). Needs no GPU:
+ * bindings use it to check their mirrored layouts. */
 int sw_abi_layout(uint32_t* sizes, uint32_t count);
 
 /* Diagnostics: copy the frame's surface arena (total_texels of sw_submit_surfaces) to host memory. */

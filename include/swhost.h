@@ -93,6 +93,12 @@ int swh_frame_destroy(SwhFrame* frame);
 int swh_frame_prepare(SwhFrame* frame, uint32_t frame_index, const SwhFrameOptions* options);
 /* Pointers into the frame's arrays, valid until the next swh_frame_prepare. */
 int swh_frame_outputs(const SwhFrame* frame, SwhFrameOutputs* out);
+/* The host half of a frame whose surfaces and world draws the GPU prepares (sw_draw_frame_view):
+ * visibility, light positioning, the skybox draws and the visible leafs with their bounds, lights and
+ * back-to-front order. swh_frame_view_input fills everything of SwViewFrameInput but mip_bias and the
+ * postprocess / destination fields; its pointers stay valid until the next prepare call. */
+int swh_frame_prepare_view(SwhFrame* frame, uint32_t frame_index, const SwhFrameOptions* options);
+int swh_frame_view_input(const SwhFrame* frame, SwViewFrameInput* out);
 
 typedef struct SwhRenderer SwhRenderer;
 
@@ -104,11 +110,16 @@ int swh_renderer_prepare_frame(SwhRenderer* renderer, uint32_t frame_index, cons
 /* Renderer::draw_frame: sw_submit_draws + sw_render into dst (optional). */
 int swh_renderer_draw_frame(SwhRenderer* renderer, void* dst, uint32_t pitch, int dst_is_device);
 /* One whole frame as the host's frame loop runs it (host.rs:400-416: prepare_frame, draw_frame and,
- * when `post` is not NULL, perform_postprocessing): host work, then sw_draw_frame (one CUDA graph:
- * uploads, surfaces, raster, postprocess) with the Color32 result (post) or the frame (no post) in dst. */
+ * when `post` is not NULL, perform_postprocessing): host work, then one CUDA graph (upload, surface and
+ * draw preparation, surfaces, raster, postprocess) with the Color32 result (post) or the frame (no
+ * post) in dst. */
 int swh_renderer_render_frame(SwhRenderer* renderer, uint32_t frame_index, const SwhFrameOptions* options,
 	const SwPostConfig* post, float frame_duration_s, const float color_modulate[3], void* dst, uint32_t pitch,
 	int dst_is_device);
+/* swh_renderer_render_frame's preparation: 1 (default) = the GPU prepares the surfaces and the world
+ * draws (swh_frame_prepare_view + sw_draw_frame_view), 0 = the host does (swh_frame_prepare +
+ * sw_draw_frame). Both give the same frame. */
+int swh_renderer_set_gpu_prep(SwhRenderer* renderer, int enable);
 /* The GPU context and the frame used by the renderer. */
 SwCtx* swh_renderer_context(SwhRenderer* renderer);
 SwhFrame* swh_renderer_frame(SwhRenderer* renderer);

@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIB_DIR = os.path.join(PKG, "lib")
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(LIB_DIR, "libswgpu.so")
-SOURCES = ["swgpu.cu", "surfaces.cu", "raster.cu", "post.cu", "post_noalloc.cu", "upscaler.cu"]
+SOURCES = ["swgpu.cu", "surfaces.cu", "raster.cu", "prep.cu", "post.cu", "post_noalloc.cu", "upscaler.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -47,6 +47,8 @@ def build(force=False, verbose=False):
     os.makedirs(BUILD_DIR, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(PKG, "..", "include", "swgpu.h"))
+    # the per-polygon preparation code shared with the host side
+    headers += [os.path.join(PKG, "host", f) for f in ("prep_math.h", "hmath.h")]
     cc = nvcc()
     jobs = []
     objs = []

@@ -307,69 +307,74 @@ __global__ void __launch_bounds__(256) raster_setup_kernel(RasterArgs a)
 	__shared__ RasterPart s_parts[SW_RASTER_MAX_PARTS];
 	__shared__ DrawRows s_dr;
 	__shared__ uint32_t s_np;
-	const uint32_t di = blockIdx.x;
-	static_assert(sizeof(SwDrawCmd) % 4 == 0 && sizeof(SwDrawCmd) / 4 <= 256, "draw record");
-	if (threadIdx.x < sizeof(SwDrawCmd) / 4)
-		reinterpret_cast<uint32_t*>(&s_d)[threadIdx.x] = reinterpret_cast<const uint32_t*>(a.draws + di)[threadIdx.x];
-	if (threadIdx.x == 0) s_dr = a.draw_rows[di];
-	__syncthreads();
-	if (threadIdx.x < s_d.vertex_count && threadIdx.x < SW_MAX_POLYGON_VERTICES)
-		s_v[threadIdx.x] = a.vertices[s_d.first_vertex + threadIdx.x];
-	__syncthreads();
-	if (threadIdx.x == 0)
+	// One draw per CTA; with the draw count on the device (GPU-side preparation) a fixed grid strides.
+	const uint32_t num_draws = a.counts ? a.counts->num_draws : a.num_draws;
+	for (uint32_t di = blockIdx.x; di < num_draws; di += gridDim.x)
 	{
-		const SwDrawCmd& d = s_d;
-		const uint32_t np = edge_walk(d, s_v, a.height, s_parts);
-		s_np = np;
-		int32_t bx0 = INT32_MAX, bx1 = INT32_MIN, by0 = INT32_MAX, by1 = INT32_MIN;
-		for (uint32_t pi = 0; pi < np; ++pi)
+		static_assert(sizeof(SwDrawCmd) % 4 == 0 && sizeof(SwDrawCmd) / 4 <= 256, "draw record");
+		if (threadIdx.x < sizeof(SwDrawCmd) / 4)
+			reinterpret_cast<uint32_t*>(&s_d)[threadIdx.x] = reinterpret_cast<const uint32_t*>(a.draws + di)[threadIdx.x];
+		if (threadIdx.x == 0) s_dr = a.draw_rows[di];
+		__syncthreads();
+		if (threadIdx.x < s_d.vertex_count && threadIdx.x < SW_MAX_POLYGON_VERTICES)
+			s_v[threadIdx.x] = a.vertices[s_d.first_vertex + threadIdx.x];
+		__syncthreads();
+		if (threadIdx.x == 0)
 		{
-			const RasterPart& p = s_parts[pi];
-			const int32_t last = p.y_end_int - 1 - p.y_start_int;
-			bx0 = min(bx0, min(p.x_left0 >> 16, wadd(p.x_left0, wmul(last, p.dx_dy_left)) >> 16));
-			bx1 = max(bx1, max(p.x_right0 >> 16, wadd(p.x_right0, wmul(last, p.dx_dy_right)) >> 16));
-			by0 = min(by0, p.y_start_int);
-			by1 = max(by1, p.y_end_int);
-		}
-		bx0 = max(bx0, 0);
-		bx1 = min(bx1, a.width);
-		const DrawRows dr = s_dr;
-		// Rows outside the host's row range have no record; clamp the box to it.
-		by0 = max(by0, dr.y0);
-		by1 = min(by1, dr.y0 + int32_t(dr.nrows));
-		a.boxes[di] = (np > 0 && bx0 < bx1 && by0 < by1) ? RasterBox{int16_t(bx0), int16_t(by0), int16_t(bx1), int16_t(by1)}
-															: RasterBox{0, 0, 0, 0};
-		RasterDraw rd;
-		rd.tex_offset = d.tex_offset;
-		rd.tex_w = d.tex_size[0];
-		rd.tex_h = d.tex_size[1];
-		rd.row_base = dr.row_base;
-		rd.y0 = dr.y0;
-		rd.mode = d.mode;
-		rd.blend = uint16_t(d.blend);
-		rd.tex_source = uint16_t(d.tex_source);
-		a.rdraws[di] = rd;
-	}
-	__syncthreads();
-	const uint32_t np = s_np;
-	const DrawEq e = draw_equations(s_d);
-	const DrawRows dr = s_dr;
-	for (uint32_t k = threadIdx.x; k < dr.nrows; k += blockDim.x)
-	{
-		const int32_t y = dr.y0 + int32_t(k);
-		RasterRow row;
-		row.xs = row.xe = 0;
-		row.a0 = row.b0 = row.a1 = row.b1 = row.a2 = row.b2 = 0;
-		for (uint32_t pi = 0; pi < np; ++pi)
-		{
-			const RasterPart& p = s_parts[pi];
-			if (y >= p.y_start_int && y < p.y_end_int)
+			const SwDrawCmd& d = s_d;
+			const uint32_t np = edge_walk(d, s_v, a.height, s_parts);
+			s_np = np;
+			int32_t bx0 = INT32_MAX, bx1 = INT32_MIN, by0 = INT32_MAX, by1 = INT32_MIN;
+			for (uint32_t pi = 0; pi < np; ++pi)
 			{
-				row = row_setup(s_d, e, p, y, a.width);
-				break;
+				const RasterPart& p = s_parts[pi];
+				const int32_t last = p.y_end_int - 1 - p.y_start_int;
+				bx0 = min(bx0, min(p.x_left0 >> 16, wadd(p.x_left0, wmul(last, p.dx_dy_left)) >> 16));
+				bx1 = max(bx1, max(p.x_right0 >> 16, wadd(p.x_right0, wmul(last, p.dx_dy_right)) >> 16));
+				by0 = min(by0, p.y_start_int);
+				by1 = max(by1, p.y_end_int);
 			}
+			bx0 = max(bx0, 0);
+			bx1 = min(bx1, a.width);
+			const DrawRows dr = s_dr;
+			// Rows outside the host's row range have no record; clamp the box to it.
+			by0 = max(by0, dr.y0);
+			by1 = min(by1, dr.y0 + int32_t(dr.nrows));
+			a.boxes[di] = (np > 0 && bx0 < bx1 && by0 < by1) ? RasterBox{int16_t(bx0), int16_t(by0), int16_t(bx1), int16_t(by1)}
+																: RasterBox{0, 0, 0, 0};
+			RasterDraw rd;
+			rd.tex_offset = d.tex_offset;
+			rd.tex_w = d.tex_size[0];
+			rd.tex_h = d.tex_size[1];
+			rd.row_base = dr.row_base;
+			rd.y0 = dr.y0;
+			rd.mode = d.mode;
+			rd.blend = uint16_t(d.blend);
+			rd.tex_source = uint16_t(d.tex_source);
+			a.rdraws[di] = rd;
 		}
-		a.rows[dr.row_base + k] = row;
+		__syncthreads();
+		const uint32_t np = s_np;
+		const DrawEq e = draw_equations(s_d);
+		const DrawRows dr = s_dr;
+		for (uint32_t k = threadIdx.x; k < dr.nrows; k += blockDim.x)
+		{
+			const int32_t y = dr.y0 + int32_t(k);
+			RasterRow row;
+			row.xs = row.xe = 0;
+			row.a0 = row.b0 = row.a1 = row.b1 = row.a2 = row.b2 = 0;
+			for (uint32_t pi = 0; pi < np; ++pi)
+			{
+				const RasterPart& p = s_parts[pi];
+				if (y >= p.y_start_int && y < p.y_end_int)
+				{
+					row = row_setup(s_d, e, p, y, a.width);
+					break;
+				}
+			}
+			a.rows[dr.row_base + k] = row;
+		}
+		__syncthreads(); // the shared records are reused by the CTA's next draw
 	}
 }
 
@@ -434,6 +439,7 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 	const int tid = threadIdx.x;
 	const int ly = tid / TPR;
 	pdl_wait(); // the surface build (launched before this kernel) has completed
+	const uint32_t num_draws = a.counts ? a.counts->num_draws : a.num_draws;
 	const int xb = tx0 + (tid % TPR) * STRIP; // first pixel of this thread's strip
 	const int y = ty0 + ly;
 	const bool row_valid = y < a.height;
@@ -459,7 +465,7 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 	unsigned int local_errors = 0, local_writes = 0;
 
 	const int lane = tid & 31, warp = tid >> 5;
-	for (uint32_t chunk = 0; chunk < a.num_draws; chunk += 256)
+	for (uint32_t chunk = 0; chunk < num_draws; chunk += 256)
 	{
 		// Ordered compaction of the chunk's draws whose box meets the tile; the hitting thread stages
 		// the draw's record and box.
@@ -467,7 +473,7 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 		bool hit = false;
 		RasterBox b{0, 0, 0, 0};
 		RasterDraw rd{};
-		if (di < a.num_draws)
+		if (di < num_draws)
 		{
 			b = a.boxes[di];
 			hit = b.x0 < tx1 && b.x1 > tx0 && b.y0 < ty1 && b.y1 > ty0 && b.x0 < b.x1 && b.y0 < b.y1;
@@ -567,7 +573,12 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 
 int launch_raster_setup(const RasterArgs& args, cudaStream_t stream)
 {
-	if (args.num_draws > 0) raster_setup_kernel<<<args.num_draws, 256, 0, stream>>>(args);
+	if (args.counts)
+	{
+		if (args.setup_blocks > 0) raster_setup_kernel<<<args.setup_blocks, 256, 0, stream>>>(args);
+	}
+	else if (args.num_draws > 0)
+		raster_setup_kernel<<<args.num_draws, 256, 0, stream>>>(args);
 	return int(cudaGetLastError());
 }
 
@@ -598,23 +609,6 @@ int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, uint32_t 
 	default: return int(cudaErrorInvalidValue);
 	}
 	return int(cudaGetLastError());
-}
-
-// Rows a draw can cover: [round(min_y), round(max_y)) clipped to the frame (the edge walk's parts lie
-// inside, rasterizer.rs:160-271 with fixed16_round_to_int).
-void draw_row_range(const SwDrawCmd& d, const SwVertex16* v, int32_t height, int32_t& y0, uint32_t& nrows)
-{
-	int32_t mn = v[d.first_vertex].y, mx = mn;
-	for (uint32_t i = 1; i < d.vertex_count; ++i)
-	{
-		mn = std::min(mn, v[d.first_vertex + i].y);
-		mx = std::max(mx, v[d.first_vertex + i].y);
-	}
-	auto round_i = [](int32_t f) { return int32_t(uint32_t(f) + uint32_t(FIXED16_HALF)) >> 16; };
-	const int32_t a = std::max(round_i(mn), 0);
-	const int32_t b = std::min(round_i(mx), height);
-	y0 = a;
-	nrows = b > a ? uint32_t(b - a) : 0u;
 }
 
 } // namespace swgpu

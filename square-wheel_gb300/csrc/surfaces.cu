@@ -292,7 +292,8 @@ __global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
 {
 	typedef typename P::T T;
 	T* arena = static_cast<T*>(a.arena);
-	const uint64_t total = a.total_work;
+	const uint64_t total = a.counts ? a.counts->total_texels : a.total_work;
+	const uint32_t num_surfaces = a.counts ? a.counts->num_surfaces : a.num_surfaces;
 	const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
 	const uint32_t lane = threadIdx.x & 31u;
 	const uint64_t warp_first = uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u);
@@ -303,7 +304,7 @@ __global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
 		uint32_t s0 = 0;
 		if (lane == 0)
 		{
-			uint32_t lo = 0, hi = a.num_surfaces; // prefix[lo] <= wbase < prefix[hi]
+			uint32_t lo = 0, hi = num_surfaces; // prefix[lo] <= wbase < prefix[hi]
 			while (hi - lo > 1)
 			{
 				const uint32_t mid = (lo + hi) >> 1;
@@ -343,90 +344,16 @@ __global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
 	pdl_trigger(); // the tile pass may be scheduled (it waits for this grid before reading the arena)
 }
 
-// f32 -> i32 `as` conversion: truncating, saturating, NaN -> 0.
-int32_t host_f2i32(float x)
-{
-	if (x != x) return 0;
-	if (x >= 2147483648.0f) return INT32_MAX;
-	if (x <= -2147483648.0f) return INT32_MIN;
-	return int32_t(x);
-}
-
-float host_dot(const float* a, const float* b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
-
 } // namespace
 
-void make_surface_gpu(const SwSurfaceDesc& d, const SwTextureMip* tex, const SwEmissiveMip* em, SurfaceGpu& o)
+int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, int blocks_per_sm, cudaStream_t stream,
+	uint64_t work_hint)
 {
-	// surfaces.rs:456-462: start + u*(tc0+0.5) + v*(tc1+0.5); normalised basis vectors.
-	const float a0 = float(d.tc_start[0]) + 0.5f, a1 = float(d.tc_start[1]) + 0.5f;
-	for (int i = 0; i < 3; ++i)
-	{
-		o.start_pos[i] = (d.basis_start[i] + d.basis_u[i] * a0) + d.basis_v[i] * a1;
-		o.u[i] = d.basis_u[i];
-		o.v[i] = d.basis_v[i];
-		o.normal[i] = d.basis_normal[i];
-	}
-	const float iu = 1.0f / std::sqrt(std::fmax(host_dot(d.basis_u, d.basis_u), MIN_POSITIVE_VALUE));
-	const float iv = 1.0f / std::sqrt(std::fmax(host_dot(d.basis_v, d.basis_v), MIN_POSITIVE_VALUE));
-	for (int i = 0; i < 3; ++i)
-	{
-		o.u_norm[i] = d.basis_u[i] * iu;
-		o.v_norm[i] = d.basis_v[i] * iv;
-	}
-	const bool has_lm = d.lightmap_offset != SW_NO_LIGHTMAP;
-	const uint32_t log2 = has_lm ? d.lightmap_scale_log2 : 0u;
-	o.inv_scale = 1.0f / float(1u << log2);
-	o.k_shift = 0.5f * o.inv_scale;
-	o.width = d.size[0];
-	o.flags = 0;
-	if (d.flags & SW_SURF_DIFFUSE_LAYER)
-	{
-		o.tex_offset = tex->offset;
-		o.tex_w = tex->width;
-		o.tex_h = tex->height;
-		o.flags |= (tex->flags & 7u) | SW_SG_DIFFUSE;
-	}
-	else
-	{
-		o.tex_offset = 0;
-		o.tex_w = o.tex_h = 1;
-	}
-	if (has_lm) o.flags |= SW_SG_LIGHTMAP;
-	o.tc0 = d.tc_start[0];
-	o.tc1 = d.tc_start[1];
-	o.lm_offset = d.lightmap_offset;
-	o.lm_width = d.lightmap_size[0];
-	o.lm_log2 = log2;
-	o.lm_shift0 = d.lightmap_tc_shift[0];
-	o.lm_shift1 = d.lightmap_tc_shift[1];
-	o.num_lights = d.num_lights;
-	for (int i = 0; i < SW_MAX_POLYGON_LIGHTS; ++i) o.lights[i] = d.lights[i];
-	if (em)
-	{
-		o.flags |= SW_SG_EMISSIVE;
-		o.em_offset = em->offset;
-		o.em_w = em->width;
-		o.em_h = em->height;
-		// ColorVecI::from_color_f32x3([l0*256, l1*256, l2*256]) -> lanes [b, g, r] (surfaces.rs:911-914)
-		o.em_light[0] = host_f2i32(d.emissive_light[2] * 256.0f);
-		o.em_light[1] = host_f2i32(d.emissive_light[1] * 256.0f);
-		o.em_light[2] = host_f2i32(d.emissive_light[0] * 256.0f);
-	}
-	else
-	{
-		o.em_offset = 0;
-		o.em_w = o.em_h = 1;
-		o.em_light[0] = o.em_light[1] = o.em_light[2] = 0;
-	}
-	o.out_offset = d.out_offset;
-}
-
-int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, int blocks_per_sm, cudaStream_t stream)
-{
-	if (args.total_work == 0) return 0;
+	const uint64_t work = args.counts ? work_hint : args.total_work;
+	if (work == 0 && !args.counts) return 0;
 	const int threads = 256;
-	uint64_t blocks_needed = (args.total_work + threads - 1) / threads;
+	uint64_t blocks_needed = (work + threads - 1) / threads;
+	if (args.counts && blocks_needed < uint64_t(num_sms)) blocks_needed = uint64_t(num_sms);
 	// At most blocks_per_sm blocks per SM (several waves of resident blocks): small frames get one
 	// texel per thread (latency hidden by parallelism), large batches stride.
 	uint64_t blocks_max = uint64_t(num_sms) * uint64_t(blocks_per_sm);

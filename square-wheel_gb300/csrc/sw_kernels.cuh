@@ -45,6 +45,7 @@ struct SurfaceKernelArgs
 	uint32_t num_surfaces;
 	uint32_t directional;
 	uint64_t total_work;
+	const SwViewCounts* counts; // GPU-side preparation: num_surfaces / total_work from here (else NULL)
 	const uint64_t* texels;
 	const uint32_t* emissive_pixels;
 	const float* lightmaps;
@@ -54,12 +55,90 @@ struct SurfaceKernelArgs
 	void* arena;
 };
 
-// Host-side construction of one SurfaceGpu (exact f32 arithmetic; the file is compiled without FMA
-// contraction).
-void make_surface_gpu(const SwSurfaceDesc& d, const SwTextureMip* tex, const SwEmissiveMip* em, SurfaceGpu& out);
+// f32 -> i32 `as` conversion: truncating, saturating, NaN -> 0.
+__host__ __device__ inline int32_t f2i32_as(float x)
+{
+	if (x != x) return 0;
+	if (x >= 2147483648.0f) return INT32_MAX;
+	if (x <= -2147483648.0f) return INT32_MIN;
+	return int32_t(x);
+}
 
-// Persistent grid of at most num_sms * blocks_per_sm blocks of 256 threads.
-int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, int blocks_per_sm, cudaStream_t stream);
+// One SurfaceGpu from its descriptor and texture tables (exact f32 arithmetic without FMA contraction;
+// the host's sw_submit_surfaces and the GPU-side preparation both use it).
+__host__ __device__ inline void make_surface_gpu(const SwSurfaceDesc& d, const SwTextureMip* tex, const SwEmissiveMip* em,
+	SurfaceGpu& o)
+{
+	// surfaces.rs:456-462: start + u*(tc0+0.5) + v*(tc1+0.5); normalised basis vectors.
+	const float a0 = float(d.tc_start[0]) + 0.5f, a1 = float(d.tc_start[1]) + 0.5f;
+	for (int i = 0; i < 3; ++i)
+	{
+		o.start_pos[i] = (d.basis_start[i] + d.basis_u[i] * a0) + d.basis_v[i] * a1;
+		o.u[i] = d.basis_u[i];
+		o.v[i] = d.basis_v[i];
+		o.normal[i] = d.basis_normal[i];
+	}
+	const float uu = d.basis_u[0] * d.basis_u[0] + (d.basis_u[1] * d.basis_u[1] + d.basis_u[2] * d.basis_u[2]);
+	const float vv = d.basis_v[0] * d.basis_v[0] + (d.basis_v[1] * d.basis_v[1] + d.basis_v[2] * d.basis_v[2]);
+	const float iu = 1.0f / sqrtf(fmaxf(uu, MIN_POSITIVE_VALUE));
+	const float iv = 1.0f / sqrtf(fmaxf(vv, MIN_POSITIVE_VALUE));
+	for (int i = 0; i < 3; ++i)
+	{
+		o.u_norm[i] = d.basis_u[i] * iu;
+		o.v_norm[i] = d.basis_v[i] * iv;
+	}
+	const bool has_lm = d.lightmap_offset != SW_NO_LIGHTMAP;
+	const uint32_t log2 = has_lm ? d.lightmap_scale_log2 : 0u;
+	o.inv_scale = 1.0f / float(1u << log2);
+	o.k_shift = 0.5f * o.inv_scale;
+	o.width = d.size[0];
+	o.flags = 0;
+	if (d.flags & SW_SURF_DIFFUSE_LAYER)
+	{
+		o.tex_offset = tex->offset;
+		o.tex_w = tex->width;
+		o.tex_h = tex->height;
+		o.flags |= (tex->flags & 7u) | SW_SG_DIFFUSE;
+	}
+	else
+	{
+		o.tex_offset = 0;
+		o.tex_w = o.tex_h = 1;
+	}
+	if (has_lm) o.flags |= SW_SG_LIGHTMAP;
+	o.tc0 = d.tc_start[0];
+	o.tc1 = d.tc_start[1];
+	o.lm_offset = d.lightmap_offset;
+	o.lm_width = d.lightmap_size[0];
+	o.lm_log2 = log2;
+	o.lm_shift0 = d.lightmap_tc_shift[0];
+	o.lm_shift1 = d.lightmap_tc_shift[1];
+	o.num_lights = d.num_lights;
+	for (int i = 0; i < SW_MAX_POLYGON_LIGHTS; ++i) o.lights[i] = d.lights[i];
+	if (em)
+	{
+		o.flags |= SW_SG_EMISSIVE;
+		o.em_offset = em->offset;
+		o.em_w = em->width;
+		o.em_h = em->height;
+		// ColorVecI::from_color_f32x3([l0*256, l1*256, l2*256]) -> lanes [b, g, r] (surfaces.rs:911-914)
+		o.em_light[0] = f2i32_as(d.emissive_light[2] * 256.0f);
+		o.em_light[1] = f2i32_as(d.emissive_light[1] * 256.0f);
+		o.em_light[2] = f2i32_as(d.emissive_light[0] * 256.0f);
+	}
+	else
+	{
+		o.em_offset = 0;
+		o.em_w = o.em_h = 1;
+		o.em_light[0] = o.em_light[1] = o.em_light[2] = 0;
+	}
+	o.out_offset = d.out_offset;
+}
+
+// Grid of at most num_sms * blocks_per_sm blocks of 256 threads that stride over the texels. With
+// args.counts set the texel count is on the device: work_hint (an estimate) sizes the grid instead.
+int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, int blocks_per_sm, cudaStream_t stream,
+	uint64_t work_hint = 0);
 
 // ---- rasteriser ----
 
@@ -127,6 +206,8 @@ struct RasterArgs
 	const SwVertex16* vertices;
 	const DrawRows* draw_rows;
 	uint32_t num_draws;
+	const SwViewCounts* counts; // GPU-side preparation: num_draws from here (else NULL)
+	uint32_t setup_blocks;      // with counts: raster setup CTAs, each striding over the draws
 	uint32_t total_rows; // row records of all draws
 	int32_t width, height;
 	uint32_t clear_background;
@@ -147,8 +228,92 @@ int launch_raster_setup(const RasterArgs& args, cudaStream_t stream);
 // variant: tile shape index (< SW_RASTER_TILE_VARIANTS, see SwTuning); every variant gives the same frame.
 int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, uint32_t variant, cudaStream_t stream);
 
-// Host side: rows [y0, y0 + nrows) a draw can cover (from its vertices).
-void draw_row_range(const SwDrawCmd& d, const SwVertex16* vertices, int32_t height, int32_t& y0, uint32_t& nrows);
+// Rows [y0, y0 + nrows) a draw can cover: [round(min_y), round(max_y)) of its vertices clipped to the
+// frame (the edge walk's parts lie inside, rasterizer.rs:160-271 with fixed16_round_to_int).
+__host__ __device__ inline void draw_row_range(const SwDrawCmd& d, const SwVertex16* v, int32_t height, int32_t& y0,
+	uint32_t& nrows)
+{
+	int32_t mn = v[d.first_vertex].y, mx = mn;
+	for (uint32_t i = 1; i < d.vertex_count; ++i)
+	{
+		const int32_t y = v[d.first_vertex + i].y;
+		mn = y < mn ? y : mn;
+		mx = y > mx ? y : mx;
+	}
+	const int32_t a0 = int32_t(uint32_t(mn) + 0x8000u) >> 16; // + half, 16.16
+	const int32_t b0 = int32_t(uint32_t(mx) + 0x8000u) >> 16;
+	const int32_t a = a0 > 0 ? a0 : 0;
+	const int32_t b = b0 < height ? b0 : height;
+	y0 = a;
+	nrows = b > a ? uint32_t(b - a) : 0u;
+}
+
+// ---- GPU-side surface and draw preparation (prep.cu) ----
+
+// Per candidate polygon (every polygon of the visible leafs, in leaf index order): the surface
+// descriptor and draw of prepare_polygon_surface / build_polygons_surfaces / draw_polygon, before
+// compaction (out_offset, first_vertex and tex_offset are filled by the compaction).
+struct PrepCand
+{
+	SwSurfaceDesc desc;
+	SwDrawCmd draw;
+	uint64_t surface_offset;
+	SwVertex16 v[SW_MAX_POLYGON_VERTICES];
+};
+// What the compaction scans, one compact record per candidate.
+struct PrepKey
+{
+	uint64_t area;       // surface texels
+	uint32_t state;      // 1: the polygon has a surface
+	uint32_t draw_count; // vertices of its draw (0: not drawn)
+	uint32_t row_n;      // rows of its draw, from row_y0
+	int32_t row_y0;
+};
+
+struct PrepArgs
+{
+	const SwMapPolygon* polygons;
+	const float* map_vertices; // xyz
+	const SwViewLeaf* leafs;
+	const uint32_t* leaf_cand_base; // num_leafs + 1: first candidate of each leaf
+	uint32_t num_leafs;
+	uint32_t num_candidates;
+	const uint16_t* leaf_lights;
+	const SwLight* lights;
+	const uint32_t* draw_leaf;      // draw order -> leaf
+	const uint32_t* draw_slot_base; // num_draw_leafs + 1: first draw slot of each drawn leaf
+	uint32_t num_draw_leafs;
+	float mip_bias;
+	float view[16], planes[16]; // column-major
+	uint32_t directional, simple_lightmaps;
+	int32_t height;
+	// draws prepared on the host (skybox), placed first
+	const SwDrawCmd* host_draws;
+	const SwVertex16* host_vertices;
+	const DrawRows* host_rows;
+	uint32_t num_host_draws, num_host_vertices;
+	uint64_t num_host_rows;
+	const SwTextureMip* texture_mips;
+	const SwEmissiveMip* emissive_mips;
+	uint32_t num_texture_mips, num_emissive_mips;
+	uint32_t num_lights;
+	uint64_t num_lightmap_elements; // of the lightmap kind in use
+	PrepCand* cands;
+	PrepKey* keys;
+	// outputs and their capacities
+	SwSurfaceDesc* descs;
+	SurfaceGpu* surfaces;
+	uint64_t* work_prefix; // cap_surfaces + 1
+	SwDrawCmd* draws;
+	SwVertex16* vertices;
+	DrawRows* draw_rows;
+	SwViewCounts* counts;
+	uint32_t cap_surfaces, cap_draws, cap_vertices;
+	uint64_t cap_texels, cap_rows;
+};
+
+// Per-candidate preparation (many CTAs), then one CTA's ordered compaction.
+int launch_prep(const PrepArgs& args, cudaStream_t stream);
 
 // ---- postprocessor / upscaler ----
 

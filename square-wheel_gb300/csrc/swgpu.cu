@@ -12,6 +12,7 @@
 // Host->device uploads go through pinned staging buffers on the context's stream. Every descriptor is
 // validated on the host before launch so that no kernel can read outside its buffers.
 #include "sw_kernels.cuh"
+#include "../host/prep_math.h"
 
 #include "../../include/swlearn.h"
 
@@ -120,6 +121,21 @@ struct SwCtx
 	Staging gstage[2];
 	uint32_t gset = 0;
 
+	// GPU-side surface and draw preparation (sw_set_map, sw_draw_frame_view): the map's polygons and
+	// vertices, per-polygon surface size bounds (prefix sums, for capacities), the candidates' scratch,
+	// the prepared descriptors, the counts (device, and a pinned copy read back after each frame).
+	DevBuf map_polygons, map_vertices, cands, keys, descs, view_counts;
+	uint32_t num_map_polygons = 0, num_map_vertices = 0;
+	std::vector<uint64_t> poly_bound_prefix;
+	SwViewCounts* h_counts = nullptr; // pinned, one per staging set (frames alternate)
+	cudaEvent_t ev_counts[2] = {nullptr, nullptr};
+	bool counts_pending[2] = {false, false};
+	uint64_t counts_seq[2] = {0, 0};
+	uint64_t view_seq = 0, hint_seq = 0;
+	uint64_t view_work_hint = 0; // texels of the latest frame read back (sizes the surface grid)
+	uint32_t view_surfaces_cap = 0, view_draws_cap = 0, view_vertices_cap = 0;
+	cudaGraphExec_t vexec = nullptr;
+
 	// Optional per-stage device timing (sw_enable_timing).
 	bool timing = false;
 	cudaEvent_t t_begin[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -145,6 +161,8 @@ RasterArgs raster_args(SwCtx* ctx)
 	a.draws = static_cast<const SwDrawCmd*>(ctx->draws.ptr);
 	a.vertices = static_cast<const SwVertex16*>(ctx->vertices.ptr);
 	a.num_draws = ctx->num_draws;
+	a.counts = nullptr;
+	a.setup_blocks = 0;
 	a.width = int32_t(ctx->frame.width);
 	a.height = int32_t(ctx->frame.height);
 	a.clear_background = ctx->frame.clear_background;
@@ -431,6 +449,10 @@ int sw_create(const SwCreateInfo* info, SwCtx** out_ctx)
 	if (cudaEventCreateWithFlags(&ctx->average_ready, cudaEventDisableTiming) != cudaSuccess) return bail(SW_ERR_CUDA);
 	if (cudaMallocHost(reinterpret_cast<void**>(&ctx->h_average), 4 * sizeof(float)) != cudaSuccess)
 		return bail(SW_ERR_CUDA);
+	for (cudaEvent_t* e : {&ctx->ev_counts[0], &ctx->ev_counts[1]})
+		if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return bail(SW_ERR_CUDA);
+	if (cudaMallocHost(reinterpret_cast<void**>(&ctx->h_counts), 2 * sizeof(SwViewCounts)) != cudaSuccess) return bail(SW_ERR_CUDA);
+	std::memset(ctx->h_counts, 0, 2 * sizeof(SwViewCounts));
 
 	int r;
 	if ((r = upload_static(ctx, ctx->texels, info->texels, info->num_texels * 8))) return bail(r);
@@ -467,10 +489,15 @@ int sw_destroy(SwCtx* ctx)
 		&ctx->skybox64, &ctx->frame_in,
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->parts, &ctx->part_counts, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
-		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst};
+		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst, &ctx->map_polygons,
+		&ctx->map_vertices, &ctx->cands, &ctx->keys, &ctx->descs, &ctx->view_counts};
 	for (DevBuf* b : bufs) release(*b);
 	for (const SwCtx::HostRange& h : ctx->registered) cudaHostUnregister(h.ptr);
 	if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+	if (ctx->vexec) cudaGraphExecDestroy(ctx->vexec);
+	if (ctx->h_counts) cudaFreeHost(ctx->h_counts);
+	for (cudaEvent_t e : ctx->ev_counts)
+		if (e) cudaEventDestroy(e);
 	Staging* st[] = {&ctx->stage_lights, &ctx->stage_surfaces, &ctx->stage_prefix, &ctx->stage_draws,
 		&ctx->stage_vertices, &ctx->stage_draw_rows, &ctx->stage_io, &ctx->gstage[0], &ctx->gstage[1]};
 	for (Staging* s : st)
@@ -575,6 +602,7 @@ static int launch_surfaces(SwCtx* ctx, const SurfaceInputs* in = nullptr)
 	a.surfaces = in ? in->surfaces : static_cast<const SurfaceGpu*>(ctx->surfaces.ptr);
 	a.work_prefix = in ? in->work_prefix : static_cast<const uint64_t*>(ctx->work_prefix.ptr);
 	a.num_surfaces = ctx->last_num_surfaces;
+	a.counts = nullptr;
 	a.directional = ctx->last_surface_directional ? 1u : 0u;
 	a.total_work = ctx->last_surface_work;
 	a.texels = static_cast<const uint64_t*>(ctx->texels.ptr);
@@ -1139,6 +1167,148 @@ int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, con
 }
 } // namespace
 
+} // extern "C"
+
+namespace
+{
+// The checks of sw_frame_begin for a whole-frame call.
+int check_frame_params(SwCtx* ctx, const SwFrameParams& p, uint32_t num_lights)
+{
+	if (p.pixel_format > SW_PIXEL_C64) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "bad pixel format");
+	if (p.width == 0 || p.height == 0 || p.width > 16384 || p.height > 16384)
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "bad frame size %ux%u", p.width, p.height);
+	if (p.use_directional_lightmaps && ctx->num_dir_lightmap_elements == 0)
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "directional lightmaps requested but none uploaded");
+	if (num_lights > 65535) return fail(ctx, SW_ERR_LIMIT, "too many lights");
+	return SW_OK;
+}
+
+// The frame buffer of the frame's size and format; a new one starts black (postprocessor.rs:56-66),
+// cleared before the graph.
+int ensure_framebuffer(SwCtx* ctx, const SwFrameParams& p)
+{
+	const uint32_t bpp = bpp_of(p.pixel_format);
+	int r;
+	if ((r = ensure(ctx, ctx->framebuffer, size_t(p.width) * p.height * bpp))) return r;
+	if (!ctx->fb_valid || ctx->fb_width != p.width || ctx->fb_height != p.height || ctx->fb_format != p.pixel_format)
+	{
+		SW_CUDA(ctx, cudaMemsetAsync(ctx->framebuffer.ptr, 0, size_t(p.width) * p.height * bpp, ctx->stream));
+		ctx->fb_width = p.width;
+		ctx->fb_height = p.height;
+		ctx->fb_format = p.pixel_format;
+		ctx->fb_valid = true;
+	}
+	return SW_OK;
+}
+
+// Postprocess arguments and destination of a graph frame. A registered host buffer is mapped into the
+// device's address space: the tonemap writes the Color32 rows straight into it (*direct_host). Other
+// host memory gets a device buffer copied out after the frame.
+int frame_post_target(SwCtx* ctx, const SwFrameParams& p, const SwPostConfig& post, const float modulate[3], void* dst,
+	uint32_t dst_pitch, int dst_is_device, PostArgs& pa, void** post_out, bool* direct_host)
+{
+	if (!dst) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocess needs a destination");
+	int r;
+	if ((r = prepare_post(ctx, &post, modulate, pa))) return r;
+	*post_out = dst;
+	*direct_host = false;
+	pa.dst_pitch = dst_pitch;
+	if (!dst_is_device)
+	{
+		void* mapped = registered_device_pointer(ctx, dst, (size_t(p.height) - 1) * dst_pitch * 4 + size_t(p.width) * 4);
+		if (mapped)
+		{
+			*post_out = mapped;
+			*direct_host = true;
+		}
+		else
+		{
+			if ((r = ensure(ctx, ctx->up_dst, size_t(p.width) * p.height * 4))) return r;
+			*post_out = ctx->up_dst.ptr;
+			pa.dst_pitch = p.width;
+		}
+	}
+	pa.dst = static_cast<uint32_t*>(*post_out);
+	return SW_OK;
+}
+
+// Capture the device work `enqueue` issues on the context's streams, update `exec` in place (or
+// instantiate it when the topology changed) and launch it.
+template <class F>
+int capture_and_launch(SwCtx* ctx, cudaGraphExec_t& exec, F&& enqueue)
+{
+	SW_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+	ctx->capturing = true;
+	const int er = enqueue();
+	ctx->capturing = false;
+	cudaGraph_t g = nullptr;
+	const cudaError_t ee = cudaStreamEndCapture(ctx->stream, &g);
+	if (er || ee != cudaSuccess)
+	{
+		if (g) cudaGraphDestroy(g);
+		cudaGetLastError();
+		return er ? er : cuda_fail(ctx, ee, "cudaStreamEndCapture");
+	}
+	if (exec)
+	{
+		cudaGraphExecUpdateResultInfo info;
+		if (cudaGraphExecUpdate(exec, g, &info) != cudaSuccess)
+		{
+			cudaGetLastError(); // the topology changed: instantiate anew
+			cudaGraphExecDestroy(exec);
+			exec = nullptr;
+		}
+	}
+	if (!exec)
+	{
+		const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+		if (ie != cudaSuccess)
+		{
+			cudaGraphDestroy(g);
+			exec = nullptr;
+			return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+		}
+	}
+	cudaGraphDestroy(g);
+	stage_begin(ctx, STAGE_FRAME);
+	SW_CUDA(ctx, cudaGraphLaunch(exec, ctx->stream));
+	stage_end(ctx, STAGE_FRAME);
+	return SW_OK;
+}
+
+// After a graph frame was launched: staging and ordering events, exposure bookkeeping, and the frame
+// into the caller's host memory (a direct-host frame only needs the stream to finish).
+int finish_graph_frame(SwCtx* ctx, Staging& st, const SwFrameParams& p, bool postprocess, const SwPostConfig& post, float dt,
+	void* dst, uint32_t dst_pitch, int dst_is_device, void* post_out, bool direct_host)
+{
+	SW_CUDA(ctx, cudaEventRecord(st.done, ctx->stream));
+	st.pending = true;
+	SW_CUDA(ctx, cudaEventRecord(ctx->ev_tiles, ctx->stream));
+	ctx->tiles_recorded = true;
+	ctx->arena_valid = true;
+	ctx->draws_valid = false;
+	ctx->frame_open = false;
+	if (postprocess)
+	{
+		SW_CUDA(ctx, cudaEventRecord(ctx->average_ready, ctx->stream));
+		ctx->exposure_pending = true;
+		ctx->pending_config = post;
+		ctx->pending_dt = dt;
+		if (direct_host)
+		{
+			SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // the frame is in the caller's buffer on return
+			return SW_OK;
+		}
+		if (!dst_is_device) return copy_out(ctx, dst, dst_pitch, 0, post_out, p.width, p.width, p.height, 4);
+	}
+	else if (dst && !dst_is_device)
+		return copy_out(ctx, dst, dst_pitch, 0, ctx->framebuffer.ptr, p.width, p.width, p.height, bpp_of(p.pixel_format));
+	return SW_OK;
+}
+} // namespace
+
+extern "C" {
+
 int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 {
 	if (!ctx || !in) return SW_ERR_INVALID_ARGUMENT;
@@ -1150,14 +1320,8 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	if (f.dst && f.dst_pitch < f.params.width) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");
 	if (!ctx->graph_enabled) return draw_frame_direct(ctx, f);
 	int r;
-	// frame parameters (the checks of sw_frame_begin)
 	const SwFrameParams& p = f.params;
-	if (p.pixel_format > SW_PIXEL_C64) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "bad pixel format");
-	if (p.width == 0 || p.height == 0 || p.width > 16384 || p.height > 16384)
-		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "bad frame size %ux%u", p.width, p.height);
-	if (p.use_directional_lightmaps && ctx->num_dir_lightmap_elements == 0)
-		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "directional lightmaps requested but none uploaded");
-	if (f.num_lights > 65535) return fail(ctx, SW_ERR_LIMIT, "too many lights");
+	if ((r = check_frame_params(ctx, p, f.num_lights))) return r;
 	SW_CUDA(ctx, cudaSetDevice(ctx->device));
 	ctx->frame = p;
 	ctx->num_lights = f.num_lights;
@@ -1197,107 +1361,349 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	if ((r = ensure(ctx, ctx->surfaces, std::max<size_t>(f.num_surfaces, 1) * sizeof(SurfaceGpu)))) return r;
 	if ((r = ensure(ctx, ctx->work_prefix, (size_t(f.num_surfaces) + 1) * 8))) return r;
 	if ((r = ensure_raster_buffers(ctx, f.num_draws, f.num_vertices, rows))) return r;
-	if ((r = ensure(ctx, ctx->framebuffer, size_t(p.width) * p.height * bpp))) return r;
-	if (!ctx->fb_valid || ctx->fb_width != p.width || ctx->fb_height != p.height || ctx->fb_format != p.pixel_format)
-	{
-		// a new frame buffer starts black (postprocessor.rs:56-66), before the graph
-		SW_CUDA(ctx, cudaMemsetAsync(ctx->framebuffer.ptr, 0, size_t(p.width) * p.height * bpp, ctx->stream));
-		ctx->fb_width = p.width;
-		ctx->fb_height = p.height;
-		ctx->fb_format = p.pixel_format;
-		ctx->fb_valid = true;
-	}
+	if ((r = ensure_framebuffer(ctx, p))) return r;
 	ctx->num_rows = rows;
 	ctx->num_draws = f.num_draws;
 	PostArgs pa;
 	void* post_out = nullptr;
 	bool direct_host = false;
-	if (f.postprocess)
-	{
-		if (!f.dst) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocess needs a destination");
-		if ((r = prepare_post(ctx, &f.post, f.color_modulate, pa))) return r;
-		post_out = f.dst;
-		pa.dst_pitch = f.dst_pitch;
-		if (!f.dst_is_device)
-		{
-			// A registered host buffer is mapped into the device's address space: the tonemap writes the
-			// Color32 rows straight into it. Otherwise it writes to a device buffer copied out after.
-			void* mapped = registered_device_pointer(ctx, f.dst, (size_t(p.height) - 1) * f.dst_pitch * 4 + size_t(p.width) * 4);
-			if (mapped)
-			{
-				post_out = mapped;
-				direct_host = true;
-			}
-			else
-			{
-				if ((r = ensure(ctx, ctx->up_dst, size_t(p.width) * p.height * 4))) return r;
-				post_out = ctx->up_dst.ptr;
-				pa.dst_pitch = p.width;
-			}
-		}
-		pa.dst = static_cast<uint32_t*>(post_out);
-	}
+	if (f.postprocess &&
+		(r = frame_post_target(ctx, p, f.post, f.color_modulate, f.dst, f.dst_pitch, f.dst_is_device, pa, &post_out, &direct_host)))
+		return r;
 
 	// 3. capture the device work and update (or instantiate) the frame graph
-	SW_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-	ctx->capturing = true;
-	const int er = enqueue_frame(ctx, f, h, off, rows, f.postprocess ? &pa : nullptr);
-	ctx->capturing = false;
-	cudaGraph_t g = nullptr;
-	const cudaError_t ee = cudaStreamEndCapture(ctx->stream, &g);
-	if (er || ee != cudaSuccess)
-	{
-		if (g) cudaGraphDestroy(g);
-		cudaGetLastError();
-		return er ? er : cuda_fail(ctx, ee, "cudaStreamEndCapture");
-	}
-	if (ctx->gexec)
-	{
-		cudaGraphExecUpdateResultInfo info;
-		if (cudaGraphExecUpdate(ctx->gexec, g, &info) != cudaSuccess)
-		{
-			cudaGetLastError(); // the topology changed: instantiate anew
-			cudaGraphExecDestroy(ctx->gexec);
-			ctx->gexec = nullptr;
-		}
-	}
-	if (!ctx->gexec)
-	{
-		const cudaError_t ie = cudaGraphInstantiate(&ctx->gexec, g, 0);
-		if (ie != cudaSuccess)
-		{
-			cudaGraphDestroy(g);
-			ctx->gexec = nullptr;
-			return cuda_fail(ctx, ie, "cudaGraphInstantiate");
-		}
-	}
-	cudaGraphDestroy(g);
-	stage_begin(ctx, STAGE_FRAME);
-	SW_CUDA(ctx, cudaGraphLaunch(ctx->gexec, ctx->stream));
-	stage_end(ctx, STAGE_FRAME);
-	SW_CUDA(ctx, cudaEventRecord(st.done, ctx->stream));
-	st.pending = true;
-	SW_CUDA(ctx, cudaEventRecord(ctx->ev_tiles, ctx->stream));
-	ctx->tiles_recorded = true;
-	ctx->arena_valid = true;
-	ctx->draws_valid = false;
-	ctx->frame_open = false;
+	if ((r = capture_and_launch(ctx, ctx->gexec, [&]() { return enqueue_frame(ctx, f, h, off, rows, f.postprocess ? &pa : nullptr); })))
+		return r;
 	ctx->stats.draws += f.num_draws; // (surfaces are counted by launch_surfaces)
-	if (f.postprocess)
+	return finish_graph_frame(ctx, st, p, f.postprocess != 0, f.post, f.frame_duration_s, f.dst, f.dst_pitch, f.dst_is_device,
+		post_out, direct_host);
+}
+
+int sw_set_map(SwCtx* ctx, const SwMapPolygon* polygons, uint32_t num_polygons, const float* vertices, uint32_t num_vertices)
+{
+	if (!ctx || (num_polygons && !polygons) || (num_vertices && !vertices)) return SW_ERR_INVALID_ARGUMENT;
+	const uint64_t simple = ctx->num_lightmap_elements, directional = ctx->num_dir_lightmap_elements;
+	std::vector<uint64_t> prefix(size_t(num_polygons) + 1, 0);
+	for (uint32_t i = 0; i < num_polygons; ++i)
 	{
-		SW_CUDA(ctx, cudaEventRecord(ctx->average_ready, ctx->stream));
-		ctx->exposure_pending = true;
-		ctx->pending_config = f.post;
-		ctx->pending_dt = f.frame_duration_s;
-		if (direct_host)
+		const SwMapPolygon& p = polygons[i];
+		if (uint64_t(p.first_vertex) + p.num_vertices > num_vertices)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "polygon %u: vertices out of range", i);
+		if (p.tex_coord_min[0] > p.tex_coord_max[0] || p.tex_coord_min[1] > p.tex_coord_max[1])
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "polygon %u: bad texture coordinate bounds", i);
+		if ((p.flags & SW_POLY_DIFFUSE_LAYER) && uint64_t(p.texture) * 5 + 4 >= ctx->h_texture_mips.size())
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "polygon %u: bad texture", i);
+		if (p.emissive_texture != SW_NO_EMISSIVE && uint64_t(p.emissive_texture) * 5 + 4 >= ctx->h_emissive_mips.size())
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "polygon %u: bad emissive texture", i);
+		if (p.blending_mode > SW_BLEND_ALPHA_BLEND) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "polygon %u: bad blending mode", i);
+		if ((p.flags & SW_POLY_DIFFUSE_LAYER) && p.lightmap_data_offset != SW_NO_LIGHTMAP)
 		{
-			SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // the frame is in the caller's buffer on return
-			return SW_OK;
+			// get_polygon_lightmap_size, lightmap.rs:11-27; every surface of the polygon reads inside it
+			const uint64_t lw = uint64_t(int64_t((p.tex_coord_max[0] + 15) >> 4) - (p.tex_coord_min[0] >> 4) + 1);
+			const uint64_t lh = uint64_t(int64_t((p.tex_coord_max[1] + 15) >> 4) - (p.tex_coord_min[1] >> 4) + 1);
+			const uint64_t end = uint64_t(p.lightmap_data_offset) + lw * lh;
+			if ((simple > 1 && end > simple) || (directional > 1 && end > directional))
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "polygon %u: lightmap out of range", i);
 		}
-		if (!f.dst_is_device) return copy_out(ctx, f.dst, f.dst_pitch, 0, post_out, p.width, p.width, p.height, 4);
+		prefix[i + 1] = prefix[i] + swhost::max_surface_texels(p);
 	}
-	else if (f.dst && !f.dst_is_device)
-		return copy_out(ctx, f.dst, f.dst_pitch, 0, ctx->framebuffer.ptr, p.width, p.width, p.height, bpp);
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	if (ctx->aux) SW_CUDA(ctx, cudaStreamSynchronize(ctx->aux));
+	int r;
+	if ((r = upload_static(ctx, ctx->map_polygons, polygons, size_t(num_polygons) * sizeof(SwMapPolygon)))) return r;
+	if ((r = upload_static(ctx, ctx->map_vertices, vertices, size_t(num_vertices) * 12))) return r;
+	ctx->num_map_polygons = num_polygons;
+	ctx->num_map_vertices = num_vertices;
+	ctx->poly_bound_prefix.swap(prefix);
+	return SW_OK;
+}
+
+namespace
+{
+// Counts of a finished view frame (staging set `slot`): statistics and the surface grid size.
+void consume_view_counts(SwCtx* ctx, uint32_t slot)
+{
+	const SwViewCounts& k = ctx->h_counts[slot];
+	ctx->counts_pending[slot] = false;
+	ctx->stats.surfaces += k.num_surfaces;
+	ctx->stats.surface_texels += k.total_texels;
+	ctx->stats.draws += k.num_draws;
+	if (ctx->counts_seq[slot] > ctx->hint_seq)
+	{
+		ctx->view_work_hint = k.total_texels;
+		ctx->hint_seq = ctx->counts_seq[slot];
+	}
+}
+} // namespace
+
+int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
+{
+	if (!ctx || !in) return SW_ERR_INVALID_ARGUMENT;
+	const SwViewFrameInput& f = *in;
+	if ((f.num_lights && !f.lights) || (f.num_leafs && !f.leafs) || (f.num_leaf_lights && !f.leaf_lights) ||
+		(f.num_draws && (!f.draws || !f.vertices)))
+		return SW_ERR_INVALID_ARGUMENT;
+	if (f.postprocess && f.params.pixel_format != SW_PIXEL_C64)
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocessing needs a colour64 frame");
+	if (f.dst && f.dst_pitch < f.params.width) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");
+	int r;
+	const SwFrameParams& p = f.params;
+	if ((r = check_frame_params(ctx, p, f.num_lights))) return r;
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	for (uint32_t k = 0; k < 2; ++k)
+		if (ctx->counts_pending[k] && cudaEventQuery(ctx->ev_counts[k]) == cudaSuccess) consume_view_counts(ctx, k);
+	cudaGetLastError(); // a not-ready query is not an error
+
+	// 1. validate the leafs and derive the candidate and draw-slot numbering and the capacities
+	const uint32_t nl = f.num_leafs;
+	std::vector<uint32_t> draw_leaf(nl, 0xFFFFFFFFu);
+	uint32_t num_draw_leafs = 0;
+	uint64_t candidates = 0, slots = 0, texel_bound = 0, row_bound = 0;
+	for (uint32_t i = 0; i < nl; ++i)
+	{
+		const SwViewLeaf& l = f.leafs[i];
+		if (uint64_t(l.first_polygon) + l.num_polygons > ctx->num_map_polygons)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "leaf %u: polygons out of range (sw_set_map)", i);
+		if (uint64_t(l.first_light) + l.num_lights > f.num_leaf_lights)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "leaf %u: lights out of range", i);
+		candidates += l.num_polygons;
+		texel_bound += ctx->poly_bound_prefix[l.first_polygon + l.num_polygons] - ctx->poly_bound_prefix[l.first_polygon];
+		if (l.draw_order != SW_LEAF_NOT_DRAWN)
+		{
+			if (l.draw_order >= nl || draw_leaf[l.draw_order] != 0xFFFFFFFFu)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "leaf %u: bad draw order", i);
+			draw_leaf[l.draw_order] = i;
+			++num_draw_leafs;
+			slots += l.num_polygons;
+			// rows of a draw lie in the leaf's draw bounds: y in [planes[3].c, -planes[2].c] (+ rounding)
+			const float y_min = l.draw_clip_planes[3][2], y_max = -l.draw_clip_planes[2][2];
+			uint64_t rows = p.height;
+			if (y_min == y_min && y_max == y_max && y_max - y_min < float(p.height))
+				rows = std::min<uint64_t>(p.height, uint64_t(std::max(0.0f, std::ceil(y_max - y_min))) + 2);
+			row_bound += uint64_t(l.num_polygons) * rows;
+		}
+	}
+	for (uint32_t j = 0; j < num_draw_leafs; ++j)
+		if (draw_leaf[j] == 0xFFFFFFFFu) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw order has a gap at %u", j);
+	for (uint32_t i = 0; i < f.num_leaf_lights; ++i)
+		if (f.leaf_lights[i] >= f.num_lights) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "leaf light %u: bad light index", i);
+	if (candidates > 0x7FFFFFFFull) return fail(ctx, SW_ERR_LIMIT, "too many polygons in the visible leafs");
+	for (uint32_t i = 0; i < f.num_draws; ++i)
+		if (f.draws[i].tex_source != SW_TEXSRC_SKYBOX)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: host draws of a view frame read the skybox", i);
+	ctx->frame = p;
+	ctx->num_lights = f.num_lights;
+	const uint64_t cap_draws = uint64_t(f.num_draws) + slots;
+	const uint64_t cap_vertices = uint64_t(f.num_vertices) + slots * SW_MAX_POLYGON_VERTICES;
+	if (cap_draws > 0x7FFFFFFFull || cap_vertices > 0x7FFFFFFFull) return fail(ctx, SW_ERR_LIMIT, "too many draws");
+
+	// 2. every per-frame array into one pinned staging block (two blocks alternate between frames)
+	const uint32_t slot = ctx->gset;
+	Staging& st = ctx->gstage[slot];
+	ctx->gset ^= 1u;
+	size_t off[10];
+	off[0] = 0;
+	off[1] = align_up(off[0] + std::max<size_t>(f.num_lights, 1) * sizeof(SwLight), 256);
+	off[2] = align_up(off[1] + std::max<size_t>(nl, 1) * sizeof(SwViewLeaf), 256);
+	off[3] = align_up(off[2] + (size_t(nl) + 1) * 4, 256);
+	off[4] = align_up(off[3] + std::max<size_t>(f.num_leaf_lights, 1) * 2, 256);
+	off[5] = align_up(off[4] + std::max<size_t>(num_draw_leafs, 1) * 4, 256);
+	off[6] = align_up(off[5] + (size_t(num_draw_leafs) + 1) * 4, 256);
+	off[7] = align_up(off[6] + std::max<size_t>(f.num_draws, 1) * sizeof(SwDrawCmd), 256);
+	off[8] = align_up(off[7] + std::max<size_t>(f.num_vertices, 1) * sizeof(SwVertex16), 256);
+	off[9] = align_up(off[8] + std::max<size_t>(f.num_draws, 1) * sizeof(DrawRows), 256);
+	void* hv = nullptr;
+	if ((r = staging_acquire(ctx, st, off[9], &hv))) return r;
+	if (ctx->counts_pending[slot])
+	{
+		// the frame that last used this staging set has finished (staging_acquire waited for it)
+		SW_CUDA(ctx, cudaEventSynchronize(ctx->ev_counts[slot]));
+		consume_view_counts(ctx, slot);
+	}
+	unsigned char* h = static_cast<unsigned char*>(hv);
+	if (f.num_lights) std::memcpy(h + off[0], f.lights, f.num_lights * sizeof(SwLight));
+	if (nl) std::memcpy(h + off[1], f.leafs, nl * sizeof(SwViewLeaf));
+	uint32_t* cand_base = reinterpret_cast<uint32_t*>(h + off[2]);
+	cand_base[0] = 0;
+	for (uint32_t i = 0; i < nl; ++i) cand_base[i + 1] = cand_base[i] + f.leafs[i].num_polygons;
+	if (f.num_leaf_lights) std::memcpy(h + off[3], f.leaf_lights, f.num_leaf_lights * 2);
+	uint32_t* dl = reinterpret_cast<uint32_t*>(h + off[4]);
+	uint32_t* slot_base = reinterpret_cast<uint32_t*>(h + off[5]);
+	slot_base[0] = 0;
+	for (uint32_t j = 0; j < num_draw_leafs; ++j)
+	{
+		dl[j] = draw_leaf[j];
+		slot_base[j + 1] = slot_base[j] + f.leafs[draw_leaf[j]].num_polygons;
+	}
+	uint64_t host_rows = 0;
+	if ((r = prepare_draws(ctx, f.draws, f.num_draws, f.vertices, f.num_vertices, reinterpret_cast<DrawRows*>(h + off[8]),
+			 &host_rows)))
+		return r;
+	if (f.num_draws) std::memcpy(h + off[6], f.draws, f.num_draws * sizeof(SwDrawCmd));
+	if (f.num_vertices) std::memcpy(h + off[7], f.vertices, f.num_vertices * sizeof(SwVertex16));
+	const uint64_t cap_rows = host_rows + row_bound;
+	const uint64_t cap_surfaces = std::max<uint64_t>(candidates, 1);
+	const uint64_t cap_texels = std::max<uint64_t>(texel_bound, 1);
+
+	// 3. device buffers at their capacities (growing them synchronises)
+	const uint32_t bpp = bpp_of(p.pixel_format);
+	if ((r = ensure(ctx, ctx->frame_in, off[9]))) return r;
+	if ((r = ensure(ctx, ctx->cands, std::max<size_t>(candidates, 1) * sizeof(PrepCand)))) return r;
+	if ((r = ensure(ctx, ctx->keys, std::max<size_t>(candidates, 1) * sizeof(PrepKey)))) return r;
+	if ((r = ensure(ctx, ctx->descs, cap_surfaces * sizeof(SwSurfaceDesc)))) return r;
+	if ((r = ensure(ctx, ctx->surfaces, cap_surfaces * sizeof(SurfaceGpu)))) return r;
+	if ((r = ensure(ctx, ctx->work_prefix, (cap_surfaces + 1) * 8))) return r;
+	if ((r = ensure(ctx, ctx->arena, cap_texels * bpp))) return r;
+	if ((r = ensure(ctx, ctx->view_counts, sizeof(SwViewCounts)))) return r;
+	if ((r = ensure_raster_buffers(ctx, uint32_t(cap_draws), uint32_t(cap_vertices), cap_rows))) return r;
+	if ((r = ensure_framebuffer(ctx, p))) return r;
+	ctx->arena_texels = cap_texels;
+	ctx->arena_format = p.pixel_format;
+	ctx->view_surfaces_cap = uint32_t(cap_surfaces);
+	ctx->view_draws_cap = uint32_t(cap_draws);
+	ctx->view_vertices_cap = uint32_t(cap_vertices);
+	PostArgs pa;
+	void* post_out = nullptr;
+	bool direct_host = false;
+	if (f.postprocess &&
+		(r = frame_post_target(ctx, p, f.post, f.color_modulate, f.dst, f.dst_pitch, f.dst_is_device, pa, &post_out, &direct_host)))
+		return r;
+
+	// 4. the graph: one upload, preparation, surface build beside the raster setup, tiles, postprocess
+	unsigned char* d = static_cast<unsigned char*>(ctx->frame_in.ptr);
+	SwViewCounts* counts = static_cast<SwViewCounts*>(ctx->view_counts.ptr);
+	PrepArgs pr;
+	pr.polygons = static_cast<const SwMapPolygon*>(ctx->map_polygons.ptr);
+	pr.map_vertices = static_cast<const float*>(ctx->map_vertices.ptr);
+	pr.leafs = reinterpret_cast<const SwViewLeaf*>(d + off[1]);
+	pr.leaf_cand_base = reinterpret_cast<const uint32_t*>(d + off[2]);
+	pr.num_leafs = nl;
+	pr.num_candidates = uint32_t(candidates);
+	pr.leaf_lights = reinterpret_cast<const uint16_t*>(d + off[3]);
+	pr.lights = reinterpret_cast<const SwLight*>(d + off[0]);
+	pr.draw_leaf = reinterpret_cast<const uint32_t*>(d + off[4]);
+	pr.draw_slot_base = reinterpret_cast<const uint32_t*>(d + off[5]);
+	pr.num_draw_leafs = num_draw_leafs;
+	pr.mip_bias = f.mip_bias;
+	std::memcpy(pr.view, f.view_matrix, sizeof(pr.view));
+	std::memcpy(pr.planes, f.planes_matrix, sizeof(pr.planes));
+	pr.directional = p.use_directional_lightmaps ? 1u : 0u;
+	pr.simple_lightmaps = ctx->num_lightmap_elements > 1 ? 1u : 0u;
+	pr.height = int32_t(p.height);
+	pr.host_draws = reinterpret_cast<const SwDrawCmd*>(d + off[6]);
+	pr.host_vertices = reinterpret_cast<const SwVertex16*>(d + off[7]);
+	pr.host_rows = reinterpret_cast<const DrawRows*>(d + off[8]);
+	pr.num_host_draws = f.num_draws;
+	pr.num_host_vertices = f.num_vertices;
+	pr.num_host_rows = host_rows;
+	pr.texture_mips = static_cast<const SwTextureMip*>(ctx->texture_mips.ptr);
+	pr.emissive_mips = static_cast<const SwEmissiveMip*>(ctx->emissive_mips.ptr);
+	pr.num_texture_mips = uint32_t(ctx->h_texture_mips.size());
+	pr.num_emissive_mips = uint32_t(ctx->h_emissive_mips.size());
+	pr.num_lights = f.num_lights;
+	pr.num_lightmap_elements = p.use_directional_lightmaps ? ctx->num_dir_lightmap_elements : ctx->num_lightmap_elements;
+	pr.cands = static_cast<PrepCand*>(ctx->cands.ptr);
+	pr.keys = static_cast<PrepKey*>(ctx->keys.ptr);
+	pr.descs = static_cast<SwSurfaceDesc*>(ctx->descs.ptr);
+	pr.surfaces = static_cast<SurfaceGpu*>(ctx->surfaces.ptr);
+	pr.work_prefix = static_cast<uint64_t*>(ctx->work_prefix.ptr);
+	pr.draws = static_cast<SwDrawCmd*>(ctx->draws.ptr);
+	pr.vertices = static_cast<SwVertex16*>(ctx->vertices.ptr);
+	pr.draw_rows = static_cast<DrawRows*>(ctx->draw_rows.ptr);
+	pr.counts = counts;
+	pr.cap_surfaces = uint32_t(cap_surfaces);
+	pr.cap_draws = uint32_t(cap_draws);
+	pr.cap_vertices = uint32_t(cap_vertices);
+	pr.cap_texels = cap_texels;
+	pr.cap_rows = cap_rows;
+
+	SurfaceKernelArgs sa;
+	sa.surfaces = pr.surfaces;
+	sa.work_prefix = pr.work_prefix;
+	sa.num_surfaces = 0;
+	sa.directional = p.use_directional_lightmaps ? 1u : 0u;
+	sa.total_work = 0;
+	sa.counts = counts;
+	sa.texels = static_cast<const uint64_t*>(ctx->texels.ptr);
+	sa.emissive_pixels = static_cast<const uint32_t*>(ctx->emissive.ptr);
+	sa.lightmaps = static_cast<const float*>(ctx->lightmaps.ptr);
+	sa.directional_lightmaps = static_cast<const SwDirectionalLightmapElement*>(ctx->dir_lightmaps.ptr);
+	sa.lights = pr.lights;
+	for (int i = 0; i < 3; ++i) sa.cam_pos[i] = p.cam_pos[i];
+	sa.arena = ctx->arena.ptr;
+	// grid: the last frame's texels with headroom (the kernel strides over whatever this frame has)
+	const uint64_t hint = ctx->view_work_hint ? ctx->view_work_hint + ctx->view_work_hint / 4 : (uint64_t(1) << 40);
+
+	RasterArgs ra = raster_args(ctx);
+	ra.counts = counts;
+	ra.num_draws = 0;
+	ra.setup_blocks = uint32_t(std::min<uint64_t>(cap_draws, uint64_t(ctx->num_sms) * 2));
+	ra.total_rows = uint32_t(std::min<uint64_t>(cap_rows, 0xFFFFFFFFull));
+
+	auto enqueue = [&]() -> int {
+		cudaStream_t s = ctx->stream, aux = ctx->aux;
+		SW_CUDA(ctx, cudaMemcpyAsync(d, h, off[9], cudaMemcpyHostToDevice, s));
+		int rr;
+		if ((rr = check_kernel(ctx, launch_prep(pr, s), "surface and draw preparation"))) return rr;
+		SW_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
+		SW_CUDA(ctx, cudaStreamWaitEvent(aux, ctx->ev_fork, 0));
+		if ((rr = check_kernel(ctx, launch_raster_setup(ra, aux), "raster setup"))) return rr;
+		SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, aux));
+		if ((rr = check_kernel(ctx,
+				 launch_surface_build(sa, p.pixel_format, ctx->num_sms, int(ctx->tuning.surface_blocks_per_sm), s, hint),
+				 "surface build")))
+			return rr;
+		SW_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_setup, 0));
+		if ((rr = check_kernel(ctx, launch_raster_tiles(ra, p.pixel_format, ctx->tuning.raster_tile, s), "raster"))) return rr;
+		if (f.postprocess)
+		{
+			if ((rr = check_kernel(ctx, launch_postprocess(pa, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join), "postprocess")))
+				return rr;
+			SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_average, ctx->average.ptr, 16, cudaMemcpyDeviceToHost, s));
+		}
+		else if (f.dst && f.dst_is_device)
+			SW_CUDA(ctx, cudaMemcpy2DAsync(f.dst, size_t(f.dst_pitch) * bpp, ctx->framebuffer.ptr, size_t(p.width) * bpp,
+							 size_t(p.width) * bpp, p.height, cudaMemcpyDeviceToDevice, s));
+		SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_counts + slot, counts, sizeof(SwViewCounts), cudaMemcpyDeviceToHost, s));
+		return SW_OK;
+	};
+	if ((r = capture_and_launch(ctx, ctx->vexec, enqueue))) return r;
+	SW_CUDA(ctx, cudaEventRecord(ctx->ev_counts[slot], ctx->stream));
+	ctx->counts_pending[slot] = true;
+	ctx->counts_seq[slot] = ++ctx->view_seq;
+	ctx->last_num_surfaces = 0; // sw_rebuild_surfaces has no host descriptors of this frame
+	ctx->last_surface_work = 0;
+	r = finish_graph_frame(ctx, st, p, f.postprocess != 0, f.post, f.frame_duration_s, f.dst, f.dst_pitch, f.dst_is_device,
+		post_out, direct_host);
+	if (r) return r;
+	if (cudaEventQuery(ctx->ev_counts[slot]) == cudaSuccess)
+	{
+		consume_view_counts(ctx, slot);
+		if (ctx->h_counts[slot].error) return fail(ctx, SW_ERR_LIMIT, "GPU-side preparation exceeded a capacity");
+	}
+	cudaGetLastError();
+	return SW_OK;
+}
+
+int sw_read_view_prep(SwCtx* ctx, SwViewCounts* out_counts, SwSurfaceDesc* surfaces, uint32_t max_surfaces, SwDrawCmd* draws,
+	uint32_t max_draws, SwVertex16* vertices, uint32_t max_vertices)
+{
+	if (!ctx || !out_counts) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->view_counts.ptr) return fail(ctx, SW_ERR_STATE, "no sw_draw_frame_view yet");
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	for (uint32_t k = 0; k < 2; ++k)
+		if (ctx->counts_pending[k]) consume_view_counts(ctx, k);
+	SwViewCounts k;
+	SW_CUDA(ctx, cudaMemcpy(&k, ctx->view_counts.ptr, sizeof(k), cudaMemcpyDeviceToHost));
+	*out_counts = k;
+	const uint32_t ns = std::min(std::min(max_surfaces, k.num_surfaces), ctx->view_surfaces_cap);
+	const uint32_t nd = std::min(std::min(max_draws, k.num_draws), ctx->view_draws_cap);
+	const uint32_t nv = std::min(std::min(max_vertices, k.num_vertices), ctx->view_vertices_cap);
+	if (surfaces && ns) SW_CUDA(ctx, cudaMemcpy(surfaces, ctx->descs.ptr, size_t(ns) * sizeof(SwSurfaceDesc), cudaMemcpyDeviceToHost));
+	if (draws && nd) SW_CUDA(ctx, cudaMemcpy(draws, ctx->draws.ptr, size_t(nd) * sizeof(SwDrawCmd), cudaMemcpyDeviceToHost));
+	if (vertices && nv) SW_CUDA(ctx, cudaMemcpy(vertices, ctx->vertices.ptr, size_t(nv) * sizeof(SwVertex16), cudaMemcpyDeviceToHost));
 	return SW_OK;
 }
 
@@ -1380,12 +1786,14 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 
 int sw_abi_layout(uint32_t* sizes, uint32_t count)
 {
-	const uint32_t s[13] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
+	const uint32_t s[17] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
 		uint32_t(sizeof(SwDirectionalLightmapElement)), uint32_t(sizeof(SwLight)), uint32_t(sizeof(SwSurfaceDesc)),
 		uint32_t(sizeof(SwVertex16)), uint32_t(sizeof(SwDrawCmd)), uint32_t(sizeof(SwFrameParams)),
-		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats)), uint32_t(sizeof(SwFrameInput)), uint32_t(sizeof(SwTuning))};
-	for (uint32_t i = 0; sizes && i < count && i < 13; ++i) sizes[i] = s[i];
-	return 13;
+		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats)), uint32_t(sizeof(SwFrameInput)), uint32_t(sizeof(SwTuning)),
+		uint32_t(sizeof(SwMapPolygon)), uint32_t(sizeof(SwViewLeaf)), uint32_t(sizeof(SwViewFrameInput)),
+		uint32_t(sizeof(SwViewCounts))};
+	for (uint32_t i = 0; sizes && i < count && i < 17; ++i) sizes[i] = s[i];
+	return 17;
 }
 
 int sw_get_stats(SwCtx* ctx, SwStats* out)

@@ -11,229 +11,10 @@ namespace swhost
 namespace
 {
 
-constexpr uint32_t MAX_VERTICES = SW_MAX_POLYGON_VERTICES; // renderer_utils.rs:4
-constexpr float Z_NEAR = 1.0f;                             // renderer_utils.rs:7
-constexpr float TC_ERROR_THRESHOLD = 0.75f;                // renderer_utils.rs:199
+constexpr uint32_t MAX_VERTICES = PREP_MAX_VERTICES;
+constexpr float Z_NEAR = PREP_Z_NEAR;
 constexpr uint32_t MAX_POLYGON_LIGHTS = SW_MAX_POLYGON_LIGHTS;
-constexpr uint32_t MAX_BSP_TREE_DEPTH = 72;                // bsp_builder.rs:53
-constexpr uint32_t MAX_MIP = 4;
-
-// f32 -> integer `as` casts: truncating, saturating, NaN -> 0.
-int32_t as_i32(float x)
-{
-	if (x != x) return 0;
-	if (x >= 2147483648.0f) return INT32_MAX;
-	if (x <= -2147483648.0f) return INT32_MIN;
-	return int32_t(x);
-}
-
-// clip_3d_polygon_by_z_plane, clipping.rs:4-51
-Vec3 line_z_intersection(Vec3 v0, Vec3 v1, float z)
-{
-	const float dist0 = v0.z - z, dist1 = v1.z - z, dist_sum = v1.z - v0.z;
-	const float k0 = dist0 / dist_sum, k1 = dist1 / dist_sum;
-	return v0 * k1 - v1 * k0;
-}
-uint32_t clip_3d_polygon_by_z_plane(const Vec3* polygon, uint32_t n, float z_dist, Vec3* out, uint32_t out_cap)
-{
-	if (n == 0) return 0;
-	const Vec3* prev_v = &polygon[n - 1];
-	uint32_t count = 0;
-	for (uint32_t i = 0; i < n; ++i)
-	{
-		const Vec3& v = polygon[i];
-		if (v.z > z_dist)
-		{
-			if (prev_v->z < z_dist)
-			{
-				out[count++] = line_z_intersection(*prev_v, v, z_dist);
-				if (count == out_cap) break;
-			}
-			out[count++] = v;
-			if (count == out_cap) break;
-		}
-		else if (v.z == z_dist)
-		{
-			out[count++] = v;
-			if (count == out_cap) break;
-		}
-		else if (prev_v->z > z_dist)
-		{
-			out[count++] = line_z_intersection(*prev_v, v, z_dist);
-			if (count == out_cap) break;
-		}
-		prev_v = &v;
-	}
-	return count;
-}
-
-// clip_2d_polygon, clipping.rs:115-175
-Vec2 line_line_intersection(Vec2 v0, Vec2 v1, Vec3 line)
-{
-	const float dist0 = dot(v0, v2(line.x, line.y)) - line.z;
-	const float dist1 = dot(v1, v2(line.x, line.y)) - line.z;
-	const float dist_sum = dist1 - dist0;
-	const float k0 = dist0 / dist_sum, k1 = dist1 / dist_sum;
-	return v0 * k1 - v1 * k0;
-}
-uint32_t clip_2d_polygon(const Vec2* polygon, uint32_t n, Vec3 line, Vec2* out, uint32_t out_cap)
-{
-	const Vec2* prev_v = &polygon[n - 1];
-	float prev_dist = dot(*prev_v, v2(line.x, line.y)) - line.z;
-	uint32_t count = 0;
-	for (uint32_t i = 0; i < n; ++i)
-	{
-		const Vec2& v = polygon[i];
-		const float dist = dot(v, v2(line.x, line.y)) - line.z;
-		if (dist > 0.0f)
-		{
-			if (prev_dist < 0.0f)
-			{
-				out[count++] = line_line_intersection(*prev_v, v, line);
-				if (count == out_cap) break;
-			}
-			out[count++] = v;
-			if (count == out_cap) break;
-		}
-		else if (dist == 0.0f)
-		{
-			out[count++] = v;
-			if (count == out_cap) break;
-		}
-		else if (prev_dist > 0.0f)
-		{
-			out[count++] = line_line_intersection(*prev_v, v, line);
-			if (count == out_cap) break;
-		}
-		prev_v = &v;
-		prev_dist = dist;
-	}
-	return count;
-}
-
-// project_and_clip_polygon, renderer_utils.rs:10-58
-uint32_t project_and_clip_polygon(const Vec3 clip_planes[8], const Vec3* vertices_transformed, uint32_t n, Vec2* out)
-{
-	uint32_t count = std::min(n, MAX_VERTICES);
-	Vec3 z_clipped[MAX_VERTICES];
-	count = clip_3d_polygon_by_z_plane(vertices_transformed, count, Z_NEAR, z_clipped, MAX_VERTICES);
-	if (count < 3) return count;
-	for (uint32_t i = 0; i < count; ++i) out[i] = v2(z_clipped[i].x, z_clipped[i].y) / z_clipped[i].z;
-	Vec2 temp[MAX_VERTICES];
-	for (uint32_t i = 0; i < 4; ++i)
-	{
-		count = clip_2d_polygon(out, count, clip_planes[i * 2], temp, MAX_VERTICES);
-		if (count < 3) return count;
-		count = clip_2d_polygon(temp, count, clip_planes[i * 2 + 1], out, MAX_VERTICES);
-		if (count < 3) return count;
-	}
-	return count;
-}
-
-// affine_texture_coordinates_interpolation_may_be_used, renderer_utils.rs:60-132
-bool affine_may_be_used(const DepthEquation& de, const TexCoordEquation& te, Vec2 min_p, Vec2 max_p)
-{
-	const Vec2 edge = max_p - min_p;
-	const float edge_square_len = dot(edge, edge);
-	if (edge_square_len == 0.0f) return true;
-	const float edge_len = std::sqrt(edge_square_len);
-	const Vec2 edge_vec_normalized = edge / edge_len;
-	const float inv_z_clamp = 1.0f / float(1 << 20);
-	const float min_point_inv_z = std::fmax(de.sample(min_p), inv_z_clamp);
-	const float max_point_inv_z = std::fmax(de.sample(max_p), inv_z_clamp);
-	(void)max_point_inv_z;
-	const float a = dot(v2(de.d_inv_z_dx, de.d_inv_z_dy), edge_vec_normalized);
-	const float b = min_point_inv_z;
-	if (std::fabs(a) < 1.0e-10f) return true;
-	const float b_div_a = b / a;
-	const float max_diff_point = std::sqrt((0.0f + b_div_a) * (edge_len + b_div_a)) - b_div_a;
-	const float max_diff_point_inv_z = a * max_diff_point + b;
-	for (int i = 0; i < 2; ++i)
-	{
-		const float min_point_tc = te.d_tc_dx[i] * min_p.x + te.d_tc_dy[i] * min_p.y + te.k[i];
-		const float max_point_tc = te.d_tc_dx[i] * max_p.x + te.d_tc_dy[i] * max_p.y + te.k[i];
-		const float tc_a = dot(v2(te.d_tc_dx[i], te.d_tc_dy[i]), edge_vec_normalized);
-		const float tc_b = min_point_tc;
-		const float min_point_tc_z_mul = min_point_tc / min_point_inv_z;
-		const float max_point_tc_z_mul = max_point_tc / std::fmax(de.sample(max_p), inv_z_clamp);
-		const float real = (tc_a * max_diff_point + tc_b) / max_diff_point_inv_z;
-		const float approx =
-			min_point_tc_z_mul + (max_point_tc_z_mul - min_point_tc_z_mul) * (max_diff_point - 0.0f) / (edge_len - 0.0f);
-		if (std::fabs(real - approx) > TC_ERROR_THRESHOLD) return false;
-	}
-	return true;
-}
-
-// line_z_corrected_texture_coordinates_interpolation_may_be_used, renderer_utils.rs:134-197
-bool line_z_may_be_used(const DepthEquation& de, const TexCoordEquation& te, Vec2 max_p, float min_x, float max_x)
-{
-	if (max_x - min_x < 1.0f) return true;
-	const float a = de.d_inv_z_dx;
-	const float b = de.d_inv_z_dy * max_p.y + de.k;
-	if (std::fabs(a) < 1.0e-10f) return true;
-	const float b_div_a = b / a;
-	const float max_diff_x = std::sqrt((min_x + b_div_a) * (max_x + b_div_a)) - b_div_a;
-	const float max_diff_point_inv_z = a * max_diff_x + b;
-	const float inv_z_at_min_x = a * min_x + b;
-	const float inv_z_at_max_x = a * max_x + b;
-	const float almost_zero = 1e-20f;
-	if (inv_z_at_min_x <= almost_zero || inv_z_at_max_x <= almost_zero || max_diff_point_inv_z <= almost_zero) return false;
-	for (int i = 0; i < 2; ++i)
-	{
-		const float ta = te.d_tc_dx[i];
-		const float tb = te.d_tc_dy[i] * max_p.y + te.k[i];
-		const float tc_at_min_x = (ta * min_x + tb) / inv_z_at_min_x;
-		const float tc_at_max_x = (ta * max_x + tb) / inv_z_at_max_x;
-		const float real = (ta * max_diff_x + tb) / max_diff_point_inv_z;
-		const float approx = tc_at_min_x + (tc_at_max_x - tc_at_min_x) * (max_diff_x - min_x) / (max_x - min_x);
-		if (std::fabs(real - approx) > TC_ERROR_THRESHOLD) return false;
-	}
-	return true;
-}
-
-// calculate_mip, renderer_utils.rs:201-242
-uint32_t calculate_mip(const Vec2* points, uint32_t n, const DepthEquation& de, const TexCoordEquation& te, float mip_bias)
-{
-	Vec2 mip_point = points[0];
-	float mip_point_inv_z = 0.0f;
-	for (uint32_t i = 0; i < n; ++i)
-	{
-		const float inv_z = de.sample(points[i]);
-		if (inv_z > mip_point_inv_z)
-		{
-			mip_point_inv_z = inv_z;
-			mip_point = points[i];
-		}
-	}
-	const float z_2 = 1.0f / (mip_point_inv_z * mip_point_inv_z);
-	const float z_4 = z_2 * z_2;
-	float d_tc_2[2];
-	for (int i = 0; i < 2; ++i)
-	{
-		const float d_tc_dx = te.d_tc_dx[i] * (de.k + de.d_inv_z_dy * mip_point.y) - (te.k[i] + te.d_tc_dy[i] * mip_point.y) * de.d_inv_z_dx;
-		const float d_tc_dy = te.d_tc_dy[i] * (de.k + de.d_inv_z_dx * mip_point.x) - (te.k[i] + te.d_tc_dx[i] * mip_point.x) * de.d_inv_z_dy;
-		d_tc_2[i] = (d_tc_dx * d_tc_dx + d_tc_dy * d_tc_dy) * z_4;
-	}
-	const float max_d_tc_2 = std::fmax(d_tc_2[0], d_tc_2[1]);
-	const float mip_f = std::log2(max_d_tc_2) * 0.5f + mip_bias;
-	return uint32_t(std::max(0, std::min(as_i32(std::ceil(mip_f)), int32_t(MAX_MIP))));
-}
-
-struct Mat3
-{
-	Vec3 c[3];
-};
-// cgmath Matrix3::invert (cofactor form), then transpose; used by polygon_is_affected_by_light.
-bool mat3_invert_transpose(Vec3 a, Vec3 b, Vec3 c, Mat3& out)
-{
-	const float det = dot(a, cross(b, c));
-	if (det == 0.0f) return false;
-	// inverse rows are cross products / det; transposed -> columns.
-	out.c[0] = cross(b, c) / det;
-	out.c[1] = cross(c, a) / det;
-	out.c[2] = cross(a, b) / det;
-	return true;
-}
+constexpr uint32_t MAX_BSP_TREE_DEPTH = 72; // bsp_builder.rs:53
 
 } // namespace
 
@@ -308,6 +89,15 @@ void ClippingPolygon::get_clip_planes(Vec3 out[8]) const
 // ---- FramePrep ----
 FramePrep::FramePrep(const Scene& scene) : sc(scene)
 {
+	sc.map_polygons(map_polygons);
+	leaf_sky_first.assign(sc.leafs.size() + 1, 0);
+	for (uint32_t i = 0; i < sc.leafs.size(); ++i)
+	{
+		leaf_sky_first[i] = uint32_t(sky_polygons.size());
+		for (uint32_t k = 0; k < sc.leafs[i].num_polygons; ++k)
+			if (map_polygons[sc.leafs[i].first_polygon + k].flags & SW_POLY_SKY) sky_polygons.push_back(sc.leafs[i].first_polygon + k);
+	}
+	leaf_sky_first[sc.leafs.size()] = uint32_t(sky_polygons.size());
 	leaf_data.resize(sc.leafs.size());
 	portal_data.resize(sc.portals.size());
 	poly.resize(sc.polygons.size());
@@ -456,105 +246,43 @@ void FramePrep::prepare_polygon_surface(const Vec3 clip_planes[8], uint64_t& off
 {
 	// partial_renderer.rs:1464-1638
 	PolyData& pd = poly[polygon_index];
-	const MapPolygon& p = sc.polygons[polygon_index];
-	const Vec4 plane_transformed = cam.planes_matrix * extend(p.plane.vec, -p.plane.dist);
-	if (plane_transformed.w <= 0.0f) return;
-	const Material& material = sc.materials[p.texture];
-	if (!material.draw) return;
-	for (uint32_t i = 0; i < p.num_vertices; ++i)
-		vertices_transformed[p.first_vertex + i] = view_transform(cam.view_matrix, sc.vertices[p.first_vertex + i]);
+	const SwMapPolygon& p = map_polygons[polygon_index];
 	Vec2 v2d[MAX_VERTICES];
-	const uint32_t count = project_and_clip_polygon(clip_planes, &vertices_transformed[p.first_vertex], p.num_vertices, v2d);
-	if (count < 3) return;
-	if (material.skybox)
+	uint32_t count = 0;
+	SurfacePrep sp;
+	const PrepResult r = swhost::prepare_polygon_surface(p, sc.vertices.data(), cam.view_matrix, cam.planes_matrix, clip_planes,
+		opt.mip_bias, &vertices_transformed[p.first_vertex], v2d, &count, sp);
+	if (r == PREP_SKY)
 	{
 		// Sky polygons are not drawn; their screen bounds say where draw_skybox must draw (:1510-1528).
-		ClippingPolygon b = ClippingPolygon::from_point(v2d[0]);
-		for (uint32_t k = 1; k < count; ++k) b.extend_with_point(v2d[k]);
-		if (has_sky)
-			sky_bounds.extend(b);
-		else
-		{
-			sky_bounds = b;
-			has_sky = true;
-		}
+		extend_sky_bounds(v2d, count);
 		return;
 	}
-
-	// DepthEquation::from_transformed_plane_equation, equations.rs:23-31
-	const float pw = -plane_transformed.w;
-	DepthEquation de{plane_transformed.x / pw, plane_transformed.y / pw, plane_transformed.z / pw};
-	// tc equations, partial_renderer.rs:1536-1544, equations.rs:55-74
-	const Vec4 tb[2] = {cam.planes_matrix * extend(p.tex_coord_equation[0].vec, p.tex_coord_equation[0].dist),
-		cam.planes_matrix * extend(p.tex_coord_equation[1].vec, p.tex_coord_equation[1].dist)};
-	TexCoordEquation te;
-	for (int i = 0; i < 2; ++i)
-	{
-		te.d_tc_dx[i] = tb[i].x + tb[i].w * de.d_inv_z_dx;
-		te.d_tc_dy[i] = tb[i].y + tb[i].w * de.d_inv_z_dy;
-		te.k[i] = tb[i].z + tb[i].w * de.k;
-	}
-	const uint32_t mip = calculate_mip(v2d, count, de, te, opt.mip_bias);
-	const float mip_scale = 1.0f / float(1u << mip);
-	TexCoordEquation ts;
-	for (int i = 0; i < 2; ++i)
-	{
-		ts.d_tc_dx[i] = te.d_tc_dx[i] * mip_scale;
-		ts.d_tc_dy[i] = te.d_tc_dy[i] * mip_scale;
-		ts.k[i] = te.k[i] * mip_scale;
-	}
-	const float inf = float(1 << 29);
-	const float max_z = float(1 << 16);
-	float tc_min[2] = {inf, inf}, tc_max[2] = {-inf, -inf};
-	for (uint32_t k = 0; k < count; ++k)
-	{
-		const float inv_z = std::fmax(de.sample(v2d[k]), 1.0f / max_z);
-		const float z = 1.0f / inv_z;
-		for (int i = 0; i < 2; ++i)
-		{
-			const float tc = z * (ts.d_tc_dx[i] * v2d[k].x + ts.d_tc_dy[i] * v2d[k].y + ts.k[i]);
-			if (tc < tc_min[i]) tc_min[i] = tc;
-			if (tc > tc_max[i]) tc_max[i] = tc;
-		}
-	}
-	int32_t surface_tc_min[2];
-	uint32_t surface_size[2];
-	for (int i = 0; i < 2; ++i)
-	{
-		const float eps = 1.0f / 32.0f;
-		tc_min[i] += eps;
-		tc_max[i] -= eps;
-		const int32_t round_mask = ~int32_t(LIGHTMAP_SCALE - 1);
-		const int32_t min_down = (p.tex_coord_min[i] & round_mask) >> mip;
-		const int32_t max_up = ((p.tex_coord_max[i] + int32_t(LIGHTMAP_SCALE) - 1) & round_mask) >> mip;
-		int32_t tmin = std::max(as_i32(std::floor(std::fmax(tc_min[i], -inf))), min_down);
-		int32_t tmax = std::min(as_i32(std::ceil(std::fmin(tc_max[i], inf))), max_up);
-		if (tmin >= tmax)
-		{
-			tmin = std::min(tmin, max_up - 1);
-			tmax = tmin + 1;
-		}
-		surface_tc_min[i] = tmin;
-		surface_size[i] = uint32_t(tmax - tmin);
-	}
+	if (r != PREP_SURFACE) return;
 	pd.visible_frame = current_frame;
-	pd.depth = de;
-	pd.tc = ts;
+	pd.depth = sp.depth;
+	pd.tc = sp.tc;
 	pd.offset = offset;
-	pd.size[0] = surface_size[0];
-	pd.size[1] = surface_size[1];
-	pd.mip = mip;
-	pd.tc_min[0] = surface_tc_min[0];
-	pd.tc_min[1] = surface_tc_min[1];
-	offset += uint64_t(surface_size[0]) * surface_size[1];
-	for (int i = 0; i < 2; ++i)
-	{
-		const float tmf = float(surface_tc_min[i]);
-		pd.tc.d_tc_dx[i] -= tmf * de.d_inv_z_dx;
-		pd.tc.d_tc_dy[i] -= tmf * de.d_inv_z_dy;
-		pd.tc.k[i] -= tmf * de.k;
-	}
+	pd.size[0] = sp.size[0];
+	pd.size[1] = sp.size[1];
+	pd.mip = sp.mip;
+	pd.tc_min[0] = sp.tc_min[0];
+	pd.tc_min[1] = sp.tc_min[1];
+	offset += uint64_t(sp.size[0]) * sp.size[1];
 	visible_polygons.push_back(polygon_index);
+}
+
+void FramePrep::extend_sky_bounds(const Vec2* v2d, uint32_t count)
+{
+	ClippingPolygon b = ClippingPolygon::from_point(v2d[0]);
+	for (uint32_t k = 1; k < count; ++k) b.extend_with_point(v2d[k]);
+	if (has_sky)
+		sky_bounds.extend(b);
+	else
+	{
+		sky_bounds = b;
+		has_sky = true;
+	}
 }
 
 void FramePrep::prepare_polygons_surfaces()
@@ -574,172 +302,54 @@ void FramePrep::prepare_polygons_surfaces()
 	total_texels = offset;
 }
 
-static bool polygon_is_affected_by_light(const MapPolygon& polygon, const PolygonBasisVecs& b, const SwLight& light)
-{
-	// partial_renderer.rs:3877-3985 (lights without a projector shadow map)
-	const Vec3 lp = v3(light.position[0], light.position[1], light.position[2]);
-	const Vec3 vec = lp - b.start;
-	const float signed_distance = dot(vec, b.normal);
-	if (signed_distance <= 0.0f) return false;
-	const float square_radius = light.radius * light.radius - signed_distance * signed_distance;
-	if (square_radius <= 0.0f) return false;
-	Mat3 m;
-	if (!mat3_invert_transpose(b.u, b.v, b.normal, m)) return false;
-	const float tc0 = dot(vec, m.c[0]), tc1 = dot(vec, m.c[1]);
-	const float radius = std::sqrt(square_radius);
-	const float u_radius = radius * (1.0f / std::sqrt(magnitude2(b.u)));
-	const float v_radius = radius * (1.0f / std::sqrt(magnitude2(b.v)));
-	if (tc0 + u_radius < float(polygon.tex_coord_min[0]) || tc1 + v_radius < float(polygon.tex_coord_min[1]) ||
-		tc0 - u_radius > float(polygon.tex_coord_max[0]) || tc1 - v_radius > float(polygon.tex_coord_max[1]))
-		return false;
-	return true;
-}
-
 void FramePrep::build_surface_descs()
 {
 	// partial_renderer.rs:1682-1819
 	surfaces.resize(visible_polygons.size());
 	const bool directional = opt.use_directional_lightmaps && sc.directional_lightmaps.size() > 1;
+	const bool simple_lightmaps = sc.lightmaps.size() > 3;
 	for (size_t si = 0; si < visible_polygons.size(); ++si)
 	{
 		const uint32_t pi = visible_polygons[si];
-		const MapPolygon& p = sc.polygons[pi];
+		const SwMapPolygon& p = map_polygons[pi];
 		const PolyData& pd = poly[pi];
-		const Material& mat = sc.materials[p.texture];
+		SurfacePrep sp;
+		sp.size[0] = pd.size[0];
+		sp.size[1] = pd.size[1];
+		sp.mip = pd.mip;
+		sp.tc_min[0] = pd.tc_min[0];
+		sp.tc_min[1] = pd.tc_min[1];
 		SwSurfaceDesc& d = surfaces[si];
-		std::memset(&d, 0, sizeof(d));
-		const int32_t shift[2] = {0, 0}; // get_texture_shift: no scrolling materials in these maps
-		const int32_t shift_mip[2] = {shift[0] >> pd.mip, shift[1] >> pd.mip};
-		d.size[0] = pd.size[0];
-		d.size[1] = pd.size[1];
-		d.tc_start[0] = pd.tc_min[0] + shift_mip[0];
-		d.tc_start[1] = pd.tc_min[1] + shift_mip[1];
-		d.out_offset = pd.offset;
-		d.emissive_mip = SW_NO_EMISSIVE;
-		const bool diffuse_layer = mat.light && mat.has_diffuse;
-		if (diffuse_layer)
-		{
-			d.flags = SW_SURF_DIFFUSE_LAYER;
-			const uint32_t leaf = sc.polygon_leaf[pi];
-			for (uint32_t li : leaf_lights[leaf])
-			{
-				if (polygon_is_affected_by_light(p, sc.basis[pi], lights[li]))
+		make_surface_desc(p, sp, pd.offset, directional, simple_lightmaps, d);
+		if (p.flags & SW_POLY_DIFFUSE_LAYER)
+			for (uint32_t li : leaf_lights[sc.polygon_leaf[pi]])
+				if (polygon_is_affected_by_light(p, lights[li]))
 				{
 					d.lights[d.num_lights++] = uint16_t(li);
 					if (d.num_lights == MAX_POLYGON_LIGHTS) break;
 				}
-			}
-			// get_basis_vecs_for_mip + texture shift correction (surfaces.rs:49-63, partial_renderer.rs:1736-1740)
-			PolygonBasisVecs b = sc.basis[pi];
-			if (pd.mip != 0)
-			{
-				const float scale = float(1u << pd.mip);
-				b.u = b.u * scale;
-				b.v = b.v * scale;
-			}
-			b.start = b.start - (float(shift_mip[0]) * b.u + float(shift_mip[1]) * b.v);
-			const Vec3* vs[4] = {&b.u, &b.v, &b.start, &b.normal};
-			float* ds[4] = {d.basis_u, d.basis_v, d.basis_start, d.basis_normal};
-			for (int k = 0; k < 4; ++k)
-			{
-				ds[k][0] = vs[k]->x;
-				ds[k][1] = vs[k]->y;
-				ds[k][2] = vs[k]->z;
-			}
-			d.texture_mip = p.texture * NUM_MIPS + pd.mip;
-			for (int i = 0; i < 2; ++i)
-			{
-				const int32_t round_mask = ~int32_t(LIGHTMAP_SCALE - 1);
-				d.lightmap_tc_shift[i] = uint32_t(pd.tc_min[i] - ((p.tex_coord_min[i] & round_mask) >> pd.mip));
-			}
-			// get_polygon_lightmap_size, lightmap.rs:11-27
-			d.lightmap_size[0] = uint32_t(((p.tex_coord_max[0] + 15) >> 4) - (p.tex_coord_min[0] >> 4) + 1);
-			d.lightmap_size[1] = uint32_t(((p.tex_coord_max[1] + 15) >> 4) - (p.tex_coord_min[1] >> 4) + 1);
-			d.lightmap_scale_log2 = LIGHTMAP_SCALE_LOG2 - pd.mip;
-			d.lightmap_offset = (directional || sc.lightmaps.size() > 3) ? p.lightmap_data_offset : SW_NO_LIGHTMAP;
-		}
-		if (mat.emissive >= 0)
-		{
-			d.emissive_mip = uint32_t(mat.emissive) * NUM_MIPS + pd.mip;
-			d.emissive_light[0] = mat.emissive_light[0];
-			d.emissive_light[1] = mat.emissive_light[1];
-			d.emissive_light[2] = mat.emissive_light[2];
-		}
 	}
 }
 
 void FramePrep::draw_polygon(const Vec3 clip_planes[8], uint32_t polygon_index)
 {
 	// draw_leaf's call of draw_polygon for a world polygon: its surface is the texture
-	const MapPolygon& p = sc.polygons[polygon_index];
+	const SwMapPolygon& p = map_polygons[polygon_index];
 	const PolyData& pd = poly[polygon_index];
 	if (p.num_vertices < 3) return;
 	emit_draw(clip_planes, &vertices_transformed[p.first_vertex], p.num_vertices, pd.depth, pd.tc, pd.size[0], pd.size[1],
-		pd.offset, SW_TEXSRC_SURFACE, sc.materials[p.texture].blending_mode);
+		pd.offset, SW_TEXSRC_SURFACE, p.blending_mode);
 }
 
 void FramePrep::emit_draw(const Vec3 clip_planes[8], const Vec3* vt, uint32_t num_vertices, const DepthEquation& depth,
 	const TexCoordEquation& tc, uint32_t tex_w, uint32_t tex_h, uint64_t tex_offset, uint32_t tex_source, uint32_t blend)
 {
-	// partial_renderer.rs:4011-4142
-	Vec2 v2d[MAX_VERTICES];
-	const uint32_t count = project_and_clip_polygon(clip_planes, vt, num_vertices, v2d);
-	if (count < 3) return;
-	float min_inv_z = 1e24f, max_inv_z = -1e24f, min_x = 1e24f, max_x = -1e24f;
-	uint32_t min_i = 0, max_i = 0;
-	for (uint32_t k = 0; k < count; ++k)
-	{
-		const float inv_z = depth.sample(v2d[k]);
-		if (inv_z < min_inv_z)
-		{
-			min_inv_z = inv_z;
-			min_i = k;
-		}
-		if (inv_z > max_inv_z)
-		{
-			max_inv_z = inv_z;
-			max_i = k;
-		}
-		if (v2d[k].x < min_x) min_x = v2d[k].x;
-		if (v2d[k].x > max_x) max_x = v2d[k].x;
-	}
+	SwVertex16 v[MAX_VERTICES];
 	SwDrawCmd d;
-	std::memset(&d, 0, sizeof(d));
+	const uint32_t count = make_draw(clip_planes, vt, num_vertices, depth, tc, tex_w, tex_h, tex_offset, tex_source, blend, v, d);
+	if (count < 3) return;
 	d.first_vertex = uint32_t(vertices.size());
-	d.vertex_count = count;
-	for (uint32_t k = 0; k < count; ++k) // f32_to_fixed16_unchecked, fixed_math.rs:335-338
-		vertices.push_back(SwVertex16{as_i32(v2d[k].x * 65536.0f), as_i32(v2d[k].y * 65536.0f)});
-	d.blend = blend;
-	d.tex_size[0] = tex_w;
-	d.tex_size[1] = tex_h;
-	d.tex_source = tex_source;
-	d.tex_offset = tex_offset;
-	DepthEquation de = depth;
-	TexCoordEquation te = tc;
-	if (affine_may_be_used(depth, tc, v2d[min_i], v2d[max_i]))
-		d.mode = SW_RASTER_AFFINE;
-	else
-	{
-		const float z_scale = std::exp2(-5.0f - std::ceil(std::log2(std::fmax(max_inv_z, 1.0f / float(1 << 20)))));
-		de = DepthEquation{de.d_inv_z_dx * z_scale, de.d_inv_z_dy * z_scale, de.k * z_scale};
-		for (int i = 0; i < 2; ++i)
-		{
-			te.d_tc_dx[i] *= z_scale;
-			te.d_tc_dy[i] *= z_scale;
-			te.k[i] *= z_scale;
-		}
-		d.mode = line_z_may_be_used(depth, tc, v2d[max_i], min_x, max_x) ? SW_RASTER_LINE_Z_CORRECTED
-																		 : SW_RASTER_FULL_PERSPECTIVE;
-	}
-	d.depth_eq[0] = de.d_inv_z_dx;
-	d.depth_eq[1] = de.d_inv_z_dy;
-	d.depth_eq[2] = de.k;
-	for (int i = 0; i < 2; ++i)
-	{
-		d.tc_eq[i] = te.d_tc_dx[i];
-		d.tc_eq[2 + i] = te.d_tc_dy[i];
-		d.tc_eq[4 + i] = te.k[i];
-	}
+	vertices.insert(vertices.end(), v, v + count);
 	draws.push_back(d);
 }
 
@@ -838,7 +448,8 @@ void FramePrep::draw_skybox(const ClippingPolygon& viewport)
 	}
 }
 
-void FramePrep::draw_tree()
+template <class F>
+void FramePrep::for_each_drawn_leaf(F&& f)
 {
 	// partial_renderer.rs:2450-2517: back-to-front traversal with the camera-space w of node planes.
 	const ClippingPolygon viewport = ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height));
@@ -859,7 +470,7 @@ void FramePrep::draw_tree()
 			if (b.is_valid_and_non_empty())
 			{
 				++stats.visible_leafs;
-				draw_leaf(b, leaf);
+				f(b, leaf);
 			}
 		}
 		else if (n < MAX_BSP_TREE_DEPTH)
@@ -876,8 +487,13 @@ void FramePrep::draw_tree()
 	}
 }
 
-void FramePrep::prepare_with_camera(const CameraMatrices& camera, const std::vector<SwLight>& frame_lights,
-	const FrameOptions& options, Quat skybox_rotation)
+void FramePrep::draw_tree()
+{
+	for_each_drawn_leaf([this](const ClippingPolygon& b, uint32_t leaf) { draw_leaf(b, leaf); });
+}
+
+void FramePrep::begin_frame(const CameraMatrices& camera, const std::vector<SwLight>& frame_lights, const FrameOptions& options,
+	Quat skybox_rotation)
 {
 	cam = camera;
 	opt = options;
@@ -887,13 +503,10 @@ void FramePrep::prepare_with_camera(const CameraMatrices& camera, const std::vec
 	++current_frame;
 	update_visibility(ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height)));
 	position_lights();
-	prepare_polygons_surfaces();
-	build_surface_descs();
-	draws.clear();
-	vertices.clear();
-	// perform_rasterization_for_viewport_part (:1285-1325): skybox first, then the tree
-	draw_skybox(ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height)));
-	draw_tree();
+}
+
+void FramePrep::finish_params()
+{
 	std::memset(&params, 0, sizeof(params));
 	params.pixel_format = opt.pixel_format;
 	params.width = opt.width;
@@ -903,19 +516,116 @@ void FramePrep::prepare_with_camera(const CameraMatrices& camera, const std::vec
 	params.cam_pos[1] = cam.position.y;
 	params.cam_pos[2] = cam.position.z;
 	params.clear_background = opt.clear_background ? 1u : 0u;
+}
+
+void FramePrep::prepare_with_camera(const CameraMatrices& camera, const std::vector<SwLight>& frame_lights,
+	const FrameOptions& options, Quat skybox_rotation)
+{
+	begin_frame(camera, frame_lights, options, skybox_rotation);
+	prepare_polygons_surfaces();
+	build_surface_descs();
+	draws.clear();
+	vertices.clear();
+	// perform_rasterization_for_viewport_part (:1285-1325): skybox first, then the tree
+	draw_skybox(ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height)));
+	draw_tree();
+	finish_params();
 	stats.visible_polygons = uint32_t(visible_polygons.size());
 	stats.draws = uint32_t(draws.size());
 	stats.surface_texels = total_texels;
 }
 
-void FramePrep::prepare(uint32_t frame_index, const FrameOptions& options)
+void FramePrep::prepare_view_with_camera(const CameraMatrices& camera, const std::vector<SwLight>& frame_lights,
+	const FrameOptions& options, Quat skybox_rotation)
+{
+	begin_frame(camera, frame_lights, options, skybox_rotation);
+	// The visible leafs in index order (prepare_polygons_surfaces' order, :1327-1359) with their bounds and
+	// lights; the sky polygons' bounds are collected here, every other polygon is the GPU's.
+	view_leafs.clear();
+	view_leaf_lights.clear();
+	surfaces.clear();
+	visible_polygons.clear();
+	total_texels = 0;
+	has_sky = false;
+	for (uint32_t i = 0; i < sc.leafs.size(); ++i)
+	{
+		if (leaf_data[i].visible_frame != current_frame) continue;
+		const BspLeaf& leaf = sc.leafs[i];
+		leaf_data[i].view_index = uint32_t(view_leafs.size());
+		SwViewLeaf vl;
+		std::memset(&vl, 0, sizeof(vl));
+		vl.first_polygon = leaf.first_polygon;
+		vl.num_polygons = leaf.num_polygons;
+		vl.first_light = uint32_t(view_leaf_lights.size());
+		vl.num_lights = uint32_t(leaf_lights[i].size());
+		for (uint32_t li : leaf_lights[i]) view_leaf_lights.push_back(uint16_t(li));
+		vl.draw_order = SW_LEAF_NOT_DRAWN;
+		Vec3 planes[8];
+		leaf_data[i].bounds.get_clip_planes(planes);
+		for (int k = 0; k < 8; ++k)
+		{
+			vl.clip_planes[k][0] = planes[k].x;
+			vl.clip_planes[k][1] = planes[k].y;
+			vl.clip_planes[k][2] = planes[k].z;
+		}
+		view_leafs.push_back(vl);
+		for (uint32_t k = leaf_sky_first[i]; k < leaf_sky_first[i + 1]; ++k)
+		{
+			const SwMapPolygon& p = map_polygons[sky_polygons[k]];
+			Vec3 vt[MAX_VERTICES];
+			Vec2 v2d[MAX_VERTICES];
+			uint32_t count = 0;
+			SurfacePrep sp;
+			if (swhost::prepare_polygon_surface(p, sc.vertices.data(), cam.view_matrix, cam.planes_matrix, planes, opt.mip_bias, vt,
+					v2d, &count, sp) == PREP_SKY)
+				extend_sky_bounds(v2d, count);
+		}
+	}
+	draws.clear();
+	vertices.clear();
+	draw_skybox(ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height)));
+	uint32_t order = 0;
+	for_each_drawn_leaf([this, &order](const ClippingPolygon& b, uint32_t leaf) {
+		SwViewLeaf& vl = view_leafs[leaf_data[leaf].view_index];
+		vl.draw_order = order++;
+		Vec3 planes[8];
+		b.get_clip_planes(planes);
+		for (int k = 0; k < 8; ++k)
+		{
+			vl.draw_clip_planes[k][0] = planes[k].x;
+			vl.draw_clip_planes[k][1] = planes[k].y;
+			vl.draw_clip_planes[k][2] = planes[k].z;
+		}
+	});
+	finish_params();
+	stats.draws = uint32_t(draws.size());
+}
+
+void FramePrep::camera_of_frame(uint32_t frame_index, const FrameOptions& options, CameraMatrices& camera,
+	std::vector<SwLight>& frame_lights, Quat& skybox_rotation) const
 {
 	const CameraKey& k = sc.camera_path[frame_index % sc.camera_path.size()];
-	const CameraMatrices camera =
-		build_view_matrix(k.position, k.azimuth, k.elevation, options.fov, float(options.width), float(options.height));
+	camera = build_view_matrix(k.position, k.azimuth, k.elevation, options.fov, float(options.width), float(options.height));
+	sc.frame_lights(frame_index % uint32_t(sc.camera_path.size()), frame_lights);
+	skybox_rotation = quat_from_angle_z(float(frame_index) * sc.config.sky_rotation_speed);
+}
+
+void FramePrep::prepare(uint32_t frame_index, const FrameOptions& options)
+{
+	CameraMatrices camera;
 	std::vector<SwLight> l;
-	sc.frame_lights(frame_index % uint32_t(sc.camera_path.size()), l);
-	prepare_with_camera(camera, l, options, quat_from_angle_z(float(frame_index) * sc.config.sky_rotation_speed));
+	Quat rotation;
+	camera_of_frame(frame_index, options, camera, l, rotation);
+	prepare_with_camera(camera, l, options, rotation);
+}
+
+void FramePrep::prepare_view(uint32_t frame_index, const FrameOptions& options)
+{
+	CameraMatrices camera;
+	std::vector<SwLight> l;
+	Quat rotation;
+	camera_of_frame(frame_index, options, camera, l, rotation);
+	prepare_view_with_camera(camera, l, options, rotation);
 }
 
 } // namespace swhost

@@ -16,6 +16,7 @@
 
 #include <vector>
 
+#include "prep_math.h"
 #include "scene.h"
 
 namespace swhost
@@ -36,16 +37,6 @@ struct ClippingPolygon
 	void extend_with_point(Vec2 p);
 	void intersect(const ClippingPolygon& o);
 	void get_clip_planes(Vec3 out[8]) const;
-};
-
-struct DepthEquation
-{
-	float d_inv_z_dx, d_inv_z_dy, k;
-	float sample(Vec2 p) const { return d_inv_z_dx * p.x + d_inv_z_dy * p.y + k; }
-};
-struct TexCoordEquation
-{
-	float d_tc_dx[2], d_tc_dy[2], k[2];
 };
 
 struct FrameOptions
@@ -73,6 +64,18 @@ public:
 	// Same with an explicit camera, light list and skybox rotation (FrameWorldInfo::skybox_rotation).
 	void prepare_with_camera(const CameraMatrices& cam, const std::vector<SwLight>& lights, const FrameOptions& opt,
 		Quat skybox_rotation = Quat{1.0f, Vec3{0.0f, 0.0f, 0.0f}});
+	// The host half of a frame whose surfaces and world draws are prepared on the GPU
+	// (sw_draw_frame_view): visibility, light positioning, the skybox draws and the visible leafs with
+	// their bounds, lights and back-to-front draw order (view_leafs, view_leaf_lights). surfaces stays
+	// empty; draws / vertices hold the skybox's.
+	void prepare_view(uint32_t frame_index, const FrameOptions& opt);
+	void prepare_view_with_camera(const CameraMatrices& cam, const std::vector<SwLight>& lights, const FrameOptions& opt,
+		Quat skybox_rotation = Quat{1.0f, Vec3{0.0f, 0.0f, 0.0f}});
+
+	const CameraMatrices& camera() const { return cam; }
+
+	// The map's polygons as the preparation reads them (uploaded by sw_set_map for the GPU side).
+	std::vector<SwMapPolygon> map_polygons;
 
 	std::vector<SwSurfaceDesc> surfaces;
 	uint64_t total_texels = 0;
@@ -81,11 +84,14 @@ public:
 	std::vector<SwLight> lights;
 	SwFrameParams params{};
 	FrameStats stats;
+	std::vector<SwViewLeaf> view_leafs;
+	std::vector<uint16_t> view_leaf_lights;
 
 private:
 	struct LeafData
 	{
 		uint32_t visible_frame = 0;
+		uint32_t view_index = 0; // position in view_leafs (prepare_view)
 		ClippingPolygon bounds{};
 	};
 	struct PortalData
@@ -119,6 +125,8 @@ private:
 	Quat sky_rotation{1.0f, Vec3{0.0f, 0.0f, 0.0f}};
 	bool has_sky = false;        // current_sky (partial_renderer.rs:35): a sky polygon is visible
 	ClippingPolygon sky_bounds{}; // union of the visible sky polygons' screen bounds
+	std::vector<uint32_t> sky_polygons;   // polygons of the sky material, grouped by leaf
+	std::vector<uint32_t> leaf_sky_first; // leaf i's sky polygons: sky_polygons[leaf_sky_first[i] .. [i + 1])
 
 	uint32_t find_current_leaf() const;
 	void update_visibility(const ClippingPolygon& frame_bounds);
@@ -128,6 +136,13 @@ private:
 	void position_sphere(uint32_t id, Vec3 center, float radius, uint32_t node);
 	void prepare_polygons_surfaces();
 	void prepare_polygon_surface(const Vec3 clip_planes[8], uint64_t& offset, uint32_t polygon_index);
+	void extend_sky_bounds(const Vec2* v2d, uint32_t count);
+	void begin_frame(const CameraMatrices& cam, const std::vector<SwLight>& lights, const FrameOptions& opt, Quat skybox_rotation);
+	void finish_params();
+	void camera_of_frame(uint32_t frame_index, const FrameOptions& opt, CameraMatrices& cam, std::vector<SwLight>& lights,
+		Quat& skybox_rotation) const;
+	template <class F>
+	void for_each_drawn_leaf(F&& f);
 	void build_surface_descs();
 	void draw_skybox(const ClippingPolygon& viewport);
 	void draw_tree();

@@ -4,11 +4,19 @@
 // linear combination of columns, Quaternion -> Matrix4) and src/common/matrix.rs for the camera.
 // cgmath's Matrix4::invert is restated as a cofactor inverse; its exact rounding is not pinned by any
 // reference test, and both the GPU path and the oracle consume the matrices computed here.
-// Compiled with -ffp-contract=off: every a*b+c is two roundings, as in the reference.
+// Compiled with -ffp-contract=off (host) and --fmad=false (device): every a*b+c is two roundings, as in
+// the reference. The vector and matrix operations are __host__ __device__ under nvcc, so the GPU-side
+// surface and draw preparation evaluates exactly the same expressions as the host.
 #pragma once
 
 #include <cmath>
 #include <cstdint>
+
+#if defined(__CUDACC__)
+#define SWH_HD __host__ __device__
+#else
+#define SWH_HD
+#endif
 
 namespace swhost
 {
@@ -26,30 +34,30 @@ struct Vec4
 	float x, y, z, w;
 };
 
-inline Vec2 v2(float x, float y) { return Vec2{x, y}; }
-inline Vec3 v3(float x, float y, float z) { return Vec3{x, y, z}; }
-inline Vec4 v4(float x, float y, float z, float w) { return Vec4{x, y, z, w}; }
-inline Vec3 operator+(Vec3 a, Vec3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
-inline Vec3 operator-(Vec3 a, Vec3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
-inline Vec3 operator-(Vec3 a) { return v3(-a.x, -a.y, -a.z); }
-inline Vec3 operator*(Vec3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
-inline Vec3 operator*(float s, Vec3 a) { return v3(s * a.x, s * a.y, s * a.z); }
-inline Vec3 operator/(Vec3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
-inline Vec2 operator+(Vec2 a, Vec2 b) { return v2(a.x + b.x, a.y + b.y); }
-inline Vec2 operator-(Vec2 a, Vec2 b) { return v2(a.x - b.x, a.y - b.y); }
-inline Vec2 operator*(Vec2 a, float s) { return v2(a.x * s, a.y * s); }
-inline Vec2 operator/(Vec2 a, float s) { return v2(a.x / s, a.y / s); }
+SWH_HD inline Vec2 v2(float x, float y) { return Vec2{x, y}; }
+SWH_HD inline Vec3 v3(float x, float y, float z) { return Vec3{x, y, z}; }
+SWH_HD inline Vec4 v4(float x, float y, float z, float w) { return Vec4{x, y, z, w}; }
+SWH_HD inline Vec3 operator+(Vec3 a, Vec3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+SWH_HD inline Vec3 operator-(Vec3 a, Vec3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+SWH_HD inline Vec3 operator-(Vec3 a) { return v3(-a.x, -a.y, -a.z); }
+SWH_HD inline Vec3 operator*(Vec3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+SWH_HD inline Vec3 operator*(float s, Vec3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+SWH_HD inline Vec3 operator/(Vec3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
+SWH_HD inline Vec2 operator+(Vec2 a, Vec2 b) { return v2(a.x + b.x, a.y + b.y); }
+SWH_HD inline Vec2 operator-(Vec2 a, Vec2 b) { return v2(a.x - b.x, a.y - b.y); }
+SWH_HD inline Vec2 operator*(Vec2 a, float s) { return v2(a.x * s, a.y * s); }
+SWH_HD inline Vec2 operator/(Vec2 a, float s) { return v2(a.x / s, a.y / s); }
 // cgmath InnerSpace::dot = (a*b).sum() = ((x*x' + y*y') + z*z') (+ w*w')
-inline float dot(Vec2 a, Vec2 b) { return a.x * b.x + a.y * b.y; }
-inline float dot(Vec3 a, Vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-inline float dot(Vec4 a, Vec4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
-inline float magnitude2(Vec3 a) { return dot(a, a); }
-inline float magnitude(Vec3 a) { return std::sqrt(magnitude2(a)); }
-inline Vec3 cross(Vec3 a, Vec3 b) { return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
-inline Vec4 extend(Vec3 a, float w) { return v4(a.x, a.y, a.z, w); }
-inline Vec3 truncate(Vec4 a) { return v3(a.x, a.y, a.z); }
-inline Vec4 operator+(Vec4 a, Vec4 b) { return v4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
-inline Vec4 operator*(Vec4 a, float s) { return v4(a.x * s, a.y * s, a.z * s, a.w * s); }
+SWH_HD inline float dot(Vec2 a, Vec2 b) { return a.x * b.x + a.y * b.y; }
+SWH_HD inline float dot(Vec3 a, Vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+SWH_HD inline float dot(Vec4 a, Vec4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+SWH_HD inline float magnitude2(Vec3 a) { return dot(a, a); }
+SWH_HD inline float magnitude(Vec3 a) { return sqrtf(magnitude2(a)); }
+SWH_HD inline Vec3 cross(Vec3 a, Vec3 b) { return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+SWH_HD inline Vec4 extend(Vec3 a, float w) { return v4(a.x, a.y, a.z, w); }
+SWH_HD inline Vec3 truncate(Vec4 a) { return v3(a.x, a.y, a.z); }
+SWH_HD inline Vec4 operator+(Vec4 a, Vec4 b) { return v4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+SWH_HD inline Vec4 operator*(Vec4 a, float s) { return v4(a.x * s, a.y * s, a.z * s, a.w * s); }
 
 // Plane: vec . p = dist (src/common/plane.rs)
 struct Plane
@@ -62,7 +70,7 @@ struct Plane
 struct Mat4
 {
 	Vec4 c[4];
-	static Mat4 identity()
+	SWH_HD static Mat4 identity()
 	{
 		Mat4 m;
 		m.c[0] = v4(1, 0, 0, 0);
@@ -71,23 +79,23 @@ struct Mat4
 		m.c[3] = v4(0, 0, 0, 1);
 		return m;
 	}
-	float at(int row, int col) const
+	SWH_HD float at(int row, int col) const
 	{
 		const Vec4& v = c[col];
 		return row == 0 ? v.x : row == 1 ? v.y : row == 2 ? v.z : v.w;
 	}
-	Vec4 row(int r) const { return v4(at(r, 0), at(r, 1), at(r, 2), at(r, 3)); }
+	SWH_HD Vec4 row(int r) const { return v4(at(r, 0), at(r, 1), at(r, 2), at(r, 3)); }
 };
 
 // matrix * vector = c0*x + c1*y + c2*z + c3*w (left to right)
-inline Vec4 operator*(const Mat4& m, Vec4 v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z + m.c[3] * v.w; }
-inline Mat4 operator*(const Mat4& a, const Mat4& b)
+SWH_HD inline Vec4 operator*(const Mat4& m, Vec4 v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z + m.c[3] * v.w; }
+SWH_HD inline Mat4 operator*(const Mat4& a, const Mat4& b)
 {
 	Mat4 r;
 	for (int i = 0; i < 4; ++i) r.c[i] = a * b.c[i];
 	return r;
 }
-inline Mat4 transpose(const Mat4& m)
+SWH_HD inline Mat4 transpose(const Mat4& m)
 {
 	Mat4 r;
 	for (int i = 0; i < 4; ++i) r.c[i] = m.row(i);
@@ -216,6 +224,6 @@ inline CameraMatrices build_view_matrix(Vec3 position, float azimuth, float elev
 }
 
 // view_matrix_transform_vertex, src/common/matrix.rs:125-128
-inline Vec3 view_transform(const Mat4& m, Vec3 v) { return truncate(m * extend(v, 1.0f)); }
+SWH_HD inline Vec3 view_transform(const Mat4& m, Vec3 v) { return truncate(m * extend(v, 1.0f)); }
 
 } // namespace swhost

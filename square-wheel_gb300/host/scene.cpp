@@ -915,6 +915,39 @@ void Scene::frame_lights(uint32_t frame, std::vector<SwLight>& out) const
 	}
 }
 
+void Scene::map_polygons(std::vector<SwMapPolygon>& out) const
+{
+	out.resize(polygons.size());
+	for (size_t i = 0; i < polygons.size(); ++i)
+	{
+		const MapPolygon& p = polygons[i];
+		const Material& m = materials[p.texture];
+		const PolygonBasisVecs& b = basis[i];
+		SwMapPolygon& o = out[i];
+		std::memset(&o, 0, sizeof(o));
+		o.plane[0] = p.plane.vec.x, o.plane[1] = p.plane.vec.y, o.plane[2] = p.plane.vec.z, o.plane[3] = p.plane.dist;
+		for (int k = 0; k < 2; ++k)
+		{
+			const Plane& t = p.tex_coord_equation[k];
+			o.tex_coord_equation[k][0] = t.vec.x, o.tex_coord_equation[k][1] = t.vec.y;
+			o.tex_coord_equation[k][2] = t.vec.z, o.tex_coord_equation[k][3] = t.dist;
+			o.tex_coord_min[k] = p.tex_coord_min[k];
+			o.tex_coord_max[k] = p.tex_coord_max[k];
+		}
+		const Vec3* vs[4] = {&b.u, &b.v, &b.start, &b.normal};
+		float* ds[4] = {o.basis_u, o.basis_v, o.basis_start, o.basis_normal};
+		for (int k = 0; k < 4; ++k) ds[k][0] = vs[k]->x, ds[k][1] = vs[k]->y, ds[k][2] = vs[k]->z;
+		o.first_vertex = p.first_vertex;
+		o.num_vertices = p.num_vertices;
+		o.texture = p.texture;
+		o.lightmap_data_offset = p.lightmap_data_offset;
+		o.flags = (m.draw ? SW_POLY_DRAW : 0u) | (m.skybox ? SW_POLY_SKY : 0u) | ((m.light && m.has_diffuse) ? SW_POLY_DIFFUSE_LAYER : 0u);
+		o.blending_mode = m.blending_mode;
+		o.emissive_texture = m.emissive >= 0 ? uint32_t(m.emissive) : SW_NO_EMISSIVE;
+		o.emissive_light[0] = m.emissive_light[0], o.emissive_light[1] = m.emissive_light[1], o.emissive_light[2] = m.emissive_light[2];
+	}
+}
+
 SwCreateInfo Scene::create_info(uint32_t device) const
 {
 	SwCreateInfo ci;

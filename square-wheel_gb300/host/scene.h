@@ -149,6 +149,8 @@ struct Scene
 
 	uint32_t root_node() const { return nodes.empty() ? FIRST_LEAF_INDEX : uint32_t(nodes.size() - 1); }
 	void frame_lights(uint32_t frame, std::vector<SwLight>& out) const;
+	// Polygons with their basis and material fields (SwMapPolygon), in polygon order.
+	void map_polygons(std::vector<SwMapPolygon>& out) const;
 	SwCreateInfo create_info(uint32_t device) const;
 };
 

@@ -24,6 +24,7 @@ struct SwhRenderer
 	const SwhScene* scene = nullptr;
 	SwCtx* ctx = nullptr;
 	SwhFrame* frame = nullptr;
+	bool gpu_prep = true; // render_frame: surfaces and world draws prepared on the GPU (sw_draw_frame_view)
 };
 
 namespace
@@ -178,6 +179,53 @@ int swh_frame_prepare(SwhFrame* f, uint32_t frame_index, const SwhFrameOptions* 
 	return SW_OK;
 }
 
+int swh_frame_prepare_view(SwhFrame* f, uint32_t frame_index, const SwhFrameOptions* o)
+{
+	if (!f || !valid_options(o)) return SW_ERR_INVALID_ARGUMENT;
+	try
+	{
+		f->prep.prepare_view(frame_index, to_options(o));
+	}
+	catch (const std::bad_alloc&)
+	{
+		g_error = "out of host memory";
+		return SW_ERR_OUT_OF_MEMORY;
+	}
+	return SW_OK;
+}
+
+int swh_frame_view_input(const SwhFrame* f, SwViewFrameInput* out)
+{
+	if (!f || !out) return SW_ERR_INVALID_ARGUMENT;
+	const FramePrep& p = f->prep;
+	std::memset(out, 0, sizeof(*out));
+	out->params = p.params;
+	out->num_lights = uint32_t(p.lights.size());
+	out->lights = p.lights.data();
+	const CameraMatrices& cam = p.camera();
+	for (int c = 0; c < 4; ++c)
+	{
+		const Vec4* cols[2] = {&cam.view_matrix.c[c], &cam.planes_matrix.c[c]};
+		float* dst[2] = {out->view_matrix + c * 4, out->planes_matrix + c * 4};
+		for (int m = 0; m < 2; ++m)
+		{
+			dst[m][0] = cols[m]->x;
+			dst[m][1] = cols[m]->y;
+			dst[m][2] = cols[m]->z;
+			dst[m][3] = cols[m]->w;
+		}
+	}
+	out->num_leafs = uint32_t(p.view_leafs.size());
+	out->leafs = p.view_leafs.data();
+	out->num_leaf_lights = uint32_t(p.view_leaf_lights.size());
+	out->leaf_lights = p.view_leaf_lights.data();
+	out->num_draws = uint32_t(p.draws.size());
+	out->draws = p.draws.data();
+	out->vertices = p.vertices.data();
+	out->num_vertices = uint32_t(p.vertices.size());
+	return SW_OK;
+}
+
 int swh_frame_outputs(const SwhFrame* f, SwhFrameOutputs* out)
 {
 	if (!f || !out) return SW_ERR_INVALID_ARGUMENT;
@@ -228,6 +276,16 @@ int swh_renderer_create(const SwhScene* s, uint32_t device, SwhRenderer** out)
 		delete r;
 		return SW_ERR_OUT_OF_MEMORY;
 	}
+	const std::vector<SwMapPolygon>& mp = r->frame->prep.map_polygons;
+	if ((st = sw_set_map(r->ctx, mp.data(), uint32_t(mp.size()), reinterpret_cast<const float*>(s->scene.vertices.data()),
+			 uint32_t(s->scene.vertices.size()))) != SW_OK)
+	{
+		g_error = std::string("sw_set_map failed: ") + sw_last_error(r->ctx);
+		sw_destroy(r->ctx);
+		delete r->frame;
+		delete r;
+		return st;
+	}
 	*out = r;
 	return SW_OK;
 }
@@ -265,6 +323,25 @@ int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFra
 	float frame_duration_s, const float color_modulate[3], void* dst, uint32_t pitch, int dst_is_device)
 {
 	if (!r || (post && (!dst || !color_modulate))) return SW_ERR_INVALID_ARGUMENT;
+	if (r->gpu_prep)
+	{
+		int st = swh_frame_prepare_view(r->frame, frame_index, o);
+		if (st) return st;
+		SwViewFrameInput vin;
+		swh_frame_view_input(r->frame, &vin);
+		vin.mip_bias = o->mip_bias;
+		if (post)
+		{
+			vin.postprocess = 1;
+			vin.post = *post;
+			vin.frame_duration_s = frame_duration_s;
+			for (int i = 0; i < 3; ++i) vin.color_modulate[i] = color_modulate[i];
+		}
+		vin.dst = dst;
+		vin.dst_pitch = pitch;
+		vin.dst_is_device = dst_is_device;
+		return sw_draw_frame_view(r->ctx, &vin);
+	}
 	int st = swh_frame_prepare(r->frame, frame_index, o);
 	if (st) return st;
 	const FramePrep& p = r->frame->prep;
@@ -291,6 +368,13 @@ int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFra
 	in.dst_pitch = pitch;
 	in.dst_is_device = dst_is_device;
 	return sw_draw_frame(r->ctx, &in);
+}
+
+int swh_renderer_set_gpu_prep(SwhRenderer* r, int enable)
+{
+	if (!r) return SW_ERR_INVALID_ARGUMENT;
+	r->gpu_prep = enable != 0;
+	return SW_OK;
 }
 
 SwCtx* swh_renderer_context(SwhRenderer* r) { return r ? r->ctx : nullptr; }

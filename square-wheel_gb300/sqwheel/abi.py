@@ -34,6 +34,8 @@ SW_MAX_POLYGON_VERTICES = 24
 SW_NO_LIGHTMAP = 0
 SW_NO_EMISSIVE = 0xFFFFFFFF
 SW_SURF_DIFFUSE_LAYER = 1
+SW_POLY_DRAW, SW_POLY_SKY, SW_POLY_DIFFUSE_LAYER = 1, 2, 4
+SW_LEAF_NOT_DRAWN = 0xFFFFFFFF
 
 TEXTURE_MIP = np.dtype([("offset", "<u8"), ("width", "<u4"), ("height", "<u4"), ("flags", "<u4"), ("reserved", "<u4")], align=True)
 EMISSIVE_MIP = np.dtype([("offset", "<u8"), ("width", "<u4"), ("height", "<u4")], align=True)
@@ -51,6 +53,16 @@ VERTEX16 = np.dtype([("x", "<i4"), ("y", "<i4")], align=True)
 DRAW_CMD = np.dtype([
     ("first_vertex", "<u4"), ("vertex_count", "<u4"), ("mode", "<u4"), ("blend", "<u4"), ("depth_eq", "<f4", 3),
     ("tc_eq", "<f4", 6), ("tex_size", "<u4", 2), ("tex_source", "<u4"), ("tex_offset", "<u8")], align=True)
+
+MAP_POLYGON = np.dtype([
+    ("plane", "<f4", 4), ("tex_coord_equation", "<f4", (2, 4)), ("basis_u", "<f4", 3), ("basis_v", "<f4", 3),
+    ("basis_start", "<f4", 3), ("basis_normal", "<f4", 3), ("tex_coord_min", "<i4", 2), ("tex_coord_max", "<i4", 2),
+    ("first_vertex", "<u4"), ("num_vertices", "<u4"), ("texture", "<u4"), ("lightmap_data_offset", "<u4"),
+    ("flags", "<u4"), ("blending_mode", "<u4"), ("emissive_texture", "<u4"), ("emissive_light", "<f4", 3)], align=True)
+VIEW_LEAF = np.dtype([
+    ("first_polygon", "<u4"), ("num_polygons", "<u4"), ("first_light", "<u4"), ("num_lights", "<u4"),
+    ("draw_order", "<u4"), ("reserved", "<u4"), ("clip_planes", "<f4", (8, 3)), ("draw_clip_planes", "<f4", (8, 3))],
+    align=True)
 
 
 class CreateInfo(ctypes.Structure):
@@ -105,6 +117,23 @@ class FrameInput(ctypes.Structure):
                 ("dst_pitch", ctypes.c_uint32), ("dst_is_device", ctypes.c_int32)]
 
 
+class ViewFrameInput(ctypes.Structure):
+    """SwViewFrameInput: one whole frame for sw_draw_frame_view (GPU-side surface and draw preparation)."""
+    _fields_ = [("params", FrameParams), ("num_lights", ctypes.c_uint32), ("lights", ctypes.c_void_p),
+                ("view_matrix", ctypes.c_float * 16), ("planes_matrix", ctypes.c_float * 16), ("mip_bias", ctypes.c_float),
+                ("num_leafs", ctypes.c_uint32), ("leafs", ctypes.c_void_p), ("num_leaf_lights", ctypes.c_uint32),
+                ("leaf_lights", ctypes.c_void_p), ("num_draws", ctypes.c_uint32), ("draws", ctypes.c_void_p),
+                ("vertices", ctypes.c_void_p), ("num_vertices", ctypes.c_uint32), ("postprocess", ctypes.c_uint32),
+                ("post", PostConfig), ("frame_duration_s", ctypes.c_float), ("color_modulate", ctypes.c_float * 3),
+                ("dst", ctypes.c_void_p), ("dst_pitch", ctypes.c_uint32), ("dst_is_device", ctypes.c_int32)]
+
+
+class ViewCounts(ctypes.Structure):
+    """SwViewCounts: what the last sw_draw_frame_view prepared."""
+    _fields_ = [("num_surfaces", ctypes.c_uint32), ("num_draws", ctypes.c_uint32), ("num_vertices", ctypes.c_uint32),
+                ("error", ctypes.c_uint32), ("total_texels", ctypes.c_uint64), ("num_rows", ctypes.c_uint64)]
+
+
 class Tuning(ctypes.Structure):
     """SwTuning: launch configuration (raster tile shape, surface-build blocks per SM)."""
     _fields_ = [("raster_tile", ctypes.c_uint32), ("surface_blocks_per_sm", ctypes.c_uint32)]
@@ -119,6 +148,8 @@ LAYOUT_ORDER = [
     ("SwDrawCmd", DRAW_CMD.itemsize), ("SwFrameParams", ctypes.sizeof(FrameParams)),
     ("SwPostConfig", ctypes.sizeof(PostConfig)), ("SwStats", ctypes.sizeof(Stats)),
     ("SwFrameInput", ctypes.sizeof(FrameInput)), ("SwTuning", ctypes.sizeof(Tuning)),
+    ("SwMapPolygon", MAP_POLYGON.itemsize), ("SwViewLeaf", VIEW_LEAF.itemsize),
+    ("SwViewFrameInput", ctypes.sizeof(ViewFrameInput)), ("SwViewCounts", ctypes.sizeof(ViewCounts)),
 ]
 
 

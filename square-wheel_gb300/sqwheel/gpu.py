@@ -24,7 +24,7 @@ EXPORTED = [
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
     "sw_postprocess_noalloc", "sw_set_learned_upscaler", "sw_draw_frame", "sw_set_frame_graph", "sw_set_tuning",
-    "sw_get_tuning", "sw_autotune",
+    "sw_get_tuning", "sw_autotune", "sw_set_map", "sw_draw_frame_view", "sw_read_view_prep",
     # learned upscaler (include/swlearn.h)
     "sw_upscaler_create", "sw_upscaler_destroy", "sw_upscaler_last_error", "sw_upscaler_get_params",
     "sw_upscaler_set_params", "sw_upscaler_gradients", "sw_upscaler_train_step", "sw_upscaler_steps",
@@ -80,6 +80,9 @@ def load_library(path=LIB_PATH):
         "sw_set_tuning": ([vp, vp], i32),
         "sw_get_tuning": ([vp, vp], i32),
         "sw_autotune": ([vp, vp, u32, vp, ctypes.POINTER(f32)], i32),
+        "sw_set_map": ([vp, vp, u32, vp, u32], i32),
+        "sw_draw_frame_view": ([vp, vp], i32),
+        "sw_read_view_prep": ([vp, vp, vp, u32, vp, u32, vp, u32], i32),
         "sw_upscaler_create": ([i32, u64, ctypes.POINTER(vp)], i32),
         "sw_upscaler_destroy": ([vp], i32),
         "sw_upscaler_last_error": ([vp], ctypes.c_char_p),
@@ -108,8 +111,8 @@ def load_library(path=LIB_PATH):
 
 def abi_layout():
     lib = load_library()
-    sizes = (ctypes.c_uint32 * 16)()
-    n = lib.sw_abi_layout(sizes, 16)
+    sizes = (ctypes.c_uint32 * 32)()
+    n = lib.sw_abi_layout(sizes, 32)
     return [int(sizes[i]) for i in range(n)]
 
 

@@ -69,6 +69,8 @@ def load_host_library():
         "swh_renderer_frame": ([vp], vp),
         "swh_scene_skybox": ([vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_uint64), vp, vp], i32),
         "swh_renderer_render_frame": ([vp, u32, vp, vp, ctypes.c_float, vp, vp, u32, i32], i32),
+        "swh_frame_prepare_view": ([vp, u32, vp], i32), "swh_frame_view_input": ([vp, vp], i32),
+        "swh_renderer_set_gpu_prep": ([vp, i32], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -82,7 +84,8 @@ HOST_EXPORTED = ["swh_scene_create", "swh_scene_destroy", "swh_scene_info", "swh
                  "swh_frame_create", "swh_frame_destroy", "swh_frame_prepare", "swh_frame_outputs",
                  "swh_renderer_create", "swh_renderer_destroy", "swh_renderer_prepare_frame",
                  "swh_renderer_draw_frame", "swh_renderer_context", "swh_renderer_frame", "swh_scene_skybox",
-                 "swh_renderer_render_frame"]
+                 "swh_renderer_render_frame", "swh_frame_prepare_view", "swh_frame_view_input",
+                 "swh_renderer_set_gpu_prep"]
 
 # The two map configurations of the benchmark plan.
 SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, num_materials=16, metal_frac=0.0,
@@ -206,6 +209,25 @@ class Frame:
         self.skybox_draws = int(o.skybox_draws)
         return self
 
+    def prepare_view(self, frame_index, options):
+        """Host half of a GPU-prepared frame: returns its SwViewFrameInput (pointers into this frame) and
+        copies of the visible leafs and their light lists."""
+        _check(self.lib, self.lib.swh_frame_prepare_view(self.handle, frame_index, ctypes.byref(options)),
+               "swh_frame_prepare_view")
+        vin = abi.ViewFrameInput()
+        _check(self.lib, self.lib.swh_frame_view_input(self.handle, ctypes.byref(vin)), "swh_frame_view_input")
+
+        def arr(p, n, dt):
+            if not p or n == 0:
+                return np.zeros(0, dt)
+            return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)),
+                                         shape=(int(n) * np.dtype(dt).itemsize,)).view(dt).copy()
+        self.view_leafs = arr(vin.leafs, vin.num_leafs, abi.VIEW_LEAF)
+        self.view_leaf_lights = arr(vin.leaf_lights, vin.num_leaf_lights, np.uint16)
+        self.draws = arr(vin.draws, vin.num_draws, abi.DRAW_CMD)
+        self.vertices = arr(vin.vertices, vin.num_vertices, abi.VERTEX16)
+        return vin
+
     def close(self):
         if self.handle:
             self.lib.swh_frame_destroy(self.handle)
@@ -259,6 +281,21 @@ class HostRenderer:
             dst, pitch, dev = None, 0, 0
         self._err(self.lib.swh_renderer_render_frame(self.handle, frame_index, ctypes.byref(options), post_p,
                                                      frame_duration_s, mod, dst, pitch or 0, dev), "render_frame")
+
+    def set_gpu_prep(self, enable):
+        """render_frame's preparation: True = on the GPU (default), False = on the host."""
+        self._err(self.lib.swh_renderer_set_gpu_prep(self.handle, 1 if enable else 0), "set_gpu_prep")
+
+    def read_view_prep(self, max_surfaces=1 << 16, max_draws=1 << 16, max_vertices=1 << 20):
+        """Counts, surface descriptors, draws and vertices of the last GPU-prepared frame (synchronises)."""
+        glib = load_library()
+        k = abi.ViewCounts()
+        s = np.zeros(max_surfaces, abi.SURFACE_DESC)
+        d = np.zeros(max_draws, abi.DRAW_CMD)
+        v = np.zeros(max_vertices, abi.VERTEX16)
+        self._err(glib.sw_read_view_prep(self.context(), ctypes.byref(k), abi.ptr(s), max_surfaces, abi.ptr(d), max_draws,
+                                         abi.ptr(v), max_vertices), "read_view_prep")
+        return k, s[:k.num_surfaces].copy(), d[:k.num_draws].copy(), v[:k.num_vertices].copy()
 
     def register_host_buffer(self, arr):
         """Page-lock `arr` (reused for frames) so frames are copied straight into it."""

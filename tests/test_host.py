@@ -91,3 +91,33 @@ def test_oracle_single_vs_split_rect(small_scene):
     oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, a, num_threads=1)
     oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, b, num_threads=4)
     assert (a != 0).all() and (b != 0).all()
+
+
+@pytest.mark.parametrize("cfg", ["small", "sky"])
+def test_prepare_view_matches_prepare(built_libs, cfg):
+    """The host half of a GPU-prepared frame (prepare_view) sees the same leafs as the host preparation: every
+    visible polygon lies in a view leaf, the drawn leafs are draw_tree's (a permutation 0..n-1), leaf light
+    lists index the frame's lights, and the skybox draws are identical."""
+    scene = host.Scene(**(host.SMALL_MAP if cfg == "small" else host.SKY_MAP))
+    fr = host.Frame(scene)
+    fv = host.Frame(scene)
+    opts = host.frame_options(800, 600, abi.SW_PIXEL_C64, directional=True)
+    for fi in (0, 5, 30, 61, 90):
+        fr.prepare(fi, opts)
+        fv.prepare_view(fi, opts)
+        leafs = fv.view_leafs
+        assert leafs.size > 0
+        order = leafs["draw_order"][leafs["draw_order"] != abi.SW_LEAF_NOT_DRAWN]
+        assert sorted(order.tolist()) == list(range(order.size))
+        assert order.size == fr.visible_leafs
+        assert int(leafs["num_polygons"].sum()) >= fr.surfaces.size
+        first, num = leafs["first_light"].astype(np.int64), leafs["num_lights"].astype(np.int64)
+        assert (first + num <= fv.view_leaf_lights.size).all()
+        assert (fv.view_leaf_lights < fr.lights.size).all()
+        n_sky = fr.skybox_draws
+        assert fv.draws.size == n_sky
+        assert np.array_equal(fv.draws.view(np.uint8), fr.draws[:n_sky].view(np.uint8))
+        sky_vertices = int(fr.draws[:n_sky]["vertex_count"].sum())
+        assert np.array_equal(fv.vertices.view(np.uint8), fr.vertices[:sky_vertices].view(np.uint8))
+        if cfg == "sky" and fi == 0:
+            assert n_sky > 0
