@@ -18,16 +18,22 @@ namespace swgpu
 namespace
 {
 
-__device__ __forceinline__ CV tonemap(CV c, const PostArgs& a)
+// TonemappingFunction::inv_scale_vec lanes of the frame: from device memory when the frame's exposure
+// is uploaded with it (a replayed frame graph), else from the arguments.
+__device__ __forceinline__ float4 tonemap_scale(const PostArgs& a)
+{
+	if (a.inv_scale_dev) return make_float4(a.inv_scale_dev[0], a.inv_scale_dev[1], a.inv_scale_dev[2], a.inv_scale_dev[3]);
+	return make_float4(a.inv_scale[0], a.inv_scale[1], a.inv_scale[2], a.inv_scale[3]);
+}
+
+__device__ __forceinline__ CV tonemap(CV c, const PostArgs& a, float4 isc)
 {
 	// TonemappingFunction::do_it: c / (c * inv_255 + inv_scale), unfused (postprocessor.rs:1019-1023).
 	// The alpha lane of both vectors is 0 (from_color_f32x3), so for the non-negative alpha sums here it
 	// divides by +0: +inf or NaN, which the Color32 conversion's min(255) turns into 255 either way.
-	const float alpha = (a.inv_255[3] == 0.0f && a.inv_scale[3] == 0.0f)
-		? 255.0f
-		: __fdiv_rn(c.a, mad2(c.a, a.inv_255[3], a.inv_scale[3]));
-	return CV{__fdiv_rn(c.b, mad2(c.b, a.inv_255[0], a.inv_scale[0])), __fdiv_rn(c.g, mad2(c.g, a.inv_255[1], a.inv_scale[1])),
-		__fdiv_rn(c.r, mad2(c.r, a.inv_255[2], a.inv_scale[2])), alpha};
+	const float alpha = (a.inv_255[3] == 0.0f && isc.w == 0.0f) ? 255.0f : __fdiv_rn(c.a, mad2(c.a, a.inv_255[3], isc.w));
+	return CV{__fdiv_rn(c.b, mad2(c.b, a.inv_255[0], isc.x)), __fdiv_rn(c.g, mad2(c.g, a.inv_255[1], isc.y)),
+		__fdiv_rn(c.r, mad2(c.r, a.inv_255[2], isc.z)), alpha};
 }
 
 // Sequential f32 sum over `n` lines of 4-lane values, in line order, as the reference's loop does; the
@@ -340,6 +346,7 @@ __global__ void __launch_bounds__(256) pp_blur_v_tonemap_kernel(PostArgs a)
 	// 4 horizontally adjacent pixels per thread: 64 threads per 256-pixel line, lines ly, ly + 4, ... of
 	// the tile (TM_H / 4 of them), their HDR loads all issued first
 	const uint32_t lx = 4 * (threadIdx.x & 63), ly0 = threadIdx.x >> 6;
+	const float4 isc = tonemap_scale(a);
 	if (lx >= tw) return;
 	const uint32_t n = min(4u, tw - lx);
 	const unsigned long long* hdr = reinterpret_cast<const unsigned long long*>(a.hdr);
@@ -379,7 +386,7 @@ __global__ void __launch_bounds__(256) pp_blur_v_tonemap_kernel(PostArgs a)
 		uint32_t o[4];
 #pragma unroll
 		for (int k = 0; k < 4; ++k)
-			o[k] = k < int(n) ? cv_to_c32(tonemap(bloom_sum<S, LINEAR>(a, tile, x + k, y, cv_from_c64(p[j][k])), a)) : 0u;
+			o[k] = k < int(n) ? cv_to_c32(tonemap(bloom_sum<S, LINEAR>(a, tile, x + k, y, cv_from_c64(p[j][k])), a, isc)) : 0u;
 		if (n == 4 && (dst & 3) == 0 && (reinterpret_cast<uintptr_t>(a.dst) & 15) == 0)
 			*reinterpret_cast<uint4*>(a.dst + dst) = make_uint4(o[0], o[1], o[2], o[3]);
 		else
@@ -418,7 +425,7 @@ __global__ void __launch_bounds__(256) pp_tonemap_plain_kernel(PostArgs a)
 	const uint32_t y = blockIdx.y;
 	if (x >= a.width) return;
 	const CV c = cv_from_c64(__ldg(reinterpret_cast<const unsigned long long*>(a.hdr) + uint64_t(y) * a.width + x));
-	a.dst[uint64_t(y) * a.dst_pitch + x] = cv_to_c32(tonemap(c, a));
+	a.dst[uint64_t(y) * a.dst_pitch + x] = cv_to_c32(tonemap(c, a, tonemap_scale(a)));
 }
 
 __device__ __forceinline__ uint32_t avg32(uint32_t a, uint32_t b) { return (((a ^ b) & 0xFEFEFEFEu) >> 1) + (a & b); }

@@ -106,15 +106,11 @@ __device__ inline uint32_t warp_clip_pass(T& v, int c, uint32_t n, T* buf, F ise
 		else if (pc == 1)
 			emit_i = true;
 	}
-	const uint32_t e = uint32_t(emit_i) + uint32_t(emit_v);
-	uint32_t incl = e;
-	for (int o = 1; o < 32; o <<= 1)
-	{
-		const uint32_t t = __shfl_up_sync(FULL_MASK, incl, o);
-		if (lane >= uint32_t(o)) incl += t;
-	}
-	const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
-	const uint32_t pos = incl - e;
+	// output position: elements emitted by the lanes before this one (each emits 0, 1 or 2)
+	const uint32_t bi = __ballot_sync(FULL_MASK, emit_i), bv = __ballot_sync(FULL_MASK, emit_v);
+	const uint32_t before = (1u << lane) - 1u;
+	const uint32_t pos = uint32_t(__popc(bi & before) + __popc(bv & before));
+	const uint32_t total = uint32_t(__popc(bi) + __popc(bv));
 	if (emit_i && pos < MAXV) buf[pos] = isect(pv, v);
 	if (emit_v && pos + uint32_t(emit_i) < MAXV) buf[pos + uint32_t(emit_i)] = v;
 	__syncwarp();
@@ -145,6 +141,28 @@ __device__ inline uint32_t warp_project_and_clip(const Vec3 planes[8], Vec3 vt, 
 	}
 	out = p;
 	return count;
+}
+
+// ceil(RN(log2(x)) * scale + bias) for the two ceil decisions of the preparation (calculate_mip:
+// scale 0.5, bias mip_bias; the z scale of draw_polygon: scale 1, bias 0) - the value the host gets from
+// log2_rn. The decision is monotone in the logarithm, so it is taken from log2f's result widened by a
+// few representable steps on both sides (more than log2f's error); only when the two ends disagree is
+// the correctly rounded logarithm evaluated in double precision.
+__device__ inline float ceil_log2_decision(float x, float scale, float bias)
+{
+	const float lf = log2f(x);
+	if (lf == lf && fabsf(lf) < 1.0e30f)
+	{
+		float lo = lf, hi = lf;
+		for (int k = 0; k < 4; ++k)
+		{
+			lo = nextafterf(lo, -INFINITY);
+			hi = nextafterf(hi, INFINITY);
+		}
+		const float c_lo = ceilf(lo * scale + bias), c_hi = ceilf(hi * scale + bias);
+		if (c_lo == c_hi) return c_lo;
+	}
+	return ceilf(swhost::log2_rn(x) * scale + bias);
 }
 
 // Sequential `if (x < best) { best = x; at = i; }` over the valid lanes in lane order, from best = init:
@@ -179,23 +197,40 @@ __device__ inline float warp_first_max(float x, bool valid, float init, int* at)
 	return __shfl_sync(FULL_MASK, x, *at);
 }
 
+constexpr uint32_t PREP_SMEM_LEAFS = 512; // leaf table staged per CTA up to this many leafs
+
 __global__ void __launch_bounds__(PREP_WARPS * 32) prep_polygons_kernel(PrepArgs a)
 {
 	__shared__ WarpClipBuf s_buf[PREP_WARPS];
+	__shared__ uint32_t s_base[PREP_SMEM_LEAFS + 1];
 	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
 	const uint32_t c = blockIdx.x * PREP_WARPS + warp;
 	pdl_trigger(); // the compaction may be scheduled; it waits for this grid before reading
-	if (c >= a.num_candidates) return;
+	const PrepFrame& frame = *a.frame;
+	const uint32_t num_candidates = frame.num_candidates, num_leafs = frame.num_leafs;
+	if (blockIdx.x * PREP_WARPS >= num_candidates) return; // the grid is sized for the capacity
+	const bool staged = num_leafs <= PREP_SMEM_LEAFS;
+	if (staged)
+	{
+		for (uint32_t i = threadIdx.x; i <= num_leafs; i += blockDim.x) s_base[i] = __ldg(a.leaf_cand_base + i);
+		__syncthreads();
+	}
+	if (c >= num_candidates) return;
 	WarpClipBuf& buf = s_buf[warp];
-	const uint32_t li = find_segment(a.leaf_cand_base, a.num_leafs, c);
+	const uint32_t* cand_base = staged ? s_base : a.leaf_cand_base;
+	const uint32_t li = find_segment(cand_base, num_leafs, c);
 	const SwViewLeaf& leaf = a.leafs[li];
-	const uint32_t pi = leaf.first_polygon + (c - a.leaf_cand_base[li]);
+	const uint32_t pi = leaf.first_polygon + (c - cand_base[li]);
 	const SwMapPolygon& p = a.polygons[pi];
+	// the leaf's first 32 lights, one per lane, loaded ahead of their use
+	const uint32_t leaf_first_light = leaf.first_light, leaf_num_lights = leaf.num_lights;
+	const uint32_t my_light = lane < leaf_num_lights ? uint32_t(a.leaf_lights[leaf_first_light + lane]) : 0u;
+	const SwLight light0 = a.lights[lane < leaf_num_lights ? my_light : 0u];
 	PrepCand& out = a.cands[c];
 	PrepKey& key = a.keys[c];
 
 	// prepare_polygon_surface (partial_renderer.rs:1464-1638)
-	const Mat4 planes_matrix = load_mat4(a.planes);
+	const Mat4 planes_matrix = load_mat4(frame.planes);
 	const Vec4 plane_transformed = planes_matrix * swhost::extend(swhost::poly_vec3(p.plane), -p.plane[3]);
 	const uint32_t flags = p.flags;
 	if (plane_transformed.w <= 0.0f || !(flags & SW_POLY_DRAW))
@@ -203,7 +238,7 @@ __global__ void __launch_bounds__(PREP_WARPS * 32) prep_polygons_kernel(PrepArgs
 		if (lane == 0) key = PrepKey{0ull, 0u, 0u, 0u, 0};
 		return;
 	}
-	const Mat4 view = load_mat4(a.view);
+	const Mat4 view = load_mat4(frame.view);
 	const uint32_t nv = p.num_vertices < MAXV ? p.num_vertices : MAXV;
 	const Vec3* mv = reinterpret_cast<const Vec3*>(a.map_vertices);
 	const Vec3 vt = lane < nv ? swhost::view_transform(view, mv[p.first_vertex + lane]) : swhost::v3(0.0f, 0.0f, 1.0f);
@@ -245,8 +280,7 @@ __global__ void __launch_bounds__(PREP_WARPS * 32) prep_polygons_kernel(PrepArgs
 				te.d_tc_dy[i] * (de.k + de.d_inv_z_dx * mip_point.x) - (te.k[i] + te.d_tc_dx[i] * mip_point.x) * de.d_inv_z_dy;
 			d_tc_2[i] = (d_tc_dx * d_tc_dx + d_tc_dy * d_tc_dy) * z_4;
 		}
-		const float mip_f = swhost::log2_rn(fmaxf(d_tc_2[0], d_tc_2[1])) * 0.5f + a.mip_bias;
-		const int32_t m = swhost::as_i32(ceilf(mip_f));
+		const int32_t m = swhost::as_i32(ceil_log2_decision(fmaxf(d_tc_2[0], d_tc_2[1]), 0.5f, frame.mip_bias));
 		mip = uint32_t(m < 0 ? 0 : (m > int32_t(swhost::PREP_MAX_MIP) ? int32_t(swhost::PREP_MAX_MIP) : m));
 	}
 	const float mip_scale = 1.0f / float(1u << mip);
@@ -304,16 +338,22 @@ __global__ void __launch_bounds__(PREP_WARPS * 32) prep_polygons_kernel(PrepArgs
 	SwSurfaceDesc d;
 	swhost::make_surface_desc(p, sp, 0, a.directional != 0, a.simple_lightmaps != 0, d);
 	if (flags & SW_POLY_DIFFUSE_LAYER)
-		for (uint32_t base = 0; base < leaf.num_lights && d.num_lights < SW_MAX_POLYGON_LIGHTS; base += 32)
+		for (uint32_t base = 0; base < leaf_num_lights && d.num_lights < SW_MAX_POLYGON_LIGHTS; base += 32)
 		{
 			const uint32_t k = base + lane;
-			const bool hit = k < leaf.num_lights && swhost::polygon_is_affected_by_light(p, a.lights[a.leaf_lights[leaf.first_light + k]]);
+			bool hit = false;
+			uint32_t light = my_light;
+			if (k < leaf_num_lights)
+			{
+				if (base > 0) light = a.leaf_lights[leaf_first_light + k];
+				hit = swhost::polygon_is_affected_by_light(p, base > 0 ? a.lights[light] : light0);
+			}
 			uint32_t mask = __ballot_sync(FULL_MASK, hit);
 			while (mask && d.num_lights < SW_MAX_POLYGON_LIGHTS)
 			{
 				const uint32_t b = uint32_t(__ffs(mask) - 1);
 				mask &= mask - 1;
-				d.lights[d.num_lights++] = a.leaf_lights[leaf.first_light + base + b];
+				d.lights[d.num_lights++] = uint16_t(__shfl_sync(FULL_MASK, light, int(b)));
 			}
 		}
 	if (lane == 0) out.desc = d;
@@ -351,7 +391,7 @@ __global__ void __launch_bounds__(PREP_WARPS * 32) prep_polygons_kernel(PrepArgs
 				dc.mode = SW_RASTER_AFFINE;
 			else
 			{
-				const float z_scale = swhost::exp2_int(-5.0f - ceilf(swhost::log2_rn(fmaxf(max_inv_z, 1.0f / float(1 << 20)))));
+				const float z_scale = swhost::exp2_int(-5.0f - ceil_log2_decision(fmaxf(max_inv_z, 1.0f / float(1 << 20)), 1.0f, 0.0f));
 				dd = swhost::DepthEquation{dd.d_inv_z_dx * z_scale, dd.d_inv_z_dy * z_scale, dd.k * z_scale};
 				for (int i = 0; i < 2; ++i)
 				{
@@ -429,35 +469,39 @@ __global__ void __launch_bounds__(COMPACT_THREADS, 1) prep_compact_kernel(PrepAr
 {
 	__shared__ uint32_t s_error;
 	__shared__ uint32_t s_cand_base[SMEM_LEAFS + 1], s_slot_base[SMEM_LEAFS + 1], s_draw_leaf[SMEM_LEAFS];
+	__shared__ uint32_t s_vcand[COMPACT_THREADS], s_vbase[COMPACT_THREADS + 1]; // the chunk's draws: vertex copy list
 	const uint32_t tid = threadIdx.x;
 	if (tid == 0) s_error = 0;
 	// Before the per-candidate grid has finished: the uploaded index arrays and the host's draws
 	// (draw_skybox: they come first, with their row records).
-	const bool staged = a.num_leafs <= SMEM_LEAFS;
+	const PrepFrame& frame = *a.frame;
+	const uint32_t num_leafs = frame.num_leafs, num_candidates = frame.num_candidates, num_draw_leafs = frame.num_draw_leafs;
+	const uint32_t num_host_draws = frame.num_host_draws, num_host_vertices = frame.num_host_vertices;
+	const bool staged = num_leafs <= SMEM_LEAFS;
 	if (staged)
 	{
-		for (uint32_t i = tid; i <= a.num_leafs; i += blockDim.x) s_cand_base[i] = __ldg(a.leaf_cand_base + i);
-		for (uint32_t i = tid; i <= a.num_draw_leafs; i += blockDim.x) s_slot_base[i] = __ldg(a.draw_slot_base + i);
-		for (uint32_t i = tid; i < a.num_draw_leafs; i += blockDim.x) s_draw_leaf[i] = __ldg(a.draw_leaf + i);
+		for (uint32_t i = tid; i <= num_leafs; i += blockDim.x) s_cand_base[i] = __ldg(a.leaf_cand_base + i);
+		for (uint32_t i = tid; i <= num_draw_leafs; i += blockDim.x) s_slot_base[i] = __ldg(a.draw_slot_base + i);
+		for (uint32_t i = tid; i < num_draw_leafs; i += blockDim.x) s_draw_leaf[i] = __ldg(a.draw_leaf + i);
 	}
 	const uint32_t* cand_base = staged ? s_cand_base : a.leaf_cand_base;
 	const uint32_t* slot_base = staged ? s_slot_base : a.draw_slot_base;
 	const uint32_t* draw_leaf = staged ? s_draw_leaf : a.draw_leaf;
-	for (uint32_t i = tid; i < a.num_host_draws && i < a.cap_draws; i += blockDim.x)
+	for (uint32_t i = tid; i < num_host_draws && i < a.cap_draws; i += blockDim.x)
 	{
 		a.draws[i] = a.host_draws[i];
 		a.draw_rows[i] = a.host_rows[i];
 	}
-	for (uint32_t i = tid; i < a.num_host_vertices && i < a.cap_vertices; i += blockDim.x) a.vertices[i] = a.host_vertices[i];
+	for (uint32_t i = tid; i < num_host_vertices && i < a.cap_vertices; i += blockDim.x) a.vertices[i] = a.host_vertices[i];
 	pdl_wait(); // prep_polygons_kernel has completed
 	__syncthreads();
 
 	// Surfaces in allocation order: index and texel offset are prefix sums over the candidates.
 	uint64_t num_surfaces = 0, total_texels = 0;
-	for (uint32_t base = 0; base < a.num_candidates; base += blockDim.x)
+	for (uint32_t base = 0; base < num_candidates; base += blockDim.x)
 	{
 		const uint32_t c = base + tid;
-		const PrepKey k = c < a.num_candidates ? a.keys[c] : PrepKey{0ull, 0u, 0u, 0u, 0};
+		const PrepKey k = c < num_candidates ? a.keys[c] : PrepKey{0ull, 0u, 0u, 0u, 0};
 		const bool vis = k.state == 1;
 		const uint64_t area = vis ? k.area : 0ull;
 		uint64_t x[2] = {vis ? 1ull : 0ull, area}, tot[2];
@@ -487,8 +531,8 @@ __global__ void __launch_bounds__(COMPACT_THREADS, 1) prep_compact_kernel(PrepAr
 	__syncthreads(); // surface offsets of every candidate are visible to the CTA
 
 	// Draws in submission order: drawn leafs back to front, each leaf's polygons in index order.
-	const uint32_t slots = a.num_draw_leafs ? slot_base[a.num_draw_leafs] : 0u;
-	uint64_t num_draws = a.num_host_draws, num_vertices = a.num_host_vertices, num_rows = a.num_host_rows;
+	const uint32_t slots = num_draw_leafs ? slot_base[num_draw_leafs] : 0u;
+	uint64_t num_draws = num_host_draws, num_vertices = num_host_vertices, num_rows = frame.num_host_rows;
 	for (uint32_t base = 0; base < slots; base += blockDim.x)
 	{
 		const uint32_t slot = base + tid;
@@ -496,7 +540,7 @@ __global__ void __launch_bounds__(COMPACT_THREADS, 1) prep_compact_kernel(PrepAr
 		uint32_t c = 0;
 		if (slot < slots)
 		{
-			const uint32_t j = find_segment(slot_base, a.num_draw_leafs, slot);
+			const uint32_t j = find_segment(slot_base, num_draw_leafs, slot);
 			c = cand_base[draw_leaf[j]] + (slot - slot_base[j]);
 			k = a.keys[c];
 		}
@@ -505,21 +549,34 @@ __global__ void __launch_bounds__(COMPACT_THREADS, 1) prep_compact_kernel(PrepAr
 		const uint32_t nr = emit ? k.row_n : 0u;
 		uint64_t x[3] = {emit ? 1ull : 0ull, nv, nr}, tot[3];
 		block_scan_exclusive<3>(x, tot);
+		const bool fits = num_draws + tot[0] <= a.cap_draws && num_vertices + tot[1] <= a.cap_vertices &&
+						  num_rows + tot[2] <= a.cap_rows;
 		if (emit)
 		{
 			const uint64_t di = num_draws + x[0], vb = num_vertices + x[1], rb = num_rows + x[2];
-			if (di < a.cap_draws && vb + nv <= a.cap_vertices && rb + nr <= a.cap_rows)
+			if (fits)
 			{
 				SwDrawCmd d = a.cands[c].draw;
 				d.first_vertex = uint32_t(vb);
 				d.tex_offset = a.cands[c].surface_offset;
 				a.draws[di] = d;
-				for (uint32_t q = 0; q < nv; ++q) a.vertices[vb + q] = a.cands[c].v[q];
 				a.draw_rows[di] = DrawRows{uint32_t(rb), k.row_y0, nr, 0u};
 			}
 			else
 				atomicOr(&s_error, 1u);
+			s_vcand[x[0]] = c;
+			s_vbase[x[0]] = uint32_t(x[1]);
 		}
+		if (tid == 0) s_vbase[tot[0]] = uint32_t(tot[1]);
+		__syncthreads();
+		// the chunk's vertices, copied by the whole CTA
+		if (fits)
+			for (uint32_t t = tid; t < uint32_t(tot[1]); t += blockDim.x)
+			{
+				const uint32_t j = find_segment(s_vbase, uint32_t(tot[0]), t);
+				a.vertices[num_vertices + t] = a.cands[s_vcand[j]].v[t - s_vbase[j]];
+			}
+		__syncthreads();
 		num_draws += tot[0];
 		num_vertices += tot[1];
 		num_rows += tot[2];
@@ -554,9 +611,9 @@ __global__ void __launch_bounds__(COMPACT_THREADS, 1) prep_compact_kernel(PrepAr
 
 int launch_prep(const PrepArgs& args, cudaStream_t stream)
 {
-	if (args.num_candidates > 0)
+	if (args.cap_candidates > 0)
 	{
-		prep_polygons_kernel<<<(args.num_candidates + PREP_WARPS - 1) / PREP_WARPS, PREP_WARPS * 32, 0, stream>>>(args);
+		prep_polygons_kernel<<<(args.cap_candidates + PREP_WARPS - 1) / PREP_WARPS, PREP_WARPS * 32, 0, stream>>>(args);
 		launch_dependent(prep_compact_kernel, dim3(1), dim3(COMPACT_THREADS), 0, stream, args);
 	}
 	else

@@ -118,7 +118,7 @@ __device__ __forceinline__ uint32_t wrap(int32_t a, uint32_t b)
 // Lighting of one texel (surfaces.rs:515-842); returns the ColorVec before conversion.
 template <bool DIRECTIONAL>
 __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const SurfaceGpu& s, uint64_t texel, uint32_t u,
-	uint32_t v)
+	uint32_t v, V3 cam)
 {
 	const uint32_t tex_flags = s.flags & 7u;
 	const bool use_normal_map = (tex_flags & SW_TEX_HAS_NORMAL_MAP) != 0;
@@ -141,8 +141,6 @@ __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const Surf
 	}
 	else if (spec != 0)
 		rough = fmul(float(packed >> 24), NORMAL_UNPACK_SCALE);
-
-	const V3 cam = mkv3(a.cam_pos[0], a.cam_pos[1], a.cam_pos[2]);
 
 	CV albedo = cv_zero(); // total_light_albedo_modulated
 	CV direct = cv_zero(); // total_light_direct
@@ -293,6 +291,8 @@ __global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
 	typedef typename P::T T;
 	T* arena = static_cast<T*>(a.arena);
 	const uint64_t total = a.counts ? a.counts->total_texels : a.total_work;
+	const V3 cam = a.cam_pos_dev ? mkv3(a.cam_pos_dev[0], a.cam_pos_dev[1], a.cam_pos_dev[2])
+								 : mkv3(a.cam_pos[0], a.cam_pos[1], a.cam_pos[2]);
 	const uint32_t num_surfaces = a.counts ? a.counts->num_surfaces : a.num_surfaces;
 	const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
 	const uint32_t lane = threadIdx.x & 31u;
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
 			const uint32_t su = wrap(s.tc0 + int32_t(u), s.tex_w);
 			const uint64_t texel =
 				__ldg(reinterpret_cast<const unsigned long long*>(a.texels) + s.tex_offset + uint64_t(sv) * s.tex_w + su);
-			out = P::from_cv(shade_texel<DIRECTIONAL>(a, s, texel, u, v));
+			out = P::from_cv(shade_texel<DIRECTIONAL>(a, s, texel, u, v, cam));
 		}
 		if (s.flags & SW_SG_EMISSIVE) out = emissive_mix<P>(a, s, u, v, out, diffuse_layer);
 		arena[s.out_offset + local] = out;

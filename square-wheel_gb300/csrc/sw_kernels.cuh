@@ -52,6 +52,7 @@ struct SurfaceKernelArgs
 	const SwDirectionalLightmapElement* directional_lightmaps;
 	const SwLight* lights;
 	float cam_pos[3];
+	const float* cam_pos_dev; // when set, the camera position is read here (a replayed frame graph)
 	void* arena;
 };
 
@@ -270,34 +271,38 @@ struct PrepKey
 	int32_t row_y0;
 };
 
+// The per-frame values of the preparation, uploaded with the frame (a replayed graph's kernel
+// arguments do not change between frames).
+struct PrepFrame
+{
+	float view[16], planes[16]; // column-major
+	float mip_bias;
+	uint32_t num_leafs;
+	uint32_t num_candidates;
+	uint32_t num_draw_leafs;
+	uint32_t num_host_draws, num_host_vertices;
+	uint64_t num_host_rows;
+};
+
 struct PrepArgs
 {
+	const PrepFrame* frame;
 	const SwMapPolygon* polygons;
 	const float* map_vertices; // xyz
 	const SwViewLeaf* leafs;
 	const uint32_t* leaf_cand_base; // num_leafs + 1: first candidate of each leaf
-	uint32_t num_leafs;
-	uint32_t num_candidates;
 	const uint16_t* leaf_lights;
 	const SwLight* lights;
 	const uint32_t* draw_leaf;      // draw order -> leaf
 	const uint32_t* draw_slot_base; // num_draw_leafs + 1: first draw slot of each drawn leaf
-	uint32_t num_draw_leafs;
-	float mip_bias;
-	float view[16], planes[16]; // column-major
 	uint32_t directional, simple_lightmaps;
 	int32_t height;
 	// draws prepared on the host (skybox), placed first
 	const SwDrawCmd* host_draws;
 	const SwVertex16* host_vertices;
 	const DrawRows* host_rows;
-	uint32_t num_host_draws, num_host_vertices;
-	uint64_t num_host_rows;
 	const SwTextureMip* texture_mips;
 	const SwEmissiveMip* emissive_mips;
-	uint32_t num_texture_mips, num_emissive_mips;
-	uint32_t num_lights;
-	uint64_t num_lightmap_elements; // of the lightmap kind in use
 	PrepCand* cands;
 	PrepKey* keys;
 	// outputs and their capacities
@@ -308,11 +313,12 @@ struct PrepArgs
 	SwVertex16* vertices;
 	DrawRows* draw_rows;
 	SwViewCounts* counts;
-	uint32_t cap_surfaces, cap_draws, cap_vertices;
+	uint32_t cap_candidates, cap_surfaces, cap_draws, cap_vertices;
 	uint64_t cap_texels, cap_rows;
 };
 
-// Per-candidate preparation (many CTAs), then one CTA's ordered compaction.
+// Per-candidate preparation (a grid for cap_candidates polygons; warps beyond the frame's candidates
+// return at once), then one CTA's ordered compaction.
 int launch_prep(const PrepArgs& args, cudaStream_t stream);
 
 // ---- postprocessor / upscaler ----
@@ -332,6 +338,7 @@ struct PostArgs
 	int32_t kernel_h[33];
 	int32_t kernel_v[33];
 	float inv_scale[4]; // TonemappingFunction::inv_scale_vec lanes
+	const float* inv_scale_dev; // when set, the four lanes are read here (a replayed frame graph)
 	float inv_255[4];
 	uint32_t linear_filter;
 	uint32_t use_bloom;

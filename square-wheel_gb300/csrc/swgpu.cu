@@ -44,6 +44,24 @@ struct Staging
 	bool pending = false;
 };
 
+// Everything a view frame graph (sw_draw_frame_view) bakes in: when this differs from the graph's, it is
+// captured again.
+struct ViewGraphKey
+{
+	PrepArgs prep;
+	SurfaceKernelArgs surf;
+	RasterArgs raster;
+	PostArgs post;
+	const void* staging;
+	size_t block_bytes;
+	unsigned surface_blocks;
+	int surface_blocks_per_sm;
+	uint32_t raster_tile, pixel_format, postprocess, dst_pitch;
+	void* dst;
+	int32_t dst_is_device;
+	uint32_t slot;
+};
+
 } // namespace
 
 struct SwCtx
@@ -134,7 +152,13 @@ struct SwCtx
 	uint64_t view_seq = 0, hint_seq = 0;
 	uint64_t view_work_hint = 0; // texels of the latest frame read back (sizes the surface grid)
 	uint32_t view_surfaces_cap = 0, view_draws_cap = 0, view_vertices_cap = 0;
-	cudaGraphExec_t vexec = nullptr;
+	cudaGraphExec_t vexec[2] = {nullptr, nullptr}; // one per staging block, replayed while its key holds
+	ViewGraphKey vkey[2];
+	uint64_t vcap_lights = 0, vcap_leafs = 0, vcap_leaf_lights = 0, vcap_host_draws = 0, vcap_host_vertices = 0;
+	unsigned view_surface_blocks = 0;
+	uint64_t view_captures = 0;
+	std::vector<uint32_t> v_draw_leaf;
+	std::vector<DrawRows> v_host_rows;
 
 	// Optional per-stage device timing (sw_enable_timing).
 	bool timing = false;
@@ -158,6 +182,7 @@ enum Stage
 RasterArgs raster_args(SwCtx* ctx)
 {
 	RasterArgs a;
+	std::memset(&a, 0, sizeof(a)); // padding included: view graph keys compare argument blocks bytewise
 	a.draws = static_cast<const SwDrawCmd*>(ctx->draws.ptr);
 	a.vertices = static_cast<const SwVertex16*>(ctx->vertices.ptr);
 	a.num_draws = ctx->num_draws;
@@ -494,7 +519,8 @@ int sw_destroy(SwCtx* ctx)
 	for (DevBuf* b : bufs) release(*b);
 	for (const SwCtx::HostRange& h : ctx->registered) cudaHostUnregister(h.ptr);
 	if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
-	if (ctx->vexec) cudaGraphExecDestroy(ctx->vexec);
+	for (cudaGraphExec_t e : ctx->vexec)
+		if (e) cudaGraphExecDestroy(e);
 	if (ctx->h_counts) cudaFreeHost(ctx->h_counts);
 	for (cudaEvent_t e : ctx->ev_counts)
 		if (e) cudaEventDestroy(e);
@@ -599,6 +625,7 @@ struct SurfaceInputs
 static int launch_surfaces(SwCtx* ctx, const SurfaceInputs* in = nullptr)
 {
 	SurfaceKernelArgs a;
+	std::memset(&a, 0, sizeof(a)); // optional fields (counts, cam_pos_dev) stay unset on this path
 	a.surfaces = in ? in->surfaces : static_cast<const SurfaceGpu*>(ctx->surfaces.ptr);
 	a.work_prefix = in ? in->work_prefix : static_cast<const uint64_t*>(ctx->work_prefix.ptr);
 	a.num_surfaces = ctx->last_num_surfaces;
@@ -1437,6 +1464,42 @@ void consume_view_counts(SwCtx* ctx, uint32_t slot)
 }
 } // namespace
 
+namespace
+{
+uint64_t pow2_at_least(uint64_t v, uint64_t floor_value)
+{
+	uint64_t c = floor_value;
+	while (c < v) c <<= 1;
+	return c;
+}
+
+// Fixed layout of a view frame's upload block for the current capacities (the replayed graph copies the
+// whole block): per-frame header (PrepFrame, camera position, tonemap scale), then the arrays.
+struct ViewBlock
+{
+	size_t frame, cam, inv_scale, lights, leafs, cand_base, leaf_lights, draw_leaf, slot_base, draws, vertices, rows, bytes;
+};
+ViewBlock view_block(const SwCtx* ctx)
+{
+	ViewBlock v;
+	v.frame = 0;
+	v.cam = align_up(v.frame + sizeof(PrepFrame), 16);
+	v.inv_scale = v.cam + 16;
+	v.lights = align_up(v.inv_scale + 16, 256);
+	v.leafs = align_up(v.lights + ctx->vcap_lights * sizeof(SwLight), 256);
+	v.cand_base = align_up(v.leafs + ctx->vcap_leafs * sizeof(SwViewLeaf), 256);
+	v.leaf_lights = align_up(v.cand_base + (ctx->vcap_leafs + 1) * 4, 256);
+	v.draw_leaf = align_up(v.leaf_lights + ctx->vcap_leaf_lights * 2, 256);
+	v.slot_base = align_up(v.draw_leaf + ctx->vcap_leafs * 4, 256);
+	v.draws = align_up(v.slot_base + (ctx->vcap_leafs + 1) * 4, 256);
+	v.vertices = align_up(v.draws + ctx->vcap_host_draws * sizeof(SwDrawCmd), 256);
+	v.rows = align_up(v.vertices + ctx->vcap_host_vertices * sizeof(SwVertex16), 256);
+	v.bytes = align_up(v.rows + ctx->vcap_host_draws * sizeof(DrawRows), 256);
+	return v;
+}
+
+} // namespace
+
 int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 {
 	if (!ctx || !in) return SW_ERR_INVALID_ARGUMENT;
@@ -1455,9 +1518,10 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 		if (ctx->counts_pending[k] && cudaEventQuery(ctx->ev_counts[k]) == cudaSuccess) consume_view_counts(ctx, k);
 	cudaGetLastError(); // a not-ready query is not an error
 
-	// 1. validate the leafs and derive the candidate and draw-slot numbering and the capacities
+	// 1. validate the leafs and derive the candidate and draw-slot numbering and the capacity bounds
 	const uint32_t nl = f.num_leafs;
-	std::vector<uint32_t> draw_leaf(nl, 0xFFFFFFFFu);
+	std::vector<uint32_t>& draw_leaf = ctx->v_draw_leaf;
+	draw_leaf.assign(nl, 0xFFFFFFFFu);
 	uint32_t num_draw_leafs = 0;
 	uint64_t candidates = 0, slots = 0, texel_bound = 0, row_bound = 0;
 	for (uint32_t i = 0; i < nl; ++i)
@@ -1492,77 +1556,57 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	for (uint32_t i = 0; i < f.num_draws; ++i)
 		if (f.draws[i].tex_source != SW_TEXSRC_SKYBOX)
 			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: host draws of a view frame read the skybox", i);
-	ctx->frame = p;
-	ctx->num_lights = f.num_lights;
-	const uint64_t cap_draws = uint64_t(f.num_draws) + slots;
-	const uint64_t cap_vertices = uint64_t(f.num_vertices) + slots * SW_MAX_POLYGON_VERTICES;
-	if (cap_draws > 0x7FFFFFFFull || cap_vertices > 0x7FFFFFFFull) return fail(ctx, SW_ERR_LIMIT, "too many draws");
-
-	// 2. every per-frame array into one pinned staging block (two blocks alternate between frames)
-	const uint32_t slot = ctx->gset;
-	Staging& st = ctx->gstage[slot];
-	ctx->gset ^= 1u;
-	size_t off[10];
-	off[0] = 0;
-	off[1] = align_up(off[0] + std::max<size_t>(f.num_lights, 1) * sizeof(SwLight), 256);
-	off[2] = align_up(off[1] + std::max<size_t>(nl, 1) * sizeof(SwViewLeaf), 256);
-	off[3] = align_up(off[2] + (size_t(nl) + 1) * 4, 256);
-	off[4] = align_up(off[3] + std::max<size_t>(f.num_leaf_lights, 1) * 2, 256);
-	off[5] = align_up(off[4] + std::max<size_t>(num_draw_leafs, 1) * 4, 256);
-	off[6] = align_up(off[5] + (size_t(num_draw_leafs) + 1) * 4, 256);
-	off[7] = align_up(off[6] + std::max<size_t>(f.num_draws, 1) * sizeof(SwDrawCmd), 256);
-	off[8] = align_up(off[7] + std::max<size_t>(f.num_vertices, 1) * sizeof(SwVertex16), 256);
-	off[9] = align_up(off[8] + std::max<size_t>(f.num_draws, 1) * sizeof(DrawRows), 256);
-	void* hv = nullptr;
-	if ((r = staging_acquire(ctx, st, off[9], &hv))) return r;
-	if (ctx->counts_pending[slot])
-	{
-		// the frame that last used this staging set has finished (staging_acquire waited for it)
-		SW_CUDA(ctx, cudaEventSynchronize(ctx->ev_counts[slot]));
-		consume_view_counts(ctx, slot);
-	}
-	unsigned char* h = static_cast<unsigned char*>(hv);
-	if (f.num_lights) std::memcpy(h + off[0], f.lights, f.num_lights * sizeof(SwLight));
-	if (nl) std::memcpy(h + off[1], f.leafs, nl * sizeof(SwViewLeaf));
-	uint32_t* cand_base = reinterpret_cast<uint32_t*>(h + off[2]);
-	cand_base[0] = 0;
-	for (uint32_t i = 0; i < nl; ++i) cand_base[i + 1] = cand_base[i] + f.leafs[i].num_polygons;
-	if (f.num_leaf_lights) std::memcpy(h + off[3], f.leaf_lights, f.num_leaf_lights * 2);
-	uint32_t* dl = reinterpret_cast<uint32_t*>(h + off[4]);
-	uint32_t* slot_base = reinterpret_cast<uint32_t*>(h + off[5]);
-	slot_base[0] = 0;
-	for (uint32_t j = 0; j < num_draw_leafs; ++j)
-	{
-		dl[j] = draw_leaf[j];
-		slot_base[j + 1] = slot_base[j] + f.leafs[draw_leaf[j]].num_polygons;
-	}
+	std::vector<DrawRows>& host_draw_rows = ctx->v_host_rows;
+	host_draw_rows.resize(std::max<size_t>(f.num_draws, 1));
 	uint64_t host_rows = 0;
-	if ((r = prepare_draws(ctx, f.draws, f.num_draws, f.vertices, f.num_vertices, reinterpret_cast<DrawRows*>(h + off[8]),
-			 &host_rows)))
-		return r;
-	if (f.num_draws) std::memcpy(h + off[6], f.draws, f.num_draws * sizeof(SwDrawCmd));
-	if (f.num_vertices) std::memcpy(h + off[7], f.vertices, f.num_vertices * sizeof(SwVertex16));
-	const uint64_t cap_rows = host_rows + row_bound;
-	const uint64_t cap_surfaces = std::max<uint64_t>(candidates, 1);
-	const uint64_t cap_texels = std::max<uint64_t>(texel_bound, 1);
+	ctx->frame = p; // prepare_draws checks the host draws against this frame's size
+	if ((r = prepare_draws(ctx, f.draws, f.num_draws, f.vertices, f.num_vertices, host_draw_rows.data(), &host_rows))) return r;
+	ctx->num_lights = f.num_lights;
+	const uint64_t need_draws = uint64_t(f.num_draws) + slots;
+	const uint64_t need_vertices = uint64_t(f.num_vertices) + slots * SW_MAX_POLYGON_VERTICES;
+	const uint64_t need_rows = host_rows + row_bound;
+	if (need_draws > 0x7FFFFFFFull || need_vertices > 0x7FFFFFFFull) return fail(ctx, SW_ERR_LIMIT, "too many draws");
 
-	// 3. device buffers at their capacities (growing them synchronises)
+	// 2. capacities only grow (power-of-two steps): the upload block's layout and the device buffers
+	// stay the same from frame to frame, and so do the replayed graphs
+	ctx->vcap_lights = pow2_at_least(f.num_lights, std::max<uint64_t>(ctx->vcap_lights, 16));
+	ctx->vcap_leafs = pow2_at_least(nl, std::max<uint64_t>(ctx->vcap_leafs, 64));
+	ctx->vcap_leaf_lights = pow2_at_least(f.num_leaf_lights, std::max<uint64_t>(ctx->vcap_leaf_lights, 256));
+	ctx->vcap_host_draws = pow2_at_least(f.num_draws, std::max<uint64_t>(ctx->vcap_host_draws, 8));
+	ctx->vcap_host_vertices = pow2_at_least(f.num_vertices, std::max<uint64_t>(ctx->vcap_host_vertices, 64));
+	const ViewBlock vb = view_block(ctx);
 	const uint32_t bpp = bpp_of(p.pixel_format);
-	if ((r = ensure(ctx, ctx->frame_in, off[9]))) return r;
-	if ((r = ensure(ctx, ctx->cands, std::max<size_t>(candidates, 1) * sizeof(PrepCand)))) return r;
-	if ((r = ensure(ctx, ctx->keys, std::max<size_t>(candidates, 1) * sizeof(PrepKey)))) return r;
-	if ((r = ensure(ctx, ctx->descs, cap_surfaces * sizeof(SwSurfaceDesc)))) return r;
-	if ((r = ensure(ctx, ctx->surfaces, cap_surfaces * sizeof(SurfaceGpu)))) return r;
-	if ((r = ensure(ctx, ctx->work_prefix, (cap_surfaces + 1) * 8))) return r;
-	if ((r = ensure(ctx, ctx->arena, cap_texels * bpp))) return r;
+	const uint64_t cand_cap = pow2_at_least(candidates, 1024);
+	const uint64_t draw_cap = pow2_at_least(need_draws, 1024);
+	const uint64_t vert_cap = pow2_at_least(need_vertices, 8192);
+	const uint64_t row_cap = pow2_at_least(need_rows, 1u << 16);
+	const uint64_t texel_cap = pow2_at_least(texel_bound, 1u << 20);
+	if ((r = ensure(ctx, ctx->frame_in, vb.bytes))) return r;
+	if ((r = ensure(ctx, ctx->cands, cand_cap * sizeof(PrepCand)))) return r;
+	if ((r = ensure(ctx, ctx->keys, cand_cap * sizeof(PrepKey)))) return r;
+	if ((r = ensure(ctx, ctx->descs, cand_cap * sizeof(SwSurfaceDesc)))) return r;
+	if ((r = ensure(ctx, ctx->surfaces, cand_cap * sizeof(SurfaceGpu)))) return r;
+	if ((r = ensure(ctx, ctx->work_prefix, (cand_cap + 1) * 8))) return r;
+	if ((r = ensure(ctx, ctx->arena, texel_cap * bpp))) return r;
 	if ((r = ensure(ctx, ctx->view_counts, sizeof(SwViewCounts)))) return r;
-	if ((r = ensure_raster_buffers(ctx, uint32_t(cap_draws), uint32_t(cap_vertices), cap_rows))) return r;
+	if ((r = ensure_raster_buffers(ctx, uint32_t(draw_cap), uint32_t(vert_cap), row_cap))) return r;
 	if ((r = ensure_framebuffer(ctx, p))) return r;
+	// what the buffers hold (growth may have left them larger than asked)
+	auto elems = [](const DevBuf& b, size_t size) { return uint64_t(b.bytes / size); };
+	const uint64_t cap_candidates = std::min(elems(ctx->cands, sizeof(PrepCand)), elems(ctx->keys, sizeof(PrepKey)));
+	const uint64_t cap_surfaces = std::min({cap_candidates, elems(ctx->descs, sizeof(SwSurfaceDesc)),
+		elems(ctx->surfaces, sizeof(SurfaceGpu)), elems(ctx->work_prefix, 8) - 1});
+	const uint64_t cap_draws = std::min({elems(ctx->draws, sizeof(SwDrawCmd)), elems(ctx->draw_rows, sizeof(DrawRows)),
+		elems(ctx->rdraws, sizeof(RasterDraw)), elems(ctx->boxes, sizeof(RasterBox)), elems(ctx->part_counts, 4),
+		elems(ctx->parts, SW_RASTER_MAX_PARTS * sizeof(RasterPart))});
+	const uint64_t cap_vertices = elems(ctx->vertices, sizeof(SwVertex16));
+	const uint64_t cap_rows = elems(ctx->rows, sizeof(RasterRow));
+	const uint64_t cap_texels = elems(ctx->arena, bpp);
 	ctx->arena_texels = cap_texels;
 	ctx->arena_format = p.pixel_format;
 	ctx->view_surfaces_cap = uint32_t(cap_surfaces);
-	ctx->view_draws_cap = uint32_t(cap_draws);
-	ctx->view_vertices_cap = uint32_t(cap_vertices);
+	ctx->view_draws_cap = uint32_t(std::min<uint64_t>(cap_draws, 0xFFFFFFFFu));
+	ctx->view_vertices_cap = uint32_t(std::min<uint64_t>(cap_vertices, 0xFFFFFFFFu));
 	PostArgs pa;
 	void* post_out = nullptr;
 	bool direct_host = false;
@@ -1570,39 +1614,81 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 		(r = frame_post_target(ctx, p, f.post, f.color_modulate, f.dst, f.dst_pitch, f.dst_is_device, pa, &post_out, &direct_host)))
 		return r;
 
-	// 4. the graph: one upload, preparation, surface build beside the raster setup, tiles, postprocess
+	// 3. the upload block of this frame (two staging blocks alternate between frames)
+	const uint32_t slot = ctx->gset;
+	Staging& st = ctx->gstage[slot];
+	ctx->gset ^= 1u;
+	void* hv = nullptr;
+	if ((r = staging_acquire(ctx, st, vb.bytes, &hv))) return r;
+	if (ctx->counts_pending[slot])
+	{
+		// the frame that last used this staging set has finished (staging_acquire waited for it)
+		SW_CUDA(ctx, cudaEventSynchronize(ctx->ev_counts[slot]));
+		consume_view_counts(ctx, slot);
+	}
+	unsigned char* h = static_cast<unsigned char*>(hv);
+	PrepFrame& pf = *reinterpret_cast<PrepFrame*>(h + vb.frame);
+	std::memcpy(pf.view, f.view_matrix, sizeof(pf.view));
+	std::memcpy(pf.planes, f.planes_matrix, sizeof(pf.planes));
+	pf.mip_bias = f.mip_bias;
+	pf.num_leafs = nl;
+	pf.num_candidates = uint32_t(candidates);
+	pf.num_draw_leafs = num_draw_leafs;
+	pf.num_host_draws = f.num_draws;
+	pf.num_host_vertices = f.num_vertices;
+	pf.num_host_rows = host_rows;
+	float* cam = reinterpret_cast<float*>(h + vb.cam);
+	cam[0] = p.cam_pos[0], cam[1] = p.cam_pos[1], cam[2] = p.cam_pos[2], cam[3] = 0.0f;
+	float* isc = reinterpret_cast<float*>(h + vb.inv_scale);
+	if (f.postprocess)
+	{
+		for (int k = 0; k < 4; ++k) isc[k] = pa.inv_scale[k];
+		for (int k = 0; k < 4; ++k) pa.inv_scale[k] = 0.0f; // read from the block
+	}
+	if (f.num_lights) std::memcpy(h + vb.lights, f.lights, f.num_lights * sizeof(SwLight));
+	if (nl) std::memcpy(h + vb.leafs, f.leafs, nl * sizeof(SwViewLeaf));
+	uint32_t* cand_base = reinterpret_cast<uint32_t*>(h + vb.cand_base);
+	cand_base[0] = 0;
+	for (uint32_t i = 0; i < nl; ++i) cand_base[i + 1] = cand_base[i] + f.leafs[i].num_polygons;
+	if (f.num_leaf_lights) std::memcpy(h + vb.leaf_lights, f.leaf_lights, f.num_leaf_lights * 2);
+	uint32_t* dl = reinterpret_cast<uint32_t*>(h + vb.draw_leaf);
+	uint32_t* slot_base = reinterpret_cast<uint32_t*>(h + vb.slot_base);
+	slot_base[0] = 0;
+	for (uint32_t j = 0; j < num_draw_leafs; ++j)
+	{
+		dl[j] = draw_leaf[j];
+		slot_base[j + 1] = slot_base[j] + f.leafs[draw_leaf[j]].num_polygons;
+	}
+	if (f.num_draws)
+	{
+		std::memcpy(h + vb.draws, f.draws, f.num_draws * sizeof(SwDrawCmd));
+		std::memcpy(h + vb.rows, host_draw_rows.data(), f.num_draws * sizeof(DrawRows));
+	}
+	if (f.num_vertices) std::memcpy(h + vb.vertices, f.vertices, f.num_vertices * sizeof(SwVertex16));
+
+	// 4. kernel arguments: buffers and capacities only (the per-frame values are in the block)
 	unsigned char* d = static_cast<unsigned char*>(ctx->frame_in.ptr);
 	SwViewCounts* counts = static_cast<SwViewCounts*>(ctx->view_counts.ptr);
-	PrepArgs pr;
+	ViewGraphKey key;
+	std::memset(&key, 0, sizeof(key)); // padding too: keys are compared bytewise
+	PrepArgs& pr = key.prep;
+	pr.frame = reinterpret_cast<const PrepFrame*>(d + vb.frame);
 	pr.polygons = static_cast<const SwMapPolygon*>(ctx->map_polygons.ptr);
 	pr.map_vertices = static_cast<const float*>(ctx->map_vertices.ptr);
-	pr.leafs = reinterpret_cast<const SwViewLeaf*>(d + off[1]);
-	pr.leaf_cand_base = reinterpret_cast<const uint32_t*>(d + off[2]);
-	pr.num_leafs = nl;
-	pr.num_candidates = uint32_t(candidates);
-	pr.leaf_lights = reinterpret_cast<const uint16_t*>(d + off[3]);
-	pr.lights = reinterpret_cast<const SwLight*>(d + off[0]);
-	pr.draw_leaf = reinterpret_cast<const uint32_t*>(d + off[4]);
-	pr.draw_slot_base = reinterpret_cast<const uint32_t*>(d + off[5]);
-	pr.num_draw_leafs = num_draw_leafs;
-	pr.mip_bias = f.mip_bias;
-	std::memcpy(pr.view, f.view_matrix, sizeof(pr.view));
-	std::memcpy(pr.planes, f.planes_matrix, sizeof(pr.planes));
+	pr.leafs = reinterpret_cast<const SwViewLeaf*>(d + vb.leafs);
+	pr.leaf_cand_base = reinterpret_cast<const uint32_t*>(d + vb.cand_base);
+	pr.leaf_lights = reinterpret_cast<const uint16_t*>(d + vb.leaf_lights);
+	pr.lights = reinterpret_cast<const SwLight*>(d + vb.lights);
+	pr.draw_leaf = reinterpret_cast<const uint32_t*>(d + vb.draw_leaf);
+	pr.draw_slot_base = reinterpret_cast<const uint32_t*>(d + vb.slot_base);
 	pr.directional = p.use_directional_lightmaps ? 1u : 0u;
 	pr.simple_lightmaps = ctx->num_lightmap_elements > 1 ? 1u : 0u;
 	pr.height = int32_t(p.height);
-	pr.host_draws = reinterpret_cast<const SwDrawCmd*>(d + off[6]);
-	pr.host_vertices = reinterpret_cast<const SwVertex16*>(d + off[7]);
-	pr.host_rows = reinterpret_cast<const DrawRows*>(d + off[8]);
-	pr.num_host_draws = f.num_draws;
-	pr.num_host_vertices = f.num_vertices;
-	pr.num_host_rows = host_rows;
+	pr.host_draws = reinterpret_cast<const SwDrawCmd*>(d + vb.draws);
+	pr.host_vertices = reinterpret_cast<const SwVertex16*>(d + vb.vertices);
+	pr.host_rows = reinterpret_cast<const DrawRows*>(d + vb.rows);
 	pr.texture_mips = static_cast<const SwTextureMip*>(ctx->texture_mips.ptr);
 	pr.emissive_mips = static_cast<const SwEmissiveMip*>(ctx->emissive_mips.ptr);
-	pr.num_texture_mips = uint32_t(ctx->h_texture_mips.size());
-	pr.num_emissive_mips = uint32_t(ctx->h_emissive_mips.size());
-	pr.num_lights = f.num_lights;
-	pr.num_lightmap_elements = p.use_directional_lightmaps ? ctx->num_dir_lightmap_elements : ctx->num_lightmap_elements;
 	pr.cands = static_cast<PrepCand*>(ctx->cands.ptr);
 	pr.keys = static_cast<PrepKey*>(ctx->keys.ptr);
 	pr.descs = static_cast<SwSurfaceDesc*>(ctx->descs.ptr);
@@ -1612,63 +1698,103 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	pr.vertices = static_cast<SwVertex16*>(ctx->vertices.ptr);
 	pr.draw_rows = static_cast<DrawRows*>(ctx->draw_rows.ptr);
 	pr.counts = counts;
-	pr.cap_surfaces = uint32_t(cap_surfaces);
-	pr.cap_draws = uint32_t(cap_draws);
-	pr.cap_vertices = uint32_t(cap_vertices);
+	pr.cap_candidates = uint32_t(std::min<uint64_t>(cap_candidates, 0x7FFFFFFFu));
+	pr.cap_surfaces = uint32_t(std::min<uint64_t>(cap_surfaces, 0x7FFFFFFFu));
+	pr.cap_draws = uint32_t(std::min<uint64_t>(cap_draws, 0x7FFFFFFFu));
+	pr.cap_vertices = uint32_t(std::min<uint64_t>(cap_vertices, 0x7FFFFFFFu));
 	pr.cap_texels = cap_texels;
 	pr.cap_rows = cap_rows;
 
-	SurfaceKernelArgs sa;
+	SurfaceKernelArgs& sa = key.surf;
 	sa.surfaces = pr.surfaces;
 	sa.work_prefix = pr.work_prefix;
-	sa.num_surfaces = 0;
 	sa.directional = p.use_directional_lightmaps ? 1u : 0u;
-	sa.total_work = 0;
 	sa.counts = counts;
 	sa.texels = static_cast<const uint64_t*>(ctx->texels.ptr);
 	sa.emissive_pixels = static_cast<const uint32_t*>(ctx->emissive.ptr);
 	sa.lightmaps = static_cast<const float*>(ctx->lightmaps.ptr);
 	sa.directional_lightmaps = static_cast<const SwDirectionalLightmapElement*>(ctx->dir_lightmaps.ptr);
 	sa.lights = pr.lights;
-	for (int i = 0; i < 3; ++i) sa.cam_pos[i] = p.cam_pos[i];
+	sa.cam_pos_dev = reinterpret_cast<const float*>(d + vb.cam);
 	sa.arena = ctx->arena.ptr;
-	// grid: the last frame's texels with headroom (the kernel strides over whatever this frame has)
-	const uint64_t hint = ctx->view_work_hint ? ctx->view_work_hint + ctx->view_work_hint / 4 : (uint64_t(1) << 40);
+	// surface grid: from the latest frame's texels with headroom; it changes (and the graphs are captured
+	// again) only when the texel count leaves [grid/2, grid] blocks' worth
+	{
+		const uint64_t hint = ctx->view_work_hint ? ctx->view_work_hint + ctx->view_work_hint / 4 : (uint64_t(1) << 40);
+		const uint64_t max_blocks = uint64_t(ctx->num_sms) * std::max<uint32_t>(ctx->tuning.surface_blocks_per_sm, 1);
+		const uint64_t needed = std::min(std::max((hint + 255) / 256, uint64_t(ctx->num_sms)), max_blocks);
+		if (ctx->view_surface_blocks == 0 || needed > ctx->view_surface_blocks || needed < ctx->view_surface_blocks / 2 ||
+			ctx->view_surface_blocks > max_blocks)
+			ctx->view_surface_blocks = unsigned(std::min(needed + needed / 4, max_blocks));
+	}
+	key.surface_blocks = ctx->view_surface_blocks;
+	key.surface_blocks_per_sm = int(ctx->tuning.surface_blocks_per_sm);
 
-	RasterArgs ra = raster_args(ctx);
+	RasterArgs& ra = key.raster;
+	ra = raster_args(ctx);
 	ra.counts = counts;
 	ra.num_draws = 0;
-	ra.setup_blocks = uint32_t(std::min<uint64_t>(cap_draws, uint64_t(ctx->num_sms) * 2));
-	ra.total_rows = uint32_t(std::min<uint64_t>(cap_rows, 0xFFFFFFFFull));
+	ra.setup_blocks = uint32_t(ctx->num_sms) * 2;
+	ra.total_rows = 0;
+	if (f.postprocess)
+	{
+		key.post = pa;
+		key.post.inv_scale_dev = reinterpret_cast<const float*>(d + vb.inv_scale);
+	}
+	key.staging = st.host;
+	key.block_bytes = vb.bytes;
+	key.raster_tile = ctx->tuning.raster_tile;
+	key.pixel_format = p.pixel_format;
+	key.postprocess = f.postprocess ? 1u : 0u;
+	key.dst = f.dst;
+	key.dst_pitch = f.dst_pitch;
+	key.dst_is_device = f.dst_is_device;
+	key.slot = slot;
 
-	auto enqueue = [&]() -> int {
-		cudaStream_t s = ctx->stream, aux = ctx->aux;
-		SW_CUDA(ctx, cudaMemcpyAsync(d, h, off[9], cudaMemcpyHostToDevice, s));
-		int rr;
-		if ((rr = check_kernel(ctx, launch_prep(pr, s), "surface and draw preparation"))) return rr;
-		SW_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
-		SW_CUDA(ctx, cudaStreamWaitEvent(aux, ctx->ev_fork, 0));
-		if ((rr = check_kernel(ctx, launch_raster_setup(ra, aux), "raster setup"))) return rr;
-		SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, aux));
-		if ((rr = check_kernel(ctx,
-				 launch_surface_build(sa, p.pixel_format, ctx->num_sms, int(ctx->tuning.surface_blocks_per_sm), s, hint),
-				 "surface build")))
-			return rr;
-		SW_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_setup, 0));
-		if ((rr = check_kernel(ctx, launch_raster_tiles(ra, p.pixel_format, ctx->tuning.raster_tile, s), "raster"))) return rr;
-		if (f.postprocess)
-		{
-			if ((rr = check_kernel(ctx, launch_postprocess(pa, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join), "postprocess")))
+	// 5. replay this staging block's graph; capture it again when its key changed
+	cudaGraphExec_t& exec = ctx->vexec[slot];
+	if (!exec || std::memcmp(&ctx->vkey[slot], &key, sizeof(key)) != 0)
+	{
+		auto enqueue = [&]() -> int {
+			cudaStream_t s = ctx->stream, aux = ctx->aux;
+			SW_CUDA(ctx, cudaMemcpyAsync(d, st.host, vb.bytes, cudaMemcpyHostToDevice, s));
+			int rr;
+			if ((rr = check_kernel(ctx, launch_prep(key.prep, s), "surface and draw preparation"))) return rr;
+			SW_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
+			SW_CUDA(ctx, cudaStreamWaitEvent(aux, ctx->ev_fork, 0));
+			if ((rr = check_kernel(ctx, launch_raster_setup(key.raster, aux), "raster setup"))) return rr;
+			SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, aux));
+			if ((rr = check_kernel(ctx,
+					 launch_surface_build(key.surf, p.pixel_format, ctx->num_sms, int(ctx->tuning.surface_blocks_per_sm), s,
+						 uint64_t(key.surface_blocks) * 256),
+					 "surface build")))
 				return rr;
-			SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_average, ctx->average.ptr, 16, cudaMemcpyDeviceToHost, s));
-		}
-		else if (f.dst && f.dst_is_device)
-			SW_CUDA(ctx, cudaMemcpy2DAsync(f.dst, size_t(f.dst_pitch) * bpp, ctx->framebuffer.ptr, size_t(p.width) * bpp,
-							 size_t(p.width) * bpp, p.height, cudaMemcpyDeviceToDevice, s));
-		SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_counts + slot, counts, sizeof(SwViewCounts), cudaMemcpyDeviceToHost, s));
-		return SW_OK;
-	};
-	if ((r = capture_and_launch(ctx, ctx->vexec, enqueue))) return r;
+			SW_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_setup, 0));
+			if ((rr = check_kernel(ctx, launch_raster_tiles(key.raster, p.pixel_format, ctx->tuning.raster_tile, s), "raster")))
+				return rr;
+			if (f.postprocess)
+			{
+				if ((rr = check_kernel(ctx, launch_postprocess(key.post, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join),
+						 "postprocess")))
+					return rr;
+				SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_average, ctx->average.ptr, 16, cudaMemcpyDeviceToHost, s));
+			}
+			else if (f.dst && f.dst_is_device)
+				SW_CUDA(ctx, cudaMemcpy2DAsync(f.dst, size_t(f.dst_pitch) * bpp, ctx->framebuffer.ptr, size_t(p.width) * bpp,
+								 size_t(p.width) * bpp, p.height, cudaMemcpyDeviceToDevice, s));
+			SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_counts + slot, counts, sizeof(SwViewCounts), cudaMemcpyDeviceToHost, s));
+			return SW_OK;
+		};
+		if ((r = capture_and_launch(ctx, exec, enqueue))) return r;
+		ctx->vkey[slot] = key;
+		++ctx->view_captures;
+	}
+	else
+	{
+		stage_begin(ctx, STAGE_FRAME);
+		SW_CUDA(ctx, cudaGraphLaunch(exec, ctx->stream));
+		stage_end(ctx, STAGE_FRAME);
+	}
 	SW_CUDA(ctx, cudaEventRecord(ctx->ev_counts[slot], ctx->stream));
 	ctx->counts_pending[slot] = true;
 	ctx->counts_seq[slot] = ++ctx->view_seq;
