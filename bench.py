@@ -12,7 +12,9 @@ Workloads
       Frames walk the seeded 256-frame camera path. The host's per-frame work (visibility, surface
       preparation, draw setup) is done before the timed region; `value` is frames/s of device time
       (sum of the three stages' CUDA-event times on the library's stream, inputs resident in HBM);
-      `e2e` is frames/s through the C ABI from host memory (host work + uploads + GPU + 8.3 MB readback).
+      `e2e` is frames/s through the C ABI from host memory (host visibility + upload + GPU-side surface
+      and draw preparation + GPU + 8.3 MB readback); `e2e.host_prepared` the same with the host
+      preparing every surface and draw.
       The same frames are then rendered the learned way (960x540 + learned 2x upscale, network trained
       first for --learn-steps steps on two other maps) and reported under "learned" with their PSNR
       against the plain frames.
@@ -413,29 +415,42 @@ def run_frame_gpu(args, world, rank, local):
     frame_ms = max_over_ranks(statistics.mean(graph_ms), world, f"cuda:{local}")
     value = world * 1e3 / frame_ms
 
-    # e2e: the C++ host renderer (host work: visibility, surface and draw setup) drives the C ABI per
-    # frame (swh_renderer_render_frame: one graph with uploads from host memory, surfaces, raster and
-    # postprocess) and the Color32 frame is copied back into a host buffer the caller registered once.
-    from sqwheel import host
-    e2e_ms = []
-    h2d = d2h = 0
-    hr = host.HostRenderer(work.scene, device=local)
+    # e2e: the C++ host renderer drives the C ABI per frame (swh_renderer_render_frame: the host's
+    # visibility, light positioning and leaf order, then one graph with the upload from host memory,
+    # GPU-side surface and draw preparation, surfaces, raster and postprocess) and the Color32 frame
+    # lands in a host buffer the caller registered once. The same loop with the host preparing every
+    # surface and draw (the reference's split) is reported beside it.
+    from sqwheel import abi, host
     import ctypes
-    gpu.load_library().sw_set_tuning(hr.context(), ctypes.byref(tune))
-    out = np.zeros((H, W), np.uint32)
-    hr.register_host_buffer(out)
-    for i, f in enumerate(work.frames[: max(3, min(args.steps, 12))]):
-        t0 = time.perf_counter()
-        hr.render_frame(f["index"], work.opts, out=out, post=work.config)
-        if i > 0:
-            e2e_ms.append((time.perf_counter() - t0) * 1e3)
-        h2d += (f["surfaces"].nbytes + f["draws"].nbytes + f["vertices"].nbytes + f["lights"].nbytes
-                + (f["surfaces"].size + 1) * 8)
-        d2h += out.nbytes
-        n_e2e = i + 1
-    hr.unregister_host_buffer(out)
-    hr.close()
-    e2e_val = 1e3 / statistics.median(e2e_ms)
+
+    def e2e_run(gpu_prep):
+        hr = host.HostRenderer(work.scene, device=local)
+        hr.set_gpu_prep(gpu_prep)
+        glib = gpu.load_library()
+        glib.sw_set_tuning(hr.context(), ctypes.byref(tune))
+        out = np.zeros((H, W), np.uint32)
+        hr.register_host_buffer(out)
+        times, up = [], 0
+        frames = work.frames[: max(4, min(args.steps, 12))]
+        for f in frames:  # warm-up pass: buffers at their capacities, the frame graphs captured
+            hr.render_frame(f["index"], work.opts, out=out, post=work.config)
+        for i, f in enumerate(frames):
+            s0 = abi.Stats()
+            glib.sw_get_stats(hr.context(), ctypes.byref(s0))
+            t0 = time.perf_counter()
+            hr.render_frame(f["index"], work.opts, out=out, post=work.config)
+            dt = time.perf_counter() - t0
+            s1 = abi.Stats()
+            glib.sw_get_stats(hr.context(), ctypes.byref(s1))
+            if i > 0:
+                times.append(dt * 1e3)
+                up += s1.upload_bytes - s0.upload_bytes
+        hr.unregister_host_buffer(out)
+        hr.close()
+        return 1e3 / statistics.median(times), up / len(times), out.nbytes
+
+    e2e_val, h2d_step, d2h_step = e2e_run(True)
+    e2e_host_val, h2d_host_step, _ = e2e_run(False)
 
     lr = run_learned(args, work, r, ldr_frames, local) if args.learn_steps > 0 else None
     if lr is not None:
@@ -484,8 +499,12 @@ def run_frame_gpu(args, world, rank, local):
                          "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": stages[dom]["algorithmic_bytes"],
                          "traffic": STAGE_TRAFFIC.get(dom)},
             "cpu_baseline": cpu,
-            "e2e": {"value": round(e2e_val, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d / n_e2e),
-                    "d2h_bytes_per_step": int(d2h / n_e2e)},
+            "e2e": {"value": round(e2e_val, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d_step),
+                    "d2h_bytes_per_step": int(d2h_step),
+                    "path": "render_frame: host visibility + GPU-side surface and draw preparation",
+                    "host_prepared": {"value": round(e2e_host_val, 2), "unit": "frames/s",
+                                      "h2d_bytes_per_step": int(h2d_host_step),
+                                      "path": "render_frame with the host preparing every surface and draw"}},
             "clocks": clocks.summary(),
             "gpu_launches": launches,
         }

@@ -310,6 +310,7 @@ typedef struct SwStats {
 	uint64_t draws;             /* draw commands submitted since sw_create */
 	uint64_t bad_texel_fetches; /* rasteriser fetches outside a surface (always 0 for well-formed draws) */
 	uint64_t pixel_writes;      /* span pixels the rasteriser wrote (texel fetch + blend) since sw_create */
+	uint64_t upload_bytes;      /* per-frame bytes copied from host to device memory since sw_create */
 } SwStats;
 int sw_get_stats(SwCtx* ctx, SwStats* out_stats);
 

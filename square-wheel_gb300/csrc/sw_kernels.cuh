@@ -256,6 +256,7 @@ __host__ __device__ inline void draw_row_range(const SwDrawCmd& d, const SwVerte
 // compaction (out_offset, first_vertex and tex_offset are filled by the compaction).
 struct PrepCand
 {
+	SurfaceGpu sgpu; // the surface build's record, out_offset 0
 	SwSurfaceDesc desc;
 	SwDrawCmd draw;
 	uint64_t surface_offset;
@@ -317,9 +318,10 @@ struct PrepArgs
 	uint64_t cap_texels, cap_rows;
 };
 
-// Per-candidate preparation (a grid for cap_candidates polygons; warps beyond the frame's candidates
-// return at once), then one CTA's ordered compaction.
-int launch_prep(const PrepArgs& args, cudaStream_t stream);
+// Per-candidate preparation on `stream` (a grid for cap_candidates polygons; CTAs beyond the frame's
+// candidates return at once), then the surface compaction on `stream` and the draw compaction on `aux`
+// (after `candidates_done`, recorded here); the caller orders the raster setup after the draw compaction.
+int launch_prep(const PrepArgs& args, cudaStream_t stream, cudaStream_t aux, cudaEvent_t candidates_done);
 
 // ---- postprocessor / upscaler ----
 

@@ -142,7 +142,13 @@ struct SwCtx
 	// GPU-side surface and draw preparation (sw_set_map, sw_draw_frame_view): the map's polygons and
 	// vertices, per-polygon surface size bounds (prefix sums, for capacities), the candidates' scratch,
 	// the prepared descriptors, the counts (device, and a pinned copy read back after each frame).
-	DevBuf map_polygons, map_vertices, cands, keys, descs, view_counts;
+	DevBuf map_polygons, map_vertices, vslab;
+	uint64_t vs_cands = 0, vs_draws = 0, vs_vertices = 0, vs_rows = 0; // the slab's capacities (only grow)
+	SwViewCounts* v_counts = nullptr; // in the slab
+	SwSurfaceDesc* v_descs = nullptr;
+	SwDrawCmd* v_draws = nullptr;
+	SwVertex16* v_vertices = nullptr;
+	float* d_average_mapped = nullptr; // h_average as the device sees it
 	uint32_t num_map_polygons = 0, num_map_vertices = 0;
 	std::vector<uint64_t> poly_bound_prefix;
 	SwViewCounts* h_counts = nullptr; // pinned, one per staging set (frames alternate)
@@ -307,6 +313,7 @@ int staging_commit(SwCtx* ctx, Staging& st, void* dst, size_t bytes, cudaStream_
 	SW_CUDA(ctx, cudaMemcpyAsync(dst, st.host, bytes, cudaMemcpyHostToDevice, stream));
 	SW_CUDA(ctx, cudaEventRecord(st.done, stream));
 	st.pending = true;
+	ctx->stats.upload_bytes += bytes;
 	return SW_OK;
 }
 
@@ -474,6 +481,8 @@ int sw_create(const SwCreateInfo* info, SwCtx** out_ctx)
 	if (cudaEventCreateWithFlags(&ctx->average_ready, cudaEventDisableTiming) != cudaSuccess) return bail(SW_ERR_CUDA);
 	if (cudaMallocHost(reinterpret_cast<void**>(&ctx->h_average), 4 * sizeof(float)) != cudaSuccess)
 		return bail(SW_ERR_CUDA);
+	if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->d_average_mapped), ctx->h_average, 0) != cudaSuccess)
+		return bail(SW_ERR_CUDA);
 	for (cudaEvent_t* e : {&ctx->ev_counts[0], &ctx->ev_counts[1]})
 		if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return bail(SW_ERR_CUDA);
 	if (cudaMallocHost(reinterpret_cast<void**>(&ctx->h_counts), 2 * sizeof(SwViewCounts)) != cudaSuccess) return bail(SW_ERR_CUDA);
@@ -515,7 +524,7 @@ int sw_destroy(SwCtx* ctx)
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->parts, &ctx->part_counts, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst, &ctx->map_polygons,
-		&ctx->map_vertices, &ctx->cands, &ctx->keys, &ctx->descs, &ctx->view_counts};
+		&ctx->map_vertices, &ctx->vslab};
 	for (DevBuf* b : bufs) release(*b);
 	for (const SwCtx::HostRange& h : ctx->registered) cudaHostUnregister(h.ptr);
 	if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
@@ -1402,6 +1411,7 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	if ((r = capture_and_launch(ctx, ctx->gexec, [&]() { return enqueue_frame(ctx, f, h, off, rows, f.postprocess ? &pa : nullptr); })))
 		return r;
 	ctx->stats.draws += f.num_draws; // (surfaces are counted by launch_surfaces)
+	ctx->stats.upload_bytes += off[6];
 	return finish_graph_frame(ctx, st, p, f.postprocess != 0, f.post, f.frame_duration_s, f.dst, f.dst_pitch, f.dst_is_device,
 		post_out, direct_host);
 }
@@ -1498,6 +1508,42 @@ ViewBlock view_block(const SwCtx* ctx)
 	return v;
 }
 
+// One device allocation for all of a view frame's small buffers (the upload block, the counts, the
+// candidates, the compacted surfaces and draws, the raster setup's records): the preparation and setup
+// kernels' dependent loads stay within a few pages.
+struct ViewSlab
+{
+	size_t frame_in, counts, keys, cands, descs, surfaces, work_prefix, draws, draw_rows, rdraws, boxes, part_counts, vertices,
+		parts, rows, bytes;
+};
+ViewSlab view_slab(size_t block_bytes, uint64_t cands, uint64_t draws, uint64_t vertices, uint64_t rows)
+{
+	ViewSlab v;
+	size_t at = 0;
+	auto take = [&](size_t bytes) {
+		const size_t o = at;
+		at = align_up(at + bytes, 256);
+		return o;
+	};
+	v.frame_in = take(block_bytes);
+	v.counts = take(sizeof(SwViewCounts));
+	v.keys = take(cands * sizeof(PrepKey));
+	v.cands = take(cands * sizeof(PrepCand));
+	v.descs = take(cands * sizeof(SwSurfaceDesc));
+	v.surfaces = take(cands * sizeof(SurfaceGpu));
+	v.work_prefix = take((cands + 1) * 8);
+	v.draws = take(draws * sizeof(SwDrawCmd));
+	v.draw_rows = take(draws * sizeof(DrawRows));
+	v.rdraws = take(draws * sizeof(RasterDraw));
+	v.boxes = take(draws * sizeof(RasterBox));
+	v.part_counts = take(draws * 4);
+	v.vertices = take(vertices * sizeof(SwVertex16));
+	v.parts = take(draws * SW_RASTER_MAX_PARTS * sizeof(RasterPart));
+	v.rows = take(rows * sizeof(RasterRow));
+	v.bytes = at;
+	return v;
+}
+
 } // namespace
 
 int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
@@ -1576,32 +1622,23 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	ctx->vcap_host_vertices = pow2_at_least(f.num_vertices, std::max<uint64_t>(ctx->vcap_host_vertices, 64));
 	const ViewBlock vb = view_block(ctx);
 	const uint32_t bpp = bpp_of(p.pixel_format);
-	const uint64_t cand_cap = pow2_at_least(candidates, 1024);
-	const uint64_t draw_cap = pow2_at_least(need_draws, 1024);
-	const uint64_t vert_cap = pow2_at_least(need_vertices, 8192);
-	const uint64_t row_cap = pow2_at_least(need_rows, 1u << 16);
+	ctx->vs_cands = pow2_at_least(candidates, std::max<uint64_t>(ctx->vs_cands, 1024));
+	ctx->vs_draws = pow2_at_least(need_draws, std::max<uint64_t>(ctx->vs_draws, 1024));
+	ctx->vs_vertices = pow2_at_least(need_vertices, std::max<uint64_t>(ctx->vs_vertices, 8192));
+	ctx->vs_rows = pow2_at_least(need_rows, std::max<uint64_t>(ctx->vs_rows, uint64_t(1) << 16));
 	const uint64_t texel_cap = pow2_at_least(texel_bound, 1u << 20);
-	if ((r = ensure(ctx, ctx->frame_in, vb.bytes))) return r;
-	if ((r = ensure(ctx, ctx->cands, cand_cap * sizeof(PrepCand)))) return r;
-	if ((r = ensure(ctx, ctx->keys, cand_cap * sizeof(PrepKey)))) return r;
-	if ((r = ensure(ctx, ctx->descs, cand_cap * sizeof(SwSurfaceDesc)))) return r;
-	if ((r = ensure(ctx, ctx->surfaces, cand_cap * sizeof(SurfaceGpu)))) return r;
-	if ((r = ensure(ctx, ctx->work_prefix, (cand_cap + 1) * 8))) return r;
+	const ViewSlab vs = view_slab(vb.bytes, ctx->vs_cands, ctx->vs_draws, ctx->vs_vertices, ctx->vs_rows);
+	if ((r = ensure(ctx, ctx->vslab, vs.bytes))) return r;
 	if ((r = ensure(ctx, ctx->arena, texel_cap * bpp))) return r;
-	if ((r = ensure(ctx, ctx->view_counts, sizeof(SwViewCounts)))) return r;
-	if ((r = ensure_raster_buffers(ctx, uint32_t(draw_cap), uint32_t(vert_cap), row_cap))) return r;
 	if ((r = ensure_framebuffer(ctx, p))) return r;
-	// what the buffers hold (growth may have left them larger than asked)
-	auto elems = [](const DevBuf& b, size_t size) { return uint64_t(b.bytes / size); };
-	const uint64_t cap_candidates = std::min(elems(ctx->cands, sizeof(PrepCand)), elems(ctx->keys, sizeof(PrepKey)));
-	const uint64_t cap_surfaces = std::min({cap_candidates, elems(ctx->descs, sizeof(SwSurfaceDesc)),
-		elems(ctx->surfaces, sizeof(SurfaceGpu)), elems(ctx->work_prefix, 8) - 1});
-	const uint64_t cap_draws = std::min({elems(ctx->draws, sizeof(SwDrawCmd)), elems(ctx->draw_rows, sizeof(DrawRows)),
-		elems(ctx->rdraws, sizeof(RasterDraw)), elems(ctx->boxes, sizeof(RasterBox)), elems(ctx->part_counts, 4),
-		elems(ctx->parts, SW_RASTER_MAX_PARTS * sizeof(RasterPart))});
-	const uint64_t cap_vertices = elems(ctx->vertices, sizeof(SwVertex16));
-	const uint64_t cap_rows = elems(ctx->rows, sizeof(RasterRow));
-	const uint64_t cap_texels = elems(ctx->arena, bpp);
+	unsigned char* slab = static_cast<unsigned char*>(ctx->vslab.ptr);
+	const uint64_t cap_candidates = ctx->vs_cands, cap_surfaces = ctx->vs_cands, cap_draws = ctx->vs_draws;
+	const uint64_t cap_vertices = ctx->vs_vertices, cap_rows = ctx->vs_rows;
+	const uint64_t cap_texels = uint64_t(ctx->arena.bytes / bpp);
+	ctx->v_counts = reinterpret_cast<SwViewCounts*>(slab + vs.counts);
+	ctx->v_descs = reinterpret_cast<SwSurfaceDesc*>(slab + vs.descs);
+	ctx->v_draws = reinterpret_cast<SwDrawCmd*>(slab + vs.draws);
+	ctx->v_vertices = reinterpret_cast<SwVertex16*>(slab + vs.vertices);
 	ctx->arena_texels = cap_texels;
 	ctx->arena_format = p.pixel_format;
 	ctx->view_surfaces_cap = uint32_t(cap_surfaces);
@@ -1667,8 +1704,8 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	if (f.num_vertices) std::memcpy(h + vb.vertices, f.vertices, f.num_vertices * sizeof(SwVertex16));
 
 	// 4. kernel arguments: buffers and capacities only (the per-frame values are in the block)
-	unsigned char* d = static_cast<unsigned char*>(ctx->frame_in.ptr);
-	SwViewCounts* counts = static_cast<SwViewCounts*>(ctx->view_counts.ptr);
+	unsigned char* d = slab + vs.frame_in;
+	SwViewCounts* counts = ctx->v_counts;
 	ViewGraphKey key;
 	std::memset(&key, 0, sizeof(key)); // padding too: keys are compared bytewise
 	PrepArgs& pr = key.prep;
@@ -1689,14 +1726,14 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	pr.host_rows = reinterpret_cast<const DrawRows*>(d + vb.rows);
 	pr.texture_mips = static_cast<const SwTextureMip*>(ctx->texture_mips.ptr);
 	pr.emissive_mips = static_cast<const SwEmissiveMip*>(ctx->emissive_mips.ptr);
-	pr.cands = static_cast<PrepCand*>(ctx->cands.ptr);
-	pr.keys = static_cast<PrepKey*>(ctx->keys.ptr);
-	pr.descs = static_cast<SwSurfaceDesc*>(ctx->descs.ptr);
-	pr.surfaces = static_cast<SurfaceGpu*>(ctx->surfaces.ptr);
-	pr.work_prefix = static_cast<uint64_t*>(ctx->work_prefix.ptr);
-	pr.draws = static_cast<SwDrawCmd*>(ctx->draws.ptr);
-	pr.vertices = static_cast<SwVertex16*>(ctx->vertices.ptr);
-	pr.draw_rows = static_cast<DrawRows*>(ctx->draw_rows.ptr);
+	pr.cands = reinterpret_cast<PrepCand*>(slab + vs.cands);
+	pr.keys = reinterpret_cast<PrepKey*>(slab + vs.keys);
+	pr.descs = ctx->v_descs;
+	pr.surfaces = reinterpret_cast<SurfaceGpu*>(slab + vs.surfaces);
+	pr.work_prefix = reinterpret_cast<uint64_t*>(slab + vs.work_prefix);
+	pr.draws = ctx->v_draws;
+	pr.vertices = ctx->v_vertices;
+	pr.draw_rows = reinterpret_cast<DrawRows*>(slab + vs.draw_rows);
 	pr.counts = counts;
 	pr.cap_candidates = uint32_t(std::min<uint64_t>(cap_candidates, 0x7FFFFFFFu));
 	pr.cap_surfaces = uint32_t(std::min<uint64_t>(cap_surfaces, 0x7FFFFFFFu));
@@ -1732,6 +1769,14 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 
 	RasterArgs& ra = key.raster;
 	ra = raster_args(ctx);
+	ra.draws = pr.draws;
+	ra.vertices = pr.vertices;
+	ra.draw_rows = pr.draw_rows;
+	ra.parts = reinterpret_cast<RasterPart*>(slab + vs.parts);
+	ra.part_counts = reinterpret_cast<uint32_t*>(slab + vs.part_counts);
+	ra.rdraws = reinterpret_cast<RasterDraw*>(slab + vs.rdraws);
+	ra.rows = reinterpret_cast<RasterRow*>(slab + vs.rows);
+	ra.boxes = reinterpret_cast<RasterBox*>(slab + vs.boxes);
 	ra.counts = counts;
 	ra.num_draws = 0;
 	ra.setup_blocks = uint32_t(ctx->num_sms) * 2;
@@ -1740,6 +1785,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	{
 		key.post = pa;
 		key.post.inv_scale_dev = reinterpret_cast<const float*>(d + vb.inv_scale);
+		key.post.average = ctx->d_average_mapped; // the frame's average colour goes straight to host memory
 	}
 	key.staging = st.host;
 	key.block_bytes = vb.bytes;
@@ -1759,9 +1805,8 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 			cudaStream_t s = ctx->stream, aux = ctx->aux;
 			SW_CUDA(ctx, cudaMemcpyAsync(d, st.host, vb.bytes, cudaMemcpyHostToDevice, s));
 			int rr;
-			if ((rr = check_kernel(ctx, launch_prep(key.prep, s), "surface and draw preparation"))) return rr;
-			SW_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
-			SW_CUDA(ctx, cudaStreamWaitEvent(aux, ctx->ev_fork, 0));
+			// per-candidate preparation, then the surface compaction here and the draw compaction on aux
+			if ((rr = check_kernel(ctx, launch_prep(key.prep, s, aux, ctx->ev_fork), "surface and draw preparation"))) return rr;
 			if ((rr = check_kernel(ctx, launch_raster_setup(key.raster, aux), "raster setup"))) return rr;
 			SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, aux));
 			if ((rr = check_kernel(ctx,
@@ -1777,7 +1822,6 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 				if ((rr = check_kernel(ctx, launch_postprocess(key.post, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join),
 						 "postprocess")))
 					return rr;
-				SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_average, ctx->average.ptr, 16, cudaMemcpyDeviceToHost, s));
 			}
 			else if (f.dst && f.dst_is_device)
 				SW_CUDA(ctx, cudaMemcpy2DAsync(f.dst, size_t(f.dst_pitch) * bpp, ctx->framebuffer.ptr, size_t(p.width) * bpp,
@@ -1798,6 +1842,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	SW_CUDA(ctx, cudaEventRecord(ctx->ev_counts[slot], ctx->stream));
 	ctx->counts_pending[slot] = true;
 	ctx->counts_seq[slot] = ++ctx->view_seq;
+	ctx->stats.upload_bytes += vb.bytes;
 	ctx->last_num_surfaces = 0; // sw_rebuild_surfaces has no host descriptors of this frame
 	ctx->last_surface_work = 0;
 	r = finish_graph_frame(ctx, st, p, f.postprocess != 0, f.post, f.frame_duration_s, f.dst, f.dst_pitch, f.dst_is_device,
@@ -1816,20 +1861,20 @@ int sw_read_view_prep(SwCtx* ctx, SwViewCounts* out_counts, SwSurfaceDesc* surfa
 	uint32_t max_draws, SwVertex16* vertices, uint32_t max_vertices)
 {
 	if (!ctx || !out_counts) return SW_ERR_INVALID_ARGUMENT;
-	if (!ctx->view_counts.ptr) return fail(ctx, SW_ERR_STATE, "no sw_draw_frame_view yet");
+	if (!ctx->v_counts) return fail(ctx, SW_ERR_STATE, "no sw_draw_frame_view yet");
 	SW_CUDA(ctx, cudaSetDevice(ctx->device));
 	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 	for (uint32_t k = 0; k < 2; ++k)
 		if (ctx->counts_pending[k]) consume_view_counts(ctx, k);
 	SwViewCounts k;
-	SW_CUDA(ctx, cudaMemcpy(&k, ctx->view_counts.ptr, sizeof(k), cudaMemcpyDeviceToHost));
+	SW_CUDA(ctx, cudaMemcpy(&k, ctx->v_counts, sizeof(k), cudaMemcpyDeviceToHost));
 	*out_counts = k;
 	const uint32_t ns = std::min(std::min(max_surfaces, k.num_surfaces), ctx->view_surfaces_cap);
 	const uint32_t nd = std::min(std::min(max_draws, k.num_draws), ctx->view_draws_cap);
 	const uint32_t nv = std::min(std::min(max_vertices, k.num_vertices), ctx->view_vertices_cap);
-	if (surfaces && ns) SW_CUDA(ctx, cudaMemcpy(surfaces, ctx->descs.ptr, size_t(ns) * sizeof(SwSurfaceDesc), cudaMemcpyDeviceToHost));
-	if (draws && nd) SW_CUDA(ctx, cudaMemcpy(draws, ctx->draws.ptr, size_t(nd) * sizeof(SwDrawCmd), cudaMemcpyDeviceToHost));
-	if (vertices && nv) SW_CUDA(ctx, cudaMemcpy(vertices, ctx->vertices.ptr, size_t(nv) * sizeof(SwVertex16), cudaMemcpyDeviceToHost));
+	if (surfaces && ns) SW_CUDA(ctx, cudaMemcpy(surfaces, ctx->v_descs, size_t(ns) * sizeof(SwSurfaceDesc), cudaMemcpyDeviceToHost));
+	if (draws && nd) SW_CUDA(ctx, cudaMemcpy(draws, ctx->v_draws, size_t(nd) * sizeof(SwDrawCmd), cudaMemcpyDeviceToHost));
+	if (vertices && nv) SW_CUDA(ctx, cudaMemcpy(vertices, ctx->v_vertices, size_t(nv) * sizeof(SwVertex16), cudaMemcpyDeviceToHost));
 	return SW_OK;
 }
 

@@ -103,7 +103,8 @@ class PostConfig(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("surfaces", ctypes.c_uint64), ("surface_texels", ctypes.c_uint64), ("draws", ctypes.c_uint64),
-                ("bad_texel_fetches", ctypes.c_uint64), ("pixel_writes", ctypes.c_uint64)]
+                ("bad_texel_fetches", ctypes.c_uint64), ("pixel_writes", ctypes.c_uint64),
+                ("upload_bytes", ctypes.c_uint64)]
 
 
 # Order reported by sw_abi_layout.
