@@ -14,6 +14,8 @@
 // order (draw index, first vertex, first row record), and writes the surface records, descriptors,
 // draws, vertices and row ranges the surface build and the rasteriser read, plus the counts they
 // take their sizes from. Everything stays on the device; the host only uploads the visible leafs.
+#include <cstddef>
+
 #include "sw_kernels.cuh"
 #include "../host/prep_math.h"
 
@@ -528,12 +530,23 @@ __device__ void prep_pair(const PrepArgs& a, const PrepFrame& frame, uint32_t nu
 constexpr uint32_t PREP_THREADS = PREP_PAIRS * 64;
 constexpr uint32_t FAST_MAX = 2048; // candidates (and draw slots) the compactions keep in registers
 
+// Record copies of the compactions in 8-byte chunks spread over the whole CTA (one chunk per thread and
+// step) instead of one thread per record: one round trip for all of them.
+constexpr uint32_t DESC_CHUNKS = sizeof(SwSurfaceDesc) / 8, SGPU_CHUNKS = sizeof(SurfaceGpu) / 8;
+constexpr uint32_t DRAW_CHUNKS = sizeof(SwDrawCmd) / 8;
+static_assert(sizeof(SwSurfaceDesc) % 8 == 0 && sizeof(SurfaceGpu) % 8 == 0 && sizeof(SwDrawCmd) % 8 == 0, "8-byte chunks");
+static_assert(offsetof(SwSurfaceDesc, out_offset) % 8 == 0 && offsetof(SurfaceGpu, out_offset) % 8 == 0 &&
+				  offsetof(SwDrawCmd, tex_offset) % 8 == 0 && offsetof(SwDrawCmd, first_vertex) == 0,
+	"patched fields");
+
 // Surfaces in allocation order: descriptors, the surface build's records, its texel prefix sums and the
 // counts it reads (one CTA of THREADS threads).
 template <uint32_t THREADS>
 __device__ void compact_surfaces(const PrepArgs& a, uint32_t num_candidates)
 {
 	constexpr uint32_t ITEMS = FAST_MAX / THREADS;
+	__shared__ uint32_t s_cand[FAST_MAX]; // surface -> candidate (fast path)
+	__shared__ uint64_t s_off[FAST_MAX];  // surface -> texel offset
 	__shared__ uint32_t s_error;
 	const uint32_t tid = threadIdx.x;
 	if (tid == 0) s_error = 0;
@@ -561,20 +574,39 @@ __device__ void compact_surfaces(const PrepArgs& a, uint32_t num_candidates)
 		total_texels = tot[1];
 		fits = num_surfaces <= a.cap_surfaces && total_texels <= a.cap_texels;
 		if (fits)
+		{
 			for (uint32_t i = 0; i < ITEMS; ++i)
 				if (k[i].state == 1)
 				{
-					const uint32_t c = tid * ITEMS + i;
-					SwSurfaceDesc d = a.cands[c].desc;
-					SurfaceGpu g = a.cands[c].sgpu;
-					d.out_offset = x[1];
-					g.out_offset = x[1];
-					a.descs[x[0]] = d;
-					a.surfaces[x[0]] = g;
+					s_cand[x[0]] = tid * ITEMS + i;
+					s_off[x[0]] = x[1];
 					a.work_prefix[x[0]] = x[1];
 					x[0] += 1;
 					x[1] += k[i].area;
 				}
+			__syncthreads();
+			const uint32_t per = DESC_CHUNKS + SGPU_CHUNKS, chunks = uint32_t(num_surfaces) * per;
+			for (uint32_t t = tid; t < chunks; t += THREADS)
+			{
+				const uint32_t sidx = t / per, q = t - sidx * per;
+				const PrepCand& cand = a.cands[s_cand[sidx]];
+				if (q < DESC_CHUNKS)
+				{
+					const uint64_t v = q == offsetof(SwSurfaceDesc, out_offset) / 8
+						? s_off[sidx]
+						: reinterpret_cast<const uint64_t*>(&cand.desc)[q];
+					reinterpret_cast<uint64_t*>(a.descs + sidx)[q] = v;
+				}
+				else
+				{
+					const uint32_t r = q - DESC_CHUNKS;
+					const uint64_t v = r == offsetof(SurfaceGpu, out_offset) / 8
+						? s_off[sidx]
+						: reinterpret_cast<const uint64_t*>(&cand.sgpu)[r];
+					reinterpret_cast<uint64_t*>(a.surfaces + sidx)[r] = v;
+				}
+			}
+		}
 	}
 	else
 		for (uint32_t base = 0; base < num_candidates; base += THREADS)
@@ -740,15 +772,7 @@ __global__ void __launch_bounds__(COMPACT_THREADS, 1) prep_draws_kernel(PrepArgs
 			if (dk[i].state == 1 && dk[i].draw_count >= 3)
 			{
 				if (fits)
-				{
-					const uint32_t c = dc[i];
-					SwDrawCmd d = a.cands[c].draw;
-					d.first_vertex = uint32_t(num_host_vertices + y[1]);
-					d.tex_offset = sh.surface_offset[c];
-					const uint64_t di = num_host_draws + y[0];
-					a.draws[di] = d;
-					a.draw_rows[di] = DrawRows{uint32_t(num_host_rows + y[2]), dk[i].row_y0, dk[i].row_n, 0u};
-				}
+					a.draw_rows[num_host_draws + y[0]] = DrawRows{uint32_t(num_host_rows + y[2]), dk[i].row_y0, dk[i].row_n, 0u};
 				sh.vcand[y[0]] = dc[i];
 				sh.vbase[y[0]] = uint32_t(y[1]);
 				y[0] += 1;
@@ -758,11 +782,24 @@ __global__ void __launch_bounds__(COMPACT_THREADS, 1) prep_draws_kernel(PrepArgs
 		if (tid == 0) sh.vbase[tot[0]] = uint32_t(tot[1]);
 		__syncthreads();
 		if (fits)
+		{
+			// draw records (first vertex and texture offset patched) and vertices, chunk by chunk
+			const uint32_t ndraws = uint32_t(tot[0]), draw_chunks = ndraws * DRAW_CHUNKS;
+			for (uint32_t t = tid; t < draw_chunks; t += blockDim.x)
+			{
+				const uint32_t j = t / DRAW_CHUNKS, q = t - j * DRAW_CHUNKS;
+				const uint32_t c = sh.vcand[j];
+				uint64_t v = reinterpret_cast<const uint64_t*>(&a.cands[c].draw)[q];
+				if (q == 0) v = (v & 0xFFFFFFFF00000000ull) | uint64_t(num_host_vertices + sh.vbase[j]);
+				if (q == offsetof(SwDrawCmd, tex_offset) / 8) v = sh.surface_offset[c];
+				reinterpret_cast<uint64_t*>(a.draws + num_host_draws + j)[q] = v;
+			}
 			for (uint32_t t = tid; t < uint32_t(tot[1]); t += blockDim.x)
 			{
 				const uint32_t j = find_segment(sh.vbase, uint32_t(tot[0]), t);
 				a.vertices[num_host_vertices + t] = a.cands[sh.vcand[j]].v[t - sh.vbase[j]];
 			}
+		}
 	}
 	else
 	{
