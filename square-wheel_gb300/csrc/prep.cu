@@ -98,6 +98,8 @@ template <class T, class F>
 __device__ inline uint32_t warp_clip_pass(T& v, int c, uint32_t n, T* buf, F isect)
 {
 	const uint32_t lane = threadIdx.x & 31u;
+	// every vertex strictly inside: the sequential pass emits its input unchanged
+	if (__all_sync(FULL_MASK, lane >= n || c == 1)) return n;
 	const int prev = int(lane == 0 ? n - 1 : lane - 1);
 	const T pv = shfl(v, prev);
 	const int pc = __shfl_sync(FULL_MASK, c, prev);
