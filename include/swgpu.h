@@ -443,6 +443,46 @@ typedef struct SwViewCounts {
 int sw_read_view_prep(SwCtx* ctx, SwViewCounts* out_counts, SwSurfaceDesc* surfaces, uint32_t max_surfaces,
 	SwDrawCmd* draws, uint32_t max_draws, SwVertex16* vertices, uint32_t max_vertices);
 
+/* ---- shadowed dynamic lights (cube shadow maps) ----
+ * DynamicLightWithShadow with ShadowMap::Cube (src/square_wheel/light.rs:4-62): the renderer draws each
+ * shadowed light's six depth maps (build_shadow_maps, partial_renderer.rs:525-592, DepthRenderer,
+ * depth_renderer.rs, DepthRasterizer, rasterizer.rs:1295-1474) into one persistent f32 storage, and the
+ * surface build multiplies the light's distance factor by cube_shadow_map_fetch (light.rs:196-258). */
+
+#define SW_SHADOW_NONE 0u
+#define SW_SHADOW_CUBE 1u
+
+/* The shadow map of one of the frame's lights. */
+typedef struct SwLightShadow {
+	uint32_t kind;   /* SW_SHADOW_* */
+	uint32_t size;   /* cube side size in texels */
+	uint64_t offset; /* side s (light.rs:14-23 order: +X, -X, +Y, -Y, +Z, -Z) starts at offset + s * size * size */
+} SwLightShadow;
+
+/* One DepthRasterizer::fill_polygon call of DepthRenderer::draw_polygon (depth_renderer.rs:199-287):
+ * the clipped polygon projected onto a cube side (f32_to_fixed16 vertices), its biased and scaled depth
+ * equation, and the side it is drawn into. */
+typedef struct SwDepthDraw {
+	uint32_t first_vertex;   /* into the SwVertex16 array */
+	uint32_t vertex_count;   /* 3..SW_MAX_POLYGON_VERTICES, clockwise */
+	uint32_t map_size;       /* side width = height */
+	uint32_t reserved;
+	uint64_t map_offset;     /* the side's first texel in the shadow-map storage */
+	float depth_eq[3];       /* d_inv_z_dx, d_inv_z_dy, k */
+	uint32_t reserved2;
+} SwDepthDraw;
+
+/* Draw the depth draws, in array order, into the shadow-map storage (grown to total_texels f32 texels,
+ * never cleared: a texel no polygon covers keeps its value, as the reference's storage does). Draws of
+ * one side must be in the depth renderer's back-to-front order; the last draw covering a texel sets it. */
+int sw_build_shadow_maps(SwCtx* ctx, const SwDepthDraw* draws, uint32_t num_draws, const SwVertex16* vertices,
+	uint32_t num_vertices, uint64_t total_texels);
+/* Shadow maps of the next frame's lights (one per light, in the frame's SwLight order; num_lights 0 or a
+ * NULL array = no shadows). Holds for the frames that follow until it is called again. */
+int sw_set_light_shadows(SwCtx* ctx, const SwLightShadow* shadows, uint32_t num_lights);
+/* Diagnostics: copy up to max_texels texels of the shadow-map storage to host memory (synchronises). */
+int sw_read_shadow_maps(SwCtx* ctx, float* dst, uint64_t max_texels);
+
 /* ---- launch configuration (no reference counterpart) ---- */
 #define SW_RASTER_TILE_VARIANTS 5
 typedef struct SwTuning {
@@ -462,8 +502,8 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 /* sizeof() of the ABI structs in this order: SwCreateInfo, SwTextureMip, SwEmissiveMip,
  * SwDirectionalLightmapElement, SwLight, SwSurfaceDesc, SwVertex16, SwDrawCmd, SwFrameParams,
  * SwPostConfig, SwStats, SwFrameInput, SwTuning, SwMapPolygon, SwViewLeaf, SwViewFrameInput,
- * SwViewCounts. Writes min(count, 17) values; returns the number of structs (17). Needs no GPU:
- * bindings use it to check their mirrored layouts. */
+ * SwViewCounts, SwLightShadow, SwDepthDraw. Writes min(count, 19) values; returns the number of structs
+ * (19). Needs no GPU: bindings use it to check their mirrored layouts. */
 int sw_abi_layout(uint32_t* sizes, uint32_t count);
 
 /* Diagnostics: copy the frame's surface arena (total_texels of sw_submit_surfaces) to host memory. */

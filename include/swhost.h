@@ -38,6 +38,7 @@ typedef struct SwhSceneConfig {
 	int32_t skybox_missing_side;  /* a side without texture (0..5: -X, +X, -Y, +Y, -Z, +Z), -1 = none */
 	float sky_rotation_speed;     /* skybox rotation about the vertical axis, radians per frame */
 	float camera_pitch;           /* added to the camera path's elevation (radians, up > 0) */
+	uint32_t shadowed_lights;     /* the first this many dynamic lights cast cube shadows */
 } SwhSceneConfig;
 
 typedef struct SwhSceneInfo {
@@ -66,6 +67,7 @@ typedef struct SwhFrameOptions {
 	uint32_t clear_background;
 	float fov;      /* radians; 0 = 0.375*pi */
 	float mip_bias;
+	float shadows_quality; /* RendererConfig::shadows_quality, -1..1 (shadow-map size scale, log2) */
 } SwhFrameOptions;
 
 typedef struct SwhFrameOutputs {
@@ -81,6 +83,14 @@ typedef struct SwhFrameOutputs {
 	SwFrameParams params;
 	uint32_t visible_leafs, camera_leaf;
 	uint32_t skybox_draws; /* draws of the skybox (the first ones) */
+	/* cube shadow maps (sw_build_shadow_maps / sw_set_light_shadows): one SwLightShadow per light, the
+	 * depth draws of every side and the storage size; num_depth_draws 0 and all kinds NONE without them */
+	const SwLightShadow* light_shadows;
+	const SwDepthDraw* depth_draws;
+	uint32_t num_depth_draws;
+	uint32_t num_depth_vertices;
+	const SwVertex16* depth_vertices;
+	uint64_t shadow_texels;
 } SwhFrameOutputs;
 
 typedef struct SwhFrame SwhFrame;

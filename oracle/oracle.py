@@ -31,14 +31,15 @@ def load():
         build()
     lib = ctypes.CDLL(LIB_PATH)
     vp, u32, u64, i32, f32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_float
-    lib.orc_build_surfaces.argtypes = [vp, vp, u32, vp, u32, vp, vp, u64, u32]
+    lib.orc_build_surfaces.argtypes = [vp, vp, u32, vp, u32, vp, vp, u64, vp, vp, u64, u32]
+    lib.orc_shadow_maps.argtypes = [vp, u32, vp, u32, vp, u64]
     lib.orc_rasterize.argtypes = [vp, u32, vp, u32, vp, u64, vp, u64, vp, vp, u32, u32, ctypes.POINTER(u64)]
     lib.orc_clear_background.argtypes = [vp, vp, u32]
     lib.orc_postprocess.argtypes = [vp, vp, u32, u32, f32, vp, ctypes.POINTER(f32), vp, u32, vp]
     lib.orc_upscale.argtypes = [u32, u32, vp, vp, u32, u32, u32]
     lib.orc_gaussian_kernel.argtypes = [f32, u32, vp]
     for fn in (lib.orc_build_surfaces, lib.orc_rasterize, lib.orc_clear_background, lib.orc_postprocess,
-               lib.orc_upscale, lib.orc_gaussian_kernel):
+               lib.orc_upscale, lib.orc_gaussian_kernel, lib.orc_shadow_maps):
         fn.restype = i32
     _lib = lib
     return lib
@@ -49,17 +50,36 @@ def _check(r, what):
         raise RuntimeError(f"{what} failed with status {r}")
 
 
-def build_surfaces(static, surfaces, lights, frame_params, total_texels, num_threads=1):
+def build_surfaces(static, surfaces, lights, frame_params, total_texels, num_threads=1, shadows=None, shadow_texels=None):
+    """shadows: one SW LightShadow per light (abi.LIGHT_SHADOW) with the f32 cube maps in shadow_texels."""
     lib = load()
     ci = static.create_info()
     surfaces = np.ascontiguousarray(surfaces, dtype=abi.SURFACE_DESC)
     lights = np.ascontiguousarray(lights if lights is not None else np.zeros(0, abi.LIGHT), dtype=abi.LIGHT)
     dt = np.uint64 if frame_params.pixel_format == abi.SW_PIXEL_C64 else np.uint32
     arena = np.zeros(int(total_texels), dt)
+    sh_ptr, tex_ptr, tex_n = None, None, 0
+    if shadows is not None and len(shadows):
+        shadows = np.ascontiguousarray(shadows, dtype=abi.LIGHT_SHADOW)
+        assert shadows.size == lights.size
+        shadow_texels = np.ascontiguousarray(shadow_texels, dtype=np.float32)
+        sh_ptr, tex_ptr, tex_n = abi.ptr(shadows), abi.ptr(shadow_texels), shadow_texels.size
     _check(lib.orc_build_surfaces(ctypes.byref(ci), abi.ptr(surfaces), surfaces.size, abi.ptr(lights), lights.size,
-                                  ctypes.byref(frame_params), abi.ptr(arena), arena.size, num_threads),
+                                  sh_ptr, tex_ptr, tex_n, ctypes.byref(frame_params), abi.ptr(arena), arena.size,
+                                  num_threads),
            "orc_build_surfaces")
     return arena
+
+
+def shadow_maps(draws, vertices, storage):
+    """Draw the depth draws in order into `storage` (f32, in place; nothing is cleared)."""
+    lib = load()
+    draws = np.ascontiguousarray(draws, dtype=abi.DEPTH_DRAW)
+    vertices = np.ascontiguousarray(vertices, dtype=abi.VERTEX16)
+    assert storage.dtype == np.float32 and storage.flags["C_CONTIGUOUS"]
+    _check(lib.orc_shadow_maps(abi.ptr(draws), draws.size, abi.ptr(vertices), vertices.size, abi.ptr(storage), storage.size),
+           "orc_shadow_maps")
+    return storage
 
 
 def rasterize(draws, vertices, arena, frame_params, framebuffer, num_threads=1, skybox=None):

@@ -150,9 +150,54 @@ inline int32_t rem_euclid(int32_t a, int32_t b)
 	return r < 0 ? r + b : r;
 }
 
+// The frame's shadow maps (NULL shadows: every light unshadowed).
+struct Shadows
+{
+	const SwLightShadow* shadows;
+	uint32_t num;
+	const float* texels;
+	uint64_t num_texels;
+};
+
+// cube_shadow_map_side_fetch, light.rs:235-258. Returns 1 if in light, 0 if in shadow.
+float cube_shadow_map_side_fetch(const float* side, uint32_t size, Vec3 vec)
+{
+	const float ONE_MINUS_EPS = 1.0f - 1.0f / 65536.0f;
+	const float cubemap_size_f = float(size);
+	const float depth = inv_fast(fmaxr(vec.z, MIN_POSITIVE_VALUE));
+	const float half_depth = 0.5f * depth;
+	const float u_f = fminr(fmaxr(f32_mul_add(vec.x, half_depth, 0.5f), 0.0f), ONE_MINUS_EPS) * cubemap_size_f;
+	const float v_f = fminr(fmaxr(f32_mul_add(vec.y, half_depth, 0.5f), 0.0f), ONE_MINUS_EPS) * cubemap_size_f;
+	const uint32_t u = uint32_t(u_f), v = uint32_t(v_f); // in [0, size): to_int_unchecked is a truncation
+	const float value = side[u + v * size];
+	return depth >= value ? 1.0f : 0.0f;
+}
+
+// get_light_shadow_factor / cube_shadow_map_fetch, light.rs:185-233 (`vec` = light position - point).
+float light_shadow_factor(const Shadows& sh, uint32_t light, Vec3 vec)
+{
+	if (!sh.shadows || light >= sh.num || sh.shadows[light].kind != SW_SHADOW_CUBE) return 1.0f; // ShadowMap::None
+	const SwLightShadow& m = sh.shadows[light];
+	const uint64_t side_texels = uint64_t(m.size) * m.size;
+	auto side = [&](uint32_t i) { return sh.texels + m.offset + i * side_texels; };
+	const Vec3 a = v3(std::fabs(vec.x), std::fabs(vec.y), std::fabs(vec.z));
+	if (a.x >= a.y && a.x >= a.z)
+	{
+		if (vec.x >= 0.0f) return cube_shadow_map_side_fetch(side(1), m.size, v3(-vec.y, vec.z, a.x));
+		return cube_shadow_map_side_fetch(side(0), m.size, v3(vec.y, vec.z, a.x));
+	}
+	if (a.y >= a.x && a.y >= a.z)
+	{
+		if (vec.y >= 0.0f) return cube_shadow_map_side_fetch(side(3), m.size, v3(vec.x, vec.z, a.y));
+		return cube_shadow_map_side_fetch(side(2), m.size, v3(-vec.x, vec.z, a.y));
+	}
+	if (vec.z >= 0.0f) return cube_shadow_map_side_fetch(side(5), m.size, v3(-vec.x, vec.y, a.z));
+	return cube_shadow_map_side_fetch(side(4), m.size, v3(-vec.x, -vec.y, a.z));
+}
+
 template <class P>
-void build_surface(const SwCreateInfo* data, const SwSurfaceDesc& s, const SwLight* lights, Vec3 cam_pos,
-	bool use_directional, typename P::T* out)
+void build_surface(const SwCreateInfo* data, const SwSurfaceDesc& s, const SwLight* lights, const Shadows& shadows,
+	Vec3 cam_pos, bool use_directional, typename P::T* out)
 {
 	typedef typename P::T T;
 	const SwTextureMip& tex = data->texture_mips[s.texture_mip];
@@ -322,7 +367,7 @@ void build_surface(const SwCreateInfo* data, const SwSurfaceDesc& s, const SwLig
 				{
 					const SwLight& light = lights[s.lights[li]];
 					Vec3 vec_to_light = v3(light.position[0], light.position[1], light.position[2]) - pos;
-					const float shadow_factor = 1.0f; // ShadowMap::None, light.rs:189
+					const float shadow_factor = light_shadow_factor(shadows, s.lights[li], vec_to_light); // light.rs:185-194
 					float vec_to_light_len2 = fmaxr(vec3_len2(vec_to_light), MIN_POSITIVE_VALUE);
 					float distance_factor = fmaxr(inv_fast(vec_to_light_len2) - light.inv_square_radius, 0.0f);
 					float shadow_distance_factor = shadow_factor * distance_factor;
@@ -419,12 +464,12 @@ void mix_surface_with_texture(const SwCreateInfo* data, const SwSurfaceDesc& s, 
 }
 
 template <class P>
-void build_one(const SwCreateInfo* data, const SwSurfaceDesc& s, const SwLight* lights, Vec3 cam_pos,
-	bool use_directional, void* arena)
+void build_one(const SwCreateInfo* data, const SwSurfaceDesc& s, const SwLight* lights, const Shadows& shadows,
+	Vec3 cam_pos, bool use_directional, void* arena)
 {
 	typename P::T* out = static_cast<typename P::T*>(arena) + s.out_offset;
 	const bool diffuse_layer = (s.flags & SW_SURF_DIFFUSE_LAYER) != 0;
-	if (diffuse_layer) build_surface<P>(data, s, lights, cam_pos, use_directional, out);
+	if (diffuse_layer) build_surface<P>(data, s, lights, shadows, cam_pos, use_directional, out);
 	if (s.emissive_mip != SW_NO_EMISSIVE)
 		mix_surface_with_texture<P>(data, s, diffuse_layer ? SW_BLEND_ADDITIVE : SW_BLEND_NONE, out);
 }
@@ -436,10 +481,15 @@ void build_one(const SwCreateInfo* data, const SwSurfaceDesc& s, const SwLight* 
 using namespace sworacle;
 
 extern "C" int orc_build_surfaces(const SwCreateInfo* data, const SwSurfaceDesc* surfaces, uint32_t num_surfaces,
-	const SwLight* lights, uint32_t num_lights, const SwFrameParams* frame, void* arena, uint64_t arena_texels,
-	uint32_t num_threads)
+	const SwLight* lights, uint32_t num_lights, const SwLightShadow* shadows, const float* shadow_texels,
+	uint64_t shadow_texel_count, const SwFrameParams* frame, void* arena, uint64_t arena_texels, uint32_t num_threads)
 {
 	if (!data || !frame || (!surfaces && num_surfaces) || (!arena && num_surfaces)) return SW_ERR_INVALID_ARGUMENT;
+	const Shadows sh{shadows, shadows ? num_lights : 0u, shadow_texels, shadow_texel_count};
+	for (uint32_t l = 0; l < sh.num; ++l)
+		if (shadows[l].kind == SW_SHADOW_CUBE &&
+			(shadows[l].size == 0 || !shadow_texels || shadows[l].offset + 6 * uint64_t(shadows[l].size) * shadows[l].size > shadow_texel_count))
+			return SW_ERR_INVALID_ARGUMENT;
 	for (uint32_t i = 0; i < num_surfaces; ++i)
 	{
 		const SwSurfaceDesc& s = surfaces[i];
@@ -455,9 +505,9 @@ extern "C" int orc_build_surfaces(const SwCreateInfo* data, const SwSurfaceDesc*
 	const bool dir = frame->use_directional_lightmaps != 0;
 	auto work = [&](uint32_t i) {
 		if (frame->pixel_format == SW_PIXEL_C64)
-			build_one<C64>(data, surfaces[i], lights, cam, dir, arena);
+			build_one<C64>(data, surfaces[i], lights, sh, cam, dir, arena);
 		else
-			build_one<C32>(data, surfaces[i], lights, cam, dir, arena);
+			build_one<C32>(data, surfaces[i], lights, sh, cam, dir, arena);
 	};
 	if (num_threads <= 1)
 	{

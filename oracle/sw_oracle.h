@@ -16,8 +16,14 @@ extern "C" {
  * `surfaces` into `arena` (pixel_format texels). num_threads 0/1 = sequential, N = N worker threads
  * with one task per surface (the reference's rayon par_iter). Returns 0 or a negative SwStatus. */
 int orc_build_surfaces(const SwCreateInfo* data, const SwSurfaceDesc* surfaces, uint32_t num_surfaces,
-	const SwLight* lights, uint32_t num_lights, const SwFrameParams* frame, void* arena, uint64_t arena_texels,
-	uint32_t num_threads);
+	const SwLight* lights, uint32_t num_lights, const SwLightShadow* shadows, const float* shadow_texels,
+	uint64_t shadow_texel_count, const SwFrameParams* frame, void* arena, uint64_t arena_texels, uint32_t num_threads);
+/* (shadows: NULL, or one SwLightShadow per light with the cube maps in shadow_texels) */
+
+/* DepthRasterizer::fill_polygon for every depth draw in order (DepthRenderer, depth_renderer.rs;
+ * rasterizer.rs:1295-1474) into `storage` (f32 texels; draws overwrite, nothing is cleared). */
+int orc_shadow_maps(const SwDepthDraw* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices,
+	float* storage, uint64_t total_texels);
 
 /* Rasterizer::fill_polygon for every draw in order (perform_rasterization, partial_renderer.rs:1192-1283)
  * into `framebuffer` (pixel_format of frame, pitch in pixels). num_threads 0/1 = the reference's

@@ -571,6 +571,95 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 
 } // namespace
 
+// ---- shadow maps: DepthRasterizer (rasterizer.rs:1295-1474) over DepthRenderer's draws ----
+//
+// Painter's order with every draw in flight at once: each texel is written as (draw sequence << 32 |
+// f32 bits) with atomicMax, so the last draw covering it wins, as the sequential overwrite does; the
+// storage's previous values enter as sequence 0 (the reference never clears its shadow-map storage).
+
+__global__ void shadow_pack_kernel(const float* storage, unsigned long long* packed, uint64_t n)
+{
+	for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+		packed[i] = __float_as_uint(storage[i]);
+}
+
+__global__ void shadow_unpack_kernel(const unsigned long long* packed, float* storage, uint64_t n)
+{
+	for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+		storage[i] = __uint_as_float(uint32_t(packed[i]));
+}
+
+// One depth draw per CTA: thread 0 walks the edges (the colour rasteriser's walk: the same parts and
+// first-row edge positions) and accumulates each part's per-row inverse depth in the reference's
+// sequential order; then one thread per row accumulates along its span.
+__global__ void __launch_bounds__(256) shadow_draw_kernel(ShadowArgs a)
+{
+	__shared__ __align__(8) SwDrawCmd s_d;
+	__shared__ SwVertex16 s_v[SW_MAX_POLYGON_VERTICES];
+	__shared__ RasterPart s_parts[SW_RASTER_MAX_PARTS];
+	__shared__ float s_line[SW_SHADOW_MAX_SIZE];
+	__shared__ uint32_t s_np;
+	for (uint32_t di = blockIdx.x; di < a.num_draws; di += gridDim.x)
+	{
+		const SwDepthDraw dd = a.draws[di];
+		const int32_t size = int32_t(dd.map_size);
+		if (threadIdx.x == 0)
+		{
+			s_d = SwDrawCmd{};
+			s_d.vertex_count = dd.vertex_count;
+			s_d.mode = SW_RASTER_FULL_PERSPECTIVE; // no texture-coordinate edges
+		}
+		if (threadIdx.x < dd.vertex_count) s_v[threadIdx.x] = a.vertices[dd.first_vertex + threadIdx.x];
+		__syncthreads();
+		if (threadIdx.x == 0) s_np = edge_walk(s_d, s_v, size, s_parts);
+		__syncthreads();
+		const float dx = dd.depth_eq[0], dy = dd.depth_eq[1], k = dd.depth_eq[2];
+		const unsigned long long seq = (unsigned long long)(di + 1) << 32;
+		unsigned long long* map = a.packed + dd.map_offset;
+		for (uint32_t pi = 0; pi < s_np; ++pi)
+		{
+			const RasterPart p = s_parts[pi];
+			const uint32_t rows = uint32_t(p.y_end_int - p.y_start_int); // <= size <= SW_SHADOW_MAX_SIZE
+			if (threadIdx.x == 0)
+			{
+				// line_inv_z = y_start * dy + 0.5 * (dx + dy) + k, then += dy per row (rasterizer.rs:1442-1471)
+				float line = fadd(fadd(fmul(float(p.y_start_int), dy), fmul(0.5f, fadd(dx, dy))), k);
+				for (uint32_t r = 0; r < rows; ++r)
+				{
+					s_line[r] = line;
+					line = fadd(line, dy);
+				}
+			}
+			__syncthreads();
+			for (uint32_t r = threadIdx.x; r < rows; r += blockDim.x)
+			{
+				const int32_t y = p.y_start_int + int32_t(r);
+				const int32_t xs = max(wadd(p.x_left0, wmul(int32_t(r), p.dx_dy_left)) >> 16, 0);
+				const int32_t xe = min(wadd(p.x_right0, wmul(int32_t(r), p.dx_dy_right)) >> 16, size);
+				if (xs >= xe) continue;
+				float inv_z = fadd(s_line[r], fmul(float(xs), dx));
+				unsigned long long* line = map + uint64_t(y) * uint32_t(size);
+				for (int32_t x = xs; x < xe; ++x)
+				{
+					atomicMax(line + x, seq | __float_as_uint(inv_z));
+					inv_z = fadd(inv_z, dx);
+				}
+			}
+			__syncthreads(); // s_line is reused by the next part
+		}
+	}
+}
+
+int launch_shadow_maps(const ShadowArgs& args, cudaStream_t stream)
+{
+	if (args.num_texels == 0) return 0;
+	const unsigned blocks = unsigned(std::min<uint64_t>((args.num_texels + 255) / 256, 4096));
+	shadow_pack_kernel<<<blocks, 256, 0, stream>>>(args.storage, args.packed, args.num_texels);
+	if (args.num_draws > 0) shadow_draw_kernel<<<std::min(args.num_draws, 65535u), 256, 0, stream>>>(args);
+	shadow_unpack_kernel<<<blocks, 256, 0, stream>>>(args.packed, args.storage, args.num_texels);
+	return int(cudaGetLastError());
+}
+
 int launch_raster_setup(const RasterArgs& args, cudaStream_t stream)
 {
 	if (args.counts)

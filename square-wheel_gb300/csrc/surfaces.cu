@@ -115,6 +115,38 @@ __device__ __forceinline__ uint32_t wrap(int32_t a, uint32_t b)
 	return uint32_t(r < 0 ? r + int32_t(b) : r);
 }
 
+// cube_shadow_map_side_fetch (light.rs:235-258): 1 in light, 0 in shadow.
+__device__ __forceinline__ float cube_side_fetch(const float* side, uint32_t size, float x, float y, float z)
+{
+	const float ONE_MINUS_EPS = 1.0f - 1.0f / 65536.0f;
+	const float size_f = float(size);
+	const float depth = inv_fast(fmaxf(z, MIN_POSITIVE_VALUE));
+	const float half_depth = fmul(0.5f, depth);
+	const float u_f = fmul(fminf(fmaxf(fadd(fmul(x, half_depth), 0.5f), 0.0f), ONE_MINUS_EPS), size_f);
+	const float v_f = fmul(fminf(fmaxf(fadd(fmul(y, half_depth), 0.5f), 0.0f), ONE_MINUS_EPS), size_f);
+	const uint32_t u = __float2uint_rz(u_f), v = __float2uint_rz(v_f); // in [0, size)
+	return depth >= __ldg(side + u + v * size) ? 1.0f : 0.0f;
+}
+
+// get_light_shadow_factor / cube_shadow_map_fetch (light.rs:185-233) for `to_light` = light - point.
+__device__ __forceinline__ float light_shadow_factor(const SurfaceKernelArgs& a, uint32_t light, V3 to_light)
+{
+	if (!a.shadows || light >= a.num_shadows) return 1.0f;
+	const SwLightShadow m = a.shadows[light];
+	if (m.kind != SW_SHADOW_CUBE) return 1.0f;
+	const uint64_t side_texels = uint64_t(m.size) * m.size;
+	const float* maps = a.shadow_texels + m.offset;
+	const float ax = fabsf(to_light.x), ay = fabsf(to_light.y), az = fabsf(to_light.z);
+	if (ax >= ay && ax >= az)
+		return to_light.x >= 0.0f ? cube_side_fetch(maps + 1 * side_texels, m.size, -to_light.y, to_light.z, ax)
+								  : cube_side_fetch(maps + 0 * side_texels, m.size, to_light.y, to_light.z, ax);
+	if (ay >= ax && ay >= az)
+		return to_light.y >= 0.0f ? cube_side_fetch(maps + 3 * side_texels, m.size, to_light.x, to_light.z, ay)
+								  : cube_side_fetch(maps + 2 * side_texels, m.size, -to_light.x, to_light.z, ay);
+	return to_light.z >= 0.0f ? cube_side_fetch(maps + 5 * side_texels, m.size, -to_light.x, to_light.y, az)
+							  : cube_side_fetch(maps + 4 * side_texels, m.size, -to_light.x, -to_light.y, az);
+}
+
 // Lighting of one texel (surfaces.rs:515-842); returns the ColorVec before conversion.
 template <bool DIRECTIONAL>
 __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const SurfaceGpu& s, uint64_t texel, uint32_t u,
@@ -241,7 +273,7 @@ __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const Surf
 			const SwLight& L = a.lights[s.lights[li]];
 			const V3 to_light = v3sub(mkv3(L.position[0], L.position[1], L.position[2]), pos);
 			const float tl_len2 = fmaxf(v3dot(to_light, to_light), MIN_POSITIVE_VALUE);
-			const float sdf = fmul(1.0f, fmaxf(fsub(inv_fast(tl_len2), L.inv_square_radius), 0.0f));
+			const float sdf = fmul(light_shadow_factor(a, s.lights[li], to_light), fmaxf(fsub(inv_fast(tl_len2), L.inv_square_radius), 0.0f));
 			float di = 0.0f;
 			if (spec != 2) di = fmaxf(fmul(v3dot(normal, to_light), inv_sqrt_fast(tl_len2)), 0.0f);
 			float si = 0.0f;

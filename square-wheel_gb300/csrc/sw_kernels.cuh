@@ -46,6 +46,9 @@ struct SurfaceKernelArgs
 	uint32_t directional;
 	uint64_t total_work;
 	const SwViewCounts* counts; // GPU-side preparation: num_surfaces / total_work from here (else NULL)
+	const SwLightShadow* shadows; // per light (NULL: no shadows), maps in shadow_texels
+	const float* shadow_texels;
+	uint32_t num_shadows;
 	const uint64_t* texels;
 	const uint32_t* emissive_pixels;
 	const float* lightmaps;
@@ -248,6 +251,23 @@ __host__ __device__ inline void draw_row_range(const SwDrawCmd& d, const SwVerte
 	y0 = a;
 	nrows = b > a ? uint32_t(b - a) : 0u;
 }
+
+// ---- shadow maps ----
+
+#define SW_SHADOW_MAX_SIZE 1024 // cube side size limit (the reference's cube maps are 64..256)
+
+struct ShadowArgs
+{
+	const SwDepthDraw* draws;
+	uint32_t num_draws;
+	const SwVertex16* vertices;
+	float* storage;               // the persistent f32 shadow-map storage
+	unsigned long long* packed;   // scratch: (draw sequence << 32 | f32 bits) per texel
+	uint64_t num_texels;
+};
+
+// Pack the storage, draw every depth draw (last draw wins per texel), unpack.
+int launch_shadow_maps(const ShadowArgs& args, cudaStream_t stream);
 
 // ---- GPU-side surface and draw preparation (prep.cu) ----
 

@@ -166,6 +166,13 @@ struct SwCtx
 	std::vector<uint32_t> v_draw_leaf;
 	std::vector<DrawRows> v_host_rows;
 
+	// Shadow maps (sw_build_shadow_maps / sw_set_light_shadows): the persistent f32 storage (grows, keeps
+	// its contents), the packing scratch, and the frame's per-light descriptors on the device.
+	DevBuf shadow_storage, shadow_packed, shadow_descs;
+	uint64_t shadow_texels = 0;
+	uint32_t num_shadow_descs = 0;
+	Staging stage_shadow, stage_shadow_descs;
+
 	// Optional per-stage device timing (sw_enable_timing).
 	bool timing = false;
 	cudaEvent_t t_begin[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -524,7 +531,7 @@ int sw_destroy(SwCtx* ctx)
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->parts, &ctx->part_counts, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst, &ctx->map_polygons,
-		&ctx->map_vertices, &ctx->vslab};
+		&ctx->map_vertices, &ctx->vslab, &ctx->shadow_storage, &ctx->shadow_packed, &ctx->shadow_descs};
 	for (DevBuf* b : bufs) release(*b);
 	for (const SwCtx::HostRange& h : ctx->registered) cudaHostUnregister(h.ptr);
 	if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
@@ -534,7 +541,8 @@ int sw_destroy(SwCtx* ctx)
 	for (cudaEvent_t e : ctx->ev_counts)
 		if (e) cudaEventDestroy(e);
 	Staging* st[] = {&ctx->stage_lights, &ctx->stage_surfaces, &ctx->stage_prefix, &ctx->stage_draws,
-		&ctx->stage_vertices, &ctx->stage_draw_rows, &ctx->stage_io, &ctx->gstage[0], &ctx->gstage[1]};
+		&ctx->stage_vertices, &ctx->stage_draw_rows, &ctx->stage_io, &ctx->gstage[0], &ctx->gstage[1], &ctx->stage_shadow,
+		&ctx->stage_shadow_descs};
 	for (Staging* s : st)
 	{
 		if (s->host) cudaFreeHost(s->host);
@@ -635,6 +643,9 @@ static int launch_surfaces(SwCtx* ctx, const SurfaceInputs* in = nullptr)
 {
 	SurfaceKernelArgs a;
 	std::memset(&a, 0, sizeof(a)); // optional fields (counts, cam_pos_dev) stay unset on this path
+	a.shadows = ctx->num_shadow_descs ? static_cast<const SwLightShadow*>(ctx->shadow_descs.ptr) : nullptr;
+	a.shadow_texels = static_cast<const float*>(ctx->shadow_storage.ptr);
+	a.num_shadows = ctx->num_shadow_descs;
 	a.surfaces = in ? in->surfaces : static_cast<const SurfaceGpu*>(ctx->surfaces.ptr);
 	a.work_prefix = in ? in->work_prefix : static_cast<const uint64_t*>(ctx->work_prefix.ptr);
 	a.num_surfaces = ctx->last_num_surfaces;
@@ -1753,6 +1764,9 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	sa.directional_lightmaps = static_cast<const SwDirectionalLightmapElement*>(ctx->dir_lightmaps.ptr);
 	sa.lights = pr.lights;
 	sa.cam_pos_dev = reinterpret_cast<const float*>(d + vb.cam);
+	sa.shadows = ctx->num_shadow_descs ? static_cast<const SwLightShadow*>(ctx->shadow_descs.ptr) : nullptr;
+	sa.shadow_texels = static_cast<const float*>(ctx->shadow_storage.ptr);
+	sa.num_shadows = ctx->num_shadow_descs;
 	sa.arena = ctx->arena.ptr;
 	// surface grid: from the latest frame's texels with headroom; it changes (and the graphs are captured
 	// again) only when the texel count leaves [grid/2, grid] blocks' worth
@@ -1878,6 +1892,104 @@ int sw_read_view_prep(SwCtx* ctx, SwViewCounts* out_counts, SwSurfaceDesc* surfa
 	return SW_OK;
 }
 
+namespace
+{
+// Grow a device buffer keeping its contents (the new part zeroed).
+int grow_preserve(SwCtx* ctx, DevBuf& b, size_t bytes)
+{
+	if (b.ptr && b.bytes >= bytes) return SW_OK;
+	const size_t want = std::max(bytes, b.bytes + b.bytes / 2);
+	void* p = nullptr;
+	cudaError_t e = cudaMalloc(&p, want);
+	if (e != cudaSuccess)
+	{
+		cudaGetLastError();
+		return fail(ctx, SW_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu bytes) failed: %s", want, cudaGetErrorString(e));
+	}
+	SW_CUDA(ctx, cudaMemsetAsync(p, 0, want, ctx->stream));
+	if (b.ptr)
+	{
+		SW_CUDA(ctx, cudaMemcpyAsync(p, b.ptr, b.bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+		SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+		if (ctx->aux) SW_CUDA(ctx, cudaStreamSynchronize(ctx->aux));
+		cudaFree(b.ptr);
+	}
+	b.ptr = p;
+	b.bytes = want;
+	return SW_OK;
+}
+} // namespace
+
+int sw_build_shadow_maps(SwCtx* ctx, const SwDepthDraw* draws, uint32_t num_draws, const SwVertex16* vertices,
+	uint32_t num_vertices, uint64_t total_texels)
+{
+	if (!ctx || (num_draws && (!draws || !vertices))) return SW_ERR_INVALID_ARGUMENT;
+	if (total_texels > (uint64_t(1) << 34)) return fail(ctx, SW_ERR_LIMIT, "shadow-map storage too large");
+	for (uint32_t i = 0; i < num_draws; ++i)
+	{
+		const SwDepthDraw& d = draws[i];
+		if (d.vertex_count < 3 || d.vertex_count > SW_MAX_POLYGON_VERTICES || uint64_t(d.first_vertex) + d.vertex_count > num_vertices)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "depth draw %u: bad vertices", i);
+		if (d.map_size == 0 || d.map_size > SW_SHADOW_MAX_SIZE || d.map_offset + uint64_t(d.map_size) * d.map_size > total_texels)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "depth draw %u: map outside the storage", i);
+	}
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	int r;
+	if ((r = grow_preserve(ctx, ctx->shadow_storage, std::max<uint64_t>(total_texels, 1) * 4))) return r;
+	ctx->shadow_texels = std::max(ctx->shadow_texels, total_texels);
+	if (num_draws == 0) return SW_OK;
+	if ((r = ensure(ctx, ctx->shadow_packed, total_texels * 8))) return r;
+	// draws and vertices in one upload
+	const size_t vo = align_up(size_t(num_draws) * sizeof(SwDepthDraw), 256);
+	const size_t bytes = vo + size_t(num_vertices) * sizeof(SwVertex16);
+	if ((r = ensure(ctx, ctx->up_src, bytes))) return r;
+	void* h = nullptr;
+	if ((r = staging_acquire(ctx, ctx->stage_shadow, bytes, &h))) return r;
+	std::memcpy(h, draws, size_t(num_draws) * sizeof(SwDepthDraw));
+	std::memcpy(static_cast<unsigned char*>(h) + vo, vertices, size_t(num_vertices) * sizeof(SwVertex16));
+	if ((r = staging_commit(ctx, ctx->stage_shadow, ctx->up_src.ptr, bytes))) return r;
+	ShadowArgs a;
+	a.draws = static_cast<const SwDepthDraw*>(ctx->up_src.ptr);
+	a.num_draws = num_draws;
+	a.vertices = reinterpret_cast<const SwVertex16*>(static_cast<unsigned char*>(ctx->up_src.ptr) + vo);
+	a.storage = static_cast<float*>(ctx->shadow_storage.ptr);
+	a.packed = static_cast<unsigned long long*>(ctx->shadow_packed.ptr);
+	a.num_texels = total_texels;
+	return check_kernel(ctx, launch_shadow_maps(a, ctx->stream), "shadow maps");
+}
+
+int sw_set_light_shadows(SwCtx* ctx, const SwLightShadow* shadows, uint32_t num_lights)
+{
+	if (!ctx || (num_lights && !shadows)) return SW_ERR_INVALID_ARGUMENT;
+	if (num_lights > 65535) return fail(ctx, SW_ERR_LIMIT, "too many lights");
+	uint32_t used = 0;
+	for (uint32_t i = 0; i < num_lights; ++i)
+	{
+		const SwLightShadow& m = shadows[i];
+		if (m.kind == SW_SHADOW_NONE) continue;
+		if (m.kind != SW_SHADOW_CUBE) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "light %u: unknown shadow kind", i);
+		if (m.size == 0 || m.size > SW_SHADOW_MAX_SIZE || m.offset + 6 * uint64_t(m.size) * m.size > ctx->shadow_texels)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "light %u: cube map outside the shadow-map storage", i);
+		used = i + 1;
+	}
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	ctx->num_shadow_descs = used; // lights past the last shadowed one need no descriptor
+	if (!used) return SW_OK;
+	int r;
+	if ((r = ensure(ctx, ctx->shadow_descs, size_t(used) * sizeof(SwLightShadow)))) return r;
+	return upload(ctx, ctx->stage_shadow_descs, ctx->shadow_descs.ptr, shadows, size_t(used) * sizeof(SwLightShadow));
+}
+
+int sw_read_shadow_maps(SwCtx* ctx, float* dst, uint64_t max_texels)
+{
+	if (!ctx || (max_texels && !dst)) return SW_ERR_INVALID_ARGUMENT;
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	const uint64_t n = std::min(max_texels, ctx->shadow_texels);
+	if (n) SW_CUDA(ctx, cudaMemcpy(dst, ctx->shadow_storage.ptr, n * 4, cudaMemcpyDeviceToHost));
+	return SW_OK;
+}
+
 int sw_set_frame_graph(SwCtx* ctx, int enable)
 {
 	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
@@ -1957,14 +2069,14 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 
 int sw_abi_layout(uint32_t* sizes, uint32_t count)
 {
-	const uint32_t s[17] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
+	const uint32_t s[19] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
 		uint32_t(sizeof(SwDirectionalLightmapElement)), uint32_t(sizeof(SwLight)), uint32_t(sizeof(SwSurfaceDesc)),
 		uint32_t(sizeof(SwVertex16)), uint32_t(sizeof(SwDrawCmd)), uint32_t(sizeof(SwFrameParams)),
 		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats)), uint32_t(sizeof(SwFrameInput)), uint32_t(sizeof(SwTuning)),
 		uint32_t(sizeof(SwMapPolygon)), uint32_t(sizeof(SwViewLeaf)), uint32_t(sizeof(SwViewFrameInput)),
-		uint32_t(sizeof(SwViewCounts))};
-	for (uint32_t i = 0; sizes && i < count && i < 17; ++i) sizes[i] = s[i];
-	return 17;
+		uint32_t(sizeof(SwViewCounts)), uint32_t(sizeof(SwLightShadow)), uint32_t(sizeof(SwDepthDraw))};
+	for (uint32_t i = 0; sizes && i < count && i < 19; ++i) sizes[i] = s[i];
+	return 19;
 }
 
 int sw_get_stats(SwCtx* ctx, SwStats* out)

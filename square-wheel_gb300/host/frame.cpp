@@ -98,14 +98,20 @@ FramePrep::FramePrep(const Scene& scene) : sc(scene)
 			if (map_polygons[sc.leafs[i].first_polygon + k].flags & SW_POLY_SKY) sky_polygons.push_back(sc.leafs[i].first_polygon + k);
 	}
 	leaf_sky_first[sc.leafs.size()] = uint32_t(sky_polygons.size());
-	leaf_data.resize(sc.leafs.size());
-	portal_data.resize(sc.portals.size());
+	leaf_view_index.resize(sc.leafs.size());
 	poly.resize(sc.polygons.size());
 	vertices_transformed.resize(sc.vertices.size());
 	leaf_lights.resize(sc.leafs.size());
 }
 
-uint32_t FramePrep::find_current_leaf() const
+// ---- VisibilityCalculator (map_visibility_calculator.rs) ----
+VisibilityCalculator::VisibilityCalculator(const Scene& scene) : sc(scene)
+{
+	leafs.resize(sc.leafs.size());
+	portals.resize(sc.portals.size());
+}
+
+uint32_t VisibilityCalculator::find_current_leaf() const
 {
 	// map_visibility_calculator.rs:133-155
 	uint32_t index = sc.root_node();
@@ -120,7 +126,7 @@ uint32_t FramePrep::find_current_leaf() const
 	return 0;
 }
 
-bool FramePrep::project_portal(const MapPortal& portal, ClippingPolygon& out) const
+bool VisibilityCalculator::project_portal(const MapPortal& portal, ClippingPolygon& out) const
 {
 	// map_visibility_calculator.rs:286-326
 	uint32_t count = std::min(portal.num_vertices, MAX_VERTICES);
@@ -133,7 +139,7 @@ bool FramePrep::project_portal(const MapPortal& portal, ClippingPolygon& out) co
 	return true;
 }
 
-void FramePrep::mark_reachable_leafs(const uint32_t* start, uint32_t n, const ClippingPolygon& start_bounds)
+void VisibilityCalculator::mark_reachable_leafs(const uint32_t* start, uint32_t n, const ClippingPolygon& start_bounds)
 {
 	// map_visibility_calculator.rs:157-267
 	wave0.clear();
@@ -141,15 +147,15 @@ void FramePrep::mark_reachable_leafs(const uint32_t* start, uint32_t n, const Cl
 	for (uint32_t i = 0; i < n; ++i)
 	{
 		wave0.push_back(start[i]);
-		leaf_data[start[i]].bounds = start_bounds;
-		leaf_data[start[i]].visible_frame = current_frame;
+		leafs[start[i]].bounds = start_bounds;
+		leafs[start[i]].visible_frame = frame;
 	}
 	uint32_t depth = 0;
 	while (!wave0.empty())
 	{
 		for (uint32_t leaf : wave0)
 		{
-			const ClippingPolygon leaf_bounds = leaf_data[leaf].bounds;
+			const ClippingPolygon leaf_bounds = leafs[leaf].bounds;
 			const BspLeaf& lv = sc.leafs[leaf];
 			for (uint32_t k = 0; k < lv.num_leaf_portals; ++k)
 			{
@@ -167,20 +173,20 @@ void FramePrep::mark_reachable_leafs(const uint32_t* start, uint32_t n, const Cl
 					if (portal_plane_pos >= 0.0f) continue;
 					next_leaf = pv.leafs[0];
 				}
-				PortalData& pd = portal_data[portal];
-				if (pd.visible_frame != current_frame)
+				Portal& pd = portals[portal];
+				if (pd.visible_frame != frame)
 				{
-					pd.visible_frame = current_frame;
+					pd.visible_frame = frame;
 					pd.has_projection = project_portal(pv, pd.projection);
 				}
 				if (!pd.has_projection) continue;
 				ClippingPolygon b = pd.projection;
 				b.intersect(leaf_bounds);
 				if (!b.is_valid_and_non_empty()) continue;
-				LeafData& nd = leaf_data[next_leaf];
-				if (nd.visible_frame != current_frame)
+				Leaf& nd = leafs[next_leaf];
+				if (nd.visible_frame != frame)
 				{
-					nd.visible_frame = current_frame;
+					nd.visible_frame = frame;
 					nd.bounds = b;
 				}
 				else
@@ -197,11 +203,13 @@ void FramePrep::mark_reachable_leafs(const uint32_t* start, uint32_t n, const Cl
 	}
 }
 
-void FramePrep::update_visibility(const ClippingPolygon& frame_bounds)
+void VisibilityCalculator::update(const CameraMatrices& camera, const ClippingPolygon& frame_bounds)
 {
 	// map_visibility_calculator.rs:52-97
+	cam = camera;
+	++frame;
 	const uint32_t current_leaf = find_current_leaf();
-	stats.camera_leaf = current_leaf;
+	camera_leaf = current_leaf;
 	uint32_t start[32];
 	uint32_t n = 1;
 	start[0] = current_leaf;
@@ -226,6 +234,7 @@ void FramePrep::position_sphere(uint32_t id, Vec3 center, float radius, uint32_t
 	if (node_index >= FIRST_LEAF_INDEX)
 	{
 		leaf_lights[node_index - FIRST_LEAF_INDEX].push_back(id);
+		light_leafs[id].push_back(node_index - FIRST_LEAF_INDEX);
 		return;
 	}
 	const BspNode& node = sc.nodes[node_index];
@@ -238,8 +247,121 @@ void FramePrep::position_sphere(uint32_t id, Vec3 center, float radius, uint32_t
 void FramePrep::position_lights()
 {
 	for (auto& l : leaf_lights) l.clear();
+	light_leafs.resize(lights.size());
+	for (auto& l : light_leafs) l.clear();
 	for (uint32_t i = 0; i < lights.size(); ++i)
 		position_sphere(i, v3(lights[i].position[0], lights[i].position[1], lights[i].position[2]), lights[i].radius, sc.root_node());
+}
+
+void FramePrep::prepare_shadows()
+{
+	// prepare_dynamic_lights (partial_renderer.rs:398-515) for cube shadow maps: a shadowed light touching
+	// a visible leaf gets six sides of 64..256 texels (by its distance from the camera), allocated in
+	// light order; build_shadow_maps (:525-592) draws them with DepthRenderer::draw_map.
+	depth_draws.clear();
+	depth_vertices.clear();
+	light_shadows.assign(lights.size(), SwLightShadow{SW_SHADOW_NONE, 0u, 0ull});
+	uint64_t offset = 0;
+	for (uint32_t li = 0; li < lights.size(); ++li)
+	{
+		if (!sc.light_is_shadowed(li)) continue;
+		bool visible = false;
+		for (uint32_t leaf : light_leafs[li])
+			if (vis.visible(leaf))
+			{
+				visible = true;
+				break;
+			}
+		if (!visible) continue;
+		const SwLight& light = lights[li];
+		const Vec3 lp = v3(light.position[0], light.position[1], light.position[2]);
+		const float dist_from_camera = magnitude(cam.position - lp);
+		const float dist_to_closest_point = dist_from_camera - light.radius;
+		const uint32_t min_size = 64, max_size = 256;
+		uint32_t size = max_size;
+		if (dist_to_closest_point > 0.0f)
+		{
+			const float target_size = 128.0f * light.radius / dist_to_closest_point;
+			const float e = std::fmax(std::log2(target_size) + opt.shadows_quality, 0.0f); // f32 log2, `as u32`
+			const uint32_t shift = e >= 31.0f ? 31u : uint32_t(e);
+			size = std::max(std::min(1u << shift, max_size), min_size);
+		}
+		light_shadows[li] = SwLightShadow{SW_SHADOW_CUBE, size, offset};
+		for (uint32_t side = 0; side < 6; ++side)
+			draw_depth_map(cube_shadow_map_side_matrices(lp, float(size), side), size, offset + uint64_t(side) * size * size);
+		offset += uint64_t(size) * size * 6;
+	}
+	shadow_texels = offset;
+}
+
+void FramePrep::draw_depth_map(const CameraMatrices& camera, uint32_t size, uint64_t map_offset)
+{
+	// DepthRenderer::draw_map / draw_tree / draw_leaf / draw_polygon (depth_renderer.rs:45-287)
+	const float fs = float(size);
+	shadow_vis.update(camera, ClippingPolygon::from_box(0.0f, 0.0f, fs, fs));
+	const Vec4 w_row = camera.planes_matrix.row(3);
+	uint32_t stack[MAX_BSP_TREE_DEPTH];
+	stack[0] = sc.root_node();
+	uint32_t n = 1;
+	while (n > 0)
+	{
+		const uint32_t node_index = stack[n - 1];
+		if (node_index >= FIRST_LEAF_INDEX)
+		{
+			--n;
+			const uint32_t leaf = node_index - FIRST_LEAF_INDEX;
+			if (!shadow_vis.visible(leaf)) continue;
+			Vec3 planes[8];
+			shadow_vis.bounds(leaf).get_clip_planes(planes);
+			const BspLeaf& lv = sc.leafs[leaf];
+			for (uint32_t k = 0; k < lv.num_polygons; ++k) draw_depth_polygon(camera, planes, lv.first_polygon + k, size, map_offset);
+		}
+		else if (n < MAX_BSP_TREE_DEPTH)
+		{
+			const BspNode& node = sc.nodes[node_index];
+			const float w = dot(w_row, extend(node.plane.vec, -node.plane.dist));
+			const uint32_t mask = w >= 0.0f ? 1u : 0u;
+			stack[n - 1] = node.children[1 ^ mask];
+			stack[n] = node.children[mask];
+			++n;
+		}
+		else
+			--n;
+	}
+}
+
+void FramePrep::draw_depth_polygon(const CameraMatrices& camera, const Vec3 clip_planes[8], uint32_t polygon_index, uint32_t size,
+	uint64_t map_offset)
+{
+	// DepthRenderer::draw_polygon::<false> + draw_depth_polygon (depth_renderer.rs:199-287)
+	const MapPolygon& p = sc.polygons[polygon_index];
+	const Material& m = sc.materials[p.texture];
+	if (!(m.shadow && m.blending_mode == SW_BLEND_NONE)) return; // materials_shadow_table (:20-38)
+	const Vec4 pt = camera.planes_matrix * extend(p.plane.vec, -p.plane.dist);
+	if (pt.w <= 0.0f) return;
+	const float pw = -pt.w;
+	const float d_inv_z_dx = pt.x / pw, d_inv_z_dy = pt.y / pw;
+	const float DEPTH_BIAS_CONST = -1.0f / float(1 << 20), DEPTH_BIAS_SLOPE = -1.0f;
+	const float DEPTH_EQUATION_SCALE = 1.0f - 1.0f / 1024.0f;
+	SwDepthDraw d;
+	std::memset(&d, 0, sizeof(d));
+	d.depth_eq[0] = DEPTH_EQUATION_SCALE * d_inv_z_dx;
+	d.depth_eq[1] = DEPTH_EQUATION_SCALE * d_inv_z_dy;
+	d.depth_eq[2] = DEPTH_EQUATION_SCALE * (pt.z / pw + DEPTH_BIAS_CONST + DEPTH_BIAS_SLOPE * (std::fabs(d_inv_z_dx) + std::fabs(d_inv_z_dy)));
+	const uint32_t nv = std::min(p.num_vertices, MAX_VERTICES);
+	if (nv < 3) return;
+	Vec3 vt[MAX_VERTICES];
+	for (uint32_t i = 0; i < nv; ++i) vt[i] = view_transform(camera.view_matrix, sc.vertices[p.first_vertex + i]);
+	Vec2 v2d[MAX_VERTICES];
+	const uint32_t count = project_and_clip_polygon(clip_planes, vt, nv, v2d);
+	if (count < 3) return;
+	d.first_vertex = uint32_t(depth_vertices.size());
+	d.vertex_count = count;
+	d.map_size = size;
+	d.map_offset = map_offset;
+	for (uint32_t k = 0; k < count; ++k) // f32_to_fixed16 (fixed_math.rs:31-34): saturating `as`
+		depth_vertices.push_back(SwVertex16{as_i32(v2d[k].x * 65536.0f), as_i32(v2d[k].y * 65536.0f)});
+	depth_draws.push_back(d);
 }
 
 void FramePrep::prepare_polygon_surface(const Vec3 clip_planes[8], uint64_t& offset, uint32_t polygon_index)
@@ -293,9 +415,9 @@ void FramePrep::prepare_polygons_surfaces()
 	uint64_t offset = 0;
 	for (uint32_t i = 0; i < sc.leafs.size(); ++i)
 	{
-		if (leaf_data[i].visible_frame != current_frame) continue;
+		if (!vis.visible(i)) continue;
 		Vec3 planes[8];
-		leaf_data[i].bounds.get_clip_planes(planes);
+		vis.bounds(i).get_clip_planes(planes);
 		const BspLeaf& leaf = sc.leafs[i];
 		for (uint32_t k = 0; k < leaf.num_polygons; ++k) prepare_polygon_surface(planes, offset, leaf.first_polygon + k);
 	}
@@ -464,8 +586,8 @@ void FramePrep::for_each_drawn_leaf(F&& f)
 		{
 			--n;
 			const uint32_t leaf = node_index - FIRST_LEAF_INDEX;
-			if (leaf_data[leaf].visible_frame != current_frame) continue;
-			ClippingPolygon b = leaf_data[leaf].bounds;
+			if (!vis.visible(leaf)) continue;
+			ClippingPolygon b = vis.bounds(leaf);
 			b.intersect(viewport);
 			if (b.is_valid_and_non_empty())
 			{
@@ -501,8 +623,10 @@ void FramePrep::begin_frame(const CameraMatrices& camera, const std::vector<SwLi
 	lights = frame_lights;
 	stats = FrameStats();
 	++current_frame;
-	update_visibility(ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height)));
+	vis.update(cam, ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height)));
+	stats.camera_leaf = vis.camera_leaf;
 	position_lights();
+	prepare_shadows();
 }
 
 void FramePrep::finish_params()
@@ -549,9 +673,9 @@ void FramePrep::prepare_view_with_camera(const CameraMatrices& camera, const std
 	has_sky = false;
 	for (uint32_t i = 0; i < sc.leafs.size(); ++i)
 	{
-		if (leaf_data[i].visible_frame != current_frame) continue;
+		if (!vis.visible(i)) continue;
 		const BspLeaf& leaf = sc.leafs[i];
-		leaf_data[i].view_index = uint32_t(view_leafs.size());
+		leaf_view_index[i] = uint32_t(view_leafs.size());
 		SwViewLeaf vl;
 		std::memset(&vl, 0, sizeof(vl));
 		vl.first_polygon = leaf.first_polygon;
@@ -561,7 +685,7 @@ void FramePrep::prepare_view_with_camera(const CameraMatrices& camera, const std
 		for (uint32_t li : leaf_lights[i]) view_leaf_lights.push_back(uint16_t(li));
 		vl.draw_order = SW_LEAF_NOT_DRAWN;
 		Vec3 planes[8];
-		leaf_data[i].bounds.get_clip_planes(planes);
+		vis.bounds(i).get_clip_planes(planes);
 		for (int k = 0; k < 8; ++k)
 		{
 			vl.clip_planes[k][0] = planes[k].x;
@@ -586,7 +710,7 @@ void FramePrep::prepare_view_with_camera(const CameraMatrices& camera, const std
 	draw_skybox(ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height)));
 	uint32_t order = 0;
 	for_each_drawn_leaf([this, &order](const ClippingPolygon& b, uint32_t leaf) {
-		SwViewLeaf& vl = view_leafs[leaf_data[leaf].view_index];
+		SwViewLeaf& vl = view_leafs[leaf_view_index[leaf]];
 		vl.draw_order = order++;
 		Vec3 planes[8];
 		b.get_clip_planes(planes);

@@ -39,6 +39,40 @@ struct ClippingPolygon
 	void get_clip_planes(Vec3 out[8]) const;
 };
 
+// MapVisibilityCalculator (src/square_wheel/map_visibility_calculator.rs:52-326): the leafs reachable
+// through portals from the camera's leaf, each with the screen bounds it is seen through.
+class VisibilityCalculator
+{
+public:
+	explicit VisibilityCalculator(const Scene& scene);
+	void update(const CameraMatrices& cam, const ClippingPolygon& frame_bounds);
+	bool visible(uint32_t leaf) const { return leafs[leaf].visible_frame == frame; }
+	const ClippingPolygon& bounds(uint32_t leaf) const { return leafs[leaf].bounds; }
+	uint32_t camera_leaf = 0;
+
+private:
+	struct Leaf
+	{
+		uint32_t visible_frame = 0;
+		ClippingPolygon bounds{};
+	};
+	struct Portal
+	{
+		uint32_t visible_frame = 0;
+		bool has_projection = false;
+		ClippingPolygon projection{};
+	};
+	const Scene& sc;
+	CameraMatrices cam{};
+	uint32_t frame = 0;
+	std::vector<Leaf> leafs;
+	std::vector<Portal> portals;
+	std::vector<uint32_t> wave0, wave1;
+	uint32_t find_current_leaf() const;
+	bool project_portal(const MapPortal& p, ClippingPolygon& out) const;
+	void mark_reachable_leafs(const uint32_t* start, uint32_t n, const ClippingPolygon& bounds);
+};
+
 struct FrameOptions
 {
 	uint32_t width = 640, height = 480;
@@ -47,6 +81,7 @@ struct FrameOptions
 	bool clear_background = false;
 	float fov = 3.14159265358979323846f * 0.375f; // test game FOV, src/test_game/game_map.rs:865
 	float mip_bias = 0.0f;                        // textures_mip_bias default, dynamic_mip_bias off
+	float shadows_quality = 0.0f;                 // RendererConfig::shadows_quality default (clamped to [-1, 1])
 };
 
 struct FrameStats
@@ -86,20 +121,14 @@ public:
 	FrameStats stats;
 	std::vector<SwViewLeaf> view_leafs;
 	std::vector<uint16_t> view_leaf_lights;
+	// Cube shadow maps of the frame's shadowed visible lights: one SwLightShadow per light, the depth draws
+	// of every side (side by side, light by light) and the storage they need.
+	std::vector<SwLightShadow> light_shadows;
+	std::vector<SwDepthDraw> depth_draws;
+	std::vector<SwVertex16> depth_vertices;
+	uint64_t shadow_texels = 0;
 
 private:
-	struct LeafData
-	{
-		uint32_t visible_frame = 0;
-		uint32_t view_index = 0; // position in view_leafs (prepare_view)
-		ClippingPolygon bounds{};
-	};
-	struct PortalData
-	{
-		uint32_t visible_frame = 0;
-		bool has_projection = false;
-		ClippingPolygon projection{};
-	};
 	struct PolyData
 	{
 		uint32_t visible_frame = 0;
@@ -113,9 +142,10 @@ private:
 
 	const Scene& sc;
 	uint32_t current_frame = 0;
-	std::vector<LeafData> leaf_data;
-	std::vector<PortalData> portal_data;
-	std::vector<uint32_t> wave0, wave1;
+	VisibilityCalculator vis{sc};        // the camera's
+	VisibilityCalculator shadow_vis{sc}; // the shadow-map sides' (one after another)
+	std::vector<std::vector<uint32_t>> light_leafs; // leafs each light's sphere touches
+	std::vector<uint32_t> leaf_view_index; // position of a visible leaf in view_leafs (prepare_view)
 	std::vector<PolyData> poly;
 	std::vector<Vec3> vertices_transformed;
 	std::vector<uint32_t> visible_polygons;
@@ -128,15 +158,15 @@ private:
 	std::vector<uint32_t> sky_polygons;   // polygons of the sky material, grouped by leaf
 	std::vector<uint32_t> leaf_sky_first; // leaf i's sky polygons: sky_polygons[leaf_sky_first[i] .. [i + 1])
 
-	uint32_t find_current_leaf() const;
-	void update_visibility(const ClippingPolygon& frame_bounds);
-	void mark_reachable_leafs(const uint32_t* start, uint32_t n, const ClippingPolygon& bounds);
-	bool project_portal(const MapPortal& p, ClippingPolygon& out) const;
 	void position_lights();
 	void position_sphere(uint32_t id, Vec3 center, float radius, uint32_t node);
 	void prepare_polygons_surfaces();
 	void prepare_polygon_surface(const Vec3 clip_planes[8], uint64_t& offset, uint32_t polygon_index);
 	void extend_sky_bounds(const Vec2* v2d, uint32_t count);
+	void prepare_shadows();
+	void draw_depth_map(const CameraMatrices& camera, uint32_t size, uint64_t map_offset);
+	void draw_depth_polygon(const CameraMatrices& camera, const Vec3 clip_planes[8], uint32_t polygon_index, uint32_t size,
+		uint64_t map_offset);
 	void begin_frame(const CameraMatrices& cam, const std::vector<SwLight>& lights, const FrameOptions& opt, Quat skybox_rotation);
 	void finish_params();
 	void camera_of_frame(uint32_t frame_index, const FrameOptions& opt, CameraMatrices& cam, std::vector<SwLight>& lights,

@@ -187,21 +187,10 @@ struct CameraMatrices
 	Mat4 planes_matrix;
 };
 
-// build_view_matrix, src/common/matrix.rs:13-109
-inline CameraMatrices build_view_matrix(Vec3 position, float azimuth, float elevation, float fov, float width, float height)
+// complete_view_matrix, src/common/matrix.rs:84-108: viewport shift * viewport scale * perspective *
+// rotation * translation, and the planes matrix as the inverse of its transpose.
+inline CameraMatrices complete_view_matrix(Vec3 position, const Mat4& rotation_matrix, Vec2 fov_scale, float width, float height)
 {
-	const float pi = 3.14159265358979323846f;
-	const Quat rotation = quat_mul(quat_from_angle_z(azimuth + pi * 0.5f), quat_from_angle_y(-elevation));
-	const float inv_half_fov_tan = 1.0f / std::tan(fov * 0.5f);
-	const float aspect = width / height;
-	const Vec2 fov_scale = v2(inv_half_fov_tan / aspect, inv_half_fov_tan);
-
-	Mat4 basis_change = Mat4::identity();
-	basis_change.c[0] = v4(0, 0, 1, 0);
-	basis_change.c[1] = v4(-1, 0, 0, 0);
-	basis_change.c[2] = v4(0, -1, 0, 0);
-	const Mat4 rotation_matrix = basis_change * mat4_from_quat(conjugate(rotation));
-
 	Mat4 translate = Mat4::identity();
 	translate.c[3] = v4(-position.x, -position.y, -position.z, 1.0f);
 	Mat4 perspective = Mat4::identity();
@@ -221,6 +210,42 @@ inline CameraMatrices build_view_matrix(Vec3 position, float azimuth, float elev
 	if (!invert(transpose(m.view_matrix), inv)) inv = Mat4::identity();
 	m.planes_matrix = inv;
 	return m;
+}
+
+// build_view_matrix, src/common/matrix.rs:13-82
+inline CameraMatrices build_view_matrix(Vec3 position, float azimuth, float elevation, float fov, float width, float height)
+{
+	const float pi = 3.14159265358979323846f;
+	const Quat rotation = quat_mul(quat_from_angle_z(azimuth + pi * 0.5f), quat_from_angle_y(-elevation));
+	const float inv_half_fov_tan = 1.0f / std::tan(fov * 0.5f);
+	const float aspect = width / height;
+	const Vec2 fov_scale = v2(inv_half_fov_tan / aspect, inv_half_fov_tan);
+
+	Mat4 basis_change = Mat4::identity();
+	basis_change.c[0] = v4(0, 0, 1, 0);
+	basis_change.c[1] = v4(-1, 0, 0, 0);
+	basis_change.c[2] = v4(0, -1, 0, 0);
+	const Mat4 rotation_matrix = basis_change * mat4_from_quat(conjugate(rotation));
+	return complete_view_matrix(position, rotation_matrix, fov_scale, width, height);
+}
+
+// calculate_cube_shadow_map_side_matrices / get_cube_map_side_matrix, src/square_wheel/light.rs:73-133:
+// side 0..5 = +X, -X, +Y, -Y, +Z, -Z; a 90-degree view (fov scale 1) over a size x size map.
+inline CameraMatrices cube_shadow_map_side_matrices(Vec3 position, float size, uint32_t side)
+{
+	Mat4 m = Mat4::identity();
+	const Vec4 ux = v4(1, 0, 0, 0), uy = v4(0, 1, 0, 0), uz = v4(0, 0, 1, 0);
+	const Vec4 nx = v4(-1, 0, 0, 0), ny = v4(0, -1, 0, 0), nz = v4(0, 0, -1, 0);
+	switch (side)
+	{
+	case 0: m.c[0] = uz, m.c[1] = nx, m.c[2] = ny; break;
+	case 1: m.c[0] = nz, m.c[1] = ux, m.c[2] = ny; break;
+	case 2: m.c[0] = ux, m.c[1] = uz, m.c[2] = ny; break;
+	case 3: m.c[0] = nx, m.c[1] = nz, m.c[2] = ny; break;
+	case 4: m.c[0] = ux, m.c[1] = uy, m.c[2] = uz; break;
+	default: m.c[0] = ux, m.c[1] = ny, m.c[2] = nz; break;
+	}
+	return complete_view_matrix(position, m, v2(1.0f, 1.0f), size, size);
 }
 
 // view_matrix_transform_vertex, src/common/matrix.rs:125-128

@@ -65,6 +65,7 @@ struct Material
 	int32_t emissive = -1; // emissive texture index or -1
 	float emissive_light[3] = {1.0f, 1.0f, 1.0f};
 	bool skybox = false; // SpecialMaterialEffect::Skybox: polygons only mark where the sky shows
+	bool shadow = true;  // casts shadows (material.rs:50-53)
 };
 
 // One mip of a skybox side (SkyboxSideTexture, src/square_wheel/textures.rs:83-87): size x size texels
@@ -117,6 +118,7 @@ struct SceneConfig
 	int32_t skybox_missing_side = -1; // a side without texture (0..5), -1 = none
 	float sky_rotation_speed = 0.01f; // skybox rotation about the vertical axis, radians per frame
 	float camera_pitch = 0.0f;        // added to the camera path's elevation (radians, up > 0)
+	uint32_t shadowed_lights = 0;     // the first this many dynamic lights cast cube shadows
 };
 
 struct Scene
@@ -149,6 +151,8 @@ struct Scene
 
 	uint32_t root_node() const { return nodes.empty() ? FIRST_LEAF_INDEX : uint32_t(nodes.size() - 1); }
 	void frame_lights(uint32_t frame, std::vector<SwLight>& out) const;
+	// DynamicLightShadowType::Cubemap for light `i` of frame_lights' list (the first shadowed_lights ones).
+	bool light_is_shadowed(uint32_t i) const { return i < config.shadowed_lights; }
 	// Polygons with their basis and material fields (SwMapPolygon), in polygon order.
 	void map_polygons(std::vector<SwMapPolygon>& out) const;
 	SwCreateInfo create_info(uint32_t device) const;

@@ -1,6 +1,7 @@
 // C ABI of the host library (include/swhost.h).
 #include "../../include/swhost.h"
 
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <string>
@@ -19,13 +20,38 @@ struct SwhFrame
 	explicit SwhFrame(const Scene& s) : prep(s) {}
 	FramePrep prep;
 };
+struct SwhRenderer;
+namespace
+{
+int submit_shadows(SwhRenderer* r, const FramePrep& p);
+}
 struct SwhRenderer
 {
 	const SwhScene* scene = nullptr;
 	SwCtx* ctx = nullptr;
 	SwhFrame* frame = nullptr;
 	bool gpu_prep = true; // render_frame: surfaces and world draws prepared on the GPU (sw_draw_frame_view)
+	bool shadows_set = false; // sw_set_light_shadows holds descriptors from an earlier frame
 };
+
+namespace
+{
+// build_shadow_maps (partial_renderer.rs:525-592) for the frame, and its lights' shadow maps.
+int submit_shadows(SwhRenderer* r, const FramePrep& p)
+{
+	if (p.depth_draws.empty() && p.shadow_texels == 0)
+	{
+		if (!r->shadows_set) return SW_OK;
+		r->shadows_set = false;
+		return sw_set_light_shadows(r->ctx, nullptr, 0);
+	}
+	int st = sw_build_shadow_maps(r->ctx, p.depth_draws.data(), uint32_t(p.depth_draws.size()), p.depth_vertices.data(),
+		uint32_t(p.depth_vertices.size()), p.shadow_texels);
+	if (st) return st;
+	r->shadows_set = true;
+	return sw_set_light_shadows(r->ctx, p.light_shadows.data(), uint32_t(p.light_shadows.size()));
+}
+} // namespace
 
 namespace
 {
@@ -41,6 +67,7 @@ FrameOptions to_options(const SwhFrameOptions* o)
 	f.clear_background = o->clear_background != 0;
 	if (o->fov > 0.0f) f.fov = o->fov;
 	f.mip_bias = o->mip_bias;
+	f.shadows_quality = std::fmax(-1.0f, std::fmin(o->shadows_quality, 1.0f)); // renderer.rs:235-242
 	return f;
 }
 
@@ -81,6 +108,7 @@ int swh_scene_create(const SwhSceneConfig* c, SwhScene** out)
 	cfg.skybox_missing_side = c->skybox_missing_side;
 	cfg.sky_rotation_speed = c->sky_rotation_speed;
 	cfg.camera_pitch = c->camera_pitch;
+	cfg.shadowed_lights = c->shadowed_lights;
 	SwhScene* s = new (std::nothrow) SwhScene();
 	if (!s) return SW_ERR_OUT_OF_MEMORY;
 	try
@@ -243,6 +271,12 @@ int swh_frame_outputs(const SwhFrame* f, SwhFrameOutputs* out)
 	out->visible_leafs = p.stats.visible_leafs;
 	out->camera_leaf = p.stats.camera_leaf;
 	out->skybox_draws = p.stats.skybox_draws;
+	out->light_shadows = p.light_shadows.data();
+	out->depth_draws = p.depth_draws.data();
+	out->num_depth_draws = uint32_t(p.depth_draws.size());
+	out->num_depth_vertices = uint32_t(p.depth_vertices.size());
+	out->depth_vertices = p.depth_vertices.data();
+	out->shadow_texels = p.shadow_texels;
 	return SW_OK;
 }
 
@@ -305,6 +339,7 @@ int swh_renderer_prepare_frame(SwhRenderer* r, uint32_t frame_index, const SwhFr
 	int st = swh_frame_prepare(r->frame, frame_index, o);
 	if (st) return st;
 	const FramePrep& p = r->frame->prep;
+	if ((st = submit_shadows(r, p))) return st;
 	st = sw_frame_begin(r->ctx, &p.params, p.lights.data(), uint32_t(p.lights.size()));
 	if (st) return st;
 	return sw_submit_surfaces(r->ctx, p.surfaces.data(), uint32_t(p.surfaces.size()), p.total_texels);
@@ -327,6 +362,7 @@ int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFra
 	{
 		int st = swh_frame_prepare_view(r->frame, frame_index, o);
 		if (st) return st;
+		if ((st = submit_shadows(r, r->frame->prep))) return st;
 		SwViewFrameInput vin;
 		swh_frame_view_input(r->frame, &vin);
 		vin.mip_bias = o->mip_bias;
@@ -345,6 +381,7 @@ int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFra
 	int st = swh_frame_prepare(r->frame, frame_index, o);
 	if (st) return st;
 	const FramePrep& p = r->frame->prep;
+	if ((st = submit_shadows(r, p))) return st;
 	SwFrameInput in;
 	std::memset(&in, 0, sizeof(in));
 	in.params = p.params;

@@ -36,6 +36,7 @@ SW_NO_EMISSIVE = 0xFFFFFFFF
 SW_SURF_DIFFUSE_LAYER = 1
 SW_POLY_DRAW, SW_POLY_SKY, SW_POLY_DIFFUSE_LAYER = 1, 2, 4
 SW_LEAF_NOT_DRAWN = 0xFFFFFFFF
+SW_SHADOW_NONE, SW_SHADOW_CUBE = 0, 1
 
 TEXTURE_MIP = np.dtype([("offset", "<u8"), ("width", "<u4"), ("height", "<u4"), ("flags", "<u4"), ("reserved", "<u4")], align=True)
 EMISSIVE_MIP = np.dtype([("offset", "<u8"), ("width", "<u4"), ("height", "<u4")], align=True)
@@ -59,6 +60,9 @@ MAP_POLYGON = np.dtype([
     ("basis_start", "<f4", 3), ("basis_normal", "<f4", 3), ("tex_coord_min", "<i4", 2), ("tex_coord_max", "<i4", 2),
     ("first_vertex", "<u4"), ("num_vertices", "<u4"), ("texture", "<u4"), ("lightmap_data_offset", "<u4"),
     ("flags", "<u4"), ("blending_mode", "<u4"), ("emissive_texture", "<u4"), ("emissive_light", "<f4", 3)], align=True)
+LIGHT_SHADOW = np.dtype([("kind", "<u4"), ("size", "<u4"), ("offset", "<u8")], align=True)
+DEPTH_DRAW = np.dtype([("first_vertex", "<u4"), ("vertex_count", "<u4"), ("map_size", "<u4"), ("reserved", "<u4"),
+                       ("map_offset", "<u8"), ("depth_eq", "<f4", 3), ("reserved2", "<u4")], align=True)
 VIEW_LEAF = np.dtype([
     ("first_polygon", "<u4"), ("num_polygons", "<u4"), ("first_light", "<u4"), ("num_lights", "<u4"),
     ("draw_order", "<u4"), ("reserved", "<u4"), ("clip_planes", "<f4", (8, 3)), ("draw_clip_planes", "<f4", (8, 3))],
@@ -151,6 +155,7 @@ LAYOUT_ORDER = [
     ("SwFrameInput", ctypes.sizeof(FrameInput)), ("SwTuning", ctypes.sizeof(Tuning)),
     ("SwMapPolygon", MAP_POLYGON.itemsize), ("SwViewLeaf", VIEW_LEAF.itemsize),
     ("SwViewFrameInput", ctypes.sizeof(ViewFrameInput)), ("SwViewCounts", ctypes.sizeof(ViewCounts)),
+    ("SwLightShadow", LIGHT_SHADOW.itemsize), ("SwDepthDraw", DEPTH_DRAW.itemsize),
 ]
 
 

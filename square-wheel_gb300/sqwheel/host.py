@@ -23,7 +23,7 @@ class SceneConfig(ctypes.Structure):
         ("num_frames", ctypes.c_uint32), ("emissive_frac", ctypes.c_float),
         ("sky_rooms", ctypes.c_uint32), ("skybox_size", ctypes.c_uint32), ("skybox_brightness", ctypes.c_float),
         ("skybox_missing_side", ctypes.c_int32), ("sky_rotation_speed", ctypes.c_float),
-        ("camera_pitch", ctypes.c_float),
+        ("camera_pitch", ctypes.c_float), ("shadowed_lights", ctypes.c_uint32),
     ]
 
 
@@ -38,7 +38,7 @@ class SceneInfo(ctypes.Structure):
 class FrameOptions(ctypes.Structure):
     _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("pixel_format", ctypes.c_uint32),
                 ("use_directional_lightmaps", ctypes.c_uint32), ("clear_background", ctypes.c_uint32),
-                ("fov", ctypes.c_float), ("mip_bias", ctypes.c_float)]
+                ("fov", ctypes.c_float), ("mip_bias", ctypes.c_float), ("shadows_quality", ctypes.c_float)]
 
 
 class FrameOutputs(ctypes.Structure):
@@ -46,7 +46,9 @@ class FrameOutputs(ctypes.Structure):
                 ("total_texels", ctypes.c_uint64), ("draws", ctypes.c_void_p), ("vertices", ctypes.c_void_p),
                 ("num_vertices", ctypes.c_uint32), ("num_lights", ctypes.c_uint32), ("lights", ctypes.c_void_p),
                 ("params", abi.FrameParams), ("visible_leafs", ctypes.c_uint32), ("camera_leaf", ctypes.c_uint32),
-                ("skybox_draws", ctypes.c_uint32)]
+                ("skybox_draws", ctypes.c_uint32), ("light_shadows", ctypes.c_void_p), ("depth_draws", ctypes.c_void_p),
+                ("num_depth_draws", ctypes.c_uint32), ("num_depth_vertices", ctypes.c_uint32),
+                ("depth_vertices", ctypes.c_void_p), ("shadow_texels", ctypes.c_uint64)]
 
 
 def load_host_library():
@@ -113,7 +115,7 @@ class Scene:
                         num_materials=16, metal_frac=0.0, dielectric_frac=0.0, normal_maps=0, directional_lightmaps=0,
                         lights_per_room=1, num_dynamic_lights=0, num_frames=64, emissive_frac=0.0, sky_rooms=0,
                         skybox_size=128, skybox_brightness=1.0, skybox_missing_side=-1, sky_rotation_speed=0.01,
-                        camera_pitch=0.0)
+                        camera_pitch=0.0, shadowed_lights=0)
         for k, v in kw.items():
             setattr(c, k, v)
         self.config = c
@@ -174,8 +176,10 @@ class Scene:
             pass
 
 
-def frame_options(width, height, pixel_format, directional=True, clear_background=False, fov=0.0, mip_bias=0.0):
-    return FrameOptions(width, height, pixel_format, 1 if directional else 0, 1 if clear_background else 0, fov, mip_bias)
+def frame_options(width, height, pixel_format, directional=True, clear_background=False, fov=0.0, mip_bias=0.0,
+                  shadows_quality=0.0):
+    return FrameOptions(width, height, pixel_format, 1 if directional else 0, 1 if clear_background else 0, fov, mip_bias,
+                        shadows_quality)
 
 
 class Frame:
@@ -207,6 +211,10 @@ class Frame:
         self.visible_leafs = int(o.visible_leafs)
         self.camera_leaf = int(o.camera_leaf)
         self.skybox_draws = int(o.skybox_draws)
+        self.light_shadows = arr(o.light_shadows, o.num_lights, abi.LIGHT_SHADOW)
+        self.depth_draws = arr(o.depth_draws, o.num_depth_draws, abi.DEPTH_DRAW)
+        self.depth_vertices = arr(o.depth_vertices, o.num_depth_vertices, abi.VERTEX16)
+        self.shadow_texels = int(o.shadow_texels)
         return self
 
     def prepare_view(self, frame_index, options):
