@@ -372,6 +372,7 @@ int sw_set_frame_graph(SwCtx* ctx, int enable);
 #define SW_POLY_DRAW 1u          /* material.draw */
 #define SW_POLY_SKY 2u           /* sky material: marks where the skybox shows, never a surface */
 #define SW_POLY_DIFFUSE_LAYER 4u /* material.light && material has a diffuse layer */
+#define SW_POLY_SHADOW 8u        /* material.shadow: casts shadows (materials_shadow_table, depth_renderer.rs:20-38) */
 
 /* One world polygon of the map with the material fields its surface needs (bsp_map_compact::Polygon,
  * src/common/bsp_map_compact.rs:60-74, PolygonBasisVecs, src/square_wheel/surfaces.rs:7-47). */
@@ -480,6 +481,30 @@ int sw_build_shadow_maps(SwCtx* ctx, const SwDepthDraw* draws, uint32_t num_draw
 /* Shadow maps of the next frame's lights (one per light, in the frame's SwLight order; num_lights 0 or a
  * NULL array = no shadows). Holds for the frames that follow until it is called again. */
 int sw_set_light_shadows(SwCtx* ctx, const SwLightShadow* shadows, uint32_t num_lights);
+/* GPU-side depth-draw preparation (replaces the host's DepthRenderer::draw_polygon loop; needs sw_set_map):
+ * one cube side as DepthRenderer::draw_map sees it (the side camera of light.rs:88-133) ... */
+typedef struct SwShadowSide {
+	float view_matrix[16];   /* CameraMatrices::view_matrix, column-major */
+	float planes_matrix[16]; /* CameraMatrices::planes_matrix, column-major */
+	uint32_t map_size;       /* side width = height, 1..SW_SHADOW_MAX_SIZE */
+	uint32_t reserved;
+	uint64_t map_offset;     /* the side's first texel in the shadow-map storage */
+} SwShadowSide;
+/* ... and one leaf that the side's visibility reaches, in DepthRenderer::draw_tree's back-to-front order
+ * (depth_renderer.rs:96-136), sides one after another. */
+typedef struct SwShadowLeaf {
+	uint32_t side;                        /* index into the sides array */
+	uint32_t first_polygon, num_polygons; /* the leaf's polygons in SwMapPolygon order */
+	uint32_t reserved;
+	float clip_planes[8][3];              /* the leaf's bounds in the side's visibility (clipping_polygon.rs:140-152) */
+} SwShadowLeaf;
+#define SW_SHADOW_MAX_SIZE 1024u
+/* Prepare the depth draws of every listed leaf's polygons on the GPU (draw_polygon::<false> and
+ * draw_depth_polygon, depth_renderer.rs:199-287: shadow-casting opaque polygons facing the light, the
+ * biased depth equation, project_and_clip_polygon, f32_to_fixed16) and draw them as sw_build_shadow_maps
+ * draws the same list prepared on the host: the same storage, texel for texel. */
+int sw_build_shadow_maps_view(SwCtx* ctx, const SwShadowSide* sides, uint32_t num_sides, const SwShadowLeaf* leafs,
+	uint32_t num_leafs, uint64_t total_texels);
 /* Diagnostics: copy up to max_texels texels of the shadow-map storage to host memory (synchronises). */
 int sw_read_shadow_maps(SwCtx* ctx, float* dst, uint64_t max_texels);
 
@@ -502,8 +527,8 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 /* sizeof() of the ABI structs in this order: SwCreateInfo, SwTextureMip, SwEmissiveMip,
  * SwDirectionalLightmapElement, SwLight, SwSurfaceDesc, SwVertex16, SwDrawCmd, SwFrameParams,
  * SwPostConfig, SwStats, SwFrameInput, SwTuning, SwMapPolygon, SwViewLeaf, SwViewFrameInput,
- * SwViewCounts, SwLightShadow, SwDepthDraw. Writes min(count, 19) values; returns the number of structs
- * (19). Needs no GPU: bindings use it to check their mirrored layouts. */
+ * SwViewCounts, SwLightShadow, SwDepthDraw, SwShadowSide, SwShadowLeaf. Writes min(count, 21) values;
+ * returns the number of structs (21). Needs no GPU: bindings use it to check their mirrored layouts. */
 int sw_abi_layout(uint32_t* sizes, uint32_t count);
 
 /* Diagnostics: copy the frame's surface arena (total_texels of sw_submit_surfaces) to host memory. */

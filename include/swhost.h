@@ -91,6 +91,12 @@ typedef struct SwhFrameOutputs {
 	uint32_t num_depth_vertices;
 	const SwVertex16* depth_vertices;
 	uint64_t shadow_texels;
+	/* swh_frame_prepare_view: the depth draws are prepared on the GPU (sw_build_shadow_maps_view) from
+	 * the cube sides and the leafs each side's visibility reaches; num_depth_draws is 0 then */
+	const SwShadowSide* shadow_sides;
+	uint32_t num_shadow_sides;
+	uint32_t num_shadow_leafs;
+	const SwShadowLeaf* shadow_leafs;
 } SwhFrameOutputs;
 
 typedef struct SwhFrame SwhFrame;

@@ -21,6 +21,7 @@
 //     at once and blends them in submission order into registers. Blending order is the reference's,
 //     the frame buffer is read and written once, and coverage and texel addresses are bit-exact.
 #include "sw_kernels.cuh"
+#include "warp_prep.cuh"
 
 #include <algorithm>
 
@@ -573,25 +574,49 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 
 // ---- shadow maps: DepthRasterizer (rasterizer.rs:1295-1474) over DepthRenderer's draws ----
 //
-// Painter's order with every draw in flight at once: each texel is written as (draw sequence << 32 |
-// f32 bits) with atomicMax, so the last draw covering it wins, as the sequential overwrite does; the
-// storage's previous values enter as sequence 0 (the reference never clears its shadow-map storage).
+// Painter's order with every draw in flight at once: the storage holds (sequence << 32 | f32 bits) per
+// texel and every draw writes with atomicMax, so the last draw covering a texel wins, as the sequential
+// overwrite does. Sequences keep growing from call to call (the caller passes each call's base), so a
+// texel no draw of the current call covers keeps its value: the reference never clears its storage.
 
-__global__ void shadow_pack_kernel(const float* storage, unsigned long long* packed, uint64_t n)
+namespace
 {
-	for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
-		packed[i] = __float_as_uint(storage[i]);
+
+// One row of a part (fill_polygon_part's row loop, rasterizer.rs:1448-1470): `line` is the row's
+// line_inv_z; inv_z is accumulated pixel by pixel as the reference does.
+__device__ __forceinline__ void draw_depth_row(unsigned long long* map, int32_t size, const RasterPart& p, uint32_t r, float line,
+	float dx, unsigned long long seq)
+{
+	const int32_t y = p.y_start_int + int32_t(r);
+	const int32_t xs = max(wadd(p.x_left0, wmul(int32_t(r), p.dx_dy_left)) >> 16, 0);
+	const int32_t xe = min(wadd(p.x_right0, wmul(int32_t(r), p.dx_dy_right)) >> 16, size);
+	if (xs >= xe) return;
+	float inv_z = fadd(line, fmul(float(xs), dx));
+	unsigned long long* row = map + uint64_t(y) * uint32_t(size);
+	for (int32_t x = xs; x < xe; ++x)
+	{
+		atomicMax(row + x, seq | __float_as_uint(inv_z));
+		inv_z = fadd(inv_z, dx);
+	}
 }
 
-__global__ void shadow_unpack_kernel(const unsigned long long* packed, float* storage, uint64_t n)
+// line_inv_z of the part's first row (rasterizer.rs:1442-1447); the next rows add dy one at a time.
+__device__ __forceinline__ float depth_first_line(const RasterPart& p, float dx, float dy, float k)
 {
-	for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
-		storage[i] = __uint_as_float(uint32_t(packed[i]));
+	return fadd(fadd(fmul(float(p.y_start_int), dy), fmul(0.5f, fadd(dx, dy))), k);
 }
 
-// One depth draw per CTA: thread 0 walks the edges (the colour rasteriser's walk: the same parts and
-// first-row edge positions) and accumulates each part's per-row inverse depth in the reference's
-// sequential order; then one thread per row accumulates along its span.
+} // namespace
+
+__global__ void shadow_rebase_kernel(unsigned long long* storage, uint64_t n)
+{
+	for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+		storage[i] &= 0xFFFFFFFFull;
+}
+
+// Host-prepared depth draws (sw_build_shadow_maps), one per CTA: thread 0 walks the edges (the colour
+// rasteriser's walk: the same parts and first-row edge positions) and accumulates each part's per-row
+// inverse depth in the reference's sequential order; then one thread per row accumulates along its span.
 __global__ void __launch_bounds__(256) shadow_draw_kernel(ShadowArgs a)
 {
 	__shared__ __align__(8) SwDrawCmd s_d;
@@ -614,16 +639,15 @@ __global__ void __launch_bounds__(256) shadow_draw_kernel(ShadowArgs a)
 		if (threadIdx.x == 0) s_np = edge_walk(s_d, s_v, size, s_parts);
 		__syncthreads();
 		const float dx = dd.depth_eq[0], dy = dd.depth_eq[1], k = dd.depth_eq[2];
-		const unsigned long long seq = (unsigned long long)(di + 1) << 32;
-		unsigned long long* map = a.packed + dd.map_offset;
+		const unsigned long long seq = (unsigned long long)(a.seq_base + di + 1u) << 32;
+		unsigned long long* map = a.storage + dd.map_offset;
 		for (uint32_t pi = 0; pi < s_np; ++pi)
 		{
 			const RasterPart p = s_parts[pi];
 			const uint32_t rows = uint32_t(p.y_end_int - p.y_start_int); // <= size <= SW_SHADOW_MAX_SIZE
 			if (threadIdx.x == 0)
 			{
-				// line_inv_z = y_start * dy + 0.5 * (dx + dy) + k, then += dy per row (rasterizer.rs:1442-1471)
-				float line = fadd(fadd(fmul(float(p.y_start_int), dy), fmul(0.5f, fadd(dx, dy))), k);
+				float line = depth_first_line(p, dx, dy, k);
 				for (uint32_t r = 0; r < rows; ++r)
 				{
 					s_line[r] = line;
@@ -631,32 +655,100 @@ __global__ void __launch_bounds__(256) shadow_draw_kernel(ShadowArgs a)
 				}
 			}
 			__syncthreads();
-			for (uint32_t r = threadIdx.x; r < rows; r += blockDim.x)
-			{
-				const int32_t y = p.y_start_int + int32_t(r);
-				const int32_t xs = max(wadd(p.x_left0, wmul(int32_t(r), p.dx_dy_left)) >> 16, 0);
-				const int32_t xe = min(wadd(p.x_right0, wmul(int32_t(r), p.dx_dy_right)) >> 16, size);
-				if (xs >= xe) continue;
-				float inv_z = fadd(s_line[r], fmul(float(xs), dx));
-				unsigned long long* line = map + uint64_t(y) * uint32_t(size);
-				for (int32_t x = xs; x < xe; ++x)
-				{
-					atomicMax(line + x, seq | __float_as_uint(inv_z));
-					inv_z = fadd(inv_z, dx);
-				}
-			}
+			for (uint32_t r = threadIdx.x; r < rows; r += blockDim.x) draw_depth_row(map, size, p, r, s_line[r], dx, seq);
 			__syncthreads(); // s_line is reused by the next part
+		}
+	}
+}
+
+// GPU-prepared depth draws (sw_build_shadow_maps_view): every polygon of every listed leaf is one warp,
+// which prepares it (DepthRenderer::draw_polygon::<false> + draw_depth_polygon, depth_renderer.rs:
+// 199-287: the shared depth_map_equation, the view transform, the warp-cooperative
+// project_and_clip_polygon, f32_to_fixed16) and draws it at once. The candidate's index in the leaf
+// list's polygon order is its painter's-order sequence, so nothing is compacted. Rows go to lanes 32 at
+// a time: lane i takes the 32-row chunk's first line_inv_z and adds dy i times, which is the
+// reference's sequential row accumulation; the next chunk starts from lane 31's value plus dy.
+constexpr int SHADOW_VIEW_WARPS = 8;
+
+struct ShadowWarpShared
+{
+	WarpClipBuf clip;
+	SwVertex16 v[SW_MAX_POLYGON_VERTICES];
+	RasterPart parts[SW_RASTER_MAX_PARTS];
+};
+
+__global__ void __launch_bounds__(SHADOW_VIEW_WARPS * 32) shadow_view_kernel(ShadowViewArgs a)
+{
+	__shared__ ShadowWarpShared s_w[SHADOW_VIEW_WARPS];
+	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+	const uint32_t c = blockIdx.x * SHADOW_VIEW_WARPS + warp;
+	if (c >= a.num_candidates) return; // whole warps; every later condition is the warp's polygon's too
+	ShadowWarpShared& sw = s_w[warp];
+	const uint32_t li = find_segment(a.leaf_base, a.num_leafs, c);
+	const SwShadowLeaf& leaf = a.leafs[li];
+	const SwShadowSide& side = a.sides[leaf.side];
+	const SwMapPolygon& p = a.polygons[leaf.first_polygon + (c - a.leaf_base[li])];
+	float eq[3];
+	if (!swhost::depth_map_equation(p, load_mat4(side.planes_matrix), eq)) return;
+	const uint32_t nv = p.num_vertices < MAXV ? p.num_vertices : MAXV;
+	if (nv < 3) return;
+	const Mat4 view = load_mat4(side.view_matrix);
+	const Vec3* mv = reinterpret_cast<const Vec3*>(a.map_vertices);
+	const Vec3 vt = lane < nv ? swhost::view_transform(view, mv[p.first_vertex + lane]) : swhost::v3(0.0f, 0.0f, 1.0f);
+	Vec3 planes[8];
+	load_planes(leaf.clip_planes, planes);
+	Vec2 v2d = swhost::v2(0.0f, 0.0f);
+	const uint32_t count = warp_project_and_clip(planes, vt, nv, v2d, sw.clip);
+	if (count < 3) return;
+	if (lane < count) // f32_to_fixed16 (fixed_math.rs:31-34)
+		sw.v[lane] = SwVertex16{swhost::as_i32(v2d.x * 65536.0f), swhost::as_i32(v2d.y * 65536.0f)};
+	__syncwarp();
+	const int32_t size = int32_t(side.map_size);
+	uint32_t np = 0;
+	if (lane == 0)
+	{
+		SwDrawCmd d{};
+		d.vertex_count = count;
+		d.mode = SW_RASTER_FULL_PERSPECTIVE; // no texture-coordinate edges
+		np = edge_walk(d, sw.v, size, sw.parts);
+	}
+	np = __shfl_sync(FULL_MASK, np, 0);
+	__syncwarp();
+	const float dx = eq[0], dy = eq[1], k = eq[2];
+	const unsigned long long seq = (unsigned long long)(a.seq_base + c + 1u) << 32;
+	unsigned long long* map = a.storage + side.map_offset;
+	for (uint32_t pi = 0; pi < np; ++pi)
+	{
+		const RasterPart pt = sw.parts[pi];
+		const uint32_t rows = uint32_t(pt.y_end_int - pt.y_start_int);
+		float chunk = depth_first_line(pt, dx, dy, k);
+		for (uint32_t r0 = 0; r0 < rows; r0 += 32)
+		{
+			float line = chunk;
+			for (uint32_t i = 0; i < lane; ++i) line = fadd(line, dy);
+			if (r0 + lane < rows) draw_depth_row(map, size, pt, r0 + lane, line, dx, seq);
+			chunk = fadd(__shfl_sync(FULL_MASK, line, 31), dy);
 		}
 	}
 }
 
 int launch_shadow_maps(const ShadowArgs& args, cudaStream_t stream)
 {
-	if (args.num_texels == 0) return 0;
-	const unsigned blocks = unsigned(std::min<uint64_t>((args.num_texels + 255) / 256, 4096));
-	shadow_pack_kernel<<<blocks, 256, 0, stream>>>(args.storage, args.packed, args.num_texels);
 	if (args.num_draws > 0) shadow_draw_kernel<<<std::min(args.num_draws, 65535u), 256, 0, stream>>>(args);
-	shadow_unpack_kernel<<<blocks, 256, 0, stream>>>(args.packed, args.storage, args.num_texels);
+	return int(cudaGetLastError());
+}
+
+int launch_shadow_view(const ShadowViewArgs& args, cudaStream_t stream)
+{
+	if (args.num_candidates == 0) return 0;
+	shadow_view_kernel<<<(args.num_candidates + SHADOW_VIEW_WARPS - 1) / SHADOW_VIEW_WARPS, SHADOW_VIEW_WARPS * 32, 0, stream>>>(args);
+	return int(cudaGetLastError());
+}
+
+int launch_shadow_rebase(unsigned long long* storage, uint64_t num_texels, cudaStream_t stream)
+{
+	if (num_texels == 0) return 0;
+	shadow_rebase_kernel<<<unsigned(std::min<uint64_t>((num_texels + 255) / 256, 4096)), 256, 0, stream>>>(storage, num_texels);
 	return int(cudaGetLastError());
 }
 

@@ -116,7 +116,7 @@ __device__ __forceinline__ uint32_t wrap(int32_t a, uint32_t b)
 }
 
 // cube_shadow_map_side_fetch (light.rs:235-258): 1 in light, 0 in shadow.
-__device__ __forceinline__ float cube_side_fetch(const float* side, uint32_t size, float x, float y, float z)
+__device__ __forceinline__ float cube_side_fetch(const unsigned long long* side, uint32_t size, float x, float y, float z)
 {
 	const float ONE_MINUS_EPS = 1.0f - 1.0f / 65536.0f;
 	const float size_f = float(size);
@@ -125,7 +125,7 @@ __device__ __forceinline__ float cube_side_fetch(const float* side, uint32_t siz
 	const float u_f = fmul(fminf(fmaxf(fadd(fmul(x, half_depth), 0.5f), 0.0f), ONE_MINUS_EPS), size_f);
 	const float v_f = fmul(fminf(fmaxf(fadd(fmul(y, half_depth), 0.5f), 0.0f), ONE_MINUS_EPS), size_f);
 	const uint32_t u = __float2uint_rz(u_f), v = __float2uint_rz(v_f); // in [0, size)
-	return depth >= __ldg(side + u + v * size) ? 1.0f : 0.0f;
+	return depth >= __uint_as_float(uint32_t(__ldg(side + u + v * size))) ? 1.0f : 0.0f; // the texel's f32 bits
 }
 
 // get_light_shadow_factor / cube_shadow_map_fetch (light.rs:185-233) for `to_light` = light - point.
@@ -135,7 +135,7 @@ __device__ __forceinline__ float light_shadow_factor(const SurfaceKernelArgs& a,
 	const SwLightShadow m = a.shadows[light];
 	if (m.kind != SW_SHADOW_CUBE) return 1.0f;
 	const uint64_t side_texels = uint64_t(m.size) * m.size;
-	const float* maps = a.shadow_texels + m.offset;
+	const unsigned long long* maps = a.shadow_texels + m.offset;
 	const float ax = fabsf(to_light.x), ay = fabsf(to_light.y), az = fabsf(to_light.z);
 	if (ax >= ay && ax >= az)
 		return to_light.x >= 0.0f ? cube_side_fetch(maps + 1 * side_texels, m.size, -to_light.y, to_light.z, ax)

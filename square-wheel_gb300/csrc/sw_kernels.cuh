@@ -47,7 +47,7 @@ struct SurfaceKernelArgs
 	uint64_t total_work;
 	const SwViewCounts* counts; // GPU-side preparation: num_surfaces / total_work from here (else NULL)
 	const SwLightShadow* shadows; // per light (NULL: no shadows), maps in shadow_texels
-	const float* shadow_texels;
+	const unsigned long long* shadow_texels; // (sequence << 32 | f32 bits) per texel
 	uint32_t num_shadows;
 	const uint64_t* texels;
 	const uint32_t* emissive_pixels;
@@ -254,20 +254,34 @@ __host__ __device__ inline void draw_row_range(const SwDrawCmd& d, const SwVerte
 
 // ---- shadow maps ----
 
-#define SW_SHADOW_MAX_SIZE 1024 // cube side size limit (the reference's cube maps are 64..256)
 
 struct ShadowArgs
 {
 	const SwDepthDraw* draws;
 	uint32_t num_draws;
+	uint32_t seq_base;               // draw i writes sequence seq_base + i + 1 (< 2^32)
 	const SwVertex16* vertices;
-	float* storage;               // the persistent f32 shadow-map storage
-	unsigned long long* packed;   // scratch: (draw sequence << 32 | f32 bits) per texel
-	uint64_t num_texels;
+	unsigned long long* storage;     // the persistent storage: (sequence << 32 | f32 bits) per texel
 };
-
-// Pack the storage, draw every depth draw (last draw wins per texel), unpack.
+// Draw every depth draw into the storage (last draw wins per texel).
 int launch_shadow_maps(const ShadowArgs& args, cudaStream_t stream);
+
+// GPU-side depth-draw preparation and drawing (sw_build_shadow_maps_view): candidate c is the c-th
+// polygon of the listed leafs, drawn with sequence seq_base + c + 1.
+struct ShadowViewArgs
+{
+	const SwShadowSide* sides;
+	const SwShadowLeaf* leafs;
+	const uint32_t* leaf_base; // first candidate of each leaf (exclusive prefix sum of num_polygons)
+	uint32_t num_leafs, num_candidates;
+	const SwMapPolygon* polygons;
+	const float* map_vertices;
+	unsigned long long* storage;
+	uint32_t seq_base;
+};
+int launch_shadow_view(const ShadowViewArgs& args, cudaStream_t stream);
+// Sequences restart at 0: keep only the f32 bits of every texel.
+int launch_shadow_rebase(unsigned long long* storage, uint64_t num_texels, cudaStream_t stream);
 
 // ---- GPU-side surface and draw preparation (prep.cu) ----
 

@@ -168,7 +168,8 @@ struct SwCtx
 
 	// Shadow maps (sw_build_shadow_maps / sw_set_light_shadows): the persistent f32 storage (grows, keeps
 	// its contents), the packing scratch, and the frame's per-light descriptors on the device.
-	DevBuf shadow_storage, shadow_packed, shadow_descs;
+	DevBuf shadow_storage, shadow_descs;
+	uint32_t shadow_seq = 0; // the next depth draw's sequence base (the storage's high words)
 	uint64_t shadow_texels = 0;
 	uint32_t num_shadow_descs = 0;
 	Staging stage_shadow, stage_shadow_descs;
@@ -531,7 +532,7 @@ int sw_destroy(SwCtx* ctx)
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->parts, &ctx->part_counts, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst, &ctx->map_polygons,
-		&ctx->map_vertices, &ctx->vslab, &ctx->shadow_storage, &ctx->shadow_packed, &ctx->shadow_descs};
+		&ctx->map_vertices, &ctx->vslab, &ctx->shadow_storage, &ctx->shadow_descs};
 	for (DevBuf* b : bufs) release(*b);
 	for (const SwCtx::HostRange& h : ctx->registered) cudaHostUnregister(h.ptr);
 	if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
@@ -644,7 +645,7 @@ static int launch_surfaces(SwCtx* ctx, const SurfaceInputs* in = nullptr)
 	SurfaceKernelArgs a;
 	std::memset(&a, 0, sizeof(a)); // optional fields (counts, cam_pos_dev) stay unset on this path
 	a.shadows = ctx->num_shadow_descs ? static_cast<const SwLightShadow*>(ctx->shadow_descs.ptr) : nullptr;
-	a.shadow_texels = static_cast<const float*>(ctx->shadow_storage.ptr);
+	a.shadow_texels = static_cast<const unsigned long long*>(ctx->shadow_storage.ptr);
 	a.num_shadows = ctx->num_shadow_descs;
 	a.surfaces = in ? in->surfaces : static_cast<const SurfaceGpu*>(ctx->surfaces.ptr);
 	a.work_prefix = in ? in->work_prefix : static_cast<const uint64_t*>(ctx->work_prefix.ptr);
@@ -1765,7 +1766,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	sa.lights = pr.lights;
 	sa.cam_pos_dev = reinterpret_cast<const float*>(d + vb.cam);
 	sa.shadows = ctx->num_shadow_descs ? static_cast<const SwLightShadow*>(ctx->shadow_descs.ptr) : nullptr;
-	sa.shadow_texels = static_cast<const float*>(ctx->shadow_storage.ptr);
+	sa.shadow_texels = static_cast<const unsigned long long*>(ctx->shadow_storage.ptr);
 	sa.num_shadows = ctx->num_shadow_descs;
 	sa.arena = ctx->arena.ptr;
 	// surface grid: from the latest frame's texels with headroom; it changes (and the graphs are captured
@@ -1918,6 +1919,31 @@ int grow_preserve(SwCtx* ctx, DevBuf& b, size_t bytes)
 	b.bytes = want;
 	return SW_OK;
 }
+// The shadow-map storage: (sequence << 32 | f32 bits) per texel, grown with its contents kept (new
+// texels read 0 with sequence 0).
+int grow_shadow_storage(SwCtx* ctx, uint64_t total_texels)
+{
+	int r = grow_preserve(ctx, ctx->shadow_storage, std::max<uint64_t>(total_texels, 1) * 8);
+	if (r) return r;
+	ctx->shadow_texels = std::max(ctx->shadow_texels, total_texels);
+	return SW_OK;
+}
+
+// Sequences of the next `count` depth draws: base + 1 .. base + count, above every sequence in the
+// storage; when they would pass 2^32 - 1 the storage drops its sequences (keeping its depths) first.
+int shadow_sequence(SwCtx* ctx, uint64_t count, uint32_t* base)
+{
+	if (uint64_t(ctx->shadow_seq) + count >= 0xFFFFFFFFull)
+	{
+		int r = check_kernel(ctx, launch_shadow_rebase(static_cast<unsigned long long*>(ctx->shadow_storage.ptr),
+			ctx->shadow_texels, ctx->stream), "shadow-map rebase");
+		if (r) return r;
+		ctx->shadow_seq = 0;
+	}
+	*base = ctx->shadow_seq;
+	ctx->shadow_seq += uint32_t(count);
+	return SW_OK;
+}
 } // namespace
 
 int sw_build_shadow_maps(SwCtx* ctx, const SwDepthDraw* draws, uint32_t num_draws, const SwVertex16* vertices,
@@ -1935,10 +1961,8 @@ int sw_build_shadow_maps(SwCtx* ctx, const SwDepthDraw* draws, uint32_t num_draw
 	}
 	SW_CUDA(ctx, cudaSetDevice(ctx->device));
 	int r;
-	if ((r = grow_preserve(ctx, ctx->shadow_storage, std::max<uint64_t>(total_texels, 1) * 4))) return r;
-	ctx->shadow_texels = std::max(ctx->shadow_texels, total_texels);
+	if ((r = grow_shadow_storage(ctx, total_texels))) return r;
 	if (num_draws == 0) return SW_OK;
-	if ((r = ensure(ctx, ctx->shadow_packed, total_texels * 8))) return r;
 	// draws and vertices in one upload
 	const size_t vo = align_up(size_t(num_draws) * sizeof(SwDepthDraw), 256);
 	const size_t bytes = vo + size_t(num_vertices) * sizeof(SwVertex16);
@@ -1949,13 +1973,72 @@ int sw_build_shadow_maps(SwCtx* ctx, const SwDepthDraw* draws, uint32_t num_draw
 	std::memcpy(static_cast<unsigned char*>(h) + vo, vertices, size_t(num_vertices) * sizeof(SwVertex16));
 	if ((r = staging_commit(ctx, ctx->stage_shadow, ctx->up_src.ptr, bytes))) return r;
 	ShadowArgs a;
+	std::memset(&a, 0, sizeof(a));
+	if ((r = shadow_sequence(ctx, num_draws, &a.seq_base))) return r;
 	a.draws = static_cast<const SwDepthDraw*>(ctx->up_src.ptr);
 	a.num_draws = num_draws;
 	a.vertices = reinterpret_cast<const SwVertex16*>(static_cast<unsigned char*>(ctx->up_src.ptr) + vo);
-	a.storage = static_cast<float*>(ctx->shadow_storage.ptr);
-	a.packed = static_cast<unsigned long long*>(ctx->shadow_packed.ptr);
-	a.num_texels = total_texels;
+	a.storage = static_cast<unsigned long long*>(ctx->shadow_storage.ptr);
 	return check_kernel(ctx, launch_shadow_maps(a, ctx->stream), "shadow maps");
+}
+
+int sw_build_shadow_maps_view(SwCtx* ctx, const SwShadowSide* sides, uint32_t num_sides, const SwShadowLeaf* leafs,
+	uint32_t num_leafs, uint64_t total_texels)
+{
+	if (!ctx || (num_sides && !sides) || (num_leafs && !leafs)) return SW_ERR_INVALID_ARGUMENT;
+	if (total_texels > (uint64_t(1) << 34)) return fail(ctx, SW_ERR_LIMIT, "shadow-map storage too large");
+	if (num_leafs && !ctx->num_map_polygons) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "no map: call sw_set_map first");
+	for (uint32_t i = 0; i < num_sides; ++i)
+	{
+		const SwShadowSide& sd = sides[i];
+		if (sd.map_size == 0 || sd.map_size > SW_SHADOW_MAX_SIZE || sd.map_offset + uint64_t(sd.map_size) * sd.map_size > total_texels)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "shadow side %u: map outside the storage", i);
+	}
+	uint64_t candidates = 0;
+	for (uint32_t i = 0; i < num_leafs; ++i)
+	{
+		const SwShadowLeaf& l = leafs[i];
+		if (l.side >= num_sides) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "shadow leaf %u: no side %u", i, l.side);
+		if (uint64_t(l.first_polygon) + l.num_polygons > ctx->num_map_polygons)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "shadow leaf %u: polygons outside the map", i);
+		candidates += l.num_polygons;
+	}
+	if (candidates > (uint64_t(1) << 30)) return fail(ctx, SW_ERR_LIMIT, "too many shadow candidates");
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	int r;
+	if ((r = grow_shadow_storage(ctx, total_texels))) return r;
+	if (candidates == 0) return SW_OK;
+	// sides, leafs and the leafs' first candidates in one upload
+	const size_t lo = align_up(size_t(num_sides) * sizeof(SwShadowSide), 256);
+	const size_t bo = align_up(lo + size_t(num_leafs) * sizeof(SwShadowLeaf), 256);
+	const size_t bytes = bo + size_t(num_leafs) * 4;
+	if ((r = ensure(ctx, ctx->up_src, bytes))) return r;
+	void* h = nullptr;
+	if ((r = staging_acquire(ctx, ctx->stage_shadow, bytes, &h))) return r;
+	unsigned char* hb = static_cast<unsigned char*>(h);
+	std::memcpy(hb, sides, size_t(num_sides) * sizeof(SwShadowSide));
+	std::memcpy(hb + lo, leafs, size_t(num_leafs) * sizeof(SwShadowLeaf));
+	uint32_t* base = reinterpret_cast<uint32_t*>(hb + bo);
+	uint32_t c = 0;
+	for (uint32_t i = 0; i < num_leafs; ++i)
+	{
+		base[i] = c;
+		c += leafs[i].num_polygons;
+	}
+	if ((r = staging_commit(ctx, ctx->stage_shadow, ctx->up_src.ptr, bytes))) return r;
+	unsigned char* db = static_cast<unsigned char*>(ctx->up_src.ptr);
+	ShadowViewArgs a;
+	std::memset(&a, 0, sizeof(a));
+	if ((r = shadow_sequence(ctx, candidates, &a.seq_base))) return r;
+	a.sides = reinterpret_cast<const SwShadowSide*>(db);
+	a.leafs = reinterpret_cast<const SwShadowLeaf*>(db + lo);
+	a.leaf_base = reinterpret_cast<const uint32_t*>(db + bo);
+	a.num_leafs = num_leafs;
+	a.num_candidates = uint32_t(candidates);
+	a.polygons = static_cast<const SwMapPolygon*>(ctx->map_polygons.ptr);
+	a.map_vertices = static_cast<const float*>(ctx->map_vertices.ptr);
+	a.storage = static_cast<unsigned long long*>(ctx->shadow_storage.ptr);
+	return check_kernel(ctx, launch_shadow_view(a, ctx->stream), "shadow maps");
 }
 
 int sw_set_light_shadows(SwCtx* ctx, const SwLightShadow* shadows, uint32_t num_lights)
@@ -1986,7 +2069,14 @@ int sw_read_shadow_maps(SwCtx* ctx, float* dst, uint64_t max_texels)
 	SW_CUDA(ctx, cudaSetDevice(ctx->device));
 	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 	const uint64_t n = std::min(max_texels, ctx->shadow_texels);
-	if (n) SW_CUDA(ctx, cudaMemcpy(dst, ctx->shadow_storage.ptr, n * 4, cudaMemcpyDeviceToHost));
+	if (!n) return SW_OK;
+	std::vector<unsigned long long> packed(n);
+	SW_CUDA(ctx, cudaMemcpy(packed.data(), ctx->shadow_storage.ptr, n * 8, cudaMemcpyDeviceToHost));
+	for (uint64_t i = 0; i < n; ++i)
+	{
+		const uint32_t bits = uint32_t(packed[i]);
+		std::memcpy(dst + i, &bits, 4);
+	}
 	return SW_OK;
 }
 
@@ -2069,14 +2159,15 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 
 int sw_abi_layout(uint32_t* sizes, uint32_t count)
 {
-	const uint32_t s[19] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
+	const uint32_t s[21] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
 		uint32_t(sizeof(SwDirectionalLightmapElement)), uint32_t(sizeof(SwLight)), uint32_t(sizeof(SwSurfaceDesc)),
 		uint32_t(sizeof(SwVertex16)), uint32_t(sizeof(SwDrawCmd)), uint32_t(sizeof(SwFrameParams)),
 		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats)), uint32_t(sizeof(SwFrameInput)), uint32_t(sizeof(SwTuning)),
 		uint32_t(sizeof(SwMapPolygon)), uint32_t(sizeof(SwViewLeaf)), uint32_t(sizeof(SwViewFrameInput)),
-		uint32_t(sizeof(SwViewCounts)), uint32_t(sizeof(SwLightShadow)), uint32_t(sizeof(SwDepthDraw))};
-	for (uint32_t i = 0; sizes && i < count && i < 19; ++i) sizes[i] = s[i];
-	return 19;
+		uint32_t(sizeof(SwViewCounts)), uint32_t(sizeof(SwLightShadow)), uint32_t(sizeof(SwDepthDraw)),
+		uint32_t(sizeof(SwShadowSide)), uint32_t(sizeof(SwShadowLeaf))};
+	for (uint32_t i = 0; sizes && i < count && i < 21; ++i) sizes[i] = s[i];
+	return 21;
 }
 
 int sw_get_stats(SwCtx* ctx, SwStats* out)

@@ -260,6 +260,8 @@ void FramePrep::prepare_shadows()
 	// light order; build_shadow_maps (:525-592) draws them with DepthRenderer::draw_map.
 	depth_draws.clear();
 	depth_vertices.clear();
+	shadow_sides.clear();
+	shadow_leafs.clear();
 	light_shadows.assign(lights.size(), SwLightShadow{SW_SHADOW_NONE, 0u, 0ull});
 	uint64_t offset = 0;
 	for (uint32_t li = 0; li < lights.size(); ++li)
@@ -294,9 +296,11 @@ void FramePrep::prepare_shadows()
 	shadow_texels = offset;
 }
 
-void FramePrep::draw_depth_map(const CameraMatrices& camera, uint32_t size, uint64_t map_offset)
+template <class F>
+void FramePrep::for_each_depth_leaf(const CameraMatrices& camera, uint32_t size, F&& leaf_fn)
 {
-	// DepthRenderer::draw_map / draw_tree / draw_leaf / draw_polygon (depth_renderer.rs:45-287)
+	// DepthRenderer::draw_map / draw_tree / draw_leaf (depth_renderer.rs:45-197): the side camera's
+	// visibility from the light, then the leafs it reaches, back to front
 	const float fs = float(size);
 	shadow_vis.update(camera, ClippingPolygon::from_box(0.0f, 0.0f, fs, fs));
 	const Vec4 w_row = camera.planes_matrix.row(3);
@@ -313,8 +317,7 @@ void FramePrep::draw_depth_map(const CameraMatrices& camera, uint32_t size, uint
 			if (!shadow_vis.visible(leaf)) continue;
 			Vec3 planes[8];
 			shadow_vis.bounds(leaf).get_clip_planes(planes);
-			const BspLeaf& lv = sc.leafs[leaf];
-			for (uint32_t k = 0; k < lv.num_polygons; ++k) draw_depth_polygon(camera, planes, lv.first_polygon + k, size, map_offset);
+			leaf_fn(leaf, planes);
 		}
 		else if (n < MAX_BSP_TREE_DEPTH)
 		{
@@ -330,25 +333,51 @@ void FramePrep::draw_depth_map(const CameraMatrices& camera, uint32_t size, uint
 	}
 }
 
+void FramePrep::draw_depth_map(const CameraMatrices& camera, uint32_t size, uint64_t map_offset)
+{
+	if (shadow_view)
+	{
+		// the GPU prepares the polygons (sw_build_shadow_maps_view): record the side and its leafs
+		SwShadowSide sd;
+		std::memset(&sd, 0, sizeof(sd));
+		std::memcpy(sd.view_matrix, &camera.view_matrix, sizeof(sd.view_matrix));
+		std::memcpy(sd.planes_matrix, &camera.planes_matrix, sizeof(sd.planes_matrix));
+		sd.map_size = size;
+		sd.map_offset = map_offset;
+		const uint32_t side = uint32_t(shadow_sides.size());
+		shadow_sides.push_back(sd);
+		for_each_depth_leaf(camera, size, [this, side](uint32_t leaf, const Vec3 planes[8]) {
+			const BspLeaf& lv = sc.leafs[leaf];
+			SwShadowLeaf sl;
+			std::memset(&sl, 0, sizeof(sl));
+			sl.side = side;
+			sl.first_polygon = lv.first_polygon;
+			sl.num_polygons = lv.num_polygons;
+			for (int k = 0; k < 8; ++k)
+			{
+				sl.clip_planes[k][0] = planes[k].x;
+				sl.clip_planes[k][1] = planes[k].y;
+				sl.clip_planes[k][2] = planes[k].z;
+			}
+			shadow_leafs.push_back(sl);
+		});
+		return;
+	}
+	for_each_depth_leaf(camera, size, [this, &camera, size, map_offset](uint32_t leaf, const Vec3 planes[8]) {
+		const BspLeaf& lv = sc.leafs[leaf];
+		for (uint32_t k = 0; k < lv.num_polygons; ++k) draw_depth_polygon(camera, planes, lv.first_polygon + k, size, map_offset);
+	});
+}
+
 void FramePrep::draw_depth_polygon(const CameraMatrices& camera, const Vec3 clip_planes[8], uint32_t polygon_index, uint32_t size,
 	uint64_t map_offset)
 {
 	// DepthRenderer::draw_polygon::<false> + draw_depth_polygon (depth_renderer.rs:199-287)
-	const MapPolygon& p = sc.polygons[polygon_index];
-	const Material& m = sc.materials[p.texture];
-	if (!(m.shadow && m.blending_mode == SW_BLEND_NONE)) return; // materials_shadow_table (:20-38)
-	const Vec4 pt = camera.planes_matrix * extend(p.plane.vec, -p.plane.dist);
-	if (pt.w <= 0.0f) return;
-	const float pw = -pt.w;
-	const float d_inv_z_dx = pt.x / pw, d_inv_z_dy = pt.y / pw;
-	const float DEPTH_BIAS_CONST = -1.0f / float(1 << 20), DEPTH_BIAS_SLOPE = -1.0f;
-	const float DEPTH_EQUATION_SCALE = 1.0f - 1.0f / 1024.0f;
+	const SwMapPolygon& p = map_polygons[polygon_index];
 	SwDepthDraw d;
 	std::memset(&d, 0, sizeof(d));
-	d.depth_eq[0] = DEPTH_EQUATION_SCALE * d_inv_z_dx;
-	d.depth_eq[1] = DEPTH_EQUATION_SCALE * d_inv_z_dy;
-	d.depth_eq[2] = DEPTH_EQUATION_SCALE * (pt.z / pw + DEPTH_BIAS_CONST + DEPTH_BIAS_SLOPE * (std::fabs(d_inv_z_dx) + std::fabs(d_inv_z_dy)));
-	const uint32_t nv = std::min(p.num_vertices, MAX_VERTICES);
+	if (!depth_map_equation(p, camera.planes_matrix, d.depth_eq)) return;
+	const uint32_t nv = std::min(p.num_vertices, PREP_MAX_VERTICES);
 	if (nv < 3) return;
 	Vec3 vt[MAX_VERTICES];
 	for (uint32_t i = 0; i < nv; ++i) vt[i] = view_transform(camera.view_matrix, sc.vertices[p.first_vertex + i]);
@@ -645,6 +674,7 @@ void FramePrep::finish_params()
 void FramePrep::prepare_with_camera(const CameraMatrices& camera, const std::vector<SwLight>& frame_lights,
 	const FrameOptions& options, Quat skybox_rotation)
 {
+	shadow_view = false;
 	begin_frame(camera, frame_lights, options, skybox_rotation);
 	prepare_polygons_surfaces();
 	build_surface_descs();
@@ -662,6 +692,7 @@ void FramePrep::prepare_with_camera(const CameraMatrices& camera, const std::vec
 void FramePrep::prepare_view_with_camera(const CameraMatrices& camera, const std::vector<SwLight>& frame_lights,
 	const FrameOptions& options, Quat skybox_rotation)
 {
+	shadow_view = true;
 	begin_frame(camera, frame_lights, options, skybox_rotation);
 	// The visible leafs in index order (prepare_polygons_surfaces' order, :1327-1359) with their bounds and
 	// lights; the sky polygons' bounds are collected here, every other polygon is the GPU's.

@@ -127,6 +127,10 @@ public:
 	std::vector<SwDepthDraw> depth_draws;
 	std::vector<SwVertex16> depth_vertices;
 	uint64_t shadow_texels = 0;
+	// prepare_view: the depth draws are the GPU's (sw_build_shadow_maps_view); the host lists each side
+	// and the leafs its visibility reaches, back to front (depth_draws / depth_vertices stay empty).
+	std::vector<SwShadowSide> shadow_sides;
+	std::vector<SwShadowLeaf> shadow_leafs;
 
 private:
 	struct PolyData
@@ -153,6 +157,7 @@ private:
 	CameraMatrices cam{};
 	FrameOptions opt;
 	Quat sky_rotation{1.0f, Vec3{0.0f, 0.0f, 0.0f}};
+	bool shadow_view = false;    // prepare_view: list the shadow sides' leafs instead of depth draws
 	bool has_sky = false;        // current_sky (partial_renderer.rs:35): a sky polygon is visible
 	ClippingPolygon sky_bounds{}; // union of the visible sky polygons' screen bounds
 	std::vector<uint32_t> sky_polygons;   // polygons of the sky material, grouped by leaf
@@ -164,6 +169,8 @@ private:
 	void prepare_polygon_surface(const Vec3 clip_planes[8], uint64_t& offset, uint32_t polygon_index);
 	void extend_sky_bounds(const Vec2* v2d, uint32_t count);
 	void prepare_shadows();
+	template <class F>
+	void for_each_depth_leaf(const CameraMatrices& camera, uint32_t size, F&& leaf_fn);
 	void draw_depth_map(const CameraMatrices& camera, uint32_t size, uint64_t map_offset);
 	void draw_depth_polygon(const CameraMatrices& camera, const Vec3 clip_planes[8], uint32_t polygon_index, uint32_t size,
 		uint64_t map_offset);

@@ -307,6 +307,25 @@ enum PrepResult
 	PREP_SKY = 2,     // visible sky polygon: v2d[0..count) is its projection
 };
 
+// DepthRenderer::draw_polygon::<false> + draw_depth_polygon (depth_renderer.rs:199-287), the part before
+// the clipping: shadow-casting opaque polygons facing the side camera (materials_shadow_table, :20-38),
+// and their depth equation (DepthEquation::from_transformed_plane_equation) with the constant and slope
+// bias added and the whole scaled by 1 - 1/1024. False: the polygon draws nothing.
+SWH_HD inline bool depth_map_equation(const SwMapPolygon& p, const Mat4& planes_matrix, float eq[3])
+{
+	if (!(p.flags & SW_POLY_SHADOW) || p.blending_mode != SW_BLEND_NONE) return false;
+	const Vec4 pt = planes_matrix * extend(poly_vec3(p.plane), -p.plane[3]);
+	if (pt.w <= 0.0f) return false;
+	const float pw = -pt.w;
+	const float d_inv_z_dx = pt.x / pw, d_inv_z_dy = pt.y / pw;
+	const float DEPTH_BIAS_CONST = -1.0f / float(1 << 20), DEPTH_BIAS_SLOPE = -1.0f;
+	const float DEPTH_EQUATION_SCALE = 1.0f - 1.0f / 1024.0f;
+	eq[0] = DEPTH_EQUATION_SCALE * d_inv_z_dx;
+	eq[1] = DEPTH_EQUATION_SCALE * d_inv_z_dy;
+	eq[2] = DEPTH_EQUATION_SCALE * (pt.z / pw + DEPTH_BIAS_CONST + DEPTH_BIAS_SLOPE * (fabsf(d_inv_z_dx) + fabsf(d_inv_z_dy)));
+	return true;
+}
+
 // prepare_polygon_surface, partial_renderer.rs:1464-1638. Transforms the polygon's first
 // min(num_vertices, PREP_MAX_VERTICES) vertices into vt (the ones project_and_clip_polygon reads) and
 // returns the projected, clipped polygon in v2d / *count.

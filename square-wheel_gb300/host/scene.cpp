@@ -941,7 +941,8 @@ void Scene::map_polygons(std::vector<SwMapPolygon>& out) const
 		o.num_vertices = p.num_vertices;
 		o.texture = p.texture;
 		o.lightmap_data_offset = p.lightmap_data_offset;
-		o.flags = (m.draw ? SW_POLY_DRAW : 0u) | (m.skybox ? SW_POLY_SKY : 0u) | ((m.light && m.has_diffuse) ? SW_POLY_DIFFUSE_LAYER : 0u);
+		o.flags = (m.draw ? SW_POLY_DRAW : 0u) | (m.skybox ? SW_POLY_SKY : 0u) | ((m.light && m.has_diffuse) ? SW_POLY_DIFFUSE_LAYER : 0u) |
+			(m.shadow ? SW_POLY_SHADOW : 0u);
 		o.blending_mode = m.blending_mode;
 		o.emissive_texture = m.emissive >= 0 ? uint32_t(m.emissive) : SW_NO_EMISSIVE;
 		o.emissive_light[0] = m.emissive_light[0], o.emissive_light[1] = m.emissive_light[1], o.emissive_light[2] = m.emissive_light[2];

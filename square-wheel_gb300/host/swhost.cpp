@@ -39,14 +39,18 @@ namespace
 // build_shadow_maps (partial_renderer.rs:525-592) for the frame, and its lights' shadow maps.
 int submit_shadows(SwhRenderer* r, const FramePrep& p)
 {
-	if (p.depth_draws.empty() && p.shadow_texels == 0)
+	if (p.shadow_texels == 0)
 	{
 		if (!r->shadows_set) return SW_OK;
 		r->shadows_set = false;
 		return sw_set_light_shadows(r->ctx, nullptr, 0);
 	}
-	int st = sw_build_shadow_maps(r->ctx, p.depth_draws.data(), uint32_t(p.depth_draws.size()), p.depth_vertices.data(),
-		uint32_t(p.depth_vertices.size()), p.shadow_texels);
+	// prepare_view lists sides and leafs (the GPU prepares their polygons); prepare lists depth draws
+	int st = !p.shadow_sides.empty()
+		? sw_build_shadow_maps_view(r->ctx, p.shadow_sides.data(), uint32_t(p.shadow_sides.size()), p.shadow_leafs.data(),
+			  uint32_t(p.shadow_leafs.size()), p.shadow_texels)
+		: sw_build_shadow_maps(r->ctx, p.depth_draws.data(), uint32_t(p.depth_draws.size()), p.depth_vertices.data(),
+			  uint32_t(p.depth_vertices.size()), p.shadow_texels);
 	if (st) return st;
 	r->shadows_set = true;
 	return sw_set_light_shadows(r->ctx, p.light_shadows.data(), uint32_t(p.light_shadows.size()));
@@ -277,6 +281,10 @@ int swh_frame_outputs(const SwhFrame* f, SwhFrameOutputs* out)
 	out->num_depth_vertices = uint32_t(p.depth_vertices.size());
 	out->depth_vertices = p.depth_vertices.data();
 	out->shadow_texels = p.shadow_texels;
+	out->shadow_sides = p.shadow_sides.data();
+	out->num_shadow_sides = uint32_t(p.shadow_sides.size());
+	out->num_shadow_leafs = uint32_t(p.shadow_leafs.size());
+	out->shadow_leafs = p.shadow_leafs.data();
 	return SW_OK;
 }
 

@@ -34,7 +34,7 @@ SW_MAX_POLYGON_VERTICES = 24
 SW_NO_LIGHTMAP = 0
 SW_NO_EMISSIVE = 0xFFFFFFFF
 SW_SURF_DIFFUSE_LAYER = 1
-SW_POLY_DRAW, SW_POLY_SKY, SW_POLY_DIFFUSE_LAYER = 1, 2, 4
+SW_POLY_DRAW, SW_POLY_SKY, SW_POLY_DIFFUSE_LAYER, SW_POLY_SHADOW = 1, 2, 4, 8
 SW_LEAF_NOT_DRAWN = 0xFFFFFFFF
 SW_SHADOW_NONE, SW_SHADOW_CUBE = 0, 1
 
@@ -63,6 +63,10 @@ MAP_POLYGON = np.dtype([
 LIGHT_SHADOW = np.dtype([("kind", "<u4"), ("size", "<u4"), ("offset", "<u8")], align=True)
 DEPTH_DRAW = np.dtype([("first_vertex", "<u4"), ("vertex_count", "<u4"), ("map_size", "<u4"), ("reserved", "<u4"),
                        ("map_offset", "<u8"), ("depth_eq", "<f4", 3), ("reserved2", "<u4")], align=True)
+SHADOW_SIDE = np.dtype([("view_matrix", "<f4", 16), ("planes_matrix", "<f4", 16), ("map_size", "<u4"),
+                        ("reserved", "<u4"), ("map_offset", "<u8")], align=True)
+SHADOW_LEAF = np.dtype([("side", "<u4"), ("first_polygon", "<u4"), ("num_polygons", "<u4"), ("reserved", "<u4"),
+                        ("clip_planes", "<f4", (8, 3))], align=True)
 VIEW_LEAF = np.dtype([
     ("first_polygon", "<u4"), ("num_polygons", "<u4"), ("first_light", "<u4"), ("num_lights", "<u4"),
     ("draw_order", "<u4"), ("reserved", "<u4"), ("clip_planes", "<f4", (8, 3)), ("draw_clip_planes", "<f4", (8, 3))],
@@ -156,6 +160,7 @@ LAYOUT_ORDER = [
     ("SwMapPolygon", MAP_POLYGON.itemsize), ("SwViewLeaf", VIEW_LEAF.itemsize),
     ("SwViewFrameInput", ctypes.sizeof(ViewFrameInput)), ("SwViewCounts", ctypes.sizeof(ViewCounts)),
     ("SwLightShadow", LIGHT_SHADOW.itemsize), ("SwDepthDraw", DEPTH_DRAW.itemsize),
+    ("SwShadowSide", SHADOW_SIDE.itemsize), ("SwShadowLeaf", SHADOW_LEAF.itemsize),
 ]
 
 

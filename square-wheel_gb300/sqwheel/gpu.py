@@ -25,7 +25,7 @@ EXPORTED = [
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
     "sw_postprocess_noalloc", "sw_set_learned_upscaler", "sw_draw_frame", "sw_set_frame_graph", "sw_set_tuning",
     "sw_get_tuning", "sw_autotune", "sw_set_map", "sw_draw_frame_view", "sw_read_view_prep",
-    "sw_build_shadow_maps", "sw_set_light_shadows", "sw_read_shadow_maps",
+    "sw_build_shadow_maps", "sw_set_light_shadows", "sw_read_shadow_maps", "sw_build_shadow_maps_view",
     # learned upscaler (include/swlearn.h)
     "sw_upscaler_create", "sw_upscaler_destroy", "sw_upscaler_last_error", "sw_upscaler_get_params",
     "sw_upscaler_set_params", "sw_upscaler_gradients", "sw_upscaler_train_step", "sw_upscaler_steps",
@@ -87,6 +87,7 @@ def load_library(path=LIB_PATH):
         "sw_build_shadow_maps": ([vp, vp, u32, vp, u32, u64], i32),
         "sw_set_light_shadows": ([vp, vp, u32], i32),
         "sw_read_shadow_maps": ([vp, vp, u64], i32),
+        "sw_build_shadow_maps_view": ([vp, vp, u32, vp, u32, u64], i32),
         "sw_upscaler_create": ([i32, u64, ctypes.POINTER(vp)], i32),
         "sw_upscaler_destroy": ([vp], i32),
         "sw_upscaler_last_error": ([vp], ctypes.c_char_p),
@@ -221,6 +222,13 @@ class GpuRenderer:
         sh = np.ascontiguousarray(shadows if shadows is not None else np.zeros(0, abi.LIGHT_SHADOW), dtype=abi.LIGHT_SHADOW)
         self._shadows = sh
         self._check(self.lib.sw_set_light_shadows(self.ctx, abi.ptr(sh), sh.size), "sw_set_light_shadows")
+
+    def build_shadow_maps_view(self, sides, leafs, total_texels):
+        """Depth draws prepared on the GPU from the cube sides and their leafs (needs set_map)."""
+        s = np.ascontiguousarray(sides, abi.SHADOW_SIDE)
+        lf = np.ascontiguousarray(leafs, abi.SHADOW_LEAF)
+        self._check(self.lib.sw_build_shadow_maps_view(self.ctx, abi.ptr(s), s.size, abi.ptr(lf), lf.size, int(total_texels)),
+                    "sw_build_shadow_maps_view")
 
     def read_shadow_maps(self, texels):
         out = np.zeros(int(texels), np.float32)

@@ -48,7 +48,9 @@ class FrameOutputs(ctypes.Structure):
                 ("params", abi.FrameParams), ("visible_leafs", ctypes.c_uint32), ("camera_leaf", ctypes.c_uint32),
                 ("skybox_draws", ctypes.c_uint32), ("light_shadows", ctypes.c_void_p), ("depth_draws", ctypes.c_void_p),
                 ("num_depth_draws", ctypes.c_uint32), ("num_depth_vertices", ctypes.c_uint32),
-                ("depth_vertices", ctypes.c_void_p), ("shadow_texels", ctypes.c_uint64)]
+                ("depth_vertices", ctypes.c_void_p), ("shadow_texels", ctypes.c_uint64),
+                ("shadow_sides", ctypes.c_void_p), ("num_shadow_sides", ctypes.c_uint32),
+                ("num_shadow_leafs", ctypes.c_uint32), ("shadow_leafs", ctypes.c_void_p)]
 
 
 def load_host_library():
@@ -193,6 +195,9 @@ class Frame:
 
     def prepare(self, frame_index, options):
         _check(self.lib, self.lib.swh_frame_prepare(self.handle, frame_index, ctypes.byref(options)), "swh_frame_prepare")
+        return self._outputs()
+
+    def _outputs(self):
         o = FrameOutputs()
         _check(self.lib, self.lib.swh_frame_outputs(self.handle, ctypes.byref(o)), "swh_frame_outputs")
 
@@ -215,6 +220,8 @@ class Frame:
         self.depth_draws = arr(o.depth_draws, o.num_depth_draws, abi.DEPTH_DRAW)
         self.depth_vertices = arr(o.depth_vertices, o.num_depth_vertices, abi.VERTEX16)
         self.shadow_texels = int(o.shadow_texels)
+        self.shadow_sides = arr(o.shadow_sides, o.num_shadow_sides, abi.SHADOW_SIDE)
+        self.shadow_leafs = arr(o.shadow_leafs, o.num_shadow_leafs, abi.SHADOW_LEAF)
         return self
 
     def prepare_view(self, frame_index, options):
@@ -230,6 +237,7 @@ class Frame:
                 return np.zeros(0, dt)
             return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)),
                                          shape=(int(n) * np.dtype(dt).itemsize,)).view(dt).copy()
+        self._outputs()  # lights, shadow maps and their sides' leafs
         self.view_leafs = arr(vin.leafs, vin.num_leafs, abi.VIEW_LEAF)
         self.view_leaf_lights = arr(vin.leaf_lights, vin.num_leaf_lights, np.uint16)
         self.draws = arr(vin.draws, vin.num_draws, abi.DRAW_CMD)

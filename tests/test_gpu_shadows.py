@@ -97,3 +97,43 @@ def test_shadow_inputs_are_validated(gpu_ok):
         r.set_light_shadows(None)
     finally:
         r.close()
+
+
+@pytest.mark.parametrize("quality", [0.0, 1.0])
+def test_shadow_maps_prepared_on_the_gpu(gpu_ok, quality):
+    """sw_build_shadow_maps_view (each side's leafs from the host, their polygons' depth draws prepared on
+    the GPU) leaves the storage that the host-prepared depth draws leave, texel for texel, frame after
+    frame; the host halves agree on the maps."""
+    scene = host.Scene(**dict(host.FULL_MAP, shadowed_lights=4))
+    fr, fv = host.Frame(scene), host.Frame(scene)
+    hr = host.HostRenderer(scene)  # its context holds the map (sw_set_map)
+    glib = gpu.load_library()
+    opts = host.frame_options(1280, 720, abi.SW_PIXEL_C64, directional=True, shadows_quality=quality)
+    storage = np.zeros(0, np.float32)
+    try:
+        for fi in (0, 7, 70, 140, 141, 250):
+            fr.prepare(fi, opts)
+            fv.prepare_view(fi, opts)
+            assert fv.depth_draws.size == 0 and fv.shadow_sides.size == 6 * (fv.light_shadows["kind"] == abi.SW_SHADOW_CUBE).sum()
+            assert fv.light_shadows.tobytes() == fr.light_shadows.tobytes() and fv.shadow_texels == fr.shadow_texels
+            if storage.size < fr.shadow_texels:
+                storage = np.concatenate([storage, np.zeros(fr.shadow_texels - storage.size, np.float32)])
+            oracle.shadow_maps(fr.depth_draws, fr.depth_vertices, storage)
+            s, lf = fv.shadow_sides, fv.shadow_leafs
+            assert glib.sw_build_shadow_maps_view(hr.context(), abi.ptr(s), s.size, abi.ptr(lf), lf.size,
+                                                  fv.shadow_texels) == abi.SW_OK
+            got = np.zeros(storage.size, np.float32)
+            assert glib.sw_read_shadow_maps(hr.context(), abi.ptr(got), got.size) == abi.SW_OK
+            assert np.array_equal(got.view(np.uint32), storage.view(np.uint32)), \
+                f"frame {fi}: {(got != storage).sum()} of {storage.size} texels differ"
+        # invalid lists are rejected before anything runs
+        bad = lf.copy()
+        bad[0]["side"] = s.size
+        assert glib.sw_build_shadow_maps_view(hr.context(), abi.ptr(s), s.size, abi.ptr(bad), bad.size,
+                                              fv.shadow_texels) == abi.SW_ERR_INVALID_ARGUMENT
+        bad = s.copy()
+        bad[0]["map_offset"] = fv.shadow_texels
+        assert glib.sw_build_shadow_maps_view(hr.context(), abi.ptr(bad), bad.size, abi.ptr(lf), lf.size,
+                                              fv.shadow_texels) == abi.SW_ERR_INVALID_ARGUMENT
+    finally:
+        hr.close()
