@@ -1,6 +1,6 @@
 """Benchmark of the GB300 Square-Wheel world-rendering path.
 
-python bench.py [--gpus N] [--steps K] [--warmup W] [--workload frame|surfaces|upscale] [--impl gpu|reference]
+python bench.py [--gpus N] [--steps K] [--warmup W] [--workload frame|surfaces|upscale|shadows] [--impl gpu|reference]
                 [--learn-steps S]
 
 Prints one JSON line (rank 0). A step is one pass of the hot path over one batch of synthetic input.
@@ -664,6 +664,122 @@ def cpu_surfaces_baseline(work):
 
 
 # ---------------------------------------------------------------------------------------------------------
+# shadows workload: shadowed dynamic lights (cube shadow maps) on the 1080p frame of the 64-room map
+
+def run_shadows_gpu(args, world, rank, local):
+    """value: shadow-map builds per second of device time (sw_build_shadow_maps_view over the frame's cube
+    sides and their leafs, already on the host; L2 flushed before each); e2e: whole 1080p frames with the
+    first `--shadowed-lights` of the 8 dynamic lights shadowed, through swh_renderer_render_frame."""
+    import ctypes
+    import torch
+    from sqwheel import abi, gpu, host
+    torch.cuda.set_device(local)
+    scene = host.Scene(**dict(host.FULL_MAP, shadowed_lights=args.shadowed_lights))
+    opts = host.frame_options(W, H, abi.SW_PIXEL_C64, directional=True)
+    cfg = abi.PostConfig.default()
+    frames = [((k * 37 + 11 * rank) % 256) for k in range(max(args.steps, 4) + args.warmup)]
+    hr = host.HostRenderer(scene, device=local)  # its context holds the map
+    glib = gpu.load_library()
+    ctx = hr.context()
+    fr = host.Frame(scene)
+    lists = []
+    for fi in frames:
+        fr.prepare_view(fi, opts)
+        lists.append((fr.shadow_sides.copy(), fr.shadow_leafs.copy(), fr.shadow_texels))
+    stream = torch.cuda.ExternalStream(hr_stream(glib, ctx))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def build(k):
+        sd, lf, n = lists[k]
+        rc = glib.sw_build_shadow_maps_view(ctx, abi.ptr(sd), sd.size, abi.ptr(lf), lf.size, n)
+        assert rc == abi.SW_OK, rc
+
+    for k in range(args.warmup):
+        build(k)
+    ms_list = []
+    with ClockSampler(local) as clocks:
+        for k in range(args.warmup, args.warmup + args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                build(k)
+                e1.record(stream)
+            e1.synchronize()
+            ms_list.append(e0.elapsed_time(e1))
+    ms = max_over_ranks(statistics.mean(ms_list), world, f"cuda:{local}")
+    # algorithmic bytes of one build: every covered texel once (8-byte read-modify-write in L2) plus each
+    # candidate's polygon record and vertices
+    texels = statistics.mean(int(n) for _, _, n in lists[args.warmup:])
+    cands = statistics.mean(int(lf["num_polygons"].sum()) for _, lf, _ in lists[args.warmup:])
+    alg = texels * 16 + cands * (abi.MAP_POLYGON.itemsize + 6 * 12)
+    peak, peak_kind = peaks()
+    gbs = alg / (ms / 1e3) / 1e9
+
+    def e2e_run(shadowed):
+        r2 = host.HostRenderer(host.Scene(**dict(host.FULL_MAP, shadowed_lights=shadowed)), device=local)
+        out = np.zeros((H, W), np.uint32)
+        r2.register_host_buffer(out)
+        for fi in frames[:4]:
+            r2.render_frame(fi, opts, out=out, post=cfg)
+        times, up = [], 0
+        for fi in frames[args.warmup:]:
+            s0, s1 = abi.Stats(), abi.Stats()
+            glib.sw_get_stats(r2.context(), ctypes.byref(s0))
+            t0 = time.perf_counter()
+            r2.render_frame(fi, opts, out=out, post=cfg)
+            times.append(time.perf_counter() - t0)
+            glib.sw_get_stats(r2.context(), ctypes.byref(s1))
+            up += s1.upload_bytes - s0.upload_bytes
+        r2.unregister_host_buffer(out)
+        r2.close()
+        return 1.0 / statistics.median(times), up / len(times), out.nbytes
+
+    e2e_val, h2d, d2h = e2e_run(args.shadowed_lights)
+    e2e_plain, _, _ = e2e_run(0)
+    if rank == 0:
+        # CPU: the host's depth-draw preparation (the reference's DepthRenderer restated in C++) and the
+        # oracle's DepthRasterizer over those draws, one thread, a bounded sample of the frames
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        sample = frames[args.warmup:args.warmup + 4]
+        storage = np.zeros(0, np.float32)
+        t0 = time.perf_counter()
+        for fi in sample:
+            fr.prepare(fi, opts)
+            if storage.size < fr.shadow_texels:
+                storage = np.concatenate([storage, np.zeros(fr.shadow_texels - storage.size, np.float32)])
+            oracle.shadow_maps(fr.depth_draws, fr.depth_vertices, storage)
+        cpu_val = len(sample) / (time.perf_counter() - t0)
+        print(json.dumps({
+            "metric": METRIC, "value": round(world * 1e3 / ms, 1), "unit": "shadow-map builds/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 depth / fixed16 edges", "data": "synthetic (seeded)",
+            "config": {"workload": f"cube shadow maps of the 1920x1080 colour64 frame, 64-room map, "
+                                   f"{args.shadowed_lights} of 8 dynamic lights shadowed",
+                       "texels_per_step": int(texels), "candidate_polygons_per_step": int(cands),
+                       "l2": "flushed (512 MiB write) before every timed step", "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "kernel": "shadow_view_kernel", "achieved": round(gbs, 2), "peak": peak,
+                         "unit": "GB/s", "frac": round(gbs / peak, 5), "peak_source": f"{peak_kind} hbm_gbs",
+                         "algorithmic_bytes_per_launch": int(alg), "traffic": None,
+                         "note": "latency-bound: a few MB per launch"},
+            "cpu_baseline": {"value": round(cpu_val, 2), "unit": "shadow-map builds/s", "cores": 1, "kind": "port",
+                             "sample": f"{len(sample)} frames: host depth-draw preparation + oracle DepthRasterizer"},
+            "e2e": {"value": round(e2e_val, 1), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "without_shadows": round(e2e_plain, 1)},
+            "clocks": clocks.summary(), "gpu_launches": args.steps}), flush=True)
+    hr.close()
+
+
+def hr_stream(glib, ctx):
+    import ctypes
+    s = ctypes.c_void_p()
+    rc = glib.sw_get_stream(ctx, ctypes.byref(s))
+    assert rc == 0, rc
+    return s.value or 0
+
+
+# ---------------------------------------------------------------------------------------------------------
 # upscale workload (the learned upscaler alone)
 
 def bf16_peak():
@@ -805,7 +921,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="frame", choices=["frame", "surfaces", "upscale"])
+    ap.add_argument("--workload", default="frame", choices=["frame", "surfaces", "upscale", "shadows"])
+    ap.add_argument("--shadowed-lights", type=int, default=2, help="shadows workload: shadowed dynamic lights (of 8)")
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--autotune-reps", type=int, default=5,
                     help="frames per configuration of the autotuner before the frame measurement (0: keep the default)")
@@ -827,6 +944,8 @@ def main():
             run_surfaces_gpu(args, world, rank, local)
         elif args.workload == "upscale":
             run_upscale_gpu(args, world, rank, local)
+        elif args.workload == "shadows":
+            run_shadows_gpu(args, world, rank, local)
         else:
             run_frame_gpu(args, world, rank, local)
     finally:
