@@ -669,6 +669,7 @@ __global__ void __launch_bounds__(256) shadow_draw_kernel(ShadowArgs a)
 // a time: lane i takes the 32-row chunk's first line_inv_z and adds dy i times, which is the
 // reference's sequential row accumulation; the next chunk starts from lane 31's value plus dy.
 constexpr int SHADOW_VIEW_WARPS = 8;
+constexpr uint32_t SHADOW_VIEW_SMEM_LEAFS = 8192; // leaf starts staged in shared memory up to this many
 
 struct ShadowWarpShared
 {
@@ -680,54 +681,68 @@ struct ShadowWarpShared
 __global__ void __launch_bounds__(SHADOW_VIEW_WARPS * 32) shadow_view_kernel(ShadowViewArgs a)
 {
 	__shared__ ShadowWarpShared s_w[SHADOW_VIEW_WARPS];
-	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-	const uint32_t c = blockIdx.x * SHADOW_VIEW_WARPS + warp;
-	if (c >= a.num_candidates) return; // whole warps; every later condition is the warp's polygon's too
-	ShadowWarpShared& sw = s_w[warp];
-	const uint32_t li = find_segment(a.leaf_base, a.num_leafs, c);
-	const SwShadowLeaf& leaf = a.leafs[li];
-	const SwShadowSide& side = a.sides[leaf.side];
-	const SwMapPolygon& p = a.polygons[leaf.first_polygon + (c - a.leaf_base[li])];
-	float eq[3];
-	if (!swhost::depth_map_equation(p, load_mat4(side.planes_matrix), eq)) return;
-	const uint32_t nv = p.num_vertices < MAXV ? p.num_vertices : MAXV;
-	if (nv < 3) return;
-	const Mat4 view = load_mat4(side.view_matrix);
-	const Vec3* mv = reinterpret_cast<const Vec3*>(a.map_vertices);
-	const Vec3 vt = lane < nv ? swhost::view_transform(view, mv[p.first_vertex + lane]) : swhost::v3(0.0f, 0.0f, 1.0f);
-	Vec3 planes[8];
-	load_planes(leaf.clip_planes, planes);
-	Vec2 v2d = swhost::v2(0.0f, 0.0f);
-	const uint32_t count = warp_project_and_clip(planes, vt, nv, v2d, sw.clip);
-	if (count < 3) return;
-	if (lane < count) // f32_to_fixed16 (fixed_math.rs:31-34)
-		sw.v[lane] = SwVertex16{swhost::as_i32(v2d.x * 65536.0f), swhost::as_i32(v2d.y * 65536.0f)};
-	__syncwarp();
-	const int32_t size = int32_t(side.map_size);
-	uint32_t np = 0;
-	if (lane == 0)
+	extern __shared__ uint32_t s_leaf_base[]; // the leafs' first candidates (dynamic: num_leafs when staged)
+	// stage the leaf starts (one round of independent loads) so the search runs in shared memory
+	const bool staged = a.num_leafs <= SHADOW_VIEW_SMEM_LEAFS;
+	if (staged)
 	{
-		SwDrawCmd d{};
-		d.vertex_count = count;
-		d.mode = SW_RASTER_FULL_PERSPECTIVE; // no texture-coordinate edges
-		np = edge_walk(d, sw.v, size, sw.parts);
+		for (uint32_t i = threadIdx.x; i < a.num_leafs; i += blockDim.x) s_leaf_base[i] = a.leaf_base[i];
+		__syncthreads();
 	}
-	np = __shfl_sync(FULL_MASK, np, 0);
-	__syncwarp();
-	const float dx = eq[0], dy = eq[1], k = eq[2];
-	const unsigned long long seq = (unsigned long long)(a.seq_base + c + 1u) << 32;
-	unsigned long long* map = a.storage + side.map_offset;
-	for (uint32_t pi = 0; pi < np; ++pi)
+	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+	ShadowWarpShared& sw = s_w[warp];
+	const uint32_t* leaf_base = staged ? s_leaf_base : a.leaf_base;
+	// persistent: the grid is what fits on the GPU at once and each warp takes candidates in turn, so a
+	// rejected candidate (facing away, clipped away: most of them) frees its warp at once
+	for (uint32_t c = blockIdx.x * SHADOW_VIEW_WARPS + warp; c < a.num_candidates; c += gridDim.x * SHADOW_VIEW_WARPS)
 	{
-		const RasterPart pt = sw.parts[pi];
-		const uint32_t rows = uint32_t(pt.y_end_int - pt.y_start_int);
-		float chunk = depth_first_line(pt, dx, dy, k);
-		for (uint32_t r0 = 0; r0 < rows; r0 += 32)
+		__syncwarp(); // the previous candidate's reads of sw are done
+		// every condition below is the warp's polygon's: the lanes stay together
+		const uint32_t li = find_segment(leaf_base, a.num_leafs, c);
+		const SwShadowLeaf& leaf = a.leafs[li];
+		const SwShadowSide& side = a.sides[leaf.side];
+		const SwMapPolygon& p = a.polygons[leaf.first_polygon + (c - leaf_base[li])];
+		float eq[3];
+		if (!swhost::depth_map_equation(p, load_mat4(side.planes_matrix), eq)) continue;
+		const uint32_t nv = p.num_vertices < MAXV ? p.num_vertices : MAXV;
+		if (nv < 3) continue;
+		const Mat4 view = load_mat4(side.view_matrix);
+		const Vec3* mv = reinterpret_cast<const Vec3*>(a.map_vertices);
+		const Vec3 vt = lane < nv ? swhost::view_transform(view, mv[p.first_vertex + lane]) : swhost::v3(0.0f, 0.0f, 1.0f);
+		Vec3 planes[8];
+		load_planes(leaf.clip_planes, planes);
+		Vec2 v2d = swhost::v2(0.0f, 0.0f);
+		const uint32_t count = warp_project_and_clip(planes, vt, nv, v2d, sw.clip);
+		if (count < 3) continue;
+		if (lane < count) // f32_to_fixed16 (fixed_math.rs:31-34)
+			sw.v[lane] = SwVertex16{swhost::as_i32(v2d.x * 65536.0f), swhost::as_i32(v2d.y * 65536.0f)};
+		__syncwarp();
+		const int32_t size = int32_t(side.map_size);
+		uint32_t np = 0;
+		if (lane == 0)
 		{
-			float line = chunk;
-			for (uint32_t i = 0; i < lane; ++i) line = fadd(line, dy);
-			if (r0 + lane < rows) draw_depth_row(map, size, pt, r0 + lane, line, dx, seq);
-			chunk = fadd(__shfl_sync(FULL_MASK, line, 31), dy);
+			SwDrawCmd d{};
+			d.vertex_count = count;
+			d.mode = SW_RASTER_FULL_PERSPECTIVE; // no texture-coordinate edges
+			np = edge_walk(d, sw.v, size, sw.parts);
+		}
+		np = __shfl_sync(FULL_MASK, np, 0);
+		__syncwarp();
+		const float dx = eq[0], dy = eq[1], k = eq[2];
+		const unsigned long long seq = (unsigned long long)(a.seq_base + c + 1u) << 32;
+		unsigned long long* map = a.storage + side.map_offset;
+		for (uint32_t pi = 0; pi < np; ++pi)
+		{
+			const RasterPart pt = sw.parts[pi];
+			const uint32_t rows = uint32_t(pt.y_end_int - pt.y_start_int);
+			float chunk = depth_first_line(pt, dx, dy, k);
+			for (uint32_t r0 = 0; r0 < rows; r0 += 32)
+			{
+				float line = chunk;
+				for (uint32_t i = 0; i < lane; ++i) line = fadd(line, dy);
+				if (r0 + lane < rows) draw_depth_row(map, size, pt, r0 + lane, line, dx, seq);
+				chunk = fadd(__shfl_sync(FULL_MASK, line, 31), dy);
+			}
 		}
 	}
 }
@@ -741,7 +756,22 @@ int launch_shadow_maps(const ShadowArgs& args, cudaStream_t stream)
 int launch_shadow_view(const ShadowViewArgs& args, cudaStream_t stream)
 {
 	if (args.num_candidates == 0) return 0;
-	shadow_view_kernel<<<(args.num_candidates + SHADOW_VIEW_WARPS - 1) / SHADOW_VIEW_WARPS, SHADOW_VIEW_WARPS * 32, 0, stream>>>(args);
+	const size_t smem = args.num_leafs <= SHADOW_VIEW_SMEM_LEAFS ? size_t(args.num_leafs) * 4 : 0; // + 16 KB static < 48 KB
+	// resident CTAs of the largest staging (registers bound it first), once per process
+	static int resident = 0;
+	if (resident == 0)
+	{
+		int dev = 0, sms = 0, per_sm = 0;
+		cudaError_t e = cudaGetDevice(&dev);
+		if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+		if (e == cudaSuccess)
+			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shadow_view_kernel, SHADOW_VIEW_WARPS * 32,
+				size_t(SHADOW_VIEW_SMEM_LEAFS) * 4);
+		if (e != cudaSuccess) return int(e);
+		resident = std::max(sms * per_sm, 1);
+	}
+	const uint32_t blocks = std::min<uint32_t>((args.num_candidates + SHADOW_VIEW_WARPS - 1) / SHADOW_VIEW_WARPS, uint32_t(resident));
+	shadow_view_kernel<<<blocks, SHADOW_VIEW_WARPS * 32, smem, stream>>>(args);
 	return int(cudaGetLastError());
 }
 
