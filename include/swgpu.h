@@ -430,6 +430,11 @@ typedef struct SwViewFrameInput {
 	void* dst;
 	uint32_t dst_pitch;
 	int32_t dst_is_device;
+	/* scrolling textures (MapMaterialsProcessor::get_texture_shift, map_materials_processor.rs:229-247,
+	 * 330-334): per material (SwMapPolygon.texture) this frame's shift in texels of mip 0, s then t;
+	 * materials at or past num_texture_shifts (or a NULL array) do not scroll */
+	uint32_t num_texture_shifts;
+	const int32_t* texture_shifts;
 } SwViewFrameInput;
 
 /* One whole frame like sw_draw_frame, with the surfaces and the leafs' draws prepared on the GPU. */

@@ -39,6 +39,7 @@ typedef struct SwhSceneConfig {
 	float sky_rotation_speed;     /* skybox rotation about the vertical axis, radians per frame */
 	float camera_pitch;           /* added to the camera path's elevation (radians, up > 0) */
 	uint32_t shadowed_lights;     /* the first this many dynamic lights cast cube shadows */
+	uint32_t scrolling_materials; /* the first this many materials scroll (s and t speeds fixed per material) */
 } SwhSceneConfig;
 
 typedef struct SwhSceneInfo {

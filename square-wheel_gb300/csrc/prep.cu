@@ -287,7 +287,13 @@ __device__ void prep_pair(const PrepArgs& a, const PrepFrame& frame, uint32_t nu
 		// build_polygons_surfaces: descriptor, the leaf's lights that reach the polygon (in order, up to 6)
 		// and the surface build's record (its texel offset is the compaction's)
 		SwSurfaceDesc d;
-		swhost::make_surface_desc(p, sp, 0, a.directional != 0, a.simple_lightmaps != 0, d);
+		int32_t shift[2] = {0, 0}; // get_texture_shift of the polygon's material
+		if (p.texture < frame.num_texture_shifts)
+		{
+			shift[0] = a.texture_shifts[2 * p.texture];
+			shift[1] = a.texture_shifts[2 * p.texture + 1];
+		}
+		swhost::make_surface_desc(p, sp, 0, a.directional != 0, a.simple_lightmaps != 0, shift, d);
 		if (diffuse)
 			for (uint32_t base = 0; base < leaf_num_lights && d.num_lights < SW_MAX_POLYGON_LIGHTS; base += 32)
 			{

@@ -471,7 +471,7 @@ void FramePrep::build_surface_descs()
 		sp.tc_min[0] = pd.tc_min[0];
 		sp.tc_min[1] = pd.tc_min[1];
 		SwSurfaceDesc& d = surfaces[si];
-		make_surface_desc(p, sp, pd.offset, directional, simple_lightmaps, d);
+		make_surface_desc(p, sp, pd.offset, directional, simple_lightmaps, &texture_shifts[2 * p.texture], d);
 		if (p.flags & SW_POLY_DIFFUSE_LAYER)
 			for (uint32_t li : leaf_lights[sc.polygon_leaf[pi]])
 				if (polygon_is_affected_by_light(p, lights[li]))
@@ -656,6 +656,19 @@ void FramePrep::begin_frame(const CameraMatrices& camera, const std::vector<SwLi
 	stats.camera_leaf = vis.camera_leaf;
 	position_lights();
 	prepare_shadows();
+	// MapMaterialsProcessor::update_shifts (map_materials_processor.rs:229-247): scrolling materials'
+	// shift at the frame's time, `(speed * t) as i32` rem_euclid the mip-0 size
+	texture_shifts.assign(2 * (sc.materials.size() + 1), 0);
+	scrolling = false;
+	for (uint32_t m = 0; m < sc.materials.size(); ++m)
+		for (int i = 0; i < 2; ++i)
+			if (sc.materials[m].scroll_speed[i] != 0.0f)
+			{
+				const int32_t size = int32_t(sc.materials[m].texture_size);
+				const int32_t s = as_i32(sc.materials[m].scroll_speed[i] * frame_time_s) % size;
+				texture_shifts[2 * m + i] = s < 0 ? s + size : s;
+				scrolling = true;
+			}
 }
 
 void FramePrep::finish_params()
@@ -767,6 +780,7 @@ void FramePrep::camera_of_frame(uint32_t frame_index, const FrameOptions& option
 
 void FramePrep::prepare(uint32_t frame_index, const FrameOptions& options)
 {
+	frame_time_s = float(frame_index) * (1.0f / 60.0f);
 	CameraMatrices camera;
 	std::vector<SwLight> l;
 	Quat rotation;
@@ -776,6 +790,7 @@ void FramePrep::prepare(uint32_t frame_index, const FrameOptions& options)
 
 void FramePrep::prepare_view(uint32_t frame_index, const FrameOptions& options)
 {
+	frame_time_s = float(frame_index) * (1.0f / 60.0f);
 	CameraMatrices camera;
 	std::vector<SwLight> l;
 	Quat rotation;

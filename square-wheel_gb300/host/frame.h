@@ -131,6 +131,12 @@ public:
 	// and the leafs its visibility reaches, back to front (depth_draws / depth_vertices stay empty).
 	std::vector<SwShadowSide> shadow_sides;
 	std::vector<SwShadowLeaf> shadow_leafs;
+	// Scrolling textures: per material (s, t) shift in mip-0 texels at the frame's time; `scrolling` is
+	// false when no material scrolls (the view input then passes no table).
+	std::vector<int32_t> texture_shifts;
+	bool scrolling = false;
+	// Game time of the frame (prepare / prepare_view: frame index / 60 s; the *_with_camera forms keep it).
+	float frame_time_s = 0.0f;
 
 private:
 	struct PolyData

@@ -428,11 +428,13 @@ SWH_HD inline uint64_t max_surface_texels(const SwMapPolygon& p)
 
 // The descriptor half of build_polygons_surfaces for one surface (partial_renderer.rs:1682-1819), without
 // its light list. `directional`: directional lightmaps in use; `simple_lightmaps`: the map has simple ones.
+// `shift`: get_texture_shift of the polygon's material (texels of mip 0), applied >> mip
+// (partial_renderer.rs:1687-1693).
 SWH_HD inline void make_surface_desc(const SwMapPolygon& p, const SurfacePrep& sp, uint64_t out_offset, bool directional,
-	bool simple_lightmaps, SwSurfaceDesc& d)
+	bool simple_lightmaps, const int32_t shift[2], SwSurfaceDesc& d)
 {
 	d = SwSurfaceDesc{};
-	const int32_t shift_mip[2] = {0, 0}; // get_texture_shift >> mip: no scrolling materials in these maps
+	const int32_t shift_mip[2] = {shift[0] >> sp.mip, shift[1] >> sp.mip};
 	d.size[0] = sp.size[0];
 	d.size[1] = sp.size[1];
 	d.tc_start[0] = sp.tc_min[0] + shift_mip[0];

@@ -1022,6 +1022,12 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 		const bool diel = !metal && m < n_metal + n_diel;
 		make_material_texture(trng, cfg.texture_size, cfg.normal_maps, metal ? 0.35f : diel ? 0.5f : 1.0f, metal, sc);
 		Material mat;
+		mat.texture_size = cfg.texture_size;
+		if (m < cfg.scrolling_materials) // fixed speeds (no generator draws: the rest of the map is unchanged)
+		{
+			mat.scroll_speed[0] = 24.0f + 8.0f * float(m);
+			mat.scroll_speed[1] = (m & 1) ? -13.5f : 6.25f;
+		}
 		if (trng.uniform() < cfg.emissive_frac)
 		{
 			mat.emissive = int32_t(n_emissive_tex++);

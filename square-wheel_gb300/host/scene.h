@@ -66,6 +66,8 @@ struct Material
 	float emissive_light[3] = {1.0f, 1.0f, 1.0f};
 	bool skybox = false; // SpecialMaterialEffect::Skybox: polygons only mark where the sky shows
 	bool shadow = true;  // casts shadows (material.rs:50-53)
+	float scroll_speed[2] = {0.0f, 0.0f}; // Material::scroll_speed, texels of mip 0 per second
+	uint32_t texture_size = 0;            // mip-0 width = height
 };
 
 // One mip of a skybox side (SkyboxSideTexture, src/square_wheel/textures.rs:83-87): size x size texels
@@ -119,6 +121,7 @@ struct SceneConfig
 	float sky_rotation_speed = 0.01f; // skybox rotation about the vertical axis, radians per frame
 	float camera_pitch = 0.0f;        // added to the camera path's elevation (radians, up > 0)
 	uint32_t shadowed_lights = 0;     // the first this many dynamic lights cast cube shadows
+	uint32_t scrolling_materials = 0; // the first this many materials scroll (Material::scroll_speed)
 };
 
 struct Scene

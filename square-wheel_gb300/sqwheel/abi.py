@@ -134,7 +134,8 @@ class ViewFrameInput(ctypes.Structure):
                 ("leaf_lights", ctypes.c_void_p), ("num_draws", ctypes.c_uint32), ("draws", ctypes.c_void_p),
                 ("vertices", ctypes.c_void_p), ("num_vertices", ctypes.c_uint32), ("postprocess", ctypes.c_uint32),
                 ("post", PostConfig), ("frame_duration_s", ctypes.c_float), ("color_modulate", ctypes.c_float * 3),
-                ("dst", ctypes.c_void_p), ("dst_pitch", ctypes.c_uint32), ("dst_is_device", ctypes.c_int32)]
+                ("dst", ctypes.c_void_p), ("dst_pitch", ctypes.c_uint32), ("dst_is_device", ctypes.c_int32),
+                ("num_texture_shifts", ctypes.c_uint32), ("texture_shifts", ctypes.c_void_p)]
 
 
 class ViewCounts(ctypes.Structure):

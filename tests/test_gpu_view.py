@@ -60,6 +60,30 @@ def test_view_prep_sky_map(gpu_ok):
     prepared_equal(scene, [0, 5, 30, 61, 90], 800, 600, abi.SW_PIXEL_C64)
 
 
+def test_view_prep_scrolling_textures(gpu_ok):
+    """Scrolling materials (get_texture_shift >> mip in the descriptors' tc start and basis start), other
+    mips included; and the frames against the oracle's through the host-prepared descriptors."""
+    scene = host.Scene(**dict(host.SMALL_MAP, scrolling_materials=12, emissive_frac=0.3))
+    prepared_equal(scene, [0, 1, 45, 123, 1000, 99999], 640, 480, abi.SW_PIXEL_C64)
+    prepared_equal(scene, [7, 500], 640, 480, abi.SW_PIXEL_C32, directional=False, mip_bias=1.5)
+    st = scene.static_data()
+    fr = host.Frame(scene)
+    hr = host.HostRenderer(scene)
+    opts = host.frame_options(640, 480, abi.SW_PIXEL_C64, directional=True, clear_background=True)
+    try:
+        for fi in (90, 777):
+            fr.prepare(fi, opts)
+            arena = oracle.build_surfaces(st, fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=8)
+            want = np.zeros((480, 640), np.uint64)
+            oracle.clear_background(fr.params, want)
+            assert oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, want) == 0
+            got = np.zeros((480, 640), np.uint64)
+            hr.render_frame(fi, opts, out=got)
+            assert np.array_equal(want, got), f"frame {fi}: {(want != got).sum()} pixels differ"
+    finally:
+        hr.close()
+
+
 def test_view_prep_mip_bias_and_emissive(gpu_ok):
     """Other mips (bias 1.5) and the emissive layer's descriptors."""
     scene = host.Scene(**dict(host.SMALL_MAP, emissive_frac=0.5, num_dynamic_lights=4))
