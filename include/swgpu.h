@@ -408,6 +408,15 @@ typedef struct SwViewLeaf {
 } SwViewLeaf;
 #define SW_LEAF_NOT_DRAWN 0xFFFFFFFFu
 
+/* One material's state this frame (MapMaterialsProcessor, map_materials_processor.rs:174-247, 305-334):
+ * the texture its polygons show (framed animation: textures_mapping_table's current frame) and that
+ * frame's scrolling shift in texels of mip 0 (get_texture_shift). */
+typedef struct SwMaterialFrame {
+	int32_t shift[2];
+	uint32_t texture; /* texture_mip = texture * 5 + mip */
+	uint32_t reserved;
+} SwMaterialFrame;
+
 typedef struct SwViewFrameInput {
 	SwFrameParams params;
 	uint32_t num_lights;
@@ -430,11 +439,10 @@ typedef struct SwViewFrameInput {
 	void* dst;
 	uint32_t dst_pitch;
 	int32_t dst_is_device;
-	/* scrolling textures (MapMaterialsProcessor::get_texture_shift, map_materials_processor.rs:229-247,
-	 * 330-334): per material (SwMapPolygon.texture) this frame's shift in texels of mip 0, s then t;
-	 * materials at or past num_texture_shifts (or a NULL array) do not scroll */
-	uint32_t num_texture_shifts;
-	const int32_t* texture_shifts;
+	/* animated materials, one SwMaterialFrame per material (SwMapPolygon.texture); materials at or past
+	 * num_material_frames (or a NULL array) show their own texture unshifted */
+	uint32_t num_material_frames;
+	const struct SwMaterialFrame* material_frames;
 } SwViewFrameInput;
 
 /* One whole frame like sw_draw_frame, with the surfaces and the leafs' draws prepared on the GPU. */
@@ -532,8 +540,8 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 /* sizeof() of the ABI structs in this order: SwCreateInfo, SwTextureMip, SwEmissiveMip,
  * SwDirectionalLightmapElement, SwLight, SwSurfaceDesc, SwVertex16, SwDrawCmd, SwFrameParams,
  * SwPostConfig, SwStats, SwFrameInput, SwTuning, SwMapPolygon, SwViewLeaf, SwViewFrameInput,
- * SwViewCounts, SwLightShadow, SwDepthDraw, SwShadowSide, SwShadowLeaf. Writes min(count, 21) values;
- * returns the number of structs (21). Needs no GPU: bindings use it to check their mirrored layouts. */
+ * SwViewCounts, SwLightShadow, SwDepthDraw, SwShadowSide, SwShadowLeaf, SwMaterialFrame. Writes
+ * min(count, 22) values; returns the number of structs (22). Needs no GPU: bindings use it to check their mirrored layouts. */
 int sw_abi_layout(uint32_t* sizes, uint32_t count);
 
 /* Diagnostics: copy the frame's surface arena (total_texels of sw_submit_surfaces) to host memory. */

@@ -40,6 +40,7 @@ typedef struct SwhSceneConfig {
 	float camera_pitch;           /* added to the camera path's elevation (radians, up > 0) */
 	uint32_t shadowed_lights;     /* the first this many dynamic lights cast cube shadows */
 	uint32_t scrolling_materials; /* the first this many materials scroll (s and t speeds fixed per material) */
+	uint32_t animated_materials;  /* the first this many materials cycle through 3 texture frames */
 } SwhSceneConfig;
 
 typedef struct SwhSceneInfo {

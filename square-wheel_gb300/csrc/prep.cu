@@ -180,11 +180,14 @@ __device__ void prep_pair(const PrepArgs& a, const PrepFrame& frame, uint32_t nu
 		const uint32_t my_light = lane < leaf_num_lights ? uint32_t(a.leaf_lights[leaf_first_light + lane]) : 0u;
 		const SwLight light0 = a.lights[lane < leaf_num_lights ? my_light : 0u];
 		const bool diffuse = (flags & SW_POLY_DIFFUSE_LAYER) != 0, emissive = p.emissive_texture != SW_NO_EMISSIVE;
+		// the material's state this frame: its current animation frame's texture and scrolling shift
+		const bool animated = p.texture < frame.num_material_frames;
+		const uint32_t texture = animated ? a.material_frames[p.texture].texture : p.texture;
 		SwTextureMip tex_mip{};
 		SwEmissiveMip em_mip{};
 		if (lane < swhost::PREP_NUM_MIPS)
 		{
-			if (diffuse) tex_mip = a.texture_mips[p.texture * swhost::PREP_NUM_MIPS + lane];
+			if (diffuse) tex_mip = a.texture_mips[texture * swhost::PREP_NUM_MIPS + lane];
 			if (emissive) em_mip = a.emissive_mips[p.emissive_texture * swhost::PREP_NUM_MIPS + lane];
 		}
 		Vec3 planes[8];
@@ -288,12 +291,12 @@ __device__ void prep_pair(const PrepArgs& a, const PrepFrame& frame, uint32_t nu
 		// and the surface build's record (its texel offset is the compaction's)
 		SwSurfaceDesc d;
 		int32_t shift[2] = {0, 0}; // get_texture_shift of the polygon's material
-		if (p.texture < frame.num_texture_shifts)
+		if (animated)
 		{
-			shift[0] = a.texture_shifts[2 * p.texture];
-			shift[1] = a.texture_shifts[2 * p.texture + 1];
+			shift[0] = a.material_frames[p.texture].shift[0];
+			shift[1] = a.material_frames[p.texture].shift[1];
 		}
-		swhost::make_surface_desc(p, sp, 0, a.directional != 0, a.simple_lightmaps != 0, shift, d);
+		swhost::make_surface_desc(p, sp, 0, a.directional != 0, a.simple_lightmaps != 0, shift, texture, d);
 		if (diffuse)
 			for (uint32_t base = 0; base < leaf_num_lights && d.num_lights < SW_MAX_POLYGON_LIGHTS; base += 32)
 			{

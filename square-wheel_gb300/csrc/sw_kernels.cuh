@@ -317,13 +317,13 @@ struct PrepFrame
 	uint32_t num_draw_leafs;
 	uint32_t num_host_draws, num_host_vertices;
 	uint64_t num_host_rows;
-	uint32_t num_texture_shifts; // materials with an entry in PrepArgs::texture_shifts
+	uint32_t num_material_frames; // materials with an entry in PrepArgs::material_frames
 };
 
 struct PrepArgs
 {
 	const PrepFrame* frame;
-	const int32_t* texture_shifts; // 2 per material (s, t), frame->num_texture_shifts of them
+	const SwMaterialFrame* material_frames; // frame->num_material_frames of them
 	const SwMapPolygon* polygons;
 	const float* map_vertices; // xyz
 	const SwViewLeaf* leafs;

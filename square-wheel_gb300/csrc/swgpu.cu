@@ -161,7 +161,7 @@ struct SwCtx
 	cudaGraphExec_t vexec[2] = {nullptr, nullptr}; // one per staging block, replayed while its key holds
 	ViewGraphKey vkey[2];
 	uint64_t vcap_lights = 0, vcap_leafs = 0, vcap_leaf_lights = 0, vcap_host_draws = 0, vcap_host_vertices = 0;
-	uint64_t vcap_shifts = 0; // materials' texture shifts in the view upload block
+	uint64_t vcap_shifts = 0; // material frames in the view upload block
 	unsigned view_surface_blocks = 0;
 	uint64_t view_captures = 0;
 	std::vector<uint32_t> v_draw_leaf;
@@ -1518,7 +1518,7 @@ ViewBlock view_block(const SwCtx* ctx)
 	v.vertices = align_up(v.draws + ctx->vcap_host_draws * sizeof(SwDrawCmd), 256);
 	v.rows = align_up(v.vertices + ctx->vcap_host_vertices * sizeof(SwVertex16), 256);
 	v.shifts = align_up(v.rows + ctx->vcap_host_draws * sizeof(DrawRows), 256);
-	v.bytes = align_up(v.shifts + ctx->vcap_shifts * 8, 256);
+	v.bytes = align_up(v.shifts + ctx->vcap_shifts * sizeof(SwMaterialFrame), 256);
 	return v;
 }
 
@@ -1565,9 +1565,12 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	if (!ctx || !in) return SW_ERR_INVALID_ARGUMENT;
 	const SwViewFrameInput& f = *in;
 	if ((f.num_lights && !f.lights) || (f.num_leafs && !f.leafs) || (f.num_leaf_lights && !f.leaf_lights) ||
-		(f.num_draws && (!f.draws || !f.vertices)) || (f.num_texture_shifts && !f.texture_shifts))
+		(f.num_draws && (!f.draws || !f.vertices)) || (f.num_material_frames && !f.material_frames))
 		return SW_ERR_INVALID_ARGUMENT;
-	if (f.num_texture_shifts > (1u << 20)) return fail(ctx, SW_ERR_LIMIT, "too many texture shifts");
+	if (f.num_material_frames > (1u << 20)) return fail(ctx, SW_ERR_LIMIT, "too many material frames");
+	for (uint32_t i = 0; i < f.num_material_frames; ++i)
+		if (uint64_t(f.material_frames[i].texture) * 5 + 4 >= ctx->h_texture_mips.size())
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "material %u: frame texture %u has no mips", i, f.material_frames[i].texture);
 	if (f.postprocess && f.params.pixel_format != SW_PIXEL_C64)
 		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocessing needs a colour64 frame");
 	if (f.dst && f.dst_pitch < f.params.width) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");
@@ -1635,7 +1638,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	ctx->vcap_leaf_lights = pow2_at_least(f.num_leaf_lights, std::max<uint64_t>(ctx->vcap_leaf_lights, 256));
 	ctx->vcap_host_draws = pow2_at_least(f.num_draws, std::max<uint64_t>(ctx->vcap_host_draws, 8));
 	ctx->vcap_host_vertices = pow2_at_least(f.num_vertices, std::max<uint64_t>(ctx->vcap_host_vertices, 64));
-	ctx->vcap_shifts = pow2_at_least(f.num_texture_shifts, std::max<uint64_t>(ctx->vcap_shifts, 16));
+	ctx->vcap_shifts = pow2_at_least(f.num_material_frames, std::max<uint64_t>(ctx->vcap_shifts, 16));
 	const ViewBlock vb = view_block(ctx);
 	const uint32_t bpp = bpp_of(p.pixel_format);
 	ctx->vs_cands = pow2_at_least(candidates, std::max<uint64_t>(ctx->vs_cands, 1024));
@@ -1690,7 +1693,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	pf.num_host_draws = f.num_draws;
 	pf.num_host_vertices = f.num_vertices;
 	pf.num_host_rows = host_rows;
-	pf.num_texture_shifts = f.num_texture_shifts;
+	pf.num_material_frames = f.num_material_frames;
 	float* cam = reinterpret_cast<float*>(h + vb.cam);
 	cam[0] = p.cam_pos[0], cam[1] = p.cam_pos[1], cam[2] = p.cam_pos[2], cam[3] = 0.0f;
 	float* isc = reinterpret_cast<float*>(h + vb.inv_scale);
@@ -1719,7 +1722,8 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 		std::memcpy(h + vb.rows, host_draw_rows.data(), f.num_draws * sizeof(DrawRows));
 	}
 	if (f.num_vertices) std::memcpy(h + vb.vertices, f.vertices, f.num_vertices * sizeof(SwVertex16));
-	if (f.num_texture_shifts) std::memcpy(h + vb.shifts, f.texture_shifts, size_t(f.num_texture_shifts) * 8);
+	if (f.num_material_frames)
+		std::memcpy(h + vb.shifts, f.material_frames, size_t(f.num_material_frames) * sizeof(SwMaterialFrame));
 
 	// 4. kernel arguments: buffers and capacities only (the per-frame values are in the block)
 	unsigned char* d = slab + vs.frame_in;
@@ -1728,7 +1732,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	std::memset(&key, 0, sizeof(key)); // padding too: keys are compared bytewise
 	PrepArgs& pr = key.prep;
 	pr.frame = reinterpret_cast<const PrepFrame*>(d + vb.frame);
-	pr.texture_shifts = reinterpret_cast<const int32_t*>(d + vb.shifts);
+	pr.material_frames = reinterpret_cast<const SwMaterialFrame*>(d + vb.shifts);
 	pr.polygons = static_cast<const SwMapPolygon*>(ctx->map_polygons.ptr);
 	pr.map_vertices = static_cast<const float*>(ctx->map_vertices.ptr);
 	pr.leafs = reinterpret_cast<const SwViewLeaf*>(d + vb.leafs);
@@ -2166,15 +2170,15 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 
 int sw_abi_layout(uint32_t* sizes, uint32_t count)
 {
-	const uint32_t s[21] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
+	const uint32_t s[22] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
 		uint32_t(sizeof(SwDirectionalLightmapElement)), uint32_t(sizeof(SwLight)), uint32_t(sizeof(SwSurfaceDesc)),
 		uint32_t(sizeof(SwVertex16)), uint32_t(sizeof(SwDrawCmd)), uint32_t(sizeof(SwFrameParams)),
 		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats)), uint32_t(sizeof(SwFrameInput)), uint32_t(sizeof(SwTuning)),
 		uint32_t(sizeof(SwMapPolygon)), uint32_t(sizeof(SwViewLeaf)), uint32_t(sizeof(SwViewFrameInput)),
 		uint32_t(sizeof(SwViewCounts)), uint32_t(sizeof(SwLightShadow)), uint32_t(sizeof(SwDepthDraw)),
-		uint32_t(sizeof(SwShadowSide)), uint32_t(sizeof(SwShadowLeaf))};
-	for (uint32_t i = 0; sizes && i < count && i < 21; ++i) sizes[i] = s[i];
-	return 21;
+		uint32_t(sizeof(SwShadowSide)), uint32_t(sizeof(SwShadowLeaf)), uint32_t(sizeof(SwMaterialFrame))};
+	for (uint32_t i = 0; sizes && i < count && i < 22; ++i) sizes[i] = s[i];
+	return 22;
 }
 
 int sw_get_stats(SwCtx* ctx, SwStats* out)

@@ -471,7 +471,8 @@ void FramePrep::build_surface_descs()
 		sp.tc_min[0] = pd.tc_min[0];
 		sp.tc_min[1] = pd.tc_min[1];
 		SwSurfaceDesc& d = surfaces[si];
-		make_surface_desc(p, sp, pd.offset, directional, simple_lightmaps, &texture_shifts[2 * p.texture], d);
+		const SwMaterialFrame& mf = material_frames[p.texture];
+		make_surface_desc(p, sp, pd.offset, directional, simple_lightmaps, mf.shift, mf.texture, d);
 		if (p.flags & SW_POLY_DIFFUSE_LAYER)
 			for (uint32_t li : leaf_lights[sc.polygon_leaf[pi]])
 				if (polygon_is_affected_by_light(p, lights[li]))
@@ -656,19 +657,55 @@ void FramePrep::begin_frame(const CameraMatrices& camera, const std::vector<SwLi
 	stats.camera_leaf = vis.camera_leaf;
 	position_lights();
 	prepare_shadows();
-	// MapMaterialsProcessor::update_shifts (map_materials_processor.rs:229-247): scrolling materials'
-	// shift at the frame's time, `(speed * t) as i32` rem_euclid the mip-0 size
-	texture_shifts.assign(2 * (sc.materials.size() + 1), 0);
-	scrolling = false;
-	for (uint32_t m = 0; m < sc.materials.size(); ++m)
+	update_materials();
+}
+
+void FramePrep::update_materials()
+{
+	// MapMaterialsProcessor::update (map_materials_processor.rs:174-247) at the frame's time, once per
+	// frame. Framed animations (:184-227): a mapping entry whose current frame has a next frame moves to
+	// it once the time reaches its change point, which then advances by the new frame's duration (0.5 s
+	// without one) and is not left behind the current time. Scrolling (:229-247): `(speed * t) as i32`
+	// rem_euclid the mip-0 size. get_texture / get_texture_shift (:311-334) read both through the mapping.
+	const uint32_t n = uint32_t(sc.materials.size());
+	if (mapping.size() != n)
+	{
+		mapping.resize(n);
+		change_time.assign(n, 0.0f);
+		for (uint32_t m = 0; m < n; ++m) mapping[m] = m;
+	}
+	std::vector<int32_t> shift(2 * size_t(n), 0);
+	animated = false;
+	for (uint32_t m = 0; m < n; ++m)
+	{
+		const Material& mat = sc.materials[m];
+		if (mat.next_frame >= 0) animated = true;
 		for (int i = 0; i < 2; ++i)
-			if (sc.materials[m].scroll_speed[i] != 0.0f)
+			if (mat.scroll_speed[i] != 0.0f)
 			{
-				const int32_t size = int32_t(sc.materials[m].texture_size);
-				const int32_t s = as_i32(sc.materials[m].scroll_speed[i] * frame_time_s) % size;
-				texture_shifts[2 * m + i] = s < 0 ? s + size : s;
-				scrolling = true;
+				const int32_t size = int32_t(mat.texture_size);
+				const int32_t s = as_i32(mat.scroll_speed[i] * frame_time_s) % size;
+				shift[2 * m + i] = s < 0 ? s + size : s;
+				animated = true;
 			}
+	}
+	for (uint32_t m = 0; m < n; ++m)
+	{
+		const int32_t next = sc.materials[mapping[m]].next_frame;
+		if (next < 0 || uint32_t(next) >= n || !(frame_time_s >= change_time[m])) continue;
+		mapping[m] = uint32_t(next);
+		const Material& cur = sc.materials[uint32_t(next)];
+		change_time[m] += cur.next_frame >= 0 ? cur.frame_duration : 0.5f;
+		if (change_time[m] < frame_time_s) change_time[m] = frame_time_s;
+	}
+	material_frames.resize(n);
+	for (uint32_t m = 0; m < n; ++m)
+	{
+		material_frames[m].shift[0] = shift[2 * mapping[m]];
+		material_frames[m].shift[1] = shift[2 * mapping[m] + 1];
+		material_frames[m].texture = mapping[m];
+		material_frames[m].reserved = 0;
+	}
 }
 
 void FramePrep::finish_params()

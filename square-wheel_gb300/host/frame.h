@@ -131,10 +131,10 @@ public:
 	// and the leafs its visibility reaches, back to front (depth_draws / depth_vertices stay empty).
 	std::vector<SwShadowSide> shadow_sides;
 	std::vector<SwShadowLeaf> shadow_leafs;
-	// Scrolling textures: per material (s, t) shift in mip-0 texels at the frame's time; `scrolling` is
-	// false when no material scrolls (the view input then passes no table).
-	std::vector<int32_t> texture_shifts;
-	bool scrolling = false;
+	// Animated materials: per material its current frame's texture and scrolling shift; `animated` is
+	// false when no material scrolls or has frames (the view input then passes no table).
+	std::vector<SwMaterialFrame> material_frames;
+	bool animated = false;
 	// Game time of the frame (prepare / prepare_view: frame index / 60 s; the *_with_camera forms keep it).
 	float frame_time_s = 0.0f;
 
@@ -180,6 +180,9 @@ private:
 	void draw_depth_map(const CameraMatrices& camera, uint32_t size, uint64_t map_offset);
 	void draw_depth_polygon(const CameraMatrices& camera, const Vec3 clip_planes[8], uint32_t polygon_index, uint32_t size,
 		uint64_t map_offset);
+	void update_materials();
+	std::vector<uint32_t> mapping; // textures_mapping_table: current frame of each material (persists)
+	std::vector<float> change_time; // its frame_change_time_point
 	void begin_frame(const CameraMatrices& cam, const std::vector<SwLight>& lights, const FrameOptions& opt, Quat skybox_rotation);
 	void finish_params();
 	void camera_of_frame(uint32_t frame_index, const FrameOptions& opt, CameraMatrices& cam, std::vector<SwLight>& lights,

@@ -429,9 +429,9 @@ SWH_HD inline uint64_t max_surface_texels(const SwMapPolygon& p)
 // The descriptor half of build_polygons_surfaces for one surface (partial_renderer.rs:1682-1819), without
 // its light list. `directional`: directional lightmaps in use; `simple_lightmaps`: the map has simple ones.
 // `shift`: get_texture_shift of the polygon's material (texels of mip 0), applied >> mip
-// (partial_renderer.rs:1687-1693).
+// (partial_renderer.rs:1687-1693); `texture`: the material's current animation frame (get_texture).
 SWH_HD inline void make_surface_desc(const SwMapPolygon& p, const SurfacePrep& sp, uint64_t out_offset, bool directional,
-	bool simple_lightmaps, const int32_t shift[2], SwSurfaceDesc& d)
+	bool simple_lightmaps, const int32_t shift[2], uint32_t texture, SwSurfaceDesc& d)
 {
 	d = SwSurfaceDesc{};
 	const int32_t shift_mip[2] = {shift[0] >> sp.mip, shift[1] >> sp.mip};
@@ -458,7 +458,7 @@ SWH_HD inline void make_surface_desc(const SwMapPolygon& p, const SurfacePrep& s
 		d.basis_v[0] = bv.x, d.basis_v[1] = bv.y, d.basis_v[2] = bv.z;
 		d.basis_start[0] = start.x, d.basis_start[1] = start.y, d.basis_start[2] = start.z;
 		d.basis_normal[0] = bn.x, d.basis_normal[1] = bn.y, d.basis_normal[2] = bn.z;
-		d.texture_mip = p.texture * PREP_NUM_MIPS + sp.mip;
+		d.texture_mip = texture * PREP_NUM_MIPS + sp.mip;
 		for (int i = 0; i < 2; ++i)
 		{
 			const int32_t round_mask = ~int32_t((1u << PREP_LIGHTMAP_SCALE_LOG2) - 1);

@@ -1058,6 +1058,31 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 		}
 	}
 
+	// Framed animations (framed_animation, material.rs:136-143): material m < animated_materials cycles
+	// m -> a -> b -> m, the two extra frames appended after every other material (their own generator, so
+	// the rest of the map is unchanged) as copies of m with their own textures.
+	if (cfg.animated_materials)
+	{
+		Rng arng(cfg.seed ^ 0xF4A3Eu);
+		const float durations[3] = {0.25f, 0.4f, 0.3f};
+		for (uint32_t m = 0; m < std::min(cfg.animated_materials, cfg.num_materials); ++m)
+		{
+			const bool metal = m < n_metal;
+			const bool diel = !metal && m < n_metal + n_diel;
+			const int32_t first = int32_t(sc.materials.size());
+			for (int k = 0; k < 2; ++k)
+			{
+				make_material_texture(arng, cfg.texture_size, cfg.normal_maps, metal ? 0.35f : diel ? 0.5f : 1.0f, metal, sc);
+				Material f = sc.materials[m];
+				f.next_frame = k == 0 ? first + 1 : int32_t(m);
+				f.frame_duration = durations[k + 1];
+				sc.materials.push_back(f);
+			}
+			sc.materials[m].next_frame = first;
+			sc.materials[m].frame_duration = durations[0];
+		}
+	}
+
 	sc.basis.resize(sc.polygons.size());
 	for (size_t p = 0; p < sc.polygons.size(); ++p)
 		sc.basis[p] = form_plane_and_tex_coord_equation(sc.polygons[p].plane, sc.polygons[p].tex_coord_equation);

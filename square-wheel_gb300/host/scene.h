@@ -68,6 +68,8 @@ struct Material
 	bool shadow = true;  // casts shadows (material.rs:50-53)
 	float scroll_speed[2] = {0.0f, 0.0f}; // Material::scroll_speed, texels of mip 0 per second
 	uint32_t texture_size = 0;            // mip-0 width = height
+	int32_t next_frame = -1;              // framed_animation.next_material_name as a material index, -1: none
+	float frame_duration = 0.5f;          // framed_animation.duration, seconds
 };
 
 // One mip of a skybox side (SkyboxSideTexture, src/square_wheel/textures.rs:83-87): size x size texels
@@ -122,6 +124,7 @@ struct SceneConfig
 	float camera_pitch = 0.0f;        // added to the camera path's elevation (radians, up > 0)
 	uint32_t shadowed_lights = 0;     // the first this many dynamic lights cast cube shadows
 	uint32_t scrolling_materials = 0; // the first this many materials scroll (Material::scroll_speed)
+	uint32_t animated_materials = 0;  // the first this many materials cycle through 3 frames (framed_animation)
 };
 
 struct Scene

@@ -114,6 +114,7 @@ int swh_scene_create(const SwhSceneConfig* c, SwhScene** out)
 	cfg.camera_pitch = c->camera_pitch;
 	cfg.shadowed_lights = c->shadowed_lights;
 	cfg.scrolling_materials = c->scrolling_materials;
+	cfg.animated_materials = c->animated_materials;
 	SwhScene* s = new (std::nothrow) SwhScene();
 	if (!s) return SW_ERR_OUT_OF_MEMORY;
 	try
@@ -256,8 +257,8 @@ int swh_frame_view_input(const SwhFrame* f, SwViewFrameInput* out)
 	out->draws = p.draws.data();
 	out->vertices = p.vertices.data();
 	out->num_vertices = uint32_t(p.vertices.size());
-	out->num_texture_shifts = p.scrolling ? uint32_t(p.texture_shifts.size() / 2) : 0u;
-	out->texture_shifts = p.scrolling ? p.texture_shifts.data() : nullptr;
+	out->num_material_frames = p.animated ? uint32_t(p.material_frames.size()) : 0u;
+	out->material_frames = p.animated ? p.material_frames.data() : nullptr;
 	return SW_OK;
 }
 

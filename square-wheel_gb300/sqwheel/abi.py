@@ -63,6 +63,7 @@ MAP_POLYGON = np.dtype([
 LIGHT_SHADOW = np.dtype([("kind", "<u4"), ("size", "<u4"), ("offset", "<u8")], align=True)
 DEPTH_DRAW = np.dtype([("first_vertex", "<u4"), ("vertex_count", "<u4"), ("map_size", "<u4"), ("reserved", "<u4"),
                        ("map_offset", "<u8"), ("depth_eq", "<f4", 3), ("reserved2", "<u4")], align=True)
+MATERIAL_FRAME = np.dtype([("shift", "<i4", 2), ("texture", "<u4"), ("reserved", "<u4")], align=True)
 SHADOW_SIDE = np.dtype([("view_matrix", "<f4", 16), ("planes_matrix", "<f4", 16), ("map_size", "<u4"),
                         ("reserved", "<u4"), ("map_offset", "<u8")], align=True)
 SHADOW_LEAF = np.dtype([("side", "<u4"), ("first_polygon", "<u4"), ("num_polygons", "<u4"), ("reserved", "<u4"),
@@ -135,7 +136,7 @@ class ViewFrameInput(ctypes.Structure):
                 ("vertices", ctypes.c_void_p), ("num_vertices", ctypes.c_uint32), ("postprocess", ctypes.c_uint32),
                 ("post", PostConfig), ("frame_duration_s", ctypes.c_float), ("color_modulate", ctypes.c_float * 3),
                 ("dst", ctypes.c_void_p), ("dst_pitch", ctypes.c_uint32), ("dst_is_device", ctypes.c_int32),
-                ("num_texture_shifts", ctypes.c_uint32), ("texture_shifts", ctypes.c_void_p)]
+                ("num_material_frames", ctypes.c_uint32), ("material_frames", ctypes.c_void_p)]
 
 
 class ViewCounts(ctypes.Structure):
@@ -162,6 +163,7 @@ LAYOUT_ORDER = [
     ("SwViewFrameInput", ctypes.sizeof(ViewFrameInput)), ("SwViewCounts", ctypes.sizeof(ViewCounts)),
     ("SwLightShadow", LIGHT_SHADOW.itemsize), ("SwDepthDraw", DEPTH_DRAW.itemsize),
     ("SwShadowSide", SHADOW_SIDE.itemsize), ("SwShadowLeaf", SHADOW_LEAF.itemsize),
+    ("SwMaterialFrame", MATERIAL_FRAME.itemsize),
 ]
 
 

@@ -84,6 +84,13 @@ def test_view_prep_scrolling_textures(gpu_ok):
         hr.close()
 
 
+def test_view_prep_framed_animations(gpu_ok):
+    """Materials cycling through texture frames (the mapping table advances once per frame; every
+    renderer and frame here sees the same sequence), with scrolling on some of them."""
+    scene = host.Scene(**dict(host.FULL_MAP, animated_materials=10, scrolling_materials=4))
+    prepared_equal(scene, [0, 1, 15, 16, 30, 31, 45, 60, 200, 201], 1280, 720, abi.SW_PIXEL_C64)
+
+
 def test_view_prep_mip_bias_and_emissive(gpu_ok):
     """Other mips (bias 1.5) and the emissive layer's descriptors."""
     scene = host.Scene(**dict(host.SMALL_MAP, emissive_frac=0.5, num_dynamic_lights=4))

@@ -48,3 +48,63 @@ def test_scrolling_moves_only_the_texture_start(built_libs, frame_index):
         assert moved == 0
     elif frame_index >= 59:  # at least ~23 texels of mip 0 by then: visible at every mip in use
         assert moved > 0
+
+
+def restated_mapping(num_materials, animated, times):
+    """textures_mapping_table after each update (map_materials_processor.rs:184-227) for the generator's
+    framed animations: material m < animated cycles m -> a -> b -> m with a, b appended after the
+    num_materials materials (durations 0.25, 0.4, 0.3 s), in float32."""
+    base = num_materials
+    total = base + 2 * animated
+
+    def next_of(x):
+        if x < animated:
+            return base + 2 * x
+        if x >= base:
+            m, j = divmod(x - base, 2)
+            return base + 2 * m + 1 if j == 0 else m
+        return None
+
+    def duration(x):
+        return np.float32(0.25 if x < animated else (0.4 if (x - base) % 2 == 0 else 0.3))
+
+    mapping = list(range(total))
+    change = [np.float32(0.0)] * total
+    out = []
+    for t in times:
+        for m in range(total):
+            n = next_of(mapping[m])
+            if n is not None and t >= change[m]:
+                mapping[m] = n
+                change[m] = np.float32(change[m] + duration(n))
+                if change[m] < t:
+                    change[m] = t
+        out.append(list(mapping))
+    return out
+
+
+def test_framed_animations_follow_the_mapping_table(built_libs):
+    animated = 5
+    cfg = dict(host.SMALL_MAP, num_dynamic_lights=1)
+    plain = host.Frame(host.Scene(**cfg))
+    anim = host.Frame(host.Scene(**dict(cfg, animated_materials=animated)))
+    opts = host.frame_options(640, 480, abi.SW_PIXEL_C64, directional=False)
+    frames = [0, 1, 2, 15, 16, 30, 31, 45, 100, 101, 5000, 5001, 5002]
+    times = [np.float32(np.float32(f) * np.float32(1.0 / 60.0)) for f in frames]
+    want = restated_mapping(host.SMALL_MAP["num_materials"], animated, times)
+    seen = set()
+    for fi, mapping in zip(frames, want):
+        a = plain.prepare(fi, opts)
+        b = anim.prepare(fi, opts)
+        assert a.surfaces.size == b.surfaces.size
+        for sa, sb in zip(a.surfaces, b.surfaces):
+            if not sa["flags"] & abi.SW_SURF_DIFFUSE_LAYER:
+                continue
+            material, mip = divmod(int(sa["texture_mip"]), 5)
+            assert int(sb["texture_mip"]) == mapping[material] * 5 + mip, f"frame {fi}, material {material}"
+            if material < animated:
+                seen.add(mapping[material] - material if mapping[material] == material else 1 + (mapping[material] - 16) % 2)
+            sa_rest = sa.copy()
+            sa_rest["texture_mip"] = sb["texture_mip"]
+            assert sa_rest.tobytes() == sb.tobytes()
+    assert seen == {0, 1, 2}  # every frame of the cycle was shown
