@@ -181,3 +181,30 @@ def test_view_frame_without_leafs_and_bad_leafs(gpu_ok):
         assert lib.sw_draw_frame_view(ctx, ctypes.byref(vin)) == abi.SW_OK
     finally:
         hr.close()
+
+
+def test_view_material_frames_are_validated(gpu_ok):
+    """A material frame naming a texture without mips is refused on the host before any launch; the
+    context stays usable, and a valid table is accepted."""
+    scene = host.Scene(**dict(host.SMALL_MAP, animated_materials=2))
+    hr = host.HostRenderer(scene)
+    lib = gpu.load_library()
+    ctx = hr.context()
+    try:
+        fr = host.Frame(scene)
+        opts = host.frame_options(320, 240, abi.SW_PIXEL_C32, directional=False)
+        out = np.zeros((240, 320), np.uint32)
+        vin = fr.prepare_view(5, opts)
+        assert vin.num_material_frames > 0 and vin.material_frames
+        frames = np.ctypeslib.as_array(ctypes.cast(vin.material_frames, ctypes.POINTER(ctypes.c_uint8)),
+                                       shape=(vin.num_material_frames * abi.MATERIAL_FRAME.itemsize,)).view(abi.MATERIAL_FRAME).copy()
+        bad = frames.copy()
+        bad[0]["texture"] = 1 << 20
+        vin.material_frames = ctypes.c_void_p(bad.ctypes.data)
+        vin.dst = ctypes.c_void_p(out.ctypes.data)
+        vin.dst_pitch = 320
+        assert lib.sw_draw_frame_view(ctx, ctypes.byref(vin)) == abi.SW_ERR_INVALID_ARGUMENT
+        vin.material_frames = ctypes.c_void_p(frames.ctypes.data)
+        assert lib.sw_draw_frame_view(ctx, ctypes.byref(vin)) == abi.SW_OK
+    finally:
+        hr.close()
