@@ -411,6 +411,7 @@ def run_frame_gpu(args, world, rank, local):
                 graph_ms.append(t[4])
                 launches += 1 + 3 + 3
         torch.cuda.synchronize()
+    gpu_ldr = ldr_frames[:4].cpu().numpy().view(np.uint32).copy()  # for the parity check against the oracle
     stage_sum_ms = (totals["surf"] + totals["raster"] + totals["post"]) / args.steps
     frame_ms = max_over_ranks(statistics.mean(graph_ms), world, f"cuda:{local}")
     value = world * 1e3 / frame_ms
@@ -475,7 +476,7 @@ def run_frame_gpu(args, world, rank, local):
                     "post": "pp_downscale_blur_h + pp_blur_v_tonemap"}
     out_line = None
     if rank == 0:
-        cpu = cpu_frame_baseline(work)
+        cpu, parity = cpu_frame_baseline(work, gpu_ldr=gpu_ldr)
         out_line = {
             "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world, "steps": s,
             "warmup": args.warmup, "ms_per_step": round(frame_ms, 4), "higher_is_better": True, "scaling": "weak",
@@ -499,6 +500,7 @@ def run_frame_gpu(args, world, rank, local):
                          "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": stages[dom]["algorithmic_bytes"],
                          "traffic": STAGE_TRAFFIC.get(dom)},
             "cpu_baseline": cpu,
+            "parity": parity,
             "e2e": {"value": round(e2e_val, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d_step),
                     "d2h_bytes_per_step": int(d2h_step),
                     "path": "render_frame: host visibility + GPU-side surface and draw preparation",
@@ -552,30 +554,76 @@ def learned_summary(lr, plain_ms, args):
     }
 
 
-def cpu_frame_baseline(work, max_frames=4):
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def cpu_frame_baseline(work, max_frames=4, gpu_ldr=None):
     """The oracle (C++ restatement of the reference CPU renderer) on the machine's host cores: the same host
     work, surfaces with one task per surface, split_rect rasterisation with one region per thread, and
-    the postprocessor single-threaded (the reference's default, use_multithreading = false)."""
+    the postprocessor single-threaded (the reference's default, use_multithreading = false). Host
+    preparation and the oracle's rendering are timed separately.
+
+    gpu_ldr (optional): the GPU's tonemapped frames of the same first frames, exposure sequence started
+    at 1.0. They are compared with the oracle's frames of the reference's num_threads == 1 raster path
+    (one whole-screen clip rect, partial_renderer.rs:1207-1234: split_rect regions clip spans and move
+    texel addresses, so the timed multithreaded raster is not the parity reference); the frame buffer
+    carries over from frame to frame as the reference's does. Returns (baseline, parity or None)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     threads = os.cpu_count() or 1
     host = work.host
     fr = host.Frame(work.scene)
-    ts = []
+    ts, prep_ts = [], []
     frames = [f["index"] for f in work.frames[:max_frames]]
     exposure = 1.0
+    arenas = []
     for fi in frames:
         t0 = time.perf_counter()
         fr.prepare(fi, work.opts)
+        t1 = time.perf_counter()
         arena = oracle.build_surfaces(work.static, fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=threads)
         fb = np.zeros((H, W), np.uint64)
         oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, fb, num_threads=threads)
         _, exposure, _ = oracle.postprocess(work.config, fb, 1.0 / 60.0, (1.0, 1.0, 1.0), exposure)
-        ts.append(time.perf_counter() - t0)
+        t2 = time.perf_counter()
+        ts.append(t2 - t0)
+        prep_ts.append(t1 - t0)
+        if gpu_ldr is not None:
+            arenas.append((fi, arena))
     v = len(ts) / sum(ts)
-    return {"value": round(v, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+    base = {"value": round(v, 3), "unit": "frames/s", "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+            "host_prep_ms": round(1e3 * statistics.mean(prep_ts), 3),
+            "oracle_ms": round(1e3 * (sum(ts) - sum(prep_ts)) / len(ts), 3),
             "sample": f"{len(frames)} frames {frames} of the same workload; host work + oracle surfaces ({threads} threads) + "
                       f"split_rect raster ({threads} regions) + single-thread postprocess"}
+    if gpu_ldr is None:
+        return base, None
+    mismatched, exposure = 0, 1.0
+    fb = np.zeros((H, W), np.uint64)
+    for k, (fi, arena) in enumerate(arenas):
+        fr.prepare(fi, work.opts)
+        oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, fb, num_threads=1)
+        ldr, exposure, _ = oracle.postprocess(work.config, fb, 1.0 / 60.0, (1.0, 1.0, 1.0), exposure)
+        mismatched += int((ldr != gpu_ldr[k]).sum())
+    parity = {"frames": len(arenas), "mismatched_pixels": mismatched,
+              "what": "tonemapped 1920x1080 frames of the measured graph pass (the first frames of its sequence) vs "
+                      "the oracle (surfaces, num_threads == 1 raster, bloom + tonemap, exposure carried over)"}
+    return base, parity
 
 
 # ---------------------------------------------------------------------------------------------------------
@@ -900,7 +948,7 @@ def run_reference(args, world, rank):
         ts = []
         for i in range(len(work_frames)):
             work.frames = work_frames[i:i + 1]
-            c = cpu_frame_baseline(work, max_frames=1)
+            c, _ = cpu_frame_baseline(work, max_frames=1)
             if i >= args.warmup:
                 ts.append(1.0 / c["value"])
         v = len(ts) / sum(ts)
@@ -911,7 +959,8 @@ def run_reference(args, world, rank):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3) if ms else None,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (lighting) / int (raster)",
            "data": "synthetic (seeded)", "config": {"workload": work.name},
-           "cpu_baseline": {"value": round(v, 3), "unit": unit, "cores": c["cores"], "kind": "port", "sample": c["sample"]},
+           "cpu_baseline": {"value": round(v, 3), "unit": unit, "cores": c["cores"], "kind": "port", "sample": c["sample"],
+                            "cpu_model": cpu_model()},
            "e2e": {"value": round(v, 3), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 

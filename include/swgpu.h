@@ -200,8 +200,8 @@ typedef struct SwFrameParams {
 	uint32_t reserved;
 } SwFrameParams;
 
-/* PostprocessorConfig after synchronize_config clamping (src/square_wheel/postprocessor_config.rs,
- * src/square_wheel/postprocessor.rs:958-977). */
+/* PostprocessorConfig (src/square_wheel/postprocessor_config.rs). Every entry point clamps it first, as
+ * Postprocessor::synchronize_config does before each frame (src/square_wheel/postprocessor.rs:958-977). */
 typedef struct SwPostConfig {
 	float exposure_update_speed;
 	float base_brightness;
@@ -286,8 +286,11 @@ int sw_postprocess(SwCtx* ctx, const SwPostConfig* config, float frame_duration_
  * SW_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit, so frames are limited
  * to SW_NOALLOC_MAX_WIDTH x SW_NOALLOC_MAX_HEIGHT (SW_ERR_LIMIT beyond). The first call on a device
  * (with that device current) looks the array's address up once; make it before any stream capture.
- * All calls share the array: calls that overlap on the GPU race. The exposure is an input; the frame's
- * average colour (postprocessor.rs:206-223 feeds it to update_exposure) is written to `average`. */
+ * cudaDeviceReset unloads the library's device code, so that address is stale afterwards: do not call
+ * this entry point after a cudaDeviceReset in the same process. All calls share the array: calls that
+ * overlap on the GPU race. The configuration is clamped as Postprocessor::synchronize_config clamps it.
+ * The exposure is an input; the frame's average colour (postprocessor.rs:206-223 feeds it to
+ * update_exposure) is written to `average`. */
 #define SW_NOALLOC_MAX_WIDTH 1920u
 #define SW_NOALLOC_MAX_HEIGHT 1080u
 #define SW_NOALLOC_SCRATCH_BYTES 8320512u
@@ -544,8 +547,12 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
  * min(count, 22) values; returns the number of structs (22). Needs no GPU: bindings use it to check their mirrored layouts. */
 int sw_abi_layout(uint32_t* sizes, uint32_t count);
 
-/* Diagnostics: copy the frame's surface arena (total_texels of sw_submit_surfaces) to host memory. */
+/* Diagnostics: copy the frame's surface arena (total_texels of sw_submit_surfaces, or of the surfaces a
+ * sw_draw_frame_view prepared) to host memory (synchronises). */
 int sw_read_surfaces(SwCtx* ctx, void* dst_host, uint64_t max_bytes);
+/* Diagnostics: copy the context's frame buffer (the last frame rasterised, width x height pixels of its
+ * pixel format, tightly packed; the HDR frame the postprocessor read) to host memory (synchronises). */
+int sw_read_framebuffer(SwCtx* ctx, void* dst_host, uint64_t max_bytes);
 /* Current exposure (Postprocessor::current_exposure). */
 int sw_get_exposure(SwCtx* ctx, float* out_exposure);
 int sw_set_exposure(SwCtx* ctx, float exposure);

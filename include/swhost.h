@@ -106,6 +106,10 @@ typedef struct SwhFrame SwhFrame;
 /* Per-frame host state (visibility marks, per-polygon frame data, output arrays). */
 int swh_frame_create(const SwhScene* scene, SwhFrame** out_frame);
 int swh_frame_destroy(SwhFrame* frame);
+/* The map's world polygons and vertices (xyz floats) as sw_set_map takes them; the pointers stay valid
+ * while the frame lives. */
+int swh_frame_map(const SwhFrame* frame, const SwMapPolygon** out_polygons, uint32_t* out_num_polygons,
+	const float** out_vertices, uint32_t* out_num_vertices);
 /* Host work of one frame of the scene's camera path: visibility, surface preparation, light
  * selection, back-to-front traversal and draw setup. */
 int swh_frame_prepare(SwhFrame* frame, uint32_t frame_index, const SwhFrameOptions* options);

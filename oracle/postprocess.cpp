@@ -274,6 +274,25 @@ float update_exposure(const SwPostConfig* cfg, float current, const ColorVec& av
 	return std::exp(std::log(current) * mix + std::log(clamped) * (1.0f - mix));
 }
 
+// Postprocessor::synchronize_config, postprocessor.rs:958-977: the host clamps the configuration before
+// every frame (host.rs:217-219, 274). f32::max / f32::min return the other operand for a NaN, as
+// fmax / fmin do.
+SwPostConfig synchronize_config(const SwPostConfig& in)
+{
+	SwPostConfig c = in;
+	c.min_exposure = fminr(fmaxr(c.min_exposure, 1.0f / 65536.0f), 16.0f);
+	c.max_exposure = fminr(fmaxr(c.max_exposure, 1.0f), 65536.0f);
+	c.exposure_update_speed = fminr(fmaxr(c.exposure_update_speed, 0.5f), 16.0f);
+	c.base_brightness = fminr(fmaxr(c.base_brightness, 0.5f), 2.0f);
+	c.zero_level_brightness = fminr(fmaxr(c.zero_level_brightness, 1.0f / 16.0f), 16.0f);
+	c.brightness_scale_power = fminr(fmaxr(c.brightness_scale_power, 0.01f), 0.5f);
+	c.bloom_sigma = fminr(fmaxr(c.bloom_sigma, 0.0f), 40.0f);
+	c.bloom_buffer_scale_log2 = std::min(std::max(c.bloom_buffer_scale_log2, uint32_t(MIN_BLOOM_BUFFER_SCALE_LOG2)),
+		uint32_t(MAX_BLOOM_BUFFER_SCALE_LOG2));
+	c.bloom_scale = fminr(fmaxr(c.bloom_scale, 1.0f / 16.0f), 1.0f / 2.0f);
+	return c;
+}
+
 } // namespace
 } // namespace sworacle
 
@@ -292,6 +311,8 @@ extern "C" int orc_postprocess(const SwPostConfig* config, const uint64_t* hdr, 
 {
 	if (!config || !hdr || !dst || !exposure || !color_modulate || pitch < width || width == 0 || height == 0)
 		return SW_ERR_INVALID_ARGUMENT;
+	const SwPostConfig synced = synchronize_config(*config);
+	config = &synced;
 	Post p;
 	p.cfg = config;
 	p.hdr = hdr;

@@ -11,7 +11,8 @@
 // Set-up: the first call on a device (with that device current) looks up the array's device address
 // with cudaGetSymbolAddress and caches it for that device; a host-side symbol is not a device address,
 // so kernels only ever receive the looked-up pointer. Make that first call on each device before any
-// stream capture.
+// stream capture. cudaDeviceReset unloads the module and the cached address goes stale with it: the
+// entry point is not for processes that reset a device and keep using the library.
 // Sharing: every call on a device uses the same array and leaves its contents behind; the per-line
 // sums that must start at zero are cleared by each call. Calls whose work overlaps on the GPU (two
 // streams, or two host threads) race on the array: serialise them.
@@ -74,14 +75,6 @@ int scratch_for_current_device(unsigned char** out)
 	return SW_OK;
 }
 
-int32_t as_i32(float x)
-{
-	if (x != x) return 0;
-	if (x >= 2147483648.0f) return INT32_MAX;
-	if (x <= -2147483648.0f) return INT32_MIN;
-	return int32_t(x);
-}
-
 } // namespace
 
 extern "C" int sw_postprocess_noalloc(const uint64_t* hdr, uint32_t width, uint32_t height, const SwPostConfig* config,
@@ -97,55 +90,15 @@ extern "C" int sw_postprocess_noalloc(const uint64_t* hdr, uint32_t width, uint3
 	swgpu::PostArgs a;
 	std::memset(&a, 0, sizeof(a));
 	a.hdr = hdr;
-	a.width = width;
-	a.height = height;
-	a.use_bloom = config->bloom_sigma > 0.0f ? 1u : 0u;
-	a.linear_filter = config->linear_bloom_filter ? 1u : 0u;
-	// TonemappingFunction::new (postprocessor.rs:1005-1017), lanes [b, g, r, a].
-	a.inv_scale[0] = 1.0f / (exposure * color_modulate[2]);
-	a.inv_scale[1] = 1.0f / (exposure * color_modulate[1]);
-	a.inv_scale[2] = 1.0f / (exposure * color_modulate[0]);
-	a.inv_scale[3] = 0.0f;
-	a.inv_255[0] = a.inv_255[1] = a.inv_255[2] = 1.0f / 255.0f;
-	a.inv_255[3] = 0.0f;
 	a.bloom0 = reinterpret_cast<uint64_t*>(scratch + OFF_BLOOM0);
 	a.bloom1 = reinterpret_cast<uint64_t*>(scratch + OFF_BLOOM1);
 	a.line_sums = reinterpret_cast<int32_t*>(scratch + OFF_LINE_SUMS);
 	a.line_sums_f = reinterpret_cast<float*>(scratch + OFF_LINE_SUMS_F);
 	a.average = average ? average : reinterpret_cast<float*>(scratch + OFF_AVERAGE);
-	if (a.use_bloom)
-	{
-		// perform_bloom, postprocessor.rs:729-789; the Gaussian weights are computed here on the host.
-		const int log2 = std::min(std::max(int(config->bloom_buffer_scale_log2), 1), 3);
-		const uint32_t S = 1u << log2;
-		a.scale = S;
-		a.bw = width / S;
-		a.bh = height / S;
-		if (a.bw < 2 || a.bh < 2) return SW_ERR_INVALID_ARGUMENT;
-		const float sigma = config->bloom_sigma / float(S);
-		const float rf = std::ceil(3.0f * sigma - 0.5f);
-		uint32_t radius = rf > 0.0f ? uint32_t(rf) : 0u;
-		if (radius > 16) radius = 16;
-		a.radius = radius;
-		float kernel[33] = {0};
-		const float samples[4] = {-0.375f, -0.125f, 0.125f, 0.375f};
-		const float tau = 6.28318530717958647692f;
-		for (int32_t x = -int32_t(radius); x <= int32_t(radius); ++x)
-		{
-			float val = 0.0f;
-			for (float smp : samples)
-			{
-				const float coord = float(x) + smp;
-				val += std::exp(-0.5f * (coord / sigma) * (coord / sigma)) / (sigma * std::sqrt(tau));
-			}
-			kernel[x + int32_t(radius)] = val / 4.0f;
-		}
-		for (int i = 0; i < 33; ++i)
-		{
-			a.kernel_h[i] = as_i32(kernel[i] * float(1 << 14));
-			a.kernel_v[i] = as_i32(kernel[i] * config->bloom_scale * float(1 << 14));
-		}
-	}
+	// The same tonemapping factors and bloom weights as the context's postprocessor, from the
+	// configuration as synchronize_config clamps it (bloom scales 2..8, so the bloom buffers fit).
+	if (!swgpu::post_args_from_config(a, swgpu::post_config_clamped(*config), exposure, color_modulate, width, height))
+		return SW_ERR_INVALID_ARGUMENT;
 	a.dst = dst;
 	a.dst_pitch = pitch;
 	// launch_postprocess clears the per-line integer sums before accumulating into them.

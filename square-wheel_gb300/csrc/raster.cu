@@ -24,6 +24,7 @@
 #include "warp_prep.cuh"
 
 #include <algorithm>
+#include <atomic>
 
 namespace swgpu
 {
@@ -757,18 +758,24 @@ int launch_shadow_view(const ShadowViewArgs& args, cudaStream_t stream)
 {
 	if (args.num_candidates == 0) return 0;
 	const size_t smem = args.num_leafs <= SHADOW_VIEW_SMEM_LEAFS ? size_t(args.num_leafs) * 4 : 0; // + 16 KB static < 48 KB
-	// resident CTAs of the largest staging (registers bound it first), once per process
-	static int resident = 0;
+	// resident CTAs of the largest staging (registers bound it first), once per device; concurrent first
+	// calls compute the same value, so a relaxed atomic store is enough
+	constexpr int MAX_DEVICES = 64;
+	static std::atomic<int> resident_per_device[MAX_DEVICES];
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return int(e);
+	int resident = dev >= 0 && dev < MAX_DEVICES ? resident_per_device[dev].load(std::memory_order_relaxed) : 0;
 	if (resident == 0)
 	{
-		int dev = 0, sms = 0, per_sm = 0;
-		cudaError_t e = cudaGetDevice(&dev);
-		if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+		int sms = 0, per_sm = 0;
+		e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 		if (e == cudaSuccess)
 			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shadow_view_kernel, SHADOW_VIEW_WARPS * 32,
 				size_t(SHADOW_VIEW_SMEM_LEAFS) * 4);
 		if (e != cudaSuccess) return int(e);
 		resident = std::max(sms * per_sm, 1);
+		if (dev >= 0 && dev < MAX_DEVICES) resident_per_device[dev].store(resident, std::memory_order_relaxed);
 	}
 	const uint32_t blocks = std::min<uint32_t>((args.num_candidates + SHADOW_VIEW_WARPS - 1) / SHADOW_VIEW_WARPS, uint32_t(resident));
 	shadow_view_kernel<<<blocks, SHADOW_VIEW_WARPS * 32, smem, stream>>>(args);

@@ -3,6 +3,9 @@
 
 #include "sw_device.cuh"
 
+#include <algorithm>
+#include <cmath>
+
 namespace swgpu
 {
 
@@ -387,6 +390,76 @@ struct PostArgs
 // aux/fork/join (optional): run the exposure-average reduction on `aux`, joined back before returning.
 int launch_postprocess(const PostArgs& args, int num_sms, cudaStream_t stream, cudaStream_t aux = nullptr,
 	cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
+
+// PostprocessorConfig as Postprocessor::synchronize_config leaves it (postprocessor.rs:958-977), which
+// the host calls before every frame: every field clamped to its range. fmax/fmin return the other
+// operand for a NaN, as Rust's f32::max/min do.
+inline SwPostConfig post_config_clamped(const SwPostConfig& in)
+{
+	SwPostConfig c = in;
+	c.min_exposure = std::fmin(std::fmax(c.min_exposure, 1.0f / 65536.0f), 16.0f);
+	c.max_exposure = std::fmin(std::fmax(c.max_exposure, 1.0f), 65536.0f);
+	c.exposure_update_speed = std::fmin(std::fmax(c.exposure_update_speed, 0.5f), 16.0f);
+	c.base_brightness = std::fmin(std::fmax(c.base_brightness, 0.5f), 2.0f);
+	c.zero_level_brightness = std::fmin(std::fmax(c.zero_level_brightness, 1.0f / 16.0f), 16.0f);
+	c.brightness_scale_power = std::fmin(std::fmax(c.brightness_scale_power, 0.01f), 0.5f);
+	c.bloom_sigma = std::fmin(std::fmax(c.bloom_sigma, 0.0f), 40.0f);
+	c.bloom_buffer_scale_log2 = c.bloom_buffer_scale_log2 < 1u ? 1u : (c.bloom_buffer_scale_log2 > 3u ? 3u : c.bloom_buffer_scale_log2);
+	c.bloom_scale = std::fmin(std::fmax(c.bloom_scale, 1.0f / 16.0f), 0.5f);
+	return c;
+}
+
+// Everything of PostArgs that comes from the (clamped) configuration, the exposure and the colour
+// modulation, for a width x height frame: TonemappingFunction::new (postprocessor.rs:1005-1017, lanes
+// [b, g, r, a]) and, with bloom, the buffer scale, bloom size, blur radius and the integer Gaussian
+// weights of perform_bloom / compute_gaussian_kernel (postprocessor.rs:729-789, 1026-1045), evaluated
+// on the host in f32 with the C library's exp and sqrt. Buffers and destination are the caller's.
+// Returns false when the frame is too small for the bloom buffer (under 2 x 2 bloom pixels).
+inline bool post_args_from_config(PostArgs& a, const SwPostConfig& c, float exposure, const float color_modulate[3],
+	uint32_t width, uint32_t height)
+{
+	a.width = width;
+	a.height = height;
+	a.use_bloom = c.bloom_sigma > 0.0f ? 1u : 0u;
+	a.linear_filter = c.linear_bloom_filter ? 1u : 0u;
+	a.inv_scale[0] = 1.0f / (exposure * color_modulate[2]);
+	a.inv_scale[1] = 1.0f / (exposure * color_modulate[1]);
+	a.inv_scale[2] = 1.0f / (exposure * color_modulate[0]);
+	a.inv_scale[3] = 0.0f;
+	a.inv_255[0] = a.inv_255[1] = a.inv_255[2] = 1.0f / 255.0f;
+	a.inv_255[3] = 0.0f;
+	if (!a.use_bloom) return true;
+	const int log2 = std::min(std::max(int(c.bloom_buffer_scale_log2), 1), 3);
+	const uint32_t S = 1u << log2;
+	a.scale = S;
+	a.bw = width / S;
+	a.bh = height / S;
+	if (a.bw < 2 || a.bh < 2) return false;
+	const float sigma = c.bloom_sigma / float(S);
+	const float rf = std::ceil(3.0f * sigma - 0.5f);
+	uint32_t radius = rf > 0.0f ? uint32_t(rf) : 0u;
+	if (radius > 16) radius = 16;
+	a.radius = radius;
+	float kernel[33] = {0};
+	const float samples[4] = {-0.375f, -0.125f, 0.125f, 0.375f};
+	const float tau = 6.28318530717958647692f;
+	for (int32_t x = -int32_t(radius); x <= int32_t(radius); ++x)
+	{
+		float val = 0.0f;
+		for (float smp : samples)
+		{
+			const float coord = float(x) + smp;
+			val += std::exp(-0.5f * (coord / sigma) * (coord / sigma)) / (sigma * std::sqrt(tau));
+		}
+		kernel[x + int32_t(radius)] = val / 4.0f;
+	}
+	for (int i = 0; i < 33; ++i)
+	{
+		a.kernel_h[i] = f2i32_as(kernel[i] * float(1 << 14));
+		a.kernel_v[i] = f2i32_as(kernel[i] * c.bloom_scale * float(1 << 14));
+	}
+	return true;
+}
 
 int launch_upscale(uint32_t mode, uint32_t scale, const uint32_t* src, uint32_t* dst, uint32_t dst_width,
 	uint32_t dst_height, uint32_t dst_pitch, cudaStream_t stream);

@@ -99,6 +99,7 @@ struct SwCtx
 	DevBuf lights, surfaces, work_prefix, arena;
 	uint64_t arena_texels = 0;
 	uint32_t arena_format = SW_PIXEL_C32;
+	bool arena_view = false; // the arena was sized by a view frame: its texels are in v_counts
 	bool arena_valid = false;
 	uint32_t last_num_surfaces = 0, last_surface_format = SW_PIXEL_C32, last_max_light = 0;
 	uint64_t last_surface_work = 0;
@@ -414,6 +415,28 @@ int check_kernel(SwCtx* ctx, int launch_result, const char* what)
 
 uint32_t bpp_of(uint32_t format) { return format == SW_PIXEL_C64 ? 8u : 4u; }
 
+bool all_finite(const float* v, int n)
+{
+	for (int i = 0; i < n; ++i)
+		if (!std::isfinite(v[i])) return false;
+	return true;
+}
+
+// Camera position and lights of a frame: a NaN or an infinity there is a caller's error, rejected before
+// anything is uploaded or launched.
+int check_frame_inputs(SwCtx* ctx, const SwFrameParams& p, const SwLight* lights, uint32_t num_lights)
+{
+	if (!all_finite(p.cam_pos, 3)) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "non-finite camera position");
+	for (uint32_t i = 0; i < num_lights; ++i)
+	{
+		const SwLight& l = lights[i];
+		if (!all_finite(l.position, 3) || !all_finite(l.color, 3) || !std::isfinite(l.radius) ||
+			!std::isfinite(l.inv_square_radius))
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "light %u: non-finite parameters", i);
+	}
+	return SW_OK;
+}
+
 // f32 -> i32 `as` conversion: truncating, saturating, NaN -> 0.
 int32_t f2i32_sat(float x)
 {
@@ -620,12 +643,13 @@ int sw_frame_begin(SwCtx* ctx, const SwFrameParams* params, const SwLight* light
 	if (params->use_directional_lightmaps && ctx->num_dir_lightmap_elements == 0)
 		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "directional lightmaps requested but none uploaded");
 	if (num_lights > 65535) return fail(ctx, SW_ERR_LIMIT, "too many lights");
+	int r = check_frame_inputs(ctx, *params, lights, num_lights);
+	if (r) return r;
 	SW_CUDA(ctx, cudaSetDevice(ctx->device));
 	ctx->frame = *params;
 	ctx->num_lights = num_lights;
 	stage_begin(ctx, STAGE_FRAME);
-	int r = ensure(ctx, ctx->lights, std::max<size_t>(num_lights, 1) * sizeof(SwLight));
-	if (r) return r;
+	if ((r = ensure(ctx, ctx->lights, std::max<size_t>(num_lights, 1) * sizeof(SwLight)))) return r;
 	if ((r = upload(ctx, ctx->stage_lights, ctx->lights.ptr, lights, num_lights * sizeof(SwLight)))) return r;
 	ctx->frame_open = true;
 	ctx->arena_valid = false;
@@ -727,6 +751,7 @@ void note_surfaces(SwCtx* ctx, uint32_t num_surfaces, uint64_t total_texels, uin
 {
 	ctx->arena_texels = total_texels;
 	ctx->arena_format = ctx->frame.pixel_format;
+	ctx->arena_view = false;
 	ctx->last_num_surfaces = num_surfaces;
 	ctx->last_surface_work = work;
 	ctx->last_surface_directional = ctx->frame.use_directional_lightmaps != 0;
@@ -825,6 +850,7 @@ int sw_set_surfaces(SwCtx* ctx, const void* texels, uint64_t total_texels)
 	if ((r = upload(ctx, ctx->stage_io, ctx->arena.ptr, texels, total_texels * bpp))) return r;
 	ctx->arena_texels = total_texels;
 	ctx->arena_format = ctx->frame.pixel_format;
+	ctx->arena_view = false;
 	ctx->arena_valid = true;
 	return SW_OK;
 }
@@ -963,7 +989,8 @@ namespace
 {
 // Postprocessor arguments for the context's colour64 frame buffer (everything but the destination):
 // tonemapping factors from the current exposure and colour modulation, bloom kernel weights, scratch
-// buffers. Runs finalize_exposure first (the previous frame's average updates the exposure).
+// buffers, from the configuration as synchronize_config clamps it. Runs finalize_exposure first (the
+// previous frame's average updates the exposure).
 int prepare_post(SwCtx* ctx, const SwPostConfig* config, const float color_modulate[3], PostArgs& a)
 {
 	const uint32_t w = ctx->fb_width, h = ctx->fb_height;
@@ -972,59 +999,17 @@ int prepare_post(SwCtx* ctx, const SwPostConfig* config, const float color_modul
 
 	std::memset(&a, 0, sizeof(a));
 	a.hdr = static_cast<const uint64_t*>(ctx->framebuffer.ptr);
-	a.width = w;
-	a.height = h;
-	a.use_bloom = config->bloom_sigma > 0.0f ? 1u : 0u;
-	a.linear_filter = config->linear_bloom_filter ? 1u : 0u;
-	// TonemappingFunction::new (postprocessor.rs:1005-1017), lanes [b, g, r, a].
-	const float inv_255 = 1.0f / 255.0f;
-	a.inv_scale[0] = 1.0f / (ctx->exposure * color_modulate[2]);
-	a.inv_scale[1] = 1.0f / (ctx->exposure * color_modulate[1]);
-	a.inv_scale[2] = 1.0f / (ctx->exposure * color_modulate[0]);
-	a.inv_scale[3] = 0.0f;
-	a.inv_255[0] = a.inv_255[1] = a.inv_255[2] = inv_255;
-	a.inv_255[3] = 0.0f;
 	a.average = static_cast<float*>(ctx->average.ptr);
+	if (!post_args_from_config(a, post_config_clamped(*config), ctx->exposure, color_modulate, w, h))
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "frame too small for bloom");
 	if (a.use_bloom)
 	{
-		// perform_bloom, postprocessor.rs:729-789 (kernel weights computed here, on the host).
-		const int log2 = std::min(std::max(int(config->bloom_buffer_scale_log2), 1), 3);
-		const uint32_t S = 1u << log2;
-		a.scale = S;
-		a.bw = w / S;
-		a.bh = h / S;
-		if (a.bw < 2 || a.bh < 2) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "frame too small for bloom");
 		if ((r = ensure(ctx, ctx->bloom0, size_t(a.bw) * a.bh * 8))) return r;
 		if ((r = ensure(ctx, ctx->bloom1, size_t(a.bw) * a.bh * 8))) return r;
 		if ((r = ensure(ctx, ctx->line_sums, size_t(a.bh) * 16))) return r;
 		a.bloom0 = static_cast<uint64_t*>(ctx->bloom0.ptr);
 		a.bloom1 = static_cast<uint64_t*>(ctx->bloom1.ptr);
 		a.line_sums = static_cast<int32_t*>(ctx->line_sums.ptr);
-		const float sigma = config->bloom_sigma / float(S);
-		const float rf = std::ceil(3.0f * sigma - 0.5f);
-		uint32_t radius = rf > 0.0f ? uint32_t(rf) : 0u;
-		if (radius > 16) radius = 16;
-		a.radius = radius;
-		float kernel[33] = {0};
-		const float samples[4] = {-0.375f, -0.125f, 0.125f, 0.375f};
-		const float tau = 6.28318530717958647692f;
-		for (int32_t x = -int32_t(radius); x <= int32_t(radius); ++x)
-		{
-			float val = 0.0f;
-			for (float smp : samples)
-			{
-				float coord = float(x) + smp;
-				val += std::exp(-0.5f * (coord / sigma) * (coord / sigma)) / (sigma * std::sqrt(tau));
-			}
-			kernel[x + int32_t(radius)] = val / 4.0f;
-		}
-		for (int i = 0; i < 33; ++i)
-		{
-			const float kh = kernel[i] * float(1 << 14);
-			const float kv = kernel[i] * config->bloom_scale * float(1 << 14);
-			a.kernel_h[i] = f2i32_sat(kh);
-			a.kernel_v[i] = f2i32_sat(kv);
-		}
 	}
 	else
 	{
@@ -1065,7 +1050,7 @@ int sw_postprocess(SwCtx* ctx, const SwPostConfig* config, float frame_duration_
 	SW_CUDA(ctx, cudaEventRecord(ctx->average_ready, ctx->stream));
 	stage_end(ctx, STAGE_FRAME);
 	ctx->exposure_pending = true;
-	ctx->pending_config = *config;
+	ctx->pending_config = post_config_clamped(*config);
 	ctx->pending_dt = frame_duration_s;
 	if (!dst_is_device) return copy_out(ctx, dst, pitch, 0, out, w, w, h, 4);
 	return SW_OK;
@@ -1134,9 +1119,29 @@ int sw_read_surfaces(SwCtx* ctx, void* dst_host, uint64_t max_bytes)
 {
 	if (!ctx || !dst_host) return SW_ERR_INVALID_ARGUMENT;
 	if (!ctx->arena_valid && ctx->arena_texels == 0) return fail(ctx, SW_ERR_STATE, "no surfaces built");
-	const uint64_t bytes = ctx->arena_texels * bpp_of(ctx->arena_format);
+	uint64_t texels = ctx->arena_texels;
+	if (ctx->arena_view && ctx->v_counts)
+	{
+		// a view frame's arena is sized by a bound: the frame's own texels are counted on the device
+		SwViewCounts k;
+		SW_CUDA(ctx, cudaMemcpyAsync(&k, ctx->v_counts, sizeof(k), cudaMemcpyDeviceToHost, ctx->stream));
+		SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+		texels = std::min<uint64_t>(k.total_texels, ctx->arena_texels);
+	}
+	const uint64_t bytes = texels * bpp_of(ctx->arena_format);
 	if (bytes > max_bytes) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "destination too small (%llu bytes needed)", (unsigned long long)bytes);
 	SW_CUDA(ctx, cudaMemcpyAsync(dst_host, ctx->arena.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	return SW_OK;
+}
+
+int sw_read_framebuffer(SwCtx* ctx, void* dst_host, uint64_t max_bytes)
+{
+	if (!ctx || !dst_host) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->fb_valid) return fail(ctx, SW_ERR_STATE, "no frame rendered");
+	const uint64_t bytes = uint64_t(ctx->fb_width) * ctx->fb_height * bpp_of(ctx->fb_format);
+	if (bytes > max_bytes) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "destination too small (%llu bytes needed)", (unsigned long long)bytes);
+	SW_CUDA(ctx, cudaMemcpyAsync(dst_host, ctx->framebuffer.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
 	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 	return SW_OK;
 }
@@ -1221,7 +1226,7 @@ int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, con
 namespace
 {
 // The checks of sw_frame_begin for a whole-frame call.
-int check_frame_params(SwCtx* ctx, const SwFrameParams& p, uint32_t num_lights)
+int check_frame_params(SwCtx* ctx, const SwFrameParams& p, const SwLight* lights, uint32_t num_lights)
 {
 	if (p.pixel_format > SW_PIXEL_C64) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "bad pixel format");
 	if (p.width == 0 || p.height == 0 || p.width > 16384 || p.height > 16384)
@@ -1229,7 +1234,7 @@ int check_frame_params(SwCtx* ctx, const SwFrameParams& p, uint32_t num_lights)
 	if (p.use_directional_lightmaps && ctx->num_dir_lightmap_elements == 0)
 		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "directional lightmaps requested but none uploaded");
 	if (num_lights > 65535) return fail(ctx, SW_ERR_LIMIT, "too many lights");
-	return SW_OK;
+	return check_frame_inputs(ctx, p, lights, num_lights);
 }
 
 // The frame buffer of the frame's size and format; a new one starts black (postprocessor.rs:56-66),
@@ -1341,7 +1346,7 @@ int finish_graph_frame(SwCtx* ctx, Staging& st, const SwFrameParams& p, bool pos
 	{
 		SW_CUDA(ctx, cudaEventRecord(ctx->average_ready, ctx->stream));
 		ctx->exposure_pending = true;
-		ctx->pending_config = post;
+		ctx->pending_config = post_config_clamped(post);
 		ctx->pending_dt = dt;
 		if (direct_host)
 		{
@@ -1370,7 +1375,7 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	if (!ctx->graph_enabled) return draw_frame_direct(ctx, f);
 	int r;
 	const SwFrameParams& p = f.params;
-	if ((r = check_frame_params(ctx, p, f.num_lights))) return r;
+	if ((r = check_frame_params(ctx, p, f.lights, f.num_lights))) return r;
 	SW_CUDA(ctx, cudaSetDevice(ctx->device));
 	ctx->frame = p;
 	ctx->num_lights = f.num_lights;
@@ -1567,6 +1572,8 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	if ((f.num_lights && !f.lights) || (f.num_leafs && !f.leafs) || (f.num_leaf_lights && !f.leaf_lights) ||
 		(f.num_draws && (!f.draws || !f.vertices)) || (f.num_material_frames && !f.material_frames))
 		return SW_ERR_INVALID_ARGUMENT;
+	if (!all_finite(f.view_matrix, 16) || !all_finite(f.planes_matrix, 16))
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "non-finite camera matrices");
 	if (f.num_material_frames > (1u << 20)) return fail(ctx, SW_ERR_LIMIT, "too many material frames");
 	for (uint32_t i = 0; i < f.num_material_frames; ++i)
 		if (uint64_t(f.material_frames[i].texture) * 5 + 4 >= ctx->h_texture_mips.size())
@@ -1576,7 +1583,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	if (f.dst && f.dst_pitch < f.params.width) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");
 	int r;
 	const SwFrameParams& p = f.params;
-	if ((r = check_frame_params(ctx, p, f.num_lights))) return r;
+	if ((r = check_frame_params(ctx, p, f.lights, f.num_lights))) return r;
 	SW_CUDA(ctx, cudaSetDevice(ctx->device));
 	for (uint32_t k = 0; k < 2; ++k)
 		if (ctx->counts_pending[k] && cudaEventQuery(ctx->ev_counts[k]) == cudaSuccess) consume_view_counts(ctx, k);
@@ -1660,6 +1667,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	ctx->v_vertices = reinterpret_cast<SwVertex16*>(slab + vs.vertices);
 	ctx->arena_texels = cap_texels;
 	ctx->arena_format = p.pixel_format;
+	ctx->arena_view = true;
 	ctx->view_surfaces_cap = uint32_t(cap_surfaces);
 	ctx->view_draws_cap = uint32_t(std::min<uint64_t>(cap_draws, 0xFFFFFFFFu));
 	ctx->view_vertices_cap = uint32_t(std::min<uint64_t>(cap_vertices, 0xFFFFFFFFu));

@@ -17,7 +17,8 @@ struct SwhScene
 };
 struct SwhFrame
 {
-	explicit SwhFrame(const Scene& s) : prep(s) {}
+	explicit SwhFrame(const Scene& s) : scene(s), prep(s) {}
+	const Scene& scene;
 	FramePrep prep;
 };
 struct SwhRenderer;
@@ -61,6 +62,14 @@ namespace
 {
 thread_local std::string g_error;
 
+// textures_mip_bias as Renderer::synchronize_config leaves it before every frame (renderer.rs:222-233).
+float clamped_mip_bias(float b)
+{
+	if (b < -1.0f) b = -1.0f;
+	if (b > 2.0f) b = 2.0f;
+	return b;
+}
+
 FrameOptions to_options(const SwhFrameOptions* o)
 {
 	FrameOptions f;
@@ -70,8 +79,11 @@ FrameOptions to_options(const SwhFrameOptions* o)
 	f.use_directional_lightmaps = o->use_directional_lightmaps != 0;
 	f.clear_background = o->clear_background != 0;
 	if (o->fov > 0.0f) f.fov = o->fov;
-	f.mip_bias = o->mip_bias;
-	f.shadows_quality = std::fmax(-1.0f, std::fmin(o->shadows_quality, 1.0f)); // renderer.rs:235-242
+	f.mip_bias = clamped_mip_bias(o->mip_bias);
+	// Renderer::synchronize_config, renderer.rs:235-244 (a NaN passes both comparisons unchanged)
+	f.shadows_quality = o->shadows_quality;
+	if (f.shadows_quality < -1.0f) f.shadows_quality = -1.0f;
+	if (f.shadows_quality > 1.0f) f.shadows_quality = 1.0f;
 	return f;
 }
 
@@ -189,6 +201,17 @@ int swh_frame_create(const SwhScene* s, SwhFrame** out)
 	if (!s || !out) return SW_ERR_INVALID_ARGUMENT;
 	*out = new (std::nothrow) SwhFrame(s->scene);
 	return *out ? SW_OK : SW_ERR_OUT_OF_MEMORY;
+}
+
+int swh_frame_map(const SwhFrame* f, const SwMapPolygon** out_polygons, uint32_t* out_num_polygons, const float** out_vertices,
+	uint32_t* out_num_vertices)
+{
+	if (!f || !out_polygons || !out_num_polygons || !out_vertices || !out_num_vertices) return SW_ERR_INVALID_ARGUMENT;
+	*out_polygons = f->prep.map_polygons.data();
+	*out_num_polygons = uint32_t(f->prep.map_polygons.size());
+	*out_vertices = reinterpret_cast<const float*>(f->scene.vertices.data());
+	*out_num_vertices = uint32_t(f->scene.vertices.size());
+	return SW_OK;
 }
 
 int swh_frame_destroy(SwhFrame* f)
@@ -377,7 +400,7 @@ int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFra
 		if ((st = submit_shadows(r, r->frame->prep))) return st;
 		SwViewFrameInput vin;
 		swh_frame_view_input(r->frame, &vin);
-		vin.mip_bias = o->mip_bias;
+		vin.mip_bias = clamped_mip_bias(o->mip_bias);
 		if (post)
 		{
 			vin.postprocess = 1;

@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(PKG_DIR, "lib", "libswgpu.so")
 EXPORTED = [
     "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_set_surfaces", "sw_set_skybox", "sw_register_host_buffer", "sw_unregister_host_buffer",
     "sw_submit_draws",
-    "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_get_exposure", "sw_set_exposure",
+    "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_read_framebuffer", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
     "sw_postprocess_noalloc", "sw_set_learned_upscaler", "sw_draw_frame", "sw_set_frame_graph", "sw_set_tuning",
     "sw_get_tuning", "sw_autotune", "sw_set_map", "sw_draw_frame_view", "sw_read_view_prep",
@@ -66,6 +66,7 @@ def load_library(path=LIB_PATH):
         "sw_postprocess": ([vp, vp, f32, vp, vp, u32, i32], i32),
         "sw_upscale": ([vp, u32, u32, vp, i32, vp, u32, u32, u32, i32], i32),
         "sw_read_surfaces": ([vp, vp, u64], i32),
+        "sw_read_framebuffer": ([vp, vp, u64], i32),
         "sw_get_exposure": ([vp, ctypes.POINTER(f32)], i32),
         "sw_set_exposure": ([vp, f32], i32),
         "sw_set_framebuffer": ([vp, vp, u32, u32, u32, i32], i32),
@@ -355,6 +356,13 @@ class GpuRenderer:
         dt = np.uint64 if pixel_format == abi.SW_PIXEL_C64 else np.uint32
         out = np.empty(int(total_texels), dt)
         self._check(self.lib.sw_read_surfaces(self.ctx, abi.ptr(out), out.nbytes), "sw_read_surfaces")
+        return out
+
+    def read_framebuffer(self, width, height, pixel_format):
+        """The context's frame buffer (the last rasterised frame) as a height x width array."""
+        dt = np.uint64 if pixel_format == abi.SW_PIXEL_C64 else np.uint32
+        out = np.empty((int(height), int(width)), dt)
+        self._check(self.lib.sw_read_framebuffer(self.ctx, abi.ptr(out), out.nbytes), "sw_read_framebuffer")
         return out
 
     def exposure(self):

@@ -76,6 +76,7 @@ def load_host_library():
         "swh_renderer_render_frame": ([vp, u32, vp, vp, ctypes.c_float, vp, vp, u32, i32], i32),
         "swh_frame_prepare_view": ([vp, u32, vp], i32), "swh_frame_view_input": ([vp, vp], i32),
         "swh_renderer_set_gpu_prep": ([vp, i32], i32),
+        "swh_frame_map": ([vp, ctypes.POINTER(vp), ctypes.POINTER(u32), ctypes.POINTER(vp), ctypes.POINTER(u32)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -90,7 +91,7 @@ HOST_EXPORTED = ["swh_scene_create", "swh_scene_destroy", "swh_scene_info", "swh
                  "swh_renderer_create", "swh_renderer_destroy", "swh_renderer_prepare_frame",
                  "swh_renderer_draw_frame", "swh_renderer_context", "swh_renderer_frame", "swh_scene_skybox",
                  "swh_renderer_render_frame", "swh_frame_prepare_view", "swh_frame_view_input",
-                 "swh_renderer_set_gpu_prep"]
+                 "swh_renderer_set_gpu_prep", "swh_frame_map"]
 
 # The two map configurations of the benchmark plan.
 SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, num_materials=16, metal_frac=0.0,
@@ -198,6 +199,18 @@ class Frame:
     def prepare(self, frame_index, options):
         _check(self.lib, self.lib.swh_frame_prepare(self.handle, frame_index, ctypes.byref(options)), "swh_frame_prepare")
         return self._outputs()
+
+    def map_data(self):
+        """Copies of the map's world polygons (abi.MAP_POLYGON) and vertices (float32, n x 3) as sw_set_map
+        takes them."""
+        pp, vp_ = ctypes.c_void_p(), ctypes.c_void_p()
+        n, nv = ctypes.c_uint32(), ctypes.c_uint32()
+        _check(self.lib, self.lib.swh_frame_map(self.handle, ctypes.byref(pp), ctypes.byref(n), ctypes.byref(vp_),
+                                                ctypes.byref(nv)), "swh_frame_map")
+        polys = np.ctypeslib.as_array(ctypes.cast(pp, ctypes.POINTER(ctypes.c_uint8)),
+                                      shape=(n.value * abi.MAP_POLYGON.itemsize,)).view(abi.MAP_POLYGON).copy()
+        verts = np.ctypeslib.as_array(ctypes.cast(vp_, ctypes.POINTER(ctypes.c_float)), shape=(nv.value * 3,)).copy()
+        return polys, verts.reshape(-1, 3)
 
     def _outputs(self):
         o = FrameOutputs()

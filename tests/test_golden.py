@@ -193,6 +193,65 @@ def test_known_answer_lightmapped_surface(built_libs):
     assert np.all(rgb == np.uint32((50 << 16) | (100 << 8) | 200)), [hex(int(x)) for x in out[:4]]
 
 
+# Out-of-range configurations and what Postprocessor::synchronize_config (postprocessor.rs:958-977)
+# clamps them to before every frame.
+CLAMP_CASES = [
+    (dict(bloom_sigma=100.0), dict(bloom_sigma=40.0)),
+    (dict(bloom_sigma=-3.0), dict(bloom_sigma=0.0)),
+    (dict(bloom_buffer_scale_log2=0), dict(bloom_buffer_scale_log2=1)),
+    (dict(bloom_buffer_scale_log2=7), dict(bloom_buffer_scale_log2=3)),
+    (dict(bloom_scale=0.001), dict(bloom_scale=1.0 / 16.0)),
+    (dict(bloom_scale=3.0), dict(bloom_scale=0.5)),
+    (dict(min_exposure=100.0, max_exposure=0.1), dict(min_exposure=16.0, max_exposure=1.0)),
+    (dict(exposure_update_speed=float("nan"), base_brightness=9.0), dict(exposure_update_speed=0.5, base_brightness=2.0)),
+    (dict(zero_level_brightness=1e-6, brightness_scale_power=4.0), dict(zero_level_brightness=1.0 / 16.0, brightness_scale_power=0.5)),
+]
+
+
+def _config(**kw):
+    c = abi.PostConfig.default()
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+@pytest.mark.parametrize("given,clamped", CLAMP_CASES)
+def test_oracle_clamps_config(built_libs, given, clamped):
+    """An out-of-range configuration gives exactly the frames and exposures of its clamped form."""
+    rng = np.random.default_rng(5)
+    lanes = rng.integers(0, 3000, (60, 88, 4), dtype=np.uint64)
+    hdr = lanes[..., 0] | (lanes[..., 1] << 16) | (lanes[..., 2] << 32) | (np.uint64(255) << 48)
+    e_a = e_b = 1.0
+    for _ in range(3):
+        a, e_a, _ = oracle.postprocess(_config(**given), hdr, 1.0 / 60.0, (1.0, 1.0, 1.0), e_a)
+        b, e_b, _ = oracle.postprocess(_config(**clamped), hdr, 1.0 / 60.0, (1.0, 1.0, 1.0), e_b)
+        assert np.array_equal(a, b)
+        assert e_a == e_b
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("given,clamped", CLAMP_CASES)
+def test_gpu_clamps_config(gpu_ok, given, clamped):
+    """The GPU postprocessor clamps the same way: frames and exposures equal the oracle's."""
+    from sqwheel import synth
+    rng = np.random.default_rng(6)
+    lanes = rng.integers(0, 3000, (60, 88, 4), dtype=np.uint64)
+    hdr = lanes[..., 0] | (lanes[..., 1] << 16) | (lanes[..., 2] << 32) | (np.uint64(255) << 48)
+    cfg = _config(**given)
+    r = gpu.GpuRenderer(synth.BatchedSurfaces(seed=1, count=1, max_side=8).static_data())
+    exposure = 1.0
+    try:
+        for _ in range(3):
+            want, exposure, _ = oracle.postprocess(cfg, hdr, 1.0 / 60.0, (1.0, 1.0, 1.0), exposure)
+            r.set_framebuffer(hdr, abi.SW_PIXEL_C64)
+            got = np.zeros_like(want)
+            r.postprocess(cfg, 1.0 / 60.0, (1.0, 1.0, 1.0), out=got)
+            assert np.array_equal(want, got)
+            assert r.exposure() == np.float32(exposure)
+    finally:
+        r.close()
+
+
 # ---------------------------------------------------------------- CUDA path (GPU)
 
 @pytest.mark.gpu

@@ -22,15 +22,30 @@ def hdr_frame(rng, w, h, hi):
     return (lanes[..., 0] | (lanes[..., 1] << 16) | (lanes[..., 2] << 32) | (lanes[..., 3] << 48)).astype(np.uint64)
 
 
-@pytest.mark.parametrize("linear", [0, 1])
-def test_noalloc_matches_context_postprocess(gpu_ok, linear):
+# (width, height, bloom_sigma, bloom_buffer_scale_log2, linear filter): bloom at scales 2, 4 and 8, both
+# filters, no bloom (the per-line float sums of the scratch array), and frames at the size limit
+CASES = [
+    (1000, 700, 3.0, 1, 0),
+    (1000, 700, 3.0, 1, 1),
+    (1920, 1080, 1.0, 1, 0),
+    (1920, 1080, 0.0, 1, 0),
+    (640, 480, 0.0, 2, 1),
+    (800, 600, 6.0, 2, 1),
+    (999, 701, 3.0, 3, 0),
+]
+
+
+@pytest.mark.parametrize("w,h,sigma,scale_log2,linear", CASES)
+def test_noalloc_matches_context_postprocess(gpu_ok, w, h, sigma, scale_log2, linear):
     import torch
+
+    import oracle
     lib = gpu.load_library()
-    rng = np.random.default_rng(17 + linear)
-    w, h = 1000, 700
+    rng = np.random.default_rng(17 + linear + 2 * scale_log2 + int(sigma))
     cfg = abi.PostConfig.default()
     cfg.linear_bloom_filter = linear
-    cfg.bloom_sigma = 3.0
+    cfg.bloom_sigma = sigma
+    cfg.bloom_buffer_scale_log2 = scale_log2
     mod = (1.0, 0.8, 1.2)
     st = synth.BatchedSurfaces(seed=1, count=1, max_side=8)
     r = gpu.GpuRenderer(st.static_data())
@@ -45,7 +60,7 @@ def test_noalloc_matches_context_postprocess(gpu_ok, linear):
             # Allocation-free entry point on device buffers.
             d_hdr = torch.from_numpy(hdr.view(np.int64)).cuda()
             d_dst = torch.zeros((h, w + 3), dtype=torch.int32, device="cuda")
-            d_avg = torch.zeros(4, dtype=torch.float32, device="cuda")
+            d_avg = torch.full((4,), -1.0, dtype=torch.float32, device="cuda")
             cmod = (ctypes.c_float * 3)(*mod)
             rc = lib.sw_postprocess_noalloc(ctypes.c_void_p(d_hdr.data_ptr()), w, h, ctypes.byref(cfg), float(exposure), cmod,
                                             ctypes.c_void_p(d_dst.data_ptr()), w + 3, ctypes.c_void_p(d_avg.data_ptr()), None)
@@ -53,7 +68,10 @@ def test_noalloc_matches_context_postprocess(gpu_ok, linear):
             torch.cuda.synchronize()
             got = d_dst.cpu().numpy().view(np.uint32)[:, :w]
             assert np.array_equal(want, got), f"call {call}: {(want != got).sum()} pixels differ"
-            assert np.isfinite(d_avg.cpu().numpy()).all()
+            # the frame's average colour, which the context turns into its next exposure: the same lanes
+            # as the oracle's (whose exposure sequence the context's matches bit for bit)
+            _, _, want_avg = oracle.postprocess(cfg, hdr, 1.0 / 60.0, mod, exposure)
+            assert np.array_equal(d_avg.cpu().numpy()[:3], want_avg[:3]), (d_avg.cpu().numpy(), want_avg)
     finally:
         r.close()
 
