@@ -530,15 +530,13 @@ def learned_summary(lr, plain_ms, args):
     if peak is None:
         peak, kind = 1900.0, "fallback"
     n = len(p["learned"])
-    # with the quality monitor: every 16th frame also renders the plain frame for the PSNR check
-    check_ms = lr["ms"] + plain_ms / 16.0
+    mon = monitored_sequence(p["learned"], lr["ms"], plain_ms)
     return {
         "what": "960x540 frame (CUDA graph: surfaces, raster, bloom + tonemap) + learned 2x upscale to 1920x1080 "
                 "(BF16 tcgen05, FP32 accumulate), same frames as the plain measurement",
         "frames_per_s": round(1e3 / lr["ms"], 2), "ms_per_frame": round(lr["ms"], 4),
         "speedup_vs_plain": round(plain_ms / lr["ms"], 3),
-        "with_psnr_check_every_16th_frame": {"frames_per_s": round(1e3 / check_ms, 2),
-                                             "speedup_vs_plain": round(plain_ms / check_ms, 3)},
+        "with_quality_monitor": mon,
         "stages_ms": lr["stages_ms"],
         "psnr_db": {"learned_mean": round(float(np.mean(p["learned"])), 3),
                     "learned_min": round(float(np.min(p["learned"])), 3),
@@ -552,6 +550,35 @@ def learned_summary(lr, plain_ms, args):
                   "maps": f"full-size configuration, seeds {list(LEARN_MAPS)} (bench map: seed 2)",
                   "seconds": round(lr["train_s"], 2)},
     }
+
+
+def monitored_sequence(psnr_db, learned_ms, plain_ms, check_interval=16, threshold_db=38.0, fallback_frames=32):
+    """What the renderer delivers with the learned path's quality monitor (sw_monitor_*: every 16th
+    learned frame also renders the plain frame and checks the PSNR; a check under 38 dB switches to the
+    plain path for 32 frames) over the measured frames in their order, each frame's PSNR the one
+    measured for it. A learned frame costs the learned path's mean time, a checked one that plus a
+    plain frame, a fallback frame the plain path's: frames/s counts only frames actually delivered."""
+    from sqwheel import learned
+    m = learned.Monitor(check_interval=check_interval, threshold_db=threshold_db, fallback_frames=fallback_frames)
+    total = 0.0
+    kinds = {"learned": 0, "learned_checked": 0, "plain_fallback": 0}
+    for db in psnr_db:
+        plan = m.plan()
+        if plan == 2:
+            total += plain_ms
+            kinds["plain_fallback"] += 1
+        elif plan == 1:
+            total += learned_ms + plain_ms
+            kinds["learned_checked"] += 1
+            m.report(db)
+        else:
+            total += learned_ms
+            kinds["learned"] += 1
+    n = len(psnr_db)
+    return {"frames_per_s": round(1e3 * n / total, 2), "speedup_vs_plain": round(plain_ms * n / total, 3),
+            "frames": kinds, "failed_checks": int(m.failed_checks),
+            "monitor": f"check every {check_interval}th learned frame at {threshold_db} dB, {fallback_frames} plain "
+                       f"frames after a failed check"}
 
 
 def cpu_model():
@@ -975,7 +1002,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--autotune-reps", type=int, default=5,
                     help="frames per configuration of the autotuner before the frame measurement (0: keep the default)")
-    ap.add_argument("--learn-steps", type=int, default=2000,
+    ap.add_argument("--learn-steps", type=int, default=20000,
                     help="training steps of the learned upscaler before its measurement (0: skip it)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
