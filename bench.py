@@ -136,18 +136,31 @@ def frame_indices(n, offset=0):
 # frame workload, from one `ncu --set full` capture of this command (cold cache: ncu replays every kernel
 # alone; the frame's writes are still in L2 when a kernel ends).
 STAGE_TRAFFIC = {
-    "post": 16.604928e6 + 20.803840e6,   # pp_downscale_blur_h_kernel + pp_blur_v_tonemap_kernel
-    "raster": 19.322368e6 + 0.054272e6,  # raster_tiles_kernel + raster_setup_kernel
-    "surf": None,                        # captured only at the 4,096-surface workload
+    "post": None,
+    "raster": None,
+    "surf": None,
 }
 
 
+# Kernels one frame launches (either preparation split on the host side): surface build, raster setup,
+# raster tiles, blur + tonemap, exposure average.
+FRAME_LAUNCHES = 5
+
+
+def raster_bytes(pixel_writes, w, h):
+    """Algorithmic bytes of the tile pass: every span pixel's texel read and frame write (colour64;
+    the metric's frames blend nothing) and the bloom downscale's read of the frame, which its epilogue
+    performs (the bloom + tonemap formula's first term)."""
+    return pixel_writes * (8 + 8) + w * h * 8
+
+
 def post_bytes(w, h, scale=2):
-    """Algorithmic bytes of bloom + tonemap as two passes over the frame: HDR read by the downscale and
-    again by the tonemap, the blurred bloom buffer written once and read once, the Color32 frame written
-    (the separate downscale / blur / blur passes would add 12 MB of bloom traffic at 1080p)."""
+    """Algorithmic bytes of bloom + tonemap after the downscale: the two blur passes (bloom buffer read
+    and written twice), the tonemap's HDR read and Color32 write, and its bloom read. With the
+    downscale's W*H*8 in raster_bytes the two stages sum to the bloom + tonemap formula
+    W*H*8 + 2*(W/S)(H/S)*8*2 + W*H*(8+4) + (W/S)(H/S)*8."""
     bw, bh = w // scale, h // scale
-    return w * h * 8 * 2 + bw * bh * 8 * 2 + w * h * 4
+    return 2 * bw * bh * 8 * 2 + w * h * (8 + 4) + bw * bh * 8
 
 
 class FrameWorkload:
@@ -376,16 +389,14 @@ def run_frame_gpu(args, world, rank, local):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        # pass 1: the per-call API with per-stage device timing (stage rooflines)
+        # pass 1: the frame's kernels launched directly (the graph's launch sequence without the graph)
+        # with CUDA events between the stages on the library's stream: the per-stage rooflines
+        r.set_frame_graph(False)
         for step, f in enumerate(work.frames):
             timed = step >= args.warmup
             with torch.cuda.stream(stream):
                 flush.fill_(1.0)
-            r.frame_begin(f["params"], f["lights"])
-            r.submit_surfaces(f["surfaces"], f["total_texels"])
-            r.submit_draws(f["draws"], f["vertices"])
-            r.render()
-            r.postprocess(work.config, 1.0 / 60.0, (1.0, 1.0, 1.0), device_ptr=ldr_frames[step].data_ptr(), pitch=W)
+            r.draw_frame(frame_input(step, f))
             t = r.timings()
             if timed:
                 totals["surf"] += t[0]
@@ -394,10 +405,11 @@ def run_frame_gpu(args, world, rank, local):
                 frame_span += t[4]
                 texels += f["total_texels"]
                 surf_bytes += work.surface_bytes(f)
-                launches += 1 + 3 + 3  # surfaces; raster walk, rows, tiles; postprocess (3 kernels)
+                launches += FRAME_LAUNCHES
             if step == args.warmup - 1:
                 pix_before = r.stats().pixel_writes
         pix_writes = r.stats().pixel_writes - pix_before
+        r.set_frame_graph(True)
         # pass 2 (the measurement): the same frames through sw_draw_frame, one CUDA graph per frame;
         # device time of the whole graph (uploads, surfaces, raster setup + tiles, postprocess, readback)
         r.set_exposure(1.0)
@@ -409,7 +421,7 @@ def run_frame_gpu(args, world, rank, local):
             t = r.timings()
             if step >= args.warmup:
                 graph_ms.append(t[4])
-                launches += 1 + 3 + 3
+                launches += FRAME_LAUNCHES
         torch.cuda.synchronize()
     gpu_ldr = ldr_frames[:4].cpu().numpy().view(np.uint32).copy()  # for the parity check against the oracle
     stage_sum_ms = (totals["surf"] + totals["raster"] + totals["post"]) / args.steps
@@ -455,14 +467,14 @@ def run_frame_gpu(args, world, rank, local):
 
     lr = run_learned(args, work, r, ldr_frames, local) if args.learn_steps > 0 else None
     if lr is not None:
-        launches += args.steps * (1 + 3 + 3 + 1)  # half-resolution frame + the fused upscale kernel
+        launches += args.steps * (FRAME_LAUNCHES + 1)  # half-resolution frame + the fused upscale kernel
     lr_small = run_learned_small_map(args, local) if args.learn_steps > 0 else None
 
     peak, peak_kind = peaks()
     s = args.steps
     stage_bytes = {
         "surf": surf_bytes / s,
-        "raster": (pix_writes / s) * 8 + W * H * 8 * 2,
+        "raster": raster_bytes(pix_writes / s, W, H),
         "post": post_bytes(W, H),
     }
     stages = {}
@@ -472,8 +484,8 @@ def run_frame_gpu(args, world, rank, local):
         stages[k] = {"ms": round(ms_per, 4), "algorithmic_bytes": int(stage_bytes[k]), "GB/s": round(gbs, 1),
                      "frac_of_measured_hbm": round(gbs / peak, 4)}
     dom = max(totals, key=totals.get)
-    kernel_names = {"surf": "surf_build_kernel", "raster": "raster_setup_kernel + raster_tiles_kernel",
-                    "post": "pp_downscale_blur_h + pp_blur_v_tonemap"}
+    kernel_names = {"surf": "surf_build_kernel", "raster": "raster_tiles_kernel (bloom downscale in its epilogue)",
+                    "post": "pp_blur_tonemap_kernel (+ pp_average_bloom_kernel beside it)"}
     out_line = None
     if rank == 0:
         cpu, parity = cpu_frame_baseline(work, gpu_ldr=gpu_ldr)

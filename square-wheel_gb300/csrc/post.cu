@@ -5,9 +5,10 @@
 // Gaussian blur (:846-956), Reinhard tonemapping with nearest or linear bloom (:226-726, :997-1024);
 // and FrameUpscaler::perform_upscale (src/square_wheel/frame_upscaler.rs:42-239).
 //
-// With bloom the frame takes two streaming launches: downscale + horizontal blur (one block per bloom
-// line, the downscaled line kept in shared memory) and vertical blur + tonemap (one block per output
-// tile, the bloom cells it samples blurred in shared memory), plus the exposure average on the side.
+// With bloom the frame takes at most two streaming launches: the downscale (one block per bloom line;
+// in a whole-frame graph the raster tile pass does it instead) and blur + tonemap (one block per output
+// tile, the bloom cells it samples blurred in both directions in shared memory), plus the exposure
+// average on the side.
 // Integer sums use wrapping 32-bit adds, which are associative, so the per-line sums can be reduced in
 // any order and remain bit-exact; the single float reduction over lines (sum of line sums, in line
 // order) runs in one thread exactly as the reference's sequential loop does.
@@ -143,17 +144,20 @@ __device__ __forceinline__ CV bloom_sum(const PostArgs& a, const Bloom& bl, uint
 	return sum;
 }
 
-// ---- fused bloom passes: two launches instead of downscale, blur h, blur v, tonemap ----
+// ---- bloom passes: downscale, then blur + tonemap ----
 //
-// pp_downscale_blur_h_kernel: one block per bloom line. The S lines of HDR pixels are box-averaged into
-// the line (downscale_hdr_buffer, postprocessor.rs:792-844) in shared memory, the line's exact integer
-// lane sums are written for the exposure average (no atomics: the block owns the line), and the
-// horizontal blur pass (:862-900) runs from shared memory into bloom1. The downscaled line never goes
-// to HBM. With radius 0 (no blur) the downscaled line itself is written.
+// In a whole-frame graph the raster tile pass writes the downscaled bloom buffer and the exact per-line
+// sums itself (its epilogue box-averages the tile's final pixels), so the frame's postprocess is one
+// launch over the HDR frame: pp_blur_tonemap_kernel. A frame that did not come from the tile pass
+// (sw_set_framebuffer, the allocation-free entry point, per-call sw_render + sw_postprocess) gets
+// pp_downscale_kernel first.
+//
+// pp_downscale_kernel: one block per bloom line. The S lines of HDR pixels are box-averaged into the
+// line (downscale_hdr_buffer, postprocessor.rs:792-844), written to bloom0, and the line's exact integer
+// lane sums are written for the exposure average (no atomics: the block owns the line).
 template <int S>
-__global__ void __launch_bounds__(256) pp_downscale_blur_h_kernel(PostArgs a)
+__global__ void __launch_bounds__(256) pp_downscale_kernel(PostArgs a)
 {
-	extern __shared__ __align__(16) uint64_t s_line[]; // bw packed Color64 bloom pixels
 	__shared__ int32_t s_sum[8][4];
 	const uint32_t by = blockIdx.x;
 	pdl_wait(); // the frame's rasterisation has completed
@@ -162,6 +166,7 @@ __global__ void __launch_bounds__(256) pp_downscale_blur_h_kernel(PostArgs a)
 	constexpr int U = S == 2 ? 4 : S == 4 ? 2 : 1;
 	const unsigned long long* hdr = reinterpret_cast<const unsigned long long*>(a.hdr);
 	const bool vec = ((a.width & 1) == 0) && ((reinterpret_cast<uintptr_t>(a.hdr) & 15) == 0); // 16-byte pairs
+	uint64_t* out = a.bloom0 + uint64_t(by) * a.bw;
 	int32_t lsum[4] = {0, 0, 0, 0};
 	for (uint32_t base = threadIdx.x; base < a.bw; base += blockDim.x * U)
 	{
@@ -214,7 +219,7 @@ __global__ void __launch_bounds__(256) pp_downscale_blur_h_kernel(PostArgs a)
 				avg.v[i] = wmul(sum[i], scaler) >> 8;
 				lsum[i] = wadd(lsum[i], avg.v[i]);
 			}
-			s_line[bx] = ci_to_c64(avg);
+			out[bx] = ci_to_c64(avg);
 		}
 	}
 	// exact per-line sums of the averages (wrapping i32: order-independent)
@@ -233,35 +238,15 @@ __global__ void __launch_bounds__(256) pp_downscale_blur_h_kernel(PostArgs a)
 		for (int w = 0; w < int(blockDim.x >> 5); ++w) t = wadd(t, s_sum[w][threadIdx.x]);
 		a.line_sums[by * 4 + threadIdx.x] = t;
 	}
-	const int32_t r = int32_t(a.radius);
-	uint64_t* out = a.bloom1 + uint64_t(by) * a.bw;
-	for (int32_t x = int32_t(threadIdx.x); x < int32_t(a.bw); x += int32_t(blockDim.x))
-	{
-		if (r == 0)
-		{
-			out[x] = s_line[x];
-			continue;
-		}
-		const CI c = ci_from_c64(s_line[x]);
-		int32_t sum[4];
-#pragma unroll
-		for (int i = 0; i < 4; ++i) sum[i] = wmul(c.v[i], a.kernel_h[r]);
-		for (int32_t dx = 1; dx <= r; ++dx)
-		{
-			const CI c0 = ci_from_c64(s_line[max(x - dx, 0)]);
-			const CI c1 = ci_from_c64(s_line[min(x + dx, int32_t(a.bw) - 1)]);
-#pragma unroll
-			for (int i = 0; i < 4; ++i) sum[i] = wadd(sum[i], wmul(wadd(c0.v[i], c1.v[i]), a.kernel_h[dx + r]));
-		}
-		out[x] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
-	}
 	pdl_trigger();
 }
 
-// pp_blur_v_tonemap_kernel: one block per TM_W x TM_H tile of the output. It stages the h-blurred bloom
-// lines its tile needs (the bloom cells its pixels sample, +-radius lines) in shared memory, runs the
-// vertical blur pass (:902-955, bloom_scale folded into the weights) for those cells, then tonemaps its
-// pixels with the nearest or linear bloom sample (:346-726) read from shared memory.
+// pp_blur_tonemap_kernel: one block per TM_W x TM_H tile of the output. It stages the downscaled bloom
+// cells its tile needs (the cells its pixels sample, +-radius cells in both directions, source indices
+// clamped to the buffer as the reference's blur clamps them) in shared memory, runs the horizontal
+// (postprocessor.rs:862-900) and the vertical blur pass (:902-955, bloom_scale folded into the weights)
+// for those cells, then tonemaps its pixels with the nearest or linear bloom sample (:346-726) read from
+// shared memory. With radius 0 the downscaled cells are sampled directly (no blur pass).
 constexpr uint32_t TM_W = 256, TM_H = 16;
 
 template <int S>
@@ -275,30 +260,32 @@ __host__ __device__ __forceinline__ void bloom_tile_range(uint32_t p0, uint32_t 
 template <int S>
 __host__ __device__ __forceinline__ uint32_t tonemap_tile_smem(uint32_t radius)
 {
-	// cells: (TM_W / S + 3) columns x (TM_H / S + 3) lines, staged lines + 2 radius more
-	const uint32_t cols = TM_W / S + 3, lines = TM_H / S + 3;
-	return (cols * (lines + 2 * radius) + cols * lines) * 8u;
+	// at most (TM_W / S + 3) columns x (TM_H / S + 3) lines of cells: the staged cells with a radius
+	// halo on every side, the horizontally blurred lines (halo lines only) and the blurred cells
+	const uint32_t cols = TM_W / S + 3, lines = TM_H / S + 3, r2 = 2 * radius;
+	return ((lines + r2) * (cols + r2) + (lines + r2) * cols + lines * cols) * 8u;
 }
 
 template <int S, bool LINEAR>
-__global__ void __launch_bounds__(256) pp_blur_v_tonemap_kernel(PostArgs a)
+__global__ void __launch_bounds__(256) pp_blur_tonemap_kernel(PostArgs a)
 {
 	extern __shared__ __align__(16) uint64_t s_tile[];
 	const uint32_t x0 = blockIdx.x * TM_W, y0 = blockIdx.y * TM_H;
-	pdl_wait(); // the downscale + horizontal blur pass has completed
+	pdl_wait(); // the downscale (the raster tile pass or pp_downscale_kernel) has completed
 	const uint32_t tw = min(TM_W, a.width - x0), th = min(TM_H, a.height - y0);
 	uint32_t cx0, cx1, cy0, cy1;
 	bloom_tile_range<S>(x0, tw, a.bw, cx0, cx1);
 	bloom_tile_range<S>(y0, th, a.bh, cy0, cy1);
 	const uint32_t cols = cx1 - cx0 + 1, lines = cy1 - cy0 + 1;
 	const int32_t r = int32_t(a.radius);
-	// staged h-blurred lines cy0 - r .. cy1 + r (clamped to the buffer when read)
-	const uint32_t staged = lines + 2 * uint32_t(r);
-	uint64_t* s_h = s_tile;
-	uint64_t* s_v = s_tile + staged * cols;
+	const uint32_t slines = lines + 2 * uint32_t(r), scols = cols + 2 * uint32_t(r);
+	uint64_t* s_b = s_tile;                              // slines x scols downscaled cells
+	uint64_t* s_h = s_b + slines * scols;                // slines x cols, horizontally blurred
+	uint64_t* s_v = r ? s_h + slines * cols : s_b;       // lines x cols, the cells the pixels sample
 	{
-		// four loads in flight per thread
-		const uint32_t total = staged * cols;
+		// four loads in flight per thread; staged cell (l, c) is cell (clamp(cy0 - r + l), clamp(cx0 - r + c))
+		const uint32_t total = slines * scols;
+		const unsigned long long* src = reinterpret_cast<const unsigned long long*>(a.bloom0);
 		for (uint32_t i0 = threadIdx.x; i0 < total; i0 += 4 * blockDim.x)
 		{
 			unsigned long long v[4];
@@ -308,40 +295,58 @@ __global__ void __launch_bounds__(256) pp_blur_v_tonemap_kernel(PostArgs a)
 				const uint32_t i = i0 + k * blockDim.x;
 				if (i < total)
 				{
-					const uint32_t l = i / cols, c = i % cols;
+					const uint32_t l = i / scols, c = i % scols;
 					const int32_t by = min(max(int32_t(cy0) - r + int32_t(l), 0), int32_t(a.bh) - 1);
-					v[k] = __ldg(reinterpret_cast<const unsigned long long*>(a.bloom1) + uint64_t(by) * a.bw + cx0 + c);
+					const int32_t bx = min(max(int32_t(cx0) - r + int32_t(c), 0), int32_t(a.bw) - 1);
+					v[k] = __ldg(src + uint64_t(by) * a.bw + uint32_t(bx));
 				}
 			}
 #pragma unroll
 			for (int k = 0; k < 4; ++k)
-				if (i0 + k * blockDim.x < total) s_h[i0 + k * blockDim.x] = v[k];
+				if (i0 + k * blockDim.x < total) s_b[i0 + k * blockDim.x] = v[k];
 		}
 	}
 	__syncthreads();
-	for (uint32_t i = threadIdx.x; i < lines * cols; i += blockDim.x)
+	if (r)
 	{
-		const uint32_t l = i / cols, c = i % cols;
-		if (r == 0)
+		// horizontal pass over every staged line: cell c of the tile sits at staged column c + r
+		for (uint32_t i = threadIdx.x; i < slines * cols; i += blockDim.x)
 		{
-			s_v[i] = s_h[l * cols + c];
-			continue;
-		}
-		// line cy0 + l is staged at l + r; its neighbours at l + r -+ dy (clamping already applied)
-		const CI cc = ci_from_c64(s_h[(l + r) * cols + c]);
-		int32_t sum[4];
+			const uint32_t l = i / cols, c = i % cols;
+			const uint64_t* line = s_b + l * scols + c + uint32_t(r);
+			const CI cc = ci_from_c64(line[0]);
+			int32_t sum[4];
 #pragma unroll
-		for (int k = 0; k < 4; ++k) sum[k] = wmul(cc.v[k], a.kernel_v[r]);
-		for (int32_t dy = 1; dy <= r; ++dy)
+			for (int k = 0; k < 4; ++k) sum[k] = wmul(cc.v[k], a.kernel_h[r]);
+			for (int32_t dx = 1; dx <= r; ++dx)
+			{
+				const CI c0 = ci_from_c64(line[-dx]);
+				const CI c1 = ci_from_c64(line[dx]);
+#pragma unroll
+				for (int k = 0; k < 4; ++k) sum[k] = wadd(sum[k], wmul(wadd(c0.v[k], c1.v[k]), a.kernel_h[dx + r]));
+			}
+			s_h[i] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
+		}
+		__syncthreads();
+		// vertical pass: line cy0 + l is staged at l + r
+		for (uint32_t i = threadIdx.x; i < lines * cols; i += blockDim.x)
 		{
-			const CI c0 = ci_from_c64(s_h[(l + r - dy) * cols + c]);
-			const CI c1 = ci_from_c64(s_h[(l + r + dy) * cols + c]);
+			const uint32_t l = i / cols, c = i % cols;
+			const CI cc = ci_from_c64(s_h[(l + r) * cols + c]);
+			int32_t sum[4];
 #pragma unroll
-			for (int k = 0; k < 4; ++k) sum[k] = wadd(sum[k], wmul(wadd(c0.v[k], c1.v[k]), a.kernel_v[dy + r]));
+			for (int k = 0; k < 4; ++k) sum[k] = wmul(cc.v[k], a.kernel_v[r]);
+			for (int32_t dy = 1; dy <= r; ++dy)
+			{
+				const CI c0 = ci_from_c64(s_h[(l + r - dy) * cols + c]);
+				const CI c1 = ci_from_c64(s_h[(l + r + dy) * cols + c]);
+#pragma unroll
+				for (int k = 0; k < 4; ++k) sum[k] = wadd(sum[k], wmul(wadd(c0.v[k], c1.v[k]), a.kernel_v[dy + r]));
+			}
+			s_v[i] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
 		}
-		s_v[i] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
+		__syncthreads();
 	}
-	__syncthreads();
 	const BloomTile tile{s_v, cx0, cy0, cols};
 	// 4 horizontally adjacent pixels per thread: 64 threads per 256-pixel line, lines ly, ly + 4, ... of
 	// the tile (TM_H / 4 of them), their HDR loads all issued first
@@ -508,30 +513,25 @@ int allow_smem(K kernel, uint32_t bytes)
 }
 
 template <int S>
-int launch_fused_bloom(const PostArgs& a, cudaStream_t stream, bool first)
+int launch_bloom_pass(const PostArgs& a, cudaStream_t stream, bool downscale)
 {
-	if (first)
-	{
-		const uint32_t smem = a.bw * 8;
-		if (int e = allow_smem(pp_downscale_blur_h_kernel<S>, smem)) return e;
-		return int(launch_dependent(pp_downscale_blur_h_kernel<S>, dim3(a.bh), dim3(256), smem, stream, a));
-	}
+	if (downscale) return int(launch_dependent(pp_downscale_kernel<S>, dim3(a.bh), dim3(256), 0, stream, a));
 	const uint32_t smem = tonemap_tile_smem<S>(a.radius);
 	const dim3 grid((a.width + TM_W - 1) / TM_W, (a.height + TM_H - 1) / TM_H);
 	if (a.linear_filter)
 	{
-		if (int e = allow_smem(pp_blur_v_tonemap_kernel<S, true>, smem)) return e;
-		return int(launch_dependent(pp_blur_v_tonemap_kernel<S, true>, grid, dim3(256), smem, stream, a));
+		if (int e = allow_smem(pp_blur_tonemap_kernel<S, true>, smem)) return e;
+		return int(launch_dependent(pp_blur_tonemap_kernel<S, true>, grid, dim3(256), smem, stream, a));
 	}
-	if (int e = allow_smem(pp_blur_v_tonemap_kernel<S, false>, smem)) return e;
-	return int(launch_dependent(pp_blur_v_tonemap_kernel<S, false>, grid, dim3(256), smem, stream, a));
+	if (int e = allow_smem(pp_blur_tonemap_kernel<S, false>, smem)) return e;
+	return int(launch_dependent(pp_blur_tonemap_kernel<S, false>, grid, dim3(256), smem, stream, a));
 }
 
-int launch_fused(const PostArgs& a, cudaStream_t stream, bool first)
+int launch_bloom(const PostArgs& a, cudaStream_t stream, bool downscale)
 {
-	return a.scale == 2 ? launch_fused_bloom<2>(a, stream, first)
-		: a.scale == 4  ? launch_fused_bloom<4>(a, stream, first)
-						: launch_fused_bloom<8>(a, stream, first);
+	return a.scale == 2 ? launch_bloom_pass<2>(a, stream, downscale)
+		: a.scale == 4  ? launch_bloom_pass<4>(a, stream, downscale)
+						: launch_bloom_pass<8>(a, stream, downscale);
 }
 
 } // namespace
@@ -545,8 +545,9 @@ int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream, cuda
 	{
 		if (a.scale != 2 && a.scale != 4 && a.scale != 8) return int(cudaErrorInvalidValue);
 		if (a.radius > 16 || a.bw == 0 || a.bh == 0) return int(cudaErrorInvalidValue);
-		// downscale + horizontal blur (writes every line's exact lane sums)
-		if (int e = launch_fused(a, stream, true)) return e;
+		// the downscale (bloom0 and every line's exact lane sums), unless the raster tile pass wrote them
+		if (!a.downscaled)
+			if (int e = launch_bloom(a, stream, true)) return e;
 		// The exposure average is consumed only after the frame: with an auxiliary stream it runs
 		// beside the vertical blur and tonemap pass.
 		const bool overlap = aux && fork && join;
@@ -557,8 +558,8 @@ int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream, cuda
 		}
 		pp_average_bloom_kernel<<<1, 256, 0, overlap ? aux : stream>>>(a);
 		if (overlap) cudaEventRecord(join, aux);
-		// vertical blur + tonemap with the bloom sample
-		if (int e = launch_fused(a, stream, false)) return e;
+		// blur + tonemap with the bloom sample
+		if (int e = launch_bloom(a, stream, false)) return e;
 		if (overlap) cudaStreamWaitEvent(stream, join, 0);
 	}
 	else

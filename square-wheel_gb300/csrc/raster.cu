@@ -416,6 +416,58 @@ __device__ __forceinline__ uint64_t pixel_address(const RasterRow& r, uint32_t m
 
 constexpr int BATCH = 32; // draws whose tile rows are staged in shared memory at a time
 
+// The bloom downscale of a tile's final colour64 pixels (downscale_hdr_buffer, postprocessor.rs:792-844):
+// the pixels go to shared memory (the row staging area, free once the draws are done), each bloom cell
+// whose S x S source pixels lie in the tile gets their box average (i32 lanes, (sum * (256 / S^2)) >> 8),
+// and the tile's part of each bloom line's lane sums is added to the line's global sums. The sums are
+// wrapping i32 additions, associative and commutative, so the atomics keep them exact in any order.
+// Every tile shape is a multiple of 8 pixels on both sides, so no cell straddles two tiles.
+template <int TILE_W, int TILE_H, int STRIP>
+__device__ __forceinline__ void bloom_epilogue(const RasterArgs& a, const uint64_t* pix, int tx0, int ty0, int tid, void* staging)
+{
+	constexpr int TPR = TILE_W / STRIP;
+	static_assert(TILE_W % 8 == 0 && TILE_H % 8 == 0, "bloom cells must not straddle tiles");
+	static_assert(size_t(TILE_W) * TILE_H * 8 <= sizeof(RasterRow) * BATCH * TILE_H, "tile pixels fit the row staging");
+	__shared__ int32_t s_ls[TILE_H / 2][4];
+	uint64_t* s_pix = static_cast<uint64_t*>(staging);
+	__syncthreads(); // the row staging area is free
+	{
+		const int ly = tid / TPR, lx = (tid % TPR) * STRIP;
+#pragma unroll
+		for (int k = 0; k < STRIP; ++k) s_pix[ly * TILE_W + lx + k] = pix[k];
+	}
+	for (int i = tid; i < (TILE_H / 2) * 4; i += 256) (&s_ls[0][0])[i] = 0;
+	__syncthreads();
+	const int S = int(a.bloom_scale);
+	const int cw = TILE_W / S, ch = TILE_H / S;
+	const int32_t scaler = 256 / (S * S);
+	const uint32_t bx0 = uint32_t(tx0 / S), by0 = uint32_t(ty0 / S);
+	for (int i = tid; i < cw * ch; i += 256)
+	{
+		const int cx = i % cw, cy = i / cw;
+		if (bx0 + cx >= a.bloom_w || by0 + cy >= a.bloom_h) continue;
+		int32_t sum[4] = {0, 0, 0, 0};
+		for (int dy = 0; dy < S; ++dy)
+			for (int dx = 0; dx < S; ++dx)
+			{
+				const CI c = ci_from_c64(s_pix[(cy * S + dy) * TILE_W + cx * S + dx]);
+#pragma unroll
+				for (int l = 0; l < 4; ++l) sum[l] = wadd(sum[l], c.v[l]);
+			}
+		CI avg;
+#pragma unroll
+		for (int l = 0; l < 4; ++l)
+		{
+			avg.v[l] = wmul(sum[l], scaler) >> 8;
+			atomicAdd(&s_ls[cy][l], avg.v[l]);
+		}
+		a.bloom_out[uint64_t(by0 + cy) * a.bloom_w + bx0 + cx] = ci_to_c64(avg);
+	}
+	__syncthreads();
+	if (tid < ch * 4 && by0 + uint32_t(tid / 4) < a.bloom_h)
+		atomicAdd(&a.bloom_line_sums[(by0 + tid / 4) * 4 + tid % 4], s_ls[tid / 4][tid % 4]);
+}
+
 // Tile shapes of the tile pass (the autotuner's choice, SwTuning.raster_tile): TILE_W x TILE_H pixels,
 // 256 threads, each thread a 1 x STRIP strip of one row. Every shape gives the same frame.
 struct TileShape
@@ -433,7 +485,7 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 	__shared__ uint32_t s_warp_counts[8];
 	__shared__ RasterDraw s_rd[256];
 	__shared__ RasterBox s_box[256];
-	__shared__ RasterRow s_row[BATCH][TILE_H];
+	__shared__ __align__(16) RasterRow s_row[BATCH][TILE_H]; // also the bloom epilogue's pixel staging (8-byte lanes)
 
 	const int tiles_x = (a.width + TILE_W - 1) / TILE_W;
 	const int tx0 = int(blockIdx.x % tiles_x) * TILE_W;
@@ -563,6 +615,8 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 		for (int k = 0; k < STRIP; ++k)
 			if (xb + k < a.width) fb[uint64_t(y) * a.width + xb + k] = pix[k];
 	}
+	if constexpr (P::FORMAT == SW_PIXEL_C64)
+		if (a.bloom_scale) bloom_epilogue<TILE_W, TILE_H, STRIP>(a, pix, tx0, ty0, tid, &s_row[0][0]);
 	if (local_errors) atomicAdd(a.error_counter, local_errors);
 	// Pixel writes (span pixels processed) for the traffic accounting, one atomic per warp.
 	for (int o = 16; o > 0; o >>= 1) local_writes += __shfl_xor_sync(0xFFFFFFFFu, local_writes, o);

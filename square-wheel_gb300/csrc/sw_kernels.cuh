@@ -228,6 +228,13 @@ struct RasterArgs
 	const void* skybox; // skybox texels of the frame's pixel format (SW_TEXSRC_SKYBOX draws)
 	void* framebuffer;  // width * height pixels, tightly packed
 	unsigned int* error_counter;
+	// Bloom downscale fused into the tile pass (colour64 frames of a whole-frame graph): with
+	// bloom_scale S != 0 each tile box-averages its final pixels into the bloom buffer (bloom_w x
+	// bloom_h cells, downscale_hdr_buffer, postprocessor.rs:792-844) and adds its part of every bloom
+	// line's exact integer lane sums to bloom_line_sums (zeroed before the pass).
+	uint64_t* bloom_out;
+	int32_t* bloom_line_sums;
+	uint32_t bloom_scale, bloom_w, bloom_h;
 };
 
 // Edge walk + row setup (raster_setup, one CTA per draw), then the tile pass (raster_tiles).
@@ -383,6 +390,7 @@ struct PostArgs
 	float inv_255[4];
 	uint32_t linear_filter;
 	uint32_t use_bloom;
+	uint32_t downscaled; // bloom0 and line_sums were written by the raster tile pass (RasterArgs::bloom_*)
 	uint32_t* dst;
 	uint32_t dst_pitch;
 };

@@ -437,14 +437,6 @@ int check_frame_inputs(SwCtx* ctx, const SwFrameParams& p, const SwLight* lights
 	return SW_OK;
 }
 
-// f32 -> i32 `as` conversion: truncating, saturating, NaN -> 0.
-int32_t f2i32_sat(float x)
-{
-	if (x != x) return 0;
-	if (x >= 2147483648.0f) return INT32_MAX;
-	if (x <= -2147483648.0f) return INT32_MIN;
-	return int32_t(x);
-}
 
 // Apply the exposure update of the previous postprocessed frame (update_exposure,
 // src/square_wheel/postprocessor.rs:206-223, with get_color_brightness :1047-1051), on the host in f32
@@ -1169,19 +1161,22 @@ namespace
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // sw_draw_frame without a graph: the per-call API in order.
-int draw_frame_direct(SwCtx* ctx, const SwFrameInput& f)
+// Device work of one graph frame, issued on the context's streams while they are being captured.
+// A graph frame with bloom: the raster tile pass writes the downscaled bloom buffer and the per-line
+// sums (zeroed here, on the stream, before the pass), and the postprocess starts at the blur.
+int fuse_bloom_downscale(SwCtx* ctx, RasterArgs& ra, PostArgs& pa, cudaStream_t s)
 {
-	int r;
-	if ((r = sw_frame_begin(ctx, &f.params, f.lights, f.num_lights))) return r;
-	if ((r = sw_submit_surfaces(ctx, f.surfaces, f.num_surfaces, f.total_texels))) return r;
-	if ((r = sw_submit_draws(ctx, f.draws, f.num_draws, f.vertices, f.num_vertices))) return r;
-	if (!f.postprocess) return sw_render(ctx, f.dst, f.dst_pitch, f.dst_is_device);
-	if ((r = sw_render(ctx, nullptr, 0, 0))) return r;
-	if (!f.dst) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocess needs a destination");
-	return sw_postprocess(ctx, &f.post, f.frame_duration_s, f.color_modulate, f.dst, f.dst_pitch, f.dst_is_device);
+	if (!pa.use_bloom) return SW_OK;
+	SW_CUDA(ctx, cudaMemsetAsync(pa.line_sums, 0, size_t(pa.bh) * 16, s));
+	ra.bloom_out = pa.bloom0;
+	ra.bloom_line_sums = pa.line_sums;
+	ra.bloom_scale = pa.scale;
+	ra.bloom_w = pa.bw;
+	ra.bloom_h = pa.bh;
+	pa.downscaled = 1;
+	return SW_OK;
 }
 
-// Device work of one graph frame, issued on the context's streams while they are being captured.
 int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, const size_t* off, uint64_t rows,
 	const PostArgs* post)
 {
@@ -1203,12 +1198,23 @@ int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, con
 		reinterpret_cast<const uint64_t*>(d + off[2])};
 	if ((r = launch_surfaces(ctx, &si))) return r;
 	SW_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_setup, 0));
-	if ((r = check_kernel(ctx, launch_raster_tiles(ra, f.params.pixel_format, ctx->tuning.raster_tile, s), "raster"))) return r;
+	PostArgs pp;
+	if (post)
+	{
+		pp = *post;
+		if ((r = fuse_bloom_downscale(ctx, ra, pp, s))) return r;
+	}
+	stage_begin(ctx, STAGE_RASTER);
+	r = check_kernel(ctx, launch_raster_tiles(ra, f.params.pixel_format, ctx->tuning.raster_tile, s), "raster");
+	stage_end(ctx, STAGE_RASTER);
+	if (r) return r;
 	(void)rows;
 	if (post)
 	{
-		if ((r = check_kernel(ctx, launch_postprocess(*post, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join), "postprocess")))
-			return r;
+		stage_begin(ctx, STAGE_POST);
+		r = check_kernel(ctx, launch_postprocess(pp, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join), "postprocess");
+		stage_end(ctx, STAGE_POST);
+		if (r) return r;
 		SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_average, ctx->average.ptr, 16, cudaMemcpyDeviceToHost, s));
 	}
 	else if (f.dst && f.dst_is_device)
@@ -1372,7 +1378,6 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	if (f.postprocess && f.params.pixel_format != SW_PIXEL_C64)
 		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocessing needs a colour64 frame");
 	if (f.dst && f.dst_pitch < f.params.width) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");
-	if (!ctx->graph_enabled) return draw_frame_direct(ctx, f);
 	int r;
 	const SwFrameParams& p = f.params;
 	if ((r = check_frame_params(ctx, p, f.lights, f.num_lights))) return r;
@@ -1425,9 +1430,20 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 		(r = frame_post_target(ctx, p, f.post, f.color_modulate, f.dst, f.dst_pitch, f.dst_is_device, pa, &post_out, &direct_host)))
 		return r;
 
-	// 3. capture the device work and update (or instantiate) the frame graph
-	if ((r = capture_and_launch(ctx, ctx->gexec, [&]() { return enqueue_frame(ctx, f, h, off, rows, f.postprocess ? &pa : nullptr); })))
-		return r;
+	// 3. capture the device work and update (or instantiate) the frame graph; with the graph off, the
+	// same work is launched directly (with per-stage timing events when timing is on)
+	auto enqueue = [&]() { return enqueue_frame(ctx, f, h, off, rows, f.postprocess ? &pa : nullptr); };
+	if (ctx->graph_enabled)
+	{
+		if ((r = capture_and_launch(ctx, ctx->gexec, enqueue))) return r;
+	}
+	else
+	{
+		stage_begin(ctx, STAGE_FRAME);
+		r = enqueue();
+		stage_end(ctx, STAGE_FRAME);
+		if (r) return r;
+	}
 	ctx->stats.draws += f.num_draws; // (surfaces are counted by launch_surfaces)
 	ctx->stats.upload_bytes += off[6];
 	return finish_graph_frame(ctx, st, p, f.postprocess != 0, f.post, f.frame_duration_s, f.dst, f.dst_pitch, f.dst_is_device,
@@ -1849,11 +1865,14 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 					 "surface build")))
 				return rr;
 			SW_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_setup, 0));
-			if ((rr = check_kernel(ctx, launch_raster_tiles(key.raster, p.pixel_format, ctx->tuning.raster_tile, s), "raster")))
+			RasterArgs ra2 = key.raster;
+			PostArgs pp2 = key.post;
+			if (f.postprocess && (rr = fuse_bloom_downscale(ctx, ra2, pp2, s))) return rr;
+			if ((rr = check_kernel(ctx, launch_raster_tiles(ra2, p.pixel_format, ctx->tuning.raster_tile, s), "raster")))
 				return rr;
 			if (f.postprocess)
 			{
-				if ((rr = check_kernel(ctx, launch_postprocess(key.post, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join),
+				if ((rr = check_kernel(ctx, launch_postprocess(pp2, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join),
 						 "postprocess")))
 					return rr;
 			}
