@@ -689,6 +689,7 @@ def run_surfaces_gpu(args, world, rank, local):
     r.enable_timing(True)
     stream = torch.cuda.ExternalStream(r.stream_handle())
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    # the persistent launch replayed as a CUDA graph (sw_rebuild_surfaces with the graph setting on)
     for _ in range(args.warmup):
         r.rebuild_surfaces()
     total = 0.0
@@ -700,6 +701,17 @@ def run_surfaces_gpu(args, world, rank, local):
             total += r.timings()[0]
     ms = max_over_ranks(total / args.steps, world, f"cuda:{local}")
     value = world * b.total_texels / 1e6 / (ms / 1e3)
+    gpu_arena = r.read_surfaces(b.total_texels, b.pixel_format)
+    # the baseline it is compared against: one launch per surface, same arena
+    r.rebuild_surfaces_per_surface()
+    per_surface_ms = []
+    for _ in range(min(args.steps, 5)):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        r.rebuild_surfaces_per_surface()
+        per_surface_ms.append(r.timings()[0])
+    per_ms = statistics.mean(per_surface_ms)
+    same = bool(np.array_equal(gpu_arena, r.read_surfaces(b.total_texels, b.pixel_format)))
     e2e = []
     for _ in range(3):
         t0 = time.perf_counter()
@@ -711,13 +723,19 @@ def run_surfaces_gpu(args, world, rank, local):
     alg = b.algorithmic_bytes()
     gbs = alg / (ms / 1e3) / 1e9
     if rank == 0:
-        cpu = cpu_surfaces_baseline(work)
+        cpu, parity = cpu_surfaces_baseline(work, gpu_arena)
         print(json.dumps({
             "metric": METRIC, "value": round(value, 2), "unit": "Mtexels/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": work.name, "texels_per_step": int(b.total_texels),
+                       "materials": "25% metal / 25% dielectric specular, normal maps; no dynamic lights",
+                       "timing": "CUDA events around the replayed graph of the persistent surface launch",
                        "l2": "flushed (512 MiB write) before every timed step", "parallelism": f"replicas x{world}"},
+            "per_surface_launches": {"ms": round(per_ms, 4), "mtexels_per_s": round(b.total_texels / 1e3 / per_ms, 1),
+                                     "persistent_speedup": round(per_ms / ms, 2), "same_arena": same,
+                                     "what": f"{b.surfaces.size} launches, one per surface (sw_rebuild_surfaces_per_surface)"},
+            "parity": parity,
             "roofline": {"bound": "hbm", "kernel": "surf_build_kernel", "achieved": round(gbs, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(gbs / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
                          "algorithmic_bytes_per_launch": int(alg), "traffic": None},
@@ -729,7 +747,10 @@ def run_surfaces_gpu(args, world, rank, local):
     r.close()
 
 
-def cpu_surfaces_baseline(work):
+def cpu_surfaces_baseline(work, gpu_arena=None):
+    """The oracle's surface build of the first surfaces (an eighth of the texels) on all host threads;
+    with gpu_arena, its texels are compared with the GPU's for those surfaces (the arena lays surfaces
+    out in order). Returns (baseline, parity or None)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from sqwheel import gpu
@@ -744,10 +765,14 @@ def cpu_surfaces_baseline(work):
     fp = gpu.frame_params(64, 64, b.pixel_format, b.cam_pos, directional=b.directional)
     static = b.static_data()
     t0 = time.perf_counter()
-    oracle.build_surfaces(static, sub, b.lights, fp, texels, num_threads=threads)
+    want = oracle.build_surfaces(static, sub, b.lights, fp, texels, num_threads=threads)
     dt = time.perf_counter() - t0
-    return {"value": round(texels / dt / 1e6, 2), "unit": "Mtexels/s", "cores": threads, "kind": "port",
+    base = {"value": round(texels / dt / 1e6, 2), "unit": "Mtexels/s", "cores": threads, "kind": "port",
+            "cpu_model": cpu_model(),
             "sample": f"{n} of {b.surfaces.size} surfaces ({texels} texels), oracle with {threads} threads"}
+    if gpu_arena is None:
+        return base, None
+    return base, {"surfaces": n, "texels": texels, "mismatched_texels": int((want != gpu_arena[:texels]).sum())}
 
 
 # ---------------------------------------------------------------------------------------------------------
@@ -975,7 +1000,7 @@ def run_reference(args, world, rank):
         return
     if args.workload == "surfaces":
         work = SurfaceWorkload(seed=3)
-        vals = [cpu_surfaces_baseline(work) for _ in range(args.warmup + args.steps)][args.warmup:]
+        vals = [cpu_surfaces_baseline(work)[0] for _ in range(args.warmup + args.steps)][args.warmup:]
         c = vals[-1]
         v = statistics.median(x["value"] for x in vals)
         unit = "Mtexels/s"

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define SWGPU_ABI_VERSION 1
+#define SWGPU_ABI_VERSION 2
 
 typedef enum SwStatus {
 	SW_OK = 0,
@@ -58,11 +58,14 @@ typedef enum SwBlend {
 	SW_BLEND_ALPHA_BLEND = 4,
 } SwBlend;
 
-/* TetureCoordinatesInterpolationMode, src/square_wheel/rasterizer.rs:4-10. */
+/* TetureCoordinatesInterpolationMode, src/square_wheel/rasterizer.rs:4-10, plus the triangle fill. */
 typedef enum SwRasterMode {
 	SW_RASTER_FULL_PERSPECTIVE = 0,
 	SW_RASTER_LINE_Z_CORRECTED = 1,
 	SW_RASTER_AFFINE = 2,
+	/* Rasterizer::fill_triangle (src/square_wheel/rasterizer.rs:731-1292): a textured triangle with
+	 * per-vertex light (models, decals, sprites); the draw's three vertices are SwTriVertex. */
+	SW_RASTER_TRIANGLE = 3,
 } SwRasterMode;
 
 /* ---- static data, uploaded once (Renderer::new, src/square_wheel/renderer.rs:24-59) ---- */
@@ -166,6 +169,15 @@ typedef struct SwVertex16 {
 	int32_t y;
 } SwVertex16;
 
+/* A projected triangle vertex in 16.16 fixed point (TrianglePointProjected, rasterizer.rs:1492-1498):
+ * screen position, texture coordinates in texels and light (1.0 = 65536, lanes r, g, b). */
+typedef struct SwTriVertex {
+	int32_t x, y;
+	int32_t tc[2];
+	int32_t light[3];
+	int32_t reserved;
+} SwTriVertex;
+
 #define SW_MAX_POLYGON_VERTICES 24 /* MAX_VERTICES, src/square_wheel/renderer_utils.rs:4 */
 
 /* Where a draw's texture lives. */
@@ -173,11 +185,16 @@ typedef enum SwTexSource {
 	SW_TEXSRC_SURFACE = 0, /* a surface of the frame's surface arena (world polygons) */
 	SW_TEXSRC_SKYBOX = 1,  /* a skybox side texture at one mip (draw_skybox, partial_renderer.rs:2311-2448),
 	                       in the texels uploaded by sw_set_skybox */
+	SW_TEXSRC_LITE = 2,    /* a Color32 texture (TextureLite, textures.rs:89-91: model skins, decals, sprites) in
+	                       the pixels uploaded by sw_set_lite_textures; triangle draws only */
 } SwTexSource;
 
 /* One Rasterizer::fill_polygon call (src/square_wheel/rasterizer.rs:35-80) as emitted by
  * draw_polygon (src/square_wheel/partial_renderer.rs:4011-4142). Equations are the ones passed to
- * fill_polygon (already scaled by z_scale for the non-affine modes). */
+ * fill_polygon (already scaled by z_scale for the non-affine modes). With mode SW_RASTER_TRIANGLE it is
+ * one Rasterizer::fill_triangle call instead (draw_view_models, draw_polygon_decals, draw_sprite,
+ * partial_renderer.rs:2284, 2794, 3290): vertex_count 3, first_vertex indexes the SwTriVertex array,
+ * tex_source SW_TEXSRC_LITE, the equations unused. */
 typedef struct SwDrawCmd {
 	uint32_t first_vertex; /* into the SwVertex16 array */
 	uint32_t vertex_count; /* 3..SW_MAX_POLYGON_VERTICES, clockwise */
@@ -238,8 +255,14 @@ int sw_frame_begin(SwCtx* ctx, const SwFrameParams* params, const SwLight* light
 int sw_submit_surfaces(SwCtx* ctx, const SwSurfaceDesc* surfaces, uint32_t num_surfaces, uint64_t total_texels);
 
 /* Build the surfaces of the last sw_submit_surfaces again without re-uploading descriptors (after a
- * sw_frame_begin that changed only the camera position or the lights' parameters). */
+ * sw_frame_begin that changed only the camera position or the lights' parameters): one persistent
+ * launch over all of them, replayed as a CUDA graph while the frame graph setting is on
+ * (sw_set_frame_graph). */
 int sw_rebuild_surfaces(SwCtx* ctx);
+/* The same build as one kernel launch per surface, in descriptor order (the reference's per-polygon
+ * tasks, partial_renderer.rs:1822-1831): the baseline the persistent launch is measured against. The
+ * arena comes out identical. Needs descriptors from sw_submit_surfaces. */
+int sw_rebuild_surfaces_per_surface(SwCtx* ctx);
 
 /* Use a surface arena built elsewhere (host memory, pixel_format of sw_frame_begin) instead of
  * sw_submit_surfaces, e.g. textures the caller prepared itself. */
@@ -265,6 +288,14 @@ int sw_unregister_host_buffer(SwCtx* ctx, void* ptr);
  * partial_renderer.rs:1285-1325, 2311-2559, 4011-4142). */
 int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices,
 	uint32_t num_vertices);
+/* The same with triangle draws among them (SW_RASTER_TRIANGLE: the leaf's decals after its polygons,
+ * then its models and sprites, draw_leaf, partial_renderer.rs:2519-2792), their vertices in tri_vertices. */
+int sw_submit_draws_ex(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices,
+	uint32_t num_vertices, const SwTriVertex* tri_vertices, uint32_t num_tri_vertices);
+/* The Color32 textures triangle draws read (SW_TEXSRC_LITE: model skins, decal and sprite textures with
+ * their mips, TextureLite, textures.rs:89-91), all in one array; a draw's tex_offset is its first pixel.
+ * Load-time data like sw_create's; synchronous. */
+int sw_set_lite_textures(SwCtx* ctx, const uint32_t* pixels, uint64_t num_pixels);
 
 /* Rasterise the submitted draws (Renderer::draw_frame, renderer.rs:106-124) into the context's
  * framebuffer. If dst != NULL the frame (pixel_format of sw_frame_begin) is also copied there:
@@ -355,6 +386,9 @@ typedef struct SwFrameInput {
 	void* dst;                 /* postprocess: Color32 output; otherwise the frame (pixel_format); may be NULL */
 	uint32_t dst_pitch;        /* pixels */
 	int32_t dst_is_device;
+	const SwTriVertex* tri_vertices; /* vertices of the SW_RASTER_TRIANGLE draws */
+	uint32_t num_tri_vertices;
+	uint32_t reserved;
 } SwFrameInput;
 int sw_draw_frame(SwCtx* ctx, const SwFrameInput* frame);
 /* Graph capture of sw_draw_frame: on (default) or off (the same work launched directly). */
@@ -543,8 +577,9 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 /* sizeof() of the ABI structs in this order: SwCreateInfo, SwTextureMip, SwEmissiveMip,
  * SwDirectionalLightmapElement, SwLight, SwSurfaceDesc, SwVertex16, SwDrawCmd, SwFrameParams,
  * SwPostConfig, SwStats, SwFrameInput, SwTuning, SwMapPolygon, SwViewLeaf, SwViewFrameInput,
- * SwViewCounts, SwLightShadow, SwDepthDraw, SwShadowSide, SwShadowLeaf, SwMaterialFrame. Writes
- * min(count, 22) values; returns the number of structs (22). Needs no GPU: bindings use it to check their mirrored layouts. */
+ * SwViewCounts, SwLightShadow, SwDepthDraw, SwShadowSide, SwShadowLeaf, SwMaterialFrame, SwTriVertex.
+ * Writes min(count, 23) values; returns the number of structs (23). Needs no GPU: bindings use it to
+ * check their mirrored layouts. */
 int sw_abi_layout(uint32_t* sizes, uint32_t count);
 
 /* Diagnostics: copy the frame's surface arena (total_texels of sw_submit_surfaces, or of the surfaces a

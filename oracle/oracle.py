@@ -34,11 +34,13 @@ def load():
     lib.orc_build_surfaces.argtypes = [vp, vp, u32, vp, u32, vp, vp, u64, vp, vp, u64, u32]
     lib.orc_shadow_maps.argtypes = [vp, u32, vp, u32, vp, u64]
     lib.orc_rasterize.argtypes = [vp, u32, vp, u32, vp, u64, vp, u64, vp, vp, u32, u32, ctypes.POINTER(u64)]
+    lib.orc_rasterize_ex.argtypes = [vp, u32, vp, u32, vp, u32, vp, u64, vp, u64, vp, u64, vp, vp, u32, u32,
+                                     ctypes.POINTER(u64)]
     lib.orc_clear_background.argtypes = [vp, vp, u32]
     lib.orc_postprocess.argtypes = [vp, vp, u32, u32, f32, vp, ctypes.POINTER(f32), vp, u32, vp]
     lib.orc_upscale.argtypes = [u32, u32, vp, vp, u32, u32, u32]
     lib.orc_gaussian_kernel.argtypes = [f32, u32, vp]
-    for fn in (lib.orc_build_surfaces, lib.orc_rasterize, lib.orc_clear_background, lib.orc_postprocess,
+    for fn in (lib.orc_build_surfaces, lib.orc_rasterize, lib.orc_rasterize_ex, lib.orc_clear_background, lib.orc_postprocess,
                lib.orc_upscale, lib.orc_gaussian_kernel, lib.orc_shadow_maps):
         fn.restype = i32
     _lib = lib
@@ -82,17 +84,22 @@ def shadow_maps(draws, vertices, storage):
     return storage
 
 
-def rasterize(draws, vertices, arena, frame_params, framebuffer, num_threads=1, skybox=None):
+def rasterize(draws, vertices, arena, frame_params, framebuffer, num_threads=1, skybox=None, tri_vertices=None, lite=None):
     """Rasterise into `framebuffer` (height, pitch) in place; returns the count of bad texel fetches.
-    skybox: the skybox texels (frame's pixel format) that SW_TEXSRC_SKYBOX draws read."""
+    skybox: the skybox texels (frame's pixel format) that SW_TEXSRC_SKYBOX draws read; tri_vertices and
+    lite: the vertices and Color32 textures of SW_RASTER_TRIANGLE draws."""
     lib = load()
     draws = np.ascontiguousarray(draws, dtype=abi.DRAW_CMD)
-    vertices = np.ascontiguousarray(vertices, dtype=abi.VERTEX16)
+    vertices = np.ascontiguousarray(vertices if vertices is not None else np.zeros(0, abi.VERTEX16), dtype=abi.VERTEX16)
     bad = ctypes.c_uint64(0)
     sky_ptr, sky_n = (None, 0) if skybox is None or len(skybox) == 0 else (abi.ptr(skybox), len(skybox))
-    _check(lib.orc_rasterize(abi.ptr(draws), draws.size, abi.ptr(vertices), vertices.size, abi.ptr(arena), arena.size,
-                             sky_ptr, sky_n, ctypes.byref(frame_params), abi.ptr(framebuffer), framebuffer.shape[1],
-                             num_threads, ctypes.byref(bad)), "orc_rasterize")
+    arena_ptr, arena_n = (None, 0) if arena is None else (abi.ptr(arena), arena.size)
+    tv = np.ascontiguousarray(tri_vertices if tri_vertices is not None else np.zeros(0, abi.TRI_VERTEX), dtype=abi.TRI_VERTEX)
+    lt = np.ascontiguousarray(lite if lite is not None else np.zeros(0, np.uint32), dtype=np.uint32).reshape(-1)
+    _check(lib.orc_rasterize_ex(abi.ptr(draws), draws.size, abi.ptr(vertices), vertices.size, abi.ptr(tv), tv.size,
+                                arena_ptr, arena_n, sky_ptr, sky_n, abi.ptr(lt), lt.size, ctypes.byref(frame_params),
+                                abi.ptr(framebuffer), framebuffer.shape[1], num_threads, ctypes.byref(bad)),
+           "orc_rasterize_ex")
     return bad.value
 
 

@@ -2,6 +2,7 @@
 //
 // Follows src/square_wheel/rasterizer.rs:137-271 (edge walk of fill_polygon_impl_2_static_params),
 // :273-454 (fill_polygon_part, full perspective), :456-581 (line-z corrected), :583-729 (affine),
+// :765-1292 (fill_triangle_impl, fill_triangle_part: textured triangles with per-vertex light),
 // :1511-1536 (write_into_framebuffer), :1573-1580 (fixed-point constants), src/common/fixed_math.rs,
 // and the driver src/square_wheel/partial_renderer.rs:1192-1283 (perform_rasterization; N-thread mode
 // uses src/square_wheel/rect_splitting.rs:23-78).
@@ -396,6 +397,251 @@ struct Raster
 			cur_y = next_y;
 		}
 	}
+
+	// ---- triangles: Rasterizer::fill_triangle_impl / fill_triangle_part, rasterizer.rs:765-1292 ----
+
+	const uint32_t* lite = nullptr; // the triangle's Color32 texture
+	uint64_t lite_len = 0;
+
+	uint32_t fetch_lite(uint64_t address) const
+	{
+		if (address >= lite_len)
+		{
+			if (bad_fetches) ++*bad_fetches;
+			return lite[0];
+		}
+		return lite[address];
+	}
+
+	void fill_triangle(const SwTriVertex* vertices, int32_t tex_w, int32_t tex_h, uint32_t blend)
+	{
+		// sort by y: upper (max), lower (min), middle (rasterizer.rs:773-793)
+		int upper_index, lower_index;
+		if (vertices[0].y >= vertices[1].y && vertices[0].y >= vertices[2].y)
+		{
+			upper_index = 0;
+			lower_index = vertices[1].y < vertices[2].y ? 1 : 2;
+		}
+		else if (vertices[1].y >= vertices[0].y && vertices[1].y >= vertices[2].y)
+		{
+			upper_index = 1;
+			lower_index = vertices[0].y < vertices[2].y ? 0 : 2;
+		}
+		else
+		{
+			upper_index = 2;
+			lower_index = vertices[0].y < vertices[1].y ? 0 : 1;
+		}
+		const int middle_index = 3 - upper_index - lower_index;
+		const SwTriVertex& upper = vertices[upper_index];
+		const SwTriVertex& lower = vertices[lower_index];
+		const SwTriVertex& middle = vertices[middle_index];
+
+		const Fixed16 long_edge_dy = std::max(wsub(upper.y, lower.y), FIXED16_HALF);
+		const Fixed16 lower_part_dy = std::max(wsub(middle.y, lower.y), FIXED16_HALF);
+		const Fixed16 upper_part_dy = std::max(wsub(upper.y, middle.y), FIXED16_HALF);
+
+		const Fixed16 long_edge_dx_dy = fixed16_div(wsub(upper.x, lower.x), long_edge_dy);
+		const Fixed16 long_edge_x_in_middle = wadd(lower.x, fixed16_mul(long_edge_dx_dy, wsub(middle.y, lower.y)));
+		const Fixed16 lower_part_dx_dy = fixed16_div(wsub(middle.x, lower.x), lower_part_dy);
+		const Fixed16 upper_part_dx_dy = fixed16_div(wsub(upper.x, middle.x), upper_part_dy);
+
+		Fixed16 long_edge_d_tc_dy[2], long_edge_tc_in_middle[2], d_tc_dy_lower[2], d_tc_dy_upper[2];
+		for (int i = 0; i < 2; ++i)
+		{
+			long_edge_d_tc_dy[i] = fixed16_div(wsub(upper.tc[i], lower.tc[i]), long_edge_dy);
+			long_edge_tc_in_middle[i] = wadd(lower.tc[i], fixed16_mul(long_edge_d_tc_dy[i], lower_part_dy));
+			d_tc_dy_lower[i] = fixed16_div(wsub(middle.tc[i], lower.tc[i]), lower_part_dy);
+			d_tc_dy_upper[i] = fixed16_div(wsub(upper.tc[i], middle.tc[i]), upper_part_dy);
+		}
+		Fixed16 long_edge_d_light_dy[3], long_edge_light_in_middle[3], d_light_dy_lower[3], d_light_dy_upper[3];
+		for (int i = 0; i < 3; ++i)
+		{
+			long_edge_d_light_dy[i] = fixed16_div(wsub(upper.light[i], lower.light[i]), long_edge_dy);
+			long_edge_light_in_middle[i] = wadd(lower.light[i], fixed16_mul(long_edge_d_light_dy[i], lower_part_dy));
+			d_light_dy_lower[i] = fixed16_div(wsub(middle.light[i], lower.light[i]), lower_part_dy);
+			d_light_dy_upper[i] = fixed16_div(wsub(upper.light[i], middle.light[i]), upper_part_dy);
+		}
+
+		if (long_edge_x_in_middle >= middle.x)
+		{
+			// the middle vertex is on the left (rasterizer.rs:829-888)
+			const Fixed16 middle_dx = std::max(wsub(long_edge_x_in_middle, middle.x), FIXED16_HALF);
+			Fixed16 d_tc_dx[2], d_light_dx[3];
+			for (int i = 0; i < 2; ++i) d_tc_dx[i] = fixed16_div(wsub(long_edge_tc_in_middle[i], middle.tc[i]), middle_dx);
+			for (int i = 0; i < 3; ++i) d_light_dx[i] = fixed16_div(wsub(long_edge_light_in_middle[i], middle.light[i]), middle_dx);
+			fill_triangle_part(lower.y, middle.y, PolygonSide{lower.x, lower_part_dx_dy}, PolygonSide{lower.x, long_edge_dx_dy},
+				lower.tc, d_tc_dy_lower, d_tc_dx, lower.light, d_light_dy_lower, d_light_dx, tex_w, tex_h, blend);
+			fill_triangle_part(middle.y, upper.y, PolygonSide{middle.x, upper_part_dx_dy},
+				PolygonSide{long_edge_x_in_middle, long_edge_dx_dy}, middle.tc, d_tc_dy_upper, d_tc_dx, middle.light,
+				d_light_dy_upper, d_light_dx, tex_w, tex_h, blend);
+		}
+		else
+		{
+			// the middle vertex is on the right (rasterizer.rs:889-950)
+			const Fixed16 middle_dx = std::max(wsub(middle.x, long_edge_x_in_middle), FIXED16_HALF);
+			Fixed16 d_tc_dx[2], d_light_dx[3];
+			for (int i = 0; i < 2; ++i) d_tc_dx[i] = fixed16_div(wsub(middle.tc[i], long_edge_tc_in_middle[i]), middle_dx);
+			for (int i = 0; i < 3; ++i) d_light_dx[i] = fixed16_div(wsub(middle.light[i], long_edge_light_in_middle[i]), middle_dx);
+			fill_triangle_part(lower.y, middle.y, PolygonSide{lower.x, long_edge_dx_dy}, PolygonSide{lower.x, lower_part_dx_dy},
+				lower.tc, long_edge_d_tc_dy, d_tc_dx, lower.light, long_edge_d_light_dy, d_light_dx, tex_w, tex_h, blend);
+			fill_triangle_part(middle.y, upper.y, PolygonSide{long_edge_x_in_middle, long_edge_dx_dy},
+				PolygonSide{middle.x, upper_part_dx_dy}, long_edge_tc_in_middle, long_edge_d_tc_dy, d_tc_dx,
+				long_edge_light_in_middle, long_edge_d_light_dy, d_light_dx, tex_w, tex_h, blend);
+		}
+	}
+
+	void fill_triangle_part(Fixed16 y_start, Fixed16 y_end, PolygonSide left_side, PolygonSide right_side,
+		const Fixed16 tc_start_left[2], const Fixed16 d_tc_dy_left_in[2], const Fixed16 d_tc_dx_in[2],
+		const Fixed16 light_start_left[3], const Fixed16 d_light_left_in[3], const Fixed16 d_light_dx_in[3], int32_t tex_w,
+		int32_t tex_h, uint32_t blend)
+	{
+		Fixed16 d_tc_dy_left[2] = {d_tc_dy_left_in[0], d_tc_dy_left_in[1]};
+		Fixed16 d_tc_dx[2] = {d_tc_dx_in[0], d_tc_dx_in[1]};
+		Fixed16 d_light_left[3] = {d_light_left_in[0], d_light_left_in[1], d_light_left_in[2]};
+		Fixed16 d_light_dx[3] = {d_light_dx_in[0], d_light_dx_in[1], d_light_dx_in[2]};
+		const int32_t y_start_int = std::max(fixed16_round_to_int(y_start), clip_rect.min_y);
+		const int32_t y_end_int = std::min(fixed16_round_to_int(y_end), clip_rect.max_y);
+		if (y_start_int >= y_end_int) return;
+
+		const Fixed16 y_start_delta = wsub(wadd(int_to_fixed16(y_start_int), FIXED16_HALF), y_start);
+		Fixed16 x_left = wadd(wadd(left_side.x_start, fixed16_mul(y_start_delta, left_side.dx_dy)), FIXED16_HALF);
+		Fixed16 x_right = wadd(wadd(right_side.x_start, fixed16_mul(y_start_delta, right_side.dx_dy)), FIXED16_HALF);
+
+		const Fixed16 y_end_delta = wsub(y_end, wadd(y_start, y_start_delta));
+		const Fixed16 d_x_lower = std::max(wsub(x_right, x_left), 0);
+		const Fixed16 x_upper_left = wadd(x_left, fixed16_mul(y_end_delta, left_side.dx_dy));
+		const Fixed16 x_upper_right = wadd(x_right, fixed16_mul(y_end_delta, right_side.dx_dy));
+		const Fixed16 d_x_upper = std::max(wsub(x_upper_right, x_upper_left), 0);
+
+		// texture coordinates kept inside the texture (rasterizer.rs:1017-1135)
+		Fixed16 tc_left[2] = {0, 0};
+		const int32_t tex_size[2] = {tex_w, tex_h};
+		for (int i = 0; i < 2; ++i)
+		{
+			const Fixed16 max_tc = wsub(int_to_fixed16(tex_size[i]), 1);
+			{
+				tc_left[i] = std::min(std::max(wadd(tc_start_left[i], fixed16_mul(y_start_delta, d_tc_dy_left[i])), 0), max_tc);
+				const Fixed16 tc_lower_delta = fixed16_mul(d_tc_dx[i], d_x_lower);
+				if (tc_lower_delta > max_tc)
+				{
+					tc_left[i] = 0;
+					d_tc_dx[i] = fixed16_div(max_tc, d_x_lower);
+				}
+				else if (tc_lower_delta < -max_tc)
+				{
+					tc_left[i] = max_tc;
+					d_tc_dx[i] = fixed16_div(-max_tc, d_x_lower);
+				}
+				else
+				{
+					const Fixed16 tc_lower_right = wadd(tc_left[i], tc_lower_delta);
+					if (tc_lower_right > max_tc)
+						tc_left[i] = wsub(tc_left[i], wsub(tc_lower_right, max_tc));
+					else if (tc_lower_right < 0)
+						tc_left[i] = wsub(tc_left[i], tc_lower_right);
+				}
+			}
+			{
+				Fixed16 tc_upper_left = std::min(std::max(wadd(tc_left[i], fixed16_mul(y_end_delta, d_tc_dy_left[i])), 0), max_tc);
+				const Fixed16 tc_upper_delta = fixed16_mul(d_tc_dx[i], d_x_upper);
+				if (tc_upper_delta > max_tc)
+				{
+					tc_upper_left = 0;
+					d_tc_dx[i] = fixed16_div(max_tc, d_x_upper);
+				}
+				else if (tc_upper_delta < -max_tc)
+				{
+					tc_upper_left = max_tc;
+					d_tc_dx[i] = fixed16_div(-max_tc, d_x_upper);
+				}
+				else
+				{
+					const Fixed16 tc_upper_right = wadd(tc_upper_left, tc_upper_delta);
+					if (tc_upper_right > max_tc)
+						tc_upper_left = wsub(tc_upper_left, wsub(tc_upper_right, max_tc));
+					else if (tc_upper_right < 0)
+						tc_upper_left = wsub(tc_upper_left, tc_upper_right);
+				}
+				d_tc_dy_left[i] = y_end_delta > 0 ? fixed16_div(wsub(tc_upper_left, tc_left[i]), y_end_delta) : 0;
+
+				const Fixed16 tc_upper_left2 = wadd(tc_left[i], fixed16_mul(y_end_delta, d_tc_dy_left[i]));
+				const Fixed16 tc_upper_right = wadd(tc_upper_left2, fixed16_mul(d_tc_dx[i], d_x_upper));
+				if (tc_upper_right < 0)
+					d_tc_dx[i] = d_x_upper > 0 ? fixed16_div(-tc_upper_left2, d_x_upper) : 0;
+				else if (tc_upper_right > max_tc)
+					d_tc_dx[i] = d_x_upper > 0 ? fixed16_div(wsub(max_tc, tc_upper_left2), d_x_upper) : 0;
+			}
+		}
+
+		// light kept non-negative (rasterizer.rs:1137-1186)
+		Fixed16 light_left[3] = {0, 0, 0};
+		for (int i = 0; i < 3; ++i)
+		{
+			light_left[i] = std::max(wadd(light_start_left[i], fixed16_mul(y_start_delta, d_light_left[i])), 0);
+			const Fixed16 light_lower_right = wadd(light_left[i], fixed16_mul(d_x_lower, d_light_dx[i]));
+			if (light_lower_right < 0) light_left[i] = wsub(light_left[i], light_lower_right);
+			{
+				Fixed16 light_upper_left = std::max(wadd(light_left[i], fixed16_mul(y_end_delta, d_light_left[i])), 0);
+				const Fixed16 light_upper_right = wadd(light_upper_left, fixed16_mul(d_x_upper, d_light_dx[i]));
+				if (light_upper_right < 0) light_upper_left = wsub(light_upper_left, light_upper_right);
+				d_light_left[i] = y_end_delta > 0 ? fixed16_div(wsub(light_upper_left, light_left[i]), y_end_delta) : 0;
+
+				const Fixed16 light_upper_left2 = wadd(light_left[i], fixed16_mul(y_end_delta, d_light_left[i]));
+				const Fixed16 light_upper_right2 = wadd(light_upper_left2, fixed16_mul(d_x_upper, d_light_dx[i]));
+				if (light_upper_right2 < 0) d_light_dx[i] = d_x_upper > 0 ? fixed16_div(-light_upper_left2, d_x_upper) : 0;
+			}
+		}
+
+		// ColorVecI::from_color_i32x3: lanes [c2, c1, c0, 0]
+		const ColorVecI d_light_dx_vec{{d_light_dx[2], d_light_dx[1], d_light_dx[0], 0}};
+		for (int32_t y_int = y_start_int; y_int < y_end_int; ++y_int)
+		{
+			const int32_t x_start_int = std::max(fixed16_floor_to_int(x_left), clip_rect.min_x);
+			const int32_t x_end_int = std::min(fixed16_floor_to_int(x_right), clip_rect.max_x);
+			if (x_start_int < x_end_int)
+			{
+				const Fixed16 x_start_delta = wsub(wadd(int_to_fixed16(x_start_int), FIXED16_ONE), x_left);
+				Fixed16 line_tc[2] = {wadd(tc_left[0], fixed16_mul(x_start_delta, d_tc_dx[0])),
+					wadd(tc_left[1], fixed16_mul(x_start_delta, d_tc_dx[1]))};
+				ColorVecI line_light{{wadd(light_left[2], fixed16_mul(x_start_delta, d_light_dx[2])),
+					wadd(light_left[1], fixed16_mul(x_start_delta, d_light_dx[1])),
+					wadd(light_left[0], fixed16_mul(x_start_delta, d_light_dx[0])), 0}};
+				T* dst_line = color_buffer + int64_t(y_int) * row_size;
+				for (int32_t x = x_start_int; x < x_end_int; ++x)
+				{
+					const int32_t u = fixed16_floor_to_int(line_tc[0]);
+					const int32_t v = fixed16_floor_to_int(line_tc[1]);
+					const uint64_t texel_address = uint64_t(int64_t(wadd(u, wmul(v, tex_w))));
+					const uint32_t texel = fetch_lite(texel_address);
+					const ColorVecI lighted = ci_shr(ci_mul(ci_from_c32(texel), line_light), 16);
+					T& dst = dst_line[x];
+					switch (blend) // rasterizer.rs:1233-1270
+					{
+					case SW_BLEND_NONE: dst = P::from_veci(lighted); break;
+					case SW_BLEND_AVERAGE: dst = P::average(dst, P::from_veci(lighted)); break;
+					case SW_BLEND_ADDITIVE: dst = P::saturated_sum(dst, P::from_veci(lighted)); break;
+					case SW_BLEND_ALPHA_TEST:
+						if (C32::test_alpha(texel)) dst = P::from_veci(lighted);
+						break;
+					case SW_BLEND_ALPHA_BLEND:
+					{
+						const int32_t alpha = C32::get_alpha(texel);
+						dst = P::from_veci(ci_shr(
+							ci_add(ci_mul_scalar(P::to_veci(dst), wsub(255, alpha)), ci_mul_scalar(lighted, alpha)), 8));
+						break;
+					}
+					}
+					for (int i = 0; i < 2; ++i) line_tc[i] = wadd(line_tc[i], d_tc_dx[i]);
+					line_light = ci_add(line_light, d_light_dx_vec);
+				}
+			}
+			x_left = wadd(x_left, left_side.dx_dy);
+			x_right = wadd(x_right, right_side.dx_dy);
+			for (int i = 0; i < 2; ++i) tc_left[i] = wadd(tc_left[i], d_tc_dy_left[i]);
+			for (int i = 0; i < 3; ++i) light_left[i] = wadd(light_left[i], d_light_left[i]);
+		}
+	}
 };
 
 // rect_splitting.rs:29-78
@@ -434,9 +680,10 @@ void split_rect_r(const RectF& r, uint32_t num_parts, std::vector<RectF>& out, s
 }
 
 template <class P>
-void rasterize_all(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, const void* arena,
-	uint64_t arena_texels, const void* skybox, uint64_t skybox_texels, const SwFrameParams* frame, void* framebuffer,
-	uint32_t pitch, uint32_t num_threads, uint64_t* bad_fetches)
+void rasterize_all(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, const SwTriVertex* tri_vertices,
+	const void* arena, uint64_t arena_texels, const void* skybox, uint64_t skybox_texels, const uint32_t* lite,
+	uint64_t lite_texels, const SwFrameParams* frame, void* framebuffer, uint32_t pitch, uint32_t num_threads,
+	uint64_t* bad_fetches)
 {
 	typedef typename P::T T;
 	auto run = [&](ClipRect clip, uint64_t* bad) {
@@ -448,6 +695,17 @@ void rasterize_all(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16*
 		for (uint32_t i = 0; i < num_draws; ++i)
 		{
 			const SwDrawCmd& d = draws[i];
+			if (d.mode == SW_RASTER_TRIANGLE)
+			{
+				// fill_triangle with a TextureLite (Color32) texture
+				r.lite = lite + d.tex_offset;
+				const uint64_t avail = lite_texels > d.tex_offset ? lite_texels - d.tex_offset : 0;
+				const uint64_t want = uint64_t(d.tex_size[0]) * d.tex_size[1];
+				r.lite_len = want < avail ? want : avail;
+				if (r.lite_len == 0) continue;
+				r.fill_triangle(tri_vertices + d.first_vertex, int32_t(d.tex_size[0]), int32_t(d.tex_size[1]), d.blend);
+				continue;
+			}
 			// draw_polygon's texture: a surface, or a skybox side mip (draw_skybox, partial_renderer.rs:2434-2444)
 			const bool sky = d.tex_source == SW_TEXSRC_SKYBOX;
 			const uint64_t texels = sky ? skybox_texels : arena_texels;
@@ -487,11 +745,28 @@ extern "C" int orc_rasterize(const SwDrawCmd* draws, uint32_t num_draws, const S
 	uint32_t num_vertices, const void* arena, uint64_t arena_texels, const void* skybox, uint64_t skybox_texels,
 	const SwFrameParams* frame, void* framebuffer, uint32_t pitch, uint32_t num_threads, uint64_t* bad_fetches)
 {
-	if (!frame || !framebuffer || (num_draws && (!draws || !vertices || !arena))) return SW_ERR_INVALID_ARGUMENT;
+	return orc_rasterize_ex(draws, num_draws, vertices, num_vertices, nullptr, 0, arena, arena_texels, skybox, skybox_texels,
+		nullptr, 0, frame, framebuffer, pitch, num_threads, bad_fetches);
+}
+
+extern "C" int orc_rasterize_ex(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices,
+	uint32_t num_vertices, const SwTriVertex* tri_vertices, uint32_t num_tri_vertices, const void* arena,
+	uint64_t arena_texels, const void* skybox, uint64_t skybox_texels, const uint32_t* lite, uint64_t lite_texels,
+	const SwFrameParams* frame, void* framebuffer, uint32_t pitch, uint32_t num_threads, uint64_t* bad_fetches)
+{
+	if (!frame || !framebuffer || (num_draws && !draws)) return SW_ERR_INVALID_ARGUMENT;
 	if (pitch < frame->width) return SW_ERR_INVALID_ARGUMENT;
 	for (uint32_t i = 0; i < num_draws; ++i)
 	{
 		const SwDrawCmd& d = draws[i];
+		if (d.mode == SW_RASTER_TRIANGLE)
+		{
+			if (d.vertex_count != 3 || !tri_vertices || uint64_t(d.first_vertex) + 3 > num_tri_vertices) return SW_ERR_INVALID_ARGUMENT;
+			if (d.tex_source != SW_TEXSRC_LITE || !lite || d.blend > SW_BLEND_ALPHA_BLEND) return SW_ERR_INVALID_ARGUMENT;
+			if (d.tex_size[0] == 0 || d.tex_size[1] == 0) return SW_ERR_INVALID_ARGUMENT;
+			continue;
+		}
+		if (!vertices || !arena) return SW_ERR_INVALID_ARGUMENT;
 		if (d.vertex_count < 3 || d.vertex_count > SW_MAX_POLYGON_VERTICES) return SW_ERR_INVALID_ARGUMENT;
 		if (uint64_t(d.first_vertex) + d.vertex_count > num_vertices) return SW_ERR_INVALID_ARGUMENT;
 		if (d.mode > SW_RASTER_AFFINE || d.blend > SW_BLEND_ALPHA_BLEND) return SW_ERR_INVALID_ARGUMENT;
@@ -499,11 +774,11 @@ extern "C" int orc_rasterize(const SwDrawCmd* draws, uint32_t num_draws, const S
 		if (d.tex_source > SW_TEXSRC_SKYBOX || (d.tex_source == SW_TEXSRC_SKYBOX && !skybox)) return SW_ERR_INVALID_ARGUMENT;
 	}
 	if (frame->pixel_format == SW_PIXEL_C64)
-		rasterize_all<C64>(draws, num_draws, vertices, arena, arena_texels, skybox, skybox_texels, frame, framebuffer, pitch,
-			num_threads, bad_fetches);
+		rasterize_all<C64>(draws, num_draws, vertices, tri_vertices, arena, arena_texels, skybox, skybox_texels, lite,
+			lite_texels, frame, framebuffer, pitch, num_threads, bad_fetches);
 	else
-		rasterize_all<C32>(draws, num_draws, vertices, arena, arena_texels, skybox, skybox_texels, frame, framebuffer, pitch,
-			num_threads, bad_fetches);
+		rasterize_all<C32>(draws, num_draws, vertices, tri_vertices, arena, arena_texels, skybox, skybox_texels, lite,
+			lite_texels, frame, framebuffer, pitch, num_threads, bad_fetches);
 	return SW_OK;
 }
 

@@ -35,6 +35,13 @@ int orc_rasterize(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* 
 	const void* arena, uint64_t arena_texels, const void* skybox, uint64_t skybox_texels, const SwFrameParams* frame,
 	void* framebuffer, uint32_t pitch, uint32_t num_threads, uint64_t* bad_fetches);
 
+/* orc_rasterize with triangle draws (SW_RASTER_TRIANGLE, Rasterizer::fill_triangle, rasterizer.rs:731-1292):
+ * their vertices are in tri_vertices and their Color32 textures in `lite`. */
+int orc_rasterize_ex(const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices,
+	const SwTriVertex* tri_vertices, uint32_t num_tri_vertices, const void* arena, uint64_t arena_texels,
+	const void* skybox, uint64_t skybox_texels, const uint32_t* lite, uint64_t lite_texels, const SwFrameParams* frame,
+	void* framebuffer, uint32_t pitch, uint32_t num_threads, uint64_t* bad_fetches);
+
 /* draw_background, partial_renderer.rs:3987-4009, colour (32,16,8) via ColorVec. */
 int orc_clear_background(const SwFrameParams* frame, void* framebuffer, uint32_t pitch);
 

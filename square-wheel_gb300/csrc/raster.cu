@@ -179,6 +179,223 @@ __device__ uint32_t edge_walk(const SwDrawCmd& d, const SwVertex16* vtx, int32_t
 	return st.num_parts;
 }
 
+// ---- triangles: Rasterizer::fill_triangle_impl / fill_triangle_part (rasterizer.rs:765-1292) ----
+
+// fill_triangle_part's prologue (rasterizer.rs:984-1186): the part's rows clipped to the frame, its
+// first-row edges and the texture-coordinate and light corrections, into one RasterPart (no part when
+// it has no row).
+__device__ void triangle_part(RasterPart* parts, uint32_t& np, int32_t height, Fixed16 y_start, Fixed16 y_end, Fixed16 xl_start,
+	Fixed16 dxl, Fixed16 xr_start, Fixed16 dxr, const Fixed16* tc_start_left, const Fixed16* d_tc_dy_left_in,
+	const Fixed16* d_tc_dx_in, const Fixed16* light_start_left, const Fixed16* d_light_left_in, const Fixed16* d_light_dx_in,
+	int32_t tex_w, int32_t tex_h)
+{
+	const int32_t y_start_int = max(round_to_int(y_start), 0);
+	const int32_t y_end_int = min(round_to_int(y_end), height);
+	if (y_start_int >= y_end_int) return;
+	Fixed16 d_tc_dy_left[2] = {d_tc_dy_left_in[0], d_tc_dy_left_in[1]};
+	Fixed16 d_tc_dx[2] = {d_tc_dx_in[0], d_tc_dx_in[1]};
+	Fixed16 d_light_left[3] = {d_light_left_in[0], d_light_left_in[1], d_light_left_in[2]};
+	Fixed16 d_light_dx[3] = {d_light_dx_in[0], d_light_dx_in[1], d_light_dx_in[2]};
+	const Fixed16 y_start_delta = wsub(wadd(int_to_fixed16(y_start_int), FIXED16_HALF), y_start);
+	const Fixed16 x_left = wadd(wadd(xl_start, fx_mul(y_start_delta, dxl)), FIXED16_HALF);
+	const Fixed16 x_right = wadd(wadd(xr_start, fx_mul(y_start_delta, dxr)), FIXED16_HALF);
+	const Fixed16 y_end_delta = wsub(y_end, wadd(y_start, y_start_delta));
+	const Fixed16 d_x_lower = max(wsub(x_right, x_left), 0);
+	const Fixed16 x_upper_left = wadd(x_left, fx_mul(y_end_delta, dxl));
+	const Fixed16 x_upper_right = wadd(x_right, fx_mul(y_end_delta, dxr));
+	const Fixed16 d_x_upper = max(wsub(x_upper_right, x_upper_left), 0);
+
+	Fixed16 tc_left[2];
+	const int32_t tex_size[2] = {tex_w, tex_h};
+#pragma unroll
+	for (int i = 0; i < 2; ++i)
+	{
+		const Fixed16 max_tc = wsub(int_to_fixed16(tex_size[i]), 1);
+		tc_left[i] = min(max(wadd(tc_start_left[i], fx_mul(y_start_delta, d_tc_dy_left[i])), 0), max_tc);
+		const Fixed16 tc_lower_delta = fx_mul(d_tc_dx[i], d_x_lower);
+		if (tc_lower_delta > max_tc)
+		{
+			tc_left[i] = 0;
+			d_tc_dx[i] = fx_div(max_tc, d_x_lower);
+		}
+		else if (tc_lower_delta < -max_tc)
+		{
+			tc_left[i] = max_tc;
+			d_tc_dx[i] = fx_div(-max_tc, d_x_lower);
+		}
+		else
+		{
+			const Fixed16 tc_lower_right = wadd(tc_left[i], tc_lower_delta);
+			if (tc_lower_right > max_tc)
+				tc_left[i] = wsub(tc_left[i], wsub(tc_lower_right, max_tc));
+			else if (tc_lower_right < 0)
+				tc_left[i] = wsub(tc_left[i], tc_lower_right);
+		}
+		Fixed16 tc_upper_left = min(max(wadd(tc_left[i], fx_mul(y_end_delta, d_tc_dy_left[i])), 0), max_tc);
+		const Fixed16 tc_upper_delta = fx_mul(d_tc_dx[i], d_x_upper);
+		if (tc_upper_delta > max_tc)
+		{
+			tc_upper_left = 0;
+			d_tc_dx[i] = fx_div(max_tc, d_x_upper);
+		}
+		else if (tc_upper_delta < -max_tc)
+		{
+			tc_upper_left = max_tc;
+			d_tc_dx[i] = fx_div(-max_tc, d_x_upper);
+		}
+		else
+		{
+			const Fixed16 tc_upper_right = wadd(tc_upper_left, tc_upper_delta);
+			if (tc_upper_right > max_tc)
+				tc_upper_left = wsub(tc_upper_left, wsub(tc_upper_right, max_tc));
+			else if (tc_upper_right < 0)
+				tc_upper_left = wsub(tc_upper_left, tc_upper_right);
+		}
+		d_tc_dy_left[i] = y_end_delta > 0 ? fx_div(wsub(tc_upper_left, tc_left[i]), y_end_delta) : 0;
+		const Fixed16 tul = wadd(tc_left[i], fx_mul(y_end_delta, d_tc_dy_left[i]));
+		const Fixed16 tur = wadd(tul, fx_mul(d_tc_dx[i], d_x_upper));
+		if (tur < 0)
+			d_tc_dx[i] = d_x_upper > 0 ? fx_div(-tul, d_x_upper) : 0;
+		else if (tur > max_tc)
+			d_tc_dx[i] = d_x_upper > 0 ? fx_div(wsub(max_tc, tul), d_x_upper) : 0;
+	}
+	Fixed16 light_left[3];
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+	{
+		light_left[i] = max(wadd(light_start_left[i], fx_mul(y_start_delta, d_light_left[i])), 0);
+		const Fixed16 llr = wadd(light_left[i], fx_mul(d_x_lower, d_light_dx[i]));
+		if (llr < 0) light_left[i] = wsub(light_left[i], llr);
+		Fixed16 lul = max(wadd(light_left[i], fx_mul(y_end_delta, d_light_left[i])), 0);
+		const Fixed16 lur = wadd(lul, fx_mul(d_x_upper, d_light_dx[i]));
+		if (lur < 0) lul = wsub(lul, lur);
+		d_light_left[i] = y_end_delta > 0 ? fx_div(wsub(lul, light_left[i]), y_end_delta) : 0;
+		const Fixed16 lul2 = wadd(light_left[i], fx_mul(y_end_delta, d_light_left[i]));
+		const Fixed16 lur2 = wadd(lul2, fx_mul(d_x_upper, d_light_dx[i]));
+		if (lur2 < 0) d_light_dx[i] = d_x_upper > 0 ? fx_div(-lul2, d_x_upper) : 0;
+	}
+	RasterPart p;
+	p.y_start_int = y_start_int;
+	p.y_end_int = y_end_int;
+	p.x_left0 = x_left;
+	p.x_right0 = x_right;
+	p.dx_dy_left = dxl;
+	p.dx_dy_right = dxr;
+#pragma unroll
+	for (int i = 0; i < 2; ++i)
+	{
+		p.tc_left0[i] = tc_left[i];
+		p.d_tc_left[i] = d_tc_dy_left[i];
+		p.tc_right0[i] = d_tc_dx[i]; // the per-pixel step
+		p.d_tc_right[i] = 0;
+	}
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+	{
+		p.light_left0[i] = light_left[i];
+		p.d_light_left[i] = d_light_left[i];
+		p.d_light_dx[i] = d_light_dx[i];
+	}
+	parts[np++] = p;
+}
+
+// fill_triangle_impl (rasterizer.rs:765-950): vertices sorted by y, the long edge, the interpolants'
+// slopes, and the two parts on either side of the middle vertex.
+__device__ uint32_t triangle_setup(const SwTriVertex* v, int32_t tex_w, int32_t tex_h, int32_t height, RasterPart* parts)
+{
+	int ui, li;
+	if (v[0].y >= v[1].y && v[0].y >= v[2].y)
+	{
+		ui = 0;
+		li = v[1].y < v[2].y ? 1 : 2;
+	}
+	else if (v[1].y >= v[0].y && v[1].y >= v[2].y)
+	{
+		ui = 1;
+		li = v[0].y < v[2].y ? 0 : 2;
+	}
+	else
+	{
+		ui = 2;
+		li = v[0].y < v[1].y ? 0 : 1;
+	}
+	const SwTriVertex up = v[ui], lo = v[li], mid = v[3 - ui - li];
+	const Fixed16 long_dy = max(wsub(up.y, lo.y), FIXED16_HALF);
+	const Fixed16 lower_dy = max(wsub(mid.y, lo.y), FIXED16_HALF);
+	const Fixed16 upper_dy = max(wsub(up.y, mid.y), FIXED16_HALF);
+	const Fixed16 long_dx_dy = fx_div(wsub(up.x, lo.x), long_dy);
+	const Fixed16 long_x_mid = wadd(lo.x, fx_mul(long_dx_dy, wsub(mid.y, lo.y)));
+	const Fixed16 lower_dx_dy = fx_div(wsub(mid.x, lo.x), lower_dy);
+	const Fixed16 upper_dx_dy = fx_div(wsub(up.x, mid.x), upper_dy);
+	Fixed16 long_d_tc[2], long_tc_mid[2], d_tc_lower[2], d_tc_upper[2];
+#pragma unroll
+	for (int i = 0; i < 2; ++i)
+	{
+		long_d_tc[i] = fx_div(wsub(up.tc[i], lo.tc[i]), long_dy);
+		long_tc_mid[i] = wadd(lo.tc[i], fx_mul(long_d_tc[i], lower_dy));
+		d_tc_lower[i] = fx_div(wsub(mid.tc[i], lo.tc[i]), lower_dy);
+		d_tc_upper[i] = fx_div(wsub(up.tc[i], mid.tc[i]), upper_dy);
+	}
+	Fixed16 long_d_light[3], long_light_mid[3], d_light_lower[3], d_light_upper[3];
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+	{
+		long_d_light[i] = fx_div(wsub(up.light[i], lo.light[i]), long_dy);
+		long_light_mid[i] = wadd(lo.light[i], fx_mul(long_d_light[i], lower_dy));
+		d_light_lower[i] = fx_div(wsub(mid.light[i], lo.light[i]), lower_dy);
+		d_light_upper[i] = fx_div(wsub(up.light[i], mid.light[i]), upper_dy);
+	}
+	uint32_t np = 0;
+	Fixed16 d_tc_dx[2], d_light_dx[3];
+	if (long_x_mid >= mid.x)
+	{
+		const Fixed16 middle_dx = max(wsub(long_x_mid, mid.x), FIXED16_HALF);
+#pragma unroll
+		for (int i = 0; i < 2; ++i) d_tc_dx[i] = fx_div(wsub(long_tc_mid[i], mid.tc[i]), middle_dx);
+#pragma unroll
+		for (int i = 0; i < 3; ++i) d_light_dx[i] = fx_div(wsub(long_light_mid[i], mid.light[i]), middle_dx);
+		triangle_part(parts, np, height, lo.y, mid.y, lo.x, lower_dx_dy, lo.x, long_dx_dy, lo.tc, d_tc_lower, d_tc_dx, lo.light,
+			d_light_lower, d_light_dx, tex_w, tex_h);
+		triangle_part(parts, np, height, mid.y, up.y, mid.x, upper_dx_dy, long_x_mid, long_dx_dy, mid.tc, d_tc_upper, d_tc_dx,
+			mid.light, d_light_upper, d_light_dx, tex_w, tex_h);
+	}
+	else
+	{
+		const Fixed16 middle_dx = max(wsub(mid.x, long_x_mid), FIXED16_HALF);
+#pragma unroll
+		for (int i = 0; i < 2; ++i) d_tc_dx[i] = fx_div(wsub(mid.tc[i], long_tc_mid[i]), middle_dx);
+#pragma unroll
+		for (int i = 0; i < 3; ++i) d_light_dx[i] = fx_div(wsub(mid.light[i], long_light_mid[i]), middle_dx);
+		triangle_part(parts, np, height, lo.y, mid.y, lo.x, long_dx_dy, lo.x, lower_dx_dy, lo.tc, long_d_tc, d_tc_dx, lo.light,
+			long_d_light, d_light_dx, tex_w, tex_h);
+		triangle_part(parts, np, height, mid.y, up.y, long_x_mid, long_dx_dy, mid.x, upper_dx_dy, long_tc_mid, long_d_tc,
+			d_tc_dx, long_light_mid, long_d_light, d_light_dx, tex_w, tex_h);
+	}
+	return np;
+}
+
+// A triangle part's row (rasterizer.rs:1188-1212): the span and its first pixel's texture coordinates
+// and light; the reference's per-row additions are start + k * step in wrapping i32 arithmetic.
+__device__ RasterRow triangle_row(const RasterPart& p, int32_t y, int32_t width, uint32_t steps_index)
+{
+	RasterRow r;
+	r.a0 = r.b0 = r.a1 = r.b1 = r.a2 = 0;
+	r.b2 = int32_t(steps_index);
+	const int32_t k = y - p.y_start_int;
+	const Fixed16 x_left = wadd(p.x_left0, wmul(k, p.dx_dy_left));
+	const Fixed16 x_right = wadd(p.x_right0, wmul(k, p.dx_dy_right));
+	r.xs = max(x_left >> 16, 0);
+	r.xe = min(x_right >> 16, width);
+	if (r.xs >= r.xe) return r;
+	const Fixed16 x_start_delta = wsub(wadd(int_to_fixed16(r.xs), FIXED16_ONE), x_left);
+	r.a0 = wadd(wadd(p.tc_left0[0], wmul(k, p.d_tc_left[0])), fx_mul(x_start_delta, p.tc_right0[0]));
+	r.b0 = wadd(wadd(p.tc_left0[1], wmul(k, p.d_tc_left[1])), fx_mul(x_start_delta, p.tc_right0[1]));
+	r.a1 = wadd(wadd(p.light_left0[0], wmul(k, p.d_light_left[0])), fx_mul(x_start_delta, p.d_light_dx[0]));
+	r.b1 = wadd(wadd(p.light_left0[1], wmul(k, p.d_light_left[1])), fx_mul(x_start_delta, p.d_light_dx[1]));
+	r.a2 = wadd(wadd(p.light_left0[2], wmul(k, p.d_light_left[2])), fx_mul(x_start_delta, p.d_light_dx[2]));
+	return r;
+}
+
 // Integer plane equations of fill_polygon_part* (rasterizer.rs:287-310).
 struct DrawEq
 {
@@ -306,6 +523,7 @@ __global__ void __launch_bounds__(256) raster_setup_kernel(RasterArgs a)
 {
 	__shared__ __align__(8) SwDrawCmd s_d;
 	__shared__ SwVertex16 s_v[SW_MAX_POLYGON_VERTICES];
+	__shared__ SwTriVertex s_tv[3];
 	__shared__ RasterPart s_parts[SW_RASTER_MAX_PARTS];
 	__shared__ DrawRows s_dr;
 	__shared__ uint32_t s_np;
@@ -318,13 +536,33 @@ __global__ void __launch_bounds__(256) raster_setup_kernel(RasterArgs a)
 			reinterpret_cast<uint32_t*>(&s_d)[threadIdx.x] = reinterpret_cast<const uint32_t*>(a.draws + di)[threadIdx.x];
 		if (threadIdx.x == 0) s_dr = a.draw_rows[di];
 		__syncthreads();
-		if (threadIdx.x < s_d.vertex_count && threadIdx.x < SW_MAX_POLYGON_VERTICES)
+		const bool tri = s_d.mode == SW_RASTER_TRIANGLE;
+		if (tri)
+		{
+			if (threadIdx.x < 3) s_tv[threadIdx.x] = a.tri_vertices[s_d.first_vertex + threadIdx.x];
+		}
+		else if (threadIdx.x < s_d.vertex_count && threadIdx.x < SW_MAX_POLYGON_VERTICES)
 			s_v[threadIdx.x] = a.vertices[s_d.first_vertex + threadIdx.x];
 		__syncthreads();
 		if (threadIdx.x == 0)
 		{
 			const SwDrawCmd& d = s_d;
-			const uint32_t np = edge_walk(d, s_v, a.height, s_parts);
+			uint32_t np;
+			if (tri)
+			{
+				np = triangle_setup(s_tv, int32_t(d.tex_size[0]), int32_t(d.tex_size[1]), a.height, s_parts);
+				for (uint32_t pi = 0; pi < np; ++pi)
+				{
+					TriSteps ts;
+					ts.d_tc_dx[0] = s_parts[pi].tc_right0[0];
+					ts.d_tc_dx[1] = s_parts[pi].tc_right0[1];
+					for (int i = 0; i < 3; ++i) ts.d_light_dx[i] = s_parts[pi].d_light_dx[i];
+					ts.reserved = 0;
+					a.tri_steps[uint64_t(di) * 2 + pi] = ts;
+				}
+			}
+			else
+				np = edge_walk(d, s_v, a.height, s_parts);
 			s_np = np;
 			int32_t bx0 = INT32_MAX, bx1 = INT32_MIN, by0 = INT32_MAX, by1 = INT32_MIN;
 			for (uint32_t pi = 0; pi < np; ++pi)
@@ -370,7 +608,7 @@ __global__ void __launch_bounds__(256) raster_setup_kernel(RasterArgs a)
 				const RasterPart& p = s_parts[pi];
 				if (y >= p.y_start_int && y < p.y_end_int)
 				{
-					row = row_setup(s_d, e, p, y, a.width);
+					row = s_d.mode == SW_RASTER_TRIANGLE ? triangle_row(p, y, a.width, di * 2 + pi) : row_setup(s_d, e, p, y, a.width);
 					break;
 				}
 			}
@@ -415,6 +653,70 @@ __device__ __forceinline__ uint64_t pixel_address(const RasterRow& r, uint32_t m
 }
 
 constexpr int BATCH = 32; // draws whose tile rows are staged in shared memory at a time
+
+// A thread's strip of one triangle row (fill_triangle_part's pixel loop, rasterizer.rs:1213-1279):
+// texture coordinates and light of span pixel i are start + i * step (the reference's per-pixel
+// additions), the Color32 texel is lit per lane ((texel * light) >> 16, the alpha lane by 0) and
+// written with the draw's blend; alpha test and alpha blend use the unlit texel's alpha.
+template <class P, int STRIP>
+__device__ __forceinline__ void triangle_strip(const RasterArgs& a, const RasterDraw& d, const RasterRow& row, int xb,
+	typename P::T* pix, unsigned int& errors, unsigned int& writes)
+{
+	const TriSteps ts = a.tri_steps[uint32_t(row.b2)];
+	uint32_t tex[STRIP];
+	bool ok[STRIP];
+#pragma unroll
+	for (int k = 0; k < STRIP; ++k)
+	{
+		const int x = xb + k;
+		ok[k] = x >= row.xs && x < row.xe;
+		tex[k] = 0;
+		if (ok[k])
+		{
+			const int32_t i = x - row.xs;
+			const int32_t u = wadd(row.a0, wmul(i, ts.d_tc_dx[0])) >> 16;
+			const int32_t v = wadd(row.b0, wmul(i, ts.d_tc_dx[1])) >> 16;
+			uint64_t ua = uint64_t(int64_t(wadd(u, wmul(v, int32_t(d.tex_w)))));
+			if (ua >= uint64_t(d.tex_w) * d.tex_h)
+			{
+				++errors;
+				ua = 0;
+			}
+			tex[k] = __ldg(a.lite + d.tex_offset + ua);
+		}
+	}
+#pragma unroll
+	for (int k = 0; k < STRIP; ++k)
+		if (ok[k])
+		{
+			const int32_t i = xb + k - row.xs;
+			const CI t = ci_from_c32(tex[k]);
+			// line_light lanes [b, g, r, 0] = [light2, light1, light0, 0] (ColorVecI::from_color_i32x3)
+			const CI lit{{wmul(t.v[0], wadd(row.a2, wmul(i, ts.d_light_dx[2]))) >> 16,
+				wmul(t.v[1], wadd(row.b1, wmul(i, ts.d_light_dx[1]))) >> 16,
+				wmul(t.v[2], wadd(row.a1, wmul(i, ts.d_light_dx[0]))) >> 16, 0}};
+			typename P::T& dst = pix[k];
+			switch (d.blend)
+			{
+			case SW_BLEND_NONE: dst = P::from_ci(lit); break;
+			case SW_BLEND_AVERAGE: dst = P::average(dst, P::from_ci(lit)); break;
+			case SW_BLEND_ADDITIVE: dst = P::saturated_sum(dst, P::from_ci(lit)); break;
+			case SW_BLEND_ALPHA_TEST:
+				if ((tex[k] & 0xFF000000u) > 0x7F000000u) dst = P::from_ci(lit);
+				break;
+			default:
+			{
+				const int32_t alpha = int32_t(tex[k] >> 24);
+				const CI dv = P::to_ci(dst);
+				CI r;
+#pragma unroll
+				for (int l = 0; l < 4; ++l) r.v[l] = wadd(wmul(dv.v[l], wsub(255, alpha)), wmul(lit.v[l], alpha)) >> 8;
+				dst = P::from_ci(r);
+			}
+			}
+			++writes;
+		}
+}
 
 // The bloom downscale of a tile's final colour64 pixels (downscale_hdr_buffer, postprocessor.rs:792-844):
 // the pixels go to shared memory (the row staging area, free once the draws are done), each bloom cell
@@ -578,6 +880,11 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 					const RasterRow row = s_row[h][ly];
 					if (xb + STRIP <= row.xs || xb >= row.xe) continue;
 					const RasterDraw& d = s_rd[b0 + h];
+					if (d.mode == SW_RASTER_TRIANGLE)
+					{
+						triangle_strip<P, STRIP>(a, d, row, xb, pix, local_errors, local_writes);
+						continue;
+					}
 					// Up to four independent texel loads, then the blends in pixel order.
 					T tex[STRIP];
 					bool ok[STRIP];

@@ -48,6 +48,7 @@ struct SurfaceKernelArgs
 	uint32_t num_surfaces;
 	uint32_t directional;
 	uint64_t total_work;
+	uint64_t work_begin; // first texel of the launch (0: all of [0, total_work)); one surface's range for per-surface launches
 	const SwViewCounts* counts; // GPU-side preparation: num_surfaces / total_work from here (else NULL)
 	const SwLightShadow* shadows; // per light (NULL: no shadows), maps in shadow_texels
 	const unsigned long long* shadow_texels; // (sequence << 32 | f32 bits) per texel
@@ -165,6 +166,12 @@ struct RasterPart
 	int32_t tc_right0[2];
 	int32_t d_tc_left[2];
 	int32_t d_tc_right[2];
+	// Triangle parts (fill_triangle_part, rasterizer.rs:984-1292), after the reference's corrections:
+	// the left edge's texture coordinates (tc_left0, per row d_tc_left) and light at row y_start_int and
+	// their per-row steps, and the per-pixel steps d_tc_right (d_tc_dx) and d_light_dx; 16.16.
+	int32_t light_left0[3];
+	int32_t d_light_left[3];
+	int32_t d_light_dx[3];
 };
 
 #define SW_RASTER_MAX_PARTS SW_MAX_POLYGON_VERTICES
@@ -183,11 +190,22 @@ struct DrawRows
 // [xs, xe) and, for pixel i = x - xs, the interpolants start + i * step of the draw's mode:
 //   full perspective: (a0, b0) span inv_z, (a1, b1) and (a2, b2) span tc (i32, wrapping)
 //   line-z corrected / affine: (a1, b1) and (a2, b2) the 16.16 texture coordinates.
+//   triangle (rasterizer.rs:1188-1212): a0, b0 the first pixel's texture coordinates, a1, b1, a2 its
+//   light (r, g, b), b2 the TriSteps index (draw * 2 + part) of the per-pixel steps.
 // xs >= xe: the row holds no pixel.
 struct RasterRow
 {
 	int32_t xs, xe;
 	int32_t a0, b0, a1, b1, a2, b2;
+};
+
+// Per-pixel steps of one part of a triangle draw (fill_triangle_part's d_tc_dx and d_light_dx after
+// its corrections, rasterizer.rs:1017-1186); the part's row records hold the row's first pixel's values.
+struct TriSteps
+{
+	int32_t d_tc_dx[2];
+	int32_t d_light_dx[3];
+	int32_t reserved;
 };
 
 // Per-draw record of the tile kernel.
@@ -211,6 +229,9 @@ struct RasterArgs
 {
 	const SwDrawCmd* draws;
 	const SwVertex16* vertices;
+	const SwTriVertex* tri_vertices; // SW_RASTER_TRIANGLE draws' vertices
+	const uint32_t* lite;            // Color32 textures of SW_TEXSRC_LITE draws
+	uint64_t lite_texels;
 	const DrawRows* draw_rows;
 	uint32_t num_draws;
 	const SwViewCounts* counts; // GPU-side preparation: num_draws from here (else NULL)
@@ -218,8 +239,7 @@ struct RasterArgs
 	uint32_t total_rows; // row records of all draws
 	int32_t width, height;
 	uint32_t clear_background;
-	RasterPart* parts;     // num_draws * SW_RASTER_MAX_PARTS
-	uint32_t* part_counts; // num_draws
+	TriSteps* tri_steps;   // num_draws * 2: per-pixel steps of a triangle draw's two parts
 	RasterDraw* rdraws;
 	RasterRow* rows;
 	RasterBox* boxes;
@@ -243,14 +263,17 @@ int launch_raster_setup(const RasterArgs& args, cudaStream_t stream);
 int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, uint32_t variant, cudaStream_t stream);
 
 // Rows [y0, y0 + nrows) a draw can cover: [round(min_y), round(max_y)) of its vertices clipped to the
-// frame (the edge walk's parts lie inside, rasterizer.rs:160-271 with fixed16_round_to_int).
+// frame (the edge walk's parts lie inside, rasterizer.rs:160-271 with fixed16_round_to_int; a triangle's
+// two parts span its lowest to its highest vertex, :984-1004). Triangle draws take their vertices from tv.
 __host__ __device__ inline void draw_row_range(const SwDrawCmd& d, const SwVertex16* v, int32_t height, int32_t& y0,
-	uint32_t& nrows)
+	uint32_t& nrows, const SwTriVertex* tv = nullptr)
 {
-	int32_t mn = v[d.first_vertex].y, mx = mn;
+	const bool tri = d.mode == SW_RASTER_TRIANGLE;
+	auto vy = [&](uint32_t i) { return tri ? tv[d.first_vertex + i].y : v[d.first_vertex + i].y; };
+	int32_t mn = vy(0), mx = mn;
 	for (uint32_t i = 1; i < d.vertex_count; ++i)
 	{
-		const int32_t y = v[d.first_vertex + i].y;
+		const int32_t y = vy(i);
 		mn = y < mn ? y : mn;
 		mx = y > mx ? y : mx;
 	}

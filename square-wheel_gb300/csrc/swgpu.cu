@@ -103,8 +103,14 @@ struct SwCtx
 	bool arena_valid = false;
 	uint32_t last_num_surfaces = 0, last_surface_format = SW_PIXEL_C32, last_max_light = 0;
 	uint64_t last_surface_work = 0;
+	std::vector<uint64_t> h_prefix; // texel prefix sums of the last sw_submit_surfaces (per-surface launches)
+	cudaGraphExec_t sexec = nullptr; // sw_rebuild_surfaces' graph: one persistent surface launch
+	SurfaceKernelArgs skey{};        // ... and the arguments it was captured with
+	unsigned sblocks = 0;
 	bool last_surface_directional = false;
-	DevBuf draws, vertices, draw_rows, rdraws, rows, boxes, parts, part_counts;
+	DevBuf draws, vertices, tri_vertices, draw_rows, rdraws, rows, boxes, tri_steps;
+	DevBuf lite; // sw_set_lite_textures: Color32 textures of triangle draws
+	uint64_t lite_texels = 0;
 	uint64_t num_rows = 0;
 	uint32_t num_draws = 0;
 	bool draws_valid = false;
@@ -121,7 +127,7 @@ struct SwCtx
 	float* h_average = nullptr; // pinned, 4 floats
 	cudaEvent_t average_ready = nullptr;
 
-	Staging stage_lights, stage_surfaces, stage_prefix, stage_draws, stage_vertices, stage_draw_rows, stage_io;
+	Staging stage_lights, stage_surfaces, stage_prefix, stage_draws, stage_vertices, stage_tri_vertices, stage_draw_rows, stage_io;
 
 	// upscale scratch (src/dst copies for host buffers)
 	DevBuf up_src, up_dst;
@@ -209,8 +215,10 @@ RasterArgs raster_args(SwCtx* ctx)
 	a.clear_background = ctx->frame.clear_background;
 	a.draw_rows = static_cast<const DrawRows*>(ctx->draw_rows.ptr);
 	a.total_rows = uint32_t(ctx->num_rows);
-	a.parts = static_cast<RasterPart*>(ctx->parts.ptr);
-	a.part_counts = static_cast<uint32_t*>(ctx->part_counts.ptr);
+	a.tri_vertices = static_cast<const SwTriVertex*>(ctx->tri_vertices.ptr);
+	a.lite = static_cast<const uint32_t*>(ctx->lite.ptr);
+	a.lite_texels = ctx->lite_texels;
+	a.tri_steps = static_cast<TriSteps*>(ctx->tri_steps.ptr);
 	a.rdraws = static_cast<RasterDraw*>(ctx->rdraws.ptr);
 	a.rows = static_cast<RasterRow*>(ctx->rows.ptr);
 	a.boxes = static_cast<RasterBox*>(ctx->boxes.ptr);
@@ -546,19 +554,20 @@ int sw_destroy(SwCtx* ctx)
 	DevBuf* bufs[] = {&ctx->texels, &ctx->texture_mips, &ctx->emissive, &ctx->emissive_mips, &ctx->lightmaps, &ctx->skybox32,
 		&ctx->skybox64, &ctx->frame_in,
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
-		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->parts, &ctx->part_counts, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
+		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->tri_steps, &ctx->tri_vertices, &ctx->lite, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst, &ctx->map_polygons,
 		&ctx->map_vertices, &ctx->vslab, &ctx->shadow_storage, &ctx->shadow_descs};
 	for (DevBuf* b : bufs) release(*b);
 	for (const SwCtx::HostRange& h : ctx->registered) cudaHostUnregister(h.ptr);
 	if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+	if (ctx->sexec) cudaGraphExecDestroy(ctx->sexec);
 	for (cudaGraphExec_t e : ctx->vexec)
 		if (e) cudaGraphExecDestroy(e);
 	if (ctx->h_counts) cudaFreeHost(ctx->h_counts);
 	for (cudaEvent_t e : ctx->ev_counts)
 		if (e) cudaEventDestroy(e);
 	Staging* st[] = {&ctx->stage_lights, &ctx->stage_surfaces, &ctx->stage_prefix, &ctx->stage_draws,
-		&ctx->stage_vertices, &ctx->stage_draw_rows, &ctx->stage_io, &ctx->gstage[0], &ctx->gstage[1], &ctx->stage_shadow,
+		&ctx->stage_vertices, &ctx->stage_tri_vertices, &ctx->stage_draw_rows, &ctx->stage_io, &ctx->gstage[0], &ctx->gstage[1], &ctx->stage_shadow,
 		&ctx->stage_shadow_descs};
 	for (Staging* s : st)
 	{
@@ -657,7 +666,7 @@ struct SurfaceInputs
 	const SurfaceGpu* surfaces;
 	const uint64_t* work_prefix;
 };
-static int launch_surfaces(SwCtx* ctx, const SurfaceInputs* in = nullptr)
+static SurfaceKernelArgs surface_args(SwCtx* ctx, const SurfaceInputs* in = nullptr)
 {
 	SurfaceKernelArgs a;
 	std::memset(&a, 0, sizeof(a)); // optional fields (counts, cam_pos_dev) stay unset on this path
@@ -677,6 +686,12 @@ static int launch_surfaces(SwCtx* ctx, const SurfaceInputs* in = nullptr)
 	a.lights = in ? in->lights : static_cast<const SwLight*>(ctx->lights.ptr);
 	for (int i = 0; i < 3; ++i) a.cam_pos[i] = ctx->frame.cam_pos[i];
 	a.arena = ctx->arena.ptr;
+	return a;
+}
+
+static int launch_surfaces(SwCtx* ctx, const SurfaceInputs* in = nullptr)
+{
+	const SurfaceKernelArgs a = surface_args(ctx, in);
 	stage_begin(ctx, STAGE_SURFACES);
 	int r = check_kernel(ctx,
 		launch_surface_build(a, ctx->frame.pixel_format, ctx->num_sms, int(ctx->tuning.surface_blocks_per_sm), ctx->stream),
@@ -767,6 +782,7 @@ int sw_submit_surfaces(SwCtx* ctx, const SwSurfaceDesc* surfaces, uint32_t num_s
 	uint64_t work = 0;
 	uint32_t max_light = 0;
 	if ((r = prepare_surfaces(ctx, surfaces, num_surfaces, total_texels, gs, prefix, &work, &max_light))) return r;
+	ctx->h_prefix.assign(prefix, prefix + num_surfaces + 1);
 	const uint32_t bpp = bpp_of(ctx->frame.pixel_format);
 	if ((r = ensure(ctx, ctx->arena, std::max<uint64_t>(total_texels, 1) * bpp))) return r;
 	if ((r = ensure(ctx, ctx->surfaces, std::max<size_t>(num_surfaces, 1) * sizeof(SurfaceGpu)))) return r;
@@ -786,7 +802,68 @@ int sw_rebuild_surfaces(SwCtx* ctx)
 		(ctx->frame.use_directional_lightmaps != 0) != ctx->last_surface_directional)
 		return fail(ctx, SW_ERR_STATE, "frame format or lightmap kind changed since sw_submit_surfaces");
 	if (ctx->last_max_light > ctx->num_lights) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "fewer lights than the surfaces use");
-	return launch_surfaces(ctx);
+	if (!ctx->graph_enabled) return launch_surfaces(ctx);
+	// the persistent launch as a CUDA graph, captured again only when its arguments change
+	const SurfaceKernelArgs a = surface_args(ctx);
+	const unsigned blocks = unsigned(ctx->tuning.surface_blocks_per_sm);
+	if (!ctx->sexec || std::memcmp(&a, &ctx->skey, sizeof(a)) != 0 || blocks != ctx->sblocks)
+	{
+		if (ctx->sexec) cudaGraphExecDestroy(ctx->sexec);
+		ctx->sexec = nullptr;
+		SW_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+		const int lr = launch_surface_build(a, ctx->frame.pixel_format, ctx->num_sms, int(blocks), ctx->stream);
+		cudaGraph_t g = nullptr;
+		const cudaError_t ee = cudaStreamEndCapture(ctx->stream, &g);
+		if (lr || ee != cudaSuccess)
+		{
+			if (g) cudaGraphDestroy(g);
+			cudaGetLastError();
+			return lr ? check_kernel(ctx, lr, "surface build") : cuda_fail(ctx, ee, "cudaStreamEndCapture");
+		}
+		const cudaError_t ie = cudaGraphInstantiate(&ctx->sexec, g, 0);
+		cudaGraphDestroy(g);
+		if (ie != cudaSuccess)
+		{
+			ctx->sexec = nullptr;
+			return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+		}
+		ctx->skey = a;
+		ctx->sblocks = blocks;
+	}
+	stage_begin(ctx, STAGE_SURFACES);
+	SW_CUDA(ctx, cudaGraphLaunch(ctx->sexec, ctx->stream));
+	stage_end(ctx, STAGE_SURFACES);
+	ctx->arena_valid = true;
+	ctx->stats.surfaces += ctx->last_num_surfaces;
+	ctx->stats.surface_texels += ctx->last_surface_work;
+	return SW_OK;
+}
+
+int sw_rebuild_surfaces_per_surface(SwCtx* ctx)
+{
+	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
+	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_rebuild_surfaces_per_surface");
+	if (ctx->h_prefix.size() != size_t(ctx->last_num_surfaces) + 1 || ctx->last_num_surfaces == 0)
+		return fail(ctx, SW_ERR_STATE, "no surfaces submitted with sw_submit_surfaces");
+	if (ctx->frame.pixel_format != ctx->last_surface_format ||
+		(ctx->frame.use_directional_lightmaps != 0) != ctx->last_surface_directional)
+		return fail(ctx, SW_ERR_STATE, "frame format or lightmap kind changed since sw_submit_surfaces");
+	if (ctx->last_max_light > ctx->num_lights) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "fewer lights than the surfaces use");
+	SurfaceKernelArgs a = surface_args(ctx);
+	stage_begin(ctx, STAGE_SURFACES);
+	for (uint32_t i = 0; i < ctx->last_num_surfaces; ++i)
+	{
+		// surface i's texels [prefix[i], prefix[i + 1]), a grid of its own
+		a.work_begin = ctx->h_prefix[i];
+		a.total_work = ctx->h_prefix[i + 1];
+		const int lr = launch_surface_build(a, ctx->frame.pixel_format, ctx->num_sms, 1 << 20, ctx->stream);
+		if (lr) return check_kernel(ctx, lr, "surface build");
+	}
+	stage_end(ctx, STAGE_SURFACES);
+	ctx->arena_valid = true;
+	ctx->stats.surfaces += ctx->last_num_surfaces;
+	ctx->stats.surface_texels += ctx->last_surface_work;
+	return SW_OK;
 }
 
 int sw_set_skybox(SwCtx* ctx, const uint32_t* texels32, const uint64_t* texels64, uint64_t num_texels)
@@ -852,12 +929,32 @@ namespace
 // Host side of sw_submit_draws: validate every draw against its vertices and the surface arena, and
 // compute the rows each draw can cover (row records are numbered in draw order).
 int prepare_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices,
-	DrawRows* rows, uint64_t* out_rows)
+	DrawRows* rows, uint64_t* out_rows, const SwTriVertex* tri_vertices = nullptr, uint32_t num_tri_vertices = 0)
 {
 	uint64_t row_acc = 0;
 	for (uint32_t i = 0; i < num_draws; ++i)
 	{
 		const SwDrawCmd& d = draws[i];
+		if (d.mode == SW_RASTER_TRIANGLE)
+		{
+			// Rasterizer::fill_triangle: three SwTriVertex, a Color32 texture of sw_set_lite_textures
+			if (d.vertex_count != 3 || uint64_t(d.first_vertex) + 3 > num_tri_vertices)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: triangle vertices out of range", i);
+			if (d.blend > SW_BLEND_ALPHA_BLEND) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: bad mode/blend", i);
+			if (d.tex_source != SW_TEXSRC_LITE)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: a triangle needs a texture source of sw_set_lite_textures", i);
+			const uint64_t area = uint64_t(d.tex_size[0]) * d.tex_size[1];
+			if (d.tex_size[0] == 0 || d.tex_size[1] == 0 || d.tex_size[0] > 32768 || d.tex_size[1] > 32768 ||
+				d.tex_offset > ctx->lite_texels || area > ctx->lite_texels - d.tex_offset)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: texture outside the lite textures", i);
+			int32_t y0;
+			uint32_t nrows;
+			draw_row_range(d, vertices, int32_t(ctx->frame.height), y0, nrows, tri_vertices);
+			rows[i] = DrawRows{uint32_t(row_acc), y0, nrows, 0u};
+			row_acc += nrows;
+			if (row_acc > 0xFFFFFFFFull) return fail(ctx, SW_ERR_LIMIT, "too many draw rows in one frame");
+			continue;
+		}
 		if (d.vertex_count < 3 || d.vertex_count > SW_MAX_POLYGON_VERTICES)
 			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: bad vertex count", i);
 		if (uint64_t(d.first_vertex) + d.vertex_count > num_vertices)
@@ -882,24 +979,45 @@ int prepare_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const 
 }
 
 // Device buffers of the raster pass for num_draws draws, num_vertices vertices and `rows` row records.
-int ensure_raster_buffers(SwCtx* ctx, uint32_t num_draws, uint32_t num_vertices, uint64_t rows)
+int ensure_raster_buffers(SwCtx* ctx, uint32_t num_draws, uint32_t num_vertices, uint64_t rows, uint32_t num_tri_vertices = 0)
 {
 	int r;
 	if ((r = ensure(ctx, ctx->draws, std::max<size_t>(num_draws, 1) * sizeof(SwDrawCmd)))) return r;
 	if ((r = ensure(ctx, ctx->vertices, std::max<size_t>(num_vertices, 1) * sizeof(SwVertex16)))) return r;
+	if ((r = ensure(ctx, ctx->tri_vertices, std::max<size_t>(num_tri_vertices, 1) * sizeof(SwTriVertex)))) return r;
 	if ((r = ensure(ctx, ctx->draw_rows, std::max<size_t>(num_draws, 1) * sizeof(DrawRows)))) return r;
 	if ((r = ensure(ctx, ctx->rdraws, std::max<size_t>(num_draws, 1) * sizeof(RasterDraw)))) return r;
 	if ((r = ensure(ctx, ctx->rows, std::max<size_t>(rows, 1) * sizeof(RasterRow)))) return r;
 	if ((r = ensure(ctx, ctx->boxes, std::max<size_t>(num_draws, 1) * sizeof(RasterBox)))) return r;
-	if ((r = ensure(ctx, ctx->parts, std::max<size_t>(num_draws, 1) * SW_RASTER_MAX_PARTS * sizeof(RasterPart)))) return r;
-	if ((r = ensure(ctx, ctx->part_counts, std::max<size_t>(num_draws, 1) * sizeof(uint32_t)))) return r;
+	if ((r = ensure(ctx, ctx->tri_steps, std::max<size_t>(num_draws, 1) * 2 * sizeof(TriSteps)))) return r;
 	return SW_OK;
 }
 } // namespace
 
 int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices)
 {
-	if (!ctx || (num_draws && (!draws || !vertices))) return SW_ERR_INVALID_ARGUMENT;
+	return sw_submit_draws_ex(ctx, draws, num_draws, vertices, num_vertices, nullptr, 0);
+}
+
+int sw_set_lite_textures(SwCtx* ctx, const uint32_t* pixels, uint64_t num_pixels)
+{
+	if (!ctx || (num_pixels && !pixels)) return SW_ERR_INVALID_ARGUMENT;
+	if (num_pixels > (uint64_t(1) << 32)) return fail(ctx, SW_ERR_LIMIT, "lite textures too large");
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	// frames in flight may read the old pixels
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	if (ctx->aux) SW_CUDA(ctx, cudaStreamSynchronize(ctx->aux));
+	int r;
+	if ((r = upload_static(ctx, ctx->lite, pixels, num_pixels * 4))) return r;
+	ctx->lite_texels = num_pixels;
+	return SW_OK;
+}
+
+int sw_submit_draws_ex(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices,
+	const SwTriVertex* tri_vertices, uint32_t num_tri_vertices)
+{
+	if (!ctx || (num_draws && !draws) || (num_vertices && !vertices) || (num_tri_vertices && !tri_vertices))
+		return SW_ERR_INVALID_ARGUMENT;
 	if (!ctx->frame_open) return fail(ctx, SW_ERR_STATE, "sw_frame_begin must precede sw_submit_draws");
 	if (!ctx->arena_valid && num_draws) return fail(ctx, SW_ERR_STATE, "sw_submit_surfaces must precede sw_submit_draws");
 	int r;
@@ -908,13 +1026,17 @@ int sw_submit_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, cons
 			 reinterpret_cast<void**>(&rows))))
 		return r;
 	uint64_t row_acc = 0;
-	if ((r = prepare_draws(ctx, draws, num_draws, vertices, num_vertices, rows, &row_acc))) return r;
-	if ((r = ensure_raster_buffers(ctx, num_draws, num_vertices, row_acc))) return r;
+	if ((r = prepare_draws(ctx, draws, num_draws, vertices, num_vertices, rows, &row_acc, tri_vertices, num_tri_vertices)))
+		return r;
+	if ((r = ensure_raster_buffers(ctx, num_draws, num_vertices, row_acc, num_tri_vertices))) return r;
 	// The draw uploads and the raster setup run on the auxiliary stream, beside the surface build; they
 	// first wait until the previous frame's tile pass has finished reading these buffers.
 	if (ctx->tiles_recorded) SW_CUDA(ctx, cudaStreamWaitEvent(ctx->aux, ctx->ev_tiles, 0));
 	if ((r = upload(ctx, ctx->stage_draws, ctx->draws.ptr, draws, num_draws * sizeof(SwDrawCmd), ctx->aux))) return r;
 	if ((r = upload(ctx, ctx->stage_vertices, ctx->vertices.ptr, vertices, num_vertices * sizeof(SwVertex16), ctx->aux)))
+		return r;
+	if ((r = upload(ctx, ctx->stage_tri_vertices, ctx->tri_vertices.ptr, tri_vertices, num_tri_vertices * sizeof(SwTriVertex),
+			 ctx->aux)))
 		return r;
 	if ((r = staging_commit(ctx, ctx->stage_draw_rows, ctx->draw_rows.ptr, num_draws * sizeof(DrawRows), ctx->aux))) return r;
 	ctx->num_rows = row_acc;
@@ -1183,7 +1305,7 @@ int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, con
 	cudaStream_t s = ctx->stream, aux = ctx->aux;
 	// every per-frame array in one copy: the device buffer has the staging block's layout
 	unsigned char* d = static_cast<unsigned char*>(ctx->frame_in.ptr);
-	SW_CUDA(ctx, cudaMemcpyAsync(d, h, off[6], cudaMemcpyHostToDevice, s));
+	SW_CUDA(ctx, cudaMemcpyAsync(d, h, off[7], cudaMemcpyHostToDevice, s));
 	// raster setup on the auxiliary stream, beside the surface build
 	SW_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
 	SW_CUDA(ctx, cudaStreamWaitEvent(aux, ctx->ev_fork, 0));
@@ -1192,6 +1314,7 @@ int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, con
 	ra.draws = reinterpret_cast<const SwDrawCmd*>(d + off[3]);
 	ra.vertices = reinterpret_cast<const SwVertex16*>(d + off[4]);
 	ra.draw_rows = reinterpret_cast<const DrawRows*>(d + off[5]);
+	ra.tri_vertices = reinterpret_cast<const SwTriVertex*>(d + off[6]);
 	if ((r = check_kernel(ctx, launch_raster_setup(ra, aux), "raster setup"))) return r;
 	SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, aux));
 	const SurfaceInputs si{reinterpret_cast<const SwLight*>(d + off[0]), reinterpret_cast<const SurfaceGpu*>(d + off[1]),
@@ -1373,7 +1496,8 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 {
 	if (!ctx || !in) return SW_ERR_INVALID_ARGUMENT;
 	const SwFrameInput& f = *in;
-	if ((f.num_lights && !f.lights) || (f.num_surfaces && !f.surfaces) || (f.num_draws && (!f.draws || !f.vertices)))
+	if ((f.num_lights && !f.lights) || (f.num_surfaces && !f.surfaces) || (f.num_draws && !f.draws) ||
+		(f.num_vertices && !f.vertices) || (f.num_tri_vertices && !f.tri_vertices))
 		return SW_ERR_INVALID_ARGUMENT;
 	if (f.postprocess && f.params.pixel_format != SW_PIXEL_C64)
 		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocessing needs a colour64 frame");
@@ -1388,7 +1512,7 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	// 1. every per-frame array into one pinned staging block (two blocks alternate between frames)
 	Staging& st = ctx->gstage[ctx->gset];
 	ctx->gset ^= 1u;
-	size_t off[7];
+	size_t off[8];
 	off[0] = 0;
 	off[1] = align_up(off[0] + std::max<size_t>(f.num_lights, 1) * sizeof(SwLight), 256);
 	off[2] = align_up(off[1] + std::max<size_t>(f.num_surfaces, 1) * sizeof(SurfaceGpu), 256);
@@ -1396,8 +1520,9 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	off[4] = align_up(off[3] + std::max<size_t>(f.num_draws, 1) * sizeof(SwDrawCmd), 256);
 	off[5] = align_up(off[4] + std::max<size_t>(f.num_vertices, 1) * sizeof(SwVertex16), 256);
 	off[6] = align_up(off[5] + std::max<size_t>(f.num_draws, 1) * sizeof(DrawRows), 256);
+	off[7] = align_up(off[6] + std::max<size_t>(f.num_tri_vertices, 1) * sizeof(SwTriVertex), 256);
 	void* hv = nullptr;
-	if ((r = staging_acquire(ctx, st, off[6], &hv))) return r;
+	if ((r = staging_acquire(ctx, st, off[7], &hv))) return r;
 	unsigned char* h = static_cast<unsigned char*>(hv);
 	if (f.num_lights) std::memcpy(h + off[0], f.lights, f.num_lights * sizeof(SwLight));
 	uint64_t work = 0;
@@ -1408,13 +1533,15 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	note_surfaces(ctx, f.num_surfaces, f.total_texels, work, max_light);
 	if (f.num_draws) std::memcpy(h + off[3], f.draws, f.num_draws * sizeof(SwDrawCmd));
 	if (f.num_vertices) std::memcpy(h + off[4], f.vertices, f.num_vertices * sizeof(SwVertex16));
+	if (f.num_tri_vertices) std::memcpy(h + off[6], f.tri_vertices, f.num_tri_vertices * sizeof(SwTriVertex));
 	uint64_t rows = 0;
-	if ((r = prepare_draws(ctx, f.draws, f.num_draws, f.vertices, f.num_vertices, reinterpret_cast<DrawRows*>(h + off[5]), &rows)))
+	if ((r = prepare_draws(ctx, f.draws, f.num_draws, f.vertices, f.num_vertices, reinterpret_cast<DrawRows*>(h + off[5]), &rows,
+			 f.tri_vertices, f.num_tri_vertices)))
 		return r;
 
 	// 2. device buffers (growing them synchronises; the next capture picks up the new addresses)
 	const uint32_t bpp = bpp_of(p.pixel_format);
-	if ((r = ensure(ctx, ctx->frame_in, off[6]))) return r;
+	if ((r = ensure(ctx, ctx->frame_in, off[7]))) return r;
 	if ((r = ensure(ctx, ctx->lights, std::max<size_t>(f.num_lights, 1) * sizeof(SwLight)))) return r;
 	if ((r = ensure(ctx, ctx->arena, std::max<uint64_t>(f.total_texels, 1) * bpp))) return r;
 	if ((r = ensure(ctx, ctx->surfaces, std::max<size_t>(f.num_surfaces, 1) * sizeof(SurfaceGpu)))) return r;
@@ -1445,7 +1572,7 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 		if (r) return r;
 	}
 	ctx->stats.draws += f.num_draws; // (surfaces are counted by launch_surfaces)
-	ctx->stats.upload_bytes += off[6];
+	ctx->stats.upload_bytes += off[7];
 	return finish_graph_frame(ctx, st, p, f.postprocess != 0, f.post, f.frame_duration_s, f.dst, f.dst_pitch, f.dst_is_device,
 		post_out, direct_host);
 }
@@ -1548,8 +1675,8 @@ ViewBlock view_block(const SwCtx* ctx)
 // kernels' dependent loads stay within a few pages.
 struct ViewSlab
 {
-	size_t frame_in, counts, keys, cands, descs, surfaces, work_prefix, draws, draw_rows, rdraws, boxes, part_counts, vertices,
-		parts, rows, bytes;
+	size_t frame_in, counts, keys, cands, descs, surfaces, work_prefix, draws, draw_rows, rdraws, boxes, vertices, tri_steps,
+		rows, bytes;
 };
 ViewSlab view_slab(size_t block_bytes, uint64_t cands, uint64_t draws, uint64_t vertices, uint64_t rows)
 {
@@ -1571,9 +1698,9 @@ ViewSlab view_slab(size_t block_bytes, uint64_t cands, uint64_t draws, uint64_t 
 	v.draw_rows = take(draws * sizeof(DrawRows));
 	v.rdraws = take(draws * sizeof(RasterDraw));
 	v.boxes = take(draws * sizeof(RasterBox));
-	v.part_counts = take(draws * 4);
+
 	v.vertices = take(vertices * sizeof(SwVertex16));
-	v.parts = take(draws * SW_RASTER_MAX_PARTS * sizeof(RasterPart));
+	v.tri_steps = take(draws * 2 * sizeof(TriSteps));
 	v.rows = take(rows * sizeof(RasterRow));
 	v.bytes = at;
 	return v;
@@ -1822,8 +1949,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	ra.draws = pr.draws;
 	ra.vertices = pr.vertices;
 	ra.draw_rows = pr.draw_rows;
-	ra.parts = reinterpret_cast<RasterPart*>(slab + vs.parts);
-	ra.part_counts = reinterpret_cast<uint32_t*>(slab + vs.part_counts);
+	ra.tri_steps = reinterpret_cast<TriSteps*>(slab + vs.tri_steps);
 	ra.rdraws = reinterpret_cast<RasterDraw*>(slab + vs.rdraws);
 	ra.rows = reinterpret_cast<RasterRow*>(slab + vs.rows);
 	ra.boxes = reinterpret_cast<RasterBox*>(slab + vs.boxes);
@@ -2197,15 +2323,16 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 
 int sw_abi_layout(uint32_t* sizes, uint32_t count)
 {
-	const uint32_t s[22] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
+	const uint32_t s[23] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
 		uint32_t(sizeof(SwDirectionalLightmapElement)), uint32_t(sizeof(SwLight)), uint32_t(sizeof(SwSurfaceDesc)),
 		uint32_t(sizeof(SwVertex16)), uint32_t(sizeof(SwDrawCmd)), uint32_t(sizeof(SwFrameParams)),
 		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats)), uint32_t(sizeof(SwFrameInput)), uint32_t(sizeof(SwTuning)),
 		uint32_t(sizeof(SwMapPolygon)), uint32_t(sizeof(SwViewLeaf)), uint32_t(sizeof(SwViewFrameInput)),
 		uint32_t(sizeof(SwViewCounts)), uint32_t(sizeof(SwLightShadow)), uint32_t(sizeof(SwDepthDraw)),
-		uint32_t(sizeof(SwShadowSide)), uint32_t(sizeof(SwShadowLeaf)), uint32_t(sizeof(SwMaterialFrame))};
-	for (uint32_t i = 0; sizes && i < count && i < 22; ++i) sizes[i] = s[i];
-	return 22;
+		uint32_t(sizeof(SwShadowSide)), uint32_t(sizeof(SwShadowLeaf)), uint32_t(sizeof(SwMaterialFrame)),
+		uint32_t(sizeof(SwTriVertex))};
+	for (uint32_t i = 0; sizes && i < count && i < 23; ++i) sizes[i] = s[i];
+	return 23;
 }
 
 int sw_get_stats(SwCtx* ctx, SwStats* out)

@@ -7,7 +7,7 @@ import ctypes
 
 import numpy as np
 
-SWGPU_ABI_VERSION = 1
+SWGPU_ABI_VERSION = 2
 
 SW_OK = 0
 SW_ERR_INVALID_ARGUMENT = -1
@@ -21,8 +21,8 @@ SW_PIXEL_C32 = 0
 SW_PIXEL_C64 = 1
 
 SW_BLEND_NONE, SW_BLEND_AVERAGE, SW_BLEND_ADDITIVE, SW_BLEND_ALPHA_TEST, SW_BLEND_ALPHA_BLEND = range(5)
-SW_RASTER_FULL_PERSPECTIVE, SW_RASTER_LINE_Z_CORRECTED, SW_RASTER_AFFINE = range(3)
-SW_TEXSRC_SURFACE, SW_TEXSRC_SKYBOX = range(2)
+SW_RASTER_FULL_PERSPECTIVE, SW_RASTER_LINE_Z_CORRECTED, SW_RASTER_AFFINE, SW_RASTER_TRIANGLE = range(4)
+SW_TEXSRC_SURFACE, SW_TEXSRC_SKYBOX, SW_TEXSRC_LITE = range(3)
 SW_UPSCALE_NEAREST, SW_UPSCALE_AVG2X, SW_UPSCALE_LEARNED = range(3)
 
 SW_TEX_HAS_NORMAL_MAP = 1
@@ -51,6 +51,7 @@ SURFACE_DESC = np.dtype([
     ("lightmap_tc_shift", "<u4", 2), ("flags", "<u4"), ("num_lights", "<u4"), ("lights", "<u2", 6),
     ("emissive_light", "<f4", 3), ("out_offset", "<u8")], align=True)
 VERTEX16 = np.dtype([("x", "<i4"), ("y", "<i4")], align=True)
+TRI_VERTEX = np.dtype([("x", "<i4"), ("y", "<i4"), ("tc", "<i4", 2), ("light", "<i4", 3), ("reserved", "<i4")], align=True)
 DRAW_CMD = np.dtype([
     ("first_vertex", "<u4"), ("vertex_count", "<u4"), ("mode", "<u4"), ("blend", "<u4"), ("depth_eq", "<f4", 3),
     ("tc_eq", "<f4", 6), ("tex_size", "<u4", 2), ("tex_source", "<u4"), ("tex_offset", "<u8")], align=True)
@@ -124,7 +125,8 @@ class FrameInput(ctypes.Structure):
                 ("num_draws", ctypes.c_uint32), ("draws", ctypes.c_void_p), ("vertices", ctypes.c_void_p),
                 ("num_vertices", ctypes.c_uint32), ("postprocess", ctypes.c_uint32), ("post", PostConfig),
                 ("frame_duration_s", ctypes.c_float), ("color_modulate", ctypes.c_float * 3), ("dst", ctypes.c_void_p),
-                ("dst_pitch", ctypes.c_uint32), ("dst_is_device", ctypes.c_int32)]
+                ("dst_pitch", ctypes.c_uint32), ("dst_is_device", ctypes.c_int32), ("tri_vertices", ctypes.c_void_p),
+                ("num_tri_vertices", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class ViewFrameInput(ctypes.Structure):
@@ -163,7 +165,7 @@ LAYOUT_ORDER = [
     ("SwViewFrameInput", ctypes.sizeof(ViewFrameInput)), ("SwViewCounts", ctypes.sizeof(ViewCounts)),
     ("SwLightShadow", LIGHT_SHADOW.itemsize), ("SwDepthDraw", DEPTH_DRAW.itemsize),
     ("SwShadowSide", SHADOW_SIDE.itemsize), ("SwShadowLeaf", SHADOW_LEAF.itemsize),
-    ("SwMaterialFrame", MATERIAL_FRAME.itemsize),
+    ("SwMaterialFrame", MATERIAL_FRAME.itemsize), ("SwTriVertex", TRI_VERTEX.itemsize),
 ]
 
 

@@ -19,8 +19,8 @@ PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_DIR, "lib", "libswgpu.so")
 
 EXPORTED = [
-    "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_set_surfaces", "sw_set_skybox", "sw_register_host_buffer", "sw_unregister_host_buffer",
-    "sw_submit_draws",
+    "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_rebuild_surfaces_per_surface", "sw_set_surfaces", "sw_set_skybox", "sw_register_host_buffer", "sw_unregister_host_buffer",
+    "sw_submit_draws", "sw_submit_draws_ex", "sw_set_lite_textures",
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_read_framebuffer", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
     "sw_postprocess_noalloc", "sw_set_learned_upscaler", "sw_draw_frame", "sw_set_frame_graph", "sw_set_tuning",
@@ -57,11 +57,14 @@ def load_library(path=LIB_PATH):
         "sw_frame_begin": ([vp, vp, vp, u32], i32),
         "sw_submit_surfaces": ([vp, vp, u32, u64], i32),
         "sw_rebuild_surfaces": ([vp], i32),
+        "sw_rebuild_surfaces_per_surface": ([vp], i32),
         "sw_set_surfaces": ([vp, vp, u64], i32),
         "sw_set_skybox": ([vp, vp, vp, u64], i32),
         "sw_register_host_buffer": ([vp, vp, u64], i32),
         "sw_unregister_host_buffer": ([vp, vp], i32),
         "sw_submit_draws": ([vp, vp, u32, vp, u32], i32),
+        "sw_submit_draws_ex": ([vp, vp, u32, vp, u32, vp, u32], i32),
+        "sw_set_lite_textures": ([vp, vp, u64], i32),
         "sw_render": ([vp, vp, u32, i32], i32),
         "sw_postprocess": ([vp, vp, f32, vp, vp, u32, i32], i32),
         "sw_upscale": ([vp, u32, u32, vp, i32, vp, u32, u32, u32, i32], i32),
@@ -236,6 +239,10 @@ class GpuRenderer:
         self._check(self.lib.sw_read_shadow_maps(self.ctx, abi.ptr(out), out.size), "sw_read_shadow_maps")
         return out
 
+    def rebuild_surfaces_per_surface(self):
+        """The last submitted surfaces again, one launch per surface (the unbatched baseline)."""
+        self._check(self.lib.sw_rebuild_surfaces_per_surface(self.ctx), "sw_rebuild_surfaces_per_surface")
+
     def rebuild_surfaces(self):
         self._check(self.lib.sw_rebuild_surfaces(self.ctx), "sw_rebuild_surfaces")
 
@@ -251,6 +258,20 @@ class GpuRenderer:
             raise SwError("skybox texel arrays differ in size")
         self._check(self.lib.sw_set_skybox(self.ctx, abi.ptr(t32) if t32.size else None,
                                            abi.ptr(t64) if t64.size else None, t32.size), "sw_set_skybox")
+
+    def set_lite_textures(self, pixels):
+        """Color32 textures of triangle draws (SW_TEXSRC_LITE), one array."""
+        pixels = np.ascontiguousarray(pixels, dtype=np.uint32).reshape(-1)
+        self._check(self.lib.sw_set_lite_textures(self.ctx, abi.ptr(pixels), pixels.size), "sw_set_lite_textures")
+
+    def submit_draws_ex(self, draws, vertices, tri_vertices):
+        """Draws with triangle draws among them (SW_RASTER_TRIANGLE, vertices in tri_vertices)."""
+        draws = np.ascontiguousarray(draws, dtype=abi.DRAW_CMD)
+        vertices = np.ascontiguousarray(vertices if vertices is not None else np.zeros(0, abi.VERTEX16), dtype=abi.VERTEX16)
+        tv = np.ascontiguousarray(tri_vertices if tri_vertices is not None else np.zeros(0, abi.TRI_VERTEX),
+                                  dtype=abi.TRI_VERTEX)
+        self._check(self.lib.sw_submit_draws_ex(self.ctx, abi.ptr(draws), draws.size, abi.ptr(vertices), vertices.size,
+                                                abi.ptr(tv), tv.size), "sw_submit_draws_ex")
 
     def submit_draws(self, draws, vertices):
         draws = np.ascontiguousarray(draws, dtype=abi.DRAW_CMD)
@@ -293,7 +314,8 @@ class GpuRenderer:
                                         width, height, pitch, 1), "sw_upscale")
 
     def frame_input(self, params, lights, surfaces, total_texels, draws, vertices, post_config=None,
-                    frame_duration_s=1.0 / 60.0, color_modulate=(1.0, 1.0, 1.0), dst=None, dst_device_ptr=None, pitch=None):
+                    frame_duration_s=1.0 / 60.0, color_modulate=(1.0, 1.0, 1.0), dst=None, dst_device_ptr=None, pitch=None,
+                    tri_vertices=None):
         """SwFrameInput for draw_frame / autotune (keeps the arrays it points to alive on the object)."""
         fi = abi.FrameInput()
         fi.params = params
@@ -310,6 +332,8 @@ class GpuRenderer:
         fi.num_surfaces, fi.surfaces, fi.total_texels = surfaces.size, abi.ptr(surfaces), int(total_texels)
         fi.num_draws, fi.draws = draws.size, abi.ptr(draws)
         fi.num_vertices, fi.vertices = vertices.size, abi.ptr(vertices)
+        tv = arr(tri_vertices, abi.TRI_VERTEX)
+        fi.num_tri_vertices, fi.tri_vertices = tv.size, abi.ptr(tv)
         if post_config is not None:
             fi.postprocess = 1
             fi.post = post_config

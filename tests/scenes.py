@@ -133,3 +133,65 @@ def make_raster_scene(seed, width, height, num_quads, modes=(0, 1, 2), blends=(0
     draws = np.array(draws, dtype=abi.DRAW_CMD) if draws else np.zeros(0, abi.DRAW_CMD)
     vertices = np.array(verts, dtype=abi.VERTEX16) if verts else np.zeros(0, abi.VERTEX16)
     return arena.astype(dt), draws, vertices
+
+
+def make_triangle_draws(seed, width, height, num_triangles, lite_offset=0, blends=(0, 1, 2, 3, 4), max_texture_side=64,
+                        degenerate_frac=0.1):
+    """Random triangle draws (SW_RASTER_TRIANGLE) the way decals, sprites and models emit them
+    (f32_to_fixed16 positions, texture coordinates inside [1/32, size - 1/32], per-vertex light in 16.16,
+    partial_renderer.rs:3028-3067): positions partly outside the frame, some thin or degenerate
+    triangles, random Color32 textures with random alpha appended after lite_offset texels.
+    Returns (lite_pixels, draws, tri_vertices)."""
+    rng = np.random.default_rng(seed)
+    lite = []
+    draws = np.zeros(num_triangles, abi.DRAW_CMD)
+    tv = np.zeros(num_triangles * 3, abi.TRI_VERTEX)
+    offset = lite_offset
+    for t in range(num_triangles):
+        tw, th = (int(2 ** rng.integers(2, int(np.log2(max_texture_side)) + 1)) for _ in range(2))
+        tex = rng.integers(0, 1 << 32, tw * th, dtype=np.uint64).astype(np.uint32)
+        lite.append(tex)
+        c = rng.uniform([-0.2 * width, -0.2 * height], [1.2 * width, 1.2 * height])
+        r = rng.uniform(1, 0.4 * max(width, height))
+        pts = c + rng.uniform(-r, r, (3, 2))
+        if rng.random() < degenerate_frac:
+            kind = rng.integers(3)
+            if kind == 0:
+                pts[1] = pts[0]  # two equal vertices
+            elif kind == 1:
+                pts[:, 1] = pts[0, 1]  # zero height
+            else:
+                pts[2] = pts[0] + (pts[1] - pts[0]) * rng.uniform(0, 1)  # collinear
+        for k in range(3):
+            v = tv[3 * t + k]
+            v["x"] = int(np.trunc(np.float32(pts[k, 0]) * np.float32(65536.0)))
+            v["y"] = int(np.trunc(np.float32(pts[k, 1]) * np.float32(65536.0)))
+            tcf = rng.uniform([1.0 / 32, 1.0 / 32], [tw - 1.0 / 32, th - 1.0 / 32]).astype(np.float32)
+            v["tc"] = (np.trunc(tcf * np.float32(65536.0))).astype(np.int32)
+            light = rng.uniform(0.0, 3.0, 3).astype(np.float32)
+            if rng.random() < 0.1:
+                light[rng.integers(3)] = 0.0
+            v["light"] = (np.trunc(light * np.float32(65536.0))).astype(np.int32)
+        d = draws[t]
+        d["first_vertex"] = 3 * t
+        d["vertex_count"] = 3
+        d["mode"] = abi.SW_RASTER_TRIANGLE
+        d["blend"] = int(rng.choice(blends))
+        d["tex_size"] = (tw, th)
+        d["tex_source"] = abi.SW_TEXSRC_LITE
+        d["tex_offset"] = offset
+        offset += tw * th
+    pixels = np.concatenate(lite) if lite else np.zeros(0, np.uint32)
+    return pixels, draws, tv
+
+
+def interleave(poly_draws, tri_draws, seed):
+    """Polygon and triangle draws merged in a random order that keeps each list's own order (painter's
+    order is observable through the blends)."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros(poly_draws.size + tri_draws.size, abi.DRAW_CMD)
+    take_tri = np.zeros(out.size, bool)
+    take_tri[rng.choice(out.size, tri_draws.size, replace=False)] = True
+    out[take_tri] = tri_draws
+    out[~take_tri] = poly_draws
+    return out
