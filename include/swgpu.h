@@ -393,6 +393,14 @@ typedef struct SwFrameInput {
 int sw_draw_frame(SwCtx* ctx, const SwFrameInput* frame);
 /* Graph capture of sw_draw_frame: on (default) or off (the same work launched directly). */
 int sw_set_frame_graph(SwCtx* ctx, int enable);
+/* Frames in flight of the whole-frame calls (sw_draw_frame, sw_draw_frame_view). 1 (default): a call
+ * returns when its frame is complete. 2: a postprocessed frame whose Color32 destination lies in a
+ * registered host buffer (sw_register_host_buffer) returns once it is enqueued and the previous frame is
+ * in its destination; its copy into host memory runs on a copy engine while the next frame computes,
+ * as the reference overlaps the next frame's preparation with the previous frame's presentation
+ * (host.rs:438-448). Give consecutive frames different destination buffers; sw_sync waits for both.
+ * Frames and exposures are the same in either mode. */
+int sw_set_frames_in_flight(SwCtx* ctx, uint32_t frames);
 
 /* ---- GPU-side surface and draw preparation (no reference counterpart; the reference runs these steps
  * on the host in prepare_polygons_surfaces / build_polygons_surfaces / draw_tree, see below) ----

@@ -142,6 +142,9 @@ int swh_renderer_render_frame(SwhRenderer* renderer, uint32_t frame_index, const
  * draws (swh_frame_prepare_view + sw_draw_frame_view), 0 = the host does (swh_frame_prepare +
  * sw_draw_frame). Both give the same frame. */
 int swh_renderer_set_gpu_prep(SwhRenderer* renderer, int enable);
+/* Frames in flight of swh_renderer_render_frame (sw_set_frames_in_flight): with 2, a call returns once its
+ * frame is enqueued and the previous frame is in its host buffer (registered buffers, alternated). */
+int swh_renderer_set_frames_in_flight(SwhRenderer* renderer, uint32_t frames);
 /* The GPU context and the frame used by the renderer. */
 SwCtx* swh_renderer_context(SwhRenderer* renderer);
 SwhFrame* swh_renderer_frame(SwhRenderer* renderer);

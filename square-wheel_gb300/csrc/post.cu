@@ -537,7 +537,7 @@ int launch_bloom(const PostArgs& a, cudaStream_t stream, bool downscale)
 } // namespace
 
 int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream, cudaStream_t aux, cudaEvent_t fork,
-	cudaEvent_t join)
+	cudaEvent_t join, cudaEvent_t average_done)
 {
 	(void)num_sms;
 	const dim3 block(256);
@@ -557,6 +557,8 @@ int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream, cuda
 			cudaStreamWaitEvent(aux, fork, 0);
 		}
 		pp_average_bloom_kernel<<<1, 256, 0, overlap ? aux : stream>>>(a);
+		// the average is final here: inside a captured graph this is an event record node
+		if (average_done) cudaEventRecordWithFlags(average_done, overlap ? aux : stream, cudaEventRecordExternal);
 		if (overlap) cudaEventRecord(join, aux);
 		// blur + tonemap with the bloom sample
 		if (int e = launch_bloom(a, stream, false)) return e;
@@ -566,6 +568,7 @@ int launch_postprocess(const PostArgs& a, int num_sms, cudaStream_t stream, cuda
 	{
 		pp_line_sums_kernel<<<(a.height + 127) / 128, 128, 0, stream>>>(a);
 		pp_average_plain_kernel<<<1, 256, 0, stream>>>(a);
+		if (average_done) cudaEventRecordWithFlags(average_done, stream, cudaEventRecordExternal);
 		pp_tonemap_plain_kernel<<<dim3((a.width + 255) / 256, a.height), block, 0, stream>>>(a);
 	}
 	return int(cudaGetLastError());

@@ -419,8 +419,10 @@ struct PostArgs
 };
 
 // aux/fork/join (optional): run the exposure-average reduction on `aux`, joined back before returning.
+// average_done (optional) is recorded as soon as the average is written (an external event record node
+// when the launch is being captured).
 int launch_postprocess(const PostArgs& args, int num_sms, cudaStream_t stream, cudaStream_t aux = nullptr,
-	cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
+	cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr, cudaEvent_t average_done = nullptr);
 
 // PostprocessorConfig as Postprocessor::synchronize_config leaves it (postprocessor.rs:958-977), which
 // the host calls before every frame: every field clamped to its range. fmax/fmin return the other

@@ -60,6 +60,7 @@ struct ViewGraphKey
 	void* dst;
 	int32_t dst_is_device;
 	uint32_t slot;
+	uint32_t in_flight; // the frame runs in flight with the next one (average event in the graph)
 };
 
 } // namespace
@@ -126,6 +127,17 @@ struct SwCtx
 	float pending_dt = 0.0f;
 	float* h_average = nullptr; // pinned, 4 floats
 	cudaEvent_t average_ready = nullptr;
+
+	// Two frames in flight (sw_set_frames_in_flight): a whole-frame call returns once its frame is
+	// enqueued and the previous frame is in its host destination. Each frame's Color32 result goes to a
+	// device buffer of its slot and a copy engine moves it to the caller's registered host buffer on the
+	// copy stream while the next frame computes; the frame's average colour is signalled by an event
+	// recorded inside the graph, so the next frame's exposure is known before this frame's tonemap ends.
+	uint32_t frames_in_flight = 1;
+	cudaStream_t copy = nullptr;
+	cudaEvent_t ev_graph_done[2] = {nullptr, nullptr}, ev_d2h[2] = {nullptr, nullptr};
+	bool d2h_pending[2] = {false, false};
+	DevBuf ldr[2];
 
 	Staging stage_lights, stage_surfaces, stage_prefix, stage_draws, stage_vertices, stage_tri_vertices, stage_draw_rows, stage_io;
 
@@ -414,6 +426,20 @@ void* registered_device_pointer(SwCtx* ctx, void* ptr, size_t bytes)
 	return nullptr;
 }
 
+// The slot of a whole frame that runs in flight with the next one (sw_set_frames_in_flight(ctx, 2)): a
+// postprocessed frame whose Color32 destination lies in a registered host buffer, so a copy engine can
+// move it there asynchronously. -1: the frame completes within its call.
+int frame_pipeline_slot(SwCtx* ctx, bool postprocess, const void* dst, uint32_t dst_pitch, const SwFrameParams& p,
+	int dst_is_device, uint32_t slot)
+{
+	if (ctx->frames_in_flight < 2 || !postprocess || !dst || dst_is_device) return -1;
+	const size_t span = (size_t(p.height) - 1) * dst_pitch * 4 + size_t(p.width) * 4;
+	for (const SwCtx::HostRange& hr : ctx->registered)
+		if (static_cast<const char*>(dst) >= hr.ptr && static_cast<const char*>(dst) + span <= hr.ptr + hr.bytes)
+			return int(slot);
+	return -1;
+}
+
 int check_kernel(SwCtx* ctx, int launch_result, const char* what)
 {
 	if (launch_result != 0)
@@ -511,6 +537,9 @@ int sw_create(const SwCreateInfo* info, SwCtx** out_ctx)
 	for (cudaEvent_t* e : {&ctx->ev_setup, &ctx->ev_tiles, &ctx->ev_fork, &ctx->ev_join})
 		if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return bail(SW_ERR_CUDA);
 	if (cudaEventCreateWithFlags(&ctx->average_ready, cudaEventDisableTiming) != cudaSuccess) return bail(SW_ERR_CUDA);
+	if (cudaStreamCreateWithFlags(&ctx->copy, cudaStreamNonBlocking) != cudaSuccess) return bail(SW_ERR_CUDA);
+	for (cudaEvent_t* e : {&ctx->ev_graph_done[0], &ctx->ev_graph_done[1], &ctx->ev_d2h[0], &ctx->ev_d2h[1]})
+		if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return bail(SW_ERR_CUDA);
 	if (cudaMallocHost(reinterpret_cast<void**>(&ctx->h_average), 4 * sizeof(float)) != cudaSuccess)
 		return bail(SW_ERR_CUDA);
 	if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->d_average_mapped), ctx->h_average, 0) != cudaSuccess)
@@ -554,7 +583,7 @@ int sw_destroy(SwCtx* ctx)
 	DevBuf* bufs[] = {&ctx->texels, &ctx->texture_mips, &ctx->emissive, &ctx->emissive_mips, &ctx->lightmaps, &ctx->skybox32,
 		&ctx->skybox64, &ctx->frame_in,
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
-		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->tri_steps, &ctx->tri_vertices, &ctx->lite, &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
+		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->tri_steps, &ctx->tri_vertices, &ctx->lite, &ctx->ldr[0], &ctx->ldr[1], &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst, &ctx->map_polygons,
 		&ctx->map_vertices, &ctx->vslab, &ctx->shadow_storage, &ctx->shadow_descs};
 	for (DevBuf* b : bufs) release(*b);
@@ -583,7 +612,9 @@ int sw_destroy(SwCtx* ctx)
 	}
 	if (ctx->stream) cudaStreamDestroy(ctx->stream);
 	if (ctx->aux) cudaStreamDestroy(ctx->aux);
-	for (cudaEvent_t e : {ctx->ev_setup, ctx->ev_tiles, ctx->ev_fork, ctx->ev_join})
+	if (ctx->copy) cudaStreamDestroy(ctx->copy);
+	for (cudaEvent_t e : {ctx->ev_setup, ctx->ev_tiles, ctx->ev_fork, ctx->ev_join, ctx->ev_graph_done[0], ctx->ev_graph_done[1],
+			 ctx->ev_d2h[0], ctx->ev_d2h[1]})
 		if (e) cudaEventDestroy(e);
 	delete ctx;
 	return SW_OK;
@@ -599,6 +630,8 @@ int sw_sync(SwCtx* ctx)
 {
 	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
 	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->copy));
+	ctx->d2h_pending[0] = ctx->d2h_pending[1] = false;
 	return SW_OK;
 }
 
@@ -1300,7 +1333,7 @@ int fuse_bloom_downscale(SwCtx* ctx, RasterArgs& ra, PostArgs& pa, cudaStream_t 
 }
 
 int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, const size_t* off, uint64_t rows,
-	const PostArgs* post)
+	const PostArgs* post, cudaEvent_t average_done = nullptr)
 {
 	cudaStream_t s = ctx->stream, aux = ctx->aux;
 	// every per-frame array in one copy: the device buffer has the staging block's layout
@@ -1335,10 +1368,11 @@ int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, con
 	if (post)
 	{
 		stage_begin(ctx, STAGE_POST);
-		r = check_kernel(ctx, launch_postprocess(pp, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join), "postprocess");
+		r = check_kernel(ctx, launch_postprocess(pp, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join, average_done),
+			"postprocess");
 		stage_end(ctx, STAGE_POST);
 		if (r) return r;
-		SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_average, ctx->average.ptr, 16, cudaMemcpyDeviceToHost, s));
+		if (!average_done) SW_CUDA(ctx, cudaMemcpyAsync(ctx->h_average, ctx->average.ptr, 16, cudaMemcpyDeviceToHost, s));
 	}
 	else if (f.dst && f.dst_is_device)
 	{
@@ -1388,7 +1422,7 @@ int ensure_framebuffer(SwCtx* ctx, const SwFrameParams& p)
 // device's address space: the tonemap writes the Color32 rows straight into it (*direct_host). Other
 // host memory gets a device buffer copied out after the frame.
 int frame_post_target(SwCtx* ctx, const SwFrameParams& p, const SwPostConfig& post, const float modulate[3], void* dst,
-	uint32_t dst_pitch, int dst_is_device, PostArgs& pa, void** post_out, bool* direct_host)
+	uint32_t dst_pitch, int dst_is_device, PostArgs& pa, void** post_out, bool* direct_host, int pslot = -1)
 {
 	if (!dst) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocess needs a destination");
 	int r;
@@ -1396,7 +1430,14 @@ int frame_post_target(SwCtx* ctx, const SwFrameParams& p, const SwPostConfig& po
 	*post_out = dst;
 	*direct_host = false;
 	pa.dst_pitch = dst_pitch;
-	if (!dst_is_device)
+	if (pslot >= 0)
+	{
+		// a frame in flight: its slot's device buffer, copied out on the copy stream after the frame
+		if ((r = ensure(ctx, ctx->ldr[pslot], size_t(p.width) * p.height * 4))) return r;
+		*post_out = ctx->ldr[pslot].ptr;
+		pa.dst_pitch = p.width;
+	}
+	else if (!dst_is_device)
 	{
 		void* mapped = registered_device_pointer(ctx, dst, (size_t(p.height) - 1) * dst_pitch * 4 + size_t(p.width) * 4);
 		if (mapped)
@@ -1462,7 +1503,7 @@ int capture_and_launch(SwCtx* ctx, cudaGraphExec_t& exec, F&& enqueue)
 // After a graph frame was launched: staging and ordering events, exposure bookkeeping, and the frame
 // into the caller's host memory (a direct-host frame only needs the stream to finish).
 int finish_graph_frame(SwCtx* ctx, Staging& st, const SwFrameParams& p, bool postprocess, const SwPostConfig& post, float dt,
-	void* dst, uint32_t dst_pitch, int dst_is_device, void* post_out, bool direct_host)
+	void* dst, uint32_t dst_pitch, int dst_is_device, void* post_out, bool direct_host, int pslot = -1)
 {
 	SW_CUDA(ctx, cudaEventRecord(st.done, ctx->stream));
 	st.pending = true;
@@ -1471,6 +1512,27 @@ int finish_graph_frame(SwCtx* ctx, Staging& st, const SwFrameParams& p, bool pos
 	ctx->arena_valid = true;
 	ctx->draws_valid = false;
 	ctx->frame_open = false;
+	if (postprocess && pslot >= 0)
+	{
+		// the graph recorded average_ready after the frame's average; the Color32 frame goes out on the
+		// copy stream, and the call returns once the previous frame is in its destination
+		ctx->exposure_pending = true;
+		ctx->pending_config = post_config_clamped(post);
+		ctx->pending_dt = dt;
+		SW_CUDA(ctx, cudaEventRecord(ctx->ev_graph_done[pslot], ctx->stream));
+		SW_CUDA(ctx, cudaStreamWaitEvent(ctx->copy, ctx->ev_graph_done[pslot], 0));
+		SW_CUDA(ctx, cudaMemcpy2DAsync(dst, size_t(dst_pitch) * 4, post_out, size_t(p.width) * 4, size_t(p.width) * 4, p.height,
+						 cudaMemcpyDeviceToHost, ctx->copy));
+		SW_CUDA(ctx, cudaEventRecord(ctx->ev_d2h[pslot], ctx->copy));
+		ctx->d2h_pending[pslot] = true;
+		const int other = pslot ^ 1;
+		if (ctx->d2h_pending[other])
+		{
+			SW_CUDA(ctx, cudaEventSynchronize(ctx->ev_d2h[other]));
+			ctx->d2h_pending[other] = false;
+		}
+		return SW_OK;
+	}
 	if (postprocess)
 	{
 		SW_CUDA(ctx, cudaEventRecord(ctx->average_ready, ctx->stream));
@@ -1510,7 +1572,8 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	ctx->num_lights = f.num_lights;
 
 	// 1. every per-frame array into one pinned staging block (two blocks alternate between frames)
-	Staging& st = ctx->gstage[ctx->gset];
+	const uint32_t slot = ctx->gset;
+	Staging& st = ctx->gstage[slot];
 	ctx->gset ^= 1u;
 	size_t off[8];
 	off[0] = 0;
@@ -1553,13 +1616,24 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	PostArgs pa;
 	void* post_out = nullptr;
 	bool direct_host = false;
-	if (f.postprocess &&
-		(r = frame_post_target(ctx, p, f.post, f.color_modulate, f.dst, f.dst_pitch, f.dst_is_device, pa, &post_out, &direct_host)))
+	const int pslot = frame_pipeline_slot(ctx, f.postprocess != 0, f.dst, f.dst_pitch, p, f.dst_is_device, slot);
+	if (f.postprocess && (r = frame_post_target(ctx, p, f.post, f.color_modulate, f.dst, f.dst_pitch, f.dst_is_device, pa,
+							  &post_out, &direct_host, pslot)))
 		return r;
+	if (pslot >= 0)
+	{
+		// a frame in flight: the average kernel writes the average straight to host memory, where the next
+		// frame's exposure update reads it once the graph's average event has fired; the slot's output
+		// buffer is free once its previous copy-out has finished
+		pa.average = ctx->d_average_mapped;
+		if (ctx->d2h_pending[pslot]) SW_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_d2h[pslot], 0));
+	}
 
 	// 3. capture the device work and update (or instantiate) the frame graph; with the graph off, the
 	// same work is launched directly (with per-stage timing events when timing is on)
-	auto enqueue = [&]() { return enqueue_frame(ctx, f, h, off, rows, f.postprocess ? &pa : nullptr); };
+	auto enqueue = [&]() {
+		return enqueue_frame(ctx, f, h, off, rows, f.postprocess ? &pa : nullptr, pslot >= 0 ? ctx->average_ready : nullptr);
+	};
 	if (ctx->graph_enabled)
 	{
 		if ((r = capture_and_launch(ctx, ctx->gexec, enqueue))) return r;
@@ -1574,7 +1648,7 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	ctx->stats.draws += f.num_draws; // (surfaces are counted by launch_surfaces)
 	ctx->stats.upload_bytes += off[7];
 	return finish_graph_frame(ctx, st, p, f.postprocess != 0, f.post, f.frame_duration_s, f.dst, f.dst_pitch, f.dst_is_device,
-		post_out, direct_host);
+		post_out, direct_host, pslot);
 }
 
 int sw_set_map(SwCtx* ctx, const SwMapPolygon* polygons, uint32_t num_polygons, const float* vertices, uint32_t num_vertices)
@@ -1817,9 +1891,12 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	PostArgs pa;
 	void* post_out = nullptr;
 	bool direct_host = false;
-	if (f.postprocess &&
-		(r = frame_post_target(ctx, p, f.post, f.color_modulate, f.dst, f.dst_pitch, f.dst_is_device, pa, &post_out, &direct_host)))
+	const int pslot = frame_pipeline_slot(ctx, f.postprocess != 0, f.dst, f.dst_pitch, p, f.dst_is_device, ctx->gset);
+	if (f.postprocess && (r = frame_post_target(ctx, p, f.post, f.color_modulate, f.dst, f.dst_pitch, f.dst_is_device, pa,
+							  &post_out, &direct_host, pslot)))
 		return r;
+	// a frame in flight: its slot's output buffer is free once its previous copy-out has finished
+	if (pslot >= 0 && ctx->d2h_pending[pslot]) SW_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_d2h[pslot], 0));
 
 	// 3. the upload block of this frame (two staging blocks alternate between frames)
 	const uint32_t slot = ctx->gset;
@@ -1972,6 +2049,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	key.dst_pitch = f.dst_pitch;
 	key.dst_is_device = f.dst_is_device;
 	key.slot = slot;
+	key.in_flight = pslot >= 0 ? 1u : 0u;
 
 	// 5. replay this staging block's graph; capture it again when its key changed
 	cudaGraphExec_t& exec = ctx->vexec[slot];
@@ -1998,7 +2076,8 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 				return rr;
 			if (f.postprocess)
 			{
-				if ((rr = check_kernel(ctx, launch_postprocess(pp2, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join),
+				if ((rr = check_kernel(ctx, launch_postprocess(pp2, ctx->num_sms, s, aux, ctx->ev_fork, ctx->ev_join,
+												key.in_flight ? ctx->average_ready : nullptr),
 						 "postprocess")))
 					return rr;
 			}
@@ -2025,7 +2104,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	ctx->last_num_surfaces = 0; // sw_rebuild_surfaces has no host descriptors of this frame
 	ctx->last_surface_work = 0;
 	r = finish_graph_frame(ctx, st, p, f.postprocess != 0, f.post, f.frame_duration_s, f.dst, f.dst_pitch, f.dst_is_device,
-		post_out, direct_host);
+		post_out, direct_host, pslot);
 	if (r) return r;
 	if (cudaEventQuery(ctx->ev_counts[slot]) == cudaSuccess)
 	{
@@ -2241,6 +2320,16 @@ int sw_read_shadow_maps(SwCtx* ctx, float* dst, uint64_t max_texels)
 		const uint32_t bits = uint32_t(packed[i]);
 		std::memcpy(dst + i, &bits, 4);
 	}
+	return SW_OK;
+}
+
+int sw_set_frames_in_flight(SwCtx* ctx, uint32_t frames)
+{
+	if (!ctx || frames < 1 || frames > 2) return SW_ERR_INVALID_ARGUMENT;
+	if (frames == ctx->frames_in_flight) return SW_OK;
+	int r;
+	if ((r = sw_sync(ctx))) return r; // every frame in flight is in its destination
+	ctx->frames_in_flight = frames;
 	return SW_OK;
 }
 

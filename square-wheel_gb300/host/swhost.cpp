@@ -442,6 +442,12 @@ int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFra
 	return sw_draw_frame(r->ctx, &in);
 }
 
+int swh_renderer_set_frames_in_flight(SwhRenderer* r, uint32_t frames)
+{
+	if (!r) return SW_ERR_INVALID_ARGUMENT;
+	return sw_set_frames_in_flight(r->ctx, frames);
+}
+
 int swh_renderer_set_gpu_prep(SwhRenderer* r, int enable)
 {
 	if (!r) return SW_ERR_INVALID_ARGUMENT;

@@ -23,7 +23,7 @@ EXPORTED = [
     "sw_submit_draws", "sw_submit_draws_ex", "sw_set_lite_textures",
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_read_framebuffer", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
-    "sw_postprocess_noalloc", "sw_set_learned_upscaler", "sw_draw_frame", "sw_set_frame_graph", "sw_set_tuning",
+    "sw_postprocess_noalloc", "sw_set_learned_upscaler", "sw_draw_frame", "sw_set_frame_graph", "sw_set_frames_in_flight", "sw_set_tuning",
     "sw_get_tuning", "sw_autotune", "sw_set_map", "sw_draw_frame_view", "sw_read_view_prep",
     "sw_build_shadow_maps", "sw_set_light_shadows", "sw_read_shadow_maps", "sw_build_shadow_maps_view",
     # learned upscaler (include/swlearn.h)
@@ -82,6 +82,7 @@ def load_library(path=LIB_PATH):
         "sw_set_learned_upscaler": ([vp, vp], i32),
         "sw_draw_frame": ([vp, vp], i32),
         "sw_set_frame_graph": ([vp, i32], i32),
+        "sw_set_frames_in_flight": ([vp, u32], i32),
         "sw_set_tuning": ([vp, vp], i32),
         "sw_get_tuning": ([vp, vp], i32),
         "sw_autotune": ([vp, vp, u32, vp, ctypes.POINTER(f32)], i32),
@@ -350,6 +351,9 @@ class GpuRenderer:
     def draw_frame(self, frame_input):
         """One whole frame through sw_draw_frame (one CUDA graph unless disabled)."""
         self._check(self.lib.sw_draw_frame(self.ctx, ctypes.byref(frame_input)), "sw_draw_frame")
+
+    def set_frames_in_flight(self, frames):
+        self._check(self.lib.sw_set_frames_in_flight(self.ctx, int(frames)), "sw_set_frames_in_flight")
 
     def set_frame_graph(self, enable):
         self._check(self.lib.sw_set_frame_graph(self.ctx, 1 if enable else 0), "sw_set_frame_graph")

@@ -76,6 +76,7 @@ def load_host_library():
         "swh_renderer_render_frame": ([vp, u32, vp, vp, ctypes.c_float, vp, vp, u32, i32], i32),
         "swh_frame_prepare_view": ([vp, u32, vp], i32), "swh_frame_view_input": ([vp, vp], i32),
         "swh_renderer_set_gpu_prep": ([vp, i32], i32),
+        "swh_renderer_set_frames_in_flight": ([vp, u32], i32),
         "swh_frame_map": ([vp, ctypes.POINTER(vp), ctypes.POINTER(u32), ctypes.POINTER(vp), ctypes.POINTER(u32)], i32),
     }
     for name, (args, res) in sig.items():
@@ -91,7 +92,7 @@ HOST_EXPORTED = ["swh_scene_create", "swh_scene_destroy", "swh_scene_info", "swh
                  "swh_renderer_create", "swh_renderer_destroy", "swh_renderer_prepare_frame",
                  "swh_renderer_draw_frame", "swh_renderer_context", "swh_renderer_frame", "swh_scene_skybox",
                  "swh_renderer_render_frame", "swh_frame_prepare_view", "swh_frame_view_input",
-                 "swh_renderer_set_gpu_prep", "swh_frame_map"]
+                 "swh_renderer_set_gpu_prep", "swh_frame_map", "swh_renderer_set_frames_in_flight"]
 
 # The two map configurations of the benchmark plan.
 SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, num_materials=16, metal_frac=0.0,
@@ -312,6 +313,14 @@ class HostRenderer:
             dst, pitch, dev = None, 0, 0
         self._err(self.lib.swh_renderer_render_frame(self.handle, frame_index, ctypes.byref(options), post_p,
                                                      frame_duration_s, mod, dst, pitch or 0, dev), "render_frame")
+
+    def set_frames_in_flight(self, frames):
+        """2: render_frame returns once its frame is enqueued and the previous frame is in its buffer."""
+        self._err(self.lib.swh_renderer_set_frames_in_flight(self.handle, int(frames)), "set_frames_in_flight")
+
+    def sync(self):
+        """Wait until every frame in flight is in its buffer."""
+        self._err(load_library().sw_sync(self.context()), "sync")
 
     def set_gpu_prep(self, enable):
         """render_frame's preparation: True = on the GPU (default), False = on the host."""
