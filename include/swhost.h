@@ -41,6 +41,9 @@ typedef struct SwhSceneConfig {
 	uint32_t shadowed_lights;     /* the first this many dynamic lights cast cube shadows */
 	uint32_t scrolling_materials; /* the first this many materials scroll (s and t speeds fixed per material) */
 	uint32_t animated_materials;  /* the first this many materials cycle through 3 texture frames */
+	uint32_t num_models;          /* per-vertex animated triangle models on the rooms' floors (0 = none) */
+	uint32_t model_triangles;     /* triangles per model mesh, about (0 = 2000) */
+	uint32_t model_frames;        /* animation keyframes per mesh (0 = 8) */
 } SwhSceneConfig;
 
 typedef struct SwhSceneInfo {
@@ -56,6 +59,9 @@ int swh_scene_destroy(SwhScene* scene);
 int swh_scene_info(const SwhScene* scene, SwhSceneInfo* out_info);
 /* Static data for sw_create; pointers stay valid while the scene lives. */
 int swh_scene_create_info(const SwhScene* scene, uint32_t device, SwCreateInfo* out_info);
+/* The models' Color32 skins with their mips for sw_set_lite_textures (pointer valid while the scene
+ * lives; *out_count 0 without models). */
+int swh_scene_lite_textures(const SwhScene* scene, const uint32_t** out_pixels, uint64_t* out_count);
 /* Skybox texels for sw_set_skybox (Color32 and Color64 copies, the same layout) and, per side
  * (-X, +X, -Y, +Y, -Z, +Z) and mip, the first texel and size (0 = none): mip_offsets[side * 5 + mip].
  * Pointers stay valid while the scene lives; *out_count is 0 without a sky material. */
@@ -99,6 +105,10 @@ typedef struct SwhFrameOutputs {
 	uint32_t num_shadow_sides;
 	uint32_t num_shadow_leafs;
 	const SwShadowLeaf* shadow_leafs;
+	/* triangle draws of the visible models (SW_RASTER_TRIANGLE draws among `draws`): their vertices */
+	const SwTriVertex* tri_vertices;
+	uint32_t num_tri_vertices;
+	uint32_t model_triangles;
 } SwhFrameOutputs;
 
 typedef struct SwhFrame SwhFrame;

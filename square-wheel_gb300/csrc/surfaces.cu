@@ -6,14 +6,14 @@
 // layer mix_surface_with_texture (src/square_wheel/surfaces.rs:903-971), fused in one pass.
 //
 // Work decomposition: the frame's surfaces form one flat texel index space (prefix sums of surface
-// areas, in descriptor order). A grid of (#SMs x resident blocks) CTAs strides over it in chunks of 256
-// texels, so surfaces from 4x4 to 512x512 texels share one launch without tail effects. In a chunk,
-// lane 0 of each warp finds its first texel's surface by binary search over the prefix array and every
-// lane steps forward to its own surface (at most a few steps, only across tiny surfaces). The chunk then
-// builds the lightmap line buffer of every surface row it touches in shared memory (the reference's
-// per-row buffer, surfaces.rs:477-502), and each thread mixes its two line entries, evaluates lighting
-// and stores its texel. Neighbouring threads read neighbouring TextureElements, so texture reads and
-// surface writes are coalesced.
+// areas, in descriptor order). A grid of (#SMs x resident blocks) threads strides over it, so surfaces
+// from 4x4 to 512x512 texels share one launch without tail effects. Each warp owns 32 consecutive
+// texels: lane 0 finds the first texel's surface by binary search over the prefix array, every lane
+// then steps forward to its own surface (at most a few steps, only across tiny surfaces). Each thread
+// rebuilds the reference's row-interpolated lightmap line entries it needs (the two vertical mixes of
+// the line buffer and the horizontal mix, in the reference's operation order), evaluates lighting and
+// stores its texel. Neighbouring threads read neighbouring TextureElements and share lightmap elements,
+// so texture reads and surface writes are coalesced and lightmap reads are L1 broadcasts.
 #include "sw_kernels.cuh"
 
 #include <cmath>
@@ -147,32 +147,10 @@ __device__ __forceinline__ float light_shadow_factor(const SurfaceKernelArgs& a,
 							  : cube_side_fetch(maps + 4 * side_texels, m.size, -to_light.x, -to_light.y, az);
 }
 
-// The texel's lightmap value straight from the lightmap rows (surfaces.rs:477-502, 523-549): the two
-// line-buffer entries it needs (row mix by kv) and their mix by ku, in the reference's operation order.
-// Used when a chunk's line entries do not fit the shared line buffer.
-template <bool DIRECTIONAL>
-__device__ __forceinline__ Lm lightmap_from_rows(const SurfaceKernelArgs& a, const SurfaceGpu& s, uint32_t u, uint32_t v)
-{
-	const uint32_t log2 = s.lm_log2;
-	const uint32_t mask = (1u << log2) - 1u;
-	const uint32_t base_v = v + s.lm_shift1;
-	const uint32_t lv = base_v >> log2;
-	const float kv = mad2(float(base_v & mask), s.inv_scale, s.k_shift);
-	const uint32_t base_u = u + s.lm_shift0;
-	const uint32_t lu = base_u >> log2;
-	const float ku = mad2(float(base_u & mask), s.inv_scale, s.k_shift);
-	const uint64_t row0 = uint64_t(s.lm_offset) + uint64_t(lv) * s.lm_width;
-	const uint64_t row1 = row0 + s.lm_width;
-	const Lm line0 = lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1 + lu), lm_load<DIRECTIONAL>(a, row0 + lu), kv);
-	const Lm line1 = lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1 + lu + 1), lm_load<DIRECTIONAL>(a, row0 + lu + 1), kv);
-	return lm_mix<DIRECTIONAL>(line1, line0, ku);
-}
-
-// Lighting of one texel (surfaces.rs:515-842) given its interpolated lightmap value `l` (unused without
-// a lightmap); returns the ColorVec before conversion.
+// Lighting of one texel (surfaces.rs:515-842); returns the ColorVec before conversion.
 template <bool DIRECTIONAL>
 __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const SurfaceGpu& s, uint64_t texel, uint32_t u,
-	uint32_t v, V3 cam, const Lm& l)
+	uint32_t v, V3 cam)
 {
 	const uint32_t tex_flags = s.flags & 7u;
 	const bool use_normal_map = (tex_flags & SW_TEX_HAS_NORMAL_MAP) != 0;
@@ -200,6 +178,22 @@ __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const Surf
 	CV direct = cv_zero(); // total_light_direct
 	if (s.flags & SW_SG_LIGHTMAP)
 	{
+		const uint32_t log2 = s.lm_log2;
+		const uint32_t mask = (1u << log2) - 1u;
+		const uint32_t base_v = v + s.lm_shift1;
+		const uint32_t lv = base_v >> log2;
+		const float kv = mad2(float(base_v & mask), s.inv_scale, s.k_shift);
+		const uint32_t base_u = u + s.lm_shift0;
+		const uint32_t lu = base_u >> log2;
+		const float ku = mad2(float(base_u & mask), s.inv_scale, s.k_shift);
+		const uint64_t row0 = uint64_t(s.lm_offset) + uint64_t(lv) * s.lm_width;
+		const uint64_t row1 = row0 + s.lm_width;
+		// line_lightmap[lu] and [lu + 1] of the reference's row buffer, then the horizontal mix.
+		const Lm line0 = lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1 + lu), lm_load<DIRECTIONAL>(a, row0 + lu), kv);
+		const Lm line1 =
+			lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1 + lu + 1), lm_load<DIRECTIONAL>(a, row0 + lu + 1), kv);
+		const Lm l = lm_mix<DIRECTIONAL>(line1, line0, ku);
+
 		if (spec == 0)
 		{
 			albedo = cv_rgb(l.amb, 1.0f);
@@ -323,94 +317,24 @@ __device__ __forceinline__ typename P::T emissive_mix(const SurfaceKernelArgs& a
 	return P::from_ci(m);
 }
 
-// Work decomposition: CTAs take chunks of CHUNK consecutive texels of the flat texel space (one texel
-// per thread). Each chunk first builds, in shared memory, the reference's lightmap line buffer of every
-// surface row it touches (surfaces.rs:477-502: line entry j of row v = mix(row1[j], row0[j], kv), computed
-// once per row and entry instead of once per texel), then every thread mixes its two line entries by ku
-// and shades its texel. A chunk whose rows need more than MAX_LINE_ENTRIES entries (rows much wider than
-// the chunk at lightmap scale 1) takes the line entries from the lightmap rows per texel instead, with
-// the same operations in the same order.
-constexpr int CHUNK = 256;
-constexpr int MAX_LINE_ENTRIES = 768;
-
-// One surface present in a chunk: where its rows' line entries start in the shared line buffer.
-struct ChunkSurface
-{
-	uint32_t entry_base; // first line entry of its first row in the chunk
-	uint32_t v0;         // that row
-	uint32_t entries;    // line entries per row
-	uint32_t lu0;        // lightmap column of a row's first entry (shift0 >> log2)
-};
-
-template <bool DIRECTIONAL>
-__device__ __forceinline__ void lm_store(float* dst, const Lm& m)
-{
-	if (DIRECTIONAL)
-	{
-		float2* d = reinterpret_cast<float2*>(dst); // 40-byte entries, 8-byte aligned
-		d[0] = make_float2(m.amb[0], m.amb[1]);
-		d[1] = make_float2(m.amb[2], m.dir.x);
-		d[2] = make_float2(m.dir.y, m.dir.z);
-		d[3] = make_float2(m.dev, m.col[0]);
-		d[4] = make_float2(m.col[1], m.col[2]);
-	}
-	else
-	{
-		dst[0] = m.amb[0];
-		dst[1] = m.amb[1];
-		dst[2] = m.amb[2];
-	}
-}
-
-template <bool DIRECTIONAL>
-__device__ __forceinline__ Lm lm_fetch(const float* src)
-{
-	Lm e;
-	if (DIRECTIONAL)
-	{
-		const float2* p = reinterpret_cast<const float2*>(src);
-		const float2 q0 = p[0], q1 = p[1], q2 = p[2], q3 = p[3], q4 = p[4];
-		e.amb[0] = q0.x;
-		e.amb[1] = q0.y;
-		e.amb[2] = q1.x;
-		e.dir = mkv3(q1.y, q2.x, q2.y);
-		e.dev = q3.x;
-		e.col[0] = q3.y;
-		e.col[1] = q4.x;
-		e.col[2] = q4.y;
-	}
-	else
-	{
-		e.amb[0] = src[0];
-		e.amb[1] = src[1];
-		e.amb[2] = src[2];
-	}
-	return e;
-}
-
 template <class P, bool DIRECTIONAL>
-__global__ void __launch_bounds__(256, 4) surf_build_kernel(SurfaceKernelArgs a)
+__global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
 {
 	typedef typename P::T T;
-	constexpr int NW = DIRECTIONAL ? 10 : 3; // floats per line entry
-	__shared__ ChunkSurface s_cs[CHUNK];
-	__shared__ __align__(16) float s_line[MAX_LINE_ENTRIES * NW];
-	__shared__ uint32_t s_first, s_last, s_warp_sum[CHUNK / 32];
 	T* arena = static_cast<T*>(a.arena);
 	const uint64_t total = a.counts ? a.counts->total_texels : a.total_work;
 	const V3 cam = a.cam_pos_dev ? mkv3(a.cam_pos_dev[0], a.cam_pos_dev[1], a.cam_pos_dev[2])
 								 : mkv3(a.cam_pos[0], a.cam_pos[1], a.cam_pos[2]);
 	const uint32_t num_surfaces = a.counts ? a.counts->num_surfaces : a.num_surfaces;
-	const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-	for (uint64_t cbase = a.work_begin + uint64_t(blockIdx.x) * CHUNK; cbase < total; cbase += uint64_t(gridDim.x) * CHUNK)
+	const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint64_t warp_first = uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u);
+	for (uint64_t wbase = a.work_begin + warp_first; wbase < total; wbase += stride)
 	{
-		const uint64_t t = cbase + tid;
-		const bool valid = t < total;
-		const uint32_t count = uint32_t(min(uint64_t(CHUNK), total - cbase)); // texels of this chunk
+		const uint64_t t = wbase + lane;
 		// Surface of the warp's first texel (binary search by lane 0), then forward steps per lane.
-		const uint64_t wbase = cbase + (tid & ~31u);
 		uint32_t s0 = 0;
-		if (lane == 0 && wbase < total)
+		if (lane == 0)
 		{
 			uint32_t lo = 0, hi = num_surfaces; // prefix[lo] <= wbase < prefix[hi]
 			while (hi - lo > 1)
@@ -424,90 +348,18 @@ __global__ void __launch_bounds__(256, 4) surf_build_kernel(SurfaceKernelArgs a)
 			s0 = lo;
 		}
 		uint32_t si = __shfl_sync(0xFFFFFFFFu, s0, 0);
-		if (valid)
+		if (t >= total) continue;
+		uint64_t next = __ldg(a.work_prefix + si + 1);
+		while (next <= t)
 		{
-			uint64_t next = __ldg(a.work_prefix + si + 1);
-			while (next <= t)
-			{
-				++si;
-				next = __ldg(a.work_prefix + si + 1);
-			}
+			++si;
+			next = __ldg(a.work_prefix + si + 1);
 		}
-		__syncthreads(); // the previous chunk is done with the shared line buffer
-		if (tid == 0) s_first = si;
-		if (tid == count - 1) s_last = si;
-		__syncthreads();
-		const uint32_t first = s_first, ns = s_last - s_first + 1; // surfaces of the chunk (<= CHUNK)
-
-		// Rows and line entries of each surface of the chunk, and their exclusive prefix sum.
-		uint32_t cnt = 0;
-		ChunkSurface cs{0u, 0u, 0u, 0u};
-		if (tid < ns)
-		{
-			const SurfaceGpu& s = a.surfaces[first + tid];
-			const uint64_t p0 = __ldg(a.work_prefix + first + tid), p1 = __ldg(a.work_prefix + first + tid + 1);
-			if ((s.flags & (SW_SG_DIFFUSE | SW_SG_LIGHTMAP)) == (SW_SG_DIFFUSE | SW_SG_LIGHTMAP) && p1 > p0)
-			{
-				const uint64_t lo = max(cbase, p0) - p0, hi = min(cbase + count, p1) - 1 - p0;
-				cs.v0 = uint32_t(lo / s.width);
-				const uint32_t v1 = uint32_t(hi / s.width);
-				cs.lu0 = s.lm_shift0 >> s.lm_log2;
-				cs.entries = ((s.width - 1 + s.lm_shift0) >> s.lm_log2) - cs.lu0 + 2;
-				cnt = (v1 - cs.v0 + 1) * cs.entries;
-			}
-		}
-		uint32_t incl = cnt;
-#pragma unroll
-		for (int o = 1; o < 32; o <<= 1)
-		{
-			const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-			if (lane >= uint32_t(o)) incl += y;
-		}
-		if (lane == 31) s_warp_sum[warp] = incl;
-		__syncthreads();
-		uint32_t before = 0, total_entries = 0;
-#pragma unroll
-		for (int w = 0; w < CHUNK / 32; ++w)
-		{
-			const uint32_t ws = s_warp_sum[w];
-			if (w < int(warp)) before += ws;
-			total_entries += ws;
-		}
-		cs.entry_base = before + incl - cnt;
-		if (tid < ns) s_cs[tid] = cs;
-		__syncthreads();
-		const bool shared_line = ns <= uint32_t(CHUNK) && total_entries <= uint32_t(MAX_LINE_ENTRIES);
-		if (shared_line)
-			for (uint32_t i = tid; i < total_entries; i += CHUNK)
-			{
-				// the chunk surface owning entry i: the last one whose entries start at or before it
-				uint32_t lo = 0, hi = ns;
-				while (hi - lo > 1)
-				{
-					const uint32_t mid = (lo + hi) >> 1;
-					if (s_cs[mid].entry_base <= i)
-						lo = mid;
-					else
-						hi = mid;
-				}
-				const ChunkSurface c = s_cs[lo];
-				const SurfaceGpu& s = a.surfaces[first + lo];
-				const uint32_t r = (i - c.entry_base) / c.entries, j = (i - c.entry_base) - r * c.entries;
-				const uint32_t base_v = c.v0 + r + s.lm_shift1;
-				const uint32_t lv = base_v >> s.lm_log2;
-				const float kv = mad2(float(base_v & ((1u << s.lm_log2) - 1u)), s.inv_scale, s.k_shift);
-				const uint64_t row0 = uint64_t(s.lm_offset) + uint64_t(lv) * s.lm_width + c.lu0 + j;
-				const uint64_t row1 = row0 + s.lm_width;
-				lm_store<DIRECTIONAL>(s_line + i * NW,
-					lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1), lm_load<DIRECTIONAL>(a, row0), kv));
-			}
-		__syncthreads();
-		if (!valid) continue;
-
 		const SurfaceGpu& s = a.surfaces[si];
 		const uint32_t local = uint32_t(t - __ldg(a.work_prefix + si));
 		const uint32_t v = local / s.width;
 		const uint32_t u = local - v * s.width;
+
 		T out = T(0);
 		const bool diffuse_layer = (s.flags & SW_SG_DIFFUSE) != 0;
 		if (diffuse_layer)
@@ -516,22 +368,7 @@ __global__ void __launch_bounds__(256, 4) surf_build_kernel(SurfaceKernelArgs a)
 			const uint32_t su = wrap(s.tc0 + int32_t(u), s.tex_w);
 			const uint64_t texel =
 				__ldg(reinterpret_cast<const unsigned long long*>(a.texels) + s.tex_offset + uint64_t(sv) * s.tex_w + su);
-			Lm l;
-			if (s.flags & SW_SG_LIGHTMAP)
-			{
-				if (shared_line)
-				{
-					// line entries lu and lu + 1 of row v, then the horizontal mix (surfaces.rs:523-549)
-					const ChunkSurface c = s_cs[si - first];
-					const uint32_t base_u = u + s.lm_shift0;
-					const float ku = mad2(float(base_u & ((1u << s.lm_log2) - 1u)), s.inv_scale, s.k_shift);
-					const uint32_t e0 = c.entry_base + (v - c.v0) * c.entries + (base_u >> s.lm_log2) - c.lu0;
-					l = lm_mix<DIRECTIONAL>(lm_fetch<DIRECTIONAL>(s_line + (e0 + 1) * NW), lm_fetch<DIRECTIONAL>(s_line + e0 * NW), ku);
-				}
-				else
-					l = lightmap_from_rows<DIRECTIONAL>(a, s, u, v);
-			}
-			out = P::from_cv(shade_texel<DIRECTIONAL>(a, s, texel, u, v, cam, l));
+			out = P::from_cv(shade_texel<DIRECTIONAL>(a, s, texel, u, v, cam));
 		}
 		if (s.flags & SW_SG_EMISSIVE) out = emissive_mix<P>(a, s, u, v, out, diffuse_layer);
 		arena[s.out_offset + local] = out;

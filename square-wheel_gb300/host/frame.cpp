@@ -517,6 +517,327 @@ void FramePrep::draw_leaf(const ClippingPolygon& bounds, uint32_t leaf_index)
 		if (poly[pi].visible_frame != current_frame) continue;
 		draw_polygon(planes, pi);
 	}
+	if (leaf_index < sc.leaf_models.size() && !sc.leaf_models[leaf_index].empty()) draw_leaf_models(bounds, leaf_index);
+}
+
+namespace
+{
+// get_light_cube_light, src/square_wheel/light.rs:296-340: the cube side facing each normal axis,
+// weighted by that axis component.
+void light_cube_light(const float cube[6][3], Vec3 n, float out[3])
+{
+	for (int i = 0; i < 3; ++i) out[i] = 0.0f;
+	const float comps[3] = {n.x, n.y, n.z};
+	for (int a = 0; a < 3; ++a)
+	{
+		const int side = comps[a] <= 0.0f ? 2 * a : 2 * a + 1;
+		const float w = comps[a] <= 0.0f ? -comps[a] : comps[a];
+		for (int i = 0; i < 3; ++i) out[i] += cube[side][i] * w;
+	}
+}
+
+// Mat3 inverse (cgmath Matrix3::invert by cofactors): get_normals_matrix's inverse transpose of the
+// model matrix's axes, triangle_models_rendering.rs:722-731 (identity if singular).
+void normals_matrix(const Mat4& m, float out[3][3])
+{
+	const float a[3][3] = {{m.c[0].x, m.c[1].x, m.c[2].x}, {m.c[0].y, m.c[1].y, m.c[2].y}, {m.c[0].z, m.c[1].z, m.c[2].z}};
+	// t = transpose(axes); out = inverse(t)
+	float t[3][3];
+	for (int r = 0; r < 3; ++r)
+		for (int c = 0; c < 3; ++c) t[r][c] = a[c][r];
+	const float det = t[0][0] * (t[1][1] * t[2][2] - t[1][2] * t[2][1]) - t[0][1] * (t[1][0] * t[2][2] - t[1][2] * t[2][0]) +
+		t[0][2] * (t[1][0] * t[2][1] - t[1][1] * t[2][0]);
+	if (det == 0.0f || !std::isfinite(det))
+	{
+		for (int r = 0; r < 3; ++r)
+			for (int c = 0; c < 3; ++c) out[r][c] = r == c ? 1.0f : 0.0f;
+		return;
+	}
+	const float id = 1.0f / det;
+	out[0][0] = (t[1][1] * t[2][2] - t[1][2] * t[2][1]) * id;
+	out[0][1] = (t[0][2] * t[2][1] - t[0][1] * t[2][2]) * id;
+	out[0][2] = (t[0][1] * t[1][2] - t[0][2] * t[1][1]) * id;
+	out[1][0] = (t[1][2] * t[2][0] - t[1][0] * t[2][2]) * id;
+	out[1][1] = (t[0][0] * t[2][2] - t[0][2] * t[2][0]) * id;
+	out[1][2] = (t[0][2] * t[1][0] - t[0][0] * t[1][2]) * id;
+	out[2][0] = (t[1][0] * t[2][1] - t[1][1] * t[2][0]) * id;
+	out[2][1] = (t[0][1] * t[2][0] - t[0][0] * t[2][1]) * id;
+	out[2][2] = (t[0][0] * t[1][1] - t[0][1] * t[1][0]) * id;
+}
+
+// f32_to_fixed16, src/common/fixed_math.rs: (x * 65536) as i32, saturating.
+int32_t to_fixed16(float x) { return as_i32(x * 65536.0f); }
+} // namespace
+
+void FramePrep::draw_leaf_models(const ClippingPolygon& bounds, uint32_t leaf_index)
+{
+	// The leaf's models back to front: farther first by camera-space depth of the model's origin (the
+	// reference's LeafObjectsSorter, draw_ordering.rs, orders objects of a leaf; models here never
+	// overlap one another's leafs).
+	std::vector<std::pair<float, uint32_t>> order;
+	for (uint32_t m : sc.leaf_models[leaf_index])
+	{
+		const Vec3 p = view_transform(cam.view_matrix, sc.models[m].position);
+		order.push_back({p.z, m});
+	}
+	std::stable_sort(order.begin(), order.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+	for (const auto& o : order) draw_model(bounds, o.second);
+}
+
+void FramePrep::draw_model(const ClippingPolygon& bounds, uint32_t model_index)
+{
+	const ModelEntity& e = sc.models[model_index];
+	const ModelMesh& mesh = sc.model_meshes[e.mesh];
+	// AnimationPoint: frames f0, f1 and the weight of f0 at the frame's time
+	const float t = frame_time_s * e.anim_speed + e.anim_phase;
+	const float ft = std::floor(t);
+	const uint32_t f0 = uint32_t(int64_t(ft) % int64_t(mesh.num_frames)), f1 = (f0 + 1) % mesh.num_frames;
+	const float lerp0 = std::fmin(std::fmax(1.0f - (t - ft), 0.0f), 1.0f), lerp1 = 1.0f - lerp0;
+	const bool perform_lerp = lerp0 > 0.01f && lerp0 < 0.99f;
+	// get_object_matrix(position, rotation): translate * rotate (src/common/matrix.rs:111-117)
+	Mat4 model_matrix = mat4_from_quat(quat_from_angle_z(e.yaw));
+	model_matrix.c[3] = v4(e.position.x, e.position.y, e.position.z, 1.0f);
+	const Mat4 model_view = cam.view_matrix * model_matrix;
+
+	// calculate_triangle_model_texture_mip, triangle_models_rendering.rs:274-322 (bbox made a cube)
+	uint32_t mip = 0;
+	{
+		const Vec3 c = (mesh.bbox_min + mesh.bbox_max) * 0.5f;
+		const Vec3 hs = (mesh.bbox_max - mesh.bbox_min) * 0.5f;
+		const float ch = (hs.x + hs.y + hs.z) / 3.0f;
+		float min_x = 0, max_x = 0, min_y = 0, max_y = 0;
+		bool behind = false;
+		for (int k = 0; k < 8; ++k)
+		{
+			const Vec3 corner = v3(c.x + ((k & 1) ? ch : -ch), c.y + ((k & 2) ? ch : -ch), c.z + ((k & 4) ? ch : -ch));
+			const Vec4 vp = model_view * extend(corner, 1.0f);
+			if (vp.w <= 0.0f)
+			{
+				behind = true;
+				break;
+			}
+			const float x = vp.x / vp.w, y = vp.y / vp.w;
+			if (k == 0)
+				min_x = max_x = x, min_y = max_y = y;
+			min_x = std::fmin(min_x, x), max_x = std::fmax(max_x, x), min_y = std::fmin(min_y, y), max_y = std::fmax(max_y, y);
+		}
+		const LiteMip& m0 = sc.lite_mips[size_t(e.texture) * NUM_MIPS];
+		const float max_dim = std::fmax(max_x - min_x, max_y - min_y);
+		if (!behind)
+		{
+			if (max_dim <= 0.0f)
+				mip = NUM_MIPS - 1;
+			else
+			{
+				const float tpp = float(std::max(m0.width, m0.height)) / max_dim;
+				mip = uint32_t(std::min<int32_t>(std::max<int32_t>(as_i32(std::floor(std::log2(tpp) + opt.mip_bias)), 0), NUM_MIPS - 1));
+			}
+		}
+	}
+	const LiteMip& tex = sc.lite_mips[size_t(e.texture) * NUM_MIPS + mip];
+
+	// animate_and_transform_triangle_mesh_vertices (VertexAnimated), triangle_models_rendering.rs:7-95,
+	// with get_vertex_light (:702-720): the light cube plus the directional component
+	float nm[3][3];
+	normals_matrix(model_matrix, nm);
+	model_vertices.resize(mesh.num_vertices);
+	const Vec3* p0 = &mesh.positions[size_t(f0) * mesh.num_vertices];
+	const Vec3* p1 = &mesh.positions[size_t(f1) * mesh.num_vertices];
+	const Vec3* n0 = &mesh.normals[size_t(f0) * mesh.num_vertices];
+	const Vec3* n1 = &mesh.normals[size_t(f1) * mesh.num_vertices];
+	const Vec3* ps = lerp0 > lerp1 ? p0 : p1;
+	const Vec3* ns = lerp0 > lerp1 ? n0 : n1;
+	for (uint32_t i = 0; i < mesh.num_vertices; ++i)
+	{
+		const Vec3 pos = perform_lerp ? p0[i] * lerp0 + p1[i] * lerp1 : ps[i];
+		const Vec3 nrm = perform_lerp ? n0[i] * lerp0 + n1[i] * lerp1 : ns[i];
+		const Vec3 nt = v3(nm[0][0] * nrm.x + nm[0][1] * nrm.y + nm[0][2] * nrm.z, nm[1][0] * nrm.x + nm[1][1] * nrm.y + nm[1][2] * nrm.z,
+			nm[2][0] * nrm.x + nm[2][1] * nrm.y + nm[2][2] * nrm.z);
+		const Vec3 nn = nt * (1.0f / std::sqrt(std::fmax(dot(nt, nt), 0.00000001f)));
+		ModelVertex3d& v = model_vertices[i];
+		v.pos = view_transform(model_view, pos);
+		v.tc[0] = mesh.tex_coords[2 * i] * float(tex.width);
+		v.tc[1] = mesh.tex_coords[2 * i + 1] * float(tex.height);
+		light_cube_light(e.light_cube, nn, v.light);
+		const float ld = std::fmax(dot(nn, e.light_dir_scaled), 0.0f);
+		for (int c = 0; c < 3; ++c) v.light[c] += e.light_color[c] * ld;
+	}
+	// reject_triangle_model_back_faces and sort_model_triangles (:324-381): front faces, back to front by
+	// each triangle's greatest z
+	model_triangles.clear();
+	for (size_t k = 0; k + 2 < mesh.triangles.size(); k += 3)
+	{
+		const Vec3 a = model_vertices[mesh.triangles[k]].pos, b = model_vertices[mesh.triangles[k + 1]].pos,
+				   c = model_vertices[mesh.triangles[k + 2]].pos;
+		if (dot(cross(b - a, c - b), a) > 0.0f) model_triangles.push_back(uint32_t(k));
+	}
+	auto max_z = [&](uint32_t k) {
+		return std::fmax(std::fmax(model_vertices[mesh.triangles[k]].pos.z, model_vertices[mesh.triangles[k + 1]].pos.z),
+			model_vertices[mesh.triangles[k + 2]].pos.z);
+	};
+	std::stable_sort(model_triangles.begin(), model_triangles.end(), [&](uint32_t a, uint32_t b) { return max_z(a) > max_z(b); });
+
+	// draw_mesh (:3525-3718): the near plane when the bbox crosses it, the leaf's box planes that are
+	// tighter than the model's screen box, then fill_triangle for every triangle of each clipped fan
+	bool near_needed = false, all_behind = true;
+	ClippingPolygon mesh_box = ClippingPolygon::from_box(1e30f, 1e30f, -1e30f, -1e30f);
+	bool first_point = true;
+	for (int k = 0; k < 8; ++k)
+	{
+		const Vec3 corner = v3((k & 1) ? mesh.bbox_max.x : mesh.bbox_min.x, (k & 2) ? mesh.bbox_max.y : mesh.bbox_min.y,
+			(k & 4) ? mesh.bbox_max.z : mesh.bbox_min.z);
+		const Vec3 v = view_transform(model_view, corner);
+		if (v.z >= PREP_Z_NEAR)
+		{
+			all_behind = false;
+			const Vec2 sp = v2(v.x / v.z, v.y / v.z);
+			if (first_point)
+				mesh_box = ClippingPolygon::from_point(sp), first_point = false;
+			else
+				mesh_box.extend_with_point(sp);
+		}
+		else
+			near_needed = true;
+	}
+	if (all_behind) return;
+	Vec3 box_planes[2][8];
+	bounds.get_clip_planes(box_planes[0]);
+	mesh_box.get_clip_planes(box_planes[1]);
+	Vec3 planes_2d[4];
+	uint32_t num_2d = 0;
+	for (int k = 0; k < 4; ++k)
+		if (near_needed || box_planes[0][k].z > box_planes[1][k].z) planes_2d[num_2d++] = box_planes[0][k];
+
+	const uint32_t blend = e.blending_mode;
+	const uint64_t tex_offset = tex.offset;
+	auto clip3 = [&](const ModelVertex3d* src, uint32_t n, ModelVertex3d* dst) {
+		// clip_3d_model_polygon_by_plane with the near plane z >= Z_NEAR (src/common/clipping.rs:259-310)
+		uint32_t out = 0;
+		const ModelVertex3d* prev = &src[n - 1];
+		float prev_d = prev->pos.z;
+		auto inter = [&](const ModelVertex3d& v0, const ModelVertex3d& v1) {
+			const float d0 = v0.pos.z - PREP_Z_NEAR, d1 = v1.pos.z - PREP_Z_NEAR;
+			const float sum = d1 - d0, k0 = d0 / sum, k1 = d1 / sum;
+			ModelVertex3d r;
+			r.pos = v0.pos * k1 - v1.pos * k0;
+			for (int i = 0; i < 2; ++i) r.tc[i] = v0.tc[i] * k1 - v1.tc[i] * k0;
+			for (int i = 0; i < 3; ++i) r.light[i] = v0.light[i] * k1 - v1.light[i] * k0;
+			return r;
+		};
+		for (uint32_t i = 0; i < n && out < MAX_VERTICES; ++i)
+		{
+			const ModelVertex3d& v = src[i];
+			const float d = v.pos.z;
+			if (d > PREP_Z_NEAR)
+			{
+				if (prev_d < PREP_Z_NEAR && out < MAX_VERTICES) dst[out++] = inter(*prev, v);
+				if (out < MAX_VERTICES) dst[out++] = v;
+			}
+			else if (d == PREP_Z_NEAR)
+				dst[out++] = v;
+			else if (prev_d > PREP_Z_NEAR)
+				dst[out++] = inter(*prev, v);
+			prev = &v;
+			prev_d = d;
+		}
+		return out;
+	};
+	struct V2
+	{
+		Vec2 pos;
+		float tc[2], light[3];
+	};
+	auto clip2 = [&](const V2* src, uint32_t n, const Vec3& line, V2* dst) {
+		// clip_2d_model_polygon, src/common/clipping.rs:203-257
+		uint32_t out = 0;
+		const V2* prev = &src[n - 1];
+		float prev_d = prev->pos.x * line.x + prev->pos.y * line.y - line.z;
+		auto inter = [&](const V2& v0, const V2& v1) {
+			const float d0 = v0.pos.x * line.x + v0.pos.y * line.y - line.z, d1 = v1.pos.x * line.x + v1.pos.y * line.y - line.z;
+			const float sum = d1 - d0, k0 = d0 / sum, k1 = d1 / sum;
+			V2 r;
+			r.pos = v2(v0.pos.x * k1 - v1.pos.x * k0, v0.pos.y * k1 - v1.pos.y * k0);
+			for (int i = 0; i < 2; ++i) r.tc[i] = v0.tc[i] * k1 - v1.tc[i] * k0;
+			for (int i = 0; i < 3; ++i) r.light[i] = v0.light[i] * k1 - v1.light[i] * k0;
+			return r;
+		};
+		for (uint32_t i = 0; i < n && out < MAX_VERTICES; ++i)
+		{
+			const V2& v = src[i];
+			const float d = v.pos.x * line.x + v.pos.y * line.y - line.z;
+			if (d > 0.0f)
+			{
+				if (prev_d < 0.0f && out < MAX_VERTICES) dst[out++] = inter(*prev, v);
+				if (out < MAX_VERTICES) dst[out++] = v;
+			}
+			else if (d == 0.0f)
+				dst[out++] = v;
+			else if (prev_d > 0.0f)
+				dst[out++] = inter(*prev, v);
+			prev = &v;
+			prev_d = d;
+		}
+		return out;
+	};
+	ModelVertex3d c3[2][MAX_VERTICES];
+	V2 c2[2][MAX_VERTICES];
+	for (uint32_t k : model_triangles)
+	{
+		uint32_t n = 3;
+		for (int i = 0; i < 3; ++i) c3[0][i] = model_vertices[mesh.triangles[k + i]];
+		int src3 = 0;
+		if (near_needed)
+		{
+			n = clip3(c3[0], n, c3[1]);
+			if (n < 3) continue;
+			src3 = 1;
+		}
+		for (uint32_t i = 0; i < n; ++i)
+		{
+			const ModelVertex3d& v = c3[src3][i];
+			c2[0][i].pos = v2(v.pos.x / v.pos.z, v.pos.y / v.pos.z);
+			for (int j = 0; j < 2; ++j) c2[0][i].tc[j] = v.tc[j];
+			for (int j = 0; j < 3; ++j) c2[0][i].light[j] = v.light[j];
+		}
+		int src2 = 0;
+		bool clipped_out = false;
+		for (uint32_t pl = 0; pl < num_2d; ++pl)
+		{
+			n = clip2(c2[src2], n, planes_2d[pl], c2[src2 ^ 1]);
+			if (n < 3)
+			{
+				clipped_out = true;
+				break;
+			}
+			src2 ^= 1;
+		}
+		if (clipped_out) continue;
+		SwTriVertex fixed[MAX_VERTICES];
+		for (uint32_t i = 0; i < n; ++i)
+		{
+			const V2& v = c2[src2][i];
+			fixed[i] = SwTriVertex{to_fixed16(v.pos.x), to_fixed16(v.pos.y), {to_fixed16(v.tc[0]), to_fixed16(v.tc[1])},
+				{to_fixed16(v.light[0]), to_fixed16(v.light[1]), to_fixed16(v.light[2])}, 0};
+		}
+		for (uint32_t tri = 0; tri + 2 < n; ++tri)
+		{
+			SwDrawCmd d;
+			std::memset(&d, 0, sizeof(d));
+			d.first_vertex = uint32_t(tri_vertices.size());
+			d.vertex_count = 3;
+			d.mode = SW_RASTER_TRIANGLE;
+			d.blend = blend;
+			d.tex_size[0] = tex.width;
+			d.tex_size[1] = tex.height;
+			d.tex_source = SW_TEXSRC_LITE;
+			d.tex_offset = tex_offset;
+			tri_vertices.push_back(fixed[0]);
+			tri_vertices.push_back(fixed[tri + 1]);
+			tri_vertices.push_back(fixed[tri + 2]);
+			draws.push_back(d);
+			++stats.model_triangles;
+		}
+	}
 }
 
 void FramePrep::draw_skybox(const ClippingPolygon& viewport)
@@ -730,6 +1051,7 @@ void FramePrep::prepare_with_camera(const CameraMatrices& camera, const std::vec
 	build_surface_descs();
 	draws.clear();
 	vertices.clear();
+	tri_vertices.clear();
 	// perform_rasterization_for_viewport_part (:1285-1325): skybox first, then the tree
 	draw_skybox(ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height)));
 	draw_tree();

@@ -87,6 +87,7 @@ struct FrameOptions
 struct FrameStats
 {
 	uint32_t visible_leafs = 0, visible_polygons = 0, draws = 0, camera_leaf = 0, skybox_draws = 0;
+	uint32_t model_triangles = 0; // triangle draws of the visible models
 	uint64_t surface_texels = 0;
 };
 
@@ -116,6 +117,7 @@ public:
 	uint64_t total_texels = 0;
 	std::vector<SwDrawCmd> draws;
 	std::vector<SwVertex16> vertices;
+	std::vector<SwTriVertex> tri_vertices; // vertices of the triangle draws (the leafs' models)
 	std::vector<SwLight> lights;
 	SwFrameParams params{};
 	FrameStats stats;
@@ -193,6 +195,18 @@ private:
 	void draw_skybox(const ClippingPolygon& viewport);
 	void draw_tree();
 	void draw_leaf(const ClippingPolygon& bounds, uint32_t leaf_index);
+	// The leaf's triangle models after its polygons (draw_leaf's dynamic models, partial_renderer.rs:
+	// 2562-2792; build_dynamic_models_buffers :1122-1190; draw_mesh :3525-3718).
+	void draw_leaf_models(const ClippingPolygon& bounds, uint32_t leaf_index);
+	void draw_model(const ClippingPolygon& bounds, uint32_t model_index);
+	struct ModelVertex3d
+	{
+		Vec3 pos;
+		float tc[2];
+		float light[3];
+	};
+	std::vector<ModelVertex3d> model_vertices; // the current model's transformed vertices
+	std::vector<uint32_t> model_triangles;     // its visible triangles, back to front
 	void draw_polygon(const Vec3 clip_planes[8], uint32_t polygon_index);
 	// draw_polygon (partial_renderer.rs:4011-4142) of transformed vertices with their equations and texture.
 	void emit_draw(const Vec3 clip_planes[8], const Vec3* vertices_transformed, uint32_t num_vertices,

@@ -39,6 +39,7 @@ struct Room
 	float cx, cy; // corridor centre lines (cell centre lines)
 	uint32_t mat_wall, mat_floor, mat_ceiling;
 	uint32_t ceiling_first = 0, ceiling_end = 0; // the ceiling's polygons
+	uint32_t leaf = 0;
 	int32_t tc_shift[2];
 	std::vector<Vec3> lights;
 	std::vector<Vec3> light_colors;
@@ -579,6 +580,7 @@ struct Builder
 
 		// Room leaf.
 		const uint32_t room_leaf = begin_leaf(int32_t(ri));
+		rooms[ri].leaf = room_leaf;
 		add_face_rect(2, 0.0f, 1.0f, r.x0, r.x1, r.y0, r.y1, r.mat_floor, r.tc_shift);
 		rooms[ri].ceiling_first = uint32_t(sc.polygons.size());
 		add_face_rect(2, r.h, -1.0f, r.x0, r.x1, r.y0, r.y1, r.mat_ceiling, r.tc_shift);
@@ -970,6 +972,98 @@ SwCreateInfo Scene::create_info(uint32_t device) const
 	return ci;
 }
 
+// ---- triangle models ------------------------------------------------------------------------
+
+// A blob mesh: a (stacks + 1) x (slices + 1) latitude-longitude grid (the seam duplicated for texture
+// coordinates), 2 * slices * (stacks - 1) triangles, whose radius ripples over the animation's frames;
+// normals are the ripple-free directions. Triangles wind so that the front side faces outwards.
+ModelMesh make_model_mesh(Rng& rng, uint32_t triangles, uint32_t frames)
+{
+	const uint32_t n = std::max<uint32_t>(3, uint32_t(std::ceil(std::sqrt(float(triangles) * 0.5f))));
+	const uint32_t stacks = n, slices = n;
+	const float pi = 3.14159265358979323846f;
+	const float radius = rng.uniform(18.0f, 36.0f);
+	const float ripple = rng.uniform(0.08f, 0.22f);
+	const float k0 = float(2 + rng.below(3)), k1 = float(1 + rng.below(3));
+	ModelMesh m;
+	m.num_frames = frames;
+	m.num_vertices = (stacks + 1) * (slices + 1);
+	m.positions.resize(size_t(frames) * m.num_vertices);
+	m.normals.resize(size_t(frames) * m.num_vertices);
+	m.tex_coords.resize(size_t(m.num_vertices) * 2);
+	m.bbox_min = v3(1e30f, 1e30f, 1e30f);
+	m.bbox_max = v3(-1e30f, -1e30f, -1e30f);
+	for (uint32_t f = 0; f < frames; ++f)
+		for (uint32_t i = 0; i <= stacks; ++i)
+			for (uint32_t j = 0; j <= slices; ++j)
+			{
+				const float theta = pi * float(i) / float(stacks), phi = 2.0f * pi * float(j) / float(slices);
+				const Vec3 dir = v3(std::sin(theta) * std::cos(phi), std::sin(theta) * std::sin(phi), std::cos(theta));
+				const float r = radius * (1.0f + ripple * std::sin(k0 * phi + 2.0f * pi * float(f) / float(frames)) *
+					std::sin(k1 * theta + pi * float(f) / float(frames)));
+				const uint32_t v = i * (slices + 1) + j;
+				const Vec3 p = dir * r;
+				m.positions[size_t(f) * m.num_vertices + v] = p;
+				m.normals[size_t(f) * m.num_vertices + v] = dir;
+				m.bbox_min = v3(std::min(m.bbox_min.x, p.x), std::min(m.bbox_min.y, p.y), std::min(m.bbox_min.z, p.z));
+				m.bbox_max = v3(std::max(m.bbox_max.x, p.x), std::max(m.bbox_max.y, p.y), std::max(m.bbox_max.z, p.z));
+				if (f == 0)
+				{
+					m.tex_coords[2 * v + 0] = float(j) / float(slices);
+					m.tex_coords[2 * v + 1] = float(i) / float(stacks);
+				}
+			}
+	for (uint32_t i = 0; i < stacks; ++i)
+		for (uint32_t j = 0; j < slices; ++j)
+		{
+			const uint32_t a = i * (slices + 1) + j, b = a + 1, c = a + slices + 1, d = c + 1;
+			if (i != 0) m.triangles.insert(m.triangles.end(), {a, c, b});
+			if (i != stacks - 1) m.triangles.insert(m.triangles.end(), {b, c, d});
+		}
+	return m;
+}
+
+// A model skin: a Color32 TextureLite with NUM_MIPS mips (each the 2x2 average of the one above, as
+// Color32::get_average pairs average, color.rs:46-49), stripes over value noise; `cutout` skins get holes
+// of zero alpha for alpha-tested models.
+void make_model_skin(Rng& rng, uint32_t size, bool cutout, Scene& sc)
+{
+	std::vector<uint32_t> img(size_t(size) * size);
+	const float base[3] = {rng.uniform(60, 230), rng.uniform(60, 230), rng.uniform(60, 230)};
+	const float stripes = float(2 + rng.below(6));
+	for (uint32_t y = 0; y < size; ++y)
+		for (uint32_t x = 0; x < size; ++x)
+		{
+			const float s = 0.75f + 0.25f * std::sin(stripes * 6.2831853f * float(x + y) / float(size));
+			const float noise = rng.uniform(0.85f, 1.0f);
+			uint32_t c = 0;
+			for (int k = 0; k < 3; ++k) c |= uint32_t(std::fmin(base[k] * s * noise, 255.0f)) << (8 * (2 - k));
+			const bool hole = cutout && ((x / 4 + y / 4) % 5 == 0);
+			c |= (hole ? 0u : 255u) << 24;
+			img[size_t(y) * size + x] = c;
+		}
+	uint32_t w = size, h = size;
+	for (uint32_t mip = 0; mip < NUM_MIPS; ++mip)
+	{
+		sc.lite_mips.push_back(LiteMip{uint64_t(sc.lite_pixels.size()), w, h});
+		sc.lite_pixels.insert(sc.lite_pixels.end(), img.begin(), img.end());
+		if (mip + 1 == NUM_MIPS) break;
+		const uint32_t nw = std::max(w / 2, 1u), nh = std::max(h / 2, 1u);
+		std::vector<uint32_t> next(size_t(nw) * nh);
+		auto avg = [](uint32_t a, uint32_t b) { return (((a ^ b) & 0xFEFEFEFEu) >> 1) + (a & b); };
+		for (uint32_t y = 0; y < nh; ++y)
+			for (uint32_t x = 0; x < nw; ++x)
+			{
+				const uint32_t* r0 = &img[size_t(2 * y) * w + 2 * x];
+				const uint32_t* r1 = r0 + w;
+				next[size_t(y) * nw + x] = avg(avg(r0[0], r0[1]), avg(r1[0], r1[1]));
+			}
+		img.swap(next);
+		w = nw;
+		h = nh;
+	}
+}
+
 bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 {
 	if (cfg.grid_x == 0 || cfg.grid_y == 0 || cfg.grid_x * cfg.grid_y > 4096)
@@ -1107,6 +1201,43 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 			if (sky[ri])
 				for (uint32_t p = b.rooms[ri].ceiling_first; p < b.rooms[ri].ceiling_end; ++p)
 					sc.polygons[p].texture = uint32_t(sc.sky_material);
+	}
+	if (cfg.num_models)
+	{
+		// Models: a few meshes and skins shared by num_models placements on the floors of the rooms (own
+		// generator: the rest of the scene is unchanged), each inside one room leaf with its light.
+		Rng mrng(cfg.seed ^ 0x30DE15u);
+		const uint32_t num_meshes = 4;
+		for (uint32_t k = 0; k < num_meshes; ++k)
+		{
+			sc.model_meshes.push_back(make_model_mesh(mrng, std::max(cfg.model_triangles, 8u), std::max(cfg.model_frames, 1u)));
+			make_model_skin(mrng, 64, k == num_meshes - 1, sc);
+		}
+		sc.leaf_models.assign(sc.leafs.size(), {});
+		const uint32_t blends[4] = {SW_BLEND_NONE, SW_BLEND_NONE, SW_BLEND_ALPHA_TEST, SW_BLEND_ADDITIVE};
+		for (uint32_t i = 0; i < cfg.num_models; ++i)
+		{
+			const uint32_t ri = mrng.below(uint32_t(b.rooms.size()));
+			const Room& r = b.rooms[ri];
+			ModelEntity e;
+			e.mesh = mrng.below(num_meshes);
+			e.texture = e.mesh;
+			e.leaf = r.leaf;
+			e.blending_mode = e.mesh == num_meshes - 1 ? SW_BLEND_ALPHA_TEST : blends[mrng.below(4)];
+			const ModelMesh& mm = sc.model_meshes[e.mesh];
+			const float margin = 48.0f;
+			e.position = v3(mrng.uniform(r.x0 + margin, r.x1 - margin), mrng.uniform(r.y0 + margin, r.y1 - margin),
+				-mm.bbox_min.z + 2.0f);
+			e.yaw = mrng.uniform(0.0f, 6.2831853f);
+			e.anim_speed = mrng.uniform(4.0f, 12.0f);
+			e.anim_phase = mrng.uniform(0.0f, float(mm.num_frames));
+			for (int s6 = 0; s6 < 6; ++s6)
+				for (int c = 0; c < 3; ++c) e.light_cube[s6][c] = mrng.uniform(0.2f, 0.9f);
+			e.light_dir_scaled = v3(mrng.uniform(-0.6f, 0.6f), mrng.uniform(-0.6f, 0.6f), mrng.uniform(0.2f, 1.0f));
+			for (int c = 0; c < 3; ++c) e.light_color[c] = mrng.uniform(0.3f, 1.2f);
+			sc.leaf_models[e.leaf].push_back(uint32_t(sc.models.size()));
+			sc.models.push_back(e);
+		}
 	}
 	for (uint32_t k = 0; k < cfg.num_dynamic_lights; ++k)
 	{

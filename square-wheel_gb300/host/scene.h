@@ -95,6 +95,38 @@ struct DynamicLightSpec
 	float color[3];
 };
 
+// A per-vertex animated triangle model mesh (TriangleModelMesh with VertexData::VertexAnimated,
+// src/square_wheel/triangle_model.rs): frame f's vertex i at positions[f * num_vertices + i].
+struct ModelMesh
+{
+	uint32_t num_vertices = 0, num_frames = 0;
+	std::vector<Vec3> positions, normals; // num_frames x num_vertices
+	std::vector<float> tex_coords;        // 2 per vertex, in units of the texture size
+	std::vector<uint32_t> triangles;      // 3 vertex indices per triangle
+	Vec3 bbox_min, bbox_max;              // over every frame
+};
+
+// A placed model (ModelEntity, src/square_wheel/frame_info.rs:44-78): its mesh, position, rotation about
+// the vertical axis, animation (frames per second and phase), blending mode, skin (a TextureLite with
+// NUM_MIPS mips) and the light it receives (LightGridElement, src/common/bsp_map_compact.rs: a light cube
+// and a directional component).
+struct ModelEntity
+{
+	uint32_t mesh, texture, leaf, blending_mode;
+	Vec3 position;
+	float yaw, anim_speed, anim_phase;
+	float light_cube[6][3];
+	Vec3 light_dir_scaled;
+	float light_color[3];
+};
+
+// One mip of a TextureLite (Color32 pixels, src/square_wheel/textures.rs:89-91) in Scene::lite_pixels.
+struct LiteMip
+{
+	uint64_t offset;
+	uint32_t width, height;
+};
+
 struct CameraKey
 {
 	Vec3 position;
@@ -125,6 +157,9 @@ struct SceneConfig
 	uint32_t shadowed_lights = 0;     // the first this many dynamic lights cast cube shadows
 	uint32_t scrolling_materials = 0; // the first this many materials scroll (Material::scroll_speed)
 	uint32_t animated_materials = 0;  // the first this many materials cycle through 3 frames (framed_animation)
+	uint32_t num_models = 0;          // per-vertex animated triangle models placed in the rooms
+	uint32_t model_triangles = 2000;  // triangles per model mesh (about)
+	uint32_t model_frames = 8;        // animation keyframes per mesh
 };
 
 struct Scene
@@ -154,6 +189,13 @@ struct Scene
 	std::vector<uint32_t> skybox32;
 	std::vector<uint64_t> skybox64;
 	SkyboxMip skybox_mips[6][NUM_MIPS];
+	// Triangle models: meshes, placed models, the models of each leaf, and their skins' mips
+	// (texture * NUM_MIPS + mip) in one Color32 array (sw_set_lite_textures).
+	std::vector<ModelMesh> model_meshes;
+	std::vector<ModelEntity> models;
+	std::vector<std::vector<uint32_t>> leaf_models;
+	std::vector<uint32_t> lite_pixels;
+	std::vector<LiteMip> lite_mips;
 
 	uint32_t root_node() const { return nodes.empty() ? FIRST_LEAF_INDEX : uint32_t(nodes.size() - 1); }
 	void frame_lights(uint32_t frame, std::vector<SwLight>& out) const;

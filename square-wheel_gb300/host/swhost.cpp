@@ -127,6 +127,14 @@ int swh_scene_create(const SwhSceneConfig* c, SwhScene** out)
 	cfg.shadowed_lights = c->shadowed_lights;
 	cfg.scrolling_materials = c->scrolling_materials;
 	cfg.animated_materials = c->animated_materials;
+	cfg.num_models = c->num_models;
+	cfg.model_triangles = c->model_triangles ? c->model_triangles : 2000;
+	cfg.model_frames = c->model_frames ? c->model_frames : 8;
+	if (cfg.num_models > 100000 || cfg.model_triangles > 200000 || cfg.model_frames > 256)
+	{
+		g_error = "too many models, model triangles or frames";
+		return SW_ERR_INVALID_ARGUMENT;
+	}
 	SwhScene* s = new (std::nothrow) SwhScene();
 	if (!s) return SW_ERR_OUT_OF_MEMORY;
 	try
@@ -193,6 +201,14 @@ int swh_scene_create_info(const SwhScene* s, uint32_t device, SwCreateInfo* out)
 {
 	if (!s || !out) return SW_ERR_INVALID_ARGUMENT;
 	*out = s->scene.create_info(device);
+	return SW_OK;
+}
+
+int swh_scene_lite_textures(const SwhScene* s, const uint32_t** out_pixels, uint64_t* out_count)
+{
+	if (!s || !out_pixels || !out_count) return SW_ERR_INVALID_ARGUMENT;
+	*out_pixels = s->scene.lite_pixels.data();
+	*out_count = s->scene.lite_pixels.size();
 	return SW_OK;
 }
 
@@ -312,6 +328,9 @@ int swh_frame_outputs(const SwhFrame* f, SwhFrameOutputs* out)
 	out->num_shadow_sides = uint32_t(p.shadow_sides.size());
 	out->num_shadow_leafs = uint32_t(p.shadow_leafs.size());
 	out->shadow_leafs = p.shadow_leafs.data();
+	out->tri_vertices = p.tri_vertices.data();
+	out->num_tri_vertices = uint32_t(p.tri_vertices.size());
+	out->model_triangles = p.stats.model_triangles;
 	return SW_OK;
 }
 
@@ -327,6 +346,14 @@ int swh_renderer_create(const SwhScene* s, uint32_t device, SwhRenderer** out)
 	if (st != SW_OK)
 	{
 		g_error = "sw_create failed";
+		delete r;
+		return st;
+	}
+	if (!s->scene.lite_pixels.empty() &&
+		(st = sw_set_lite_textures(r->ctx, s->scene.lite_pixels.data(), s->scene.lite_pixels.size())) != SW_OK)
+	{
+		g_error = "sw_set_lite_textures failed";
+		sw_destroy(r->ctx);
 		delete r;
 		return st;
 	}
@@ -393,7 +420,9 @@ int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFra
 	float frame_duration_s, const float color_modulate[3], void* dst, uint32_t pitch, int dst_is_device)
 {
 	if (!r || (post && (!dst || !color_modulate))) return SW_ERR_INVALID_ARGUMENT;
-	if (r->gpu_prep)
+	// The GPU-side preparation emits each leaf's polygons only; a scene with triangle models (drawn after
+	// their leaf's polygons) takes the host-prepared draw list.
+	if (r->gpu_prep && r->scene->scene.models.empty())
 	{
 		int st = swh_frame_prepare_view(r->frame, frame_index, o);
 		if (st) return st;
@@ -429,6 +458,8 @@ int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFra
 	in.draws = p.draws.data();
 	in.vertices = p.vertices.data();
 	in.num_vertices = uint32_t(p.vertices.size());
+	in.tri_vertices = p.tri_vertices.data();
+	in.num_tri_vertices = uint32_t(p.tri_vertices.size());
 	if (post)
 	{
 		in.postprocess = 1;

@@ -24,7 +24,8 @@ class SceneConfig(ctypes.Structure):
         ("sky_rooms", ctypes.c_uint32), ("skybox_size", ctypes.c_uint32), ("skybox_brightness", ctypes.c_float),
         ("skybox_missing_side", ctypes.c_int32), ("sky_rotation_speed", ctypes.c_float),
         ("camera_pitch", ctypes.c_float), ("shadowed_lights", ctypes.c_uint32), ("scrolling_materials", ctypes.c_uint32),
-        ("animated_materials", ctypes.c_uint32),
+        ("animated_materials", ctypes.c_uint32), ("num_models", ctypes.c_uint32), ("model_triangles", ctypes.c_uint32),
+        ("model_frames", ctypes.c_uint32),
     ]
 
 
@@ -51,7 +52,9 @@ class FrameOutputs(ctypes.Structure):
                 ("num_depth_draws", ctypes.c_uint32), ("num_depth_vertices", ctypes.c_uint32),
                 ("depth_vertices", ctypes.c_void_p), ("shadow_texels", ctypes.c_uint64),
                 ("shadow_sides", ctypes.c_void_p), ("num_shadow_sides", ctypes.c_uint32),
-                ("num_shadow_leafs", ctypes.c_uint32), ("shadow_leafs", ctypes.c_void_p)]
+                ("num_shadow_leafs", ctypes.c_uint32), ("shadow_leafs", ctypes.c_void_p),
+                ("tri_vertices", ctypes.c_void_p), ("num_tri_vertices", ctypes.c_uint32),
+                ("model_triangles", ctypes.c_uint32)]
 
 
 def load_host_library():
@@ -77,6 +80,7 @@ def load_host_library():
         "swh_frame_prepare_view": ([vp, u32, vp], i32), "swh_frame_view_input": ([vp, vp], i32),
         "swh_renderer_set_gpu_prep": ([vp, i32], i32),
         "swh_renderer_set_frames_in_flight": ([vp, u32], i32),
+        "swh_scene_lite_textures": ([vp, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_uint64)], i32),
         "swh_frame_map": ([vp, ctypes.POINTER(vp), ctypes.POINTER(u32), ctypes.POINTER(vp), ctypes.POINTER(u32)], i32),
     }
     for name, (args, res) in sig.items():
@@ -92,7 +96,8 @@ HOST_EXPORTED = ["swh_scene_create", "swh_scene_destroy", "swh_scene_info", "swh
                  "swh_renderer_create", "swh_renderer_destroy", "swh_renderer_prepare_frame",
                  "swh_renderer_draw_frame", "swh_renderer_context", "swh_renderer_frame", "swh_scene_skybox",
                  "swh_renderer_render_frame", "swh_frame_prepare_view", "swh_frame_view_input",
-                 "swh_renderer_set_gpu_prep", "swh_frame_map", "swh_renderer_set_frames_in_flight"]
+                 "swh_renderer_set_gpu_prep", "swh_frame_map", "swh_renderer_set_frames_in_flight",
+                 "swh_scene_lite_textures"]
 
 # The two map configurations of the benchmark plan.
 SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, num_materials=16, metal_frac=0.0,
@@ -101,6 +106,9 @@ SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, 
 FULL_MAP = dict(seed=2, grid_x=8, grid_y=8, tile_size=80.0, texture_size=256, num_materials=32, metal_frac=0.25,
                 dielectric_frac=0.25, normal_maps=1, directional_lightmaps=1, lights_per_room=2,
                 num_dynamic_lights=8, num_frames=256)
+# The full-size map with triangle models: 200 per-vertex animated models of about 2k triangles and 8
+# keyframes each on the rooms' floors (the stress configuration's models).
+MODEL_MAP = dict(FULL_MAP, num_models=200, model_triangles=2000, model_frames=8)
 # The small map with a sky: three rooms open to a skybox (the sky material's six 128x128 sides, HDR
 # brightness 2, rotating slowly), the camera looking 0.45 rad up so ceilings are in view.
 SKY_MAP = dict(SMALL_MAP, sky_rooms=3, skybox_size=128, skybox_brightness=2.0, sky_rotation_speed=0.01,
@@ -121,7 +129,7 @@ class Scene:
                         lights_per_room=1, num_dynamic_lights=0, num_frames=64, emissive_frac=0.0, sky_rooms=0,
                         skybox_size=128, skybox_brightness=1.0, skybox_missing_side=-1, sky_rotation_speed=0.01,
                         camera_pitch=0.0, shadowed_lights=0, scrolling_materials=0,
-                        animated_materials=0)
+                        animated_materials=0, num_models=0, model_triangles=2000, model_frames=8)
         for k, v in kw.items():
             setattr(c, k, v)
         self.config = c
@@ -153,6 +161,15 @@ class Scene:
             return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)),
                                          shape=(count * np.dtype(dt).itemsize,)).view(dt).copy()
         return arr(t32, np.uint32), arr(t64, np.uint64), offs.reshape(6, 5), sizes.reshape(6, 5)
+
+    def lite_textures(self):
+        """The models' Color32 skins with their mips (one uint32 array, sw_set_lite_textures)."""
+        p, n = ctypes.c_void_p(), ctypes.c_uint64()
+        _check(self.lib, self.lib.swh_scene_lite_textures(self.handle, ctypes.byref(p), ctypes.byref(n)),
+               "swh_scene_lite_textures")
+        if not p.value or n.value == 0:
+            return np.zeros(0, np.uint32)
+        return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint32)), shape=(int(n.value),)).copy()
 
     def static_data(self):
         """numpy copies of the static data (for the oracle and GpuRenderer)."""
@@ -225,6 +242,8 @@ class Frame:
         self.surfaces = arr(o.surfaces, o.num_surfaces, abi.SURFACE_DESC)
         self.draws = arr(o.draws, o.num_draws, abi.DRAW_CMD)
         self.vertices = arr(o.vertices, o.num_vertices, abi.VERTEX16)
+        self.tri_vertices = arr(o.tri_vertices, o.num_tri_vertices, abi.TRI_VERTEX)
+        self.model_triangles = int(o.model_triangles)
         self.lights = arr(o.lights, o.num_lights, abi.LIGHT)
         self.total_texels = int(o.total_texels)
         self.params = abi.FrameParams()

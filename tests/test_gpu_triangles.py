@@ -89,3 +89,29 @@ def test_triangle_validation(gpu_ok):
             r.submit_draws_ex(bad, None, tv)
     finally:
         r.close()
+
+
+@pytest.mark.parametrize("fmt", [abi.SW_PIXEL_C32, abi.SW_PIXEL_C64])
+def test_model_frames(gpu_ok, fmt):
+    """Whole frames of a map with animated triangle models (drawn after their leaf's polygons) through
+    the C++ host renderer and one frame graph, against the oracle's frames from the same host arrays."""
+    from sqwheel import host
+    scene = host.Scene(**dict(host.SMALL_MAP, num_models=40))
+    st = scene.static_data()
+    lite = scene.lite_textures()
+    hr = host.HostRenderer(scene)
+    fr = host.Frame(scene)
+    dt = np.uint64 if fmt == abi.SW_PIXEL_C64 else np.uint32
+    opts = host.frame_options(640, 480, fmt, directional=False)
+    want = np.zeros((480, 640), dt)
+    try:
+        for fi in (0, 10, 11, 30, 47):
+            fr.prepare(fi, opts)
+            assert fr.model_triangles > 0 or fi == 30
+            arena = oracle.build_surfaces(st, fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=8)
+            assert oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, want, tri_vertices=fr.tri_vertices, lite=lite) == 0
+            got = np.zeros((480, 640), dt)
+            hr.render_frame(fi, opts, out=got)
+            assert np.array_equal(want, got), f"frame {fi}: {(want != got).sum()} pixels differ"
+    finally:
+        hr.close()
