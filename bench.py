@@ -678,6 +678,154 @@ def cpu_frame_baseline(work, max_frames=4, gpu_ldr=None):
 
 
 # ---------------------------------------------------------------------------------------------------------
+# models workload: the frame with triangle models (the stress configuration's animated models)
+
+def run_models_gpu(args, world, rank, local):
+    """value: frames/s of device time of the 1920x1080 colour64 + bloom + tonemap frame of the 64-room map
+    with 200 per-vertex animated triangle models (about 2k triangles, 8 keyframes each) drawn after their
+    leaf's polygons (host-prepared draw list, one CUDA graph per frame, L2 flushed before each);
+    e2e: the same frames through swh_renderer_render_frame with two frames in flight."""
+    import ctypes
+    import torch
+    from sqwheel import abi, gpu, host
+    torch.cuda.set_device(local)
+    scene = host.Scene(**host.MODEL_MAP)
+    static = scene.static_data()
+    lite = scene.lite_textures()
+    opts = host.frame_options(W, H, abi.SW_PIXEL_C64, directional=True)
+    cfg = abi.PostConfig.default()
+    fr = host.Frame(scene)
+    frames, prep_ms = [], []
+    for fi in frame_indices(args.warmup + args.steps, replica_offset(rank)):
+        t0 = time.perf_counter()
+        fr.prepare(fi, opts)
+        prep_ms.append((time.perf_counter() - t0) * 1e3)
+        frames.append(dict(index=fi, surfaces=fr.surfaces, draws=fr.draws, vertices=fr.vertices, tri=fr.tri_vertices,
+                           lights=fr.lights, params=fr.params, total_texels=fr.total_texels, tris=fr.model_triangles))
+    r = gpu.GpuRenderer(static, device=local)
+    r.set_lite_textures(lite)
+    r.enable_timing(True)
+    stream = torch.cuda.ExternalStream(r.stream_handle())
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    ldr = torch.empty((H, W), dtype=torch.int32, device=f"cuda:{local}")
+
+    def fin(f):
+        return r.frame_input(f["params"], f["lights"], f["surfaces"], f["total_texels"], f["draws"], f["vertices"],
+                             post_config=cfg, dst_device_ptr=ldr.data_ptr(), pitch=W, tri_vertices=f["tri"])
+
+    stage = {"surf": 0.0, "raster": 0.0, "post": 0.0}
+    graph_ms = []
+    with ClockSampler(local) as clocks:
+        r.set_frame_graph(False)
+        for step, f in enumerate(frames):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            r.draw_frame(fin(f))
+            t = r.timings()
+            if step >= args.warmup:
+                stage["surf"] += t[0]
+                stage["raster"] += t[1]
+                stage["post"] += t[2]
+        r.set_frame_graph(True)
+        r.set_exposure(1.0)
+        pix0 = r.stats().pixel_writes
+        for step, f in enumerate(frames):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            if step == args.warmup:
+                pix0 = r.stats().pixel_writes
+            r.draw_frame(fin(f))
+            t = r.timings()
+            if step >= args.warmup:
+                graph_ms.append(t[4])
+        torch.cuda.synchronize()
+        pix = (r.stats().pixel_writes - pix0) / args.steps
+    ms = max_over_ranks(statistics.mean(graph_ms), world, f"cuda:{local}")
+    s = args.steps
+    tris = statistics.mean(f["tris"] for f in frames[args.warmup:])
+    # e2e: host work (models included) + one graph per frame, two frames in flight
+    hr = host.HostRenderer(scene, device=local)
+    hr.set_frames_in_flight(2)
+    glib = gpu.load_library()
+    outs = [np.zeros((H, W), np.uint32) for _ in range(2)]
+    for o in outs:
+        hr.register_host_buffer(o)
+    efr = frames[: max(4, min(s, 12))]
+    for k, f in enumerate(efr):
+        hr.render_frame(f["index"], opts, out=outs[k % 2], post=cfg)
+    hr.sync()
+    s0 = abi.Stats()
+    glib.sw_get_stats(hr.context(), ctypes.byref(s0))
+    t0 = time.perf_counter()
+    for k, f in enumerate(efr):
+        hr.render_frame(f["index"], opts, out=outs[k % 2], post=cfg)
+    hr.sync()
+    e2e = len(efr) / (time.perf_counter() - t0)
+    s1 = abi.Stats()
+    glib.sw_get_stats(hr.context(), ctypes.byref(s1))
+    for o in outs:
+        hr.unregister_host_buffer(o)
+    hr.close()
+    peak, peak_kind = peaks()
+    raster_ms = stage["raster"] / s
+    rbytes = raster_bytes(pix, W, H)
+    gbs = rbytes / (raster_ms / 1e3) / 1e9
+    if rank == 0:
+        # CPU: host work + the oracle's surfaces, split_rect raster (polygons and triangles) and
+        # postprocess on a bounded sample; parity: the first frames against the oracle's single-thread raster
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        threads = os.cpu_count() or 1
+        sample = frames[:3]
+        t0 = time.perf_counter()
+        exposure = 1.0
+        for f in sample:
+            fr.prepare(f["index"], opts)
+            arena = oracle.build_surfaces(static, fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=threads)
+            fb = np.zeros((H, W), np.uint64)
+            oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, fb, num_threads=threads, tri_vertices=fr.tri_vertices,
+                             lite=lite)
+            _, exposure, _ = oracle.postprocess(cfg, fb, 1.0 / 60.0, (1.0, 1.0, 1.0), exposure)
+        cpu_v = len(sample) / (time.perf_counter() - t0)
+        # parity of one frame through the graph path (fresh context, exposure 1.0)
+        r2 = gpu.GpuRenderer(static, device=local)
+        r2.set_lite_textures(lite)
+        f = frames[0]
+        got = np.zeros((H, W), np.uint32)
+        r2.draw_frame(r2.frame_input(f["params"], f["lights"], f["surfaces"], f["total_texels"], f["draws"], f["vertices"],
+                                     post_config=cfg, dst=got, tri_vertices=f["tri"]))
+        r2.close()
+        arena = oracle.build_surfaces(static, f["surfaces"], f["lights"], f["params"], f["total_texels"], num_threads=threads)
+        fb = np.zeros((H, W), np.uint64)
+        oracle.rasterize(f["draws"], f["vertices"], arena, f["params"], fb, tri_vertices=f["tri"], lite=lite)
+        want, _, _ = oracle.postprocess(cfg, fb, 1.0 / 60.0, (1.0, 1.0, 1.0), 1.0)
+        print(json.dumps({
+            "metric": METRIC, "value": round(world * 1e3 / ms, 2), "unit": "frames/s", "n_gpus": world, "steps": s,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (lighting) / int (raster)", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": "models: the 1920x1080 colour64 + bloom + tonemap frame of the 64-room map with 200 "
+                                   "per-vertex animated triangle models (about 2k triangles, 8 keyframes each)",
+                       "mean_model_triangle_draws": int(tris), "mean_pixel_writes": int(pix),
+                       "mean_host_prep_ms": round(statistics.mean(prep_ms), 3),
+                       "timing": "CUDA-event device time of the frame's CUDA graph (host-prepared draw list)",
+                       "l2": "flushed (512 MiB write) before every timed step", "parallelism": f"replicas x{world}"},
+            "stages_ms": {k: round(v / s, 4) for k, v in stage.items()},
+            "roofline": {"bound": "hbm", "kernel": "raster_tiles_kernel (polygons and triangles, bloom downscale epilogue)",
+                         "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4),
+                         "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": int(rbytes), "traffic": None},
+            "parity": {"frames": 1, "mismatched_pixels": int((want != got).sum())},
+            "cpu_baseline": {"value": round(cpu_v, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(),
+                             "sample": f"{len(sample)} frames: host work + oracle surfaces, split_rect raster with the "
+                                       f"triangles, postprocess"},
+            "e2e": {"value": round(e2e, 2), "unit": "frames/s", "h2d_bytes_per_step": int((s1.upload_bytes - s0.upload_bytes) / len(efr)),
+                    "d2h_bytes_per_step": int(outs[0].nbytes), "path": "render_frame (host models + host-prepared draws), "
+                                                                       "two frames in flight"},
+            "clocks": clocks.summary(), "gpu_launches": s * FRAME_LAUNCHES}), flush=True)
+    r.close()
+
+
+# ---------------------------------------------------------------------------------------------------------
 # surfaces workload
 
 class SurfaceWorkload:
@@ -1046,7 +1194,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="frame", choices=["frame", "surfaces", "upscale", "shadows"])
+    ap.add_argument("--workload", default="frame", choices=["frame", "surfaces", "upscale", "shadows", "models"])
     ap.add_argument("--shadowed-lights", type=int, default=2, help="shadows workload: shadowed dynamic lights (of 8)")
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--autotune-reps", type=int, default=5,
@@ -1071,6 +1219,8 @@ def main():
             run_upscale_gpu(args, world, rank, local)
         elif args.workload == "shadows":
             run_shadows_gpu(args, world, rank, local)
+        elif args.workload == "models":
+            run_models_gpu(args, world, rank, local)
         else:
             run_frame_gpu(args, world, rank, local)
     finally:
