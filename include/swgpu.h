@@ -510,12 +510,18 @@ int sw_read_view_prep(SwCtx* ctx, SwViewCounts* out_counts, SwSurfaceDesc* surfa
 
 #define SW_SHADOW_NONE 0u
 #define SW_SHADOW_CUBE 1u
+#define SW_SHADOW_PROJECTOR 2u /* ShadowMap::Projector (light.rs:53-60): one size x size map of a cone */
 
 /* The shadow map of one of the frame's lights. */
 typedef struct SwLightShadow {
 	uint32_t kind;   /* SW_SHADOW_* */
-	uint32_t size;   /* cube side size in texels */
-	uint64_t offset; /* side s (light.rs:14-23 order: +X, -X, +Y, -Y, +Z, -Z) starts at offset + s * size * size */
+	uint32_t size;   /* cube side size (or projector map size) in texels */
+	uint64_t offset; /* cube: side s (light.rs:14-23 order: +X, -X, +Y, -Y, +Z, -Z) starts at offset + s * size * size;
+	                  projector: the map */
+	/* projector only (create_dynamic_light_projector_shadow_map, renderer_structs.rs:288-308): the
+	 * light's rotated y and z axes scaled by 1/tan(fov/2), and its -x axis */
+	float basis_x[3], basis_y[3], basis_z[3];
+	uint32_t reserved;
 } SwLightShadow;
 
 /* One DepthRasterizer::fill_polygon call of DepthRenderer::draw_polygon (depth_renderer.rs:199-287):
@@ -537,7 +543,9 @@ typedef struct SwDepthDraw {
 int sw_build_shadow_maps(SwCtx* ctx, const SwDepthDraw* draws, uint32_t num_draws, const SwVertex16* vertices,
 	uint32_t num_vertices, uint64_t total_texels);
 /* Shadow maps of the next frame's lights (one per light, in the frame's SwLight order; num_lights 0 or a
- * NULL array = no shadows). Holds for the frames that follow until it is called again. */
+ * NULL array = no shadows). Holds for the frames that follow until it is called again. Call it after the
+ * frame's shadow-map builds: a projector map's corners outside its inscribed circle are then set to
+ * 1e24 (make_shadow_map_circle, light.rs:135-156), after its depth draws. */
 int sw_set_light_shadows(SwCtx* ctx, const SwLightShadow* shadows, uint32_t num_lights);
 /* GPU-side depth-draw preparation (replaces the host's DepthRenderer::draw_polygon loop; needs sw_set_map):
  * one cube side as DepthRenderer::draw_map sees it (the side camera of light.rs:88-133) ... */

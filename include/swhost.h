@@ -41,6 +41,7 @@ typedef struct SwhSceneConfig {
 	uint32_t shadowed_lights;     /* the first this many dynamic lights cast cube shadows */
 	uint32_t scrolling_materials; /* the first this many materials scroll (s and t speeds fixed per material) */
 	uint32_t animated_materials;  /* the first this many materials cycle through 3 texture frames */
+	uint32_t projector_lights;    /* the dynamic lights after the shadowed ones that are shadowed projectors */
 	uint32_t num_models;          /* per-vertex animated triangle models on the rooms' floors (0 = none) */
 	uint32_t model_triangles;     /* triangles per model mesh, about (0 = 2000) */
 	uint32_t model_frames;        /* animation keyframes per mesh (0 = 8) */

@@ -37,11 +37,12 @@ def load():
     lib.orc_rasterize_ex.argtypes = [vp, u32, vp, u32, vp, u32, vp, u64, vp, u64, vp, u64, vp, vp, u32, u32,
                                      ctypes.POINTER(u64)]
     lib.orc_clear_background.argtypes = [vp, vp, u32]
+    lib.orc_shadow_map_circle.argtypes = [vp, u64, u64, u32]
     lib.orc_postprocess.argtypes = [vp, vp, u32, u32, f32, vp, ctypes.POINTER(f32), vp, u32, vp]
     lib.orc_upscale.argtypes = [u32, u32, vp, vp, u32, u32, u32]
     lib.orc_gaussian_kernel.argtypes = [f32, u32, vp]
     for fn in (lib.orc_build_surfaces, lib.orc_rasterize, lib.orc_rasterize_ex, lib.orc_clear_background, lib.orc_postprocess,
-               lib.orc_upscale, lib.orc_gaussian_kernel, lib.orc_shadow_maps):
+               lib.orc_upscale, lib.orc_gaussian_kernel, lib.orc_shadow_maps, lib.orc_shadow_map_circle):
         fn.restype = i32
     _lib = lib
     return lib
@@ -82,6 +83,11 @@ def shadow_maps(draws, vertices, storage):
     _check(lib.orc_shadow_maps(abi.ptr(draws), draws.size, abi.ptr(vertices), vertices.size, abi.ptr(storage), storage.size),
            "orc_shadow_maps")
     return storage
+
+
+def shadow_map_circle(storage, offset, size):
+    """make_shadow_map_circle on the projector map at `offset` of the f32 storage, in place."""
+    _check(load().orc_shadow_map_circle(abi.ptr(storage), storage.size, int(offset), int(size)), "orc_shadow_map_circle")
 
 
 def rasterize(draws, vertices, arena, frame_params, framebuffer, num_threads=1, skybox=None, tri_vertices=None, lite=None):

@@ -9,6 +9,7 @@
 #include "sw_oracle_math.h"
 
 #include <algorithm>
+#include <cmath>
 
 namespace sworacle
 {
@@ -140,6 +141,26 @@ extern "C" int orc_shadow_maps(const SwDepthDraw* draws, uint32_t num_draws, con
 		const SwDepthDraw& d = draws[i];
 		DepthRaster r{storage + d.map_offset, int32_t(d.map_size), int32_t(d.map_size), d.depth_eq};
 		r.fill_polygon(vertices + d.first_vertex, d.vertex_count);
+	}
+	return SW_OK;
+}
+
+// make_shadow_map_circle, light.rs:135-156: every texel of a projector map outside the circle inscribed
+// in it becomes 1e24 (nothing behind it is lit).
+extern "C" int orc_shadow_map_circle(float* storage, uint64_t total_texels, uint64_t offset, uint32_t size)
+{
+	if (!storage || size == 0 || offset + uint64_t(size) * size > total_texels) return SW_ERR_INVALID_ARGUMENT;
+	const float inf = 1.0e24f;
+	const int32_t size_signed = int32_t(size);
+	const int32_t radius = size_signed / 2;
+	for (int32_t y = 0; y < size_signed; ++y)
+	{
+		const int32_t dy = y - radius;
+		const int32_t rr = std::max(radius * radius - dy * dy, 0);
+		const int32_t dx = radius - std::min(int32_t(std::ceil(std::sqrt(float(rr)))), radius);
+		float* line = storage + offset + uint64_t(y) * size;
+		for (int32_t x = 0; x < dx; ++x) line[x] = inf;
+		for (int32_t x = size_signed - dx; x < size_signed; ++x) line[x] = inf;
 	}
 	return SW_OK;
 }

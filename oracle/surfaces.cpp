@@ -173,9 +173,29 @@ float cube_shadow_map_side_fetch(const float* side, uint32_t size, Vec3 vec)
 	return depth >= value ? 1.0f : 0.0f;
 }
 
+// projector_shadow_map_fetch, light.rs:261-294: 0 behind the projector or outside its map.
+float projector_shadow_map_fetch(const SwLightShadow& m, const float* data, Vec3 vec)
+{
+	const Vec3 bx = v3(m.basis_x[0], m.basis_x[1], m.basis_x[2]);
+	const Vec3 by = v3(m.basis_y[0], m.basis_y[1], m.basis_y[2]);
+	const Vec3 bz = v3(m.basis_z[0], m.basis_z[1], m.basis_z[2]);
+	const float z = vec3_dot(bz, vec);
+	if (z <= 0.0f) return 0.0f;
+	const float depth = inv_fast(z);
+	const float half_depth = 0.5f * depth;
+	const float size_f = float(m.size);
+	const float u_f = f32_mul_add(vec3_dot(bx, vec), half_depth, 0.5f) * size_f;
+	const float v_f = f32_mul_add(vec3_dot(by, vec), half_depth, 0.5f) * size_f;
+	if (u_f < 0.0f || v_f < 0.0f || u_f >= size_f || v_f >= size_f) return 0.0f;
+	const uint32_t u = uint32_t(u_f), v = uint32_t(v_f); // in [0, size): to_int_unchecked is a truncation
+	return depth >= data[u + v * m.size] ? 1.0f : 0.0f;
+}
+
 // get_light_shadow_factor / cube_shadow_map_fetch, light.rs:185-233 (`vec` = light position - point).
 float light_shadow_factor(const Shadows& sh, uint32_t light, Vec3 vec)
 {
+	if (sh.shadows && light < sh.num && sh.shadows[light].kind == SW_SHADOW_PROJECTOR)
+		return projector_shadow_map_fetch(sh.shadows[light], sh.texels + sh.shadows[light].offset, vec);
 	if (!sh.shadows || light >= sh.num || sh.shadows[light].kind != SW_SHADOW_CUBE) return 1.0f; // ShadowMap::None
 	const SwLightShadow& m = sh.shadows[light];
 	const uint64_t side_texels = uint64_t(m.size) * m.size;

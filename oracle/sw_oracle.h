@@ -25,6 +25,9 @@ int orc_build_surfaces(const SwCreateInfo* data, const SwSurfaceDesc* surfaces, 
 int orc_shadow_maps(const SwDepthDraw* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices,
 	float* storage, uint64_t total_texels);
 
+/* make_shadow_map_circle (light.rs:135-156) on the projector map at `offset` (size x size texels). */
+int orc_shadow_map_circle(float* storage, uint64_t total_texels, uint64_t offset, uint32_t size);
+
 /* Rasterizer::fill_polygon for every draw in order (perform_rasterization, partial_renderer.rs:1192-1283)
  * into `framebuffer` (pixel_format of frame, pitch in pixels). num_threads 0/1 = the reference's
  * single-thread path (one full-screen ClipRect); N > 1 = split_rect into N regions with one ClipRect each.

@@ -306,7 +306,8 @@ __device__ void prep_pair(const PrepArgs& a, const PrepFrame& frame, uint32_t nu
 				if (k < leaf_num_lights)
 				{
 					if (base > 0) light = a.leaf_lights[leaf_first_light + k];
-					hit = swhost::polygon_is_affected_by_light(p, base > 0 ? a.lights[light] : light0);
+					hit = swhost::polygon_is_affected_by_light(p, base > 0 ? a.lights[light] : light0,
+						light < a.num_shadows ? a.shadows + light : nullptr);
 				}
 				uint32_t mask = __ballot_sync(FULL_MASK, hit);
 				while (mask && d.num_lights < SW_MAX_POLYGON_LIGHTS)

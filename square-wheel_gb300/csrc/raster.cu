@@ -1143,6 +1143,34 @@ int launch_shadow_view(const ShadowViewArgs& args, cudaStream_t stream)
 	return int(cudaGetLastError());
 }
 
+namespace
+{
+// make_shadow_map_circle (light.rs:135-156) on one projector map: row y's first and last dx texels
+// (outside the inscribed circle) become 1e24, written with sequence `seq` so that they replace every
+// depth draw before them and give way to every later one.
+__global__ void __launch_bounds__(256) shadow_circle_kernel(unsigned long long* map, uint32_t size, uint32_t seq)
+{
+	const int32_t s = int32_t(size), radius = s / 2, y = int32_t(blockIdx.x);
+	const int32_t dy = y - radius;
+	const int32_t rr = max(radius * radius - dy * dy, 0);
+	const int32_t dx = radius - min(int32_t(ceilf(sqrtf(float(rr)))), radius);
+	const unsigned long long v = (static_cast<unsigned long long>(seq) << 32) | __float_as_uint(1.0e24f);
+	unsigned long long* line = map + uint64_t(y) * size;
+	for (int32_t x = int32_t(threadIdx.x); x < dx; x += int32_t(blockDim.x))
+	{
+		line[x] = v;
+		line[s - 1 - x] = v;
+	}
+}
+} // namespace
+
+int launch_shadow_circle(unsigned long long* map, uint32_t size, uint32_t seq, cudaStream_t stream)
+{
+	if (size == 0) return 0;
+	shadow_circle_kernel<<<size, 256, 0, stream>>>(map, size, seq);
+	return int(cudaGetLastError());
+}
+
 int launch_shadow_rebase(unsigned long long* storage, uint64_t num_texels, cudaStream_t stream)
 {
 	if (num_texels == 0) return 0;

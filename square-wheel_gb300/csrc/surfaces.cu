@@ -128,11 +128,27 @@ __device__ __forceinline__ float cube_side_fetch(const unsigned long long* side,
 	return depth >= __uint_as_float(uint32_t(__ldg(side + u + v * size))) ? 1.0f : 0.0f; // the texel's f32 bits
 }
 
+// projector_shadow_map_fetch (light.rs:261-294): 0 behind the projector or outside its map.
+__device__ __forceinline__ float projector_fetch(const SurfaceKernelArgs& a, const SwLightShadow& m, V3 vec)
+{
+	const float z = v3dot(mkv3(m.basis_z[0], m.basis_z[1], m.basis_z[2]), vec);
+	if (z <= 0.0f) return 0.0f;
+	const float depth = inv_fast(z);
+	const float half_depth = fmul(0.5f, depth);
+	const float size_f = float(m.size);
+	const float u_f = fmul(mad2(v3dot(mkv3(m.basis_x[0], m.basis_x[1], m.basis_x[2]), vec), half_depth, 0.5f), size_f);
+	const float v_f = fmul(mad2(v3dot(mkv3(m.basis_y[0], m.basis_y[1], m.basis_y[2]), vec), half_depth, 0.5f), size_f);
+	if (u_f < 0.0f || v_f < 0.0f || u_f >= size_f || v_f >= size_f) return 0.0f;
+	const uint32_t u = __float2uint_rz(u_f), v = __float2uint_rz(v_f); // in [0, size)
+	return depth >= __uint_as_float(uint32_t(__ldg(a.shadow_texels + m.offset + u + v * m.size))) ? 1.0f : 0.0f;
+}
+
 // get_light_shadow_factor / cube_shadow_map_fetch (light.rs:185-233) for `to_light` = light - point.
 __device__ __forceinline__ float light_shadow_factor(const SurfaceKernelArgs& a, uint32_t light, V3 to_light)
 {
 	if (!a.shadows || light >= a.num_shadows) return 1.0f;
 	const SwLightShadow m = a.shadows[light];
+	if (m.kind == SW_SHADOW_PROJECTOR) return projector_fetch(a, m, to_light);
 	if (m.kind != SW_SHADOW_CUBE) return 1.0f;
 	const uint64_t side_texels = uint64_t(m.size) * m.size;
 	const unsigned long long* maps = a.shadow_texels + m.offset;

@@ -313,6 +313,8 @@ struct ShadowViewArgs
 	uint32_t seq_base;
 };
 int launch_shadow_view(const ShadowViewArgs& args, cudaStream_t stream);
+// make_shadow_map_circle on the size x size projector map at `map` with sequence `seq`.
+int launch_shadow_circle(unsigned long long* map, uint32_t size, uint32_t seq, cudaStream_t stream);
 // Sequences restart at 0: keep only the f32 bits of every texel.
 int launch_shadow_rebase(unsigned long long* storage, uint64_t num_texels, cudaStream_t stream);
 
@@ -373,6 +375,8 @@ struct PrepArgs
 	const DrawRows* host_rows;
 	const SwTextureMip* texture_mips;
 	const SwEmissiveMip* emissive_mips;
+	const SwLightShadow* shadows; // the frame's lights' shadow maps (projector cones narrow the light lists)
+	uint32_t num_shadows;
 	PrepCand* cands;
 	PrepKey* keys;
 	// outputs and their capacities

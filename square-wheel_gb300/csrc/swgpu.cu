@@ -1977,6 +1977,8 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	pr.host_rows = reinterpret_cast<const DrawRows*>(d + vb.rows);
 	pr.texture_mips = static_cast<const SwTextureMip*>(ctx->texture_mips.ptr);
 	pr.emissive_mips = static_cast<const SwEmissiveMip*>(ctx->emissive_mips.ptr);
+	pr.shadows = ctx->num_shadow_descs ? static_cast<const SwLightShadow*>(ctx->shadow_descs.ptr) : nullptr;
+	pr.num_shadows = ctx->num_shadow_descs;
 	pr.cands = reinterpret_cast<PrepCand*>(slab + vs.cands);
 	pr.keys = reinterpret_cast<PrepKey*>(slab + vs.keys);
 	pr.descs = ctx->v_descs;
@@ -2293,15 +2295,31 @@ int sw_set_light_shadows(SwCtx* ctx, const SwLightShadow* shadows, uint32_t num_
 	{
 		const SwLightShadow& m = shadows[i];
 		if (m.kind == SW_SHADOW_NONE) continue;
-		if (m.kind != SW_SHADOW_CUBE) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "light %u: unknown shadow kind", i);
-		if (m.size == 0 || m.size > SW_SHADOW_MAX_SIZE || m.offset + 6 * uint64_t(m.size) * m.size > ctx->shadow_texels)
-			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "light %u: cube map outside the shadow-map storage", i);
+		if (m.kind != SW_SHADOW_CUBE && m.kind != SW_SHADOW_PROJECTOR)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "light %u: unknown shadow kind", i);
+		const uint64_t maps = m.kind == SW_SHADOW_CUBE ? 6u : 1u;
+		if (m.size == 0 || m.size > SW_SHADOW_MAX_SIZE || m.offset + maps * uint64_t(m.size) * m.size > ctx->shadow_texels)
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "light %u: shadow map outside the shadow-map storage", i);
+		if (m.kind == SW_SHADOW_PROJECTOR &&
+			!(all_finite(m.basis_x, 3) && all_finite(m.basis_y, 3) && all_finite(m.basis_z, 3)))
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "light %u: non-finite projector basis", i);
 		used = i + 1;
 	}
 	SW_CUDA(ctx, cudaSetDevice(ctx->device));
 	ctx->num_shadow_descs = used; // lights past the last shadowed one need no descriptor
 	if (!used) return SW_OK;
 	int r;
+	// projector maps: the corners outside the inscribed circle, after the frame's depth draws
+	for (uint32_t i = 0; i < used; ++i)
+		if (shadows[i].kind == SW_SHADOW_PROJECTOR)
+		{
+			uint32_t base = 0;
+			if ((r = shadow_sequence(ctx, 1, &base))) return r;
+			if ((r = check_kernel(ctx, launch_shadow_circle(static_cast<unsigned long long*>(ctx->shadow_storage.ptr) + shadows[i].offset,
+									shadows[i].size, base + 1, ctx->stream),
+					 "projector shadow-map circle")))
+				return r;
+		}
 	if ((r = ensure(ctx, ctx->shadow_descs, size_t(used) * sizeof(SwLightShadow)))) return r;
 	return upload(ctx, ctx->stage_shadow_descs, ctx->shadow_descs.ptr, shadows, size_t(used) * sizeof(SwLightShadow));
 }

@@ -262,10 +262,17 @@ void FramePrep::prepare_shadows()
 	depth_vertices.clear();
 	shadow_sides.clear();
 	shadow_leafs.clear();
-	light_shadows.assign(lights.size(), SwLightShadow{SW_SHADOW_NONE, 0u, 0ull});
+	SwLightShadow none;
+	std::memset(&none, 0, sizeof(none));
+	light_shadows.assign(lights.size(), none);
 	uint64_t offset = 0;
 	for (uint32_t li = 0; li < lights.size(); ++li)
 	{
+		if (sc.light_is_projector(li))
+		{
+			prepare_projector(li, offset);
+			continue;
+		}
 		if (!sc.light_is_shadowed(li)) continue;
 		bool visible = false;
 		for (uint32_t leaf : light_leafs[li])
@@ -288,12 +295,60 @@ void FramePrep::prepare_shadows()
 			const uint32_t shift = e >= 31.0f ? 31u : uint32_t(e);
 			size = std::max(std::min(1u << shift, max_size), min_size);
 		}
-		light_shadows[li] = SwLightShadow{SW_SHADOW_CUBE, size, offset};
+		light_shadows[li] = none;
+		light_shadows[li].kind = SW_SHADOW_CUBE;
+		light_shadows[li].size = size;
+		light_shadows[li].offset = offset;
 		for (uint32_t side = 0; side < 6; ++side)
 			draw_depth_map(cube_shadow_map_side_matrices(lp, float(size), side), size, offset + uint64_t(side) * size * size);
 		offset += uint64_t(size) * size * 6;
 	}
 	shadow_texels = offset;
+}
+
+void FramePrep::prepare_projector(uint32_t li, uint64_t& offset)
+{
+	// prepare_dynamic_lights' projector branch (partial_renderer.rs:462-513): the map size from the
+	// closest of the cone's five reference points, 32..1024 texels; build_shadow_maps (:565-590) draws it
+	// with the light's matrices; its shadow map (renderer_structs.rs:288-308) carries the rotated axes.
+	bool visible = false;
+	for (uint32_t leaf : light_leafs[li])
+		if (vis.visible(leaf))
+		{
+			visible = true;
+			break;
+		}
+	if (!visible) return;
+	const SwLight& light = lights[li];
+	const Vec3 lp = v3(light.position[0], light.position[1], light.position[2]);
+	Quat rotation;
+	float fov;
+	sc.projector_pose(li, frame_time_s, rotation, fov);
+	const float hft = light.radius * std::tan(fov * 0.5f);
+	Mat4 light_matrix = mat4_from_quat(rotation);
+	light_matrix.c[3] = v4(lp.x, lp.y, lp.z, 1.0f);
+	const Vec3 pts[5] = {v3(light.radius, 0, 0), v3(light.radius, hft, hft), v3(light.radius, hft, -hft),
+		v3(light.radius, -hft, hft), v3(light.radius, -hft, -hft)};
+	float closest_square = 1.0e24f;
+	for (const Vec3& v : pts)
+		closest_square = std::fmin(closest_square, magnitude2(cam.position - truncate(light_matrix * extend(v, 1.0f))));
+	const float target_size = 1024.0f * hft / std::sqrt(closest_square);
+	const float e = std::fmax(std::log2(target_size) + opt.shadows_quality, 0.0f);
+	const uint32_t shift = e >= 31.0f ? 31u : uint32_t(e);
+	const uint32_t size = std::max(std::min(1u << shift, 1024u), 32u);
+	SwLightShadow& m = light_shadows[li];
+	m.kind = SW_SHADOW_PROJECTOR;
+	m.size = size;
+	m.offset = offset;
+	const float inv_half_fov_tan = 1.0f / std::tan(fov * 0.5f);
+	const Vec3 bx = rotate_vector(rotation, v3(0, 1, 0)) * inv_half_fov_tan;
+	const Vec3 by = rotate_vector(rotation, v3(0, 0, 1)) * inv_half_fov_tan;
+	const Vec3 bz = rotate_vector(rotation, v3(-1, 0, 0));
+	m.basis_x[0] = bx.x, m.basis_x[1] = bx.y, m.basis_x[2] = bx.z;
+	m.basis_y[0] = by.x, m.basis_y[1] = by.y, m.basis_y[2] = by.z;
+	m.basis_z[0] = bz.x, m.basis_z[1] = bz.y, m.basis_z[2] = bz.z;
+	draw_depth_map(build_view_matrix_with_full_rotation(lp, rotation, fov, float(size), float(size)), size, offset);
+	offset += uint64_t(size) * size;
 }
 
 template <class F>
@@ -475,7 +530,7 @@ void FramePrep::build_surface_descs()
 		make_surface_desc(p, sp, pd.offset, directional, simple_lightmaps, mf.shift, mf.texture, d);
 		if (p.flags & SW_POLY_DIFFUSE_LAYER)
 			for (uint32_t li : leaf_lights[sc.polygon_leaf[pi]])
-				if (polygon_is_affected_by_light(p, lights[li]))
+				if (polygon_is_affected_by_light(p, lights[li], li < light_shadows.size() ? &light_shadows[li] : nullptr))
 				{
 					d.lights[d.num_lights++] = uint16_t(li);
 					if (d.num_lights == MAX_POLYGON_LIGHTS) break;

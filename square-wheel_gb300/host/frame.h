@@ -195,6 +195,8 @@ private:
 	void draw_skybox(const ClippingPolygon& viewport);
 	void draw_tree();
 	void draw_leaf(const ClippingPolygon& bounds, uint32_t leaf_index);
+	// A projector light's map (size, storage at `offset`, then advanced) and its depth draws.
+	void prepare_projector(uint32_t light_index, uint64_t& offset);
 	// The leaf's triangle models after its polygons (draw_leaf's dynamic models, partial_renderer.rs:
 	// 2562-2792; build_dynamic_models_buffers :1122-1190; draw_mesh :3525-3718).
 	void draw_leaf_models(const ClippingPolygon& bounds, uint32_t leaf_index);

@@ -229,6 +229,23 @@ inline CameraMatrices build_view_matrix(Vec3 position, float azimuth, float elev
 	return complete_view_matrix(position, rotation_matrix, fov_scale, width, height);
 }
 
+// build_view_matrix_with_full_rotation with get_full_ortation_matrix, src/common/matrix.rs:31-80 (used by
+// calculate_projector_shadow_map_matrices, light.rs:63-71).
+inline CameraMatrices build_view_matrix_with_full_rotation(Vec3 position, Quat rotation, float fov, float width, float height)
+{
+	const float inv_half_fov_tan = 1.0f / std::tan(fov * 0.5f);
+	const float aspect = width / height;
+	const Vec2 fov_scale = v2(inv_half_fov_tan / aspect, inv_half_fov_tan);
+	Mat4 basis_change = Mat4::identity();
+	basis_change.c[0] = v4(0, 0, 1, 0);
+	basis_change.c[1] = v4(-1, 0, 0, 0);
+	basis_change.c[2] = v4(0, -1, 0, 0);
+	return complete_view_matrix(position, basis_change * mat4_from_quat(conjugate(rotation)), fov_scale, width, height);
+}
+
+// Quaternion::rotate_vector (through the rotation matrix).
+inline Vec3 rotate_vector(Quat q, Vec3 v) { return truncate(mat4_from_quat(q) * extend(v, 0.0f)); }
+
 // calculate_cube_shadow_map_side_matrices / get_cube_map_side_matrix, src/square_wheel/light.rs:73-133:
 // side 0..5 = +X, -X, +Y, -Y, +Z, -Z; a 90-degree view (fov scale 1) over a size x size map.
 inline CameraMatrices cube_shadow_map_side_matrices(Vec3 position, float size, uint32_t side)

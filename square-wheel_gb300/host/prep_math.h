@@ -268,8 +268,10 @@ SWH_HD inline bool mat3_invert_transpose(Vec3 a, Vec3 b, Vec3 c, Mat3& out)
 
 SWH_HD inline Vec3 poly_vec3(const float* f) { return v3(f[0], f[1], f[2]); }
 
-// polygon_is_affected_by_light, partial_renderer.rs:3877-3985 (lights without a projector shadow map)
-SWH_HD inline bool polygon_is_affected_by_light(const SwMapPolygon& polygon, const SwLight& light)
+// polygon_is_affected_by_light, partial_renderer.rs:3877-3985; `shadow` (may be null) is the light's
+// shadow map: a projector's cone is tested against the polygon's texture-coordinate rectangle corners.
+SWH_HD inline bool polygon_is_affected_by_light(const SwMapPolygon& polygon, const SwLight& light,
+	const SwLightShadow* shadow = nullptr)
 {
 	const Vec3 lp = v3(light.position[0], light.position[1], light.position[2]);
 	const Vec3 bu = poly_vec3(polygon.basis_u), bv = poly_vec3(polygon.basis_v), bn = poly_vec3(polygon.basis_normal);
@@ -278,6 +280,25 @@ SWH_HD inline bool polygon_is_affected_by_light(const SwMapPolygon& polygon, con
 	if (signed_distance <= 0.0f) return false;
 	const float square_radius = light.radius * light.radius - signed_distance * signed_distance;
 	if (square_radius <= 0.0f) return false;
+	if (shadow && shadow->kind == SW_SHADOW_PROJECTOR)
+	{
+		// the light pyramid's five planes against the (approximate) polygon corners (:3901-3944)
+		const Vec3 start = poly_vec3(polygon.basis_start);
+		const Vec3 u0 = bu * float(polygon.tex_coord_min[0]), u1 = bu * float(polygon.tex_coord_max[0]);
+		const Vec3 v0 = bv * float(polygon.tex_coord_min[1]), v1 = bv * float(polygon.tex_coord_max[1]);
+		const Vec3 corners[4] = {start + u0 + v0, start + u0 + v1, start + u1 + v0, start + u1 + v1};
+		const Vec3 bx = poly_vec3(shadow->basis_x), by = poly_vec3(shadow->basis_y), bz = poly_vec3(shadow->basis_z);
+		const Vec3 plane_vecs[5] = {bz, bz - bx, bz + bx, bz - by, bz + by};
+		for (int k = 0; k < 5; ++k)
+		{
+			const float dist = dot(plane_vecs[k], lp);
+			int front = 0;
+			for (int c = 0; c < 4; ++c)
+				if (dot(plane_vecs[k], corners[c]) >= dist) ++front;
+			if (front >= 4) return false;
+		}
+		return true;
+	}
 	Mat3 m;
 	if (!mat3_invert_transpose(bu, bv, bn, m)) return false;
 	const float tc0 = dot(vec, m.c[0]), tc1 = dot(vec, m.c[1]);

@@ -917,6 +917,14 @@ void Scene::frame_lights(uint32_t frame, std::vector<SwLight>& out) const
 	}
 }
 
+void Scene::projector_pose(uint32_t light, float t, Quat& rotation, float& fov) const
+{
+	// the cone sweeps around the vertical axis (1.2 rad/s) and looks 0.4 rad down; fov 60..94 degrees
+	const float yaw = t * 1.2f + float(light) * 1.7f;
+	rotation = quat_mul(quat_from_angle_z(yaw), quat_from_angle_y(0.4f));
+	fov = 1.05f + 0.6f * float(light % 3) / 2.0f;
+}
+
 void Scene::map_polygons(std::vector<SwMapPolygon>& out) const
 {
 	out.resize(polygons.size());

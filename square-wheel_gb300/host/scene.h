@@ -155,6 +155,7 @@ struct SceneConfig
 	float sky_rotation_speed = 0.01f; // skybox rotation about the vertical axis, radians per frame
 	float camera_pitch = 0.0f;        // added to the camera path's elevation (radians, up > 0)
 	uint32_t shadowed_lights = 0;     // the first this many dynamic lights cast cube shadows
+	uint32_t projector_lights = 0;    // the next this many dynamic lights are shadowed projectors (cones)
 	uint32_t scrolling_materials = 0; // the first this many materials scroll (Material::scroll_speed)
 	uint32_t animated_materials = 0;  // the first this many materials cycle through 3 frames (framed_animation)
 	uint32_t num_models = 0;          // per-vertex animated triangle models placed in the rooms
@@ -201,6 +202,13 @@ struct Scene
 	void frame_lights(uint32_t frame, std::vector<SwLight>& out) const;
 	// DynamicLightShadowType::Cubemap for light `i` of frame_lights' list (the first shadowed_lights ones).
 	bool light_is_shadowed(uint32_t i) const { return i < config.shadowed_lights; }
+	// DynamicLightShadowType::Projector for the projector_lights lights after them.
+	bool light_is_projector(uint32_t i) const
+	{
+		return i >= config.shadowed_lights && i < config.shadowed_lights + config.projector_lights;
+	}
+	// A projector light's rotation (yaw about the vertical axis, then pitch) and fov at time t (seconds).
+	void projector_pose(uint32_t light, float t, Quat& rotation, float& fov) const;
 	// Polygons with their basis and material fields (SwMapPolygon), in polygon order.
 	void map_polygons(std::vector<SwMapPolygon>& out) const;
 	SwCreateInfo create_info(uint32_t device) const;

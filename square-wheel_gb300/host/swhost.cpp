@@ -127,6 +127,7 @@ int swh_scene_create(const SwhSceneConfig* c, SwhScene** out)
 	cfg.shadowed_lights = c->shadowed_lights;
 	cfg.scrolling_materials = c->scrolling_materials;
 	cfg.animated_materials = c->animated_materials;
+	cfg.projector_lights = c->projector_lights;
 	cfg.num_models = c->num_models;
 	cfg.model_triangles = c->model_triangles ? c->model_triangles : 2000;
 	cfg.model_frames = c->model_frames ? c->model_frames : 8;

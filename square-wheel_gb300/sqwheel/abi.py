@@ -36,7 +36,7 @@ SW_NO_EMISSIVE = 0xFFFFFFFF
 SW_SURF_DIFFUSE_LAYER = 1
 SW_POLY_DRAW, SW_POLY_SKY, SW_POLY_DIFFUSE_LAYER, SW_POLY_SHADOW = 1, 2, 4, 8
 SW_LEAF_NOT_DRAWN = 0xFFFFFFFF
-SW_SHADOW_NONE, SW_SHADOW_CUBE = 0, 1
+SW_SHADOW_NONE, SW_SHADOW_CUBE, SW_SHADOW_PROJECTOR = 0, 1, 2
 
 TEXTURE_MIP = np.dtype([("offset", "<u8"), ("width", "<u4"), ("height", "<u4"), ("flags", "<u4"), ("reserved", "<u4")], align=True)
 EMISSIVE_MIP = np.dtype([("offset", "<u8"), ("width", "<u4"), ("height", "<u4")], align=True)
@@ -61,7 +61,8 @@ MAP_POLYGON = np.dtype([
     ("basis_start", "<f4", 3), ("basis_normal", "<f4", 3), ("tex_coord_min", "<i4", 2), ("tex_coord_max", "<i4", 2),
     ("first_vertex", "<u4"), ("num_vertices", "<u4"), ("texture", "<u4"), ("lightmap_data_offset", "<u4"),
     ("flags", "<u4"), ("blending_mode", "<u4"), ("emissive_texture", "<u4"), ("emissive_light", "<f4", 3)], align=True)
-LIGHT_SHADOW = np.dtype([("kind", "<u4"), ("size", "<u4"), ("offset", "<u8")], align=True)
+LIGHT_SHADOW = np.dtype([("kind", "<u4"), ("size", "<u4"), ("offset", "<u8"), ("basis_x", "<f4", 3), ("basis_y", "<f4", 3),
+                         ("basis_z", "<f4", 3), ("reserved", "<u4")], align=True)
 DEPTH_DRAW = np.dtype([("first_vertex", "<u4"), ("vertex_count", "<u4"), ("map_size", "<u4"), ("reserved", "<u4"),
                        ("map_offset", "<u8"), ("depth_eq", "<f4", 3), ("reserved2", "<u4")], align=True)
 MATERIAL_FRAME = np.dtype([("shift", "<i4", 2), ("texture", "<u4"), ("reserved", "<u4")], align=True)

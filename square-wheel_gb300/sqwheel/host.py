@@ -24,7 +24,7 @@ class SceneConfig(ctypes.Structure):
         ("sky_rooms", ctypes.c_uint32), ("skybox_size", ctypes.c_uint32), ("skybox_brightness", ctypes.c_float),
         ("skybox_missing_side", ctypes.c_int32), ("sky_rotation_speed", ctypes.c_float),
         ("camera_pitch", ctypes.c_float), ("shadowed_lights", ctypes.c_uint32), ("scrolling_materials", ctypes.c_uint32),
-        ("animated_materials", ctypes.c_uint32), ("num_models", ctypes.c_uint32), ("model_triangles", ctypes.c_uint32),
+        ("animated_materials", ctypes.c_uint32), ("projector_lights", ctypes.c_uint32), ("num_models", ctypes.c_uint32), ("model_triangles", ctypes.c_uint32),
         ("model_frames", ctypes.c_uint32),
     ]
 
@@ -129,7 +129,7 @@ class Scene:
                         lights_per_room=1, num_dynamic_lights=0, num_frames=64, emissive_frac=0.0, sky_rooms=0,
                         skybox_size=128, skybox_brightness=1.0, skybox_missing_side=-1, sky_rotation_speed=0.01,
                         camera_pitch=0.0, shadowed_lights=0, scrolling_materials=0,
-                        animated_materials=0, num_models=0, model_triangles=2000, model_frames=8)
+                        animated_materials=0, projector_lights=0, num_models=0, model_triangles=2000, model_frames=8)
         for k, v in kw.items():
             setattr(c, k, v)
         self.config = c

@@ -141,3 +141,43 @@ def test_oracle_depth_rasteriser_against_restatement(built_libs):
         got = np.full(size * size, -1.0, np.float32)
         oracle.shadow_maps(d, v, got)
         assert np.array_equal(want.view(np.uint32), got.view(np.uint32)), f"trial {trial}"
+
+
+def test_projector_circle_known_answer(built_libs):
+    """make_shadow_map_circle on a 16x16 map: row y keeps [dx, 16 - dx) with dx = 8 - min(ceil(sqrt(64 -
+    (y - 8)^2)), 8) (light.rs:135-156); the rest becomes 1e24."""
+    import math
+    storage = np.zeros(300, np.float32)
+    oracle.shadow_map_circle(storage, 40, 16)
+    m = storage[40:40 + 256].reshape(16, 16)
+    for y in range(16):
+        dx = 8 - min(math.ceil(math.sqrt(max(64 - (y - 8) ** 2, 0))), 8)
+        row = np.zeros(16, np.float32)
+        row[:dx] = 1e24
+        row[16 - dx:] = 1e24
+        assert np.array_equal(m[y], row), y
+    assert not storage[:40].any() and not storage[40 + 256:].any()
+
+
+def test_projector_lights_narrow_light_lists(built_libs):
+    """A projector's cone (the five pyramid planes) leaves polygons outside it without the light, which
+    the same light as an unshadowed point light would reach; its map size follows the reference's
+    formula (partial_renderer.rs:462-513)."""
+    base = dict(host.SMALL_MAP, num_dynamic_lights=4)
+    plain = host.Scene(**base)
+    proj = host.Scene(**dict(base, projector_lights=4))
+    fp, fq = host.Frame(plain), host.Frame(proj)
+    opts = host.frame_options(640, 480, abi.SW_PIXEL_C64, directional=False)
+    fewer = 0
+    for fi in (0, 12, 40):
+        fp.prepare(fi, opts)
+        fq.prepare(fi, opts)
+        assert fp.surfaces.size == fq.surfaces.size
+        lp, lq = fp.surfaces["num_lights"].sum(), fq.surfaces["num_lights"].sum()
+        assert lq <= lp
+        fewer += int(lp - lq)
+        for m in fq.light_shadows:
+            if m["kind"] == abi.SW_SHADOW_PROJECTOR:
+                assert 32 <= m["size"] <= 1024 and (int(m["size"]) & (int(m["size"]) - 1)) == 0
+                assert abs(np.linalg.norm(m["basis_z"]) - 1.0) < 1e-5
+    assert fewer > 0
