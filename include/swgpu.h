@@ -276,6 +276,20 @@ int sw_set_surfaces(SwCtx* ctx, const void* texels, uint64_t total_texels);
  * Synchronous upload; NULL / 0 texels removes the skybox. Load-time data like sw_create's. */
 int sw_set_skybox(SwCtx* ctx, const uint32_t* texels32, const uint64_t* texels64, uint64_t num_texels);
 
+/* Replace the lightmaps with a compiled map's compressed lightmap lumps, uploaded as the file holds them
+ * and decoded on the GPU (LightmapElementCompressed::decompress and
+ * DirectionalLightmapElementCompressed::decompress, src/common/lightmap_compression.rs:64-68, 88-130;
+ * what load_map does on the host, bsp_map_save_load.rs:208-215): `lightmaps` holds num_elements 4-byte
+ * CompressedColor records (r, g, b, scale: value = component * scale / 255), `directional` holds
+ * num_directional_elements 13-byte records (ambient CompressedColor, direction CompressedVector - three
+ * i8 and a scale, value = component * scale / 127 -, u8 deviation / 255, directional CompressedColor).
+ * Fails if sw_set_map's polygons read past the new lightmaps. Load-time data like sw_create's;
+ * synchronous (waits for frames in flight). */
+#define SW_LIGHTMAP_COMPRESSED_BYTES 4
+#define SW_DIR_LIGHTMAP_COMPRESSED_BYTES 13
+int sw_set_lightmaps_compressed(SwCtx* ctx, const void* lightmaps, uint64_t num_elements, const void* directional,
+	uint64_t num_directional_elements);
+
 /* Page-lock a host buffer the caller reuses for its frames (the window surface's pixels, say) with
  * cudaHostRegister (mapped), so that frames written to host memory inside it go straight from the
  * device into it instead of through the library's pinned staging buffer and a host copy (sw_draw_frame's
@@ -604,6 +618,10 @@ int sw_read_surfaces(SwCtx* ctx, void* dst_host, uint64_t max_bytes);
 /* Diagnostics: copy the context's frame buffer (the last frame rasterised, width x height pixels of its
  * pixel format, tightly packed; the HDR frame the postprocessor read) to host memory (synchronises). */
 int sw_read_framebuffer(SwCtx* ctx, void* dst_host, uint64_t max_bytes);
+/* Diagnostics: copy the context's decoded lightmaps (up to max_elements simple and max_directional_elements
+ * directional elements) to host memory (synchronises). */
+int sw_read_lightmaps(SwCtx* ctx, float* lightmaps, uint64_t max_elements, SwDirectionalLightmapElement* directional,
+	uint64_t max_directional_elements);
 /* Current exposure (Postprocessor::current_exposure). */
 int sw_get_exposure(SwCtx* ctx, float* out_exposure);
 int sw_set_exposure(SwCtx* ctx, float exposure);

@@ -68,6 +68,28 @@ int swh_scene_lite_textures(const SwhScene* scene, const uint32_t** out_pixels, 
  * Pointers stay valid while the scene lives; *out_count is 0 without a sky material. */
 int swh_scene_skybox(const SwhScene* scene, const uint32_t** out_texels32, const uint64_t** out_texels64,
 	uint64_t* out_count, uint64_t mip_offsets[30], uint32_t mip_sizes[30]);
+/* A scene from a compiled map file (.sqwm, format version 11: load_map, src/common/bsp_map_save_load.rs:162-226,
+ * lightmaps decompressed as lightmap_compression.rs does). The map's BSP tree, leafs, polygons, portals,
+ * vertices and lightmaps are rendered as they are, after every index and range rendering follows is
+ * checked; each texture name gets a procedural material (texture_size, normal_maps, metal_frac,
+ * dielectric_frac and scrolling_materials apply; the image files the names refer to are not part of a
+ * map); the camera path starts at the info_player_start entity (or leaf 0) and runs through leafs and
+ * portals; num_dynamic_lights, shadowed_lights, projector_lights, num_frames, camera_pitch and
+ * directional_lightmaps apply. grid_x, grid_y, room_min, room_max, tile_size and lights_per_room are
+ * ignored; sky_rooms, num_models and animated_materials must be 0. A renderer created for such a scene
+ * uploads the compressed lightmaps and decodes them on the GPU (sw_set_lightmaps_compressed).
+ * Errors: SW_ERR_INVALID_ARGUMENT with swh_last_error() set (can't open, not a map, wrong version, a lump
+ * past the end of the file, an index out of range). */
+int swh_scene_load_map(const char* path, const SwhSceneConfig* config, SwhScene** out_scene);
+int swh_scene_load_map_memory(const void* data, uint64_t size, const SwhSceneConfig* config, SwhScene** out_scene);
+/* Write a scene's map data as a compiled map (save_map, bsp_map_save_load.rs:24-160): geometry as is, a
+ * texture name per material, lightmaps compressed, a worldspawn entity and an info_player_start at the
+ * camera path's first position. */
+int swh_scene_save_map(const SwhScene* scene, const char* path);
+/* A loaded map's compressed lightmap lumps as the file holds them (4-byte and 13-byte records; counts 0
+ * for generated scenes). Pointers stay valid while the scene lives. */
+int swh_scene_compressed_lightmaps(const SwhScene* scene, const void** out_lightmaps, uint64_t* out_count,
+	const void** out_directional, uint64_t* out_directional_count);
 const char* swh_last_error(void);
 
 typedef struct SwhFrameOptions {

@@ -315,6 +315,10 @@ struct ShadowViewArgs
 int launch_shadow_view(const ShadowViewArgs& args, cudaStream_t stream);
 // make_shadow_map_circle on the size x size projector map at `map` with sequence `seq`.
 int launch_shadow_circle(unsigned long long* map, uint32_t size, uint32_t seq, cudaStream_t stream);
+// Compressed lightmap lumps (4-byte simple, 13-byte directional elements, 16-byte aligned inputs) decoded
+// into f32 lightmaps (lightmaps.cu).
+int launch_lightmap_decompress(const void* simple_in, uint64_t num_simple, float* simple_out, const void* dir_in,
+	uint64_t num_dir, SwDirectionalLightmapElement* dir_out, cudaStream_t stream);
 // Sequences restart at 0: keep only the f32 bits of every texel.
 int launch_shadow_rebase(unsigned long long* storage, uint64_t num_texels, cudaStream_t stream);
 

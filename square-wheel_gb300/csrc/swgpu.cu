@@ -79,6 +79,7 @@ struct SwCtx
 
 	// static
 	DevBuf texels, texture_mips, emissive, emissive_mips, lightmaps, dir_lightmaps;
+	DevBuf lm_compressed; // sw_set_lightmaps_compressed: the compressed lumps as uploaded
 	DevBuf skybox32, skybox64; // sw_set_skybox: the same texels in Color32 and Color64
 	DevBuf frame_in;           // sw_draw_frame: all per-frame arrays of one frame, uploaded by one copy
 	struct HostRange
@@ -169,6 +170,7 @@ struct SwCtx
 	SwVertex16* v_vertices = nullptr;
 	float* d_average_mapped = nullptr; // h_average as the device sees it
 	uint32_t num_map_polygons = 0, num_map_vertices = 0;
+	uint64_t map_lightmap_end = 0; // the largest lightmap end (offset + size) over sw_set_map's polygons
 	std::vector<uint64_t> poly_bound_prefix;
 	SwViewCounts* h_counts = nullptr; // pinned, one per staging set (frames alternate)
 	cudaEvent_t ev_counts[2] = {nullptr, nullptr};
@@ -580,7 +582,7 @@ int sw_destroy(SwCtx* ctx)
 	cudaSetDevice(ctx->device);
 	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
 	if (ctx->aux) cudaStreamSynchronize(ctx->aux);
-	DevBuf* bufs[] = {&ctx->texels, &ctx->texture_mips, &ctx->emissive, &ctx->emissive_mips, &ctx->lightmaps, &ctx->skybox32,
+	DevBuf* bufs[] = {&ctx->texels, &ctx->texture_mips, &ctx->emissive, &ctx->emissive_mips, &ctx->lightmaps, &ctx->lm_compressed, &ctx->skybox32,
 		&ctx->skybox64, &ctx->frame_in,
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->tri_steps, &ctx->tri_vertices, &ctx->lite, &ctx->ldr[0], &ctx->ldr[1], &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
@@ -1293,6 +1295,57 @@ int sw_read_framebuffer(SwCtx* ctx, void* dst_host, uint64_t max_bytes)
 	return SW_OK;
 }
 
+int sw_set_lightmaps_compressed(SwCtx* ctx, const void* lightmaps, uint64_t num_elements, const void* directional,
+	uint64_t num_directional_elements)
+{
+	if (!ctx || (num_elements && !lightmaps) || (num_directional_elements && !directional)) return SW_ERR_INVALID_ARGUMENT;
+	if (num_elements > (1ull << 31) || num_directional_elements > (1ull << 31))
+		return fail(ctx, SW_ERR_LIMIT, "too many lightmap elements");
+	// the map's polygons (sw_set_map) must still read inside the lightmaps
+	const uint64_t end = ctx->map_lightmap_end;
+	if ((num_elements > 1 && num_elements < end) || (num_directional_elements > 1 && num_directional_elements < end))
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "lightmaps shorter than the map's polygons read (%llu elements)",
+			(unsigned long long)end);
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	// frames in flight may still read the lightmaps being replaced
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	if (ctx->aux) SW_CUDA(ctx, cudaStreamSynchronize(ctx->aux));
+	if (ctx->copy) SW_CUDA(ctx, cudaStreamSynchronize(ctx->copy));
+	const size_t simple_bytes = size_t(num_elements) * SW_LIGHTMAP_COMPRESSED_BYTES, dir_at = (simple_bytes + 255) / 256 * 256;
+	const size_t dir_bytes = size_t(num_directional_elements) * SW_DIR_LIGHTMAP_COMPRESSED_BYTES;
+	int r;
+	if ((r = ensure(ctx, ctx->lm_compressed, dir_at + dir_bytes + 16))) return r;
+	if ((r = ensure(ctx, ctx->lightmaps, std::max<size_t>(num_elements * 12, 16)))) return r;
+	if ((r = ensure(ctx, ctx->dir_lightmaps, std::max<size_t>(num_directional_elements * sizeof(SwDirectionalLightmapElement), 16))))
+		return r;
+	unsigned char* staged = static_cast<unsigned char*>(ctx->lm_compressed.ptr);
+	if (simple_bytes) SW_CUDA(ctx, cudaMemcpy(staged, lightmaps, simple_bytes, cudaMemcpyHostToDevice));
+	if (dir_bytes) SW_CUDA(ctx, cudaMemcpy(staged + dir_at, directional, dir_bytes, cudaMemcpyHostToDevice));
+	if ((r = check_kernel(ctx,
+			 launch_lightmap_decompress(staged, num_elements, static_cast<float*>(ctx->lightmaps.ptr), staged + dir_at,
+				 num_directional_elements, static_cast<SwDirectionalLightmapElement*>(ctx->dir_lightmaps.ptr), ctx->stream),
+			 "lightmap decompression")))
+		return r;
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	ctx->num_lightmap_elements = num_elements;
+	ctx->num_dir_lightmap_elements = num_directional_elements;
+	ctx->stats.upload_bytes += simple_bytes + dir_bytes;
+	return SW_OK;
+}
+
+int sw_read_lightmaps(SwCtx* ctx, float* lightmaps, uint64_t max_elements, SwDirectionalLightmapElement* directional,
+	uint64_t max_directional_elements)
+{
+	if (!ctx || (max_elements && !lightmaps) || (max_directional_elements && !directional)) return SW_ERR_INVALID_ARGUMENT;
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	const uint64_t n = std::min(max_elements, ctx->num_lightmap_elements);
+	const uint64_t nd = std::min(max_directional_elements, ctx->num_dir_lightmap_elements);
+	if (n) SW_CUDA(ctx, cudaMemcpy(lightmaps, ctx->lightmaps.ptr, n * 12, cudaMemcpyDeviceToHost));
+	if (nd) SW_CUDA(ctx, cudaMemcpy(directional, ctx->dir_lightmaps.ptr, nd * sizeof(SwDirectionalLightmapElement), cudaMemcpyDeviceToHost));
+	return SW_OK;
+}
+
 int sw_get_exposure(SwCtx* ctx, float* out_exposure)
 {
 	if (!ctx || !out_exposure) return SW_ERR_INVALID_ARGUMENT;
@@ -1655,6 +1708,7 @@ int sw_set_map(SwCtx* ctx, const SwMapPolygon* polygons, uint32_t num_polygons, 
 {
 	if (!ctx || (num_polygons && !polygons) || (num_vertices && !vertices)) return SW_ERR_INVALID_ARGUMENT;
 	const uint64_t simple = ctx->num_lightmap_elements, directional = ctx->num_dir_lightmap_elements;
+	uint64_t lightmap_end = 0;
 	std::vector<uint64_t> prefix(size_t(num_polygons) + 1, 0);
 	for (uint32_t i = 0; i < num_polygons; ++i)
 	{
@@ -1676,6 +1730,7 @@ int sw_set_map(SwCtx* ctx, const SwMapPolygon* polygons, uint32_t num_polygons, 
 			const uint64_t end = uint64_t(p.lightmap_data_offset) + lw * lh;
 			if ((simple > 1 && end > simple) || (directional > 1 && end > directional))
 				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "polygon %u: lightmap out of range", i);
+			lightmap_end = std::max(lightmap_end, end);
 		}
 		prefix[i + 1] = prefix[i] + swhost::max_surface_texels(p);
 	}
@@ -1687,6 +1742,7 @@ int sw_set_map(SwCtx* ctx, const SwMapPolygon* polygons, uint32_t num_polygons, 
 	if ((r = upload_static(ctx, ctx->map_vertices, vertices, size_t(num_vertices) * 12))) return r;
 	ctx->num_map_polygons = num_polygons;
 	ctx->num_map_vertices = num_vertices;
+	ctx->map_lightmap_end = lightmap_end;
 	ctx->poly_bound_prefix.swap(prefix);
 	return SW_OK;
 }

@@ -1,7 +1,9 @@
 // Seeded synthetic scene generator (see scene.h). Load-time work, not on the timed path.
 #include "scene.h"
+#include "sqwm.h"
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <functional>
 
@@ -327,6 +329,89 @@ void make_emissive_texture(Rng& rng, uint32_t size, Scene& sc)
 }
 
 // ---- geometry -------------------------------------------------------------------------------
+
+// The config's moving point lights: each follows the camera path some frames ahead, orbiting a point
+// displaced from it.
+void add_dynamic_lights(const SceneConfig& cfg, Rng& rng, Scene& sc)
+{
+	for (uint32_t k = 0; k < cfg.num_dynamic_lights; ++k)
+	{
+		DynamicLightSpec d;
+		d.path_offset = 8 + rng.below(48);
+		d.offset = v3(rng.uniform(-24, 24), rng.uniform(-24, 24), rng.uniform(-16, 40));
+		d.orbit_radius = rng.uniform(8, 40);
+		d.radius = rng.uniform(192, 448);
+		const float intensity = rng.uniform(4e4f, 1.2e5f);
+		d.color[0] = intensity * rng.uniform(0.5f, 1.0f);
+		d.color[1] = intensity * rng.uniform(0.5f, 1.0f);
+		d.color[2] = intensity * rng.uniform(0.5f, 1.0f);
+		sc.dynamic_lights.push_back(d);
+	}
+}
+
+// The camera keys of a way-point polyline (densified as a Catmull-Rom spline when `smooth`): one key
+// per frame, 6 units apart along the line, looking 6 dense points ahead.
+void camera_path_from_way(const std::vector<Vec3>& way, bool smooth, const SceneConfig& cfg, Scene& sc)
+{
+	std::vector<Vec3> dense;
+	if (smooth)
+	{
+		for (size_t k = 0; k + 1 < way.size(); ++k)
+		{
+			const Vec3 p0 = way[k == 0 ? 0 : k - 1], p1 = way[k], p2 = way[k + 1], p3 = way[std::min(k + 2, way.size() - 1)];
+			for (int s = 0; s < 32; ++s)
+			{
+				const float t = s / 32.0f, t2 = t * t, t3 = t2 * t;
+				dense.push_back((p1 * 2.0f + (p2 - p0) * t + (p0 * 2.0f - p1 * 5.0f + p2 * 4.0f - p3) * t2 +
+					(p1 * 3.0f - p0 - p2 * 3.0f + p3) * t3) * 0.5f);
+			}
+		}
+		dense.push_back(way.back());
+	}
+	else
+	{
+		// straight segments, 8 points each (so "6 points ahead" still looks ahead)
+		for (size_t k = 0; k + 1 < way.size(); ++k)
+			for (int s = 0; s < 8; ++s) dense.push_back(way[k] + (way[k + 1] - way[k]) * (float(s) / 8.0f));
+		dense.push_back(way.back());
+	}
+	const float speed = 6.0f; // units per frame
+	sc.camera_path.clear();
+	size_t seg = 0;
+	float along = 0.0f;
+	Vec3 pos = dense[0];
+	for (uint32_t f = 0; f < cfg.num_frames; ++f)
+	{
+		// Advance `speed` units along the polyline.
+		float left = f == 0 ? 0.0f : speed;
+		while (left > 0.0f && seg + 1 < dense.size())
+		{
+			const float seg_len = magnitude(dense[seg + 1] - dense[seg]);
+			if (along + left < seg_len)
+			{
+				along += left;
+				left = 0.0f;
+			}
+			else
+			{
+				left -= seg_len - along;
+				along = 0.0f;
+				++seg;
+			}
+		}
+		const size_t s2 = std::min(seg + 1, dense.size() - 1);
+		const float seg_len = std::fmax(magnitude(dense[s2] - dense[seg]), 1e-6f);
+		pos = dense[seg] + (dense[s2] - dense[seg]) * (along / seg_len);
+		const size_t ahead = std::min(seg + 6, dense.size() - 1);
+		Vec3 dir = dense[ahead] - pos;
+		if (magnitude2(dir) < 1e-6f) dir = v3(1, 0, 0);
+		CameraKey k;
+		k.position = pos;
+		k.azimuth = std::atan2(dir.y, dir.x);
+		k.elevation = 0.08f * std::sin(float(f) * 0.07f) + cfg.camera_pitch;
+		sc.camera_path.push_back(k);
+	}
+}
 
 struct Builder
 {
@@ -817,55 +902,7 @@ struct Builder
 			prev = cur;
 			cur = next;
 		}
-		// Dense Catmull-Rom polyline.
-		std::vector<Vec3> dense;
-		for (size_t k = 0; k + 1 < way.size(); ++k)
-		{
-			const Vec3 p0 = way[k == 0 ? 0 : k - 1], p1 = way[k], p2 = way[k + 1], p3 = way[std::min(k + 2, way.size() - 1)];
-			for (int s = 0; s < 32; ++s)
-			{
-				const float t = s / 32.0f, t2 = t * t, t3 = t2 * t;
-				dense.push_back((p1 * 2.0f + (p2 - p0) * t + (p0 * 2.0f - p1 * 5.0f + p2 * 4.0f - p3) * t2 +
-					(p1 * 3.0f - p0 - p2 * 3.0f + p3) * t3) * 0.5f);
-			}
-		}
-		dense.push_back(way.back());
-		const float speed = 6.0f; // units per frame
-		sc.camera_path.clear();
-		size_t seg = 0;
-		float along = 0.0f;
-		Vec3 pos = dense[0];
-		for (uint32_t f = 0; f < cfg.num_frames; ++f)
-		{
-			// Advance `speed` units along the polyline.
-			float left = f == 0 ? 0.0f : speed;
-			while (left > 0.0f && seg + 1 < dense.size())
-			{
-				const float seg_len = magnitude(dense[seg + 1] - dense[seg]);
-				if (along + left < seg_len)
-				{
-					along += left;
-					left = 0.0f;
-				}
-				else
-				{
-					left -= seg_len - along;
-					along = 0.0f;
-					++seg;
-				}
-			}
-			const size_t s2 = std::min(seg + 1, dense.size() - 1);
-			const float seg_len = std::fmax(magnitude(dense[s2] - dense[seg]), 1e-6f);
-			pos = dense[seg] + (dense[s2] - dense[seg]) * (along / seg_len);
-			const size_t ahead = std::min(seg + 6, dense.size() - 1);
-			Vec3 dir = dense[ahead] - pos;
-			if (magnitude2(dir) < 1e-6f) dir = v3(1, 0, 0);
-			CameraKey k;
-			k.position = pos;
-			k.azimuth = std::atan2(dir.y, dir.x);
-			k.elevation = 0.08f * std::sin(float(f) * 0.07f) + cfg.camera_pitch;
-			sc.camera_path.push_back(k);
-		}
+		camera_path_from_way(way, true, cfg, sc);
 	}
 };
 
@@ -1231,7 +1268,7 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 			e.mesh = mrng.below(num_meshes);
 			e.texture = e.mesh;
 			e.leaf = r.leaf;
-			e.blending_mode = e.mesh == num_meshes - 1 ? SW_BLEND_ALPHA_TEST : blends[mrng.below(4)];
+			e.blending_mode = e.mesh == num_meshes - 1 ? uint32_t(SW_BLEND_ALPHA_TEST) : blends[mrng.below(4)];
 			const ModelMesh& mm = sc.model_meshes[e.mesh];
 			const float margin = 48.0f;
 			e.position = v3(mrng.uniform(r.x0 + margin, r.x1 - margin), mrng.uniform(r.y0 + margin, r.y1 - margin),
@@ -1247,19 +1284,245 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 			sc.models.push_back(e);
 		}
 	}
-	for (uint32_t k = 0; k < cfg.num_dynamic_lights; ++k)
+	add_dynamic_lights(cfg, rng, sc);
+	return true;
+}
+
+// ---- scenes from compiled maps ----------------------------------------------------------------
+
+namespace
+{
+
+uint64_t fnv1a(const char* s, size_t n)
+{
+	uint64_t h = 1469598103934665603ull;
+	for (size_t i = 0; i < n; ++i) h = (h ^ uint8_t(s[i])) * 1099511628211ull;
+	return h;
+}
+
+// Every index and range of the map that rendering follows; false with a message on the first bad one.
+bool check_map(const SqwmMap& m, bool directional, std::string& error)
+{
+	char buf[160];
+	auto bad = [&](const char* fmt, uint64_t i) {
+		std::snprintf(buf, sizeof(buf), fmt, (unsigned long long)i);
+		error = buf;
+		return false;
+	};
+	if (m.nodes.empty() || m.leafs.empty()) return bad("map has no BSP tree (%llu nodes)", m.nodes.size());
+	if (m.textures.empty()) return bad("map has no textures (%llu)", 0);
+	// children: leafs in range, nodes before their parent (the root is the last node), depth bounded
+	std::vector<uint32_t> depth(m.nodes.size(), 0);
+	for (size_t n = 0; n < m.nodes.size(); ++n)
+		for (int c = 0; c < 2; ++c)
+		{
+			const uint32_t ch = m.nodes[n].children[c];
+			if (ch >= FIRST_LEAF_INDEX)
+			{
+				if (ch - FIRST_LEAF_INDEX >= m.leafs.size()) return bad("node %llu: leaf child out of range", n);
+			}
+			else if (ch >= n)
+				return bad("node %llu: child node not before its parent", n);
+			else
+				depth[n] = std::max(depth[n], depth[ch] + 1);
+		}
+	if (depth.back() + 1 >= 72) return bad("BSP tree deeper than 72 (%llu)", depth.back() + 1);
+	std::vector<uint8_t> owned(m.polygons.size(), 0);
+	for (size_t l = 0; l < m.leafs.size(); ++l)
 	{
-		DynamicLightSpec d;
-		d.path_offset = 8 + rng.below(48);
-		d.offset = v3(rng.uniform(-24, 24), rng.uniform(-24, 24), rng.uniform(-16, 40));
-		d.orbit_radius = rng.uniform(8, 40);
-		d.radius = rng.uniform(192, 448);
-		const float intensity = rng.uniform(4e4f, 1.2e5f);
-		d.color[0] = intensity * rng.uniform(0.5f, 1.0f);
-		d.color[1] = intensity * rng.uniform(0.5f, 1.0f);
-		d.color[2] = intensity * rng.uniform(0.5f, 1.0f);
-		sc.dynamic_lights.push_back(d);
+		const BspLeaf& f = m.leafs[l];
+		if (uint64_t(f.first_polygon) + f.num_polygons > m.polygons.size()) return bad("leaf %llu: polygons out of range", l);
+		if (uint64_t(f.first_leaf_portal) + f.num_leaf_portals > m.leafs_portals.size())
+			return bad("leaf %llu: portals out of range", l);
+		for (uint32_t p = 0; p < f.num_polygons; ++p)
+			if (owned[f.first_polygon + p]++) return bad("polygon %llu in two leafs", f.first_polygon + p);
 	}
+	for (size_t i = 0; i < m.leafs_portals.size(); ++i)
+		if (m.leafs_portals[i] >= m.portals.size()) return bad("leaf portal %llu out of range", i);
+	for (size_t i = 0; i < m.portals.size(); ++i)
+	{
+		const MapPortal& p = m.portals[i];
+		if (p.leafs[0] >= m.leafs.size() || p.leafs[1] >= m.leafs.size()) return bad("portal %llu: leaf out of range", i);
+		if (p.num_vertices < 3 || uint64_t(p.first_vertex) + p.num_vertices > m.vertices.size())
+			return bad("portal %llu: vertices out of range", i);
+	}
+	const uint64_t lm_elems = directional ? m.directional_lightmaps.size() : m.lightmaps.size() / 3;
+	for (size_t i = 0; i < m.polygons.size(); ++i)
+	{
+		const MapPolygon& p = m.polygons[i];
+		if (p.num_vertices < 3 || uint64_t(p.first_vertex) + p.num_vertices > m.vertices.size())
+			return bad("polygon %llu: vertices out of range", i);
+		if (p.texture >= m.textures.size()) return bad("polygon %llu: texture out of range", i);
+		if (p.tex_coord_min[0] > p.tex_coord_max[0] || p.tex_coord_min[1] > p.tex_coord_max[1] ||
+			int64_t(p.tex_coord_max[0]) - p.tex_coord_min[0] > 4096 || int64_t(p.tex_coord_max[1]) - p.tex_coord_min[1] > 4096)
+			return bad("polygon %llu: bad texture coordinate bounds", i);
+		if (p.lightmap_data_offset != 0)
+		{
+			// get_polygon_lightmap_size, lightmap.rs:11-27
+			const uint64_t lw = uint64_t(((p.tex_coord_max[0] + 15) >> 4) - (p.tex_coord_min[0] >> 4) + 1);
+			const uint64_t lh = uint64_t(((p.tex_coord_max[1] + 15) >> 4) - (p.tex_coord_min[1] >> 4) + 1);
+			if (uint64_t(p.lightmap_data_offset) + lw * lh > lm_elems) return bad("polygon %llu: lightmap out of range", i);
+		}
+	}
+	return true;
+}
+
+uint32_t leaf_of_point(const SqwmMap& m, const Vec3& p)
+{
+	// get_leaf_for_point, bsp_map_compact.rs:241-261
+	uint32_t index = uint32_t(m.nodes.size() - 1);
+	while (index < FIRST_LEAF_INDEX)
+	{
+		const BspNode& n = m.nodes[index];
+		index = dot(n.plane.vec, p) > n.plane.dist ? n.children[0] : n.children[1];
+	}
+	return index - FIRST_LEAF_INDEX;
+}
+
+Vec3 sum_points(const std::vector<Vec3>& v, uint32_t first, uint32_t count, Vec3 sum, uint32_t& n)
+{
+	for (uint32_t i = 0; i < count; ++i) sum = sum + v[first + i];
+	n += count;
+	return sum;
+}
+
+} // namespace
+
+bool scene_from_map(const SqwmMap& m, const SceneConfig& cfg, Scene& sc, std::string& error)
+{
+	if (cfg.texture_size < 16 || (cfg.texture_size & (cfg.texture_size - 1)))
+	{
+		error = "texture_size must be a power of two >= 16";
+		return false;
+	}
+	if (cfg.directional_lightmaps && m.directional_lightmaps.empty())
+	{
+		error = "the map has no directional lightmaps";
+		return false;
+	}
+	if (!cfg.directional_lightmaps && m.lightmaps.empty())
+	{
+		error = "the map has no lightmaps";
+		return false;
+	}
+	if (cfg.sky_rooms || cfg.num_models || cfg.animated_materials)
+	{
+		error = "sky rooms, models and animated materials are options of generated scenes only";
+		return false;
+	}
+	if (!check_map(m, cfg.directional_lightmaps, error)) return false;
+	sc = Scene();
+	sc.config = cfg;
+	sc.config.num_materials = uint32_t(m.textures.size());
+	sc.nodes = m.nodes;
+	sc.leafs = m.leafs;
+	sc.polygons = m.polygons;
+	sc.portals = m.portals;
+	sc.leafs_portals = m.leafs_portals;
+	sc.vertices = m.vertices;
+	sc.lightmaps = m.lightmaps;
+	sc.directional_lightmaps = m.directional_lightmaps;
+	sc.lightmap_elements = cfg.directional_lightmaps ? m.directional_lightmaps.size() : m.lightmaps.size() / 3;
+	sc.lightmaps_compressed.resize(m.lightmaps_compressed.size() * sizeof(CompressedColor));
+	if (!sc.lightmaps_compressed.empty())
+		std::memcpy(sc.lightmaps_compressed.data(), m.lightmaps_compressed.data(), sc.lightmaps_compressed.size());
+	sc.directional_lightmaps_compressed.resize(m.directional_lightmaps_compressed.size() * sizeof(DirectionalLightmapElementCompressed));
+	if (!sc.directional_lightmaps_compressed.empty())
+		std::memcpy(sc.directional_lightmaps_compressed.data(), m.directional_lightmaps_compressed.data(),
+			sc.directional_lightmaps_compressed.size());
+	sc.polygon_leaf.assign(sc.polygons.size(), 0);
+	for (size_t l = 0; l < sc.leafs.size(); ++l)
+		for (uint32_t p = 0; p < sc.leafs[l].num_polygons; ++p) sc.polygon_leaf[sc.leafs[l].first_polygon + p] = uint32_t(l);
+
+	// One material per texture name, its texture procedural (seeded by the name: the image files the
+	// names refer to are not part of a compiled map).
+	const uint32_t nm = uint32_t(m.textures.size());
+	const uint32_t n_metal = uint32_t(cfg.metal_frac * nm + 0.5f);
+	const uint32_t n_diel = uint32_t(cfg.dielectric_frac * nm + 0.5f);
+	for (uint32_t t = 0; t < nm; ++t)
+	{
+		const char* name = m.textures[t].name;
+		Rng trng(fnv1a(name, strnlen(name, sizeof(m.textures[t].name))) ^ cfg.seed);
+		const bool metal = t < n_metal;
+		const bool diel = !metal && t < n_metal + n_diel;
+		make_material_texture(trng, cfg.texture_size, cfg.normal_maps, metal ? 0.35f : diel ? 0.5f : 1.0f, metal, sc);
+		Material mat;
+		mat.texture_size = cfg.texture_size;
+		if (t < cfg.scrolling_materials)
+		{
+			mat.scroll_speed[0] = 24.0f + 8.0f * float(t);
+			mat.scroll_speed[1] = (t & 1) ? -13.5f : 6.25f;
+		}
+		sc.materials.push_back(mat);
+	}
+	sc.basis.resize(sc.polygons.size());
+	for (size_t p = 0; p < sc.polygons.size(); ++p)
+		sc.basis[p] = form_plane_and_tex_coord_equation(sc.polygons[p].plane, sc.polygons[p].tex_coord_equation);
+
+	// Camera path: from the player start (or leaf 0's centre) through leaf centres and the centres of
+	// the portals between them, turning back only at dead ends.
+	std::vector<Vec3> leaf_center(sc.leafs.size());
+	for (size_t l = 0; l < sc.leafs.size(); ++l)
+	{
+		Vec3 sum = v3(0, 0, 0);
+		uint32_t n = 0;
+		const BspLeaf& f = sc.leafs[l];
+		for (uint32_t p = 0; p < f.num_polygons; ++p)
+		{
+			const MapPolygon& poly = sc.polygons[f.first_polygon + p];
+			sum = sum_points(sc.vertices, poly.first_vertex, poly.num_vertices, sum, n);
+		}
+		for (uint32_t k = 0; k < f.num_leaf_portals; ++k)
+		{
+			const MapPortal& portal = sc.portals[sc.leafs_portals[f.first_leaf_portal + k]];
+			sum = sum_points(sc.vertices, portal.first_vertex, portal.num_vertices, sum, n);
+		}
+		leaf_center[l] = n ? sum * (1.0f / float(n)) : v3(0, 0, 0);
+	}
+	Rng rng(cfg.seed);
+	std::vector<Vec3> way;
+	uint32_t cur = 0;
+	for (uint32_t e = 0; e < m.entities.size(); ++e)
+		if (map_entity_value(m, e, "classname") == "info_player_start")
+		{
+			float x, y, z;
+			if (std::sscanf(map_entity_value(m, e, "origin").c_str(), "%f %f %f", &x, &y, &z) == 3)
+			{
+				way.push_back(v3(x, y, z));
+				cur = leaf_of_point(m, way.back());
+			}
+			break;
+		}
+	if (way.empty()) way.push_back(leaf_center[cur]);
+	uint32_t prev = ~0u;
+	for (int step = 0; step < 64; ++step)
+	{
+		const BspLeaf& f = sc.leafs[cur];
+		std::vector<uint32_t> nb, fresh;
+		for (uint32_t k = 0; k < f.num_leaf_portals; ++k)
+		{
+			const uint32_t pi = sc.leafs_portals[f.first_leaf_portal + k];
+			const MapPortal& portal = sc.portals[pi];
+			const uint32_t other = portal.leafs[0] == cur ? portal.leafs[1] : portal.leafs[0];
+			if (other == cur) continue;
+			nb.push_back(pi);
+			if (other != prev) fresh.push_back(pi);
+		}
+		if (nb.empty()) break;
+		const std::vector<uint32_t>& pick = fresh.empty() ? nb : fresh;
+		const MapPortal& portal = sc.portals[pick[rng.below(uint32_t(pick.size()))]];
+		const uint32_t next = portal.leafs[0] == cur ? portal.leafs[1] : portal.leafs[0];
+		uint32_t n = 0;
+		const Vec3 psum = sum_points(sc.vertices, portal.first_vertex, portal.num_vertices, v3(0, 0, 0), n);
+		const Vec3 pc = psum * (1.0f / float(n));
+		if (step > 0 || magnitude2(way.back() - leaf_center[cur]) > 1.0f) way.push_back(leaf_center[cur]);
+		way.push_back(pc);
+		prev = cur;
+		cur = next;
+	}
+	way.push_back(leaf_center[cur]);
+	camera_path_from_way(way, false, cfg, sc);
+	add_dynamic_lights(cfg, rng, sc);
 	return true;
 }
 

@@ -197,6 +197,11 @@ struct Scene
 	std::vector<std::vector<uint32_t>> leaf_models;
 	std::vector<uint32_t> lite_pixels;
 	std::vector<LiteMip> lite_mips;
+	// A scene loaded from a compiled map keeps its compressed lightmap lumps (4 bytes per simple
+	// element, 13 per directional element, as the file holds them) for upload and decompression on the
+	// GPU; empty for generated scenes.
+	std::vector<uint8_t> lightmaps_compressed;
+	std::vector<uint8_t> directional_lightmaps_compressed;
 
 	uint32_t root_node() const { return nodes.empty() ? FIRST_LEAF_INDEX : uint32_t(nodes.size() - 1); }
 	void frame_lights(uint32_t frame, std::vector<SwLight>& out) const;

@@ -2,12 +2,14 @@
 #include "../../include/swhost.h"
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
 
 #include "frame.h"
 #include "scene.h"
+#include "sqwm.h"
 
 using namespace swhost;
 
@@ -97,11 +99,10 @@ extern "C" {
 
 const char* swh_last_error(void) { return g_error.c_str(); }
 
-int swh_scene_create(const SwhSceneConfig* c, SwhScene** out)
+namespace
 {
-	if (!c || !out) return SW_ERR_INVALID_ARGUMENT;
-	*out = nullptr;
-	SceneConfig cfg;
+int scene_config_from(const SwhSceneConfig* c, SceneConfig& cfg)
+{
 	cfg.seed = c->seed;
 	cfg.grid_x = c->grid_x;
 	cfg.grid_y = c->grid_y;
@@ -136,6 +137,17 @@ int swh_scene_create(const SwhSceneConfig* c, SwhScene** out)
 		g_error = "too many models, model triangles or frames";
 		return SW_ERR_INVALID_ARGUMENT;
 	}
+	return SW_OK;
+}
+} // namespace
+
+int swh_scene_create(const SwhSceneConfig* c, SwhScene** out)
+{
+	if (!c || !out) return SW_ERR_INVALID_ARGUMENT;
+	*out = nullptr;
+	SceneConfig cfg;
+	const int st = scene_config_from(c, cfg);
+	if (st != SW_OK) return st;
 	SwhScene* s = new (std::nothrow) SwhScene();
 	if (!s) return SW_ERR_OUT_OF_MEMORY;
 	try
@@ -160,6 +172,113 @@ int swh_scene_destroy(SwhScene* s)
 {
 	if (!s) return SW_ERR_INVALID_ARGUMENT;
 	delete s;
+	return SW_OK;
+}
+
+int swh_scene_load_map_memory(const void* data, uint64_t size, const SwhSceneConfig* c, SwhScene** out)
+{
+	if (!data || !c || !out) return SW_ERR_INVALID_ARGUMENT;
+	*out = nullptr;
+	SceneConfig cfg;
+	int st = scene_config_from(c, cfg);
+	if (st != SW_OK) return st;
+	try
+	{
+		SqwmMap map;
+		std::string error;
+		if (sqwm_parse(static_cast<const uint8_t*>(data), size_t(size), map, error) != SQWM_OK)
+		{
+			g_error = error;
+			return SW_ERR_INVALID_ARGUMENT;
+		}
+		SwhScene* s = new SwhScene();
+		if (!scene_from_map(map, cfg, s->scene, g_error))
+		{
+			delete s;
+			return SW_ERR_INVALID_ARGUMENT;
+		}
+		*out = s;
+		return SW_OK;
+	}
+	catch (const std::bad_alloc&)
+	{
+		g_error = "out of host memory";
+		return SW_ERR_OUT_OF_MEMORY;
+	}
+}
+
+int swh_scene_load_map(const char* path, const SwhSceneConfig* c, SwhScene** out)
+{
+	if (!path || !c || !out) return SW_ERR_INVALID_ARGUMENT;
+	*out = nullptr;
+	std::FILE* f = std::fopen(path, "rb");
+	if (!f)
+	{
+		g_error = std::string("can't open ") + path;
+		return SW_ERR_INVALID_ARGUMENT;
+	}
+	std::vector<uint8_t> bytes;
+	try
+	{
+		uint8_t buf[1 << 16];
+		size_t n;
+		while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) bytes.insert(bytes.end(), buf, buf + n);
+	}
+	catch (const std::bad_alloc&)
+	{
+		std::fclose(f);
+		g_error = "out of host memory";
+		return SW_ERR_OUT_OF_MEMORY;
+	}
+	const bool read_error = std::ferror(f) != 0;
+	std::fclose(f);
+	if (read_error)
+	{
+		g_error = std::string("can't read ") + path;
+		return SW_ERR_INVALID_ARGUMENT;
+	}
+	return swh_scene_load_map_memory(bytes.data(), bytes.size(), c, out);
+}
+
+int swh_scene_save_map(const SwhScene* s, const char* path)
+{
+	if (!s || !path) return SW_ERR_INVALID_ARGUMENT;
+	try
+	{
+		SqwmMap map;
+		map_from_scene(s->scene, map);
+		std::vector<uint8_t> bytes;
+		sqwm_serialize(map, bytes);
+		std::FILE* f = std::fopen(path, "wb");
+		if (!f)
+		{
+			g_error = std::string("can't create ") + path;
+			return SW_ERR_INVALID_ARGUMENT;
+		}
+		const bool ok = std::fwrite(bytes.data(), 1, bytes.size(), f) == bytes.size();
+		if (std::fclose(f) != 0 || !ok)
+		{
+			g_error = std::string("can't write ") + path;
+			return SW_ERR_INVALID_ARGUMENT;
+		}
+		return SW_OK;
+	}
+	catch (const std::bad_alloc&)
+	{
+		g_error = "out of host memory";
+		return SW_ERR_OUT_OF_MEMORY;
+	}
+}
+
+int swh_scene_compressed_lightmaps(const SwhScene* s, const void** out_lightmaps, uint64_t* out_count,
+	const void** out_directional, uint64_t* out_directional_count)
+{
+	if (!s || !out_lightmaps || !out_count || !out_directional || !out_directional_count) return SW_ERR_INVALID_ARGUMENT;
+	const Scene& sc = s->scene;
+	*out_lightmaps = sc.lightmaps_compressed.data();
+	*out_count = sc.lightmaps_compressed.size() / SW_LIGHTMAP_COMPRESSED_BYTES;
+	*out_directional = sc.directional_lightmaps_compressed.data();
+	*out_directional_count = sc.directional_lightmaps_compressed.size() / SW_DIR_LIGHTMAP_COMPRESSED_BYTES;
 	return SW_OK;
 }
 
@@ -343,10 +462,30 @@ int swh_renderer_create(const SwhScene* s, uint32_t device, SwhRenderer** out)
 	if (!r) return SW_ERR_OUT_OF_MEMORY;
 	r->scene = s;
 	SwCreateInfo ci = s->scene.create_info(device);
+	// a loaded map's lightmaps go up compressed, as the file holds them, and are decoded on the GPU
+	const Scene& sc = s->scene;
+	const bool compressed = !sc.lightmaps_compressed.empty() || !sc.directional_lightmaps_compressed.empty();
+	if (compressed)
+	{
+		ci.lightmaps = nullptr;
+		ci.num_lightmap_elements = 0;
+		ci.directional_lightmaps = nullptr;
+		ci.num_directional_lightmap_elements = 0;
+	}
 	int st = sw_create(&ci, &r->ctx);
 	if (st != SW_OK)
 	{
 		g_error = "sw_create failed";
+		delete r;
+		return st;
+	}
+	if (compressed &&
+		(st = sw_set_lightmaps_compressed(r->ctx, sc.lightmaps_compressed.data(),
+			 sc.lightmaps_compressed.size() / SW_LIGHTMAP_COMPRESSED_BYTES, sc.directional_lightmaps_compressed.data(),
+			 sc.directional_lightmaps_compressed.size() / SW_DIR_LIGHTMAP_COMPRESSED_BYTES)) != SW_OK)
+	{
+		g_error = std::string("sw_set_lightmaps_compressed failed: ") + sw_last_error(r->ctx);
+		sw_destroy(r->ctx);
 		delete r;
 		return st;
 	}

@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(PKG_DIR, "lib", "libswgpu.so")
 
 EXPORTED = [
     "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_rebuild_surfaces_per_surface", "sw_set_surfaces", "sw_set_skybox", "sw_register_host_buffer", "sw_unregister_host_buffer",
-    "sw_submit_draws", "sw_submit_draws_ex", "sw_set_lite_textures",
+    "sw_submit_draws", "sw_submit_draws_ex", "sw_set_lite_textures", "sw_set_lightmaps_compressed", "sw_read_lightmaps",
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_read_framebuffer", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
     "sw_postprocess_noalloc", "sw_set_learned_upscaler", "sw_draw_frame", "sw_set_frame_graph", "sw_set_frames_in_flight", "sw_set_tuning",
@@ -65,6 +65,8 @@ def load_library(path=LIB_PATH):
         "sw_submit_draws": ([vp, vp, u32, vp, u32], i32),
         "sw_submit_draws_ex": ([vp, vp, u32, vp, u32, vp, u32], i32),
         "sw_set_lite_textures": ([vp, vp, u64], i32),
+        "sw_set_lightmaps_compressed": ([vp, vp, u64, vp, u64], i32),
+        "sw_read_lightmaps": ([vp, vp, u64, vp, u64], i32),
         "sw_render": ([vp, vp, u32, i32], i32),
         "sw_postprocess": ([vp, vp, f32, vp, vp, u32, i32], i32),
         "sw_upscale": ([vp, u32, u32, vp, i32, vp, u32, u32, u32, i32], i32),
@@ -264,6 +266,21 @@ class GpuRenderer:
         """Color32 textures of triangle draws (SW_TEXSRC_LITE), one array."""
         pixels = np.ascontiguousarray(pixels, dtype=np.uint32).reshape(-1)
         self._check(self.lib.sw_set_lite_textures(self.ctx, abi.ptr(pixels), pixels.size), "sw_set_lite_textures")
+
+    def set_lightmaps_compressed(self, simple, directional):
+        """Replace the lightmaps with compressed records decoded on the GPU: simple (n, 4) and directional
+        (m, 13) uint8 arrays as a compiled map holds them."""
+        a = np.ascontiguousarray(simple, dtype=np.uint8).reshape(-1, 4)
+        d = np.ascontiguousarray(directional, dtype=np.uint8).reshape(-1, 13)
+        self._check(self.lib.sw_set_lightmaps_compressed(self.ctx, abi.ptr(a), a.shape[0], abi.ptr(d), d.shape[0]),
+                    "sw_set_lightmaps_compressed")
+
+    def read_lightmaps(self, num_elements, num_directional):
+        """The decoded lightmaps: (float32 (n, 3), DIR_LIGHTMAP_ELEMENT (m,))."""
+        a = np.zeros((int(num_elements), 3), np.float32)
+        d = np.zeros(int(num_directional), abi.DIR_LIGHTMAP_ELEMENT)
+        self._check(self.lib.sw_read_lightmaps(self.ctx, abi.ptr(a), a.shape[0], abi.ptr(d), d.size), "sw_read_lightmaps")
+        return a, d
 
     def submit_draws_ex(self, draws, vertices, tri_vertices):
         """Draws with triangle draws among them (SW_RASTER_TRIANGLE, vertices in tri_vertices)."""

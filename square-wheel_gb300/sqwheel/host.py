@@ -82,6 +82,11 @@ def load_host_library():
         "swh_renderer_set_frames_in_flight": ([vp, u32], i32),
         "swh_scene_lite_textures": ([vp, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_uint64)], i32),
         "swh_frame_map": ([vp, ctypes.POINTER(vp), ctypes.POINTER(u32), ctypes.POINTER(vp), ctypes.POINTER(u32)], i32),
+        "swh_scene_load_map": ([ctypes.c_char_p, vp, ctypes.POINTER(vp)], i32),
+        "swh_scene_load_map_memory": ([vp, ctypes.c_uint64, vp, ctypes.POINTER(vp)], i32),
+        "swh_scene_save_map": ([vp, ctypes.c_char_p], i32),
+        "swh_scene_compressed_lightmaps": ([vp, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(vp),
+                                            ctypes.POINTER(ctypes.c_uint64)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -97,7 +102,8 @@ HOST_EXPORTED = ["swh_scene_create", "swh_scene_destroy", "swh_scene_info", "swh
                  "swh_renderer_draw_frame", "swh_renderer_context", "swh_renderer_frame", "swh_scene_skybox",
                  "swh_renderer_render_frame", "swh_frame_prepare_view", "swh_frame_view_input",
                  "swh_renderer_set_gpu_prep", "swh_frame_map", "swh_renderer_set_frames_in_flight",
-                 "swh_scene_lite_textures"]
+                 "swh_scene_lite_textures", "swh_scene_load_map", "swh_scene_load_map_memory", "swh_scene_save_map",
+                 "swh_scene_compressed_lightmaps"]
 
 # The two map configurations of the benchmark plan.
 SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, num_materials=16, metal_frac=0.0,
@@ -122,7 +128,9 @@ def _check(lib, r, what):
 
 
 class Scene:
-    def __init__(self, **kw):
+    def __init__(self, _map=None, **kw):
+        """A generated scene (keyword arguments: SceneConfig fields), or with _map (a path or the bytes of a
+        compiled .sqwm map) the scene swh_scene_load_map makes of that map."""
         self.lib = load_host_library()
         c = SceneConfig(seed=1, grid_x=4, grid_y=2, room_min=256.0, room_max=1024.0, tile_size=128.0, texture_size=128,
                         num_materials=16, metal_frac=0.0, dielectric_frac=0.0, normal_maps=0, directional_lightmaps=0,
@@ -134,7 +142,37 @@ class Scene:
             setattr(c, k, v)
         self.config = c
         self.handle = ctypes.c_void_p()
-        _check(self.lib, self.lib.swh_scene_create(ctypes.byref(c), ctypes.byref(self.handle)), "swh_scene_create")
+        if _map is None:
+            _check(self.lib, self.lib.swh_scene_create(ctypes.byref(c), ctypes.byref(self.handle)), "swh_scene_create")
+        elif isinstance(_map, (bytes, bytearray)):
+            buf = ctypes.create_string_buffer(bytes(_map), len(_map))
+            _check(self.lib, self.lib.swh_scene_load_map_memory(buf, len(_map), ctypes.byref(c), ctypes.byref(self.handle)),
+                   "swh_scene_load_map_memory")
+        else:
+            _check(self.lib, self.lib.swh_scene_load_map(os.fsencode(_map), ctypes.byref(c), ctypes.byref(self.handle)),
+                   "swh_scene_load_map")
+
+    @classmethod
+    def load_map(cls, path_or_bytes, **kw):
+        return cls(_map=path_or_bytes, **kw)
+
+    def save_map(self, path):
+        _check(self.lib, self.lib.swh_scene_save_map(self.handle, os.fsencode(path)), "swh_scene_save_map")
+
+    def compressed_lightmaps(self):
+        """(simple, directional) compressed lightmap records of a loaded map as uint8 arrays of shape (n, 4)
+        and (n, 13); empty for generated scenes."""
+        p, n, pd, nd = ctypes.c_void_p(), ctypes.c_uint64(), ctypes.c_void_p(), ctypes.c_uint64()
+        _check(self.lib, self.lib.swh_scene_compressed_lightmaps(self.handle, ctypes.byref(p), ctypes.byref(n),
+                                                                 ctypes.byref(pd), ctypes.byref(nd)),
+               "swh_scene_compressed_lightmaps")
+
+        def arr(ptr, count, width):
+            if not ptr.value or count.value == 0:
+                return np.zeros((0, width), np.uint8)
+            return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_uint8)),
+                                         shape=(int(count.value) * width,)).copy().reshape(-1, width)
+        return arr(p, n, 4), arr(pd, nd, 13)
 
     def info(self):
         i = SceneInfo()
