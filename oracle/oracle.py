@@ -41,6 +41,9 @@ def load():
     lib.orc_postprocess.argtypes = [vp, vp, u32, u32, f32, vp, ctypes.POINTER(f32), vp, u32, vp]
     lib.orc_upscale.argtypes = [u32, u32, vp, vp, u32, u32, u32]
     lib.orc_gaussian_kernel.argtypes = [f32, u32, vp]
+    for name in ("orc_compress_lightmaps", "orc_decompress_lightmaps", "orc_compress_directional_lightmaps",
+                 "orc_decompress_directional_lightmaps"):
+        getattr(lib, name).argtypes = [vp, u64, vp]
     for fn in (lib.orc_build_surfaces, lib.orc_rasterize, lib.orc_rasterize_ex, lib.orc_clear_background, lib.orc_postprocess,
                lib.orc_upscale, lib.orc_gaussian_kernel, lib.orc_shadow_maps, lib.orc_shadow_map_circle):
         fn.restype = i32
@@ -140,4 +143,36 @@ def upscale(mode, scale, src, dst_width, dst_height):
 def gaussian_kernel(sigma, radius):
     out = np.zeros(33, np.float32)
     _check(load().orc_gaussian_kernel(float(sigma), radius, abi.ptr(out)), "orc_gaussian_kernel")
+    return out
+
+
+def compress_lightmaps(rgb):
+    """CompressedColor records (n, 4) uint8 of float32 (n, 3) lightmap elements."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32).reshape(-1, 3)
+    out = np.zeros((rgb.shape[0], 4), np.uint8)
+    _check(load().orc_compress_lightmaps(abi.ptr(rgb), rgb.shape[0], abi.ptr(out)), "orc_compress_lightmaps")
+    return out
+
+
+def decompress_lightmaps(records):
+    records = np.ascontiguousarray(records, dtype=np.uint8).reshape(-1, 4)
+    out = np.zeros((records.shape[0], 3), np.float32)
+    _check(load().orc_decompress_lightmaps(abi.ptr(records), records.shape[0], abi.ptr(out)), "orc_decompress_lightmaps")
+    return out
+
+
+def compress_directional_lightmaps(elements):
+    """13-byte records (n, 13) uint8 of abi.DIR_LIGHTMAP_ELEMENT elements."""
+    elements = np.ascontiguousarray(elements, dtype=abi.DIR_LIGHTMAP_ELEMENT)
+    out = np.zeros((elements.size, 13), np.uint8)
+    _check(load().orc_compress_directional_lightmaps(abi.ptr(elements), elements.size, abi.ptr(out)),
+           "orc_compress_directional_lightmaps")
+    return out
+
+
+def decompress_directional_lightmaps(records):
+    records = np.ascontiguousarray(records, dtype=np.uint8).reshape(-1, 13)
+    out = np.zeros(records.shape[0], abi.DIR_LIGHTMAP_ELEMENT)
+    _check(load().orc_decompress_directional_lightmaps(abi.ptr(records), records.shape[0], abi.ptr(out)),
+           "orc_decompress_directional_lightmaps")
     return out

@@ -59,6 +59,13 @@ int orc_postprocess(const SwPostConfig* config, const uint64_t* hdr, uint32_t wi
 int orc_upscale(uint32_t mode, uint32_t scale, const uint32_t* src, uint32_t* dst, uint32_t dst_width,
 	uint32_t dst_height, uint32_t dst_pitch);
 
+/* Lossy lightmap compression (src/common/lightmap_compression.rs:48-130): simple elements as 4-byte
+ * CompressedColor records, directional elements as 13-byte records. */
+int orc_compress_lightmaps(const float* rgb, uint64_t n, uint8_t* out);
+int orc_decompress_lightmaps(const uint8_t* in, uint64_t n, float* rgb);
+int orc_compress_directional_lightmaps(const SwDirectionalLightmapElement* in, uint64_t n, uint8_t* out);
+int orc_decompress_directional_lightmaps(const uint8_t* in, uint64_t n, SwDirectionalLightmapElement* out);
+
 /* compute_gaussian_kernel (postprocessor.rs:1026-1045) and the integer blur weights of
  * perform_blur_impl (postprocessor.rs:848-907); exported for known-answer tests. */
 int orc_gaussian_kernel(float sigma, uint32_t radius, float* out33);
