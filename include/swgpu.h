@@ -290,6 +290,37 @@ int sw_set_skybox(SwCtx* ctx, const uint32_t* texels32, const uint64_t* texels64
 int sw_set_lightmaps_compressed(SwCtx* ctx, const void* lightmaps, uint64_t num_elements, const void* directional,
 	uint64_t num_directional_elements);
 
+/* Generative texture effects (GenerativeTextureEffect::update, map_materials_processor.rs:249-303): each
+ * frame the caller submits the passes that rewrite the effects' output textures, which are ordinary
+ * texture slots (texture_mips entries, or emissive_mips entries) of the static data that surfaces then
+ * read through SwMaterialFrame.texture / the surface descriptors. Passes run before the next frame's
+ * surfaces, on the context's stream.
+ *   SW_TEXPASS_TURB (make_turb_distortion, generative_texture_effect_turb.rs:91-138): dst texel (x, y) =
+ *     src texel ((x + s[y]) & (w - 1), (y + s[x]) & (h - 1)), s = the pass's max(w, h) shifts starting at
+ *     shifts_offset; src and dst the same power-of-two size; with SW_TEXPASS_EMISSIVE both are emissive
+ *     (Color32) mips, else material mips.
+ *   SW_TEXPASS_LAYER (apply_texture_layer, generative_texture_effect_layered.rs:163-381): the src mip,
+ *     tiled over dst with offset `shift` (rem_euclid of the src size), modulated by `light` (applied when
+ *     a component is outside [0.98, 1.02]) and blended into dst's current texels with blending_mode
+ *     (SW_BLEND_*); an additive layer whose light is at most 1/128 in every component is skipped.
+ *     Consecutive LAYER passes with the same dst form one group applied in order.
+ * A pass's dst must not be another pass's src, and two groups must not share a dst. Validated before
+ * anything is uploaded or launched. */
+#define SW_TEXPASS_TURB 1u
+#define SW_TEXPASS_LAYER 2u
+#define SW_TEXPASS_EMISSIVE 0x100u
+typedef struct SwTexturePass {
+	uint32_t kind;          /* SW_TEXPASS_TURB or SW_TEXPASS_LAYER, | SW_TEXPASS_EMISSIVE (TURB only) */
+	uint32_t dst_mip;       /* texture_mips (emissive_mips) index of the output mip */
+	uint32_t src_mip;       /* texture_mips (emissive_mips) index of the source mip */
+	uint32_t blending_mode; /* LAYER: SW_BLEND_* of the layer's material */
+	int32_t shift[2];       /* LAYER: layer texture offset (tex_coord_shift evaluated, >> mip) */
+	float light[3];         /* LAYER: modulate colour (r, g, b) */
+	uint32_t shifts_offset; /* TURB: first of the mip's max(w, h) shifts in `shifts` */
+} SwTexturePass;
+int sw_update_textures(SwCtx* ctx, const SwTexturePass* passes, uint32_t num_passes, const int32_t* shifts,
+	uint32_t num_shifts);
+
 /* Page-lock a host buffer the caller reuses for its frames (the window surface's pixels, say) with
  * cudaHostRegister (mapped), so that frames written to host memory inside it go straight from the
  * device into it instead of through the library's pinned staging buffer and a host copy (sw_draw_frame's
@@ -618,6 +649,9 @@ int sw_read_surfaces(SwCtx* ctx, void* dst_host, uint64_t max_bytes);
 /* Diagnostics: copy the context's frame buffer (the last frame rasterised, width x height pixels of its
  * pixel format, tightly packed; the HDR frame the postprocessor read) to host memory (synchronises). */
 int sw_read_framebuffer(SwCtx* ctx, void* dst_host, uint64_t max_bytes);
+/* Diagnostics: copy the context's material texels and emissive pixels (as texture effect passes left them)
+ * to host memory (synchronises). */
+int sw_read_texels(SwCtx* ctx, uint64_t* texels, uint64_t max_texels, uint32_t* emissive, uint64_t max_emissive);
 /* Diagnostics: copy the context's decoded lightmaps (up to max_elements simple and max_directional_elements
  * directional elements) to host memory (synchronises). */
 int sw_read_lightmaps(SwCtx* ctx, float* lightmaps, uint64_t max_elements, SwDirectionalLightmapElement* directional,

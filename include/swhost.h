@@ -45,6 +45,8 @@ typedef struct SwhSceneConfig {
 	uint32_t num_models;          /* per-vertex animated triangle models on the rooms' floors (0 = none) */
 	uint32_t model_triangles;     /* triangles per model mesh, about (0 = 2000) */
 	uint32_t model_frames;        /* animation keyframes per mesh (0 = 8) */
+	uint32_t turb_materials;      /* base materials with a turbulence effect (before the layered ones) */
+	uint32_t layered_materials;   /* the last this many base materials are layered animations */
 } SwhSceneConfig;
 
 typedef struct SwhSceneInfo {
@@ -90,6 +92,16 @@ int swh_scene_save_map(const SwhScene* scene, const char* path);
  * for generated scenes). Pointers stay valid while the scene lives. */
 int swh_scene_compressed_lightmaps(const SwhScene* scene, const void** out_lightmaps, uint64_t* out_count,
 	const void** out_directional, uint64_t* out_directional_count);
+/* A material's generative texture effect (SpecialMaterialEffect::Turb / LayeredAnimation, material.rs:146-197):
+ * kind 0 none, 1 turbulence, 2 layered animation; the texture slot its output is written to; for
+ * turbulence its TurbParams (amplitude, wave_length, frequency). */
+typedef struct SwhTextureEffect {
+	uint32_t kind;
+	int32_t output_texture;
+	uint32_t num_layers;
+	float turb[3];
+} SwhTextureEffect;
+int swh_scene_texture_effect(const SwhScene* scene, uint32_t material, SwhTextureEffect* out_effect);
 const char* swh_last_error(void);
 
 typedef struct SwhFrameOptions {
@@ -132,6 +144,11 @@ typedef struct SwhFrameOutputs {
 	const SwTriVertex* tri_vertices;
 	uint32_t num_tri_vertices;
 	uint32_t model_triangles;
+	/* generative texture effects of the frame (sw_update_textures, before the frame's surfaces) */
+	const SwTexturePass* texture_passes;
+	uint32_t num_texture_passes;
+	uint32_t num_texture_shifts;
+	const int32_t* texture_shifts;
 } SwhFrameOutputs;
 
 typedef struct SwhFrame SwhFrame;

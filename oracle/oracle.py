@@ -41,6 +41,8 @@ def load():
     lib.orc_postprocess.argtypes = [vp, vp, u32, u32, f32, vp, ctypes.POINTER(f32), vp, u32, vp]
     lib.orc_upscale.argtypes = [u32, u32, vp, vp, u32, u32, u32]
     lib.orc_gaussian_kernel.argtypes = [f32, u32, vp]
+    lib.orc_turb_shifts.argtypes = [f32, f32, f32, f32, u32, u32, u32, vp, u32]
+    lib.orc_apply_texture_passes.argtypes = [vp, u32, vp, u32, vp, u32, vp, vp, u32, vp]
     for name in ("orc_compress_lightmaps", "orc_decompress_lightmaps", "orc_compress_directional_lightmaps",
                  "orc_decompress_directional_lightmaps"):
         getattr(lib, name).argtypes = [vp, u64, vp]
@@ -176,3 +178,22 @@ def decompress_directional_lightmaps(records):
     _check(load().orc_decompress_directional_lightmaps(abi.ptr(records), records.shape[0], abi.ptr(out)),
            "orc_decompress_directional_lightmaps")
     return out
+
+
+def turb_shifts(amplitude, wave_length, frequency, time_s, width, height, mip, buffer):
+    """make_turb_distortion's shift table into `buffer` (int32, len >= max(width, height)), in place."""
+    assert buffer.dtype == np.int32 and buffer.flags["C_CONTIGUOUS"]
+    _check(load().orc_turb_shifts(amplitude, wave_length, frequency, time_s, width, height, mip, abi.ptr(buffer),
+                                  buffer.size), "orc_turb_shifts")
+    return buffer
+
+
+def apply_texture_passes(passes, shifts, static):
+    """The texture effect passes applied in order to static.texels / static.emissive_pixels, in place."""
+    passes = np.ascontiguousarray(passes, dtype=abi.TEXTURE_PASS)
+    shifts = np.ascontiguousarray(shifts if shifts is not None else np.zeros(0, np.int32), dtype=np.int32)
+    assert static.texels.flags["C_CONTIGUOUS"] and static.emissive_pixels.flags["C_CONTIGUOUS"]
+    _check(load().orc_apply_texture_passes(abi.ptr(passes), passes.size, abi.ptr(shifts), shifts.size,
+                                           abi.ptr(static.texture_mips), static.texture_mips.size, abi.ptr(static.texels),
+                                           abi.ptr(static.emissive_mips), static.emissive_mips.size,
+                                           abi.ptr(static.emissive_pixels)), "orc_apply_texture_passes")

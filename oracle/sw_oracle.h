@@ -59,6 +59,16 @@ int orc_postprocess(const SwPostConfig* config, const uint64_t* hdr, uint32_t wi
 int orc_upscale(uint32_t mode, uint32_t scale, const uint32_t* src, uint32_t* dst, uint32_t dst_width,
 	uint32_t dst_height, uint32_t dst_pitch);
 
+/* Generative texture effects: make_turb_distortion's shift table (generative_texture_effect_turb.rs:100-113)
+ * into `buffer` (persisting between calls like the effect's temp_buffer: entries below w rewritten), and
+ * the passes of sw_update_textures applied in order to the texel and emissive arrays (turbulence gathers,
+ * apply_texture_layer of generative_texture_effect_layered.rs:163-381). */
+int orc_turb_shifts(float amplitude, float wave_length, float frequency, float time_s, uint32_t w, uint32_t h, uint32_t mip,
+	int32_t* buffer, uint32_t buffer_len);
+int orc_apply_texture_passes(const SwTexturePass* passes, uint32_t num_passes, const int32_t* shifts, uint32_t num_shifts,
+	const SwTextureMip* mips, uint32_t num_mips, uint64_t* texels, const SwEmissiveMip* emissive_mips,
+	uint32_t num_emissive_mips, uint32_t* emissive);
+
 /* Lossy lightmap compression (src/common/lightmap_compression.rs:48-130): simple elements as 4-byte
  * CompressedColor records, directional elements as 13-byte records. */
 int orc_compress_lightmaps(const float* rgb, uint64_t n, uint8_t* out);

@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIB_DIR = os.path.join(PKG, "lib")
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(LIB_DIR, "libswgpu.so")
-SOURCES = ["swgpu.cu", "surfaces.cu", "raster.cu", "prep.cu", "post.cu", "post_noalloc.cu", "upscaler.cu", "lightmaps.cu"]
+SOURCES = ["swgpu.cu", "surfaces.cu", "raster.cu", "prep.cu", "post.cu", "post_noalloc.cu", "upscaler.cu", "lightmaps.cu", "effects.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

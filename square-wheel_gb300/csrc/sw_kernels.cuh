@@ -315,6 +315,36 @@ struct ShadowViewArgs
 int launch_shadow_view(const ShadowViewArgs& args, cudaStream_t stream);
 // make_shadow_map_circle on the size x size projector map at `map` with sequence `seq`.
 int launch_shadow_circle(unsigned long long* map, uint32_t size, uint32_t seq, cudaStream_t stream);
+// sw_update_textures (effects.cu): one group per output mip - a turbulence gather, or layers applied in
+// order. Groups are in texel order (first_texel ascending).
+struct TextureEffectGroup
+{
+	uint64_t first_texel;         // of the launch's flat texel space
+	uint64_t dst_offset, src_offset; // texel (or emissive pixel) offsets; src for turbulence only
+	uint32_t width, height;       // of the output mip
+	uint32_t first_pass, num_passes;
+};
+struct TextureEffectLayer // per pass (LAYER passes only)
+{
+	uint64_t src_offset;
+	uint32_t src_width, src_height;
+	uint32_t modulate, skip;
+	int32_t light[3]; // ColorVecI lanes b, g, r of light * 256
+	uint32_t reserved;
+};
+struct TextureEffectArgs
+{
+	const TextureEffectGroup* groups;
+	const TextureEffectLayer* layers;
+	const SwTexturePass* passes;
+	const int32_t* shifts;
+	uint32_t num_groups;
+	uint64_t total_texels;
+	uint64_t* texels;
+	uint32_t* emissive;
+};
+int launch_texture_effects(const TextureEffectArgs& a, cudaStream_t stream);
+
 // Compressed lightmap lumps (4-byte simple, 13-byte directional elements, 16-byte aligned inputs) decoded
 // into f32 lightmaps (lightmaps.cu).
 int launch_lightmap_decompress(const void* simple_in, uint64_t num_simple, float* simple_out, const void* dir_in,

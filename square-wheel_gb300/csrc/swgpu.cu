@@ -195,6 +195,9 @@ struct SwCtx
 	uint64_t shadow_texels = 0;
 	uint32_t num_shadow_descs = 0;
 	Staging stage_shadow, stage_shadow_descs;
+	// sw_update_textures: the groups, layers, passes and shifts of one call, uploaded together
+	DevBuf effect_buf;
+	Staging stage_effects;
 
 	// Optional per-stage device timing (sw_enable_timing).
 	bool timing = false;
@@ -587,7 +590,7 @@ int sw_destroy(SwCtx* ctx)
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->tri_steps, &ctx->tri_vertices, &ctx->lite, &ctx->ldr[0], &ctx->ldr[1], &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst, &ctx->map_polygons,
-		&ctx->map_vertices, &ctx->vslab, &ctx->shadow_storage, &ctx->shadow_descs};
+		&ctx->map_vertices, &ctx->vslab, &ctx->shadow_storage, &ctx->shadow_descs, &ctx->effect_buf};
 	for (DevBuf* b : bufs) release(*b);
 	for (const SwCtx::HostRange& h : ctx->registered) cudaHostUnregister(h.ptr);
 	if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
@@ -599,7 +602,7 @@ int sw_destroy(SwCtx* ctx)
 		if (e) cudaEventDestroy(e);
 	Staging* st[] = {&ctx->stage_lights, &ctx->stage_surfaces, &ctx->stage_prefix, &ctx->stage_draws,
 		&ctx->stage_vertices, &ctx->stage_tri_vertices, &ctx->stage_draw_rows, &ctx->stage_io, &ctx->gstage[0], &ctx->gstage[1], &ctx->stage_shadow,
-		&ctx->stage_shadow_descs};
+		&ctx->stage_shadow_descs, &ctx->stage_effects};
 	for (Staging* s : st)
 	{
 		if (s->host) cudaFreeHost(s->host);
@@ -1295,6 +1298,131 @@ int sw_read_framebuffer(SwCtx* ctx, void* dst_host, uint64_t max_bytes)
 	return SW_OK;
 }
 
+int sw_update_textures(SwCtx* ctx, const SwTexturePass* passes, uint32_t num_passes, const int32_t* shifts,
+	uint32_t num_shifts)
+{
+	if (!ctx || (num_passes && !passes) || (num_shifts && !shifts)) return SW_ERR_INVALID_ARGUMENT;
+	if (num_passes == 0) return SW_OK;
+	if (num_passes > (1u << 20) || num_shifts > (1u << 26)) return fail(ctx, SW_ERR_LIMIT, "too many texture passes or shifts");
+	const std::vector<SwTextureMip>& tm = ctx->h_texture_mips;
+	const std::vector<SwEmissiveMip>& em = ctx->h_emissive_mips;
+	std::vector<TextureEffectGroup> groups;
+	std::vector<TextureEffectLayer> layers(num_passes);
+	// destinations (index | emissive bit 31) of the groups, and every source, for the race checks
+	std::vector<uint32_t> dsts, srcs;
+	uint64_t total = 0;
+	for (uint32_t p = 0; p < num_passes;)
+	{
+		const SwTexturePass& a = passes[p];
+		const bool emissive = (a.kind & SW_TEXPASS_EMISSIVE) != 0;
+		const uint32_t kind = a.kind & ~SW_TEXPASS_EMISSIVE;
+		TextureEffectGroup g;
+		std::memset(&g, 0, sizeof(g));
+		g.first_pass = p;
+		g.first_texel = total;
+		if (kind == SW_TEXPASS_TURB)
+		{
+			const size_t n = emissive ? em.size() : tm.size();
+			if (a.dst_mip >= n || a.src_mip >= n || a.dst_mip == a.src_mip)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "texture pass %u: bad mip", p);
+			const uint32_t w = emissive ? em[a.dst_mip].width : tm[a.dst_mip].width;
+			const uint32_t h = emissive ? em[a.dst_mip].height : tm[a.dst_mip].height;
+			const uint32_t sw = emissive ? em[a.src_mip].width : tm[a.src_mip].width;
+			const uint32_t sh = emissive ? em[a.src_mip].height : tm[a.src_mip].height;
+			if (w == 0 || h == 0 || (w & (w - 1)) || (h & (h - 1)) || w != sw || h != sh)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "texture pass %u: turbulence needs equal power-of-two sizes", p);
+			if (uint64_t(a.shifts_offset) + std::max(w, h) > num_shifts)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "texture pass %u: shifts out of range", p);
+			g.width = w;
+			g.height = h;
+			g.dst_offset = emissive ? em[a.dst_mip].offset : tm[a.dst_mip].offset;
+			g.src_offset = emissive ? em[a.src_mip].offset : tm[a.src_mip].offset;
+			g.num_passes = 1;
+			dsts.push_back(a.dst_mip | (emissive ? 0x80000000u : 0u));
+			srcs.push_back(a.src_mip | (emissive ? 0x80000000u : 0u));
+			++p;
+		}
+		else if (kind == SW_TEXPASS_LAYER && !emissive)
+		{
+			if (a.dst_mip >= tm.size()) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "texture pass %u: bad mip", p);
+			g.width = tm[a.dst_mip].width;
+			g.height = tm[a.dst_mip].height;
+			g.dst_offset = tm[a.dst_mip].offset;
+			dsts.push_back(a.dst_mip);
+			uint32_t q = p;
+			for (; q < num_passes && passes[q].kind == SW_TEXPASS_LAYER && passes[q].dst_mip == a.dst_mip; ++q)
+			{
+				const SwTexturePass& l = passes[q];
+				if (l.src_mip >= tm.size() || tm[l.src_mip].width == 0 || tm[l.src_mip].height == 0 ||
+					tm[l.src_mip].width > (1u << 16) || tm[l.src_mip].height > (1u << 16))
+					return fail(ctx, SW_ERR_INVALID_ARGUMENT, "texture pass %u: bad layer mip", q);
+				if (l.blending_mode > SW_BLEND_ALPHA_BLEND) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "texture pass %u: bad blending mode", q);
+				bool modulate = false, zero = true;
+				for (int c = 0; c < 3; ++c)
+				{
+					const float v = l.light[c];
+					if (!(v >= 0.0f && v <= 127.0f)) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "texture pass %u: light outside [0, 127]", q);
+					modulate |= v < 0.98f || v > 1.02f;
+					zero &= v <= 1.0f / 128.0f;
+				}
+				TextureEffectLayer& L = layers[q];
+				L.src_offset = tm[l.src_mip].offset;
+				L.src_width = tm[l.src_mip].width;
+				L.src_height = tm[l.src_mip].height;
+				L.modulate = modulate ? 1u : 0u;
+				L.skip = (l.blending_mode == SW_BLEND_ADDITIVE && zero) ? 1u : 0u;
+				// ColorVecI::from_color_f32x3 of light * 256: lanes b, g, r (f32 -> i32 truncation)
+				L.light[0] = int32_t(l.light[2] * 256.0f);
+				L.light[1] = int32_t(l.light[1] * 256.0f);
+				L.light[2] = int32_t(l.light[0] * 256.0f);
+				srcs.push_back(l.src_mip);
+			}
+			g.num_passes = q - p;
+			p = q;
+		}
+		else
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "texture pass %u: unknown kind", p);
+		total += uint64_t(g.width) * g.height;
+		groups.push_back(g);
+	}
+	std::vector<uint32_t> sorted = dsts;
+	std::sort(sorted.begin(), sorted.end());
+	if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "two texture pass groups write the same mip");
+	for (uint32_t s : srcs)
+		if (std::binary_search(sorted.begin(), sorted.end(), s))
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "a texture pass reads a mip that another pass writes");
+	// one upload: groups | layers | passes | shifts
+	auto up16 = [](size_t v) { return (v + 15) / 16 * 16; };
+	const size_t o_layers = up16(groups.size() * sizeof(TextureEffectGroup));
+	const size_t o_passes = o_layers + up16(layers.size() * sizeof(TextureEffectLayer));
+	const size_t o_shifts = o_passes + up16(size_t(num_passes) * sizeof(SwTexturePass));
+	const size_t bytes = o_shifts + up16(size_t(num_shifts) * 4 + 4);
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	int r;
+	if ((r = ensure(ctx, ctx->effect_buf, bytes))) return r;
+	void* h = nullptr;
+	if ((r = staging_acquire(ctx, ctx->stage_effects, bytes, &h))) return r;
+	unsigned char* hb = static_cast<unsigned char*>(h);
+	std::memcpy(hb, groups.data(), groups.size() * sizeof(TextureEffectGroup));
+	std::memcpy(hb + o_layers, layers.data(), layers.size() * sizeof(TextureEffectLayer));
+	std::memcpy(hb + o_passes, passes, size_t(num_passes) * sizeof(SwTexturePass));
+	if (num_shifts) std::memcpy(hb + o_shifts, shifts, size_t(num_shifts) * 4);
+	if ((r = staging_commit(ctx, ctx->stage_effects, ctx->effect_buf.ptr, bytes))) return r;
+	unsigned char* d = static_cast<unsigned char*>(ctx->effect_buf.ptr);
+	TextureEffectArgs a;
+	std::memset(&a, 0, sizeof(a));
+	a.groups = reinterpret_cast<const TextureEffectGroup*>(d);
+	a.layers = reinterpret_cast<const TextureEffectLayer*>(d + o_layers);
+	a.passes = reinterpret_cast<const SwTexturePass*>(d + o_passes);
+	a.shifts = reinterpret_cast<const int32_t*>(d + o_shifts);
+	a.num_groups = uint32_t(groups.size());
+	a.total_texels = total;
+	a.texels = static_cast<uint64_t*>(ctx->texels.ptr);
+	a.emissive = static_cast<uint32_t*>(ctx->emissive.ptr);
+	return check_kernel(ctx, launch_texture_effects(a, ctx->stream), "texture effects");
+}
+
 int sw_set_lightmaps_compressed(SwCtx* ctx, const void* lightmaps, uint64_t num_elements, const void* directional,
 	uint64_t num_directional_elements)
 {
@@ -1330,6 +1458,17 @@ int sw_set_lightmaps_compressed(SwCtx* ctx, const void* lightmaps, uint64_t num_
 	ctx->num_lightmap_elements = num_elements;
 	ctx->num_dir_lightmap_elements = num_directional_elements;
 	ctx->stats.upload_bytes += simple_bytes + dir_bytes;
+	return SW_OK;
+}
+
+int sw_read_texels(SwCtx* ctx, uint64_t* texels, uint64_t max_texels, uint32_t* emissive, uint64_t max_emissive)
+{
+	if (!ctx || (max_texels && !texels) || (max_emissive && !emissive)) return SW_ERR_INVALID_ARGUMENT;
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	const uint64_t n = std::min(max_texels, ctx->num_texels), ne = std::min(max_emissive, ctx->num_emissive_pixels);
+	if (n) SW_CUDA(ctx, cudaMemcpy(texels, ctx->texels.ptr, n * 8, cudaMemcpyDeviceToHost));
+	if (ne) SW_CUDA(ctx, cudaMemcpy(emissive, ctx->emissive.ptr, ne * 4, cudaMemcpyDeviceToHost));
 	return SW_OK;
 }
 
@@ -2486,16 +2625,16 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 
 int sw_abi_layout(uint32_t* sizes, uint32_t count)
 {
-	const uint32_t s[23] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
+	const uint32_t s[24] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
 		uint32_t(sizeof(SwDirectionalLightmapElement)), uint32_t(sizeof(SwLight)), uint32_t(sizeof(SwSurfaceDesc)),
 		uint32_t(sizeof(SwVertex16)), uint32_t(sizeof(SwDrawCmd)), uint32_t(sizeof(SwFrameParams)),
 		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats)), uint32_t(sizeof(SwFrameInput)), uint32_t(sizeof(SwTuning)),
 		uint32_t(sizeof(SwMapPolygon)), uint32_t(sizeof(SwViewLeaf)), uint32_t(sizeof(SwViewFrameInput)),
 		uint32_t(sizeof(SwViewCounts)), uint32_t(sizeof(SwLightShadow)), uint32_t(sizeof(SwDepthDraw)),
 		uint32_t(sizeof(SwShadowSide)), uint32_t(sizeof(SwShadowLeaf)), uint32_t(sizeof(SwMaterialFrame)),
-		uint32_t(sizeof(SwTriVertex))};
-	for (uint32_t i = 0; sizes && i < count && i < 23; ++i) sizes[i] = s[i];
-	return 23;
+		uint32_t(sizeof(SwTriVertex)), uint32_t(sizeof(SwTexturePass))};
+	for (uint32_t i = 0; sizes && i < count && i < 24; ++i) sizes[i] = s[i];
+	return 24;
 }
 
 int sw_get_stats(SwCtx* ctx, SwStats* out)

@@ -1077,10 +1077,80 @@ void FramePrep::update_materials()
 	material_frames.resize(n);
 	for (uint32_t m = 0; m < n; ++m)
 	{
+		// get_texture (:311-327): the current frame's generated texture when it has a generative effect
+		const Material& cur = sc.materials[mapping[m]];
 		material_frames[m].shift[0] = shift[2 * mapping[m]];
 		material_frames[m].shift[1] = shift[2 * mapping[m] + 1];
-		material_frames[m].texture = mapping[m];
+		material_frames[m].texture = cur.effect_texture >= 0 ? uint32_t(cur.effect_texture) : mapping[m];
 		material_frames[m].reserved = 0;
+		if (cur.effect != Material::NO_EFFECT) animated = true;
+	}
+	update_texture_effects();
+}
+
+void FramePrep::update_texture_effects()
+{
+	// update_animations (map_materials_processor.rs:249-303) with the default update period of one frame:
+	// every effect's GenerativeTextureEffect::update at the frame's time, as texture passes.
+	const float tau = 6.28318530717958647692f;
+	texture_passes.clear();
+	texture_shifts.clear();
+	turb_buffers.resize(sc.materials.size());
+	for (uint32_t m = 0; m < uint32_t(sc.materials.size()); ++m)
+	{
+		const Material& mat = sc.materials[m];
+		if (mat.effect == Material::NO_EFFECT) continue;
+		for (uint32_t mip = 0; mip < NUM_MIPS; ++mip)
+		{
+			const uint32_t dst = uint32_t(mat.effect_texture) * NUM_MIPS + mip;
+			if (mat.effect == Material::TURB)
+			{
+				// make_turb_distortion (generative_texture_effect_turb.rs:91-138): the shift table, kept in the
+				// effect's buffer (resized to max(w, h), only the first w entries rewritten)
+				const SwTextureMip& src = sc.texture_mips[m * NUM_MIPS + mip];
+				std::vector<int32_t>& buf = turb_buffers[m];
+				buf.resize(std::max(src.width, src.height), 0);
+				const float mip_scale = 1.0f / float(1 << mip);
+				const float amplitude = mip_scale * mat.turb_amplitude;
+				const float frequency_scaled = tau / (mat.turb_wave_length * mip_scale);
+				const float time_shift = frame_time_s * mat.turb_frequency * tau;
+				for (uint32_t x = 0; x < src.width; ++x)
+					buf[x] = as_i32(std::round(std::sin(float(x) * frequency_scaled + time_shift) * amplitude));
+				SwTexturePass p;
+				std::memset(&p, 0, sizeof(p));
+				p.kind = SW_TEXPASS_TURB;
+				p.dst_mip = dst;
+				p.src_mip = m * NUM_MIPS + mip;
+				p.shifts_offset = uint32_t(texture_shifts.size());
+				texture_shifts.insert(texture_shifts.end(), buf.begin(), buf.end());
+				texture_passes.push_back(p);
+				continue;
+			}
+			// GenerativeTextureEffectLayered::update (generative_texture_effect_layered.rs:63-161)
+			for (const EffectLayer& l : mat.layers)
+			{
+				SwTexturePass p;
+				std::memset(&p, 0, sizeof(p));
+				p.kind = SW_TEXPASS_LAYER;
+				p.dst_mip = dst;
+				for (int i = 0; i < 2; ++i) p.shift[i] = as_i32(l.tex_coord_shift[i].evaluate(frame_time_s)) >> mip;
+				const float max_light = 127.0f;
+				for (int c = 0; c < 3; ++c)
+				{
+					float v = 1.0f;
+					if (l.has_modulate_color) v = l.modulate_color[c].evaluate(frame_time_s);
+					else if (l.has_modulate) v = l.modulate.evaluate(frame_time_s);
+					if (l.has_modulate_color || l.has_modulate) v = std::fmin(std::fmax(v, 0.0f), max_light);
+					p.light[c] = v;
+				}
+				const uint32_t tex = l.follow_framed_animation ? mapping[l.material] : l.material;
+				const Material& lm = sc.materials[tex];
+				if (!lm.has_diffuse) continue;
+				p.src_mip = tex * NUM_MIPS + mip;
+				p.blending_mode = lm.blending_mode;
+				texture_passes.push_back(p);
+			}
+		}
 	}
 }
 

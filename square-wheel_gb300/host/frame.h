@@ -136,6 +136,9 @@ public:
 	// Animated materials: per material its current frame's texture and scrolling shift; `animated` is
 	// false when no material scrolls or has frames (the view input then passes no table).
 	std::vector<SwMaterialFrame> material_frames;
+	// the frame's generative texture effect passes (sw_update_textures) and their turbulence shifts
+	std::vector<SwTexturePass> texture_passes;
+	std::vector<int32_t> texture_shifts;
 	bool animated = false;
 	// Game time of the frame (prepare / prepare_view: frame index / 60 s; the *_with_camera forms keep it).
 	float frame_time_s = 0.0f;
@@ -185,6 +188,8 @@ private:
 	void update_materials();
 	std::vector<uint32_t> mapping; // textures_mapping_table: current frame of each material (persists)
 	std::vector<float> change_time; // its frame_change_time_point
+	std::vector<std::vector<int32_t>> turb_buffers; // each turbulent material's temp_buffer (persists)
+	void update_texture_effects();
 	void begin_frame(const CameraMatrices& cam, const std::vector<SwLight>& lights, const FrameOptions& opt, Quat skybox_rotation);
 	void finish_params();
 	void camera_of_frame(uint32_t frame_index, const FrameOptions& opt, CameraMatrices& cam, std::vector<SwLight>& lights,

@@ -1109,6 +1109,140 @@ void make_model_skin(Rng& rng, uint32_t size, bool cutout, Scene& sc)
 	}
 }
 
+float TimeFunction::evaluate(float x) const
+{
+	// SingleArgumentFunction::evaluate, material_function.rs:91-150
+	const float tau = 6.28318530717958647692f;
+	auto fract = [](float v) { return v - std::floor(v); };
+	switch (kind)
+	{
+	case CONSTANT: return a;
+	case LINEAR: return x * a + b;
+	case SIN_WAVE: return std::sin(x * a * tau + b) * c + d;
+	case TRIANGLE_WAVE:
+	{
+		const float f = fract(x * a + b);
+		const float wave = f <= 0.25f ? 4.0f * f : f <= 0.75f ? 2.0f - 4.0f * f : -4.0f + 4.0f * f;
+		return wave * c + d;
+	}
+	case SAW_TOOTH_WAVE: return (fract(x * a + b) * 2.0f - 1.0f) * c + d;
+	default: return (fract(x * a + b) <= 0.5f ? 1.0f : -1.0f) * c + d;
+	}
+}
+
+namespace
+{
+
+// Texture slots of the effects' outputs: for every effect material, NUM_MIPS mips appended after all
+// materials' textures, initially a copy of the effect's source (turbulence: the material's texture;
+// layered: the first layer's), flags the OR of what the layers carry (layered.rs:113-133).
+void add_effect_outputs(Scene& sc)
+{
+	for (size_t m = 0; m < sc.materials.size(); ++m)
+	{
+		Material& mat = sc.materials[m];
+		if (mat.effect == Material::NO_EFFECT) continue;
+		const uint32_t src = mat.effect == Material::TURB ? uint32_t(m) : mat.layers[0].material;
+		mat.effect_texture = int32_t(sc.texture_mips.size() / NUM_MIPS);
+		for (uint32_t mip = 0; mip < NUM_MIPS; ++mip)
+		{
+			SwTextureMip tm = sc.texture_mips[src * NUM_MIPS + mip];
+			const uint64_t n = uint64_t(tm.width) * tm.height;
+			const uint64_t from = tm.offset;
+			tm.offset = sc.texels.size();
+			sc.texels.insert(sc.texels.end(), sc.texels.begin() + from, sc.texels.begin() + from + n);
+			if (mat.effect == Material::LAYERED)
+			{
+				tm.flags = 0;
+				for (const EffectLayer& l : mat.layers) tm.flags |= sc.texture_mips[l.material * NUM_MIPS + mip].flags;
+			}
+			sc.texture_mips.push_back(tm);
+		}
+	}
+}
+
+} // namespace
+
+void add_texture_effects(const SceneConfig& cfg, uint32_t n_metal, uint32_t n_diel, Scene& sc)
+{
+	Rng erng(cfg.seed ^ 0xEFFEC7u);
+	const uint32_t nb = cfg.num_materials;
+	const uint32_t first = nb - cfg.layered_materials - cfg.turb_materials;
+	auto wave = [&](uint32_t kind, float amplitude, float offset) {
+		TimeFunction f;
+		f.kind = kind;
+		f.a = erng.uniform(0.2f, 1.5f);
+		f.b = erng.uniform(0.0f, 6.28f);
+		f.c = amplitude;
+		f.d = offset;
+		return f;
+	};
+	for (uint32_t m = first; m < nb; ++m)
+	{
+		sc.materials[m].emissive = -1;
+		if (m < nb - cfg.layered_materials)
+		{
+			Material& mat = sc.materials[m];
+			mat.effect = Material::TURB;
+			mat.turb_amplitude = erng.uniform(2.0f, 8.0f);
+			mat.turb_wave_length = erng.uniform(16.0f, 96.0f);
+			mat.turb_frequency = erng.uniform(0.2f, 1.5f);
+			continue;
+		}
+		// layer 0: the material's own texture scrolling along s; layers 1..3: additive (modulated by a sine),
+		// alpha-blended (alpha ripples) and alpha-tested (per-component modulation) materials of their own
+		std::vector<EffectLayer> layers(4);
+		layers[0].material = m;
+		layers[0].tex_coord_shift[0].kind = TimeFunction::LINEAR;
+		layers[0].tex_coord_shift[0].a = erng.uniform(-40.0f, 40.0f);
+		const uint32_t blends[3] = {SW_BLEND_ADDITIVE, SW_BLEND_ALPHA_BLEND, SW_BLEND_ALPHA_TEST};
+		for (int k = 1; k < 4; ++k)
+		{
+			const bool metal = m < n_metal;
+			const bool diel = !metal && m < n_metal + n_diel;
+			make_material_texture(erng, cfg.texture_size, cfg.normal_maps, metal ? 0.35f : diel ? 0.5f : 1.0f, metal, sc);
+			// alpha of the new texture's mips: a diagonal ripple over the whole 0..255 range
+			for (uint32_t mip = 0; mip < NUM_MIPS; ++mip)
+			{
+				const SwTextureMip& tm = sc.texture_mips[sc.texture_mips.size() - NUM_MIPS + mip];
+				for (uint32_t y = 0; y < tm.height; ++y)
+					for (uint32_t x = 0; x < tm.width; ++x)
+					{
+						uint64_t& t = sc.texels[tm.offset + uint64_t(y) * tm.width + x];
+						const uint64_t alpha = uint64_t(((x << mip) * 5 + (y << mip) * 3) & 255u);
+						t = (t & ~0xFF000000ull) | (alpha << 24);
+					}
+			}
+			Material lm;
+			lm.texture_size = cfg.texture_size;
+			lm.blending_mode = blends[k - 1];
+			sc.materials.push_back(lm);
+			EffectLayer& l = layers[k];
+			l.material = uint32_t(sc.materials.size() - 1);
+			l.tex_coord_shift[0] = wave(TimeFunction::SIN_WAVE, erng.uniform(4.0f, 24.0f), 0.0f);
+			l.tex_coord_shift[1].kind = TimeFunction::LINEAR;
+			l.tex_coord_shift[1].a = erng.uniform(-30.0f, 30.0f);
+			l.tex_coord_shift[1].b = erng.uniform(-64.0f, 64.0f);
+			if (k == 1)
+			{
+				l.has_modulate = true;
+				l.modulate = wave(TimeFunction::SIN_WAVE, 0.6f, 0.4f); // below 1/128 for part of the period
+			}
+			else if (k == 3)
+			{
+				l.has_modulate_color = true;
+				l.modulate_color[0] = wave(TimeFunction::TRIANGLE_WAVE, 0.5f, 1.0f);
+				l.modulate_color[1] = wave(TimeFunction::SAW_TOOTH_WAVE, 0.3f, 0.8f);
+				l.modulate_color[2] = wave(TimeFunction::STEP_WAVE, 0.02f, 1.0f); // stays within [0.98, 1.02]
+			}
+		}
+		Material& mat = sc.materials[m];
+		mat.effect = Material::LAYERED;
+		mat.layers = layers;
+	}
+	add_effect_outputs(sc);
+}
+
 bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 {
 	if (cfg.grid_x == 0 || cfg.grid_y == 0 || cfg.grid_x * cfg.grid_y > 4096)
@@ -1124,6 +1258,12 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 	if (cfg.tile_size < 16.0f || cfg.tile_size > 256.0f)
 	{
 		error = "tile_size must lie in [16, 256] (lightmaps stay within 17 texels)";
+		return false;
+	}
+	if (uint64_t(cfg.turb_materials) + cfg.layered_materials + std::max(cfg.animated_materials, cfg.scrolling_materials) >
+		cfg.num_materials)
+	{
+		error = "turb_materials + layered_materials + max(animated_materials, scrolling_materials) exceed num_materials";
 		return false;
 	}
 	if (cfg.texture_size < 16 || (cfg.texture_size & (cfg.texture_size - 1)) || cfg.num_materials == 0)
@@ -1221,6 +1361,13 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 			sc.materials[m].frame_duration = durations[0];
 		}
 	}
+
+	// Generative effects (their own generator: the rest of the scene is unchanged): the last
+	// layered_materials base materials are layered animations over their own texture and three layer
+	// materials (appended; no polygon uses them) with other blending modes; the turb_materials before
+	// them are turbulent. Effect materials get no emissive layer.
+	if (cfg.turb_materials || cfg.layered_materials)
+		add_texture_effects(cfg, n_metal, n_diel, sc);
 
 	sc.basis.resize(sc.polygons.size());
 	for (size_t p = 0; p < sc.polygons.size(); ++p)

@@ -54,6 +54,34 @@ struct MapPortal
 	uint32_t first_vertex, num_vertices;
 };
 
+// SingleArgumentFunction (src/common/material_function.rs:5-140): a function of time.
+struct TimeFunction
+{
+	enum Kind : uint32_t
+	{
+		CONSTANT = 0, // c
+		LINEAR,       // x * scale + offset
+		SIN_WAVE,     // amplitude * sin(2 pi (x * frequency) + phase) + offset
+		TRIANGLE_WAVE,
+		SAW_TOOTH_WAVE,
+		STEP_WAVE,
+	};
+	uint32_t kind = CONSTANT;
+	float a = 0.0f, b = 0.0f, c = 0.0f, d = 0.0f; // CONSTANT: a; LINEAR: scale a, offset b; waves: frequency a, phase b, amplitude c, offset d
+	float evaluate(float x) const;
+};
+
+// LayeredAnimationLayer (src/common/material.rs:208-235)
+struct EffectLayer
+{
+	uint32_t material = 0;
+	bool follow_framed_animation = false;
+	TimeFunction tex_coord_shift[2];
+	bool has_modulate = false, has_modulate_color = false;
+	TimeFunction modulate;
+	TimeFunction modulate_color[3];
+};
+
 // Material flags the renderer reads (src/common/material.rs): draw, light, diffuse layer, blending,
 // optional emissive layer.
 struct Material
@@ -70,6 +98,18 @@ struct Material
 	uint32_t texture_size = 0;            // mip-0 width = height
 	int32_t next_frame = -1;              // framed_animation.next_material_name as a material index, -1: none
 	float frame_duration = 0.5f;          // framed_animation.duration, seconds
+	// Generative effect (SpecialMaterialEffect::Turb / LayeredAnimation, material.rs:146-160): its output
+	// texture is the texture slot effect_texture (after the materials' own), rewritten every frame.
+	enum Effect : uint32_t
+	{
+		NO_EFFECT = 0,
+		TURB = 1,
+		LAYERED = 2,
+	};
+	uint32_t effect = NO_EFFECT;
+	int32_t effect_texture = -1;
+	float turb_amplitude = 0.0f, turb_wave_length = 1.0f, turb_frequency = 0.0f; // TurbParams
+	std::vector<EffectLayer> layers;                                              // LayeredAnimation
 };
 
 // One mip of a skybox side (SkyboxSideTexture, src/square_wheel/textures.rs:83-87): size x size texels
@@ -161,6 +201,8 @@ struct SceneConfig
 	uint32_t num_models = 0;          // per-vertex animated triangle models placed in the rooms
 	uint32_t model_triangles = 2000;  // triangles per model mesh (about)
 	uint32_t model_frames = 8;        // animation keyframes per mesh
+	uint32_t turb_materials = 0;      // the last base materials but layered_materials have a turbulence effect
+	uint32_t layered_materials = 0;   // the last this many base materials are layered animations
 };
 
 struct Scene
@@ -220,6 +262,9 @@ struct Scene
 };
 
 bool generate_scene(const SceneConfig& cfg, Scene& out, std::string& error);
+// The config's generative texture effects on the base materials (and their layer materials and output
+// texture slots); part of generate_scene.
+void add_texture_effects(const SceneConfig& cfg, uint32_t n_metal, uint32_t n_diel, Scene& sc);
 
 PolygonBasisVecs form_plane_and_tex_coord_equation(const Plane& plane, const Plane tc[2]);
 

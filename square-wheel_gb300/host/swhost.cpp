@@ -39,9 +39,17 @@ struct SwhRenderer
 
 namespace
 {
-// build_shadow_maps (partial_renderer.rs:525-592) for the frame, and its lights' shadow maps.
+// The frame's texture effect passes (update_animations, map_materials_processor.rs:249-303), then
+// build_shadow_maps (partial_renderer.rs:525-592) for the frame and its lights' shadow maps.
 int submit_shadows(SwhRenderer* r, const FramePrep& p)
 {
+	// the generative texture effects of the frame first: the surfaces read their output textures
+	if (!p.texture_passes.empty())
+	{
+		const int st = sw_update_textures(r->ctx, p.texture_passes.data(), uint32_t(p.texture_passes.size()),
+			p.texture_shifts.data(), uint32_t(p.texture_shifts.size()));
+		if (st) return st;
+	}
 	if (p.shadow_texels == 0)
 	{
 		if (!r->shadows_set) return SW_OK;
@@ -132,6 +140,8 @@ int scene_config_from(const SwhSceneConfig* c, SceneConfig& cfg)
 	cfg.num_models = c->num_models;
 	cfg.model_triangles = c->model_triangles ? c->model_triangles : 2000;
 	cfg.model_frames = c->model_frames ? c->model_frames : 8;
+	cfg.turb_materials = c->turb_materials;
+	cfg.layered_materials = c->layered_materials;
 	if (cfg.num_models > 100000 || cfg.model_triangles > 200000 || cfg.model_frames > 256)
 	{
 		g_error = "too many models, model triangles or frames";
@@ -279,6 +289,19 @@ int swh_scene_compressed_lightmaps(const SwhScene* s, const void** out_lightmaps
 	*out_count = sc.lightmaps_compressed.size() / SW_LIGHTMAP_COMPRESSED_BYTES;
 	*out_directional = sc.directional_lightmaps_compressed.data();
 	*out_directional_count = sc.directional_lightmaps_compressed.size() / SW_DIR_LIGHTMAP_COMPRESSED_BYTES;
+	return SW_OK;
+}
+
+int swh_scene_texture_effect(const SwhScene* s, uint32_t material, SwhTextureEffect* out)
+{
+	if (!s || !out || material >= s->scene.materials.size()) return SW_ERR_INVALID_ARGUMENT;
+	const Material& m = s->scene.materials[material];
+	out->kind = m.effect;
+	out->output_texture = m.effect_texture;
+	out->num_layers = uint32_t(m.layers.size());
+	out->turb[0] = m.turb_amplitude;
+	out->turb[1] = m.turb_wave_length;
+	out->turb[2] = m.turb_frequency;
 	return SW_OK;
 }
 
@@ -451,6 +474,10 @@ int swh_frame_outputs(const SwhFrame* f, SwhFrameOutputs* out)
 	out->tri_vertices = p.tri_vertices.data();
 	out->num_tri_vertices = uint32_t(p.tri_vertices.size());
 	out->model_triangles = p.stats.model_triangles;
+	out->texture_passes = p.texture_passes.data();
+	out->num_texture_passes = uint32_t(p.texture_passes.size());
+	out->texture_shifts = p.texture_shifts.data();
+	out->num_texture_shifts = uint32_t(p.texture_shifts.size());
 	return SW_OK;
 }
 

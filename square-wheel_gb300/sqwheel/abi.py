@@ -51,6 +51,9 @@ SURFACE_DESC = np.dtype([
     ("lightmap_tc_shift", "<u4", 2), ("flags", "<u4"), ("num_lights", "<u4"), ("lights", "<u2", 6),
     ("emissive_light", "<f4", 3), ("out_offset", "<u8")], align=True)
 VERTEX16 = np.dtype([("x", "<i4"), ("y", "<i4")], align=True)
+TEXTURE_PASS = np.dtype([("kind", "<u4"), ("dst_mip", "<u4"), ("src_mip", "<u4"), ("blending_mode", "<u4"),
+                         ("shift", "<i4", 2), ("light", "<f4", 3), ("shifts_offset", "<u4")], align=True)
+SW_TEXPASS_TURB, SW_TEXPASS_LAYER, SW_TEXPASS_EMISSIVE = 1, 2, 0x100
 TRI_VERTEX = np.dtype([("x", "<i4"), ("y", "<i4"), ("tc", "<i4", 2), ("light", "<i4", 3), ("reserved", "<i4")], align=True)
 DRAW_CMD = np.dtype([
     ("first_vertex", "<u4"), ("vertex_count", "<u4"), ("mode", "<u4"), ("blend", "<u4"), ("depth_eq", "<f4", 3),
@@ -167,6 +170,7 @@ LAYOUT_ORDER = [
     ("SwLightShadow", LIGHT_SHADOW.itemsize), ("SwDepthDraw", DEPTH_DRAW.itemsize),
     ("SwShadowSide", SHADOW_SIDE.itemsize), ("SwShadowLeaf", SHADOW_LEAF.itemsize),
     ("SwMaterialFrame", MATERIAL_FRAME.itemsize), ("SwTriVertex", TRI_VERTEX.itemsize),
+    ("SwTexturePass", TEXTURE_PASS.itemsize),
 ]
 
 

@@ -21,6 +21,7 @@ LIB_PATH = os.path.join(PKG_DIR, "lib", "libswgpu.so")
 EXPORTED = [
     "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_rebuild_surfaces_per_surface", "sw_set_surfaces", "sw_set_skybox", "sw_register_host_buffer", "sw_unregister_host_buffer",
     "sw_submit_draws", "sw_submit_draws_ex", "sw_set_lite_textures", "sw_set_lightmaps_compressed", "sw_read_lightmaps",
+    "sw_update_textures", "sw_read_texels",
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_read_framebuffer", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
     "sw_postprocess_noalloc", "sw_set_learned_upscaler", "sw_draw_frame", "sw_set_frame_graph", "sw_set_frames_in_flight", "sw_set_tuning",
@@ -66,6 +67,8 @@ def load_library(path=LIB_PATH):
         "sw_submit_draws_ex": ([vp, vp, u32, vp, u32, vp, u32], i32),
         "sw_set_lite_textures": ([vp, vp, u64], i32),
         "sw_set_lightmaps_compressed": ([vp, vp, u64, vp, u64], i32),
+        "sw_update_textures": ([vp, vp, u32, vp, u32], i32),
+        "sw_read_texels": ([vp, vp, u64, vp, u64], i32),
         "sw_read_lightmaps": ([vp, vp, u64, vp, u64], i32),
         "sw_render": ([vp, vp, u32, i32], i32),
         "sw_postprocess": ([vp, vp, f32, vp, vp, u32, i32], i32),
@@ -274,6 +277,20 @@ class GpuRenderer:
         d = np.ascontiguousarray(directional, dtype=np.uint8).reshape(-1, 13)
         self._check(self.lib.sw_set_lightmaps_compressed(self.ctx, abi.ptr(a), a.shape[0], abi.ptr(d), d.shape[0]),
                     "sw_set_lightmaps_compressed")
+
+    def update_textures(self, passes, shifts):
+        """Run generative texture effect passes (abi.TEXTURE_PASS) with their turbulence shifts (int32)."""
+        passes = np.ascontiguousarray(passes, dtype=abi.TEXTURE_PASS)
+        shifts = np.ascontiguousarray(shifts if shifts is not None else np.zeros(0, np.int32), dtype=np.int32)
+        self._check(self.lib.sw_update_textures(self.ctx, abi.ptr(passes), passes.size, abi.ptr(shifts), shifts.size),
+                    "sw_update_textures")
+
+    def read_texels(self, num_texels, num_emissive=0):
+        """The context's material texels (uint64) and emissive pixels (uint32), e.g. after texture passes."""
+        out = np.empty(int(num_texels), np.uint64)
+        em = np.empty(int(num_emissive), np.uint32)
+        self._check(self.lib.sw_read_texels(self.ctx, abi.ptr(out), out.size, abi.ptr(em), em.size), "sw_read_texels")
+        return out, em
 
     def read_lightmaps(self, num_elements, num_directional):
         """The decoded lightmaps: (float32 (n, 3), DIR_LIGHTMAP_ELEMENT (m,))."""

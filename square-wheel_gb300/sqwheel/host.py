@@ -25,7 +25,7 @@ class SceneConfig(ctypes.Structure):
         ("skybox_missing_side", ctypes.c_int32), ("sky_rotation_speed", ctypes.c_float),
         ("camera_pitch", ctypes.c_float), ("shadowed_lights", ctypes.c_uint32), ("scrolling_materials", ctypes.c_uint32),
         ("animated_materials", ctypes.c_uint32), ("projector_lights", ctypes.c_uint32), ("num_models", ctypes.c_uint32), ("model_triangles", ctypes.c_uint32),
-        ("model_frames", ctypes.c_uint32),
+        ("model_frames", ctypes.c_uint32), ("turb_materials", ctypes.c_uint32), ("layered_materials", ctypes.c_uint32),
     ]
 
 
@@ -35,6 +35,11 @@ class SceneInfo(ctypes.Structure):
                 ("dynamic_lights", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
                 ("lightmap_elements", ctypes.c_uint64), ("texels", ctypes.c_uint64),
                 ("skybox_texels", ctypes.c_uint64)]
+
+
+class TextureEffectInfo(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("output_texture", ctypes.c_int32), ("num_layers", ctypes.c_uint32),
+                ("turb", ctypes.c_float * 3)]
 
 
 class FrameOptions(ctypes.Structure):
@@ -54,7 +59,9 @@ class FrameOutputs(ctypes.Structure):
                 ("shadow_sides", ctypes.c_void_p), ("num_shadow_sides", ctypes.c_uint32),
                 ("num_shadow_leafs", ctypes.c_uint32), ("shadow_leafs", ctypes.c_void_p),
                 ("tri_vertices", ctypes.c_void_p), ("num_tri_vertices", ctypes.c_uint32),
-                ("model_triangles", ctypes.c_uint32)]
+                ("model_triangles", ctypes.c_uint32), ("texture_passes", ctypes.c_void_p),
+                ("num_texture_passes", ctypes.c_uint32), ("num_texture_shifts", ctypes.c_uint32),
+                ("texture_shifts", ctypes.c_void_p)]
 
 
 def load_host_library():
@@ -85,6 +92,7 @@ def load_host_library():
         "swh_scene_load_map": ([ctypes.c_char_p, vp, ctypes.POINTER(vp)], i32),
         "swh_scene_load_map_memory": ([vp, ctypes.c_uint64, vp, ctypes.POINTER(vp)], i32),
         "swh_scene_save_map": ([vp, ctypes.c_char_p], i32),
+        "swh_scene_texture_effect": ([vp, u32, vp], i32),
         "swh_scene_compressed_lightmaps": ([vp, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(vp),
                                             ctypes.POINTER(ctypes.c_uint64)], i32),
     }
@@ -103,7 +111,7 @@ HOST_EXPORTED = ["swh_scene_create", "swh_scene_destroy", "swh_scene_info", "swh
                  "swh_renderer_render_frame", "swh_frame_prepare_view", "swh_frame_view_input",
                  "swh_renderer_set_gpu_prep", "swh_frame_map", "swh_renderer_set_frames_in_flight",
                  "swh_scene_lite_textures", "swh_scene_load_map", "swh_scene_load_map_memory", "swh_scene_save_map",
-                 "swh_scene_compressed_lightmaps"]
+                 "swh_scene_compressed_lightmaps", "swh_scene_texture_effect"]
 
 # The two map configurations of the benchmark plan.
 SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, num_materials=16, metal_frac=0.0,
@@ -155,6 +163,13 @@ class Scene:
     @classmethod
     def load_map(cls, path_or_bytes, **kw):
         return cls(_map=path_or_bytes, **kw)
+
+    def texture_effect(self, material):
+        """(kind, output_texture, num_layers, (amplitude, wave_length, frequency)) of a material's generative
+        texture effect (kind 0 none, 1 turbulence, 2 layered)."""
+        e = TextureEffectInfo()
+        _check(self.lib, self.lib.swh_scene_texture_effect(self.handle, material, ctypes.byref(e)), "swh_scene_texture_effect")
+        return int(e.kind), int(e.output_texture), int(e.num_layers), tuple(e.turb)
 
     def save_map(self, path):
         _check(self.lib, self.lib.swh_scene_save_map(self.handle, os.fsencode(path)), "swh_scene_save_map")
@@ -282,6 +297,8 @@ class Frame:
         self.vertices = arr(o.vertices, o.num_vertices, abi.VERTEX16)
         self.tri_vertices = arr(o.tri_vertices, o.num_tri_vertices, abi.TRI_VERTEX)
         self.model_triangles = int(o.model_triangles)
+        self.texture_passes = arr(o.texture_passes, o.num_texture_passes, abi.TEXTURE_PASS)
+        self.texture_shifts = arr(o.texture_shifts, o.num_texture_shifts, np.int32)
         self.lights = arr(o.lights, o.num_lights, abi.LIGHT)
         self.total_texels = int(o.total_texels)
         self.params = abi.FrameParams()
