@@ -143,8 +143,8 @@ STAGE_TRAFFIC = {
 
 
 # Kernels one frame launches (either preparation split on the host side): surface build, raster setup,
-# raster tiles, blur + tonemap, exposure average.
-FRAME_LAUNCHES = 5
+# raster tiles, bloom blur, tonemap, exposure average.
+FRAME_LAUNCHES = 6
 
 
 def raster_bytes(pixel_writes, w, h):
@@ -494,7 +494,7 @@ def run_frame_gpu(args, world, rank, local):
                      "frac_of_measured_hbm": round(gbs / peak, 4)}
     dom = max(totals, key=totals.get)
     kernel_names = {"surf": "surf_build_kernel", "raster": "raster_tiles_kernel (bloom downscale in its epilogue)",
-                    "post": "pp_blur_tonemap_kernel (+ pp_average_bloom_kernel beside it)"}
+                    "post": "pp_blur_kernel + pp_tonemap_bloom_kernel (+ pp_average_bloom_kernel beside it)"}
     out_line = None
     if rank == 0:
         cpu, parity = cpu_frame_baseline(work, gpu_ldr=gpu_ldr)

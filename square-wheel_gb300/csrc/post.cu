@@ -5,10 +5,10 @@
 // Gaussian blur (:846-956), Reinhard tonemapping with nearest or linear bloom (:226-726, :997-1024);
 // and FrameUpscaler::perform_upscale (src/square_wheel/frame_upscaler.rs:42-239).
 //
-// With bloom the frame takes at most two streaming launches: the downscale (one block per bloom line;
-// in a whole-frame graph the raster tile pass does it instead) and blur + tonemap (one block per output
-// tile, the bloom cells it samples blurred in both directions in shared memory), plus the exposure
-// average on the side.
+// With bloom the frame takes at most three launches: the downscale (one block per bloom line; in a
+// whole-frame graph the raster tile pass does it instead), the blur of the downscaled cells (once per
+// cell, both directions in shared memory) and the tonemap, a streaming pass over the HDR frame that
+// samples the blurred cells from L2, plus the exposure average on the side.
 // Integer sums use wrapping 32-bit adds, which are associative, so the per-line sums can be reduced in
 // any order and remain bit-exact; the single float reduction over lines (sum of line sums, in line
 // order) runs in one thread exactly as the reference's sequential loop does.
@@ -91,14 +91,6 @@ __global__ void __launch_bounds__(256) pp_average_bloom_kernel(PostArgs a)
 	ordered_line_sum(a.bh, [&](uint32_t i) { return float(sums[i]); }, __fdiv_rn(1.0f, float(a.bw * a.bh)), a.average);
 }
 
-// Bloom cells of a tile held in shared memory: cell (x, y) of the bloom buffer at [y - y0][x - x0].
-struct BloomTile
-{
-	const uint64_t* cells;
-	uint32_t x0, y0, pitch;
-	__device__ CV at(uint32_t x, uint32_t y) const { return cv_from_c64(cells[(y - y0) * pitch + (x - x0)]); }
-};
-
 // HDR pixel (x, y) plus its bloom sample, nearest (postprocessor.rs:346-462) or linear (:464-726).
 template <int S, bool LINEAR, class Bloom>
 __device__ __forceinline__ CV bloom_sum(const PostArgs& a, const Bloom& bl, uint32_t x, uint32_t y, CV c)
@@ -147,8 +139,9 @@ __device__ __forceinline__ CV bloom_sum(const PostArgs& a, const Bloom& bl, uint
 // ---- bloom passes: downscale, then blur + tonemap ----
 //
 // In a whole-frame graph the raster tile pass writes the downscaled bloom buffer and the exact per-line
-// sums itself (its epilogue box-averages the tile's final pixels), so the frame's postprocess is one
-// launch over the HDR frame: pp_blur_tonemap_kernel. A frame that did not come from the tile pass
+// sums itself (its epilogue box-averages the tile's final pixels), so the frame's postprocess is the
+// blur of the bloom cells and one pass over the HDR frame (pp_blur_kernel, pp_tonemap_bloom_kernel).
+// A frame that did not come from the tile pass
 // (sw_set_framebuffer, the allocation-free entry point, per-call sw_render + sw_postprocess) gets
 // pp_downscale_kernel first.
 //
@@ -241,47 +234,29 @@ __global__ void __launch_bounds__(256) pp_downscale_kernel(PostArgs a)
 	pdl_trigger();
 }
 
-// pp_blur_tonemap_kernel: one block per TM_W x TM_H tile of the output. It stages the downscaled bloom
-// cells its tile needs (the cells its pixels sample, +-radius cells in both directions, source indices
-// clamped to the buffer as the reference's blur clamps them) in shared memory, runs the horizontal
-// (postprocessor.rs:862-900) and the vertical blur pass (:902-955, bloom_scale folded into the weights)
-// for those cells, then tonemaps its pixels with the nearest or linear bloom sample (:346-726) read from
-// shared memory. With radius 0 the downscaled cells are sampled directly (no blur pass).
-constexpr uint32_t TM_W = 256, TM_H = 16;
+// pp_blur_kernel: the separable blur of the downscaled bloom buffer, once per cell (perform_blur_impl,
+// postprocessor.rs:846-956): one block per BL_W x BL_H tile of cells stages its cells with a radius halo
+// on every side (source indices clamped to the buffer as the reference's blur clamps them), runs the
+// horizontal pass over every staged line and the vertical pass (bloom_scale folded into its weights)
+// over the tile, and writes the blurred cells to bloom1.
+constexpr uint32_t BL_W = 64, BL_H = 16;
 
-template <int S>
-__host__ __device__ __forceinline__ void bloom_tile_range(uint32_t p0, uint32_t n, uint32_t cells, uint32_t& lo, uint32_t& hi)
+__host__ __device__ __forceinline__ uint32_t blur_tile_smem(uint32_t radius)
 {
-	constexpr uint32_t half = S / 2;
-	lo = min(p0 >= half ? (p0 - half) / S : 0u, cells - 1);
-	hi = min((p0 + n - 1) / S + 1, cells - 1);
+	const uint32_t lines = BL_H + 2 * radius, cols = BL_W + 2 * radius;
+	return (lines * cols + lines * BL_W) * 8u;
 }
 
-template <int S>
-__host__ __device__ __forceinline__ uint32_t tonemap_tile_smem(uint32_t radius)
-{
-	// at most (TM_W / S + 3) columns x (TM_H / S + 3) lines of cells: the staged cells with a radius
-	// halo on every side, the horizontally blurred lines (halo lines only) and the blurred cells
-	const uint32_t cols = TM_W / S + 3, lines = TM_H / S + 3, r2 = 2 * radius;
-	return ((lines + r2) * (cols + r2) + (lines + r2) * cols + lines * cols) * 8u;
-}
-
-template <int S, bool LINEAR>
-__global__ void __launch_bounds__(256) pp_blur_tonemap_kernel(PostArgs a)
+__global__ void __launch_bounds__(256) pp_blur_kernel(PostArgs a)
 {
 	extern __shared__ __align__(16) uint64_t s_tile[];
-	const uint32_t x0 = blockIdx.x * TM_W, y0 = blockIdx.y * TM_H;
+	const uint32_t cx0 = blockIdx.x * BL_W, cy0 = blockIdx.y * BL_H;
 	pdl_wait(); // the downscale (the raster tile pass or pp_downscale_kernel) has completed
-	const uint32_t tw = min(TM_W, a.width - x0), th = min(TM_H, a.height - y0);
-	uint32_t cx0, cx1, cy0, cy1;
-	bloom_tile_range<S>(x0, tw, a.bw, cx0, cx1);
-	bloom_tile_range<S>(y0, th, a.bh, cy0, cy1);
-	const uint32_t cols = cx1 - cx0 + 1, lines = cy1 - cy0 + 1;
 	const int32_t r = int32_t(a.radius);
+	const uint32_t cols = min(BL_W, a.bw - cx0), lines = min(BL_H, a.bh - cy0);
 	const uint32_t slines = lines + 2 * uint32_t(r), scols = cols + 2 * uint32_t(r);
-	uint64_t* s_b = s_tile;                              // slines x scols downscaled cells
-	uint64_t* s_h = s_b + slines * scols;                // slines x cols, horizontally blurred
-	uint64_t* s_v = r ? s_h + slines * cols : s_b;       // lines x cols, the cells the pixels sample
+	uint64_t* s_b = s_tile;               // slines x scols downscaled cells
+	uint64_t* s_h = s_b + slines * scols; // slines x cols, horizontally blurred
 	{
 		// four loads in flight per thread; staged cell (l, c) is cell (clamp(cy0 - r + l), clamp(cx0 - r + c))
 		const uint32_t total = slines * scols;
@@ -307,99 +282,91 @@ __global__ void __launch_bounds__(256) pp_blur_tonemap_kernel(PostArgs a)
 		}
 	}
 	__syncthreads();
-	if (r)
+	// horizontal pass over every staged line: cell c of the tile sits at staged column c + r
+	for (uint32_t i = threadIdx.x; i < slines * cols; i += blockDim.x)
 	{
-		// horizontal pass over every staged line: cell c of the tile sits at staged column c + r
-		for (uint32_t i = threadIdx.x; i < slines * cols; i += blockDim.x)
+		const uint32_t l = i / cols, c = i % cols;
+		const uint64_t* line = s_b + l * scols + c + uint32_t(r);
+		const CI cc = ci_from_c64(line[0]);
+		int32_t sum[4];
+#pragma unroll
+		for (int k = 0; k < 4; ++k) sum[k] = wmul(cc.v[k], a.kernel_h[r]);
+		for (int32_t dx = 1; dx <= r; ++dx)
 		{
-			const uint32_t l = i / cols, c = i % cols;
-			const uint64_t* line = s_b + l * scols + c + uint32_t(r);
-			const CI cc = ci_from_c64(line[0]);
-			int32_t sum[4];
+			const CI c0 = ci_from_c64(line[-dx]);
+			const CI c1 = ci_from_c64(line[dx]);
 #pragma unroll
-			for (int k = 0; k < 4; ++k) sum[k] = wmul(cc.v[k], a.kernel_h[r]);
-			for (int32_t dx = 1; dx <= r; ++dx)
-			{
-				const CI c0 = ci_from_c64(line[-dx]);
-				const CI c1 = ci_from_c64(line[dx]);
-#pragma unroll
-				for (int k = 0; k < 4; ++k) sum[k] = wadd(sum[k], wmul(wadd(c0.v[k], c1.v[k]), a.kernel_h[dx + r]));
-			}
-			s_h[i] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
+			for (int k = 0; k < 4; ++k) sum[k] = wadd(sum[k], wmul(wadd(c0.v[k], c1.v[k]), a.kernel_h[dx + r]));
 		}
-		__syncthreads();
-		// vertical pass: line cy0 + l is staged at l + r
-		for (uint32_t i = threadIdx.x; i < lines * cols; i += blockDim.x)
-		{
-			const uint32_t l = i / cols, c = i % cols;
-			const CI cc = ci_from_c64(s_h[(l + r) * cols + c]);
-			int32_t sum[4];
-#pragma unroll
-			for (int k = 0; k < 4; ++k) sum[k] = wmul(cc.v[k], a.kernel_v[r]);
-			for (int32_t dy = 1; dy <= r; ++dy)
-			{
-				const CI c0 = ci_from_c64(s_h[(l + r - dy) * cols + c]);
-				const CI c1 = ci_from_c64(s_h[(l + r + dy) * cols + c]);
-#pragma unroll
-				for (int k = 0; k < 4; ++k) sum[k] = wadd(sum[k], wmul(wadd(c0.v[k], c1.v[k]), a.kernel_v[dy + r]));
-			}
-			s_v[i] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
-		}
-		__syncthreads();
+		s_h[i] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
 	}
-	const BloomTile tile{s_v, cx0, cy0, cols};
-	// 4 horizontally adjacent pixels per thread: 64 threads per 256-pixel line, lines ly, ly + 4, ... of
-	// the tile (TM_H / 4 of them), their HDR loads all issued first
-	const uint32_t lx = 4 * (threadIdx.x & 63), ly0 = threadIdx.x >> 6;
+	__syncthreads();
+	// vertical pass: line cy0 + l is staged at l + r
+	for (uint32_t i = threadIdx.x; i < lines * cols; i += blockDim.x)
+	{
+		const uint32_t l = i / cols, c = i % cols;
+		const CI cc = ci_from_c64(s_h[(l + r) * cols + c]);
+		int32_t sum[4];
+#pragma unroll
+		for (int k = 0; k < 4; ++k) sum[k] = wmul(cc.v[k], a.kernel_v[r]);
+		for (int32_t dy = 1; dy <= r; ++dy)
+		{
+			const CI c0 = ci_from_c64(s_h[(l + r - dy) * cols + c]);
+			const CI c1 = ci_from_c64(s_h[(l + r + dy) * cols + c]);
+#pragma unroll
+			for (int k = 0; k < 4; ++k) sum[k] = wadd(sum[k], wmul(wadd(c0.v[k], c1.v[k]), a.kernel_v[dy + r]));
+		}
+		a.bloom1[uint64_t(cy0 + l) * a.bw + cx0 + c] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
+	}
+	pdl_trigger();
+}
+
+// Bloom cells read straight from the (blurred) bloom buffer in global memory (L2-resident).
+struct BloomGlobal
+{
+	const unsigned long long* cells;
+	uint32_t pitch;
+	__device__ CV at(uint32_t x, uint32_t y) const { return cv_from_c64(__ldg(cells + uint64_t(y) * pitch + x)); }
+};
+
+// pp_tonemap_bloom_kernel: the HDR frame tonemapped with its nearest or linear bloom sample
+// (postprocessor.rs:346-726, :997-1024), 4 horizontally adjacent pixels per thread over the flat pixel
+// space (one 32-byte HDR load pair and one 16-byte store when the row width is a multiple of 4).
+template <int S, bool LINEAR>
+__global__ void __launch_bounds__(256) pp_tonemap_bloom_kernel(PostArgs a, const uint64_t* bloom)
+{
+	const uint64_t first = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) * 4;
+	pdl_wait(); // the blur (or the downscale) has completed
+	const uint64_t total = uint64_t(a.width) * a.height;
+	if (first >= total) return;
+	const BloomGlobal bl{reinterpret_cast<const unsigned long long*>(bloom), a.bw};
 	const float4 isc = tonemap_scale(a);
-	if (lx >= tw) return;
-	const uint32_t n = min(4u, tw - lx);
 	const unsigned long long* hdr = reinterpret_cast<const unsigned long long*>(a.hdr);
-	unsigned long long p[TM_H / 4][4];
-#pragma unroll
-	for (int j = 0; j < int(TM_H / 4); ++j)
+	const bool vec = (a.width & 3) == 0 && (reinterpret_cast<uintptr_t>(a.hdr) & 15) == 0;
+	if (vec)
 	{
-		const uint32_t ly = ly0 + 4 * j;
-#pragma unroll
-		for (int k = 0; k < 4; ++k) p[j][k] = 0;
-		if (ly >= th) continue;
-		const uint64_t src = uint64_t(y0 + ly) * a.width + x0 + lx;
-		const unsigned long long* h = hdr + src;
-		if (n == 4 && (src & 1) == 0 && (reinterpret_cast<uintptr_t>(a.hdr) & 15) == 0)
-		{
-			const ulonglong2 v0 = __ldg(reinterpret_cast<const ulonglong2*>(h));
-			const ulonglong2 v1 = __ldg(reinterpret_cast<const ulonglong2*>(h + 2));
-			p[j][0] = v0.x;
-			p[j][1] = v0.y;
-			p[j][2] = v1.x;
-			p[j][3] = v1.y;
-		}
-		else
-		{
-#pragma unroll
-			for (int k = 0; k < 4; ++k)
-				if (k < int(n)) p[j][k] = __ldg(h + k);
-		}
-	}
-#pragma unroll
-	for (int j = 0; j < int(TM_H / 4); ++j)
-	{
-		const uint32_t ly = ly0 + 4 * j;
-		if (ly >= th) break;
-		const uint32_t x = x0 + lx, y = y0 + ly;
-		const uint64_t dst = uint64_t(y) * a.dst_pitch + x;
+		// the 4 pixels share a row: x = first % width ... + 3
+		const uint32_t y = uint32_t(first / a.width), x = uint32_t(first % a.width);
+		const ulonglong2 v0 = __ldg(reinterpret_cast<const ulonglong2*>(hdr + first));
+		const ulonglong2 v1 = __ldg(reinterpret_cast<const ulonglong2*>(hdr + first + 2));
+		const unsigned long long p[4] = {v0.x, v0.y, v1.x, v1.y};
 		uint32_t o[4];
 #pragma unroll
-		for (int k = 0; k < 4; ++k)
-			o[k] = k < int(n) ? cv_to_c32(tonemap(bloom_sum<S, LINEAR>(a, tile, x + k, y, cv_from_c64(p[j][k])), a, isc)) : 0u;
-		if (n == 4 && (dst & 3) == 0 && (reinterpret_cast<uintptr_t>(a.dst) & 15) == 0)
+		for (int k = 0; k < 4; ++k) o[k] = cv_to_c32(tonemap(bloom_sum<S, LINEAR>(a, bl, x + k, y, cv_from_c64(p[k])), a, isc));
+		const uint64_t dst = uint64_t(y) * a.dst_pitch + x;
+		if ((dst & 3) == 0 && (reinterpret_cast<uintptr_t>(a.dst) & 15) == 0)
 			*reinterpret_cast<uint4*>(a.dst + dst) = make_uint4(o[0], o[1], o[2], o[3]);
 		else
 		{
 #pragma unroll
-			for (int k = 0; k < 4; ++k)
-				if (k < int(n)) a.dst[dst + k] = o[k];
+			for (int k = 0; k < 4; ++k) a.dst[dst + k] = o[k];
 		}
+		return;
+	}
+	for (uint64_t i = first; i < first + 4 && i < total; ++i)
+	{
+		const uint32_t y = uint32_t(i / a.width), x = uint32_t(i % a.width);
+		a.dst[uint64_t(y) * a.dst_pitch + x] = cv_to_c32(tonemap(bloom_sum<S, LINEAR>(a, bl, x, y, cv_from_c64(__ldg(hdr + i))), a, isc));
 	}
 }
 
@@ -516,15 +483,19 @@ template <int S>
 int launch_bloom_pass(const PostArgs& a, cudaStream_t stream, bool downscale)
 {
 	if (downscale) return int(launch_dependent(pp_downscale_kernel<S>, dim3(a.bh), dim3(256), 0, stream, a));
-	const uint32_t smem = tonemap_tile_smem<S>(a.radius);
-	const dim3 grid((a.width + TM_W - 1) / TM_W, (a.height + TM_H - 1) / TM_H);
-	if (a.linear_filter)
+	// the blur (radius 0: the downscaled cells are sampled directly), then the tonemap
+	const uint64_t* bloom = a.bloom0;
+	if (a.radius)
 	{
-		if (int e = allow_smem(pp_blur_tonemap_kernel<S, true>, smem)) return e;
-		return int(launch_dependent(pp_blur_tonemap_kernel<S, true>, grid, dim3(256), smem, stream, a));
+		const uint32_t smem = blur_tile_smem(a.radius);
+		if (int e = allow_smem(pp_blur_kernel, smem)) return e;
+		const dim3 grid((a.bw + BL_W - 1) / BL_W, (a.bh + BL_H - 1) / BL_H);
+		if (int e = int(launch_dependent(pp_blur_kernel, grid, dim3(256), smem, stream, a))) return e;
+		bloom = a.bloom1;
 	}
-	if (int e = allow_smem(pp_blur_tonemap_kernel<S, false>, smem)) return e;
-	return int(launch_dependent(pp_blur_tonemap_kernel<S, false>, grid, dim3(256), smem, stream, a));
+	const dim3 grid(unsigned((uint64_t(a.width) * a.height + 1023) / 1024));
+	if (a.linear_filter) return int(launch_dependent(pp_tonemap_bloom_kernel<S, true>, grid, dim3(256), 0, stream, a, bloom));
+	return int(launch_dependent(pp_tonemap_bloom_kernel<S, false>, grid, dim3(256), 0, stream, a, bloom));
 }
 
 int launch_bloom(const PostArgs& a, cudaStream_t stream, bool downscale)

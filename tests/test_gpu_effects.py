@@ -83,7 +83,7 @@ def test_malformed_passes_refused(gpu_ok):
         p["dst_mip"], p["src_mip"], p["light"] = [0, 10], [5, 0], 1.0  # pass 2 reads pass 1's destination
         cases = [(p, "reads a mip that another pass writes")]
         q = p.copy()
-        q["dst_mip"], q["src_mip"] = [0, 0], [5, 6]
+        q["dst_mip"], q["src_mip"] = [0, 0], [5, 10]  # two groups (a layer, a turbulence) writing mip 0
         q["kind"] = [abi.SW_TEXPASS_LAYER, abi.SW_TEXPASS_TURB]
         cases.append((q, "same mip"))
         q = p[:1].copy()
