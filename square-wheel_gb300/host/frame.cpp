@@ -572,7 +572,9 @@ void FramePrep::draw_leaf(const ClippingPolygon& bounds, uint32_t leaf_index)
 		if (poly[pi].visible_frame != current_frame) continue;
 		draw_polygon(planes, pi);
 	}
-	if (leaf_index < sc.leaf_models.size() && !sc.leaf_models[leaf_index].empty()) draw_leaf_models(bounds, leaf_index);
+	const bool models = leaf_index < sc.leaf_models.size() && !sc.leaf_models[leaf_index].empty();
+	const bool sprites = leaf_index < sc.leaf_sprites.size() && !sc.leaf_sprites[leaf_index].empty();
+	if (models || sprites) draw_leaf_models(bounds, leaf_index);
 }
 
 namespace
@@ -624,19 +626,223 @@ void normals_matrix(const Mat4& m, float out[3][3])
 int32_t to_fixed16(float x) { return as_i32(x * 65536.0f); }
 } // namespace
 
+// clip_3d_model_polygon_by_plane with the near plane z >= Z_NEAR (src/common/clipping.rs:259-310)
+uint32_t FramePrep::clip_model_near(const ModelVertex3d* src, uint32_t n, ModelVertex3d* dst)
+{
+	uint32_t out = 0;
+	const ModelVertex3d* prev = &src[n - 1];
+	float prev_d = prev->pos.z;
+	auto inter = [&](const ModelVertex3d& v0, const ModelVertex3d& v1) {
+		const float d0 = v0.pos.z - PREP_Z_NEAR, d1 = v1.pos.z - PREP_Z_NEAR;
+		const float sum = d1 - d0, k0 = d0 / sum, k1 = d1 / sum;
+		ModelVertex3d r;
+		r.pos = v0.pos * k1 - v1.pos * k0;
+		for (int i = 0; i < 2; ++i) r.tc[i] = v0.tc[i] * k1 - v1.tc[i] * k0;
+		for (int i = 0; i < 3; ++i) r.light[i] = v0.light[i] * k1 - v1.light[i] * k0;
+		return r;
+	};
+	for (uint32_t i = 0; i < n && out < MAX_VERTICES; ++i)
+	{
+		const ModelVertex3d& v = src[i];
+		const float d = v.pos.z;
+		if (d > PREP_Z_NEAR)
+		{
+			if (prev_d < PREP_Z_NEAR && out < MAX_VERTICES) dst[out++] = inter(*prev, v);
+			if (out < MAX_VERTICES) dst[out++] = v;
+		}
+		else if (d == PREP_Z_NEAR)
+			dst[out++] = v;
+		else if (prev_d > PREP_Z_NEAR)
+			dst[out++] = inter(*prev, v);
+		prev = &v;
+		prev_d = d;
+	}
+	return out;
+}
+
 void FramePrep::draw_leaf_models(const ClippingPolygon& bounds, uint32_t leaf_index)
 {
-	// The leaf's models back to front: farther first by camera-space depth of the model's origin (the
-	// reference's LeafObjectsSorter, draw_ordering.rs, orders objects of a leaf; models here never
-	// overlap one another's leafs).
-	std::vector<std::pair<float, uint32_t>> order;
-	for (uint32_t m : sc.leaf_models[leaf_index])
+	// The leaf's models and sprites back to front: farther first by camera-space depth of the object's
+	// origin, models before sprites at equal depth (the reference's LeafObjectsSorter, draw_ordering.rs,
+	// orders the objects of a leaf by their projected boxes; objects here never leave their leaf).
+	struct Obj
 	{
-		const Vec3 p = view_transform(cam.view_matrix, sc.models[m].position);
-		order.push_back({p.z, m});
+		float z;
+		uint32_t kind, index; // kind 0 model, 1 sprite
+	};
+	std::vector<Obj> order;
+	if (leaf_index < sc.leaf_models.size())
+		for (uint32_t m : sc.leaf_models[leaf_index]) order.push_back({view_transform(cam.view_matrix, sc.models[m].position).z, 0u, m});
+	if (leaf_index < sc.leaf_sprites.size())
+		for (uint32_t k : sc.leaf_sprites[leaf_index])
+			order.push_back({view_transform(cam.view_matrix, sc.sprites[k].position).z, 1u, k});
+	std::stable_sort(order.begin(), order.end(), [](const Obj& a, const Obj& b) { return a.z > b.z; });
+	for (const Obj& o : order)
+	{
+		if (o.kind == 0)
+			draw_model(bounds, o.index);
+		else
+			draw_sprite(bounds, o.index);
 	}
-	std::stable_sort(order.begin(), order.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
-	for (const auto& o : order) draw_model(bounds, o.second);
+}
+
+void FramePrep::draw_sprite(const ClippingPolygon& bounds, uint32_t sprite_index)
+{
+	const SpriteEntity& sprite = sc.sprites[sprite_index];
+	// prepare_sprites (partial_renderer.rs:740-991): the sprite's plane vectors from the camera basis
+	Mat4 view_inverse;
+	if (!invert(cam.view_matrix, view_inverse)) return;
+	const Vec3 u_base_initial = truncate(view_inverse * v4(1, 0, 0, 0));
+	const Vec3 u_base = u_base_initial / magnitude(u_base_initial);
+	const Vec3 v_base_initial = truncate(view_inverse * v4(0, 1, 0, 0));
+	const Vec3 v_base = v_base_initial / magnitude(v_base_initial);
+	const Vec3 camera_direction = cross(u_base, v_base);
+	Vec3 u_n = u_base, v_n = v_base;
+	switch (sprite.orientation)
+	{
+	case SpriteEntity::PARALLEL_TO_CAMERA_PLANE:
+		break;
+	case SpriteEntity::FACING_TOWARDS_CAMERA:
+	{
+		const Vec3 to_camera = cam.position - sprite.position;
+		const Vec3 plane_normal = to_camera / std::fmax(magnitude(to_camera), 0.001f);
+		const Vec3 u_projected = u_base - plane_normal * dot(u_base, plane_normal);
+		const float len = magnitude(u_projected);
+		u_n = len < 0.0001f ? v3(1, 0, 0) : u_projected / len;
+		v_n = cross(u_n, plane_normal);
+		break;
+	}
+	case SpriteEntity::ALIGN_TO_Z_AXIS_PARALLEL_TO_CAMERA_PLANE:
+	{
+		v_n = v3(0, 0, -1);
+		const Vec3 u = cross(v_n, camera_direction);
+		const float len = magnitude(u);
+		u_n = len < 0.0001f ? v3(1, 0, 0) : u / len;
+		break;
+	}
+	default:
+	{
+		const Vec3 to_camera = cam.position - sprite.position;
+		v_n = v3(0, 0, -1);
+		const Vec3 u = cross(to_camera, v_n);
+		const float len = magnitude(u);
+		u_n = len < 0.0001f ? v3(1, 0, 0) : u / len;
+		break;
+	}
+	}
+	if (sprite.angle != 0.0f)
+	{
+		const float c = std::cos(sprite.angle), s = std::sin(sprite.angle);
+		const Vec3 nu = u_n * c - v_n * s, nv = u_n * s + v_n * c;
+		u_n = nu;
+		v_n = nv;
+	}
+	const LiteMip& mip0 = sc.lite_mips[size_t(sprite.texture) * NUM_MIPS];
+	const float ratio_h_w = float(mip0.height) / float(mip0.width);
+	const float step_u = sprite.radius * (1.0f / std::sqrt(1.0f + ratio_h_w * ratio_h_w)); // inv_sqrt_fast, generic
+	const float ratio_w_h = float(mip0.width) / float(mip0.height);
+	const float step_v = sprite.radius * (1.0f / std::sqrt(1.0f + ratio_w_h * ratio_w_h));
+	const Vec3 u_vec = u_n * step_u, v_vec = v_n * step_v;
+	const Vec3 corners[4] = {sprite.position + u_vec + v_vec, sprite.position + u_vec - v_vec, sprite.position - u_vec - v_vec,
+		sprite.position - u_vec + v_vec};
+	Vec3 vp[4];
+	for (int k = 0; k < 4; ++k) vp[k] = view_transform(cam.view_matrix, corners[k]);
+	uint32_t mip = 0;
+	if (vp[0].z > 0.0f && vp[1].z > 0.0f && vp[2].z > 0.0f && vp[3].z > 0.0f)
+	{
+		Vec2 pts[4];
+		for (int k = 0; k < 4; ++k) pts[k] = v2(vp[k].x / vp[k].z, vp[k].y / vp[k].z);
+		const Vec2 d0 = v2(pts[0].x - pts[2].x, pts[0].y - pts[2].y), d1 = v2(pts[1].x - pts[3].x, pts[1].y - pts[3].y);
+		const float shortest = std::fmin(d0.x * d0.x + d0.y * d0.y, d1.x * d1.x + d1.y * d1.y);
+		if (shortest <= 0.0f)
+			mip = NUM_MIPS - 1;
+		else
+		{
+			const float tc_diag = float(mip0.width) * float(mip0.width) + float(mip0.height) * float(mip0.height);
+			const float mip_f = std::log2(tc_diag / shortest) * 0.5f + opt.mip_bias;
+			mip = std::min<uint32_t>(uint32_t(as_i32(std::fmax(std::round(mip_f), 0.0f))), NUM_MIPS - 1);
+		}
+	}
+	const float min_z = std::fmin(std::fmin(std::fmin(vp[0].z, vp[1].z), vp[2].z), vp[3].z);
+	const float max_z = std::fmax(std::fmax(std::fmax(vp[0].z, vp[1].z), vp[2].z), vp[3].z);
+	const uint32_t max_tess = 4; // MAX_SPRITE_TESSELATION_LEVEL, renderer_structs.rs:164
+	const uint32_t tess = min_z <= 0.0f ? max_tess
+										: std::min<uint32_t>(uint32_t(as_i32(std::fmax((max_z / min_z - 1.0f) * 4.0f, 1.0f))), max_tess);
+	// the sprite's light: light_add, plus light_scale x (the light cube's mean, half the directional
+	// component, half the visible unshadowed dynamic lights)
+	float light[3] = {sprite.light_add[0], sprite.light_add[1], sprite.light_add[2]};
+	if (sprite.light_scale > 0.0f)
+	{
+		const float side_scale = sprite.light_scale / 6.0f;
+		for (int s6 = 0; s6 < 6; ++s6)
+			for (int c = 0; c < 3; ++c) light[c] += sprite.light_cube[s6][c] * side_scale;
+		const float dir_scale = sprite.light_scale * 0.5f * magnitude(sprite.light_dir_scaled);
+		for (int c = 0; c < 3; ++c) light[c] += dir_scale * sprite.light_color[c];
+		const float dyn_scale = sprite.light_scale * 0.5f;
+		const float min_square_distance = sprite.radius * sprite.radius;
+		for (size_t li = 0; li < lights.size(); ++li)
+		{
+			if (li < light_shadows.size() && light_shadows[li].kind != SW_SHADOW_NONE) continue;
+			bool visible = false;
+			if (li < light_leafs.size())
+				for (uint32_t lf : light_leafs[li]) visible = visible || vis.visible(lf);
+			if (!visible) continue;
+			const SwLight& l = lights[li];
+			const Vec3 to_light = v3(l.position[0], l.position[1], l.position[2]) - sprite.position;
+			const float inv_square_dist = 1.0f / std::fmax(magnitude2(to_light), min_square_distance);
+			const float light_inv_square_radius = 1.0f / (l.radius * l.radius);
+			if (inv_square_dist < light_inv_square_radius) continue;
+			const float scale = dyn_scale * 1.0f * (inv_square_dist - light_inv_square_radius);
+			for (int c = 0; c < 3; ++c) light[c] += scale * l.color[c];
+		}
+	}
+
+	// draw_sprite (partial_renderer.rs:3290-3523)
+	const LiteMip& tex = sc.lite_mips[size_t(sprite.texture) * NUM_MIPS + mip];
+	const float tw = float(tex.width), th = float(tex.height), tc_reduce = 1.0f / 16.0f;
+	ModelVertex3d quad[4];
+	const float tcs[4][2] = {{tw - tc_reduce, th - tc_reduce}, {tw - tc_reduce, tc_reduce}, {tc_reduce, tc_reduce}, {tc_reduce, th - tc_reduce}};
+	for (int k = 0; k < 4; ++k)
+	{
+		quad[k].pos = vp[k];
+		quad[k].tc[0] = tcs[k][0];
+		quad[k].tc[1] = tcs[k][1];
+		for (int c = 0; c < 3; ++c) quad[k].light[c] = light[c];
+	}
+	Vec3 planes[8];
+	bounds.get_clip_planes(planes);
+	ModelVertex3d clipped[MAX_VERTICES];
+	if (tess <= 1)
+	{
+		const uint32_t n = clip_model_near(quad, 4, clipped);
+		if (n < 3) return;
+		stats.model_triangles += emit_model_polygon(clipped, n, planes, 8, tex, sprite.blending_mode, nullptr);
+		return;
+	}
+	const uint32_t row = tess + 1;
+	ModelVertex3d grid[(4 + 1) * (4 + 1)];
+	const float inv_step = 1.0f / float(tess);
+	for (uint32_t y = 0; y < row; ++y)
+	{
+		const float ym = float(y) * inv_step;
+		for (uint32_t x = 0; x < row; ++x)
+		{
+			const float xm = float(x) * inv_step;
+			const float w[4] = {xm * ym, (1.0f - xm) * ym, (1.0f - xm) * (1.0f - ym), xm * (1.0f - ym)};
+			ModelVertex3d& g = grid[x + y * row];
+			g.pos = quad[0].pos * w[0] + quad[1].pos * w[1] + quad[2].pos * w[2] + quad[3].pos * w[3];
+			for (int i = 0; i < 2; ++i) g.tc[i] = w[0] * quad[0].tc[i] + w[1] * quad[1].tc[i] + w[2] * quad[2].tc[i] + w[3] * quad[3].tc[i];
+			for (int c = 0; c < 3; ++c) g.light[c] = 0.0f;
+		}
+	}
+	for (uint32_t x = 0; x < tess; ++x)
+		for (uint32_t y = 0; y < tess; ++y)
+		{
+			ModelVertex3d sub[4] = {grid[x + y * row], grid[x + (y + 1) * row], grid[1 + x + (y + 1) * row], grid[1 + x + y * row]};
+			const uint32_t n = clip_model_near(sub, 4, clipped);
+			if (n < 3) continue;
+			stats.model_triangles += emit_model_polygon(clipped, n, planes, 8, tex, sprite.blending_mode, light);
+		}
 }
 
 void FramePrep::draw_model(const ClippingPolygon& bounds, uint32_t model_index)
@@ -763,49 +969,37 @@ void FramePrep::draw_model(const ClippingPolygon& bounds, uint32_t model_index)
 	for (int k = 0; k < 4; ++k)
 		if (near_needed || box_planes[0][k].z > box_planes[1][k].z) planes_2d[num_2d++] = box_planes[0][k];
 
-	const uint32_t blend = e.blending_mode;
-	const uint64_t tex_offset = tex.offset;
-	auto clip3 = [&](const ModelVertex3d* src, uint32_t n, ModelVertex3d* dst) {
-		// clip_3d_model_polygon_by_plane with the near plane z >= Z_NEAR (src/common/clipping.rs:259-310)
-		uint32_t out = 0;
-		const ModelVertex3d* prev = &src[n - 1];
-		float prev_d = prev->pos.z;
-		auto inter = [&](const ModelVertex3d& v0, const ModelVertex3d& v1) {
-			const float d0 = v0.pos.z - PREP_Z_NEAR, d1 = v1.pos.z - PREP_Z_NEAR;
-			const float sum = d1 - d0, k0 = d0 / sum, k1 = d1 / sum;
-			ModelVertex3d r;
-			r.pos = v0.pos * k1 - v1.pos * k0;
-			for (int i = 0; i < 2; ++i) r.tc[i] = v0.tc[i] * k1 - v1.tc[i] * k0;
-			for (int i = 0; i < 3; ++i) r.light[i] = v0.light[i] * k1 - v1.light[i] * k0;
-			return r;
-		};
-		for (uint32_t i = 0; i < n && out < MAX_VERTICES; ++i)
+	ModelVertex3d c3[2][MAX_VERTICES];
+	for (uint32_t k : model_triangles)
+	{
+		for (int i = 0; i < 3; ++i) c3[0][i] = model_vertices[mesh.triangles[k + i]];
+		uint32_t n = 3;
+		int src3 = 0;
+		if (near_needed)
 		{
-			const ModelVertex3d& v = src[i];
-			const float d = v.pos.z;
-			if (d > PREP_Z_NEAR)
-			{
-				if (prev_d < PREP_Z_NEAR && out < MAX_VERTICES) dst[out++] = inter(*prev, v);
-				if (out < MAX_VERTICES) dst[out++] = v;
-			}
-			else if (d == PREP_Z_NEAR)
-				dst[out++] = v;
-			else if (prev_d > PREP_Z_NEAR)
-				dst[out++] = inter(*prev, v);
-			prev = &v;
-			prev_d = d;
+			n = clip_model_near(c3[0], n, c3[1]);
+			if (n < 3) continue;
+			src3 = 1;
 		}
-		return out;
-	};
+		stats.model_triangles += emit_model_polygon(c3[src3], n, planes_2d, num_2d, tex, e.blending_mode, nullptr);
+	}
+}
+
+// draw_mesh's and draw_sprite's tail (partial_renderer.rs:3380-3418, 3640-3718): project the camera-space
+// polygon, clip it by the given 2D planes (clip_2d_model_polygon, src/common/clipping.rs:203-257), convert
+// to fixed point (f32_to_fixed16) and emit one fill_triangle draw per triangle of the fan. `light`, when
+// given, replaces every vertex's light (the tessellated sprite path). Returns the triangles emitted.
+uint32_t FramePrep::emit_model_polygon(const ModelVertex3d* verts, uint32_t n, const Vec3* planes_2d, uint32_t num_2d,
+	const LiteMip& tex, uint32_t blend, const float* light)
+{
 	struct V2
 	{
 		Vec2 pos;
 		float tc[2], light[3];
 	};
-	auto clip2 = [&](const V2* src, uint32_t n, const Vec3& line, V2* dst) {
-		// clip_2d_model_polygon, src/common/clipping.rs:203-257
+	auto clip2 = [&](const V2* src, uint32_t count, const Vec3& line, V2* dst) {
 		uint32_t out = 0;
-		const V2* prev = &src[n - 1];
+		const V2* prev = &src[count - 1];
 		float prev_d = prev->pos.x * line.x + prev->pos.y * line.y - line.z;
 		auto inter = [&](const V2& v0, const V2& v1) {
 			const float d0 = v0.pos.x * line.x + v0.pos.y * line.y - line.z, d1 = v1.pos.x * line.x + v1.pos.y * line.y - line.z;
@@ -816,7 +1010,7 @@ void FramePrep::draw_model(const ClippingPolygon& bounds, uint32_t model_index)
 			for (int i = 0; i < 3; ++i) r.light[i] = v0.light[i] * k1 - v1.light[i] * k0;
 			return r;
 		};
-		for (uint32_t i = 0; i < n && out < MAX_VERTICES; ++i)
+		for (uint32_t i = 0; i < count && out < MAX_VERTICES; ++i)
 		{
 			const V2& v = src[i];
 			const float d = v.pos.x * line.x + v.pos.y * line.y - line.z;
@@ -834,65 +1028,49 @@ void FramePrep::draw_model(const ClippingPolygon& bounds, uint32_t model_index)
 		}
 		return out;
 	};
-	ModelVertex3d c3[2][MAX_VERTICES];
 	V2 c2[2][MAX_VERTICES];
-	for (uint32_t k : model_triangles)
+	for (uint32_t i = 0; i < n; ++i)
 	{
-		uint32_t n = 3;
-		for (int i = 0; i < 3; ++i) c3[0][i] = model_vertices[mesh.triangles[k + i]];
-		int src3 = 0;
-		if (near_needed)
-		{
-			n = clip3(c3[0], n, c3[1]);
-			if (n < 3) continue;
-			src3 = 1;
-		}
-		for (uint32_t i = 0; i < n; ++i)
-		{
-			const ModelVertex3d& v = c3[src3][i];
-			c2[0][i].pos = v2(v.pos.x / v.pos.z, v.pos.y / v.pos.z);
-			for (int j = 0; j < 2; ++j) c2[0][i].tc[j] = v.tc[j];
-			for (int j = 0; j < 3; ++j) c2[0][i].light[j] = v.light[j];
-		}
-		int src2 = 0;
-		bool clipped_out = false;
-		for (uint32_t pl = 0; pl < num_2d; ++pl)
-		{
-			n = clip2(c2[src2], n, planes_2d[pl], c2[src2 ^ 1]);
-			if (n < 3)
-			{
-				clipped_out = true;
-				break;
-			}
-			src2 ^= 1;
-		}
-		if (clipped_out) continue;
-		SwTriVertex fixed[MAX_VERTICES];
-		for (uint32_t i = 0; i < n; ++i)
-		{
-			const V2& v = c2[src2][i];
-			fixed[i] = SwTriVertex{to_fixed16(v.pos.x), to_fixed16(v.pos.y), {to_fixed16(v.tc[0]), to_fixed16(v.tc[1])},
-				{to_fixed16(v.light[0]), to_fixed16(v.light[1]), to_fixed16(v.light[2])}, 0};
-		}
-		for (uint32_t tri = 0; tri + 2 < n; ++tri)
-		{
-			SwDrawCmd d;
-			std::memset(&d, 0, sizeof(d));
-			d.first_vertex = uint32_t(tri_vertices.size());
-			d.vertex_count = 3;
-			d.mode = SW_RASTER_TRIANGLE;
-			d.blend = blend;
-			d.tex_size[0] = tex.width;
-			d.tex_size[1] = tex.height;
-			d.tex_source = SW_TEXSRC_LITE;
-			d.tex_offset = tex_offset;
-			tri_vertices.push_back(fixed[0]);
-			tri_vertices.push_back(fixed[tri + 1]);
-			tri_vertices.push_back(fixed[tri + 2]);
-			draws.push_back(d);
-			++stats.model_triangles;
-		}
+		const ModelVertex3d& v = verts[i];
+		c2[0][i].pos = v2(v.pos.x / v.pos.z, v.pos.y / v.pos.z);
+		for (int j = 0; j < 2; ++j) c2[0][i].tc[j] = v.tc[j];
+		for (int j = 0; j < 3; ++j) c2[0][i].light[j] = v.light[j];
 	}
+	int src2 = 0;
+	for (uint32_t pl = 0; pl < num_2d; ++pl)
+	{
+		n = clip2(c2[src2], n, planes_2d[pl], c2[src2 ^ 1]);
+		if (n < 3) return 0;
+		src2 ^= 1;
+	}
+	SwTriVertex fixed[MAX_VERTICES];
+	for (uint32_t i = 0; i < n; ++i)
+	{
+		const V2& v = c2[src2][i];
+		const float* l = light ? light : v.light;
+		fixed[i] = SwTriVertex{to_fixed16(v.pos.x), to_fixed16(v.pos.y), {to_fixed16(v.tc[0]), to_fixed16(v.tc[1])},
+			{to_fixed16(l[0]), to_fixed16(l[1]), to_fixed16(l[2])}, 0};
+	}
+	uint32_t emitted = 0;
+	for (uint32_t tri = 0; tri + 2 < n; ++tri)
+	{
+		SwDrawCmd d;
+		std::memset(&d, 0, sizeof(d));
+		d.first_vertex = uint32_t(tri_vertices.size());
+		d.vertex_count = 3;
+		d.mode = SW_RASTER_TRIANGLE;
+		d.blend = blend;
+		d.tex_size[0] = tex.width;
+		d.tex_size[1] = tex.height;
+		d.tex_source = SW_TEXSRC_LITE;
+		d.tex_offset = tex.offset;
+		tri_vertices.push_back(fixed[0]);
+		tri_vertices.push_back(fixed[tri + 1]);
+		tri_vertices.push_back(fixed[tri + 2]);
+		draws.push_back(d);
+		++emitted;
+	}
+	return emitted;
 }
 
 void FramePrep::draw_skybox(const ClippingPolygon& viewport)

@@ -206,6 +206,7 @@ private:
 	// 2562-2792; build_dynamic_models_buffers :1122-1190; draw_mesh :3525-3718).
 	void draw_leaf_models(const ClippingPolygon& bounds, uint32_t leaf_index);
 	void draw_model(const ClippingPolygon& bounds, uint32_t model_index);
+	void draw_sprite(const ClippingPolygon& bounds, uint32_t sprite_index);
 	struct ModelVertex3d
 	{
 		Vec3 pos;
@@ -213,6 +214,9 @@ private:
 		float light[3];
 	};
 	std::vector<ModelVertex3d> model_vertices; // the current model's transformed vertices
+	static uint32_t clip_model_near(const ModelVertex3d* src, uint32_t n, ModelVertex3d* dst);
+	uint32_t emit_model_polygon(const ModelVertex3d* verts, uint32_t n, const Vec3* planes_2d, uint32_t num_2d,
+		const LiteMip& tex, uint32_t blend, const float* light);
 	std::vector<uint32_t> model_triangles;     // its visible triangles, back to front
 	void draw_polygon(const Vec3 clip_planes[8], uint32_t polygon_index);
 	// draw_polygon (partial_renderer.rs:4011-4142) of transformed vertices with their equations and texture.

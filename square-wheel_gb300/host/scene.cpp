@@ -1109,6 +1109,46 @@ void make_model_skin(Rng& rng, uint32_t size, bool cutout, Scene& sc)
 	}
 }
 
+// A sprite texture: a w x h Color32 TextureLite with NUM_MIPS mips (2x2 averages, as make_model_skin):
+// a glowing blob whose alpha falls off from the centre (alpha-blended and additive sprites) or a hard
+// disc (alpha-tested ones).
+void make_sprite_texture(Rng& rng, uint32_t w, uint32_t h, bool hard, Scene& sc)
+{
+	std::vector<uint32_t> img(size_t(w) * h);
+	const float base[3] = {rng.uniform(120, 255), rng.uniform(80, 255), rng.uniform(40, 255)};
+	for (uint32_t y = 0; y < h; ++y)
+		for (uint32_t x = 0; x < w; ++x)
+		{
+			const float dx = (float(x) + 0.5f) / float(w) * 2.0f - 1.0f, dy = (float(y) + 0.5f) / float(h) * 2.0f - 1.0f;
+			const float r = std::sqrt(dx * dx + dy * dy);
+			const float f = std::fmax(1.0f - r, 0.0f);
+			uint32_t c = 0;
+			for (int k = 0; k < 3; ++k) c |= uint32_t(std::fmin(base[k] * (0.4f + 0.6f * f) * rng.uniform(0.9f, 1.0f), 255.0f)) << (8 * (2 - k));
+			const uint32_t alpha = hard ? (r < 0.8f ? 255u : 0u) : uint32_t(std::fmin(f * 1.5f, 1.0f) * 255.0f);
+			img[size_t(y) * w + x] = c | (alpha << 24);
+		}
+	for (uint32_t mip = 0; mip < NUM_MIPS; ++mip)
+	{
+		sc.lite_mips.push_back(LiteMip{uint64_t(sc.lite_pixels.size()), w, h});
+		sc.lite_pixels.insert(sc.lite_pixels.end(), img.begin(), img.end());
+		if (mip + 1 == NUM_MIPS) break;
+		const uint32_t nw = std::max(w / 2, 1u), nh = std::max(h / 2, 1u);
+		std::vector<uint32_t> next(size_t(nw) * nh);
+		auto avg = [](uint32_t a, uint32_t b) { return (((a ^ b) & 0xFEFEFEFEu) >> 1) + (a & b); };
+		for (uint32_t y = 0; y < nh; ++y)
+			for (uint32_t x = 0; x < nw; ++x)
+			{
+				const uint32_t* r0 = &img[size_t(std::min(2 * y, h - 1)) * w + std::min(2 * x, w - 1)];
+				const uint32_t* r1 = &img[size_t(std::min(2 * y + 1, h - 1)) * w + std::min(2 * x, w - 1)];
+				const uint32_t x1 = (2 * x + 1 < w) ? 1 : 0;
+				next[size_t(y) * nw + x] = avg(avg(r0[0], r0[x1]), avg(r1[0], r1[x1]));
+			}
+		img.swap(next);
+		w = nw;
+		h = nh;
+	}
+}
+
 float TimeFunction::evaluate(float x) const
 {
 	// SingleArgumentFunction::evaluate, material_function.rs:91-150
@@ -1429,6 +1469,40 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 			for (int c = 0; c < 3; ++c) e.light_color[c] = mrng.uniform(0.3f, 1.2f);
 			sc.leaf_models[e.leaf].push_back(uint32_t(sc.models.size()));
 			sc.models.push_back(e);
+		}
+	}
+	if (cfg.num_sprites)
+	{
+		// Sprites (own generator): a few textures of other aspect ratios, placed inside the rooms' leafs
+		// well away from their walls, every orientation, blending modes from the alpha family and additive.
+		Rng prng(cfg.seed ^ 0x5B417E5u);
+		const uint32_t first_texture = uint32_t(sc.lite_mips.size() / NUM_MIPS);
+		const uint32_t sizes[4][2] = {{64, 64}, {32, 64}, {64, 32}, {128, 64}};
+		for (int k = 0; k < 4; ++k) make_sprite_texture(prng, sizes[k][0], sizes[k][1], k == 3, sc);
+		sc.leaf_sprites.assign(sc.leafs.size(), {});
+		const uint32_t blends[3] = {SW_BLEND_ALPHA_BLEND, SW_BLEND_ADDITIVE, SW_BLEND_AVERAGE};
+		for (uint32_t i = 0; i < cfg.num_sprites; ++i)
+		{
+			const Room& r = b.rooms[prng.below(uint32_t(b.rooms.size()))];
+			SpriteEntity e;
+			const uint32_t t = prng.below(4);
+			e.texture = first_texture + t;
+			e.blending_mode = t == 3 ? uint32_t(SW_BLEND_ALPHA_TEST) : blends[prng.below(3)];
+			e.orientation = prng.below(4);
+			e.radius = prng.uniform(12.0f, 48.0f);
+			e.angle = prng.below(2) ? 0.0f : prng.uniform(-3.1f, 3.1f);
+			const float margin = e.radius + 8.0f;
+			e.position = v3(prng.uniform(r.x0 + margin, r.x1 - margin), prng.uniform(r.y0 + margin, r.y1 - margin),
+				prng.uniform(margin, std::fmax(r.h - margin, margin + 1.0f)));
+			e.leaf = r.leaf;
+			e.light_scale = prng.below(4) ? prng.uniform(0.5f, 1.5f) : 0.0f;
+			for (int c = 0; c < 3; ++c) e.light_add[c] = prng.uniform(0.0f, 0.6f);
+			for (int s6 = 0; s6 < 6; ++s6)
+				for (int c = 0; c < 3; ++c) e.light_cube[s6][c] = prng.uniform(0.2f, 0.9f);
+			e.light_dir_scaled = v3(prng.uniform(-0.6f, 0.6f), prng.uniform(-0.6f, 0.6f), prng.uniform(0.2f, 1.0f));
+			for (int c = 0; c < 3; ++c) e.light_color[c] = prng.uniform(0.3f, 1.2f);
+			sc.leaf_sprites[e.leaf].push_back(uint32_t(sc.sprites.size()));
+			sc.sprites.push_back(e);
 		}
 	}
 	add_dynamic_lights(cfg, rng, sc);

@@ -160,6 +160,30 @@ struct ModelEntity
 	float light_color[3];
 };
 
+// A sprite (Sprite, src/square_wheel/frame_info.rs:126-147): a textured quad of `radius` (half its
+// diagonal) at `position`, turned by `angle` in its plane, oriented by one of the four SpriteOrientation
+// rules, lit by light_add plus light_scale times its light (a light cube and directional component
+// standing in for fetch_light_from_grid, and the frame's unshadowed dynamic lights), in one leaf.
+struct SpriteEntity
+{
+	enum Orientation : uint32_t
+	{
+		PARALLEL_TO_CAMERA_PLANE = 0,
+		FACING_TOWARDS_CAMERA,
+		ALIGN_TO_Z_AXIS_PARALLEL_TO_CAMERA_PLANE,
+		ALIGN_TO_Z_AXIS_FACING_TOWARDS_CAMERA,
+	};
+	Vec3 position;
+	float angle, radius;
+	uint32_t texture; // lite texture: mips at texture * NUM_MIPS in Scene::lite_mips
+	uint32_t blending_mode, orientation, leaf;
+	float light_scale;
+	float light_add[3];
+	float light_cube[6][3];
+	Vec3 light_dir_scaled;
+	float light_color[3];
+};
+
 // One mip of a TextureLite (Color32 pixels, src/square_wheel/textures.rs:89-91) in Scene::lite_pixels.
 struct LiteMip
 {
@@ -201,6 +225,7 @@ struct SceneConfig
 	uint32_t num_models = 0;          // per-vertex animated triangle models placed in the rooms
 	uint32_t model_triangles = 2000;  // triangles per model mesh (about)
 	uint32_t model_frames = 8;        // animation keyframes per mesh
+	uint32_t num_sprites = 0;         // sprites in the rooms (all four orientations, several blending modes)
 	uint32_t turb_materials = 0;      // the last base materials but layered_materials have a turbulence effect
 	uint32_t layered_materials = 0;   // the last this many base materials are layered animations
 };
@@ -239,6 +264,9 @@ struct Scene
 	std::vector<std::vector<uint32_t>> leaf_models;
 	std::vector<uint32_t> lite_pixels;
 	std::vector<LiteMip> lite_mips;
+	// Sprites and the sprites of each leaf; their textures are lite textures after the model skins.
+	std::vector<SpriteEntity> sprites;
+	std::vector<std::vector<uint32_t>> leaf_sprites;
 	// A scene loaded from a compiled map keeps its compressed lightmap lumps (4 bytes per simple
 	// element, 13 per directional element, as the file holds them) for upload and decompression on the
 	// GPU; empty for generated scenes.
