@@ -48,6 +48,7 @@ typedef struct SwhSceneConfig {
 	uint32_t turb_materials;      /* base materials with a turbulence effect (before the layered ones) */
 	uint32_t layered_materials;   /* the last this many base materials are layered animations */
 	uint32_t num_sprites;         /* sprites in the rooms (every orientation, alpha-family and additive blending) */
+	uint32_t num_decals;          /* decals on the rooms' walls and floors (every blending mode) */
 } SwhSceneConfig;
 
 typedef struct SwhSceneInfo {

@@ -572,6 +572,9 @@ void FramePrep::draw_leaf(const ClippingPolygon& bounds, uint32_t leaf_index)
 		if (poly[pi].visible_frame != current_frame) continue;
 		draw_polygon(planes, pi);
 	}
+	// decals after all the leaf's polygons (partial_renderer.rs:2561-2575)
+	if (leaf_index < sc.leaf_decals.size() && !sc.leaf_decals[leaf_index].empty())
+		for (uint32_t k = 0; k < leaf.num_polygons; ++k) draw_polygon_decals(planes, leaf.first_polygon + k, sc.leaf_decals[leaf_index]);
 	const bool models = leaf_index < sc.leaf_models.size() && !sc.leaf_models[leaf_index].empty();
 	const bool sprites = leaf_index < sc.leaf_sprites.size() && !sc.leaf_sprites[leaf_index].empty();
 	if (models || sprites) draw_leaf_models(bounds, leaf_index);
@@ -1071,6 +1074,282 @@ uint32_t FramePrep::emit_model_polygon(const ModelVertex3d* verts, uint32_t n, c
 		++emitted;
 	}
 	return emitted;
+}
+
+const FramePrep::DecalInfo& FramePrep::prepare_decal(uint32_t decal_index)
+{
+	if (decal_info.size() < sc.decals.size()) decal_info.resize(sc.decals.size());
+	DecalInfo& info = decal_info[decal_index];
+	if (info.frame == current_frame) return info;
+	info.frame = current_frame;
+	const DecalEntity& d = sc.decals[decal_index];
+	// get_object_matrix_with_scale: translate * rotate * scale (src/common/matrix.rs:111-122)
+	Mat4 m = mat4_from_quat(d.rotation);
+	m.c[0] = m.c[0] * d.scale.x;
+	m.c[1] = m.c[1] * d.scale.y;
+	m.c[2] = m.c[2] * d.scale.z;
+	m.c[3] = v4(d.position.x, d.position.y, d.position.z, 1.0f);
+	Mat4 inv;
+	if (!invert(transpose(m), inv)) inv = Mat4::identity();
+	info.planes = cam.planes_matrix * inv;
+	// the light cube of the dynamic lights at the decal's position (LightCube, src/common/light_cube.rs)
+	float cube[6][3] = {};
+	Vec3 sum_dirs[3] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)};
+	const float min_vec_len = 0.00000001f;
+	if (d.lightmap_light_scale > 0.0f)
+	{
+		const float min_square_distance = magnitude2(d.scale) * 0.25f;
+		for (size_t li = 0; li < lights.size(); ++li)
+		{
+			if (li < light_shadows.size() && light_shadows[li].kind != SW_SHADOW_NONE) continue;
+			bool visible = false;
+			if (li < light_leafs.size())
+				for (uint32_t lf : light_leafs[li]) visible = visible || vis.visible(lf);
+			if (!visible) continue;
+			const SwLight& l = lights[li];
+			const Vec3 to_light = v3(l.position[0], l.position[1], l.position[2]) - d.position;
+			const float inv_square_dist = 1.0f / std::fmax(magnitude2(to_light), min_square_distance);
+			const float light_inv_square_radius = 1.0f / (l.radius * l.radius);
+			if (inv_square_dist < light_inv_square_radius) continue;
+			const float scale = 1.0f * (inv_square_dist - light_inv_square_radius);
+			const float ls[3] = {l.color[0] * scale, l.color[1] * scale, l.color[2] * scale};
+			// add_light_sample
+			const Vec3 dn = to_light / std::fmax(magnitude(to_light), min_vec_len);
+			const float comps[3] = {dn.x, dn.y, dn.z};
+			for (int a = 0; a < 3; ++a)
+				for (int c = 0; c < 3; ++c)
+				{
+					if (comps[a] <= 0.0f)
+						cube[2 * a][c] += ls[c] * (-comps[a]);
+					else
+						cube[2 * a + 1][c] += ls[c] * comps[a];
+				}
+			for (int c = 0; c < 3; ++c) sum_dirs[c] = sum_dirs[c] + dn * ls[c];
+		}
+	}
+	// convert_into_light_grid_sample
+	const Vec3 dir = 0.33f * (sum_dirs[0] + sum_dirs[1] + sum_dirs[2]);
+	const float len2 = std::fmax(magnitude2(dir), min_vec_len);
+	for (int c = 0; c < 3; ++c) info.color[c] = std::fmax(dot(sum_dirs[c], dir), 0.0f) / len2;
+	const float dcomps[3] = {dir.x, dir.y, dir.z};
+	for (int c = 0; c < 3; ++c)
+		for (int a = 0; a < 3; ++a)
+		{
+			if (dcomps[a] <= 0.0f)
+				cube[2 * a][c] = std::fmax(cube[2 * a][c] - info.color[c] * (-dcomps[a]), 0.0f);
+			else
+				cube[2 * a + 1][c] = std::fmax(cube[2 * a + 1][c] - info.color[c] * dcomps[a], 0.0f);
+		}
+	std::memcpy(info.cube, cube, sizeof(cube));
+	info.dir = dir;
+	return info;
+}
+
+// draw_polygon_decals (partial_renderer.rs:2794-2957): the decals of the leaf cut out of one polygon
+void FramePrep::draw_polygon_decals(const Vec3 clip_planes[8], uint32_t polygon_index, const std::vector<uint32_t>& leaf_decals)
+{
+	const PolyData& pd = poly[polygon_index];
+	if (pd.visible_frame != current_frame) return;
+	const MapPolygon& polygon = sc.polygons[polygon_index];
+	const uint32_t cur_material = polygon.texture < mapping.size() ? mapping[polygon.texture] : polygon.texture;
+	if (!sc.materials[cur_material].decals) return;
+	const Vec3 normal = sc.basis[polygon_index].normal;
+	static const float CUBE_SIDES[6][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+	for (uint32_t di : leaf_decals)
+	{
+		const DecalEntity& d = sc.decals[di];
+		if (dot(normal, rotate_vector(d.rotation, v3(-1, 0, 0))) < 0.1f) continue; // MAX_ANGLE_COS
+		const DecalInfo& info = prepare_decal(di);
+		Vec3 vc[2][MAX_VERTICES];
+		uint32_t n = std::min<uint32_t>(polygon.num_vertices, MAX_VERTICES);
+		for (uint32_t i = 0; i < n; ++i) vc[0][i] = vertices_transformed[polygon.first_vertex + i];
+		int src = 0;
+		bool cut = false;
+		for (const float* side : CUBE_SIDES)
+		{
+			const Vec4 pv = info.planes * v4(side[0], side[1], side[2], 1.0f);
+			const Vec3 pn = truncate(pv);
+			const float pdist = -pv.w;
+			// clip_3d_polygon_by_plane (src/common/clipping.rs:53-105)
+			uint32_t out = 0;
+			const Vec3* prev = &vc[src][n - 1];
+			float prev_dist = dot(pn, *prev);
+			auto inter = [&](const Vec3& v0, const Vec3& v1) {
+				const float d0 = dot(v0, pn) - pdist, d1 = dot(v1, pn) - pdist;
+				const float sum = d1 - d0, k0 = d0 / sum, k1 = d1 / sum;
+				return v0 * k1 - v1 * k0;
+			};
+			for (uint32_t i = 0; i < n; ++i)
+			{
+				const Vec3& v = vc[src][i];
+				const float dist = dot(pn, v);
+				if (dist > pdist)
+				{
+					if (prev_dist < pdist)
+					{
+						vc[src ^ 1][out++] = inter(*prev, v);
+						if (out == MAX_VERTICES) break;
+					}
+					vc[src ^ 1][out++] = v;
+					if (out == MAX_VERTICES) break;
+				}
+				else if (dist == pdist)
+				{
+					vc[src ^ 1][out++] = v;
+					if (out == MAX_VERTICES) break;
+				}
+				else if (prev_dist > pdist)
+				{
+					vc[src ^ 1][out++] = inter(*prev, v);
+					if (out == MAX_VERTICES) break;
+				}
+				prev = &v;
+				prev_dist = dist;
+			}
+			n = out;
+			if (n < 3)
+			{
+				cut = true;
+				break;
+			}
+			src ^= 1;
+		}
+		if (cut) continue;
+		Vec2 projected[MAX_VERTICES];
+		n = project_and_clip_polygon(clip_planes, vc[src], n, projected);
+		if (n < 3) continue;
+		const LiteMip& tex0 = sc.lite_mips[size_t(d.texture) * NUM_MIPS];
+		const Vec4 basis0 = info.planes * (v4(0.0f, -0.5f, 0.0f, 0.5f) * float(tex0.width));
+		const Vec4 basis1 = info.planes * (v4(0.0f, 0.0f, -0.5f, 0.5f) * float(tex0.height));
+		const DepthEquation& de = pd.depth;
+		TexCoordEquation tc; // from_depth_equation_and_transformed_tex_coord_equations (equations.rs:55-74)
+		tc.d_tc_dx[0] = basis0.x + basis0.w * de.d_inv_z_dx;
+		tc.d_tc_dx[1] = basis1.x + basis1.w * de.d_inv_z_dx;
+		tc.d_tc_dy[0] = basis0.y + basis0.w * de.d_inv_z_dy;
+		tc.d_tc_dy[1] = basis1.y + basis1.w * de.d_inv_z_dy;
+		tc.k[0] = basis0.z + basis0.w * de.k;
+		tc.k[1] = basis1.z + basis1.w * de.k;
+		const uint32_t mip = calculate_mip(projected, n, de, tc, opt.mip_bias);
+		const LiteMip& tex = sc.lite_mips[size_t(d.texture) * NUM_MIPS + mip];
+		const float ms = 1.0f / float(1 << mip);
+		TexCoordEquation tcs;
+		for (int i = 0; i < 2; ++i)
+			tcs.d_tc_dx[i] = tc.d_tc_dx[i] * ms, tcs.d_tc_dy[i] = tc.d_tc_dy[i] * ms, tcs.k[i] = tc.k[i] * ms;
+		// the polygon's surface coordinates give the lightmap coordinates of the decal's points
+		const float lm_scale = float(1 << pd.mip) / float(LIGHTMAP_SCALE);
+		const float lm_shift[2] = {float(pd.tc_min[0]) * lm_scale - float(polygon.tex_coord_min[0] >> LIGHTMAP_SCALE_LOG2),
+			float(pd.tc_min[1]) * lm_scale - float(polygon.tex_coord_min[1] >> LIGHTMAP_SCALE_LOG2)};
+		TexCoordEquation lm;
+		for (int i = 0; i < 2; ++i)
+			lm.d_tc_dx[i] = pd.tc.d_tc_dx[i] * lm_scale, lm.d_tc_dy[i] = pd.tc.d_tc_dy[i] * lm_scale, lm.k[i] = pd.tc.k[i] * lm_scale;
+		float dyn[3];
+		light_cube_light(info.cube, normal, dyn);
+		const float dir_dot = std::fmax(dot(normal, info.dir), 0.0f);
+		for (int c = 0; c < 3; ++c) dyn[c] += dir_dot * info.color[c];
+		for (uint32_t t = 0; t + 2 < n; ++t)
+		{
+			const Vec2 tri[3] = {projected[0], projected[t + 1], projected[t + 2]};
+			subdivide_decal_triangle(d, polygon, de, tcs, lm, lm_shift, tri, tex, dyn, 0);
+		}
+	}
+}
+
+namespace
+{
+// get_polygon_lightmap_light (partial_renderer.rs:3807-3875): the polygon's simple lightmap, bilinear,
+// renormalised where samples fall outside it
+void polygon_lightmap_light(const Scene& sc, const MapPolygon& p, Vec2 c, float out[3])
+{
+	out[0] = out[1] = out[2] = 0.0f;
+	if (p.lightmap_data_offset == 0 || sc.lightmaps.empty()) return;
+	const float* data = &sc.lightmaps[size_t(p.lightmap_data_offset) * 3];
+	const int32_t ci[2] = {as_i32(std::floor(c.x)), as_i32(std::floor(c.y))};
+	const int32_t lw = ((p.tex_coord_max[0] + 15) >> 4) - (p.tex_coord_min[0] >> 4) + 1;
+	const int32_t lh = ((p.tex_coord_max[1] + 15) >> 4) - (p.tex_coord_min[1] >> 4) + 1;
+	float total_factor = 0.0f;
+	for (int dy = 0; dy <= 1; ++dy)
+	{
+		const int32_t y = ci[1] + dy;
+		if (y < 0 || y >= lh) continue;
+		const float fy = 1.0f - std::fabs(c.y - float(y));
+		for (int dx = 0; dx <= 1; ++dx)
+		{
+			const int32_t x = ci[0] + dx;
+			if (x < 0 || x >= lw) continue;
+			const float fx = 1.0f - std::fabs(c.x - float(x));
+			const float* l = data + size_t(x + y * lw) * 3;
+			const float f = fx * fy;
+			for (int i = 0; i < 3; ++i) out[i] += f * l[i];
+			total_factor += f;
+		}
+	}
+	if (total_factor < 1.0f)
+	{
+		const float inv = 1.0f / total_factor;
+		for (int i = 0; i < 3; ++i) out[i] *= inv;
+	}
+}
+} // namespace
+
+// subdivide_and_draw_decal_triangle (partial_renderer.rs:2959-3080)
+void FramePrep::subdivide_decal_triangle(const DecalEntity& d, const MapPolygon& polygon, const DepthEquation& de,
+	const TexCoordEquation& tc, const TexCoordEquation& lm_eq, const float lm_shift[2], const Vec2 pts[3], const LiteMip& tex,
+	const float dyn[3], int depth)
+{
+	const Vec2* min_p = &pts[0];
+	const Vec2* max_p = &pts[0];
+	float min_inv_z = de.sample(pts[0]), max_inv_z = min_inv_z;
+	for (int k = 1; k < 3; ++k)
+	{
+		const float iz = de.sample(pts[k]);
+		if (iz < min_inv_z) min_inv_z = iz, min_p = &pts[k];
+		if (iz > max_inv_z) max_inv_z = iz, max_p = &pts[k];
+	}
+	if (depth >= 2 || affine_may_be_used(de, tc, *min_p, *max_p))
+	{
+		const float tc_eps = 1.0f / 32.0f;
+		const float max_tc[2] = {float(tex.width) - tc_eps, float(tex.height) - tc_eps};
+		SwTriVertex v[3];
+		for (int k = 0; k < 3; ++k)
+		{
+			const Vec2& p = pts[k];
+			const float z = 1.0f / de.sample(p);
+			float light[3] = {d.light_add[0], d.light_add[1], d.light_add[2]};
+			if (d.lightmap_light_scale > 0.0f)
+			{
+				const Vec2 lc = v2(z * (lm_eq.d_tc_dx[0] * p.x + lm_eq.d_tc_dy[0] * p.y + lm_eq.k[0]) + lm_shift[0],
+					z * (lm_eq.d_tc_dx[1] * p.x + lm_eq.d_tc_dy[1] * p.y + lm_eq.k[1]) + lm_shift[1]);
+				float lml[3];
+				polygon_lightmap_light(sc, polygon, lc, lml);
+				for (int i = 0; i < 3; ++i)
+				{
+					light[i] += lml[i] * d.lightmap_light_scale;
+					light[i] += dyn[i];
+				}
+			}
+			const float u = std::fmin(std::fmax(z * (tc.d_tc_dx[0] * p.x + tc.d_tc_dy[0] * p.y + tc.k[0]), tc_eps), max_tc[0]);
+			const float w = std::fmin(std::fmax(z * (tc.d_tc_dx[1] * p.x + tc.d_tc_dy[1] * p.y + tc.k[1]), tc_eps), max_tc[1]);
+			v[k] = SwTriVertex{to_fixed16(p.x), to_fixed16(p.y), {to_fixed16(u), to_fixed16(w)},
+				{to_fixed16(light[0]), to_fixed16(light[1]), to_fixed16(light[2])}, 0};
+		}
+		SwDrawCmd c;
+		std::memset(&c, 0, sizeof(c));
+		c.first_vertex = uint32_t(tri_vertices.size());
+		c.vertex_count = 3;
+		c.mode = SW_RASTER_TRIANGLE;
+		c.blend = d.blending_mode;
+		c.tex_size[0] = tex.width;
+		c.tex_size[1] = tex.height;
+		c.tex_source = SW_TEXSRC_LITE;
+		c.tex_offset = tex.offset;
+		for (int k = 0; k < 3; ++k) tri_vertices.push_back(v[k]);
+		draws.push_back(c);
+		++stats.model_triangles;
+		return;
+	}
+	const Vec2 c0 = (pts[0] + pts[1]) / 2.0f, c1 = (pts[1] + pts[2]) / 2.0f, c2 = (pts[2] + pts[0]) / 2.0f;
+	const Vec2 subs[4][3] = {{pts[0], c0, c2}, {pts[1], c1, c0}, {pts[2], c2, c1}, {c0, c1, c2}};
+	for (const auto& s : subs) subdivide_decal_triangle(d, polygon, de, tc, lm_eq, lm_shift, s, tex, dyn, depth + 1);
 }
 
 void FramePrep::draw_skybox(const ClippingPolygon& viewport)

@@ -207,6 +207,22 @@ private:
 	void draw_leaf_models(const ClippingPolygon& bounds, uint32_t leaf_index);
 	void draw_model(const ClippingPolygon& bounds, uint32_t model_index);
 	void draw_sprite(const ClippingPolygon& bounds, uint32_t sprite_index);
+	// prepare_decals (partial_renderer.rs:665-737) for one decal, once per frame: its camera-space
+	// planes matrix and its light (a light cube of the visible unshadowed dynamic lights)
+	struct DecalInfo
+	{
+		uint32_t frame = 0;
+		Mat4 planes;
+		float cube[6][3];
+		Vec3 dir;
+		float color[3];
+	};
+	std::vector<DecalInfo> decal_info;
+	const DecalInfo& prepare_decal(uint32_t decal_index);
+	void draw_polygon_decals(const Vec3 clip_planes[8], uint32_t polygon_index, const std::vector<uint32_t>& leaf_decals);
+	void subdivide_decal_triangle(const DecalEntity& d, const MapPolygon& polygon, const DepthEquation& de,
+		const TexCoordEquation& tc, const TexCoordEquation& lm_eq, const float lm_shift[2], const Vec2 pts[3],
+		const LiteMip& tex, const float dyn[3], int depth);
 	struct ModelVertex3d
 	{
 		Vec3 pos;

@@ -1505,6 +1505,69 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 			sc.sprites.push_back(e);
 		}
 	}
+	if (cfg.num_decals)
+	{
+		// Decals (own generator) on the walls and floors of the rooms, the cube's -x axis along the surface
+		// normal: textures of their own, every blending mode, some lit by the lightmap.
+		Rng drng(cfg.seed ^ 0xDECA1u);
+		const uint32_t first_texture = uint32_t(sc.lite_mips.size() / NUM_MIPS);
+		const uint32_t sizes[3][2] = {{64, 64}, {64, 32}, {32, 64}};
+		for (int k = 0; k < 3; ++k) make_sprite_texture(drng, sizes[k][0], sizes[k][1], k == 2, sc);
+		sc.leaf_decals.assign(sc.leafs.size(), {});
+		const float pi = 3.14159265358979f;
+		for (uint32_t i = 0; i < cfg.num_decals; ++i)
+		{
+			const Room& r = b.rooms[drng.below(uint32_t(b.rooms.size()))];
+			DecalEntity d;
+			const uint32_t t = drng.below(3);
+			d.texture = first_texture + t;
+			d.blending_mode = t == 2 ? uint32_t(SW_BLEND_ALPHA_TEST) : drng.below(5);
+			d.scale = v3(drng.uniform(4.0f, 16.0f), drng.uniform(12.0f, 48.0f), drng.uniform(12.0f, 48.0f));
+			const float ext = std::fmax(d.scale.y, d.scale.z) + 8.0f;
+			// the surface: 0..3 the walls at x0, x1, y0, y1 (cube +x into the wall), 4 the floor
+			const uint32_t side = drng.below(5);
+			Quat facing;
+			if (side == 0) facing = quat_from_angle_z(pi), d.position = v3(r.x0, drng.uniform(r.y0 + ext, r.y1 - ext), drng.uniform(ext, r.h - ext));
+			else if (side == 1) facing = quat_from_angle_z(0.0f), d.position = v3(r.x1, drng.uniform(r.y0 + ext, r.y1 - ext), drng.uniform(ext, r.h - ext));
+			else if (side == 2) facing = quat_from_angle_z(-0.5f * pi), d.position = v3(drng.uniform(r.x0 + ext, r.x1 - ext), r.y0, drng.uniform(ext, r.h - ext));
+			else if (side == 3) facing = quat_from_angle_z(0.5f * pi), d.position = v3(drng.uniform(r.x0 + ext, r.x1 - ext), r.y1, drng.uniform(ext, r.h - ext));
+			else facing = quat_from_angle_y(0.5f * pi), d.position = v3(drng.uniform(r.x0 + ext, r.x1 - ext), drng.uniform(r.y0 + ext, r.y1 - ext), 0.0f);
+			// a turn of the texture about the cube's x axis
+			const float roll = drng.uniform(-pi, pi);
+			d.rotation = quat_mul(facing, Quat{std::cos(roll * 0.5f), v3(std::sin(roll * 0.5f), 0.0f, 0.0f)});
+			d.lightmap_light_scale = drng.below(3) ? drng.uniform(0.5f, 1.5f) : 0.0f;
+			for (int c = 0; c < 3; ++c) d.light_add[c] = drng.uniform(0.0f, 0.5f);
+			// position_object_bbox (dynamic_objects_index.rs:159-205): the leafs the cube's convex hull reaches
+			Mat4 m = mat4_from_quat(d.rotation);
+			m.c[0] = m.c[0] * d.scale.x;
+			m.c[1] = m.c[1] * d.scale.y;
+			m.c[2] = m.c[2] * d.scale.z;
+			m.c[3] = v4(d.position.x, d.position.y, d.position.z, 1.0f);
+			Vec3 corners[8];
+			for (int k = 0; k < 8; ++k)
+				corners[k] = truncate(m * v4((k & 4) ? 1.0f : -1.0f, (k & 2) ? 1.0f : -1.0f, (k & 1) ? 1.0f : -1.0f, 1.0f));
+			const uint32_t id = uint32_t(sc.decals.size());
+			std::vector<uint32_t> stack{sc.root_node()};
+			while (!stack.empty())
+			{
+				const uint32_t node = stack.back();
+				stack.pop_back();
+				if (node >= FIRST_LEAF_INDEX)
+				{
+					sc.leaf_decals[node - FIRST_LEAF_INDEX].push_back(id);
+					continue;
+				}
+				const BspNode& nd = sc.nodes[node];
+				uint32_t front = 0;
+				for (const Vec3& v : corners)
+					if (dot(nd.plane.vec, v) > nd.plane.dist) ++front;
+				// the recursion's order (front child first): pushed back child first
+				if (front < 8) stack.push_back(nd.children[1]);
+				if (front > 0) stack.push_back(nd.children[0]);
+			}
+			sc.decals.push_back(d);
+		}
+	}
 	add_dynamic_lights(cfg, rng, sc);
 	return true;
 }

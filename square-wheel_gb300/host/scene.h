@@ -94,6 +94,7 @@ struct Material
 	float emissive_light[3] = {1.0f, 1.0f, 1.0f};
 	bool skybox = false; // SpecialMaterialEffect::Skybox: polygons only mark where the sky shows
 	bool shadow = true;  // casts shadows (material.rs:50-53)
+	bool decals = true;  // decals are drawn on its polygons (material.rs)
 	float scroll_speed[2] = {0.0f, 0.0f}; // Material::scroll_speed, texels of mip 0 per second
 	uint32_t texture_size = 0;            // mip-0 width = height
 	int32_t next_frame = -1;              // framed_animation.next_material_name as a material index, -1: none
@@ -184,6 +185,20 @@ struct SpriteEntity
 	float light_color[3];
 };
 
+// A decal (Decal, src/square_wheel/frame_info.rs): the cube [-1, 1]^3 of the object matrix
+// (position, rotation, scale) projected along its -x axis onto the polygons it cuts, with a lite texture
+// spanning its y and z extent, lit by light_add plus lightmap_light_scale times the polygon's lightmap
+// and the dynamic light at its position; `leafs`: the leafs its cube reaches (position_object_bbox).
+struct DecalEntity
+{
+	Vec3 position;
+	Quat rotation;
+	Vec3 scale;
+	uint32_t texture, blending_mode;
+	float lightmap_light_scale;
+	float light_add[3];
+};
+
 // One mip of a TextureLite (Color32 pixels, src/square_wheel/textures.rs:89-91) in Scene::lite_pixels.
 struct LiteMip
 {
@@ -226,6 +241,7 @@ struct SceneConfig
 	uint32_t model_triangles = 2000;  // triangles per model mesh (about)
 	uint32_t model_frames = 8;        // animation keyframes per mesh
 	uint32_t num_sprites = 0;         // sprites in the rooms (all four orientations, several blending modes)
+	uint32_t num_decals = 0;          // decals on the rooms' walls and floors
 	uint32_t turb_materials = 0;      // the last base materials but layered_materials have a turbulence effect
 	uint32_t layered_materials = 0;   // the last this many base materials are layered animations
 };
@@ -267,6 +283,9 @@ struct Scene
 	// Sprites and the sprites of each leaf; their textures are lite textures after the model skins.
 	std::vector<SpriteEntity> sprites;
 	std::vector<std::vector<uint32_t>> leaf_sprites;
+	// Decals and the decals of each leaf, in decal order; their textures are lite textures too.
+	std::vector<DecalEntity> decals;
+	std::vector<std::vector<uint32_t>> leaf_decals;
 	// A scene loaded from a compiled map keeps its compressed lightmap lumps (4 bytes per simple
 	// element, 13 per directional element, as the file holds them) for upload and decompression on the
 	// GPU; empty for generated scenes.

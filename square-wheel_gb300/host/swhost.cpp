@@ -142,8 +142,10 @@ int scene_config_from(const SwhSceneConfig* c, SceneConfig& cfg)
 	cfg.model_frames = c->model_frames ? c->model_frames : 8;
 	cfg.turb_materials = c->turb_materials;
 	cfg.num_sprites = c->num_sprites;
+	cfg.num_decals = c->num_decals;
 	cfg.layered_materials = c->layered_materials;
-	if (cfg.num_models > 100000 || cfg.model_triangles > 200000 || cfg.model_frames > 256 || cfg.num_sprites > 1000000)
+	if (cfg.num_models > 100000 || cfg.model_triangles > 200000 || cfg.model_frames > 256 || cfg.num_sprites > 1000000 ||
+		cfg.num_decals > 1000000)
 	{
 		g_error = "too many models, model triangles, frames or sprites";
 		return SW_ERR_INVALID_ARGUMENT;
@@ -588,9 +590,9 @@ int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFra
 	float frame_duration_s, const float color_modulate[3], void* dst, uint32_t pitch, int dst_is_device)
 {
 	if (!r || (post && (!dst || !color_modulate))) return SW_ERR_INVALID_ARGUMENT;
-	// The GPU-side preparation emits each leaf's polygons only; a scene with triangle models or sprites
+	// The GPU-side preparation emits each leaf's polygons only; a scene with triangle models, sprites or decals
 	// (drawn after their leaf's polygons) takes the host-prepared draw list.
-	if (r->gpu_prep && r->scene->scene.models.empty() && r->scene->scene.sprites.empty())
+	if (r->gpu_prep && r->scene->scene.models.empty() && r->scene->scene.sprites.empty() && r->scene->scene.decals.empty())
 	{
 		int st = swh_frame_prepare_view(r->frame, frame_index, o);
 		if (st) return st;

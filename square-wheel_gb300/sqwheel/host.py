@@ -26,6 +26,7 @@ class SceneConfig(ctypes.Structure):
         ("camera_pitch", ctypes.c_float), ("shadowed_lights", ctypes.c_uint32), ("scrolling_materials", ctypes.c_uint32),
         ("animated_materials", ctypes.c_uint32), ("projector_lights", ctypes.c_uint32), ("num_models", ctypes.c_uint32), ("model_triangles", ctypes.c_uint32),
         ("model_frames", ctypes.c_uint32), ("turb_materials", ctypes.c_uint32), ("layered_materials", ctypes.c_uint32), ("num_sprites", ctypes.c_uint32),
+        ("num_decals", ctypes.c_uint32),
     ]
 
 

@@ -115,3 +115,33 @@ def test_model_frames(gpu_ok, fmt):
             assert np.array_equal(want, got), f"frame {fi}: {(want != got).sum()} pixels differ"
     finally:
         hr.close()
+
+
+@pytest.mark.parametrize("fmt", [abi.SW_PIXEL_C32, abi.SW_PIXEL_C64])
+def test_decal_and_sprite_frames(gpu_ok, fmt):
+    """Whole frames with decals (cut out of the polygons they cover, subdivided, lightmap-lit:
+    draw_polygon_decals) and sprites (every orientation, tessellated near the camera: draw_sprite) among
+    animated models, through the host renderer and one frame graph, against the oracle's frames from
+    the same host arrays."""
+    from sqwheel import host
+    scene = host.Scene(**dict(host.SMALL_MAP, num_models=8, num_sprites=60, num_decals=300, num_dynamic_lights=3))
+    st = scene.static_data()
+    lite = scene.lite_textures()
+    hr = host.HostRenderer(scene)
+    fr = host.Frame(scene)
+    dt = np.uint64 if fmt == abi.SW_PIXEL_C64 else np.uint32
+    opts = host.frame_options(640, 480, fmt, directional=False)
+    want = np.zeros((480, 640), dt)
+    triangles = 0
+    try:
+        for fi in (0, 6, 20, 21, 40, 55):
+            fr.prepare(fi, opts)
+            triangles += fr.model_triangles
+            arena = oracle.build_surfaces(st, fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=8)
+            assert oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, want, tri_vertices=fr.tri_vertices, lite=lite) == 0
+            got = np.zeros((480, 640), dt)
+            hr.render_frame(fi, opts, out=got)
+            assert np.array_equal(want, got), f"frame {fi}: {(want != got).sum()} pixels differ"
+        assert triangles > 200
+    finally:
+        hr.close()
