@@ -499,11 +499,19 @@ typedef struct SwViewLeaf {
 #define SW_LEAF_NOT_DRAWN 0xFFFFFFFFu
 
 /* One material's state this frame (MapMaterialsProcessor, map_materials_processor.rs:174-247, 305-334):
- * the texture its polygons show (framed animation: textures_mapping_table's current frame) and that
- * frame's scrolling shift in texels of mip 0 (get_texture_shift). */
+ * the texture its polygons show (framed animation: textures_mapping_table's current frame; a generative
+ * effect's output texture) and that frame's scrolling shift in texels of mip 0 (get_texture_shift), and
+ * every other material property the renderer reads through the mapping table (get_material,
+ * get_emissive_texture): the SW_POLY_* flags (draw, sky, diffuse layer, shadow) of the current frame's
+ * material, its blending mode, and its emissive texture (SW_NO_EMISSIVE: none) with the light. These
+ * replace the polygon's own (SwMapPolygon) for every polygon of the material. */
 typedef struct SwMaterialFrame {
 	int32_t shift[2];
 	uint32_t texture; /* texture_mip = texture * 5 + mip */
+	uint32_t flags;
+	uint32_t blending_mode;
+	uint32_t emissive_texture;
+	float emissive_light[3];
 	uint32_t reserved;
 } SwMaterialFrame;
 

@@ -157,7 +157,11 @@ __device__ void prep_pair(const PrepArgs& a, const PrepFrame& frame, uint32_t nu
 	// both warps: back-face and material test, the transformed vertices (one per lane)
 	const Mat4 planes_matrix = load_mat4(frame.planes);
 	const Vec4 plane_transformed = planes_matrix * swhost::extend(swhost::poly_vec3(p.plane), -p.plane[3]);
-	const uint32_t flags = p.flags;
+	// the material's state this frame: its current animation frame's texture, shift, flags, blending and
+	// emissive layer (get_material / get_texture / get_emissive_texture through the mapping table)
+	const bool animated = p.texture < frame.num_material_frames;
+	const SwMaterialFrame* mf = animated ? a.material_frames + p.texture : nullptr;
+	const uint32_t flags = animated ? mf->flags : p.flags;
 	if (plane_transformed.w <= 0.0f || !(flags & SW_POLY_DRAW))
 	{
 		if (role == 1 && lane == 0) key = PrepKey{0ull, 0u, 0u, 0u, 0};
@@ -179,16 +183,15 @@ __device__ void prep_pair(const PrepArgs& a, const PrepFrame& frame, uint32_t nu
 		const uint32_t leaf_first_light = leaf.first_light, leaf_num_lights = leaf.num_lights;
 		const uint32_t my_light = lane < leaf_num_lights ? uint32_t(a.leaf_lights[leaf_first_light + lane]) : 0u;
 		const SwLight light0 = a.lights[lane < leaf_num_lights ? my_light : 0u];
-		const bool diffuse = (flags & SW_POLY_DIFFUSE_LAYER) != 0, emissive = p.emissive_texture != SW_NO_EMISSIVE;
-		// the material's state this frame: its current animation frame's texture and scrolling shift
-		const bool animated = p.texture < frame.num_material_frames;
-		const uint32_t texture = animated ? a.material_frames[p.texture].texture : p.texture;
+		const uint32_t emissive_texture = animated ? mf->emissive_texture : p.emissive_texture;
+		const bool diffuse = (flags & SW_POLY_DIFFUSE_LAYER) != 0, emissive = emissive_texture != SW_NO_EMISSIVE;
+		const uint32_t texture = animated ? mf->texture : p.texture;
 		SwTextureMip tex_mip{};
 		SwEmissiveMip em_mip{};
 		if (lane < swhost::PREP_NUM_MIPS)
 		{
 			if (diffuse) tex_mip = a.texture_mips[texture * swhost::PREP_NUM_MIPS + lane];
-			if (emissive) em_mip = a.emissive_mips[p.emissive_texture * swhost::PREP_NUM_MIPS + lane];
+			if (emissive) em_mip = a.emissive_mips[emissive_texture * swhost::PREP_NUM_MIPS + lane];
 		}
 		Vec3 planes[8];
 		load_planes(leaf.clip_planes, planes);
@@ -290,13 +293,7 @@ __device__ void prep_pair(const PrepArgs& a, const PrepFrame& frame, uint32_t nu
 		// build_polygons_surfaces: descriptor, the leaf's lights that reach the polygon (in order, up to 6)
 		// and the surface build's record (its texel offset is the compaction's)
 		SwSurfaceDesc d;
-		int32_t shift[2] = {0, 0}; // get_texture_shift of the polygon's material
-		if (animated)
-		{
-			shift[0] = a.material_frames[p.texture].shift[0];
-			shift[1] = a.material_frames[p.texture].shift[1];
-		}
-		swhost::make_surface_desc(p, sp, 0, a.directional != 0, a.simple_lightmaps != 0, shift, texture, d);
+		swhost::make_surface_desc(p, sp, 0, a.directional != 0, a.simple_lightmaps != 0, mf, d);
 		if (diffuse)
 			for (uint32_t base = 0; base < leaf_num_lights && d.num_lights < SW_MAX_POLYGON_LIGHTS; base += 32)
 			{
@@ -382,7 +379,7 @@ __device__ void prep_pair(const PrepArgs& a, const PrepFrame& frame, uint32_t nu
 		const Vec2 p_min = shfl(v, min_i < 0 ? 0 : min_i), p_max = shfl(v, max_i < 0 ? 0 : max_i);
 		SwDrawCmd dc = SwDrawCmd{};
 		dc.vertex_count = n;
-		dc.blend = p.blending_mode;
+		dc.blend = animated ? mf->blending_mode : p.blending_mode;
 		dc.tex_size[0] = sp.size[0];
 		dc.tex_size[1] = sp.size[1];
 		dc.tex_source = SW_TEXSRC_SURFACE;

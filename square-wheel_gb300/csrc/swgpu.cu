@@ -1988,8 +1988,15 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "non-finite camera matrices");
 	if (f.num_material_frames > (1u << 20)) return fail(ctx, SW_ERR_LIMIT, "too many material frames");
 	for (uint32_t i = 0; i < f.num_material_frames; ++i)
-		if (uint64_t(f.material_frames[i].texture) * 5 + 4 >= ctx->h_texture_mips.size())
-			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "material %u: frame texture %u has no mips", i, f.material_frames[i].texture);
+	{
+		const SwMaterialFrame& m = f.material_frames[i];
+		if (uint64_t(m.texture) * 5 + 4 >= ctx->h_texture_mips.size())
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "material %u: frame texture %u has no mips", i, m.texture);
+		if (m.emissive_texture != SW_NO_EMISSIVE && uint64_t(m.emissive_texture) * 5 + 4 >= ctx->h_emissive_mips.size())
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "material %u: bad emissive texture", i);
+		if (m.blending_mode > SW_BLEND_ALPHA_BLEND) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "material %u: bad blending mode", i);
+		if (!all_finite(m.emissive_light, 3)) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "material %u: non-finite emissive light", i);
+	}
 	if (f.postprocess && f.params.pixel_format != SW_PIXEL_C64)
 		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocessing needs a colour64 frame");
 	if (f.dst && f.dst_pitch < f.params.width) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");

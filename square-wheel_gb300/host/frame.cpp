@@ -90,6 +90,14 @@ void ClippingPolygon::get_clip_planes(Vec3 out[8]) const
 FramePrep::FramePrep(const Scene& scene) : sc(scene)
 {
 	sc.map_polygons(map_polygons);
+	map_polygons_base = map_polygons;
+	// the polygons of every material with a framed animation (their material fields follow its frames)
+	material_polygons.assign(sc.materials.size(), {});
+	for (uint32_t pi = 0; pi < uint32_t(sc.polygons.size()); ++pi)
+	{
+		const uint32_t m = sc.polygons[pi].texture;
+		if (m < sc.materials.size() && sc.materials[m].next_frame >= 0) material_polygons[m].push_back(pi);
+	}
 	leaf_sky_first.assign(sc.leafs.size() + 1, 0);
 	for (uint32_t i = 0; i < sc.leafs.size(); ++i)
 	{
@@ -527,7 +535,7 @@ void FramePrep::build_surface_descs()
 		sp.tc_min[1] = pd.tc_min[1];
 		SwSurfaceDesc& d = surfaces[si];
 		const SwMaterialFrame& mf = material_frames[p.texture];
-		make_surface_desc(p, sp, pd.offset, directional, simple_lightmaps, mf.shift, mf.texture, d);
+		make_surface_desc(p, sp, pd.offset, directional, simple_lightmaps, &mf, d);
 		if (p.flags & SW_POLY_DIFFUSE_LAYER)
 			for (uint32_t li : leaf_lights[sc.polygon_leaf[pi]])
 				if (polygon_is_affected_by_light(p, lights[li], li < light_shadows.size() ? &light_shadows[li] : nullptr))
@@ -1534,13 +1542,28 @@ void FramePrep::update_materials()
 	material_frames.resize(n);
 	for (uint32_t m = 0; m < n; ++m)
 	{
-		// get_texture (:311-327): the current frame's generated texture when it has a generative effect
+		// get_texture (:311-327): the current frame's generated texture when it has a generative effect;
+		// get_material and get_emissive_texture (:305-309, 336-360): the current frame's properties
 		const Material& cur = sc.materials[mapping[m]];
-		material_frames[m].shift[0] = shift[2 * mapping[m]];
-		material_frames[m].shift[1] = shift[2 * mapping[m] + 1];
-		material_frames[m].texture = cur.effect_texture >= 0 ? uint32_t(cur.effect_texture) : mapping[m];
-		material_frames[m].reserved = 0;
+		SwMaterialFrame& f = material_frames[m];
+		f.shift[0] = shift[2 * mapping[m]];
+		f.shift[1] = shift[2 * mapping[m] + 1];
+		f.texture = cur.effect_texture >= 0 ? uint32_t(cur.effect_texture) : mapping[m];
+		f.flags = Scene::material_polygon_flags(cur);
+		f.blending_mode = cur.blending_mode;
+		f.emissive_texture = cur.emissive >= 0 ? uint32_t(cur.emissive) : SW_NO_EMISSIVE;
+		for (int c = 0; c < 3; ++c) f.emissive_light[c] = cur.emissive_light[c];
+		f.reserved = 0;
 		if (cur.effect != Material::NO_EFFECT) animated = true;
+		// the polygons the host prepares read the frame's material fields
+		for (uint32_t pi : material_polygons[m])
+		{
+			SwMapPolygon& p = map_polygons[pi];
+			p.flags = f.flags;
+			p.blending_mode = f.blending_mode;
+			p.emissive_texture = f.emissive_texture;
+			for (int c = 0; c < 3; ++c) p.emissive_light[c] = f.emissive_light[c];
+		}
 	}
 	update_texture_effects();
 }

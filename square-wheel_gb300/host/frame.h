@@ -110,8 +110,12 @@ public:
 
 	const CameraMatrices& camera() const { return cam; }
 
-	// The map's polygons as the preparation reads them (uploaded by sw_set_map for the GPU side).
+	// The map's polygons as the preparation reads them this frame (the material fields of animated
+	// materials follow their current frame), and as the map holds them (uploaded by sw_set_map: the GPU
+	// side applies the frame's SwMaterialFrame itself).
 	std::vector<SwMapPolygon> map_polygons;
+	std::vector<SwMapPolygon> map_polygons_base;
+	std::vector<std::vector<uint32_t>> material_polygons;
 
 	std::vector<SwSurfaceDesc> surfaces;
 	uint64_t total_texels = 0;

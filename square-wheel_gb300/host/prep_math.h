@@ -451,18 +451,23 @@ SWH_HD inline uint64_t max_surface_texels(const SwMapPolygon& p)
 // its light list. `directional`: directional lightmaps in use; `simple_lightmaps`: the map has simple ones.
 // `shift`: get_texture_shift of the polygon's material (texels of mip 0), applied >> mip
 // (partial_renderer.rs:1687-1693); `texture`: the material's current animation frame (get_texture).
+// `mf`: the polygon's material this frame (texture, scrolling shift, flags and emissive layer of the
+// current animation frame), or NULL for the polygon's own material, unshifted.
 SWH_HD inline void make_surface_desc(const SwMapPolygon& p, const SurfacePrep& sp, uint64_t out_offset, bool directional,
-	bool simple_lightmaps, const int32_t shift[2], uint32_t texture, SwSurfaceDesc& d)
+	bool simple_lightmaps, const SwMaterialFrame* mf, SwSurfaceDesc& d)
 {
 	d = SwSurfaceDesc{};
-	const int32_t shift_mip[2] = {shift[0] >> sp.mip, shift[1] >> sp.mip};
+	const int32_t shift_mip[2] = {mf ? mf->shift[0] >> sp.mip : 0, mf ? mf->shift[1] >> sp.mip : 0};
+	const uint32_t texture = mf ? mf->texture : p.texture, flags = mf ? mf->flags : p.flags;
+	const uint32_t emissive_texture = mf ? mf->emissive_texture : p.emissive_texture;
+	const float* emissive_light = mf ? mf->emissive_light : p.emissive_light;
 	d.size[0] = sp.size[0];
 	d.size[1] = sp.size[1];
 	d.tc_start[0] = sp.tc_min[0] + shift_mip[0];
 	d.tc_start[1] = sp.tc_min[1] + shift_mip[1];
 	d.out_offset = out_offset;
 	d.emissive_mip = SW_NO_EMISSIVE;
-	if (p.flags & SW_POLY_DIFFUSE_LAYER)
+	if (flags & SW_POLY_DIFFUSE_LAYER)
 	{
 		d.flags = SW_SURF_DIFFUSE_LAYER;
 		// get_basis_vecs_for_mip + texture shift correction (surfaces.rs:49-63, partial_renderer.rs:1736-1740)
@@ -491,12 +496,12 @@ SWH_HD inline void make_surface_desc(const SwMapPolygon& p, const SurfacePrep& s
 		d.lightmap_scale_log2 = PREP_LIGHTMAP_SCALE_LOG2 - sp.mip;
 		d.lightmap_offset = (directional || simple_lightmaps) ? p.lightmap_data_offset : SW_NO_LIGHTMAP;
 	}
-	if (p.emissive_texture != SW_NO_EMISSIVE)
+	if (emissive_texture != SW_NO_EMISSIVE)
 	{
-		d.emissive_mip = p.emissive_texture * PREP_NUM_MIPS + sp.mip;
-		d.emissive_light[0] = p.emissive_light[0];
-		d.emissive_light[1] = p.emissive_light[1];
-		d.emissive_light[2] = p.emissive_light[2];
+		d.emissive_mip = emissive_texture * PREP_NUM_MIPS + sp.mip;
+		d.emissive_light[0] = emissive_light[0];
+		d.emissive_light[1] = emissive_light[1];
+		d.emissive_light[2] = emissive_light[2];
 	}
 }
 

@@ -988,8 +988,7 @@ void Scene::map_polygons(std::vector<SwMapPolygon>& out) const
 		o.num_vertices = p.num_vertices;
 		o.texture = p.texture;
 		o.lightmap_data_offset = p.lightmap_data_offset;
-		o.flags = (m.draw ? SW_POLY_DRAW : 0u) | (m.skybox ? SW_POLY_SKY : 0u) | ((m.light && m.has_diffuse) ? SW_POLY_DIFFUSE_LAYER : 0u) |
-			(m.shadow ? SW_POLY_SHADOW : 0u);
+		o.flags = material_polygon_flags(m);
 		o.blending_mode = m.blending_mode;
 		o.emissive_texture = m.emissive >= 0 ? uint32_t(m.emissive) : SW_NO_EMISSIVE;
 		o.emissive_light[0] = m.emissive_light[0], o.emissive_light[1] = m.emissive_light[1], o.emissive_light[2] = m.emissive_light[2];
@@ -1395,6 +1394,16 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 				Material f = sc.materials[m];
 				f.next_frame = k == 0 ? first + 1 : int32_t(m);
 				f.frame_duration = durations[k + 1];
+				// every property can change from frame to frame: the first extra frame glows (an emissive
+				// layer of its own), the second is averaged with what is behind it
+				if (k == 0)
+				{
+					f.emissive = int32_t(sc.emissive_mips.size() / NUM_MIPS);
+					make_emissive_texture(arng, cfg.texture_size, sc);
+					f.emissive_light[0] = 1.5f, f.emissive_light[1] = 0.75f, f.emissive_light[2] = 0.25f;
+				}
+				else
+					f.blending_mode = SW_BLEND_AVERAGE;
 				sc.materials.push_back(f);
 			}
 			sc.materials[m].next_frame = first;

@@ -303,6 +303,12 @@ struct Scene
 	}
 	// A projector light's rotation (yaw about the vertical axis, then pitch) and fov at time t (seconds).
 	void projector_pose(uint32_t light, float t, Quat& rotation, float& fov) const;
+	// The SW_POLY_* flags a material gives its polygons (draw, sky, diffuse layer, shadow).
+	static uint32_t material_polygon_flags(const Material& m)
+	{
+		return (m.draw ? SW_POLY_DRAW : 0u) | (m.skybox ? SW_POLY_SKY : 0u) | ((m.light && m.has_diffuse) ? SW_POLY_DIFFUSE_LAYER : 0u) |
+			(m.shadow ? SW_POLY_SHADOW : 0u);
+	}
 	// Polygons with their basis and material fields (SwMapPolygon), in polygon order.
 	void map_polygons(std::vector<SwMapPolygon>& out) const;
 	SwCreateInfo create_info(uint32_t device) const;

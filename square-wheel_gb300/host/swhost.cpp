@@ -369,8 +369,8 @@ int swh_frame_map(const SwhFrame* f, const SwMapPolygon** out_polygons, uint32_t
 	uint32_t* out_num_vertices)
 {
 	if (!f || !out_polygons || !out_num_polygons || !out_vertices || !out_num_vertices) return SW_ERR_INVALID_ARGUMENT;
-	*out_polygons = f->prep.map_polygons.data();
-	*out_num_polygons = uint32_t(f->prep.map_polygons.size());
+	*out_polygons = f->prep.map_polygons_base.data();
+	*out_num_polygons = uint32_t(f->prep.map_polygons_base.size());
 	*out_vertices = reinterpret_cast<const float*>(f->scene.vertices.data());
 	*out_num_vertices = uint32_t(f->scene.vertices.size());
 	return SW_OK;
@@ -542,7 +542,7 @@ int swh_renderer_create(const SwhScene* s, uint32_t device, SwhRenderer** out)
 		delete r;
 		return SW_ERR_OUT_OF_MEMORY;
 	}
-	const std::vector<SwMapPolygon>& mp = r->frame->prep.map_polygons;
+	const std::vector<SwMapPolygon>& mp = r->frame->prep.map_polygons_base;
 	if ((st = sw_set_map(r->ctx, mp.data(), uint32_t(mp.size()), reinterpret_cast<const float*>(s->scene.vertices.data()),
 			 uint32_t(s->scene.vertices.size()))) != SW_OK)
 	{

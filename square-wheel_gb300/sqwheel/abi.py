@@ -68,7 +68,8 @@ LIGHT_SHADOW = np.dtype([("kind", "<u4"), ("size", "<u4"), ("offset", "<u8"), ("
                          ("basis_z", "<f4", 3), ("reserved", "<u4")], align=True)
 DEPTH_DRAW = np.dtype([("first_vertex", "<u4"), ("vertex_count", "<u4"), ("map_size", "<u4"), ("reserved", "<u4"),
                        ("map_offset", "<u8"), ("depth_eq", "<f4", 3), ("reserved2", "<u4")], align=True)
-MATERIAL_FRAME = np.dtype([("shift", "<i4", 2), ("texture", "<u4"), ("reserved", "<u4")], align=True)
+MATERIAL_FRAME = np.dtype([("shift", "<i4", 2), ("texture", "<u4"), ("flags", "<u4"), ("blending_mode", "<u4"),
+                           ("emissive_texture", "<u4"), ("emissive_light", "<f4", 3), ("reserved", "<u4")], align=True)
 SHADOW_SIDE = np.dtype([("view_matrix", "<f4", 16), ("planes_matrix", "<f4", 16), ("map_size", "<u4"),
                         ("reserved", "<u4"), ("map_offset", "<u8")], align=True)
 SHADOW_LEAF = np.dtype([("side", "<u4"), ("first_polygon", "<u4"), ("num_polygons", "<u4"), ("reserved", "<u4"),

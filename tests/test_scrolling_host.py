@@ -106,5 +106,11 @@ def test_framed_animations_follow_the_mapping_table(built_libs):
                 seen.add(mapping[material] - material if mapping[material] == material else 1 + (mapping[material] - 16) % 2)
             sa_rest = sa.copy()
             sa_rest["texture_mip"] = sb["texture_mip"]
+            if material < animated and mapping[material] != material and (mapping[material] - 16) % 2 == 0:
+                # the cycle's first extra frame carries an emissive layer of its own (get_emissive_texture
+                # through the mapping table)
+                assert int(sb["emissive_mip"]) != 0xFFFFFFFF and int(sb["emissive_mip"]) % 5 == mip
+                assert list(sb["emissive_light"]) == [1.5, 0.75, 0.25]
+                sa_rest["emissive_mip"], sa_rest["emissive_light"] = sb["emissive_mip"], sb["emissive_light"]
             assert sa_rest.tobytes() == sb.tobytes()
     assert seen == {0, 1, 2}  # every frame of the cycle was shown
