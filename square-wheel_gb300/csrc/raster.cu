@@ -57,24 +57,16 @@ __device__ __forceinline__ int64_t f2i64(float x) { return __float2ll_rz(x); }
 __device__ __forceinline__ int64_t w64add(int64_t a, int64_t b) { return int64_t(uint64_t(a) + uint64_t(b)); }
 __device__ __forceinline__ int64_t w64mul(int64_t a, int64_t b) { return int64_t(uint64_t(a) * uint64_t(b)); }
 
-struct SetupState
-{
-	const SwDrawCmd* d;
-	int32_t height;
-	RasterPart* parts;
-	uint32_t num_parts;
-};
-
 // The draw_func body up to the row loop: first-row edge positions (rasterizer.rs:316-320) and, for
-// the affine mode, the per-part texture coordinate edges (rasterizer.rs:597-682).
-__device__ void emit_part(SetupState& st, Fixed16 y_start, Fixed16 y_end, Fixed16 xl_start, Fixed16 dxl,
-	Fixed16 xr_start, Fixed16 dxr)
+// the affine mode, the per-part texture coordinate edges (rasterizer.rs:597-682). False when the part
+// has no row in the frame (the reference's loop runs no iteration).
+__device__ bool make_part(const SwDrawCmd& d, int32_t height, Fixed16 y_start, Fixed16 y_end, Fixed16 xl_start, Fixed16 dxl,
+	Fixed16 xr_start, Fixed16 dxr, RasterPart& p)
 {
 	const int32_t y_start_int = max(round_to_int(y_start), 0);
-	const int32_t y_end_int = min(round_to_int(y_end), st.height);
-	if (y_start_int >= y_end_int || st.num_parts >= SW_RASTER_MAX_PARTS) return;
+	const int32_t y_end_int = min(round_to_int(y_end), height);
+	if (y_start_int >= y_end_int) return false;
 	const Fixed16 y_start_delta = wsub(wadd(int_to_fixed16(y_start_int), FIXED16_HALF), y_start);
-	RasterPart p;
 	p.y_start_int = y_start_int;
 	p.y_end_int = y_end_int;
 	p.x_left0 = wadd(wadd(xl_start, fx_mul(y_start_delta, dxl)), FIXED16_HALF);
@@ -83,7 +75,6 @@ __device__ void emit_part(SetupState& st, Fixed16 y_start, Fixed16 y_end, Fixed1
 	p.dx_dy_right = dxr;
 	p.tc_left0[0] = p.tc_left0[1] = p.tc_right0[0] = p.tc_right0[1] = 0;
 	p.d_tc_left[0] = p.d_tc_left[1] = p.d_tc_right[0] = p.d_tc_right[1] = 0;
-	const SwDrawCmd& d = *st.d;
 	if (d.mode == SW_RASTER_AFFINE)
 	{
 		const float* de = d.depth_eq;
@@ -118,18 +109,26 @@ __device__ void emit_part(SetupState& st, Fixed16 y_start, Fixed16 y_end, Fixed1
 			p.tc_right0[i] = wadd(tsr, fx_mul(y_start_delta, p.d_tc_right[i]));
 		}
 	}
-	st.parts[st.num_parts++] = p;
+	return true;
 }
 
-// Edge walk of fill_polygon_impl_2_static_params (rasterizer.rs:160-270) for one draw.
-__device__ uint32_t edge_walk(const SwDrawCmd& d, const SwVertex16* vtx, int32_t height, RasterPart* parts)
+// Edge walk of fill_polygon_impl_2_static_params (rasterizer.rs:160-270) for one draw, by one warp.
+// The walk's control flow (which edges pair up between which y values) is cheap and sequential: lane 0
+// records its steps. The costly part of every step - the 64-bit fixed-point divisions and, for affine
+// draws, the texture-coordinate edges with their f32 divisions - is independent from step to step, so
+// the lanes compute the steps' parts in parallel and an in-order compaction keeps the parts that have
+// rows, at most SW_RASTER_MAX_PARTS of them, in the walk's order.
+struct WalkStep
 {
-	SetupState st;
-	st.d = &d;
-	st.height = height;
-	st.parts = parts;
-	st.num_parts = 0;
-	const uint32_t n = d.vertex_count;
+	Fixed16 cur_y, next_y;
+	uint8_t li, nli, ri, nri;
+	uint32_t kind; // 1: both edges taller than half a pixel, 2: a thin part
+};
+constexpr uint32_t MAX_WALK_STEPS = 2 * SW_MAX_POLYGON_VERTICES + 2;
+
+template <class F>
+__device__ __forceinline__ void walk(const SwVertex16* vtx, uint32_t n, F&& on_step)
+{
 	uint32_t lower = 0;
 	Fixed16 min_y = vtx[0].y;
 	for (uint32_t i = 0; i < n; ++i)
@@ -140,43 +139,85 @@ __device__ uint32_t edge_walk(const SwDrawCmd& d, const SwVertex16* vtx, int32_t
 		}
 	uint32_t li = lower, ri = lower;
 	Fixed16 cur_y = min_y;
-	for (uint32_t guard = 0; guard < 2 * SW_MAX_POLYGON_VERTICES + 2; ++guard)
+	for (uint32_t guard = 0; guard < MAX_WALK_STEPS; ++guard)
 	{
 		uint32_t nli = li + n - 1;
 		if (nli >= n) nli -= n;
 		uint32_t nri = ri + 1;
 		if (nri >= n) nri -= n;
-		const SwVertex16 lv = vtx[li], nlv = vtx[nli], rv = vtx[ri], nrv = vtx[nri];
-		const Fixed16 dy_left = wsub(nlv.y, lv.y);
-		const Fixed16 dy_right = wsub(nrv.y, rv.y);
-		const Fixed16 next_y = min(nlv.y, nrv.y);
+		const Fixed16 dy_left = wsub(vtx[nli].y, vtx[li].y);
+		const Fixed16 dy_right = wsub(vtx[nri].y, vtx[ri].y);
+		const Fixed16 next_y = min(vtx[nli].y, vtx[nri].y);
+		uint32_t kind = 0;
 		if (dy_left > FIXED16_HALF && dy_right > FIXED16_HALF)
-		{
-			const Fixed16 dxl = fx_div(wsub(nlv.x, lv.x), dy_left);
-			const Fixed16 dxr = fx_div(wsub(nrv.x, rv.x), dy_right);
-			emit_part(st, cur_y, next_y, wadd(lv.x, fx_mul(dxl, wsub(cur_y, lv.y))), dxl,
-				wadd(rv.x, fx_mul(dxr, wsub(cur_y, rv.y))), dxr);
-		}
-		else if (dy_left > 0 && dy_right > 0)
-		{
-			const int32_t cur_y_int = round_to_int(cur_y);
-			const int32_t next_y_int = round_to_int(next_y);
-			if (cur_y_int < next_y_int)
-			{
-				const Fixed16 thin_y = wadd(int_to_fixed16(cur_y_int), FIXED16_HALF);
-				const Fixed16 xsl = wadd(lv.x, fx_mul_div(wsub(thin_y, lv.y), wsub(nlv.x, lv.x), dy_left));
-				const Fixed16 xsr = wadd(rv.x, fx_mul_div(wsub(thin_y, rv.y), wsub(nrv.x, rv.x), dy_right));
-				emit_part(st, cur_y, next_y, xsl, 0, xsr, 0);
-			}
-		}
+			kind = 1;
+		else if (dy_left > 0 && dy_right > 0 && round_to_int(cur_y) < round_to_int(next_y))
+			kind = 2;
+		if (kind) on_step(WalkStep{cur_y, next_y, uint8_t(li), uint8_t(nli), uint8_t(ri), uint8_t(nri), kind});
 		if (nli == nri) break;
-		if (nrv.y < nlv.y)
+		if (vtx[nri].y < vtx[nli].y)
 			ri = nri;
 		else
 			li = nli;
 		cur_y = next_y;
 	}
-	return st.num_parts;
+}
+
+// A step's part (the divisions of the walk's loop body); false when it has no row in the frame.
+__device__ __forceinline__ bool step_part(const SwDrawCmd& d, const SwVertex16* vtx, int32_t height, const WalkStep& st, RasterPart& p)
+{
+	const SwVertex16 lv = vtx[st.li], nlv = vtx[st.nli], rv = vtx[st.ri], nrv = vtx[st.nri];
+	const Fixed16 dy_left = wsub(nlv.y, lv.y), dy_right = wsub(nrv.y, rv.y);
+	if (st.kind == 1)
+	{
+		const Fixed16 dxl = fx_div(wsub(nlv.x, lv.x), dy_left);
+		const Fixed16 dxr = fx_div(wsub(nrv.x, rv.x), dy_right);
+		return make_part(d, height, st.cur_y, st.next_y, wadd(lv.x, fx_mul(dxl, wsub(st.cur_y, lv.y))), dxl,
+			wadd(rv.x, fx_mul(dxr, wsub(st.cur_y, rv.y))), dxr, p);
+	}
+	const Fixed16 thin_y = wadd(int_to_fixed16(round_to_int(st.cur_y)), FIXED16_HALF);
+	const Fixed16 xsl = wadd(lv.x, fx_mul_div(wsub(thin_y, lv.y), wsub(nlv.x, lv.x), dy_left));
+	const Fixed16 xsr = wadd(rv.x, fx_mul_div(wsub(thin_y, rv.y), wsub(nrv.x, rv.x), dy_right));
+	return make_part(d, height, st.cur_y, st.next_y, xsl, 0, xsr, 0, p);
+}
+
+// One warp: the draw's parts into `parts`; returns their count (to every lane).
+__device__ uint32_t edge_walk_warp(const SwDrawCmd& d, const SwVertex16* vtx, int32_t height, RasterPart* parts, WalkStep* steps,
+	uint32_t* s_count)
+{
+	const uint32_t lane = threadIdx.x & 31u;
+	if (lane == 0)
+	{
+		uint32_t count = 0;
+		walk(vtx, d.vertex_count, [&](const WalkStep& st) { steps[count++] = st; });
+		*s_count = count;
+	}
+	__syncwarp();
+	const uint32_t count = *s_count;
+	uint32_t np = 0;
+	for (uint32_t base = 0; base < count; base += 32)
+	{
+		const uint32_t k = base + lane;
+		RasterPart p;
+		const bool ok = k < count && step_part(d, vtx, height, steps[k], p);
+		const unsigned mask = __ballot_sync(0xFFFFFFFFu, ok);
+		const uint32_t pos = np + __popc(mask & ((1u << lane) - 1u));
+		if (ok && pos < SW_RASTER_MAX_PARTS) parts[pos] = p;
+		np += __popc(mask);
+	}
+	__syncwarp();
+	return np < SW_RASTER_MAX_PARTS ? np : SW_RASTER_MAX_PARTS;
+}
+
+// The same walk by one thread (the shadow-map kernels draw one candidate per warp or per block and
+// keep their shared memory small): the steps and their parts one after another.
+__device__ uint32_t edge_walk(const SwDrawCmd& d, const SwVertex16* vtx, int32_t height, RasterPart* parts)
+{
+	uint32_t np = 0;
+	walk(vtx, d.vertex_count, [&](const WalkStep& st) {
+		if (np < SW_RASTER_MAX_PARTS && step_part(d, vtx, height, st, parts[np])) ++np;
+	});
+	return np;
 }
 
 // ---- triangles: Rasterizer::fill_triangle_impl / fill_triangle_part (rasterizer.rs:765-1292) ----
@@ -526,7 +567,8 @@ __global__ void __launch_bounds__(256) raster_setup_kernel(RasterArgs a)
 	__shared__ SwTriVertex s_tv[3];
 	__shared__ RasterPart s_parts[SW_RASTER_MAX_PARTS];
 	__shared__ DrawRows s_dr;
-	__shared__ uint32_t s_np;
+	__shared__ uint32_t s_np, s_steps_count;
+	__shared__ WalkStep s_steps[MAX_WALK_STEPS];
 	// One draw per CTA; with the draw count on the device (GPU-side preparation) a fixed grid strides.
 	const uint32_t num_draws = a.counts ? a.counts->num_draws : a.num_draws;
 	for (uint32_t di = blockIdx.x; di < num_draws; di += gridDim.x)
@@ -544,6 +586,8 @@ __global__ void __launch_bounds__(256) raster_setup_kernel(RasterArgs a)
 		else if (threadIdx.x < s_d.vertex_count && threadIdx.x < SW_MAX_POLYGON_VERTICES)
 			s_v[threadIdx.x] = a.vertices[s_d.first_vertex + threadIdx.x];
 		__syncthreads();
+		uint32_t walked = 0;
+		if (!tri && threadIdx.x < 32) walked = edge_walk_warp(s_d, s_v, a.height, s_parts, s_steps, &s_steps_count);
 		if (threadIdx.x == 0)
 		{
 			const SwDrawCmd& d = s_d;
@@ -562,7 +606,7 @@ __global__ void __launch_bounds__(256) raster_setup_kernel(RasterArgs a)
 				}
 			}
 			else
-				np = edge_walk(d, s_v, a.height, s_parts);
+				np = walked;
 			s_np = np;
 			int32_t bx0 = INT32_MAX, bx1 = INT32_MIN, by0 = INT32_MAX, by1 = INT32_MIN;
 			for (uint32_t pi = 0; pi < np; ++pi)
@@ -770,6 +814,45 @@ __device__ __forceinline__ void bloom_epilogue(const RasterArgs& a, const uint64
 		atomicAdd(&a.bloom_line_sums[(by0 + tid / 4) * 4 + tid % 4], s_ls[tid / 4][tid % 4]);
 }
 
+// raster_bin_kernel: one CTA per bin. The draws whose box meets the bin, in draw order: chunks of 256
+// draws, one box test per thread, an in-order ballot compaction, appended to the bin's list.
+__global__ void __launch_bounds__(256) raster_bin_kernel(RasterArgs a)
+{
+	__shared__ uint32_t s_counts[8];
+	const int32_t bx0 = int32_t(blockIdx.x % a.bins_x) * RASTER_BIN_W, by0 = int32_t(blockIdx.x / a.bins_x) * RASTER_BIN_H;
+	const int32_t bx1 = min(bx0 + RASTER_BIN_W, a.width), by1 = min(by0 + RASTER_BIN_H, a.height);
+	pdl_wait(); // the raster setup wrote the boxes
+	const uint32_t num_draws = a.counts ? a.counts->num_draws : a.num_draws;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	uint32_t* list = a.bin_lists + uint64_t(blockIdx.x) * a.bin_cap;
+	uint32_t total = 0;
+	for (uint32_t chunk = 0; chunk < num_draws; chunk += 256)
+	{
+		const uint32_t di = chunk + threadIdx.x;
+		bool hit = false;
+		if (di < num_draws)
+		{
+			const RasterBox b = a.boxes[di];
+			hit = b.x0 < bx1 && b.x1 > bx0 && b.y0 < by1 && b.y1 > by0 && b.x0 < b.x1 && b.y0 < b.y1;
+		}
+		const unsigned mask = __ballot_sync(0xFFFFFFFFu, hit);
+		if (lane == 0) s_counts[warp] = __popc(mask);
+		__syncthreads();
+		uint32_t base = total, sum = 0;
+#pragma unroll
+		for (int w = 0; w < 8; ++w)
+		{
+			if (w < warp) base += s_counts[w];
+			sum += s_counts[w];
+		}
+		if (hit) list[base + __popc(mask & ((1u << lane) - 1u))] = di;
+		total += sum;
+		__syncthreads(); // s_counts is rewritten by the next chunk
+	}
+	if (threadIdx.x == 0) a.bin_counts[blockIdx.x] = total;
+	pdl_trigger();
+}
+
 // Tile shapes of the tile pass (the autotuner's choice, SwTuning.raster_tile): TILE_W x TILE_H pixels,
 // 256 threads, each thread a 1 x STRIP strip of one row. Every shape gives the same frame.
 struct TileShape
@@ -821,16 +904,26 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 	unsigned int local_errors = 0, local_writes = 0;
 
 	const int lane = tid & 31, warp = tid >> 5;
-	for (uint32_t chunk = 0; chunk < num_draws; chunk += 256)
+	// the draws to scan: the tile's bin's list (draw order), or every draw
+	const uint32_t* list = nullptr;
+	uint32_t list_len = num_draws;
+	if (a.bin_lists)
+	{
+		const uint32_t bin = uint32_t(tx0 / RASTER_BIN_W) + uint32_t(ty0 / RASTER_BIN_H) * a.bins_x;
+		list = a.bin_lists + uint64_t(bin) * a.bin_cap;
+		list_len = a.bin_counts[bin];
+	}
+	for (uint32_t chunk = 0; chunk < list_len; chunk += 256)
 	{
 		// Ordered compaction of the chunk's draws whose box meets the tile; the hitting thread stages
 		// the draw's record and box.
-		const uint32_t di = chunk + tid;
+		const uint32_t k = chunk + tid;
 		bool hit = false;
 		RasterBox b{0, 0, 0, 0};
 		RasterDraw rd{};
-		if (di < num_draws)
+		if (k < list_len)
 		{
+			const uint32_t di = list ? list[k] : k;
 			b = a.boxes[di];
 			hit = b.x0 < tx1 && b.x1 > tx0 && b.y0 < ty1 && b.y1 > ty0 && b.x0 < b.x1 && b.y0 < b.y1;
 			if (hit) rd = a.rdraws[di];
@@ -1203,6 +1296,12 @@ void launch_tiles_variant(const RasterArgs& args, uint32_t pixel_format, cudaStr
 		launch_dependent(raster_tiles_kernel<PixC32, t.w, t.h, t.strip>, dim3(tiles), dim3(256), 0, stream, args);
 }
 } // namespace
+
+int launch_raster_bins(const RasterArgs& args, cudaStream_t stream)
+{
+	if (!args.bin_lists) return 0;
+	return int(launch_dependent(raster_bin_kernel, dim3(args.bins_x * args.bins_y), dim3(256), 0, stream, args));
+}
 
 int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, uint32_t variant, cudaStream_t stream)
 {

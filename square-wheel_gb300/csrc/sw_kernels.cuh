@@ -255,10 +255,22 @@ struct RasterArgs
 	uint64_t* bloom_out;
 	int32_t* bloom_line_sums;
 	uint32_t bloom_scale, bloom_w, bloom_h;
+	// Bins (raster_bin_kernel): the frame cut into RASTER_BIN_W x RASTER_BIN_H rectangles, each with the
+	// draws whose box meets it in draw order (bin_lists[bin * bin_cap + i], bin_counts[bin] of them); a
+	// tile scans its bin's list instead of every draw. NULL lists: every tile scans every draw.
+	uint32_t* bin_lists;
+	uint32_t* bin_counts;
+	uint32_t bin_cap, bins_x, bins_y;
 };
 
-// Edge walk + row setup (raster_setup, one CTA per draw), then the tile pass (raster_tiles).
+// Every tile shape divides the bin, so a tile lies in one bin.
+constexpr int32_t RASTER_BIN_W = 128, RASTER_BIN_H = 64;
+inline uint32_t raster_bins(int32_t extent, int32_t bin) { return uint32_t((extent + bin - 1) / bin); }
+
+// Edge walk + row setup (raster_setup, one CTA per draw), the bins (raster_bins, one CTA per bin), then
+// the tile pass (raster_tiles).
 int launch_raster_setup(const RasterArgs& args, cudaStream_t stream);
+int launch_raster_bins(const RasterArgs& args, cudaStream_t stream);
 // variant: tile shape index (< SW_RASTER_TILE_VARIANTS, see SwTuning); every variant gives the same frame.
 int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, uint32_t variant, cudaStream_t stream);
 

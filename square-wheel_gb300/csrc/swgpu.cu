@@ -80,6 +80,9 @@ struct SwCtx
 	// static
 	DevBuf texels, texture_mips, emissive, emissive_mips, lightmaps, dir_lightmaps;
 	DevBuf lm_compressed; // sw_set_lightmaps_compressed: the compressed lumps as uploaded
+	// the tile pass's bins (raster_bin_kernel): bins_x * bins_y lists of bin_cap draw indices and counts
+	DevBuf bin_lists, bin_counts;
+	uint32_t bin_cap = 0, bins_x = 0, bins_y = 0;
 	DevBuf skybox32, skybox64; // sw_set_skybox: the same texels in Color32 and Color64
 	DevBuf frame_in;           // sw_draw_frame: all per-frame arrays of one frame, uploaded by one copy
 	struct HostRange
@@ -244,8 +247,15 @@ RasterArgs raster_args(SwCtx* ctx)
 	a.skybox = ctx->frame.pixel_format == SW_PIXEL_C64 ? ctx->skybox64.ptr : ctx->skybox32.ptr;
 	a.framebuffer = ctx->framebuffer.ptr;
 	a.error_counter = static_cast<unsigned int*>(ctx->error_counter.ptr);
+	a.bin_lists = static_cast<uint32_t*>(ctx->bin_lists.ptr);
+	a.bin_counts = static_cast<uint32_t*>(ctx->bin_counts.ptr);
+	a.bin_cap = ctx->bin_cap;
+	a.bins_x = ctx->bins_x;
+	a.bins_y = ctx->bins_y;
 	return a;
 }
+
+
 
 void stage_begin(SwCtx* ctx, int s)
 {
@@ -308,6 +318,22 @@ int ensure(SwCtx* ctx, DevBuf& b, size_t bytes)
 		return fail(ctx, SW_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu bytes) failed: %s", want, cudaGetErrorString(e));
 	}
 	b.bytes = want;
+	return SW_OK;
+}
+
+// The bins of a width x height frame for up to `draws` draws (capacities only grow, so replayed graphs
+// keep their buffers).
+int ensure_bins(SwCtx* ctx, uint32_t width, uint32_t height, uint64_t draws)
+{
+	const uint32_t bx = raster_bins(int32_t(width), RASTER_BIN_W), by = raster_bins(int32_t(height), RASTER_BIN_H);
+	uint32_t cap = std::max<uint32_t>(ctx->bin_cap, 256);
+	while (cap < draws) cap *= 2;
+	int r;
+	if ((r = ensure(ctx, ctx->bin_lists, size_t(bx) * by * cap * 4))) return r;
+	if ((r = ensure(ctx, ctx->bin_counts, size_t(bx) * by * 4))) return r;
+	ctx->bin_cap = cap;
+	ctx->bins_x = bx;
+	ctx->bins_y = by;
 	return SW_OK;
 }
 
@@ -585,7 +611,7 @@ int sw_destroy(SwCtx* ctx)
 	cudaSetDevice(ctx->device);
 	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
 	if (ctx->aux) cudaStreamSynchronize(ctx->aux);
-	DevBuf* bufs[] = {&ctx->texels, &ctx->texture_mips, &ctx->emissive, &ctx->emissive_mips, &ctx->lightmaps, &ctx->lm_compressed, &ctx->skybox32,
+	DevBuf* bufs[] = {&ctx->texels, &ctx->texture_mips, &ctx->emissive, &ctx->emissive_mips, &ctx->lightmaps, &ctx->lm_compressed, &ctx->bin_lists, &ctx->bin_counts, &ctx->skybox32,
 		&ctx->skybox64, &ctx->frame_in,
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->tri_steps, &ctx->tri_vertices, &ctx->lite, &ctx->ldr[0], &ctx->ldr[1], &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
@@ -1067,6 +1093,7 @@ int sw_submit_draws_ex(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, c
 	if ((r = prepare_draws(ctx, draws, num_draws, vertices, num_vertices, rows, &row_acc, tri_vertices, num_tri_vertices)))
 		return r;
 	if ((r = ensure_raster_buffers(ctx, num_draws, num_vertices, row_acc, num_tri_vertices))) return r;
+	if ((r = ensure_bins(ctx, ctx->frame.width, ctx->frame.height, num_draws))) return r;
 	// The draw uploads and the raster setup run on the auxiliary stream, beside the surface build; they
 	// first wait until the previous frame's tile pass has finished reading these buffers.
 	if (ctx->tiles_recorded) SW_CUDA(ctx, cudaStreamWaitEvent(ctx->aux, ctx->ev_tiles, 0));
@@ -1081,6 +1108,7 @@ int sw_submit_draws_ex(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, c
 	ctx->num_draws = num_draws;
 	const RasterArgs a = raster_args(ctx);
 	if ((r = check_kernel(ctx, launch_raster_setup(a, ctx->aux), "raster setup"))) return r;
+	if ((r = check_kernel(ctx, launch_raster_bins(a, ctx->aux), "raster bins"))) return r;
 	SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, ctx->aux));
 	ctx->draws_valid = true;
 	ctx->stats.draws += num_draws;
@@ -1541,6 +1569,7 @@ int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, con
 	ra.draw_rows = reinterpret_cast<const DrawRows*>(d + off[5]);
 	ra.tri_vertices = reinterpret_cast<const SwTriVertex*>(d + off[6]);
 	if ((r = check_kernel(ctx, launch_raster_setup(ra, aux), "raster setup"))) return r;
+	if ((r = check_kernel(ctx, launch_raster_bins(ra, aux), "raster bins"))) return r;
 	SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, aux));
 	const SurfaceInputs si{reinterpret_cast<const SwLight*>(d + off[0]), reinterpret_cast<const SurfaceGpu*>(d + off[1]),
 		reinterpret_cast<const uint64_t*>(d + off[2])};
@@ -1802,6 +1831,7 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	if ((r = ensure(ctx, ctx->surfaces, std::max<size_t>(f.num_surfaces, 1) * sizeof(SurfaceGpu)))) return r;
 	if ((r = ensure(ctx, ctx->work_prefix, (size_t(f.num_surfaces) + 1) * 8))) return r;
 	if ((r = ensure_raster_buffers(ctx, f.num_draws, f.num_vertices, rows))) return r;
+	if ((r = ensure_bins(ctx, f.params.width, f.params.height, f.num_draws))) return r;
 	if ((r = ensure_framebuffer(ctx, p))) return r;
 	ctx->num_rows = rows;
 	ctx->num_draws = f.num_draws;
@@ -2226,6 +2256,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	key.surface_blocks_per_sm = int(ctx->tuning.surface_blocks_per_sm);
 
 	RasterArgs& ra = key.raster;
+	if ((r = ensure_bins(ctx, p.width, p.height, cap_draws))) return r;
 	ra = raster_args(ctx);
 	ra.draws = pr.draws;
 	ra.vertices = pr.vertices;
@@ -2266,6 +2297,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 			// per-candidate preparation, then the surface compaction here and the draw compaction on aux
 			if ((rr = check_kernel(ctx, launch_prep(key.prep, s, aux, ctx->ev_fork), "surface and draw preparation"))) return rr;
 			if ((rr = check_kernel(ctx, launch_raster_setup(key.raster, aux), "raster setup"))) return rr;
+			if ((rr = check_kernel(ctx, launch_raster_bins(key.raster, aux), "raster bins"))) return rr;
 			SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, aux));
 			if ((rr = check_kernel(ctx,
 					 launch_surface_build(key.surf, p.pixel_format, ctx->num_sms, int(ctx->tuning.surface_blocks_per_sm), s,

@@ -195,3 +195,47 @@ def interleave(poly_draws, tri_draws, seed):
     out[take_tri] = tri_draws
     out[~take_tri] = poly_draws
     return out
+
+
+def make_small_draws(seed, width, height, n, modes=(0, 1, 2), blends=(0, 1, 2, 3, 4), pixel_format=abi.SW_PIXEL_C32,
+                     max_radius=20.0):
+    """Returns (arena, draws, vertices): n small convex polygons (3..6 vertices, radius 2..max_radius px)
+    inside the frame, each textured by its own surface at constant depth (texture coordinates one texel
+    per pixel from the polygon's corner, inside the surface), any mode and blend. Vectorised."""
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(2.0, max_radius, n)
+    cx = rng.uniform(r + 1, width - r - 1)
+    cy = rng.uniform(r + 1, height - r - 1)
+    k = rng.integers(3, 7, n)
+    phase = rng.uniform(0, 2 * np.pi, n)
+    draws = np.zeros(n, abi.DRAW_CMD)
+    verts = []
+    offset = 0
+    inv_z = np.float32(1.0 / 64.0)
+    sizes = np.ceil(2 * r).astype(np.int64) + 3
+    for i in range(n):
+        ang = phase[i] + 2 * np.pi * np.arange(k[i]) / k[i]
+        px = (cx[i] + r[i] * np.cos(ang)).astype(np.float32)
+        py = (cy[i] + r[i] * np.sin(ang)).astype(np.float32)
+        area = float(np.sum(np.roll(px, 1) * py - px * np.roll(py, 1)))
+        if area < 0:
+            px, py = px[::-1], py[::-1]
+        first = len(verts)
+        verts.extend(zip(np.trunc(px * np.float32(65536.0)).astype(np.int64).tolist(),
+                         np.trunc(py * np.float32(65536.0)).astype(np.int64).tolist()))
+        x0, y0 = np.float32(cx[i] - r[i] - 1), np.float32(cy[i] - r[i] - 1)
+        d = draws[i]
+        d["first_vertex"], d["vertex_count"] = first, k[i]
+        d["mode"], d["blend"] = int(rng.choice(modes)), int(rng.choice(blends))
+        d["depth_eq"] = (0.0, 0.0, inv_z)
+        # tc / z = (p - p0) / 64: tc = x - x0 and y - y0 (1..2r+2, inside the size 2r+3 surface)
+        d["tc_eq"] = (inv_z, 0.0, 0.0, inv_z, -x0 * inv_z, -y0 * inv_z)
+        d["tex_size"] = (sizes[i], sizes[i])
+        d["tex_offset"] = offset
+        offset += int(sizes[i] * sizes[i])
+    dt = np.uint64 if pixel_format == abi.SW_PIXEL_C64 else np.uint32
+    if pixel_format == abi.SW_PIXEL_C64:
+        arena = rng.integers(0, 1 << 62, offset, dtype=np.uint64)
+    else:
+        arena = rng.integers(0, 1 << 32, offset, dtype=np.uint64).astype(np.uint32)
+    return arena.astype(dt), draws, np.array(verts, dtype=abi.VERTEX16)

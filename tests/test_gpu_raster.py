@@ -102,3 +102,19 @@ def test_raster_thin_and_degenerate(gpu_ok):
     want, got, bad, _ = render_both(arena, draws, verts, w, h, abi.SW_PIXEL_C32)
     assert bad == 0
     assert_frames_equal(want, got)
+
+
+@pytest.mark.parametrize("fmt", [abi.SW_PIXEL_C32, abi.SW_PIXEL_C64])
+def test_many_small_draws_binned(gpu_ok, fmt):
+    """Over 10k small draws with heavy overdraw and every blend mode, on a frame of many bins (the tile
+    pass scans each bin's ordered draw list): bit-exact, painter's order kept across bins."""
+    w, h = 700, 450  # bins cut by the frame edges
+    arena, draws, verts = scenes.make_small_draws(77 + fmt, w, h, 12000, pixel_format=fmt)
+    assert draws.size > 10000
+    rng = np.random.default_rng(5)
+    init = rng.integers(0, 1 << 62, (h, w), dtype=np.uint64)
+    if fmt == abi.SW_PIXEL_C32:
+        init = init.astype(np.uint32)
+    want, got, bad, stats = render_both(arena, draws, verts, w, h, fmt, init=init)
+    assert bad == 0 and stats.bad_texel_fetches == 0
+    assert_frames_equal(want, got)
