@@ -79,6 +79,12 @@ int sw_upscaler_infer(SwUpscaler* ups, const uint32_t* lo, uint32_t lo_width, ui
 int sw_upscaler_set_fused(SwUpscaler* ups, int enable);
 /* Wait for the device and report whether any upscaler kernel gave up on a bounded wait. */
 int sw_upscaler_check(SwUpscaler* ups);
+/* Failure-detection check of the bounded waits (no counterpart in the reference): one kernel arms an
+ * mbarrier that nothing completes (no copy or MMA in flight), waits at most max_polls polls
+ * (1..2^21), and takes the upscaler kernels' recovery path - error code 5 recorded, TMEM freed, return.
+ * *out_code receives the recorded code (5 when the wait ran out); the record is then cleared, so the
+ * upscaler stays usable. Fails with SW_ERR_STATE if an earlier kernel's failure is still recorded. */
+int sw_upscaler_wait_probe(SwUpscaler* ups, uint32_t max_polls, int* out_code);
 
 /* PSNR (dB, colour channels b, g, r) between two device Color32 frames; 99 when identical. Waits. */
 int sw_upscaler_psnr(SwUpscaler* ups, const uint32_t* a, uint32_t a_pitch, const uint32_t* b, uint32_t b_pitch,

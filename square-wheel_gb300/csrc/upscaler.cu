@@ -1533,6 +1533,39 @@ int pack_weights(SwUpscaler* u, int update, float lr, cudaStream_t s)
 	return SW_OK;
 }
 
+// The failure path every upscaler kernel takes when a bounded mbarrier wait runs out, on a barrier
+// that nothing completes: one CTA allocates TMEM as the kernels do, arms an mbarrier with one arrival
+// and 16 transaction bytes that no copy will ever deliver (no copy or MMA is issued, so nothing is in
+// flight), waits at most max_polls polls, then records code 5 in the error flag, frees the TMEM and
+// returns - the recovery the real kernels run.
+__global__ void __launch_bounds__(128) wait_probe_kernel(int* error, uint32_t max_polls)
+{
+	__shared__ __align__(8) uint64_t bar;
+	__shared__ uint32_t s_tmem;
+	if (threadIdx.x == 0)
+	{
+		mbar_init(&bar, 1);
+		fence_mbar_init();
+	}
+	if (threadIdx.x < 32)
+	{
+		tmem_alloc(&s_tmem, 32);
+		tmem_relinquish();
+	}
+	fence_before_sync();
+	__syncthreads();
+	fence_after_sync();
+	const uint32_t tmem = s_tmem;
+	if (threadIdx.x == 0) mbar_expect_tx(&bar, 16);
+	__syncthreads();
+	const bool completed = mbar_wait_bounded(&bar, 0, max_polls);
+	if (__syncthreads_or(!completed) && threadIdx.x == 0) atomicExch(error, 5);
+	fence_before_sync();
+	__syncthreads();
+	fence_after_sync();
+	if (threadIdx.x < 32) tmem_dealloc(tmem, 32);
+}
+
 int check_error_flag(SwUpscaler* u, cudaStream_t s)
 {
 	int h = 0;
@@ -1890,6 +1923,24 @@ int sw_upscaler_set_fused(SwUpscaler* u, int enable)
 {
 	if (!u) return SW_ERR_INVALID_ARGUMENT;
 	u->fused = enable != 0;
+	return SW_OK;
+}
+
+int sw_upscaler_wait_probe(SwUpscaler* u, uint32_t max_polls, int* out_code)
+{
+	if (!u || !out_code || max_polls == 0 || max_polls > POLL_LIMIT) return SW_ERR_INVALID_ARGUMENT;
+	UP_CUDA(u, cudaSetDevice(u->device));
+	UP_CUDA(u, cudaStreamSynchronize(u->stream));
+	int prior = 0;
+	UP_CUDA(u, cudaMemcpy(&prior, u->error.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+	if (prior) return fail(u, SW_ERR_STATE, "an earlier kernel already gave up (code %d)", prior);
+	wait_probe_kernel<<<1, 128, 0, u->stream>>>(static_cast<int*>(u->error.ptr), max_polls);
+	UP_CUDA(u, cudaGetLastError());
+	UP_CUDA(u, cudaMemcpyAsync(out_code, u->error.ptr, sizeof(int), cudaMemcpyDeviceToHost, u->stream));
+	UP_CUDA(u, cudaStreamSynchronize(u->stream));
+	// the probe's record is not a failure of the upscaler's work: clear it
+	UP_CUDA(u, cudaMemsetAsync(u->error.ptr, 0, sizeof(int), u->stream));
+	UP_CUDA(u, cudaStreamSynchronize(u->stream));
 	return SW_OK;
 }
 

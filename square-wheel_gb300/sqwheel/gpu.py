@@ -31,7 +31,7 @@ EXPORTED = [
     "sw_upscaler_create", "sw_upscaler_destroy", "sw_upscaler_last_error", "sw_upscaler_get_params",
     "sw_upscaler_set_params", "sw_upscaler_gradients", "sw_upscaler_train_step", "sw_upscaler_steps",
     "sw_upscaler_infer", "sw_upscaler_psnr", "sw_upscaler_save", "sw_upscaler_load",
-    "sw_monitor_init", "sw_monitor_plan", "sw_monitor_report", "sw_upscaler_set_fused", "sw_upscaler_check",
+    "sw_monitor_init", "sw_monitor_plan", "sw_monitor_report", "sw_upscaler_set_fused", "sw_upscaler_check", "sw_upscaler_wait_probe",
 ]
 
 _lib = None
@@ -113,6 +113,7 @@ def load_library(path=LIB_PATH):
         "sw_monitor_init": ([vp, u32, f32, u32], i32),
         "sw_upscaler_set_fused": ([vp, i32], i32),
         "sw_upscaler_check": ([vp], i32),
+        "sw_upscaler_wait_probe": ([vp, u32, ctypes.POINTER(ctypes.c_int)], i32),
         "sw_monitor_plan": ([vp, ctypes.POINTER(u32)], i32),
         "sw_monitor_report": ([vp, ctypes.c_double], i32),
     }

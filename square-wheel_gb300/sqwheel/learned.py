@@ -132,6 +132,12 @@ class Upscaler:
         """Wait for the device; raises if a kernel gave up on a bounded wait."""
         self._check(self.lib.sw_upscaler_check(self.h), "check")
 
+    def wait_probe(self, max_polls=1 << 14):
+        """Runs the bounded-wait failure path on a barrier nothing completes; returns the recorded code."""
+        code = ctypes.c_int()
+        self._check(self.lib.sw_upscaler_wait_probe(self.h, max_polls, ctypes.byref(code)), "wait_probe")
+        return code.value
+
     def psnr(self, a, b, stream=0):
         out = ctypes.c_double()
         self._check(self.lib.sw_upscaler_psnr(self.h, _ptr(a), a.stride(0), _ptr(b), b.stride(0), a.shape[1], a.shape[0],

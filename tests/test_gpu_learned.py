@@ -228,3 +228,25 @@ def test_psnr_kernel(ups):
     d = _lanes(a)[..., :3] - _lanes(b)[..., :3]
     want = 10 * np.log10(255.0 ** 2 / np.mean(d.astype(np.float64) ** 2))
     assert ups.psnr(_dev(a), _dev(b)) == pytest.approx(want, abs=1e-9)
+
+
+def test_bounded_wait_runs_out_and_recovers(ups):
+    """Failure detection without a fault: a kernel waits on an mbarrier that nothing completes (no copy
+    or MMA in flight), gives up after a bounded number of polls, records its error code, frees its TMEM
+    and returns; the host reads the code, and the upscaler keeps working (same bytes as before)."""
+    import torch
+    rng = np.random.default_rng(11)
+    lo = _dev(_frame(rng, 64, 200))
+    before = torch.zeros((128, 400), dtype=torch.int32, device="cuda:0")
+    ups.infer(lo, before)
+    ups.check()
+    for polls in (1, 1 << 10, 1 << 14):
+        assert ups.wait_probe(polls) == 5
+    ups.check()  # the probe's record was cleared: no kernel failure is reported
+    after = torch.zeros_like(before)
+    ups.infer(lo, after)
+    ups.check()
+    torch.cuda.synchronize()
+    assert torch.equal(before, after)
+    with pytest.raises(gpu.SwError):
+        ups.wait_probe(0)
