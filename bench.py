@@ -825,6 +825,110 @@ def run_models_gpu(args, world, rank, local):
     r.close()
 
 
+def run_small_gpu(args, world, rank, local):
+    """The small CPU-runnable configuration: the 8-room map (~2k polygons, 16 128x128 textures, simple
+    lightmaps, no dynamic lights) at 640x480 colour32 on its 64-frame camera path. value: frames/s of
+    device time of each frame's CUDA graph (host-prepared arrays, L2 flushed before each); e2e: the same
+    frames through swh_renderer_render_frame (host visibility + GPU-side preparation, frame into a host
+    buffer); cpu_baseline: host work + the oracle with every host thread; parity: the frames against the
+    oracle's single-thread raster."""
+    import ctypes
+    import torch
+    from sqwheel import abi, gpu, host
+    torch.cuda.set_device(local)
+    w, h = 640, 480
+    scene = host.Scene(**host.SMALL_MAP)
+    static = scene.static_data()
+    opts = host.frame_options(w, h, abi.SW_PIXEL_C32, directional=False)
+    fr = host.Frame(scene)
+    n = scene.info().frames
+    idx = [(replica_offset(rank) + k * 5) % n for k in range(args.warmup + args.steps)]
+    frames, prep_ms = [], []
+    for fi in idx:
+        t0 = time.perf_counter()
+        fr.prepare(fi, opts)
+        prep_ms.append((time.perf_counter() - t0) * 1e3)
+        frames.append(dict(index=fi, surfaces=fr.surfaces, draws=fr.draws, vertices=fr.vertices, lights=fr.lights,
+                           params=fr.params, total_texels=fr.total_texels))
+    r = gpu.GpuRenderer(static, device=local)
+    r.enable_timing(True)
+    stream = torch.cuda.ExternalStream(r.stream_handle())
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    out = torch.empty((len(frames), h, w), dtype=torch.int32, device=f"cuda:{local}")
+    graph_ms = []
+    with ClockSampler(local) as clocks:
+        for step, f in enumerate(frames):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            r.draw_frame(r.frame_input(f["params"], f["lights"], f["surfaces"], f["total_texels"], f["draws"], f["vertices"],
+                                       dst_device_ptr=out[step].data_ptr(), pitch=w))
+            t = r.timings()
+            if step >= args.warmup:
+                graph_ms.append(t[4])
+        torch.cuda.synchronize()
+    ms = max_over_ranks(statistics.mean(graph_ms), world, f"cuda:{local}")
+    gpu_frames = out.cpu().numpy().view(np.uint32)
+    r.close()
+    # e2e through the C ABI, one frame at a time into a registered host buffer
+    hr = host.HostRenderer(scene, device=local)
+    glib = gpu.load_library()
+    hbuf = np.zeros((h, w), np.uint32)
+    hr.register_host_buffer(hbuf)
+    for f in frames[: args.warmup]:
+        hr.render_frame(f["index"], opts, out=hbuf)
+    s0 = abi.Stats()
+    glib.sw_get_stats(hr.context(), ctypes.byref(s0))
+    t0 = time.perf_counter()
+    for f in frames[args.warmup:]:
+        hr.render_frame(f["index"], opts, out=hbuf)
+    hr.sync()
+    e2e = args.steps / (time.perf_counter() - t0)
+    s1 = abi.Stats()
+    glib.sw_get_stats(hr.context(), ctypes.byref(s1))
+    hr.unregister_host_buffer(hbuf)
+    hr.close()
+    if rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        threads = os.cpu_count() or 1
+        # CPU baseline: host work + oracle surfaces (all threads) + split_rect raster (all threads), a
+        # bounded sample of the same frames
+        sample = frames[:16]
+        t0 = time.perf_counter()
+        for f in sample:
+            fr.prepare(f["index"], opts)
+            arena = oracle.build_surfaces(static, fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=threads)
+            fb = np.zeros((h, w), np.uint32)
+            oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, fb, num_threads=threads)
+        cpu_v = len(sample) / (time.perf_counter() - t0)
+        # parity: every graph frame against the oracle's single-thread raster (the frame buffer carries over)
+        want = np.zeros((h, w), np.uint32)
+        mism = 0
+        for step, f in enumerate(frames):
+            arena = oracle.build_surfaces(static, f["surfaces"], f["lights"], f["params"], f["total_texels"], num_threads=threads)
+            oracle.rasterize(f["draws"], f["vertices"], arena, f["params"], want)
+            mism += int((want != gpu_frames[step]).sum())
+        print(json.dumps({
+            "metric": METRIC, "value": round(world * 1e3 / ms, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (lighting) / int (raster)", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": "small: the 8-room map (~2k polygons, 16 128x128 textures, simple lightmaps, no dynamic "
+                                   "lights) at 640x480 colour32, every 5th frame of its 64-frame camera path",
+                       "frames": idx[args.warmup:][:8], "mean_surface_texels": int(statistics.mean(f["total_texels"] for f in frames)),
+                       "mean_host_prep_ms": round(statistics.mean(prep_ms), 3),
+                       "timing": "CUDA-event device time of the frame's CUDA graph (sw_draw_frame)",
+                       "l2": "flushed (512 MiB write) before every timed step", "parallelism": f"replicas x{world}"},
+            "parity": {"frames": len(frames), "mismatched_pixels": mism},
+            "cpu_baseline": {"value": round(cpu_v, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(),
+                             "sample": f"{len(sample)} frames: host work + oracle surfaces and split_rect raster, {threads} threads"},
+            "e2e": {"value": round(e2e, 2), "unit": "frames/s",
+                    "h2d_bytes_per_step": int((s1.upload_bytes - s0.upload_bytes) / args.steps),
+                    "d2h_bytes_per_step": int(hbuf.nbytes),
+                    "path": "render_frame: host visibility + GPU-side surface and draw preparation, one frame at a time"},
+            "clocks": clocks.summary(), "gpu_launches": args.steps * 4}), flush=True)
+
+
 # ---------------------------------------------------------------------------------------------------------
 # surfaces workload
 
@@ -1194,7 +1298,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="frame", choices=["frame", "surfaces", "upscale", "shadows", "models"])
+    ap.add_argument("--workload", default="frame", choices=["frame", "surfaces", "upscale", "shadows", "models", "small"])
     ap.add_argument("--shadowed-lights", type=int, default=2, help="shadows workload: shadowed dynamic lights (of 8)")
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--autotune-reps", type=int, default=5,
@@ -1221,6 +1325,8 @@ def main():
             run_shadows_gpu(args, world, rank, local)
         elif args.workload == "models":
             run_models_gpu(args, world, rank, local)
+        elif args.workload == "small":
+            run_small_gpu(args, world, rank, local)
         else:
             run_frame_gpu(args, world, rank, local)
     finally:
