@@ -244,19 +244,28 @@ constexpr uint32_t BL_W = 64, BL_H = 16;
 __host__ __device__ __forceinline__ uint32_t blur_tile_smem(uint32_t radius)
 {
 	const uint32_t lines = BL_H + 2 * radius, cols = BL_W + 2 * radius;
-	return (lines * cols + lines * BL_W) * 8u;
+	return (lines * cols + lines * BL_W) * 16u; // cells as four i32 lanes
 }
+
+// Colour64 cell -> its four u16 lanes as i32 (ColorVecI::from_color64).
+__device__ __forceinline__ int4 lanes_of(unsigned long long c)
+{
+	return make_int4(int32_t(uint32_t(c) & 0xFFFFu), int32_t(uint32_t(c) >> 16), int32_t(uint32_t(c >> 32) & 0xFFFFu),
+		int32_t(uint32_t(c >> 48)));
+}
+// A blur pass's result as the reference stores it: (sum >> 14) into a Colour64 lane, (v as u64).min(65535).
+__device__ __forceinline__ int32_t pass_lane(int32_t sum) { return int32_t(min(uint32_t(sum >> 14), 65535u)); }
 
 __global__ void __launch_bounds__(256) pp_blur_kernel(PostArgs a)
 {
-	extern __shared__ __align__(16) uint64_t s_tile[];
+	extern __shared__ __align__(16) int4 s_cells[];
 	const uint32_t cx0 = blockIdx.x * BL_W, cy0 = blockIdx.y * BL_H;
 	pdl_wait(); // the downscale (the raster tile pass or pp_downscale_kernel) has completed
 	const int32_t r = int32_t(a.radius);
 	const uint32_t cols = min(BL_W, a.bw - cx0), lines = min(BL_H, a.bh - cy0);
 	const uint32_t slines = lines + 2 * uint32_t(r), scols = cols + 2 * uint32_t(r);
-	uint64_t* s_b = s_tile;               // slines x scols downscaled cells
-	uint64_t* s_h = s_b + slines * scols; // slines x cols, horizontally blurred
+	int4* s_b = s_cells;                  // slines x scols downscaled cells, unpacked once
+	int4* s_h = s_b + slines * scols;     // slines x cols, horizontally blurred (already clamped lanes)
 	{
 		// four loads in flight per thread; staged cell (l, c) is cell (clamp(cy0 - r + l), clamp(cx0 - r + c))
 		const uint32_t total = slines * scols;
@@ -278,7 +287,7 @@ __global__ void __launch_bounds__(256) pp_blur_kernel(PostArgs a)
 			}
 #pragma unroll
 			for (int k = 0; k < 4; ++k)
-				if (i0 + k * blockDim.x < total) s_b[i0 + k * blockDim.x] = v[k];
+				if (i0 + k * blockDim.x < total) s_b[i0 + k * blockDim.x] = lanes_of(v[k]);
 		}
 	}
 	__syncthreads();
@@ -286,37 +295,40 @@ __global__ void __launch_bounds__(256) pp_blur_kernel(PostArgs a)
 	for (uint32_t i = threadIdx.x; i < slines * cols; i += blockDim.x)
 	{
 		const uint32_t l = i / cols, c = i % cols;
-		const uint64_t* line = s_b + l * scols + c + uint32_t(r);
-		const CI cc = ci_from_c64(line[0]);
-		int32_t sum[4];
-#pragma unroll
-		for (int k = 0; k < 4; ++k) sum[k] = wmul(cc.v[k], a.kernel_h[r]);
+		const int4* line = s_b + l * scols + c + uint32_t(r);
+		const int4 cc = line[0];
+		const int32_t k0 = a.kernel_h[r];
+		int32_t s0 = wmul(cc.x, k0), s1 = wmul(cc.y, k0), s2 = wmul(cc.z, k0), s3 = wmul(cc.w, k0);
 		for (int32_t dx = 1; dx <= r; ++dx)
 		{
-			const CI c0 = ci_from_c64(line[-dx]);
-			const CI c1 = ci_from_c64(line[dx]);
-#pragma unroll
-			for (int k = 0; k < 4; ++k) sum[k] = wadd(sum[k], wmul(wadd(c0.v[k], c1.v[k]), a.kernel_h[dx + r]));
+			const int4 c0 = line[-dx], c1 = line[dx];
+			const int32_t k = a.kernel_h[dx + r];
+			s0 = wadd(s0, wmul(wadd(c0.x, c1.x), k));
+			s1 = wadd(s1, wmul(wadd(c0.y, c1.y), k));
+			s2 = wadd(s2, wmul(wadd(c0.z, c1.z), k));
+			s3 = wadd(s3, wmul(wadd(c0.w, c1.w), k));
 		}
-		s_h[i] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
+		s_h[i] = make_int4(pass_lane(s0), pass_lane(s1), pass_lane(s2), pass_lane(s3));
 	}
 	__syncthreads();
 	// vertical pass: line cy0 + l is staged at l + r
 	for (uint32_t i = threadIdx.x; i < lines * cols; i += blockDim.x)
 	{
 		const uint32_t l = i / cols, c = i % cols;
-		const CI cc = ci_from_c64(s_h[(l + r) * cols + c]);
-		int32_t sum[4];
-#pragma unroll
-		for (int k = 0; k < 4; ++k) sum[k] = wmul(cc.v[k], a.kernel_v[r]);
+		const int4 cc = s_h[(l + r) * cols + c];
+		const int32_t k0 = a.kernel_v[r];
+		int32_t s0 = wmul(cc.x, k0), s1 = wmul(cc.y, k0), s2 = wmul(cc.z, k0), s3 = wmul(cc.w, k0);
 		for (int32_t dy = 1; dy <= r; ++dy)
 		{
-			const CI c0 = ci_from_c64(s_h[(l + r - dy) * cols + c]);
-			const CI c1 = ci_from_c64(s_h[(l + r + dy) * cols + c]);
-#pragma unroll
-			for (int k = 0; k < 4; ++k) sum[k] = wadd(sum[k], wmul(wadd(c0.v[k], c1.v[k]), a.kernel_v[dy + r]));
+			const int4 c0 = s_h[(l + r - dy) * cols + c], c1 = s_h[(l + r + dy) * cols + c];
+			const int32_t k = a.kernel_v[dy + r];
+			s0 = wadd(s0, wmul(wadd(c0.x, c1.x), k));
+			s1 = wadd(s1, wmul(wadd(c0.y, c1.y), k));
+			s2 = wadd(s2, wmul(wadd(c0.z, c1.z), k));
+			s3 = wadd(s3, wmul(wadd(c0.w, c1.w), k));
 		}
-		a.bloom1[uint64_t(cy0 + l) * a.bw + cx0 + c] = ci_to_c64(CI{{sum[0] >> 14, sum[1] >> 14, sum[2] >> 14, sum[3] >> 14}});
+		a.bloom1[uint64_t(cy0 + l) * a.bw + cx0 + c] = uint64_t(uint32_t(pass_lane(s0))) | (uint64_t(uint32_t(pass_lane(s1))) << 16) |
+			(uint64_t(uint32_t(pass_lane(s2))) << 32) | (uint64_t(uint32_t(pass_lane(s3))) << 48);
 	}
 	pdl_trigger();
 }

@@ -853,6 +853,60 @@ __global__ void __launch_bounds__(256) raster_bin_kernel(RasterArgs a)
 	pdl_trigger();
 }
 
+// The scale-2 bloom downscale without shared memory, when a tile row's threads share a warp with the
+// next row's (TILE_W / STRIP <= 16): the thread of an even row takes the odd row's STRIP pixels from
+// its partner by a shuffle, box-averages its STRIP / 2 cells and stores them; the line's lane sums of
+// the row pair are reduced over its threads by shuffles and added to the global sums, one atomic per
+// lane. Same integer arithmetic as bloom_epilogue, so the same values.
+template <int TILE_W, int STRIP>
+__device__ __forceinline__ void bloom_epilogue_s2(const RasterArgs& a, const uint64_t* pix, int tx0, int ty0, int tid)
+{
+	constexpr int TPR = TILE_W / STRIP;
+	static_assert(TPR <= 16 && (TPR & (TPR - 1)) == 0 && STRIP % 2 == 0, "row pairs within a warp");
+	const int ly = tid / TPR, lx = (tid % TPR) * STRIP;
+	uint64_t other[STRIP];
+#pragma unroll
+	for (int k = 0; k < STRIP; ++k) other[k] = __shfl_xor_sync(0xFFFFFFFFu, pix[k], TPR);
+	int32_t line[4] = {0, 0, 0, 0};
+	const bool even = (ly & 1) == 0;
+	const uint32_t by = uint32_t((ty0 + ly) / 2);
+	if (even && by < a.bloom_h)
+	{
+#pragma unroll
+		for (int c = 0; c < STRIP / 2; ++c)
+		{
+			const uint32_t bx = uint32_t((tx0 + lx) / 2 + c);
+			if (bx >= a.bloom_w) continue;
+			int32_t sum[4] = {0, 0, 0, 0};
+			const uint64_t q[4] = {pix[2 * c], pix[2 * c + 1], other[2 * c], other[2 * c + 1]};
+#pragma unroll
+			for (int j = 0; j < 4; ++j)
+			{
+				const CI v = ci_from_c64(q[j]);
+#pragma unroll
+				for (int l = 0; l < 4; ++l) sum[l] = wadd(sum[l], v.v[l]);
+			}
+			CI avg;
+#pragma unroll
+			for (int l = 0; l < 4; ++l)
+			{
+				avg.v[l] = wmul(sum[l], 64) >> 8; // scaler 256 / (2 * 2)
+				line[l] = wadd(line[l], avg.v[l]);
+			}
+			a.bloom_out[uint64_t(by) * a.bloom_w + bx] = ci_to_c64(avg);
+		}
+	}
+	// the row pair's threads are TPR consecutive lanes (the odd row's add zeros)
+#pragma unroll
+	for (int l = 0; l < 4; ++l)
+		for (int o = TPR / 2; o > 0; o >>= 1) line[l] = wadd(line[l], __shfl_xor_sync(0xFFFFFFFFu, line[l], o));
+	if (even && (tid % TPR) == 0 && by < a.bloom_h)
+	{
+#pragma unroll
+		for (int l = 0; l < 4; ++l) atomicAdd(&a.bloom_line_sums[by * 4 + l], line[l]);
+	}
+}
+
 // Tile shapes of the tile pass (the autotuner's choice, SwTuning.raster_tile): TILE_W x TILE_H pixels,
 // 256 threads, each thread a 1 x STRIP strip of one row. Every shape gives the same frame.
 struct TileShape
@@ -1016,7 +1070,17 @@ __global__ void __launch_bounds__(256) raster_tiles_kernel(RasterArgs a)
 			if (xb + k < a.width) fb[uint64_t(y) * a.width + xb + k] = pix[k];
 	}
 	if constexpr (P::FORMAT == SW_PIXEL_C64)
-		if (a.bloom_scale) bloom_epilogue<TILE_W, TILE_H, STRIP>(a, pix, tx0, ty0, tid, &s_row[0][0]);
+	{
+		if constexpr (TILE_W / STRIP <= 16)
+		{
+			if (a.bloom_scale == 2)
+				bloom_epilogue_s2<TILE_W, STRIP>(a, reinterpret_cast<const uint64_t*>(pix), tx0, ty0, tid);
+			else if (a.bloom_scale)
+				bloom_epilogue<TILE_W, TILE_H, STRIP>(a, pix, tx0, ty0, tid, &s_row[0][0]);
+		}
+		else if (a.bloom_scale)
+			bloom_epilogue<TILE_W, TILE_H, STRIP>(a, pix, tx0, ty0, tid, &s_row[0][0]);
+	}
 	if (local_errors) atomicAdd(a.error_counter, local_errors);
 	// Pixel writes (span pixels processed) for the traffic accounting, one atomic per warp.
 	for (int o = 16; o > 0; o >>= 1) local_writes += __shfl_xor_sync(0xFFFFFFFFu, local_writes, o);
