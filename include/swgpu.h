@@ -321,6 +321,73 @@ typedef struct SwTexturePass {
 int sw_update_textures(SwCtx* ctx, const SwTexturePass* passes, uint32_t num_passes, const int32_t* shifts,
 	uint32_t num_shifts);
 
+/* Simulated generative texture effects, water (GenerativeTextureEffectWater, generative_texture_effect_water.rs)
+ * and fire (GenerativeTextureEffectFire, generative_texture_effect_fire.rs). Their fields live on the
+ * device in the context's simulation state: sw_reserve_simulation_state allocates it (`words` 4-byte
+ * words, zeroed; a second call with another size replaces it, zeroed). Each frame the caller submits the
+ * passes of that frame's update steps and texture generation; the library runs them on the context's
+ * stream, one kernel launch per distinct `launch` number, in increasing order (passes must be sorted by
+ * it), every pass of a launch in parallel. Kinds (field and heat maps are 2^size_log2[0] x
+ * 2^size_log2[1] words, row-major, both edges wrapping unless stated):
+ *   SW_SIM_WATER_POINTS: the wave sources of one step (generative_texture_effect_water.rs:57-215): for each
+ *     point in order, state_src[address] += value and state_dst[address] -= value (f32; value holds the
+ *     f32's bits). Points with equal addresses must be consecutive (the host sorts them stably).
+ *   SW_SIM_WATER_STEP (update_wave_field, :308-418): state_dst[x, y] = ((src[x-1, y] + src[x+1, y] +
+ *     src[x, y-1] + src[x, y+1]) * 0.5 - state_dst[x, y]) * attenuation, src = state_src, attenuation =
+ *     `param` as f32 bits.
+ *   SW_SIM_FIRE_STEP (update_heat_map, generative_texture_effect_fire.rs:430-550): the heat map at state_src
+ *     propagated upwards into state_dst (u32 words holding 0..255), attenuation_i = `param`; with
+ *     SW_SIM_FIRE_SLOW in flags, the row-sequential slow form. The last row becomes 0.
+ *   SW_SIM_FIRE_POINTS (the heat sources and particles of one step, :62-321): state_dst[address] =
+ *     max(state_dst[address], value).
+ *   SW_SIM_WATER_TEXTURE (make_wavy_texture, generative_texture_effect_water.rs:420-682): texture mip
+ *     dst_mip (the field's size) gets the normals of the field at state_src with roughness `param` (f32
+ *     bits); its diffuse per colour mode (flags >> SW_SIM_COLOR_MODE_SHIFT: 0 single colour, 1 source
+ *     texture, 2 source deformed by the normal, 3 deformed along x only) from base_color or from mip
+ *     src_mip (the material's mip 0, nearest-resized to the field's size); modes 0 and 1 write diffuse
+ *     only with SW_SIM_WATER_INIT_DIFFUSE (the first generation) and keep it afterwards.
+ *   SW_SIM_FIRE_TEXTURE (generate_emissive_texture_based_on_heat_map, :552-566): emissive mip dst_mip =
+ *     palette[heat at state_src], the palette being the pass's 256 points (value = Color32).
+ *   SW_SIM_TEXTURE_MIP / SW_SIM_EMISSIVE_MIP (build_texture_mip / build_texture_lite_mip, textures.rs:
+ *     309-415): mip dst_mip (half of src_mip's size) rebuilt from mip src_mip.
+ * Everything (kinds, offsets against the state, mips and sizes, point ranges and addresses) is validated
+ * before anything is uploaded or launched. */
+#define SW_SIM_WATER_POINTS 1u
+#define SW_SIM_WATER_STEP 2u
+#define SW_SIM_FIRE_STEP 3u
+#define SW_SIM_FIRE_POINTS 4u
+#define SW_SIM_WATER_TEXTURE 5u
+#define SW_SIM_FIRE_TEXTURE 6u
+#define SW_SIM_TEXTURE_MIP 7u
+#define SW_SIM_EMISSIVE_MIP 8u
+#define SW_SIM_FIRE_SLOW 1u
+#define SW_SIM_WATER_INIT_DIFFUSE 2u
+#define SW_SIM_COLOR_MODE_SHIFT 8u
+typedef struct SwSimPoint {
+	uint32_t address; /* word index within the pass's field / heat map (palette index for FIRE_TEXTURE) */
+	uint32_t value;   /* f32 bits (water), heat 0..255 (fire), Color32 (palette) */
+} SwSimPoint;
+typedef struct SwSimPass {
+	uint32_t kind;         /* SW_SIM_* */
+	uint32_t launch;       /* launch number, non-decreasing over the pass list */
+	uint32_t size_log2[2]; /* field / heat map size (all kinds but the MIP ones) */
+	uint64_t state_src;    /* word offset of the field / heat map read */
+	uint64_t state_dst;    /* word offset of the field / heat map written */
+	uint32_t first_point;  /* POINTS and FIRE_TEXTURE: the pass's points */
+	uint32_t num_points;
+	uint32_t dst_mip;      /* TEXTURE and MIP passes: texture_mips (EMISSIVE: emissive_mips) index written */
+	uint32_t src_mip;      /* WATER_TEXTURE: colour source mip; MIP passes: the mip read */
+	uint32_t flags;        /* SW_SIM_FIRE_SLOW, SW_SIM_WATER_INIT_DIFFUSE, colour mode << SW_SIM_COLOR_MODE_SHIFT */
+	uint32_t param;        /* see the kinds */
+	uint32_t base_color;   /* WATER_TEXTURE colour mode 0: the Color32 */
+	uint32_t reserved;
+} SwSimPass;
+int sw_reserve_simulation_state(SwCtx* ctx, uint64_t words);
+int sw_update_simulations(SwCtx* ctx, const SwSimPass* passes, uint32_t num_passes, const SwSimPoint* points,
+	uint32_t num_points);
+/* Diagnostics: copy words [first, first + count) of the simulation state to host memory (synchronises). */
+int sw_read_simulation_state(SwCtx* ctx, uint64_t first, uint64_t count, uint32_t* out);
+
 /* Page-lock a host buffer the caller reuses for its frames (the window surface's pixels, say) with
  * cudaHostRegister (mapped), so that frames written to host memory inside it go straight from the
  * device into it instead of through the library's pinned staging buffer and a host copy (sw_draw_frame's

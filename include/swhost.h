@@ -49,6 +49,8 @@ typedef struct SwhSceneConfig {
 	uint32_t layered_materials;   /* the last this many base materials are layered animations */
 	uint32_t num_sprites;         /* sprites in the rooms (every orientation, alpha-family and additive blending) */
 	uint32_t num_decals;          /* decals on the rooms' walls and floors (every blending mode) */
+	uint32_t water_materials;     /* base materials with a water effect (before the turbulence ones) */
+	uint32_t fire_materials;      /* base materials with a fire effect (before the water ones) */
 } SwhSceneConfig;
 
 typedef struct SwhSceneInfo {
@@ -104,6 +106,49 @@ typedef struct SwhTextureEffect {
 	float turb[3];
 } SwhTextureEffect;
 int swh_scene_texture_effect(const SwhScene* scene, uint32_t material, SwhTextureEffect* out_effect);
+/* A material's simulated effect (SpecialMaterialEffect::Water / Fire, src/common/material_water.rs,
+ * material_fire.rs), flattened: kind 3 water, 4 fire (0: none); its sources (WaveSource / HeatSource,
+ * kinds in the order those enums list them), its output slot and its words of simulation state. A time
+ * function is SingleArgumentFunction: kind 0 constant a, 1 linear (scale a, offset b), 2 sine, 3 triangle,
+ * 4 saw-tooth, 5 step wave (frequency a, phase b, amplitude c, offset d); a random value is
+ * ValueWithRandomDeviation (value, deviation). */
+typedef struct SwhTimeFunction {
+	uint32_t kind;
+	float a, b, c, d;
+} SwhTimeFunction;
+typedef struct SwhRandomValue {
+	SwhTimeFunction value, deviation;
+} SwhRandomValue;
+typedef struct SwhSimSource {
+	uint32_t kind;
+	uint32_t points[2][2];           /* a single-point source uses points[0] */
+	SwhTimeFunction offsets[2][2];   /* water: center_offset (offsets[0]) / points_offset */
+	float frequency, phase, amplitude, offset, radius; /* water; fire fountains: frequency */
+	uint32_t ramp;                   /* fire lightning */
+	SwhRandomValue fire_offsets[2][2]; /* fire: point offset (fire_offsets[0]) / lightning offsets */
+	SwhRandomValue heat, angle, speed, gravity, spawn_angle, spawn_distance, lifetime;
+} SwhSimSource;
+#define SWH_MAX_SIM_SOURCES 8
+typedef struct SwhSimEffect {
+	uint32_t kind;
+	uint32_t resolution_log2[2];
+	float update_frequency;
+	float attenuation_param; /* water: fluidity; fire: heat_conductivity */
+	uint32_t color_mode;     /* water: ColorTextureApplyMode */
+	uint32_t slow;           /* fire */
+	uint32_t has_color;      /* fire: palette from `color` */
+	float color[3];
+	float roughness;         /* water: Material::roughness */
+	int32_t output_texture;  /* water: texture slot written */
+	int32_t output_emissive; /* fire: emissive slot written */
+	int32_t source_emissive; /* fire: the material's emissive texture, -1 without */
+	uint32_t num_sources;
+	uint64_t state_offset;   /* word offset of its two fields / heat maps */
+	SwhSimSource sources[SWH_MAX_SIM_SOURCES];
+} SwhSimEffect;
+int swh_scene_simulated_effect(const SwhScene* scene, uint32_t material, SwhSimEffect* out_effect);
+/* Words of simulation state the scene's simulated effects use (sw_reserve_simulation_state). */
+int swh_scene_simulation_words(const SwhScene* scene, uint64_t* out_words);
 const char* swh_last_error(void);
 
 typedef struct SwhFrameOptions {
@@ -151,6 +196,11 @@ typedef struct SwhFrameOutputs {
 	uint32_t num_texture_passes;
 	uint32_t num_texture_shifts;
 	const int32_t* texture_shifts;
+	/* simulated texture effects of the frame (sw_update_simulations, after the texture passes) */
+	const SwSimPass* sim_passes;
+	uint32_t num_sim_passes;
+	uint32_t num_sim_points;
+	const SwSimPoint* sim_points;
 } SwhFrameOutputs;
 
 typedef struct SwhFrame SwhFrame;
@@ -167,6 +217,10 @@ int swh_frame_map(const SwhFrame* frame, const SwMapPolygon** out_polygons, uint
 int swh_frame_prepare(SwhFrame* frame, uint32_t frame_index, const SwhFrameOptions* options);
 /* Pointers into the frame's arrays, valid until the next swh_frame_prepare. */
 int swh_frame_outputs(const SwhFrame* frame, SwhFrameOutputs* out);
+/* A simulated effect's host state after the last prepared frame: its update step, the state buffer (0 or
+ * 1) holding its current field / heat map, whether it has generated its texture, its live particles. */
+int swh_frame_effect_state(const SwhFrame* frame, uint32_t material, uint32_t* out_update_step,
+	uint32_t* out_current_buffer, uint32_t* out_generated, uint32_t* out_particles);
 /* The host half of a frame whose surfaces and world draws the GPU prepares (sw_draw_frame_view):
  * visibility, light positioning, the skybox draws and the visible leafs with their bounds, lights and
  * back-to-front order. swh_frame_view_input fills everything of SwViewFrameInput but mip_bias and the

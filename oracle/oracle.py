@@ -43,6 +43,14 @@ def load():
     lib.orc_gaussian_kernel.argtypes = [f32, u32, vp]
     lib.orc_turb_shifts.argtypes = [f32, f32, f32, f32, u32, u32, u32, vp, u32]
     lib.orc_apply_texture_passes.argtypes = [vp, u32, vp, u32, vp, u32, vp, vp, u32, vp]
+    lib.orc_sim_effect_size.restype = u32
+    lib.orc_sim_create.argtypes = [vp]
+    lib.orc_sim_create.restype = vp
+    lib.orc_sim_destroy.argtypes = [vp]
+    lib.orc_sim_update.argtypes = [vp, f32, vp, u32, vp, vp, u32, vp, u32]
+    lib.orc_sim_state.argtypes = [vp, vp, u64, vp, vp, vp]
+    lib.orc_xoshiro_outputs.argtypes = [vp, vp, u32]
+    lib.orc_small_rng_state.argtypes = [u64, vp]
     for name in ("orc_compress_lightmaps", "orc_decompress_lightmaps", "orc_compress_directional_lightmaps",
                  "orc_decompress_directional_lightmaps"):
         getattr(lib, name).argtypes = [vp, u64, vp]
@@ -197,3 +205,57 @@ def apply_texture_passes(passes, shifts, static):
                                            abi.ptr(static.texture_mips), static.texture_mips.size, abi.ptr(static.texels),
                                            abi.ptr(static.emissive_mips), static.emissive_mips.size,
                                            abi.ptr(static.emissive_pixels)), "orc_apply_texture_passes")
+
+
+class SimEffect:
+    """A water or fire effect run whole on the CPU (orc_sim_*): created from the effect description's bytes
+    (the host's SwhSimEffect layout), updated at frame times against a copy of the static texture data,
+    into which each update writes the generated texture at the effect's output slot."""
+
+    def __init__(self, effect):
+        lib = load()
+        raw = bytes(effect)
+        assert len(raw) == lib.orc_sim_effect_size(), "effect description layout differs from the oracle's"
+        self._buf = ctypes.create_string_buffer(raw, len(raw))
+        self.handle = lib.orc_sim_create(self._buf)
+        if not self.handle:
+            raise RuntimeError("orc_sim_create refused the effect")
+        self.area = 1 << (effect.resolution_log2[0] + effect.resolution_log2[1])
+
+    def update(self, time_s, static, source_texture):
+        """One GenerativeTextureEffect::update; True when it generated the texture this time."""
+        r = load().orc_sim_update(self.handle, time_s, abi.ptr(static.texture_mips), static.texture_mips.size,
+                                  abi.ptr(static.texels), abi.ptr(static.emissive_mips), static.emissive_mips.size,
+                                  abi.ptr(static.emissive_pixels), source_texture)
+        if r < 0:
+            raise RuntimeError(f"orc_sim_update failed with status {r}")
+        return r == 1
+
+    def state(self):
+        """(field words: f32 bits of the wave field or the heat values, update_step, generated, particles)."""
+        words = np.zeros(self.area, np.uint32)
+        v = [ctypes.c_uint32() for _ in range(3)]
+        _check(load().orc_sim_state(self.handle, abi.ptr(words), words.size, *[ctypes.byref(x) for x in v]),
+               "orc_sim_state")
+        return words, int(v[0].value), int(v[1].value), int(v[2].value)
+
+    def close(self):
+        if self.handle:
+            load().orc_sim_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
+
+
+def xoshiro_outputs(state, n):
+    st = np.ascontiguousarray(state, dtype=np.uint64)
+    out = np.zeros(n, np.uint64)
+    load().orc_xoshiro_outputs(abi.ptr(st), abi.ptr(out), n)
+    return out
+
+
+def small_rng_state(seed):
+    out = np.zeros(4, np.uint64)
+    load().orc_small_rng_state(seed, abi.ptr(out))
+    return out

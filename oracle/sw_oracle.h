@@ -80,6 +80,50 @@ int orc_decompress_directional_lightmaps(const uint8_t* in, uint64_t n, SwDirect
  * perform_blur_impl (postprocessor.rs:848-907); exported for known-answer tests. */
 int orc_gaussian_kernel(float sigma, uint32_t radius, float* out33);
 
+/* Simulated texture effects (generative_texture_effect_water.rs, generative_texture_effect_fire.rs), whole
+ * on the CPU. The effect description: kind 3 water, 4 fire; a time function is SingleArgumentFunction
+ * (kind 0 constant a, 1 linear a x + b, 2 sine, 3 triangle, 4 saw-tooth, 5 step: frequency a, phase b,
+ * amplitude c, offset d), a random value is ValueWithRandomDeviation. */
+typedef struct OrcTimeFunction {
+	uint32_t kind;
+	float a, b, c, d;
+} OrcTimeFunction;
+typedef struct OrcRandomValue {
+	OrcTimeFunction value, deviation;
+} OrcRandomValue;
+typedef struct OrcSimSource {
+	uint32_t kind; /* water: WavySpot, WavyLine, PeriodicDroplet, Rain; fire: Point, Line, Lightning, Fountain */
+	uint32_t points[2][2];
+	OrcTimeFunction offsets[2][2];
+	float frequency, phase, amplitude, offset, radius;
+	uint32_t ramp;
+	OrcRandomValue fire_offsets[2][2];
+	OrcRandomValue heat, angle, speed, gravity, spawn_angle, spawn_distance, lifetime;
+} OrcSimSource;
+#define ORC_MAX_SIM_SOURCES 8
+typedef struct OrcSimEffect {
+	uint32_t kind;
+	uint32_t resolution_log2[2];
+	float update_frequency;
+	float attenuation_param; /* fluidity (water), heat_conductivity (fire) */
+	uint32_t color_mode, slow, has_color;
+	float color[3];
+	float roughness;
+	int32_t output_texture, output_emissive, source_emissive;
+	uint32_t num_sources;
+	uint64_t state_offset;
+	OrcSimSource sources[ORC_MAX_SIM_SOURCES];
+} OrcSimEffect;
+uint32_t orc_sim_effect_size(void);
+void* orc_sim_create(const OrcSimEffect* effect); /* runs the constructor's equilibrium steps; NULL if malformed */
+void orc_sim_destroy(void* sim);
+int orc_sim_update(void* sim, float current_time_s, const SwTextureMip* mips, uint32_t num_mips, uint64_t* texels,
+	const SwEmissiveMip* emissive_mips, uint32_t num_emissive_mips, uint32_t* emissive, uint32_t source_texture);
+int orc_sim_state(void* sim, uint32_t* out_words, uint64_t max_words, uint32_t* out_update_step, uint32_t* out_generated,
+	uint32_t* out_particles);
+void orc_xoshiro_outputs(const uint64_t state[4], uint64_t* out, uint32_t n);
+void orc_small_rng_state(uint64_t seed, uint64_t out_state[4]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,7 +17,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIB_DIR = os.path.join(PKG, "lib")
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(LIB_DIR, "libswgpu.so")
-SOURCES = ["swgpu.cu", "surfaces.cu", "raster.cu", "prep.cu", "post.cu", "post_noalloc.cu", "upscaler.cu", "lightmaps.cu", "effects.cu"]
+SOURCES = ["swgpu.cu", "surfaces.cu", "raster.cu", "prep.cu", "post.cu", "post_noalloc.cu", "upscaler.cu", "lightmaps.cu", "effects.cu",
+           "sims.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -77,7 +78,7 @@ def build(force=False, verbose=False):
     return LIB
 
 
-HOST_SOURCES = ["scene.cpp", "frame.cpp", "swhost.cpp", "sqwm.cpp"]
+HOST_SOURCES = ["scene.cpp", "frame.cpp", "swhost.cpp", "sqwm.cpp", "sims.cpp"]
 HOST_LIB = os.path.join(LIB_DIR, "libswhost.so")
 
 

@@ -356,6 +356,29 @@ struct TextureEffectArgs
 	uint32_t* emissive;
 };
 int launch_texture_effects(const TextureEffectArgs& a, cudaStream_t stream);
+// sw_update_simulations (sims.cu): one group per pass of a launch, groups in item order (first_item
+// ascending); an item is a point (POINTS), a word (STEP, TEXTURE), a row (slow FIRE_STEP) or a texel of
+// the destination mip (MIP passes).
+struct SimGroup
+{
+	uint64_t first_item;
+	uint64_t dst_offset, src_offset; // TEXTURE / MIP passes: texel (emissive pixel) offsets of dst and src mips
+	uint32_t pass;
+	uint32_t src_width, src_height;  // WATER_TEXTURE: colour source mip; MIP passes: the source mip
+	uint32_t reserved;
+};
+struct SimArgs
+{
+	const SimGroup* groups;
+	const SwSimPass* passes;
+	const SwSimPoint* points;
+	uint32_t num_groups;
+	uint64_t total_items;
+	uint32_t* state;
+	uint64_t* texels;
+	uint32_t* emissive;
+};
+int launch_simulation(const SimArgs& a, cudaStream_t stream);
 
 // Compressed lightmap lumps (4-byte simple, 13-byte directional elements, 16-byte aligned inputs) decoded
 // into f32 lightmaps (lightmaps.cu).

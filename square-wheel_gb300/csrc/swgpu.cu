@@ -201,6 +201,10 @@ struct SwCtx
 	// sw_update_textures: the groups, layers, passes and shifts of one call, uploaded together
 	DevBuf effect_buf;
 	Staging stage_effects;
+	// sw_update_simulations: the fields / heat maps (sim_words 4-byte words) and one call's upload
+	DevBuf sim_state, sim_buf;
+	uint64_t sim_words = 0;
+	Staging stage_sims;
 
 	// Optional per-stage device timing (sw_enable_timing).
 	bool timing = false;
@@ -616,7 +620,7 @@ int sw_destroy(SwCtx* ctx)
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->tri_steps, &ctx->tri_vertices, &ctx->lite, &ctx->ldr[0], &ctx->ldr[1], &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst, &ctx->map_polygons,
-		&ctx->map_vertices, &ctx->vslab, &ctx->shadow_storage, &ctx->shadow_descs, &ctx->effect_buf};
+		&ctx->map_vertices, &ctx->vslab, &ctx->shadow_storage, &ctx->shadow_descs, &ctx->effect_buf, &ctx->sim_state, &ctx->sim_buf};
 	for (DevBuf* b : bufs) release(*b);
 	for (const SwCtx::HostRange& h : ctx->registered) cudaHostUnregister(h.ptr);
 	if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
@@ -628,7 +632,7 @@ int sw_destroy(SwCtx* ctx)
 		if (e) cudaEventDestroy(e);
 	Staging* st[] = {&ctx->stage_lights, &ctx->stage_surfaces, &ctx->stage_prefix, &ctx->stage_draws,
 		&ctx->stage_vertices, &ctx->stage_tri_vertices, &ctx->stage_draw_rows, &ctx->stage_io, &ctx->gstage[0], &ctx->gstage[1], &ctx->stage_shadow,
-		&ctx->stage_shadow_descs, &ctx->stage_effects};
+		&ctx->stage_shadow_descs, &ctx->stage_effects, &ctx->stage_sims};
 	for (Staging* s : st)
 	{
 		if (s->host) cudaFreeHost(s->host);
@@ -1449,6 +1453,173 @@ int sw_update_textures(SwCtx* ctx, const SwTexturePass* passes, uint32_t num_pas
 	a.texels = static_cast<uint64_t*>(ctx->texels.ptr);
 	a.emissive = static_cast<uint32_t*>(ctx->emissive.ptr);
 	return check_kernel(ctx, launch_texture_effects(a, ctx->stream), "texture effects");
+}
+
+int sw_reserve_simulation_state(SwCtx* ctx, uint64_t words)
+{
+	if (!ctx) return SW_ERR_INVALID_ARGUMENT;
+	if (words > (1ull << 32)) return fail(ctx, SW_ERR_LIMIT, "simulation state above 2^32 words");
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	if (ctx->aux) SW_CUDA(ctx, cudaStreamSynchronize(ctx->aux));
+	if (words * 4 > ctx->sim_state.bytes)
+	{
+		release(ctx->sim_state);
+		int r = ensure(ctx, ctx->sim_state, size_t(words) * 4);
+		if (r) return r;
+	}
+	ctx->sim_words = words;
+	if (words) SW_CUDA(ctx, cudaMemsetAsync(ctx->sim_state.ptr, 0, size_t(words) * 4, ctx->stream));
+	return SW_OK;
+}
+
+int sw_update_simulations(SwCtx* ctx, const SwSimPass* passes, uint32_t num_passes, const SwSimPoint* points,
+	uint32_t num_points)
+{
+	if (!ctx || (num_passes && !passes) || (num_points && !points)) return SW_ERR_INVALID_ARGUMENT;
+	if (num_passes == 0) return SW_OK;
+	if (num_passes > (1u << 20) || num_points > (1u << 26)) return fail(ctx, SW_ERR_LIMIT, "too many simulation passes or points");
+	const std::vector<SwTextureMip>& tm = ctx->h_texture_mips;
+	const std::vector<SwEmissiveMip>& em = ctx->h_emissive_mips;
+	std::vector<SimGroup> groups(num_passes);
+	std::vector<uint32_t> launch_first; // first group of each launch
+	std::vector<uint64_t> launch_items;
+	uint64_t items = 0;
+	for (uint32_t p = 0; p < num_passes; ++p)
+	{
+		const SwSimPass& a = passes[p];
+		if (p > 0 && a.launch < passes[p - 1].launch) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: launches out of order", p);
+		if (p == 0 || a.launch != passes[p - 1].launch)
+		{
+			if (p > 0) launch_items.push_back(items);
+			launch_first.push_back(p);
+			items = 0;
+		}
+		SimGroup& g = groups[p];
+		std::memset(&g, 0, sizeof(g));
+		g.pass = p;
+		g.first_item = items;
+		const bool mip_pass = a.kind == SW_SIM_TEXTURE_MIP || a.kind == SW_SIM_EMISSIVE_MIP;
+		if (!mip_pass && (a.size_log2[0] < 2 || a.size_log2[1] < 2 || a.size_log2[0] + a.size_log2[1] > 24))
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: field size out of range", p);
+		const uint64_t area = mip_pass ? 0 : (1ull << (a.size_log2[0] + a.size_log2[1]));
+		auto in_state = [&](uint64_t off) { return off <= ctx->sim_words && area <= ctx->sim_words - off; };
+		auto points_ok = [&](uint64_t need) {
+			return uint64_t(a.first_point) + a.num_points <= num_points && (need == 0 || a.num_points == need);
+		};
+		uint64_t n = 0;
+		switch (a.kind)
+		{
+		case SW_SIM_WATER_POINTS:
+		case SW_SIM_FIRE_POINTS:
+			if (!in_state(a.state_dst) || (a.kind == SW_SIM_WATER_POINTS && !in_state(a.state_src)) || !points_ok(0))
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: state or points out of range", p);
+			for (uint32_t i = 0; i < a.num_points; ++i)
+				if (points[a.first_point + i].address >= area)
+					return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: point %u outside the field", p, i);
+			n = a.num_points;
+			break;
+		case SW_SIM_WATER_STEP:
+		case SW_SIM_FIRE_STEP:
+			if (!in_state(a.state_src) || !in_state(a.state_dst) || a.state_src == a.state_dst)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: state out of range", p);
+			if (a.kind == SW_SIM_FIRE_STEP && a.param > (1u << 18))
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: attenuation above 2^18", p);
+			n = (a.kind == SW_SIM_FIRE_STEP && (a.flags & SW_SIM_FIRE_SLOW)) ? (1ull << a.size_log2[1]) : area;
+			break;
+		case SW_SIM_WATER_TEXTURE:
+		case SW_SIM_FIRE_TEXTURE:
+		{
+			const bool water = a.kind == SW_SIM_WATER_TEXTURE;
+			const size_t nm = water ? tm.size() : em.size();
+			if (!in_state(a.state_src) || a.dst_mip >= nm || (water && (a.src_mip >= tm.size() || a.src_mip == a.dst_mip)) ||
+				(!water && !points_ok(256)) || (water && (a.flags >> SW_SIM_COLOR_MODE_SHIFT) > 3))
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: state, mips, palette or colour mode out of range", p);
+			const uint32_t w = water ? tm[a.dst_mip].width : em[a.dst_mip].width;
+			const uint32_t h = water ? tm[a.dst_mip].height : em[a.dst_mip].height;
+			if (w != (1u << a.size_log2[0]) || h != (1u << a.size_log2[1]))
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: output mip is not the field's size", p);
+			g.dst_offset = water ? tm[a.dst_mip].offset : em[a.dst_mip].offset;
+			if (water)
+			{
+				const SwTextureMip& s = tm[a.src_mip];
+				if (s.width == 0 || s.height == 0 || s.width > (1u << 16) || s.height > (1u << 16))
+					return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: bad colour source mip", p);
+				g.src_offset = s.offset;
+				g.src_width = s.width;
+				g.src_height = s.height;
+			}
+			n = area;
+			break;
+		}
+		case SW_SIM_TEXTURE_MIP:
+		case SW_SIM_EMISSIVE_MIP:
+		{
+			const bool lite = a.kind == SW_SIM_EMISSIVE_MIP;
+			const size_t nm = lite ? em.size() : tm.size();
+			if (a.dst_mip >= nm || a.src_mip >= nm || a.dst_mip == a.src_mip)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: bad mip", p);
+			const uint32_t sw = lite ? em[a.src_mip].width : tm[a.src_mip].width, sh = lite ? em[a.src_mip].height : tm[a.src_mip].height;
+			const uint32_t dw = lite ? em[a.dst_mip].width : tm[a.dst_mip].width, dh = lite ? em[a.dst_mip].height : tm[a.dst_mip].height;
+			if (dw != sw >> 1 || dh != sh >> 1 || dw == 0 || dh == 0)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: destination is not half the source", p);
+			g.dst_offset = lite ? em[a.dst_mip].offset : tm[a.dst_mip].offset;
+			g.src_offset = lite ? em[a.src_mip].offset : tm[a.src_mip].offset;
+			g.src_width = sw;
+			g.src_height = sh;
+			n = uint64_t(dw) * dh;
+			break;
+		}
+		default:
+			return fail(ctx, SW_ERR_INVALID_ARGUMENT, "simulation pass %u: unknown kind", p);
+		}
+		items += n;
+	}
+	launch_items.push_back(items);
+	// one upload: groups | passes | points
+	auto up16 = [](size_t v) { return (v + 15) / 16 * 16; };
+	const size_t o_passes = up16(groups.size() * sizeof(SimGroup));
+	const size_t o_points = o_passes + up16(size_t(num_passes) * sizeof(SwSimPass));
+	const size_t bytes = o_points + up16(size_t(num_points) * sizeof(SwSimPoint) + 8);
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	int r;
+	if ((r = ensure(ctx, ctx->sim_buf, bytes))) return r;
+	void* h = nullptr;
+	if ((r = staging_acquire(ctx, ctx->stage_sims, bytes, &h))) return r;
+	unsigned char* hb = static_cast<unsigned char*>(h);
+	std::memcpy(hb, groups.data(), groups.size() * sizeof(SimGroup));
+	std::memcpy(hb + o_passes, passes, size_t(num_passes) * sizeof(SwSimPass));
+	if (num_points) std::memcpy(hb + o_points, points, size_t(num_points) * sizeof(SwSimPoint));
+	if ((r = staging_commit(ctx, ctx->stage_sims, ctx->sim_buf.ptr, bytes))) return r;
+	unsigned char* d = static_cast<unsigned char*>(ctx->sim_buf.ptr);
+	for (size_t l = 0; l < launch_first.size(); ++l)
+	{
+		SimArgs a;
+		std::memset(&a, 0, sizeof(a));
+		const uint32_t first = launch_first[l];
+		const uint32_t end = l + 1 < launch_first.size() ? launch_first[l + 1] : num_passes;
+		a.groups = reinterpret_cast<const SimGroup*>(d) + first;
+		a.passes = reinterpret_cast<const SwSimPass*>(d + o_passes);
+		a.points = reinterpret_cast<const SwSimPoint*>(d + o_points);
+		a.num_groups = end - first;
+		a.total_items = launch_items[l];
+		a.state = static_cast<uint32_t*>(ctx->sim_state.ptr);
+		a.texels = static_cast<uint64_t*>(ctx->texels.ptr);
+		a.emissive = static_cast<uint32_t*>(ctx->emissive.ptr);
+		if ((r = check_kernel(ctx, launch_simulation(a, ctx->stream), "simulation"))) return r;
+	}
+	return SW_OK;
+}
+
+int sw_read_simulation_state(SwCtx* ctx, uint64_t first, uint64_t count, uint32_t* out)
+{
+	if (!ctx || (count && !out)) return SW_ERR_INVALID_ARGUMENT;
+	if (first > ctx->sim_words || count > ctx->sim_words - first)
+		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "range outside the simulation state (%llu words)", (unsigned long long)ctx->sim_words);
+	SW_CUDA(ctx, cudaSetDevice(ctx->device));
+	SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	if (count) SW_CUDA(ctx, cudaMemcpy(out, static_cast<uint32_t*>(ctx->sim_state.ptr) + first, count * 4, cudaMemcpyDeviceToHost));
+	return SW_OK;
 }
 
 int sw_set_lightmaps_compressed(SwCtx* ctx, const void* lightmaps, uint64_t num_elements, const void* directional,
@@ -2664,16 +2835,16 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 
 int sw_abi_layout(uint32_t* sizes, uint32_t count)
 {
-	const uint32_t s[24] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
+	const uint32_t s[26] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
 		uint32_t(sizeof(SwDirectionalLightmapElement)), uint32_t(sizeof(SwLight)), uint32_t(sizeof(SwSurfaceDesc)),
 		uint32_t(sizeof(SwVertex16)), uint32_t(sizeof(SwDrawCmd)), uint32_t(sizeof(SwFrameParams)),
 		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats)), uint32_t(sizeof(SwFrameInput)), uint32_t(sizeof(SwTuning)),
 		uint32_t(sizeof(SwMapPolygon)), uint32_t(sizeof(SwViewLeaf)), uint32_t(sizeof(SwViewFrameInput)),
 		uint32_t(sizeof(SwViewCounts)), uint32_t(sizeof(SwLightShadow)), uint32_t(sizeof(SwDepthDraw)),
 		uint32_t(sizeof(SwShadowSide)), uint32_t(sizeof(SwShadowLeaf)), uint32_t(sizeof(SwMaterialFrame)),
-		uint32_t(sizeof(SwTriVertex)), uint32_t(sizeof(SwTexturePass))};
-	for (uint32_t i = 0; sizes && i < count && i < 24; ++i) sizes[i] = s[i];
-	return 24;
+		uint32_t(sizeof(SwTriVertex)), uint32_t(sizeof(SwTexturePass)), uint32_t(sizeof(SwSimPass)), uint32_t(sizeof(SwSimPoint))};
+	for (uint32_t i = 0; sizes && i < count && i < 26; ++i) sizes[i] = s[i];
+	return 26;
 }
 
 int sw_get_stats(SwCtx* ctx, SwStats* out)

@@ -1539,19 +1539,27 @@ void FramePrep::update_materials()
 		change_time[m] += cur.next_frame >= 0 ? cur.frame_duration : 0.5f;
 		if (change_time[m] < frame_time_s) change_time[m] = frame_time_s;
 	}
+	// update_animations (:249-303) runs after the framed animations and shifts, before anything reads the
+	// textures
+	update_texture_effects();
+	update_simulations();
 	material_frames.resize(n);
 	for (uint32_t m = 0; m < n; ++m)
 	{
-		// get_texture (:311-327): the current frame's generated texture when it has a generative effect;
-		// get_material and get_emissive_texture (:305-309, 336-360): the current frame's properties
+		// get_texture (:311-327): the current frame's generated texture when it has a generative effect
+		// (simulated ones once they have generated one); get_material and get_emissive_texture (:305-309,
+		// 336-360): the current frame's properties
 		const Material& cur = sc.materials[mapping[m]];
+		const EffectSim* sim = effect_sim(mapping[m]);
+		const bool generated = !sim || sim->generated();
 		SwMaterialFrame& f = material_frames[m];
 		f.shift[0] = shift[2 * mapping[m]];
 		f.shift[1] = shift[2 * mapping[m] + 1];
-		f.texture = cur.effect_texture >= 0 ? uint32_t(cur.effect_texture) : mapping[m];
+		f.texture = (cur.effect_texture >= 0 && generated) ? uint32_t(cur.effect_texture) : mapping[m];
 		f.flags = Scene::material_polygon_flags(cur);
 		f.blending_mode = cur.blending_mode;
 		f.emissive_texture = cur.emissive >= 0 ? uint32_t(cur.emissive) : SW_NO_EMISSIVE;
+		if (cur.emissive >= 0 && cur.effect_emissive >= 0 && generated) f.emissive_texture = uint32_t(cur.effect_emissive);
 		for (int c = 0; c < 3; ++c) f.emissive_light[c] = cur.emissive_light[c];
 		f.reserved = 0;
 		if (cur.effect != Material::NO_EFFECT) animated = true;
@@ -1565,7 +1573,37 @@ void FramePrep::update_materials()
 			for (int c = 0; c < 3; ++c) p.emissive_light[c] = f.emissive_light[c];
 		}
 	}
-	update_texture_effects();
+}
+
+void FramePrep::update_simulations()
+{
+	// the water and fire effects' GenerativeTextureEffect::update at the frame's time (their state persists
+	// from frame to frame; each is created, running its equilibrium steps, on its first update)
+	simulations.clear();
+	sims.resize(sc.materials.size());
+	for (uint32_t m = 0; m < uint32_t(sc.materials.size()); ++m)
+	{
+		const Material& mat = sc.materials[m];
+		if (mat.effect != Material::WATER && mat.effect != Material::FIRE) continue;
+		if (!sims[m]) sims[m].reset(new EffectSim(mat, mat.sim_state));
+		SimTextures t;
+		std::memset(&t, 0, sizeof(t));
+		t.source_texture = m;
+		t.output_texture = mat.effect_texture;
+		t.output_emissive = mat.effect_emissive;
+		t.source_emissive = mat.emissive;
+		// the source's last mip's first texel (water.rs:280), Material::roughness clamped (:289)
+		t.base_color = uint32_t(sc.texels[sc.texture_mips[size_t(m) * NUM_MIPS + NUM_MIPS - 1].offset]);
+		t.roughness = std::fmin(std::fmax(mat.roughness, 1.0f / 126.0f), 1.0f);
+		if (mat.emissive >= 0)
+		{
+			const SwEmissiveMip& em = sc.emissive_mips[size_t(mat.emissive) * NUM_MIPS];
+			t.emissive_width = em.width * em.height ? em.width : 0;
+			t.emissive_row = sc.emissive_pixels.data() + em.offset;
+		}
+		sims[m]->update(frame_time_s, t, simulations);
+	}
+	simulations.finish();
 }
 
 void FramePrep::update_texture_effects()

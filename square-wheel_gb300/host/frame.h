@@ -14,10 +14,12 @@
 // (in exact submission order) that the GPU path consumes.
 #pragma once
 
+#include <memory>
 #include <vector>
 
 #include "prep_math.h"
 #include "scene.h"
+#include "sims.h"
 
 namespace swhost
 {
@@ -143,6 +145,12 @@ public:
 	// the frame's generative texture effect passes (sw_update_textures) and their turbulence shifts
 	std::vector<SwTexturePass> texture_passes;
 	std::vector<int32_t> texture_shifts;
+	// the frame's simulated effect work (sw_update_simulations): water and fire steps, textures, mips
+	SimBatch simulations;
+	const EffectSim* effect_sim(uint32_t material) const
+	{
+		return material < sims.size() ? sims[material].get() : nullptr;
+	}
 	bool animated = false;
 	// Game time of the frame (prepare / prepare_view: frame index / 60 s; the *_with_camera forms keep it).
 	float frame_time_s = 0.0f;
@@ -194,6 +202,8 @@ private:
 	std::vector<float> change_time; // its frame_change_time_point
 	std::vector<std::vector<int32_t>> turb_buffers; // each turbulent material's temp_buffer (persists)
 	void update_texture_effects();
+	std::vector<std::unique_ptr<EffectSim>> sims; // each water / fire material's effect state (persists)
+	void update_simulations();
 	void begin_frame(const CameraMatrices& cam, const std::vector<SwLight>& lights, const FrameOptions& opt, Quat skybox_rotation);
 	void finish_params();
 	void camera_of_frame(uint32_t frame_index, const FrameOptions& opt, CameraMatrices& cam, std::vector<SwLight>& lights,

@@ -1181,6 +1181,40 @@ void add_effect_outputs(Scene& sc)
 	{
 		Material& mat = sc.materials[m];
 		if (mat.effect == Material::NO_EFFECT) continue;
+		if (mat.effect == Material::WATER || mat.effect == Material::FIRE)
+		{
+			// the simulation's output slot, the field's size, zero until the first generation (surfaces read
+			// the material's own texture until then, as get_texture / get_emissive_texture do)
+			const bool water = mat.effect == Material::WATER;
+			const uint32_t* lg = water ? mat.water.resolution_log2 : mat.fire.resolution_log2;
+			if (water) mat.effect_texture = int32_t(sc.texture_mips.size() / NUM_MIPS);
+			else mat.effect_emissive = int32_t(sc.emissive_mips.size() / NUM_MIPS);
+			for (uint32_t mip = 0; mip < NUM_MIPS; ++mip)
+			{
+				const uint32_t w = (1u << lg[0]) >> mip, h = (1u << lg[1]) >> mip;
+				if (water)
+				{
+					SwTextureMip tm;
+					std::memset(&tm, 0, sizeof(tm));
+					tm.offset = sc.texels.size();
+					tm.width = w;
+					tm.height = h;
+					// make_wavy_texture: a normal map, roughness below 1 when the material's is; is_metal the material's
+					tm.flags = SW_TEX_HAS_NORMAL_MAP | (mat.roughness < 1.0f ? SW_TEX_HAS_NON_ONE_ROUGHNESS : 0u) |
+						(mat.is_metal ? SW_TEX_IS_METAL : 0u);
+					sc.texels.resize(sc.texels.size() + size_t(w) * h, 0);
+					sc.texture_mips.push_back(tm);
+				}
+				else
+				{
+					sc.emissive_mips.push_back(SwEmissiveMip{sc.emissive_pixels.size(), w, h});
+					sc.emissive_pixels.resize(sc.emissive_pixels.size() + size_t(w) * h, 0);
+				}
+			}
+			mat.sim_state = sc.sim_state_words;
+			sc.sim_state_words += 2ull << (lg[0] + lg[1]);
+			continue;
+		}
 		const uint32_t src = mat.effect == Material::TURB ? uint32_t(m) : mat.layers[0].material;
 		mat.effect_texture = int32_t(sc.texture_mips.size() / NUM_MIPS);
 		for (uint32_t mip = 0; mip < NUM_MIPS; ++mip)
@@ -1202,11 +1236,142 @@ void add_effect_outputs(Scene& sc)
 
 } // namespace
 
+namespace
+{
+
+// Water and fire materials (their own generator): fire_materials materials from `first`, then
+// water_materials, each with sources of every kind, over the material's own texture.
+void add_simulated_effects(const SceneConfig& cfg, uint32_t first, Scene& sc)
+{
+	Rng r(cfg.seed ^ 0x5171u);
+	uint32_t size_log2 = 0;
+	while ((1u << size_log2) < cfg.texture_size) ++size_log2;
+	auto sine = [&](float amplitude, float offset) {
+		TimeFunction f;
+		f.kind = TimeFunction::SIN_WAVE;
+		f.a = r.uniform(0.1f, 0.8f);
+		f.b = r.uniform(0.0f, 6.28f);
+		f.c = amplitude;
+		f.d = offset;
+		return f;
+	};
+	auto constant = [](float c) {
+		TimeFunction f;
+		f.kind = TimeFunction::CONSTANT;
+		f.a = c;
+		return f;
+	};
+	auto deviated = [&](float value, float deviation) {
+		RandomValue v;
+		v.value = constant(value);
+		v.deviation = constant(deviation);
+		return v;
+	};
+	for (uint32_t i = 0; i < cfg.fire_materials; ++i)
+	{
+		Material& mat = sc.materials[first + i];
+		FireEffect& f = mat.fire;
+		f.resolution_log2[0] = std::max(4u, size_log2 - (i % 2));
+		f.resolution_log2[1] = std::max(4u, size_log2 - ((i / 2) % 2));
+		const uint32_t w = 1u << f.resolution_log2[0], h = 1u << f.resolution_log2[1];
+		f.update_frequency = r.uniform(24.0f, 60.0f);
+		f.heat_conductivity = r.uniform(8.0f, 30.0f);
+		f.slow = (i % 2) == 1;
+		f.has_color = (i % 3) == 0;
+		f.color[0] = 1.0f, f.color[1] = r.uniform(0.3f, 0.7f), f.color[2] = r.uniform(0.0f, 0.3f);
+		HeatSource point;
+		point.kind = HeatSource::POINT;
+		point.points[0][0] = w / 4, point.points[0][1] = h - 3;
+		point.offset[0][0] = deviated(0.0f, 3.0f);
+		point.offset[0][1] = deviated(0.0f, 1.0f);
+		point.heat = deviated(0.9f, 0.1f);
+		HeatSource line;
+		line.kind = HeatSource::LINE;
+		line.points[0][0] = 2, line.points[0][1] = h - 2, line.points[1][0] = w - 3, line.points[1][1] = h - 5;
+		line.heat.value = sine(0.3f, 0.7f);
+		HeatSource lightning;
+		lightning.kind = HeatSource::LIGHTNING;
+		lightning.points[0][0] = w / 2, lightning.points[0][1] = h - 4;
+		lightning.points[1][0] = w / 2 + w / 8, lightning.points[1][1] = h / 4;
+		lightning.offset[1][0] = deviated(0.0f, float(w) / 16.0f);
+		lightning.heat = deviated(1.0f, 0.0f);
+		lightning.ramp = (i % 2) == 0;
+		HeatSource fountain;
+		fountain.kind = HeatSource::FOUNTAIN;
+		fountain.points[0][0] = 3 * w / 4, fountain.points[0][1] = h - 6;
+		fountain.frequency = r.uniform(10.0f, 40.0f);
+		fountain.heat = deviated(0.8f, 0.2f);
+		fountain.angle = deviated(-1.5708f, 0.5f);
+		fountain.speed = deviated(float(h) * 0.6f, float(h) * 0.2f);
+		fountain.gravity = deviated(float(h) * 0.3f, 2.0f);
+		fountain.spawn_angle = deviated(0.0f, 3.14159f);
+		fountain.spawn_distance = deviated(2.0f, 2.0f);
+		fountain.lifetime = deviated(1.0f, 0.5f);
+		f.sources = {point, line, lightning, fountain};
+		mat.effect = Material::FIRE;
+		// the emissive layer the generated texture replaces (and, without a colour, the palette's source)
+		mat.emissive = int32_t(sc.emissive_mips.size() / NUM_MIPS);
+		make_emissive_texture(r, cfg.texture_size, sc);
+		mat.emissive_light[0] = r.uniform(1.0f, 3.0f);
+		mat.emissive_light[1] = r.uniform(0.5f, 2.0f);
+		mat.emissive_light[2] = r.uniform(0.5f, 1.0f);
+	}
+	for (uint32_t i = 0; i < cfg.water_materials; ++i)
+	{
+		const uint32_t m = first + cfg.fire_materials + i;
+		Material& mat = sc.materials[m];
+		WaterEffect& wcfg = mat.water;
+		// the second water material's field is narrower than its texture (the colour image is resized)
+		wcfg.resolution_log2[0] = i == 1 ? std::max(4u, size_log2 - 1) : size_log2;
+		wcfg.resolution_log2[1] = size_log2;
+		const uint32_t w = 1u << wcfg.resolution_log2[0], h = 1u << wcfg.resolution_log2[1];
+		wcfg.update_frequency = r.uniform(24.0f, 60.0f);
+		wcfg.fluidity = r.uniform(40.0f, 300.0f);
+		wcfg.color_mode = i % 4;
+		WaveSource spot;
+		spot.kind = WaveSource::WAVY_SPOT;
+		spot.points[0][0] = w / 3, spot.points[0][1] = h / 3;
+		spot.offsets[0][0] = sine(float(w) / 8.0f, 0.0f);
+		spot.frequency = r.uniform(0.5f, 2.0f);
+		spot.phase = r.uniform(0.0f, 6.0f);
+		spot.amplitude = r.uniform(0.5f, 2.0f);
+		WaveSource wline;
+		wline.kind = WaveSource::WAVY_LINE;
+		wline.points[0][0] = 1, wline.points[0][1] = h / 2, wline.points[1][0] = w / 2, wline.points[1][1] = h - 2;
+		wline.offsets[1][1] = sine(float(h) / 6.0f, 0.0f);
+		wline.frequency = r.uniform(0.5f, 2.0f);
+		wline.amplitude = r.uniform(0.2f, 1.0f);
+		wline.offset = r.uniform(-0.1f, 0.1f);
+		WaveSource steep = wline; // more rows than columns: the other rasterisation branch
+		steep.points[0][0] = w - 2, steep.points[0][1] = 1, steep.points[1][0] = w - 5, steep.points[1][1] = h / 2;
+		steep.offsets[1][1] = TimeFunction();
+		WaveSource drop;
+		drop.kind = WaveSource::PERIODIC_DROPLET;
+		drop.points[0][0] = 2 * w / 3, drop.points[0][1] = 2 * h / 3;
+		drop.frequency = r.uniform(1.0f, 4.0f);
+		drop.phase = 0.3f;
+		drop.amplitude = r.uniform(2.0f, 6.0f);
+		WaveSource rain;
+		rain.kind = WaveSource::RAIN;
+		rain.points[0][0] = w / 2, rain.points[0][1] = h / 2;
+		rain.frequency = r.uniform(5.0f, 20.0f);
+		rain.radius = (i % 2) ? 0.0f : float(w) / 4.0f;
+		rain.amplitude = r.uniform(1.0f, 4.0f);
+		wcfg.sources = {spot, wline, steep, drop, rain};
+		mat.effect = Material::WATER;
+		mat.roughness = r.uniform(0.2f, 0.6f);
+		mat.is_metal = (sc.texture_mips[size_t(m) * NUM_MIPS].flags & SW_TEX_IS_METAL) != 0;
+	}
+}
+
+} // namespace
+
 void add_texture_effects(const SceneConfig& cfg, uint32_t n_metal, uint32_t n_diel, Scene& sc)
 {
 	Rng erng(cfg.seed ^ 0xEFFEC7u);
 	const uint32_t nb = cfg.num_materials;
 	const uint32_t first = nb - cfg.layered_materials - cfg.turb_materials;
+	add_simulated_effects(cfg, first - cfg.water_materials - cfg.fire_materials, sc);
 	auto wave = [&](uint32_t kind, float amplitude, float offset) {
 		TimeFunction f;
 		f.kind = kind;
@@ -1299,10 +1464,11 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 		error = "tile_size must lie in [16, 256] (lightmaps stay within 17 texels)";
 		return false;
 	}
-	if (uint64_t(cfg.turb_materials) + cfg.layered_materials + std::max(cfg.animated_materials, cfg.scrolling_materials) >
+	if (uint64_t(cfg.turb_materials) + cfg.layered_materials + cfg.water_materials + cfg.fire_materials +
+			std::max(cfg.animated_materials, cfg.scrolling_materials) >
 		cfg.num_materials)
 	{
-		error = "turb_materials + layered_materials + max(animated_materials, scrolling_materials) exceed num_materials";
+		error = "fire, water, turb and layered materials + max(animated_materials, scrolling_materials) exceed num_materials";
 		return false;
 	}
 	if (cfg.texture_size < 16 || (cfg.texture_size & (cfg.texture_size - 1)) || cfg.num_materials == 0)
@@ -1415,7 +1581,7 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 	// layered_materials base materials are layered animations over their own texture and three layer
 	// materials (appended; no polygon uses them) with other blending modes; the turb_materials before
 	// them are turbulent. Effect materials get no emissive layer.
-	if (cfg.turb_materials || cfg.layered_materials)
+	if (cfg.turb_materials || cfg.layered_materials || cfg.water_materials || cfg.fire_materials)
 		add_texture_effects(cfg, n_metal, n_diel, sc);
 
 	sc.basis.resize(sc.polygons.size());

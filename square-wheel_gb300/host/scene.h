@@ -82,6 +82,64 @@ struct EffectLayer
 	TimeFunction modulate_color[3];
 };
 
+// WaterEffect (src/common/material_water.rs): a wave field simulated at update_frequency steps per second,
+// disturbed by wave sources; its normals (and, per colour mode, a deformed copy of the material's colours)
+// make the output texture.
+struct WaveSource
+{
+	enum Kind : uint32_t
+	{
+		WAVY_SPOT = 0,        // sine at points[0] (+ offsets[0])
+		WAVY_LINE = 1,        // sine along points[0] - points[1] (+ offsets)
+		PERIODIC_DROPLET = 2, // `amplitude` at points[0] (+ offsets[0]) `frequency` times per second
+		RAIN = 3,             // random droplets within `radius` of points[0] (anywhere for radius 0)
+	};
+	uint32_t kind = WAVY_SPOT;
+	uint32_t points[2][2] = {{0, 0}, {0, 0}};
+	TimeFunction offsets[2][2]; // center_offset = offsets[0], points_offset
+	float frequency = 1.0f, phase = 0.0f, amplitude = 1.0f, offset = 0.0f, radius = 0.0f;
+};
+struct WaterEffect
+{
+	uint32_t resolution_log2[2] = {4, 4};
+	float update_frequency = 30.0f, fluidity = 200.0f;
+	uint32_t color_mode = 0; // ColorTextureApplyMode: single colour, source texture, deformed, deformed along x
+	std::vector<WaveSource> sources;
+};
+// ValueWithRandomDeviation: value - deviation + uniform [0, 2 max(deviation, 0)]
+struct RandomValue
+{
+	TimeFunction value, deviation;
+};
+// FireEffect (src/common/material_fire.rs): a heat map propagated upwards at update_frequency steps per
+// second from heat sources; a palette maps it to the output emissive texture.
+struct HeatSource
+{
+	enum Kind : uint32_t
+	{
+		POINT = 0,     // heat at points[0] + offset[0]
+		LINE = 1,      // heat along points[0] - points[1]
+		LIGHTNING = 2, // a jittered line between points (+ offset), heat optionally ramped
+		FOUNTAIN = 3,  // particles emitted from points[0]
+	};
+	uint32_t kind = POINT;
+	uint32_t points[2][2] = {{0, 0}, {0, 0}};
+	RandomValue offset[2][2]; // POINT: offset[0]; LIGHTNING: per point and coordinate
+	RandomValue heat;
+	bool ramp = false;
+	float frequency = 1.0f; // FOUNTAIN: particles per second
+	RandomValue angle, speed, gravity, spawn_angle, spawn_distance, lifetime;
+};
+struct FireEffect
+{
+	uint32_t resolution_log2[2] = {4, 4};
+	float update_frequency = 30.0f, heat_conductivity = 20.0f;
+	bool slow = false;
+	bool has_color = false;
+	float color[3] = {1.0f, 1.0f, 1.0f};
+	std::vector<HeatSource> sources;
+};
+
 // Material flags the renderer reads (src/common/material.rs): draw, light, diffuse layer, blending,
 // optional emissive layer.
 struct Material
@@ -106,9 +164,17 @@ struct Material
 		NO_EFFECT = 0,
 		TURB = 1,
 		LAYERED = 2,
+		WATER = 3, // output texture effect_texture (the field's size)
+		FIRE = 4,  // output emissive texture effect_emissive (the heat map's size)
 	};
 	uint32_t effect = NO_EFFECT;
 	int32_t effect_texture = -1;
+	int32_t effect_emissive = -1;
+	uint64_t sim_state = 0; // WATER / FIRE: word offset of its two fields / heat maps in the simulation state
+	float roughness = 1.0f; // Material::roughness (WATER: the output's roughness)
+	bool is_metal = false;
+	WaterEffect water;
+	FireEffect fire;
 	float turb_amplitude = 0.0f, turb_wave_length = 1.0f, turb_frequency = 0.0f; // TurbParams
 	std::vector<EffectLayer> layers;                                              // LayeredAnimation
 };
@@ -244,6 +310,8 @@ struct SceneConfig
 	uint32_t num_decals = 0;          // decals on the rooms' walls and floors
 	uint32_t turb_materials = 0;      // the last base materials but layered_materials have a turbulence effect
 	uint32_t layered_materials = 0;   // the last this many base materials are layered animations
+	uint32_t water_materials = 0;     // before the turbulence ones: water effects
+	uint32_t fire_materials = 0;      // before the water ones: fire effects
 };
 
 struct Scene
@@ -258,6 +326,7 @@ struct Scene
 	std::vector<float> lightmaps; // [f32; 3] elements, element 0 unused
 	std::vector<SwDirectionalLightmapElement> directional_lightmaps;
 	std::vector<Material> materials;
+	uint64_t sim_state_words = 0; // the simulated effects' device state (sw_reserve_simulation_state)
 	std::vector<uint64_t> texels; // TextureElement raw values of all materials' mips
 	std::vector<SwTextureMip> texture_mips; // material * NUM_MIPS + mip
 	std::vector<uint32_t> emissive_pixels;

@@ -50,6 +50,12 @@ int submit_shadows(SwhRenderer* r, const FramePrep& p)
 			p.texture_shifts.data(), uint32_t(p.texture_shifts.size()));
 		if (st) return st;
 	}
+	if (!p.simulations.passes.empty())
+	{
+		const int st = sw_update_simulations(r->ctx, p.simulations.passes.data(), uint32_t(p.simulations.passes.size()),
+			p.simulations.points.data(), uint32_t(p.simulations.points.size()));
+		if (st) return st;
+	}
 	if (p.shadow_texels == 0)
 	{
 		if (!r->shadows_set) return SW_OK;
@@ -144,6 +150,8 @@ int scene_config_from(const SwhSceneConfig* c, SceneConfig& cfg)
 	cfg.num_sprites = c->num_sprites;
 	cfg.num_decals = c->num_decals;
 	cfg.layered_materials = c->layered_materials;
+	cfg.water_materials = c->water_materials;
+	cfg.fire_materials = c->fire_materials;
 	if (cfg.num_models > 100000 || cfg.model_triangles > 200000 || cfg.model_frames > 256 || cfg.num_sprites > 1000000 ||
 		cfg.num_decals > 1000000)
 	{
@@ -308,6 +316,96 @@ int swh_scene_texture_effect(const SwhScene* s, uint32_t material, SwhTextureEff
 	return SW_OK;
 }
 
+namespace
+{
+SwhTimeFunction flat_function(const TimeFunction& f) { return SwhTimeFunction{f.kind, f.a, f.b, f.c, f.d}; }
+SwhRandomValue flat_random(const RandomValue& v) { return SwhRandomValue{flat_function(v.value), flat_function(v.deviation)}; }
+} // namespace
+
+int swh_scene_simulated_effect(const SwhScene* s, uint32_t material, SwhSimEffect* out)
+{
+	if (!s || !out || material >= s->scene.materials.size()) return SW_ERR_INVALID_ARGUMENT;
+	const Material& m = s->scene.materials[material];
+	std::memset(out, 0, sizeof(*out));
+	out->output_texture = m.effect_texture;
+	out->output_emissive = m.effect_emissive;
+	out->source_emissive = m.emissive;
+	out->roughness = m.roughness;
+	out->state_offset = m.sim_state;
+	if (m.effect == Material::WATER)
+	{
+		const WaterEffect& w = m.water;
+		out->kind = m.effect;
+		out->resolution_log2[0] = w.resolution_log2[0];
+		out->resolution_log2[1] = w.resolution_log2[1];
+		out->update_frequency = w.update_frequency;
+		out->attenuation_param = w.fluidity;
+		out->color_mode = w.color_mode;
+		if (w.sources.size() > SWH_MAX_SIM_SOURCES) return SW_ERR_LIMIT;
+		out->num_sources = uint32_t(w.sources.size());
+		for (size_t i = 0; i < w.sources.size(); ++i)
+		{
+			const WaveSource& a = w.sources[i];
+			SwhSimSource& o = out->sources[i];
+			o.kind = a.kind;
+			for (int p = 0; p < 2; ++p)
+				for (int c = 0; c < 2; ++c)
+				{
+					o.points[p][c] = a.points[p][c];
+					o.offsets[p][c] = flat_function(a.offsets[p][c]);
+				}
+			o.frequency = a.frequency;
+			o.phase = a.phase;
+			o.amplitude = a.amplitude;
+			o.offset = a.offset;
+			o.radius = a.radius;
+		}
+	}
+	else if (m.effect == Material::FIRE)
+	{
+		const FireEffect& f = m.fire;
+		out->kind = m.effect;
+		out->resolution_log2[0] = f.resolution_log2[0];
+		out->resolution_log2[1] = f.resolution_log2[1];
+		out->update_frequency = f.update_frequency;
+		out->attenuation_param = f.heat_conductivity;
+		out->slow = f.slow ? 1u : 0u;
+		out->has_color = f.has_color ? 1u : 0u;
+		for (int c = 0; c < 3; ++c) out->color[c] = f.color[c];
+		if (f.sources.size() > SWH_MAX_SIM_SOURCES) return SW_ERR_LIMIT;
+		out->num_sources = uint32_t(f.sources.size());
+		for (size_t i = 0; i < f.sources.size(); ++i)
+		{
+			const HeatSource& a = f.sources[i];
+			SwhSimSource& o = out->sources[i];
+			o.kind = a.kind;
+			for (int p = 0; p < 2; ++p)
+				for (int c = 0; c < 2; ++c)
+				{
+					o.points[p][c] = a.points[p][c];
+					o.fire_offsets[p][c] = flat_random(a.offset[p][c]);
+				}
+			o.frequency = a.frequency;
+			o.ramp = a.ramp ? 1u : 0u;
+			o.heat = flat_random(a.heat);
+			o.angle = flat_random(a.angle);
+			o.speed = flat_random(a.speed);
+			o.gravity = flat_random(a.gravity);
+			o.spawn_angle = flat_random(a.spawn_angle);
+			o.spawn_distance = flat_random(a.spawn_distance);
+			o.lifetime = flat_random(a.lifetime);
+		}
+	}
+	return SW_OK;
+}
+
+int swh_scene_simulation_words(const SwhScene* s, uint64_t* out)
+{
+	if (!s || !out) return SW_ERR_INVALID_ARGUMENT;
+	*out = s->scene.sim_state_words;
+	return SW_OK;
+}
+
 int swh_scene_info(const SwhScene* s, SwhSceneInfo* out)
 {
 	if (!s || !out) return SW_ERR_INVALID_ARGUMENT;
@@ -447,6 +545,19 @@ int swh_frame_view_input(const SwhFrame* f, SwViewFrameInput* out)
 	return SW_OK;
 }
 
+int swh_frame_effect_state(const SwhFrame* f, uint32_t material, uint32_t* out_update_step, uint32_t* out_current_buffer,
+	uint32_t* out_generated, uint32_t* out_particles)
+{
+	if (!f || !out_update_step || !out_current_buffer || !out_generated || !out_particles) return SW_ERR_INVALID_ARGUMENT;
+	const EffectSim* e = f->prep.effect_sim(material);
+	if (!e) return SW_ERR_INVALID_ARGUMENT;
+	*out_update_step = e->update_step();
+	*out_current_buffer = e->current_buffer();
+	*out_generated = e->generated() ? 1u : 0u;
+	*out_particles = e->num_particles();
+	return SW_OK;
+}
+
 int swh_frame_outputs(const SwhFrame* f, SwhFrameOutputs* out)
 {
 	if (!f || !out) return SW_ERR_INVALID_ARGUMENT;
@@ -481,6 +592,10 @@ int swh_frame_outputs(const SwhFrame* f, SwhFrameOutputs* out)
 	out->num_texture_passes = uint32_t(p.texture_passes.size());
 	out->texture_shifts = p.texture_shifts.data();
 	out->num_texture_shifts = uint32_t(p.texture_shifts.size());
+	out->sim_passes = p.simulations.passes.data();
+	out->num_sim_passes = uint32_t(p.simulations.passes.size());
+	out->sim_points = p.simulations.points.data();
+	out->num_sim_points = uint32_t(p.simulations.points.size());
 	return SW_OK;
 }
 
@@ -531,6 +646,13 @@ int swh_renderer_create(const SwhScene* s, uint32_t device, SwhRenderer** out)
 		(st = sw_set_skybox(r->ctx, s->scene.skybox32.data(), s->scene.skybox64.data(), s->scene.skybox32.size())) != SW_OK)
 	{
 		g_error = "sw_set_skybox failed";
+		sw_destroy(r->ctx);
+		delete r;
+		return st;
+	}
+	if (s->scene.sim_state_words && (st = sw_reserve_simulation_state(r->ctx, s->scene.sim_state_words)) != SW_OK)
+	{
+		g_error = std::string("sw_reserve_simulation_state failed: ") + sw_last_error(r->ctx);
 		sw_destroy(r->ctx);
 		delete r;
 		return st;

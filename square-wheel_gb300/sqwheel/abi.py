@@ -54,6 +54,14 @@ VERTEX16 = np.dtype([("x", "<i4"), ("y", "<i4")], align=True)
 TEXTURE_PASS = np.dtype([("kind", "<u4"), ("dst_mip", "<u4"), ("src_mip", "<u4"), ("blending_mode", "<u4"),
                          ("shift", "<i4", 2), ("light", "<f4", 3), ("shifts_offset", "<u4")], align=True)
 SW_TEXPASS_TURB, SW_TEXPASS_LAYER, SW_TEXPASS_EMISSIVE = 1, 2, 0x100
+# SwSimPass / SwSimPoint (sw_update_simulations): simulated water and fire effects
+SIM_PASS = np.dtype([("kind", "<u4"), ("launch", "<u4"), ("size_log2", "<u4", 2), ("state_src", "<u8"),
+                     ("state_dst", "<u8"), ("first_point", "<u4"), ("num_points", "<u4"), ("dst_mip", "<u4"),
+                     ("src_mip", "<u4"), ("flags", "<u4"), ("param", "<u4"), ("base_color", "<u4"), ("reserved", "<u4")])
+SIM_POINT = np.dtype([("address", "<u4"), ("value", "<u4")])
+(SW_SIM_WATER_POINTS, SW_SIM_WATER_STEP, SW_SIM_FIRE_STEP, SW_SIM_FIRE_POINTS, SW_SIM_WATER_TEXTURE,
+ SW_SIM_FIRE_TEXTURE, SW_SIM_TEXTURE_MIP, SW_SIM_EMISSIVE_MIP) = range(1, 9)
+SW_SIM_FIRE_SLOW, SW_SIM_WATER_INIT_DIFFUSE, SW_SIM_COLOR_MODE_SHIFT = 1, 2, 8
 TRI_VERTEX = np.dtype([("x", "<i4"), ("y", "<i4"), ("tc", "<i4", 2), ("light", "<i4", 3), ("reserved", "<i4")], align=True)
 DRAW_CMD = np.dtype([
     ("first_vertex", "<u4"), ("vertex_count", "<u4"), ("mode", "<u4"), ("blend", "<u4"), ("depth_eq", "<f4", 3),
@@ -171,7 +179,7 @@ LAYOUT_ORDER = [
     ("SwLightShadow", LIGHT_SHADOW.itemsize), ("SwDepthDraw", DEPTH_DRAW.itemsize),
     ("SwShadowSide", SHADOW_SIDE.itemsize), ("SwShadowLeaf", SHADOW_LEAF.itemsize),
     ("SwMaterialFrame", MATERIAL_FRAME.itemsize), ("SwTriVertex", TRI_VERTEX.itemsize),
-    ("SwTexturePass", TEXTURE_PASS.itemsize),
+    ("SwTexturePass", TEXTURE_PASS.itemsize), ("SwSimPass", SIM_PASS.itemsize), ("SwSimPoint", SIM_POINT.itemsize),
 ]
 
 

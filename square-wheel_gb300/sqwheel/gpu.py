@@ -21,7 +21,8 @@ LIB_PATH = os.path.join(PKG_DIR, "lib", "libswgpu.so")
 EXPORTED = [
     "sw_create", "sw_destroy", "sw_last_error", "sw_sync", "sw_frame_begin", "sw_submit_surfaces", "sw_rebuild_surfaces", "sw_rebuild_surfaces_per_surface", "sw_set_surfaces", "sw_set_skybox", "sw_register_host_buffer", "sw_unregister_host_buffer",
     "sw_submit_draws", "sw_submit_draws_ex", "sw_set_lite_textures", "sw_set_lightmaps_compressed", "sw_read_lightmaps",
-    "sw_update_textures", "sw_read_texels",
+    "sw_update_textures", "sw_read_texels", "sw_reserve_simulation_state", "sw_update_simulations",
+    "sw_read_simulation_state",
     "sw_render", "sw_postprocess", "sw_upscale", "sw_read_surfaces", "sw_read_framebuffer", "sw_get_exposure", "sw_set_exposure",
     "sw_set_framebuffer", "sw_get_stats", "sw_get_stream", "sw_abi_layout", "sw_enable_timing", "sw_get_timings",
     "sw_postprocess_noalloc", "sw_set_learned_upscaler", "sw_draw_frame", "sw_set_frame_graph", "sw_set_frames_in_flight", "sw_set_tuning",
@@ -69,6 +70,9 @@ def load_library(path=LIB_PATH):
         "sw_set_lightmaps_compressed": ([vp, vp, u64, vp, u64], i32),
         "sw_update_textures": ([vp, vp, u32, vp, u32], i32),
         "sw_read_texels": ([vp, vp, u64, vp, u64], i32),
+        "sw_reserve_simulation_state": ([vp, u64], i32),
+        "sw_update_simulations": ([vp, vp, u32, vp, u32], i32),
+        "sw_read_simulation_state": ([vp, u64, u64, vp], i32),
         "sw_read_lightmaps": ([vp, vp, u64, vp, u64], i32),
         "sw_render": ([vp, vp, u32, i32], i32),
         "sw_postprocess": ([vp, vp, f32, vp, vp, u32, i32], i32),
@@ -285,6 +289,22 @@ class GpuRenderer:
         shifts = np.ascontiguousarray(shifts if shifts is not None else np.zeros(0, np.int32), dtype=np.int32)
         self._check(self.lib.sw_update_textures(self.ctx, abi.ptr(passes), passes.size, abi.ptr(shifts), shifts.size),
                     "sw_update_textures")
+
+    def reserve_simulation_state(self, words):
+        self._check(self.lib.sw_reserve_simulation_state(self.ctx, int(words)), "sw_reserve_simulation_state")
+
+    def update_simulations(self, passes, points):
+        """Run simulated texture effect passes (abi.SIM_PASS, sorted by launch) with their points (abi.SIM_POINT)."""
+        passes = np.ascontiguousarray(passes, dtype=abi.SIM_PASS)
+        points = np.ascontiguousarray(points if points is not None else np.zeros(0, abi.SIM_POINT), dtype=abi.SIM_POINT)
+        self._check(self.lib.sw_update_simulations(self.ctx, abi.ptr(passes), passes.size, abi.ptr(points), points.size),
+                    "sw_update_simulations")
+
+    def read_simulation_state(self, first, count):
+        out = np.empty(int(count), np.uint32)
+        self._check(self.lib.sw_read_simulation_state(self.ctx, int(first), out.size, abi.ptr(out)),
+                    "sw_read_simulation_state")
+        return out
 
     def read_texels(self, num_texels, num_emissive=0):
         """The context's material texels (uint64) and emissive pixels (uint32), e.g. after texture passes."""

@@ -26,7 +26,7 @@ class SceneConfig(ctypes.Structure):
         ("camera_pitch", ctypes.c_float), ("shadowed_lights", ctypes.c_uint32), ("scrolling_materials", ctypes.c_uint32),
         ("animated_materials", ctypes.c_uint32), ("projector_lights", ctypes.c_uint32), ("num_models", ctypes.c_uint32), ("model_triangles", ctypes.c_uint32),
         ("model_frames", ctypes.c_uint32), ("turb_materials", ctypes.c_uint32), ("layered_materials", ctypes.c_uint32), ("num_sprites", ctypes.c_uint32),
-        ("num_decals", ctypes.c_uint32),
+        ("num_decals", ctypes.c_uint32), ("water_materials", ctypes.c_uint32), ("fire_materials", ctypes.c_uint32),
     ]
 
 
@@ -41,6 +41,38 @@ class SceneInfo(ctypes.Structure):
 class TextureEffectInfo(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_uint32), ("output_texture", ctypes.c_int32), ("num_layers", ctypes.c_uint32),
                 ("turb", ctypes.c_float * 3)]
+
+
+class TimeFunction(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("a", ctypes.c_float), ("b", ctypes.c_float), ("c", ctypes.c_float),
+                ("d", ctypes.c_float)]
+
+
+class RandomValue(ctypes.Structure):
+    _fields_ = [("value", TimeFunction), ("deviation", TimeFunction)]
+
+
+class SimSource(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("points", (ctypes.c_uint32 * 2) * 2), ("offsets", (TimeFunction * 2) * 2),
+                ("frequency", ctypes.c_float), ("phase", ctypes.c_float), ("amplitude", ctypes.c_float),
+                ("offset", ctypes.c_float), ("radius", ctypes.c_float), ("ramp", ctypes.c_uint32),
+                ("fire_offsets", (RandomValue * 2) * 2), ("heat", RandomValue), ("angle", RandomValue),
+                ("speed", RandomValue), ("gravity", RandomValue), ("spawn_angle", RandomValue),
+                ("spawn_distance", RandomValue), ("lifetime", RandomValue)]
+
+
+MAX_SIM_SOURCES = 8
+EFFECT_WATER, EFFECT_FIRE = 3, 4
+
+
+class SimEffect(ctypes.Structure):
+    """SwhSimEffect: a material's water or fire effect, flattened (the oracle takes the same bytes)."""
+    _fields_ = [("kind", ctypes.c_uint32), ("resolution_log2", ctypes.c_uint32 * 2), ("update_frequency", ctypes.c_float),
+                ("attenuation_param", ctypes.c_float), ("color_mode", ctypes.c_uint32), ("slow", ctypes.c_uint32),
+                ("has_color", ctypes.c_uint32), ("color", ctypes.c_float * 3), ("roughness", ctypes.c_float),
+                ("output_texture", ctypes.c_int32), ("output_emissive", ctypes.c_int32),
+                ("source_emissive", ctypes.c_int32), ("num_sources", ctypes.c_uint32), ("state_offset", ctypes.c_uint64),
+                ("sources", SimSource * MAX_SIM_SOURCES)]
 
 
 class FrameOptions(ctypes.Structure):
@@ -62,7 +94,8 @@ class FrameOutputs(ctypes.Structure):
                 ("tri_vertices", ctypes.c_void_p), ("num_tri_vertices", ctypes.c_uint32),
                 ("model_triangles", ctypes.c_uint32), ("texture_passes", ctypes.c_void_p),
                 ("num_texture_passes", ctypes.c_uint32), ("num_texture_shifts", ctypes.c_uint32),
-                ("texture_shifts", ctypes.c_void_p)]
+                ("texture_shifts", ctypes.c_void_p), ("sim_passes", ctypes.c_void_p),
+                ("num_sim_passes", ctypes.c_uint32), ("num_sim_points", ctypes.c_uint32), ("sim_points", ctypes.c_void_p)]
 
 
 def load_host_library():
@@ -94,6 +127,10 @@ def load_host_library():
         "swh_scene_load_map_memory": ([vp, ctypes.c_uint64, vp, ctypes.POINTER(vp)], i32),
         "swh_scene_save_map": ([vp, ctypes.c_char_p], i32),
         "swh_scene_texture_effect": ([vp, u32, vp], i32),
+        "swh_scene_simulated_effect": ([vp, u32, vp], i32),
+        "swh_scene_simulation_words": ([vp, ctypes.POINTER(ctypes.c_uint64)], i32),
+        "swh_frame_effect_state": ([vp, u32, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u32),
+                                    ctypes.POINTER(u32)], i32),
         "swh_scene_compressed_lightmaps": ([vp, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(vp),
                                             ctypes.POINTER(ctypes.c_uint64)], i32),
     }
@@ -112,7 +149,8 @@ HOST_EXPORTED = ["swh_scene_create", "swh_scene_destroy", "swh_scene_info", "swh
                  "swh_renderer_render_frame", "swh_frame_prepare_view", "swh_frame_view_input",
                  "swh_renderer_set_gpu_prep", "swh_frame_map", "swh_renderer_set_frames_in_flight",
                  "swh_scene_lite_textures", "swh_scene_load_map", "swh_scene_load_map_memory", "swh_scene_save_map",
-                 "swh_scene_compressed_lightmaps", "swh_scene_texture_effect"]
+                 "swh_scene_compressed_lightmaps", "swh_scene_texture_effect", "swh_scene_simulated_effect",
+                 "swh_scene_simulation_words", "swh_frame_effect_state"]
 
 # The two map configurations of the benchmark plan.
 SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, num_materials=16, metal_frac=0.0,
@@ -171,6 +209,18 @@ class Scene:
         e = TextureEffectInfo()
         _check(self.lib, self.lib.swh_scene_texture_effect(self.handle, material, ctypes.byref(e)), "swh_scene_texture_effect")
         return int(e.kind), int(e.output_texture), int(e.num_layers), tuple(e.turb)
+
+    def simulated_effect(self, material):
+        """The material's water / fire effect as a SimEffect (kind 0 for other materials)."""
+        e = SimEffect()
+        _check(self.lib, self.lib.swh_scene_simulated_effect(self.handle, material, ctypes.byref(e)),
+               "swh_scene_simulated_effect")
+        return e
+
+    def simulation_words(self):
+        n = ctypes.c_uint64()
+        _check(self.lib, self.lib.swh_scene_simulation_words(self.handle, ctypes.byref(n)), "swh_scene_simulation_words")
+        return int(n.value)
 
     def save_map(self, path):
         _check(self.lib, self.lib.swh_scene_save_map(self.handle, os.fsencode(path)), "swh_scene_save_map")
@@ -272,6 +322,13 @@ class Frame:
         _check(self.lib, self.lib.swh_frame_prepare(self.handle, frame_index, ctypes.byref(options)), "swh_frame_prepare")
         return self._outputs()
 
+    def effect_state(self, material):
+        """(update_step, current_buffer, generated, particles) of a simulated effect after the last prepared frame."""
+        v = [ctypes.c_uint32() for _ in range(4)]
+        _check(self.lib, self.lib.swh_frame_effect_state(self.handle, material, *[ctypes.byref(x) for x in v]),
+               "swh_frame_effect_state")
+        return tuple(int(x.value) for x in v)
+
     def map_data(self):
         """Copies of the map's world polygons (abi.MAP_POLYGON) and vertices (float32, n x 3) as sw_set_map
         takes them."""
@@ -300,6 +357,8 @@ class Frame:
         self.model_triangles = int(o.model_triangles)
         self.texture_passes = arr(o.texture_passes, o.num_texture_passes, abi.TEXTURE_PASS)
         self.texture_shifts = arr(o.texture_shifts, o.num_texture_shifts, np.int32)
+        self.sim_passes = arr(o.sim_passes, o.num_sim_passes, abi.SIM_PASS)
+        self.sim_points = arr(o.sim_points, o.num_sim_points, abi.SIM_POINT)
         self.lights = arr(o.lights, o.num_lights, abi.LIGHT)
         self.total_texels = int(o.total_texels)
         self.params = abi.FrameParams()
