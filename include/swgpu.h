@@ -480,6 +480,28 @@ int sw_get_stream(SwCtx* ctx, void** out_stream);
  * device work (uploads, surface build, raster setup and tiles, postprocess, exposure readback) is
  * captured into one CUDA graph: the first frame instantiates it, later frames update it in place and
  * replay it, so the kernels run back to back without host submission gaps. */
+/* A nested view of a whole frame (sw_draw_frame): a portal's texture (build_view_portals_textures,
+ * partial_renderer.rs:2008-2283) rendered before the frame's own draws. Its render target is the
+ * width x height region of the surface arena at target_offset (row pitch = width), cleared to black, then
+ * drawn from draws [first_draw, first_draw + num_draws) (background first if clear_background) and
+ * finally mixed with the portal's texture (mix_surface_with_texture, surfaces.rs:854-971): the lite
+ * texture mip of mix_size pixels at mix_offset (SwCreateInfo lite pixels, sw_set_lite_textures),
+ * tiled from mix_tc_min, modulated by mix_light, blended with mix_blend (SW_VIEW_NO_MIX: no texture).
+ * A view may sample regions that earlier views rendered; views render in array order. */
+#define SW_VIEW_NO_MIX 0xFFFFFFFFu
+typedef struct SwView {
+	uint64_t target_offset;
+	uint32_t width, height;
+	uint32_t first_draw, num_draws;
+	uint32_t clear_background;
+	uint32_t mix_blend;
+	uint64_t mix_offset;
+	uint32_t mix_size[2];
+	int32_t mix_tc_min[2];
+	float mix_light[3];
+	uint32_t reserved;
+} SwView;
+
 typedef struct SwFrameInput {
 	SwFrameParams params;
 	uint32_t num_lights;
@@ -500,6 +522,9 @@ typedef struct SwFrameInput {
 	int32_t dst_is_device;
 	const SwTriVertex* tri_vertices; /* vertices of the SW_RASTER_TRIANGLE draws */
 	uint32_t num_tri_vertices;
+	uint32_t num_views;        /* nested views (portal textures), rendered first; 0: none */
+	const SwView* views;
+	uint32_t main_draws;       /* with views: the frame's own draws are [0, main_draws) */
 	uint32_t reserved;
 } SwFrameInput;
 int sw_draw_frame(SwCtx* ctx, const SwFrameInput* frame);

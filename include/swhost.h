@@ -51,6 +51,8 @@ typedef struct SwhSceneConfig {
 	uint32_t num_decals;          /* decals on the rooms' walls and floors (every blending mode) */
 	uint32_t water_materials;     /* base materials with a water effect (before the turbulence ones) */
 	uint32_t fire_materials;      /* base materials with a fire effect (before the water ones) */
+	uint32_t num_portals;         /* portals (mirrors, cameras, parallax windows) in the camera path's rooms */
+	uint32_t portals_depth;       /* RendererConfig::portals_depth: nested portal view levels (the reference's default is 2; at most 8; 0: portals show black mixed with their texture) */
 } SwhSceneConfig;
 
 typedef struct SwhSceneInfo {
@@ -201,6 +203,13 @@ typedef struct SwhFrameOutputs {
 	uint32_t num_sim_passes;
 	uint32_t num_sim_points;
 	const SwSimPoint* sim_points;
+	/* portal views (SwFrameInput.views): rendered before the frame's own draws [0, main_draws); the
+	 * draws after them are the views'; total_texels spans the surfaces (surface_texels), the portal
+	 * textures and the nested views' arenas */
+	const SwView* views;
+	uint32_t num_views;
+	uint32_t main_draws;
+	uint64_t surface_texels;
 } SwhFrameOutputs;
 
 typedef struct SwhFrame SwhFrame;

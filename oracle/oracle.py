@@ -51,6 +51,7 @@ def load():
     lib.orc_sim_state.argtypes = [vp, vp, u64, vp, vp, vp]
     lib.orc_xoshiro_outputs.argtypes = [vp, vp, u32]
     lib.orc_small_rng_state.argtypes = [u64, vp]
+    lib.orc_mix_view.argtypes = [vp, vp, u32, vp, u64]
     for name in ("orc_compress_lightmaps", "orc_decompress_lightmaps", "orc_compress_directional_lightmaps",
                  "orc_decompress_directional_lightmaps"):
         getattr(lib, name).argtypes = [vp, u64, vp]
@@ -259,3 +260,28 @@ def small_rng_state(seed):
     out = np.zeros(4, np.uint64)
     load().orc_small_rng_state(seed, abi.ptr(out))
     return out
+
+
+def render_views(views, draws, vertices, arena, frame_params, tri_vertices=None, lite=None, skybox=None, num_threads=1):
+    """The nested views of a whole frame (SwView), in order, into the arena: each region cleared to black,
+    its background drawn when it says so, rasterised from its draws and mixed with its texture."""
+    lt = np.ascontiguousarray(lite if lite is not None else np.zeros(1, np.uint32), dtype=np.uint32).reshape(-1)
+    for v in np.atleast_1d(views):
+        w, h = int(v["width"]), int(v["height"])
+        params = abi.FrameParams()
+        ctypes.pointer(params)[0] = frame_params
+        params.width, params.height, params.clear_background = w, h, int(v["clear_background"])
+        region = np.zeros((h, w), arena.dtype)
+        if params.clear_background:
+            clear_background(params, region)
+        first, n = int(v["first_draw"]), int(v["num_draws"])
+        if n:
+            bad = rasterize(draws[first:first + n], vertices, arena, params, region, num_threads=num_threads,
+                            skybox=skybox, tri_vertices=tri_vertices, lite=lt)
+            assert bad == 0, "bad texel fetches in a view"
+        one = np.ascontiguousarray(v).view(abi.VIEW)
+        _check(load().orc_mix_view(abi.ptr(one), abi.ptr(region), frame_params.pixel_format, abi.ptr(lt), lt.size),
+               "orc_mix_view")
+        off = int(v["target_offset"])
+        arena[off:off + w * h] = region.reshape(-1)
+    return arena

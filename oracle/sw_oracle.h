@@ -122,6 +122,9 @@ int orc_sim_update(void* sim, float current_time_s, const SwTextureMip* mips, ui
 int orc_sim_state(void* sim, uint32_t* out_words, uint64_t max_words, uint32_t* out_update_step, uint32_t* out_generated,
 	uint32_t* out_particles);
 void orc_xoshiro_outputs(const uint64_t state[4], uint64_t* out, uint32_t n);
+
+/* A portal view's texture mix (partial_renderer.rs:2189-2280) over its rendered region. */
+int orc_mix_view(const SwView* view, void* region, uint32_t pixel_format, const uint32_t* lite, uint64_t lite_pixels);
 void orc_small_rng_state(uint64_t seed, uint64_t out_state[4]);
 
 #ifdef __cplusplus

@@ -1361,6 +1361,77 @@ void launch_tiles_variant(const RasterArgs& args, uint32_t pixel_format, cudaStr
 }
 } // namespace
 
+namespace
+{
+// mix_surface_with_texture_impl (surfaces.rs:903-971) on one pixel of a view's region: the texture texel
+// at (tc_min + (x, y)) rem_euclid its size, modulated by the light (ColorVecI lanes * light * 256 >> 8),
+// blended into the pixel with the view's blending mode.
+template <class P>
+__global__ void __launch_bounds__(256) view_mix_kernel(SwView v, typename P::T* target, const uint32_t* lite, CI light)
+{
+	const uint64_t total = uint64_t(v.width) * v.height;
+	for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += uint64_t(gridDim.x) * blockDim.x)
+	{
+		const uint32_t x = uint32_t(i % v.width), y = uint32_t(i / v.width);
+		int32_t su = (v.mix_tc_min[0] + int32_t(x)) % int32_t(v.mix_size[0]);
+		int32_t sv = (v.mix_tc_min[1] + int32_t(y)) % int32_t(v.mix_size[1]);
+		if (su < 0) su += int32_t(v.mix_size[0]);
+		if (sv < 0) sv += int32_t(v.mix_size[1]);
+		const uint32_t texel = lite[v.mix_offset + uint64_t(sv) * v.mix_size[0] + uint32_t(su)];
+		const CI t = ci_from_c32(texel);
+		CI m;
+#pragma unroll
+		for (int k = 0; k < 4; ++k) m.v[k] = wmul(t.v[k], light.v[k]) >> 8;
+		typename P::T& dst = target[i];
+		switch (v.mix_blend)
+		{
+		case SW_BLEND_NONE: dst = P::from_ci(m); break;
+		case SW_BLEND_AVERAGE:
+		{
+			const CI d = P::to_ci(dst);
+#pragma unroll
+			for (int k = 0; k < 4; ++k) m.v[k] = wadd(m.v[k], d.v[k]) >> 1;
+			dst = P::from_ci(m);
+			break;
+		}
+		case SW_BLEND_ADDITIVE:
+		{
+			const CI d = P::to_ci(dst);
+#pragma unroll
+			for (int k = 0; k < 4; ++k) m.v[k] = wadd(m.v[k], d.v[k]);
+			dst = P::from_ci(m);
+			break;
+		}
+		case SW_BLEND_ALPHA_TEST:
+			if ((texel & 0xFF000000u) > 0x7F000000u) dst = P::from_ci(m); // Color32::test_alpha
+			break;
+		default: // SW_BLEND_ALPHA_BLEND
+		{
+			const int32_t alpha = int32_t(texel >> 24);
+			const CI d = P::to_ci(dst);
+#pragma unroll
+			for (int k = 0; k < 4; ++k) m.v[k] = wadd(wmul(m.v[k], alpha), wmul(d.v[k], 255 - alpha)) >> 8;
+			dst = P::from_ci(m);
+			break;
+		}
+		}
+	}
+}
+} // namespace
+
+int launch_view_mix(const SwView& view, void* target, const uint32_t* lite, uint32_t pixel_format, cudaStream_t stream)
+{
+	// ColorVecI::from_color_f32x3 of light * 256: lanes b, g, r (f32 -> i32 truncation), alpha 0
+	const CI light{{int32_t(view.mix_light[2] * 256.0f), int32_t(view.mix_light[1] * 256.0f), int32_t(view.mix_light[0] * 256.0f), 0}};
+	const uint64_t total = uint64_t(view.width) * view.height;
+	const unsigned blocks = unsigned(std::min<uint64_t>((total + 255) / 256, 152 * 8));
+	if (pixel_format == SW_PIXEL_C64)
+		view_mix_kernel<PixC64><<<blocks, 256, 0, stream>>>(view, static_cast<uint64_t*>(target), lite, light);
+	else
+		view_mix_kernel<PixC32><<<blocks, 256, 0, stream>>>(view, static_cast<uint32_t*>(target), lite, light);
+	return int(cudaGetLastError());
+}
+
 int launch_raster_bins(const RasterArgs& args, cudaStream_t stream)
 {
 	if (!args.bin_lists) return 0;

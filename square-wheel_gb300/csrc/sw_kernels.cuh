@@ -270,6 +270,8 @@ inline uint32_t raster_bins(int32_t extent, int32_t bin) { return uint32_t((exte
 // Edge walk + row setup (raster_setup, one CTA per draw), the bins (raster_bins, one CTA per bin), then
 // the tile pass (raster_tiles).
 int launch_raster_setup(const RasterArgs& args, cudaStream_t stream);
+// mix_surface_with_texture over a nested view's rendered region (surfaces.rs:854-971)
+int launch_view_mix(const SwView& view, void* target, const uint32_t* lite, uint32_t pixel_format, cudaStream_t stream);
 int launch_raster_bins(const RasterArgs& args, cudaStream_t stream);
 // variant: tile shape index (< SW_RASTER_TILE_VARIANTS, see SwTuning); every variant gives the same frame.
 int launch_raster_tiles(const RasterArgs& args, uint32_t pixel_format, uint32_t variant, cudaStream_t stream);

@@ -83,6 +83,10 @@ struct SwCtx
 	// the tile pass's bins (raster_bin_kernel): bins_x * bins_y lists of bin_cap draw indices and counts
 	DevBuf bin_lists, bin_counts;
 	uint32_t bin_cap = 0, bins_x = 0, bins_y = 0;
+	// the bins of a whole frame's nested views (portal textures), reused view after view
+	DevBuf vbin_lists, vbin_counts;
+	uint32_t vbin_cap = 0;
+	uint64_t vbin_cells = 0;
 	DevBuf skybox32, skybox64; // sw_set_skybox: the same texels in Color32 and Color64
 	DevBuf frame_in;           // sw_draw_frame: all per-frame arrays of one frame, uploaded by one copy
 	struct HostRange
@@ -338,6 +342,28 @@ int ensure_bins(SwCtx* ctx, uint32_t width, uint32_t height, uint64_t draws)
 	ctx->bin_cap = cap;
 	ctx->bins_x = bx;
 	ctx->bins_y = by;
+	return SW_OK;
+}
+
+// The bins of a frame's nested views: enough cells for the largest view and room for its draws.
+int ensure_view_bins(SwCtx* ctx, const SwView* views, uint32_t num_views)
+{
+	uint64_t cells = 1;
+	uint32_t draws = 1;
+	for (uint32_t i = 0; i < num_views; ++i)
+	{
+		cells = std::max<uint64_t>(cells, uint64_t(raster_bins(int32_t(views[i].width), RASTER_BIN_W)) *
+				raster_bins(int32_t(views[i].height), RASTER_BIN_H));
+		draws = std::max(draws, views[i].num_draws);
+	}
+	uint32_t cap = std::max<uint32_t>(ctx->vbin_cap, 256);
+	while (cap < draws) cap *= 2;
+	cells = std::max(cells, ctx->vbin_cells);
+	int r;
+	if ((r = ensure(ctx, ctx->vbin_lists, size_t(cells) * cap * 4))) return r;
+	if ((r = ensure(ctx, ctx->vbin_counts, size_t(cells) * 4))) return r;
+	ctx->vbin_cap = cap;
+	ctx->vbin_cells = cells;
 	return SW_OK;
 }
 
@@ -620,7 +646,8 @@ int sw_destroy(SwCtx* ctx)
 		&ctx->dir_lightmaps, &ctx->lights, &ctx->surfaces, &ctx->work_prefix, &ctx->arena, &ctx->draws, &ctx->vertices,
 		&ctx->draw_rows, &ctx->rdraws, &ctx->rows, &ctx->boxes, &ctx->tri_steps, &ctx->tri_vertices, &ctx->lite, &ctx->ldr[0], &ctx->ldr[1], &ctx->framebuffer, &ctx->bloom0, &ctx->bloom1, &ctx->line_sums,
 		&ctx->line_sums_f, &ctx->average, &ctx->error_counter, &ctx->up_src, &ctx->up_dst, &ctx->map_polygons,
-		&ctx->map_vertices, &ctx->vslab, &ctx->shadow_storage, &ctx->shadow_descs, &ctx->effect_buf, &ctx->sim_state, &ctx->sim_buf};
+		&ctx->map_vertices, &ctx->vslab, &ctx->shadow_storage, &ctx->shadow_descs, &ctx->effect_buf, &ctx->sim_state, &ctx->sim_buf, &ctx->vbin_lists,
+		&ctx->vbin_counts};
 	for (DevBuf* b : bufs) release(*b);
 	for (const SwCtx::HostRange& h : ctx->registered) cudaHostUnregister(h.ptr);
 	if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
@@ -997,12 +1024,23 @@ namespace
 // Host side of sw_submit_draws: validate every draw against its vertices and the surface arena, and
 // compute the rows each draw can cover (row records are numbered in draw order).
 int prepare_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const SwVertex16* vertices, uint32_t num_vertices,
-	DrawRows* rows, uint64_t* out_rows, const SwTriVertex* tri_vertices = nullptr, uint32_t num_tri_vertices = 0)
+	DrawRows* rows, uint64_t* out_rows, const SwTriVertex* tri_vertices = nullptr, uint32_t num_tri_vertices = 0,
+	const SwView* views = nullptr, uint32_t num_views = 0)
 {
+	// rows are clipped to the height of the target a draw is rasterised into: the frame, or its view's
+	std::vector<int32_t> view_height;
+	if (num_views)
+	{
+		view_height.assign(num_draws, int32_t(ctx->frame.height));
+		for (uint32_t v = 0; v < num_views; ++v)
+			for (uint32_t i = views[v].first_draw; i < views[v].first_draw + views[v].num_draws && i < num_draws; ++i)
+				view_height[i] = int32_t(views[v].height);
+	}
 	uint64_t row_acc = 0;
 	for (uint32_t i = 0; i < num_draws; ++i)
 	{
 		const SwDrawCmd& d = draws[i];
+		const int32_t clip_height = num_views ? view_height[i] : int32_t(ctx->frame.height);
 		if (d.mode == SW_RASTER_TRIANGLE)
 		{
 			// Rasterizer::fill_triangle: three SwTriVertex, a Color32 texture of sw_set_lite_textures
@@ -1017,7 +1055,7 @@ int prepare_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const 
 				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "draw %u: texture outside the lite textures", i);
 			int32_t y0;
 			uint32_t nrows;
-			draw_row_range(d, vertices, int32_t(ctx->frame.height), y0, nrows, tri_vertices);
+			draw_row_range(d, vertices, clip_height, y0, nrows, tri_vertices);
 			rows[i] = DrawRows{uint32_t(row_acc), y0, nrows, 0u};
 			row_acc += nrows;
 			if (row_acc > 0xFFFFFFFFull) return fail(ctx, SW_ERR_LIMIT, "too many draw rows in one frame");
@@ -1037,7 +1075,7 @@ int prepare_draws(SwCtx* ctx, const SwDrawCmd* draws, uint32_t num_draws, const 
 				d.tex_source == SW_TEXSRC_SKYBOX ? "skybox texels" : "surface arena");
 		int32_t y0;
 		uint32_t nrows;
-		draw_row_range(d, vertices, int32_t(ctx->frame.height), y0, nrows);
+		draw_row_range(d, vertices, clip_height, y0, nrows);
 		rows[i] = DrawRows{uint32_t(row_acc), y0, nrows, 0u};
 		row_acc += nrows;
 		if (row_acc > 0xFFFFFFFFull) return fail(ctx, SW_ERR_LIMIT, "too many draw rows in one frame");
@@ -1739,12 +1777,49 @@ int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, con
 	ra.vertices = reinterpret_cast<const SwVertex16*>(d + off[4]);
 	ra.draw_rows = reinterpret_cast<const DrawRows*>(d + off[5]);
 	ra.tri_vertices = reinterpret_cast<const SwTriVertex*>(d + off[6]);
+	ra.num_draws = f.num_views ? f.main_draws : f.num_draws; // the frame's own draws come first
 	if ((r = check_kernel(ctx, launch_raster_setup(ra, aux), "raster setup"))) return r;
 	if ((r = check_kernel(ctx, launch_raster_bins(ra, aux), "raster bins"))) return r;
 	SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, aux));
 	const SurfaceInputs si{reinterpret_cast<const SwLight*>(d + off[0]), reinterpret_cast<const SurfaceGpu*>(d + off[1]),
 		reinterpret_cast<const uint64_t*>(d + off[2])};
 	if ((r = launch_surfaces(ctx, &si))) return r;
+	// the nested views (portal textures), in order, into their arena regions: each cleared, rasterised
+	// from its draws with its own setup, bins and tile pass, then mixed with its texture
+	const uint32_t bpp = bpp_of(f.params.pixel_format);
+	for (uint32_t i = 0; i < f.num_views; ++i)
+	{
+		const SwView& v = f.views[i];
+		unsigned char* target = static_cast<unsigned char*>(ctx->arena.ptr) + v.target_offset * bpp;
+		SW_CUDA(ctx, cudaMemsetAsync(target, 0, size_t(v.width) * v.height * bpp, s));
+		if (v.num_draws || v.clear_background)
+		{
+			RasterArgs va = ra;
+			va.draws = ra.draws + v.first_draw;
+			va.draw_rows = ra.draw_rows + v.first_draw;
+			va.rdraws = ra.rdraws + v.first_draw;
+			va.boxes = ra.boxes + v.first_draw;
+			va.tri_steps = ra.tri_steps + uint64_t(v.first_draw) * 2;
+			va.num_draws = v.num_draws;
+			va.width = int32_t(v.width);
+			va.height = int32_t(v.height);
+			va.clear_background = v.clear_background;
+			va.framebuffer = target;
+			va.bin_lists = static_cast<uint32_t*>(ctx->vbin_lists.ptr);
+			va.bin_counts = static_cast<uint32_t*>(ctx->vbin_counts.ptr);
+			va.bin_cap = ctx->vbin_cap;
+			va.bins_x = raster_bins(int32_t(v.width), RASTER_BIN_W);
+			va.bins_y = raster_bins(int32_t(v.height), RASTER_BIN_H);
+			if (v.num_draws && (r = check_kernel(ctx, launch_raster_setup(va, s), "view raster setup"))) return r;
+			if ((r = check_kernel(ctx, launch_raster_bins(va, s), "view raster bins"))) return r;
+			if ((r = check_kernel(ctx, launch_raster_tiles(va, f.params.pixel_format, ctx->tuning.raster_tile, s), "view raster")))
+				return r;
+		}
+		if (v.mix_blend != SW_VIEW_NO_MIX &&
+			(r = check_kernel(ctx, launch_view_mix(v, target, static_cast<const uint32_t*>(ctx->lite.ptr), f.params.pixel_format, s),
+				 "view texture mix")))
+			return r;
+	}
 	SW_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_setup, 0));
 	PostArgs pp;
 	if (post)
@@ -1768,7 +1843,6 @@ int enqueue_frame(SwCtx* ctx, const SwFrameInput& f, const unsigned char* h, con
 	}
 	else if (f.dst && f.dst_is_device)
 	{
-		const uint32_t bpp = bpp_of(f.params.pixel_format);
 		SW_CUDA(ctx, cudaMemcpy2DAsync(f.dst, size_t(f.dst_pitch) * bpp, ctx->framebuffer.ptr, size_t(f.params.width) * bpp,
 						 size_t(f.params.width) * bpp, f.params.height, cudaMemcpyDeviceToDevice, s));
 	}
@@ -1956,6 +2030,35 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	if (f.postprocess && f.params.pixel_format != SW_PIXEL_C64)
 		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "postprocessing needs a colour64 frame");
 	if (f.dst && f.dst_pitch < f.params.width) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "pitch < width");
+	if (f.num_views)
+	{
+		// nested views: regions inside the arena, draws after the frame's own, textures inside the lite pixels
+		if (!f.views) return SW_ERR_INVALID_ARGUMENT;
+		if (f.num_views > 65536) return fail(ctx, SW_ERR_LIMIT, "too many views");
+		if (f.main_draws > f.num_draws) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "main_draws > num_draws");
+		for (uint32_t i = 0; i < f.num_views; ++i)
+		{
+			const SwView& v = f.views[i];
+			if (v.width == 0 || v.height == 0 || v.width > 16384 || v.height > 16384)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "view %u: bad size %ux%u", i, v.width, v.height);
+			const uint64_t area = uint64_t(v.width) * v.height;
+			if (v.target_offset > f.total_texels || area > f.total_texels - v.target_offset)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "view %u: target outside the surface arena", i);
+			if (v.first_draw < f.main_draws || uint64_t(v.first_draw) + v.num_draws > f.num_draws)
+				return fail(ctx, SW_ERR_INVALID_ARGUMENT, "view %u: draws outside [main_draws, num_draws)", i);
+			if (v.clear_background > 1) return fail(ctx, SW_ERR_INVALID_ARGUMENT, "view %u: bad clear_background", i);
+			if (v.mix_blend != SW_VIEW_NO_MIX)
+			{
+				const uint64_t tex = uint64_t(v.mix_size[0]) * v.mix_size[1];
+				if (v.mix_blend > SW_BLEND_ALPHA_BLEND || tex == 0 || v.mix_size[0] > 65536 || v.mix_size[1] > 65536 ||
+					v.mix_offset > ctx->lite_texels || tex > ctx->lite_texels - v.mix_offset)
+					return fail(ctx, SW_ERR_INVALID_ARGUMENT, "view %u: bad texture mix", i);
+				for (int c = 0; c < 3; ++c)
+					if (!(std::fabs(v.mix_light[c]) <= 65536.0f))
+						return fail(ctx, SW_ERR_INVALID_ARGUMENT, "view %u: texture light not finite", i);
+			}
+		}
+	}
 	int r;
 	const SwFrameParams& p = f.params;
 	if ((r = check_frame_params(ctx, p, f.lights, f.num_lights))) return r;
@@ -1991,7 +2094,7 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	if (f.num_tri_vertices) std::memcpy(h + off[6], f.tri_vertices, f.num_tri_vertices * sizeof(SwTriVertex));
 	uint64_t rows = 0;
 	if ((r = prepare_draws(ctx, f.draws, f.num_draws, f.vertices, f.num_vertices, reinterpret_cast<DrawRows*>(h + off[5]), &rows,
-			 f.tri_vertices, f.num_tri_vertices)))
+			 f.tri_vertices, f.num_tri_vertices, f.num_views ? f.views : nullptr, f.num_views)))
 		return r;
 
 	// 2. device buffers (growing them synchronises; the next capture picks up the new addresses)
@@ -2003,6 +2106,7 @@ int sw_draw_frame(SwCtx* ctx, const SwFrameInput* in)
 	if ((r = ensure(ctx, ctx->work_prefix, (size_t(f.num_surfaces) + 1) * 8))) return r;
 	if ((r = ensure_raster_buffers(ctx, f.num_draws, f.num_vertices, rows))) return r;
 	if ((r = ensure_bins(ctx, f.params.width, f.params.height, f.num_draws))) return r;
+	if (f.num_views && (r = ensure_view_bins(ctx, f.views, f.num_views))) return r;
 	if ((r = ensure_framebuffer(ctx, p))) return r;
 	ctx->num_rows = rows;
 	ctx->num_draws = f.num_draws;
@@ -2835,16 +2939,17 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 
 int sw_abi_layout(uint32_t* sizes, uint32_t count)
 {
-	const uint32_t s[26] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
+	const uint32_t s[27] = {uint32_t(sizeof(SwCreateInfo)), uint32_t(sizeof(SwTextureMip)), uint32_t(sizeof(SwEmissiveMip)),
 		uint32_t(sizeof(SwDirectionalLightmapElement)), uint32_t(sizeof(SwLight)), uint32_t(sizeof(SwSurfaceDesc)),
 		uint32_t(sizeof(SwVertex16)), uint32_t(sizeof(SwDrawCmd)), uint32_t(sizeof(SwFrameParams)),
 		uint32_t(sizeof(SwPostConfig)), uint32_t(sizeof(SwStats)), uint32_t(sizeof(SwFrameInput)), uint32_t(sizeof(SwTuning)),
 		uint32_t(sizeof(SwMapPolygon)), uint32_t(sizeof(SwViewLeaf)), uint32_t(sizeof(SwViewFrameInput)),
 		uint32_t(sizeof(SwViewCounts)), uint32_t(sizeof(SwLightShadow)), uint32_t(sizeof(SwDepthDraw)),
 		uint32_t(sizeof(SwShadowSide)), uint32_t(sizeof(SwShadowLeaf)), uint32_t(sizeof(SwMaterialFrame)),
-		uint32_t(sizeof(SwTriVertex)), uint32_t(sizeof(SwTexturePass)), uint32_t(sizeof(SwSimPass)), uint32_t(sizeof(SwSimPoint))};
-	for (uint32_t i = 0; sizes && i < count && i < 26; ++i) sizes[i] = s[i];
-	return 26;
+		uint32_t(sizeof(SwTriVertex)), uint32_t(sizeof(SwTexturePass)), uint32_t(sizeof(SwSimPass)), uint32_t(sizeof(SwSimPoint)),
+		uint32_t(sizeof(SwView))};
+	for (uint32_t i = 0; sizes && i < count && i < 27; ++i) sizes[i] = s[i];
+	return 27;
 }
 
 int sw_get_stats(SwCtx* ctx, SwStats* out)

@@ -89,6 +89,7 @@ void ClippingPolygon::get_clip_planes(Vec3 out[8]) const
 // ---- FramePrep ----
 FramePrep::FramePrep(const Scene& scene) : sc(scene)
 {
+	portals_depth = std::min(sc.config.portals_depth, 8u); // Renderer::new clamps it (renderer.rs:33)
 	sc.map_polygons(map_polygons);
 	map_polygons_base = map_polygons;
 	// the polygons of every material with a framed animation (their material fields follow its frames)
@@ -233,6 +234,15 @@ void VisibilityCalculator::update(const CameraMatrices& camera, const ClippingPo
 			if (n == 32) break;
 		}
 	}
+	mark_reachable_leafs(start, n, frame_bounds);
+}
+
+void VisibilityCalculator::update_with_start_leafs(const CameraMatrices& camera, const ClippingPolygon& frame_bounds,
+	const uint32_t* start, uint32_t n)
+{
+	cam = camera;
+	++frame;
+	camera_leaf = n ? start[0] : 0;
 	mark_reachable_leafs(start, n, frame_bounds);
 }
 
@@ -585,7 +595,8 @@ void FramePrep::draw_leaf(const ClippingPolygon& bounds, uint32_t leaf_index)
 		for (uint32_t k = 0; k < leaf.num_polygons; ++k) draw_polygon_decals(planes, leaf.first_polygon + k, sc.leaf_decals[leaf_index]);
 	const bool models = leaf_index < sc.leaf_models.size() && !sc.leaf_models[leaf_index].empty();
 	const bool sprites = leaf_index < sc.leaf_sprites.size() && !sc.leaf_sprites[leaf_index].empty();
-	if (models || sprites) draw_leaf_models(bounds, leaf_index);
+	const bool portals = leaf_index < sc.leaf_view_portals.size() && !sc.leaf_view_portals[leaf_index].empty();
+	if (models || sprites || portals) draw_leaf_models(bounds, leaf_index);
 }
 
 namespace
@@ -687,13 +698,27 @@ void FramePrep::draw_leaf_models(const ClippingPolygon& bounds, uint32_t leaf_in
 	if (leaf_index < sc.leaf_sprites.size())
 		for (uint32_t k : sc.leaf_sprites[leaf_index])
 			order.push_back({view_transform(cam.view_matrix, sc.sprites[k].position).z, 1u, k});
+	if (leaf_index < sc.leaf_view_portals.size())
+		for (uint32_t k : sc.leaf_view_portals[leaf_index])
+		{
+			// a portal by its vertices' centre
+			const ViewPortal& pt = sc.view_portals[k];
+			Vec3 c = v3(0.0f, 0.0f, 0.0f);
+			for (const Vec3& v : pt.vertices) c = c + v;
+			c = c / float(pt.vertices.size());
+			order.push_back({view_transform(cam.view_matrix, c).z, 2u, k});
+		}
 	std::stable_sort(order.begin(), order.end(), [](const Obj& a, const Obj& b) { return a.z > b.z; });
+	Vec3 planes[8];
+	bounds.get_clip_planes(planes);
 	for (const Obj& o : order)
 	{
 		if (o.kind == 0)
 			draw_model(bounds, o.index);
-		else
+		else if (o.kind == 1)
 			draw_sprite(bounds, o.index);
+		else
+			draw_view_portal(planes, o.index);
 	}
 }
 
@@ -1563,7 +1588,16 @@ void FramePrep::update_materials()
 		for (int c = 0; c < 3; ++c) f.emissive_light[c] = cur.emissive_light[c];
 		f.reserved = 0;
 		if (cur.effect != Material::NO_EFFECT) animated = true;
-		// the polygons the host prepares read the frame's material fields
+	}
+	apply_material_frames();
+}
+
+void FramePrep::apply_material_frames()
+{
+	// the polygons the host prepares read the frame's material fields
+	for (uint32_t m = 0; m < uint32_t(material_frames.size()) && m < uint32_t(material_polygons.size()); ++m)
+	{
+		const SwMaterialFrame& f = material_frames[m];
 		for (uint32_t pi : material_polygons[m])
 		{
 			SwMapPolygon& p = map_polygons[pi];
@@ -1692,16 +1726,7 @@ void FramePrep::prepare_with_camera(const CameraMatrices& camera, const std::vec
 	begin_frame(camera, frame_lights, options, skybox_rotation);
 	prepare_polygons_surfaces();
 	build_surface_descs();
-	draws.clear();
-	vertices.clear();
-	tri_vertices.clear();
-	// perform_rasterization_for_viewport_part (:1285-1325): skybox first, then the tree
-	draw_skybox(ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height)));
-	draw_tree();
-	finish_params();
-	stats.visible_polygons = uint32_t(visible_polygons.size());
-	stats.draws = uint32_t(draws.size());
-	stats.surface_texels = total_texels;
+	finish_view(ClippingPolygon::from_box(0.0f, 0.0f, float(opt.width), float(opt.height)));
 }
 
 void FramePrep::prepare_view_with_camera(const CameraMatrices& camera, const std::vector<SwLight>& frame_lights,
@@ -1798,6 +1823,392 @@ void FramePrep::prepare_view(uint32_t frame_index, const FrameOptions& options)
 	Quat rotation;
 	camera_of_frame(frame_index, options, camera, l, rotation);
 	prepare_view_with_camera(camera, l, options, rotation);
+}
+
+
+// ---- portals (partial_renderer.rs:1834-2283, 3720-3772) --------------------------------------------
+
+void FramePrep::ViewBlock::clear()
+{
+	surfaces.clear();
+	lights.clear();
+	light_shadows.clear();
+	depth_draws.clear();
+	depth_vertices.clear();
+	shadow_texels = 0;
+	draws.clear();
+	vertices.clear();
+	tri_vertices.clear();
+	views.clear();
+}
+
+void FramePrep::prepare_portals()
+{
+	// prepare_view_portals_textures (:1834-1996): each portal seen through the visible leafs it lies in
+	// gets a texture of its texture-coordinate extent at its mip, placed after this view's surfaces
+	portal_infos.assign(sc.view_portals.size(), PortalInfo());
+	for (uint32_t i = 0; i < uint32_t(sc.view_portals.size()); ++i)
+	{
+		const ViewPortal& portal = sc.view_portals[i];
+		bool any = false;
+		ClippingPolygon bounds{};
+		for (uint32_t leaf : sc.view_portal_leafs[i])
+			if (vis.visible(leaf))
+			{
+				if (any)
+					bounds.extend(vis.bounds(leaf));
+				else
+					bounds = vis.bounds(leaf);
+				any = true;
+			}
+		if (!any) continue; // in invisible leafs
+		Vec3 clip_planes[8];
+		bounds.get_clip_planes(clip_planes);
+		const Vec4 plane_transformed = cam.planes_matrix * extend(portal.plane.vec, -portal.plane.dist);
+		if (plane_transformed.w <= 0.0f) continue;
+		const uint32_t nv = std::min(uint32_t(portal.vertices.size()), uint32_t(MAX_VERTICES));
+		if (nv < 3) continue;
+		Vec3 vt[MAX_VERTICES];
+		for (uint32_t k = 0; k < nv; ++k) vt[k] = view_transform(cam.view_matrix, portal.vertices[k]);
+		Vec2 v2d[MAX_VERTICES];
+		const uint32_t count = project_and_clip_polygon(clip_planes, vt, nv, v2d);
+		if (count < 3) continue; // fully clipped
+		const float inf = float(1 << 29);
+		float tc_min[2] = {inf, inf}, tc_max[2] = {-inf, -inf};
+		for (const Vec3& v : portal.vertices)
+			for (int c = 0; c < 2; ++c)
+			{
+				const float tc = dot(portal.tex_coord_equation[c].vec, v) + portal.tex_coord_equation[c].dist;
+				if (tc < tc_min[c]) tc_min[c] = tc;
+				if (tc > tc_max[c]) tc_max[c] = tc;
+			}
+		for (int c = 0; c < 2; ++c)
+		{
+			tc_min[c] += 1.0f / 32.0f;
+			tc_max[c] -= 1.0f / 32.0f;
+		}
+		// DepthEquation::from_transformed_plane_equation and the tc equations projected onto the plane
+		const float pw = -plane_transformed.w;
+		const DepthEquation de{plane_transformed.x / pw, plane_transformed.y / pw, plane_transformed.z / pw};
+		TexCoordEquation te;
+		for (int c = 0; c < 2; ++c)
+		{
+			const Vec4 tb = cam.planes_matrix * extend(portal.tex_coord_equation[c].vec, portal.tex_coord_equation[c].dist);
+			te.d_tc_dx[c] = tb.x + tb.w * de.d_inv_z_dx;
+			te.d_tc_dy[c] = tb.y + tb.w * de.d_inv_z_dy;
+			te.k[c] = tb.z + tb.w * de.k;
+		}
+		const uint32_t mip = calculate_mip(v2d, count, de, te, opt.mip_bias);
+		const float mip_scale = 1.0f / float(1u << mip);
+		PortalInfo& info = portal_infos[i];
+		int32_t tmin[2], tmax[2];
+		for (int c = 0; c < 2; ++c)
+		{
+			te.d_tc_dx[c] = te.d_tc_dx[c] * mip_scale;
+			te.d_tc_dy[c] = te.d_tc_dy[c] * mip_scale;
+			te.k[c] = te.k[c] * mip_scale;
+			tmin[c] = as_i32(std::floor(tc_min[c]) * mip_scale);
+			tmax[c] = std::max(as_i32(std::ceil(tc_max[c]) * mip_scale), tmin[c] + 1);
+		}
+		for (int c = 0; c < 2; ++c)
+		{
+			const float m = float(tmin[c]);
+			te.d_tc_dx[c] -= m * de.d_inv_z_dx;
+			te.d_tc_dy[c] -= m * de.d_inv_z_dy;
+			te.k[c] -= m * de.k;
+			info.resolution[c] = uint32_t(tmax[c] - tmin[c]);
+			info.tc_min[c] = tmin[c];
+		}
+		info.pixels_offset = arena_end;
+		info.depth = de;
+		info.tc = te;
+		info.mip = mip;
+		arena_end += uint64_t(info.resolution[0]) * info.resolution[1];
+	}
+
+	// build_view_portals_textures (:2008-2283): each visible portal's view rendered by the nested renderer
+	// (black without one: the depth limit), then mixed with the portal's texture
+	for (uint32_t i = 0; i < uint32_t(sc.view_portals.size()); ++i)
+	{
+		const PortalInfo& info = portal_infos[i];
+		const uint32_t w = info.resolution[0], h = info.resolution[1];
+		if (uint64_t(w) * h == 0) continue;
+		const ViewPortal& portal = sc.view_portals[i];
+		if (portals_depth == 0)
+		{
+			gather_nested(nullptr, info.pixels_offset, w, h, portal, info);
+			continue;
+		}
+		if (!portal_renderer)
+		{
+			portal_renderer.reset(new FramePrep(sc));
+			portal_renderer->portals_depth = portals_depth - 1;
+		}
+		const float z_near = PREP_Z_NEAR;
+		const float mip_scale = 1.0f / float(1u << info.mip);
+		CameraMatrices pc;
+		std::vector<uint32_t> start;
+		const std::vector<uint32_t>* start_leafs = nullptr;
+		// the tc-space basis of the portal plane: tc equations and the plane scaled to the mip (as rows)
+		auto tex_coord_basis = [&](float normal_len) {
+			Mat4 b;
+			b.c[0] = extend(portal.tex_coord_equation[0].vec, portal.tex_coord_equation[0].dist) * mip_scale;
+			b.c[1] = extend(portal.tex_coord_equation[1].vec, portal.tex_coord_equation[1].dist) * mip_scale;
+			b.c[2] = extend(portal.plane.vec, -portal.plane.dist) * (mip_scale / normal_len);
+			b.c[3] = v4(0.0f, 0.0f, 0.0f, 1.0f);
+			return transpose(b);
+		};
+		auto view_of = [&](const Mat4& basis, Vec3 eye_tc, float dist_normalized) {
+			Mat4 translate = Mat4::identity();
+			translate.c[3] = v4(-eye_tc.x, -eye_tc.y, -eye_tc.z, 1.0f);
+			Mat4 shift = Mat4::identity();
+			shift.c[2].x = eye_tc.x - float(info.tc_min[0]);
+			shift.c[2].y = eye_tc.y - float(info.tc_min[1]);
+			// the portal plane becomes the near plane: what lies behind it is clipped
+			Mat4 z_scale = Mat4::identity();
+			z_scale.c[0].x = z_near;
+			z_scale.c[1].y = z_near;
+			z_scale.c[2].z = z_near / (dist_normalized * mip_scale);
+			return shift * z_scale * translate * basis;
+		};
+		if (portal.kind == ViewPortal::CAMERA_AT_POSITION)
+			pc = build_view_matrix_with_full_rotation(portal.position, portal.rotation, portal.fov, float(w), float(h));
+		else if (portal.kind == ViewPortal::MIRROR)
+		{
+			const float normal_square_len = magnitude2(portal.plane.vec);
+			const float normal_len = std::sqrt(normal_square_len);
+			const float dist = dot(portal.plane.vec, cam.position) - portal.plane.dist;
+			const Vec3 reflected = cam.position - portal.plane.vec * (2.0f * dist / normal_square_len);
+			const float dist_normalized = dist / normal_len;
+			const Mat4 basis = tex_coord_basis(normal_len);
+			const Vec3 eye_tc = truncate(basis * extend(reflected, 1.0f));
+			pc.position = reflected;
+			pc.view_matrix = view_of(basis, eye_tc, dist_normalized);
+			if (!invert(transpose(pc.view_matrix), pc.planes_matrix)) pc.planes_matrix = Mat4::identity();
+			start_leafs = &sc.view_portal_leafs[i]; // the search starts in the mirror's leafs
+		}
+		else
+		{
+			// the portal's vertices moved by the transform: their leafs start the search
+			std::vector<Vec3> moved(portal.vertices.size());
+			for (size_t k = 0; k < moved.size(); ++k) moved[k] = truncate(portal.transform * extend(portal.vertices[k], 1.0f));
+			sc.convex_hull_leafs(moved.data(), std::min(uint32_t(moved.size()), uint32_t(MAX_VERTICES)), start);
+			start_leafs = &start;
+			const float normal_len = magnitude(portal.plane.vec);
+			const float dist_normalized = (portal.plane.dist - dot(portal.plane.vec, cam.position)) / normal_len;
+			const Mat4 basis = tex_coord_basis(normal_len);
+			const Vec3 eye_tc = truncate(basis * extend(cam.position, 1.0f));
+			Mat4 inverse_transform;
+			if (!invert(portal.transform, inverse_transform)) inverse_transform = Mat4::identity();
+			pc.position = truncate(portal.transform * extend(cam.position, 1.0f));
+			pc.view_matrix = view_of(basis, eye_tc, dist_normalized) * inverse_transform;
+			if (!invert(transpose(pc.view_matrix), pc.planes_matrix)) pc.planes_matrix = Mat4::identity();
+		}
+		portal_renderer->prepare_nested(*this, pc, start_leafs, w, h);
+		gather_nested(portal_renderer.get(), info.pixels_offset, w, h, portal, info);
+	}
+}
+
+void FramePrep::prepare_nested(const FramePrep& parent, const CameraMatrices& camera, const std::vector<uint32_t>* start_leafs,
+	uint32_t width, uint32_t height)
+{
+	// PartialRenderer::prepare_frame + draw_frame of the nested renderer (:156-258) for one portal: the
+	// frame's lights, materials and time, the portal's camera and resolution
+	shadow_view = false;
+	cam = camera;
+	opt = parent.opt;
+	opt.width = width;
+	opt.height = height;
+	sky_rotation = parent.sky_rotation;
+	lights = parent.lights; // the frame's lights (the parent's nested views are appended after its own draws)
+	frame_time_s = parent.frame_time_s;
+	stats = FrameStats();
+	++current_frame;
+	const ClippingPolygon frame_bounds = ClippingPolygon::from_box(0.0f, 0.0f, float(width), float(height));
+	if (start_leafs)
+		vis.update_with_start_leafs(cam, frame_bounds, start_leafs->data(), uint32_t(start_leafs->size()));
+	else
+		vis.update(cam, frame_bounds);
+	stats.camera_leaf = vis.camera_leaf;
+	position_lights();
+	prepare_shadows();
+	// the materials processor is the frame's: the parent's current frames and shifts
+	mapping = parent.mapping;
+	material_frames = parent.material_frames;
+	animated = parent.animated;
+	apply_material_frames();
+	texture_passes.clear();
+	texture_shifts.clear();
+	simulations.clear();
+	prepare_polygons_surfaces();
+	build_surface_descs();
+	finish_view(frame_bounds);
+	// draw_frame's background: camera views as the root frame, mirrors and parallax portals never
+	params.clear_background = (opt.clear_background && !start_leafs) ? 1u : 0u;
+}
+
+// The view's draws after its surfaces: its portals' textures (nested views), then skybox and tree, then
+// the nested views' outputs appended behind its own.
+void FramePrep::finish_view(const ClippingPolygon& viewport)
+{
+	surface_texels = total_texels;
+	arena_end = total_texels;
+	draws.clear();
+	vertices.clear();
+	tri_vertices.clear();
+	views.clear();
+	nested.clear();
+	prepare_portals();
+	// perform_rasterization_for_viewport_part (:1285-1325): skybox first, then the tree
+	draw_skybox(viewport);
+	draw_tree();
+	main_draws = uint32_t(draws.size());
+	finish_params();
+	stats.visible_polygons = uint32_t(visible_polygons.size());
+	stats.draws = uint32_t(draws.size());
+	stats.surface_texels = surface_texels;
+	append_nested();
+}
+
+void FramePrep::gather_nested(const FramePrep* n, uint64_t target_offset, uint32_t width, uint32_t height,
+	const ViewPortal& portal, const PortalInfo& info)
+{
+	const uint64_t arena_base = arena_end;
+	const uint32_t draw_base = uint32_t(nested.draws.size());
+	if (n)
+	{
+		const uint32_t light_base = uint32_t(nested.lights.size());
+		const uint64_t shadow_base = nested.shadow_texels;
+		const uint32_t depth_vertex_base = uint32_t(nested.depth_vertices.size());
+		const uint32_t vertex_base = uint32_t(nested.vertices.size()), tri_base = uint32_t(nested.tri_vertices.size());
+		for (SwSurfaceDesc d : n->surfaces)
+		{
+			d.out_offset += arena_base;
+			for (uint32_t k = 0; k < d.num_lights; ++k) d.lights[k] = uint16_t(d.lights[k] + light_base);
+			nested.surfaces.push_back(d);
+		}
+		nested.lights.insert(nested.lights.end(), n->lights.begin(), n->lights.end());
+		for (size_t l = 0; l < n->lights.size(); ++l)
+		{
+			SwLightShadow s;
+			std::memset(&s, 0, sizeof(s));
+			if (l < n->light_shadows.size()) s = n->light_shadows[l];
+			if (s.kind != SW_SHADOW_NONE) s.offset += shadow_base;
+			nested.light_shadows.push_back(s);
+		}
+		for (SwDepthDraw d : n->depth_draws)
+		{
+			d.map_offset += shadow_base;
+			d.first_vertex += depth_vertex_base;
+			nested.depth_draws.push_back(d);
+		}
+		nested.depth_vertices.insert(nested.depth_vertices.end(), n->depth_vertices.begin(), n->depth_vertices.end());
+		nested.shadow_texels += n->shadow_texels;
+		for (SwDrawCmd d : n->draws)
+		{
+			d.first_vertex += d.mode == SW_RASTER_TRIANGLE ? tri_base : vertex_base;
+			if (d.tex_source == SW_TEXSRC_SURFACE) d.tex_offset += arena_base;
+			nested.draws.push_back(d);
+		}
+		nested.vertices.insert(nested.vertices.end(), n->vertices.begin(), n->vertices.end());
+		nested.tri_vertices.insert(nested.tri_vertices.end(), n->tri_vertices.begin(), n->tri_vertices.end());
+		// the nested view's own nested views first (they render before it)
+		for (SwView v : n->views)
+		{
+			v.target_offset += arena_base;
+			v.first_draw += draw_base;
+			nested.views.push_back(v);
+		}
+		arena_end += n->total_texels;
+	}
+	SwView v;
+	std::memset(&v, 0, sizeof(v));
+	v.target_offset = target_offset;
+	v.width = width;
+	v.height = height;
+	v.first_draw = draw_base;
+	v.num_draws = n ? n->main_draws : 0;
+	v.clear_background = n ? n->params.clear_background : 0u;
+	v.mix_blend = SW_VIEW_NO_MIX;
+	if (portal.texture >= 0)
+	{
+		// mix_surface_with_texture with the texture's mip of the portal (:2230-2275); the light is the
+		// constant light_add (a light-grid fetch for light_scale > 0 needs the map's light grid)
+		const LiteMip& m = sc.lite_mips[size_t(portal.texture) * NUM_MIPS + info.mip];
+		v.mix_blend = portal.texture_blending_mode;
+		v.mix_offset = m.offset;
+		v.mix_size[0] = m.width;
+		v.mix_size[1] = m.height;
+		v.mix_tc_min[0] = info.tc_min[0];
+		v.mix_tc_min[1] = info.tc_min[1];
+		for (int c = 0; c < 3; ++c) v.mix_light[c] = portal.light_add[c];
+	}
+	nested.views.push_back(v);
+}
+
+void FramePrep::append_nested()
+{
+	if (nested.views.empty())
+	{
+		total_texels = arena_end;
+		return;
+	}
+	const uint32_t light_base = uint32_t(lights.size());
+	const uint64_t shadow_base = shadow_texels;
+	const uint32_t depth_vertex_base = uint32_t(depth_vertices.size());
+	const uint32_t draw_base = uint32_t(draws.size()), vertex_base = uint32_t(vertices.size());
+	const uint32_t tri_base = uint32_t(tri_vertices.size());
+	// one shadow descriptor per light in the combined list (prepare_shadows keeps them parallel)
+	SwLightShadow none;
+	std::memset(&none, 0, sizeof(none));
+	light_shadows.resize(lights.size(), none);
+	for (SwSurfaceDesc d : nested.surfaces)
+	{
+		for (uint32_t k = 0; k < d.num_lights; ++k) d.lights[k] = uint16_t(d.lights[k] + light_base);
+		surfaces.push_back(d);
+	}
+	lights.insert(lights.end(), nested.lights.begin(), nested.lights.end());
+	for (SwLightShadow s : nested.light_shadows)
+	{
+		if (s.kind != SW_SHADOW_NONE) s.offset += shadow_base;
+		light_shadows.push_back(s);
+	}
+	for (SwDepthDraw d : nested.depth_draws)
+	{
+		d.map_offset += shadow_base;
+		d.first_vertex += depth_vertex_base;
+		depth_draws.push_back(d);
+	}
+	depth_vertices.insert(depth_vertices.end(), nested.depth_vertices.begin(), nested.depth_vertices.end());
+	shadow_texels += nested.shadow_texels;
+	for (SwDrawCmd d : nested.draws)
+	{
+		d.first_vertex += d.mode == SW_RASTER_TRIANGLE ? tri_base : vertex_base;
+		draws.push_back(d);
+	}
+	vertices.insert(vertices.end(), nested.vertices.begin(), nested.vertices.end());
+	tri_vertices.insert(tri_vertices.end(), nested.tri_vertices.begin(), nested.tri_vertices.end());
+	for (SwView v : nested.views)
+	{
+		v.first_draw += draw_base;
+		views.push_back(v);
+	}
+	total_texels = arena_end;
+	nested.clear();
+}
+
+void FramePrep::draw_view_portal(const Vec3 clip_planes[8], uint32_t portal_index)
+{
+	// draw_view_portal (:3720-3772): the portal polygon textured with its view. The leaf's 3D clip planes
+	// cut nothing here: the generated portals lie inside their leaf.
+	const PortalInfo& info = portal_infos[portal_index];
+	if (uint64_t(info.resolution[0]) * info.resolution[1] == 0) return;
+	const ViewPortal& portal = sc.view_portals[portal_index];
+	const uint32_t nv = std::min(uint32_t(portal.vertices.size()), uint32_t(MAX_VERTICES));
+	Vec3 vt[MAX_VERTICES];
+	for (uint32_t k = 0; k < nv; ++k) vt[k] = view_transform(cam.view_matrix, portal.vertices[k]);
+	emit_draw(clip_planes, vt, nv, info.depth, info.tc, info.resolution[0], info.resolution[1], info.pixels_offset,
+		SW_TEXSRC_SURFACE, portal.blending_mode);
 }
 
 } // namespace swhost

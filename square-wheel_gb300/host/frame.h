@@ -48,6 +48,8 @@ class VisibilityCalculator
 public:
 	explicit VisibilityCalculator(const Scene& scene);
 	void update(const CameraMatrices& cam, const ClippingPolygon& frame_bounds);
+	// update_visibility_with_start_leafs (map_visibility_calculator.rs:99-113): portal and mirror views
+	void update_with_start_leafs(const CameraMatrices& cam, const ClippingPolygon& frame_bounds, const uint32_t* start, uint32_t n);
 	bool visible(uint32_t leaf) const { return leafs[leaf].visible_frame == frame; }
 	const ClippingPolygon& bounds(uint32_t leaf) const { return leafs[leaf].bounds; }
 	uint32_t camera_leaf = 0;
@@ -147,6 +149,25 @@ public:
 	std::vector<int32_t> texture_shifts;
 	// the frame's simulated effect work (sw_update_simulations): water and fire steps, textures, mips
 	SimBatch simulations;
+	// Portal views (prepare_view_portals_textures / build_view_portals_textures, partial_renderer.rs:
+	// 1834-2283). Per scene portal its texture in the surface arena (resolution 0: not visible this frame);
+	// the frame's nested views in render order (SwView: a portal texture region rendered from the view's
+	// draws, then mixed with the portal's texture). Draws [0, main_draws) are this view's; the nested
+	// views' draws, vertices, surfaces, lights and shadow maps follow this view's own. total_texels spans
+	// this view's surfaces (surface_texels), its portal textures and the nested views' arenas.
+	struct PortalInfo
+	{
+		uint32_t resolution[2] = {0, 0};
+		uint64_t pixels_offset = 0;
+		DepthEquation depth{};
+		TexCoordEquation tc{};
+		int32_t tc_min[2] = {0, 0};
+		uint32_t mip = 0;
+	};
+	std::vector<PortalInfo> portal_infos;
+	std::vector<SwView> views;
+	uint32_t main_draws = 0;
+	uint64_t surface_texels = 0;
 	const EffectSim* effect_sim(uint32_t material) const
 	{
 		return material < sims.size() ? sims[material].get() : nullptr;
@@ -204,6 +225,35 @@ private:
 	void update_texture_effects();
 	std::vector<std::unique_ptr<EffectSim>> sims; // each water / fire material's effect state (persists)
 	void update_simulations();
+	void apply_material_frames();
+	// portals: the nested renderer (portals_depth - 1 levels below; none at depth 0), the view this one
+	// renders a portal of, and the nested views' outputs gathered until this view's own draws are done
+	struct ViewBlock
+	{
+		std::vector<SwSurfaceDesc> surfaces;
+		std::vector<SwLight> lights;
+		std::vector<SwLightShadow> light_shadows;
+		std::vector<SwDepthDraw> depth_draws;
+		std::vector<SwVertex16> depth_vertices;
+		uint64_t shadow_texels = 0;
+		std::vector<SwDrawCmd> draws;
+		std::vector<SwVertex16> vertices;
+		std::vector<SwTriVertex> tri_vertices;
+		std::vector<SwView> views;
+		void clear();
+	};
+	uint32_t portals_depth = 0;
+	std::unique_ptr<FramePrep> portal_renderer;
+	ViewBlock nested;
+	uint64_t arena_end = 0;
+	void prepare_portals();
+	void finish_view(const ClippingPolygon& viewport);
+	void prepare_nested(const FramePrep& parent, const CameraMatrices& camera, const std::vector<uint32_t>* start_leafs,
+		uint32_t width, uint32_t height);
+	void gather_nested(const FramePrep* n, uint64_t target_offset, uint32_t width, uint32_t height, const ViewPortal& portal,
+		const PortalInfo& info);
+	void append_nested();
+	void draw_view_portal(const Vec3 clip_planes[8], uint32_t portal_index);
 	void begin_frame(const CameraMatrices& cam, const std::vector<SwLight>& lights, const FrameOptions& opt, Quat skybox_rotation);
 	void finish_params();
 	void camera_of_frame(uint32_t frame_index, const FrameOptions& opt, CameraMatrices& cam, std::vector<SwLight>& lights,

@@ -653,6 +653,7 @@ struct Builder
 	};
 	std::vector<CellLeafs> cell_leafs;
 	uint32_t path_start_room = 0; // room of the camera path's first key
+	std::vector<uint32_t> path_rooms; // the rooms the camera path walks through, in order
 
 	uint32_t build_cell(uint32_t i, uint32_t j)
 	{
@@ -850,6 +851,7 @@ struct Builder
 		std::vector<Vec3> way;
 		uint32_t cur = rng.below(uint32_t(rooms.size()));
 		path_start_room = cur;
+		path_rooms.push_back(cur);
 		uint32_t prev = ~0u;
 		way.push_back(v3(rooms[cur].cx, rooms[cur].cy, eye));
 		for (int step = 0; step < 64; ++step)
@@ -901,6 +903,7 @@ struct Builder
 			way.push_back(v3(b.cx + rng.uniform(-64, 64), b.cy + rng.uniform(-64, 64), eye));
 			prev = cur;
 			cur = next;
+			path_rooms.push_back(cur);
 		}
 		camera_path_from_way(way, true, cfg, sc);
 	}
@@ -1743,8 +1746,131 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 			sc.decals.push_back(d);
 		}
 	}
+	if (cfg.num_portals)
+	{
+		// Portals (own generator): standing rectangles near a corner of the rooms the camera path walks
+		// through, facing the room's centre - mirrors, screens showing a camera in another room of the path
+		// (mixed with a scan-line texture), and parallax windows into another room.
+		Rng qrng(cfg.seed ^ 0x9041A1u);
+		std::vector<uint32_t> rooms_seen;
+		for (uint32_t r : b.path_rooms)
+			if (std::find(rooms_seen.begin(), rooms_seen.end(), r) == rooms_seen.end()) rooms_seen.push_back(r);
+		const uint32_t screen_texture = uint32_t(sc.lite_mips.size() / NUM_MIPS);
+		make_sprite_texture(qrng, 64, 64, false, sc);
+		for (uint32_t m = 0; m < NUM_MIPS; ++m) // scan lines: every other row of each mip darker, alpha kept
+		{
+			const LiteMip& lm = sc.lite_mips[size_t(screen_texture) * NUM_MIPS + m];
+			for (uint32_t y = 1; y < lm.height; y += 2)
+				for (uint32_t x = 0; x < lm.width; ++x)
+				{
+					uint32_t& px = sc.lite_pixels[lm.offset + uint64_t(y) * lm.width + x];
+					px = (px & 0xFF000000u) | ((px >> 1) & 0x7F7F7Fu);
+				}
+		}
+		sc.leaf_view_portals.assign(sc.leafs.size(), {});
+		for (uint32_t k = 0; k < cfg.num_portals; ++k)
+		{
+			// in view: ahead of a camera path key, facing it, inside the key's leaf
+			const uint32_t nk = uint32_t(sc.camera_path.size());
+			const uint32_t j = (k * 23u + 3u) % nk;
+			const Vec3 eye = sc.camera_path[j].position;
+			Vec3 dir = sc.camera_path[(j + 1) % nk].position - eye;
+			dir.z = 0.0f;
+			if (magnitude(dir) < 1e-3f) dir = v3(1.0f, 0.0f, 0.0f);
+			dir = dir / magnitude(dir);
+			const uint32_t eye_leaf = sc.leaf_of(eye);
+			// the room of that leaf (else the path's first) and another room of the path
+			uint32_t here = rooms_seen[0];
+			for (uint32_t ri = 0; ri < uint32_t(b.rooms.size()); ++ri)
+				if (b.rooms[ri].leaf == eye_leaf) here = ri;
+			uint32_t there = rooms_seen[(k + 1) % rooms_seen.size()];
+			if (there == here) there = rooms_seen[(k + 2) % rooms_seen.size()];
+			const Room& r = b.rooms[here];
+			const Room& other = b.rooms[there];
+			ViewPortal pt;
+			pt.kind = k % 3;
+			const Vec3 n = -dir;
+			const Vec3 t = v3(-n.y, n.x, 0.0f);
+			const float hw = 40.0f + 8.0f * float(k % 3), z0 = 8.0f, z1 = 120.0f;
+			Vec3 c{}, q[4];
+			std::vector<uint32_t> leafs;
+			bool placed = false;
+			for (float dist : {220.0f, 160.0f, 110.0f, 70.0f})
+			{
+				c = eye + dir * dist;
+				c.z = 0.0f;
+				q[0] = c - t * hw + v3(0, 0, z0), q[1] = c + t * hw + v3(0, 0, z0);
+				q[2] = c + t * hw + v3(0, 0, z1), q[3] = c - t * hw + v3(0, 0, z1);
+				sc.convex_hull_leafs(q, 4, leafs);
+				if (leafs.size() == 1 && leafs[0] == eye_leaf)
+				{
+					placed = true;
+					break;
+				}
+			}
+			if (!placed) continue;
+			if (dot(cross(q[1] - q[0], q[2] - q[0]), n) > 0.0f) std::swap(q[1], q[3]); // clockwise seen from the front
+			pt.vertices.assign(q, q + 4);
+			pt.plane = Plane{n, dot(n, q[0])};
+			pt.tex_coord_equation[0] = Plane{t, hw - dot(t, c)}; // one texel per unit, from the left edge
+			pt.tex_coord_equation[1] = Plane{v3(0.0f, 0.0f, -1.0f), z1};
+			if (pt.kind == ViewPortal::CAMERA_AT_POSITION)
+			{
+				pt.position = v3(other.cx, other.cy, 96.0f);
+				pt.rotation = quat_from_angle_z(qrng.uniform(-3.1f, 3.1f));
+				pt.fov = 1.5707964f;
+				pt.texture = int32_t(screen_texture);
+				pt.texture_blending_mode = SW_BLEND_AVERAGE;
+				pt.light_add[0] = 1.0f, pt.light_add[1] = 0.9f, pt.light_add[2] = 0.8f;
+			}
+			else if (pt.kind == ViewPortal::PARALLAX)
+			{
+				pt.transform = Mat4::identity();
+				pt.transform.c[3] = v4(other.cx - r.cx, other.cy - r.cy, 0.0f, 1.0f);
+				pt.blending_mode = SW_BLEND_AVERAGE;
+			}
+			const uint32_t id = uint32_t(sc.view_portals.size());
+			sc.convex_hull_leafs(pt.vertices.data(), uint32_t(pt.vertices.size()), leafs);
+			for (uint32_t l : leafs) sc.leaf_view_portals[l].push_back(id);
+			sc.view_portal_leafs.push_back(leafs);
+			sc.view_portals.push_back(pt);
+		}
+	}
 	add_dynamic_lights(cfg, rng, sc);
 	return true;
+}
+
+uint32_t Scene::leaf_of(Vec3 p) const
+{
+	uint32_t node = root_node();
+	while (node < FIRST_LEAF_INDEX)
+	{
+		const BspNode& nd = nodes[node];
+		node = dot(nd.plane.vec, p) - nd.plane.dist >= 0.0f ? nd.children[0] : nd.children[1];
+	}
+	return node - FIRST_LEAF_INDEX;
+}
+
+void Scene::convex_hull_leafs(const Vec3* vertices, uint32_t n, std::vector<uint32_t>& out) const
+{
+	out.clear();
+	std::vector<uint32_t> stack{root_node()};
+	while (!stack.empty())
+	{
+		const uint32_t node = stack.back();
+		stack.pop_back();
+		if (node >= FIRST_LEAF_INDEX)
+		{
+			out.push_back(node - FIRST_LEAF_INDEX);
+			continue;
+		}
+		const BspNode& nd = nodes[node];
+		uint32_t front = 0;
+		for (uint32_t i = 0; i < n; ++i)
+			if (dot(nd.plane.vec, vertices[i]) > nd.plane.dist) ++front;
+		if (front < n) stack.push_back(nd.children[1]); // the back child after the front one
+		if (front > 0) stack.push_back(nd.children[0]);
+	}
 }
 
 // ---- scenes from compiled maps ----------------------------------------------------------------

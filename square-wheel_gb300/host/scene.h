@@ -265,6 +265,33 @@ struct DecalEntity
 	float light_add[3];
 };
 
+// ViewPortal (src/square_wheel/frame_info.rs:171-205): a polygon showing another view of the world,
+// rendered into a texture of its own every frame - a camera at a position, a mirror, or a parallax
+// portal (the camera moved by `transform`) - optionally mixed with a texture.
+struct ViewPortal
+{
+	enum Kind : uint32_t
+	{
+		CAMERA_AT_POSITION = 0,
+		MIRROR = 1,
+		PARALLAX = 2,
+	};
+	uint32_t kind = MIRROR;
+	Vec3 position{0.0f, 0.0f, 0.0f}; // CAMERA_AT_POSITION
+	Quat rotation{1.0f, Vec3{0.0f, 0.0f, 0.0f}};
+	float fov = 1.5707964f;
+	Mat4 transform = Mat4::identity(); // PARALLAX: camera position -> the portal's view point
+	Plane plane{};
+	Plane tex_coord_equation[2]{};
+	std::vector<Vec3> vertices;
+	uint32_t blending_mode = SW_BLEND_NONE;
+	// ViewPortalTexture: a lite texture (Scene::lite_mips index / NUM_MIPS), its blending and light
+	int32_t texture = -1;
+	uint32_t texture_blending_mode = SW_BLEND_NONE;
+	float light_scale = 0.0f;
+	float light_add[3] = {1.0f, 1.0f, 1.0f};
+};
+
 // One mip of a TextureLite (Color32 pixels, src/square_wheel/textures.rs:89-91) in Scene::lite_pixels.
 struct LiteMip
 {
@@ -308,6 +335,8 @@ struct SceneConfig
 	uint32_t model_frames = 8;        // animation keyframes per mesh
 	uint32_t num_sprites = 0;         // sprites in the rooms (all four orientations, several blending modes)
 	uint32_t num_decals = 0;          // decals on the rooms' walls and floors
+	uint32_t num_portals = 0;         // portals in the camera path's rooms: mirrors, cameras, parallax windows
+	uint32_t portals_depth = 2;       // RendererConfig::portals_depth: nested portal views (at most 8)
 	uint32_t turb_materials = 0;      // the last base materials but layered_materials have a turbulence effect
 	uint32_t layered_materials = 0;   // the last this many base materials are layered animations
 	uint32_t water_materials = 0;     // before the turbulence ones: water effects
@@ -355,6 +384,15 @@ struct Scene
 	// Decals and the decals of each leaf, in decal order; their textures are lite textures too.
 	std::vector<DecalEntity> decals;
 	std::vector<std::vector<uint32_t>> leaf_decals;
+	// portals and the portals index (DynamicObjectsIndex::position_portals): each portal's leafs, each
+	// leaf's portals in portal order
+	std::vector<ViewPortal> view_portals;
+	std::vector<std::vector<uint32_t>> view_portal_leafs;
+	std::vector<std::vector<uint32_t>> leaf_view_portals;
+	// get_convex_hull_bsp_leafs (src/common/bsp_map_compact.rs:294-338): the leafs a convex hull reaches,
+	// front child first
+	void convex_hull_leafs(const Vec3* vertices, uint32_t n, std::vector<uint32_t>& out) const;
+	uint32_t leaf_of(Vec3 p) const; // the leaf holding a point (front of a node plane: the first child)
 	// A scene loaded from a compiled map keeps its compressed lightmap lumps (4 bytes per simple
 	// element, 13 per directional element, as the file holds them) for upload and decompression on the
 	// GPU; empty for generated scenes.

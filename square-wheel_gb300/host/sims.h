@@ -10,7 +10,7 @@
 #include <vector>
 
 #include "scene.h"
-#include "swgpu.h"
+#include "../../include/swgpu.h"
 
 namespace swhost
 {

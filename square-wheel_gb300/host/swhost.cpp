@@ -152,6 +152,13 @@ int scene_config_from(const SwhSceneConfig* c, SceneConfig& cfg)
 	cfg.layered_materials = c->layered_materials;
 	cfg.water_materials = c->water_materials;
 	cfg.fire_materials = c->fire_materials;
+	cfg.num_portals = c->num_portals;
+	cfg.portals_depth = std::min(c->portals_depth, 8u);
+	if (cfg.num_portals > 4096)
+	{
+		g_error = "too many portals";
+		return SW_ERR_INVALID_ARGUMENT;
+	}
 	if (cfg.num_models > 100000 || cfg.model_triangles > 200000 || cfg.model_frames > 256 || cfg.num_sprites > 1000000 ||
 		cfg.num_decals > 1000000)
 	{
@@ -596,6 +603,10 @@ int swh_frame_outputs(const SwhFrame* f, SwhFrameOutputs* out)
 	out->num_sim_passes = uint32_t(p.simulations.passes.size());
 	out->sim_points = p.simulations.points.data();
 	out->num_sim_points = uint32_t(p.simulations.points.size());
+	out->views = p.views.data();
+	out->num_views = uint32_t(p.views.size());
+	out->main_draws = p.main_draws;
+	out->surface_texels = p.surface_texels;
 	return SW_OK;
 }
 
@@ -703,6 +714,11 @@ int swh_renderer_draw_frame(SwhRenderer* r, void* dst, uint32_t pitch, int dst_i
 {
 	if (!r) return SW_ERR_INVALID_ARGUMENT;
 	const FramePrep& p = r->frame->prep;
+	if (!p.views.empty())
+	{
+		g_error = "a frame with portal views renders through swh_renderer_render_frame";
+		return SW_ERR_STATE;
+	}
 	int st = sw_submit_draws(r->ctx, p.draws.data(), uint32_t(p.draws.size()), p.vertices.data(), uint32_t(p.vertices.size()));
 	if (st) return st;
 	return sw_render(r->ctx, dst, pitch, dst_is_device);
@@ -712,9 +728,10 @@ int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFra
 	float frame_duration_s, const float color_modulate[3], void* dst, uint32_t pitch, int dst_is_device)
 {
 	if (!r || (post && (!dst || !color_modulate))) return SW_ERR_INVALID_ARGUMENT;
-	// The GPU-side preparation emits each leaf's polygons only; a scene with triangle models, sprites or decals
-	// (drawn after their leaf's polygons) takes the host-prepared draw list.
-	if (r->gpu_prep && r->scene->scene.models.empty() && r->scene->scene.sprites.empty() && r->scene->scene.decals.empty())
+	// The GPU-side preparation emits each leaf's polygons only; a scene with triangle models, sprites, decals
+	// or portals (drawn after their leaf's polygons) takes the host-prepared draw list.
+	const Scene& scene = r->scene->scene;
+	if (r->gpu_prep && scene.models.empty() && scene.sprites.empty() && scene.decals.empty() && scene.view_portals.empty())
 	{
 		int st = swh_frame_prepare_view(r->frame, frame_index, o);
 		if (st) return st;
@@ -752,6 +769,9 @@ int swh_renderer_render_frame(SwhRenderer* r, uint32_t frame_index, const SwhFra
 	in.num_vertices = uint32_t(p.vertices.size());
 	in.tri_vertices = p.tri_vertices.data();
 	in.num_tri_vertices = uint32_t(p.tri_vertices.size());
+	in.num_views = uint32_t(p.views.size());
+	in.views = p.views.data();
+	in.main_draws = p.main_draws;
 	if (post)
 	{
 		in.postprocess = 1;

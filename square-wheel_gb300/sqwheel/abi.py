@@ -54,6 +54,11 @@ VERTEX16 = np.dtype([("x", "<i4"), ("y", "<i4")], align=True)
 TEXTURE_PASS = np.dtype([("kind", "<u4"), ("dst_mip", "<u4"), ("src_mip", "<u4"), ("blending_mode", "<u4"),
                          ("shift", "<i4", 2), ("light", "<f4", 3), ("shifts_offset", "<u4")], align=True)
 SW_TEXPASS_TURB, SW_TEXPASS_LAYER, SW_TEXPASS_EMISSIVE = 1, 2, 0x100
+# SwView: a nested view of a whole frame (a portal's texture rendered before the frame's own draws)
+VIEW = np.dtype([("target_offset", "<u8"), ("width", "<u4"), ("height", "<u4"), ("first_draw", "<u4"),
+                 ("num_draws", "<u4"), ("clear_background", "<u4"), ("mix_blend", "<u4"), ("mix_offset", "<u8"),
+                 ("mix_size", "<u4", 2), ("mix_tc_min", "<i4", 2), ("mix_light", "<f4", 3), ("reserved", "<u4")])
+SW_VIEW_NO_MIX = 0xFFFFFFFF
 # SwSimPass / SwSimPoint (sw_update_simulations): simulated water and fire effects
 SIM_PASS = np.dtype([("kind", "<u4"), ("launch", "<u4"), ("size_log2", "<u4", 2), ("state_src", "<u8"),
                      ("state_dst", "<u8"), ("first_point", "<u4"), ("num_points", "<u4"), ("dst_mip", "<u4"),
@@ -139,7 +144,8 @@ class FrameInput(ctypes.Structure):
                 ("num_vertices", ctypes.c_uint32), ("postprocess", ctypes.c_uint32), ("post", PostConfig),
                 ("frame_duration_s", ctypes.c_float), ("color_modulate", ctypes.c_float * 3), ("dst", ctypes.c_void_p),
                 ("dst_pitch", ctypes.c_uint32), ("dst_is_device", ctypes.c_int32), ("tri_vertices", ctypes.c_void_p),
-                ("num_tri_vertices", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("num_tri_vertices", ctypes.c_uint32), ("num_views", ctypes.c_uint32), ("views", ctypes.c_void_p),
+                ("main_draws", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class ViewFrameInput(ctypes.Structure):
@@ -180,6 +186,7 @@ LAYOUT_ORDER = [
     ("SwShadowSide", SHADOW_SIDE.itemsize), ("SwShadowLeaf", SHADOW_LEAF.itemsize),
     ("SwMaterialFrame", MATERIAL_FRAME.itemsize), ("SwTriVertex", TRI_VERTEX.itemsize),
     ("SwTexturePass", TEXTURE_PASS.itemsize), ("SwSimPass", SIM_PASS.itemsize), ("SwSimPoint", SIM_POINT.itemsize),
+    ("SwView", VIEW.itemsize),
 ]
 
 

@@ -27,6 +27,7 @@ class SceneConfig(ctypes.Structure):
         ("animated_materials", ctypes.c_uint32), ("projector_lights", ctypes.c_uint32), ("num_models", ctypes.c_uint32), ("model_triangles", ctypes.c_uint32),
         ("model_frames", ctypes.c_uint32), ("turb_materials", ctypes.c_uint32), ("layered_materials", ctypes.c_uint32), ("num_sprites", ctypes.c_uint32),
         ("num_decals", ctypes.c_uint32), ("water_materials", ctypes.c_uint32), ("fire_materials", ctypes.c_uint32),
+        ("num_portals", ctypes.c_uint32), ("portals_depth", ctypes.c_uint32),
     ]
 
 
@@ -95,7 +96,9 @@ class FrameOutputs(ctypes.Structure):
                 ("model_triangles", ctypes.c_uint32), ("texture_passes", ctypes.c_void_p),
                 ("num_texture_passes", ctypes.c_uint32), ("num_texture_shifts", ctypes.c_uint32),
                 ("texture_shifts", ctypes.c_void_p), ("sim_passes", ctypes.c_void_p),
-                ("num_sim_passes", ctypes.c_uint32), ("num_sim_points", ctypes.c_uint32), ("sim_points", ctypes.c_void_p)]
+                ("num_sim_passes", ctypes.c_uint32), ("num_sim_points", ctypes.c_uint32), ("sim_points", ctypes.c_void_p),
+                ("views", ctypes.c_void_p), ("num_views", ctypes.c_uint32), ("main_draws", ctypes.c_uint32),
+                ("surface_texels", ctypes.c_uint64)]
 
 
 def load_host_library():
@@ -359,6 +362,9 @@ class Frame:
         self.texture_shifts = arr(o.texture_shifts, o.num_texture_shifts, np.int32)
         self.sim_passes = arr(o.sim_passes, o.num_sim_passes, abi.SIM_PASS)
         self.sim_points = arr(o.sim_points, o.num_sim_points, abi.SIM_POINT)
+        self.views = arr(o.views, o.num_views, abi.VIEW)
+        self.main_draws = int(o.main_draws) if o.num_views else int(o.num_draws)
+        self.surface_texels = int(o.surface_texels)
         self.lights = arr(o.lights, o.num_lights, abi.LIGHT)
         self.total_texels = int(o.total_texels)
         self.params = abi.FrameParams()
