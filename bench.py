@@ -513,6 +513,7 @@ def run_frame_gpu(args, world, rank, local):
                        "stage_kernel_sum_ms": round(stage_sum_ms, 4),
                        "per_call_api_frame_span_ms": round(frame_span / s, 4),
                        "tuning": {"raster_tile": int(tune.raster_tile), "surface_blocks_per_sm": int(tune.surface_blocks_per_sm),
+                                  "surface_texels_per_thread": int(tune.surface_texels_per_thread),
                                   "autotune_best_ms": round(tune_ms, 4)},
                        "parallelism": f"replicas x{world}"},
             "stages": stages,

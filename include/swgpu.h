@@ -727,6 +727,10 @@ typedef struct SwTuning {
 	uint32_t raster_tile;
 	/* persistent grid of the surface build: blocks per SM, 1..64 */
 	uint32_t surface_blocks_per_sm;
+	/* texels per surface-build thread: 1, or 4 consecutive texels sharing their lightmap line entries
+	 * (0 = the default, 1) */
+	uint32_t surface_texels_per_thread;
+	uint32_t reserved;
 } SwTuning;
 int sw_set_tuning(SwCtx* ctx, const SwTuning* tuning);
 int sw_get_tuning(SwCtx* ctx, SwTuning* out_tuning);

@@ -114,6 +114,30 @@ __device__ __forceinline__ uint32_t wrap(int32_t a, uint32_t b)
 	int32_t r = a % int32_t(b);
 	return uint32_t(r < 0 ? r + int32_t(b) : r);
 }
+// rem_euclid by a texture side: a mask for powers of two (mask != ~0u), else the remainder
+__device__ __forceinline__ uint32_t wrap_side(int32_t a, uint32_t b, uint32_t mask)
+{
+	return mask != ~0u ? uint32_t(a) & mask : wrap(a, b);
+}
+// n / d and n % d: the float estimate of the quotient (truncated product with the rounded reciprocal) is
+// within one of it while the quotient stays below 2^22 (a surface's row), then corrected exactly
+__device__ __forceinline__ void div_row(uint32_t n, uint32_t d, float inv_d, uint32_t& q, uint32_t& r)
+{
+	int32_t qi = int32_t(__fmul_rz(float(n), inv_d));
+	int32_t ri = int32_t(n) - qi * int32_t(d);
+	if (ri < 0)
+	{
+		--qi;
+		ri += int32_t(d);
+	}
+	else if (ri >= int32_t(d))
+	{
+		++qi;
+		ri -= int32_t(d);
+	}
+	q = uint32_t(qi);
+	r = uint32_t(ri);
+}
 
 // cube_shadow_map_side_fetch (light.rs:235-258): 1 in light, 0 in shadow.
 __device__ __forceinline__ float cube_side_fetch(const unsigned long long* side, uint32_t size, float x, float y, float z)
@@ -163,10 +187,72 @@ __device__ __forceinline__ float light_shadow_factor(const SurfaceKernelArgs& a,
 							  : cube_side_fetch(maps + 4 * side_texels, m.size, -to_light.x, -to_light.y, az);
 }
 
-// Lighting of one texel (surfaces.rs:515-842); returns the ColorVec before conversion.
+// The line buffer of the reference's row loop (surfaces.rs:477-502) for one thread's run of texels: the
+// entries line_lightmap[lu] and [lu + 1] of texel row v (the vertical mixes of lightmap rows lv and
+// lv + 1 at ratio kv), kept while the run stays in that row and column and shifted by one when it
+// steps into the next lightmap column, as the reference's row buffer holds them.
+template <bool DIRECTIONAL>
+struct LineCache
+{
+	uint32_t si = 0xFFFFFFFFu, v = 0, lu = 0;
+	Lm line0, line1;
+};
+
+template <bool DIRECTIONAL>
+__device__ __forceinline__ void line_entries(const SurfaceKernelArgs& a, const SurfaceGpu& s, uint32_t si, uint32_t v,
+	uint32_t lv, uint32_t lu, float kv, LineCache<DIRECTIONAL>& c)
+{
+	if (c.si == si && c.v == v && c.lu == lu) return;
+	const uint64_t row0 = uint64_t(s.lm_offset) + uint64_t(lv) * s.lm_width;
+	const uint64_t row1 = row0 + s.lm_width;
+	if (c.si == si && c.v == v && c.lu + 1 == lu)
+		c.line0 = c.line1;
+	else
+		c.line0 = lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1 + lu), lm_load<DIRECTIONAL>(a, row0 + lu), kv);
+	c.line1 = lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1 + lu + 1), lm_load<DIRECTIONAL>(a, row0 + lu + 1), kv);
+	c.si = si;
+	c.v = v;
+	c.lu = lu;
+}
+
+// The texel's lightmap element (surfaces.rs:504-513): the horizontal mix of its two line entries.
+template <bool DIRECTIONAL>
+__device__ __forceinline__ Lm lightmap_sample(const SurfaceKernelArgs& a, const SurfaceGpu& s, uint32_t si, uint32_t u,
+	uint32_t v, LineCache<DIRECTIONAL>& c)
+{
+	const uint32_t log2 = s.lm_log2;
+	const uint32_t mask = (1u << log2) - 1u;
+	const uint32_t base_v = v + s.lm_shift1;
+	const float kv = mad2(float(base_v & mask), s.inv_scale, s.k_shift);
+	const uint32_t base_u = u + s.lm_shift0;
+	const float ku = mad2(float(base_u & mask), s.inv_scale, s.k_shift);
+	line_entries<DIRECTIONAL>(a, s, si, v, base_v >> log2, base_u >> log2, kv, c);
+	return lm_mix<DIRECTIONAL>(c.line1, c.line0, ku);
+}
+
+// The same element for a single texel: both line entries built for it alone.
+template <bool DIRECTIONAL>
+__device__ __forceinline__ Lm lightmap_sample_once(const SurfaceKernelArgs& a, const SurfaceGpu& s, uint32_t u, uint32_t v)
+{
+	const uint32_t log2 = s.lm_log2;
+	const uint32_t mask = (1u << log2) - 1u;
+	const uint32_t base_v = v + s.lm_shift1;
+	const float kv = mad2(float(base_v & mask), s.inv_scale, s.k_shift);
+	const uint32_t base_u = u + s.lm_shift0;
+	const uint32_t lu = base_u >> log2;
+	const float ku = mad2(float(base_u & mask), s.inv_scale, s.k_shift);
+	const uint64_t row0 = uint64_t(s.lm_offset) + uint64_t(base_v >> log2) * s.lm_width;
+	const uint64_t row1 = row0 + s.lm_width;
+	const Lm line0 = lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1 + lu), lm_load<DIRECTIONAL>(a, row0 + lu), kv);
+	const Lm line1 = lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1 + lu + 1), lm_load<DIRECTIONAL>(a, row0 + lu + 1), kv);
+	return lm_mix<DIRECTIONAL>(line1, line0, ku);
+}
+
+// Lighting of one texel (surfaces.rs:515-842) with its lightmap element `l` (when the surface has a
+// lightmap); returns the ColorVec before conversion.
 template <bool DIRECTIONAL>
 __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const SurfaceGpu& s, uint64_t texel, uint32_t u,
-	uint32_t v, V3 cam)
+	uint32_t v, V3 cam, const Lm& l)
 {
 	const uint32_t tex_flags = s.flags & 7u;
 	const bool use_normal_map = (tex_flags & SW_TEX_HAS_NORMAL_MAP) != 0;
@@ -194,22 +280,6 @@ __device__ __forceinline__ CV shade_texel(const SurfaceKernelArgs& a, const Surf
 	CV direct = cv_zero(); // total_light_direct
 	if (s.flags & SW_SG_LIGHTMAP)
 	{
-		const uint32_t log2 = s.lm_log2;
-		const uint32_t mask = (1u << log2) - 1u;
-		const uint32_t base_v = v + s.lm_shift1;
-		const uint32_t lv = base_v >> log2;
-		const float kv = mad2(float(base_v & mask), s.inv_scale, s.k_shift);
-		const uint32_t base_u = u + s.lm_shift0;
-		const uint32_t lu = base_u >> log2;
-		const float ku = mad2(float(base_u & mask), s.inv_scale, s.k_shift);
-		const uint64_t row0 = uint64_t(s.lm_offset) + uint64_t(lv) * s.lm_width;
-		const uint64_t row1 = row0 + s.lm_width;
-		// line_lightmap[lu] and [lu + 1] of the reference's row buffer, then the horizontal mix.
-		const Lm line0 = lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1 + lu), lm_load<DIRECTIONAL>(a, row0 + lu), kv);
-		const Lm line1 =
-			lm_mix<DIRECTIONAL>(lm_load<DIRECTIONAL>(a, row1 + lu + 1), lm_load<DIRECTIONAL>(a, row0 + lu + 1), kv);
-		const Lm l = lm_mix<DIRECTIONAL>(line1, line0, ku);
-
 		if (spec == 0)
 		{
 			albedo = cv_rgb(l.amb, 1.0f);
@@ -321,8 +391,8 @@ template <class P>
 __device__ __forceinline__ typename P::T emissive_mix(const SurfaceKernelArgs& a, const SurfaceGpu& s, uint32_t u,
 	uint32_t v, typename P::T dst, bool additive)
 {
-	const uint32_t sv = wrap(s.tc1 + int32_t(v), s.em_h);
-	const uint32_t su = wrap(s.tc0 + int32_t(u), s.em_w);
+	const uint32_t sv = wrap_side(s.tc1 + int32_t(v), s.em_h, s.em_mask[1]);
+	const uint32_t su = wrap_side(s.tc0 + int32_t(u), s.em_w, s.em_mask[0]);
 	const uint32_t texel = __ldg(a.emissive_pixels + s.em_offset + uint64_t(sv) * s.em_w + su);
 	const CI t = ci_from_c32(texel);
 	CI m{{wmul(t.v[0], s.em_light[0]) >> 8, wmul(t.v[1], s.em_light[1]) >> 8, wmul(t.v[2], s.em_light[2]) >> 8, 0}};
@@ -333,8 +403,14 @@ __device__ __forceinline__ typename P::T emissive_mix(const SurfaceKernelArgs& a
 	return P::from_ci(m);
 }
 
-template <class P, bool DIRECTIONAL>
-__global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
+// K consecutive texels of the flat texel space per thread (a warp owns 32 * K): the thread's surface is
+// found once (lane 0's binary search for the warp, then forward steps), its later texels step along the
+// row and into following surfaces, and its line-buffer entries carry from texel to texel. K = 1 runs
+// four blocks per SM (64 registers, a few bytes spilled): the kernel issues ~600 instructions per
+// texel of exact, unfused f32 shading and integer indexing, and more resident warps hide their latency
+// better than fewer, longer threads (K = 4 and its shared line entries measured no faster).
+template <class P, bool DIRECTIONAL, int K>
+__global__ void __launch_bounds__(256, K == 1 ? 4 : 2) surf_build_kernel(SurfaceKernelArgs a)
 {
 	typedef typename P::T T;
 	T* arena = static_cast<T*>(a.arena);
@@ -342,12 +418,12 @@ __global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
 	const V3 cam = a.cam_pos_dev ? mkv3(a.cam_pos_dev[0], a.cam_pos_dev[1], a.cam_pos_dev[2])
 								 : mkv3(a.cam_pos[0], a.cam_pos[1], a.cam_pos[2]);
 	const uint32_t num_surfaces = a.counts ? a.counts->num_surfaces : a.num_surfaces;
-	const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+	const uint64_t stride = uint64_t(gridDim.x) * blockDim.x * K;
 	const uint32_t lane = threadIdx.x & 31u;
-	const uint64_t warp_first = uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u);
+	const uint64_t warp_first = (uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u)) * K;
 	for (uint64_t wbase = a.work_begin + warp_first; wbase < total; wbase += stride)
 	{
-		const uint64_t t = wbase + lane;
+		const uint64_t t0 = wbase + uint64_t(lane) * K;
 		// Surface of the warp's first texel (binary search by lane 0), then forward steps per lane.
 		uint32_t s0 = 0;
 		if (lane == 0)
@@ -364,30 +440,70 @@ __global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
 			s0 = lo;
 		}
 		uint32_t si = __shfl_sync(0xFFFFFFFFu, s0, 0);
-		if (t >= total) continue;
+		if (t0 >= total) continue;
 		uint64_t next = __ldg(a.work_prefix + si + 1);
-		while (next <= t)
+		while (next <= t0)
 		{
 			++si;
 			next = __ldg(a.work_prefix + si + 1);
 		}
-		const SurfaceGpu& s = a.surfaces[si];
-		const uint32_t local = uint32_t(t - __ldg(a.work_prefix + si));
-		const uint32_t v = local / s.width;
-		const uint32_t u = local - v * s.width;
-
-		T out = T(0);
-		const bool diffuse_layer = (s.flags & SW_SG_DIFFUSE) != 0;
-		if (diffuse_layer)
+		uint32_t local = uint32_t(t0 - __ldg(a.work_prefix + si));
+		uint32_t width = a.surfaces[si].width;
+		uint32_t v, u;
+		div_row(local, width, a.surfaces[si].inv_width, v, u);
+		[[maybe_unused]] LineCache<DIRECTIONAL> cache;
+#pragma unroll 1
+		for (int k = 0; k < K; ++k)
 		{
-			const uint32_t sv = wrap(s.tc1 + int32_t(v), s.tex_h);
-			const uint32_t su = wrap(s.tc0 + int32_t(u), s.tex_w);
-			const uint64_t texel =
-				__ldg(reinterpret_cast<const unsigned long long*>(a.texels) + s.tex_offset + uint64_t(sv) * s.tex_w + su);
-			out = P::from_cv(shade_texel<DIRECTIONAL>(a, s, texel, u, v, cam));
+			if (k > 0)
+			{
+				const uint64_t t = t0 + uint64_t(k);
+				if (t >= total) break;
+				if (t >= next)
+				{
+					// the next surface with texels: its first texel
+					do
+					{
+						++si;
+						next = __ldg(a.work_prefix + si + 1);
+					} while (next <= t);
+					width = a.surfaces[si].width;
+					local = 0;
+					u = 0;
+					v = 0;
+				}
+				else
+				{
+					++local;
+					if (++u == width)
+					{
+						u = 0;
+						++v;
+					}
+				}
+			}
+			const SurfaceGpu& s = a.surfaces[si];
+			T out = T(0);
+			const bool diffuse_layer = (s.flags & SW_SG_DIFFUSE) != 0;
+			if (diffuse_layer)
+			{
+				const uint32_t sv = wrap_side(s.tc1 + int32_t(v), s.tex_h, s.tex_mask[1]);
+				const uint32_t su = wrap_side(s.tc0 + int32_t(u), s.tex_w, s.tex_mask[0]);
+				const uint64_t texel =
+					__ldg(reinterpret_cast<const unsigned long long*>(a.texels) + s.tex_offset + uint64_t(sv) * s.tex_w + su);
+				Lm l;
+				if (s.flags & SW_SG_LIGHTMAP)
+				{
+					if constexpr (K == 1)
+						l = lightmap_sample_once<DIRECTIONAL>(a, s, u, v);
+					else
+						l = lightmap_sample<DIRECTIONAL>(a, s, si, u, v, cache);
+				}
+				out = P::from_cv(shade_texel<DIRECTIONAL>(a, s, texel, u, v, cam, l));
+			}
+			if (s.flags & SW_SG_EMISSIVE) out = emissive_mix<P>(a, s, u, v, out, diffuse_layer);
+			arena[s.out_offset + local] = out;
 		}
-		if (s.flags & SW_SG_EMISSIVE) out = emissive_mix<P>(a, s, u, v, out, diffuse_layer);
-		arena[s.out_offset + local] = out;
 	}
 	pdl_trigger(); // the tile pass may be scheduled (it waits for this grid before reading the arena)
 }
@@ -395,31 +511,36 @@ __global__ void __launch_bounds__(256, 3) surf_build_kernel(SurfaceKernelArgs a)
 } // namespace
 
 int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, int blocks_per_sm, cudaStream_t stream,
-	uint64_t work_hint)
+	uint64_t work_hint, uint32_t texels_per_thread)
 {
 	const uint64_t work = args.counts ? work_hint : args.total_work - args.work_begin;
 	if (work == 0 && !args.counts) return 0;
 	const int threads = 256;
-	uint64_t blocks_needed = (work + threads - 1) / threads;
+	// texels per thread: as tuned (by default 1: the shading arithmetic, not the lightmap mixes, bounds the
+	// kernel, and carrying line entries over 4 texels measured no faster)
+	const int k = texels_per_thread == 4 ? 4 : 1;
+	uint64_t blocks_needed = (work + uint64_t(threads) * k - 1) / (uint64_t(threads) * k);
 	if (args.counts && blocks_needed < uint64_t(num_sms)) blocks_needed = uint64_t(num_sms);
 	// At most blocks_per_sm blocks per SM (several waves of resident blocks): small frames get one
 	// texel per thread (latency hidden by parallelism), large batches stride.
 	uint64_t blocks_max = uint64_t(num_sms) * uint64_t(blocks_per_sm);
 	unsigned blocks = unsigned(blocks_needed < blocks_max ? blocks_needed : blocks_max);
-	if (pixel_format == SW_PIXEL_C64)
+	const bool c64 = pixel_format == SW_PIXEL_C64;
+	if (k == 4)
 	{
-		if (args.directional)
-			surf_build_kernel<PixC64, true><<<blocks, threads, 0, stream>>>(args);
+		if (c64)
+			args.directional ? surf_build_kernel<PixC64, true, 4><<<blocks, threads, 0, stream>>>(args)
+							 : surf_build_kernel<PixC64, false, 4><<<blocks, threads, 0, stream>>>(args);
 		else
-			surf_build_kernel<PixC64, false><<<blocks, threads, 0, stream>>>(args);
+			args.directional ? surf_build_kernel<PixC32, true, 4><<<blocks, threads, 0, stream>>>(args)
+							 : surf_build_kernel<PixC32, false, 4><<<blocks, threads, 0, stream>>>(args);
 	}
+	else if (c64)
+		args.directional ? surf_build_kernel<PixC64, true, 1><<<blocks, threads, 0, stream>>>(args)
+						 : surf_build_kernel<PixC64, false, 1><<<blocks, threads, 0, stream>>>(args);
 	else
-	{
-		if (args.directional)
-			surf_build_kernel<PixC32, true><<<blocks, threads, 0, stream>>>(args);
-		else
-			surf_build_kernel<PixC32, false><<<blocks, threads, 0, stream>>>(args);
-	}
+		args.directional ? surf_build_kernel<PixC32, true, 1><<<blocks, threads, 0, stream>>>(args)
+						 : surf_build_kernel<PixC32, false, 1><<<blocks, threads, 0, stream>>>(args);
 	return int(cudaGetLastError());
 }
 

@@ -35,6 +35,11 @@ struct __align__(16) SurfaceGpu
 	uint32_t em_w, em_h;
 	int32_t em_light[3]; // ColorVecI lanes [b, g, r] of the emissive light * 256 (truncated)
 	uint64_t out_offset;
+	// size - 1 of the texture (tex_mask) and emissive (em_mask) sides that are powers of two, whose
+	// rem_euclid is then a mask; ~0u for other sizes
+	uint32_t tex_mask[2], em_mask[2];
+	float inv_width; // 1 / width: the row of a texel index by a float estimate and an exact correction
+	uint32_t reserved;
 };
 
 #define SW_SG_DIFFUSE (1u << 8)
@@ -141,12 +146,19 @@ __host__ __device__ inline void make_surface_gpu(const SwSurfaceDesc& d, const S
 		o.em_light[0] = o.em_light[1] = o.em_light[2] = 0;
 	}
 	o.out_offset = d.out_offset;
+	auto pow2_mask = [](uint32_t n) { return (n != 0 && (n & (n - 1)) == 0) ? n - 1 : ~0u; };
+	o.tex_mask[0] = pow2_mask(o.tex_w);
+	o.tex_mask[1] = pow2_mask(o.tex_h);
+	o.em_mask[0] = pow2_mask(o.em_w);
+	o.em_mask[1] = pow2_mask(o.em_h);
+	o.inv_width = 1.0f / float(d.size[0] ? d.size[0] : 1u);
+	o.reserved = 0;
 }
 
 // Grid of at most num_sms * blocks_per_sm blocks of 256 threads that stride over the texels. With
 // args.counts set the texel count is on the device: work_hint (an estimate) sizes the grid instead.
 int launch_surface_build(const SurfaceKernelArgs& args, uint32_t pixel_format, int num_sms, int blocks_per_sm, cudaStream_t stream,
-	uint64_t work_hint = 0);
+	uint64_t work_hint = 0, uint32_t texels_per_thread = 0);
 
 // ---- rasteriser ----
 

@@ -56,6 +56,7 @@ struct ViewGraphKey
 	size_t block_bytes;
 	unsigned surface_blocks;
 	int surface_blocks_per_sm;
+	int surface_texels_per_thread;
 	uint32_t raster_tile, pixel_format, postprocess, dst_pitch;
 	void* dst;
 	int32_t dst_is_device;
@@ -156,7 +157,7 @@ struct SwCtx
 	SwStats stats{};
 
 	// Launch configuration (sw_set_tuning / sw_autotune).
-	SwTuning tuning{0u, 24u};
+	SwTuning tuning{0u, 24u, 0u, 0u};
 
 	// Whole-frame CUDA graph (sw_draw_frame): double-buffered pinned staging of all per-frame arrays,
 	// the instantiated graph, updated in place from each frame's capture.
@@ -789,7 +790,8 @@ static int launch_surfaces(SwCtx* ctx, const SurfaceInputs* in = nullptr)
 	const SurfaceKernelArgs a = surface_args(ctx, in);
 	stage_begin(ctx, STAGE_SURFACES);
 	int r = check_kernel(ctx,
-		launch_surface_build(a, ctx->frame.pixel_format, ctx->num_sms, int(ctx->tuning.surface_blocks_per_sm), ctx->stream),
+		launch_surface_build(a, ctx->frame.pixel_format, ctx->num_sms, int(ctx->tuning.surface_blocks_per_sm), ctx->stream, 0,
+			ctx->tuning.surface_texels_per_thread),
 		"surface build");
 	stage_end(ctx, STAGE_SURFACES);
 	if (r) return r;
@@ -2529,6 +2531,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 	}
 	key.surface_blocks = ctx->view_surface_blocks;
 	key.surface_blocks_per_sm = int(ctx->tuning.surface_blocks_per_sm);
+	key.surface_texels_per_thread = int(ctx->tuning.surface_texels_per_thread);
 
 	RasterArgs& ra = key.raster;
 	if ((r = ensure_bins(ctx, p.width, p.height, cap_draws))) return r;
@@ -2576,7 +2579,7 @@ int sw_draw_frame_view(SwCtx* ctx, const SwViewFrameInput* in)
 			SW_CUDA(ctx, cudaEventRecord(ctx->ev_setup, aux));
 			if ((rr = check_kernel(ctx,
 					 launch_surface_build(key.surf, p.pixel_format, ctx->num_sms, int(ctx->tuning.surface_blocks_per_sm), s,
-						 uint64_t(key.surface_blocks) * 256),
+						 uint64_t(key.surface_blocks) * 256, uint32_t(key.surface_texels_per_thread)),
 					 "surface build")))
 				return rr;
 			SW_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_setup, 0));
@@ -2870,9 +2873,11 @@ int sw_set_frame_graph(SwCtx* ctx, int enable)
 int sw_set_tuning(SwCtx* ctx, const SwTuning* t)
 {
 	if (!ctx || !t) return SW_ERR_INVALID_ARGUMENT;
-	if (t->raster_tile >= SW_RASTER_TILE_VARIANTS || t->surface_blocks_per_sm < 1 || t->surface_blocks_per_sm > 64)
+	if (t->raster_tile >= SW_RASTER_TILE_VARIANTS || t->surface_blocks_per_sm < 1 || t->surface_blocks_per_sm > 64 ||
+		(t->surface_texels_per_thread != 0 && t->surface_texels_per_thread != 1 && t->surface_texels_per_thread != 4))
 		return fail(ctx, SW_ERR_INVALID_ARGUMENT, "tuning out of range");
-	if (t->raster_tile != ctx->tuning.raster_tile || t->surface_blocks_per_sm != ctx->tuning.surface_blocks_per_sm)
+	if (t->raster_tile != ctx->tuning.raster_tile || t->surface_blocks_per_sm != ctx->tuning.surface_blocks_per_sm ||
+		t->surface_texels_per_thread != ctx->tuning.surface_texels_per_thread)
 	{
 		// other kernels: the frame graph is instantiated anew
 		SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -2900,31 +2905,34 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 	const SwTuning start = ctx->tuning;
 	if (!ctx->timing && (r = sw_enable_timing(ctx, 1))) return r;
 	const uint32_t blocks[] = {8u, 16u, 24u, 32u, 48u};
+	const uint32_t texels[] = {1u, 4u};
 	SwTuning best = start;
 	float best_ms = 1e30f;
 	std::vector<float> ms(reps);
 	for (uint32_t tile = 0; tile < SW_RASTER_TILE_VARIANTS && r == SW_OK; ++tile)
-		for (uint32_t b : blocks)
-		{
-			const SwTuning t{tile, b};
-			if ((r = sw_set_tuning(ctx, &t))) break;
-			for (uint32_t i = 0; i < 2 + reps && r == SW_OK; ++i)
+		for (uint32_t bi = 0; bi < sizeof(blocks) / sizeof(blocks[0]) && r == SW_OK; ++bi)
+			for (uint32_t ki = 0; ki < sizeof(texels) / sizeof(texels[0]) && r == SW_OK; ++ki)
 			{
-				if ((r = sw_draw_frame(ctx, sample))) break;
-				float t5[5];
-				if ((r = sw_get_timings(ctx, t5))) break;
-				if (i >= 2) ms[i - 2] = t5[STAGE_FRAME];
+				const uint32_t b = blocks[bi], k = texels[ki];
+				const SwTuning t{tile, b, k, 0u};
+				if ((r = sw_set_tuning(ctx, &t))) break;
+				for (uint32_t i = 0; i < 2 + reps && r == SW_OK; ++i)
+				{
+					if ((r = sw_draw_frame(ctx, sample))) break;
+					float t5[5];
+					if ((r = sw_get_timings(ctx, t5))) break;
+					if (i >= 2) ms[i - 2] = t5[STAGE_FRAME];
+				}
+				if (r) break;
+				std::vector<float> sorted = ms;
+				std::sort(sorted.begin(), sorted.end());
+				const float med = sorted[sorted.size() / 2];
+				if (med < best_ms)
+				{
+					best_ms = med;
+					best = t;
+				}
 			}
-			if (r) break;
-			std::vector<float> sorted = ms;
-			std::sort(sorted.begin(), sorted.end());
-			const float med = sorted[sorted.size() / 2];
-			if (med < best_ms)
-			{
-				best_ms = med;
-				best = t;
-			}
-		}
 	// restore the exposure state and the timing switch; keep the best configuration
 	const int r2 = finalize_exposure(ctx);
 	ctx->exposure = exposure;

@@ -168,7 +168,8 @@ class ViewCounts(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     """SwTuning: launch configuration (raster tile shape, surface-build blocks per SM)."""
-    _fields_ = [("raster_tile", ctypes.c_uint32), ("surface_blocks_per_sm", ctypes.c_uint32)]
+    _fields_ = [("raster_tile", ctypes.c_uint32), ("surface_blocks_per_sm", ctypes.c_uint32),
+                ("surface_texels_per_thread", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 SW_RASTER_TILE_VARIANTS = 5

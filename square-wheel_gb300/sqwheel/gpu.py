@@ -418,8 +418,8 @@ class GpuRenderer:
         self._check(self.lib.sw_get_tuning(self.ctx, ctypes.byref(t)), "sw_get_tuning")
         return t
 
-    def set_tuning(self, raster_tile, surface_blocks_per_sm):
-        t = abi.Tuning(raster_tile, surface_blocks_per_sm)
+    def set_tuning(self, raster_tile, surface_blocks_per_sm, surface_texels_per_thread=0):
+        t = abi.Tuning(raster_tile, surface_blocks_per_sm, surface_texels_per_thread, 0)
         self._check(self.lib.sw_set_tuning(self.ctx, ctypes.byref(t)), "sw_set_tuning")
 
     def autotune(self, frame_input, reps=5):
