@@ -735,8 +735,9 @@ typedef struct SwTuning {
 int sw_set_tuning(SwCtx* ctx, const SwTuning* tuning);
 int sw_get_tuning(SwCtx* ctx, SwTuning* out_tuning);
 /* Autotuner: times `reps` replays of the sample frame (sw_draw_frame) for every raster tile shape and a
- * set of surface grid sizes, keeps the fastest configuration in the context and returns it with its
- * median device time per frame in ms. The exposure state is restored afterwards. */
+ * set of surface grid sizes (texels per surface thread kept as set), keeps the fastest configuration in
+ * the context and returns it with its median device time per frame in ms. The exposure state is
+ * restored afterwards. */
 int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning* out_best, float* out_best_ms);
 
 /* sizeof() of the ABI structs in this order: SwCreateInfo, SwTextureMip, SwEmissiveMip,

@@ -2905,7 +2905,8 @@ int sw_autotune(SwCtx* ctx, const SwFrameInput* sample, uint32_t reps, SwTuning*
 	const SwTuning start = ctx->tuning;
 	if (!ctx->timing && (r = sw_enable_timing(ctx, 1))) return r;
 	const uint32_t blocks[] = {8u, 16u, 24u, 32u, 48u};
-	const uint32_t texels[] = {1u, 4u};
+	// texels per surface thread stay as set: 4 measured slower than 1 on frames (fewer resident warps)
+	const uint32_t texels[] = {start.surface_texels_per_thread};
 	SwTuning best = start;
 	float best_ms = 1e30f;
 	std::vector<float> ms(reps);
