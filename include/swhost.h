@@ -53,6 +53,7 @@ typedef struct SwhSceneConfig {
 	uint32_t fire_materials;      /* base materials with a fire effect (before the water ones) */
 	uint32_t num_portals;         /* portals (mirrors, cameras, parallax windows) in the camera path's rooms */
 	uint32_t portals_depth;       /* RendererConfig::portals_depth: nested portal view levels (the reference's default is 2; at most 8; 0: portals show black mixed with their texture) */
+	uint32_t light_grid;          /* nonzero: a seeded light grid over the rooms; models, sprites and portal textures take their light from it */
 } SwhSceneConfig;
 
 typedef struct SwhSceneInfo {
@@ -151,6 +152,14 @@ typedef struct SwhSimEffect {
 int swh_scene_simulated_effect(const SwhScene* scene, uint32_t material, SwhSimEffect* out_effect);
 /* Words of simulation state the scene's simulated effects use (sw_reserve_simulation_state). */
 int swh_scene_simulation_words(const SwhScene* scene, uint64_t* out_words);
+/* The scene's light grid (bsp_map_compact.rs:162-188): the header (cell size[3], start[3] as floats, then
+   size[3] as u32: 36 bytes), columns (start_z, first_sample, num_samples as u32) and samples (light cube
+   6x3, light_direction_vector_scaled 3, directional_light_color 3: 24 floats each). With null arrays only
+   the counts are written; otherwise the arrays hold at least those counts. */
+int swh_scene_light_grid(const SwhScene* scene, void* out_header, uint32_t* out_columns, float* out_samples,
+	uint64_t* num_columns, uint64_t* num_samples);
+/* fetch_light_from_grid (triangle_models_rendering.rs:582-700) at a position: 24 floats as one sample. */
+int swh_scene_fetch_light(const SwhScene* scene, const float pos[3], float out_sample[24]);
 const char* swh_last_error(void);
 
 typedef struct SwhFrameOptions {

@@ -2132,16 +2132,34 @@ void FramePrep::gather_nested(const FramePrep* n, uint64_t target_offset, uint32
 	v.mix_blend = SW_VIEW_NO_MIX;
 	if (portal.texture >= 0)
 	{
-		// mix_surface_with_texture with the texture's mip of the portal (:2230-2275); the light is the
-		// constant light_add (a light-grid fetch for light_scale > 0 needs the map's light grid)
+		// mix_surface_with_texture with the texture's mip of the portal (:2230-2275); the light is
+		// light_add, plus light_scale x the light grid's light at the portal polygon's centre (the cube
+		// side facing the normal and the directional component) when light_scale > 0
 		const LiteMip& m = sc.lite_mips[size_t(portal.texture) * NUM_MIPS + info.mip];
+		float light[3] = {portal.light_add[0], portal.light_add[1], portal.light_add[2]};
+		if (portal.light_scale > 0.0f)
+		{
+			const PolygonBasisVecs bv = form_plane_and_tex_coord_equation(portal.plane, portal.tex_coord_equation);
+			const float scale = float(1u << info.mip);
+			const Vec3 center = bv.start + (bv.u * scale) * (float(info.tc_min[0]) + float(width) * 0.5f) +
+				(bv.v * scale) * (float(info.tc_min[1]) + float(height) * 0.5f);
+			const LightGridElement g = sc.fetch_light_from_grid(center);
+			float total[3];
+			light_cube_light(g.light_cube, bv.normal, total);
+			const float ld = std::fmax(dot(bv.normal, g.light_direction_vector_scaled), 0.0f);
+			for (int c = 0; c < 3; ++c)
+			{
+				total[c] += g.directional_light_color[c] * ld;
+				light[c] = total[c] * portal.light_scale + portal.light_add[c];
+			}
+		}
 		v.mix_blend = portal.texture_blending_mode;
 		v.mix_offset = m.offset;
 		v.mix_size[0] = m.width;
 		v.mix_size[1] = m.height;
 		v.mix_tc_min[0] = info.tc_min[0];
 		v.mix_tc_min[1] = info.tc_min[1];
-		for (int c = 0; c < 3; ++c) v.mix_light[c] = portal.light_add[c];
+		for (int c = 0; c < 3; ++c) v.mix_light[c] = light[c];
 	}
 	nested.views.push_back(v);
 }

@@ -1836,8 +1836,172 @@ bool generate_scene(const SceneConfig& cfg, Scene& sc, std::string& error)
 			sc.view_portals.push_back(pt);
 		}
 	}
+	if (cfg.light_grid)
+	{
+		// A seeded light grid (own generator): 64-unit cells over the rooms; a column inside a room holds
+		// samples from the floor to one cell above its ceiling (the top one zero, as a lightmapper leaves
+		// samples in solid space), each the room's static lights gathered into a light cube plus the
+		// strongest as the directional component.
+		Rng grng(cfg.seed ^ 0x6121Du);
+		const float cell = 64.0f;
+		float lo[2] = {1e30f, 1e30f}, hi[2] = {-1e30f, -1e30f}, top = 0.0f;
+		for (const Room& r : b.rooms)
+		{
+			lo[0] = std::fmin(lo[0], r.x0), lo[1] = std::fmin(lo[1], r.y0);
+			hi[0] = std::fmax(hi[0], r.x1), hi[1] = std::fmax(hi[1], r.y1);
+			top = std::fmax(top, r.h);
+		}
+		LightGridHeader& hd = sc.light_grid_header;
+		for (int i = 0; i < 3; ++i) hd.grid_cell_size[i] = cell;
+		hd.grid_start[0] = lo[0], hd.grid_start[1] = lo[1], hd.grid_start[2] = 0.0f;
+		hd.grid_size[0] = uint32_t(std::ceil((hi[0] - lo[0]) / cell)) + 1;
+		hd.grid_size[1] = uint32_t(std::ceil((hi[1] - lo[1]) / cell)) + 1;
+		hd.grid_size[2] = uint32_t(std::ceil(top / cell)) + 2;
+		const Vec3 sides[6] = {v3(-1, 0, 0), v3(1, 0, 0), v3(0, -1, 0), v3(0, 1, 0), v3(0, 0, -1), v3(0, 0, 1)};
+		const float ambient = grng.uniform(0.05f, 0.2f);
+		for (uint32_t y = 0; y < hd.grid_size[1]; ++y)
+			for (uint32_t x = 0; x < hd.grid_size[0]; ++x)
+			{
+				const float px = lo[0] + float(x) * cell, py = lo[1] + float(y) * cell;
+				const Room* in = nullptr;
+				for (const Room& r : b.rooms)
+					if (px >= r.x0 && px <= r.x1 && py >= r.y0 && py <= r.y1) in = &r;
+				LightGridColumn col{0, uint32_t(sc.light_grid_samples.size()), 0};
+				if (in)
+				{
+					col.num_samples = uint32_t(std::floor(in->h / cell)) + 2;
+					for (uint32_t z = 0; z < col.num_samples; ++z)
+					{
+						LightGridElement e;
+						std::memset(&e, 0, sizeof(e));
+						if (z + 1 < col.num_samples)
+						{
+							const Vec3 p = v3(px, py, float(z) * cell);
+							float best = 0.0f;
+							for (int s6 = 0; s6 < 6; ++s6)
+								for (int c = 0; c < 3; ++c) e.light_cube[s6][c] = ambient;
+							for (size_t li = 0; li < in->lights.size(); ++li)
+							{
+								// the light's intensity / distance^2 (the lightmaps' units), spread over the cube sides
+								// facing it; the strongest also as the directional component
+								const Vec3 to = in->lights[li] - p;
+								const float d2 = std::fmax(dot(to, to), 32.0f * 32.0f);
+								const Vec3 dir = to / std::sqrt(d2);
+								const Vec3 c3 = in->light_colors[li] * (1.0f / d2);
+								for (int s6 = 0; s6 < 6; ++s6)
+								{
+									const float f = std::fmax(dot(dir, sides[s6]), 0.0f) * 0.5f;
+									e.light_cube[s6][0] += f * c3.x, e.light_cube[s6][1] += f * c3.y, e.light_cube[s6][2] += f * c3.z;
+								}
+								const float strength = c3.x + c3.y + c3.z;
+								if (strength > best)
+								{
+									best = strength;
+									e.light_direction_vector_scaled = dir * 0.5f;
+									e.directional_light_color[0] = c3.x, e.directional_light_color[1] = c3.y, e.directional_light_color[2] = c3.z;
+								}
+							}
+						}
+						sc.light_grid_samples.push_back(e);
+					}
+				}
+				sc.light_grid_columns.push_back(col);
+			}
+		// ModelLighting::Default (triangle_models_rendering.rs:541-546) and the sprites' grid fetch
+		// (partial_renderer.rs:911-932): the static light at the (fixed) position, fetched from the grid
+		for (ModelEntity& e : sc.models)
+		{
+			const LightGridElement g = sc.fetch_light_from_grid(e.position);
+			std::memcpy(e.light_cube, g.light_cube, sizeof(e.light_cube));
+			e.light_dir_scaled = g.light_direction_vector_scaled;
+			std::memcpy(e.light_color, g.directional_light_color, sizeof(e.light_color));
+		}
+		for (SpriteEntity& e : sc.sprites)
+		{
+			const LightGridElement g = sc.fetch_light_from_grid(e.position);
+			std::memcpy(e.light_cube, g.light_cube, sizeof(e.light_cube));
+			e.light_dir_scaled = g.light_direction_vector_scaled;
+			std::memcpy(e.light_color, g.directional_light_color, sizeof(e.light_color));
+		}
+		for (ViewPortal& vp : sc.view_portals)
+			if (vp.texture >= 0) vp.light_scale = 1.0f;
+	}
 	add_dynamic_lights(cfg, rng, sc);
 	return true;
+}
+
+LightGridElement Scene::fetch_light_from_grid(Vec3 pos) const
+{
+	// triangle_models_rendering.rs:582-700
+	LightGridElement total;
+	std::memset(&total, 0, sizeof(total));
+	const LightGridHeader& h = light_grid_header;
+	if (h.grid_size[0] == 0 || h.grid_size[1] == 0 || h.grid_size[2] == 0 || h.grid_cell_size[0] == 0.0f ||
+		h.grid_cell_size[1] == 0.0f || h.grid_cell_size[2] == 0.0f || light_grid_samples.empty() || light_grid_columns.empty())
+		return total;
+	const float gp[3] = {(pos.x - h.grid_start[0]) / h.grid_cell_size[0], (pos.y - h.grid_start[1]) / h.grid_cell_size[1],
+		(pos.z - h.grid_start[2]) / h.grid_cell_size[2]};
+	int32_t gi[3];
+	for (int i = 0; i < 3; ++i)
+	{
+		const float f = std::floor(gp[i]);
+		gi[i] = std::isnan(f) ? 0 : (f >= 2147483647.0f ? 2147483647 : (f <= -2147483648.0f ? int32_t(-2147483647 - 1) : int32_t(f)));
+	}
+	float total_factor = 0.0f;
+	for (int32_t dx = 0; dx <= 1; ++dx)
+	{
+		const int32_t x = gi[0] + dx;
+		if (x < 0 || x >= int32_t(h.grid_size[0])) continue;
+		const float fx = 1.0f - std::fabs(gp[0] - float(x));
+		for (int32_t dy = 0; dy <= 1; ++dy)
+		{
+			const int32_t y = gi[1] + dy;
+			if (y < 0 || y >= int32_t(h.grid_size[1])) continue;
+			const LightGridColumn& column = light_grid_columns[uint32_t(x) + uint32_t(y) * h.grid_size[0]];
+			if (column.num_samples == 0) continue;
+			const float fy = 1.0f - std::fabs(gp[1] - float(y));
+			for (int32_t dz = 0; dz <= 1; ++dz)
+			{
+				const int32_t z = gi[2] + dz;
+				if (z < 0 || z >= int32_t(h.grid_size[2])) continue;
+				if (uint32_t(z) < column.start_z || uint32_t(z) >= column.start_z + column.num_samples) continue;
+				const LightGridElement& sample = light_grid_samples[column.first_sample + (uint32_t(z) - column.start_z)];
+				bool zero = true;
+				for (int s6 = 0; s6 < 6 && zero; ++s6)
+					for (int c = 0; c < 3; ++c) zero = zero && sample.light_cube[s6][c] == 0.0f;
+				for (int c = 0; c < 3; ++c) zero = zero && sample.directional_light_color[c] == 0.0f;
+				zero = zero && sample.light_direction_vector_scaled.x == 0.0f && sample.light_direction_vector_scaled.y == 0.0f &&
+					sample.light_direction_vector_scaled.z == 0.0f;
+				if (zero) continue;
+				const float fz = 1.0f - std::fabs(gp[2] - float(z));
+				const float f = fx * fy * fz;
+				for (int c = 0; c < 3; ++c)
+				{
+					for (int s6 = 0; s6 < 6; ++s6) total.light_cube[s6][c] += sample.light_cube[s6][c] * f;
+					total.directional_light_color[c] += sample.directional_light_color[c] * f;
+				}
+				total.light_direction_vector_scaled = total.light_direction_vector_scaled + sample.light_direction_vector_scaled * f;
+				total_factor += f;
+			}
+		}
+	}
+	if (total_factor <= 0.0f)
+	{
+		std::memset(&total, 0, sizeof(total));
+		return total;
+	}
+	if (total_factor < 0.995f)
+	{
+		// renormalised when some of the 8 samples were missing
+		const float inv = 1.0f / total_factor;
+		for (int c = 0; c < 3; ++c)
+		{
+			for (int s6 = 0; s6 < 6; ++s6) total.light_cube[s6][c] *= inv;
+			total.directional_light_color[c] *= inv;
+		}
+		total.light_direction_vector_scaled = total.light_direction_vector_scaled * inv;
+	}
+	return total;
 }
 
 uint32_t Scene::leaf_of(Vec3 p) const
@@ -1949,6 +2113,19 @@ bool check_map(const SqwmMap& m, bool directional, std::string& error)
 			if (uint64_t(p.lightmap_data_offset) + lw * lh > lm_elems) return bad("polygon %llu: lightmap out of range", i);
 		}
 	}
+	// the light grid: one column per (x, y) cell, each column's samples inside the sample list
+	const LightGridHeader& g = m.light_grid_header;
+	if (!m.light_grid_columns.empty() || !m.light_grid_samples.empty())
+	{
+		if (uint64_t(g.grid_size[0]) * g.grid_size[1] != m.light_grid_columns.size())
+			return bad("light grid: %llu columns, not one per grid cell", m.light_grid_columns.size());
+		for (size_t i = 0; i < m.light_grid_columns.size(); ++i)
+		{
+			const LightGridColumn& c = m.light_grid_columns[i];
+			if (c.num_samples != 0 && uint64_t(c.first_sample) + c.num_samples > m.light_grid_samples.size())
+				return bad("light grid column %llu: samples out of range", i);
+		}
+	}
 	return true;
 }
 
@@ -2007,6 +2184,9 @@ bool scene_from_map(const SqwmMap& m, const SceneConfig& cfg, Scene& sc, std::st
 	sc.vertices = m.vertices;
 	sc.lightmaps = m.lightmaps;
 	sc.directional_lightmaps = m.directional_lightmaps;
+	sc.light_grid_header = m.light_grid_header;
+	sc.light_grid_columns = m.light_grid_columns;
+	sc.light_grid_samples = m.light_grid_samples;
 	sc.lightmap_elements = cfg.directional_lightmaps ? m.directional_lightmaps.size() : m.lightmaps.size() / 3;
 	sc.lightmaps_compressed.resize(m.lightmaps_compressed.size() * sizeof(CompressedColor));
 	if (!sc.lightmaps_compressed.empty())

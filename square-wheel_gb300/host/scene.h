@@ -292,6 +292,26 @@ struct ViewPortal
 	float light_add[3] = {1.0f, 1.0f, 1.0f};
 };
 
+// The map's light grid (bsp_map_compact.rs:162-188): columns of samples over a regular grid, each
+// sample a light cube and one directional component; models, sprites and portal textures take their
+// light from it (fetch_light_from_grid).
+struct LightGridElement
+{
+	float light_cube[6][3];
+	Vec3 light_direction_vector_scaled;
+	float directional_light_color[3];
+};
+struct LightGridHeader
+{
+	float grid_cell_size[3];
+	float grid_start[3];
+	uint32_t grid_size[3];
+};
+struct LightGridColumn
+{
+	uint32_t start_z, first_sample, num_samples;
+};
+
 // One mip of a TextureLite (Color32 pixels, src/square_wheel/textures.rs:89-91) in Scene::lite_pixels.
 struct LiteMip
 {
@@ -336,6 +356,7 @@ struct SceneConfig
 	uint32_t num_sprites = 0;         // sprites in the rooms (all four orientations, several blending modes)
 	uint32_t num_decals = 0;          // decals on the rooms' walls and floors
 	uint32_t num_portals = 0;         // portals in the camera path's rooms: mirrors, cameras, parallax windows
+	uint32_t light_grid = 0;          // a seeded light grid from the rooms' lights (models, sprites and portals lit from it)
 	uint32_t portals_depth = 2;       // RendererConfig::portals_depth: nested portal views (at most 8)
 	uint32_t turb_materials = 0;      // the last base materials but layered_materials have a turbulence effect
 	uint32_t layered_materials = 0;   // the last this many base materials are layered animations
@@ -386,6 +407,12 @@ struct Scene
 	std::vector<std::vector<uint32_t>> leaf_decals;
 	// portals and the portals index (DynamicObjectsIndex::position_portals): each portal's leafs, each
 	// leaf's portals in portal order
+	LightGridHeader light_grid_header{};
+	std::vector<LightGridColumn> light_grid_columns;
+	std::vector<LightGridElement> light_grid_samples;
+	// fetch_light_from_grid (triangle_models_rendering.rs:582-700): the trilinear mix of the up to 8
+	// existing non-zero samples around `pos`, renormalised when some were missing; zero without a grid
+	LightGridElement fetch_light_from_grid(Vec3 pos) const;
 	std::vector<ViewPortal> view_portals;
 	std::vector<std::vector<uint32_t>> view_portal_leafs;
 	std::vector<std::vector<uint32_t>> leaf_view_portals;

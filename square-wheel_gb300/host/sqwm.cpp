@@ -354,6 +354,9 @@ void map_from_scene(const Scene& sc, SqwmMap& m)
 	}
 	m.lightmaps = sc.lightmaps;
 	m.directional_lightmaps = sc.directional_lightmaps;
+	m.light_grid_header = sc.light_grid_header;
+	m.light_grid_columns = sc.light_grid_columns;
+	m.light_grid_samples = sc.light_grid_samples;
 	// Entities (deduplicated strings, StringRef offsets and sizes in u16): worldspawn and the player start.
 	auto add_string = [&](const std::string& s) {
 		for (size_t at = 0; at + s.size() <= m.strings_data.size(); ++at)

@@ -46,28 +46,12 @@ struct DirectionalLightmapElementCompressed
 	uint8_t directional_light_deviation;
 	CompressedColor directional_light_color;
 };
-// LightGridElement (bsp_map_compact.rs:179-188) and its compressed form (lightmap_compression.rs:14-20).
-struct LightGridElement
-{
-	float light_cube[6][3];
-	Vec3 light_direction_vector_scaled;
-	float directional_light_color[3];
-};
+// LightGridElement (scene.h) in its compressed form (lightmap_compression.rs:14-20).
 struct LightGridElementCompressed
 {
 	CompressedColor light_cube[6];
 	CompressedVector light_direction_vector_scaled;
 	CompressedColor directional_light_color;
-};
-struct LightGridHeader
-{
-	float grid_cell_size[3];
-	float grid_start[3];
-	uint32_t grid_size[3];
-};
-struct LightGridColumn
-{
-	uint32_t start_z, first_sample, num_samples;
 };
 struct MapSubmodel
 {

@@ -154,6 +154,7 @@ int scene_config_from(const SwhSceneConfig* c, SceneConfig& cfg)
 	cfg.fire_materials = c->fire_materials;
 	cfg.num_portals = c->num_portals;
 	cfg.portals_depth = std::min(c->portals_depth, 8u);
+	cfg.light_grid = c->light_grid;
 	if (cfg.num_portals > 4096)
 	{
 		g_error = "too many portals";
@@ -410,6 +411,30 @@ int swh_scene_simulation_words(const SwhScene* s, uint64_t* out)
 {
 	if (!s || !out) return SW_ERR_INVALID_ARGUMENT;
 	*out = s->scene.sim_state_words;
+	return SW_OK;
+}
+
+int swh_scene_light_grid(const SwhScene* s, void* out_header, uint32_t* out_columns, float* out_samples, uint64_t* num_columns,
+	uint64_t* num_samples)
+{
+	if (!s || !num_columns || !num_samples) return SW_ERR_INVALID_ARGUMENT;
+	const Scene& sc = s->scene;
+	*num_columns = sc.light_grid_columns.size();
+	*num_samples = sc.light_grid_samples.size();
+	static_assert(sizeof(LightGridHeader) == 36 && sizeof(LightGridColumn) == 12 && sizeof(LightGridElement) == 96, "grid layout");
+	if (out_header) std::memcpy(out_header, &sc.light_grid_header, sizeof(LightGridHeader));
+	if (out_columns && !sc.light_grid_columns.empty())
+		std::memcpy(out_columns, sc.light_grid_columns.data(), sc.light_grid_columns.size() * sizeof(LightGridColumn));
+	if (out_samples && !sc.light_grid_samples.empty())
+		std::memcpy(out_samples, sc.light_grid_samples.data(), sc.light_grid_samples.size() * sizeof(LightGridElement));
+	return SW_OK;
+}
+
+int swh_scene_fetch_light(const SwhScene* s, const float pos[3], float out_sample[24])
+{
+	if (!s || !pos || !out_sample) return SW_ERR_INVALID_ARGUMENT;
+	const LightGridElement e = s->scene.fetch_light_from_grid(v3(pos[0], pos[1], pos[2]));
+	std::memcpy(out_sample, &e, sizeof(e));
 	return SW_OK;
 }
 

@@ -27,7 +27,7 @@ class SceneConfig(ctypes.Structure):
         ("animated_materials", ctypes.c_uint32), ("projector_lights", ctypes.c_uint32), ("num_models", ctypes.c_uint32), ("model_triangles", ctypes.c_uint32),
         ("model_frames", ctypes.c_uint32), ("turb_materials", ctypes.c_uint32), ("layered_materials", ctypes.c_uint32), ("num_sprites", ctypes.c_uint32),
         ("num_decals", ctypes.c_uint32), ("water_materials", ctypes.c_uint32), ("fire_materials", ctypes.c_uint32),
-        ("num_portals", ctypes.c_uint32), ("portals_depth", ctypes.c_uint32),
+        ("num_portals", ctypes.c_uint32), ("portals_depth", ctypes.c_uint32), ("light_grid", ctypes.c_uint32),
     ]
 
 
@@ -132,6 +132,8 @@ def load_host_library():
         "swh_scene_texture_effect": ([vp, u32, vp], i32),
         "swh_scene_simulated_effect": ([vp, u32, vp], i32),
         "swh_scene_simulation_words": ([vp, ctypes.POINTER(ctypes.c_uint64)], i32),
+        "swh_scene_light_grid": ([vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)], i32),
+        "swh_scene_fetch_light": ([vp, vp, vp], i32),
         "swh_frame_effect_state": ([vp, u32, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u32),
                                     ctypes.POINTER(u32)], i32),
         "swh_scene_compressed_lightmaps": ([vp, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(vp),
@@ -153,7 +155,7 @@ HOST_EXPORTED = ["swh_scene_create", "swh_scene_destroy", "swh_scene_info", "swh
                  "swh_renderer_set_gpu_prep", "swh_frame_map", "swh_renderer_set_frames_in_flight",
                  "swh_scene_lite_textures", "swh_scene_load_map", "swh_scene_load_map_memory", "swh_scene_save_map",
                  "swh_scene_compressed_lightmaps", "swh_scene_texture_effect", "swh_scene_simulated_effect",
-                 "swh_scene_simulation_words", "swh_frame_effect_state"]
+                 "swh_scene_simulation_words", "swh_frame_effect_state", "swh_scene_light_grid", "swh_scene_fetch_light"]
 
 # The two map configurations of the benchmark plan.
 SMALL_MAP = dict(seed=1, grid_x=4, grid_y=2, tile_size=128.0, texture_size=128, num_materials=16, metal_frac=0.0,
@@ -224,6 +226,25 @@ class Scene:
         n = ctypes.c_uint64()
         _check(self.lib, self.lib.swh_scene_simulation_words(self.handle, ctypes.byref(n)), "swh_scene_simulation_words")
         return int(n.value)
+
+    def light_grid(self):
+        """(header: cell size, start and size arrays; columns (n, 3) u32; samples (m, 24) f32)."""
+        nc, ns = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self.lib, self.lib.swh_scene_light_grid(self.handle, None, None, None, ctypes.byref(nc), ctypes.byref(ns)),
+               "swh_scene_light_grid")
+        hdr = np.zeros(9, np.float32)
+        cols = np.zeros((nc.value, 3), np.uint32)
+        samples = np.zeros((ns.value, 24), np.float32)
+        _check(self.lib, self.lib.swh_scene_light_grid(self.handle, hdr.ctypes.data, cols.ctypes.data, samples.ctypes.data,
+                                                       ctypes.byref(nc), ctypes.byref(ns)), "swh_scene_light_grid")
+        header = dict(cell_size=hdr[0:3].copy(), start=hdr[3:6].copy(), size=hdr[6:9].view(np.uint32).copy())
+        return header, cols, samples
+
+    def fetch_light(self, pos):
+        p = np.asarray(pos, np.float32)
+        out = np.zeros(24, np.float32)
+        _check(self.lib, self.lib.swh_scene_fetch_light(self.handle, p.ctypes.data, out.ctypes.data), "swh_scene_fetch_light")
+        return out
 
     def save_map(self, path):
         _check(self.lib, self.lib.swh_scene_save_map(self.handle, os.fsencode(path)), "swh_scene_save_map")

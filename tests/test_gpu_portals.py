@@ -1,8 +1,8 @@
 """Portals on the GPU (sw_draw_frame with nested views) against the oracle: whole frames of a map with a
 mirror, a camera screen mixed with a texture and a parallax window, two nested levels, dynamic and
 shadowed lights, in both pixel formats (and through the HDR postprocess), equal the oracle's frames
-composed view by view (each portal texture rendered, mixed, then sampled by the frame's portal draws);
-the depth limit (black portals mixed with their texture) likewise; malformed views are refused."""
+composed view by view (each portal texture rendered, mixed, then sampled by the frame's portal draws),
+also with models, sprites and portal textures lit from a light grid; the depth limit (black portals mixed with their texture) likewise; malformed views are refused."""
 import ctypes
 
 import numpy as np
@@ -37,9 +37,12 @@ def oracle_frame(scene, fr, storage, w, h, fmt):
     return want, storage
 
 
-@pytest.mark.parametrize("fmt,depth", [(abi.SW_PIXEL_C32, 2), (abi.SW_PIXEL_C64, 2), (abi.SW_PIXEL_C32, 0)])
-def test_portal_frames(gpu_ok, fmt, depth):
-    scene = host.Scene(**dict(PORTAL_MAP, portals_depth=depth))
+@pytest.mark.parametrize("fmt,depth,grid", [(abi.SW_PIXEL_C32, 2, 0), (abi.SW_PIXEL_C64, 2, 0), (abi.SW_PIXEL_C32, 0, 0),
+                                            (abi.SW_PIXEL_C64, 1, 1)])
+def test_portal_frames(gpu_ok, fmt, depth, grid):
+    """grid=1: a light-grid map with models and sprites, all of them and the portal textures lit from the grid."""
+    extra = dict(light_grid=1, num_models=3, num_sprites=10) if grid else {}
+    scene = host.Scene(**dict(PORTAL_MAP, portals_depth=depth, **extra))
     fr = host.Frame(scene)
     hr = host.HostRenderer(scene)
     w, h = 640, 360
