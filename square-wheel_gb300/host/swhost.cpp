@@ -744,7 +744,8 @@ int swh_renderer_draw_frame(SwhRenderer* r, void* dst, uint32_t pitch, int dst_i
 		g_error = "a frame with portal views renders through swh_renderer_render_frame";
 		return SW_ERR_STATE;
 	}
-	int st = sw_submit_draws(r->ctx, p.draws.data(), uint32_t(p.draws.size()), p.vertices.data(), uint32_t(p.vertices.size()));
+	int st = sw_submit_draws_ex(r->ctx, p.draws.data(), uint32_t(p.draws.size()), p.vertices.data(), uint32_t(p.vertices.size()),
+		p.tri_vertices.data(), uint32_t(p.tri_vertices.size()));
 	if (st) return st;
 	return sw_render(r->ctx, dst, pitch, dst_is_device);
 }

@@ -167,6 +167,13 @@ FULL_MAP = dict(seed=2, grid_x=8, grid_y=8, tile_size=80.0, texture_size=256, nu
 # The full-size map with triangle models: 200 per-vertex animated models of about 2k triangles and 8
 # keyframes each on the rooms' floors (the stress configuration's models).
 MODEL_MAP = dict(FULL_MAP, num_models=200, model_triangles=2000, model_frames=8)
+# The stress configuration's map: 128 rooms (16 x 8) of the full-size configuration with portals
+# (mirrors, cameras, parallax windows; two nested levels), translucent (averaging animated frames),
+# alpha-blended and alpha-tested (layered) surfaces, 2k decals, sprites and the 200 models, all lit from
+# a seeded light grid.
+STRESS_MAP = dict(FULL_MAP, seed=5, grid_x=16, grid_y=8, num_models=200, model_triangles=2000, model_frames=8,
+                  num_decals=2000, num_sprites=64, num_portals=12, portals_depth=2, light_grid=1,
+                  layered_materials=4, animated_materials=4)
 # The small map with a sky: three rooms open to a skybox (the sky material's six 128x128 sides, HDR
 # brightness 2, rotating slowly), the camera looking 0.45 rad up so ceilings are in view.
 SKY_MAP = dict(SMALL_MAP, sky_rooms=3, skybox_size=128, skybox_brightness=2.0, sky_rotation_speed=0.01,

@@ -114,6 +114,33 @@ def test_host_renderer_sky_map(gpu_ok):
     assert np.array_equal(want, got)
 
 
+def test_host_renderer_draw_frame_models(gpu_ok):
+    """The per-call host path (swh_renderer_prepare_frame + swh_renderer_draw_frame) with triangle models,
+    sprites and decals: their triangle draws and vertices reach the rasteriser; equal to the oracle."""
+    scene = host.Scene(**dict(host.SMALL_MAP, num_models=3, model_triangles=600, num_sprites=8, num_decals=16))
+    hr = host.HostRenderer(scene)
+    opts = host.frame_options(320, 240, abi.SW_PIXEL_C64, directional=False)
+    st = scene.static_data()
+    lite = scene.lite_textures()
+    fr = host.Frame(scene)
+    tris = 0
+    try:
+        for fi in (5, 21, 40):
+            hr.prepare_frame(fi, opts)
+            got = np.zeros((240, 320), np.uint64)
+            hr.draw_frame(got)
+            fr.prepare(fi, opts)
+            tris += fr.model_triangles
+            arena = oracle.build_surfaces(st, fr.surfaces, fr.lights, fr.params, fr.total_texels, num_threads=4)
+            want = np.zeros((240, 320), np.uint64)
+            assert oracle.rasterize(fr.draws, fr.vertices, arena, fr.params, want, tri_vertices=fr.tri_vertices,
+                                    lite=lite) == 0
+            assert np.array_equal(want, got), f"frame {fi}: {(want != got).sum()} pixels differ"
+    finally:
+        hr.close()
+    assert tris > 0
+
+
 def test_host_renderer_render_frame_graph(gpu_ok):
     """swh_renderer_render_frame: host work + the whole frame as one graph with postprocess, the result
     copied straight into a registered host buffer; equal to the oracle's frame and tonemap."""
