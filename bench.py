@@ -883,7 +883,7 @@ def run_stress_gpu(args, world, rank, local):
                                ctypes.c_void_p(up.data_ptr()), SW, SH, SW, 1) == 0
 
     idx = frame_indices(args.warmup + args.steps, replica_offset(rank))
-    plain_ms, learned_ms, psnr, views, tris = [], [], [], 0, 0
+    plain_ms, learned_ms, psnr, views, tris, launches = [], [], [], 0, 0, 0
     fr = host.Frame(scene)
     with ClockSampler(local) as clocks:
         for step, fi in enumerate(idx):
@@ -905,6 +905,9 @@ def run_stress_gpu(args, world, rank, local):
             fr.prepare(fi, opts_hi)
             views += len(fr.views)
             tris += fr.model_triangles
+            # per frame: the frame's kernels, per portal view setup / bins / tiles / mix, the texture-effect
+            # pass; the two frames of the step (views counted at 3840x2160 for both) and the upscale
+            launches += 2 * (FRAME_LAUNCHES + 4 * len(fr.views) + (1 if fr.texture_passes.size else 0)) + 1
     p_ms = statistics.mean(plain_ms)
     l_ms = statistics.mean(learned_ms)
     mon = monitored_sequence(psnr, l_ms, p_ms)
@@ -918,11 +921,16 @@ def run_stress_gpu(args, world, rank, local):
     for fi in efr[:2]:
         hr.render_frame(fi, opts_hi, out=out, post=cfg)
     hr.sync()
+    st0 = abi.Stats()
+    assert glib.sw_get_stats(ctx, ctypes.byref(st0)) == 0
     for fi in efr:
         t0 = time.perf_counter()
         hr.render_frame(fi, opts_hi, out=out, post=cfg)
         hr.sync()
         e_plain.append((time.perf_counter() - t0) * 1e3)
+    st1 = abi.Stats()
+    assert glib.sw_get_stats(ctx, ctypes.byref(st1)) == 0
+    h2d = int((st1.upload_bytes - st0.upload_bytes) / len(efr))
     hr.render_frame(efr[0], opts_lo, device_ptr=half.data_ptr(), pitch=W, post=cfg)
     hr.sync()
     for fi in efr:
@@ -1001,10 +1009,10 @@ def run_stress_gpu(args, world, rank, local):
             "e2e": {"value": round(e_mon["frames_per_s"], 2), "unit": "frames/s",
                     "plain_frames_per_s": round(1e3 / statistics.mean(e_plain), 2),
                     "learned_frames_per_s": round(1e3 / statistics.mean(e_learned), 2),
-                    "h2d_bytes_per_step": None, "d2h_bytes_per_step": int(out.nbytes),
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(out.nbytes),
                     "path": "swh_renderer_render_frame (host visibility, portals and models) per frame, wall clock, "
                             "the delivered frame copied to pinned host memory; monitor applied as for value"},
-            "clocks": clocks.summary(), "gpu_launches": None}), flush=True)
+            "clocks": clocks.summary(), "gpu_launches": launches}), flush=True)
     ups.close()
     hr.close()
 
