@@ -4,7 +4,7 @@
 // :273-454 (fill_polygon_part, full perspective), :456-581 (line-z corrected), :583-729 (affine),
 // :765-1292 (fill_triangle_impl, fill_triangle_part: textured triangles with per-vertex light),
 // :1511-1536 (write_into_framebuffer), :1573-1580 (fixed-point constants), src/common/fixed_math.rs,
-// and the driver src/square_wheel/partial_renderer.rs:1192-1283 (perform_rasterization; N-thread mode
+// and its caller src/square_wheel/partial_renderer.rs:1192-1283 (perform_rasterization; N-thread mode
 // uses src/square_wheel/rect_splitting.rs:23-78).
 #include "sw_oracle.h"
 #include "sw_oracle_math.h"
