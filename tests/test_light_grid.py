@@ -136,3 +136,24 @@ def test_models_and_sprites_lit_from_grid(grid_scene):
         assert differ > 0, "model/sprite vertex lights do not depend on the grid"
     finally:
         unlit.close()
+
+
+def test_stress_configuration_prepares():
+    """The stress configuration's map (128 rooms, portals, decals, sprites, 200 grid-lit models): frames
+    of its camera path carry portal views and model triangles, and the map has a light grid."""
+    s = host.Scene(**host.STRESS_MAP)
+    try:
+        info = s.info()
+        assert info.polygons > 60000
+        _, cols, samples = s.light_grid()
+        assert cols.size > 0 and samples.size > 0
+        fr = host.Frame(s)
+        opts = host.frame_options(960, 540, abi.SW_PIXEL_C64, directional=True)
+        views = tris = 0
+        for fi in (0, 37, 74, 208, 224):
+            fr.prepare(fi, opts)
+            views += len(fr.views)
+            tris += fr.model_triangles
+        assert views > 0 and tris > 0
+    finally:
+        s.close()
